@@ -1,0 +1,283 @@
+/*
+ * nunatak_gb300.h — C ABI of libnunatak_gb300.so, the GB300 (sm_103a) velocity solver for
+ * Nunatak.jl's depth-integrated (SSA / DIVA) stress balance.
+ *
+ * The entry points replace the Julia call chain of the reference at its Picard + PCG call site:
+ *
+ *   update_velocities!(model, ::StressBalanceSolver, ::SSA | ::DIVA)
+ *       src/Models/ice_sheet_model_methods.jl:119-147
+ *     -> picard_solve!(x, picard, linear_solver, update_coefficients!, b, coefficients...)
+ *       src/Solvers/picard.jl:63-90
+ *       -> update_stress_balance_coefficients!   src/StressBalances/stress_balance_coefficients.jl:10-20
+ *          update_diva_coefficients!             src/StressBalances/diva.jl:221-235
+ *       -> solve!(x, solver, b, args...)         src/Solvers/conjugate_gradient.jl:269-364
+ *          -> ssa_operator!                      src/StressBalances/ssa_operator.jl:47-89
+ *          -> precondition!                      src/StressBalances/diagonal_preconditioner.jl:132-175
+ *                                                src/StressBalances/multigrid_preconditioner.jl:122-360
+ *
+ * Plain C types only: no CUDA, C++ or torch types cross this boundary.  Every function returns an
+ * nk_status and never throws.  Host arrays are caller-owned; the library copies them to and from its
+ * own device buffers inside the call and keeps no host pointer after the call returns.
+ *
+ * Array layout ("interior layout"): the memory order of Oceananigans' interior(field) — column-major,
+ * x fastest, no halos.  Sizes for an Nx x Ny grid with x topology TX and y topology TY:
+ *   Center-Center (H, b, s, N, mu, eta_H, F2, C, A2D) : Nx * Ny
+ *   Face-Center   (u, beta_u, tau_u, phi_u, ...)      : nfx * Ny,  nfx = Nx + 1 (Bounded) or Nx (Periodic)
+ *   Center-Face   (v, beta_v, tau_v, phi_v, ...)      : Nx * nfy,  nfy = Ny + 1 (Bounded) or Ny (Periodic)
+ *   Face-Face     (eta_H_ff)                          : nfx * nfy
+ *   sigma fields  (eta_sigma, A3D, T)                 : Nx * Ny * Nsigma  (k slowest)
+ *   face sigma    (u_sigma / v_sigma)                 : nfx * Ny * Nsigma / Nx * nfy * Nsigma
+ */
+#ifndef NUNATAK_GB300_H
+#define NUNATAK_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NK_API_VERSION 1
+
+/* Status codes.  The reference signals these through return values, @warn and ArgumentError
+ * (src/Solvers/conjugate_gradient.jl:326-341 stops silently at maxiter, src/Solvers/picard.jl:79-89 likewise,
+ *  src/StressBalances/ssa_operator.jl:56 throws ArgumentError). */
+typedef int32_t nk_status;
+#define NK_OK               0
+#define NK_NOT_CONVERGED    1   /* an iteration control with Convergence reached maxiter (result still written) */
+#define NK_NONFINITE        2   /* a NaN / Inf residual or velocity */
+#define NK_BREAKDOWN        3   /* p.q <= 0 in conjugate gradients (operator not SPD on the active points) */
+#define NK_OOM              4   /* device allocation failed */
+#define NK_BAD_ARGUMENT     5   /* invalid descriptor, field id, size or null pointer */
+#define NK_TIMEOUT          6   /* a device wait ran out of its bound */
+#define NK_CUDA_ERROR       7   /* any other CUDA runtime error */
+#define NK_BUSY             8   /* server queue full / request not finished */
+
+/* Topology of one horizontal direction (Oceananigans Bounded / Periodic). */
+#define NK_BOUNDED   0
+#define NK_PERIODIC  1
+
+/* Tangential wall condition, src/StressBalances/depth_integrated.jl:204-220. */
+#define NK_FREE_SLIP 0
+#define NK_NO_SLIP   1
+
+/* Stress balance, src/StressBalances/depth_integrated.jl:187-233 (SSA = shear nothing, DIVA = DIVAShear()). */
+#define NK_SSA  0
+#define NK_DIVA 1
+
+/* Friction law, src/Frictions/frictions.jl:9-89. */
+#define NK_FRICTION_NONE        0
+#define NK_WEERTMAN             1
+#define NK_REGULARIZED_COULOMB  2
+
+/* Rate factor layout of GlenFlowLaw, src/Rheologies/glen_flow_law.jl:161-169. */
+#define NK_RATE_FACTOR_2D     0   /* Center-Center field, uniform in depth */
+#define NK_RATE_FACTOR_SIGMA  1   /* field on the sigma grid */
+
+/* Preconditioner of the velocity conjugate-gradient solver. */
+#define NK_PRECONDITIONER_NONE       0   /* precondition!(z, ::Nothing, r)          conjugate_gradient.jl:174 */
+#define NK_PRECONDITIONER_DIAGONAL   1   /* StressBalanceDiagonalPreconditioner     diagonal_preconditioner.jl:130 */
+#define NK_PRECONDITIONER_MULTIGRID  2   /* StressBalanceMultigridPreconditioner    multigrid_preconditioner.jl:18 */
+
+/* Multigrid smoother, src/StressBalances/multigrid_preconditioner.jl:69-78. */
+#define NK_SMOOTHER_POINT_JACOBI 0
+#define NK_SMOOTHER_LINE_JACOBI  1
+
+/* Arithmetic of the solve.  FP64 reproduces the reference; MIXED runs the multigrid preconditioner
+ * (operator applies, smoother state, transfers) in FP32 under an FP64 flexible conjugate gradient whose
+ * residual, dot products and Picard test stay FP64. */
+#define NK_PRECISION_FP64  0
+#define NK_PRECISION_MIXED 1
+
+/* Iteration control, src/Solvers/iteration_controls.jl:99-133. */
+#define NK_CONVERGENCE      0
+#define NK_FIXED_ITERATIONS 1
+
+typedef struct nk_iteration_control {
+    int32_t kind;        /* NK_CONVERGENCE or NK_FIXED_ITERATIONS */
+    int32_t iterations;  /* FixedIterations(iterations) */
+    int32_t maxiter;     /* Convergence: maxiter */
+    int32_t reserved;
+    double  reltol;      /* Convergence: reltol */
+    double  abstol;      /* Convergence: abstol */
+} nk_iteration_control;
+
+/* Horizontal RectilinearGrid (Flat z) plus the sigma column of SigmaGrid, src/Grids/sigma_grid.jl:264-306. */
+typedef struct nk_grid_desc {
+    int32_t Nx, Ny;
+    int32_t topology_x, topology_y;   /* NK_BOUNDED / NK_PERIODIC */
+    int32_t halo_x, halo_y;           /* only the multigrid coarsening rule reads the halo (multigrid_preconditioner.jl:86) */
+    int32_t Nsigma;                   /* number of sigma levels (>= 1) */
+    int32_t reserved;
+    const double* x_faces;            /* Nx+1 face coordinates, or NULL for a regular grid on [x0, x0 + Lx] */
+    const double* y_faces;            /* Ny+1 face coordinates, or NULL for a regular grid on [y0, y0 + Ly] */
+    double x0, Lx, y0, Ly;
+    const double* sigma_faces;        /* Nsigma+1 faces zeta_0 = 0 .. zeta_Nsigma = 1, or NULL for (k/Nsigma)^bed_refinement */
+    double bed_refinement;
+} nk_grid_desc;
+
+/* Physics of the solve: DepthIntegrated, GlenFlowLaw, friction law, IceSheetConstants, SmoothIceMask. */
+typedef struct nk_physics_desc {
+    int32_t stress_balance;           /* NK_SSA / NK_DIVA */
+    int32_t side_walls;               /* NK_FREE_SLIP / NK_NO_SLIP */
+    int32_t rate_factor_layout;       /* NK_RATE_FACTOR_2D / NK_RATE_FACTOR_SIGMA */
+    int32_t friction;                 /* NK_FRICTION_NONE / NK_WEERTMAN / NK_REGULARIZED_COULOMB */
+    double  glen_exponent;            /* n */
+    double  strain_rate_regularization;   /* epsilon_0 (1/s) */
+    double  friction_exponent;        /* m */
+    double  coulomb_coefficient;      /* alpha^2 */
+    double  velocity_regularization;  /* u_0 (m/s) */
+    double  ice_density, ocean_density, gravitational_acceleration;
+    int32_t use_ice_mask;             /* 1: eta_H is scaled by mu and faces with mu = 0 on both sides drop out */
+    int32_t grounding;                /* 0: nothing (all grounded), 1: SubgridGroundedFraction */
+    int32_t grounding_line_driving_stress;   /* SubgridGroundedFraction(driving_stress = true) */
+    int32_t use_effective_pressure;   /* 1: the friction law receives N (0 passes `nothing`) */
+    double  mask_minimum_thickness;   /* SmoothIceMask, src/Models/smooth_ice_mask.jl:398 */
+    double  mask_transition_thickness;
+} nk_physics_desc;
+
+/* StressBalanceSolver options, src/StressBalances/stress_balance_solver.jl:176-185. */
+typedef struct nk_solver_desc {
+    int32_t precision;                /* NK_PRECISION_FP64 / NK_PRECISION_MIXED */
+    int32_t preconditioner;           /* NK_PRECONDITIONER_* */
+    int32_t smoother;                 /* NK_SMOOTHER_* */
+    int32_t smoothing_sweeps;         /* default 2 */
+    int32_t coarsest_sweeps;          /* default 20 */
+    int32_t minimum_coarse_size;      /* default 2 */
+    nk_iteration_control linear;      /* default Convergence(reltol = 1e-8, maxiter = 10_000) */
+    nk_iteration_control picard;      /* default Convergence(reltol = 1e-6, maxiter = 100) */
+} nk_solver_desc;
+
+/* Field identifiers for nk_problem_set_field / nk_problem_get_field (the reference's names). */
+#define NK_FIELD_U              0   /* model.velocities.u                   Face-Center */
+#define NK_FIELD_V              1   /* model.velocities.v                   Center-Face */
+#define NK_FIELD_H              2   /* model.geometry.H                     Center-Center */
+#define NK_FIELD_BED            3   /* model.bed                            Center-Center */
+#define NK_FIELD_SURFACE        4   /* model.geometry.s                     Center-Center */
+#define NK_FIELD_ICE_MASK       5   /* model.geometry.ice_mask (mu)         Center-Center */
+#define NK_FIELD_PHI            6   /* model.geometry.phi                   Center-Center */
+#define NK_FIELD_PHI_U          7   /* model.geometry.phi_u                 Face-Center */
+#define NK_FIELD_PHI_V          8   /* model.geometry.phi_v                 Center-Face */
+#define NK_FIELD_EFFECTIVE_PRESSURE 9   /* model.geometry.N                 Center-Center */
+#define NK_FIELD_TAU_U         10   /* model.auxiliary.tau_u (RHS)          Face-Center */
+#define NK_FIELD_TAU_V         11   /* model.auxiliary.tau_v                Center-Face */
+#define NK_FIELD_RATE_FACTOR   12   /* GlenFlowLaw rate factor A            Center-Center or sigma */
+#define NK_FIELD_FRICTION_COEFFICIENT 13  /* friction.coefficient C         Center-Center */
+#define NK_FIELD_ETA_H         14   /* model.auxiliary.eta_bar_H            Center-Center */
+#define NK_FIELD_ETA_H_FF      15   /* model.auxiliary.eta_bar_H_ff         Face-Face */
+#define NK_FIELD_BETA_U        16   /* model.auxiliary.beta_u               Face-Center */
+#define NK_FIELD_BETA_V        17   /* model.auxiliary.beta_v               Center-Face */
+#define NK_FIELD_ETA_SIGMA     18   /* model.auxiliary.eta_sigma            sigma */
+#define NK_FIELD_F2            19   /* model.auxiliary.F2                   Center-Center */
+#define NK_FIELD_BETA_B_U      20   /* model.auxiliary.beta_b_u (DIVA)      Face-Center */
+#define NK_FIELD_BETA_B_V      21   /* model.auxiliary.beta_b_v (DIVA)      Center-Face */
+#define NK_FIELD_U_B           22   /* model.velocities.u_b                 Face-Center */
+#define NK_FIELD_V_B           23   /* model.velocities.v_b                 Center-Face */
+#define NK_FIELD_U_SIGMA       24   /* model.velocities.u_sigma             Face-Center x sigma */
+#define NK_FIELD_V_SIGMA       25   /* model.velocities.v_sigma             Center-Face x sigma */
+#define NK_FIELD_TEMPERATURE   26   /* temperature on the sigma grid (input of nk_compute_rate_factor) */
+#define NK_FIELD_COUNT         27
+
+typedef struct nk_solve_stats {
+    int32_t status;                   /* nk_status of the solve */
+    int32_t picard_iterations;        /* return value of picard_solve! */
+    int32_t linear_iterations_last;   /* linear_solver.iteration after the last solve */
+    int32_t linear_iterations_total;  /* sum over the Picard iterations */
+    double  residual_norm;            /* final ||r|| of the last linear solve (unpreconditioned, FP64) */
+    double  initial_residual_norm;    /* ||r0|| of the last linear solve */
+    double  picard_change;            /* last ||x - x_prev|| (Convergence) */
+    double  picard_norm;              /* last ||x|| (Convergence) */
+    double  device_ms;                /* device time of the call, CUDA events */
+} nk_solve_stats;
+
+typedef struct nk_context nk_context;
+typedef struct nk_problem nk_problem;
+typedef struct nk_server  nk_server;
+
+/* ---- context ------------------------------------------------------------------------------------ */
+
+/* One context per device.  device = CUDA ordinal. */
+nk_status   nk_context_create(int32_t device, nk_context** out);
+nk_status   nk_context_destroy(nk_context* ctx);
+const char* nk_last_error(const nk_context* ctx);
+int32_t     nk_api_version(void);
+
+/* ---- problem: one grid with its fields, coefficients, solver state and multigrid hierarchy ---------- */
+
+/* IceSheetModel(grid; stress_balance, rheology, friction, grounding, masking, velocity_solver)
+ * restricted to what the velocity solve reads (src/Models/ice_sheet_model.jl:79-120,
+ * src/StressBalances/stress_balance_solver.jl:176-185).  Allocates every device buffer once. */
+nk_status nk_problem_create(nk_context* ctx, const nk_grid_desc* grid, const nk_physics_desc* physics,
+                            const nk_solver_desc* solver, nk_problem** out);
+nk_status nk_problem_destroy(nk_problem* problem);
+
+/* Copy a host array in interior layout into a field (set!(field, array) + fill_halo_regions!). */
+nk_status nk_problem_set_field(nk_problem* problem, int32_t field, const double* host, int64_t count);
+/* Copy a field out in interior layout. */
+nk_status nk_problem_get_field(const nk_problem* problem, int32_t field, double* host, int64_t count);
+/* Number of values of a field in interior layout (0 for an unknown id). */
+int64_t   nk_problem_field_size(const nk_problem* problem, int32_t field);
+
+/* update_geometry! + compute_driving_stress! (src/Models/ice_sheet_model_methods.jl:103-111, :126):
+ * s, phi, phi_u, phi_v, N, mu from H and bed, then tau.  Replaces the reference's
+ * compute_surface_elevation!, compute_grounded_fractions!, compute_effective_pressure!, compute_ice_mask!
+ * (src/Groundings/subgrid_grounded_fraction.jl:234-357, src/Models/smooth_ice_mask.jl:417-426) and
+ * compute_driving_stress! (src/StressBalances/driving_stress.jl:43-125). */
+nk_status nk_compute_geometry(nk_problem* problem);
+
+/* Rate factor on the sigma grid from the temperature field with omega = 0:
+ * A = arrhenius_rate_factor(T - T_pm(p) + T_0, 0) (src/Thermodynamics/column_energy_solve.jl:104-110,
+ * src/Rheologies/arrhenius_rate_factor.jl:102-110), p = rho_i g H (1 - zeta_k). */
+nk_status nk_compute_rate_factor(nk_problem* problem, double cold_prefactor, double warm_prefactor,
+                                 double cold_activation_energy, double warm_activation_energy,
+                                 double transition_temperature, double transition_width, double gas_constant,
+                                 double clausius_clapeyron, double melting_temperature);
+
+/* update_stress_balance_coefficients!(x, ...) (SSA) or update_diva_coefficients!(x, ...) (DIVA) at the
+ * current velocity fields U, V: eta_sigma, eta_H, F2, eta_H_ff, beta (and beta_b, u_b, v_b for DIVA). */
+nk_status nk_update_coefficients(nk_problem* problem);
+
+/* ssa_operator!(q, p, eta_H, eta_H_ff, beta_u, beta_v, walls) with the problem's coefficients.
+ * p and q are host arrays in interior layout (u part then v part sizes as above); q is fully written
+ * on the Nx x Ny range, its other entries are left as passed. */
+nk_status nk_apply_operator(nk_problem* problem, const double* pu, const double* pv, double* qu, double* qv);
+
+/* precondition!(z, P, r, coefficients...) with the configured preconditioner (multigrid coarse
+ * coefficients are rebuilt from the current coefficients first, as update_preconditioner! does). */
+nk_status nk_precondition(nk_problem* problem, const double* ru, const double* rv, double* zu, double* zv);
+
+/* solve!(x, linear_solver, b, coefficients...) from the warm start in the U, V fields; b host arrays. */
+nk_status nk_linear_solve(nk_problem* problem, const double* bu, const double* bv, nk_solve_stats* stats);
+/* adjoint_solve!(lambda, solver, b, ...): the operator is self-adjoint, so the same solve. */
+nk_status nk_adjoint_solve(nk_problem* problem, const double* bu, const double* bv, nk_solve_stats* stats);
+
+/* picard_solve!(x, picard, linear_solver, update_coefficients!, tau, coefficients...) on device-resident
+ * fields: x = (U, V) warm start, b = (TAU_U, TAU_V).  Updates U, V and every coefficient field. */
+nk_status nk_picard_solve(nk_problem* problem, nk_solve_stats* stats);
+
+/* The whole update_velocities! body for host callers: copies u, v (warm start) in, runs
+ * nk_picard_solve and copies u, v out.  u, v in interior layout. */
+nk_status nk_solve_velocities(nk_problem* problem, double* u, double* v, nk_solve_stats* stats);
+
+/* DIVA: compute_velocity_profile! (src/StressBalances/diva.jl:249-269); SSA: extend_depth_average!
+ * (src/Models/ice_sheet_model_methods.jl:167-180).  Fills U_B, V_B, U_SIGMA, V_SIGMA. */
+nk_status nk_velocity_profile(nk_problem* problem);
+
+/* Number of multigrid levels below the finest and the size of each (multigrid_preconditioner.jl:86-120). */
+nk_status nk_multigrid_levels(const nk_problem* problem, int32_t* count, int32_t* nx, int32_t* ny, int32_t capacity);
+
+/* Multigrid transfers between level `level` - 1 (the finest grid for level 0) and coarse level `level`,
+ * with masks from the coarse coefficients rebuilt from the current ones (coarsen_coefficients!):
+ *   restrict!(coarse, fine, ...)      coarse = R fine    multigrid_preconditioner.jl:182-186, :346-352
+ *   prolongate!(fine, coarse, ...)    fine  += P coarse  multigrid_preconditioner.jl:188-192, :354-360
+ * Vectors in interior layout of their grids (u part, v part). */
+nk_status nk_multigrid_restrict(nk_problem* problem, int32_t level, const double* fine_u, const double* fine_v,
+                                double* coarse_u, double* coarse_v);
+nk_status nk_multigrid_prolongate(nk_problem* problem, int32_t level, const double* coarse_u, const double* coarse_v,
+                                  double* fine_u, double* fine_v);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NUNATAK_GB300_H */

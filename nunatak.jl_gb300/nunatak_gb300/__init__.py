@@ -1,0 +1,19 @@
+"""nunatak_gb300 — GB300-native velocity solve of Nunatak.jl (SSA / DIVA Picard + PCG) behind a C ABI.
+
+The compute path is libnunatak_gb300.so (hand-written CUDA for sm_103a); this package is the host-side
+mirror of the reference's configuration objects and solver entry points."""
+from . import abi
+from .model import (YEAR, Convergence, DepthIntegrated, DIVAShear, FixedIterations, FreeSlipWalls, GlenFlowLaw,
+                    IceSheetConstants, LineJacobi, NoSlipWalls, PointJacobi, RectilinearGrid,
+                    RegularizedCoulombFriction, SmoothIceMask, StressBalanceDiagonalPreconditioner,
+                    StressBalanceMultigridPreconditioner, StressBalanceSolver, SubgridGroundedFraction,
+                    WeertmanFriction, make_descriptors, field_shape)
+from .problem import NunatakError, Problem
+
+__all__ = [
+    "abi", "YEAR", "Convergence", "DepthIntegrated", "DIVAShear", "FixedIterations", "FreeSlipWalls", "GlenFlowLaw",
+    "IceSheetConstants", "LineJacobi", "NoSlipWalls", "PointJacobi", "RectilinearGrid", "RegularizedCoulombFriction",
+    "SmoothIceMask", "StressBalanceDiagonalPreconditioner", "StressBalanceMultigridPreconditioner",
+    "StressBalanceSolver", "SubgridGroundedFraction", "WeertmanFriction", "make_descriptors", "field_shape",
+    "NunatakError", "Problem",
+]

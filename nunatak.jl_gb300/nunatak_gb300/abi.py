@@ -1,0 +1,87 @@
+"""ctypes mirror of include/nunatak_gb300.h: constants and descriptor structs of the C ABI."""
+import ctypes as C
+
+NK_API_VERSION = 1
+
+NK_OK = 0
+NK_NOT_CONVERGED = 1
+NK_NONFINITE = 2
+NK_BREAKDOWN = 3
+NK_OOM = 4
+NK_BAD_ARGUMENT = 5
+NK_TIMEOUT = 6
+NK_CUDA_ERROR = 7
+NK_BUSY = 8
+
+STATUS_NAMES = {0: "OK", 1: "NOT_CONVERGED", 2: "NONFINITE", 3: "BREAKDOWN", 4: "OOM",
+                5: "BAD_ARGUMENT", 6: "TIMEOUT", 7: "CUDA_ERROR", 8: "BUSY"}
+
+NK_BOUNDED, NK_PERIODIC = 0, 1
+NK_FREE_SLIP, NK_NO_SLIP = 0, 1
+NK_SSA, NK_DIVA = 0, 1
+NK_FRICTION_NONE, NK_WEERTMAN, NK_REGULARIZED_COULOMB = 0, 1, 2
+NK_RATE_FACTOR_2D, NK_RATE_FACTOR_SIGMA = 0, 1
+NK_PRECONDITIONER_NONE, NK_PRECONDITIONER_DIAGONAL, NK_PRECONDITIONER_MULTIGRID = 0, 1, 2
+NK_SMOOTHER_POINT_JACOBI, NK_SMOOTHER_LINE_JACOBI = 0, 1
+NK_PRECISION_FP64, NK_PRECISION_MIXED = 0, 1
+NK_CONVERGENCE, NK_FIXED_ITERATIONS = 0, 1
+
+FIELD_IDS = {
+    "u": 0, "v": 1, "H": 2, "bed": 3, "s": 4, "ice_mask": 5, "phi": 6, "phi_u": 7, "phi_v": 8,
+    "N": 9, "tau_u": 10, "tau_v": 11, "A": 12, "C": 13, "eta_H": 14, "eta_H_ff": 15,
+    "beta_u": 16, "beta_v": 17, "eta_sigma": 18, "F2": 19, "beta_b_u": 20, "beta_b_v": 21,
+    "u_b": 22, "v_b": 23, "u_sigma": 24, "v_sigma": 25, "T": 26,
+}
+
+# (location x, location y, on the sigma grid) of each field: "c" Center, "f" Face.
+FIELD_LOCATIONS = {
+    "u": ("f", "c", False), "v": ("c", "f", False), "H": ("c", "c", False), "bed": ("c", "c", False),
+    "s": ("c", "c", False), "ice_mask": ("c", "c", False), "phi": ("c", "c", False),
+    "phi_u": ("f", "c", False), "phi_v": ("c", "f", False), "N": ("c", "c", False),
+    "tau_u": ("f", "c", False), "tau_v": ("c", "f", False), "A": ("c", "c", None),
+    "C": ("c", "c", False), "eta_H": ("c", "c", False), "eta_H_ff": ("f", "f", False),
+    "beta_u": ("f", "c", False), "beta_v": ("c", "f", False), "eta_sigma": ("c", "c", True),
+    "F2": ("c", "c", False), "beta_b_u": ("f", "c", False), "beta_b_v": ("c", "f", False),
+    "u_b": ("f", "c", False), "v_b": ("c", "f", False), "u_sigma": ("f", "c", True),
+    "v_sigma": ("c", "f", True), "T": ("c", "c", True),
+}
+
+
+class IterationControl(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("iterations", C.c_int32), ("maxiter", C.c_int32),
+                ("reserved", C.c_int32), ("reltol", C.c_double), ("abstol", C.c_double)]
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("Nx", C.c_int32), ("Ny", C.c_int32), ("topology_x", C.c_int32), ("topology_y", C.c_int32),
+                ("halo_x", C.c_int32), ("halo_y", C.c_int32), ("Nsigma", C.c_int32), ("reserved", C.c_int32),
+                ("x_faces", C.POINTER(C.c_double)), ("y_faces", C.POINTER(C.c_double)),
+                ("x0", C.c_double), ("Lx", C.c_double), ("y0", C.c_double), ("Ly", C.c_double),
+                ("sigma_faces", C.POINTER(C.c_double)), ("bed_refinement", C.c_double)]
+
+
+class PhysicsDesc(C.Structure):
+    _fields_ = [("stress_balance", C.c_int32), ("side_walls", C.c_int32), ("rate_factor_layout", C.c_int32),
+                ("friction", C.c_int32), ("glen_exponent", C.c_double), ("strain_rate_regularization", C.c_double),
+                ("friction_exponent", C.c_double), ("coulomb_coefficient", C.c_double),
+                ("velocity_regularization", C.c_double), ("ice_density", C.c_double),
+                ("ocean_density", C.c_double), ("gravitational_acceleration", C.c_double),
+                ("use_ice_mask", C.c_int32), ("grounding", C.c_int32),
+                ("grounding_line_driving_stress", C.c_int32), ("use_effective_pressure", C.c_int32),
+                ("mask_minimum_thickness", C.c_double), ("mask_transition_thickness", C.c_double)]
+
+
+class SolverDesc(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("preconditioner", C.c_int32), ("smoother", C.c_int32),
+                ("smoothing_sweeps", C.c_int32), ("coarsest_sweeps", C.c_int32), ("minimum_coarse_size", C.c_int32),
+                ("linear", IterationControl), ("picard", IterationControl)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("status", C.c_int32), ("picard_iterations", C.c_int32), ("linear_iterations_last", C.c_int32),
+                ("linear_iterations_total", C.c_int32), ("residual_norm", C.c_double),
+                ("initial_residual_norm", C.c_double), ("picard_change", C.c_double),
+                ("picard_norm", C.c_double), ("device_ms", C.c_double)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}

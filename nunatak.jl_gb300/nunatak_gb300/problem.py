@@ -1,0 +1,211 @@
+"""Host-side mirror of the reference's solver API over the C ABI of libnunatak_gb300.so.
+
+`Problem` holds one nk_problem: a grid, its fields and coefficients, the solver state and the multigrid
+hierarchy, resident on the GPU.  Its methods are the reference's entry points for this path:
+
+  set! / interior(field)            -> Problem.set / Problem.get
+  update_geometry! + driving stress -> Problem.compute_geometry   (src/Models/ice_sheet_model_methods.jl:103-111, :126)
+  update_stress_balance_coefficients! / update_diva_coefficients!
+                                    -> Problem.update_coefficients (stress_balance_coefficients.jl:10-20, diva.jl:221-235)
+  ssa_operator!(q, p, ...)          -> Problem.apply_operator      (src/StressBalances/ssa_operator.jl:47-52)
+  precondition!(z, P, r, ...)       -> Problem.precondition
+  solve!(x, solver, b, ...)         -> Problem.linear_solve        (src/Solvers/conjugate_gradient.jl:269-270)
+  adjoint_solve!(λ, solver, b, ...) -> Problem.adjoint_solve       (src/Solvers/conjugate_gradient.jl:296-297)
+  picard_solve!(x, picard, ...)     -> Problem.picard_solve        (src/Solvers/picard.jl:63-90)
+  compute_velocity_profile! / extend_depth_average! -> Problem.velocity_profile
+
+Errors map the reference's behaviour: a bad argument raises ValueError (ArgumentError), a solve that
+stops at maxiter returns its iteration count with stats.status == NOT_CONVERGED (the reference stops
+silently), a non-finite result raises FloatingPointError.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .model import Descriptors, field_shape
+
+_dptr = C.POINTER(C.c_double)
+
+
+class NunatakError(RuntimeError):
+    pass
+
+
+def _check(status, what, message=""):
+    if status == abi.NK_OK:
+        return
+    name = abi.STATUS_NAMES.get(status, str(status))
+    if status == abi.NK_BAD_ARGUMENT:
+        raise ValueError(f"{what}: {name} {message}".strip())
+    if status == abi.NK_NONFINITE:
+        raise FloatingPointError(f"{what}: {name} {message}".strip())
+    raise NunatakError(f"{what}: {name} {message}".strip())
+
+
+def _as_f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Problem:
+    """One grid's velocity solve on the GPU (nk_problem)."""
+
+    prefix = "nk_"
+
+    def __init__(self, grid, desc: Descriptors, context=None):
+        from . import library
+        self.grid = grid
+        self.desc = desc
+        self.Nsigma = desc.grid.Nsigma
+        self.sigma_rate = desc.physics.rate_factor_layout == abi.NK_RATE_FACTOR_SIGMA
+        self._lib = self._load()
+        self._ctx = context if context is not None else (library.default_context() if self.prefix == "nk_" else None)
+        self._h = C.c_void_p()
+        self._create()
+
+    # -- library plumbing ------------------------------------------------------------------------
+    def _load(self):
+        from . import library
+        return library.load()
+
+    def _fn(self, name):
+        return getattr(self._lib, self.prefix + name)
+
+    def _create(self):
+        st = self._fn("problem_create")(self._ctx.handle, C.byref(self.desc.grid), C.byref(self.desc.physics),
+                                         C.byref(self.desc.solver), C.byref(self._h))
+        _check(st, "problem_create", self._ctx.last_error())
+
+    def _err(self):
+        return self._ctx.last_error() if self._ctx is not None else ""
+
+    def close(self):
+        if self._h:
+            self._fn("problem_destroy")(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- fields ----------------------------------------------------------------------------------------
+    def shape(self, name):
+        return field_shape(self.grid, name, self.Nsigma, self.sigma_rate)
+
+    def set(self, name, value):
+        """set!(field, value): a number, or an array in interior layout of shape self.shape(name)."""
+        shp = self.shape(name)
+        a = np.broadcast_to(np.asarray(value, dtype=np.float64), shp)
+        a = _as_f64(a)
+        st = self._fn("problem_set_field")(self._h, abi.FIELD_IDS[name], a.ctypes.data_as(_dptr), C.c_int64(a.size))
+        _check(st, f"set {name}", self._err())
+
+    def get(self, name):
+        out = np.empty(self.shape(name), dtype=np.float64)
+        st = self._fn("problem_get_field")(self._h, abi.FIELD_IDS[name], out.ctypes.data_as(_dptr), C.c_int64(out.size))
+        _check(st, f"get {name}", self._err())
+        return out
+
+    # -- the solve --------------------------------------------------------------------------------------
+    def compute_geometry(self):
+        _check(self._fn("compute_geometry")(self._h), "compute_geometry", self._err())
+
+    def compute_rate_factor(self, cold_prefactor=3.61e-13, warm_prefactor=1.73e3, cold_activation_energy=6.0e4,
+                            warm_activation_energy=13.9e4, transition_temperature=263.15, transition_width=1.0,
+                            gas_constant=8.31441, clausius_clapeyron=7.9e-8, melting_temperature=273.15):
+        """ArrheniusRateFactor defaults (src/Rheologies/arrhenius_rate_factor.jl:60-69) and
+        EnthalpyThermodynamics' clausius_clapeyron / melting_temperature (enthalpy_thermodynamics.jl:99-100)."""
+        st = self._fn("compute_rate_factor")(self._h, *[C.c_double(v) for v in (
+            cold_prefactor, warm_prefactor, cold_activation_energy, warm_activation_energy, transition_temperature,
+            transition_width, gas_constant, clausius_clapeyron, melting_temperature)])
+        _check(st, "compute_rate_factor", self._err())
+
+    def update_coefficients(self):
+        _check(self._fn("update_coefficients")(self._h), "update_coefficients", self._err())
+
+    def _vec_in(self, u, v):
+        return _as_f64(np.broadcast_to(np.asarray(u, dtype=np.float64), self.shape("u"))), \
+               _as_f64(np.broadcast_to(np.asarray(v, dtype=np.float64), self.shape("v")))
+
+    def apply_operator(self, pu, pv, qu=None, qv=None):
+        """q = A p (ssa_operator!).  Entries of q outside the Nx x Ny range keep the values passed in."""
+        pu, pv = self._vec_in(pu, pv)
+        qu = np.zeros(self.shape("u")) if qu is None else _as_f64(qu).copy()
+        qv = np.zeros(self.shape("v")) if qv is None else _as_f64(qv).copy()
+        st = self._fn("apply_operator")(self._h, pu.ctypes.data_as(_dptr), pv.ctypes.data_as(_dptr),
+                                        qu.ctypes.data_as(_dptr), qv.ctypes.data_as(_dptr))
+        _check(st, "apply_operator", self._err())
+        return qu, qv
+
+    def precondition(self, ru, rv, zu=None, zv=None):
+        ru, rv = self._vec_in(ru, rv)
+        zu = np.zeros(self.shape("u")) if zu is None else _as_f64(zu).copy()
+        zv = np.zeros(self.shape("v")) if zv is None else _as_f64(zv).copy()
+        st = self._fn("precondition")(self._h, ru.ctypes.data_as(_dptr), rv.ctypes.data_as(_dptr),
+                                      zu.ctypes.data_as(_dptr), zv.ctypes.data_as(_dptr))
+        _check(st, "precondition", self._err())
+        return zu, zv
+
+    def linear_solve(self, bu, bv):
+        """solve!(x, solver, b, coefficients...) from the warm start in fields u, v; returns stats."""
+        bu, bv = self._vec_in(bu, bv)
+        stats = abi.SolveStats()
+        st = self._fn("linear_solve")(self._h, bu.ctypes.data_as(_dptr), bv.ctypes.data_as(_dptr), C.byref(stats))
+        _check(st, "linear_solve", self._err())
+        return stats
+
+    def adjoint_solve(self, bu, bv):
+        """adjoint_solve!(λ, solver, b, ...): λ in fields u, v."""
+        bu, bv = self._vec_in(bu, bv)
+        stats = abi.SolveStats()
+        st = self._fn("adjoint_solve")(self._h, bu.ctypes.data_as(_dptr), bv.ctypes.data_as(_dptr), C.byref(stats))
+        _check(st, "adjoint_solve", self._err())
+        return stats
+
+    def picard_solve(self):
+        """picard_solve!(x, picard, linear_solver, update!, tau, coefficients...): returns stats
+        (stats.picard_iterations is the reference's return value)."""
+        stats = abi.SolveStats()
+        st = self._fn("picard_solve")(self._h, C.byref(stats))
+        _check(st, "picard_solve", self._err())
+        return stats
+
+    def velocity_profile(self):
+        _check(self._fn("velocity_profile")(self._h), "velocity_profile", self._err())
+
+    def multigrid_levels(self):
+        cap = 64
+        nx = (C.c_int32 * cap)()
+        ny = (C.c_int32 * cap)()
+        count = C.c_int32()
+        _check(self._fn("multigrid_levels")(self._h, C.byref(count), nx, ny, cap), "multigrid_levels", self._err())
+        return [(nx[i], ny[i]) for i in range(count.value)]
+
+    # -- multigrid transfers -------------------------------------------------------------------------------
+    def _level_shape(self, level, comp):
+        """(ny, nx) of component comp of a vector on multigrid level `level` (-1 = the finest grid)."""
+        nx, ny = (self.grid.Nx, self.grid.Ny) if level < 0 else self.multigrid_levels()[level]
+        fx = nx if self.grid.periodic(0) else nx + 1
+        fy = ny if self.grid.periodic(1) else ny + 1
+        return (ny, fx) if comp == "u" else (fy, nx)
+
+    def restrict(self, level, fu, fv):
+        """restrict!: coarse = R fine between level - 1 and coarse level `level` (0 = first coarse level)."""
+        fu, fv = _as_f64(fu), _as_f64(fv)
+        cu, cv = np.zeros(self._level_shape(level, "u")), np.zeros(self._level_shape(level, "v"))
+        st = self._fn("multigrid_restrict")(self._h, level, fu.ctypes.data_as(_dptr), fv.ctypes.data_as(_dptr),
+                                            cu.ctypes.data_as(_dptr), cv.ctypes.data_as(_dptr))
+        _check(st, "multigrid_restrict", self._err())
+        return cu, cv
+
+    def prolongate(self, level, cu, cv, fu=None, fv=None):
+        """prolongate!: fine += P coarse (fine starts at zero unless given)."""
+        cu, cv = _as_f64(cu), _as_f64(cv)
+        fu = np.zeros(self._level_shape(level - 1, "u")) if fu is None else _as_f64(fu).copy()
+        fv = np.zeros(self._level_shape(level - 1, "v")) if fv is None else _as_f64(fv).copy()
+        st = self._fn("multigrid_prolongate")(self._h, level, cu.ctypes.data_as(_dptr), cv.ctypes.data_as(_dptr),
+                                              fu.ctypes.data_as(_dptr), fv.ctypes.data_as(_dptr))
+        _check(st, "multigrid_prolongate", self._err())
+        return fu, fv

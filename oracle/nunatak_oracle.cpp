@@ -1,0 +1,1292 @@
+// nunatak_oracle.cpp — TEST INFRASTRUCTURE ONLY.
+//
+// A plain FP64 CPU restatement of Nunatak.jl's velocity solve (Picard iteration around preconditioned
+// conjugate gradients for the SSA / DIVA stress balance on the C grid).  It is the checker of the GPU
+// library: only the tests, the smoke check and the CPU-baseline leg of the benchmark load it.  It is
+// never linked into, or called by, libnunatak_gb300.so.
+//
+// Every function names the reference file:line it restates.  The reference runs on Oceananigans fields
+// with halos; this file keeps that representation (fields with halo cells, fill_halo_regions! with
+// periodic wrap and zero-gradient copies for cell-centred data in Bounded directions) so that the
+// index semantics are the reference's, not the GPU library's clamped / wrapped indexing.
+//
+// Floating-point expressions keep the reference's evaluation order (left-associative sums and
+// products as written in the Julia source).  Build with -ffp-contract=off so that no multiply-add is
+// fused and the results are the same on x86-64 and aarch64.
+//
+// Oceananigans conventions restated here (Oceananigans is not vendored in the reference):
+//   face i is the west face of centre i; Bounded faces run 1..N+1, Periodic faces 1..N;
+//   δxᶠ f(i) = f(i) - f(i-1), δxᶜ f(i) = f(i+1) - f(i); ℑxᶠ f(i) = (f(i-1) + f(i)) / 2,
+//   ℑxᶜ f(i) = (f(i) + f(i+1)) / 2; two-dimensional interpolations interpolate in x, then in y;
+//   Δxᶜ(i) = xᶠ(i+1) - xᶠ(i) (cell width), Δxᶠ(i) = xᶜ(i) - xᶜ(i-1) (centre spacing); Az = Δx Δy at
+//   the location; regular grids use the single spacing L/N for both;
+//   a cell is inactive outside 1..N in a Bounded direction; a Face point is peripheral when either
+//   neighbouring cell is inactive, a Face-Face corner when any of its four cells is.
+#include "../include/nunatak_gb300.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <string>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace oracle {
+
+enum Loc { CENTER = 0, FACE = 1 };
+
+// ------------------------------------------------------------------------------------------------
+// Grid: one axis of a RectilinearGrid (Oceananigans generate_coordinate), with halo nodes.
+// ------------------------------------------------------------------------------------------------
+struct Axis {
+    int N = 0, H = 0;
+    bool periodic = false;
+    bool regular = true;
+    double delta = 0;
+    int lo = 0;                        // lowest stored index (1 - H - 1)
+    std::vector<double> F, C, dC, dF;  // faces, centres, cell widths Δᶜ, centre spacings Δᶠ
+
+    int at(int i) const { return i - lo; }
+    double face(int i) const { return F[at(i)]; }
+    double center(int i) const { return C[at(i)]; }
+    double dc(int i) const { return regular ? delta : dC[at(i)]; }
+    double df(int i) const { return regular ? delta : dF[at(i)]; }
+
+    void build_regular(int n, int h, bool per, double x0, double L) {
+        N = n; H = h; periodic = per; regular = true; delta = L / n;
+        lo = -H - 1;
+        int count = N + 2 * H + 4;
+        F.assign(count, 0); C.assign(count, 0); dC.assign(count, delta); dF.assign(count, delta);
+        for (int i = lo; i < lo + count; ++i) {
+            F[at(i)] = x0 + ((i - 1) * L) / N;
+            C[at(i)] = x0 + ((i - 1) * L) / N + delta / 2;
+        }
+    }
+
+    // Vector of N+1 interior faces: halo faces extend the edge spacing (Bounded) or wrap (Periodic).
+    void build_faces(int n, int h, bool per, const double* faces) {
+        N = n; H = h; periodic = per; regular = false; delta = 0;
+        lo = -H - 1;
+        int count = N + 2 * H + 4;
+        F.assign(count, 0); C.assign(count, 0); dC.assign(count, 0); dF.assign(count, 0);
+        for (int i = 1; i <= N + 1; ++i) F[at(i)] = faces[i - 1];
+        if (per) {
+            double L = faces[N] - faces[0];
+            for (int m = 1; at(1 - m) >= 0; ++m) F[at(1 - m)] = F[at(N + 1 - m)] - L;
+            for (int m = 1; at(N + 1 + m) < count; ++m) F[at(N + 1 + m)] = F[at(1 + m)] + L;
+        } else {
+            double dm = faces[1] - faces[0], dp = faces[N] - faces[N - 1];
+            for (int m = 1; at(1 - m) >= 0; ++m) F[at(1 - m)] = faces[0] - m * dm;
+            for (int m = 1; at(N + 1 + m) < count; ++m) F[at(N + 1 + m)] = faces[N] + m * dp;
+        }
+        for (int i = lo; i < lo + count - 1; ++i) {
+            C[at(i)] = (F[at(i + 1)] + F[at(i)]) / 2;
+            dC[at(i)] = F[at(i + 1)] - F[at(i)];
+        }
+        for (int i = lo + 1; i < lo + count - 1; ++i) dF[at(i)] = C[at(i)] - C[at(i - 1)];
+    }
+
+    // Number of interior points of a field located at `loc` along this axis.
+    int size(Loc loc) const { return (loc == FACE && !periodic) ? N + 1 : N; }
+    bool inactive_cell(int i) const { return !periodic && (i < 1 || i > N); }
+};
+
+struct Grid {
+    Axis x, y;
+    int Nx() const { return x.N; }
+    int Ny() const { return y.N; }
+    bool inactive_cell(int i, int j) const { return x.inactive_cell(i) || y.inactive_cell(j); }
+    // peripheral_node(i, j, k, grid, Face, Center, Center) and friends (Oceananigans Grids/inactive_node.jl)
+    bool peripheral_fc(int i, int j) const { return inactive_cell(i, j) || inactive_cell(i - 1, j); }
+    bool peripheral_cf(int i, int j) const { return inactive_cell(i, j) || inactive_cell(i, j - 1); }
+    bool peripheral_ff(int i, int j) const {
+        return inactive_cell(i, j) || inactive_cell(i - 1, j) || inactive_cell(i, j - 1) || inactive_cell(i - 1, j - 1);
+    }
+    // Metrics (Oceananigans Operators/spacings_and_areas_and_volumes.jl on a RectilinearGrid).
+    double dx_c(int i) const { return x.dc(i); }   // Δxᶜᶜᶜ, Δxᶜᶠᶜ
+    double dx_f(int i) const { return x.df(i); }   // Δxᶠᶜᶜ, Δxᶠᶠᶜ
+    double dy_c(int j) const { return y.dc(j); }   // Δyᶜᶜᶜ, Δyᶠᶜᶜ
+    double dy_f(int j) const { return y.df(j); }   // Δyᶜᶠᶜ, Δyᶠᶠᶜ
+    double Az_ccc(int i, int j) const { return dx_c(i) * dy_c(j); }
+    double Az_fcc(int i, int j) const { return dx_f(i) * dy_c(j); }
+    double Az_cfc(int i, int j) const { return dx_c(i) * dy_f(j); }
+};
+
+// ------------------------------------------------------------------------------------------------
+// Field: two-dimensional Oceananigans Field at (lx, ly) with halos.
+// ------------------------------------------------------------------------------------------------
+struct Field {
+    Loc lx = CENTER, ly = CENTER;
+    const Grid* g = nullptr;
+    int ox = 0, oy = 0, sx = 0, sy = 0;
+    std::vector<double> d;
+    Field() = default;
+    Field(const Grid* grid, Loc lx_, Loc ly_) { init(grid, lx_, ly_); }
+    void init(const Grid* grid, Loc lx_, Loc ly_) {
+        g = grid; lx = lx_; ly = ly_;
+        ox = grid->x.H + 2; oy = grid->y.H + 2;
+        sx = grid->x.N + 2 * grid->x.H + 5; sy = grid->y.N + 2 * grid->y.H + 5;
+        d.assign((size_t)sx * sy, 0.0);
+    }
+    double& operator()(int i, int j) { return d[(size_t)(j + oy) * sx + (i + ox)]; }
+    double operator()(int i, int j) const { return d[(size_t)(j + oy) * sx + (i + ox)]; }
+    int nx() const { return g->x.size(lx); }
+    int ny() const { return g->y.size(ly); }
+    void zero() { std::fill(d.begin(), d.end(), 0.0); }
+};
+
+// fill_halo_regions! with default boundary conditions: Periodic wraps; in a Bounded direction a
+// Center location copies the edge value (zero flux), a Face location is left as it is (its boundary
+// values are interior points and its halo is never read unmasked by the velocity solve).
+static void fill_halo(Field& f) {
+    const Grid& g = *f.g;
+    int Hx = g.x.H + 1, Hy = g.y.H + 1;
+    int Nx = g.x.N, Ny = g.y.N;
+    int nyi = f.ny();
+    for (int j = 1; j <= nyi; ++j) {
+        if (g.x.periodic) {
+            for (int m = 1; m <= Hx; ++m) { f(1 - m, j) = f(Nx + 1 - m, j); f(Nx + m, j) = f(m, j); }
+        } else if (f.lx == CENTER) {
+            for (int m = 1; m <= Hx; ++m) { f(1 - m, j) = f(1, j); f(Nx + m, j) = f(Nx, j); }
+        }
+    }
+    for (int i = -Hx; i <= Nx + 1 + Hx - 1; ++i) {
+        if (g.y.periodic) {
+            for (int m = 1; m <= Hy; ++m) { f(i, 1 - m) = f(i, Ny + 1 - m); f(i, Ny + m) = f(i, m); }
+        } else if (f.ly == CENTER) {
+            for (int m = 1; m <= Hy; ++m) { f(i, 1 - m) = f(i, 1); f(i, Ny + m) = f(i, Ny); }
+        }
+    }
+}
+
+// Field on the sigma grid: Nσ horizontal layers (Center in z).
+struct SigmaField {
+    std::vector<Field> k;
+    void init(const Grid* g, Loc lx, Loc ly, int Ns) { k.assign(Ns, Field(g, lx, ly)); }
+};
+
+struct VelocityVector {        // src/Solvers/velocity_vector.jl:10-33
+    Field u, v;
+    void init(const Grid* g) { u.init(g, FACE, CENTER); v.init(g, CENTER, FACE); }
+};
+
+static void fill_halo(VelocityVector& x) { fill_halo(x.u); fill_halo(x.v); }
+
+template <class F>
+static void for_xy(int Nx, int Ny, F&& f) {   // launch!(arch, grid, :xyz, ...) over 1..Nx x 1..Ny
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= Ny; ++j)
+        for (int i = 1; i <= Nx; ++i) f(i, j);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Masks and strain rates, src/StressBalances/strain_rates.jl:1-32 and
+// src/StressBalances/ssa_operator.jl:90-121.  `eta` is η̄H (operator) or nullptr (`nothing`).
+// ------------------------------------------------------------------------------------------------
+static inline bool ice_free_fc(int i, int j, const Field* mu) { return mu && ((*mu)(i - 1, j) + (*mu)(i, j)) == 0.0; }   // smooth_ice_mask.jl:429
+static inline bool ice_free_cf(int i, int j, const Field* mu) { return mu && ((*mu)(i, j - 1) + (*mu)(i, j)) == 0.0; }   // smooth_ice_mask.jl:430
+static inline bool inactive_fc(const Grid& g, int i, int j, const Field* eta) { return g.peripheral_fc(i, j) || ice_free_fc(i, j, eta); }  // ssa_operator.jl:91
+static inline bool inactive_cf(const Grid& g, int i, int j, const Field* eta) { return g.peripheral_cf(i, j) || ice_free_cf(i, j, eta); }  // ssa_operator.jl:92
+static inline double interior_u(const Grid& g, int i, int j, const Field& u, const Field* eta) { return inactive_fc(g, i, j, eta) ? 0.0 : u(i, j); }  // :94
+static inline double interior_v(const Grid& g, int i, int j, const Field& v, const Field* eta) { return inactive_cf(g, i, j, eta) ? 0.0 : v(i, j); }  // :95
+
+static inline double strain_rate_xx(const Grid& g, int i, int j, const Field& u, const Field* eta) {   // :97
+    return (interior_u(g, i + 1, j, u, eta) - interior_u(g, i, j, u, eta)) / g.dx_c(i);
+}
+static inline double strain_rate_yy(const Grid& g, int i, int j, const Field& v, const Field* eta) {   // :98
+    return (interior_v(g, i, j + 1, v, eta) - interior_v(g, i, j, v, eta)) / g.dy_c(j);
+}
+static inline double wall_shear_factor(int walls) { return walls == NK_NO_SLIP ? 2.0 : 0.0; }         // :100-101
+static inline double strain_rate_xy(const Grid& g, int i, int j, const Field& u, const Field& v, int walls, const Field* eta) {  // :103-106
+    double dudy = (interior_u(g, i, j, u, eta) - interior_u(g, i, j - 1, u, eta)) / g.dy_f(j);
+    double dvdx = (interior_v(g, i, j, v, eta) - interior_v(g, i - 1, j, v, eta)) / g.dx_f(i);
+    double e = (dudy + dvdx) / 2;
+    return g.peripheral_ff(i, j) ? wall_shear_factor(walls) * e : e;
+}
+static inline double strain_rate_xy2(const Grid& g, int i, int j, const Field& u, const Field& v, int walls) {  // :108
+    double e = strain_rate_xy(g, i, j, u, v, walls, nullptr);
+    return e * e;
+}
+// effective_strain_rate², strain_rates.jl:116-121; ℑxyᶜᶜᵃ = ℑyᵃᶜᵃ(ℑxᶜᵃᵃ(·))
+static inline double effective_strain_rate2(const Grid& g, int i, int j, const Field& u, const Field& v, int walls) {
+    double exx = strain_rate_xx(g, i, j, u, nullptr);
+    double eyy = strain_rate_yy(g, i, j, v, nullptr);
+    double a = (strain_rate_xy2(g, i, j, u, v, walls) + strain_rate_xy2(g, i + 1, j, u, v, walls)) / 2;
+    double b = (strain_rate_xy2(g, i, j + 1, u, v, walls) + strain_rate_xy2(g, i + 1, j + 1, u, v, walls)) / 2;
+    double exy2 = (a + b) / 2;
+    return exx * exx + eyy * eyy + exx * eyy + exy2;
+}
+
+// ------------------------------------------------------------------------------------------------
+// SSA operator, src/StressBalances/ssa_operator.jl:47-89.
+// ------------------------------------------------------------------------------------------------
+struct Coefficients {   // the (η̄H, η̄Hᶠᶠ, βᵘ, βᵛ) prefix of the coefficient tuple
+    Field* etaH; Field* etaHff; Field* bu; Field* bv;
+};
+
+static inline double normal_stress_xx(const Grid& g, int i, int j, const Field& u, const Field& v, const Field& eta) {  // :60
+    return 2 * eta(i, j) * (2 * strain_rate_xx(g, i, j, u, &eta) + strain_rate_yy(g, i, j, v, &eta));
+}
+static inline double normal_stress_yy(const Grid& g, int i, int j, const Field& u, const Field& v, const Field& eta) {  // :61
+    return 2 * eta(i, j) * (2 * strain_rate_yy(g, i, j, v, &eta) + strain_rate_xx(g, i, j, u, &eta));
+}
+static inline double shear_stress(const Grid& g, int i, int j, const Field& u, const Field& v, const Field& etaff, int walls, const Field& eta) {  // :62
+    return 2 * etaff(i, j) * strain_rate_xy(g, i, j, u, v, walls, &eta);
+}
+static inline double x_stress_balance(const Grid& g, int i, int j, const Field& u, const Field& v, const Field& eta,
+                                      const Field& etaff, const Field& bu, int walls) {   // :69-73
+    double div = (g.dy_c(j) * normal_stress_xx(g, i, j, u, v, eta) - g.dy_c(j) * normal_stress_xx(g, i - 1, j, u, v, eta)) +
+                 (g.dx_f(i) * shear_stress(g, i, j + 1, u, v, etaff, walls, eta) - g.dx_f(i) * shear_stress(g, i, j, u, v, etaff, walls, eta));
+    return g.Az_fcc(i, j) * bu(i, j) * u(i, j) - div;
+}
+static inline double y_stress_balance(const Grid& g, int i, int j, const Field& u, const Field& v, const Field& eta,
+                                      const Field& etaff, const Field& bv, int walls) {   // :75-79
+    double div = (g.dx_c(i) * normal_stress_yy(g, i, j, u, v, eta) - g.dx_c(i) * normal_stress_yy(g, i, j - 1, u, v, eta)) +
+                 (g.dy_f(j) * shear_stress(g, i + 1, j, u, v, etaff, walls, eta) - g.dy_f(j) * shear_stress(g, i, j, u, v, etaff, walls, eta));
+    return g.Az_cfc(i, j) * bv(i, j) * v(i, j) - div;
+}
+
+// The halos of p, η̄H and η̄Hᶠᶠ must be filled.
+static void ssa_operator(const Grid& g, VelocityVector& q, const VelocityVector& p, const Coefficients& c, int walls) {  // :47-52, :81-89
+    for_xy(g.Nx(), g.Ny(), [&](int i, int j) {
+        bool wu = inactive_fc(g, i, j, c.etaH), wv = inactive_cf(g, i, j, c.etaH);
+        q.u(i, j) = wu ? p.u(i, j) : x_stress_balance(g, i, j, p.u, p.v, *c.etaH, *c.etaHff, *c.bu, walls);
+        q.v(i, j) = wv ? p.v(i, j) : y_stress_balance(g, i, j, p.u, p.v, *c.etaH, *c.etaHff, *c.bv, walls);
+    });
+}
+
+// ------------------------------------------------------------------------------------------------
+// Diagonal preconditioner, src/StressBalances/diagonal_preconditioner.jl:130-175.
+// ------------------------------------------------------------------------------------------------
+static inline double x_normal_diagonal(const Grid& g, int i, int j, const Field& eta) { return 4 * g.dy_c(j) * eta(i, j) / g.dx_c(i); }  // :141
+static inline double y_normal_diagonal(const Grid& g, int i, int j, const Field& eta) { return 4 * g.dx_c(i) * eta(i, j) / g.dy_c(j); }  // :142
+static inline double corner_shear_factor(const Grid& g, int i, int j, int walls) { return g.peripheral_ff(i, j) ? wall_shear_factor(walls) : 1.0; }  // :146
+static inline double x_shear_diagonal(const Grid& g, int i, int j, const Field& ff, int walls) {   // :148-149
+    return corner_shear_factor(g, i, j, walls) * g.dx_f(i) * ff(i, j) / g.dy_f(j);
+}
+static inline double y_shear_diagonal(const Grid& g, int i, int j, const Field& ff, int walls) {   // :150-151
+    return corner_shear_factor(g, i, j, walls) * g.dy_f(j) * ff(i, j) / g.dx_f(i);
+}
+static inline double x_diagonal(const Grid& g, int i, int j, const Coefficients& c, int walls) {   // :153-158
+    double d = g.Az_fcc(i, j) * (*c.bu)(i, j) + x_normal_diagonal(g, i, j, *c.etaH) + x_normal_diagonal(g, i - 1, j, *c.etaH) +
+               x_shear_diagonal(g, i, j, *c.etaHff, walls) + x_shear_diagonal(g, i, j + 1, *c.etaHff, walls);
+    return (inactive_fc(g, i, j, c.etaH) || d == 0.0) ? 1.0 : d;
+}
+static inline double y_diagonal(const Grid& g, int i, int j, const Coefficients& c, int walls) {   // :160-165
+    double d = g.Az_cfc(i, j) * (*c.bv)(i, j) + y_normal_diagonal(g, i, j, *c.etaH) + y_normal_diagonal(g, i, j - 1, *c.etaH) +
+               y_shear_diagonal(g, i, j, *c.etaHff, walls) + y_shear_diagonal(g, i + 1, j, *c.etaHff, walls);
+    return (inactive_cf(g, i, j, c.etaH) || d == 0.0) ? 1.0 : d;
+}
+static void diagonal_precondition(const Grid& g, VelocityVector& z, const VelocityVector& r, const Coefficients& c, int walls) {  // :132-139
+    int nux = z.u.nx(), nuy = z.u.ny(), nvx = z.v.nx(), nvy = z.v.ny();
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= nuy; ++j) for (int i = 1; i <= nux; ++i) z.u(i, j) = r.u(i, j) / x_diagonal(g, i, j, c, walls);
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= nvy; ++j) for (int i = 1; i <= nvx; ++i) z.v(i, j) = r.v(i, j) / y_diagonal(g, i, j, c, walls);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Vector operations, src/Solvers/velocity_vector.jl:48-141.  All act on the Nx x Ny range.
+// ------------------------------------------------------------------------------------------------
+static void linear_combination(const Grid& g, VelocityVector& z, double a, const VelocityVector& x, double b, const VelocityVector& y) {  // :48-62
+    for_xy(g.Nx(), g.Ny(), [&](int i, int j) {
+        z.u(i, j) = a * x.u(i, j) + b * y.u(i, j);
+        z.v(i, j) = a * x.v(i, j) + b * y.v(i, j);
+    });
+}
+static void copyto(const Grid& g, VelocityVector& x, const VelocityVector& y) { linear_combination(g, x, 1.0, y, 0.0, y); }  // :69
+static void axpy(const Grid& g, double a, const VelocityVector& y, VelocityVector& x) { linear_combination(g, x, 1.0, x, a, y); }  // :82
+static void xpby(const Grid& g, const VelocityVector& y, double b, VelocityVector& x) { linear_combination(g, x, 1.0, y, b, x); }  // :89
+static void subtract(const Grid& g, VelocityVector& r, const VelocityVector& b, const VelocityVector& q) { linear_combination(g, r, 1.0, b, -1.0, q); }  // :96
+static void fill_interior(VelocityVector& x, double value) {   // :71-75 (interior includes wall faces)
+    for (int j = 1; j <= x.u.ny(); ++j) for (int i = 1; i <= x.u.nx(); ++i) x.u(i, j) = value;
+    for (int j = 1; j <= x.v.ny(); ++j) for (int i = 1; i <= x.v.nx(); ++i) x.v(i, j) = value;
+}
+
+// Dot product over the Nx x Ny range of each component, vector_dot! :125-133.  Rows are summed in
+// order of increasing i, then rows in order of increasing j, so the result does not depend on the
+// thread count.  (Julia's pairwise `sum` over the parent array differs only in rounding.)
+static double component_dot(const Grid& g, const Field& x, const Field& y) {
+    int Nx = g.Nx(), Ny = g.Ny();
+    std::vector<double> rows(Ny + 1, 0.0);
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= Ny; ++j) {
+        double s = 0;
+        for (int i = 1; i <= Nx; ++i) s += x(i, j) * y(i, j);
+        rows[j] = s;
+    }
+    double s = 0;
+    for (int j = 1; j <= Ny; ++j) s += rows[j];
+    return s;
+}
+static double vector_dot(const Grid& g, const VelocityVector& x, const VelocityVector& y) {
+    return component_dot(g, x.u, y.u) + component_dot(g, x.v, y.v);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Multigrid, src/StressBalances/multigrid_preconditioner.jl.
+// ------------------------------------------------------------------------------------------------
+enum Coarsening { UNCHANGED = 1, HALVED = 2 };
+
+static Coarsening coarsening(int N, int H, int minimum) {   // :86
+    return ((N % 2 == 0) && (N / 2 >= std::max(minimum, H))) ? HALVED : UNCHANGED;
+}
+
+struct Level {   // :98-107
+    std::unique_ptr<Grid> grid;
+    Coarsening cx, cy;
+    Field etaH, etaHff, bu, bv, scratch;
+    VelocityVector x, b, q;
+    std::vector<double> line_t;   // unused: the line solver keeps t in `scratch`
+};
+
+static std::unique_ptr<Grid> coarsened_grid(const Grid& g, Coarsening cx, Coarsening cy) {   // :111-120
+    auto c = std::make_unique<Grid>();
+    int fx = cx, fy = cy;
+    std::vector<double> xf, yf;
+    for (int i = 1; i <= g.x.N + 1; i += fx) xf.push_back(g.x.face(i));
+    for (int j = 1; j <= g.y.N + 1; j += fy) yf.push_back(g.y.face(j));
+    c->x.build_faces(g.x.N / fx, g.x.H, g.x.periodic, xf.data());
+    c->y.build_faces(g.y.N / fy, g.y.H, g.y.periodic, yf.data());
+    return c;
+}
+
+static void coarse_levels(const Grid& g, int minimum, std::vector<std::unique_ptr<Level>>& out) {   // :88-109
+    Coarsening cx = coarsening(g.x.N, g.x.H, minimum), cy = coarsening(g.y.N, g.y.H, minimum);
+    if (cx == UNCHANGED && cy == UNCHANGED) return;
+    auto L = std::make_unique<Level>();
+    L->grid = coarsened_grid(g, cx, cy);
+    L->cx = cx; L->cy = cy;
+    const Grid* cg = L->grid.get();
+    L->etaH.init(cg, CENTER, CENTER); L->etaHff.init(cg, FACE, FACE);
+    L->bu.init(cg, FACE, CENTER); L->bv.init(cg, CENTER, FACE);
+    L->scratch.init(cg, CENTER, CENTER);
+    L->x.init(cg); L->b.init(cg); L->q.init(cg);
+    const Grid& next = *cg;
+    out.push_back(std::move(L));
+    coarse_levels(next, minimum, out);
+}
+
+// restriction_offsets / restriction_index / restriction_weight, :264-283
+static inline void restriction_offsets(Loc l, Coarsening c, int& a0, int& a1) {
+    if (c == UNCHANGED) { a0 = 0; a1 = 0; } else if (l == FACE) { a0 = -1; a1 = 1; } else { a0 = -1; a1 = 2; }
+}
+static inline int mod1(int x, int N) { int r = (x - 1) % N; if (r < 0) r += N; return r + 1; }
+static inline int restriction_index(int I, int a, int N, bool periodic, Loc l, Coarsening c) {
+    if (c == UNCHANGED) return I;
+    if (periodic) return mod1(2 * I - 1 + a, N);
+    if (l == FACE) return std::max(2 * I - 1 + a, 1);
+    return std::min(std::max(2 * I - 1 + a, 1), N);
+}
+static inline double restriction_weight(int I, int a, int Nc, bool periodic, Loc l, Coarsening c) {
+    if (c == UNCHANGED) return 1.0;
+    if (l == FACE) {
+        double w = (a == 0) ? 1.0 : 1.0 / 2;
+        if (!periodic && 2 * I - 1 + a < 1) return 0.0;
+        return w;
+    }
+    double w = (a == 0 || a == 1) ? 3.0 / 4 : 1.0 / 4;
+    if (periodic) return w;
+    bool outside = (I == 1 && a == -1) || (I == Nc && a == 2);
+    bool folded = (I == 1 && a == 0) || (I == Nc && a == 1);
+    w = w + (folded ? 1.0 / 4 : 0.0);
+    return outside ? 0.0 : w;
+}
+// parents, :286-305
+static inline void parents(int i, int Nc, bool periodic, Loc l, Coarsening c, int& I1, int& I2, double& w1, double& w2) {
+    if (c == UNCHANGED) { I1 = i; I2 = i; w1 = 1.0; w2 = 0.0; return; }
+    int I = (i + 1) / 2;
+    bool odd = (i % 2) != 0;
+    if (l == FACE) {
+        int up = periodic ? mod1(I + 1, Nc) : I + 1;
+        I1 = I; I2 = odd ? I : up; w1 = odd ? 1.0 : 1.0 / 2; w2 = odd ? 0.0 : 1.0 / 2;
+    } else {
+        int Ip = odd ? I - 1 : I + 1;
+        I1 = I; I2 = periodic ? mod1(Ip, Nc) : std::min(std::max(Ip, 1), Nc); w1 = 3.0 / 4; w2 = 1.0 / 4;
+    }
+}
+
+// restrict(I, J, k, ℓx, ℓy, cx, cy, coarse_grid, fine_grid, ϕ, args...), :307-318
+template <class Phi>
+static double restrict_point(int I, int J, Loc lx, Loc ly, Coarsening cx, Coarsening cy, const Grid& coarse, const Grid& fine, Phi&& phi) {
+    int a0, a1, b0, b1;
+    restriction_offsets(lx, cx, a0, a1);
+    restriction_offsets(ly, cy, b0, b1);
+    double s = 0;
+    for (int a = a0; a <= a1; ++a)
+        for (int b = b0; b <= b1; ++b) {
+            int i = restriction_index(I, a, fine.x.N, fine.x.periodic, lx, cx);
+            int j = restriction_index(J, b, fine.y.N, fine.y.periodic, ly, cy);
+            double w = restriction_weight(I, a, coarse.x.N, fine.x.periodic, lx, cx) * restriction_weight(J, b, coarse.y.N, fine.y.periodic, ly, cy);
+            s += w * phi(i, j);
+        }
+    return s;
+}
+// prolongate(i, j, k, ℓx, ℓy, cx, cy, fine_grid, coarse_grid, ϕ, args...), :320-327
+template <class Phi>
+static double prolongate_point(int i, int j, Loc lx, Loc ly, Coarsening cx, Coarsening cy, const Grid& fine, const Grid& coarse, Phi&& phi) {
+    int I1, I2, J1, J2; double wx1, wx2, wy1, wy2;
+    parents(i, coarse.x.N, fine.x.periodic, lx, cx, I1, I2, wx1, wx2);
+    parents(j, coarse.y.N, fine.y.periodic, ly, cy, J1, J2, wy1, wy2);
+    return wx1 * (wy1 * phi(I1, J1) + wy2 * phi(I1, J2)) + wx2 * (wy1 * phi(I2, J1) + wy2 * phi(I2, J2));
+}
+
+// ℑxyᶠᶠᵃ(η̄H) over size(η̄Hᶠᶠ), _interpolate_to_corners!, src/StressBalances/stress_balance_coefficients.jl:26-29
+static void interpolate_to_corners(const Grid& g, Field& ff, const Field& eta) {
+    int nx = ff.nx(), ny = ff.ny();
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+            double lo = (eta(i - 1, j - 1) + eta(i, j - 1)) / 2;
+            double hi = (eta(i - 1, j) + eta(i, j)) / 2;
+            ff(i, j) = (lo + hi) / 2;
+        }
+    (void)g;
+}
+
+// _coarsen_coefficients!, :331-344, and coarsen_coefficients!, :130-141
+static void coarsen_coefficients(std::vector<std::unique_ptr<Level>>& levels, size_t l, const Field& eta, const Field& bu, const Field& bv) {
+    if (l >= levels.size()) return;
+    Level& L = *levels[l];
+    const Grid& cg = *L.grid;
+    const Grid& fg = *eta.g;
+    int fx = L.cx, fy = L.cy;
+    for_xy(cg.Nx(), cg.Ny(), [&](int I, int J) {
+        int i = fx * (I - 1) + 1, j = fy * (J - 1) + 1;
+        double S = 0;
+        for (int a = 0; a <= fx - 1; ++a)
+            for (int b = 0; b <= fy - 1; ++b) S += fg.Az_ccc(i + a, j + b) * eta(i + a, j + b);
+        L.etaH(I, J) = S / cg.Az_ccc(I, J);
+        L.bu(I, J) = restrict_point(I, J, FACE, CENTER, L.cx, L.cy, cg, fg, [&](int ii, int jj) { return fg.Az_fcc(ii, jj) * bu(ii, jj); }) / cg.Az_fcc(I, J);
+        L.bv(I, J) = restrict_point(I, J, CENTER, FACE, L.cx, L.cy, cg, fg, [&](int ii, int jj) { return fg.Az_cfc(ii, jj) * bv(ii, jj); }) / cg.Az_cfc(I, J);
+    });
+    fill_halo(L.etaH);
+    interpolate_to_corners(cg, L.etaHff, L.etaH);
+    fill_halo(L.etaHff);
+    fill_halo(L.bu); fill_halo(L.bv);
+    coarsen_coefficients(levels, l + 1, L.etaH, L.bu, L.bv);
+}
+
+// _restrict!, :346-352
+static void restrict_vector(const Grid& cg, const Grid& fg, Level& L, VelocityVector& coarse, const VelocityVector& fine, const Field& coarse_eta, const Field& fine_eta) {
+    for_xy(cg.Nx(), cg.Ny(), [&](int I, int J) {
+        coarse.u(I, J) = inactive_fc(cg, I, J, &coarse_eta) ? 0.0 :
+            restrict_point(I, J, FACE, CENTER, L.cx, L.cy, cg, fg, [&](int i, int j) { return interior_u(fg, i, j, fine.u, &fine_eta); });
+        coarse.v(I, J) = inactive_cf(cg, I, J, &coarse_eta) ? 0.0 :
+            restrict_point(I, J, CENTER, FACE, L.cx, L.cy, cg, fg, [&](int i, int j) { return interior_v(fg, i, j, fine.v, &fine_eta); });
+    });
+}
+// _prolongate!, :354-360
+static void prolongate_vector(const Grid& fg, const Grid& cg, Level& L, VelocityVector& fine, const VelocityVector& coarse, const Field& fine_eta, const Field& coarse_eta) {
+    for_xy(fg.Nx(), fg.Ny(), [&](int i, int j) {
+        fine.u(i, j) += inactive_fc(fg, i, j, &fine_eta) ? 0.0 :
+            prolongate_point(i, j, FACE, CENTER, L.cx, L.cy, fg, cg, [&](int I, int J) { return interior_u(cg, I, J, coarse.u, &coarse_eta); });
+        fine.v(i, j) += inactive_cf(fg, i, j, &fine_eta) ? 0.0 :
+            prolongate_point(i, j, CENTER, FACE, L.cx, L.cy, fg, cg, [&](int I, int J) { return interior_v(cg, I, J, coarse.v, &coarse_eta); });
+    });
+}
+
+// ℓ1-Jacobi row sums, :195-211
+static inline double x_absolute_row_sum(const Grid& g, int i, int j, const Coefficients& c, int walls) {
+    const Field& eta = *c.etaH; const Field& ff = *c.etaHff;
+    double s = g.Az_fcc(i, j) * (*c.bu)(i, j) +
+               2 * (x_normal_diagonal(g, i, j, eta) + x_normal_diagonal(g, i - 1, j, eta)) +
+               4 * (eta(i, j) + eta(i - 1, j)) +
+               2 * (x_shear_diagonal(g, i, j, ff, walls) + x_shear_diagonal(g, i, j + 1, ff, walls)) +
+               2 * (corner_shear_factor(g, i, j, walls) * ff(i, j) + corner_shear_factor(g, i, j + 1, walls) * ff(i, j + 1));
+    return (inactive_fc(g, i, j, &eta) || s == 0.0) ? 1.0 : s;
+}
+static inline double y_absolute_row_sum(const Grid& g, int i, int j, const Coefficients& c, int walls) {
+    const Field& eta = *c.etaH; const Field& ff = *c.etaHff;
+    double s = g.Az_cfc(i, j) * (*c.bv)(i, j) +
+               2 * (y_normal_diagonal(g, i, j, eta) + y_normal_diagonal(g, i, j - 1, eta)) +
+               4 * (eta(i, j) + eta(i, j - 1)) +
+               2 * (y_shear_diagonal(g, i, j, ff, walls) + y_shear_diagonal(g, i + 1, j, ff, walls)) +
+               2 * (corner_shear_factor(g, i, j, walls) * ff(i, j) + corner_shear_factor(g, i + 1, j, walls) * ff(i + 1, j));
+    return (inactive_cf(g, i, j, &eta) || s == 0.0) ? 1.0 : s;
+}
+// y-line couplings, :223-227
+static inline double x_line_coupling(const Grid& g, int i, int j, const Coefficients& c, int walls) {
+    return (inactive_fc(g, i, j - 1, c.etaH) || inactive_fc(g, i, j, c.etaH)) ? 0.0 : x_shear_diagonal(g, i, j, *c.etaHff, walls);
+}
+static inline double y_line_coupling(const Grid& g, int i, int j, const Coefficients& c, int walls) {
+    return (inactive_cf(g, i, j - 1, c.etaH) || inactive_cf(g, i, j, c.etaH)) ? 0.0 : y_normal_diagonal(g, i, j - 1, *c.etaH);
+}
+
+// line_relax!, :231-253 (Thomas algorithm along j with M = tridiagonal block + absolute couplings)
+template <class RowSum, class Coupling>
+static void line_relax(const Grid& g, Field& x, const Field& b, Field& q, Field& t, int i, RowSum&& row_sum, Coupling&& coupling) {
+    int Ny = g.Ny();
+    double cj = 0, tj = 0, dj = 0;
+    for (int j = 1; j <= Ny; ++j) {
+        double s = row_sum(i, j);
+        double cj1 = (j == Ny) ? 0.0 : coupling(i, j + 1);
+        double m = s - cj - cj1 + cj * tj;
+        dj = (b(i, j) - q(i, j) + cj * dj) / m;
+        tj = -cj1 / m;
+        t(i, j) = tj;
+        q(i, j) = dj;
+        cj = cj1;
+    }
+    double delta = 0;
+    for (int j = Ny; j >= 1; --j) {
+        delta = q(i, j) - t(i, j) * delta;
+        x(i, j) += delta;
+    }
+}
+
+// smooth!, :165-180 and _smooth! / _line_smooth!, :213-219, :255-259
+static void smooth(const Grid& g, VelocityVector& x, const VelocityVector& b, VelocityVector& q, Field& t, const Coefficients& c,
+                   int walls, int smoother, int sweeps) {
+    for (int s = 0; s < sweeps; ++s) {
+        fill_halo(x);
+        ssa_operator(g, q, x, c, walls);
+        if (smoother == NK_SMOOTHER_POINT_JACOBI) {
+            for_xy(g.Nx(), g.Ny(), [&](int i, int j) {
+                x.u(i, j) += (b.u(i, j) - q.u(i, j)) / x_absolute_row_sum(g, i, j, c, walls);
+                x.v(i, j) += (b.v(i, j) - q.v(i, j)) / y_absolute_row_sum(g, i, j, c, walls);
+            });
+        } else {
+#pragma omp parallel for schedule(static)
+            for (int i = 1; i <= g.Nx(); ++i) {
+                line_relax(g, x.u, b.u, q.u, t, i, [&](int ii, int jj) { return x_absolute_row_sum(g, ii, jj, c, walls); },
+                           [&](int ii, int jj) { return x_line_coupling(g, ii, jj, c, walls); });
+                line_relax(g, x.v, b.v, q.v, t, i, [&](int ii, int jj) { return y_absolute_row_sum(g, ii, jj, c, walls); },
+                           [&](int ii, int jj) { return y_line_coupling(g, ii, jj, c, walls); });
+            }
+        }
+    }
+}
+
+struct Multigrid {   // StressBalanceMultigridPreconditioner, :18-62
+    std::vector<std::unique_ptr<Level>> levels;
+    VelocityVector residual;
+    Field scratch;
+    int smoother = NK_SMOOTHER_POINT_JACOBI, sweeps = 2, coarsest = 20;
+};
+
+// v_cycle!, :144-163
+static void v_cycle(const Grid& g, VelocityVector& x, const VelocityVector& b, VelocityVector& q, Field& t, const Coefficients& c,
+                    Multigrid& P, size_t l, int walls) {
+    if (l >= P.levels.size()) {
+        fill_interior(x, 0.0);
+        smooth(g, x, b, q, t, c, walls, P.smoother, P.coarsest);
+        return;
+    }
+    Level& C = *P.levels[l];
+    fill_interior(x, 0.0);
+    smooth(g, x, b, q, t, c, walls, P.smoother, P.sweeps);
+    fill_halo(x);
+    ssa_operator(g, q, x, c, walls);
+    subtract(g, q, b, q);
+    fill_halo(q);
+    restrict_vector(*C.grid, g, C, C.b, q, C.etaH, *c.etaH);
+    Coefficients cc{&C.etaH, &C.etaHff, &C.bu, &C.bv};
+    v_cycle(*C.grid, C.x, C.b, C.q, C.scratch, cc, P, l + 1, walls);
+    fill_halo(C.x);
+    prolongate_vector(g, *C.grid, C, x, C.x, *c.etaH, C.etaH);
+    smooth(g, x, b, q, t, c, walls, P.smoother, P.sweeps);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Rheology, friction, column integrals, DIVA.
+// ------------------------------------------------------------------------------------------------
+struct Sigma {   // SigmaGrid column: faces ζ_0..ζ_Nσ (src/Grids/sigma_grid.jl:264-266)
+    int N = 1;
+    std::vector<double> faces;
+    double zf(int k) const { return faces[k - 1]; }                       // znode(k, Face), k = 1..N+1
+    double zc(int k) const { return (faces[k - 1] + faces[k]) / 2; }      // znode(k, Center)
+};
+
+// Exact integral of (1 - ζ)^p, src/StressBalances/column_integrals.jl:31
+static inline double ipow(double x, int n) { double r = x; for (int m = 1; m < n; ++m) r *= x; return r; }
+static inline double power_integral(double zm, double zp, int p) { return (ipow(1 - zm, p + 1) - ipow(1 - zp, p + 1)) / (p + 1); }
+static inline double layer_weight(const Sigma& s, int k, int p) { return power_integral(s.zf(k), s.zf(k + 1), p); }   // :34-35
+static inline double profile_weight(const Sigma& s, int kp, int k, int p) {   // :38-43
+    double zm = s.zf(kp);
+    double zp = (kp == k) ? s.zc(k) : s.zf(kp + 1);
+    return power_integral(zm, zp, p);
+}
+static inline double layer_thickness(const Sigma& s, int k) { return s.zf(k + 1) - s.zf(k); }   // :73-74
+
+struct Physics {
+    int walls = NK_FREE_SLIP;
+    double n = 3, eps0 = 1e-13;
+    int friction = NK_FRICTION_NONE;
+    double m = 1.0 / 3, alpha2 = 0.5, u0 = 1e-8;
+    double rho_i = 918, rho_w = 1028, g = 9.81;
+};
+
+static inline double basal_drag(double U, double C, double N, const Physics& ph) {   // frictions.jl:83-89
+    if (ph.friction == NK_WEERTMAN) return C * std::pow(U, ph.m - 1);
+    double tc = ph.alpha2 * N;
+    return C * std::pow(U, ph.m - 1) * tc / std::pow(std::pow(C, 1 / ph.m) * U + std::pow(tc, 1 / ph.m), ph.m);
+}
+
+// compute_basal_drag!, frictions.jl:127-160.  N may be nullptr (`nothing`).
+static void compute_basal_drag(const Grid& g, Field& bu, Field& bv, const Physics& ph, const Field& u, const Field& v,
+                               const Field& phu, const Field& phv, const Field* N, const Field& C) {
+    if (ph.friction == NK_FRICTION_NONE) return;
+    double u02 = ph.u0 * ph.u0;
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= bu.ny(); ++j)
+        for (int i = 1; i <= bu.nx(); ++i) {
+            double vf = ((v(i - 1, j) + v(i, j)) / 2 + (v(i - 1, j + 1) + v(i, j + 1)) / 2) / 2;   // ℑxyᶠᶜᵃ(v)
+            double U = std::sqrt(u(i, j) * u(i, j) + vf * vf + u02);
+            double Cf = (C(i - 1, j) + C(i, j)) / 2;
+            double Nf = N ? ((*N)(i - 1, j) + (*N)(i, j)) / 2 : 0.0;
+            double b = phu(i, j) * basal_drag(U, Cf, Nf, ph);
+            bu(i, j) = g.peripheral_fc(i, j) ? 0.0 : b;
+        }
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= bv.ny(); ++j)
+        for (int i = 1; i <= bv.nx(); ++i) {
+            double uf = ((u(i, j - 1) + u(i + 1, j - 1)) / 2 + (u(i, j) + u(i + 1, j)) / 2) / 2;   // ℑxyᶜᶠᵃ(u)
+            double U = std::sqrt(v(i, j) * v(i, j) + uf * uf + u02);
+            double Cf = (C(i, j - 1) + C(i, j)) / 2;
+            double Nf = N ? ((*N)(i, j - 1) + (*N)(i, j)) / 2 : 0.0;
+            double b = phv(i, j) * basal_drag(U, Cf, Nf, ph);
+            bv(i, j) = g.peripheral_cf(i, j) ? 0.0 : b;
+        }
+}
+
+// Glen viscosity, src/Rheologies/glen_flow_law.jl:198-212 (membrane) and :223-244 (DIVA vertical shear).
+// A is 2-D (A2) or on the sigma grid (A3); bbu/bbv/ub/vb non-null selects the DIVA form.
+static void compute_viscosity(const Grid& g, const Sigma& sg, SigmaField& eta_s, const Physics& ph, const Field& u, const Field& v,
+                              const Field* A2, const SigmaField* A3,
+                              const Field* bbu, const Field* bbv, const Field* ub, const Field* vb) {
+    double n = ph.n;
+    double e0 = ph.eps0;
+    for_xy(g.Nx(), g.Ny(), [&](int i, int j) {
+        double e2 = effective_strain_rate2(g, i, j, u, v, ph.walls);
+        for (int k = 1; k <= sg.N; ++k) {
+            double A = A3 ? A3->k[k - 1](i, j) : (*A2)(i, j);
+            double ee;
+            if (bbu) {
+                double zeta = sg.zc(k);
+                double em = eta_s.k[k - 1](i, j);
+                em = (em == 0.0) ? std::numeric_limits<double>::infinity() : em;
+                double tx = ((*bbu)(i, j) * (*ub)(i, j) + (*bbu)(i + 1, j) * (*ub)(i + 1, j)) / 2;   // ℑxᶜᵃᵃ(βᵇᵘ uᵇ)
+                double ty = ((*bbv)(i, j) * (*vb)(i, j) + (*bbv)(i, j + 1) * (*vb)(i, j + 1)) / 2;   // ℑyᵃᶜᵃ(βᵇᵛ vᵇ)
+                double exz = tx * (1 - zeta) / (2 * em);
+                double eyz = ty * (1 - zeta) / (2 * em);
+                ee = e2 + exz * exz + eyz * eyz + e0 * e0;
+            } else {
+                ee = e2 + e0 * e0;
+            }
+            eta_s.k[k - 1](i, j) = std::pow(A, -1 / n) * std::pow(ee, (1 - n) / (2 * n)) / 2;
+        }
+    });
+}
+
+// compute_column_integrals!, src/StressBalances/column_integrals.jl:83-101.  mu may be nullptr.
+static void compute_column_integrals(const Grid& g, const Sigma& sg, Field& etaH, Field& F2, const SigmaField& eta_s,
+                                     const Field& H, const Field* mu) {
+    for_xy(g.Nx(), g.Ny(), [&](int i, int j) {
+        double e = 0, F = 0;
+        for (int k = 1; k <= sg.N; ++k) {
+            e += eta_s.k[k - 1](i, j) * layer_thickness(sg, k);
+            F += (1 / eta_s.k[k - 1](i, j)) * layer_weight(sg, k, 2);
+        }
+        double m = mu ? (*mu)(i, j) : 1.0;
+        etaH(i, j) = mu ? e * H(i, j) * m : e * H(i, j);
+        F2(i, j) = F * H(i, j);
+    });
+}
+
+// DIVA, src/StressBalances/diva.jl:161-211
+static void compute_basal_velocities(const Grid& g, Field& ub, Field& vb, const Field& u, const Field& v, const Field& bbu, const Field& bbv, const Field& F2) {
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= ub.ny(); ++j)
+        for (int i = 1; i <= ub.nx(); ++i) ub(i, j) = u(i, j) / (1 + bbu(i, j) * ((F2(i - 1, j) + F2(i, j)) / 2));
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= vb.ny(); ++j)
+        for (int i = 1; i <= vb.nx(); ++i) vb(i, j) = v(i, j) / (1 + bbv(i, j) * ((F2(i, j - 1) + F2(i, j)) / 2));
+    (void)g;
+}
+static void compute_effective_drag(Field& bu, Field& bv, const Field& bbu, const Field& bbv, const Field& F2) {
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= bu.ny(); ++j)
+        for (int i = 1; i <= bu.nx(); ++i) bu(i, j) = bbu(i, j) / (1 + bbu(i, j) * ((F2(i - 1, j) + F2(i, j)) / 2));
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= bv.ny(); ++j)
+        for (int i = 1; i <= bv.nx(); ++i) bv(i, j) = bbv(i, j) / (1 + bbv(i, j) * ((F2(i, j - 1) + F2(i, j)) / 2));
+}
+
+// ------------------------------------------------------------------------------------------------
+// Geometry and driving stress.
+// ------------------------------------------------------------------------------------------------
+static inline double nonzero(double x) { return x == 0.0 ? 1.0 : x; }   // subgrid_grounded_fraction.jl:176
+static inline double segment_grounded_fraction(double f1, double f2) {   // :159-163
+    double fp = std::max(f1, 0.0) + std::max(f2, 0.0);
+    double S = std::abs(f1) + std::abs(f2);
+    return S == 0.0 ? 1.0 : fp / nonzero(S);
+}
+static inline double triangle_grounded_fraction(double f1, double f2, double f3) {   // :166-174
+    double a = std::min(std::min(f1, f2), f3);
+    double c = std::max(std::max(f1, f2), f3);
+    double b = f1 + f2 + f3 - a - c;
+    double one_grounded = c * c / nonzero((c - a) * (c - b));
+    double one_floating = 1.0 - a * a / nonzero((b - a) * (c - a));
+    double phi = b > 0 ? one_floating : one_grounded;
+    return a >= 0 ? 1.0 : (c <= 0 ? 0.0 : phi);
+}
+
+struct Problem;
+
+}  // namespace oracle
+
+// ==================================================================================================
+// Problem object and the C entry points (same shape as the library's nk_* functions).
+// ==================================================================================================
+namespace oracle {
+
+struct Problem {
+    Grid grid;
+    Sigma sigma;
+    Physics ph;
+    nk_physics_desc pdesc{};
+    nk_solver_desc sdesc{};
+    int stress_balance = NK_SSA;
+    int rate_layout = NK_RATE_FACTOR_2D;
+    bool use_mask = true, use_N = true;
+    int grounding = 1, gl_stress = 0;
+    double mask_min = 1, mask_trans = 1;
+
+    VelocityVector x, tau;
+    Field H, bed, s, mu, phi, phu, phv, N, C, A2, etaH, etaHff, bu, bv, F2, bbu, bbv, ub, vb;
+    SigmaField A3, eta_s, T, us, vs;
+
+    // CG workspace (VelocityConjugateGradientSolver, conjugate_gradient.jl:193-243) and Picard x⁻
+    VelocityVector r, z, p, q, w, xprev;
+    Multigrid mg;
+    bool mg_ready = false;
+};
+
+static Coefficients coeffs(Problem& P) { return Coefficients{&P.etaH, &P.etaHff, &P.bu, &P.bv}; }
+
+static void update_preconditioner(Problem& P) {   // conjugate_gradient.jl:177; multigrid_preconditioner.jl:128
+    if (P.sdesc.preconditioner == NK_PRECONDITIONER_MULTIGRID) coarsen_coefficients(P.mg.levels, 0, P.etaH, P.bu, P.bv);
+}
+
+static void precondition(Problem& P, VelocityVector& z, VelocityVector& r) {
+    Coefficients c = coeffs(P);
+    switch (P.sdesc.preconditioner) {
+        case NK_PRECONDITIONER_NONE: copyto(P.grid, z, r); break;                        // conjugate_gradient.jl:174
+        case NK_PRECONDITIONER_DIAGONAL: diagonal_precondition(P.grid, z, r, c, P.ph.walls); break;
+        default: v_cycle(P.grid, z, r, P.mg.residual, P.mg.scratch, c, P.mg, 0, P.ph.walls); break;  // multigrid :122-126
+    }
+}
+
+// conjugate_gradient!, conjugate_gradient.jl:299-364.  Returns the iteration count.
+static int conjugate_gradient(Problem& P, VelocityVector& x, const VelocityVector& b, nk_solve_stats* st, int* status) {
+    const Grid& g = P.grid;
+    Coefficients c = coeffs(P);
+    VelocityVector &r = P.r, &z = P.z, &p = P.p, &q = P.q;
+    fill_halo(x);
+    ssa_operator(g, q, x, c, P.ph.walls);
+    subtract(g, r, b, q);
+    update_preconditioner(P);
+    precondition(P, z, r);
+    copyto(g, p, z);
+    double rho = vector_dot(g, r, z);
+
+    auto step = [&](double rho_) {   // conjugate_gradient_step!, :343-364
+        fill_halo(p);
+        ssa_operator(g, q, p, c, P.ph.walls);
+        double pq = vector_dot(g, p, q);
+        double alpha = pq == 0.0 ? 0.0 : rho_ / pq;
+        axpy(g, alpha, p, x);
+        axpy(g, -alpha, q, r);
+        precondition(P, z, r);
+        double rho1 = vector_dot(g, r, z);
+        double beta = rho_ == 0.0 ? 0.0 : rho1 / rho_;
+        xpby(g, z, beta, p);
+        return rho1;
+    };
+
+    const nk_iteration_control& ctl = P.sdesc.linear;
+    int it = 0;
+    double r0 = std::sqrt(vector_dot(g, r, r));
+    double rn = r0;
+    if (ctl.kind == NK_FIXED_ITERATIONS) {   // :319-324
+        for (int k = 0; k < ctl.iterations; ++k) rho = step(rho);
+        it = ctl.iterations;
+        rn = std::sqrt(vector_dot(g, r, r));
+    } else {                                  // :326-341
+        double tol = std::max(ctl.reltol * r0, ctl.abstol);
+        while (rn > tol && it < ctl.maxiter) {
+            rho = step(rho);
+            rn = std::sqrt(vector_dot(g, r, r));
+            ++it;
+        }
+        if (rn > tol && *status == NK_OK) *status = NK_NOT_CONVERGED;
+    }
+    if (!std::isfinite(rn)) *status = NK_NONFINITE;
+    if (st) { st->residual_norm = rn; st->initial_residual_norm = r0; st->linear_iterations_last = it; st->linear_iterations_total += it; }
+    return it;
+}
+
+static const Field* mu_or_null(Problem& P) { return P.use_mask ? &P.mu : nullptr; }
+
+// update_stress_balance_coefficients!, stress_balance_coefficients.jl:10-20
+static void update_ssa(Problem& P) {
+    const Grid& g = P.grid;
+    fill_halo(P.x);
+    compute_viscosity(g, P.sigma, P.eta_s, P.ph, P.x.u, P.x.v, P.rate_layout == NK_RATE_FACTOR_2D ? &P.A2 : nullptr,
+                      P.rate_layout == NK_RATE_FACTOR_SIGMA ? &P.A3 : nullptr, nullptr, nullptr, nullptr, nullptr);
+    compute_column_integrals(g, P.sigma, P.etaH, P.F2, P.eta_s, P.H, mu_or_null(P));
+    fill_halo(P.etaH);
+    interpolate_to_corners(g, P.etaHff, P.etaH);
+    fill_halo(P.etaHff);
+    compute_basal_drag(g, P.bu, P.bv, P.ph, P.x.u, P.x.v, P.phu, P.phv, P.use_N ? &P.N : nullptr, P.C);
+    fill_halo(P.bu); fill_halo(P.bv);
+}
+
+// update_diva_coefficients!, diva.jl:221-235
+static void update_diva(Problem& P) {
+    const Grid& g = P.grid;
+    fill_halo(P.x);
+    compute_basal_velocities(g, P.ub, P.vb, P.x.u, P.x.v, P.bbu, P.bbv, P.F2);
+    fill_halo(P.ub); fill_halo(P.vb);
+    compute_basal_drag(g, P.bbu, P.bbv, P.ph, P.ub, P.vb, P.phu, P.phv, P.use_N ? &P.N : nullptr, P.C);
+    fill_halo(P.bbu); fill_halo(P.bbv);
+    compute_viscosity(g, P.sigma, P.eta_s, P.ph, P.x.u, P.x.v, P.rate_layout == NK_RATE_FACTOR_2D ? &P.A2 : nullptr,
+                      P.rate_layout == NK_RATE_FACTOR_SIGMA ? &P.A3 : nullptr, &P.bbu, &P.bbv, &P.ub, &P.vb);
+    compute_column_integrals(g, P.sigma, P.etaH, P.F2, P.eta_s, P.H, mu_or_null(P));
+    fill_halo(P.etaH); fill_halo(P.F2);
+    interpolate_to_corners(g, P.etaHff, P.etaH);
+    fill_halo(P.etaHff);
+    compute_effective_drag(P.bu, P.bv, P.bbu, P.bbv, P.F2);
+    fill_halo(P.bu); fill_halo(P.bv);
+}
+
+static void update_coefficients(Problem& P) { if (P.stress_balance == NK_DIVA) update_diva(P); else update_ssa(P); }
+
+// picard_solve!, picard.jl:63-90
+static void picard_solve(Problem& P, nk_solve_stats* st) {
+    const Grid& g = P.grid;
+    int status = NK_OK;
+    const nk_iteration_control& ctl = P.sdesc.picard;
+    int it = 0;
+    if (st) { std::memset(st, 0, sizeof(*st)); }
+    if (ctl.kind == NK_FIXED_ITERATIONS) {
+        for (int k = 0; k < ctl.iterations; ++k) { update_coefficients(P); conjugate_gradient(P, P.x, P.tau, st, &status); }
+        it = ctl.iterations;
+    } else {
+        double D = std::numeric_limits<double>::infinity(), X = 0;
+        while (D > std::max(ctl.reltol * X, ctl.abstol) && it < ctl.maxiter) {
+            copyto(g, P.xprev, P.x);
+            update_coefficients(P);
+            conjugate_gradient(P, P.x, P.tau, st, &status);
+            axpy(g, -1.0, P.x, P.xprev);
+            D = std::sqrt(vector_dot(g, P.xprev, P.xprev));
+            X = std::sqrt(vector_dot(g, P.x, P.x));
+            ++it;
+        }
+        if (D > std::max(ctl.reltol * X, ctl.abstol) && status == NK_OK) status = NK_NOT_CONVERGED;
+        if (st) { st->picard_change = D; st->picard_norm = X; }
+        if (!std::isfinite(D) && it > 0) status = NK_NONFINITE;
+    }
+    fill_halo(P.x);
+    if (st) { st->picard_iterations = it; st->status = status; }
+}
+
+// update_geometry!, ice_sheet_model_methods.jl:103-111, and compute_driving_stress!, driving_stress.jl:43-125.
+static void compute_geometry(Problem& P) {
+    const Grid& g = P.grid;
+    double rw_ri = P.ph.rho_w / P.ph.rho_i, ri_rw = P.ph.rho_i / P.ph.rho_w;
+    int Nx = g.Nx(), Ny = g.Ny();
+    // compute_surface_elevation!, subgrid_grounded_fraction.jl:336-357
+    for_xy(Nx, Ny, [&](int i, int j) {
+        P.s(i, j) = P.grounding ? std::max(P.bed(i, j) + P.H(i, j), (1 - ri_rw) * P.H(i, j)) : P.bed(i, j) + P.H(i, j);
+    });
+    // compute_grounded_fractions!, :234-264
+    auto f = [&](int i, int j) { return P.H(i, j) + rw_ri * P.bed(i, j); };
+    if (P.grounding) {
+        for_xy(Nx, Ny, [&](int i, int j) {
+            double fc = f(i, j);
+            double fe = (fc + f(i + 1, j)) / 2, fw = (fc + f(i - 1, j)) / 2, fn = (fc + f(i, j + 1)) / 2, fs = (fc + f(i, j - 1)) / 2;
+            double fne = (fc + f(i + 1, j) + f(i, j + 1) + f(i + 1, j + 1)) / 4;
+            double fnw = (fc + f(i - 1, j) + f(i, j + 1) + f(i - 1, j + 1)) / 4;
+            double fse = (fc + f(i + 1, j) + f(i, j - 1) + f(i + 1, j - 1)) / 4;
+            double fsw = (fc + f(i - 1, j) + f(i, j - 1) + f(i - 1, j - 1)) / 4;
+            double phi = triangle_grounded_fraction(fc, fe, fne) + triangle_grounded_fraction(fc, fn, fne) +
+                         triangle_grounded_fraction(fc, fn, fnw) + triangle_grounded_fraction(fc, fw, fnw) +
+                         triangle_grounded_fraction(fc, fw, fsw) + triangle_grounded_fraction(fc, fs, fsw) +
+                         triangle_grounded_fraction(fc, fs, fse) + triangle_grounded_fraction(fc, fe, fse);
+            P.phi(i, j) = phi / 8;
+        });
+        for (int j = 1; j <= P.phu.ny(); ++j) for (int i = 1; i <= P.phu.nx(); ++i) P.phu(i, j) = segment_grounded_fraction(f(i - 1, j), f(i, j));
+        for (int j = 1; j <= P.phv.ny(); ++j) for (int i = 1; i <= P.phv.nx(); ++i) P.phv(i, j) = segment_grounded_fraction(f(i, j - 1), f(i, j));
+    } else {
+        for (int j = 1; j <= Ny; ++j) for (int i = 1; i <= Nx; ++i) P.phi(i, j) = 1;
+        for (int j = 1; j <= P.phu.ny(); ++j) for (int i = 1; i <= P.phu.nx(); ++i) P.phu(i, j) = 1;
+        for (int j = 1; j <= P.phv.ny(); ++j) for (int i = 1; i <= P.phv.nx(); ++i) P.phv(i, j) = 1;
+    }
+    // compute_effective_pressure!, :293-308 (ocean-connected law)
+    double rig = P.ph.rho_i * P.ph.g, rwg = P.ph.rho_w * P.ph.g;
+    for_xy(Nx, Ny, [&](int i, int j) {
+        double P0 = rig * P.H(i, j);
+        P.N(i, j) = std::max(P0 + rwg * std::min(P.bed(i, j), 0.0), 0.0);
+    });
+    // compute_ice_mask!, smooth_ice_mask.jl:407-426
+    for_xy(Nx, Ny, [&](int i, int j) {
+        double t = std::min(std::max((P.H(i, j) - P.mask_min) / P.mask_trans, 0.0), 1.0);
+        P.mu(i, j) = t * t * (3 - 2 * t);
+    });
+    fill_halo(P.s); fill_halo(P.N); fill_halo(P.mu); fill_halo(P.phi); fill_halo(P.phu); fill_halo(P.phv);
+
+    // compute_driving_stress!, driving_stress.jl:43-125
+    const Field* mu = mu_or_null(P);
+    double ri = P.ph.rho_i, rw = P.ph.rho_w, gg = P.ph.g;
+    auto front_force = [&](int i, int j) {   // :56-60
+        double Hi = P.H(i, j);
+        double D = std::min(std::max(Hi - P.s(i, j), 0.0), Hi);
+        return gg * (ri * Hi * Hi - rw * D * D) / 2;
+    };
+    auto gl_stress = [&](double H1, double H2, double s1, double s2, double b1, double b2, bool& straddles) {   // :84-92
+        double f1 = H1 + rw / ri * b1, f2 = H2 + rw / ri * b2;
+        straddles = ((f1 > 0) != (f2 > 0)) && (H1 > 0) && (H2 > 0);
+        double theta = f1 / (straddles ? f1 - f2 : 1.0);
+        double Hg = H1 + theta * (H2 - H1);
+        double sg = (1 - ri / rw) * Hg;
+        return -ri * gg * ((H1 + Hg) * (sg - s1) + (Hg + H2) * (s2 - sg)) / 2;
+    };
+    for (int j = 1; j <= P.tau.u.ny(); ++j)
+        for (int i = 1; i <= P.tau.u.nx(); ++i) {   // _compute_x_driving_stress!, :109-116
+            bool wall = inactive_fc(g, i, j, mu);
+            bool front = false; double tf = 0;
+            if (mu) {
+                bool w = (*mu)(i - 1, j) > 0 && !((*mu)(i, j) > 0), e = !((*mu)(i - 1, j) > 0) && (*mu)(i, j) > 0;
+                double F = (w ? front_force(i - 1, j) : 0.0) - (e ? front_force(i, j) : 0.0);
+                front = w || e; tf = g.dy_c(j) * F;
+            }
+            bool straddles = false; double tg = 0;
+            if (P.gl_stress) {
+                tg = g.dy_c(j) * gl_stress(P.H(i - 1, j), P.H(i, j), P.s(i - 1, j), P.s(i, j), P.bed(i - 1, j), P.bed(i, j), straddles);
+            }
+            double t = -g.Az_fcc(i, j) * ri * gg * ((P.H(i - 1, j) + P.H(i, j)) / 2) * ((P.s(i, j) - P.s(i - 1, j)) / g.dx_f(i));
+            P.tau.u(i, j) = wall ? 0.0 : (front ? tf : (straddles ? tg : t));
+        }
+    for (int j = 1; j <= P.tau.v.ny(); ++j)
+        for (int i = 1; i <= P.tau.v.nx(); ++i) {   // _compute_y_driving_stress!, :118-125
+            bool wall = inactive_cf(g, i, j, mu);
+            bool front = false; double tf = 0;
+            if (mu) {
+                bool s_ = (*mu)(i, j - 1) > 0 && !((*mu)(i, j) > 0), n_ = !((*mu)(i, j - 1) > 0) && (*mu)(i, j) > 0;
+                double F = (s_ ? front_force(i, j - 1) : 0.0) - (n_ ? front_force(i, j) : 0.0);
+                front = s_ || n_; tf = g.dx_c(i) * F;
+            }
+            bool straddles = false; double tg = 0;
+            if (P.gl_stress) {
+                tg = g.dx_c(i) * gl_stress(P.H(i, j - 1), P.H(i, j), P.s(i, j - 1), P.s(i, j), P.bed(i, j - 1), P.bed(i, j), straddles);
+            }
+            double t = -g.Az_cfc(i, j) * ri * gg * ((P.H(i, j - 1) + P.H(i, j)) / 2) * ((P.s(i, j) - P.s(i, j - 1)) / g.dy_f(j));
+            P.tau.v(i, j) = wall ? 0.0 : (front ? tf : (straddles ? tg : t));
+        }
+}
+
+// compute_velocity_profile! (DIVA, diva.jl:249-269) / extend_depth_average! (SSA, ice_sheet_model_methods.jl:167-180)
+static void velocity_profile(Problem& P) {
+    const Grid& g = P.grid;
+    fill_halo(P.x);
+    if (P.stress_balance == NK_SSA) {
+        for (int j = 1; j <= P.ub.ny(); ++j) for (int i = 1; i <= P.ub.nx(); ++i) P.ub(i, j) = P.x.u(i, j);
+        for (int j = 1; j <= P.vb.ny(); ++j) for (int i = 1; i <= P.vb.nx(); ++i) P.vb(i, j) = P.x.v(i, j);
+        for (int k = 0; k < P.sigma.N; ++k) {
+            for (int j = 1; j <= P.ub.ny(); ++j) for (int i = 1; i <= P.ub.nx(); ++i) P.us.k[k](i, j) = P.x.u(i, j);
+            for (int j = 1; j <= P.vb.ny(); ++j) for (int i = 1; i <= P.vb.nx(); ++i) P.vs.k[k](i, j) = P.x.v(i, j);
+        }
+        return;
+    }
+    for (auto& f : P.eta_s.k) fill_halo(f);
+    compute_basal_velocities(g, P.ub, P.vb, P.x.u, P.x.v, P.bbu, P.bbv, P.F2);
+    const Sigma& sg = P.sigma;
+    auto shear_integral = [&](int i, int j, int k) {   // column_integrals.jl:71
+        double I = 0;
+        for (int kp = 1; kp <= k; ++kp) I += (1 / P.eta_s.k[kp - 1](i, j)) * profile_weight(sg, kp, k, 1);
+        return I * P.H(i, j);
+    };
+    for (int k = 1; k <= sg.N; ++k) {
+        for (int j = 1; j <= P.ub.ny(); ++j)
+            for (int i = 1; i <= P.ub.nx(); ++i) {
+                double F1 = (shear_integral(i - 1, j, k) + shear_integral(i, j, k)) / 2;
+                P.us.k[k - 1](i, j) = P.ub(i, j) * (1 + P.bbu(i, j) * F1);
+            }
+        for (int j = 1; j <= P.vb.ny(); ++j)
+            for (int i = 1; i <= P.vb.nx(); ++i) {
+                double F1 = (shear_integral(i, j - 1, k) + shear_integral(i, j, k)) / 2;
+                P.vs.k[k - 1](i, j) = P.vb(i, j) * (1 + P.bbv(i, j) * F1);
+            }
+    }
+}
+
+// ---- field access in interior layout -------------------------------------------------------------
+struct FieldRef { Field* f = nullptr; SigmaField* s = nullptr; };
+
+static FieldRef field_ref(Problem& P, int id) {
+    FieldRef r;
+    switch (id) {
+        case NK_FIELD_U: r.f = &P.x.u; break;
+        case NK_FIELD_V: r.f = &P.x.v; break;
+        case NK_FIELD_H: r.f = &P.H; break;
+        case NK_FIELD_BED: r.f = &P.bed; break;
+        case NK_FIELD_SURFACE: r.f = &P.s; break;
+        case NK_FIELD_ICE_MASK: r.f = &P.mu; break;
+        case NK_FIELD_PHI: r.f = &P.phi; break;
+        case NK_FIELD_PHI_U: r.f = &P.phu; break;
+        case NK_FIELD_PHI_V: r.f = &P.phv; break;
+        case NK_FIELD_EFFECTIVE_PRESSURE: r.f = &P.N; break;
+        case NK_FIELD_TAU_U: r.f = &P.tau.u; break;
+        case NK_FIELD_TAU_V: r.f = &P.tau.v; break;
+        case NK_FIELD_RATE_FACTOR: if (P.rate_layout == NK_RATE_FACTOR_SIGMA) r.s = &P.A3; else r.f = &P.A2; break;
+        case NK_FIELD_FRICTION_COEFFICIENT: r.f = &P.C; break;
+        case NK_FIELD_ETA_H: r.f = &P.etaH; break;
+        case NK_FIELD_ETA_H_FF: r.f = &P.etaHff; break;
+        case NK_FIELD_BETA_U: r.f = &P.bu; break;
+        case NK_FIELD_BETA_V: r.f = &P.bv; break;
+        case NK_FIELD_ETA_SIGMA: r.s = &P.eta_s; break;
+        case NK_FIELD_F2: r.f = &P.F2; break;
+        case NK_FIELD_BETA_B_U: r.f = &P.bbu; break;
+        case NK_FIELD_BETA_B_V: r.f = &P.bbv; break;
+        case NK_FIELD_U_B: r.f = &P.ub; break;
+        case NK_FIELD_V_B: r.f = &P.vb; break;
+        case NK_FIELD_U_SIGMA: r.s = &P.us; break;
+        case NK_FIELD_V_SIGMA: r.s = &P.vs; break;
+        case NK_FIELD_TEMPERATURE: r.s = &P.T; break;
+        default: break;
+    }
+    return r;
+}
+
+static int64_t field_size(Problem& P, int id) {
+    FieldRef r = field_ref(P, id);
+    if (r.f) return (int64_t)r.f->nx() * r.f->ny();
+    if (r.s) return (int64_t)r.s->k[0].nx() * r.s->k[0].ny() * (int64_t)r.s->k.size();
+    return 0;
+}
+
+static void copy_in(Field& f, const double* src) {
+    int nx = f.nx(), ny = f.ny();
+    for (int j = 1; j <= ny; ++j) for (int i = 1; i <= nx; ++i) f(i, j) = src[(size_t)(j - 1) * nx + (i - 1)];
+    fill_halo(f);
+}
+static void copy_out(const Field& f, double* dst) {
+    int nx = f.nx(), ny = f.ny();
+    for (int j = 1; j <= ny; ++j) for (int i = 1; i <= nx; ++i) dst[(size_t)(j - 1) * nx + (i - 1)] = f(i, j);
+}
+
+}  // namespace oracle
+
+using namespace oracle;
+
+extern "C" {
+
+typedef struct nko_problem nko_problem;
+
+int nko_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
+}
+
+nk_status nko_problem_create(const nk_grid_desc* gd, const nk_physics_desc* pd, const nk_solver_desc* sd, nko_problem** out) {
+    if (!gd || !pd || !sd || !out || gd->Nx < 1 || gd->Ny < 1 || gd->Nsigma < 1) return NK_BAD_ARGUMENT;
+    auto P = new Problem();
+    bool px = gd->topology_x == NK_PERIODIC, py = gd->topology_y == NK_PERIODIC;
+    if (gd->x_faces) P->grid.x.build_faces(gd->Nx, gd->halo_x, px, gd->x_faces); else P->grid.x.build_regular(gd->Nx, gd->halo_x, px, gd->x0, gd->Lx);
+    if (gd->y_faces) P->grid.y.build_faces(gd->Ny, gd->halo_y, py, gd->y_faces); else P->grid.y.build_regular(gd->Ny, gd->halo_y, py, gd->y0, gd->Ly);
+    P->sigma.N = gd->Nsigma;
+    P->sigma.faces.resize(gd->Nsigma + 1);
+    for (int k = 0; k <= gd->Nsigma; ++k)
+        P->sigma.faces[k] = gd->sigma_faces ? gd->sigma_faces[k] : std::pow((double)k / gd->Nsigma, gd->bed_refinement);
+    P->pdesc = *pd; P->sdesc = *sd;
+    P->stress_balance = pd->stress_balance;
+    P->rate_layout = pd->rate_factor_layout;
+    P->ph.walls = pd->side_walls; P->ph.n = pd->glen_exponent; P->ph.eps0 = pd->strain_rate_regularization;
+    P->ph.friction = pd->friction; P->ph.m = pd->friction_exponent; P->ph.alpha2 = pd->coulomb_coefficient;
+    P->ph.u0 = pd->velocity_regularization; P->ph.rho_i = pd->ice_density; P->ph.rho_w = pd->ocean_density;
+    P->ph.g = pd->gravitational_acceleration;
+    P->use_mask = pd->use_ice_mask != 0; P->use_N = pd->use_effective_pressure != 0;
+    P->grounding = pd->grounding; P->gl_stress = pd->grounding_line_driving_stress;
+    P->mask_min = pd->mask_minimum_thickness; P->mask_trans = pd->mask_transition_thickness;
+
+    const Grid* g = &P->grid;
+    P->x.init(g); P->tau.init(g);
+    for (Field* f : {&P->H, &P->bed, &P->s, &P->mu, &P->phi, &P->N, &P->C, &P->A2, &P->etaH, &P->F2}) f->init(g, CENTER, CENTER);
+    for (Field* f : {&P->phu, &P->bu, &P->bbu, &P->ub}) f->init(g, FACE, CENTER);
+    for (Field* f : {&P->phv, &P->bv, &P->bbv, &P->vb}) f->init(g, CENTER, FACE);
+    P->etaHff.init(g, FACE, FACE);
+    P->A3.init(g, CENTER, CENTER, gd->Nsigma); P->eta_s.init(g, CENTER, CENTER, gd->Nsigma); P->T.init(g, CENTER, CENTER, gd->Nsigma);
+    P->us.init(g, FACE, CENTER, gd->Nsigma); P->vs.init(g, CENTER, FACE, gd->Nsigma);
+    P->r.init(g); P->z.init(g); P->p.init(g); P->q.init(g); P->w.init(g); P->xprev.init(g);
+    if (sd->preconditioner == NK_PRECONDITIONER_MULTIGRID) {
+        coarse_levels(P->grid, sd->minimum_coarse_size, P->mg.levels);
+        P->mg.residual.init(g); P->mg.scratch.init(g, CENTER, CENTER);
+        P->mg.smoother = sd->smoother; P->mg.sweeps = sd->smoothing_sweeps; P->mg.coarsest = sd->coarsest_sweeps;
+    }
+    // Defaults of the geometry fields match a fresh model: φ = 1 where no grounding treatment is set.
+    *out = reinterpret_cast<nko_problem*>(P);
+    return NK_OK;
+}
+
+nk_status nko_problem_destroy(nko_problem* h) { delete reinterpret_cast<Problem*>(h); return NK_OK; }
+
+int64_t nko_problem_field_size(nko_problem* h, int32_t id) { return field_size(*reinterpret_cast<Problem*>(h), id); }
+
+nk_status nko_problem_set_field(nko_problem* h, int32_t id, const double* src, int64_t count) {
+    Problem& P = *reinterpret_cast<Problem*>(h);
+    FieldRef r = field_ref(P, id);
+    if ((!r.f && !r.s) || !src || count != field_size(P, id)) return NK_BAD_ARGUMENT;
+    if (r.f) copy_in(*r.f, src);
+    else {
+        int64_t layer = (int64_t)r.s->k[0].nx() * r.s->k[0].ny();
+        for (size_t k = 0; k < r.s->k.size(); ++k) copy_in(r.s->k[k], src + k * layer);
+    }
+    return NK_OK;
+}
+
+nk_status nko_problem_get_field(nko_problem* h, int32_t id, double* dst, int64_t count) {
+    Problem& P = *reinterpret_cast<Problem*>(h);
+    FieldRef r = field_ref(P, id);
+    if ((!r.f && !r.s) || !dst || count != field_size(P, id)) return NK_BAD_ARGUMENT;
+    if (r.f) copy_out(*r.f, dst);
+    else {
+        int64_t layer = (int64_t)r.s->k[0].nx() * r.s->k[0].ny();
+        for (size_t k = 0; k < r.s->k.size(); ++k) copy_out(r.s->k[k], dst + k * layer);
+    }
+    return NK_OK;
+}
+
+nk_status nko_compute_geometry(nko_problem* h) { compute_geometry(*reinterpret_cast<Problem*>(h)); return NK_OK; }
+
+// Rate factor from temperature, column_energy_solve.jl:104-110 with ω = 0 and arrhenius_rate_factor, arrhenius_rate_factor.jl:102-110
+nk_status nko_compute_rate_factor(nko_problem* h, double Ac, double Aw, double Qc, double Qw, double Tt, double Tw, double R,
+                                  double beta_cc, double Tm) {
+    Problem& P = *reinterpret_cast<Problem*>(h);
+    if (P.rate_layout != NK_RATE_FACTOR_SIGMA) return NK_BAD_ARGUMENT;
+    const Grid& g = P.grid;
+    for (int k = 1; k <= P.sigma.N; ++k) {
+        double zeta = P.sigma.zc(k);
+        for_xy(g.Nx(), g.Ny(), [&](int i, int j) {
+            double p = P.ph.rho_i * P.ph.g * P.H(i, j) * (1 - zeta);          // layer_pressure, enthalpy_conversions.jl:61-64
+            double Tp = P.T.k[k - 1](i, j) - (Tm - beta_cc * p) + Tm;         // T′ = T - Tₚₘ(p) + T₀
+            double log_cold = std::log(Ac) - Qc / (R * Tp);
+            double log_warm = std::log(Aw) - Qw / (R * Tp);
+            double x = std::min(std::max((Tp - Tt) / Tw + 1.0 / 2, 0.0), 1.0);
+            double s = x * x * (3 - 2 * x);
+            double softening = 1 + 181.25 * std::min(0.0, 0.01);                // ω = 0
+            P.A3.k[k - 1](i, j) = std::exp((1 - s) * log_cold + s * log_warm) * softening;
+        });
+        fill_halo(P.A3.k[k - 1]);
+    }
+    return NK_OK;
+}
+
+nk_status nko_update_coefficients(nko_problem* h) { update_coefficients(*reinterpret_cast<Problem*>(h)); return NK_OK; }
+
+static void load_vector(VelocityVector& x, const double* u, const double* v) { copy_in(x.u, u); copy_in(x.v, v); }
+static void store_vector(const VelocityVector& x, double* u, double* v) { copy_out(x.u, u); copy_out(x.v, v); }
+
+nk_status nko_apply_operator(nko_problem* h, const double* pu, const double* pv, double* qu, double* qv) {
+    Problem& P = *reinterpret_cast<Problem*>(h);
+    VelocityVector p, q; p.init(&P.grid); q.init(&P.grid);
+    load_vector(p, pu, pv); load_vector(q, qu, qv);
+    Coefficients c = coeffs(P);
+    ssa_operator(P.grid, q, p, c, P.ph.walls);
+    store_vector(q, qu, qv);
+    return NK_OK;
+}
+
+nk_status nko_precondition(nko_problem* h, const double* ru, const double* rv, double* zu, double* zv) {
+    Problem& P = *reinterpret_cast<Problem*>(h);
+    VelocityVector r, z; r.init(&P.grid); z.init(&P.grid);
+    load_vector(r, ru, rv); load_vector(z, zu, zv);
+    update_preconditioner(P);
+    precondition(P, z, r);
+    store_vector(z, zu, zv);
+    return NK_OK;
+}
+
+nk_status nko_linear_solve(nko_problem* h, const double* bu, const double* bv, nk_solve_stats* st) {
+    Problem& P = *reinterpret_cast<Problem*>(h);
+    VelocityVector b; b.init(&P.grid);
+    load_vector(b, bu, bv);
+    if (st) std::memset(st, 0, sizeof(*st));
+    int status = NK_OK;
+    conjugate_gradient(P, P.x, b, st, &status);
+    fill_halo(P.x);
+    if (st) st->status = status;
+    return status == NK_NONFINITE ? NK_NONFINITE : NK_OK;
+}
+
+nk_status nko_picard_solve(nko_problem* h, nk_solve_stats* st) {
+    nk_solve_stats local{};
+    picard_solve(*reinterpret_cast<Problem*>(h), st ? st : &local);
+    return (st ? st : &local)->status == NK_NONFINITE ? NK_NONFINITE : NK_OK;
+}
+
+nk_status nko_velocity_profile(nko_problem* h) { velocity_profile(*reinterpret_cast<Problem*>(h)); return NK_OK; }
+
+nk_status nko_multigrid_levels(nko_problem* h, int32_t* count, int32_t* nx, int32_t* ny, int32_t cap) {
+    Problem& P = *reinterpret_cast<Problem*>(h);
+    *count = (int32_t)P.mg.levels.size();
+    for (int l = 0; l < *count && l < cap; ++l) { nx[l] = P.mg.levels[l]->grid->Nx(); ny[l] = P.mg.levels[l]->grid->Ny(); }
+    return NK_OK;
+}
+
+// Transfers on level `level` (0 = first coarse level) with the current (coarsened) coefficients:
+// coarse = R fine, or fine += P coarse.  Vectors in interior layout of the respective grids.
+nk_status nko_multigrid_restrict(nko_problem* h, int32_t level, const double* fu, const double* fv, double* cu, double* cv) {
+    Problem& P = *reinterpret_cast<Problem*>(h);
+    if (level < 0 || level >= (int)P.mg.levels.size()) return NK_BAD_ARGUMENT;
+    update_preconditioner(P);
+    const Grid& fg = level == 0 ? P.grid : *P.mg.levels[level - 1]->grid;
+    const Field& feta = level == 0 ? P.etaH : P.mg.levels[level - 1]->etaH;
+    Level& L = *P.mg.levels[level];
+    VelocityVector f, c; f.init(&fg); c.init(L.grid.get());
+    load_vector(f, fu, fv); load_vector(c, cu, cv);
+    restrict_vector(*L.grid, fg, L, c, f, L.etaH, feta);
+    store_vector(c, cu, cv);
+    return NK_OK;
+}
+
+nk_status nko_multigrid_prolongate(nko_problem* h, int32_t level, const double* cu, const double* cv, double* fu, double* fv) {
+    Problem& P = *reinterpret_cast<Problem*>(h);
+    if (level < 0 || level >= (int)P.mg.levels.size()) return NK_BAD_ARGUMENT;
+    update_preconditioner(P);
+    const Grid& fg = level == 0 ? P.grid : *P.mg.levels[level - 1]->grid;
+    const Field& feta = level == 0 ? P.etaH : P.mg.levels[level - 1]->etaH;
+    Level& L = *P.mg.levels[level];
+    VelocityVector f, c; f.init(&fg); c.init(L.grid.get());
+    load_vector(f, fu, fv); load_vector(c, cu, cv);
+    prolongate_vector(fg, *L.grid, L, f, c, feta, L.etaH);
+    store_vector(f, fu, fv);
+    return NK_OK;
+}
+
+// Grid metrics for cross-checks: which = 0 Δxᶜ(1..Nx), 1 Δxᶠ(1..Nx+1), 2 Δyᶜ(1..Ny), 3 Δyᶠ(1..Ny+1).
+nk_status nko_grid_metrics(nko_problem* h, int32_t which, double* out) {
+    Problem& P = *reinterpret_cast<Problem*>(h);
+    const Grid& g = P.grid;
+    switch (which) {
+        case 0: for (int i = 1; i <= g.Nx(); ++i) out[i - 1] = g.dx_c(i); break;
+        case 1: for (int i = 1; i <= g.Nx() + 1; ++i) out[i - 1] = g.dx_f(i); break;
+        case 2: for (int j = 1; j <= g.Ny(); ++j) out[j - 1] = g.dy_c(j); break;
+        case 3: for (int j = 1; j <= g.Ny() + 1; ++j) out[j - 1] = g.dy_f(j); break;
+        default: return NK_BAD_ARGUMENT;
+    }
+    return NK_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,86 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes wrapper of the FP64 CPU oracle (oracle/_build/libnunatak_oracle.so).
+
+Used by tests/, __graft_entry__.smoke() and the CPU-baseline leg of bench.py as the checker.  The
+oracle has the same entry points as the GPU library (nko_* for nk_*), so `OracleProblem` reuses the
+argument marshalling of nunatak_gb300.Problem with the oracle's library in place of the GPU one.
+"""
+import ctypes as C
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+PKG_PARENT = os.path.join(ROOT, "nunatak.jl_gb300")
+if PKG_PARENT not in sys.path:
+    sys.path.insert(0, PKG_PARENT)
+
+import numpy as np  # noqa: E402
+
+from nunatak_gb300 import abi  # noqa: E402
+from nunatak_gb300.problem import Problem, _check, _dptr  # noqa: E402
+
+sys.path.insert(0, HERE)
+import build as _oracle_build  # noqa: E402
+
+_LIB = None
+
+
+def load():
+    global _LIB
+    if _LIB is None:
+        path = _oracle_build.build()
+        lib = C.CDLL(path)
+        vp, i32, i64, dp = C.c_void_p, C.c_int32, C.c_int64, C.POINTER(C.c_double)
+        sig = {
+            "nko_problem_create": [C.POINTER(abi.GridDesc), C.POINTER(abi.PhysicsDesc), C.POINTER(abi.SolverDesc), C.POINTER(vp)],
+            "nko_problem_destroy": [vp],
+            "nko_problem_field_size": [vp, i32],
+            "nko_problem_set_field": [vp, i32, dp, i64],
+            "nko_problem_get_field": [vp, i32, dp, i64],
+            "nko_compute_geometry": [vp],
+            "nko_compute_rate_factor": [vp] + [C.c_double] * 9,
+            "nko_update_coefficients": [vp],
+            "nko_apply_operator": [vp, dp, dp, dp, dp],
+            "nko_precondition": [vp, dp, dp, dp, dp],
+            "nko_linear_solve": [vp, dp, dp, C.POINTER(abi.SolveStats)],
+            "nko_picard_solve": [vp, C.POINTER(abi.SolveStats)],
+            "nko_velocity_profile": [vp],
+            "nko_multigrid_levels": [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), i32],
+            "nko_multigrid_restrict": [vp, i32, dp, dp, dp, dp],
+            "nko_multigrid_prolongate": [vp, i32, dp, dp, dp, dp],
+            "nko_grid_metrics": [vp, i32, dp],
+            "nko_set_threads": [C.c_int],
+        }
+        for name, args in sig.items():
+            f = getattr(lib, name)
+            f.argtypes = args
+            f.restype = C.c_int64 if name == "nko_problem_field_size" else C.c_int32
+        _LIB = lib
+    return _LIB
+
+
+def set_threads(n):
+    return load().nko_set_threads(n)
+
+
+class OracleProblem(Problem):
+    """The oracle's FP64 CPU restatement behind the same methods as nunatak_gb300.Problem."""
+
+    prefix = "nko_"
+
+    def _load(self):
+        return load()
+
+    def _create(self):
+        st = self._lib.nko_problem_create(C.byref(self.desc.grid), C.byref(self.desc.physics),
+                                          C.byref(self.desc.solver), C.byref(self._h))
+        _check(st, "oracle problem_create")
+
+    def adjoint_solve(self, bu, bv):
+        return self.linear_solve(bu, bv)
+
+    def grid_metrics(self, which):
+        n = (self.grid.Nx if which in (0,) else self.grid.Nx + 1 if which == 1 else self.grid.Ny if which == 2 else self.grid.Ny + 1)
+        out = np.empty(n)
+        _check(self._lib.nko_grid_metrics(self._h, which, out.ctypes.data_as(_dptr)), "grid_metrics")
+        return out
