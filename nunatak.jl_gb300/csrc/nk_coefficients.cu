@@ -1,0 +1,407 @@
+// nk_coefficients.cu — Picard coefficient update, geometry and driving stress (FP64).
+//
+// One thread per cell or face.  The viscosity kernel computes the membrane strain rate once per
+// column and walks the sigma levels in registers, fusing compute_viscosity! with
+// compute_column_integrals! (the reference launches them over Nx x Ny x Nsigma and Nx x Ny).
+#include <cmath>
+
+#include "nk_kernels.cuh"
+
+namespace nk {
+
+// ---- wall-masked velocities of the viscosity (interior_u / interior_v without η̄H, strain_rates.jl:5-6) ----
+__device__ __forceinline__ double wall_u(const DevGrid<double>& g, const double2* __restrict__ x, int i, int j) {
+    return g.peripheral_fc(i, j) ? 0.0 : x[g.u_idx(i, j)].x;
+}
+__device__ __forceinline__ double wall_v(const DevGrid<double>& g, const double2* __restrict__ x, int i, int j) {
+    return g.peripheral_cf(i, j) ? 0.0 : x[g.v_idx(i, j)].y;
+}
+__device__ __forceinline__ double strain_xy(const DevGrid<double>& g, const double2* __restrict__ x, int i, int j, double wf) {
+    double dudy = (wall_u(g, x, i, j) - wall_u(g, x, i, j - 1)) * g.rdyf[j];
+    double dvdx = (wall_v(g, x, i, j) - wall_v(g, x, i - 1, j)) * g.rdxf[i];
+    double e = (dudy + dvdx) / 2;
+    return g.peripheral_ff(i, j) ? wf * e : e;
+}
+// effective_strain_rate², strain_rates.jl:116-121
+__device__ __forceinline__ double effective_strain_rate2(const DevGrid<double>& g, const double2* __restrict__ x, int i, int j, double wf) {
+    double exx = (wall_u(g, x, i + 1, j) - wall_u(g, x, i, j)) * g.rdxc[i];
+    double eyy = (wall_v(g, x, i, j + 1) - wall_v(g, x, i, j)) * g.rdyc[j];
+    double e00 = strain_xy(g, x, i, j, wf), e10 = strain_xy(g, x, i + 1, j, wf);
+    double e01 = strain_xy(g, x, i, j + 1, wf), e11 = strain_xy(g, x, i + 1, j + 1, wf);
+    double exy2 = ((e00 * e00 + e10 * e10) / 2 + (e01 * e01 + e11 * e11) / 2) / 2;
+    return exx * exx + eyy * eyy + exx * eyy + exy2;
+}
+
+// η = ½ A^(-1/n) ε̇ₑ²^((1-n)/2n) (glen_flow_law.jl:211).  For n = 3 both powers are reciprocal cube roots.
+__device__ __forceinline__ double glen(double A, double ee, double n) {
+    if (n == 3.0) return rcbrt(A) * rcbrt(ee) / 2;
+    return pow(A, -1 / n) * pow(ee, (1 - n) / (2 * n)) / 2;
+}
+
+__device__ __forceinline__ double rate_factor(const PhysView& ph, int c, int k) {
+    return ph.rate_sigma ? ph.A[(long long)k * ph.plane + c] : ph.A[c];
+}
+
+// compute_viscosity! (glen_flow_law.jl:198-212) fused with compute_column_integrals! (column_integrals.jl:83-101)
+__global__ void k_viscosity(PhysView ph, const double2* __restrict__ x, double* eta_sigma, double4* coef, double* F2) {
+    const DevGrid<double>& g = ph.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int c = g.idx(i, j);
+    double ee = effective_strain_rate2(g, x, i, j, ph.wall_factor) + ph.eps0 * ph.eps0;
+    double eta_bar = 0.0, F = 0.0;
+    double eta_uniform = ph.rate_sigma ? 0.0 : glen(ph.A[c], ee, ph.n);
+    for (int k = 0; k < ph.sig.N; ++k) {
+        double eta = ph.rate_sigma ? glen(rate_factor(ph, c, k), ee, ph.n) : eta_uniform;
+        eta_sigma[(long long)k * ph.plane + c] = eta;
+        eta_bar += eta * ph.sig.dz[k];
+        F += (1 / eta) * ph.sig.w2[k];
+    }
+    double H = ph.H[c];
+    coef[c].x = ph.use_mask ? eta_bar * H * ph.mu[c] : eta_bar * H;
+    F2[c] = F * H;
+}
+void launch_viscosity(const PhysView& ph, const double2* x, double* eta_sigma, double4* coef, double* F2, cudaStream_t s) {
+    LaunchDims d = dims2d(ph.g.Nx, ph.g.Ny);
+    k_viscosity<<<d.grid, d.block, 0, s>>>(ph, x, eta_sigma, coef, F2);
+}
+
+// _compute_shear_viscosity! (glen_flow_law.jl:235-244): the basal stress βᵇ uᵇ drives a vertical shear
+// ε̇xz = ℑxᶜ(βᵇᵘ uᵇ)(1 - ζ) / 2η⁻ with the previous viscosity η⁻ (left out where η⁻ is still zero)
+__global__ void k_viscosity_diva(PhysView ph, const double2* __restrict__ x, const double2* __restrict__ bb,
+                                 const double2* __restrict__ ub, double* eta_sigma, double4* coef, double* F2) {
+    const DevGrid<double>& g = ph.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int c = g.idx(i, j);
+    double e2 = effective_strain_rate2(g, x, i, j, ph.wall_factor);
+    int u0 = g.u_idx(i, j), u1 = g.u_idx(i + 1, j), v0 = g.v_idx(i, j), v1 = g.v_idx(i, j + 1);
+    double tx = (bb[u0].x * ub[u0].x + bb[u1].x * ub[u1].x) / 2;
+    double ty = (bb[v0].y * ub[v0].y + bb[v1].y * ub[v1].y) / 2;
+    double eta_bar = 0.0, F = 0.0;
+    for (int k = 0; k < ph.sig.N; ++k) {
+        long long o = (long long)k * ph.plane + c;
+        double zeta = ph.sig.zc[k];
+        double em = eta_sigma[o];
+        em = (em == 0.0) ? INFINITY : em;
+        double exz = tx * (1 - zeta) / (2 * em);
+        double eyz = ty * (1 - zeta) / (2 * em);
+        double ee = e2 + exz * exz + eyz * eyz + ph.eps0 * ph.eps0;
+        double eta = glen(rate_factor(ph, c, k), ee, ph.n);
+        eta_sigma[o] = eta;
+        eta_bar += eta * ph.sig.dz[k];
+        F += (1 / eta) * ph.sig.w2[k];
+    }
+    double H = ph.H[c];
+    coef[c].x = ph.use_mask ? eta_bar * H * ph.mu[c] : eta_bar * H;
+    F2[c] = F * H;
+}
+void launch_viscosity_diva(const PhysView& ph, const double2* x, const double2* bb, const double2* ub, double* eta_sigma,
+                           double4* coef, double* F2, cudaStream_t s) {
+    LaunchDims d = dims2d(ph.g.Nx, ph.g.Ny);
+    k_viscosity_diva<<<d.grid, d.block, 0, s>>>(ph, x, bb, ub, eta_sigma, coef, F2);
+}
+
+// _interpolate_to_corners! (stress_balance_coefficients.jl:26-29): ℑxyᶠᶠᵃ = ℑyᵃᶠᵃ(ℑxᶠᵃᵃ(η̄H))
+template <typename T>
+__global__ void k_corners(DevGrid<T> g, typename Vec4<T>::type* coef) {
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i > g.Nx || j > g.Ny) return;
+    T lo = (coef[g.c_idx(i - 1, j - 1)].x + coef[g.c_idx(i, j - 1)].x) / T(2);
+    T hi = (coef[g.c_idx(i - 1, j)].x + coef[g.c_idx(i, j)].x) / T(2);
+    coef[g.idx(i, j)].y = (lo + hi) / T(2);
+}
+template <typename T>
+void launch_corners(const DevGrid<T>& g, typename Vec4<T>::type* coef, cudaStream_t s) {
+    LaunchDims d = dims2d(g.Nx + 1, g.Ny + 1);
+    k_corners<T><<<d.grid, d.block, 0, s>>>(g, coef);
+}
+template void launch_corners<double>(const DevGrid<double>&, double4*, cudaStream_t);
+template void launch_corners<float>(const DevGrid<float>&, float4*, cudaStream_t);
+
+// basal_drag, frictions.jl:83-89
+__device__ __forceinline__ double basal_drag(const PhysView& ph, double U, double C, double N) {
+    double w = C * pow(U, ph.m - 1);
+    if (ph.friction == NK_WEERTMAN) return w;
+    double tc = ph.alpha2 * N;
+    return w * tc / pow(pow(C, 1 / ph.m) * U + pow(tc, 1 / ph.m), ph.m);
+}
+
+// _compute_x_basal_drag! / _compute_y_basal_drag!, frictions.jl:142-160, over size(βᵘ), size(βᵛ)
+__global__ void k_basal_drag(PhysView ph, const double2* __restrict__ x, double4* coef, double2* bb) {
+    const DevGrid<double>& g = ph.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i > g.Nx || j > g.Ny) return;
+    int k = g.idx(i, j);
+    double u02 = ph.u0 * ph.u0;
+    bool has_u = j < g.Ny && (i < g.Nx || !g.px);
+    bool has_v = i < g.Nx && (j < g.Ny || !g.py);
+    double bu = 0.0, bv = 0.0;
+    if (has_u) {
+        double vf = ((x[g.v_idx(i - 1, j)].y + x[g.v_idx(i, j)].y) / 2 + (x[g.v_idx(i - 1, j + 1)].y + x[g.v_idx(i, j + 1)].y) / 2) / 2;
+        double u = x[k].x;
+        double U = sqrt(u * u + vf * vf + u02);
+        double Cf = (ph.C[g.c_idx(i - 1, j)] + ph.C[g.c_idx(i, j)]) / 2;
+        double Nf = ph.use_N ? (ph.N[g.c_idx(i - 1, j)] + ph.N[g.c_idx(i, j)]) / 2 : 0.0;
+        double b = ph.phi[k].x * basal_drag(ph, U, Cf, Nf);
+        bu = g.peripheral_fc(i, j) ? 0.0 : b;
+    }
+    if (has_v) {
+        double uf = ((x[g.u_idx(i, j - 1)].x + x[g.u_idx(i + 1, j - 1)].x) / 2 + (x[g.u_idx(i, j)].x + x[g.u_idx(i + 1, j)].x) / 2) / 2;
+        double v = x[k].y;
+        double U = sqrt(v * v + uf * uf + u02);
+        double Cf = (ph.C[g.c_idx(i, j - 1)] + ph.C[g.c_idx(i, j)]) / 2;
+        double Nf = ph.use_N ? (ph.N[g.c_idx(i, j - 1)] + ph.N[g.c_idx(i, j)]) / 2 : 0.0;
+        double b = ph.phi[k].y * basal_drag(ph, U, Cf, Nf);
+        bv = g.peripheral_cf(i, j) ? 0.0 : b;
+    }
+    if (coef) {
+        if (has_u) coef[k].z = bu;
+        if (has_v) coef[k].w = bv;
+    } else {
+        double2 o = bb[k];
+        if (has_u) o.x = bu;
+        if (has_v) o.y = bv;
+        bb[k] = o;
+    }
+}
+void launch_basal_drag(const PhysView& ph, const double2* x, double4* coef, double2* bb, cudaStream_t s) {
+    if (ph.friction == NK_FRICTION_NONE) return;   // compute_basal_drag!(βᵘ, βᵛ, ::Nothing, ...) = nothing
+    LaunchDims d = dims2d(ph.g.Nx + 1, ph.g.Ny + 1);
+    k_basal_drag<<<d.grid, d.block, 0, s>>>(ph, x, coef, bb);
+}
+
+// 1 + βᵇ ℑF₂ at the velocity points, diva.jl:161-163
+__device__ __forceinline__ double x_shear_factor(const DevGrid<double>& g, double b, const double* F2, int i, int j) {
+    return 1 + b * ((F2[g.c_idx(i - 1, j)] + F2[g.c_idx(i, j)]) / 2);
+}
+__device__ __forceinline__ double y_shear_factor(const DevGrid<double>& g, double b, const double* F2, int i, int j) {
+    return 1 + b * ((F2[g.c_idx(i, j - 1)] + F2[g.c_idx(i, j)]) / 2);
+}
+
+__global__ void k_basal_velocity(PhysView ph, const double2* __restrict__ x, const double2* __restrict__ bb, const double* __restrict__ F2,
+                                 double2* ub) {
+    const DevGrid<double>& g = ph.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i > g.Nx || j > g.Ny) return;
+    int k = g.idx(i, j);
+    bool has_u = j < g.Ny && (i < g.Nx || !g.px);
+    bool has_v = i < g.Nx && (j < g.Ny || !g.py);
+    double2 o = ub[k], xx = x[k], b = bb[k];
+    if (has_u) o.x = xx.x / x_shear_factor(g, b.x, F2, i, j);
+    if (has_v) o.y = xx.y / y_shear_factor(g, b.y, F2, i, j);
+    ub[k] = o;
+}
+void launch_basal_velocity(const PhysView& ph, const double2* x, const double2* bb, const double* F2, double2* ub, cudaStream_t s) {
+    LaunchDims d = dims2d(ph.g.Nx + 1, ph.g.Ny + 1);
+    k_basal_velocity<<<d.grid, d.block, 0, s>>>(ph, x, bb, F2, ub);
+}
+
+__global__ void k_effective_drag(PhysView ph, const double2* __restrict__ bb, const double* __restrict__ F2, double4* coef) {
+    const DevGrid<double>& g = ph.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i > g.Nx || j > g.Ny) return;
+    int k = g.idx(i, j);
+    bool has_u = j < g.Ny && (i < g.Nx || !g.px);
+    bool has_v = i < g.Nx && (j < g.Ny || !g.py);
+    double2 b = bb[k];
+    if (has_u) coef[k].z = b.x / x_shear_factor(g, b.x, F2, i, j);
+    if (has_v) coef[k].w = b.y / y_shear_factor(g, b.y, F2, i, j);
+}
+void launch_effective_drag(const PhysView& ph, const double2* bb, const double* F2, double4* coef, cudaStream_t s) {
+    LaunchDims d = dims2d(ph.g.Nx + 1, ph.g.Ny + 1);
+    k_effective_drag<<<d.grid, d.block, 0, s>>>(ph, bb, F2, coef);
+}
+
+// shear_integral (column_integrals.jl:71): H ∫₀^ζₖ (1 - ζ′)/η dζ′
+__device__ __forceinline__ double shear_integral(const PhysView& ph, const double* eta_sigma, int c, int k) {
+    double I = 0.0;
+    for (int kp = 0; kp <= k; ++kp) I += (1 / eta_sigma[(long long)kp * ph.plane + c]) * ph.sig.w1[k * ph.sig.N + kp];
+    return I * ph.H[c];
+}
+
+// _compute_x/y_velocity_profile! (diva.jl:259-269) or _extend_depth_average! (SSA)
+__global__ void k_velocity_profile(PhysView ph, int diva, const double2* __restrict__ x, const double2* __restrict__ bb,
+                                   const double* __restrict__ eta_sigma, const double2* __restrict__ ub, double2* usig) {
+    const DevGrid<double>& g = ph.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i > g.Nx || j > g.Ny) return;
+    int c = g.idx(i, j);
+    bool has_u = j < g.Ny && (i < g.Nx || !g.px);
+    bool has_v = i < g.Nx && (j < g.Ny || !g.py);
+    for (int k = 0; k < ph.sig.N; ++k) {
+        long long o = (long long)k * ph.plane + c;
+        double2 out = usig[o];
+        if (!diva) {
+            if (has_u) out.x = x[c].x;
+            if (has_v) out.y = x[c].y;
+        } else {
+            if (has_u) {
+                double F1 = (shear_integral(ph, eta_sigma, g.c_idx(i - 1, j), k) + shear_integral(ph, eta_sigma, g.c_idx(i, j), k)) / 2;
+                out.x = ub[c].x * (1 + bb[c].x * F1);
+            }
+            if (has_v) {
+                double F1 = (shear_integral(ph, eta_sigma, g.c_idx(i, j - 1), k) + shear_integral(ph, eta_sigma, g.c_idx(i, j), k)) / 2;
+                out.y = ub[c].y * (1 + bb[c].y * F1);
+            }
+        }
+        usig[o] = out;
+    }
+}
+__global__ void k_copy_faces(DevGrid<double> g, const double2* __restrict__ x, double2* ub) {
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i > g.Nx || j > g.Ny) return;
+    ub[g.idx(i, j)] = x[g.idx(i, j)];
+}
+void launch_velocity_profile(const PhysView& ph, int diva, const double2* x, const double2* bb, const double* F2,
+                             const double* eta_sigma, double2* ub, double2* usig, cudaStream_t s) {
+    LaunchDims d = dims2d(ph.g.Nx + 1, ph.g.Ny + 1);
+    if (diva) k_basal_velocity<<<d.grid, d.block, 0, s>>>(ph, x, bb, F2, ub);
+    else k_copy_faces<<<d.grid, d.block, 0, s>>>(ph.g, x, ub);
+    k_velocity_profile<<<d.grid, d.block, 0, s>>>(ph, diva, x, bb, eta_sigma, ub, usig);
+}
+
+// ---- geometry ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ double nonzero(double x) { return x == 0.0 ? 1.0 : x; }
+// segment_grounded_fraction, subgrid_grounded_fraction.jl:159-163
+__device__ __forceinline__ double segment_fraction(double f1, double f2) {
+    double fp = fmax(f1, 0.0) + fmax(f2, 0.0);
+    double S = fabs(f1) + fabs(f2);
+    return S == 0.0 ? 1.0 : fp / nonzero(S);
+}
+// triangle_grounded_fraction, :166-174
+__device__ __forceinline__ double triangle_fraction(double f1, double f2, double f3) {
+    double a = fmin(fmin(f1, f2), f3);
+    double c = fmax(fmax(f1, f2), f3);
+    double b = f1 + f2 + f3 - a - c;
+    double one_grounded = c * c / nonzero((c - a) * (c - b));
+    double one_floating = 1.0 - a * a / nonzero((b - a) * (c - a));
+    double phi = b > 0 ? one_floating : one_grounded;
+    return a >= 0 ? 1.0 : (c <= 0 ? 0.0 : phi);
+}
+
+// update_geometry! (ice_sheet_model_methods.jl:103-111): s, φ, φᵘ, φᵛ, N, μ
+__global__ void k_geometry(GeometryView v) {
+    const DevGrid<double>& g = v.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i > g.Nx || j > g.Ny) return;
+    double rw_ri = v.rho_w / v.rho_i, ri_rw = v.rho_i / v.rho_w;
+    auto f = [&](int a, int b) { int c = g.c_idx(a, b); return v.H[c] + rw_ri * v.bed[c]; };
+    int k = g.idx(i, j);
+    if (i < g.Nx && j < g.Ny) {
+        double H = v.H[k], b = v.bed[k];
+        v.s[k] = v.grounding ? fmax(b + H, (1 - ri_rw) * H) : b + H;
+        double rig = v.rho_i * v.gacc, rwg = v.rho_w * v.gacc;
+        v.N[k] = fmax(rig * H + rwg * fmin(b, 0.0), 0.0);
+        double t = fmin(fmax((H - v.mask_min) / v.mask_trans, 0.0), 1.0);
+        v.mu[k] = t * t * (3 - 2 * t);
+        if (v.grounding) {
+            double fc = f(i, j);
+            double fe = (fc + f(i + 1, j)) / 2, fw = (fc + f(i - 1, j)) / 2, fn = (fc + f(i, j + 1)) / 2, fs = (fc + f(i, j - 1)) / 2;
+            double fne = (fc + f(i + 1, j) + f(i, j + 1) + f(i + 1, j + 1)) / 4;
+            double fnw = (fc + f(i - 1, j) + f(i, j + 1) + f(i - 1, j + 1)) / 4;
+            double fse = (fc + f(i + 1, j) + f(i, j - 1) + f(i + 1, j - 1)) / 4;
+            double fsw = (fc + f(i - 1, j) + f(i, j - 1) + f(i - 1, j - 1)) / 4;
+            double phi = triangle_fraction(fc, fe, fne) + triangle_fraction(fc, fn, fne) + triangle_fraction(fc, fn, fnw) +
+                         triangle_fraction(fc, fw, fnw) + triangle_fraction(fc, fw, fsw) + triangle_fraction(fc, fs, fsw) +
+                         triangle_fraction(fc, fs, fse) + triangle_fraction(fc, fe, fse);
+            v.phi[k] = phi / 8;
+        } else {
+            v.phi[k] = 1.0;
+        }
+    }
+    double2 ph = v.phi_uv[k];
+    if (j < g.Ny && (i < g.Nx || !g.px)) ph.x = v.grounding ? segment_fraction(f(i - 1, j), f(i, j)) : 1.0;
+    if (i < g.Nx && (j < g.Ny || !g.py)) ph.y = v.grounding ? segment_fraction(f(i, j - 1), f(i, j)) : 1.0;
+    v.phi_uv[k] = ph;
+}
+
+// compute_driving_stress!, driving_stress.jl:43-125
+struct DrivingStressArgs { GeometryView v; };
+
+__device__ __forceinline__ double front_force(const GeometryView& v, int c) {   // :56-60
+    double Hi = v.H[c];
+    double D = fmin(fmax(Hi - v.s[c], 0.0), Hi);
+    return v.gacc * (v.rho_i * Hi * Hi - v.rho_w * D * D) / 2;
+}
+__device__ __forceinline__ double gl_stress(const GeometryView& v, int c1, int c2, bool& straddles) {   // :84-92
+    double ri = v.rho_i, rw = v.rho_w;
+    double H1 = v.H[c1], H2 = v.H[c2], s1 = v.s[c1], s2 = v.s[c2], b1 = v.bed[c1], b2 = v.bed[c2];
+    double f1 = H1 + rw / ri * b1, f2 = H2 + rw / ri * b2;
+    straddles = ((f1 > 0) != (f2 > 0)) && (H1 > 0) && (H2 > 0);
+    double theta = f1 / (straddles ? f1 - f2 : 1.0);
+    double Hg = H1 + theta * (H2 - H1);
+    double sg = (1 - ri / rw) * Hg;
+    return -ri * v.gacc * ((H1 + Hg) * (sg - s1) + (Hg + H2) * (s2 - sg)) / 2;
+}
+
+__global__ void k_driving_stress(GeometryView v) {
+    const DevGrid<double>& g = v.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i > g.Nx || j > g.Ny) return;
+    int k = g.idx(i, j);
+    double2 tau = v.tau[k];
+    if (j < g.Ny && (i < g.Nx || !g.px)) {   // _compute_x_driving_stress!, :109-116
+        int cw = g.c_idx(i - 1, j), ce = g.c_idx(i, j);
+        bool wall = g.peripheral_fc(i, j) || (v.use_mask && (v.mu[cw] + v.mu[ce]) == 0.0);
+        bool front = false, straddles = false;
+        double tf = 0.0, tg = 0.0;
+        if (v.use_mask) {
+            bool w = v.mu[cw] > 0 && !(v.mu[ce] > 0), e = !(v.mu[cw] > 0) && v.mu[ce] > 0;
+            double F = (w ? front_force(v, cw) : 0.0) - (e ? front_force(v, ce) : 0.0);
+            front = w || e;
+            tf = g.dyc[j] * F;
+        }
+        if (v.gl_stress) tg = g.dyc[j] * gl_stress(v, cw, ce, straddles);
+        double t = -g.Az_fc(i, j) * v.rho_i * v.gacc * ((v.H[cw] + v.H[ce]) / 2) * ((v.s[ce] - v.s[cw]) * g.rdxf[i]);
+        tau.x = wall ? 0.0 : (front ? tf : (straddles ? tg : t));
+    }
+    if (i < g.Nx && (j < g.Ny || !g.py)) {   // _compute_y_driving_stress!, :118-125
+        int cs = g.c_idx(i, j - 1), cn = g.c_idx(i, j);
+        bool wall = g.peripheral_cf(i, j) || (v.use_mask && (v.mu[cs] + v.mu[cn]) == 0.0);
+        bool front = false, straddles = false;
+        double tf = 0.0, tg = 0.0;
+        if (v.use_mask) {
+            bool so = v.mu[cs] > 0 && !(v.mu[cn] > 0), no = !(v.mu[cs] > 0) && v.mu[cn] > 0;
+            double F = (so ? front_force(v, cs) : 0.0) - (no ? front_force(v, cn) : 0.0);
+            front = so || no;
+            tf = g.dxc[i] * F;
+        }
+        if (v.gl_stress) tg = g.dxc[i] * gl_stress(v, cs, cn, straddles);
+        double t = -g.Az_cf(i, j) * v.rho_i * v.gacc * ((v.H[cs] + v.H[cn]) / 2) * ((v.s[cn] - v.s[cs]) * g.rdyf[j]);
+        tau.y = wall ? 0.0 : (front ? tf : (straddles ? tg : t));
+    }
+    v.tau[k] = tau;
+}
+
+void launch_geometry(const GeometryView& v, cudaStream_t s) {
+    LaunchDims d = dims2d(v.g.Nx + 1, v.g.Ny + 1);
+    k_geometry<<<d.grid, d.block, 0, s>>>(v);
+    k_driving_stress<<<d.grid, d.block, 0, s>>>(v);
+}
+
+// _compute_rate_factor! with ω = 0 (column_energy_solve.jl:104-110) and arrhenius_rate_factor (arrhenius_rate_factor.jl:102-110)
+__global__ void k_rate_factor(DevGrid<double> g, SigmaTable sig, int plane, const double* __restrict__ H, const double* __restrict__ T,
+                              double* A, double rho_i, double gacc, const double* __restrict__ prm) {
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int c = g.idx(i, j);
+    double Ac = prm[0], Aw = prm[1], Qc = prm[2], Qw = prm[3], Tt = prm[4], Tw = prm[5], R = prm[6], bcc = prm[7], Tm = prm[8];
+    for (int k = 0; k < sig.N; ++k) {
+        long long o = (long long)k * plane + c;
+        double p = rho_i * gacc * H[c] * (1 - sig.zc[k]);
+        double Tp = T[o] - (Tm - bcc * p) + Tm;
+        double log_cold = log(Ac) - Qc / (R * Tp);
+        double log_warm = log(Aw) - Qw / (R * Tp);
+        double x = fmin(fmax((Tp - Tt) / Tw + 1.0 / 2, 0.0), 1.0);
+        double s = x * x * (3 - 2 * x);
+        A[o] = exp((1 - s) * log_cold + s * log_warm) * 1.0;   // water softening 1 + c min(ω, ω_max) = 1 at ω = 0
+    }
+}
+void launch_rate_factor(const DevGrid<double>& g, const SigmaTable& sig, int plane, const double* H, const double* T, double* A,
+                        double rho_i, double gacc, const double* params, cudaStream_t s) {
+    LaunchDims d = dims2d(g.Nx, g.Ny);
+    k_rate_factor<<<d.grid, d.block, 0, s>>>(g, sig, plane, H, T, A, rho_i, gacc, params);
+}
+
+}  // namespace nk

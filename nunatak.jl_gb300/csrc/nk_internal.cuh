@@ -1,0 +1,162 @@
+// nk_internal.cuh — shared device definitions of libnunatak_gb300.
+//
+// Device layout.  Every two-dimensional field of an Nx x Ny grid is stored in one pitched array of
+// (Ny + 1) rows of `pitch` >= Nx + 1 elements, x fastest; element (i, j), 0-based, is
+//   cell (i, j) for a Center-Center field, the west face of cell (i, j) for a Face-Center field,
+//   the south face for a Center-Face field, the south-west corner for a Face-Face field.
+// Index i = Nx holds the east wall face (Bounded x), row j = Ny the north wall face (Bounded y).
+// A velocity vector stores (u, v) of the same (i, j) interleaved as one 16-byte (8-byte in FP32) pair,
+// so one load brings both components of a cell; the coefficients of the operator are one packed record
+// per (i, j): (eta_H at the centre, eta_H at the south-west corner, beta_u, beta_v).
+//
+// Halo semantics.  Oceananigans fills halos by a periodic wrap or, for cell-centred data in a Bounded
+// direction, by copying the edge value.  The kernels read the same values through index maps: wrap()
+// for Periodic directions, clamp() for Bounded ones.  Face data in a Bounded direction is never read
+// unmasked outside 0..N, so clamping it is equivalent.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/nunatak_gb300.h"
+
+namespace nk {
+
+constexpr int BX = 32;   // thread-block tile of the 2-D kernels: BX x BY cells
+constexpr int BY = 8;
+constexpr int BLOCK_THREADS = BX * BY;
+
+// Mask bits of the operator (one byte per (i, j)).
+constexpr uint8_t U_INACTIVE = 1;   // u point is a wall or ice free: identity row, zero in strain rates
+constexpr uint8_t V_INACTIVE = 2;
+constexpr uint8_t U_WALL = 4;       // wall (peripheral) only: the viscosity masks walls, not ice-free points
+constexpr uint8_t V_WALL = 8;
+
+template <typename T> struct Vec2;
+template <> struct Vec2<double> { using type = double2; };
+template <> struct Vec2<float> { using type = float2; };
+template <typename T> struct Vec4;
+template <> struct Vec4<double> { using type = double4; };
+template <> struct Vec4<float> { using type = float4; };
+
+// Grid of one multigrid level as the kernels see it.  Metric arrays hold indices -2 .. N+2 (the pointer
+// is offset by 2): dxc(i) = cell width of centre i, dxf(i) = centre spacing at face i (west of centre i).
+template <typename T>
+struct DevGrid {
+    int Nx, Ny, pitch;
+    int px, py;                         // periodic flags
+    const T* dxc; const T* dxf; const T* dyc; const T* dyf;      // spacings
+    const T* rdxc; const T* rdxf; const T* rdyc; const T* rdyf;  // their reciprocals
+
+    __device__ __forceinline__ int idx(int i, int j) const { return j * pitch + i; }
+    __device__ __forceinline__ static int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+    __device__ __forceinline__ static int clampi(int i, int lo, int hi) { return i < lo ? lo : (i > hi ? hi : i); }
+    // index maps with halo semantics
+    __device__ __forceinline__ int cx(int i) const { return px ? wrap(i, Nx) : clampi(i, 0, Nx - 1); }
+    __device__ __forceinline__ int cy(int j) const { return py ? wrap(j, Ny) : clampi(j, 0, Ny - 1); }
+    __device__ __forceinline__ int fx(int i) const { return px ? wrap(i, Nx) : clampi(i, 0, Nx); }
+    __device__ __forceinline__ int fy(int j) const { return py ? wrap(j, Ny) : clampi(j, 0, Ny); }
+    __device__ __forceinline__ int c_idx(int i, int j) const { return idx(cx(i), cy(j)); }   // Center-Center
+    __device__ __forceinline__ int u_idx(int i, int j) const { return idx(fx(i), cy(j)); }   // Face-Center
+    __device__ __forceinline__ int v_idx(int i, int j) const { return idx(cx(i), fy(j)); }   // Center-Face
+    __device__ __forceinline__ int ff_idx(int i, int j) const { return idx(fx(i), fy(j)); }  // Face-Face
+    // inactive_cell and peripheral_node (Oceananigans Grids/inactive_node.jl) for Bounded directions
+    __device__ __forceinline__ bool out_x(int i) const { return !px && (i < 0 || i >= Nx); }
+    __device__ __forceinline__ bool out_y(int j) const { return !py && (j < 0 || j >= Ny); }
+    __device__ __forceinline__ bool peripheral_fc(int i, int j) const { return out_y(j) || out_x(i) || out_x(i - 1); }
+    __device__ __forceinline__ bool peripheral_cf(int i, int j) const { return out_x(i) || out_y(j) || out_y(j - 1); }
+    __device__ __forceinline__ bool peripheral_ff(int i, int j) const { return out_x(i) || out_x(i - 1) || out_y(j) || out_y(j - 1); }
+    __device__ __forceinline__ T Az_fc(int i, int j) const { return dxf[i] * dyc[j]; }
+    __device__ __forceinline__ T Az_cf(int i, int j) const { return dxc[i] * dyf[j]; }
+    __device__ __forceinline__ T Az_cc(int i, int j) const { return dxc[i] * dyc[j]; }
+};
+
+// Per-solve scalars of conjugate gradients and Picard, device resident.
+struct SolverScalars {
+    double rho;          // r . z of the current step
+    double rho_new;
+    double alpha, beta;
+    double pq;
+    double rr;           // r . r
+    double rz_old;       // r_new . z_old (flexible conjugate gradients)
+    double r0, tol, rnorm;
+    double picard_dd, picard_xx;   // ||x - x_prev||^2, ||x||^2
+    double reltol, abstol;
+    int it, done, done_next, status;
+    int fixed, iterations, maxiter, flexible;
+    unsigned int ticket;           // last-block counter of the fused reductions
+    unsigned int ticket2;
+};
+
+// ---- warp / block reductions (fixed order, so results do not depend on scheduling) --------------------
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sum over the block of up to two values; result valid in thread 0.  `sh` holds 2 * 32 doubles.
+__device__ __forceinline__ void block_sum2(double& a, double& b, double* sh) {
+    int lane = threadIdx.x + threadIdx.y * blockDim.x;
+    int w = lane >> 5, l = lane & 31;
+    int nw = (blockDim.x * blockDim.y + 31) >> 5;
+    a = warp_sum(a);
+    b = warp_sum(b);
+    if (l == 0) { sh[w] = a; sh[32 + w] = b; }
+    __syncthreads();
+    if (w == 0) {
+        a = l < nw ? sh[l] : 0.0;
+        b = l < nw ? sh[32 + l] : 0.0;
+        a = warp_sum(a);
+        b = warp_sum(b);
+    }
+    __syncthreads();
+}
+
+// Deterministic grid-wide reduction of two values: every block writes its partial sums, the last block
+// to arrive sums the partials in index order (fixed partition + fixed tree) and returns true in all its
+// threads with the totals in `ta`, `tb`.  `partials` holds 2 * gridDim entries.
+__device__ __forceinline__ bool grid_sum2(double a, double b, double2* partials, unsigned int* ticket,
+                                          double& ta, double& tb) {
+    __shared__ double sh[64];
+    __shared__ bool last;
+    block_sum2(a, b, sh);
+    int nblocks = gridDim.x * gridDim.y;
+    int bid = blockIdx.x + blockIdx.y * gridDim.x;
+    int tid = threadIdx.x + threadIdx.y * blockDim.x;
+    if (tid == 0) {
+        partials[bid] = make_double2(a, b);
+        __threadfence();
+        unsigned int t = atomicAdd(ticket, 1u);
+        last = (t == (unsigned int)nblocks - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    int nt = blockDim.x * blockDim.y;
+    double sa = 0.0, sb = 0.0;
+    for (int k = tid; k < nblocks; k += nt) {
+        double2 p = __ldcg(&partials[k]);   // L2 read: the other blocks' partials are not in this SM's L1
+        sa += p.x;
+        sb += p.y;
+    }
+    block_sum2(sa, sb, sh);
+    if (tid == 0) { *ticket = 0u; }
+    ta = sa;
+    tb = sb;
+    return true;   // totals valid in thread 0
+}
+
+// ---- host side helpers ------------------------------------------------------------------------------
+struct LaunchDims {
+    dim3 grid, block;
+};
+inline LaunchDims dims2d(int nx, int ny) {
+    LaunchDims d;
+    d.block = dim3(BX, BY);
+    d.grid = dim3((nx + BX - 1) / BX, (ny + BY - 1) / BY);
+    return d;
+}
+
+}  // namespace nk

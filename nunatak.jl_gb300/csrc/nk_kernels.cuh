@@ -1,0 +1,157 @@
+// nk_kernels.cuh — host-callable launchers of the kernels, shared between the translation units.
+#pragma once
+
+#include "nk_operator.cuh"
+
+namespace nk {
+
+// Sigma column constants (src/StressBalances/column_integrals.jl:31-74, src/Grids/sigma_grid.jl:264-266).
+constexpr int MAX_SIGMA = 64;
+struct SigmaTable {
+    int N;
+    const double* dz;     // layer_thickness(k)
+    const double* w2;     // layer_weight(k, 2)
+    const double* zc;     // znode(k, Center)
+    const double* w1;     // profile_weight(k', k, 1) at [k * N + k'] for k' <= k
+};
+
+// Fine-grid inputs of the coefficient update (all FP64, pitched; pairs interleave the u and v faces).
+struct PhysView {
+    DevGrid<double> g;
+    SigmaTable sig;
+    double n, eps0, wall_factor;
+    int friction;                 // NK_FRICTION_*
+    double m, alpha2, u0;
+    int rate_sigma;               // A on the sigma grid
+    int plane;                    // elements of one pitched plane: (Ny + 1) * pitch
+    const double* A;
+    const double* H;
+    const double* C;
+    const double* N;
+    const double* mu;
+    const double2* phi;           // (phi_u, phi_v)
+    int use_mask, use_N;
+};
+
+// ---- layout conversion ---------------------------------------------------------------------------------
+// dst[(j * pitch + i) * stride + offset] = src[j * nx + i] for i < nx, j < ny, `planes` planes.
+void launch_pack(double* dst, int pitch, int plane, int stride, int offset, const double* src, int nx, int ny, int planes,
+                 cudaStream_t s);
+void launch_unpack(double* dst, const double* src, int pitch, int plane, int stride, int offset, int nx, int ny, int planes,
+                   cudaStream_t s);
+void launch_fill(double* dst, int count, double value, cudaStream_t s);
+
+// ---- operator and conjugate gradients (FP64 fine grid) --------------------------------------------------
+void launch_apply(const OpView<double>& o, const double2* p, double2* q, cudaStream_t s);
+// mask bits from eta_H and the topology, over 0..Nx x 0..Ny
+template <typename T>
+void launch_mask(const OpView<T>& o, uint8_t* mask, cudaStream_t s);
+// inverse diagonal (Jacobi) of the fine grid
+void launch_inverse_diagonal(const OpView<double>& o, double2* invd, cudaStream_t s);
+template <typename T>
+void launch_inverse_row_sum(const OpView<T>& o, typename Vec2<T>::type* irs, cudaStream_t s);
+
+struct CGView {
+    OpView<double> o;
+    double2* x; const double2* b; double2* r; double2* z; double2* p; double2* q; double2* zold;
+    const double2* invd;          // Jacobi inverse diagonal or nullptr
+    int precond;                  // NK_PRECONDITIONER_*
+    SolverScalars* sc;
+    double2* partials;
+};
+// r = b - A x; if the preconditioner is not multigrid also z = M r, p = z, rho = r.z; r0, tol, done
+void launch_cg_init(const CGView& v, cudaStream_t s);
+// multigrid: after z = V(r): p = z, rho = r.z, done
+void launch_cg_init_finish(const CGView& v, cudaStream_t s);
+// q = A p, alpha = rho / p.q
+void launch_cg_apply(const CGView& v, cudaStream_t s);
+// x += alpha p, r -= alpha q (and z = M r for Jacobi / none); dots for beta and the stopping test
+void launch_cg_update(const CGView& v, cudaStream_t s);
+// multigrid: z = V(r) done; dots r.z (and r.z_old when flexible), beta
+void launch_cg_dots_after_precondition(const CGView& v, cudaStream_t s);
+// p = z + beta p, then commit the stopping decision of this step
+void launch_cg_xpby(const CGView& v, cudaStream_t s);
+// z = r * invd on the Nx x Ny range, z = r on the wall faces (unit diagonal)
+void launch_precondition_diagonal(const DevGrid<double>& g, double2* z, const double2* r, const double2* invd, cudaStream_t s);
+// Picard: xprev = x (over the Nx x Ny range)
+void launch_copy_range(const DevGrid<double>& g, double2* dst, const double2* src, cudaStream_t s);
+// Picard: xprev -= x, ||xprev||^2, ||x||^2 into sc
+void launch_picard_delta(const DevGrid<double>& g, double2* xprev, const double2* x, SolverScalars* sc, double2* partials,
+                         cudaStream_t s);
+
+// ---- coefficients ---------------------------------------------------------------------------------------
+// SSA membrane viscosity (glen_flow_law.jl:208-212) and column integrals (column_integrals.jl:90-101)
+void launch_viscosity(const PhysView& ph, const double2* x, double* eta_sigma, double4* coef, double* F2, cudaStream_t s);
+// DIVA viscosity with lagged vertical shear (glen_flow_law.jl:235-244) and column integrals
+void launch_viscosity_diva(const PhysView& ph, const double2* x, const double2* bb, const double2* ub, double* eta_sigma,
+                           double4* coef, double* F2, cudaStream_t s);
+// eta_H_ff = ℑxyᶠᶠ(eta_H) over 0..Nx x 0..Ny (stress_balance_coefficients.jl:26-29)
+template <typename T>
+void launch_corners(const DevGrid<T>& g, typename Vec4<T>::type* coef, cudaStream_t s);
+// basal drag at the faces from the velocity `x` (frictions.jl:142-160): writes beta into (coef.z, coef.w)
+// when `coef` is given, else into the pair array `bb` (DIVA friction-law drag)
+void launch_basal_drag(const PhysView& ph, const double2* x, double4* coef, double2* bb, cudaStream_t s);
+// DIVA basal velocity u_b = u / (1 + beta_b ℑF2) (diva.jl:179-187)
+void launch_basal_velocity(const PhysView& ph, const double2* x, const double2* bb, const double* F2, double2* ub, cudaStream_t s);
+// DIVA effective drag beta = beta_b / (1 + beta_b ℑF2) (diva.jl:203-211)
+void launch_effective_drag(const PhysView& ph, const double2* bb, const double* F2, double4* coef, cudaStream_t s);
+// DIVA velocity profile (diva.jl:259-269) / SSA depth extension (ice_sheet_model_methods.jl:167-180)
+void launch_velocity_profile(const PhysView& ph, int diva, const double2* x, const double2* bb, const double* F2,
+                             const double* eta_sigma, double2* ub, double2* usig, cudaStream_t s);
+
+// ---- geometry -------------------------------------------------------------------------------------------
+struct GeometryView {
+    DevGrid<double> g;
+    const double* H; const double* bed;
+    double* s; double* N; double* mu; double* phi; double2* phi_uv; double2* tau;
+    double rho_i, rho_w, gacc;
+    int grounding, gl_stress, use_mask;
+    double mask_min, mask_trans;
+};
+void launch_geometry(const GeometryView& v, cudaStream_t s);
+void launch_rate_factor(const DevGrid<double>& g, const SigmaTable& sig, int plane, const double* H, const double* T, double* A,
+                        double rho_i, double gacc, const double* params, cudaStream_t s);
+
+// ---- multigrid ------------------------------------------------------------------------------------------
+template <typename T>
+struct LevelView {
+    OpView<T> o;
+    typename Vec2<T>::type* x;
+    typename Vec2<T>::type* x2;      // ping-pong partner of x for the point smoother
+    typename Vec2<T>::type* b;
+    typename Vec2<T>::type* q;
+    T* t;                            // line-smoother scratch (one T per cell)
+    const typename Vec2<T>::type* irs;  // inverse ℓ1 row sums
+    int cx, cy;                      // coarsening factor from the finer level (1 or 2)
+};
+// coarse coefficients from the finer level (multigrid_preconditioner.jl:331-344), then corners
+template <typename T, typename TF>
+void launch_coarsen(const LevelView<T>& coarse, const DevGrid<TF>& fine_g, const typename Vec4<TF>::type* fine_coef,
+                    typename Vec4<T>::type* coarse_coef, cudaStream_t s);
+// x_out = x_in + (b - A x_in) / rowsum (x_in = 0 when `first`: x_out = b / rowsum)
+template <typename T>
+void launch_smooth_point(const LevelView<T>& L, const typename Vec2<T>::type* x_in, typename Vec2<T>::type* x_out, int first,
+                         const int* done, cudaStream_t s);
+// q = A x (line smoother first half) or q = b - A x (residual)
+template <typename T>
+void launch_level_apply(const LevelView<T>& L, const typename Vec2<T>::type* x, typename Vec2<T>::type* q, int residual,
+                        const int* done, cudaStream_t s);
+// `first`: x starts at zero (q = A x = 0 is not read, x is overwritten)
+template <typename T>
+void launch_line_relax(const LevelView<T>& L, typename Vec2<T>::type* x, int first, const int* done, cudaStream_t s);
+template <typename T>
+void launch_restrict(const LevelView<T>& coarse, const LevelView<T>& fine, const typename Vec2<T>::type* r_fine,
+                     typename Vec2<T>::type* b_coarse, const int* done, cudaStream_t s);
+template <typename T>
+void launch_prolongate(const LevelView<T>& fine, const LevelView<T>& coarse, typename Vec2<T>::type* x_fine,
+                       const typename Vec2<T>::type* x_coarse, const int* done, cudaStream_t s);
+template <typename T>
+void launch_zero_vec(const DevGrid<T>& g, typename Vec2<T>::type* x, const int* done, cudaStream_t s);
+// FP64 <-> FP32 conversions of vectors and of the coefficient record
+void launch_to_float(const DevGrid<double>& g, const double2* src, float2* dst, const int* done, cudaStream_t s);
+void launch_to_double(const DevGrid<double>& g, const float2* src, double2* dst, const int* done, cudaStream_t s);
+void launch_coef_to_float(const DevGrid<double>& g, const double4* src, float4* dst, cudaStream_t s);
+// FP64 vector copy on the Nx x Ny range under the done predicate
+void launch_copy_vec(const DevGrid<double>& g, double2* dst, const double2* src, const int* done, cudaStream_t s);
+
+}  // namespace nk

@@ -1,0 +1,314 @@
+// nk_multigrid.cu — geometric multigrid V-cycle kernels, in FP64 (plain solve) or FP32 (mixed solve).
+//
+// Restates src/StressBalances/multigrid_preconditioner.jl: semi-coarsening levels, rediscretised
+// coarse coefficients (:331-344), ℓ1-Jacobi point smoother (:213-219) and y-line ℓ1-block Jacobi
+// smoother (:231-259), C-grid restriction (:264-318, :346-352) and prolongation (:286-327, :354-360).
+// Indices here are 0-based: coarse point I0 gathers fine points 2 I0 + a.
+//
+// The point smoother reads x from one buffer and writes the next iterate into another, so one kernel
+// does a whole Jacobi sweep (the reference computes q = A x in one launch, then x += (b - q) / rowsum).
+// Every kernel takes the conjugate-gradient `done` flag and returns once the solve has stopped.
+#include "nk_kernels.cuh"
+
+namespace nk {
+
+__device__ __forceinline__ bool stopped(const int* done) { return done && *(volatile const int*)done; }
+
+// ---- restriction / prolongation index rules (0-based) ------------------------------------------------------
+__device__ __forceinline__ void offsets(bool face, int c, int& a0, int& a1) {
+    if (c == 1) { a0 = 0; a1 = 0; } else if (face) { a0 = -1; a1 = 1; } else { a0 = -1; a1 = 2; }
+}
+__device__ __forceinline__ int wrapn(int i, int n) { int r = i % n; return r < 0 ? r + n : r; }
+// restriction_index (multigrid_preconditioner.jl:268-271)
+__device__ __forceinline__ int ridx(int I, int a, int Nf, bool periodic, bool face, int c) {
+    if (c == 1) return I;
+    int i = 2 * I + a;
+    if (periodic) return wrapn(i, Nf);
+    if (face) return i < 0 ? 0 : i;
+    return i < 0 ? 0 : (i > Nf - 1 ? Nf - 1 : i);
+}
+// restriction_weight (:273-283)
+template <typename T>
+__device__ __forceinline__ T rweight(int I, int a, int Nc, bool periodic, bool face, int c) {
+    if (c == 1) return T(1);
+    if (face) {
+        if (!periodic && 2 * I + a < 0) return T(0);
+        return a == 0 ? T(1) : T(1) / T(2);
+    }
+    T w = (a == 0 || a == 1) ? T(3) / T(4) : T(1) / T(4);
+    if (periodic) return w;
+    bool outside = (I == 0 && a == -1) || (I == Nc - 1 && a == 2);
+    bool folded = (I == 0 && a == 0) || (I == Nc - 1 && a == 1);
+    w = w + (folded ? T(1) / T(4) : T(0));
+    return outside ? T(0) : w;
+}
+// parents (:286-305)
+template <typename T>
+__device__ __forceinline__ void parents(int i, int Nc, bool periodic, bool face, int c, int& I1, int& I2, T& w1, T& w2) {
+    if (c == 1) { I1 = i; I2 = i; w1 = T(1); w2 = T(0); return; }
+    int I = i / 2;
+    bool odd1 = (i % 2) == 0;   // the 1-based index i + 1 is odd
+    if (face) {
+        int up = periodic ? wrapn(I + 1, Nc) : I + 1;
+        I1 = I; I2 = odd1 ? I : up;
+        w1 = odd1 ? T(1) : T(1) / T(2);
+        w2 = odd1 ? T(0) : T(1) / T(2);
+    } else {
+        int Ip = odd1 ? I - 1 : I + 1;
+        I1 = I;
+        I2 = periodic ? wrapn(Ip, Nc) : (Ip < 0 ? 0 : (Ip > Nc - 1 ? Nc - 1 : Ip));
+        w1 = T(3) / T(4); w2 = T(1) / T(4);
+    }
+}
+
+// ---- coarse coefficients (_coarsen_coefficients!, :331-344), accumulated in FP64 ---------------------------------
+template <typename T, typename TF>
+__global__ void k_coarsen(OpView<T> co, int cxf, int cyf, DevGrid<TF> fg, const typename Vec4<TF>::type* __restrict__ fcoef,
+                          typename Vec4<T>::type* ccoef) {
+    const DevGrid<T>& cg = co.g;
+    int I = blockIdx.x * BX + threadIdx.x, J = blockIdx.y * BY + threadIdx.y;
+    if (I >= cg.Nx || J >= cg.Ny) return;
+    int i0 = cxf * I, j0 = cyf * J;
+    double S = 0.0;
+    for (int a = 0; a < cxf; ++a)
+        for (int b = 0; b < cyf; ++b) S += (double)fg.Az_cc(i0 + a, j0 + b) * (double)fcoef[fg.idx(i0 + a, j0 + b)].x;
+    double su = 0.0, sv = 0.0;
+    int a0, a1, b0, b1;
+    offsets(true, cxf, a0, a1);
+    offsets(false, cyf, b0, b1);
+    for (int a = a0; a <= a1; ++a)
+        for (int b = b0; b <= b1; ++b) {
+            int i = ridx(I, a, fg.Nx, fg.px, true, cxf), j = ridx(J, b, fg.Ny, fg.py, false, cyf);
+            double w = rweight<double>(I, a, cg.Nx, fg.px, true, cxf) * rweight<double>(J, b, cg.Ny, fg.py, false, cyf);
+            su += w * ((double)fg.Az_fc(i, j) * (double)fcoef[fg.idx(i, j)].z);
+        }
+    offsets(false, cxf, a0, a1);
+    offsets(true, cyf, b0, b1);
+    for (int a = a0; a <= a1; ++a)
+        for (int b = b0; b <= b1; ++b) {
+            int i = ridx(I, a, fg.Nx, fg.px, false, cxf), j = ridx(J, b, fg.Ny, fg.py, true, cyf);
+            double w = rweight<double>(I, a, cg.Nx, fg.px, false, cxf) * rweight<double>(J, b, cg.Ny, fg.py, true, cyf);
+            sv += w * ((double)fg.Az_cf(i, j) * (double)fcoef[fg.idx(i, j)].w);
+        }
+    int k = cg.idx(I, J);
+    typename Vec4<T>::type c = ccoef[k];
+    c.x = (T)(S / (double)cg.Az_cc(I, J));
+    c.z = (T)(su / (double)cg.Az_fc(I, J));
+    c.w = (T)(sv / (double)cg.Az_cf(I, J));
+    ccoef[k] = c;
+}
+template <typename T, typename TF>
+void launch_coarsen(const LevelView<T>& coarse, const DevGrid<TF>& fine_g, const typename Vec4<TF>::type* fine_coef,
+                    typename Vec4<T>::type* coarse_coef, cudaStream_t s) {
+    LaunchDims d = dims2d(coarse.o.g.Nx, coarse.o.g.Ny);
+    k_coarsen<T, TF><<<d.grid, d.block, 0, s>>>(coarse.o, coarse.cx, coarse.cy, fine_g, fine_coef, coarse_coef);
+    launch_corners<T>(coarse.o.g, coarse_coef, s);
+}
+template void launch_coarsen<double, double>(const LevelView<double>&, const DevGrid<double>&, const double4*, double4*, cudaStream_t);
+template void launch_coarsen<float, double>(const LevelView<float>&, const DevGrid<double>&, const double4*, float4*, cudaStream_t);
+template void launch_coarsen<float, float>(const LevelView<float>&, const DevGrid<float>&, const float4*, float4*, cudaStream_t);
+
+// ---- smoothers ---------------------------------------------------------------------------------------------
+template <typename T>
+__global__ void k_smooth_point(LevelView<T> L, const typename Vec2<T>::type* __restrict__ xin, typename Vec2<T>::type* __restrict__ xout,
+                               int first, const int* done) {
+    if (stopped(done)) return;
+    using V2 = typename Vec2<T>::type;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= L.o.g.Nx || j >= L.o.g.Ny) return;
+    int k = L.o.g.idx(i, j);
+    V2 b = L.b[k], w = L.irs[k], out;
+    if (first) {
+        out.x = b.x * w.x;
+        out.y = b.y * w.y;
+    } else {
+        V2 q = apply_at(L.o, xin, i, j);
+        V2 x = xin[k];
+        out.x = x.x + (b.x - q.x) * w.x;
+        out.y = x.y + (b.y - q.y) * w.y;
+    }
+    xout[k] = out;
+}
+template <typename T>
+void launch_smooth_point(const LevelView<T>& L, const typename Vec2<T>::type* x_in, typename Vec2<T>::type* x_out, int first,
+                         const int* done, cudaStream_t s) {
+    LaunchDims d = dims2d(L.o.g.Nx, L.o.g.Ny);
+    k_smooth_point<T><<<d.grid, d.block, 0, s>>>(L, x_in, x_out, first, done);
+}
+
+template <typename T>
+__global__ void k_level_apply(LevelView<T> L, const typename Vec2<T>::type* __restrict__ x, typename Vec2<T>::type* __restrict__ q,
+                              int residual, const int* done) {
+    if (stopped(done)) return;
+    using V2 = typename Vec2<T>::type;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= L.o.g.Nx || j >= L.o.g.Ny) return;
+    int k = L.o.g.idx(i, j);
+    V2 a = apply_at(L.o, x, i, j);
+    if (residual) {
+        V2 b = L.b[k];
+        a.x = b.x - a.x;
+        a.y = b.y - a.y;
+    }
+    q[k] = a;
+}
+template <typename T>
+void launch_level_apply(const LevelView<T>& L, const typename Vec2<T>::type* x, typename Vec2<T>::type* q, int residual,
+                        const int* done, cudaStream_t s) {
+    LaunchDims d = dims2d(L.o.g.Nx, L.o.g.Ny);
+    k_level_apply<T><<<d.grid, d.block, 0, s>>>(L, x, q, residual, done);
+}
+
+// line_relax!, :231-253: Thomas algorithm along j for the u line and then the v line of column i.
+// `first`: x starts at zero, so q = A x = 0 is not read and x is overwritten by δ.
+template <typename T>
+__global__ void k_line_relax(LevelView<T> L, typename Vec2<T>::type* x, int first, const int* done) {
+    if (stopped(done)) return;
+    const DevGrid<T>& g = L.o.g;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.Nx) return;
+    int Ny = g.Ny;
+    for (int comp = 0; comp < 2; ++comp) {
+        T cj = 0, tj = 0, dj = 0;
+        for (int j = 0; j < Ny; ++j) {
+            int k = g.idx(i, j);
+            uint8_t m = L.o.mask[k];
+            T s = comp == 0 ? x_row_sum(L.o, i, j, m) : y_row_sum(L.o, i, j, m);
+            T cj1 = (j == Ny - 1) ? T(0) : (comp == 0 ? x_line_coupling(L.o, i, j + 1) : y_line_coupling(L.o, i, j + 1));
+            T mm = s - cj - cj1 + cj * tj;
+            T bq = comp == 0 ? (L.b[k].x - (first ? T(0) : L.q[k].x)) : (L.b[k].y - (first ? T(0) : L.q[k].y));
+            dj = (bq + cj * dj) / mm;
+            tj = -cj1 / mm;
+            L.t[k] = tj;
+            if (comp == 0) L.q[k].x = dj; else L.q[k].y = dj;
+            cj = cj1;
+        }
+        T delta = 0;
+        for (int j = Ny - 1; j >= 0; --j) {
+            int k = g.idx(i, j);
+            delta = (comp == 0 ? L.q[k].x : L.q[k].y) - L.t[k] * delta;
+            if (comp == 0) x[k].x = first ? delta : x[k].x + delta;
+            else x[k].y = first ? delta : x[k].y + delta;
+        }
+    }
+}
+template <typename T>
+void launch_line_relax(const LevelView<T>& L, typename Vec2<T>::type* x, int first, const int* done, cudaStream_t s) {
+    int nb = (L.o.g.Nx + 127) / 128;
+    k_line_relax<T><<<nb, 128, 0, s>>>(L, x, first, done);
+}
+
+// ---- transfers --------------------------------------------------------------------------------------------
+// _restrict!, :346-352: b_coarse = R r_fine with fine and coarse masks
+template <typename T>
+__global__ void k_restrict(LevelView<T> C, OpView<T> fo, const typename Vec2<T>::type* __restrict__ rf,
+                           typename Vec2<T>::type* bc, const int* done) {
+    if (stopped(done)) return;
+    const DevGrid<T>& cg = C.o.g;
+    const DevGrid<T>& fg = fo.g;
+    int I = blockIdx.x * BX + threadIdx.x, J = blockIdx.y * BY + threadIdx.y;
+    if (I >= cg.Nx || J >= cg.Ny) return;
+    int k = cg.idx(I, J);
+    uint8_t m = C.o.mask[k];
+    T su = T(0), sv = T(0);
+    int a0, a1, b0, b1;
+    if (!(m & U_INACTIVE)) {
+        offsets(true, C.cx, a0, a1);
+        offsets(false, C.cy, b0, b1);
+        for (int a = a0; a <= a1; ++a)
+            for (int b = b0; b <= b1; ++b) {
+                int i = ridx(I, a, fg.Nx, fg.px, true, C.cx), j = ridx(J, b, fg.Ny, fg.py, false, C.cy);
+                T w = rweight<T>(I, a, cg.Nx, fg.px, true, C.cx) * rweight<T>(J, b, cg.Ny, fg.py, false, C.cy);
+                su += w * masked_u(fo, rf, i, j);
+            }
+    }
+    if (!(m & V_INACTIVE)) {
+        offsets(false, C.cx, a0, a1);
+        offsets(true, C.cy, b0, b1);
+        for (int a = a0; a <= a1; ++a)
+            for (int b = b0; b <= b1; ++b) {
+                int i = ridx(I, a, fg.Nx, fg.px, false, C.cx), j = ridx(J, b, fg.Ny, fg.py, true, C.cy);
+                T w = rweight<T>(I, a, cg.Nx, fg.px, false, C.cx) * rweight<T>(J, b, cg.Ny, fg.py, true, C.cy);
+                sv += w * masked_v(fo, rf, i, j);
+            }
+    }
+    typename Vec2<T>::type o;
+    o.x = su;
+    o.y = sv;
+    bc[k] = o;
+}
+template <typename T>
+void launch_restrict(const LevelView<T>& coarse, const LevelView<T>& fine, const typename Vec2<T>::type* r_fine,
+                     typename Vec2<T>::type* b_coarse, const int* done, cudaStream_t s) {
+    LaunchDims d = dims2d(coarse.o.g.Nx, coarse.o.g.Ny);
+    k_restrict<T><<<d.grid, d.block, 0, s>>>(coarse, fine.o, r_fine, b_coarse, done);
+}
+
+// _prolongate!, :354-360: x_fine += P x_coarse with fine and coarse masks
+template <typename T>
+__global__ void k_prolongate(OpView<T> fo, LevelView<T> C, typename Vec2<T>::type* xf, const typename Vec2<T>::type* __restrict__ xc,
+                             const int* done) {
+    if (stopped(done)) return;
+    const DevGrid<T>& fg = fo.g;
+    const DevGrid<T>& cg = C.o.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= fg.Nx || j >= fg.Ny) return;
+    int k = fg.idx(i, j);
+    uint8_t m = fo.mask[k];
+    typename Vec2<T>::type x = xf[k];
+    int I1, I2, J1, J2;
+    T wx1, wx2, wy1, wy2;
+    T pu = T(0), pv = T(0);
+    if (!(m & U_INACTIVE)) {
+        parents<T>(i, cg.Nx, fg.px, true, C.cx, I1, I2, wx1, wx2);
+        parents<T>(j, cg.Ny, fg.py, false, C.cy, J1, J2, wy1, wy2);
+        pu = wx1 * (wy1 * masked_u(C.o, xc, I1, J1) + wy2 * masked_u(C.o, xc, I1, J2)) +
+             wx2 * (wy1 * masked_u(C.o, xc, I2, J1) + wy2 * masked_u(C.o, xc, I2, J2));
+    }
+    if (!(m & V_INACTIVE)) {
+        parents<T>(i, cg.Nx, fg.px, false, C.cx, I1, I2, wx1, wx2);
+        parents<T>(j, cg.Ny, fg.py, true, C.cy, J1, J2, wy1, wy2);
+        pv = wx1 * (wy1 * masked_v(C.o, xc, I1, J1) + wy2 * masked_v(C.o, xc, I1, J2)) +
+             wx2 * (wy1 * masked_v(C.o, xc, I2, J1) + wy2 * masked_v(C.o, xc, I2, J2));
+    }
+    x.x += pu;
+    x.y += pv;
+    xf[k] = x;
+}
+template <typename T>
+void launch_prolongate(const LevelView<T>& fine, const LevelView<T>& coarse, typename Vec2<T>::type* x_fine,
+                       const typename Vec2<T>::type* x_coarse, const int* done, cudaStream_t s) {
+    LaunchDims d = dims2d(fine.o.g.Nx, fine.o.g.Ny);
+    k_prolongate<T><<<d.grid, d.block, 0, s>>>(fine.o, coarse, x_fine, x_coarse, done);
+}
+
+template <typename T>
+__global__ void k_zero_vec(DevGrid<T> g, typename Vec2<T>::type* x, const int* done) {
+    if (stopped(done)) return;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i > g.Nx || j > g.Ny) return;
+    typename Vec2<T>::type z;
+    z.x = T(0);
+    z.y = T(0);
+    x[g.idx(i, j)] = z;
+}
+template <typename T>
+void launch_zero_vec(const DevGrid<T>& g, typename Vec2<T>::type* x, const int* done, cudaStream_t s) {
+    LaunchDims d = dims2d(g.Nx + 1, g.Ny + 1);
+    k_zero_vec<T><<<d.grid, d.block, 0, s>>>(g, x, done);
+}
+
+#define NK_INSTANTIATE(T)                                                                                                   \
+    template void launch_smooth_point<T>(const LevelView<T>&, const Vec2<T>::type*, Vec2<T>::type*, int, const int*, cudaStream_t); \
+    template void launch_level_apply<T>(const LevelView<T>&, const Vec2<T>::type*, Vec2<T>::type*, int, const int*, cudaStream_t);  \
+    template void launch_line_relax<T>(const LevelView<T>&, Vec2<T>::type*, int, const int*, cudaStream_t);                        \
+    template void launch_restrict<T>(const LevelView<T>&, const LevelView<T>&, const Vec2<T>::type*, Vec2<T>::type*, const int*,   \
+                                     cudaStream_t);                                                                                 \
+    template void launch_prolongate<T>(const LevelView<T>&, const LevelView<T>&, Vec2<T>::type*, const Vec2<T>::type*, const int*, \
+                                       cudaStream_t);                                                                               \
+    template void launch_zero_vec<T>(const DevGrid<T>&, Vec2<T>::type*, const int*, cudaStream_t);
+
+NK_INSTANTIATE(double)
+NK_INSTANTIATE(float)
+
+}  // namespace nk

@@ -1,0 +1,431 @@
+// nk_solver.cu — operator apply, operator masks and diagonals, and the fused conjugate-gradient kernels.
+//
+// Conjugate gradients restate src/Solvers/conjugate_gradient.jl:299-364 with the vector operations of
+// src/Solvers/velocity_vector.jl:48-141 fused into the kernels that produce their operands:
+//   step k:  apply   q = A p,  alpha = rho / p.q                       (one kernel + fused dot)
+//            update  x += alpha p, r -= alpha q [, z = r / diag], dots (one kernel + fused dots)
+//            [multigrid: z = V-cycle(r), then the r.z dot]
+//            xpby    p = z + beta p, commit the stopping decision        (one kernel)
+// Every dot is a deterministic two-stage reduction (fixed block partition and tree); its result stays
+// on the device, so no step needs a host synchronisation.  Every kernel of a step first reads the
+// device `done` flag and returns when the solve has stopped, so steps can be launched in batches (or
+// replayed from a CUDA graph) past convergence at the cost of empty launches.
+#include <cmath>
+
+#include "nk_kernels.cuh"
+
+namespace nk {
+
+// ---- layout conversion --------------------------------------------------------------------------------
+__global__ void k_pack(double* dst, int pitch, int plane, int stride, int offset, const double* __restrict__ src, int nx, int ny,
+                       int planes) {
+    long long n = (long long)nx * ny * planes;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(t % nx);
+        long long r = t / nx;
+        int j = (int)(r % ny);
+        int k = (int)(r / ny);
+        dst[((long long)k * plane + (long long)j * pitch + i) * stride + offset] = src[t];
+    }
+}
+__global__ void k_unpack(double* __restrict__ dst, const double* src, int pitch, int plane, int stride, int offset, int nx, int ny,
+                         int planes) {
+    long long n = (long long)nx * ny * planes;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(t % nx);
+        long long r = t / nx;
+        int j = (int)(r % ny);
+        int k = (int)(r / ny);
+        dst[t] = src[((long long)k * plane + (long long)j * pitch + i) * stride + offset];
+    }
+}
+__global__ void k_fill(double* dst, int count, double value) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) dst[t] = value;
+}
+
+static int blocks_for(long long n) {
+    long long b = (n + 255) / 256;
+    return (int)(b > 4096 ? 4096 : (b < 1 ? 1 : b));
+}
+
+void launch_pack(double* dst, int pitch, int plane, int stride, int offset, const double* src, int nx, int ny, int planes,
+                 cudaStream_t s) {
+    k_pack<<<blocks_for((long long)nx * ny * planes), 256, 0, s>>>(dst, pitch, plane, stride, offset, src, nx, ny, planes);
+}
+void launch_unpack(double* dst, const double* src, int pitch, int plane, int stride, int offset, int nx, int ny, int planes,
+                   cudaStream_t s) {
+    k_unpack<<<blocks_for((long long)nx * ny * planes), 256, 0, s>>>(dst, src, pitch, plane, stride, offset, nx, ny, planes);
+}
+void launch_fill(double* dst, int count, double value, cudaStream_t s) {
+    k_fill<<<blocks_for(count), 256, 0, s>>>(dst, count, value);
+}
+
+// ---- operator, masks, diagonals ---------------------------------------------------------------------------
+__global__ void k_apply(OpView<double> o, const double2* __restrict__ p, double2* __restrict__ q) {
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= o.g.Nx || j >= o.g.Ny) return;
+    q[o.g.idx(i, j)] = apply_at(o, p, i, j);
+}
+void launch_apply(const OpView<double>& o, const double2* p, double2* q, cudaStream_t s) {
+    LaunchDims d = dims2d(o.g.Nx, o.g.Ny);
+    k_apply<<<d.grid, d.block, 0, s>>>(o, p, q);
+}
+
+// inactiveᶠᶜᶜ / inactiveᶜᶠᶜ with η̄H (ssa_operator.jl:91-92, smooth_ice_mask.jl:429-430) and the wall bits
+template <typename T>
+__global__ void k_mask(OpView<T> o, uint8_t* mask) {
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    const DevGrid<T>& g = o.g;
+    if (i > g.Nx || j > g.Ny) return;
+    uint8_t m = 0;
+    bool wu = g.peripheral_fc(i, j), wv = g.peripheral_cf(i, j);
+    bool fu = (o.coef[g.c_idx(i - 1, j)].x + o.coef[g.c_idx(i, j)].x) == T(0);
+    bool fv = (o.coef[g.c_idx(i, j - 1)].x + o.coef[g.c_idx(i, j)].x) == T(0);
+    if (wu) m |= U_WALL;
+    if (wv) m |= V_WALL;
+    if (wu || fu) m |= U_INACTIVE;
+    if (wv || fv) m |= V_INACTIVE;
+    mask[g.idx(i, j)] = m;
+}
+template <typename T>
+void launch_mask(const OpView<T>& o, uint8_t* mask, cudaStream_t s) {
+    LaunchDims d = dims2d(o.g.Nx + 1, o.g.Ny + 1);
+    k_mask<T><<<d.grid, d.block, 0, s>>>(o, mask);
+}
+template void launch_mask<double>(const OpView<double>&, uint8_t*, cudaStream_t);
+template void launch_mask<float>(const OpView<float>&, uint8_t*, cudaStream_t);
+
+__global__ void k_inverse_diagonal(OpView<double> o, double2* invd) {
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= o.g.Nx || j >= o.g.Ny) return;
+    uint8_t m = o.mask[o.g.idx(i, j)];
+    invd[o.g.idx(i, j)] = make_double2(1.0 / x_diagonal(o, i, j, m), 1.0 / y_diagonal(o, i, j, m));
+}
+void launch_inverse_diagonal(const OpView<double>& o, double2* invd, cudaStream_t s) {
+    LaunchDims d = dims2d(o.g.Nx, o.g.Ny);
+    k_inverse_diagonal<<<d.grid, d.block, 0, s>>>(o, invd);
+}
+
+template <typename T>
+__global__ void k_inverse_row_sum(OpView<T> o, typename Vec2<T>::type* irs) {
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= o.g.Nx || j >= o.g.Ny) return;
+    uint8_t m = o.mask[o.g.idx(i, j)];
+    typename Vec2<T>::type r;
+    r.x = T(1) / x_row_sum(o, i, j, m);
+    r.y = T(1) / y_row_sum(o, i, j, m);
+    irs[o.g.idx(i, j)] = r;
+}
+template <typename T>
+void launch_inverse_row_sum(const OpView<T>& o, typename Vec2<T>::type* irs, cudaStream_t s) {
+    LaunchDims d = dims2d(o.g.Nx, o.g.Ny);
+    k_inverse_row_sum<T><<<d.grid, d.block, 0, s>>>(o, irs);
+}
+template void launch_inverse_row_sum<double>(const OpView<double>&, double2*, cudaStream_t);
+template void launch_inverse_row_sum<float>(const OpView<float>&, float2*, cudaStream_t);
+
+// ---- conjugate gradients ------------------------------------------------------------------------------------
+__device__ __forceinline__ int read_done(const SolverScalars* sc) { return *(volatile const int*)&sc->done; }
+
+__device__ __forceinline__ int stop_after(const SolverScalars* sc, double rnorm, int it) {
+    if (!isfinite(rnorm)) return 1;
+    if (sc->fixed) return it >= sc->iterations;
+    return !(rnorm > sc->tol && it < sc->maxiter);
+}
+
+// conjugate_gradient!, conjugate_gradient.jl:306-312: r = b - A x, z = M r, p = z, rho = r.z
+__global__ void k_cg_init(CGView v) {
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    double rz = 0.0, rr = 0.0;
+    if (i < v.o.g.Nx && j < v.o.g.Ny) {
+        int k = v.o.g.idx(i, j);
+        double2 q = apply_at(v.o, (const double2*)v.x, i, j);
+        double2 b = v.b[k];
+        double2 r = make_double2(b.x - q.x, b.y - q.y);
+        v.r[k] = r;
+        rr = r.x * r.x + r.y * r.y;
+        if (v.precond != NK_PRECONDITIONER_MULTIGRID) {
+            double2 z = r;
+            if (v.precond == NK_PRECONDITIONER_DIAGONAL) {
+                double2 d = v.invd[k];
+                z = make_double2(r.x * d.x, r.y * d.y);
+            }
+            v.z[k] = z;
+            v.p[k] = z;
+            rz = r.x * z.x + r.y * z.y;
+        }
+    }
+    double trz, trr;
+    if (grid_sum2(rz, rr, v.partials, &v.sc->ticket, trz, trr) && threadIdx.x == 0 && threadIdx.y == 0) {
+        SolverScalars* sc = v.sc;
+        double r0 = sqrt(trr);
+        sc->rr = trr;
+        sc->r0 = r0;
+        sc->rnorm = r0;
+        sc->tol = fmax(sc->reltol * r0, sc->abstol);
+        sc->it = 0;
+        sc->rho = trz;
+        sc->status = isfinite(r0) ? NK_OK : NK_NONFINITE;
+        int done = sc->fixed ? (sc->iterations <= 0) : !(r0 > sc->tol && 0 < sc->maxiter);
+        if (!isfinite(r0)) done = 1;
+        sc->done = done;
+        sc->done_next = done;
+    }
+}
+void launch_cg_init(const CGView& v, cudaStream_t s) {
+    LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
+    k_cg_init<<<d.grid, d.block, 0, s>>>(v);
+}
+
+// multigrid start: p = z, rho = r.z (and z_old = z for flexible conjugate gradients)
+__global__ void k_cg_init_finish(CGView v) {
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    double rz = 0.0;
+    if (i < v.o.g.Nx && j < v.o.g.Ny) {
+        int k = v.o.g.idx(i, j);
+        double2 z = v.z[k], r = v.r[k];
+        v.p[k] = z;
+        if (v.zold) v.zold[k] = z;
+        rz = r.x * z.x + r.y * z.y;
+    }
+    double trz, dummy;
+    if (grid_sum2(rz, 0.0, v.partials, &v.sc->ticket, trz, dummy) && threadIdx.x == 0 && threadIdx.y == 0) v.sc->rho = trz;
+}
+void launch_cg_init_finish(const CGView& v, cudaStream_t s) {
+    LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
+    k_cg_init_finish<<<d.grid, d.block, 0, s>>>(v);
+}
+
+// conjugate_gradient_step!, conjugate_gradient.jl:350-353: q = A p, alpha = rho / p.q (0 if p.q = 0)
+__global__ void k_cg_apply(CGView v) {
+    if (read_done(v.sc)) return;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    double pq = 0.0;
+    if (i < v.o.g.Nx && j < v.o.g.Ny) {
+        int k = v.o.g.idx(i, j);
+        double2 q = apply_at(v.o, (const double2*)v.p, i, j);
+        v.q[k] = q;
+        double2 p = v.p[k];
+        pq = p.x * q.x + p.y * q.y;
+    }
+    double tpq, dummy;
+    if (grid_sum2(pq, 0.0, v.partials, &v.sc->ticket, tpq, dummy) && threadIdx.x == 0 && threadIdx.y == 0) {
+        SolverScalars* sc = v.sc;
+        sc->pq = tpq;
+        sc->alpha = (tpq == 0.0) ? 0.0 : sc->rho / tpq;
+        if (tpq < 0.0 && sc->status == NK_OK) sc->status = NK_BREAKDOWN;
+    }
+}
+void launch_cg_apply(const CGView& v, cudaStream_t s) {
+    LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
+    k_cg_apply<<<d.grid, d.block, 0, s>>>(v);
+}
+
+// conjugate_gradient_step!, :355-360 and the stopping test of :334-338
+__global__ void k_cg_update(CGView v) {
+    if (read_done(v.sc)) return;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    double alpha = v.sc->alpha;
+    double rz = 0.0, rr = 0.0;
+    if (i < v.o.g.Nx && j < v.o.g.Ny) {
+        int k = v.o.g.idx(i, j);
+        double2 p = v.p[k], q = v.q[k], x = v.x[k], r = v.r[k];
+        x.x = x.x + alpha * p.x;
+        x.y = x.y + alpha * p.y;
+        r.x = r.x + (-alpha) * q.x;
+        r.y = r.y + (-alpha) * q.y;
+        v.x[k] = x;
+        v.r[k] = r;
+        rr = r.x * r.x + r.y * r.y;
+        if (v.precond != NK_PRECONDITIONER_MULTIGRID) {
+            double2 z = r;
+            if (v.precond == NK_PRECONDITIONER_DIAGONAL) {
+                double2 d = v.invd[k];
+                z = make_double2(r.x * d.x, r.y * d.y);
+            }
+            v.z[k] = z;
+            rz = r.x * z.x + r.y * z.y;
+        }
+    }
+    double trz, trr;
+    if (grid_sum2(rz, rr, v.partials, &v.sc->ticket, trz, trr) && threadIdx.x == 0 && threadIdx.y == 0) {
+        SolverScalars* sc = v.sc;
+        sc->rr = trr;
+        double rn = sqrt(trr);
+        sc->rnorm = rn;
+        int it = sc->it + 1;
+        sc->it = it;
+        if (v.precond != NK_PRECONDITIONER_MULTIGRID) {
+            double rho = sc->rho;
+            sc->beta = (rho == 0.0) ? 0.0 : trz / rho;
+            sc->rho = trz;
+        }
+        if (!isfinite(rn)) sc->status = NK_NONFINITE;
+        sc->done_next = stop_after(sc, rn, it);
+    }
+}
+void launch_cg_update(const CGView& v, cudaStream_t s) {
+    LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
+    k_cg_update<<<d.grid, d.block, 0, s>>>(v);
+}
+
+// after z = V-cycle(r): rho_new = r.z; beta = rho_new / rho, or the flexible (Polak-Ribière) form
+// beta = (r.z - r.z_old) / rho when the preconditioner varies between steps
+__global__ void k_cg_dots_after_precondition(CGView v) {
+    if (read_done(v.sc)) return;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    double rz = 0.0, rzo = 0.0;
+    if (i < v.o.g.Nx && j < v.o.g.Ny) {
+        int k = v.o.g.idx(i, j);
+        double2 r = v.r[k], z = v.z[k];
+        rz = r.x * z.x + r.y * z.y;
+        if (v.zold) {
+            double2 zo = v.zold[k];
+            rzo = r.x * zo.x + r.y * zo.y;
+        }
+    }
+    double trz, trzo;
+    if (grid_sum2(rz, rzo, v.partials, &v.sc->ticket, trz, trzo) && threadIdx.x == 0 && threadIdx.y == 0) {
+        SolverScalars* sc = v.sc;
+        double rho = sc->rho;
+        double num = sc->flexible ? (trz - trzo) : trz;
+        sc->beta = (rho == 0.0) ? 0.0 : num / rho;
+        sc->rho = trz;
+        sc->rz_old = trzo;
+    }
+}
+void launch_cg_dots_after_precondition(const CGView& v, cudaStream_t s) {
+    LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
+    k_cg_dots_after_precondition<<<d.grid, d.block, 0, s>>>(v);
+}
+
+// xpby!(z, beta, p), conjugate_gradient.jl:361; the last block commits the stopping decision
+__global__ void k_cg_xpby(CGView v) {
+    if (read_done(v.sc)) return;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    double beta = v.sc->beta;
+    if (i < v.o.g.Nx && j < v.o.g.Ny) {
+        int k = v.o.g.idx(i, j);
+        double2 z = v.z[k], p = v.p[k];
+        p.x = z.x + beta * p.x;
+        p.y = z.y + beta * p.y;
+        v.p[k] = p;
+        if (v.zold) v.zold[k] = z;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        __threadfence();
+        unsigned int n = gridDim.x * gridDim.y;
+        unsigned int t = atomicAdd(&v.sc->ticket2, 1u);
+        if (t == n - 1) {
+            v.sc->ticket2 = 0u;
+            v.sc->done = v.sc->done_next;
+        }
+    }
+}
+void launch_cg_xpby(const CGView& v, cudaStream_t s) {
+    LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
+    k_cg_xpby<<<d.grid, d.block, 0, s>>>(v);
+}
+
+// precondition!(z, ::StressBalanceDiagonalPreconditioner, r, ...) over size(z.u), size(z.v)
+__global__ void k_precondition_diagonal(DevGrid<double> g, double2* z, const double2* __restrict__ r, const double2* __restrict__ invd) {
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i > g.Nx || j > g.Ny) return;
+    int k = g.idx(i, j);
+    double2 o = z[k], rr = r[k];
+    bool has_u = j < g.Ny && (i < g.Nx || !g.px);
+    bool has_v = i < g.Nx && (j < g.Ny || !g.py);
+    bool inside = i < g.Nx && j < g.Ny;
+    double2 d = inside ? invd[k] : make_double2(1.0, 1.0);
+    if (has_u) o.x = (i < g.Nx) ? rr.x * d.x : rr.x;
+    if (has_v) o.y = (j < g.Ny) ? rr.y * d.y : rr.y;
+    z[k] = o;
+}
+void launch_precondition_diagonal(const DevGrid<double>& g, double2* z, const double2* r, const double2* invd, cudaStream_t s) {
+    LaunchDims d = dims2d(g.Nx + 1, g.Ny + 1);
+    k_precondition_diagonal<<<d.grid, d.block, 0, s>>>(g, z, r, invd);
+}
+
+// ---- Picard -------------------------------------------------------------------------------------------------
+__global__ void k_copy_range(DevGrid<double> g, double2* dst, const double2* __restrict__ src) {
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    dst[g.idx(i, j)] = src[g.idx(i, j)];
+}
+void launch_copy_range(const DevGrid<double>& g, double2* dst, const double2* src, cudaStream_t s) {
+    LaunchDims d = dims2d(g.Nx, g.Ny);
+    k_copy_range<<<d.grid, d.block, 0, s>>>(g, dst, src);
+}
+
+// picard.jl:83-85: x⁻ = x⁻ - x, Δ² = x⁻.x⁻, X² = x.x
+__global__ void k_picard_delta(DevGrid<double> g, double2* xprev, const double2* __restrict__ x, SolverScalars* sc, double2* partials) {
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    double dd = 0.0, xx = 0.0;
+    if (i < g.Nx && j < g.Ny) {
+        int k = g.idx(i, j);
+        double2 a = xprev[k], b = x[k];
+        a.x = a.x + (-1.0) * b.x;
+        a.y = a.y + (-1.0) * b.y;
+        xprev[k] = a;
+        dd = a.x * a.x + a.y * a.y;
+        xx = b.x * b.x + b.y * b.y;
+    }
+    double tdd, txx;
+    if (grid_sum2(dd, xx, partials, &sc->ticket, tdd, txx) && threadIdx.x == 0 && threadIdx.y == 0) {
+        sc->picard_dd = tdd;
+        sc->picard_xx = txx;
+    }
+}
+void launch_picard_delta(const DevGrid<double>& g, double2* xprev, const double2* x, SolverScalars* sc, double2* partials,
+                         cudaStream_t s) {
+    LaunchDims d = dims2d(g.Nx, g.Ny);
+    k_picard_delta<<<d.grid, d.block, 0, s>>>(g, xprev, x, sc, partials);
+}
+
+// ---- vector helpers under the done predicate -------------------------------------------------------------------
+__global__ void k_copy_vec(DevGrid<double> g, double2* dst, const double2* __restrict__ src, const int* done) {
+    if (done && *(volatile const int*)done) return;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    dst[g.idx(i, j)] = src[g.idx(i, j)];
+}
+void launch_copy_vec(const DevGrid<double>& g, double2* dst, const double2* src, const int* done, cudaStream_t s) {
+    LaunchDims d = dims2d(g.Nx, g.Ny);
+    k_copy_vec<<<d.grid, d.block, 0, s>>>(g, dst, src, done);
+}
+
+__global__ void k_to_float(DevGrid<double> g, const double2* __restrict__ src, float2* dst, const int* done) {
+    if (done && *(volatile const int*)done) return;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    double2 a = src[g.idx(i, j)];
+    dst[g.idx(i, j)] = make_float2((float)a.x, (float)a.y);
+}
+void launch_to_float(const DevGrid<double>& g, const double2* src, float2* dst, const int* done, cudaStream_t s) {
+    LaunchDims d = dims2d(g.Nx, g.Ny);
+    k_to_float<<<d.grid, d.block, 0, s>>>(g, src, dst, done);
+}
+__global__ void k_to_double(DevGrid<double> g, const float2* __restrict__ src, double2* dst, const int* done) {
+    if (done && *(volatile const int*)done) return;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    float2 a = src[g.idx(i, j)];
+    dst[g.idx(i, j)] = make_double2((double)a.x, (double)a.y);
+}
+void launch_to_double(const DevGrid<double>& g, const float2* src, double2* dst, const int* done, cudaStream_t s) {
+    LaunchDims d = dims2d(g.Nx, g.Ny);
+    k_to_double<<<d.grid, d.block, 0, s>>>(g, src, dst, done);
+}
+__global__ void k_coef_to_float(DevGrid<double> g, const double4* __restrict__ src, float4* dst) {
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i > g.Nx || j > g.Ny) return;
+    double4 a = src[g.idx(i, j)];
+    dst[g.idx(i, j)] = make_float4((float)a.x, (float)a.y, (float)a.z, (float)a.w);
+}
+void launch_coef_to_float(const DevGrid<double>& g, const double4* src, float4* dst, cudaStream_t s) {
+    LaunchDims d = dims2d(g.Nx + 1, g.Ny + 1);
+    k_coef_to_float<<<d.grid, d.block, 0, s>>>(g, src, dst);
+}
+
+}  // namespace nk

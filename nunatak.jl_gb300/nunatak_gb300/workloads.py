@@ -1,0 +1,143 @@
+"""Seeded synthetic workloads of the velocity solve (no dataset involved).
+
+  channel_shelf   floating shelf in a channel, 80 km long, no-slip walls, calving front at 80 km
+  marine_sheet    marine ice sheet on a random bed, Weertman friction with a random coefficient
+  serving_stream  Poisson stream of marine_sheet requests of four sizes on one 512 km x 256 km domain
+  diva_sheet      DIVA marine sheet with an Arrhenius rate factor from a seeded temperature field
+
+Random fields are standard normal draws from numpy.random.default_rng(seed), Gaussian-filtered
+(reflect mode) to the stated correlation length and renormalised to zero mean and unit deviation.
+Units are SI with a year of 31556926 s."""
+from dataclasses import dataclass, field
+from typing import Callable, Dict, Optional
+
+import numpy as np
+
+from . import model as M
+
+YEAR = M.YEAR
+
+
+def random_field(shape, seed, correlation_cells):
+    """Smoothed, renormalised standard normal field of shape (ny, nx)."""
+    from scipy.ndimage import gaussian_filter
+    g = np.random.default_rng(seed).standard_normal(shape)
+    g = gaussian_filter(g, sigma=correlation_cells, mode="reflect")
+    g = g - g.mean()
+    s = g.std()
+    return g / s if s > 0 else g
+
+
+@dataclass
+class Case:
+    """A grid, the configuration objects and the input fields of one velocity solve."""
+    name: str
+    grid: M.RectilinearGrid
+    config: Dict
+    fields: Dict[str, np.ndarray]
+    initial: Dict[str, np.ndarray] = field(default_factory=dict)
+    temperature: Optional[np.ndarray] = None
+
+    def descriptors(self):
+        return M.make_descriptors(self.grid, **self.config)
+
+    def problem(self, cls, context=None):
+        """Problem of class `cls` with the fields set and the geometry and driving stress computed."""
+        P = cls(self.grid, self.descriptors()) if context is None else cls(self.grid, self.descriptors(), context=context)
+        for k, v in self.fields.items():
+            P.set(k, v)
+        if self.temperature is not None:
+            P.set("T", self.temperature)
+            P.compute_rate_factor()
+        P.compute_geometry()
+        for k, v in self.initial.items():
+            P.set(k, v)
+        return P
+
+    @property
+    def cells(self):
+        return self.grid.Nx * self.grid.Ny
+
+
+def _centers(grid):
+    return np.meshgrid(grid.centers(0), grid.centers(1))
+
+
+def channel_shelf(Nx=84, Ny=40, dx=1e3, velocity_solver=None):
+    """Floating shelf in a channel: H = 600 - 400 x / 80 km up to the calving front at x = 80 km (ice free
+    beyond), bed -1000 m (all floating), Glen n = 3, A = 3.17e-24, no-slip side walls, no friction,
+    Jacobi-PCG to 1e-10 inside Picard to 1e-6.  The west wall is impenetrable (u = 0)."""
+    grid = M.RectilinearGrid(size=(Nx, Ny), x=(0.0, Nx * dx), y=(0.0, Ny * dx), halo=(4, 4))
+    X, _ = _centers(grid)
+    H = np.where(X < 80e3, 600.0 - 400.0 * X / 80e3, 0.0)
+    solver = velocity_solver or M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-10, maxiter=10_000),
+                                                      picard_iteration_control=M.Convergence(reltol=1e-6, maxiter=100),
+                                                      preconditioner=M.StressBalanceDiagonalPreconditioner())
+    cfg = dict(Nsigma=10, stress_balance=M.DepthIntegrated(side_walls=M.NoSlipWalls()),
+               rheology=M.GlenFlowLaw(rate_factor=3.17e-24, strain_rate_regularization=1e-13), friction=None,
+               grounding=M.SubgridGroundedFraction(), velocity_solver=solver)
+    return Case("channel_shelf", grid, cfg, {"H": H, "bed": np.full_like(H, -1000.0), "A": np.full_like(H, 3.17e-24)})
+
+
+def marine_sheet(Nx=256, Ny=128, seed=1, seed_friction=None, Lx=512e3, Ly=256e3, velocity_solver=None,
+                 minimum_coarse_size=32, precision="fp64"):
+    """Marine ice sheet on a Lx x Ly domain: bed -100 - 600 x / 512 km + 50 m g (g a 20 km random field),
+    H = 2000 sqrt(max(0, 1 - (x / 420 km)²)), Weertman m = 1/3 with C = 10^(6.5 + 0.3 ξ) Pa (m/yr)^(-1/3)
+    (ξ a 20 km random field), Glen n = 3, A = 3.17e-24, free-slip walls, subgrid grounded fraction,
+    multigrid PCG (2 + 2 point sweeps, coarsening stops at 32 cells)."""
+    grid = M.RectilinearGrid(size=(Nx, Ny), x=(0.0, Lx), y=(0.0, Ly), halo=(4, 4))
+    dx = Lx / Nx
+    X, _ = _centers(grid)
+    g = random_field((Ny, Nx), seed, 20e3 / dx)
+    xi = random_field((Ny, Nx), seed + 7919 if seed_friction is None else seed_friction, 20e3 / dx)
+    bed = -100.0 - 600.0 * X / 512e3 + 50.0 * g
+    H = 2000.0 * np.sqrt(np.maximum(0.0, 1.0 - (X / 420e3) ** 2))
+    C = 10.0 ** (6.5 + 0.3 * xi) * YEAR ** (1.0 / 3.0)
+    mg = M.StressBalanceMultigridPreconditioner(minimum_coarse_size=minimum_coarse_size)
+    solver = velocity_solver or M.StressBalanceSolver(preconditioner=mg, precision=precision)
+    cfg = dict(Nsigma=10, stress_balance=M.DepthIntegrated(side_walls=M.FreeSlipWalls()),
+               rheology=M.GlenFlowLaw(rate_factor=3.17e-24, strain_rate_regularization=1e-13),
+               friction=M.WeertmanFriction(coefficient=None, exponent=1.0 / 3.0), grounding=M.SubgridGroundedFraction(),
+               velocity_solver=solver)
+    return Case("marine_sheet", grid, cfg, {"H": H, "bed": bed, "C": C, "A": np.full_like(H, 3.17e-24)})
+
+
+SERVING_SIZES = ((128, 64), (256, 128), (512, 256), (1024, 512))
+
+
+def serving_stream(n_requests=512, rate=200.0, seed=11, base_seed=1000):
+    """Request list of the serving workload: arrival times from a Poisson process at `rate` requests/s and
+    grid sizes drawn uniformly from 128x64 ... 1024x512, all on the 512 km x 256 km marine-sheet domain,
+    request k carrying friction seed base_seed + k."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, n_requests)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    sizes = rng.integers(len(SERVING_SIZES), size=n_requests)
+    return [dict(index=k, arrival=float(arrivals[k]), size=SERVING_SIZES[int(sizes[k])], seed_friction=base_seed + k)
+            for k in range(n_requests)]
+
+
+def diva_sheet(Nx=2048, Ny=1024, seed=3, dx=1e3, velocity_solver=None, precision="fp64", Nsigma=10):
+    """DIVA marine sheet on a 2048 km x 1024 km domain (marine-sheet geometry stretched by 4), calving front
+    at x = 1900 km, Arrhenius rate factor from T(ζ) = 270 - 17 ζ + 3 K × (30 km random field),
+    regularised Coulomb friction (m = 1/3, α² = 0.5) with the ocean-connected effective pressure."""
+    Lx, Ly = Nx * dx, Ny * dx
+    grid = M.RectilinearGrid(size=(Nx, Ny), x=(0.0, Lx), y=(0.0, Ly), halo=(4, 4))
+    X, _ = _centers(grid)
+    s = Lx / 512e3
+    g = random_field((Ny, Nx), seed, 20e3 * s / dx)
+    xi = random_field((Ny, Nx), seed + 7919, 20e3 * s / dx)
+    dT = random_field((Ny, Nx), seed + 104729, 30e3 / dx)
+    bed = -100.0 - 600.0 * X / Lx + 50.0 * g
+    H = np.where(X < 1900e3, 2000.0 * np.sqrt(np.maximum(0.0, 1.0 - (X / (420e3 * s)) ** 2)), 0.0)
+    C = 10.0 ** (6.5 + 0.3 * xi) * YEAR ** (1.0 / 3.0)
+    faces = np.array([(k / Nsigma) ** 2 for k in range(Nsigma + 1)])
+    zeta = (faces[1:] + faces[:-1]) / 2
+    T = np.stack([270.0 - 17.0 * z + 3.0 * dT for z in zeta])
+    mg = M.StressBalanceMultigridPreconditioner(minimum_coarse_size=32)
+    solver = velocity_solver or M.StressBalanceSolver(preconditioner=mg, precision=precision)
+    cfg = dict(Nsigma=Nsigma, stress_balance=M.DepthIntegrated(shear=M.DIVAShear(), side_walls=M.FreeSlipWalls()),
+               rheology=M.GlenFlowLaw(rate_factor="sigma", strain_rate_regularization=1e-13),
+               friction=M.RegularizedCoulombFriction(coefficient=None, coulomb_coefficient=0.5, exponent=1.0 / 3.0),
+               grounding=M.SubgridGroundedFraction(), velocity_solver=solver)
+    return Case("diva_sheet", grid, cfg, {"H": H, "bed": bed, "C": C}, temperature=T)
