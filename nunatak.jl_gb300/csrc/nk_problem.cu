@@ -55,8 +55,8 @@ struct HostAxis {
 
     void build_regular(int n, int h, bool per, double x0, double L) {
         N = n; H = h; periodic = per; regular = true; delta = L / n;
-        lo = -H - 1;
-        int count = N + 2 * H + 4;
+        lo = -H - 3;                     // two nodes beyond the halo: the metric arrays read indices -1 .. N + 3
+        int count = N + 2 * H + 8;
         F.assign(count, 0); C.assign(count, 0); dC.assign(count, delta); dF.assign(count, delta);
         for (int i = lo; i < lo + count; ++i) {
             F[at(i)] = x0 + ((i - 1) * L) / N;
@@ -65,8 +65,8 @@ struct HostAxis {
     }
     void build_faces(int n, int h, bool per, const double* faces) {
         N = n; H = h; periodic = per; regular = false; delta = 0;
-        lo = -H - 1;
-        int count = N + 2 * H + 4;
+        lo = -H - 3;
+        int count = N + 2 * H + 8;
         F.assign(count, 0); C.assign(count, 0); dC.assign(count, 0); dF.assign(count, 0);
         for (int i = 1; i <= N + 1; ++i) F[at(i)] = faces[i - 1];
         if (per) {
