@@ -188,6 +188,8 @@ typedef struct nk_solve_stats {
     double  picard_change;            /* last ||x - x_prev|| (Convergence) */
     double  picard_norm;              /* last ||x|| (Convergence) */
     double  device_ms;                /* device time of the call, CUDA events */
+    double  device_start_ms;          /* CUDA-event times of the solve's start and end, in ms after the context's */
+    double  device_end_ms;            /* reference event (comparable across the problems of one context) */
 } nk_solve_stats;
 
 typedef struct nk_context nk_context;
@@ -255,6 +257,12 @@ nk_status nk_adjoint_solve(nk_problem* problem, const double* bu, const double* 
  * fields: x = (U, V) warm start, b = (TAU_U, TAU_V).  Updates U, V and every coefficient field. */
 nk_status nk_picard_solve(nk_problem* problem, nk_solve_stats* stats);
 
+/* picard_solve! enqueued on the problem's stream without waiting (one CUDA-graph launch); independent problems
+ * solved this way run concurrently on the device.  nk_problem_wait blocks until it has finished and returns its
+ * statistics (the status of the solve is the return value, as for nk_picard_solve). */
+nk_status nk_picard_solve_async(nk_problem* problem);
+nk_status nk_problem_wait(nk_problem* problem, nk_solve_stats* stats);
+
 /* The whole update_velocities! body for host callers: copies u, v (warm start) in, runs
  * nk_picard_solve and copies u, v out.  u, v in interior layout. */
 nk_status nk_solve_velocities(nk_problem* problem, double* u, double* v, nk_solve_stats* stats);
@@ -275,6 +283,78 @@ nk_status nk_multigrid_restrict(nk_problem* problem, int32_t level, const double
                                 double* coarse_u, double* coarse_v);
 nk_status nk_multigrid_prolongate(nk_problem* problem, int32_t level, const double* coarse_u, const double* coarse_v,
                                   double* fine_u, double* fine_v);
+
+/* ---- serving -------------------------------------------------------------------------------------------
+ *
+ * A request loop for many independent velocity solves (ensemble members, inversion line-search trials,
+ * requests of different grid sizes).  It has no counterpart in the reference, whose model solves one grid
+ * per update_state! (src/Models/ice_sheet_model_methods.jl:80-101); each request is the reference's
+ * set!(model; H) velocity solve (geometry, driving stress, picard_solve!) on its own inputs.
+ *
+ * The server keeps solved problems resident in HBM and reuses a resident problem for a later request with
+ * the same grid, physics and solver (only the input fields change), so each problem's device buffers,
+ * multigrid hierarchy and captured CUDA graph are built once.  Up to max_in_flight requests run at once, each
+ * on its own stream, so requests that arrive while others are on the GPU are admitted as soon as a slot and
+ * memory are free and their kernels overlap on the device.  A new problem is created only while the device
+ * memory of all resident problems stays within memory_cap_bytes (idle problems of other shapes are evicted
+ * first).  Results do not depend on the mix: every request's arithmetic is that of a solve alone. */
+typedef struct nk_server_desc {
+    int32_t max_in_flight;          /* requests on the device at once (>= 1) */
+    int32_t reserved;
+    int64_t memory_cap_bytes;       /* device memory the resident problems may hold */
+} nk_server_desc;
+
+typedef struct nk_request {
+    nk_grid_desc grid;              /* face / sigma vectors, if any, are read during nk_server_submit */
+    nk_physics_desc physics;
+    nk_solver_desc solver;
+    const double* H;                /* interior layout, Nx * Ny */
+    const double* bed;              /* Nx * Ny */
+    const double* friction_coefficient;   /* Nx * Ny, or NULL without friction */
+    const double* rate_factor;      /* Nx * Ny (NK_RATE_FACTOR_2D) */
+    const double* u_init;           /* warm start, or NULL for zero */
+    const double* v_init;
+    double* u_out;                  /* written when the request completes */
+    double* v_out;
+} nk_request;
+
+nk_status nk_server_create(nk_context* ctx, const nk_server_desc* desc, nk_server** out);
+nk_status nk_server_destroy(nk_server* server);
+/* Queue a request; its inputs are copied before the call returns.  *ticket identifies it. */
+nk_status nk_server_submit(nk_server* server, const nk_request* request, int64_t* ticket);
+/* Retire finished requests and admit queued ones; never blocks.  *pending = requests not yet finished. */
+nk_status nk_server_progress(nk_server* server, int32_t* pending);
+/* Block until request `ticket` has finished (driving the loop meanwhile); its statistics and host
+ * timestamps in seconds on the server's clock: submitted, admitted (launched), finished (seen complete). */
+nk_status nk_server_wait(nk_server* server, int64_t ticket, nk_solve_stats* stats, double* t_submit, double* t_admit,
+                         double* t_done);
+/* Block until every submitted request has finished. */
+nk_status nk_server_wait_all(nk_server* server);
+/* Seconds on the server's clock (the clock of the timestamps above). */
+double nk_server_clock(const nk_server* server);
+/* Resident problems, their device bytes, and the largest number of requests that were on the device at once. */
+nk_status nk_server_info(const nk_server* server, int32_t* resident, int64_t* device_bytes, int32_t* peak_in_flight);
+
+/* ---- measurement ----------------------------------------------------------------------------------------- */
+
+/* Kernels that nk_time_kernel can time. */
+#define NK_KERNEL_OPERATOR_FP64   0   /* q = A p on the fine grid (FP64), the apply of every CG step */
+#define NK_KERNEL_SMOOTHER        1   /* one fine-level ℓ1-Jacobi sweep x' = x + (b - A x) / rowsum, in the
+                                         multigrid precision (FP32 when mixed, FP64 otherwise) */
+#define NK_KERNEL_CG_UPDATE       2   /* x += alpha p, r -= alpha q with the fused r.r (and r.z) reductions */
+
+/* Instrumentation (no counterpart in the reference, which times whole solves with @elapsed,
+ * benchmarks/multigrid_scaling.jl:146-157): launches one hot kernel `repeats` times on the problem's
+ * current state and stream, each launch bracketed by CUDA events; when flush_bytes > 0 a device buffer of
+ * that size is overwritten before every launch so the launch starts with a cold L2.  Returns the mean
+ * launch duration and the algorithmic bytes of one launch (every array it reads or writes counted once).
+ * Leaves the solver state changed; call it after a solve, not inside one. */
+nk_status nk_time_kernel(nk_problem* problem, int32_t kernel, int32_t repeats, int64_t flush_bytes,
+                         double* mean_ms, double* bytes_per_launch);
+
+/* Instrumentation (no counterpart in the reference): number of CUDA kernels this library has launched in
+ * the process so far. */
+int64_t nk_launch_count(void);
 
 #ifdef __cplusplus
 }

@@ -63,7 +63,7 @@ __global__ void k_viscosity(PhysView ph, const double2* __restrict__ x, double* 
 }
 void launch_viscosity(const PhysView& ph, const double2* x, double* eta_sigma, double4* coef, double* F2, cudaStream_t s) {
     LaunchDims d = dims2d(ph.g.Nx, ph.g.Ny);
-    k_viscosity<<<d.grid, d.block, 0, s>>>(ph, x, eta_sigma, coef, F2);
+    k_viscosity<<<d.grid, d.block, 0, s>>>(ph, x, eta_sigma, coef, F2); count_launch();
 }
 
 // _compute_shear_viscosity! (glen_flow_law.jl:235-244): the basal stress βᵇ uᵇ drives a vertical shear
@@ -99,7 +99,7 @@ __global__ void k_viscosity_diva(PhysView ph, const double2* __restrict__ x, con
 void launch_viscosity_diva(const PhysView& ph, const double2* x, const double2* bb, const double2* ub, double* eta_sigma,
                            double4* coef, double* F2, cudaStream_t s) {
     LaunchDims d = dims2d(ph.g.Nx, ph.g.Ny);
-    k_viscosity_diva<<<d.grid, d.block, 0, s>>>(ph, x, bb, ub, eta_sigma, coef, F2);
+    k_viscosity_diva<<<d.grid, d.block, 0, s>>>(ph, x, bb, ub, eta_sigma, coef, F2); count_launch();
 }
 
 // _interpolate_to_corners! (stress_balance_coefficients.jl:26-29): ℑxyᶠᶠᵃ = ℑyᵃᶠᵃ(ℑxᶠᵃᵃ(η̄H))
@@ -114,7 +114,7 @@ __global__ void k_corners(DevGrid<T> g, typename Vec4<T>::type* coef) {
 template <typename T>
 void launch_corners(const DevGrid<T>& g, typename Vec4<T>::type* coef, cudaStream_t s) {
     LaunchDims d = dims2d(g.Nx + 1, g.Ny + 1);
-    k_corners<T><<<d.grid, d.block, 0, s>>>(g, coef);
+    k_corners<T><<<d.grid, d.block, 0, s>>>(g, coef); count_launch();
 }
 template void launch_corners<double>(const DevGrid<double>&, double4*, cudaStream_t);
 template void launch_corners<float>(const DevGrid<float>&, float4*, cudaStream_t);
@@ -168,7 +168,7 @@ __global__ void k_basal_drag(PhysView ph, const double2* __restrict__ x, double4
 void launch_basal_drag(const PhysView& ph, const double2* x, double4* coef, double2* bb, cudaStream_t s) {
     if (ph.friction == NK_FRICTION_NONE) return;   // compute_basal_drag!(βᵘ, βᵛ, ::Nothing, ...) = nothing
     LaunchDims d = dims2d(ph.g.Nx + 1, ph.g.Ny + 1);
-    k_basal_drag<<<d.grid, d.block, 0, s>>>(ph, x, coef, bb);
+    k_basal_drag<<<d.grid, d.block, 0, s>>>(ph, x, coef, bb); count_launch();
 }
 
 // 1 + βᵇ ℑF₂ at the velocity points, diva.jl:161-163
@@ -194,7 +194,7 @@ __global__ void k_basal_velocity(PhysView ph, const double2* __restrict__ x, con
 }
 void launch_basal_velocity(const PhysView& ph, const double2* x, const double2* bb, const double* F2, double2* ub, cudaStream_t s) {
     LaunchDims d = dims2d(ph.g.Nx + 1, ph.g.Ny + 1);
-    k_basal_velocity<<<d.grid, d.block, 0, s>>>(ph, x, bb, F2, ub);
+    k_basal_velocity<<<d.grid, d.block, 0, s>>>(ph, x, bb, F2, ub); count_launch();
 }
 
 __global__ void k_effective_drag(PhysView ph, const double2* __restrict__ bb, const double* __restrict__ F2, double4* coef) {
@@ -210,7 +210,7 @@ __global__ void k_effective_drag(PhysView ph, const double2* __restrict__ bb, co
 }
 void launch_effective_drag(const PhysView& ph, const double2* bb, const double* F2, double4* coef, cudaStream_t s) {
     LaunchDims d = dims2d(ph.g.Nx + 1, ph.g.Ny + 1);
-    k_effective_drag<<<d.grid, d.block, 0, s>>>(ph, bb, F2, coef);
+    k_effective_drag<<<d.grid, d.block, 0, s>>>(ph, bb, F2, coef); count_launch();
 }
 
 // shear_integral (column_integrals.jl:71): H ∫₀^ζₖ (1 - ζ′)/η dζ′
@@ -256,9 +256,9 @@ __global__ void k_copy_faces(DevGrid<double> g, const double2* __restrict__ x, d
 void launch_velocity_profile(const PhysView& ph, int diva, const double2* x, const double2* bb, const double* F2,
                              const double* eta_sigma, double2* ub, double2* usig, cudaStream_t s) {
     LaunchDims d = dims2d(ph.g.Nx + 1, ph.g.Ny + 1);
-    if (diva) k_basal_velocity<<<d.grid, d.block, 0, s>>>(ph, x, bb, F2, ub);
-    else k_copy_faces<<<d.grid, d.block, 0, s>>>(ph.g, x, ub);
-    k_velocity_profile<<<d.grid, d.block, 0, s>>>(ph, diva, x, bb, eta_sigma, ub, usig);
+    if (diva) { k_basal_velocity<<<d.grid, d.block, 0, s>>>(ph, x, bb, F2, ub); count_launch(); }
+    else { k_copy_faces<<<d.grid, d.block, 0, s>>>(ph.g, x, ub); count_launch(); }
+    k_velocity_profile<<<d.grid, d.block, 0, s>>>(ph, diva, x, bb, eta_sigma, ub, usig); count_launch();
 }
 
 // ---- geometry ---------------------------------------------------------------------------------------------
@@ -376,8 +376,8 @@ __global__ void k_driving_stress(GeometryView v) {
 
 void launch_geometry(const GeometryView& v, cudaStream_t s) {
     LaunchDims d = dims2d(v.g.Nx + 1, v.g.Ny + 1);
-    k_geometry<<<d.grid, d.block, 0, s>>>(v);
-    k_driving_stress<<<d.grid, d.block, 0, s>>>(v);
+    k_geometry<<<d.grid, d.block, 0, s>>>(v); count_launch();
+    k_driving_stress<<<d.grid, d.block, 0, s>>>(v); count_launch();
 }
 
 // _compute_rate_factor! with ω = 0 (column_energy_solve.jl:104-110) and arrhenius_rate_factor (arrhenius_rate_factor.jl:102-110)
@@ -401,7 +401,7 @@ __global__ void k_rate_factor(DevGrid<double> g, SigmaTable sig, int plane, cons
 void launch_rate_factor(const DevGrid<double>& g, const SigmaTable& sig, int plane, const double* H, const double* T, double* A,
                         double rho_i, double gacc, const double* params, cudaStream_t s) {
     LaunchDims d = dims2d(g.Nx, g.Ny);
-    k_rate_factor<<<d.grid, d.block, 0, s>>>(g, sig, plane, H, T, A, rho_i, gacc, params);
+    k_rate_factor<<<d.grid, d.block, 0, s>>>(g, sig, plane, H, T, A, rho_i, gacc, params); count_launch();
 }
 
 }  // namespace nk

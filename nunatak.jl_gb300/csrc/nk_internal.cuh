@@ -86,6 +86,10 @@ struct SolverScalars {
     int fixed, iterations, maxiter, flexible;
     unsigned int ticket;           // last-block counter of the fused reductions
     unsigned int ticket2;
+    // Picard (picard.jl:63-90), evaluated on the device between the conjugate-gradient solves
+    double p_reltol, p_abstol, p_D, p_X;
+    int p_fixed, p_iterations, p_maxiter, p_it;
+    int p_done, it_total, cg_unconverged, pad;
 };
 
 // ---- warp / block reductions (fixed order, so results do not depend on scheduling) --------------------
@@ -148,7 +152,14 @@ __device__ __forceinline__ bool grid_sum2(double a, double b, double2* partials,
     return true;   // totals valid in thread 0
 }
 
-// ---- host side helpers ------------------------------------------------------------------------------
+// ---- host side helpers ------------------------------------------------------------------------------------
+// Kernels launched by the library in this process (instrumentation; every launch site calls count_launch()).
+void count_launch();
+void count_launches(long long n);
+void set_capturing(bool on);
+long long launch_count();
+
+// ---- host side helpers (continued) ------------------------------------------------------------------------------
 struct LaunchDims {
     dim3 grid, block;
 };

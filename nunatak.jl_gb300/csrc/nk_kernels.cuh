@@ -58,6 +58,9 @@ struct CGView {
     int precond;                  // NK_PRECONDITIONER_*
     SolverScalars* sc;
     double2* partials;
+    unsigned long long cond;      // conditional-node handle of the conjugate-gradient while loop (0: none)
+    float2* r32;                  // mixed precision: FP32 copy of r written for the V-cycle (or nullptr)
+    const float2* z32;            // mixed precision: FP32 V-cycle result read back as z (or nullptr)
 };
 // r = b - A x; if the preconditioner is not multigrid also z = M r, p = z, rho = r.z; r0, tol, done
 void launch_cg_init(const CGView& v, cudaStream_t s);
@@ -75,9 +78,11 @@ void launch_cg_xpby(const CGView& v, cudaStream_t s);
 void launch_precondition_diagonal(const DevGrid<double>& g, double2* z, const double2* r, const double2* invd, cudaStream_t s);
 // Picard: xprev = x (over the Nx x Ny range)
 void launch_copy_range(const DevGrid<double>& g, double2* dst, const double2* src, cudaStream_t s);
-// Picard: xprev -= x, ||xprev||^2, ||x||^2 into sc
-void launch_picard_delta(const DevGrid<double>& g, double2* xprev, const double2* x, SolverScalars* sc, double2* partials,
-                         cudaStream_t s);
+// Picard loop control on the device: begin (iteration 0) and end of one iteration (Δ, X, stopping test),
+// each setting the conditional-node handle `cond` of the Picard while loop
+void launch_picard_begin(SolverScalars* sc, unsigned long long cond, cudaStream_t s);
+void launch_picard_end(const DevGrid<double>& g, double2* xprev, const double2* x, SolverScalars* sc, double2* partials,
+                       unsigned long long cond, cudaStream_t s);
 
 // ---- coefficients ---------------------------------------------------------------------------------------
 // SSA membrane viscosity (glen_flow_law.jl:208-212) and column integrals (column_integrals.jl:90-101)
@@ -139,14 +144,26 @@ void launch_level_apply(const LevelView<T>& L, const typename Vec2<T>::type* x, 
 // `first`: x starts at zero (q = A x = 0 is not read, x is overwritten)
 template <typename T>
 void launch_line_relax(const LevelView<T>& L, typename Vec2<T>::type* x, int first, const int* done, cudaStream_t s);
+// b_coarse = R r_fine; when first_out is given also first_out = b_coarse / rowsum (the coarse level's first sweep)
 template <typename T>
 void launch_restrict(const LevelView<T>& coarse, const LevelView<T>& fine, const typename Vec2<T>::type* r_fine,
-                     typename Vec2<T>::type* b_coarse, const int* done, cudaStream_t s);
+                     typename Vec2<T>::type* b_coarse, typename Vec2<T>::type* first_out, const int* done, cudaStream_t s);
 template <typename T>
 void launch_prolongate(const LevelView<T>& fine, const LevelView<T>& coarse, typename Vec2<T>::type* x_fine,
                        const typename Vec2<T>::type* x_coarse, const int* done, cudaStream_t s);
 template <typename T>
 void launch_zero_vec(const DevGrid<T>& g, typename Vec2<T>::type* x, const int* done, cudaStream_t s);
+// Every level from one level down to the coarsest, handled by a single thread block.
+constexpr int MAX_COARSE_LEVELS = 12;
+template <typename T>
+struct CoarseLevels {
+    LevelView<T> lv[MAX_COARSE_LEVELS];
+    int n;                  // number of levels in lv (>= 1); lv[n - 1] is the coarsest
+    int sweeps, coarsest;   // smoothing_sweeps, coarsest_sweeps
+    int line;               // y-line smoother
+};
+template <typename T>
+void launch_coarse_vcycle(const CoarseLevels<T>& C, const int* done, cudaStream_t s);
 // FP64 <-> FP32 conversions of vectors and of the coefficient record
 void launch_to_float(const DevGrid<double>& g, const double2* src, float2* dst, const int* done, cudaStream_t s);
 void launch_to_double(const DevGrid<double>& g, const float2* src, double2* dst, const int* done, cudaStream_t s);

@@ -101,21 +101,19 @@ template <typename T, typename TF>
 void launch_coarsen(const LevelView<T>& coarse, const DevGrid<TF>& fine_g, const typename Vec4<TF>::type* fine_coef,
                     typename Vec4<T>::type* coarse_coef, cudaStream_t s) {
     LaunchDims d = dims2d(coarse.o.g.Nx, coarse.o.g.Ny);
-    k_coarsen<T, TF><<<d.grid, d.block, 0, s>>>(coarse.o, coarse.cx, coarse.cy, fine_g, fine_coef, coarse_coef);
+    k_coarsen<T, TF><<<d.grid, d.block, 0, s>>>(coarse.o, coarse.cx, coarse.cy, fine_g, fine_coef, coarse_coef); count_launch();
     launch_corners<T>(coarse.o.g, coarse_coef, s);
 }
 template void launch_coarsen<double, double>(const LevelView<double>&, const DevGrid<double>&, const double4*, double4*, cudaStream_t);
 template void launch_coarsen<float, double>(const LevelView<float>&, const DevGrid<double>&, const double4*, float4*, cudaStream_t);
 template void launch_coarsen<float, float>(const LevelView<float>&, const DevGrid<float>&, const float4*, float4*, cudaStream_t);
 
-// ---- smoothers ---------------------------------------------------------------------------------------------
+// ---- per-point operations (shared by the grid-wide kernels and the fused coarse V-cycle) -------------------
+// ℓ1-Jacobi update of one cell (_smooth!, :213-219); `first`: x_in = 0, so A x_in = 0 and x_out = b / rowsum
 template <typename T>
-__global__ void k_smooth_point(LevelView<T> L, const typename Vec2<T>::type* __restrict__ xin, typename Vec2<T>::type* __restrict__ xout,
-                               int first, const int* done) {
-    if (stopped(done)) return;
+__device__ __forceinline__ void smooth_point_at(const LevelView<T>& L, const typename Vec2<T>::type* __restrict__ xin,
+                                                typename Vec2<T>::type* __restrict__ xout, bool first, int i, int j) {
     using V2 = typename Vec2<T>::type;
-    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
-    if (i >= L.o.g.Nx || j >= L.o.g.Ny) return;
     int k = L.o.g.idx(i, j);
     V2 b = L.b[k], w = L.irs[k], out;
     if (first) {
@@ -129,20 +127,12 @@ __global__ void k_smooth_point(LevelView<T> L, const typename Vec2<T>::type* __r
     }
     xout[k] = out;
 }
-template <typename T>
-void launch_smooth_point(const LevelView<T>& L, const typename Vec2<T>::type* x_in, typename Vec2<T>::type* x_out, int first,
-                         const int* done, cudaStream_t s) {
-    LaunchDims d = dims2d(L.o.g.Nx, L.o.g.Ny);
-    k_smooth_point<T><<<d.grid, d.block, 0, s>>>(L, x_in, x_out, first, done);
-}
 
+// q = A x, or the residual q = b - A x
 template <typename T>
-__global__ void k_level_apply(LevelView<T> L, const typename Vec2<T>::type* __restrict__ x, typename Vec2<T>::type* __restrict__ q,
-                              int residual, const int* done) {
-    if (stopped(done)) return;
+__device__ __forceinline__ void apply_or_residual_at(const LevelView<T>& L, const typename Vec2<T>::type* __restrict__ x,
+                                                     typename Vec2<T>::type* __restrict__ q, bool residual, int i, int j) {
     using V2 = typename Vec2<T>::type;
-    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
-    if (i >= L.o.g.Nx || j >= L.o.g.Ny) return;
     int k = L.o.g.idx(i, j);
     V2 a = apply_at(L.o, x, i, j);
     if (residual) {
@@ -152,62 +142,14 @@ __global__ void k_level_apply(LevelView<T> L, const typename Vec2<T>::type* __re
     }
     q[k] = a;
 }
-template <typename T>
-void launch_level_apply(const LevelView<T>& L, const typename Vec2<T>::type* x, typename Vec2<T>::type* q, int residual,
-                        const int* done, cudaStream_t s) {
-    LaunchDims d = dims2d(L.o.g.Nx, L.o.g.Ny);
-    k_level_apply<T><<<d.grid, d.block, 0, s>>>(L, x, q, residual, done);
-}
 
-// line_relax!, :231-253: Thomas algorithm along j for the u line and then the v line of column i.
-// `first`: x starts at zero, so q = A x = 0 is not read and x is overwritten by δ.
+// restrict (:307-318) of one coarse point with the fine and coarse masks (_restrict!, :346-352).
+// first_out != nullptr also performs the coarse level's first smoothing sweep from zero: first_out = b / rowsum.
 template <typename T>
-__global__ void k_line_relax(LevelView<T> L, typename Vec2<T>::type* x, int first, const int* done) {
-    if (stopped(done)) return;
-    const DevGrid<T>& g = L.o.g;
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= g.Nx) return;
-    int Ny = g.Ny;
-    for (int comp = 0; comp < 2; ++comp) {
-        T cj = 0, tj = 0, dj = 0;
-        for (int j = 0; j < Ny; ++j) {
-            int k = g.idx(i, j);
-            uint8_t m = L.o.mask[k];
-            T s = comp == 0 ? x_row_sum(L.o, i, j, m) : y_row_sum(L.o, i, j, m);
-            T cj1 = (j == Ny - 1) ? T(0) : (comp == 0 ? x_line_coupling(L.o, i, j + 1) : y_line_coupling(L.o, i, j + 1));
-            T mm = s - cj - cj1 + cj * tj;
-            T bq = comp == 0 ? (L.b[k].x - (first ? T(0) : L.q[k].x)) : (L.b[k].y - (first ? T(0) : L.q[k].y));
-            dj = (bq + cj * dj) / mm;
-            tj = -cj1 / mm;
-            L.t[k] = tj;
-            if (comp == 0) L.q[k].x = dj; else L.q[k].y = dj;
-            cj = cj1;
-        }
-        T delta = 0;
-        for (int j = Ny - 1; j >= 0; --j) {
-            int k = g.idx(i, j);
-            delta = (comp == 0 ? L.q[k].x : L.q[k].y) - L.t[k] * delta;
-            if (comp == 0) x[k].x = first ? delta : x[k].x + delta;
-            else x[k].y = first ? delta : x[k].y + delta;
-        }
-    }
-}
-template <typename T>
-void launch_line_relax(const LevelView<T>& L, typename Vec2<T>::type* x, int first, const int* done, cudaStream_t s) {
-    int nb = (L.o.g.Nx + 127) / 128;
-    k_line_relax<T><<<nb, 128, 0, s>>>(L, x, first, done);
-}
-
-// ---- transfers --------------------------------------------------------------------------------------------
-// _restrict!, :346-352: b_coarse = R r_fine with fine and coarse masks
-template <typename T>
-__global__ void k_restrict(LevelView<T> C, OpView<T> fo, const typename Vec2<T>::type* __restrict__ rf,
-                           typename Vec2<T>::type* bc, const int* done) {
-    if (stopped(done)) return;
+__device__ __forceinline__ void restrict_at(const LevelView<T>& C, const OpView<T>& fo, const typename Vec2<T>::type* __restrict__ rf,
+                                            typename Vec2<T>::type* bc, typename Vec2<T>::type* first_out, int I, int J) {
     const DevGrid<T>& cg = C.o.g;
     const DevGrid<T>& fg = fo.g;
-    int I = blockIdx.x * BX + threadIdx.x, J = blockIdx.y * BY + threadIdx.y;
-    if (I >= cg.Nx || J >= cg.Ny) return;
     int k = cg.idx(I, J);
     uint8_t m = C.o.mask[k];
     T su = T(0), sv = T(0);
@@ -236,23 +178,20 @@ __global__ void k_restrict(LevelView<T> C, OpView<T> fo, const typename Vec2<T>:
     o.x = su;
     o.y = sv;
     bc[k] = o;
-}
-template <typename T>
-void launch_restrict(const LevelView<T>& coarse, const LevelView<T>& fine, const typename Vec2<T>::type* r_fine,
-                     typename Vec2<T>::type* b_coarse, const int* done, cudaStream_t s) {
-    LaunchDims d = dims2d(coarse.o.g.Nx, coarse.o.g.Ny);
-    k_restrict<T><<<d.grid, d.block, 0, s>>>(coarse, fine.o, r_fine, b_coarse, done);
+    if (first_out) {
+        typename Vec2<T>::type w = C.irs[k], x;
+        x.x = su * w.x;
+        x.y = sv * w.y;
+        first_out[k] = x;
+    }
 }
 
-// _prolongate!, :354-360: x_fine += P x_coarse with fine and coarse masks
+// prolongate (:320-327) into one fine point, x_fine += P x_coarse (_prolongate!, :354-360)
 template <typename T>
-__global__ void k_prolongate(OpView<T> fo, LevelView<T> C, typename Vec2<T>::type* xf, const typename Vec2<T>::type* __restrict__ xc,
-                             const int* done) {
-    if (stopped(done)) return;
+__device__ __forceinline__ void prolong_at(const OpView<T>& fo, const LevelView<T>& C, typename Vec2<T>::type* xf,
+                                           const typename Vec2<T>::type* __restrict__ xc, int i, int j) {
     const DevGrid<T>& fg = fo.g;
     const DevGrid<T>& cg = C.o.g;
-    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
-    if (i >= fg.Nx || j >= fg.Ny) return;
     int k = fg.idx(i, j);
     uint8_t m = fo.mask[k];
     typename Vec2<T>::type x = xf[k];
@@ -275,11 +214,134 @@ __global__ void k_prolongate(OpView<T> fo, LevelView<T> C, typename Vec2<T>::typ
     x.y += pv;
     xf[k] = x;
 }
+
+// line_relax!, :231-253: Thomas algorithm along j for the u line and then the v line of column i.
+// `first`: x starts at zero, so q = A x = 0 is not read and x is overwritten by δ.
+template <typename T>
+__device__ __forceinline__ void line_relax_column(const LevelView<T>& L, typename Vec2<T>::type* x, bool first, int i) {
+    const DevGrid<T>& g = L.o.g;
+    int Ny = g.Ny;
+    for (int comp = 0; comp < 2; ++comp) {
+        T cj = 0, tj = 0, dj = 0;
+        for (int j = 0; j < Ny; ++j) {
+            int k = g.idx(i, j);
+            uint8_t m = L.o.mask[k];
+            T s = comp == 0 ? x_row_sum(L.o, i, j, m) : y_row_sum(L.o, i, j, m);
+            T cj1 = (j == Ny - 1) ? T(0) : (comp == 0 ? x_line_coupling(L.o, i, j + 1) : y_line_coupling(L.o, i, j + 1));
+            T mm = s - cj - cj1 + cj * tj;
+            T bq = comp == 0 ? (L.b[k].x - (first ? T(0) : L.q[k].x)) : (L.b[k].y - (first ? T(0) : L.q[k].y));
+            dj = (bq + cj * dj) / mm;
+            tj = -cj1 / mm;
+            L.t[k] = tj;
+            if (comp == 0) L.q[k].x = dj; else L.q[k].y = dj;
+            cj = cj1;
+        }
+        T delta = 0;
+        for (int j = Ny - 1; j >= 0; --j) {
+            int k = g.idx(i, j);
+            delta = (comp == 0 ? L.q[k].x : L.q[k].y) - L.t[k] * delta;
+            if (comp == 0) x[k].x = first ? delta : x[k].x + delta;
+            else x[k].y = first ? delta : x[k].y + delta;
+        }
+    }
+}
+
+// ---- grid-wide kernels ---------------------------------------------------------------------------------------
+template <typename T>
+__global__ void k_smooth_point(LevelView<T> L, const typename Vec2<T>::type* __restrict__ xin, typename Vec2<T>::type* __restrict__ xout,
+                               int first, const int* done) {
+    if (stopped(done)) return;
+    using V2 = typename Vec2<T>::type;
+    int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY;
+    int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+    bool inside = i < L.o.g.Nx && j < L.o.g.Ny;
+    if (first) {
+        if (inside) smooth_point_at(L, xin, xout, true, i, j);
+        return;
+    }
+    __shared__ ApplyTile<T> sm;
+    V2 q = tiled_apply(L.o, xin, sm, i0, j0, i, j, inside);
+    if (!inside) return;
+    int k = L.o.g.idx(i, j);
+    V2 b = L.b[k], w = L.irs[k], x = xin[k], out;
+    out.x = x.x + (b.x - q.x) * w.x;
+    out.y = x.y + (b.y - q.y) * w.y;
+    xout[k] = out;
+}
+template <typename T>
+void launch_smooth_point(const LevelView<T>& L, const typename Vec2<T>::type* x_in, typename Vec2<T>::type* x_out, int first,
+                         const int* done, cudaStream_t s) {
+    LaunchDims d = dims2d(L.o.g.Nx, L.o.g.Ny);
+    k_smooth_point<T><<<d.grid, d.block, 0, s>>>(L, x_in, x_out, first, done); count_launch();
+}
+
+template <typename T>
+__global__ void k_level_apply(LevelView<T> L, const typename Vec2<T>::type* __restrict__ x, typename Vec2<T>::type* __restrict__ q,
+                              int residual, const int* done) {
+    if (stopped(done)) return;
+    using V2 = typename Vec2<T>::type;
+    __shared__ ApplyTile<T> sm;
+    int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY;
+    int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+    bool inside = i < L.o.g.Nx && j < L.o.g.Ny;
+    V2 a = tiled_apply(L.o, x, sm, i0, j0, i, j, inside);
+    if (!inside) return;
+    int k = L.o.g.idx(i, j);
+    if (residual) {
+        V2 b = L.b[k];
+        a.x = b.x - a.x;
+        a.y = b.y - a.y;
+    }
+    q[k] = a;
+}
+template <typename T>
+void launch_level_apply(const LevelView<T>& L, const typename Vec2<T>::type* x, typename Vec2<T>::type* q, int residual,
+                        const int* done, cudaStream_t s) {
+    LaunchDims d = dims2d(L.o.g.Nx, L.o.g.Ny);
+    k_level_apply<T><<<d.grid, d.block, 0, s>>>(L, x, q, residual, done); count_launch();
+}
+
+template <typename T>
+__global__ void k_line_relax(LevelView<T> L, typename Vec2<T>::type* x, int first, const int* done) {
+    if (stopped(done)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= L.o.g.Nx) return;
+    line_relax_column(L, x, first != 0, i);
+}
+template <typename T>
+void launch_line_relax(const LevelView<T>& L, typename Vec2<T>::type* x, int first, const int* done, cudaStream_t s) {
+    int nb = (L.o.g.Nx + 127) / 128;
+    k_line_relax<T><<<nb, 128, 0, s>>>(L, x, first, done); count_launch();
+}
+
+template <typename T>
+__global__ void k_restrict(LevelView<T> C, OpView<T> fo, const typename Vec2<T>::type* __restrict__ rf,
+                           typename Vec2<T>::type* bc, typename Vec2<T>::type* first_out, const int* done) {
+    if (stopped(done)) return;
+    int I = blockIdx.x * BX + threadIdx.x, J = blockIdx.y * BY + threadIdx.y;
+    if (I >= C.o.g.Nx || J >= C.o.g.Ny) return;
+    restrict_at(C, fo, rf, bc, first_out, I, J);
+}
+template <typename T>
+void launch_restrict(const LevelView<T>& coarse, const LevelView<T>& fine, const typename Vec2<T>::type* r_fine,
+                     typename Vec2<T>::type* b_coarse, typename Vec2<T>::type* first_out, const int* done, cudaStream_t s) {
+    LaunchDims d = dims2d(coarse.o.g.Nx, coarse.o.g.Ny);
+    k_restrict<T><<<d.grid, d.block, 0, s>>>(coarse, fine.o, r_fine, b_coarse, first_out, done); count_launch();
+}
+
+template <typename T>
+__global__ void k_prolongate(OpView<T> fo, LevelView<T> C, typename Vec2<T>::type* xf, const typename Vec2<T>::type* __restrict__ xc,
+                             const int* done) {
+    if (stopped(done)) return;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= fo.g.Nx || j >= fo.g.Ny) return;
+    prolong_at(fo, C, xf, xc, i, j);
+}
 template <typename T>
 void launch_prolongate(const LevelView<T>& fine, const LevelView<T>& coarse, typename Vec2<T>::type* x_fine,
                        const typename Vec2<T>::type* x_coarse, const int* done, cudaStream_t s) {
     LaunchDims d = dims2d(fine.o.g.Nx, fine.o.g.Ny);
-    k_prolongate<T><<<d.grid, d.block, 0, s>>>(fine.o, coarse, x_fine, x_coarse, done);
+    k_prolongate<T><<<d.grid, d.block, 0, s>>>(fine.o, coarse, x_fine, x_coarse, done); count_launch();
 }
 
 template <typename T>
@@ -295,18 +357,98 @@ __global__ void k_zero_vec(DevGrid<T> g, typename Vec2<T>::type* x, const int* d
 template <typename T>
 void launch_zero_vec(const DevGrid<T>& g, typename Vec2<T>::type* x, const int* done, cudaStream_t s) {
     LaunchDims d = dims2d(g.Nx + 1, g.Ny + 1);
-    k_zero_vec<T><<<d.grid, d.block, 0, s>>>(g, x, done);
+    k_zero_vec<T><<<d.grid, d.block, 0, s>>>(g, x, done); count_launch();
+}
+
+// ---- fused coarse V-cycle: one thread block runs every remaining level ----------------------------------------
+// The coarse levels of a V-cycle are a few thousand cells or less, where a grid-wide launch per sweep costs more
+// than the sweep.  One 1024-thread block walks the rest of v_cycle! (:144-163) level by level — smooth, residual,
+// restrict, the coarsest sweeps, prolongate, smooth — with a block barrier between phases; all data stays in
+// global memory (L1/L2 resident at these sizes).  Level 0 of `C` holds its right-hand side on entry and its
+// correction on exit.
+template <typename T>
+__device__ void block_smooth(const CoarseLevels<T>& C, const LevelView<T>& L, int sweeps, bool first) {
+    using V2 = typename Vec2<T>::type;
+    const DevGrid<T>& g = L.o.g;
+    int n = g.Nx * g.Ny, tid = threadIdx.x, nt = blockDim.x;
+    if (sweeps <= 0) {
+        if (first)
+            for (int c = tid; c < n; c += nt) { V2 z; z.x = T(0); z.y = T(0); L.x[g.idx(c % g.Nx, c / g.Nx)] = z; }
+        __syncthreads();
+        return;
+    }
+    if (C.line) {
+        for (int k = 0; k < sweeps; ++k) {
+            bool f = first && k == 0;
+            if (!f) {
+                for (int c = tid; c < n; c += nt) apply_or_residual_at(L, (const V2*)L.x, L.q, false, c % g.Nx, c / g.Nx);
+                __syncthreads();
+            }
+            for (int i = tid; i < g.Nx; i += nt) line_relax_column(L, L.x, f, i);
+            __syncthreads();
+        }
+        return;
+    }
+    const V2* in = L.x;
+    if (!first && sweeps % 2 == 1) {
+        for (int c = tid; c < n; c += nt) { int k = g.idx(c % g.Nx, c / g.Nx); L.x2[k] = L.x[k]; }
+        __syncthreads();
+        in = L.x2;
+    }
+    for (int k = 0; k < sweeps; ++k) {
+        V2* out = ((sweeps - 1 - k) % 2 == 0) ? L.x : L.x2;
+        bool f = first && k == 0;
+        for (int c = tid; c < n; c += nt) smooth_point_at(L, in, out, f, c % g.Nx, c / g.Nx);
+        __syncthreads();
+        in = out;
+    }
+}
+
+template <typename T>
+constexpr int coarse_threads() { return sizeof(T) == 8 ? 512 : 1024; }   // FP64 needs more registers per thread
+
+template <typename T>
+__global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024, 1) k_coarse_vcycle(CoarseLevels<T> C, const int* done) {
+    if (stopped(done)) return;
+    using V2 = typename Vec2<T>::type;
+    int tid = threadIdx.x, nt = blockDim.x;
+    int last = C.n - 1;
+    for (int l = 0; l < last; ++l) {
+        const LevelView<T>& L = C.lv[l];
+        const LevelView<T>& N = C.lv[l + 1];
+        block_smooth(C, L, C.sweeps, true);
+        int n = L.o.g.Nx * L.o.g.Ny;
+        for (int c = tid; c < n; c += nt) apply_or_residual_at(L, (const V2*)L.x, L.q, true, c % L.o.g.Nx, c / L.o.g.Nx);
+        __syncthreads();
+        int m = N.o.g.Nx * N.o.g.Ny;
+        for (int c = tid; c < m; c += nt) restrict_at(N, L.o, (const V2*)L.q, N.b, (V2*)nullptr, c % N.o.g.Nx, c / N.o.g.Nx);
+        __syncthreads();
+    }
+    block_smooth(C, C.lv[last], C.coarsest, true);
+    for (int l = last - 1; l >= 0; --l) {
+        const LevelView<T>& L = C.lv[l];
+        const LevelView<T>& N = C.lv[l + 1];
+        int n = L.o.g.Nx * L.o.g.Ny;
+        for (int c = tid; c < n; c += nt) prolong_at(L.o, N, L.x, (const V2*)N.x, c % L.o.g.Nx, c / L.o.g.Nx);
+        __syncthreads();
+        block_smooth(C, L, C.sweeps, false);
+    }
+}
+template <typename T>
+void launch_coarse_vcycle(const CoarseLevels<T>& C, const int* done, cudaStream_t s) {
+    k_coarse_vcycle<T><<<1, coarse_threads<T>(), 0, s>>>(C, done); count_launch();
 }
 
 #define NK_INSTANTIATE(T)                                                                                                   \
     template void launch_smooth_point<T>(const LevelView<T>&, const Vec2<T>::type*, Vec2<T>::type*, int, const int*, cudaStream_t); \
     template void launch_level_apply<T>(const LevelView<T>&, const Vec2<T>::type*, Vec2<T>::type*, int, const int*, cudaStream_t);  \
     template void launch_line_relax<T>(const LevelView<T>&, Vec2<T>::type*, int, const int*, cudaStream_t);                        \
-    template void launch_restrict<T>(const LevelView<T>&, const LevelView<T>&, const Vec2<T>::type*, Vec2<T>::type*, const int*,   \
-                                     cudaStream_t);                                                                                 \
+    template void launch_restrict<T>(const LevelView<T>&, const LevelView<T>&, const Vec2<T>::type*, Vec2<T>::type*, Vec2<T>::type*, \
+                                     const int*, cudaStream_t);                                                                     \
     template void launch_prolongate<T>(const LevelView<T>&, const LevelView<T>&, Vec2<T>::type*, const Vec2<T>::type*, const int*, \
                                        cudaStream_t);                                                                               \
-    template void launch_zero_vec<T>(const DevGrid<T>&, Vec2<T>::type*, const int*, cudaStream_t);
+    template void launch_zero_vec<T>(const DevGrid<T>&, Vec2<T>::type*, const int*, cudaStream_t);                                 \
+    template void launch_coarse_vcycle<T>(const CoarseLevels<T>&, const int*, cudaStream_t);
 
 NK_INSTANTIATE(double)
 NK_INSTANTIATE(float)

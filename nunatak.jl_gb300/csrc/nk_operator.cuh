@@ -154,3 +154,77 @@ __device__ __forceinline__ T y_line_coupling(const OpView<T>& o, int i, int j) {
 }
 
 }  // namespace nk
+
+namespace nk {
+
+// ---- tiled operator apply ------------------------------------------------------------------------------------
+// One BX x BY thread block computes q = A p for its BX x BY cells in three phases:
+//   1. the masked velocities (interior_u / interior_v) of the tile and a one-cell halo into shared memory;
+//   2. every centre stress Δy Txx, Δx Tyy and corner stress Txy the tile needs, once each, into shared memory
+//      (the per-cell form recomputes each of them two to three times);
+//   3. the divergence of the stresses plus the drag term for the thread's own cell.
+// Every thread of the block must call tiled_apply (it synchronises the block); `inside` tells whether the
+// thread's cell exists.
+template <typename T>
+struct ApplyTile {
+    typename Vec2<T>::type pm[BY + 2][BX + 2];   // masked p at (i0 - 1 + a, j0 - 1 + b) -> [b][a]
+    T sxx[BY + 1][BX + 1];                        // Δy Txx at centre (i0 - 1 + a, j0 - 1 + b)
+    T syy[BY + 1][BX + 1];                        // Δx Tyy at the same centres
+    T txy[BY + 1][BX + 1];                        // Txy at corner (i0 + a, j0 + b)
+};
+
+template <typename T, typename V2>
+__device__ __forceinline__ V2 tiled_apply(const OpView<T>& o, const V2* __restrict__ p, ApplyTile<T>& sm, int i0, int j0,
+                                          int i, int j, bool inside) {
+    const DevGrid<T>& g = o.g;
+    int tid = threadIdx.y * BX + threadIdx.x;
+    for (int t = tid; t < (BX + 2) * (BY + 2); t += BX * BY) {
+        int a = t % (BX + 2), b = t / (BX + 2);
+        int ii = i0 - 1 + a, jj = j0 - 1 + b;
+        V2 m;
+        m.x = T(0);
+        m.y = T(0);
+        if (ii <= g.Nx && jj <= g.Ny) {   // beyond index N nothing of the tile's cells is read (and wrap() covers one period)
+            m.x = masked_u(o, p, ii, jj);
+            m.y = masked_v(o, p, ii, jj);
+        }
+        sm.pm[b][a] = m;
+    }
+    __syncthreads();
+    for (int t = tid; t < (BX + 1) * (BY + 1); t += BX * BY) {
+        int a = t % (BX + 1), b = t / (BX + 1);
+        int ci = i0 - 1 + a, cj = j0 - 1 + b;   // centre
+        if (ci < g.Nx && cj < g.Ny) {
+            T exx = (sm.pm[b][a + 1].x - sm.pm[b][a].x) * g.rdxc[ci];
+            T eyy = (sm.pm[b + 1][a].y - sm.pm[b][a].y) * g.rdyc[cj];
+            T eta = o.coef[g.c_idx(ci, cj)].x;
+            sm.sxx[b][a] = g.dyc[cj] * (T(2) * eta * (T(2) * exx + eyy));
+            sm.syy[b][a] = g.dxc[ci] * (T(2) * eta * (T(2) * eyy + exx));
+        }
+        int fi = i0 + a, fj = j0 + b;           // corner
+        if (fi <= g.Nx && fj <= g.Ny) {
+            T dudy = (sm.pm[b + 1][a + 1].x - sm.pm[b][a + 1].x) * g.rdyf[fj];
+            T dvdx = (sm.pm[b + 1][a + 1].y - sm.pm[b + 1][a].y) * g.rdxf[fi];
+            T e = (dudy + dvdx) / T(2);
+            if (g.peripheral_ff(fi, fj)) e = o.wall_factor * e;
+            sm.txy[b][a] = T(2) * o.coef[g.ff_idx(fi, fj)].y * e;
+        }
+    }
+    __syncthreads();
+    V2 q;
+    q.x = T(0);
+    q.y = T(0);
+    if (!inside) return q;
+    int tx = threadIdx.x, ty = threadIdx.y;
+    int k = g.idx(i, j);
+    V2 pc = p[k];
+    uint8_t m = __ldg(o.mask + k);
+    auto c = o.coef[k];
+    T divu = (sm.sxx[ty + 1][tx + 1] - sm.sxx[ty + 1][tx]) + (g.dxf[i] * sm.txy[ty + 1][tx] - g.dxf[i] * sm.txy[ty][tx]);
+    T divv = (sm.syy[ty + 1][tx + 1] - sm.syy[ty][tx + 1]) + (g.dyf[j] * sm.txy[ty][tx + 1] - g.dyf[j] * sm.txy[ty][tx]);
+    q.x = (m & U_INACTIVE) ? pc.x : g.Az_fc(i, j) * c.z * pc.x - divu;
+    q.y = (m & V_INACTIVE) ? pc.y : g.Az_cf(i, j) * c.w * pc.y - divv;
+    return q;
+}
+
+}  // namespace nk

@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -21,6 +22,8 @@
 struct nk_context {
     int device = 0;
     std::string error;
+    cudaStream_t stream = nullptr;   // records the reference event
+    cudaEvent_t ref = nullptr;       // time origin of nk_solve_stats::device_start_ms / device_end_ms
 };
 
 namespace nk {
@@ -167,6 +170,11 @@ struct nk_problem {
     std::vector<Level<double>> lv64;           // FP64 hierarchy: [0] is the fine grid view
     std::vector<Level<float>> lv32;            // FP32 hierarchy (mixed): [0] is a float copy of the fine grid
     int nlevels = 0;                           // coarse levels below the fine grid
+    cudaGraph_t picard_graph = nullptr, linear_graph = nullptr;
+    cudaGraphExec_t picard_exec = nullptr, linear_exec = nullptr;
+    long long picard_kernels[3] = {0, 0, 0};   // kernel nodes: top level, Picard body, CG body
+    long long linear_kernels[2] = {0, 0};      // kernel nodes: top level, CG body
+    bool async_pending = false;                // nk_picard_solve_async issued, nk_problem_wait not yet called
 
     // ---- views ---------------------------------------------------------------------------------------------
     OpView<double> fine_op() const {
@@ -229,6 +237,10 @@ struct nk_problem {
         v.precond = precond;
         v.sc = sc;
         v.partials = partials;
+        v.cond = 0;
+        bool fused = mixed && precond == NK_PRECONDITIONER_MULTIGRID;
+        v.r32 = fused ? lv32[0].b : nullptr;
+        v.z32 = fused ? lv32[0].x : nullptr;
         return v;
     }
 };
@@ -296,7 +308,7 @@ static void upload_metrics(Level<T>& L, cudaStream_t s) {
 static double ipow(double x, int n) { double r = x; for (int m = 1; m < n; ++m) r *= x; return r; }
 static double power_integral(double zm, double zp, int p) { return (ipow(1 - zm, p + 1) - ipow(1 - zp, p + 1)) / (p + 1); }
 
-static void build(nk_problem* P) {
+static void build(nk_problem* P, bool dry = false) {
     const nk_grid_desc& gd = P->gd;
     P->Nx = gd.Nx; P->Ny = gd.Ny; P->Ns = gd.Nsigma;
     P->px = gd.topology_x == NK_PERIODIC; P->py = gd.topology_y == NK_PERIODIC;
@@ -403,6 +415,7 @@ static void build(nk_problem* P) {
             for (int l = 1; l <= P->nlevels; ++l) reserve_level(A, P->lv64[l], slots, true, true);
         }
     }
+    if (dry) return;   // sizing only: A.size is the device footprint
     NK_CUDA(cudaMalloc((void**)&A.base, A.size));
     NK_CUDA(cudaMemsetAsync(A.base, 0, A.size, P->stream));
     for (auto& sl : slots) *sl.first = A.base + sl.second;
@@ -468,9 +481,45 @@ static void update_preconditioner(nk_problem* P) {
     NK_CHECK_LAUNCH();
 }
 
-// smooth!, multigrid_preconditioner.jl:165-174, leaving the result in L.x
+// Levels of at most `coarse_cells` cells run inside one thread block (k_coarse_vcycle), FP32 only: one SM's
+// FP64 rate is 1/152 of the chip's, so FP64 coarse levels always run as grid-wide kernels.  Tunable with
+// NK_COARSE_CELLS (default 0, off: measured on GB300, one SM is slower than grid-wide launches even for the
+// 32 x 32 coarsest level with its 20 sweeps).
+static int coarse_cells_limit() {
+    static int limit = [] {
+        const char* e = std::getenv("NK_COARSE_CELLS");
+        return e ? std::atoi(e) : 0;
+    }();
+    return limit;
+}
+
 template <typename T>
-static void smooth(nk_problem* P, Level<T>& L, int sweeps, bool first, const int* done) {
+static int fused_level(const std::vector<Level<T>>& lv, int nlevels) {
+    if (sizeof(T) == 8) return nlevels + 1;
+    for (int l = 0; l <= nlevels; ++l)
+        if ((long long)lv[l].Nx * lv[l].Ny <= coarse_cells_limit()) return l;
+    return nlevels + 1;
+}
+
+// CUDA graphs are the solve path.  NK_GRAPHS=0 issues the same kernel sequence from a host loop (steps in
+// batches, one read of the device stopping flag per batch): profilers cannot see inside graphs with
+// conditional nodes.
+static bool use_graphs() {
+    static bool on = [] {
+        const char* e = std::getenv("NK_GRAPHS");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
+// Buffer that receives the first of `sweeps` point sweeps started from zero, so that the last lands in L.x.
+template <typename T>
+static typename Vec2<T>::type* first_sweep_target(Level<T>& L, int sweeps) { return ((sweeps - 1) % 2 == 0) ? L.x : L.x2; }
+
+// smooth!, multigrid_preconditioner.jl:165-174, leaving the result in L.x.  `first`: x starts at zero;
+// `first_done`: the first sweep from zero was already written (by the restriction) into first_sweep_target.
+template <typename T>
+static void smooth(nk_problem* P, Level<T>& L, int sweeps, bool first, const int* done, bool first_done = false) {
     cudaStream_t s = P->stream;
     LevelView<T> v = P->level_view(L);
     if (sweeps <= 0) {
@@ -487,59 +536,95 @@ static void smooth(nk_problem* P, Level<T>& L, int sweeps, bool first, const int
     }
     using V2 = typename Vec2<T>::type;
     const V2* in = L.x;
-    if (!first && sweeps % 2 == 1) {   // an odd number of ping-pong sweeps starting from L.x would write L.x in place
+    int k0 = 0;
+    if (first && first_done) {
+        in = first_sweep_target(L, sweeps);
+        k0 = 1;
+    } else if (!first && sweeps % 2 == 1) {   // an odd number of ping-pong sweeps starting from L.x would write L.x in place
         cudaMemcpyAsync(L.x2, L.x, L.plane() * sizeof(V2), cudaMemcpyDeviceToDevice, s);
         in = L.x2;
     }
-    for (int k = 0; k < sweeps; ++k) {
+    for (int k = k0; k < sweeps; ++k) {
         V2* out = ((sweeps - 1 - k) % 2 == 0) ? L.x : L.x2;
         launch_smooth_point<T>(v, in, out, (first && k == 0) ? 1 : 0, done, s);
         in = out;
     }
 }
 
-// v_cycle!, multigrid_preconditioner.jl:144-163 (x ≈ A⁻¹ b from a zero guess on level l)
+// v_cycle!, multigrid_preconditioner.jl:144-163 (x ≈ A⁻¹ b from a zero guess on level l).  Levels from
+// `fused_level` down run in one k_coarse_vcycle launch; above it each phase is one grid-wide kernel, and the
+// restriction also performs the coarse level's first sweep from zero.
 template <typename T>
-static void v_cycle(nk_problem* P, std::vector<Level<T>>& lv, int l, const int* done) {
+static void v_cycle(nk_problem* P, std::vector<Level<T>>& lv, int l, const int* done, bool first_done = false) {
     cudaStream_t s = P->stream;
-    Level<T>& L = lv[l];
-    if (l == P->nlevels) {
-        smooth(P, L, P->sd.coarsest_sweeps, true, done);
+    int lc = fused_level(lv, P->nlevels);
+    if (l == lc) {
+        CoarseLevels<T> C{};
+        C.n = P->nlevels - l + 1;
+        if (C.n > MAX_COARSE_LEVELS) bad("too many coarse multigrid levels");
+        for (int k = 0; k < C.n; ++k) C.lv[k] = P->level_view(lv[l + k]);
+        C.sweeps = P->sd.smoothing_sweeps;
+        C.coarsest = P->sd.coarsest_sweeps;
+        C.line = P->sd.smoother == NK_SMOOTHER_LINE_JACOBI;
+        launch_coarse_vcycle<T>(C, done, s);
         return;
     }
-    smooth(P, L, P->sd.smoothing_sweeps, true, done);
+    Level<T>& L = lv[l];
+    if (l == P->nlevels) {
+        smooth(P, L, P->sd.coarsest_sweeps, true, done, first_done);
+        return;
+    }
+    smooth(P, L, P->sd.smoothing_sweeps, true, done, first_done);
     LevelView<T> v = P->level_view(L);
     launch_level_apply<T>(v, L.x, L.q, 1, done, s);
-    LevelView<T> c = P->level_view(lv[l + 1]);
-    // the restriction reads the residual in L.q through the fine mask
-    launch_restrict<T>(c, v, L.q, lv[l + 1].b, done, s);
-    v_cycle(P, lv, l + 1, done);
-    launch_prolongate<T>(v, c, L.x, lv[l + 1].x, done, s);
+    Level<T>& N = lv[l + 1];
+    LevelView<T> c = P->level_view(N);
+    bool fuse_first = (l + 1 != lc) && P->sd.smoother == NK_SMOOTHER_POINT_JACOBI;
+    int next_sweeps = (l + 1 == P->nlevels) ? P->sd.coarsest_sweeps : P->sd.smoothing_sweeps;
+    fuse_first = fuse_first && next_sweeps > 0;
+    launch_restrict<T>(c, v, L.q, N.b, fuse_first ? first_sweep_target(N, next_sweeps) : nullptr, done, s);
+    v_cycle(P, lv, l + 1, done, fuse_first);
+    launch_prolongate<T>(v, c, L.x, N.x, done, s);
     smooth(P, L, P->sd.smoothing_sweeps, false, done);
 }
 
-// z = M r with the configured preconditioner (inside conjugate gradients, predicated on `done`)
-static void precondition_mg(nk_problem* P, const int* done) {
+// z = M r with the multigrid preconditioner.  `fused`: inside conjugate gradients, where the FP32 copy of r
+// and the FP64 copy of the result are made by the CG kernels themselves (CGView::r32 / z32).
+static void precondition_mg(nk_problem* P, const int* done, bool fused = false) {
     cudaStream_t s = P->stream;
     if (!P->mixed) {
         v_cycle<double>(P, P->lv64, 0, done);
     } else {
-        launch_to_float(P->fine.g, P->r, P->lv32[0].b, done, s);
+        if (!fused) launch_to_float(P->fine.g, P->r, P->lv32[0].b, done, s);
         v_cycle<float>(P, P->lv32, 0, done);
-        launch_to_double(P->fine.g, P->lv32[0].x, P->z, done, s);
+        if (!fused) launch_to_double(P->fine.g, P->lv32[0].x, P->z, done, s);
     }
     NK_CHECK_LAUNCH();
 }
 
-// ---- conjugate gradients ----------------------------------------------------------------------------------------
-static void set_control(nk_problem* P, const nk_iteration_control& c) {
+// ---- conjugate gradients and Picard as CUDA graphs ------------------------------------------------------------
+// A whole solve is one graph launch.  Picard and conjugate gradients are conditional WHILE nodes whose
+// conditions the kernels set on the device (cudaGraphSetConditional) when they take the stopping decision,
+// so a solve needs no host round trip until it has finished:
+//
+//   picard_begin ─► WHILE(picard) { x⁻ = x ─► coefficient update ─► coarse coefficients ─► CG start
+//                                    ─► WHILE(cg) { apply ─► update ─► [V-cycle ─► dots] ─► xpby }
+//                                    ─► picard_end (Δ, X, stopping test) }
+static void set_control(nk_problem* P) {
     SolverScalars h{};
+    const nk_iteration_control& c = P->sd.linear;
     h.reltol = c.reltol;
     h.abstol = c.abstol;
     h.fixed = c.kind == NK_FIXED_ITERATIONS;
     h.iterations = c.iterations;
     h.maxiter = c.maxiter;
     h.flexible = (P->mixed && P->precond == NK_PRECONDITIONER_MULTIGRID) ? 1 : 0;
+    const nk_iteration_control& pc = P->sd.picard;
+    h.p_reltol = pc.reltol;
+    h.p_abstol = pc.abstol;
+    h.p_fixed = pc.kind == NK_FIXED_ITERATIONS;
+    h.p_iterations = pc.iterations;
+    h.p_maxiter = pc.maxiter;
     *P->sc_host = h;
     NK_CUDA(cudaMemcpyAsync(P->sc, P->sc_host, sizeof(SolverScalars), cudaMemcpyHostToDevice, P->stream));
 }
@@ -549,10 +634,21 @@ static void cg_step(nk_problem* P, const CGView& v) {
     launch_cg_apply(v, s);
     launch_cg_update(v, s);
     if (P->precond == NK_PRECONDITIONER_MULTIGRID) {
-        precondition_mg(P, &P->sc->done);
+        precondition_mg(P, &P->sc->done, true);
         launch_cg_dots_after_precondition(v, s);
     }
     launch_cg_xpby(v, s);
+}
+
+// conjugate_gradient!, conjugate_gradient.jl:306-312 (everything before the iteration loop)
+static void cg_start(nk_problem* P, const CGView& v) {
+    update_preconditioner(P);
+    launch_cg_init(v, P->stream);
+    if (P->precond == NK_PRECONDITIONER_MULTIGRID) {
+        precondition_mg(P, nullptr, true);
+        launch_cg_init_finish(v, P->stream);
+    }
+    NK_CHECK_LAUNCH();
 }
 
 static void read_scalars(nk_problem* P) {
@@ -560,44 +656,191 @@ static void read_scalars(nk_problem* P) {
     NK_CUDA(cudaStreamSynchronize(P->stream));
 }
 
-// conjugate_gradient!, conjugate_gradient.jl:299-341, on x (warm start) with right-hand side b
-static void cg_solve(nk_problem* P, const double2* b, nk_solve_stats* st) {
-    const nk_iteration_control& ctl = P->sd.linear;
-    set_control(P, ctl);
-    update_preconditioner(P);
-    CGView v = P->cg_view(b);
-    launch_cg_init(v, P->stream);
-    if (P->precond == NK_PRECONDITIONER_MULTIGRID) {
-        precondition_mg(P, nullptr);
-        launch_cg_init_finish(v, P->stream);
+static std::vector<cudaGraphNode_t> leaves(cudaGraph_t g) {
+    size_t n = 0;
+    NK_CUDA(cudaGraphGetNodes(g, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n), out;
+    if (n) NK_CUDA(cudaGraphGetNodes(g, nodes.data(), &n));
+    for (cudaGraphNode_t node : nodes) {
+        size_t d = 0;
+        NK_CUDA(cudaGraphNodeGetDependentNodes(node, nullptr, nullptr, &d));
+        if (d == 0) out.push_back(node);
     }
-    NK_CHECK_LAUNCH();
+    return out;
+}
+
+template <typename F>
+static void capture_into(nk_problem* P, cudaGraph_t g, const std::vector<cudaGraphNode_t>& deps, F&& body) {
+    NK_CUDA(cudaStreamBeginCaptureToGraph(P->stream, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(),
+                                          cudaStreamCaptureModeThreadLocal));
+    set_capturing(true);
+    try {
+        body();
+    } catch (...) {
+        set_capturing(false);
+        cudaGraph_t dropped;
+        cudaStreamEndCapture(P->stream, &dropped);
+        throw;
+    }
+    set_capturing(false);
+    cudaGraph_t captured;
+    NK_CUDA(cudaStreamEndCapture(P->stream, &captured));
+}
+
+static long long kernel_nodes(cudaGraph_t g) {
+    size_t n = 0;
+    NK_CUDA(cudaGraphGetNodes(g, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (n) NK_CUDA(cudaGraphGetNodes(g, nodes.data(), &n));
+    long long k = 0;
+    for (cudaGraphNode_t node : nodes) {
+        cudaGraphNodeType t;
+        NK_CUDA(cudaGraphNodeGetType(node, &t));
+        if (t == cudaGraphNodeTypeKernel) ++k;
+    }
+    return k;
+}
+
+static cudaGraph_t add_while(cudaGraph_t g, const std::vector<cudaGraphNode_t>& deps, cudaGraphConditionalHandle h) {
+    cudaGraphNodeParams params = {};
+    params.type = cudaGraphNodeTypeConditional;
+    params.conditional.handle = h;
+    params.conditional.type = cudaGraphCondTypeWhile;
+    params.conditional.size = 1;
+    cudaGraphNode_t node;
+    NK_CUDA(cudaGraphAddNode(&node, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(), &params));
+    return params.conditional.phGraph_out[0];
+}
+
+// update_stress_balance_coefficients! / update_diva_coefficients!
+static void update_coefficients(nk_problem* P);
+
+static void build_picard_graph(nk_problem* P) {
+    cudaGraph_t g;
+    NK_CUDA(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle hp;
+    NK_CUDA(cudaGraphConditionalHandleCreate(&hp, g, 0, 0));
+    capture_into(P, g, {}, [&] { launch_picard_begin(P->sc, hp, P->stream); });
+    cudaGraph_t body = add_while(g, leaves(g), hp);
+    cudaGraphConditionalHandle hc;
+    NK_CUDA(cudaGraphConditionalHandleCreate(&hc, body, 0, 0));
+    CGView v = P->cg_view(P->tau);
+    v.cond = hc;
+    capture_into(P, body, {}, [&] {
+        launch_copy_range(P->fine.g, P->xprev, P->x, P->stream);
+        update_coefficients(P);
+        cg_start(P, v);
+    });
+    cudaGraph_t cg_body = add_while(body, leaves(body), hc);
+    capture_into(P, cg_body, {}, [&] { cg_step(P, v); });
+    capture_into(P, body, leaves(body), [&] { launch_picard_end(P->fine.g, P->xprev, P->x, P->sc, P->partials, hp, P->stream); });
+    P->picard_kernels[0] = kernel_nodes(g);
+    P->picard_kernels[1] = kernel_nodes(body);
+    P->picard_kernels[2] = kernel_nodes(cg_body);
+    NK_CUDA(cudaGraphInstantiate(&P->picard_exec, g, 0));
+    P->picard_graph = g;
+}
+
+static void build_linear_graph(nk_problem* P) {
+    cudaGraph_t g;
+    NK_CUDA(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle hc;
+    NK_CUDA(cudaGraphConditionalHandleCreate(&hc, g, 0, 0));
+    CGView v = P->cg_view(P->tmp_b);
+    v.cond = hc;
+    capture_into(P, g, {}, [&] { cg_start(P, v); });
+    cudaGraph_t cg_body = add_while(g, leaves(g), hc);
+    capture_into(P, cg_body, {}, [&] { cg_step(P, v); });
+    P->linear_kernels[0] = kernel_nodes(g);
+    P->linear_kernels[1] = kernel_nodes(cg_body);
+    NK_CUDA(cudaGraphInstantiate(&P->linear_exec, g, 0));
+    P->linear_graph = g;
+}
+
+static void fill_stats_from(const SolverScalars& h, nk_solve_stats* st, bool picard) {
+    st->linear_iterations_last = h.it;
+    st->linear_iterations_total = picard ? h.it_total : h.it;
+    st->residual_norm = h.rnorm;
+    st->initial_residual_norm = h.r0;
+    st->picard_iterations = picard ? h.p_it : 0;
+    st->picard_change = picard ? h.p_D : 0.0;
+    st->picard_norm = picard ? h.p_X : 0.0;
+    st->status = NK_OK;
+    if (h.status == NK_NONFINITE) st->status = NK_NONFINITE;
+    else if (picard && !h.p_fixed && !(h.p_D <= std::max(h.p_reltol * h.p_X, h.p_abstol))) st->status = NK_NOT_CONVERGED;
+    else if (!h.fixed && !(h.rnorm <= h.tol)) st->status = NK_NOT_CONVERGED;
+    else if (h.status == NK_BREAKDOWN) st->status = NK_BREAKDOWN;
+}
+
+static void fill_stats(nk_problem* P, nk_solve_stats* st, bool picard) { fill_stats_from(*P->sc_host, st, picard); }
+
+// The same solve issued from the host (NK_GRAPHS=0): CG steps in growing batches, the device `done` flag read
+// after each batch; Picard reads its stopping decision after every iteration.
+static void host_cg(nk_problem* P, const double2* b) {
+    CGView v = P->cg_view(b);
+    cg_start(P, v);
+    const nk_iteration_control& ctl = P->sd.linear;
     int limit = ctl.kind == NK_FIXED_ITERATIONS ? ctl.iterations : ctl.maxiter;
-    int issued = 0;
-    int batch = 4;
+    int issued = 0, batch = 4;
     while (issued < limit) {
         int n = std::min(batch, limit - issued);
         for (int k = 0; k < n; ++k) cg_step(P, v);
         NK_CHECK_LAUNCH();
         issued += n;
-        if (ctl.kind == NK_FIXED_ITERATIONS) continue;
         read_scalars(P);
         if (P->sc_host->done) break;
         batch = std::min(batch * 2, 64);
     }
+}
+
+static void host_picard(nk_problem* P) {
+    launch_picard_begin(P->sc, 0, P->stream);
     read_scalars(P);
-    const SolverScalars& h = *P->sc_host;
-    if (st) {
-        st->linear_iterations_last = h.it;
-        st->linear_iterations_total += h.it;
-        st->residual_norm = h.rnorm;
-        st->initial_residual_norm = h.r0;
-        if (h.status == NK_NONFINITE) st->status = NK_NONFINITE;
-        else if (ctl.kind == NK_CONVERGENCE && h.rnorm > h.tol && st->status == NK_OK) st->status = NK_NOT_CONVERGED;
+    while (!P->sc_host->p_done) {
+        launch_copy_range(P->fine.g, P->xprev, P->x, P->stream);
+        update_coefficients(P);
+        host_cg(P, P->tau);
+        launch_picard_end(P->fine.g, P->xprev, P->x, P->sc, P->partials, 0, P->stream);
+        NK_CHECK_LAUNCH();
+        read_scalars(P);
     }
 }
 
-// update_stress_balance_coefficients! / update_diva_coefficients!
+// solve!(x, solver, b, ...) with b already on the device in tmp_b
+static void linear_solve(nk_problem* P, nk_solve_stats* st) {
+    if (!use_graphs()) {
+        set_control(P);
+        host_cg(P, P->tmp_b);
+        read_scalars(P);
+        fill_stats(P, st, false);
+        return;
+    }
+    if (!P->linear_exec) build_linear_graph(P);
+    set_control(P);
+    NK_CUDA(cudaGraphLaunch(P->linear_exec, P->stream));
+    read_scalars(P);
+    fill_stats(P, st, false);
+    count_launches(P->linear_kernels[0] + (long long)P->sc_host->it * P->linear_kernels[1]);
+}
+
+// picard_solve!, picard.jl:63-90
+static void picard_solve(nk_problem* P, nk_solve_stats* st) {
+    if (!use_graphs()) {
+        set_control(P);
+        host_picard(P);
+        read_scalars(P);
+        fill_stats(P, st, true);
+        return;
+    }
+    if (!P->picard_exec) build_picard_graph(P);
+    set_control(P);
+    NK_CUDA(cudaGraphLaunch(P->picard_exec, P->stream));
+    read_scalars(P);
+    fill_stats(P, st, true);
+    const SolverScalars& h = *P->sc_host;
+    count_launches(P->picard_kernels[0] + (long long)h.p_it * P->picard_kernels[1] + (long long)h.it_total * P->picard_kernels[2]);
+}
+
 static void update_coefficients(nk_problem* P) {
     cudaStream_t s = P->stream;
     PhysView ph = P->phys();
@@ -614,38 +857,6 @@ static void update_coefficients(nk_problem* P) {
     }
     NK_CHECK_LAUNCH();
     prepare_operator(P);
-}
-
-// picard_solve!, picard.jl:63-90
-static void picard_solve(nk_problem* P, nk_solve_stats* st) {
-    const nk_iteration_control& ctl = P->sd.picard;
-    std::memset(st, 0, sizeof(*st));
-    int it = 0;
-    if (ctl.kind == NK_FIXED_ITERATIONS) {
-        for (int k = 0; k < ctl.iterations; ++k) {
-            update_coefficients(P);
-            cg_solve(P, P->tau, st);
-        }
-        it = ctl.iterations;
-    } else {
-        double D = INFINITY, X = 0.0;
-        while (D > std::max(ctl.reltol * X, ctl.abstol) && it < ctl.maxiter) {
-            launch_copy_range(P->fine.g, P->xprev, P->x, P->stream);
-            update_coefficients(P);
-            cg_solve(P, P->tau, st);
-            launch_picard_delta(P->fine.g, P->xprev, P->x, P->sc, P->partials, P->stream);
-            NK_CHECK_LAUNCH();
-            read_scalars(P);
-            D = std::sqrt(P->sc_host->picard_dd);
-            X = std::sqrt(P->sc_host->picard_xx);
-            ++it;
-            if (!std::isfinite(D)) { st->status = NK_NONFINITE; break; }
-        }
-        st->picard_change = D;
-        st->picard_norm = X;
-        if (st->status == NK_OK && D > std::max(ctl.reltol * X, ctl.abstol)) st->status = NK_NOT_CONVERGED;
-    }
-    st->picard_iterations = it;
 }
 
 // ---- fields in interior layout -----------------------------------------------------------------------------------
@@ -753,17 +964,30 @@ extern "C" {
 
 int32_t nk_api_version(void) { return NK_API_VERSION; }
 
+int64_t nk_launch_count(void) { return (int64_t)nk::launch_count(); }
+
 nk_status nk_context_create(int32_t device, nk_context** out) {
     if (!out) return NK_BAD_ARGUMENT;
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) return NK_CUDA_ERROR;
     auto* c = new nk_context();
     c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&c->ref) != cudaSuccess || cudaEventRecord(c->ref, c->stream) != cudaSuccess ||
+        cudaEventSynchronize(c->ref) != cudaSuccess) {
+        delete c;
+        return NK_CUDA_ERROR;
+    }
     *out = c;
     return NK_OK;
 }
 
 nk_status nk_context_destroy(nk_context* ctx) {
+    if (ctx) {
+        cudaSetDevice(ctx->device);
+        if (ctx->ref) cudaEventDestroy(ctx->ref);
+        if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    }
     delete ctx;
     return NK_OK;
 }
@@ -809,6 +1033,10 @@ nk_status nk_problem_destroy(nk_problem* P) {
     if (!P) return NK_OK;
     if (P->ctx) cudaSetDevice(P->ctx->device);
     if (P->stream) cudaStreamSynchronize(P->stream);
+    if (P->picard_exec) cudaGraphExecDestroy(P->picard_exec);
+    if (P->linear_exec) cudaGraphExecDestroy(P->linear_exec);
+    if (P->picard_graph) cudaGraphDestroy(P->picard_graph);
+    if (P->linear_graph) cudaGraphDestroy(P->linear_graph);
     if (P->arena.base) cudaFree(P->arena.base);
     if (P->sc_host) cudaFreeHost(P->sc_host);
     if (P->ev0) cudaEventDestroy(P->ev0);
@@ -919,6 +1147,17 @@ nk_status nk_precondition(nk_problem* P, const double* ru, const double* rv, dou
     });
 }
 
+// device_ms, device_start_ms, device_end_ms of the solve bracketed by ev0 and ev1 (both complete)
+static void event_times(nk_problem* P, nk_solve_stats* st) {
+    float ms = 0, a = 0, b = 0;
+    NK_CUDA(cudaEventElapsedTime(&ms, P->ev0, P->ev1));
+    NK_CUDA(cudaEventElapsedTime(&a, P->ctx->ref, P->ev0));
+    NK_CUDA(cudaEventElapsedTime(&b, P->ctx->ref, P->ev1));
+    st->device_ms = ms;
+    st->device_start_ms = a;
+    st->device_end_ms = b;
+}
+
 static nk_status linear_solve_impl(nk_problem* P, const double* bu, const double* bv, nk_solve_stats* stats) {
     return guarded(P->ctx, [&] {
         nk_solve_stats local{};
@@ -926,12 +1165,10 @@ static nk_status linear_solve_impl(nk_problem* P, const double* bu, const double
         std::memset(st, 0, sizeof(*st));
         vector_in(P, P->tmp_b, bu, bv);
         NK_CUDA(cudaEventRecord(P->ev0, P->stream));
-        cg_solve(P, P->tmp_b, st);
+        linear_solve(P, st);
         NK_CUDA(cudaEventRecord(P->ev1, P->stream));
         NK_CUDA(cudaEventSynchronize(P->ev1));
-        float ms = 0;
-        cudaEventElapsedTime(&ms, P->ev0, P->ev1);
-        st->device_ms = ms;
+        event_times(P, st);
         if (st->status == NK_NONFINITE) throw Failure{NK_NONFINITE, "non-finite residual"};
     });
 }
@@ -955,9 +1192,37 @@ nk_status nk_picard_solve(nk_problem* P, nk_solve_stats* stats) {
         picard_solve(P, st);
         NK_CUDA(cudaEventRecord(P->ev1, P->stream));
         NK_CUDA(cudaEventSynchronize(P->ev1));
-        float ms = 0;
-        cudaEventElapsedTime(&ms, P->ev0, P->ev1);
-        st->device_ms = ms;
+        event_times(P, st);
+        if (st->status == NK_NONFINITE) throw Failure{NK_NONFINITE, "non-finite velocity change"};
+    });
+}
+
+nk_status nk_picard_solve_async(nk_problem* P) {
+    if (!P) return NK_BAD_ARGUMENT;
+    return guarded(P->ctx, [&] {
+        if (!use_graphs()) bad("asynchronous solves need CUDA graphs (NK_GRAPHS=0 is set)");
+        if (!P->picard_exec) build_picard_graph(P);
+        set_control(P);
+        NK_CUDA(cudaEventRecord(P->ev0, P->stream));
+        NK_CUDA(cudaGraphLaunch(P->picard_exec, P->stream));
+        NK_CUDA(cudaMemcpyAsync(P->sc_host, P->sc, sizeof(SolverScalars), cudaMemcpyDeviceToHost, P->stream));
+        NK_CUDA(cudaEventRecord(P->ev1, P->stream));
+        P->async_pending = true;
+    });
+}
+
+nk_status nk_problem_wait(nk_problem* P, nk_solve_stats* stats) {
+    if (!P) return NK_BAD_ARGUMENT;
+    return guarded(P->ctx, [&] {
+        if (!P->async_pending) bad("no asynchronous solve pending");
+        NK_CUDA(cudaEventSynchronize(P->ev1));
+        P->async_pending = false;
+        nk_solve_stats local{};
+        nk_solve_stats* st = stats ? stats : &local;
+        fill_stats(P, st, true);
+        const SolverScalars& h = *P->sc_host;
+        count_launches(P->picard_kernels[0] + (long long)h.p_it * P->picard_kernels[1] + (long long)h.it_total * P->picard_kernels[2]);
+        event_times(P, st);
         if (st->status == NK_NONFINITE) throw Failure{NK_NONFINITE, "non-finite velocity change"};
     });
 }
@@ -1031,7 +1296,7 @@ static nk_status transfer(nk_problem* P, int32_t level, const double* au, const 
         if (restrict_) {
             in(fbuf, Lf.pitch, Lf.plane(), ffx, fny, fnx, ffy, au, av);
             NK_CUDA(cudaMemsetAsync(cbuf, 0, Lc.plane() * sizeof(double2), P->stream));
-            launch_restrict<double>(vc, vf, fbuf, cbuf, nullptr, P->stream);
+            launch_restrict<double>(vc, vf, fbuf, cbuf, nullptr, nullptr, P->stream);
             NK_CHECK_LAUNCH();
             out(cbuf, Lc.pitch, Lc.plane(), cfx, cny, cnx, cfy, bu, bv);
         } else {
@@ -1052,6 +1317,407 @@ nk_status nk_multigrid_restrict(nk_problem* P, int32_t level, const double* fine
 nk_status nk_multigrid_prolongate(nk_problem* P, int32_t level, const double* coarse_u, const double* coarse_v, double* fine_u, double* fine_v) {
     if (!P || !coarse_u || !coarse_v || !fine_u || !fine_v) return NK_BAD_ARGUMENT;
     return transfer(P, level, coarse_u, coarse_v, fine_u, fine_v, false);
+}
+
+nk_status nk_time_kernel(nk_problem* P, int32_t kernel, int32_t repeats, int64_t flush_bytes, double* mean_ms, double* bytes_per_launch) {
+    if (!P || !mean_ms || !bytes_per_launch || repeats < 1 || flush_bytes < 0) return NK_BAD_ARGUMENT;
+    return guarded(P->ctx, [&] {
+        cudaStream_t s = P->stream;
+        double cells = (double)P->Nx * P->Ny;
+        char* flush = nullptr;
+        if (flush_bytes > 0) NK_CUDA(cudaMalloc((void**)&flush, (size_t)flush_bytes));
+        double total = 0.0;
+        double bytes = 0.0;
+        auto launch = [&]() {
+            if (kernel == NK_KERNEL_OPERATOR_FP64) {
+                launch_apply(P->fine_op(), P->p, P->q, s);
+            } else if (kernel == NK_KERNEL_SMOOTHER) {
+                if (P->precond != NK_PRECONDITIONER_MULTIGRID) bad("the smoother needs the multigrid preconditioner");
+                if (P->mixed) {
+                    LevelView<float> v = P->level_view(P->lv32[0]);
+                    launch_smooth_point<float>(v, v.x, v.x2, 0, nullptr, s);
+                } else {
+                    LevelView<double> v = P->level_view(P->lv64[0]);
+                    launch_smooth_point<double>(v, v.x, v.x2, 0, nullptr, s);
+                }
+            } else if (kernel == NK_KERNEL_CG_UPDATE) {
+                CGView v = P->cg_view(P->tau);
+                launch_cg_update(v, s);
+            } else {
+                bad("unknown kernel id");
+            }
+        };
+        if (kernel == NK_KERNEL_OPERATOR_FP64) bytes = cells * (16 + 32 + 1 + 16);
+        else if (kernel == NK_KERNEL_SMOOTHER) bytes = cells * (P->mixed ? (8 + 8 + 8 + 16 + 1 + 8) : (16 + 16 + 16 + 32 + 1 + 16));
+        else bytes = cells * (64 + 32 + (P->precond == NK_PRECONDITIONER_DIAGONAL ? 16 + 16 : 0));
+        if (kernel == NK_KERNEL_CG_UPDATE) {
+            // run the update with done = 0 so it is not skipped
+            P->sc_host->done = 0;
+            NK_CUDA(cudaMemcpyAsync(&P->sc->done, &P->sc_host->done, sizeof(int), cudaMemcpyHostToDevice, s));
+        }
+        for (int rep = 0; rep < repeats; ++rep) {
+            if (flush) NK_CUDA(cudaMemsetAsync(flush, rep & 0xff, (size_t)flush_bytes, s));
+            NK_CUDA(cudaEventRecord(P->ev0, s));
+            launch();
+            NK_CUDA(cudaEventRecord(P->ev1, s));
+            NK_CUDA(cudaEventSynchronize(P->ev1));
+            NK_CHECK_LAUNCH();
+            float ms = 0;
+            NK_CUDA(cudaEventElapsedTime(&ms, P->ev0, P->ev1));
+            total += ms;
+        }
+        if (flush) cudaFree(flush);
+        *mean_ms = total / repeats;
+        *bytes_per_launch = bytes;
+    });
+}
+
+}  // extern "C"
+
+// =================================================================================================================
+// Serving: a request loop over resident problems, one stream per in-flight request.
+// =================================================================================================================
+#include <chrono>
+#include <deque>
+#include <thread>
+#include <unordered_map>
+
+namespace {
+
+struct ServerRequest {
+    int64_t ticket = 0;
+    nk_grid_desc grid{};
+    nk_physics_desc physics{};
+    nk_solver_desc solver{};
+    std::vector<double> xf, yf, sf, H, bed, C, A, u0, v0;
+    double* u_out = nullptr;
+    double* v_out = nullptr;
+    std::string key;
+    double t_submit = 0, t_admit = 0, t_done = 0;
+    nk_solve_stats stats{};
+    int state = 0;   // 0 queued, 1 on the device, 2 finished
+    nk_status status = NK_OK;
+};
+
+struct Resident {
+    nk_problem* P = nullptr;
+    std::string key;
+    bool busy = false;
+    int64_t ticket = 0;
+    size_t bytes = 0;
+    double last_used = 0;
+    double* pin = nullptr;          // pinned staging: H, bed, C, A, u0, v0 in; u, v out
+    size_t pin_count = 0;
+    SolverScalars* sc_out = nullptr; // pinned copy of the solver scalars at completion
+    cudaEvent_t done = nullptr;
+};
+
+void append_bytes(std::string& k, const void* p, size_t n) { k.append(reinterpret_cast<const char*>(p), n); }
+
+// Identity of a problem shape: grid (with face vectors), physics and solver, without pointers.
+std::string request_key(const ServerRequest& R) {
+    std::string k;
+    nk_grid_desc g = R.grid;
+    g.x_faces = g.y_faces = g.sigma_faces = nullptr;
+    append_bytes(k, &g, sizeof(g));
+    append_bytes(k, &R.physics, sizeof(R.physics));
+    append_bytes(k, &R.solver, sizeof(R.solver));
+    for (const auto* v : {&R.xf, &R.yf, &R.sf}) {
+        size_t n = v->size();
+        append_bytes(k, &n, sizeof(n));
+        if (n) append_bytes(k, v->data(), n * sizeof(double));
+    }
+    return k;
+}
+
+nk_grid_desc grid_with_vectors(ServerRequest& R) {
+    nk_grid_desc g = R.grid;
+    g.x_faces = R.xf.empty() ? nullptr : R.xf.data();
+    g.y_faces = R.yf.empty() ? nullptr : R.yf.data();
+    g.sigma_faces = R.sf.empty() ? nullptr : R.sf.data();
+    return g;
+}
+
+}  // namespace
+
+struct nk_server {
+    nk_context* ctx = nullptr;
+    nk_server_desc desc{};
+    std::chrono::steady_clock::time_point t0;
+    std::deque<int64_t> queue;
+    std::unordered_map<int64_t, std::unique_ptr<ServerRequest>> requests;
+    std::vector<std::unique_ptr<Resident>> residents;
+    int64_t next_ticket = 1;
+    int64_t device_bytes = 0;
+    int in_flight = 0, peak = 0;
+
+    double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+};
+
+namespace nk {
+
+static size_t problem_bytes(ServerRequest& R) {
+    nk_problem probe;
+    probe.gd = grid_with_vectors(R);
+    probe.pd = R.physics;
+    probe.sd = R.solver;
+    build(&probe, true);
+    return probe.arena.size;
+}
+
+static void destroy_resident(nk_server* S, size_t idx) {
+    Resident* r = S->residents[idx].get();
+    S->device_bytes -= (int64_t)r->bytes;
+    if (r->done) cudaEventDestroy(r->done);
+    if (r->pin) cudaFreeHost(r->pin);
+    if (r->sc_out) cudaFreeHost(r->sc_out);
+    nk_problem_destroy(r->P);
+    S->residents.erase(S->residents.begin() + idx);
+}
+
+// A resident problem for R: an idle one of the same shape, else a new one within the memory cap (evicting
+// idle problems of other shapes, least recently used first).  nullptr: wait for memory to free up.
+static Resident* acquire(nk_server* S, ServerRequest& R) {
+    for (auto& r : S->residents)
+        if (!r->busy && r->key == R.key) return r.get();
+    size_t need = problem_bytes(R);
+    while (S->device_bytes + (int64_t)need > S->desc.memory_cap_bytes) {
+        int victim = -1;
+        for (size_t i = 0; i < S->residents.size(); ++i)
+            if (!S->residents[i]->busy && (victim < 0 || S->residents[i]->last_used < S->residents[victim]->last_used)) victim = (int)i;
+        if (victim < 0) break;
+        destroy_resident(S, victim);
+    }
+    if (S->device_bytes + (int64_t)need > S->desc.memory_cap_bytes) {
+        if (S->in_flight > 0) return nullptr;
+        throw Failure{NK_OOM, "a request needs more device memory than memory_cap_bytes"};
+    }
+    auto r = std::make_unique<Resident>();
+    nk_grid_desc g = grid_with_vectors(R);
+    nk_status st = nk_problem_create(S->ctx, &g, &R.physics, &R.solver, &r->P);
+    if (st != NK_OK) throw Failure{st, S->ctx->error};
+    r->key = R.key;
+    r->bytes = r->P->arena.size;
+    nk_problem* P = r->P;
+    size_t cells = (size_t)P->Nx * P->Ny, faces = (size_t)(P->Nx + 1) * (P->Ny + 1);
+    r->pin_count = 4 * cells + 4 * faces;
+    NK_CUDA(cudaHostAlloc((void**)&r->pin, r->pin_count * sizeof(double), cudaHostAllocDefault));
+    NK_CUDA(cudaHostAlloc((void**)&r->sc_out, sizeof(SolverScalars), cudaHostAllocDefault));
+    NK_CUDA(cudaEventCreateWithFlags(&r->done, cudaEventDisableTiming));
+    if (use_graphs()) build_picard_graph(P);
+    S->device_bytes += (int64_t)r->bytes;
+    S->residents.push_back(std::move(r));
+    return S->residents.back().get();
+}
+
+// Stage the request's inputs and enqueue its whole solve on the resident problem's stream.
+static void start(nk_server* S, ServerRequest& R, Resident& r) {
+    nk_problem* P = r.P;
+    cudaStream_t s = P->stream;
+    size_t cells = (size_t)P->Nx * P->Ny;
+    FieldLoc fu = field_loc(P, NK_FIELD_U), fv = field_loc(P, NK_FIELD_V);
+    size_t nu = (size_t)fu.nx * fu.ny, nv = (size_t)fv.nx * fv.ny;
+    double* pin = r.pin;
+    auto stage = [&](int id, const std::vector<double>& src, double* at) {
+        FieldLoc f = field_loc(P, id);
+        std::memcpy(at, src.data(), src.size() * sizeof(double));
+        size_t n = (size_t)f.nx * f.ny * f.planes;
+        NK_CUDA(cudaMemcpyAsync(P->staging, at, n * sizeof(double), cudaMemcpyHostToDevice, s));
+        launch_pack(f.base, P->pitch, (int)P->plane, f.stride, f.offset, P->staging, f.nx, f.ny, f.planes, s);
+    };
+    stage(NK_FIELD_H, R.H, pin);
+    stage(NK_FIELD_BED, R.bed, pin + cells);
+    if (!R.C.empty()) stage(NK_FIELD_FRICTION_COEFFICIENT, R.C, pin + 2 * cells);
+    stage(NK_FIELD_RATE_FACTOR, R.A, pin + 3 * cells);
+    double* uin = pin + 4 * cells;
+    NK_CUDA(cudaMemsetAsync(P->x, 0, P->plane * sizeof(double2), s));
+    if (!R.u0.empty()) stage(NK_FIELD_U, R.u0, uin);
+    if (!R.v0.empty()) stage(NK_FIELD_V, R.v0, uin + nu);
+    GeometryView gv;
+    gv.g = P->fine.g;
+    gv.H = P->H; gv.bed = P->bed; gv.s = P->s; gv.N = P->N; gv.mu = P->mu; gv.phi = P->phi; gv.phi_uv = P->phi_uv; gv.tau = P->tau;
+    gv.rho_i = P->pd.ice_density; gv.rho_w = P->pd.ocean_density; gv.gacc = P->pd.gravitational_acceleration;
+    gv.grounding = P->pd.grounding; gv.gl_stress = P->pd.grounding_line_driving_stress; gv.use_mask = P->pd.use_ice_mask;
+    gv.mask_min = P->pd.mask_minimum_thickness; gv.mask_trans = P->pd.mask_transition_thickness;
+    launch_geometry(gv, s);
+    set_control(P);
+    if (use_graphs()) {
+        NK_CUDA(cudaGraphLaunch(P->picard_exec, s));
+    } else {
+        host_picard(P);
+    }
+    double* uout = uin + nu + nv;
+    launch_unpack(P->staging, (const double*)P->x, P->pitch, (int)P->plane, 2, 0, fu.nx, fu.ny, 1, s);
+    NK_CUDA(cudaMemcpyAsync(uout, P->staging, nu * sizeof(double), cudaMemcpyDeviceToHost, s));
+    launch_unpack(P->staging, (const double*)P->x, P->pitch, (int)P->plane, 2, 1, fv.nx, fv.ny, 1, s);
+    NK_CUDA(cudaMemcpyAsync(uout + nu, P->staging, nv * sizeof(double), cudaMemcpyDeviceToHost, s));
+    NK_CUDA(cudaMemcpyAsync(r.sc_out, P->sc, sizeof(SolverScalars), cudaMemcpyDeviceToHost, s));
+    NK_CUDA(cudaEventRecord(r.done, s));
+    NK_CHECK_LAUNCH();
+    r.busy = true;
+    r.ticket = R.ticket;
+    R.state = 1;
+    R.t_admit = S->now();
+    S->in_flight += 1;
+    S->peak = std::max(S->peak, S->in_flight);
+}
+
+static void finish(nk_server* S, Resident& r) {
+    ServerRequest& R = *S->requests.at(r.ticket);
+    nk_problem* P = r.P;
+    FieldLoc fu = field_loc(P, NK_FIELD_U), fv = field_loc(P, NK_FIELD_V);
+    size_t nu = (size_t)fu.nx * fu.ny, nv = (size_t)fv.nx * fv.ny;
+    size_t cells = (size_t)P->Nx * P->Ny;
+    const double* uout = r.pin + 4 * cells + nu + nv;
+    if (R.u_out) std::memcpy(R.u_out, uout, nu * sizeof(double));
+    if (R.v_out) std::memcpy(R.v_out, uout + nu, nv * sizeof(double));
+    fill_stats_from(*r.sc_out, &R.stats, true);
+    const SolverScalars& h = *r.sc_out;
+    if (use_graphs())
+        count_launches(P->picard_kernels[0] + (long long)h.p_it * P->picard_kernels[1] + (long long)h.it_total * P->picard_kernels[2]);
+    R.status = R.stats.status == NK_NONFINITE ? NK_NONFINITE : NK_OK;
+    R.state = 2;
+    R.t_done = S->now();
+    r.busy = false;
+    r.last_used = R.t_done;
+    S->in_flight -= 1;
+}
+
+static void progress(nk_server* S) {
+    for (auto& r : S->residents) {
+        if (!r->busy) continue;
+        cudaError_t e = cudaEventQuery(r->done);
+        if (e == cudaSuccess) finish(S, *r);
+        else if (e != cudaErrorNotReady) NK_CUDA(e);
+    }
+    while (!S->queue.empty() && S->in_flight < S->desc.max_in_flight) {
+        ServerRequest& R = *S->requests.at(S->queue.front());
+        Resident* r = nullptr;
+        try {
+            r = acquire(S, R);
+        } catch (const Failure& f) {
+            R.status = f.status;
+            R.state = 2;
+            R.t_done = S->now();
+            S->queue.pop_front();
+            continue;
+        }
+        if (!r) break;   // wait for memory
+        S->queue.pop_front();
+        start(S, R, *r);
+    }
+}
+
+}  // namespace nk
+
+extern "C" {
+
+nk_status nk_server_create(nk_context* ctx, const nk_server_desc* desc, nk_server** out) {
+    if (!ctx || !desc || !out || desc->max_in_flight < 1 || desc->memory_cap_bytes <= 0) return NK_BAD_ARGUMENT;
+    auto* S = new nk_server();
+    S->ctx = ctx;
+    S->desc = *desc;
+    S->t0 = std::chrono::steady_clock::now();
+    *out = S;
+    return NK_OK;
+}
+
+nk_status nk_server_destroy(nk_server* S) {
+    if (!S) return NK_OK;
+    guarded(S->ctx, [&] {
+        for (auto& r : S->residents)
+            if (r->busy) cudaEventSynchronize(r->done);
+        while (!S->residents.empty()) destroy_resident(S, S->residents.size() - 1);
+    });
+    delete S;
+    return NK_OK;
+}
+
+double nk_server_clock(const nk_server* S) { return S ? S->now() : 0.0; }
+
+nk_status nk_server_submit(nk_server* S, const nk_request* q, int64_t* ticket) {
+    if (!S || !q || !ticket || !q->H || !q->bed || !q->rate_factor) return NK_BAD_ARGUMENT;
+    return guarded(S->ctx, [&] {
+        if (q->physics.rate_factor_layout != NK_RATE_FACTOR_2D) bad("served requests take a 2-D rate factor");
+        if (q->grid.Nx < 1 || q->grid.Ny < 1) bad("empty grid");
+        auto R = std::make_unique<ServerRequest>();
+        R->grid = q->grid;
+        R->physics = q->physics;
+        R->solver = q->solver;
+        int Nx = q->grid.Nx, Ny = q->grid.Ny;
+        if (q->grid.x_faces) R->xf.assign(q->grid.x_faces, q->grid.x_faces + Nx + 1);
+        if (q->grid.y_faces) R->yf.assign(q->grid.y_faces, q->grid.y_faces + Ny + 1);
+        if (q->grid.sigma_faces) R->sf.assign(q->grid.sigma_faces, q->grid.sigma_faces + q->grid.Nsigma + 1);
+        size_t cells = (size_t)Nx * Ny;
+        int nfx = q->grid.topology_x == NK_PERIODIC ? Nx : Nx + 1, nfy = q->grid.topology_y == NK_PERIODIC ? Ny : Ny + 1;
+        R->H.assign(q->H, q->H + cells);
+        R->bed.assign(q->bed, q->bed + cells);
+        if (q->friction_coefficient) R->C.assign(q->friction_coefficient, q->friction_coefficient + cells);
+        R->A.assign(q->rate_factor, q->rate_factor + cells);
+        if (q->u_init) R->u0.assign(q->u_init, q->u_init + (size_t)nfx * Ny);
+        if (q->v_init) R->v0.assign(q->v_init, q->v_init + (size_t)Nx * nfy);
+        R->u_out = q->u_out;
+        R->v_out = q->v_out;
+        R->key = request_key(*R);
+        R->ticket = S->next_ticket++;
+        R->t_submit = S->now();
+        *ticket = R->ticket;
+        S->queue.push_back(R->ticket);
+        S->requests[R->ticket] = std::move(R);
+        progress(S);
+    });
+}
+
+nk_status nk_server_progress(nk_server* S, int32_t* pending) {
+    if (!S) return NK_BAD_ARGUMENT;
+    return guarded(S->ctx, [&] {
+        progress(S);
+        if (pending) {
+            int32_t n = 0;
+            for (auto& kv : S->requests) n += kv.second->state != 2;
+            *pending = n;
+        }
+    });
+}
+
+nk_status nk_server_wait(nk_server* S, int64_t ticket, nk_solve_stats* stats, double* t_submit, double* t_admit, double* t_done) {
+    if (!S) return NK_BAD_ARGUMENT;
+    auto it = S->requests.find(ticket);
+    if (it == S->requests.end()) return NK_BAD_ARGUMENT;
+    nk_status st = guarded(S->ctx, [&] {
+        while (it->second->state != 2) {
+            progress(S);
+            if (it->second->state != 2) std::this_thread::sleep_for(std::chrono::microseconds(20));
+        }
+    });
+    if (st != NK_OK) return st;
+    ServerRequest& R = *it->second;
+    if (stats) *stats = R.stats;
+    if (t_submit) *t_submit = R.t_submit;
+    if (t_admit) *t_admit = R.t_admit;
+    if (t_done) *t_done = R.t_done;
+    return R.status;
+}
+
+nk_status nk_server_wait_all(nk_server* S) {
+    if (!S) return NK_BAD_ARGUMENT;
+    return guarded(S->ctx, [&] {
+        while (true) {
+            progress(S);
+            bool all = true;
+            for (auto& kv : S->requests) all = all && kv.second->state == 2;
+            if (all) break;
+            std::this_thread::sleep_for(std::chrono::microseconds(20));
+        }
+    });
+}
+
+nk_status nk_server_info(const nk_server* S, int32_t* resident, int64_t* device_bytes, int32_t* peak_in_flight) {
+    if (!S) return NK_BAD_ARGUMENT;
+    if (resident) *resident = (int32_t)S->residents.size();
+    if (device_bytes) *device_bytes = S->device_bytes;
+    if (peak_in_flight) *peak_in_flight = S->peak;
+    return NK_OK;
 }
 
 }  // extern "C"

@@ -10,11 +10,19 @@
 // on the device, so no step needs a host synchronisation.  Every kernel of a step first reads the
 // device `done` flag and returns when the solve has stopped, so steps can be launched in batches (or
 // replayed from a CUDA graph) past convergence at the cost of empty launches.
+#include <atomic>
 #include <cmath>
 
 #include "nk_kernels.cuh"
 
 namespace nk {
+
+static std::atomic<long long> g_launches{0};
+static thread_local bool g_capturing = false;   // launches recorded into a graph are counted when the graph runs
+void count_launch() { if (!g_capturing) g_launches.fetch_add(1, std::memory_order_relaxed); }
+void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+void set_capturing(bool on) { g_capturing = on; }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 // ---- layout conversion --------------------------------------------------------------------------------
 __global__ void k_pack(double* dst, int pitch, int plane, int stride, int offset, const double* __restrict__ src, int nx, int ny,
@@ -50,25 +58,28 @@ static int blocks_for(long long n) {
 
 void launch_pack(double* dst, int pitch, int plane, int stride, int offset, const double* src, int nx, int ny, int planes,
                  cudaStream_t s) {
-    k_pack<<<blocks_for((long long)nx * ny * planes), 256, 0, s>>>(dst, pitch, plane, stride, offset, src, nx, ny, planes);
+    k_pack<<<blocks_for((long long)nx * ny * planes), 256, 0, s>>>(dst, pitch, plane, stride, offset, src, nx, ny, planes); count_launch();
 }
 void launch_unpack(double* dst, const double* src, int pitch, int plane, int stride, int offset, int nx, int ny, int planes,
                    cudaStream_t s) {
-    k_unpack<<<blocks_for((long long)nx * ny * planes), 256, 0, s>>>(dst, src, pitch, plane, stride, offset, nx, ny, planes);
+    k_unpack<<<blocks_for((long long)nx * ny * planes), 256, 0, s>>>(dst, src, pitch, plane, stride, offset, nx, ny, planes); count_launch();
 }
 void launch_fill(double* dst, int count, double value, cudaStream_t s) {
-    k_fill<<<blocks_for(count), 256, 0, s>>>(dst, count, value);
+    k_fill<<<blocks_for(count), 256, 0, s>>>(dst, count, value); count_launch();
 }
 
 // ---- operator, masks, diagonals ---------------------------------------------------------------------------
 __global__ void k_apply(OpView<double> o, const double2* __restrict__ p, double2* __restrict__ q) {
-    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
-    if (i >= o.g.Nx || j >= o.g.Ny) return;
-    q[o.g.idx(i, j)] = apply_at(o, p, i, j);
+    __shared__ ApplyTile<double> sm;
+    int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY;
+    int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+    bool inside = i < o.g.Nx && j < o.g.Ny;
+    double2 a = tiled_apply(o, p, sm, i0, j0, i, j, inside);
+    if (inside) q[o.g.idx(i, j)] = a;
 }
 void launch_apply(const OpView<double>& o, const double2* p, double2* q, cudaStream_t s) {
     LaunchDims d = dims2d(o.g.Nx, o.g.Ny);
-    k_apply<<<d.grid, d.block, 0, s>>>(o, p, q);
+    k_apply<<<d.grid, d.block, 0, s>>>(o, p, q); count_launch();
 }
 
 // inactiveᶠᶜᶜ / inactiveᶜᶠᶜ with η̄H (ssa_operator.jl:91-92, smooth_ice_mask.jl:429-430) and the wall bits
@@ -90,7 +101,7 @@ __global__ void k_mask(OpView<T> o, uint8_t* mask) {
 template <typename T>
 void launch_mask(const OpView<T>& o, uint8_t* mask, cudaStream_t s) {
     LaunchDims d = dims2d(o.g.Nx + 1, o.g.Ny + 1);
-    k_mask<T><<<d.grid, d.block, 0, s>>>(o, mask);
+    k_mask<T><<<d.grid, d.block, 0, s>>>(o, mask); count_launch();
 }
 template void launch_mask<double>(const OpView<double>&, uint8_t*, cudaStream_t);
 template void launch_mask<float>(const OpView<float>&, uint8_t*, cudaStream_t);
@@ -103,7 +114,7 @@ __global__ void k_inverse_diagonal(OpView<double> o, double2* invd) {
 }
 void launch_inverse_diagonal(const OpView<double>& o, double2* invd, cudaStream_t s) {
     LaunchDims d = dims2d(o.g.Nx, o.g.Ny);
-    k_inverse_diagonal<<<d.grid, d.block, 0, s>>>(o, invd);
+    k_inverse_diagonal<<<d.grid, d.block, 0, s>>>(o, invd); count_launch();
 }
 
 template <typename T>
@@ -119,7 +130,7 @@ __global__ void k_inverse_row_sum(OpView<T> o, typename Vec2<T>::type* irs) {
 template <typename T>
 void launch_inverse_row_sum(const OpView<T>& o, typename Vec2<T>::type* irs, cudaStream_t s) {
     LaunchDims d = dims2d(o.g.Nx, o.g.Ny);
-    k_inverse_row_sum<T><<<d.grid, d.block, 0, s>>>(o, irs);
+    k_inverse_row_sum<T><<<d.grid, d.block, 0, s>>>(o, irs); count_launch();
 }
 template void launch_inverse_row_sum<double>(const OpView<double>&, double2*, cudaStream_t);
 template void launch_inverse_row_sum<float>(const OpView<float>&, float2*, cudaStream_t);
@@ -135,14 +146,18 @@ __device__ __forceinline__ int stop_after(const SolverScalars* sc, double rnorm,
 
 // conjugate_gradient!, conjugate_gradient.jl:306-312: r = b - A x, z = M r, p = z, rho = r.z
 __global__ void k_cg_init(CGView v) {
-    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    __shared__ ApplyTile<double> sm;
+    int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY;
+    int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+    bool inside = i < v.o.g.Nx && j < v.o.g.Ny;
+    double2 q = tiled_apply(v.o, (const double2*)v.x, sm, i0, j0, i, j, inside);
     double rz = 0.0, rr = 0.0;
-    if (i < v.o.g.Nx && j < v.o.g.Ny) {
+    if (inside) {
         int k = v.o.g.idx(i, j);
-        double2 q = apply_at(v.o, (const double2*)v.x, i, j);
         double2 b = v.b[k];
         double2 r = make_double2(b.x - q.x, b.y - q.y);
         v.r[k] = r;
+        if (v.r32) v.r32[k] = make_float2((float)r.x, (float)r.y);
         rr = r.x * r.x + r.y * r.y;
         if (v.precond != NK_PRECONDITIONER_MULTIGRID) {
             double2 z = r;
@@ -170,11 +185,12 @@ __global__ void k_cg_init(CGView v) {
         if (!isfinite(r0)) done = 1;
         sc->done = done;
         sc->done_next = done;
+        if (v.cond && v.precond != NK_PRECONDITIONER_MULTIGRID) cudaGraphSetConditional(v.cond, done ? 0u : 1u);
     }
 }
 void launch_cg_init(const CGView& v, cudaStream_t s) {
     LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
-    k_cg_init<<<d.grid, d.block, 0, s>>>(v);
+    k_cg_init<<<d.grid, d.block, 0, s>>>(v); count_launch();
 }
 
 // multigrid start: p = z, rho = r.z (and z_old = z for flexible conjugate gradients)
@@ -183,27 +199,40 @@ __global__ void k_cg_init_finish(CGView v) {
     double rz = 0.0;
     if (i < v.o.g.Nx && j < v.o.g.Ny) {
         int k = v.o.g.idx(i, j);
-        double2 z = v.z[k], r = v.r[k];
+        double2 z, r = v.r[k];
+        if (v.z32) {
+            float2 f = v.z32[k];
+            z = make_double2((double)f.x, (double)f.y);
+            v.z[k] = z;
+        } else {
+            z = v.z[k];
+        }
         v.p[k] = z;
         if (v.zold) v.zold[k] = z;
         rz = r.x * z.x + r.y * z.y;
     }
     double trz, dummy;
-    if (grid_sum2(rz, 0.0, v.partials, &v.sc->ticket, trz, dummy) && threadIdx.x == 0 && threadIdx.y == 0) v.sc->rho = trz;
+    if (grid_sum2(rz, 0.0, v.partials, &v.sc->ticket, trz, dummy) && threadIdx.x == 0 && threadIdx.y == 0) {
+        v.sc->rho = trz;
+        if (v.cond) cudaGraphSetConditional(v.cond, v.sc->done ? 0u : 1u);
+    }
 }
 void launch_cg_init_finish(const CGView& v, cudaStream_t s) {
     LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
-    k_cg_init_finish<<<d.grid, d.block, 0, s>>>(v);
+    k_cg_init_finish<<<d.grid, d.block, 0, s>>>(v); count_launch();
 }
 
 // conjugate_gradient_step!, conjugate_gradient.jl:350-353: q = A p, alpha = rho / p.q (0 if p.q = 0)
 __global__ void k_cg_apply(CGView v) {
     if (read_done(v.sc)) return;
-    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    __shared__ ApplyTile<double> sm;
+    int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY;
+    int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+    bool inside = i < v.o.g.Nx && j < v.o.g.Ny;
+    double2 q = tiled_apply(v.o, (const double2*)v.p, sm, i0, j0, i, j, inside);
     double pq = 0.0;
-    if (i < v.o.g.Nx && j < v.o.g.Ny) {
+    if (inside) {
         int k = v.o.g.idx(i, j);
-        double2 q = apply_at(v.o, (const double2*)v.p, i, j);
         v.q[k] = q;
         double2 p = v.p[k];
         pq = p.x * q.x + p.y * q.y;
@@ -218,7 +247,7 @@ __global__ void k_cg_apply(CGView v) {
 }
 void launch_cg_apply(const CGView& v, cudaStream_t s) {
     LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
-    k_cg_apply<<<d.grid, d.block, 0, s>>>(v);
+    k_cg_apply<<<d.grid, d.block, 0, s>>>(v); count_launch();
 }
 
 // conjugate_gradient_step!, :355-360 and the stopping test of :334-338
@@ -236,6 +265,7 @@ __global__ void k_cg_update(CGView v) {
         r.y = r.y + (-alpha) * q.y;
         v.x[k] = x;
         v.r[k] = r;
+        if (v.r32) v.r32[k] = make_float2((float)r.x, (float)r.y);
         rr = r.x * r.x + r.y * r.y;
         if (v.precond != NK_PRECONDITIONER_MULTIGRID) {
             double2 z = r;
@@ -261,12 +291,14 @@ __global__ void k_cg_update(CGView v) {
             sc->rho = trz;
         }
         if (!isfinite(rn)) sc->status = NK_NONFINITE;
-        sc->done_next = stop_after(sc, rn, it);
+        int stop = stop_after(sc, rn, it);
+        sc->done_next = stop;
+        if (stop && !sc->fixed && !(rn <= sc->tol)) sc->cg_unconverged += 1;
     }
 }
 void launch_cg_update(const CGView& v, cudaStream_t s) {
     LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
-    k_cg_update<<<d.grid, d.block, 0, s>>>(v);
+    k_cg_update<<<d.grid, d.block, 0, s>>>(v); count_launch();
 }
 
 // after z = V-cycle(r): rho_new = r.z; beta = rho_new / rho, or the flexible (Polak-Ribière) form
@@ -277,7 +309,14 @@ __global__ void k_cg_dots_after_precondition(CGView v) {
     double rz = 0.0, rzo = 0.0;
     if (i < v.o.g.Nx && j < v.o.g.Ny) {
         int k = v.o.g.idx(i, j);
-        double2 r = v.r[k], z = v.z[k];
+        double2 r = v.r[k], z;
+        if (v.z32) {
+            float2 f = v.z32[k];
+            z = make_double2((double)f.x, (double)f.y);
+            v.z[k] = z;
+        } else {
+            z = v.z[k];
+        }
         rz = r.x * z.x + r.y * z.y;
         if (v.zold) {
             double2 zo = v.zold[k];
@@ -296,7 +335,7 @@ __global__ void k_cg_dots_after_precondition(CGView v) {
 }
 void launch_cg_dots_after_precondition(const CGView& v, cudaStream_t s) {
     LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
-    k_cg_dots_after_precondition<<<d.grid, d.block, 0, s>>>(v);
+    k_cg_dots_after_precondition<<<d.grid, d.block, 0, s>>>(v); count_launch();
 }
 
 // xpby!(z, beta, p), conjugate_gradient.jl:361; the last block commits the stopping decision
@@ -319,13 +358,15 @@ __global__ void k_cg_xpby(CGView v) {
         unsigned int t = atomicAdd(&v.sc->ticket2, 1u);
         if (t == n - 1) {
             v.sc->ticket2 = 0u;
-            v.sc->done = v.sc->done_next;
+            int d = v.sc->done_next;
+            v.sc->done = d;
+            if (v.cond) cudaGraphSetConditional(v.cond, d ? 0u : 1u);
         }
     }
 }
 void launch_cg_xpby(const CGView& v, cudaStream_t s) {
     LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
-    k_cg_xpby<<<d.grid, d.block, 0, s>>>(v);
+    k_cg_xpby<<<d.grid, d.block, 0, s>>>(v); count_launch();
 }
 
 // precondition!(z, ::StressBalanceDiagonalPreconditioner, r, ...) over size(z.u), size(z.v)
@@ -344,7 +385,7 @@ __global__ void k_precondition_diagonal(DevGrid<double> g, double2* z, const dou
 }
 void launch_precondition_diagonal(const DevGrid<double>& g, double2* z, const double2* r, const double2* invd, cudaStream_t s) {
     LaunchDims d = dims2d(g.Nx + 1, g.Ny + 1);
-    k_precondition_diagonal<<<d.grid, d.block, 0, s>>>(g, z, r, invd);
+    k_precondition_diagonal<<<d.grid, d.block, 0, s>>>(g, z, r, invd); count_launch();
 }
 
 // ---- Picard -------------------------------------------------------------------------------------------------
@@ -355,11 +396,28 @@ __global__ void k_copy_range(DevGrid<double> g, double2* dst, const double2* __r
 }
 void launch_copy_range(const DevGrid<double>& g, double2* dst, const double2* src, cudaStream_t s) {
     LaunchDims d = dims2d(g.Nx, g.Ny);
-    k_copy_range<<<d.grid, d.block, 0, s>>>(g, dst, src);
+    k_copy_range<<<d.grid, d.block, 0, s>>>(g, dst, src); count_launch();
 }
 
-// picard.jl:83-85: x⁻ = x⁻ - x, Δ² = x⁻.x⁻, X² = x.x
-__global__ void k_picard_delta(DevGrid<double> g, double2* xprev, const double2* __restrict__ x, SolverScalars* sc, double2* partials) {
+// picard_solve! loop head (picard.jl:71-79): Δ = ∞, X = 0, iteration = 0
+__global__ void k_picard_begin(SolverScalars* sc, unsigned long long cond) {
+    sc->p_it = 0;
+    sc->p_D = INFINITY;
+    sc->p_X = 0.0;
+    sc->it_total = 0;
+    sc->cg_unconverged = 0;
+    sc->status = NK_OK;
+    int run = sc->p_fixed ? (sc->p_iterations > 0) : (sc->p_maxiter > 0);
+    sc->p_done = !run;
+    if (cond) cudaGraphSetConditional(cond, run ? 1u : 0u);
+}
+void launch_picard_begin(SolverScalars* sc, unsigned long long cond, cudaStream_t s) {
+    k_picard_begin<<<1, 1, 0, s>>>(sc, cond); count_launch();
+}
+
+// end of one Picard iteration (picard.jl:83-86): x⁻ = x⁻ - x, Δ = ‖x⁻‖, X = ‖x‖, then the loop test of :79
+__global__ void k_picard_end(DevGrid<double> g, double2* xprev, const double2* __restrict__ x, SolverScalars* sc, double2* partials,
+                             unsigned long long cond) {
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     double dd = 0.0, xx = 0.0;
     if (i < g.Nx && j < g.Ny) {
@@ -373,14 +431,27 @@ __global__ void k_picard_delta(DevGrid<double> g, double2* xprev, const double2*
     }
     double tdd, txx;
     if (grid_sum2(dd, xx, partials, &sc->ticket, tdd, txx) && threadIdx.x == 0 && threadIdx.y == 0) {
+        double D = sqrt(tdd), X = sqrt(txx);
         sc->picard_dd = tdd;
         sc->picard_xx = txx;
+        sc->p_D = D;
+        sc->p_X = X;
+        int it = sc->p_it + 1;
+        sc->p_it = it;
+        sc->it_total += sc->it;
+        int more = sc->p_fixed ? (it < sc->p_iterations) : (D > fmax(sc->p_reltol * X, sc->p_abstol) && it < sc->p_maxiter);
+        if (!isfinite(D) || sc->status == NK_NONFINITE) {
+            sc->status = NK_NONFINITE;
+            more = 0;
+        }
+        sc->p_done = !more;
+        if (cond) cudaGraphSetConditional(cond, more ? 1u : 0u);
     }
 }
-void launch_picard_delta(const DevGrid<double>& g, double2* xprev, const double2* x, SolverScalars* sc, double2* partials,
-                         cudaStream_t s) {
+void launch_picard_end(const DevGrid<double>& g, double2* xprev, const double2* x, SolverScalars* sc, double2* partials,
+                       unsigned long long cond, cudaStream_t s) {
     LaunchDims d = dims2d(g.Nx, g.Ny);
-    k_picard_delta<<<d.grid, d.block, 0, s>>>(g, xprev, x, sc, partials);
+    k_picard_end<<<d.grid, d.block, 0, s>>>(g, xprev, x, sc, partials, cond); count_launch();
 }
 
 // ---- vector helpers under the done predicate -------------------------------------------------------------------
@@ -392,7 +463,7 @@ __global__ void k_copy_vec(DevGrid<double> g, double2* dst, const double2* __res
 }
 void launch_copy_vec(const DevGrid<double>& g, double2* dst, const double2* src, const int* done, cudaStream_t s) {
     LaunchDims d = dims2d(g.Nx, g.Ny);
-    k_copy_vec<<<d.grid, d.block, 0, s>>>(g, dst, src, done);
+    k_copy_vec<<<d.grid, d.block, 0, s>>>(g, dst, src, done); count_launch();
 }
 
 __global__ void k_to_float(DevGrid<double> g, const double2* __restrict__ src, float2* dst, const int* done) {
@@ -404,7 +475,7 @@ __global__ void k_to_float(DevGrid<double> g, const double2* __restrict__ src, f
 }
 void launch_to_float(const DevGrid<double>& g, const double2* src, float2* dst, const int* done, cudaStream_t s) {
     LaunchDims d = dims2d(g.Nx, g.Ny);
-    k_to_float<<<d.grid, d.block, 0, s>>>(g, src, dst, done);
+    k_to_float<<<d.grid, d.block, 0, s>>>(g, src, dst, done); count_launch();
 }
 __global__ void k_to_double(DevGrid<double> g, const float2* __restrict__ src, double2* dst, const int* done) {
     if (done && *(volatile const int*)done) return;
@@ -415,7 +486,7 @@ __global__ void k_to_double(DevGrid<double> g, const float2* __restrict__ src, d
 }
 void launch_to_double(const DevGrid<double>& g, const float2* src, double2* dst, const int* done, cudaStream_t s) {
     LaunchDims d = dims2d(g.Nx, g.Ny);
-    k_to_double<<<d.grid, d.block, 0, s>>>(g, src, dst, done);
+    k_to_double<<<d.grid, d.block, 0, s>>>(g, src, dst, done); count_launch();
 }
 __global__ void k_coef_to_float(DevGrid<double> g, const double4* __restrict__ src, float4* dst) {
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
@@ -425,7 +496,7 @@ __global__ void k_coef_to_float(DevGrid<double> g, const double4* __restrict__ s
 }
 void launch_coef_to_float(const DevGrid<double>& g, const double4* src, float4* dst, cudaStream_t s) {
     LaunchDims d = dims2d(g.Nx + 1, g.Ny + 1);
-    k_coef_to_float<<<d.grid, d.block, 0, s>>>(g, src, dst);
+    k_coef_to_float<<<d.grid, d.block, 0, s>>>(g, src, dst); count_launch();
 }
 
 }  // namespace nk

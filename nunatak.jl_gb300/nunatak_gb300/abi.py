@@ -81,7 +81,20 @@ class SolveStats(C.Structure):
     _fields_ = [("status", C.c_int32), ("picard_iterations", C.c_int32), ("linear_iterations_last", C.c_int32),
                 ("linear_iterations_total", C.c_int32), ("residual_norm", C.c_double),
                 ("initial_residual_norm", C.c_double), ("picard_change", C.c_double),
-                ("picard_norm", C.c_double), ("device_ms", C.c_double)]
+                ("picard_norm", C.c_double), ("device_ms", C.c_double),
+                ("device_start_ms", C.c_double), ("device_end_ms", C.c_double)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class ServerDesc(C.Structure):
+    _fields_ = [("max_in_flight", C.c_int32), ("reserved", C.c_int32), ("memory_cap_bytes", C.c_int64)]
+
+
+class Request(C.Structure):
+    _fields_ = [("grid", GridDesc), ("physics", PhysicsDesc), ("solver", SolverDesc),
+                ("H", C.POINTER(C.c_double)), ("bed", C.POINTER(C.c_double)),
+                ("friction_coefficient", C.POINTER(C.c_double)), ("rate_factor", C.POINTER(C.c_double)),
+                ("u_init", C.POINTER(C.c_double)), ("v_init", C.POINTER(C.c_double)),
+                ("u_out", C.POINTER(C.c_double)), ("v_out", C.POINTER(C.c_double))]

@@ -19,6 +19,7 @@ def _declare(lib):
     ip = C.POINTER(C.c_int32)
     sig = {
         "nk_api_version": ([], i32),
+        "nk_launch_count": ([], i64),
         "nk_context_create": ([i32, C.POINTER(vp)], i32),
         "nk_context_destroy": ([vp], i32),
         "nk_last_error": ([vp], C.c_char_p),
@@ -35,10 +36,21 @@ def _declare(lib):
         "nk_linear_solve": ([vp, dp, dp, C.POINTER(abi.SolveStats)], i32),
         "nk_adjoint_solve": ([vp, dp, dp, C.POINTER(abi.SolveStats)], i32),
         "nk_picard_solve": ([vp, C.POINTER(abi.SolveStats)], i32),
+        "nk_picard_solve_async": ([vp], i32),
+        "nk_problem_wait": ([vp, C.POINTER(abi.SolveStats)], i32),
         "nk_solve_velocities": ([vp, dp, dp, C.POINTER(abi.SolveStats)], i32),
         "nk_velocity_profile": ([vp], i32),
         "nk_multigrid_levels": ([vp, ip, ip, ip, i32], i32),
         "nk_multigrid_restrict": ([vp, i32, dp, dp, dp, dp], i32),
+        "nk_time_kernel": ([vp, i32, i32, i64, dp, dp], i32),
+        "nk_server_create": ([vp, C.POINTER(abi.ServerDesc), C.POINTER(vp)], i32),
+        "nk_server_destroy": ([vp], i32),
+        "nk_server_submit": ([vp, C.POINTER(abi.Request), C.POINTER(i64)], i32),
+        "nk_server_progress": ([vp, ip], i32),
+        "nk_server_wait": ([vp, i64, C.POINTER(abi.SolveStats), dp, dp, dp], i32),
+        "nk_server_wait_all": ([vp], i32),
+        "nk_server_clock": ([vp], C.c_double),
+        "nk_server_info": ([vp, ip, C.POINTER(i64), ip], i32),
         "nk_multigrid_prolongate": ([vp, i32, dp, dp, dp, dp], i32),
     }
     for name, (args, res) in sig.items():
@@ -86,3 +98,8 @@ def default_context():
     if _CTX is None:
         _CTX = Context(0)
     return _CTX
+
+
+def launch_count():
+    """Kernels launched by libnunatak_gb300 in this process so far."""
+    return int(load().nk_launch_count())

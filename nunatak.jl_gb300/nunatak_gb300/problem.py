@@ -172,6 +172,16 @@ class Problem:
         _check(st, "picard_solve", self._err())
         return stats
 
+    def picard_solve_async(self):
+        """Enqueue picard_solve! on this problem's stream and return at once (see wait())."""
+        _check(self._fn("picard_solve_async")(self._h), "picard_solve_async", self._err())
+
+    def wait(self):
+        """Block until the asynchronous solve has finished; returns its stats."""
+        stats = abi.SolveStats()
+        _check(self._fn("problem_wait")(self._h, C.byref(stats)), "problem_wait", self._err())
+        return stats
+
     def velocity_profile(self):
         _check(self._fn("velocity_profile")(self._h), "velocity_profile", self._err())
 
@@ -209,3 +219,14 @@ class Problem:
                                               fu.ctypes.data_as(_dptr), fv.ctypes.data_as(_dptr))
         _check(st, "multigrid_prolongate", self._err())
         return fu, fv
+
+    # -- measurement ---------------------------------------------------------------------------------------
+    KERNELS = {"operator_fp64": 0, "smoother": 1, "cg_update": 2}
+
+    def time_kernel(self, kernel, repeats=20, flush_bytes=0):
+        """Mean CUDA-event duration (ms) of one launch of a hot kernel and its algorithmic bytes
+        (nk_time_kernel); flush_bytes > 0 overwrites a buffer of that size before each launch."""
+        ms, by = C.c_double(), C.c_double()
+        st = self._fn("time_kernel")(self._h, self.KERNELS[kernel], repeats, C.c_int64(flush_bytes), C.byref(ms), C.byref(by))
+        _check(st, "time_kernel", self._err())
+        return ms.value, by.value

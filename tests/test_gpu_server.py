@@ -1,0 +1,56 @@
+"""Serving: requests solved in a mix of concurrent requests give the same bits as each request solved alone."""
+import numpy as np
+import pytest
+
+import nunatak_gb300 as nk
+from nunatak_gb300 import workloads
+from nunatak_gb300.server import Server
+
+pytestmark = pytest.mark.gpu
+
+
+def requests():
+    out = []
+    for k, (nx, ny) in enumerate([(64, 32), (128, 64), (64, 32), (128, 64), (64, 32), (96, 48)]):
+        out.append(workloads.marine_sheet(nx, ny, seed=1, seed_friction=100 + k, precision="mixed",
+                                          minimum_coarse_size=8))
+    return out
+
+
+def alone(case):
+    P = case.problem(nk.Problem)
+    st = P.picard_solve()
+    return P.get("u"), P.get("v"), st
+
+
+def test_requests_in_a_mix_equal_solves_alone():
+    cases = requests()
+    ref = [alone(c) for c in cases]
+    S = Server(max_in_flight=4)
+    tickets = [S.submit(c) for c in cases]
+    got = [S.wait(t) for t in tickets]
+    info = S.info()
+    S.close()
+    for (u, v, st, times), (ur, vr, sr) in zip(got, ref):
+        assert st.status == 0 and st.picard_iterations == sr.picard_iterations
+        assert np.array_equal(u, ur) and np.array_equal(v, vr)
+        assert times[0] <= times[1] <= times[2]
+    assert info["peak_in_flight"] > 1
+    assert info["resident"] >= 3
+
+
+def test_memory_cap_admits_one_problem_at_a_time():
+    cases = requests()[:3]
+    ref = [alone(c) for c in cases]
+    probe = Server(max_in_flight=1)
+    probe.wait(probe.submit(cases[1]))
+    one = probe.info()["device_bytes"]
+    probe.close()
+    S = Server(max_in_flight=4, memory_cap_bytes=one + 1)   # room for the largest problem only
+    tickets = [S.submit(c) for c in cases]
+    got = [S.wait(t) for t in tickets]
+    info = S.info()
+    S.close()
+    for (u, v, st, _), (ur, vr, _) in zip(got, ref):
+        assert np.array_equal(u, ur) and np.array_equal(v, vr)
+    assert info["peak_in_flight"] == 1 and info["device_bytes"] <= one + 1
