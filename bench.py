@@ -31,6 +31,8 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "nunatak.jl_gb300"))
+# concurrent solves use one stream each: 32 hardware work queues instead of 8 (before any CUDA context exists)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 METRIC = "SSA solves/s & p99 latency, mixed vs FP64 on GB300 at <=1e-6 rel velocity error"
 WORKLOAD = ("marine_sheet 256x128 dx=2km (seeded bed + Weertman C), ensemble batch of {B} friction seeds per step, "
@@ -294,7 +296,7 @@ def main():
 
     # ---- end to end through the serving loop with host buffers --------------------------------------------
     from nunatak_gb300.server import Server
-    S = Server(max_in_flight=B, memory_cap_bytes=64 << 30, context=ctx)
+    S = Server(max_in_flight=B, memory_cap_bytes=8 << 30, context=ctx)
     for c in cases[:2]:
         S.wait(S.submit(c))             # warm-up: resident problems and their graphs
     e2e_times, e2e_lat = [], []

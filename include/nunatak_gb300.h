@@ -295,13 +295,16 @@ nk_status nk_multigrid_prolongate(nk_problem* problem, int32_t level, const doub
  * the same grid, physics and solver (only the input fields change), so each problem's device buffers,
  * multigrid hierarchy and captured CUDA graph are built once.  Up to max_in_flight requests run at once, each
  * on its own stream, so requests that arrive while others are on the GPU are admitted as soon as a slot and
- * memory are free and their kernels overlap on the device.  A new problem is created only while the device
- * memory of all resident problems stays within memory_cap_bytes (idle problems of other shapes are evicted
- * first).  Results do not depend on the mix: every request's arithmetic is that of a solve alone. */
+ * memory are free and their kernels overlap on the device.  The server reserves memory_cap_bytes of HBM (one
+ * cudaMalloc) and a pinned host staging pool of a thirty-second of it (at least 64 MiB) when it is created, and
+ * carves every resident problem out of them: admission by footprint, and no allocation call (which can wait on
+ * running work) while requests are on the device.  When a new problem does not fit, idle problems of other
+ * shapes are evicted, least recently used first.  Results do not depend on the mix: every request's arithmetic
+ * is that of a solve alone. */
 typedef struct nk_server_desc {
     int32_t max_in_flight;          /* requests on the device at once (>= 1) */
     int32_t reserved;
-    int64_t memory_cap_bytes;       /* device memory the resident problems may hold */
+    int64_t memory_cap_bytes;       /* device memory reserved for the resident problems */
 } nk_server_desc;
 
 typedef struct nk_request {

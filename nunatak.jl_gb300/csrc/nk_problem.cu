@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -151,6 +152,8 @@ struct nk_problem {
     int precond = NK_PRECONDITIONER_DIAGONAL;
 
     Arena arena;
+    bool external_arena = false;              // arena.base sub-allocated by a server (not cudaMalloc'd here)
+    bool external_pinned = false;             // sc_host sub-allocated from a server's pinned pool
     // fine level (FP64)
     Level<double> fine;                         // metrics, coef, mask, irs (multigrid FP64), x2, q, t
     double *H = nullptr, *bed = nullptr, *s = nullptr, *N = nullptr, *mu = nullptr, *phi = nullptr, *C = nullptr, *F2 = nullptr, *A2 = nullptr;
@@ -175,6 +178,7 @@ struct nk_problem {
     long long picard_kernels[3] = {0, 0, 0};   // kernel nodes: top level, Picard body, CG body
     long long linear_kernels[2] = {0, 0};      // kernel nodes: top level, CG body
     bool async_pending = false;                // nk_picard_solve_async issued, nk_problem_wait not yet called
+    double instantiate_s = 0;                  // host seconds of the last graph instantiation
 
     // ---- views ---------------------------------------------------------------------------------------------
     OpView<double> fine_op() const {
@@ -416,7 +420,7 @@ static void build(nk_problem* P, bool dry = false) {
         }
     }
     if (dry) return;   // sizing only: A.size is the device footprint
-    NK_CUDA(cudaMalloc((void**)&A.base, A.size));
+    if (!P->external_arena) NK_CUDA(cudaMalloc((void**)&A.base, A.size));
     NK_CUDA(cudaMemsetAsync(A.base, 0, A.size, P->stream));
     for (auto& sl : slots) *sl.first = A.base + sl.second;
 
@@ -438,7 +442,7 @@ static void build(nk_problem* P, bool dry = false) {
             for (int l = 1; l <= P->nlevels; ++l) upload_metrics(P->lv64[l], P->stream);
         }
     }
-    NK_CUDA(cudaHostAlloc((void**)&P->sc_host, sizeof(SolverScalars), cudaHostAllocDefault));
+    if (!P->external_pinned) NK_CUDA(cudaHostAlloc((void**)&P->sc_host, sizeof(SolverScalars), cudaHostAllocDefault));
     std::memset(P->sc_host, 0, sizeof(SolverScalars));
 }
 
@@ -737,7 +741,9 @@ static void build_picard_graph(nk_problem* P) {
     P->picard_kernels[0] = kernel_nodes(g);
     P->picard_kernels[1] = kernel_nodes(body);
     P->picard_kernels[2] = kernel_nodes(cg_body);
+    auto ti0 = std::chrono::steady_clock::now();
     NK_CUDA(cudaGraphInstantiate(&P->picard_exec, g, 0));
+    P->instantiate_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - ti0).count();
     P->picard_graph = g;
 }
 
@@ -968,6 +974,10 @@ int64_t nk_launch_count(void) { return (int64_t)nk::launch_count(); }
 
 nk_status nk_context_create(int32_t device, nk_context** out) {
     if (!out) return NK_BAD_ARGUMENT;
+    // Independent solves run on one stream each; with the default of 8 hardware work queues, streams beyond the
+    // eighth share a queue and wait on each other's work.  Effective only if the process has no CUDA context yet
+    // (hosts that create one first set CUDA_DEVICE_MAX_CONNECTIONS themselves).
+    setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) return NK_CUDA_ERROR;
     auto* c = new nk_context();
@@ -994,10 +1004,27 @@ nk_status nk_context_destroy(nk_context* ctx) {
 
 const char* nk_last_error(const nk_context* ctx) { return ctx ? ctx->error.c_str() : "no context"; }
 
+static nk_status problem_create(nk_context* ctx, const nk_grid_desc* grid, const nk_physics_desc* physics, const nk_solver_desc* solver,
+                                nk_problem** out, char* device_arena, SolverScalars* pinned_scalars);
+
 nk_status nk_problem_create(nk_context* ctx, const nk_grid_desc* grid, const nk_physics_desc* physics, const nk_solver_desc* solver,
                             nk_problem** out) {
+    return problem_create(ctx, grid, physics, solver, out, nullptr, nullptr);
+}
+
+// A problem whose device arena (problem_bytes) and pinned scalar block are supplied by the caller (the server).
+static nk_status problem_create(nk_context* ctx, const nk_grid_desc* grid, const nk_physics_desc* physics, const nk_solver_desc* solver,
+                                nk_problem** out, char* device_arena, SolverScalars* pinned_scalars) {
     if (!ctx || !grid || !physics || !solver || !out) return NK_BAD_ARGUMENT;
     auto* P = new nk_problem();
+    if (device_arena) {
+        P->arena.base = device_arena;
+        P->external_arena = true;
+    }
+    if (pinned_scalars) {
+        P->sc_host = pinned_scalars;
+        P->external_pinned = true;
+    }
     nk_status st = guarded(ctx, [&] {
         if (grid->Nx < 1 || grid->Ny < 1 || grid->Nsigma < 1 || grid->Nsigma > MAX_SIGMA) bad("grid size or Nsigma out of range");
         if (grid->halo_x < 0 || grid->halo_y < 0) bad("negative halo");
@@ -1037,8 +1064,8 @@ nk_status nk_problem_destroy(nk_problem* P) {
     if (P->linear_exec) cudaGraphExecDestroy(P->linear_exec);
     if (P->picard_graph) cudaGraphDestroy(P->picard_graph);
     if (P->linear_graph) cudaGraphDestroy(P->linear_graph);
-    if (P->arena.base) cudaFree(P->arena.base);
-    if (P->sc_host) cudaFreeHost(P->sc_host);
+    if (P->arena.base && !P->external_arena) cudaFree(P->arena.base);
+    if (P->sc_host && !P->external_pinned) cudaFreeHost(P->sc_host);
     if (P->ev0) cudaEventDestroy(P->ev0);
     if (P->ev1) cudaEventDestroy(P->ev1);
     if (P->stream) cudaStreamDestroy(P->stream);
@@ -1379,10 +1406,51 @@ nk_status nk_time_kernel(nk_problem* P, int32_t kernel, int32_t repeats, int64_t
 // =================================================================================================================
 #include <chrono>
 #include <deque>
+#include <map>
 #include <thread>
 #include <unordered_map>
 
 namespace {
+
+// First-fit sub-allocator over one reserved range, with coalescing of freed blocks (256-byte granules).
+struct SubAllocator {
+    size_t cap = 0;
+    std::map<size_t, size_t> free_blocks;   // offset -> size
+    void init(size_t bytes) {
+        cap = bytes;
+        free_blocks.clear();
+        free_blocks[0] = bytes;
+    }
+    static size_t round(size_t b) { return (b + 255) & ~size_t(255); }
+    bool alloc(size_t bytes, size_t& off) {
+        bytes = round(bytes);
+        for (auto it = free_blocks.begin(); it != free_blocks.end(); ++it) {
+            if (it->second < bytes) continue;
+            off = it->first;
+            size_t rest = it->second - bytes;
+            free_blocks.erase(it);
+            if (rest) free_blocks[off + bytes] = rest;
+            return true;
+        }
+        return false;
+    }
+    void release(size_t off, size_t bytes) {
+        bytes = round(bytes);
+        auto it = free_blocks.emplace(off, bytes).first;
+        auto next = std::next(it);
+        if (next != free_blocks.end() && it->first + it->second == next->first) {
+            it->second += next->second;
+            free_blocks.erase(next);
+        }
+        if (it != free_blocks.begin()) {
+            auto prev = std::prev(it);
+            if (prev->first + prev->second == it->first) {
+                prev->second += it->second;
+                free_blocks.erase(it);
+            }
+        }
+    }
+};
 
 struct ServerRequest {
     int64_t ticket = 0;
@@ -1404,7 +1472,8 @@ struct Resident {
     std::string key;
     bool busy = false;
     int64_t ticket = 0;
-    size_t bytes = 0;
+    size_t bytes = 0;                // device bytes sub-allocated at dev_off
+    size_t dev_off = 0, pin_off = 0, pin_bytes = 0;
     double last_used = 0;
     double* pin = nullptr;          // pinned staging: H, bed, C, A, u0, v0 in; u, v out
     size_t pin_count = 0;
@@ -1443,6 +1512,9 @@ nk_grid_desc grid_with_vectors(ServerRequest& R) {
 struct nk_server {
     nk_context* ctx = nullptr;
     nk_server_desc desc{};
+    // host seconds spent creating problems, starting and finishing requests (NK_SERVER_TRACE=1 prints them)
+    double t_create = 0, t_start = 0, t_finish = 0, t_graph = 0;
+    int created = 0;
     std::chrono::steady_clock::time_point t0;
     std::deque<int64_t> queue;
     std::unordered_map<int64_t, std::unique_ptr<ServerRequest>> requests;
@@ -1450,6 +1522,11 @@ struct nk_server {
     int64_t next_ticket = 1;
     int64_t device_bytes = 0;
     int in_flight = 0, peak = 0;
+    // the HBM budget and a pinned staging pool, reserved once when the server is created, so that no
+    // allocation call (which can wait on running work) happens while requests are on the device
+    char* dev_base = nullptr;
+    char* pin_base = nullptr;
+    SubAllocator dev, pin;
 
     double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
 };
@@ -1469,44 +1546,76 @@ static void destroy_resident(nk_server* S, size_t idx) {
     Resident* r = S->residents[idx].get();
     S->device_bytes -= (int64_t)r->bytes;
     if (r->done) cudaEventDestroy(r->done);
-    if (r->pin) cudaFreeHost(r->pin);
-    if (r->sc_out) cudaFreeHost(r->sc_out);
     nk_problem_destroy(r->P);
+    S->dev.release(r->dev_off, r->bytes);
+    S->pin.release(r->pin_off, r->pin_bytes);
     S->residents.erase(S->residents.begin() + idx);
 }
 
-// A resident problem for R: an idle one of the same shape, else a new one within the memory cap (evicting
-// idle problems of other shapes, least recently used first).  nullptr: wait for memory to free up.
+static size_t pinned_bytes(const ServerRequest& R) {
+    size_t cells = (size_t)R.grid.Nx * R.grid.Ny, faces = (size_t)(R.grid.Nx + 1) * (R.grid.Ny + 1);
+    return (4 * cells + 4 * faces) * sizeof(double) + 2 * 256 + 2 * sizeof(SolverScalars);
+}
+
+// A resident problem for R: an idle one of the same shape, else a new one carved out of the server's
+// reserved HBM and pinned pool (evicting idle problems of other shapes, least recently used first).
+// nullptr: wait until running requests release memory.
 static Resident* acquire(nk_server* S, ServerRequest& R) {
     for (auto& r : S->residents)
         if (!r->busy && r->key == R.key) return r.get();
-    size_t need = problem_bytes(R);
-    while (S->device_bytes + (int64_t)need > S->desc.memory_cap_bytes) {
+    size_t need = problem_bytes(R), pneed = pinned_bytes(R);
+    size_t off = 0, poff = 0;
+    auto fits = [&] {
+        if (!S->dev.alloc(need, off)) return false;
+        if (!S->pin.alloc(pneed, poff)) {
+            S->dev.release(off, need);
+            return false;
+        }
+        return true;
+    };
+    while (!fits()) {
         int victim = -1;
         for (size_t i = 0; i < S->residents.size(); ++i)
             if (!S->residents[i]->busy && (victim < 0 || S->residents[i]->last_used < S->residents[victim]->last_used)) victim = (int)i;
-        if (victim < 0) break;
+        if (victim < 0) {
+            if (S->in_flight > 0) return nullptr;
+            throw Failure{NK_OOM, "a request needs more device or pinned memory than the server reserved"};
+        }
         destroy_resident(S, victim);
     }
-    if (S->device_bytes + (int64_t)need > S->desc.memory_cap_bytes) {
-        if (S->in_flight > 0) return nullptr;
-        throw Failure{NK_OOM, "a request needs more device memory than memory_cap_bytes"};
-    }
+    double tc0 = S->now();
     auto r = std::make_unique<Resident>();
+    r->dev_off = off;
+    r->bytes = need;
+    r->pin_off = poff;
+    r->pin_bytes = pneed;
+    char* pin = S->pin_base + poff;
+    r->sc_out = reinterpret_cast<SolverScalars*>(pin);
+    SolverScalars* sc_host = reinterpret_cast<SolverScalars*>(pin + 256);
+    r->pin = reinterpret_cast<double*>(pin + 512);
     nk_grid_desc g = grid_with_vectors(R);
-    nk_status st = nk_problem_create(S->ctx, &g, &R.physics, &R.solver, &r->P);
-    if (st != NK_OK) throw Failure{st, S->ctx->error};
+    nk_status st = problem_create(S->ctx, &g, &R.physics, &R.solver, &r->P, S->dev_base + off, sc_host);
+    if (st != NK_OK) {
+        S->dev.release(off, need);
+        S->pin.release(poff, pneed);
+        throw Failure{st, S->ctx->error};
+    }
     r->key = R.key;
-    r->bytes = r->P->arena.size;
     nk_problem* P = r->P;
     size_t cells = (size_t)P->Nx * P->Ny, faces = (size_t)(P->Nx + 1) * (P->Ny + 1);
     r->pin_count = 4 * cells + 4 * faces;
-    NK_CUDA(cudaHostAlloc((void**)&r->pin, r->pin_count * sizeof(double), cudaHostAllocDefault));
-    NK_CUDA(cudaHostAlloc((void**)&r->sc_out, sizeof(SolverScalars), cudaHostAllocDefault));
     NK_CUDA(cudaEventCreateWithFlags(&r->done, cudaEventDisableTiming));
+    double tg0 = S->now();
     if (use_graphs()) build_picard_graph(P);
+    S->t_graph += S->now() - tg0;
+    if (const char* e = std::getenv("NK_SERVER_TRACE"))
+        if (e[0] == '1')
+            std::fprintf(stderr, "nk_server: problem %d: setup %.1f ms, graph %.1f ms (instantiate %.1f ms), %d in flight\n", S->created + 1,
+                         1e3 * (tg0 - tc0), 1e3 * (S->now() - tg0), 1e3 * P->instantiate_s, S->in_flight);
     S->device_bytes += (int64_t)r->bytes;
     S->residents.push_back(std::move(r));
+    S->created += 1;
+    S->t_create += S->now() - tc0;
     return S->residents.back().get();
 }
 
@@ -1587,7 +1696,11 @@ static void progress(nk_server* S) {
     for (auto& r : S->residents) {
         if (!r->busy) continue;
         cudaError_t e = cudaEventQuery(r->done);
-        if (e == cudaSuccess) finish(S, *r);
+        if (e == cudaSuccess) {
+            double tf0 = S->now();
+            finish(S, *r);
+            S->t_finish += S->now() - tf0;
+        }
         else if (e != cudaErrorNotReady) NK_CUDA(e);
     }
     while (!S->queue.empty() && S->in_flight < S->desc.max_in_flight) {
@@ -1604,7 +1717,9 @@ static void progress(nk_server* S) {
         }
         if (!r) break;   // wait for memory
         S->queue.pop_front();
+        double ts0 = S->now();
         start(S, R, *r);
+        S->t_start += S->now() - ts0;
     }
 }
 
@@ -1618,16 +1733,35 @@ nk_status nk_server_create(nk_context* ctx, const nk_server_desc* desc, nk_serve
     S->ctx = ctx;
     S->desc = *desc;
     S->t0 = std::chrono::steady_clock::now();
+    // pinned staging: inputs and outputs of the requests in flight (a thirty-second of the device budget, >= 64 MiB)
+    size_t pin_cap = std::max<size_t>(64ull << 20, (size_t)desc->memory_cap_bytes / 32);
+    nk_status st = guarded(ctx, [&] {
+        NK_CUDA(cudaMalloc((void**)&S->dev_base, (size_t)desc->memory_cap_bytes));
+        NK_CUDA(cudaHostAlloc((void**)&S->pin_base, pin_cap, cudaHostAllocDefault));
+    });
+    if (st != NK_OK) {
+        if (S->dev_base) cudaFree(S->dev_base);
+        delete S;
+        return st;
+    }
+    S->dev.init((size_t)desc->memory_cap_bytes);
+    S->pin.init(pin_cap);
     *out = S;
     return NK_OK;
 }
 
 nk_status nk_server_destroy(nk_server* S) {
     if (!S) return NK_OK;
+    if (const char* e = std::getenv("NK_SERVER_TRACE"))
+        if (e[0] == '1')
+            std::fprintf(stderr, "nk_server: %d problems created in %.3f s (graph capture %.3f s); host time starting requests %.3f s, "
+                                 "finishing %.3f s; peak in flight %d\n", S->created, S->t_create, S->t_graph, S->t_start, S->t_finish, S->peak);
     guarded(S->ctx, [&] {
         for (auto& r : S->residents)
             if (r->busy) cudaEventSynchronize(r->done);
         while (!S->residents.empty()) destroy_resident(S, S->residents.size() - 1);
+        if (S->dev_base) cudaFree(S->dev_base);
+        if (S->pin_base) cudaFreeHost(S->pin_base);
     });
     delete S;
     return NK_OK;

@@ -18,7 +18,7 @@ def _ptr(a):
 
 
 class Server:
-    def __init__(self, max_in_flight=16, memory_cap_bytes=64 << 30, context=None):
+    def __init__(self, max_in_flight=16, memory_cap_bytes=16 << 30, context=None):
         self.ctx = context or library.default_context()
         self.lib = library.load()
         self.h = C.c_void_p()
