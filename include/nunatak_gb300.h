@@ -284,6 +284,32 @@ nk_status nk_multigrid_restrict(nk_problem* problem, int32_t level, const double
 nk_status nk_multigrid_prolongate(nk_problem* problem, int32_t level, const double* coarse_u, const double* coarse_v,
                                   double* fine_u, double* fine_v);
 
+/* ---- velocity change without device allocation ---------------------------------------------------------
+ *
+ * No counterpart in the reference.  For callers that cannot let the library allocate device memory while
+ * they run: a model whose host framework pools the whole device (a CUDA.jl or PyTorch caching allocator),
+ * where an extra cudaMalloc fails and a cudaFree stalls the device, or a coupled time loop that must not
+ * synchronise.  Computes the Picard change measure of picard_solve! (src/Solvers/picard.jl:83-86)
+ *   change_and_norm[0] = ||(u, v) - (u_prev, v_prev)||,   change_and_norm[1] = ||(u, v)||
+ * over the cells of the grid (u at the west and v at the south face of each cell), with the same reduction
+ * and summation order as the picard_change and picard_norm of nk_picard_solve.  u, v, u_prev, v_prev and
+ * change_and_norm are DEVICE pointers: u, v in the interior layout of nk_problem_get_field (u rows of Nx + 1
+ * faces when x is Bounded, Nx when Periodic; v rows of Nx), change_and_norm two doubles.  Enqueued on
+ * `stream` (a cudaStream_t; NULL = the legacy default stream) without waiting; the result is there when the
+ * stream reaches it.
+ *
+ * Scratch lives in a fixed __device__ array of 262,400 bytes that every GPU loading the library holds until
+ * exit: one partial per 32 x 8 block of cells, at most NK_NOALLOC_MAX_BLOCKS, so ceil(Nx / 32) * ceil(Ny / 8)
+ * must not exceed it (2048 x 2048 cells fit); larger grids return NK_BAD_ARGUMENT with the sizes in
+ * nk_last_error.  The first call on a device looks the array's address up (cudaGetSymbolAddress): make that
+ * first call before any stream capture.  Every call on a device shares the one array, and each clears the
+ * block counter on its stream before its kernel: calls whose work overlaps on the GPU (other streams or
+ * threads without ordering between them) race and give wrong results.  Nothing is allocated or freed. */
+#define NK_NOALLOC_MAX_BLOCKS 16384
+nk_status nk_picard_change_noalloc(nk_context* ctx, const nk_grid_desc* grid, const double* u, const double* v,
+                                   const double* u_prev, const double* v_prev, double* change_and_norm,
+                                   void* stream);
+
 /* ---- serving -------------------------------------------------------------------------------------------
  *
  * A request loop for many independent velocity solves (ensemble members, inversion line-search trials,

@@ -18,7 +18,17 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "../../include/nunatak_gb300.h"
+
+// Device context of the C ABI: the CUDA ordinal made current by every call, and the last error message.
+struct nk_context {
+    int device = 0;
+    std::string error;
+    cudaStream_t stream = nullptr;   // records the reference event
+    cudaEvent_t ref = nullptr;       // time origin of nk_solve_stats::device_start_ms / device_end_ms
+};
 
 namespace nk {
 

@@ -20,13 +20,6 @@
 
 #include "nk_kernels.cuh"
 
-struct nk_context {
-    int device = 0;
-    std::string error;
-    cudaStream_t stream = nullptr;   // records the reference event
-    cudaEvent_t ref = nullptr;       // time origin of nk_solve_stats::device_start_ms / device_end_ms
-};
-
 namespace nk {
 
 // ---- error handling ---------------------------------------------------------------------------------------
