@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--profile", choices=["solve", "smoother", "operator"], default=None,
                     help="profiling runs for ncu: 'solve' = warm-up solves then one timed solve of the workload; "
                          "'smoother' / 'operator' = the roofline kernel on the 2048x1024 grid, 3 launches")
+    ap.add_argument("--profile-grid", type=int, nargs=2, default=[256, 128], metavar=("NX", "NY"),
+                    help="grid of the marine-sheet solve that --profile solve runs")
     return ap.parse_args()
 
 
@@ -122,9 +124,9 @@ def rel_l2(ua, va, ub, vb):
     return float(math.sqrt(np.sum((ua - ub) ** 2) + np.sum((va - vb) ** 2)) / math.sqrt(np.sum(ub ** 2) + np.sum(vb ** 2)))
 
 
-def workload(precision, member=0):
+def workload(precision, member=0, grid=(256, 128)):
     from nunatak_gb300 import workloads
-    return workloads.marine_sheet(256, 128, seed=1, seed_friction=1000 + member, precision=precision)
+    return workloads.marine_sheet(grid[0], grid[1], seed=1, seed_friction=1000 + member, precision=precision)
 
 
 def cpu_solve(case, threads):
@@ -183,7 +185,7 @@ def roofline_problem(nk, workloads, ctx):
 def profile(args, nk, workloads, ctx):
     import numpy as np
     if args.profile == "solve":
-        P = workload("mixed").problem(nk.Problem, context=ctx)
+        P = workload("mixed", grid=tuple(args.profile_grid)).problem(nk.Problem, context=ctx)
         zu, zv = np.zeros(P.shape("u")), np.zeros(P.shape("v"))
         for _ in range(max(1, args.warmup) + 1):
             P.set("u", zu)

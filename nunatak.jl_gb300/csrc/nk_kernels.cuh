@@ -1,7 +1,7 @@
 // nk_kernels.cuh — host-callable launchers of the kernels, shared between the translation units.
 #pragma once
 
-#include "nk_operator.cuh"
+#include "nk_strip.cuh"
 
 namespace nk {
 

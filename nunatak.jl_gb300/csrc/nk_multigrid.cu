@@ -248,57 +248,68 @@ __device__ __forceinline__ void line_relax_column(const LevelView<T>& L, typenam
 
 // ---- grid-wide kernels ---------------------------------------------------------------------------------------
 template <typename T>
-__global__ void k_smooth_point(LevelView<T> L, const typename Vec2<T>::type* __restrict__ xin, typename Vec2<T>::type* __restrict__ xout,
-                               int first, const int* done) {
+__global__ void k_smooth_first(LevelView<T> L, const typename Vec2<T>::type* __restrict__ xin, typename Vec2<T>::type* __restrict__ xout,
+                               const int* done) {
+    if (stopped(done)) return;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i < L.o.g.Nx && j < L.o.g.Ny) smooth_point_at(L, xin, xout, true, i, j);
+}
+
+// One ℓ1-Jacobi sweep x' = x + (b - A x) / rowsum with the column-marching operator apply.
+template <typename T, int R>
+__global__ void __launch_bounds__(32 * STRIP_WARPS) k_smooth_point(LevelView<T> L, const typename Vec2<T>::type* __restrict__ xin,
+                                                                  typename Vec2<T>::type* __restrict__ xout, const int* done) {
     if (stopped(done)) return;
     using V2 = typename Vec2<T>::type;
-    int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY;
-    int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
-    bool inside = i < L.o.g.Nx && j < L.o.g.Ny;
-    if (first) {
-        if (inside) smooth_point_at(L, xin, xout, true, i, j);
-        return;
-    }
-    __shared__ ApplyTile<T> sm;
-    V2 q = tiled_apply(L.o, xin, sm, i0, j0, i, j, inside);
-    if (!inside) return;
-    int k = L.o.g.idx(i, j);
-    V2 b = L.b[k], w = L.irs[k], x = xin[k], out;
-    out.x = x.x + (b.x - q.x) * w.x;
-    out.y = x.y + (b.y - q.y) * w.y;
-    xout[k] = out;
+    int i, j0;
+    strip_origin<R>(i, j0);
+    if (j0 >= L.o.g.Ny) return;   // whole warp
+    struct BW { V2 b, w; };
+    strip_apply<R>(L.o, xin, i, j0, [&](int k) { return BW{L.b[k], L.irs[k]}; }, [&](int k, V2 q, V2 x, const BW& e) {
+        V2 out;
+        out.x = x.x + (e.b.x - q.x) * e.w.x;
+        out.y = x.y + (e.b.y - q.y) * e.w.y;
+        xout[k] = out;
+    });
 }
 template <typename T>
 void launch_smooth_point(const LevelView<T>& L, const typename Vec2<T>::type* x_in, typename Vec2<T>::type* x_out, int first,
                          const int* done, cudaStream_t s) {
-    LaunchDims d = dims2d(L.o.g.Nx, L.o.g.Ny);
-    k_smooth_point<T><<<d.grid, d.block, 0, s>>>(L, x_in, x_out, first, done); count_launch();
+    if (first) {
+        LaunchDims d = dims2d(L.o.g.Nx, L.o.g.Ny);
+        k_smooth_first<T><<<d.grid, d.block, 0, s>>>(L, x_in, x_out, done); count_launch();
+    } else {
+        int rows = strip_rows(L.o.g.Nx, L.o.g.Ny, (int)sizeof(T));
+        LaunchDims d = strip_dims(L.o.g.Nx, L.o.g.Ny, rows);
+        with_strip_rows(rows, [&](auto r) { k_smooth_point<T, decltype(r)::value><<<d.grid, d.block, 0, s>>>(L, x_in, x_out, done); });
+        count_launch();
+    }
 }
 
-template <typename T>
-__global__ void k_level_apply(LevelView<T> L, const typename Vec2<T>::type* __restrict__ x, typename Vec2<T>::type* __restrict__ q,
-                              int residual, const int* done) {
+template <typename T, int R>
+__global__ void __launch_bounds__(32 * STRIP_WARPS) k_level_apply(LevelView<T> L, const typename Vec2<T>::type* __restrict__ x,
+                                                                 typename Vec2<T>::type* __restrict__ q, int residual, const int* done) {
     if (stopped(done)) return;
     using V2 = typename Vec2<T>::type;
-    __shared__ ApplyTile<T> sm;
-    int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY;
-    int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
-    bool inside = i < L.o.g.Nx && j < L.o.g.Ny;
-    V2 a = tiled_apply(L.o, x, sm, i0, j0, i, j, inside);
-    if (!inside) return;
-    int k = L.o.g.idx(i, j);
-    if (residual) {
-        V2 b = L.b[k];
-        a.x = b.x - a.x;
-        a.y = b.y - a.y;
-    }
-    q[k] = a;
+    int i, j0;
+    strip_origin<R>(i, j0);
+    if (j0 >= L.o.g.Ny) return;   // whole warp
+    strip_apply<R>(L.o, x, i, j0, [&](int k) { V2 b; b.x = T(0); b.y = T(0); if (residual) b = L.b[k]; return b; },
+                   [&](int k, V2 a, V2, const V2& b) {
+        if (residual) {
+            a.x = b.x - a.x;
+            a.y = b.y - a.y;
+        }
+        q[k] = a;
+    });
 }
 template <typename T>
 void launch_level_apply(const LevelView<T>& L, const typename Vec2<T>::type* x, typename Vec2<T>::type* q, int residual,
                         const int* done, cudaStream_t s) {
-    LaunchDims d = dims2d(L.o.g.Nx, L.o.g.Ny);
-    k_level_apply<T><<<d.grid, d.block, 0, s>>>(L, x, q, residual, done); count_launch();
+    int rows = strip_rows(L.o.g.Nx, L.o.g.Ny, (int)sizeof(T));
+    LaunchDims d = strip_dims(L.o.g.Nx, L.o.g.Ny, rows);
+    with_strip_rows(rows, [&](auto r) { k_level_apply<T, decltype(r)::value><<<d.grid, d.block, 0, s>>>(L, x, q, residual, done); });
+    count_launch();
 }
 
 template <typename T>

@@ -38,6 +38,22 @@ struct Failure {
 
 static void bad(const std::string& m) { throw Failure{NK_BAD_ARGUMENT, m}; }
 
+// Rows per warp of the column-marching kernels: NK_STRIP_ROWS (1, 2, 4 or 8) when set, else by grid size.
+// FP64 walks stop at 4 rows: the FP64 kernels are bound by the FP64 pipe, and longer walks only add registers.
+int strip_rows(int nx, int ny, int elem_bytes) {
+    static const int forced = [] {
+        const char* e = std::getenv("NK_STRIP_ROWS");
+        int r = e ? std::atoi(e) : 0;
+        return (r == 1 || r == 2 || r == 4 || r == 8) ? r : 0;
+    }();
+    int rows = forced;
+    if (!rows) {
+        long long cells = (long long)nx * ny;
+        rows = cells >= (1 << 18) ? 4 : 2;
+    }
+    return elem_bytes == 8 ? std::min(rows, 4) : rows;
+}
+
 // ---- grid axis: Oceananigans generate_coordinate with halo nodes ----------------------------------------------
 // Regular axes use the single spacing L / N; face vectors extend the edge spacing into the halo (Bounded)
 // or wrap (Periodic); centres are face midpoints; Δᶜ(i) = F(i+1) - F(i), Δᶠ(i) = C(i) - C(i-1).
@@ -397,8 +413,8 @@ static void build(nk_problem* P, bool dry = false) {
     slots.push_back({(void**)&P->usig, A.reserve(d2 * P->Ns)});
     P->staging_count = (size_t)(P->Nx + 1) * (P->Ny + 1) * P->Ns;
     slots.push_back({(void**)&P->staging, A.reserve(P->staging_count * sizeof(double))});
-    LaunchDims big = dims2d(P->Nx + 1, P->Ny + 1);
-    size_t nblocks = (size_t)big.grid.x * big.grid.y;
+    LaunchDims big = dims2d(P->Nx + 1, P->Ny + 1), strips = strip_dims(P->Nx, P->Ny, STRIP_MIN_ROWS);
+    size_t nblocks = std::max((size_t)big.grid.x * big.grid.y, (size_t)strips.grid.x * strips.grid.y);
     slots.push_back({(void**)&P->partials, A.reserve(nblocks * sizeof(double2))});
     slots.push_back({(void**)&P->sc, A.reserve(sizeof(SolverScalars))});
     slots.push_back({(void**)&P->sig_tables, A.reserve((3 * P->Ns + (size_t)P->Ns * P->Ns) * sizeof(double))});

@@ -69,17 +69,18 @@ void launch_fill(double* dst, int count, double value, cudaStream_t s) {
 }
 
 // ---- operator, masks, diagonals ---------------------------------------------------------------------------
-__global__ void k_apply(OpView<double> o, const double2* __restrict__ p, double2* __restrict__ q) {
-    __shared__ ApplyTile<double> sm;
-    int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY;
-    int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
-    bool inside = i < o.g.Nx && j < o.g.Ny;
-    double2 a = tiled_apply(o, p, sm, i0, j0, i, j, inside);
-    if (inside) q[o.g.idx(i, j)] = a;
+template <int R>
+__global__ void __launch_bounds__(32 * STRIP_WARPS) k_apply(OpView<double> o, const double2* __restrict__ p, double2* __restrict__ q) {
+    int i, j0;
+    strip_origin<R>(i, j0);
+    if (j0 >= o.g.Ny) return;   // whole warp
+    strip_apply<R>(o, p, i, j0, [](int) { return NoExtra{}; }, [&](int k, double2 a, double2, NoExtra) { q[k] = a; });
 }
 void launch_apply(const OpView<double>& o, const double2* p, double2* q, cudaStream_t s) {
-    LaunchDims d = dims2d(o.g.Nx, o.g.Ny);
-    k_apply<<<d.grid, d.block, 0, s>>>(o, p, q); count_launch();
+    int rows = strip_rows(o.g.Nx, o.g.Ny, 8);
+    LaunchDims d = strip_dims(o.g.Nx, o.g.Ny, rows);
+    with_strip_rows(rows, [&](auto r) { k_apply<decltype(r)::value><<<d.grid, d.block, 0, s>>>(o, p, q); });
+    count_launch();
 }
 
 // inactiveᶠᶜᶜ / inactiveᶜᶠᶜ with η̄H (ssa_operator.jl:91-92, smooth_ice_mask.jl:429-430) and the wall bits
@@ -145,30 +146,28 @@ __device__ __forceinline__ int stop_after(const SolverScalars* sc, double rnorm,
 }
 
 // conjugate_gradient!, conjugate_gradient.jl:306-312: r = b - A x, z = M r, p = z, rho = r.z
-__global__ void k_cg_init(CGView v) {
-    __shared__ ApplyTile<double> sm;
-    int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY;
-    int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
-    bool inside = i < v.o.g.Nx && j < v.o.g.Ny;
-    double2 q = tiled_apply(v.o, (const double2*)v.x, sm, i0, j0, i, j, inside);
+template <int R>
+__global__ void __launch_bounds__(32 * STRIP_WARPS) k_cg_init(CGView v) {
+    int i, j0;
+    strip_origin<R>(i, j0);
     double rz = 0.0, rr = 0.0;
-    if (inside) {
-        int k = v.o.g.idx(i, j);
-        double2 b = v.b[k];
-        double2 r = make_double2(b.x - q.x, b.y - q.y);
-        v.r[k] = r;
-        if (v.r32) v.r32[k] = make_float2((float)r.x, (float)r.y);
-        rr = r.x * r.x + r.y * r.y;
-        if (v.precond != NK_PRECONDITIONER_MULTIGRID) {
-            double2 z = r;
-            if (v.precond == NK_PRECONDITIONER_DIAGONAL) {
-                double2 d = v.invd[k];
-                z = make_double2(r.x * d.x, r.y * d.y);
+    if (j0 < v.o.g.Ny) {   // warps below the grid still take part in the block reduction
+        strip_apply<R>(v.o, (const double2*)v.x, i, j0, [&](int k) { return v.b[k]; }, [&](int k, double2 q, double2, const double2& b) {
+            double2 r = make_double2(b.x - q.x, b.y - q.y);
+            v.r[k] = r;
+            if (v.r32) v.r32[k] = make_float2((float)r.x, (float)r.y);
+            rr += r.x * r.x + r.y * r.y;
+            if (v.precond != NK_PRECONDITIONER_MULTIGRID) {
+                double2 z = r;
+                if (v.precond == NK_PRECONDITIONER_DIAGONAL) {
+                    double2 d = v.invd[k];
+                    z = make_double2(r.x * d.x, r.y * d.y);
+                }
+                v.z[k] = z;
+                v.p[k] = z;
+                rz += r.x * z.x + r.y * z.y;
             }
-            v.z[k] = z;
-            v.p[k] = z;
-            rz = r.x * z.x + r.y * z.y;
-        }
+        });
     }
     double trz, trr;
     if (grid_sum2(rz, rr, v.partials, &v.sc->ticket, trz, trr) && threadIdx.x == 0 && threadIdx.y == 0) {
@@ -189,8 +188,10 @@ __global__ void k_cg_init(CGView v) {
     }
 }
 void launch_cg_init(const CGView& v, cudaStream_t s) {
-    LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
-    k_cg_init<<<d.grid, d.block, 0, s>>>(v); count_launch();
+    int rows = strip_rows(v.o.g.Nx, v.o.g.Ny, 8);
+    LaunchDims d = strip_dims(v.o.g.Nx, v.o.g.Ny, rows);
+    with_strip_rows(rows, [&](auto r) { k_cg_init<decltype(r)::value><<<d.grid, d.block, 0, s>>>(v); });
+    count_launch();
 }
 
 // multigrid start: p = z, rho = r.z (and z_old = z for flexible conjugate gradients)
@@ -223,19 +224,17 @@ void launch_cg_init_finish(const CGView& v, cudaStream_t s) {
 }
 
 // conjugate_gradient_step!, conjugate_gradient.jl:350-353: q = A p, alpha = rho / p.q (0 if p.q = 0)
-__global__ void k_cg_apply(CGView v) {
+template <int R>
+__global__ void __launch_bounds__(32 * STRIP_WARPS) k_cg_apply(CGView v) {
     if (read_done(v.sc)) return;
-    __shared__ ApplyTile<double> sm;
-    int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY;
-    int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
-    bool inside = i < v.o.g.Nx && j < v.o.g.Ny;
-    double2 q = tiled_apply(v.o, (const double2*)v.p, sm, i0, j0, i, j, inside);
+    int i, j0;
+    strip_origin<R>(i, j0);
     double pq = 0.0;
-    if (inside) {
-        int k = v.o.g.idx(i, j);
-        v.q[k] = q;
-        double2 p = v.p[k];
-        pq = p.x * q.x + p.y * q.y;
+    if (j0 < v.o.g.Ny) {   // warps below the grid still take part in the block reduction
+        strip_apply<R>(v.o, (const double2*)v.p, i, j0, [](int) { return NoExtra{}; }, [&](int k, double2 q, double2 p, NoExtra) {
+            v.q[k] = q;
+            pq += p.x * q.x + p.y * q.y;
+        });
     }
     double tpq, dummy;
     if (grid_sum2(pq, 0.0, v.partials, &v.sc->ticket, tpq, dummy) && threadIdx.x == 0 && threadIdx.y == 0) {
@@ -246,8 +245,10 @@ __global__ void k_cg_apply(CGView v) {
     }
 }
 void launch_cg_apply(const CGView& v, cudaStream_t s) {
-    LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
-    k_cg_apply<<<d.grid, d.block, 0, s>>>(v); count_launch();
+    int rows = strip_rows(v.o.g.Nx, v.o.g.Ny, 8);
+    LaunchDims d = strip_dims(v.o.g.Nx, v.o.g.Ny, rows);
+    with_strip_rows(rows, [&](auto r) { k_cg_apply<decltype(r)::value><<<d.grid, d.block, 0, s>>>(v); });
+    count_launch();
 }
 
 // conjugate_gradient_step!, :355-360 and the stopping test of :334-338
