@@ -1,24 +1,37 @@
 #!/usr/bin/env python
-"""bench.py — SSA velocity solves per second on GB300 (mixed precision vs FP64).
+"""bench.py — SSA velocity solves per second and latency on GB300, mixed precision vs FP64.
 
-Workload: the marine ice sheet on a 256 x 128 grid at 2 km (seeded random bed, Weertman friction with a
-seeded random coefficient, Glen n = 3, free-slip walls, subgrid grounded fraction), Picard to 1e-6 relative
-velocity change around multigrid PCG to 1e-8 (levels 256x128, 128x64, 64x32, 32x32; 2 + 2 point sweeps, 20
-on the coarsest).  One step solves a batch of B ensemble members (the same geometry, friction seeds 1000+k)
-from a zero initial guess.  The mixed solver runs the multigrid preconditioner in FP32 under FP64 flexible
-conjugate gradients, the B members concurrently on B streams; the plain FP64 solver is timed on the same
-members one solve at a time.
+Workload: the serving stream.  512 SSA velocity-solve requests arrive as a Poisson process at 200 requests/s,
+with grid sizes drawn uniformly from 128x64, 256x128, 512x256 and 1024x512.  Every size covers the same
+512 km x 256 km marine ice sheet (dx = 4, 2, 1, 0.5 km).  Each request has a seeded random bed, a Weertman
+friction coefficient from its own seed (1000 + request index), Glen n = 3, free-slip walls and a subgrid
+grounded fraction.  It is solved with Picard to 1e-6 relative velocity change around multigrid PCG to 1e-8
+(coarsening stops at 32 cells; 2 + 2 point sweeps, 20 on the coarsest level), starting from zero.  The mixed
+solver runs the multigrid in FP32 under FP64 flexible CG.  The plain FP64 solver runs the multigrid in FP64.
 
-  value     solves/s of the mixed solver, inputs resident in HBM, CUDA events (first start to last end of the
-            batch), L2 flushed (256 MiB write) between steps; latency p50 / p99 of the individual solves
-  e2e       the same batch through the serving loop of the C ABI (nk_server_*) from host buffers: upload of
-            H, bed, C, A, geometry, solve, read-back of u and v, host wall clock
-  roofline  the dominant kernel (the fine-level FP32 ℓ1-Jacobi sweep) timed with CUDA events on a 2048 x 1024
-            grid with L2 flushed before each launch, against the measured HBM copy bandwidth
-  cpu_baseline  the FP64 CPU restatement of the reference solve (the oracle) on the host cores, one full solve
+One step is one batch of B consecutive requests of the stream (B = --batch, default 32).  The timed steps
+walk the stream from its first request and wrap around after 512.  The warm-up steps come from its end.
 
-`--impl reference` times that CPU restatement alone (all host threads, full solves of the same workload).
-Multi-GPU: replicas only (each rank solves its own batch; no collective on the data path)."""
+  value     solves/s of the mixed solver with every request's inputs staged in HBM before the timed region.
+            Up to B solves are in flight on B streams.  A finished solve frees its resident problem for the
+            next request at once (continuous batching).  Time runs from the first solve's start event to the
+            last one's end event.  Requests of up to 1024x512 keep the working set far above L2, so L2 is not
+            flushed.
+  e2e       the same requests through the C ABI serving loop (nk_server_*) from host buffers, submitted at
+            their Poisson arrival times.  Covers upload, geometry, solve and read-back of u and v; host wall
+            clock.  p50 and p99 latency run from arrival to result.
+  fp64      the plain FP64 solver one solve at a time, timed on one request of each size.  Its stream rate is
+            the stream's size mix divided by those times.
+  roofline  the fine-level FP32 l1-Jacobi sweep (the most frequent kernel) on a 2048x1024 grid with L2
+            flushed before each launch, against the measured HBM copy bandwidth.  The FP64 CG operator is
+            given with its FP64-pipe bound.
+  cpu_baseline  the FP64 CPU restatement of the reference solve (the oracle) on all host cores, timed on the
+            stream's smallest requests (a bounded sample).
+
+`--impl reference` times that CPU restatement alone.  One step is one request from the stream's 128x64 and
+256x128 requests, in stream order.
+Multi-GPU: replicas only.  Each rank serves its own copy of the stream; there is no collective on the data
+path."""
 import argparse
 import json
 import math
@@ -29,14 +42,20 @@ import sys
 import tempfile
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "nunatak.jl_gb300"))
 # concurrent solves use one stream each: 32 hardware work queues instead of 8 (before any CUDA context exists)
 os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 METRIC = "SSA solves/s & p99 latency, mixed vs FP64 on GB300 at <=1e-6 rel velocity error"
-WORKLOAD = ("marine_sheet 256x128 dx=2km (seeded bed + Weertman C), ensemble batch of {B} friction seeds per step, "
-            "Picard reltol 1e-6 x multigrid PCG reltol 1e-8, 4 levels, mixed precision (FP32 multigrid, FP64 outer CG / Picard)")
+WORKLOAD = ("serving stream: 512 marine-sheet SSA solve requests, Poisson arrivals at 200/s, grids uniform over "
+            "128x64 / 256x128 / 512x256 / 1024x512 on 512x256 km, friction seed 1000+k per request; Picard reltol 1e-6 x "
+            "multigrid PCG reltol 1e-8 (coarsest >= 32 cells); mixed precision (FP32 multigrid, FP64 outer CG / Picard); "
+            "steps of {B} consecutive requests")
+N_REQUESTS = 512
+ARRIVAL_RATE = 200.0
 
 
 def parse():
@@ -45,7 +64,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="nunatak", choices=["nunatak", "reference"])
-    ap.add_argument("--batch", type=int, default=32, help="ensemble members solved concurrently per step")
+    ap.add_argument("--batch", type=int, default=32, help="requests per step, and solves in flight at once")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", choices=["solve", "smoother", "operator"], default=None,
                     help="profiling runs for ncu: 'solve' = warm-up solves then one timed solve of the workload; "
@@ -129,6 +148,24 @@ def workload(precision, member=0, grid=(256, 128)):
     return workloads.marine_sheet(grid[0], grid[1], seed=1, seed_friction=1000 + member, precision=precision)
 
 
+def stream_requests(n, batch, steps, warmup):
+    """(warm-up requests, timed requests) of the serving stream: timed steps walk the stream from its start,
+    wrapping after N_REQUESTS; warm-up steps take the batches before the stream's end."""
+    from nunatak_gb300 import workloads
+    stream = workloads.serving_stream(n_requests=n, rate=ARRIVAL_RATE)
+    timed = [stream[k % n] for k in range(steps * batch)]
+    warm = [stream[(n - warmup * batch + k) % n] for k in range(warmup * batch)]
+    return warm, timed
+
+
+def build_cases(requests, precision):
+    """serving_case of every request, built on a thread pool (the FFT filters release the GIL)."""
+    import concurrent.futures as cf
+    from nunatak_gb300 import workloads
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        return list(ex.map(lambda r: workloads.serving_case(r, precision), requests))
+
+
 def cpu_solve(case, threads):
     """One full FP64 solve of the CPU restatement (the oracle) with `threads` OpenMP threads."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -141,34 +178,65 @@ def cpu_solve(case, threads):
     return dt, st, P.get("u"), P.get("v"), used
 
 
+def cpu_sample_requests(n):
+    """The first n requests of the stream with the two smallest grids, in stream order: the bounded CPU sample
+    (a 512x256 or 1024x512 FP64 solve takes minutes on the host cores)."""
+    from nunatak_gb300 import workloads
+    small = [r for r in workloads.serving_stream(n_requests=N_REQUESTS, rate=ARRIVAL_RATE) if r["size"][0] <= 256]
+    return [small[k % len(small)] for k in range(n)]
+
+
 def run_reference(args, rank):
     """`--impl reference`: the reference's CPU path (restated as the FP64 oracle) on all host threads."""
     if rank != 0:
         return
     sys.path.insert(0, ROOT)
     import __graft_entry__
+    from nunatak_gb300 import workloads
     __graft_entry__.build()
     threads = os.cpu_count() or 1
-    case = workload("fp64")
-    for _ in range(args.warmup):
-        cpu_solve(case, threads)
-    times = []
+    reqs = cpu_sample_requests(args.warmup + args.steps)
     used = threads
-    for _ in range(args.steps):
-        dt, st, _, _, used = cpu_solve(case, threads)
+    for r in reqs[:args.warmup]:
+        cpu_solve(workloads.serving_case(r, "fp64"), threads)
+    times = []
+    for r in reqs[args.warmup:]:
+        dt, st, _, _, used = cpu_solve(workloads.serving_case(r, "fp64"), threads)
         times.append(dt)
     total = sum(times)
     value = args.steps / total
+    sizes = sorted({"%dx%d" % r["size"] for r in reqs[args.warmup:]})
+    sample = (f"{args.steps} FP64 solves (oracle restatement of the reference solve, multigrid PCG) of the stream's "
+              f"requests with grids {', '.join(sizes)}, in stream order; one request per step")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded marine ice sheet)",
-            "config": {"workload": WORKLOAD.replace("mixed precision (FP32 multigrid, FP64 outer CG / Picard)", "FP64 throughout"),
-                       "grid": [256, 128]},
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded marine ice sheets)",
+            "config": {"workload": WORKLOAD.format(B=1).replace(
+                "mixed precision (FP32 multigrid, FP64 outer CG / Picard)", "FP64 throughout"), "sample_grids": sizes},
             "latency_ms": {"p50": 1e3 * statistics.median(times), "p99": 1e3 * max(times)},
-            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": used, "kind": "port",
-                             "sample": f"{args.steps} full FP64 solves (oracle restatement of the reference solve)"},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": used, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# FP64 instructions (DADD + DMUL + DFMA) per cell of the operator apply, from the ncu counts of
+# smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on on the 2048x1024 k_apply (12.3 + 18.2 + 7.6).
+FP64_OPERATOR_INSTR_PER_CELL = 38.1
+FP64_INSTR_PER_SM_CLOCK = 2      # GB300 FP64 pipe: 2 thread instructions per SM per clock
+SMS = 152
+
+
+def profile_traffic(name):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from a committed ncu summary's
+    `traffic_bytes_per_launch:` line, or None."""
+    path = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].strip())
+    return None
 
 
 def roofline_problem(nk, workloads, ctx):
@@ -200,6 +268,109 @@ def profile(args, nk, workloads, ctx):
         print(json.dumps({"profile": kernel, "ms_per_launch": ms, "bytes_per_launch": by}))
 
 
+class ResidentPool:
+    """Resident mixed-precision problems keyed by grid size.  A request takes a free problem of its size (or a
+    new one) and gives it back when its solve has finished."""
+
+    def __init__(self, nk, ctx):
+        self.nk, self.ctx, self.free, self.created = nk, ctx, {}, 0
+
+    def take(self, case):
+        lst = self.free.setdefault((case.grid.Nx, case.grid.Ny), [])
+        if lst:
+            return lst.pop()
+        self.created += 1
+        return case.problem(self.nk.Problem, context=self.ctx)
+
+    def give(self, P):
+        self.free[(P.grid.Nx, P.grid.Ny)].append(P)
+
+    def close(self):
+        for lst in self.free.values():
+            for P in lst:
+                P.close()
+        self.free = {}
+
+
+def stage(cases):
+    """Every request's input fields copied to HBM (float64 CUDA tensors), plus zero velocities per grid size."""
+    import torch
+    staged = [{k: torch.from_numpy(np.ascontiguousarray(v, dtype=np.float64)).cuda() for k, v in c.fields.items()}
+              for c in cases]
+    zeros = {}
+    for c in cases:
+        key = (c.grid.Nx, c.grid.Ny)
+        if key not in zeros:
+            nfx, nfy = c.grid.face_count(0), c.grid.face_count(1)
+            zeros[key] = (torch.zeros(c.grid.Ny * nfx, dtype=torch.float64, device="cuda"),
+                          torch.zeros(nfy * c.grid.Nx, dtype=torch.float64, device="cuda"))
+    torch.cuda.synchronize()
+    return staged, zeros
+
+
+def run_resident(pool, cases, staged, zeros, in_flight, keep=()):
+    """Continuous batching of `cases` through resident problems: up to `in_flight` solves on the device, the
+    next request started as soon as a solve finishes.  Inputs come from HBM (set_field from device memory).
+    Returns the per-request stats and the (u, v) of the requests in `keep`."""
+    order = list(range(len(cases)))
+    running, stats, kept = {}, [None] * len(cases), {}
+
+    def start(k):
+        P = pool.take(cases[k])
+        for name, t in staged[k].items():
+            P.set_device(name, t.data_ptr())
+        P.compute_geometry()
+        zu, zv = zeros[(cases[k].grid.Nx, cases[k].grid.Ny)]
+        P.set_device("u", zu.data_ptr())
+        P.set_device("v", zv.data_ptr())
+        P.picard_solve_async()
+        running[id(P)] = (P, k)
+
+    while order or running:
+        while order and len(running) < in_flight:
+            start(order.pop(0))
+        finished = [(P, k) for P, k in running.values() if P.query()]
+        for P, k in finished:
+            stats[k] = P.wait()
+            if k in keep:
+                kept[k] = (P.get("u"), P.get("v"))
+            del running[id(P)]
+            pool.give(P)
+        if not finished:
+            time.sleep(0.0002)
+    return stats, kept
+
+
+def arrival_times(requests):
+    """Arrival of each request in seconds; a wrapped pass of the stream arrives after the previous one."""
+    from nunatak_gb300 import workloads
+    period = workloads.serving_stream(n_requests=N_REQUESTS, rate=ARRIVAL_RATE)[-1]["arrival"] + 1.0 / ARRIVAL_RATE
+    out, passes, last = [], 0, -1
+    for r in requests:
+        if r["index"] <= last:
+            passes += 1
+        last = r["index"]
+        out.append(r["arrival"] + passes * period)
+    return out
+
+
+def run_server(S, cases, arrivals):
+    """Submit each case at its arrival time (host clock), drive the serving loop, collect every result.
+    Returns (throughput solves/s, latencies ms from arrival to result, stats)."""
+    t_host0 = time.perf_counter()
+    t_srv0 = S.clock()
+    tickets = []
+    for case, t in zip(cases, arrivals):
+        while time.perf_counter() - t_host0 < t:
+            S.progress()
+            time.sleep(0.0002)
+        tickets.append(S.submit(case))
+    res = [S.wait(tk) for tk in tickets]
+    done = [r[3][2] - t_srv0 for r in res]
+    lat = [1e3 * (d - t) for d, t in zip(done, arrivals)]
+    return len(cases) / (max(done) - arrivals[0]), lat, [r[2] for r in res]
+
+
 def main():
     args = parse()
     rank, world, local_rank = dist_env()
@@ -228,93 +399,77 @@ def main():
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-
     B = args.batch
-    cases = [workload("mixed", k) for k in range(B)]
-    probs = [c.problem(nk.Problem, context=ctx) for c in cases]
-    zu, zv = np.zeros(probs[0].shape("u")), np.zeros(probs[0].shape("v"))
+    warm_reqs, timed_reqs = stream_requests(N_REQUESTS, B, args.steps, args.warmup)
+    warm_cases = build_cases(warm_reqs, "mixed")
+    cases = build_cases(timed_reqs, "mixed")
+    sizes = sorted({(c.grid.Nx, c.grid.Ny) for c in cases})
+    first_of_size = {}
+    for k, c in enumerate(cases):
+        first_of_size.setdefault((c.grid.Nx, c.grid.Ny), k)
 
-    def batch_step(ps):
-        """Solve every problem of `ps` concurrently from zero; returns (device span ms, per-solve stats)."""
-        for p in ps:
-            p.set("u", zu)
-            p.set("v", zv)
-        flush.random_(0, 255)
-        torch.cuda.synchronize()
-        for p in ps:
-            p.picard_solve_async()
-        st = [p.wait() for p in ps]
-        span = max(x.device_end_ms for x in st) - min(x.device_start_ms for x in st)
-        return span, st
-
-    for _ in range(args.warmup):
-        batch_step(probs)
-
-    # ---- timed region: K batches of B mixed-precision solves on resident inputs ----------------------
-    spans, solves = [], []
+    # ---- value: the timed requests with inputs staged in HBM, continuous batching of B in flight --------------
+    pool = ResidentPool(nk, ctx)
+    w_staged, w_zeros = stage(warm_cases)
+    run_resident(pool, warm_cases, w_staged, w_zeros, B)
+    del w_staged, w_zeros
+    staged, zeros = stage(cases)
     barrier()
+    created0 = pool.created
     launches0 = library.launch_count()
     with ClockSampler(local_rank) as clocks:
         t0 = time.perf_counter()
-        for _ in range(args.steps):
-            span, st = batch_step(probs)
-            spans.append(span)
-            solves.extend(st)
+        stats, kept = run_resident(pool, cases, staged, zeros, B, keep=set(first_of_size.values()))
         barrier()
         wall = time.perf_counter() - t0
     launches = library.launch_count() - launches0
-    busy = sum(spans) / 1e3
+    span_ms = max(x.device_end_ms for x in stats) - min(x.device_start_ms for x in stats)
     if world > 1:
-        t = torch.tensor([busy], device="cuda", dtype=torch.float64)
+        t = torch.tensor([span_ms], device="cuda", dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        busy = float(t.item())
-    value = world * args.steps * B / busy
-    lat = [x.device_ms for x in solves]
-    u_mixed, v_mixed = probs[0].get("u"), probs[0].get("v")
+        span_ms = float(t.item())
+    value = world * len(cases) / (span_ms / 1e3)
+    service = [x.device_end_ms - x.device_start_ms for x in stats]
+    created_timed = pool.created - created0
+    pool.close()
+    del staged, zeros
+    torch.cuda.empty_cache()
 
     if rank != 0:
         if world > 1:
             torch.distributed.barrier()
         return
 
-    # ---- the plain FP64 solver, one solve at a time, on the same members -----------------------------------
-    n64 = min(B, 4)
-    s64 = []
-    P64s = [workload("fp64", k).problem(nk.Problem, context=ctx) for k in range(n64)]
-    for k, P64 in enumerate(P64s):
+    # ---- fp64: the plain FP64 solver one solve at a time, one request of each size ----------------------------
+    fp64_ms, rel_err = {}, {}
+    for key, k in sorted(first_of_size.items()):
+        from nunatak_gb300 import workloads as W
+        P64 = W.serving_case(timed_reqs[k], "fp64").problem(nk.Problem, context=ctx)
+        zu, zv = np.zeros(P64.shape("u")), np.zeros(P64.shape("v"))
+        P64.picard_solve()                  # warm-up: graph capture
         P64.set("u", zu)
         P64.set("v", zv)
-        if k == 0:
-            P64.picard_solve()          # warm-up (graph capture)
-            P64.set("u", zu)
-            P64.set("v", zv)
-        flush.random_(0, 255)
-        torch.cuda.synchronize()
-        s64.append(P64.picard_solve())
-    fp64_value = len(s64) / (sum(x.device_ms for x in s64) / 1e3)
-    u64, v64 = P64s[0].get("u"), P64s[0].get("v")
-    del P64s
+        st = P64.picard_solve()
+        fp64_ms["%dx%d" % key] = st.device_ms
+        um, vm = kept[k]
+        rel_err["%dx%d" % key] = rel_l2(um, vm, P64.get("u"), P64.get("v"))
+        P64.close()
+    count = {"%dx%d" % key: sum(1 for c in cases if (c.grid.Nx, c.grid.Ny) == key) for key in sizes}
+    fp64_value = len(cases) / (sum(count[k] * fp64_ms[k] for k in count) / 1e3)
 
-    # ---- end to end through the serving loop with host buffers --------------------------------------------
+    # ---- e2e: the same requests through the serving loop of the C ABI, host buffers, Poisson arrivals ---------
     from nunatak_gb300.server import Server
-    S = Server(max_in_flight=B, memory_cap_bytes=8 << 30, context=ctx)
-    for c in cases[:2]:
-        S.wait(S.submit(c))             # warm-up: resident problems and their graphs
-    e2e_times, e2e_lat = [], []
-    for _ in range(args.steps):
-        flush.random_(0, 255)
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        tickets = [S.submit(c) for c in cases]
-        res = [S.wait(tk) for tk in tickets]
-        e2e_times.append(time.perf_counter() - t)
-        e2e_lat.extend(1e3 * (r[3][2] - r[3][0]) for r in res)
-    e2e_value = args.steps * B / sum(e2e_times)
+    S = Server(max_in_flight=B, memory_cap_bytes=64 << 30, context=ctx)
+    for c in warm_cases:
+        S.submit(c)
+    S.wait_all()
+    arrivals = arrival_times(timed_reqs)
+    e2e_value, e2e_lat, e2e_stats = run_server(S, cases, arrivals)
     sinfo = S.info()
     S.close()
-    h2d = B * sum(np.asarray(v).nbytes for v in cases[0].fields.values())
-    d2h = B * (zu.nbytes + zv.nbytes)
+    h2d = sum(sum(np.asarray(v).nbytes for v in c.fields.values()) for c in cases) / args.steps
+    d2h = sum(8 * (c.grid.Ny * c.grid.face_count(0) + c.grid.face_count(1) * c.grid.Nx) for c in cases) / args.steps
+    e2e_err = max(abs(a.picard_iterations - b.picard_iterations) for a, b in zip(stats, e2e_stats))
 
     # ---- roofline of the dominant kernel on a grid larger than L2 ---------------------------------------
     peak, peak_kind = measured_peaks()
@@ -325,38 +480,69 @@ def main():
     achieved = sm_bytes / (sm_ms * 1e-3) / 1e9
     del Pb
 
+    piters = [x.picard_iterations for x in stats]
+    citers = [x.linear_iterations_total for x in stats]
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * busy / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 (multigrid) + f64 (CG, Picard)", "data": "synthetic (seeded marine ice sheet, no dataset)",
-        "config": {"workload": WORKLOAD.format(B=B), "grid": [256, 128], "dx_m": 2000.0, "batch": B,
-                   "parallelism": f"replicas{world}", "l2": "flushed between steps (256 MiB write outside the timed events)",
-                   "wall_s": wall},
-        "latency_ms": {"p50": statistics.median(lat), "p99": float(np.percentile(lat, 99)), "max": max(lat),
-                       "note": "per solve, device events; all B members start together"},
-        "picard_iterations": solves[-1].picard_iterations, "cg_iterations_per_solve": solves[-1].linear_iterations_total,
-        "fp64": {"value": fp64_value, "unit": "solves/s", "ms_per_solve": 1e3 / fp64_value, "solves_timed": len(s64),
-                 "mode": "plain FP64 solver (FP64 multigrid PCG), one solve at a time",
-                 "picard_iterations": s64[-1].picard_iterations, "cg_iterations_per_solve": s64[-1].linear_iterations_total},
+        "ms_per_step": span_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (multigrid) + f64 (CG, Picard)", "data": "synthetic (seeded marine ice sheets, no dataset)",
+        "config": {"workload": WORKLOAD.format(B=B), "requests": len(cases), "batch": B, "in_flight": B,
+                   "grids": {k: count[k] for k in count}, "parallelism": f"replicas{world}",
+                   "l2": "not flushed: inputs larger than L2 (up to 32 resident 1024x512 problems in flight)",
+                   "wall_s": wall, "problems_created_in_timed_region": created_timed},
+        "latency_ms": {"p50": statistics.median(service), "p99": float(np.percentile(service, 99)),
+                       "note": "device time of each solve (start to end event) while sharing the GPU with the others"},
+        "picard_iterations": {"min": min(piters), "max": max(piters)},
+        "cg_iterations_per_solve": {"min": min(citers), "max": max(citers)},
+        "fp64": {"value": fp64_value, "unit": "solves/s", "ms_per_solve": fp64_ms,
+                 "mode": "plain FP64 solver (FP64 multigrid PCG) one solve at a time; stream rate from one timed solve "
+                         "of each grid size weighted by the stream's size counts"},
         "speedup_mixed_vs_fp64": value / world / fp64_value,
-        "rel_error_mixed_vs_fp64_gpu": rel_l2(u_mixed, v_mixed, u64, v64),
-        "roofline": {"bound": "hbm", "kernel": "fine-level FP32 l1-Jacobi sweep (k_smooth_point<float>), 2048x1024, L2 flushed",
-                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": None, "bytes_per_launch": sm_bytes, "ms_per_launch": sm_ms,
-                     "operator_fp64": {"ms_per_launch": op_ms, "achieved_gbs": op_bytes / (op_ms * 1e-3) / 1e9}},
+        "speedup_e2e_vs_fp64": e2e_value / fp64_value,
+        "rel_error_mixed_vs_fp64_gpu": rel_err,
+        "roofline": None,
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "latency_ms": {"p50": statistics.median(e2e_lat), "p99": float(np.percentile(e2e_lat, 99))},
+                "latency_ms": {"p50": statistics.median(e2e_lat), "p99": float(np.percentile(e2e_lat, 99)),
+                               "note": "arrival (Poisson, 200/s) to result on the host"},
                 "path": "nk_server_submit / nk_server_wait (host inputs, upload, geometry, solve, read-back)",
-                "server": sinfo},
+                "picard_iteration_mismatch_vs_resident": e2e_err, "server": sinfo},
         "clocks": clocks.summary(),
         "gpu_launches": int(launches),
     }
+
+    # ---- roofline of the most frequent kernel on a grid larger than L2 ----------------------------------------
+    peak, peak_kind = measured_peaks()
+    Pb = roofline_problem(nk, workloads, ctx)
+    Pb.time_kernel("smoother", repeats=3, flush_bytes=0)
+    sm_ms, sm_bytes = Pb.time_kernel("smoother", repeats=20, flush_bytes=512 << 20)
+    op_ms, op_bytes = Pb.time_kernel("operator_fp64", repeats=20, flush_bytes=512 << 20)
+    Pb.close()
+    achieved = sm_bytes / (sm_ms * 1e-3) / 1e9
+    sm_mhz = line["clocks"].get("sm_mhz") or 2070.0
+    fp64_rate = FP64_OPERATOR_INSTR_PER_CELL * 2048 * 1024 / (op_ms * 1e-3) / 1e9
+    fp64_peak = FP64_INSTR_PER_SM_CLOCK * SMS * sm_mhz * 1e6 / 1e9
+    line["roofline"] = {
+        "bound": "hbm", "kernel": "fine-level FP32 l1-Jacobi sweep (k_smooth_point<float>), 2048x1024, L2 flushed",
+        "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+        "traffic": profile_traffic("smoother_fp32_2048x1024.md"), "bytes_per_launch": sm_bytes, "ms_per_launch": sm_ms,
+        "operator_fp64": {"kernel": "k_apply (FP64 operator, 2048x1024, L2 flushed)", "ms_per_launch": op_ms,
+                          "achieved_gbs": op_bytes / (op_ms * 1e-3) / 1e9, "bound": "fp64 pipe",
+                          "fp64_ginstr_per_s": fp64_rate, "fp64_peak_ginstr_per_s": fp64_peak, "frac": fp64_rate / fp64_peak,
+                          "traffic": profile_traffic("operator_fp64_2048x1024.md")}}
     if not args.no_cpu_baseline:
-        dt, st, uo, vo, used = cpu_solve(workload("fp64", 0), os.cpu_count() or 1)
-        line["cpu_baseline"] = {"value": 1.0 / dt, "unit": "solves/s", "cores": used, "kind": "port",
-                                "sample": "one full FP64 solve of the same workload (oracle restatement, multigrid PCG)"}
-        line["rel_error_vs_fp64_oracle"] = rel_l2(u_mixed, v_mixed, uo, vo)
-        line["fp64_rel_error_vs_fp64_oracle"] = rel_l2(u64, v64, uo, vo)
+        from nunatak_gb300 import workloads as W
+        reqs = cpu_sample_requests(2)
+        total, used, errs = 0.0, 1, {}
+        for r in reqs:
+            dt, st, uo, vo, used = cpu_solve(W.serving_case(r, "fp64"), os.cpu_count() or 1)
+            total += dt
+            for k, tr in enumerate(timed_reqs):
+                if tr["index"] == r["index"] and k in kept:
+                    errs[str(r["index"])] = rel_l2(kept[k][0], kept[k][1], uo, vo)
+        line["cpu_baseline"] = {"value": len(reqs) / total, "unit": "solves/s", "cores": used, "kind": "port",
+                                "sample": "FP64 solves of the stream's first 128x64 and first 256x128 requests "
+                                          "(oracle restatement, multigrid PCG, OpenMP on all host cores)"}
+        line["rel_error_mixed_vs_fp64_oracle"] = errs
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.barrier()

@@ -213,9 +213,10 @@ nk_status nk_problem_create(nk_context* ctx, const nk_grid_desc* grid, const nk_
                             const nk_solver_desc* solver, nk_problem** out);
 nk_status nk_problem_destroy(nk_problem* problem);
 
-/* Copy a host array in interior layout into a field (set!(field, array) + fill_halo_regions!). */
+/* Copy an array in interior layout into a field (set!(field, array) + fill_halo_regions!).  The array may be in
+ * host memory or in device memory of the problem's device (unified addressing). */
 nk_status nk_problem_set_field(nk_problem* problem, int32_t field, const double* host, int64_t count);
-/* Copy a field out in interior layout. */
+/* Copy a field out in interior layout, to host memory or to device memory of the problem's device. */
 nk_status nk_problem_get_field(const nk_problem* problem, int32_t field, double* host, int64_t count);
 /* Number of values of a field in interior layout (0 for an unknown id). */
 int64_t   nk_problem_field_size(const nk_problem* problem, int32_t field);
@@ -262,6 +263,9 @@ nk_status nk_picard_solve(nk_problem* problem, nk_solve_stats* stats);
  * statistics (the status of the solve is the return value, as for nk_picard_solve). */
 nk_status nk_picard_solve_async(nk_problem* problem);
 nk_status nk_problem_wait(nk_problem* problem, nk_solve_stats* stats);
+/* Without blocking: *done = 1 when the pending asynchronous solve has finished (nk_problem_wait then returns at
+ * once), 0 while it runs. */
+nk_status nk_problem_query(nk_problem* problem, int32_t* done);
 
 /* The whole update_velocities! body for host callers: copies u, v (warm start) in, runs
  * nk_picard_solve and copies u, v out.  u, v in interior layout. */

@@ -924,7 +924,7 @@ static FieldLoc field_loc(nk_problem* P, int id) {
 
 static void copy_in(nk_problem* P, const FieldLoc& f, const double* host) {
     size_t n = (size_t)f.nx * f.ny * f.planes;
-    NK_CUDA(cudaMemcpyAsync(P->staging, host, n * sizeof(double), cudaMemcpyHostToDevice, P->stream));
+    NK_CUDA(cudaMemcpyAsync(P->staging, host, n * sizeof(double), cudaMemcpyDefault, P->stream));   // host or device source
     launch_pack(f.base, P->pitch, (int)P->plane, f.stride, f.offset, P->staging, f.nx, f.ny, f.planes, P->stream);
     NK_CHECK_LAUNCH();
 }
@@ -932,7 +932,7 @@ static void copy_out(nk_problem* P, const FieldLoc& f, double* host) {
     size_t n = (size_t)f.nx * f.ny * f.planes;
     launch_unpack(P->staging, f.base, P->pitch, (int)P->plane, f.stride, f.offset, f.nx, f.ny, f.planes, P->stream);
     NK_CHECK_LAUNCH();
-    NK_CUDA(cudaMemcpyAsync(host, P->staging, n * sizeof(double), cudaMemcpyDeviceToHost, P->stream));
+    NK_CUDA(cudaMemcpyAsync(host, P->staging, n * sizeof(double), cudaMemcpyDefault, P->stream));   // host or device target
     NK_CUDA(cudaStreamSynchronize(P->stream));
 }
 // a velocity vector (u part, v part) from host arrays into a pair buffer
@@ -1244,6 +1244,20 @@ nk_status nk_picard_solve_async(nk_problem* P) {
         NK_CUDA(cudaMemcpyAsync(P->sc_host, P->sc, sizeof(SolverScalars), cudaMemcpyDeviceToHost, P->stream));
         NK_CUDA(cudaEventRecord(P->ev1, P->stream));
         P->async_pending = true;
+    });
+}
+
+nk_status nk_problem_query(nk_problem* P, int32_t* done) {
+    if (!P || !done) return NK_BAD_ARGUMENT;
+    return guarded(P->ctx, [&] {
+        if (!P->async_pending) bad("no asynchronous solve pending");
+        cudaError_t e = cudaEventQuery(P->ev1);
+        if (e == cudaErrorNotReady) {
+            *done = 0;
+            return;
+        }
+        NK_CUDA(e);
+        *done = 1;
     });
 }
 

@@ -102,6 +102,13 @@ class Problem:
         st = self._fn("problem_set_field")(self._h, abi.FIELD_IDS[name], a.ctypes.data_as(_dptr), C.c_int64(a.size))
         _check(st, f"set {name}", self._err())
 
+    def set_device(self, name, address):
+        """set!(field, array) from a contiguous float64 array in device memory (its address, e.g. a CUDA
+        tensor's data_ptr()) in interior layout of shape self.shape(name)."""
+        n = int(np.prod(self.shape(name)))
+        st = self._fn("problem_set_field")(self._h, abi.FIELD_IDS[name], C.cast(C.c_void_p(int(address)), _dptr), C.c_int64(n))
+        _check(st, f"set {name}", self._err())
+
     def get(self, name):
         out = np.empty(self.shape(name), dtype=np.float64)
         st = self._fn("problem_get_field")(self._h, abi.FIELD_IDS[name], out.ctypes.data_as(_dptr), C.c_int64(out.size))
@@ -175,6 +182,12 @@ class Problem:
     def picard_solve_async(self):
         """Enqueue picard_solve! on this problem's stream and return at once (see wait())."""
         _check(self._fn("picard_solve_async")(self._h), "picard_solve_async", self._err())
+
+    def query(self):
+        """True once the asynchronous solve has finished (wait() then returns at once)."""
+        d = C.c_int32()
+        _check(self._fn("problem_query")(self._h, C.byref(d)), "problem_query", self._err())
+        return bool(d.value)
 
     def wait(self):
         """Block until the asynchronous solve has finished; returns its stats."""

@@ -11,6 +11,8 @@ Units are SI with a year of 31556926 s."""
 from dataclasses import dataclass, field
 from typing import Callable, Dict, Optional
 
+import functools
+
 import numpy as np
 
 from . import model as M
@@ -18,11 +20,23 @@ from . import model as M
 YEAR = M.YEAR
 
 
+def _gaussian_reflect(a, sigma, truncate=4.0):
+    """Gaussian filter of a 2-D array with reflected edges (scipy.ndimage.gaussian_filter, mode "reflect", the
+    same truncated kernel) evaluated as two FFT convolutions of the padded array."""
+    from scipy.signal import fftconvolve
+    r = int(truncate * float(sigma) + 0.5)
+    x = np.arange(-r, r + 1, dtype=np.float64)
+    k = np.exp(-0.5 * (x / sigma) ** 2)
+    k /= k.sum()
+    p = np.pad(a, r, mode="symmetric")
+    p = fftconvolve(p, k[None, :], mode="valid", axes=1)
+    return fftconvolve(p, k[:, None], mode="valid", axes=0)
+
+
 def random_field(shape, seed, correlation_cells):
     """Smoothed, renormalised standard normal field of shape (ny, nx)."""
-    from scipy.ndimage import gaussian_filter
     g = np.random.default_rng(seed).standard_normal(shape)
-    g = gaussian_filter(g, sigma=correlation_cells, mode="reflect")
+    g = _gaussian_reflect(g, correlation_cells)
     g = g - g.mean()
     s = g.std()
     return g / s if s > 0 else g
@@ -59,6 +73,14 @@ class Case:
         return self.grid.Nx * self.grid.Ny
 
 
+@functools.lru_cache(maxsize=16)
+def _bed_field(ny, nx, seed, correlation_cells):
+    """random_field of the bed, shared by every case of one grid and seed (read-only)."""
+    g = random_field((ny, nx), seed, correlation_cells)
+    g.setflags(write=False)
+    return g
+
+
 def _centers(grid):
     return np.meshgrid(grid.centers(0), grid.centers(1))
 
@@ -88,7 +110,7 @@ def marine_sheet(Nx=256, Ny=128, seed=1, seed_friction=None, Lx=512e3, Ly=256e3,
     grid = M.RectilinearGrid(size=(Nx, Ny), x=(0.0, Lx), y=(0.0, Ly), halo=(4, 4))
     dx = Lx / Nx
     X, _ = _centers(grid)
-    g = random_field((Ny, Nx), seed, 20e3 / dx)
+    g = _bed_field(Ny, Nx, seed, 20e3 / dx)
     xi = random_field((Ny, Nx), seed + 7919 if seed_friction is None else seed_friction, 20e3 / dx)
     bed = -100.0 - 600.0 * X / 512e3 + 50.0 * g
     H = 2000.0 * np.sqrt(np.maximum(0.0, 1.0 - (X / 420e3) ** 2))
@@ -115,6 +137,12 @@ def serving_stream(n_requests=512, rate=200.0, seed=11, base_seed=1000):
     sizes = rng.integers(len(SERVING_SIZES), size=n_requests)
     return [dict(index=k, arrival=float(arrivals[k]), size=SERVING_SIZES[int(sizes[k])], seed_friction=base_seed + k)
             for k in range(n_requests)]
+
+
+def serving_case(request, precision="mixed"):
+    """The marine-sheet Case of one serving_stream request."""
+    nx, ny = request["size"]
+    return marine_sheet(nx, ny, seed=1, seed_friction=request["seed_friction"], precision=precision)
 
 
 def diva_sheet(Nx=2048, Ny=1024, seed=3, dx=1e3, velocity_solver=None, precision="fp64", Nsigma=10):
