@@ -258,6 +258,18 @@ nk_status nk_adjoint_solve(nk_problem* problem, const double* bu, const double* 
  * fields: x = (U, V) warm start, b = (TAU_U, TAU_V).  Updates U, V and every coefficient field. */
 nk_status nk_picard_solve(nk_problem* problem, nk_solve_stats* stats);
 
+/* Fixed-point adjoint of a converged picard_solve! (the Enzyme reverse rule of ext/NunatakEnzymeExt.jl:167-240,
+ * Christianson 1994) for the SSA with Weertman or regularised-Coulomb friction.  x* = (U, V) is the problem's
+ * converged velocity and x̄ = (ubar, vbar) = ∂J/∂x* in the interior layout of U, V.  The coefficients are
+ * refreshed to c(x*), then λ ← A⁻¹ (x̄ - (∂[A(c(x)) x*]/∂x)ᵀ λ) is iterated from λ = 0, each step one
+ * preconditioned CG solve of the problem's linear control warm-started from λ, until
+ * ‖λ⁺ - λ‖ ≤ max(reltol ‖λ⁺‖, abstol) (control; NULL = the problem's Picard control).  Returns λ = ∂J/∂τ
+ * (lambda_u, lambda_v, same layout as U, V) and ∂J/∂log C per cell (grad_log_C, Nx x Ny); any output may be
+ * NULL.  stats: picard_iterations = adjoint iterations, picard_change = ‖λ⁺ - λ‖, picard_norm = ‖λ‖,
+ * status NK_NOT_CONVERGED when maxiter ended it.  U, V are left at x*. */
+nk_status nk_picard_adjoint(nk_problem* problem, const double* ubar, const double* vbar, const nk_iteration_control* control,
+                            double* lambda_u, double* lambda_v, double* grad_log_C, nk_solve_stats* stats);
+
 /* picard_solve! enqueued on the problem's stream without waiting (one CUDA-graph launch); independent problems
  * solved this way run concurrently on the device.  nk_problem_wait blocks until it has finished and returns its
  * statistics (the status of the solve is the return value, as for nk_picard_solve). */

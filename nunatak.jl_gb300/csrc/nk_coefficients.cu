@@ -404,4 +404,299 @@ void launch_rate_factor(const DevGrid<double>& g, const SigmaTable& sig, int pla
     k_rate_factor<<<d.grid, d.block, 0, s>>>(g, sig, plane, H, T, A, rho_i, gacc, params); count_launch();
 }
 
+// ---- fixed-point adjoint of the SSA Picard step -------------------------------------------------------------
+// The reverse of picard_coefficient_step! (ext/NunatakEnzymeExt.jl:142-157): with q = A(c(x)) x*, the seed
+// q̄ = -λ, and x* the converged velocity, it returns ȳ = -(∂q/∂x)ᵀ λ.  Only active operator rows depend on
+// the coefficients (inactive rows are identities), so λ enters as λ̃ = λ masked like the operator's
+// interior_u / interior_v.  The chain runs back through _compute_basal_drag!, _interpolate_to_corners! and
+// compute_viscosity! exactly as they are evaluated in the forward kernels above.
+
+// basal_drag and its derivatives with respect to the speed U and the face coefficient C (frictions.jl:83-89)
+__device__ __forceinline__ void basal_drag_derivatives(const PhysView& ph, double U, double C, double N, double& b, double& dbdU,
+                                                       double& dbdC) {
+    double pw = pow(U, ph.m - 1);
+    double w = C * pw;
+    if (ph.friction == NK_WEERTMAN) {
+        b = w;
+        dbdU = (ph.m - 1) * w / U;
+        dbdC = pw;
+        return;
+    }
+    double tc = ph.alpha2 * N;
+    double cm = pow(C, 1 / ph.m), den = cm * U + pow(tc, 1 / ph.m);
+    b = w * tc / pow(den, ph.m);
+    if (b == 0.0) {
+        dbdU = 0.0;
+        dbdC = 0.0;
+        return;
+    }
+    dbdU = b * ((ph.m - 1) / U - ph.m * cm / den);
+    dbdC = b * (1 / C - cm * U / (C * den));
+}
+
+// Speed and drag of the u face (i, j) as k_basal_drag evaluates them; returns false where βᵘ is zero or absent.
+__device__ __forceinline__ bool u_drag(const PhysView& ph, const double2* __restrict__ x, int i, int j, double& u, double& vf,
+                                       double& U, double& phi, double& b, double& dbdU, double& dbdC) {
+    const DevGrid<double>& g = ph.g;
+    if (ph.friction == NK_FRICTION_NONE || j >= g.Ny || (i >= g.Nx && g.px) || g.peripheral_fc(i, j)) return false;
+    int k = g.idx(i, j);
+    vf = ((x[g.v_idx(i - 1, j)].y + x[g.v_idx(i, j)].y) / 2 + (x[g.v_idx(i - 1, j + 1)].y + x[g.v_idx(i, j + 1)].y) / 2) / 2;
+    u = x[k].x;
+    U = sqrt(u * u + vf * vf + ph.u0 * ph.u0);
+    double Cf = (ph.C[g.c_idx(i - 1, j)] + ph.C[g.c_idx(i, j)]) / 2;
+    double Nf = ph.use_N ? (ph.N[g.c_idx(i - 1, j)] + ph.N[g.c_idx(i, j)]) / 2 : 0.0;
+    phi = ph.phi[k].x;
+    basal_drag_derivatives(ph, U, Cf, Nf, b, dbdU, dbdC);
+    return true;
+}
+__device__ __forceinline__ bool v_drag(const PhysView& ph, const double2* __restrict__ x, int i, int j, double& v, double& uf,
+                                       double& U, double& phi, double& b, double& dbdU, double& dbdC) {
+    const DevGrid<double>& g = ph.g;
+    if (ph.friction == NK_FRICTION_NONE || i >= g.Nx || (j >= g.Ny && g.py) || g.peripheral_cf(i, j)) return false;
+    int k = g.idx(i, j);
+    uf = ((x[g.u_idx(i, j - 1)].x + x[g.u_idx(i + 1, j - 1)].x) / 2 + (x[g.u_idx(i, j)].x + x[g.u_idx(i + 1, j)].x) / 2) / 2;
+    v = x[k].y;
+    U = sqrt(v * v + uf * uf + ph.u0 * ph.u0);
+    double Cf = (ph.C[g.c_idx(i, j - 1)] + ph.C[g.c_idx(i, j)]) / 2;
+    double Nf = ph.use_N ? (ph.N[g.c_idx(i, j - 1)] + ph.N[g.c_idx(i, j)]) / 2 : 0.0;
+    phi = ph.phi[k].y;
+    basal_drag_derivatives(ph, U, Cf, Nf, b, dbdU, dbdC);
+    return true;
+}
+
+// Coefficient adjoints from λ̃ and x*: at centre (i, j) ∂(λ̃ᵀq)/∂η̄H through Δy Txx and Δx Tyy; at corner (i, j)
+// ∂(λ̃ᵀq)/∂η̄Hᶠᶠ through the shear stress; at faces ∂(λ̃ᵀq)/∂β = λ̃ Az x* (ssa_operator.jl:60-89).
+__global__ void k_adjoint_coefficients(AdjointView v) {
+    const OpView<double>& o = v.o;
+    const DevGrid<double>& g = o.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i > g.Nx || j > g.Ny) return;
+    int k = g.idx(i, j);
+    double2 cb = make_double2(0.0, 0.0), bb = make_double2(0.0, 0.0);
+    if (i < g.Nx && j < g.Ny) {
+        double exx = (masked_u(o, v.xs, i + 1, j) - masked_u(o, v.xs, i, j)) * g.rdxc[i];
+        double eyy = (masked_v(o, v.xs, i, j + 1) - masked_v(o, v.xs, i, j)) * g.rdyc[j];
+        double dlu = masked_u(o, v.lam, i + 1, j) - masked_u(o, v.lam, i, j);
+        double dlv = masked_v(o, v.lam, i, j + 1) - masked_v(o, v.lam, i, j);
+        cb.x = g.dyc[j] * (2.0 * (2.0 * exx + eyy)) * dlu + g.dxc[i] * (2.0 * (2.0 * eyy + exx)) * dlv;
+    }
+    {
+        double dudy = (masked_u(o, v.xs, i, j) - masked_u(o, v.xs, i, j - 1)) * g.rdyf[j];
+        double dvdx = (masked_v(o, v.xs, i, j) - masked_v(o, v.xs, i - 1, j)) * g.rdxf[i];
+        double e = (dudy + dvdx) / 2;
+        if (g.peripheral_ff(i, j)) e = o.wall_factor * e;
+        double lu = masked_u(o, v.lam, i, j) - masked_u(o, v.lam, i, j - 1);
+        double lv = masked_v(o, v.lam, i, j) - masked_v(o, v.lam, i - 1, j);
+        cb.y = 2.0 * e * (g.dxf[i] * lu + g.dyf[j] * lv);
+    }
+    bool has_u = j < g.Ny && (i < g.Nx || !g.px), has_v = i < g.Nx && (j < g.Ny || !g.py);
+    uint8_t m = o.mask[k];
+    if (has_u && !(m & U_INACTIVE)) bb.x = v.lam[k].x * g.Az_fc(i, j) * v.xs[k].x;
+    if (has_v && !(m & V_INACTIVE)) bb.y = v.lam[k].y * g.Az_cf(i, j) * v.xs[k].y;
+    v.cbar[k] = cb;
+    v.bbar[k] = bb;
+}
+void launch_adjoint_coefficients(const AdjointView& v, cudaStream_t s) {
+    LaunchDims d = dims2d(v.o.g.Nx + 1, v.o.g.Ny + 1);
+    k_adjoint_coefficients<<<d.grid, d.block, 0, s>>>(v); count_launch();
+}
+
+// The distinct corner indices around centre index c along one axis, with the number of times _interpolate_to_corners!
+// reads centre c for each (its clamped / wrapped index map can hit c twice).
+__device__ __forceinline__ int corners_of_centre(int c, int n, bool periodic, int* f, int* w) {
+    int a = c, b = periodic ? DevGrid<double>::wrap(c + 1, n) : c + 1;
+    auto cmap = [&](int i) { return periodic ? DevGrid<double>::wrap(i, n) : DevGrid<double>::clampi(i, 0, n - 1); };
+    f[0] = a;
+    w[0] = (cmap(a - 1) == c) + (cmap(a) == c);
+    if (b == a) return 1;
+    f[1] = b;
+    w[1] = (cmap(b - 1) == c) + (cmap(b) == c);
+    return 2;
+}
+
+// Per centre: η̄H̄ = the centre-stress part + ¼ of the corner adjoints that _interpolate_to_corners! spreads from
+// it; then back through η̄H = μ H Σₖ Δζₖ ½ Aₖ^(-1/n) S^((1-n)/2n), S = ε̇ₑ² + ε̇₀²: ḡ = η̄H̄ η̄H (1-n)/(2n) / S.
+__global__ void k_adjoint_viscosity(AdjointView v) {
+    const DevGrid<double>& g = v.o.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int k = g.idx(i, j);
+    int fx[2], wx[2], fy[2], wy[2];
+    int nx = corners_of_centre(i, g.Nx, g.px, fx, wx), ny = corners_of_centre(j, g.Ny, g.py, fy, wy);
+    double eb = v.cbar[k].x;
+    for (int a = 0; a < nx; ++a)
+        for (int b = 0; b < ny; ++b) eb += (wx[a] * wy[b]) * v.cbar[g.idx(fx[a], fy[b])].y / 4;
+    const PhysView& ph = v.ph;
+    double S = effective_strain_rate2(g, v.xs, i, j, ph.wall_factor) + ph.eps0 * ph.eps0;
+    v.gbar[k] = eb * v.o.coef[k].x * ((1 - ph.n) / (2 * ph.n)) / S;
+}
+void launch_adjoint_viscosity(const AdjointView& v, cudaStream_t s) {
+    LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
+    k_adjoint_viscosity<<<d.grid, d.block, 0, s>>>(v); count_launch();
+}
+
+// Map a candidate index to a stored one (wrap when periodic); false when it is outside a Bounded range [0, hi).
+__device__ __forceinline__ bool map_index(int i, int n, bool periodic, int hi, int& out) {
+    if (periodic) {
+        out = DevGrid<double>::wrap(i, n);
+        return true;
+    }
+    out = i;
+    return i >= 0 && i < hi;
+}
+// Append `k` to a short list unless already there (tiny periodic grids map two candidates to one point).
+__device__ __forceinline__ bool first_time(int* seen, int& n, int k) {
+    for (int a = 0; a < n; ++a)
+        if (seen[a] == k) return false;
+    seen[n++] = k;
+    return true;
+}
+
+// ∂S/∂(u or v at stored index k) for the centre (ci, cj): S = ε̇xx² + ε̇yy² + ε̇xx ε̇yy + ℑxyᶜᶜ(ε̇xy²) with the
+// wall-masked velocities of effective_strain_rate2; `comp` 0 = u, 1 = v.  Every reference to the velocity is
+// matched through the same index maps and masks as the forward evaluation.
+__device__ double strain_sensitivity(const DevGrid<double>& g, const double2* __restrict__ x, double wf, int ci, int cj, int k, int comp) {
+    auto uref = [&](int a, int b) { return !g.peripheral_fc(a, b) && g.u_idx(a, b) == k; };
+    auto vref = [&](int a, int b) { return !g.peripheral_cf(a, b) && g.v_idx(a, b) == k; };
+    double exx = (wall_u(g, x, ci + 1, cj) - wall_u(g, x, ci, cj)) * g.rdxc[ci];
+    double eyy = (wall_v(g, x, ci, cj + 1) - wall_v(g, x, ci, cj)) * g.rdyc[cj];
+    double d = 0.0;
+    if (comp == 0) d += (2 * exx + eyy) * g.rdxc[ci] * ((double)uref(ci + 1, cj) - (double)uref(ci, cj));
+    else d += (2 * eyy + exx) * g.rdyc[cj] * ((double)vref(ci, cj + 1) - (double)vref(ci, cj));
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b) {
+            int fi = ci + a, fj = cj + b;
+            double e = strain_xy(g, x, fi, fj, wf);
+            double sf = g.peripheral_ff(fi, fj) ? wf : 1.0;
+            double de = comp == 0 ? sf / 2 * g.rdyf[fj] * ((double)uref(fi, fj) - (double)uref(fi, fj - 1))
+                                  : sf / 2 * g.rdxf[fi] * ((double)vref(fi, fj) - (double)vref(fi - 1, fj));
+            d += e / 2 * de;   // ∂(¼ Σ e²)/∂e = e / 2
+        }
+    return d;
+}
+
+// r = x̄ + ȳ with ȳ = -(∂[A(c(x)) x*]/∂x)ᵀ λ, gathered per velocity point from the centres whose strain rates
+// read it (viscosity) and the faces whose speed reads it (drag).
+__global__ void k_adjoint_velocity(AdjointView v) {
+    const PhysView& ph = v.ph;
+    const DevGrid<double>& g = v.o.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i > g.Nx || j > g.Ny) return;
+    int k = g.idx(i, j);
+    bool has_u = j < g.Ny && (i < g.Nx || !g.px), has_v = i < g.Nx && (j < g.Ny || !g.py);
+    double ub = 0.0, vb = 0.0;
+    double u, vf, U, phi, b, dbdU, dbdC;
+    for (int comp = 0; comp < 2; ++comp) {
+        if (comp == 0 ? !has_u : !has_v) continue;
+        double acc = 0.0;
+        // viscosity: centres ci in i-1..i (u) or i-1..i+1 (v), cj in j-1..j+1 (u) or j-1..j (v)
+        int seen[6], ns = 0;
+        int ilo = i - 1, ihi = comp == 0 ? i : i + 1, jlo = j - 1, jhi = comp == 0 ? j + 1 : j;
+        for (int a = ilo; a <= ihi; ++a)
+            for (int b2 = jlo; b2 <= jhi; ++b2) {
+                int ci, cj;
+                if (!map_index(a, g.Nx, g.px, g.Nx, ci) || !map_index(b2, g.Ny, g.py, g.Ny, cj)) continue;
+                int c = g.idx(ci, cj);
+                if (!first_time(seen, ns, c)) continue;
+                double gb = v.gbar[c];
+                if (gb != 0.0) acc += gb * strain_sensitivity(g, v.xs, ph.wall_factor, ci, cj, k, comp);
+            }
+        // drag of the point itself
+        if (comp == 0 && u_drag(ph, v.xs, i, j, u, vf, U, phi, b, dbdU, dbdC)) acc += v.bbar[k].x * phi * dbdU * u / U;
+        if (comp == 1 && v_drag(ph, v.xs, i, j, u, vf, U, phi, b, dbdU, dbdC)) acc += v.bbar[k].y * phi * dbdU * u / U;
+        // drag of the faces of the other component whose ℑxy average reads this point
+        int fseen[4], nf = 0;
+        for (int a = (comp == 0 ? i - 1 : i); a <= (comp == 0 ? i : i + 1); ++a)
+            for (int b2 = (comp == 0 ? j : j - 1); b2 <= (comp == 0 ? j + 1 : j); ++b2) {
+                int fi, fj;
+                if (comp == 0) {
+                    if (!map_index(a, g.Nx, g.px, g.Nx, fi) || !map_index(b2, g.Ny, g.py, g.Ny + 1, fj)) continue;
+                } else {
+                    if (!map_index(a, g.Nx, g.px, g.Nx + 1, fi) || !map_index(b2, g.Ny, g.py, g.Ny, fj)) continue;
+                }
+                int kf = g.idx(fi, fj);
+                if (!first_time(fseen, nf, kf)) continue;
+                double w, avg, Uf, phif, bf, dUf, dCf;
+                int m;
+                if (comp == 0) {
+                    if (!v_drag(ph, v.xs, fi, fj, w, avg, Uf, phif, bf, dUf, dCf)) continue;
+                    m = (g.u_idx(fi, fj - 1) == k) + (g.u_idx(fi + 1, fj - 1) == k) + (g.u_idx(fi, fj) == k) + (g.u_idx(fi + 1, fj) == k);
+                    acc += v.bbar[kf].y * phif * dUf * avg / Uf * (m / 4.0);
+                } else {
+                    if (!u_drag(ph, v.xs, fi, fj, w, avg, Uf, phif, bf, dUf, dCf)) continue;
+                    m = (g.v_idx(fi - 1, fj) == k) + (g.v_idx(fi, fj) == k) + (g.v_idx(fi - 1, fj + 1) == k) + (g.v_idx(fi, fj + 1) == k);
+                    acc += v.bbar[kf].x * phif * dUf * avg / Uf * (m / 4.0);
+                }
+            }
+        if (comp == 0) ub = acc; else vb = acc;
+    }
+    double2 xb = v.xbar[k];
+    v.r[k] = make_double2(xb.x - ub, xb.y - vb);
+}
+void launch_adjoint_velocity(const AdjointView& v, cudaStream_t s) {
+    LaunchDims d = dims2d(v.o.g.Nx + 1, v.o.g.Ny + 1);
+    k_adjoint_velocity<<<d.grid, d.block, 0, s>>>(v); count_launch();
+}
+
+// ∂J/∂log C = -C λ̃ᵀ ∂[A(c) x*]/∂C: each face coefficient is the mean of the two cells beside it (frictions.jl:142-160).
+__global__ void k_adjoint_gradient(AdjointView v) {
+    const PhysView& ph = v.ph;
+    const DevGrid<double>& g = v.o.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int k = g.idx(i, j);
+    double acc = 0.0, w, avg, U, phi, b, dbdU, dbdC;
+    int seen[2], n = 0;
+    for (int a = i; a <= i + 1; ++a) {
+        int fi;
+        if (!map_index(a, g.Nx, g.px, g.Nx + 1, fi)) continue;
+        int kf = g.idx(fi, j);
+        if (!first_time(seen, n, kf) || !u_drag(ph, v.xs, fi, j, w, avg, U, phi, b, dbdU, dbdC)) continue;
+        int m = (g.c_idx(fi - 1, j) == k) + (g.c_idx(fi, j) == k);
+        acc += v.bbar[kf].x * phi * dbdC * (m / 2.0);
+    }
+    n = 0;
+    for (int b2 = j; b2 <= j + 1; ++b2) {
+        int fj;
+        if (!map_index(b2, g.Ny, g.py, g.Ny + 1, fj)) continue;
+        int kf = g.idx(i, fj);
+        if (!first_time(seen, n, kf) || !v_drag(ph, v.xs, i, fj, w, avg, U, phi, b, dbdU, dbdC)) continue;
+        int m = (g.c_idx(i, fj - 1) == k) + (g.c_idx(i, fj) == k);
+        acc += v.bbar[kf].y * phi * dbdC * (m / 2.0);
+    }
+    v.grad_log_C[k] = -ph.C[k] * acc;
+}
+void launch_adjoint_gradient(const AdjointView& v, cudaStream_t s) {
+    LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
+    k_adjoint_gradient<<<d.grid, d.block, 0, s>>>(v); count_launch();
+}
+
+// Picard-adjoint progress (ext/NunatakEnzymeExt.jl:216-220): Δ = ‖λ⁺ - λ‖, M = ‖λ⁺‖ over the solved cells, then
+// λ = λ⁺ over every stored point.
+__global__ void k_adjoint_change(DevGrid<double> g, const double2* __restrict__ lam_new, double2* lam, SolverScalars* sc,
+                                 double2* partials) {
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    double dd = 0.0, ll = 0.0;
+    if (i <= g.Nx && j <= g.Ny) {
+        int k = g.idx(i, j);
+        double2 a = lam_new[k], b = lam[k];
+        if (i < g.Nx && j < g.Ny) {
+            double dx = a.x - b.x, dy = a.y - b.y;
+            dd = dx * dx + dy * dy;
+            ll = a.x * a.x + a.y * a.y;
+        }
+        lam[k] = a;
+    }
+    double tdd, tll;
+    if (grid_sum2(dd, ll, partials, &sc->ticket, tdd, tll) && threadIdx.x == 0 && threadIdx.y == 0) {
+        sc->p_D = sqrt(tdd);
+        sc->p_X = sqrt(tll);
+    }
+}
+void launch_adjoint_change(const DevGrid<double>& g, const double2* lam_new, double2* lam, SolverScalars* sc, double2* partials,
+                           cudaStream_t s) {
+    LaunchDims d = dims2d(g.Nx + 1, g.Ny + 1);
+    k_adjoint_change<<<d.grid, d.block, 0, s>>>(g, lam_new, lam, sc, partials); count_launch();
+}
+
 }  // namespace nk

@@ -99,8 +99,16 @@ struct SolverScalars {
     // Picard (picard.jl:63-90), evaluated on the device between the conjugate-gradient solves
     double p_reltol, p_abstol, p_D, p_X;
     int p_fixed, p_iterations, p_maxiter, p_it;
-    int p_done, it_total, cg_unconverged, pad;
+    int p_done, it_total, cg_unconverged;
+    int r32_exp;                   // mixed precision: r32 = r 2^-r32_exp, z = z32 2^r32_exp (keeps FP32 values near 1)
 };
+
+// Binary exponent that brings a residual of norm `norm` near 1 before it is rounded to FP32.  Scaling by a power of
+// two is exact, so the multigrid (linear and homogeneous from a zero guess) gives the same digits as unscaled,
+// but right-hand sides of any magnitude stay clear of FP32 overflow and of its subnormal range.
+__device__ __forceinline__ int residual_exponent(double norm) {
+    return (norm > 0.0 && isfinite(norm)) ? ilogb(norm) : 0;
+}
 
 // ---- warp / block reductions (fixed order, so results do not depend on scheduling) --------------------
 template <typename T>

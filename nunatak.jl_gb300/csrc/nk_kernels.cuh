@@ -66,6 +66,7 @@ struct CGView {
 void launch_cg_init(const CGView& v, cudaStream_t s);
 // multigrid: after z = V(r): p = z, rho = r.z, done
 void launch_cg_init_finish(const CGView& v, cudaStream_t s);
+void launch_cg_scale_r32(const CGView& v, cudaStream_t s);
 // q = A p, alpha = rho / p.q
 void launch_cg_apply(const CGView& v, cudaStream_t s);
 // x += alpha p, r -= alpha q (and z = M r for Jacobi / none); dots for beta and the stopping test
@@ -100,6 +101,29 @@ void launch_basal_drag(const PhysView& ph, const double2* x, double4* coef, doub
 void launch_basal_velocity(const PhysView& ph, const double2* x, const double2* bb, const double* F2, double2* ub, cudaStream_t s);
 // DIVA effective drag beta = beta_b / (1 + beta_b ℑF2) (diva.jl:203-211)
 void launch_effective_drag(const PhysView& ph, const double2* bb, const double* F2, double4* coef, cudaStream_t s);
+
+// ---- fixed-point adjoint of the SSA Picard step (nk_coefficients.cu) ------------------------------------------
+// One Picard step maps x to A(c(x))⁻¹ b with c = (η̄H, η̄Hᶠᶠ, βᵘ, βᵛ) from the viscosity, corner and drag
+// updates.  These kernels apply the transpose of ∂[A(c(x)) x*]/∂x at the fixed point x* to an adjoint state λ.
+struct AdjointView {
+    PhysView ph;                  // grid, rheology and friction parameters and inputs
+    OpView<double> o;             // coefficients c(x*) and the operator mask
+    const double2* xs;            // converged velocity x*
+    const double2* lam;           // adjoint state λ
+    const double2* xbar;          // ∂J/∂x
+    double2* cbar;                // (∂/∂η̄H at centre (i, j) through the centre stresses, ∂/∂η̄Hᶠᶠ at corner (i, j))
+    double2* bbar;                // (∂/∂βᵘ, ∂/∂βᵛ) at faces (i, j)
+    double* gbar;                 // ∂/∂(ε̇ₑ² + ε̇₀²) at centre (i, j)
+    double2* r;                   // x̄ − (∂[A(c(x)) x*]/∂x)ᵀ λ
+    double* grad_log_C;           // −λᵀ ∂[A(c) x*]/∂ log C per cell
+};
+void launch_adjoint_coefficients(const AdjointView& v, cudaStream_t s);
+void launch_adjoint_viscosity(const AdjointView& v, cudaStream_t s);
+void launch_adjoint_velocity(const AdjointView& v, cudaStream_t s);
+void launch_adjoint_gradient(const AdjointView& v, cudaStream_t s);
+// Δ = ‖λ⁺ − λ‖, M = ‖λ⁺‖ over the solved cells into sc->p_D / sc->p_X, then λ = λ⁺
+void launch_adjoint_change(const DevGrid<double>& g, const double2* lam_new, double2* lam, SolverScalars* sc, double2* partials,
+                           cudaStream_t s);
 // DIVA velocity profile (diva.jl:259-269) / SSA depth extension (ice_sheet_model_methods.jl:167-180)
 void launch_velocity_profile(const PhysView& ph, int diva, const double2* x, const double2* bb, const double* F2,
                              const double* eta_sigma, double2* ub, double2* usig, cudaStream_t s);

@@ -188,6 +188,12 @@ struct nk_problem {
     long long linear_kernels[2] = {0, 0};      // kernel nodes: top level, CG body
     bool async_pending = false;                // nk_picard_solve_async issued, nk_problem_wait not yet called
     double instantiate_s = 0;                  // host seconds of the last graph instantiation
+    // Picard adjoint scratch, allocated by the first nk_picard_adjoint: ∂J/∂x (pairs), the strain-rate adjoint
+    // per centre and the log C gradient per cell
+    void* adj_base = nullptr;
+    double2* adj_xbar = nullptr;
+    double* adj_g = nullptr;
+    double* adj_grad = nullptr;
 
     // ---- views ---------------------------------------------------------------------------------------------
     OpView<double> fine_op() const {
@@ -658,6 +664,7 @@ static void cg_start(nk_problem* P, const CGView& v) {
     update_preconditioner(P);
     launch_cg_init(v, P->stream);
     if (P->precond == NK_PRECONDITIONER_MULTIGRID) {
+        if (v.r32) launch_cg_scale_r32(v, P->stream);
         precondition_mg(P, nullptr, true);
         launch_cg_init_finish(v, P->stream);
     }
@@ -1077,6 +1084,7 @@ nk_status nk_problem_destroy(nk_problem* P) {
     if (P->sc_host && !P->external_pinned) cudaFreeHost(P->sc_host);
     if (P->ev0) cudaEventDestroy(P->ev0);
     if (P->ev1) cudaEventDestroy(P->ev1);
+    if (P->adj_base) cudaFree(P->adj_base);
     if (P->stream) cudaStreamDestroy(P->stream);
     delete P;
     return NK_OK;
@@ -1217,6 +1225,104 @@ nk_status nk_linear_solve(nk_problem* P, const double* bu, const double* bv, nk_
 nk_status nk_adjoint_solve(nk_problem* P, const double* bu, const double* bv, nk_solve_stats* stats) {
     if (!P || !bu || !bv) return NK_BAD_ARGUMENT;
     return linear_solve_impl(P, bu, bv, stats);   // the operator is self-adjoint (conjugate_gradient.jl:186-189)
+}
+
+// Fixed-point adjoint of a converged picard_solve! (ext/NunatakEnzymeExt.jl:167-240).  The Picard step maps x to
+// A(c(x))⁻¹ b; at its fixed point x* the adjoint λ solves λ = A⁻ᵀ (x̄ - Nᵀ λ), N = ∂[A(c(x)) x*]/∂x, iterated
+// from λ = 0 with the problem's preconditioned CG warm-started from the previous λ, until
+// ‖λ⁺ - λ‖ ≤ max(reltol ‖λ⁺‖, abstol).  Then b̄ = λ and p̄ = -(∂[A(c(p)) x*]/∂p)ᵀ λ.
+static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar, const nk_iteration_control& ctl, double* lu,
+                           double* lv, double* grad, nk_solve_stats* st) {
+    if (P->pd.stress_balance == NK_DIVA)
+        bad("nk_picard_adjoint covers the SSA; the DIVA step's lagged basal-drag state is not differentiated");
+    cudaStream_t s = P->stream;
+    size_t pl = P->plane;
+    if (!P->adj_base) {
+        NK_CUDA(cudaMalloc(&P->adj_base, pl * (sizeof(double2) + 2 * sizeof(double))));
+        P->adj_xbar = (double2*)P->adj_base;
+        P->adj_g = (double*)(P->adj_xbar + pl);
+        P->adj_grad = P->adj_g + pl;
+    }
+    NK_CUDA(cudaMemcpyAsync(P->xprev, P->x, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));   // x*
+    update_coefficients(P);                                                                         // c(x*)
+    vector_in(P, P->adj_xbar, ubar, vbar);
+    NK_CUDA(cudaMemsetAsync(P->adj_g, 0, pl * sizeof(double), s));
+    NK_CUDA(cudaMemsetAsync(P->tmp_a, 0, pl * sizeof(double2), s));                                 // λ
+    NK_CUDA(cudaMemsetAsync(P->x, 0, pl * sizeof(double2), s));                                     // CG iterate
+    AdjointView v;
+    v.ph = P->phys();
+    v.o = P->fine_op();
+    v.xs = P->xprev;
+    v.lam = P->tmp_a;
+    v.xbar = P->adj_xbar;
+    v.cbar = P->ub;
+    v.bbar = P->bb;
+    v.gbar = P->adj_g;
+    v.r = P->tmp_b;
+    v.grad_log_C = P->adj_grad;
+    bool fixed = ctl.kind == NK_FIXED_ITERATIONS;
+    int limit = fixed ? ctl.iterations : ctl.maxiter;
+    int it = 0, cg_total = 0, cg_last = 0;
+    double D = INFINITY, M = 0.0, rnorm = 0.0;
+    bool cg_failed = false;
+    while (it < limit && (fixed || D > std::max(ctl.reltol * M, ctl.abstol))) {
+        launch_adjoint_coefficients(v, s);
+        launch_adjoint_viscosity(v, s);
+        launch_adjoint_velocity(v, s);                       // tmp_b = x̄ - Nᵀ λ
+        nk_solve_stats lst{};
+        linear_solve(P, &lst);                               // x = A⁻¹ tmp_b, from x = λ
+        cg_total += lst.linear_iterations_total;
+        cg_last = lst.linear_iterations_last;
+        rnorm = lst.residual_norm;
+        if (lst.status == NK_NONFINITE || lst.status == NK_BREAKDOWN) cg_failed = true;
+        launch_adjoint_change(P->fine.g, P->x, P->tmp_a, P->sc, P->partials, s);   // Δ, M; λ = x
+        NK_CHECK_LAUNCH();
+        read_scalars(P);
+        D = P->sc_host->p_D;
+        M = P->sc_host->p_X;
+        ++it;
+        if (!std::isfinite(D) || cg_failed) break;
+    }
+    launch_adjoint_coefficients(v, s);
+    launch_adjoint_gradient(v, s);
+    NK_CHECK_LAUNCH();
+    if (lu && lv) vector_out(P, P->tmp_a, lu, lv);
+    if (grad) {
+        FieldLoc f;
+        f.base = P->adj_grad;
+        f.nx = P->Nx;
+        f.ny = P->Ny;
+        copy_out(P, f, grad);
+    }
+    NK_CUDA(cudaMemcpyAsync(P->x, P->xprev, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));   // U, V = x*
+    NK_CUDA(cudaStreamSynchronize(s));
+    std::memset(st, 0, sizeof(*st));
+    st->picard_iterations = it;
+    st->linear_iterations_total = cg_total;
+    st->linear_iterations_last = cg_last;
+    st->residual_norm = rnorm;
+    st->picard_change = D;
+    st->picard_norm = M;
+    st->status = NK_OK;
+    if (!std::isfinite(D) || cg_failed) st->status = NK_NONFINITE;
+    else if (!fixed && !(D <= std::max(ctl.reltol * M, ctl.abstol))) st->status = NK_NOT_CONVERGED;
+}
+
+nk_status nk_picard_adjoint(nk_problem* P, const double* ubar, const double* vbar, const nk_iteration_control* control,
+                            double* lambda_u, double* lambda_v, double* grad_log_C, nk_solve_stats* stats) {
+    if (!P || !ubar || !vbar) return NK_BAD_ARGUMENT;
+    return guarded(P->ctx, [&] {
+        nk_iteration_control ctl = control ? *control : P->sd.picard;
+        if (ctl.kind == NK_FIXED_ITERATIONS ? ctl.iterations < 0 : ctl.maxiter < 0) bad("negative iteration count");
+        nk_solve_stats local{};
+        nk_solve_stats* st = stats ? stats : &local;
+        NK_CUDA(cudaEventRecord(P->ev0, P->stream));
+        picard_adjoint(P, ubar, vbar, ctl, lambda_u, lambda_v, grad_log_C, st);
+        NK_CUDA(cudaEventRecord(P->ev1, P->stream));
+        NK_CUDA(cudaEventSynchronize(P->ev1));
+        event_times(P, st);
+        if (st->status == NK_NONFINITE) throw Failure{NK_NONFINITE, "non-finite Picard adjoint"};
+    });
 }
 
 nk_status nk_picard_solve(nk_problem* P, nk_solve_stats* stats) {

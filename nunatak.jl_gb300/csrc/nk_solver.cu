@@ -154,8 +154,7 @@ __global__ void __launch_bounds__(32 * STRIP_WARPS) k_cg_init(CGView v) {
     if (j0 < v.o.g.Ny) {   // warps below the grid still take part in the block reduction
         strip_apply<R>(v.o, (const double2*)v.x, i, j0, [&](int k) { return v.b[k]; }, [&](int k, double2 q, double2, const double2& b) {
             double2 r = make_double2(b.x - q.x, b.y - q.y);
-            v.r[k] = r;
-            if (v.r32) v.r32[k] = make_float2((float)r.x, (float)r.y);
+            v.r[k] = r;   // the FP32 copy for the multigrid follows in k_cg_scale_r32, once ‖r0‖ is known
             rr += r.x * r.x + r.y * r.y;
             if (v.precond != NK_PRECONDITIONER_MULTIGRID) {
                 double2 z = r;
@@ -194,6 +193,23 @@ void launch_cg_init(const CGView& v, cudaStream_t s) {
     count_launch();
 }
 
+// mixed precision start: the FP32 copy of r0 for the first V-cycle, scaled by 2^-e with e the exponent of ‖r0‖
+__global__ void k_cg_scale_r32(CGView v) {
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    int e = residual_exponent(v.sc->rnorm);
+    if (i == 0 && j == 0) v.sc->r32_exp = e;
+    if (i < v.o.g.Nx && j < v.o.g.Ny) {
+        int k = v.o.g.idx(i, j);
+        double s = ldexp(1.0, -e);
+        double2 r = v.r[k];
+        v.r32[k] = make_float2((float)(r.x * s), (float)(r.y * s));
+    }
+}
+void launch_cg_scale_r32(const CGView& v, cudaStream_t s) {
+    LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
+    k_cg_scale_r32<<<d.grid, d.block, 0, s>>>(v); count_launch();
+}
+
 // multigrid start: p = z, rho = r.z (and z_old = z for flexible conjugate gradients)
 __global__ void k_cg_init_finish(CGView v) {
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
@@ -203,7 +219,8 @@ __global__ void k_cg_init_finish(CGView v) {
         double2 z, r = v.r[k];
         if (v.z32) {
             float2 f = v.z32[k];
-            z = make_double2((double)f.x, (double)f.y);
+            double zs = ldexp(1.0, v.sc->r32_exp);
+            z = make_double2((double)f.x * zs, (double)f.y * zs);
             v.z[k] = z;
         } else {
             z = v.z[k];
@@ -256,6 +273,9 @@ __global__ void k_cg_update(CGView v) {
     if (read_done(v.sc)) return;
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     double alpha = v.sc->alpha;
+    // FP32 copy of the new residual scaled by the previous norm (read here, before the last block replaces it)
+    int r32_exp = residual_exponent(v.sc->rnorm);
+    double r32_scale = ldexp(1.0, -r32_exp);
     double rz = 0.0, rr = 0.0;
     if (i < v.o.g.Nx && j < v.o.g.Ny) {
         int k = v.o.g.idx(i, j);
@@ -266,7 +286,7 @@ __global__ void k_cg_update(CGView v) {
         r.y = r.y + (-alpha) * q.y;
         v.x[k] = x;
         v.r[k] = r;
-        if (v.r32) v.r32[k] = make_float2((float)r.x, (float)r.y);
+        if (v.r32) v.r32[k] = make_float2((float)(r.x * r32_scale), (float)(r.y * r32_scale));
         rr = r.x * r.x + r.y * r.y;
         if (v.precond != NK_PRECONDITIONER_MULTIGRID) {
             double2 z = r;
@@ -282,6 +302,7 @@ __global__ void k_cg_update(CGView v) {
     if (grid_sum2(rz, rr, v.partials, &v.sc->ticket, trz, trr) && threadIdx.x == 0 && threadIdx.y == 0) {
         SolverScalars* sc = v.sc;
         sc->rr = trr;
+        sc->r32_exp = r32_exp;
         double rn = sqrt(trr);
         sc->rnorm = rn;
         int it = sc->it + 1;
@@ -313,7 +334,8 @@ __global__ void k_cg_dots_after_precondition(CGView v) {
         double2 r = v.r[k], z;
         if (v.z32) {
             float2 f = v.z32[k];
-            z = make_double2((double)f.x, (double)f.y);
+            double zs = ldexp(1.0, v.sc->r32_exp);
+            z = make_double2((double)f.x * zs, (double)f.y * zs);
             v.z[k] = z;
         } else {
             z = v.z[k];
