@@ -100,14 +100,31 @@ struct SolverScalars {
     double p_reltol, p_abstol, p_D, p_X;
     int p_fixed, p_iterations, p_maxiter, p_it;
     int p_done, it_total, cg_unconverged;
-    int r32_exp;                   // mixed precision: r32 = r 2^-r32_exp, z = z32 2^r32_exp (keeps FP32 values near 1)
+    int r32_exp;                   // mixed precision: the FP32 residual in the V-cycle is r 2^-r32_exp, z = z32 2^r32_exp
+    int r32_exp_next;              // exponent the next k_cg_update scales its residual with (from the latest ‖r‖)
+    int pad;
 };
 
 // Binary exponent that brings a residual of norm `norm` near 1 before it is rounded to FP32.  Scaling by a power of
 // two is exact, so the multigrid (linear and homogeneous from a zero guess) gives the same digits as unscaled,
-// but right-hand sides of any magnitude stay clear of FP32 overflow and of its subnormal range.
+// but right-hand sides of any magnitude stay clear of FP32 overflow and of its subnormal range.  Evaluated by
+// one thread per kernel (it costs FP64 instructions); the cells apply it with scale_pow2.
 __device__ __forceinline__ int residual_exponent(double norm) {
     return (norm > 0.0 && isfinite(norm)) ? ilogb(norm) : 0;
+}
+
+// x 2^k by an integer add to the exponent field (no FP64 instruction): exact for normal x and results.  Zeros,
+// infinities and NaNs pass through; subnormal x and results below the normal range flush to a signed zero,
+// results above it become infinite.
+__device__ __forceinline__ double scale_pow2(double x, int k) {
+    long long b = __double_as_longlong(x);
+    int ex = (int)((b >> 52) & 0x7ff);
+    if (ex == 0x7ff || k == 0) return x;
+    long long sign = b & (long long)0x8000000000000000ULL;
+    int en = ex + k;
+    if (ex == 0 || en <= 0) return __longlong_as_double(sign);
+    if (en >= 0x7ff) return __longlong_as_double(sign | 0x7ff0000000000000LL);
+    return __longlong_as_double(b + ((long long)k << 52));
 }
 
 // ---- warp / block reductions (fixed order, so results do not depend on scheduling) --------------------
@@ -158,10 +175,22 @@ __device__ __forceinline__ bool grid_sum2(double a, double b, double2* partials,
     __threadfence();
     int nt = blockDim.x * blockDim.y;
     double sa = 0.0, sb = 0.0;
-    for (int k = tid; k < nblocks; k += nt) {
-        double2 p = __ldcg(&partials[k]);   // L2 read: the other blocks' partials are not in this SM's L1
-        sa += p.x;
-        sb += p.y;
+    // k = tid, tid + nt, ... in order; eight L2 reads issued before their adds (the partials of the other blocks
+    // are not in this SM's L1, so __ldcg), which keeps the summation order and overlaps the read latencies
+    for (int base = tid; base < nblocks; base += 8 * nt) {
+        double2 p[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            int k = base + u * nt;
+            p[u] = k < nblocks ? __ldcg(&partials[k]) : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (base + u * nt < nblocks) {
+                sa += p[u].x;
+                sb += p[u].y;
+            }
+        }
     }
     block_sum2(sa, sb, sh);
     if (tid == 0) { *ticket = 0u; }
@@ -181,6 +210,15 @@ long long launch_count();
 struct LaunchDims {
     dim3 grid, block;
 };
+// The per-iteration CG vector kernels give each thread VEC_ROWS cells of one column (rows j, j + BY, ...):
+// the thread sums its cells before the block reduction, whose FP64 butterfly then costs a quarter per cell.
+constexpr int VEC_ROWS = 4;
+inline LaunchDims vec_dims(int nx, int ny) {
+    LaunchDims d;
+    d.block = dim3(BX, BY);
+    d.grid = dim3((nx + BX - 1) / BX, (ny + BY * VEC_ROWS - 1) / (BY * VEC_ROWS));
+    return d;
+}
 inline LaunchDims dims2d(int nx, int ny) {
     LaunchDims d;
     d.block = dim3(BX, BY);

@@ -175,6 +175,8 @@ __global__ void __launch_bounds__(32 * STRIP_WARPS) k_cg_init(CGView v) {
         sc->rr = trr;
         sc->r0 = r0;
         sc->rnorm = r0;
+        sc->r32_exp = residual_exponent(r0);
+        sc->r32_exp_next = sc->r32_exp;
         sc->tol = fmax(sc->reltol * r0, sc->abstol);
         sc->it = 0;
         sc->rho = trz;
@@ -196,13 +198,11 @@ void launch_cg_init(const CGView& v, cudaStream_t s) {
 // mixed precision start: the FP32 copy of r0 for the first V-cycle, scaled by 2^-e with e the exponent of ‖r0‖
 __global__ void k_cg_scale_r32(CGView v) {
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
-    int e = residual_exponent(v.sc->rnorm);
-    if (i == 0 && j == 0) v.sc->r32_exp = e;
+    int e = v.sc->r32_exp;   // set with ‖r0‖ by the last block of k_cg_init
     if (i < v.o.g.Nx && j < v.o.g.Ny) {
         int k = v.o.g.idx(i, j);
-        double s = ldexp(1.0, -e);
         double2 r = v.r[k];
-        v.r32[k] = make_float2((float)(r.x * s), (float)(r.y * s));
+        v.r32[k] = make_float2((float)scale_pow2(r.x, -e), (float)scale_pow2(r.y, -e));
     }
 }
 void launch_cg_scale_r32(const CGView& v, cudaStream_t s) {
@@ -212,22 +212,26 @@ void launch_cg_scale_r32(const CGView& v, cudaStream_t s) {
 
 // multigrid start: p = z, rho = r.z (and z_old = z for flexible conjugate gradients)
 __global__ void k_cg_init_finish(CGView v) {
-    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    int i = blockIdx.x * BX + threadIdx.x, j0 = blockIdx.y * BY * VEC_ROWS + threadIdx.y;
     double rz = 0.0;
-    if (i < v.o.g.Nx && j < v.o.g.Ny) {
-        int k = v.o.g.idx(i, j);
-        double2 z, r = v.r[k];
-        if (v.z32) {
-            float2 f = v.z32[k];
-            double zs = ldexp(1.0, v.sc->r32_exp);
-            z = make_double2((double)f.x * zs, (double)f.y * zs);
-            v.z[k] = z;
-        } else {
-            z = v.z[k];
+#pragma unroll
+    for (int row = 0; row < VEC_ROWS; ++row) {
+        int j = j0 + row * BY;
+        if (i < v.o.g.Nx && j < v.o.g.Ny) {
+            int k = v.o.g.idx(i, j);
+            double2 z, r = v.r[k];
+            if (v.z32) {
+                float2 f = v.z32[k];
+                int ze = v.sc->r32_exp;
+                z = make_double2(scale_pow2((double)f.x, ze), scale_pow2((double)f.y, ze));
+                v.z[k] = z;
+            } else {
+                z = v.z[k];
+            }
+            v.p[k] = z;
+            if (v.zold) v.zold[k] = z;
+            rz += r.x * z.x + r.y * z.y;
         }
-        v.p[k] = z;
-        if (v.zold) v.zold[k] = z;
-        rz = r.x * z.x + r.y * z.y;
     }
     double trz, dummy;
     if (grid_sum2(rz, 0.0, v.partials, &v.sc->ticket, trz, dummy) && threadIdx.x == 0 && threadIdx.y == 0) {
@@ -236,7 +240,7 @@ __global__ void k_cg_init_finish(CGView v) {
     }
 }
 void launch_cg_init_finish(const CGView& v, cudaStream_t s) {
-    LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
+    LaunchDims d = vec_dims(v.o.g.Nx, v.o.g.Ny);
     k_cg_init_finish<<<d.grid, d.block, 0, s>>>(v); count_launch();
 }
 
@@ -271,39 +275,44 @@ void launch_cg_apply(const CGView& v, cudaStream_t s) {
 // conjugate_gradient_step!, :355-360 and the stopping test of :334-338
 __global__ void k_cg_update(CGView v) {
     if (read_done(v.sc)) return;
-    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    int i = blockIdx.x * BX + threadIdx.x, j0 = blockIdx.y * BY * VEC_ROWS + threadIdx.y;
     double alpha = v.sc->alpha;
-    // FP32 copy of the new residual scaled by the previous norm (read here, before the last block replaces it)
-    int r32_exp = residual_exponent(v.sc->rnorm);
-    double r32_scale = ldexp(1.0, -r32_exp);
+    // FP32 copy of the new residual scaled by the exponent of the previous norm (read before the last block
+    // replaces it)
+    int r32_exp = v.sc->r32_exp_next;
     double rz = 0.0, rr = 0.0;
-    if (i < v.o.g.Nx && j < v.o.g.Ny) {
-        int k = v.o.g.idx(i, j);
-        double2 p = v.p[k], q = v.q[k], x = v.x[k], r = v.r[k];
-        x.x = x.x + alpha * p.x;
-        x.y = x.y + alpha * p.y;
-        r.x = r.x + (-alpha) * q.x;
-        r.y = r.y + (-alpha) * q.y;
-        v.x[k] = x;
-        v.r[k] = r;
-        if (v.r32) v.r32[k] = make_float2((float)(r.x * r32_scale), (float)(r.y * r32_scale));
-        rr = r.x * r.x + r.y * r.y;
-        if (v.precond != NK_PRECONDITIONER_MULTIGRID) {
-            double2 z = r;
-            if (v.precond == NK_PRECONDITIONER_DIAGONAL) {
-                double2 d = v.invd[k];
-                z = make_double2(r.x * d.x, r.y * d.y);
+#pragma unroll
+    for (int row = 0; row < VEC_ROWS; ++row) {
+        int j = j0 + row * BY;
+        if (i < v.o.g.Nx && j < v.o.g.Ny) {
+            int k = v.o.g.idx(i, j);
+            double2 p = v.p[k], q = v.q[k], x = v.x[k], r = v.r[k];
+            x.x = x.x + alpha * p.x;
+            x.y = x.y + alpha * p.y;
+            r.x = r.x + (-alpha) * q.x;
+            r.y = r.y + (-alpha) * q.y;
+            v.x[k] = x;
+            v.r[k] = r;
+            if (v.r32) v.r32[k] = make_float2((float)scale_pow2(r.x, -r32_exp), (float)scale_pow2(r.y, -r32_exp));
+            rr += r.x * r.x + r.y * r.y;
+            if (v.precond != NK_PRECONDITIONER_MULTIGRID) {
+                double2 z = r;
+                if (v.precond == NK_PRECONDITIONER_DIAGONAL) {
+                    double2 d = v.invd[k];
+                    z = make_double2(r.x * d.x, r.y * d.y);
+                }
+                v.z[k] = z;
+                rz += r.x * z.x + r.y * z.y;
             }
-            v.z[k] = z;
-            rz = r.x * z.x + r.y * z.y;
         }
     }
     double trz, trr;
     if (grid_sum2(rz, rr, v.partials, &v.sc->ticket, trz, trr) && threadIdx.x == 0 && threadIdx.y == 0) {
         SolverScalars* sc = v.sc;
         sc->rr = trr;
-        sc->r32_exp = r32_exp;
         double rn = sqrt(trr);
+        sc->r32_exp = r32_exp;
+        sc->r32_exp_next = residual_exponent(rn);
         sc->rnorm = rn;
         int it = sc->it + 1;
         sc->it = it;
@@ -319,7 +328,7 @@ __global__ void k_cg_update(CGView v) {
     }
 }
 void launch_cg_update(const CGView& v, cudaStream_t s) {
-    LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
+    LaunchDims d = vec_dims(v.o.g.Nx, v.o.g.Ny);
     k_cg_update<<<d.grid, d.block, 0, s>>>(v); count_launch();
 }
 
@@ -327,23 +336,27 @@ void launch_cg_update(const CGView& v, cudaStream_t s) {
 // beta = (r.z - r.z_old) / rho when the preconditioner varies between steps
 __global__ void k_cg_dots_after_precondition(CGView v) {
     if (read_done(v.sc)) return;
-    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    int i = blockIdx.x * BX + threadIdx.x, j0 = blockIdx.y * BY * VEC_ROWS + threadIdx.y;
     double rz = 0.0, rzo = 0.0;
-    if (i < v.o.g.Nx && j < v.o.g.Ny) {
-        int k = v.o.g.idx(i, j);
-        double2 r = v.r[k], z;
-        if (v.z32) {
-            float2 f = v.z32[k];
-            double zs = ldexp(1.0, v.sc->r32_exp);
-            z = make_double2((double)f.x * zs, (double)f.y * zs);
-            v.z[k] = z;
-        } else {
-            z = v.z[k];
-        }
-        rz = r.x * z.x + r.y * z.y;
-        if (v.zold) {
-            double2 zo = v.zold[k];
-            rzo = r.x * zo.x + r.y * zo.y;
+#pragma unroll
+    for (int row = 0; row < VEC_ROWS; ++row) {
+        int j = j0 + row * BY;
+        if (i < v.o.g.Nx && j < v.o.g.Ny) {
+            int k = v.o.g.idx(i, j);
+            double2 r = v.r[k], z;
+            if (v.z32) {
+                float2 f = v.z32[k];
+                int ze = v.sc->r32_exp;
+                z = make_double2(scale_pow2((double)f.x, ze), scale_pow2((double)f.y, ze));
+                v.z[k] = z;
+            } else {
+                z = v.z[k];
+            }
+            rz += r.x * z.x + r.y * z.y;
+            if (v.zold) {
+                double2 zo = v.zold[k];
+                rzo += r.x * zo.x + r.y * zo.y;
+            }
         }
     }
     double trz, trzo;
@@ -357,22 +370,26 @@ __global__ void k_cg_dots_after_precondition(CGView v) {
     }
 }
 void launch_cg_dots_after_precondition(const CGView& v, cudaStream_t s) {
-    LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
+    LaunchDims d = vec_dims(v.o.g.Nx, v.o.g.Ny);
     k_cg_dots_after_precondition<<<d.grid, d.block, 0, s>>>(v); count_launch();
 }
 
 // xpby!(z, beta, p), conjugate_gradient.jl:361; the last block commits the stopping decision
 __global__ void k_cg_xpby(CGView v) {
     if (read_done(v.sc)) return;
-    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    int i = blockIdx.x * BX + threadIdx.x, j0 = blockIdx.y * BY * VEC_ROWS + threadIdx.y;
     double beta = v.sc->beta;
-    if (i < v.o.g.Nx && j < v.o.g.Ny) {
-        int k = v.o.g.idx(i, j);
-        double2 z = v.z[k], p = v.p[k];
-        p.x = z.x + beta * p.x;
-        p.y = z.y + beta * p.y;
-        v.p[k] = p;
-        if (v.zold) v.zold[k] = z;
+#pragma unroll
+    for (int row = 0; row < VEC_ROWS; ++row) {
+        int j = j0 + row * BY;
+        if (i < v.o.g.Nx && j < v.o.g.Ny) {
+            int k = v.o.g.idx(i, j);
+            double2 z = v.z[k], p = v.p[k];
+            p.x = z.x + beta * p.x;
+            p.y = z.y + beta * p.y;
+            v.p[k] = p;
+            if (v.zold) v.zold[k] = z;
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0 && threadIdx.y == 0) {
@@ -388,7 +405,7 @@ __global__ void k_cg_xpby(CGView v) {
     }
 }
 void launch_cg_xpby(const CGView& v, cudaStream_t s) {
-    LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
+    LaunchDims d = vec_dims(v.o.g.Nx, v.o.g.Ny);
     k_cg_xpby<<<d.grid, d.block, 0, s>>>(v); count_launch();
 }
 
