@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--impl", default="nunatak", choices=["nunatak", "reference"])
     ap.add_argument("--batch", type=int, default=32, help="requests per step, and solves in flight at once")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--rate", type=float, default=ARRIVAL_RATE,
+                    help="Poisson arrival rate of the e2e leg, requests/s (the workload's is 200)")
     ap.add_argument("--profile", choices=["solve", "smoother", "operator"], default=None,
                     help="profiling runs for ncu: 'solve' = warm-up solves then one timed solve of the workload; "
                          "'smoother' / 'operator' = the roofline kernel on the 2048x1024 grid, 3 launches")
@@ -152,11 +154,11 @@ def workload(precision, member=0, grid=(256, 128)):
     return workloads.marine_sheet(grid[0], grid[1], seed=1, seed_friction=1000 + member, precision=precision)
 
 
-def stream_requests(n, batch, steps, warmup):
+def stream_requests(n, batch, steps, warmup, rate=ARRIVAL_RATE):
     """(warm-up requests, timed requests) of the serving stream: timed steps walk the stream from its start,
     wrapping after N_REQUESTS; warm-up steps take the batches before the stream's end."""
     from nunatak_gb300 import workloads
-    stream = workloads.serving_stream(n_requests=n, rate=ARRIVAL_RATE)
+    stream = workloads.serving_stream(n_requests=n, rate=rate)
     timed = [stream[k % n] for k in range(steps * batch)]
     warm = [stream[(n - warmup * batch + k) % n] for k in range(warmup * batch)]
     return warm, timed
@@ -188,6 +190,17 @@ def cpu_sample_requests(n):
     from nunatak_gb300 import workloads
     small = [r for r in workloads.serving_stream(n_requests=N_REQUESTS, rate=ARRIVAL_RATE) if r["size"][0] <= 256]
     return [small[k % len(small)] for k in range(n)]
+
+
+def replica_throughput(requests, span_ms, world, device):
+    """Whole-job solves/s of `world` replicas that each served `requests`: the slowest replica's span (max over
+    ranks, one all-reduce of the timing only) divides the requests of all ranks.  Returns (value, span_ms)."""
+    if world > 1:
+        import torch
+        t = torch.tensor([span_ms], device=device, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        span_ms = float(t.item())
+    return world * requests / (span_ms / 1e3), span_ms
 
 
 def run_reference(args, rank):
@@ -345,10 +358,10 @@ def run_resident(pool, cases, staged, zeros, in_flight, keep=()):
     return stats, kept
 
 
-def arrival_times(requests):
+def arrival_times(requests, rate=ARRIVAL_RATE):
     """Arrival of each request in seconds; a wrapped pass of the stream arrives after the previous one."""
     from nunatak_gb300 import workloads
-    period = workloads.serving_stream(n_requests=N_REQUESTS, rate=ARRIVAL_RATE)[-1]["arrival"] + 1.0 / ARRIVAL_RATE
+    period = workloads.serving_stream(n_requests=N_REQUESTS, rate=rate)[-1]["arrival"] + 1.0 / rate
     out, passes, last = [], 0, -1
     for r in requests:
         if r["index"] <= last:
@@ -485,7 +498,7 @@ def main():
         torch.cuda.synchronize()
 
     B = args.batch
-    warm_reqs, timed_reqs = stream_requests(N_REQUESTS, B, args.steps, args.warmup)
+    warm_reqs, timed_reqs = stream_requests(N_REQUESTS, B, args.steps, args.warmup, args.rate)
     warm_cases = build_cases(warm_reqs, "mixed")
     cases = build_cases(timed_reqs, "mixed")
     sizes = sorted({(c.grid.Nx, c.grid.Ny) for c in cases})
@@ -509,11 +522,7 @@ def main():
         wall = time.perf_counter() - t0
     launches = library.launch_count() - launches0
     span_ms = max(x.device_end_ms for x in stats) - min(x.device_start_ms for x in stats)
-    if world > 1:
-        t = torch.tensor([span_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        span_ms = float(t.item())
-    value = world * len(cases) / (span_ms / 1e3)
+    value, span_ms = replica_throughput(len(cases), span_ms, world, "cuda")
     service = [x.device_end_ms - x.device_start_ms for x in stats]
     created_timed = pool.created - created0
     pool.close()
@@ -548,7 +557,7 @@ def main():
     for c in warm_cases:
         S.submit(c)
     S.wait_all()
-    arrivals = arrival_times(timed_reqs)
+    arrivals = arrival_times(timed_reqs, args.rate)
     e2e_value, e2e_lat, e2e_stats = run_server(S, cases, arrivals)
     sinfo = S.info()
     S.close()
@@ -588,7 +597,7 @@ def main():
         "roofline": None,
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "latency_ms": {"p50": statistics.median(e2e_lat), "p99": float(np.percentile(e2e_lat, 99)),
-                               "note": "arrival (Poisson, 200/s) to result on the host"},
+                               "note": f"arrival (Poisson, {args.rate:g}/s) to result on the host"},
                 "path": "nk_server_submit / nk_server_wait (host inputs, upload, geometry, solve, read-back)",
                 "picard_iteration_mismatch_vs_resident": e2e_err, "server": sinfo},
         "clocks": clocks.summary(),

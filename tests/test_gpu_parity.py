@@ -44,6 +44,12 @@ GRIDS = [
     ("periodic", dict(size=(32, 16), x=(0.0, 1.0), y=(0.0, 1.0), topology=("Periodic", "Periodic"))),
     ("mixed", dict(size=(20, 30), x=(0.0, 1.0), y=(0.0, 1.0), topology=("Periodic", "Bounded"))),
     ("stretched", dict(size=(24, 12), x=list(np.linspace(0, 1, 25) ** 1.3), y=(0.0, 1.0), topology=("Bounded", "Bounded"))),
+    # edge shapes of the column-marching kernels: one cell, a sliver narrower than a warp, and ragged sizes whose
+    # last 30-column strip and last row walk are partial
+    ("one_cell", dict(size=(1, 1), x=(0.0, 1.0), y=(0.0, 1.0), topology=("Bounded", "Bounded"))),
+    ("sliver_periodic", dict(size=(2, 5), x=(0.0, 1.0), y=(0.0, 2.0), topology=("Periodic", "Bounded"))),
+    ("ragged", dict(size=(61, 33), x=(0.0, 6.1), y=(0.0, 3.3), topology=("Bounded", "Bounded"))),
+    ("ragged_periodic", dict(size=(45, 17), x=(0.0, 4.5), y=(0.0, 1.7), topology=("Periodic", "Periodic"))),
 ]
 
 
