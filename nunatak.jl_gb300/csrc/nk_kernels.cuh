@@ -161,6 +161,9 @@ void launch_coarsen(const LevelView<T>& coarse, const DevGrid<TF>& fine_g, const
 template <typename T>
 void launch_smooth_point(const LevelView<T>& L, const typename Vec2<T>::type* x_in, typename Vec2<T>::type* x_out, int first,
                          const int* done, cudaStream_t s);
+// the first two sweeps from a zero guess in one pass (x1 = b / rowsum formed on load)
+template <typename T>
+void launch_smooth_first2(const LevelView<T>& L, typename Vec2<T>::type* x_out, const int* done, cudaStream_t s);
 // q = A x (line smoother first half) or q = b - A x (residual)
 template <typename T>
 void launch_level_apply(const LevelView<T>& L, const typename Vec2<T>::type* x, typename Vec2<T>::type* q, int residual,

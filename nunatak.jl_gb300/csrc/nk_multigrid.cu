@@ -188,13 +188,10 @@ __device__ __forceinline__ void restrict_at(const LevelView<T>& C, const OpView<
 
 // prolongate (:320-327) into one fine point, x_fine += P x_coarse (_prolongate!, :354-360)
 template <typename T>
-__device__ __forceinline__ void prolong_at(const OpView<T>& fo, const LevelView<T>& C, typename Vec2<T>::type* xf,
-                                           const typename Vec2<T>::type* __restrict__ xc, int i, int j) {
-    const DevGrid<T>& fg = fo.g;
+__device__ __forceinline__ typename Vec2<T>::type prolonged(const OpView<T>& fo, const LevelView<T>& C, typename Vec2<T>::type x,
+                                                            uint8_t m, const typename Vec2<T>::type* __restrict__ xc, int i, int j) {
     const DevGrid<T>& cg = C.o.g;
-    int k = fg.idx(i, j);
-    uint8_t m = fo.mask[k];
-    typename Vec2<T>::type x = xf[k];
+    const DevGrid<T>& fg = fo.g;
     int I1, I2, J1, J2;
     T wx1, wx2, wy1, wy2;
     T pu = T(0), pv = T(0);
@@ -212,7 +209,13 @@ __device__ __forceinline__ void prolong_at(const OpView<T>& fo, const LevelView<
     }
     x.x += pu;
     x.y += pv;
-    xf[k] = x;
+    return x;
+}
+template <typename T>
+__device__ __forceinline__ void prolong_at(const OpView<T>& fo, const LevelView<T>& C, typename Vec2<T>::type* xf,
+                                           const typename Vec2<T>::type* __restrict__ xc, int i, int j) {
+    int k = fo.g.idx(i, j);
+    xf[k] = prolonged(fo, C, xf[k], fo.mask[k], xc, i, j);
 }
 
 // line_relax!, :231-253: Thomas algorithm along j for the u line and then the v line of column i.
@@ -284,6 +287,46 @@ void launch_smooth_point(const LevelView<T>& L, const typename Vec2<T>::type* x_
         with_strip_rows(rows, [&](auto r) { k_smooth_point<T, decltype(r)::value><<<d.grid, d.block, 0, s>>>(L, x_in, x_out, done); });
         count_launch();
     }
+}
+
+// The first two sweeps from a zero guess in one pass: the operand of the second sweep, x1 = b / rowsum, is formed
+// where it is loaded (the same single rounding as the separate first sweep), so x1 is never stored.
+template <typename T, int R>
+__global__ void __launch_bounds__(32 * STRIP_WARPS) k_smooth_first2(LevelView<T> L, typename Vec2<T>::type* __restrict__ xout,
+                                                                   const int* done) {
+    if (stopped(done)) return;
+    using V2 = typename Vec2<T>::type;
+    int i, j0;
+    strip_origin<R>(i, j0);
+    if (j0 >= L.o.g.Ny) return;   // whole warp
+    const V2* b = L.b;
+    const V2* w = L.irs;
+    int Nx = L.o.g.Nx, Ny = L.o.g.Ny;
+    auto src = [=](int k, int iw, int jw) {
+        V2 x;
+        x.x = T(0);
+        x.y = T(0);
+        if (iw < Nx && jw < Ny) {
+            V2 bb = b[k], ww = w[k];
+            x.x = bb.x * ww.x;
+            x.y = bb.y * ww.y;
+        }
+        return x;
+    };
+    struct BW { V2 b, w; };
+    strip_apply_src<R>(L.o, src, i, j0, [&](int k) { return BW{L.b[k], L.irs[k]}; }, [&](int k, V2 q, V2 x, const BW& e) {
+        V2 out;
+        out.x = x.x + (e.b.x - q.x) * e.w.x;
+        out.y = x.y + (e.b.y - q.y) * e.w.y;
+        xout[k] = out;
+    });
+}
+template <typename T>
+void launch_smooth_first2(const LevelView<T>& L, typename Vec2<T>::type* x_out, const int* done, cudaStream_t s) {
+    int rows = strip_rows(L.o.g.Nx, L.o.g.Ny, (int)sizeof(T));
+    LaunchDims d = strip_dims(L.o.g.Nx, L.o.g.Ny, rows);
+    with_strip_rows(rows, [&](auto r) { k_smooth_first2<T, decltype(r)::value><<<d.grid, d.block, 0, s>>>(L, x_out, done); });
+    count_launch();
 }
 
 template <typename T, int R>
@@ -452,6 +495,7 @@ void launch_coarse_vcycle(const CoarseLevels<T>& C, const int* done, cudaStream_
 
 #define NK_INSTANTIATE(T)                                                                                                   \
     template void launch_smooth_point<T>(const LevelView<T>&, const Vec2<T>::type*, Vec2<T>::type*, int, const int*, cudaStream_t); \
+    template void launch_smooth_first2<T>(const LevelView<T>&, Vec2<T>::type*, const int*, cudaStream_t); \
     template void launch_level_apply<T>(const LevelView<T>&, const Vec2<T>::type*, Vec2<T>::type*, int, const int*, cudaStream_t);  \
     template void launch_line_relax<T>(const LevelView<T>&, Vec2<T>::type*, int, const int*, cudaStream_t);                        \
     template void launch_restrict<T>(const LevelView<T>&, const LevelView<T>&, const Vec2<T>::type*, Vec2<T>::type*, Vec2<T>::type*, \

@@ -559,6 +559,11 @@ static void smooth(nk_problem* P, Level<T>& L, int sweeps, bool first, const int
     if (first && first_done) {
         in = first_sweep_target(L, sweeps);
         k0 = 1;
+    } else if (first && sweeps >= 2) {        // sweeps 1 and 2 from zero in one pass
+        V2* out = ((sweeps - 2) % 2 == 0) ? L.x : L.x2;
+        launch_smooth_first2<T>(v, out, done, s);
+        in = out;
+        k0 = 2;
     } else if (!first && sweeps % 2 == 1) {   // an odd number of ping-pong sweeps starting from L.x would write L.x in place
         cudaMemcpyAsync(L.x2, L.x, L.plane() * sizeof(V2), cudaMemcpyDeviceToDevice, s);
         in = L.x2;

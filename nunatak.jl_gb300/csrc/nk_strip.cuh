@@ -58,9 +58,9 @@ struct StripRow {
 };
 
 // The pair at (i, j) as masked_u / masked_v read it; zero outside the ranges those functions read.
-template <typename T>
-__device__ __forceinline__ StripRow<T> strip_load(const OpView<T>& o, const typename Vec2<T>::type* __restrict__ p, int i, int j,
-                                                  bool col_ok) {
+// `src(k, iw, jw)` returns the stored pair at pitched index k = idx(iw, jw) (iw, jw wrapped when periodic).
+template <typename T, typename Src>
+__device__ __forceinline__ StripRow<T> strip_load(const OpView<T>& o, Src&& src, int i, int j, bool col_ok) {
     const DevGrid<T>& g = o.g;
     StripRow<T> r;
     r.raw.x = T(0);
@@ -72,9 +72,10 @@ __device__ __forceinline__ StripRow<T> strip_load(const OpView<T>& o, const type
     r.uok = (g.px || (i >= 0 && i <= g.Nx)) && !g.out_y(j);
     r.vok = !g.out_x(i) && (g.py || (j >= 0 && j <= g.Ny));
     if (!(r.uok || r.vok)) return r;
-    int k = g.idx(g.px ? g.wrap(i, g.Nx) : i, g.py ? g.wrap(j, g.Ny) : j);
+    int iw = g.px ? g.wrap(i, g.Nx) : i, jw = g.py ? g.wrap(j, g.Ny) : j;
+    int k = g.idx(iw, jw);
     r.m = __ldg(o.mask + k);
-    r.raw = p[k];
+    r.raw = src(k, iw, jw);
     return r;
 }
 
@@ -84,9 +85,8 @@ struct NoExtra {};
 // `extra(k)` is called first (with the loads of the walk, so its global reads are in flight together with them)
 // and later `emit(k, q, raw, e)` with k = idx(i, j), q the operator result, raw the stored pair p(i, j) and e what
 // extra(k) returned.  Every lane of the warp must call this (shuffles); lanes with nothing to do pass through.
-template <int R, typename T, typename Extra, typename Emit>
-__device__ __forceinline__ void strip_apply(const OpView<T>& o, const typename Vec2<T>::type* __restrict__ p, int i, int j0,
-                                            Extra&& extra, Emit&& emit) {
+template <int R, typename T, typename Src, typename Extra, typename Emit>
+__device__ __forceinline__ void strip_apply_src(const OpView<T>& o, Src&& src, int i, int j0, Extra&& extra, Emit&& emit) {
     using V2 = typename Vec2<T>::type;
     using V4 = typename Vec4<T>::type;
     using E = decltype(extra(0));
@@ -114,7 +114,7 @@ __device__ __forceinline__ void strip_apply(const OpView<T>& o, const typename V
     T rdyc[R + 1], dyc[R + 1], rdyf[R + 1], dyf[R];
     E ex[R];
 #pragma unroll
-    for (int r = 0; r < R + 2; ++r) row[r] = strip_load(o, p, i, j0 - 1 + r, col_ok);
+    for (int r = 0; r < R + 2; ++r) row[r] = strip_load(o, src, i, j0 - 1 + r, col_ok);
 #pragma unroll
     for (int r = 0; r < R + 1; ++r) {
         int jc = j0 - 1 + r, jf = j0 + r;
@@ -179,6 +179,13 @@ __device__ __forceinline__ void strip_apply(const OpView<T>& o, const typename V
         syy_s = syy;
         t_c = t_n;
     }
+}
+
+// strip_apply_src with the operand read from an array.
+template <int R, typename T, typename Extra, typename Emit>
+__device__ __forceinline__ void strip_apply(const OpView<T>& o, const typename Vec2<T>::type* __restrict__ p, int i, int j0,
+                                            Extra&& extra, Emit&& emit) {
+    strip_apply_src<R>(o, [p](int k, int, int) { return p[k]; }, i, j0, extra, emit);
 }
 
 // Column and first row of the calling thread in a strip launch of R rows per warp (strip_dims).
