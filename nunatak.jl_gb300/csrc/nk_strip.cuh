@@ -150,9 +150,12 @@ __device__ __forceinline__ void strip_apply_src(const OpView<T>& o, Src&& src, i
         T mvw = __shfl_up_sync(full, mv, 1);
         T dudy = (mu - mus) * rdyf[c];
         T dvdx = (mv - mvw) * rdxf_i;
-        T e = (dudy + dvdx) / T(2);
+        // 2 η̄Hᶠᶠ ε̇xy with ε̇xy = (dudy + dvdx) / 2 (× the wall factor), written as η̄Hᶠᶠ (dudy + dvdx): the
+        // halving and doubling are exact, so this drops two operations and changes only how the compiler may
+        // contract the sum into a multiply-add (last-bit differences)
+        T e = dudy + dvdx;
         if (per_ff_x || g.out_y(j) || g.out_y(j - 1)) e = o.wall_factor * e;
-        return T(2) * cff[c] * e;
+        return cff[c] * e;
     };
 
     T sxx_s, syy_s;
