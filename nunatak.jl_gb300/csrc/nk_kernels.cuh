@@ -164,6 +164,15 @@ void launch_smooth_point(const LevelView<T>& L, const typename Vec2<T>::type* x_
 // the first two sweeps from a zero guess in one pass (x1 = b / rowsum formed on load)
 template <typename T>
 void launch_smooth_first2(const LevelView<T>& L, typename Vec2<T>::type* x_out, const int* done, cudaStream_t s);
+// the coarsest level's sweeps in one thread block with the level in shared memory (x_in = nullptr: from zero;
+// from_zero: the first sweep is x = b / rowsum); result in x_out
+template <typename T>
+bool coarsest_smem_fits(const LevelView<T>& L, int plane);
+template <typename T>
+void configure_coarsest_smem();
+template <typename T>
+void launch_coarsest_smem(const LevelView<T>& L, int plane, const typename Vec2<T>::type* x_in, int sweeps, int from_zero,
+                          typename Vec2<T>::type* x_out, const int* done, cudaStream_t s);
 // q = A x (line smoother first half) or q = b - A x (residual)
 template <typename T>
 void launch_level_apply(const LevelView<T>& L, const typename Vec2<T>::type* x, typename Vec2<T>::type* q, int residual,

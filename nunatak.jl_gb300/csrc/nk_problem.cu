@@ -512,6 +512,15 @@ static int coarse_cells_limit() {
     return limit;
 }
 
+// NK_COARSEST_SMEM=0 runs the coarsest level's sweeps as separate launches instead of one shared-memory block.
+static bool coarsest_in_shared_memory() {
+    static bool on = [] {
+        const char* e = std::getenv("NK_COARSEST_SMEM");
+        return !(e && std::atoi(e) == 0);
+    }();
+    return on;
+}
+
 template <typename T>
 static int fused_level(const std::vector<Level<T>>& lv, int nlevels) {
     if (sizeof(T) == 8) return nlevels + 1;
@@ -595,7 +604,16 @@ static void v_cycle(nk_problem* P, std::vector<Level<T>>& lv, int l, const int* 
     }
     Level<T>& L = lv[l];
     if (l == P->nlevels) {
-        smooth(P, L, P->sd.coarsest_sweeps, true, done, first_done);
+        int sweeps = P->sd.coarsest_sweeps;
+        LevelView<T> v = P->level_view(L);
+        int plane = (int)L.plane();
+        if (coarsest_in_shared_memory() && P->sd.smoother == NK_SMOOTHER_POINT_JACOBI && sweeps > 0 &&
+            coarsest_smem_fits<T>(v, plane)) {
+            if (first_done) launch_coarsest_smem<T>(v, plane, first_sweep_target(L, sweeps), sweeps - 1, 0, L.x, done, s);
+            else launch_coarsest_smem<T>(v, plane, nullptr, sweeps, 1, L.x, done, s);
+            return;
+        }
+        smooth(P, L, sweeps, true, done, first_done);
         return;
     }
     smooth(P, L, P->sd.smoothing_sweeps, true, done, first_done);
@@ -1066,6 +1084,8 @@ static nk_status problem_create(nk_context* ctx, const nk_grid_desc* grid, const
         NK_CUDA(cudaEventCreate(&P->ev0));
         NK_CUDA(cudaEventCreate(&P->ev1));
         build(P);
+        configure_coarsest_smem<float>();   // shared-memory limit of the coarsest-level kernel, once, outside any capture
+        configure_coarsest_smem<double>();
         P->gd.x_faces = nullptr; P->gd.y_faces = nullptr; P->gd.sigma_faces = nullptr;   // no pointer kept after the call
         NK_CUDA(cudaStreamSynchronize(P->stream));
     });
