@@ -416,158 +416,15 @@ void launch_zero_vec(const DevGrid<T>& g, typename Vec2<T>::type* x, const int* 
 
 // ---- the coarsest level in shared memory ----------------------------------------------------------------------
 // The coarsest level takes many sweeps (20 by default) of a grid of about a thousand cells: as separate launches
-// each sweep is a few microseconds of latency on the solve's critical path.  One thread block keeps the level in
-// shared memory and runs every sweep there.  A sweep (1) builds the masked velocities (interior_u / interior_v
-// with the operator mask) of the current x on the grid padded by one point, wrapped when periodic and zero outside
-// a Bounded range, (2) computes every centre's Δy Txx, Δx Tyy and every corner's shear once from that padded copy
-// (the expressions of the column-marching apply), (3) combines them into x' = x + (b - A x) / rowsum per cell and
-// (4) stores x'.  Block barriers separate the phases; every read inside the sweeps is from shared memory.
-// Launched only when the level fits (coarsest_smem_fits).
-template <typename T>
-size_t coarsest_smem_bytes(int plane, int nx, int ny) {
-    using V2 = typename Vec2<T>::type;
-    using V4 = typename Vec4<T>::type;
-    return (size_t)plane * (sizeof(V4) + 3 * sizeof(V2) + 1) + (size_t)nx * ny * sizeof(V2) + (size_t)(nx + 1) * (ny + 1) * sizeof(T) +
-           (size_t)(nx + 2) * (ny + 2) * sizeof(V2) + (size_t)4 * (nx + ny + 2) * sizeof(T) + 64;
-}
-template <typename T>
-constexpr int coarsest_threads() { return sizeof(T) == 8 ? 512 : 1024; }
-constexpr int COARSEST_CELLS = 8;   // cells per thread the kernel holds
-
-template <typename T>
-__global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024, 1)
-    k_coarsest_smem(LevelView<T> L, int plane, const typename Vec2<T>::type* __restrict__ xin, int sweeps, int from_zero,
-                    typename Vec2<T>::type* xout, const int* done) {
-    if (stopped(done)) return;
-    using V2 = typename Vec2<T>::type;
-    using V4 = typename Vec4<T>::type;
-    const DevGrid<T>& g = L.o.g;
-    const int Nx = g.Nx, Ny = g.Ny, tid = threadIdx.x, nt = blockDim.x;
-    const int n = Nx * Ny, ncorner = (Nx + 1) * (Ny + 1), PW = Nx + 2, npad = (Nx + 2) * (Ny + 2);
-    extern __shared__ __align__(32) unsigned char smem[];
-    V4* coef = reinterpret_cast<V4*>(smem);
-    V2* b = reinterpret_cast<V2*>(coef + plane);
-    V2* w = b + plane;
-    V2* x = w + plane;
-    V2* st = x + plane;                    // (Δy Txx, Δx Tyy) at centre c = j Nx + i
-    V2* M = st + n;                        // masked (u, v) at (i, j), i in -1..Nx, j in -1..Ny: (j + 1) PW + i + 1
-    T* sh = reinterpret_cast<T*>(M + npad);   // shear at corner j (Nx + 1) + i
-    T* rdxc = sh + ncorner;                // metrics of the axes, 0..N
-    T* dxc = rdxc + (Nx + 1);
-    T* rdxf = dxc + (Nx + 1);
-    T* dxf = rdxf + (Nx + 1);
-    T* rdyc = dxf + (Nx + 1);
-    T* dyc = rdyc + (Ny + 1);
-    T* rdyf = dyc + (Ny + 1);
-    T* dyf = rdyf + (Ny + 1);
-    uint8_t* mask = reinterpret_cast<uint8_t*>(dyf + (Ny + 1));
-    for (int k = tid; k < plane; k += nt) {
-        coef[k] = L.o.coef[k];
-        b[k] = L.b[k];
-        w[k] = L.irs[k];
-        mask[k] = L.o.mask[k];
-        V2 z;
-        z.x = T(0);
-        z.y = T(0);
-        x[k] = xin ? xin[k] : z;
-    }
-    for (int i = tid; i <= Nx; i += nt) {
-        rdxc[i] = g.rdxc[i]; dxc[i] = g.dxc[i]; rdxf[i] = g.rdxf[i]; dxf[i] = g.dxf[i];
-    }
-    for (int j = tid; j <= Ny; j += nt) {
-        rdyc[j] = g.rdyc[j]; dyc[j] = g.dyc[j]; rdyf[j] = g.rdyf[j]; dyf[j] = g.dyf[j];
-    }
-    __syncthreads();
-    for (int sweep = 0; sweep < sweeps; ++sweep) {
-        bool zero = from_zero && sweep == 0;
-        if (!zero) {
-            for (int e = tid; e < npad; e += nt) {     // (1) masked velocities, padded
-                int i = e % PW - 1, j = e / PW - 1;
-                V2 m;
-                m.x = T(0);
-                m.y = T(0);
-                bool uok = (g.px || (i >= 0 && i <= Nx)) && !g.out_y(j);
-                bool vok = !g.out_x(i) && (g.py || (j >= 0 && j <= Ny));
-                if (uok || vok) {
-                    int k = g.idx(g.px ? g.wrap(i, Nx) : i, g.py ? g.wrap(j, Ny) : j);
-                    uint8_t mk = mask[k];
-                    V2 xx = x[k];
-                    if (uok && !(mk & U_INACTIVE)) m.x = xx.x;
-                    if (vok && !(mk & V_INACTIVE)) m.y = xx.y;
-                }
-                M[e] = m;
-            }
-            __syncthreads();
-            for (int c = tid; c < n; c += nt) {         // (2) centre stresses
-                int i = c % Nx, j = c / Nx;
-                V2 m0 = M[(j + 1) * PW + i + 1], me = M[(j + 1) * PW + i + 2], mn = M[(j + 2) * PW + i + 1];
-                T exx = (me.x - m0.x) * rdxc[i];
-                T eyy = (mn.y - m0.y) * rdyc[j];
-                T eta = coef[g.idx(i, j)].x;
-                V2 sv;
-                sv.x = dyc[j] * (T(2) * eta * (T(2) * exx + eyy));
-                sv.y = dxc[i] * (T(2) * eta * (T(2) * eyy + exx));
-                st[c] = sv;
-            }
-            for (int c = tid; c < ncorner; c += nt) {   // (2) corner shears
-                int i = c % (Nx + 1), j = c / (Nx + 1);
-                V2 m0 = M[(j + 1) * PW + i + 1], ms = M[j * PW + i + 1], mw = M[(j + 1) * PW + i];
-                T e = (m0.x - ms.x) * rdyf[j] + (m0.y - mw.y) * rdxf[i];
-                if (g.peripheral_ff(i, j)) e = L.o.wall_factor * e;
-                sh[c] = coef[g.ff_idx(i, j)].y * e;
-            }
-            __syncthreads();
-        }
-        V2 nv[COARSEST_CELLS];
-#pragma unroll
-        for (int m = 0; m < COARSEST_CELLS; ++m) {      // (3) x' per cell
-            int c = tid + m * nt;
-            if (c < n) {
-                int i = c % Nx, j = c / Nx, k = g.idx(i, j);
-                V2 bb = b[k], ww = w[k];
-                if (zero) {
-                    nv[m].x = bb.x * ww.x;
-                    nv[m].y = bb.y * ww.y;
-                } else {
-                    // west and south centres: wrapped when periodic, zero stresses outside a Bounded range
-                    V2 s0 = st[c], sw, ss;
-                    sw.x = T(0); sw.y = T(0); ss.x = T(0); ss.y = T(0);
-                    if (i > 0) sw = st[c - 1]; else if (g.px) sw = st[j * Nx + Nx - 1];
-                    if (j > 0) ss = st[c - Nx]; else if (g.py) ss = st[(Ny - 1) * Nx + i];
-                    int jn = (g.py && j + 1 == Ny) ? 0 : j + 1, ie = (g.px && i + 1 == Nx) ? 0 : i + 1;
-                    T t00 = sh[j * (Nx + 1) + i], t01 = sh[jn * (Nx + 1) + i], t10 = sh[j * (Nx + 1) + ie];
-                    T fx = dxf[i], fy = dyf[j];
-                    T divu = (s0.x - sw.x) + (fx * t01 - fx * t00);
-                    T divv = (s0.y - ss.y) + (fy * t10 - fy * t00);
-                    V4 cc = coef[k];
-                    V2 xx = x[k];
-                    uint8_t mk = mask[k];
-                    V2 q;
-                    q.x = (mk & U_INACTIVE) ? xx.x : (fx * dyc[j]) * cc.z * xx.x - divu;
-                    q.y = (mk & V_INACTIVE) ? xx.y : (dxc[i] * fy) * cc.w * xx.y - divv;
-                    nv[m].x = xx.x + (bb.x - q.x) * ww.x;
-                    nv[m].y = xx.y + (bb.y - q.y) * ww.y;
-                }
-            }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int m = 0; m < COARSEST_CELLS; ++m) {      // (4)
-            int c = tid + m * nt;
-            if (c < n) x[g.idx(c % Nx, c / Nx)] = nv[m];
-        }
-        __syncthreads();
-    }
-    for (int c = tid; c < n; c += nt) {
-        int k = g.idx(c % Nx, c / Nx);
-        xout[k] = x[k];
-    }
-}
-
-// The same sweeps when every thread owns at most one cell, one corner beyond the cells and two padded points
-// (n <= threads): everything that does not change between sweeps (shared-memory indices, mask tests, metrics,
-// 2η, η̄Hᶠᶠ times the wall factor, Az β, b, 1/rowsum) is computed once into registers, so a sweep is a few dozen
-// instructions per cell.
+// each sweep is a few microseconds of latency on the solve's critical path.  For FP32 levels of at most 1024 cells
+// one block of 1024 threads runs every sweep on-chip, each thread owning one cell.  Everything that does not
+// change between sweeps (shared-memory indices, mask tests, metrics, 2η, η̄Hᶠᶠ times the wall factor, Az β, b,
+// 1/rowsum) is computed once into registers; a sweep (1) builds the masked velocities (interior_u / interior_v)
+// of the current x on the grid padded by one point (wrapped when periodic, zero outside a Bounded range),
+// (2) computes every centre's Δy Txx, Δx Tyy and every corner's shear once (the expressions of the column-marching
+// apply), (3) combines them into x' = x + (b - A x) / rowsum and (4) stores x', with block barriers between the
+// phases.  (A variant holding several cells per thread, with the constants re-read each sweep, was slower than
+// separate launches, in FP64 as well; those levels keep the launches.)
 template <typename T>
 __global__ void __launch_bounds__(1024, 1)
     k_coarsest_smem_1(LevelView<T> L, int plane, const typename Vec2<T>::type* __restrict__ xin, int sweeps, int from_zero,
@@ -710,46 +567,37 @@ __global__ void __launch_bounds__(1024, 1)
     if (has_cell) xout[kc] = x[kc];
 }
 
-// True when the level fits one block (shared memory and cells per thread).
+// True when the level can run in one block: FP32, at most one cell, one corner beyond the cells and two padded
+// points per thread.
 template <typename T>
 bool coarsest_smem_fits(const LevelView<T>& L, int plane) {
-    static int max_smem = [] {
-        int dev = 0, v = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        return v;
-    }();
-    return coarsest_smem_bytes<T>(plane, L.o.g.Nx, L.o.g.Ny) <= (size_t)max_smem &&
-           L.o.g.Nx * L.o.g.Ny <= COARSEST_CELLS * coarsest_threads<T>();
+    (void)plane;
+    int nx = L.o.g.Nx, ny = L.o.g.Ny;
+    return sizeof(T) == 4 && nx * ny <= 1024 && (nx + 2) * (ny + 2) <= 2048 && (nx + 1) * (ny + 1) <= 2048;
 }
 template <typename T>
 void configure_coarsest_smem() {
-    static bool done = [] {
-        int dev = 0, v = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        cudaFuncSetAttribute(k_coarsest_smem<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
-        if constexpr (sizeof(T) == 4) cudaFuncSetAttribute(k_coarsest_smem_1<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
-        return true;
-    }();
-    (void)done;
+    if constexpr (sizeof(T) == 4) {
+        static bool done = [] {
+            int dev = 0, v = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+            cudaFuncSetAttribute(k_coarsest_smem_1<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+            return true;
+        }();
+        (void)done;
+    }
 }
 template <typename T>
 void launch_coarsest_smem(const LevelView<T>& L, int plane, const typename Vec2<T>::type* x_in, int sweeps, int from_zero,
                           typename Vec2<T>::type* x_out, const int* done, cudaStream_t s) {
-    int nx = L.o.g.Nx, ny = L.o.g.Ny;
-    if constexpr (sizeof(T) == 4) {   // FP32 levels of at most 1024 cells: one cell per thread, constants in registers
-        if (nx * ny <= 1024 && (nx + 2) * (ny + 2) <= 2048 && (nx + 1) * (ny + 1) <= 2048) {
-            size_t bytes = (size_t)plane * sizeof(typename Vec2<T>::type) + (size_t)nx * ny * sizeof(typename Vec2<T>::type) +
-                           (size_t)(nx + 2) * (ny + 2) * sizeof(typename Vec2<T>::type) + (size_t)(nx + 1) * (ny + 1) * sizeof(T);
-            k_coarsest_smem_1<T><<<1, 1024, bytes, s>>>(L, plane, x_in, sweeps, from_zero, x_out, done);
-            count_launch();
-            return;
-        }
+    if constexpr (sizeof(T) == 4) {
+        int nx = L.o.g.Nx, ny = L.o.g.Ny;
+        size_t bytes = (size_t)plane * sizeof(typename Vec2<T>::type) + (size_t)nx * ny * sizeof(typename Vec2<T>::type) +
+                       (size_t)(nx + 2) * (ny + 2) * sizeof(typename Vec2<T>::type) + (size_t)(nx + 1) * (ny + 1) * sizeof(T);
+        k_coarsest_smem_1<T><<<1, 1024, bytes, s>>>(L, plane, x_in, sweeps, from_zero, x_out, done);
+        count_launch();
     }
-    size_t bytes = coarsest_smem_bytes<T>(plane, nx, ny);
-    k_coarsest_smem<T><<<1, coarsest_threads<T>(), bytes, s>>>(L, plane, x_in, sweeps, from_zero, x_out, done);
-    count_launch();
 }
 
 // ---- fused coarse V-cycle: one thread block runs every remaining level ----------------------------------------
