@@ -29,8 +29,9 @@ def _rank(rank, world, port, spans, out):
 
 
 def test_replica_throughput_takes_the_slowest_rank():
+    import multiprocessing
     world, spans = 2, [2000.0, 2500.0]
-    with mp.Manager() as m:
+    with multiprocessing.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.spawn(_rank, args=(world, _free_port(), spans, out), nprocs=world, join=True)
         res = dict(out)
