@@ -425,7 +425,7 @@ def run_adjoint(args, nk, workloads, ctx):
     xs = (P.get("u"), P.get("v"))
     P.picard_adjoint(ub, vb)                          # warm-up (graph capture of the linear solve)
     torch.cuda.synchronize()
-    _, _, grad, ast = P.picard_adjoint(ub, vb)
+    _, _, grad, _, ast = P.picard_adjoint(ub, vb)
     phi, H = P.get("phi"), P.get("H")
     cand = np.argwhere((phi > 0.5) & (H > 200.0))
     cells = [tuple(cand[k]) for k in np.random.default_rng(5).choice(len(cand), size=args.fd_cells, replace=False)]

@@ -264,11 +264,12 @@ nk_status nk_picard_solve(nk_problem* problem, nk_solve_stats* stats);
  * refreshed to c(x*), then λ ← A⁻¹ (x̄ - (∂[A(c(x)) x*]/∂x)ᵀ λ) is iterated from λ = 0, each step one
  * preconditioned CG solve of the problem's linear control warm-started from λ, until
  * ‖λ⁺ - λ‖ ≤ max(reltol ‖λ⁺‖, abstol) (control; NULL = the problem's Picard control).  Returns λ = ∂J/∂τ
- * (lambda_u, lambda_v, same layout as U, V) and ∂J/∂log C per cell (grad_log_C, Nx x Ny); any output may be
+ * (lambda_u, lambda_v, same layout as U, V), ∂J/∂log C per cell (grad_log_C, Nx x Ny) and ∂J/∂log A in the
+ * layout of RATE_FACTOR (grad_log_A: Nx x Ny, or Nσ planes of them for a σ-grid rate factor); any output may be
  * NULL.  stats: picard_iterations = adjoint iterations, picard_change = ‖λ⁺ - λ‖, picard_norm = ‖λ‖,
  * status NK_NOT_CONVERGED when maxiter ended it.  U, V are left at x*. */
 nk_status nk_picard_adjoint(nk_problem* problem, const double* ubar, const double* vbar, const nk_iteration_control* control,
-                            double* lambda_u, double* lambda_v, double* grad_log_C, nk_solve_stats* stats);
+                            double* lambda_u, double* lambda_v, double* grad_log_C, double* grad_log_A, nk_solve_stats* stats);
 
 /* picard_solve! enqueued on the problem's stream without waiting (one CUDA-graph launch); independent problems
  * solved this way run concurrently on the device.  nk_problem_wait blocks until it has finished and returns its

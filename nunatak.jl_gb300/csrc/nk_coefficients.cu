@@ -529,6 +529,19 @@ __global__ void k_adjoint_viscosity(AdjointView v) {
     const PhysView& ph = v.ph;
     double S = effective_strain_rate2(g, v.xs, i, j, ph.wall_factor) + ph.eps0 * ph.eps0;
     v.gbar[k] = eb * v.o.coef[k].x * ((1 - ph.n) / (2 * ph.n)) / S;
+    if (v.grad_log_A) {
+        // η = ½ A^(-1/n) S^((1-n)/2n): ∂η/∂log A = -η / n; with a 2-D A every layer shares it, so the cell's
+        // gradient is -η̄H̄ η̄H / n, and with a σ-grid A layer k carries -η̄H̄ μ H Δζₖ ηₖ / n
+        if (ph.rate_sigma) {
+            double muH = (ph.use_mask ? ph.mu[k] : 1.0) * ph.H[k];
+            for (int l = 0; l < ph.sig.N; ++l) {
+                long long o = (long long)l * ph.plane + k;
+                v.grad_log_A[o] = -eb * (muH * ph.sig.dz[l] * v.eta_sigma[o]) / ph.n;
+            }
+        } else {
+            v.grad_log_A[k] = -eb * v.o.coef[k].x / ph.n;
+        }
+    }
 }
 void launch_adjoint_viscosity(const AdjointView& v, cudaStream_t s) {
     LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);

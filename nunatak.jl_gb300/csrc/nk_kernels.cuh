@@ -116,6 +116,9 @@ struct AdjointView {
     double* gbar;                 // ∂/∂(ε̇ₑ² + ε̇₀²) at centre (i, j)
     double2* r;                   // x̄ − (∂[A(c(x)) x*]/∂x)ᵀ λ
     double* grad_log_C;           // −λᵀ ∂[A(c) x*]/∂ log C per cell
+    const double* eta_sigma;      // ησ of c(x*) (Nσ planes)
+    double* grad_log_A;           // −λᵀ ∂[A(c) x*]/∂ log A per cell (2-D rate factor) or per cell and layer (σ);
+                                  // written by k_adjoint_viscosity when not null
 };
 void launch_adjoint_coefficients(const AdjointView& v, cudaStream_t s);
 void launch_adjoint_viscosity(const AdjointView& v, cudaStream_t s);

@@ -194,6 +194,7 @@ struct nk_problem {
     double2* adj_xbar = nullptr;
     double* adj_g = nullptr;
     double* adj_grad = nullptr;
+    double* adj_grad_A = nullptr;                // Nσ planes (the first alone for a 2-D rate factor)
 
     // ---- views ---------------------------------------------------------------------------------------------
     OpView<double> fine_op() const {
@@ -1257,16 +1258,17 @@ nk_status nk_adjoint_solve(nk_problem* P, const double* bu, const double* bv, nk
 // from λ = 0 with the problem's preconditioned CG warm-started from the previous λ, until
 // ‖λ⁺ - λ‖ ≤ max(reltol ‖λ⁺‖, abstol).  Then b̄ = λ and p̄ = -(∂[A(c(p)) x*]/∂p)ᵀ λ.
 static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar, const nk_iteration_control& ctl, double* lu,
-                           double* lv, double* grad, nk_solve_stats* st) {
+                           double* lv, double* grad, double* grad_A, nk_solve_stats* st) {
     if (P->pd.stress_balance == NK_DIVA)
         bad("nk_picard_adjoint covers the SSA; the DIVA step's lagged basal-drag state is not differentiated");
     cudaStream_t s = P->stream;
     size_t pl = P->plane;
     if (!P->adj_base) {
-        NK_CUDA(cudaMalloc(&P->adj_base, pl * (sizeof(double2) + 2 * sizeof(double))));
+        NK_CUDA(cudaMalloc(&P->adj_base, pl * (sizeof(double2) + (2 + (size_t)P->Ns) * sizeof(double))));
         P->adj_xbar = (double2*)P->adj_base;
         P->adj_g = (double*)(P->adj_xbar + pl);
         P->adj_grad = P->adj_g + pl;
+        P->adj_grad_A = P->adj_grad + pl;
     }
     NK_CUDA(cudaMemcpyAsync(P->xprev, P->x, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));   // x*
     update_coefficients(P);                                                                         // c(x*)
@@ -1285,6 +1287,8 @@ static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar
     v.gbar = P->adj_g;
     v.r = P->tmp_b;
     v.grad_log_C = P->adj_grad;
+    v.eta_sigma = P->eta_sigma;
+    v.grad_log_A = nullptr;   // only in the final pass
     bool fixed = ctl.kind == NK_FIXED_ITERATIONS;
     int limit = fixed ? ctl.iterations : ctl.maxiter;
     int it = 0, cg_total = 0, cg_last = 0;
@@ -1309,6 +1313,10 @@ static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar
         if (!std::isfinite(D) || cg_failed) break;
     }
     launch_adjoint_coefficients(v, s);
+    if (grad_A) {
+        v.grad_log_A = P->adj_grad_A;
+        launch_adjoint_viscosity(v, s);
+    }
     launch_adjoint_gradient(v, s);
     NK_CHECK_LAUNCH();
     if (lu && lv) vector_out(P, P->tmp_a, lu, lv);
@@ -1318,6 +1326,14 @@ static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar
         f.nx = P->Nx;
         f.ny = P->Ny;
         copy_out(P, f, grad);
+    }
+    if (grad_A) {
+        FieldLoc f;
+        f.base = P->adj_grad_A;
+        f.nx = P->Nx;
+        f.ny = P->Ny;
+        f.planes = P->pd.rate_factor_layout == NK_RATE_FACTOR_SIGMA ? P->Ns : 1;
+        copy_out(P, f, grad_A);
     }
     NK_CUDA(cudaMemcpyAsync(P->x, P->xprev, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));   // U, V = x*
     NK_CUDA(cudaStreamSynchronize(s));
@@ -1334,7 +1350,7 @@ static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar
 }
 
 nk_status nk_picard_adjoint(nk_problem* P, const double* ubar, const double* vbar, const nk_iteration_control* control,
-                            double* lambda_u, double* lambda_v, double* grad_log_C, nk_solve_stats* stats) {
+                            double* lambda_u, double* lambda_v, double* grad_log_C, double* grad_log_A, nk_solve_stats* stats) {
     if (!P || !ubar || !vbar) return NK_BAD_ARGUMENT;
     return guarded(P->ctx, [&] {
         nk_iteration_control ctl = control ? *control : P->sd.picard;
@@ -1342,7 +1358,7 @@ nk_status nk_picard_adjoint(nk_problem* P, const double* ubar, const double* vba
         nk_solve_stats local{};
         nk_solve_stats* st = stats ? stats : &local;
         NK_CUDA(cudaEventRecord(P->ev0, P->stream));
-        picard_adjoint(P, ubar, vbar, ctl, lambda_u, lambda_v, grad_log_C, st);
+        picard_adjoint(P, ubar, vbar, ctl, lambda_u, lambda_v, grad_log_C, grad_log_A, st);
         NK_CUDA(cudaEventRecord(P->ev1, P->stream));
         NK_CUDA(cudaEventSynchronize(P->ev1));
         event_times(P, st);

@@ -185,18 +185,19 @@ class Problem:
 
     def picard_adjoint(self, ubar, vbar, control=None):
         """Fixed-point adjoint of the converged picard_solve! (the reverse rule of ext/NunatakEnzymeExt.jl:167-240)
-        for x̄ = (ubar, vbar) = ∂J/∂(u, v): returns (λu, λv, ∂J/∂log C per cell, stats), λ being ∂J/∂τ.
-        `control` is a Convergence / FixedIterations (default: the Picard control)."""
+        for x̄ = (ubar, vbar) = ∂J/∂(u, v): returns (λu, λv, ∂J/∂log C per cell, ∂J/∂log A in the layout of the rate
+        factor, stats), λ being ∂J/∂τ.  `control` is a Convergence / FixedIterations (default: the Picard control)."""
         ub, vb = self._vec_in(ubar, vbar)
         lu, lv = np.empty(self.shape("u")), np.empty(self.shape("v"))
         grad = np.empty((self.grid.Ny, self.grid.Nx))
+        grad_a = np.empty(self.shape("A"))
         stats = abi.SolveStats()
         ctl = C.byref(control.desc()) if control is not None else None
         st = self._fn("picard_adjoint")(self._h, ub.ctypes.data_as(_dptr), vb.ctypes.data_as(_dptr), ctl,
                                         lu.ctypes.data_as(_dptr), lv.ctypes.data_as(_dptr), grad.ctypes.data_as(_dptr),
-                                        C.byref(stats))
+                                        grad_a.ctypes.data_as(_dptr), C.byref(stats))
         _check(st, "picard_adjoint", self._err())
-        return lu, lv, grad, stats
+        return lu, lv, grad, grad_a, stats
 
     def query(self):
         """True once the asynchronous solve has finished (wait() then returns at once)."""
