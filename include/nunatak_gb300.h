@@ -176,7 +176,15 @@ typedef struct nk_solver_desc {
 #define NK_FIELD_U_SIGMA       24   /* model.velocities.u_sigma             Face-Center x sigma */
 #define NK_FIELD_V_SIGMA       25   /* model.velocities.v_sigma             Center-Face x sigma */
 #define NK_FIELD_TEMPERATURE   26   /* temperature on the sigma grid (input of nk_compute_rate_factor) */
-#define NK_FIELD_COUNT         27
+/* Prescribed velocities (an extension; the reference has no velocity boundary condition): NaN = free, a finite
+ * value = that face's velocity is held at it.  Such a face solves an identity row (x = u_D) and its value enters
+ * the neighbouring strain rates, viscosity and stresses, also on the boundary faces that are walls otherwise
+ * (an inflow at x = 0 is u_D on the faces i = 0).  Setting either field: the driving stress (the right-hand side)
+ * and the velocity take u_D there, and nk_compute_geometry keeps them.  Problems with prescribed velocities
+ * refuse nk_adjoint_solve and nk_picard_adjoint (the lifted operator is not symmetric) with NK_BAD_ARGUMENT. */
+#define NK_FIELD_U_PRESCRIBED  27   /* u_D                                  Face-Center */
+#define NK_FIELD_V_PRESCRIBED  28   /* v_D                                  Center-Face */
+#define NK_FIELD_COUNT         29
 
 typedef struct nk_solve_stats {
     int32_t status;                   /* nk_status of the solve */

@@ -10,24 +10,27 @@
 namespace nk {
 
 // ---- wall-masked velocities of the viscosity (interior_u / interior_v without η̄H, strain_rates.jl:5-6) ----
-__device__ __forceinline__ double wall_u(const DevGrid<double>& g, const double2* __restrict__ x, int i, int j) {
-    return g.peripheral_fc(i, j) ? 0.0 : x[g.u_idx(i, j)].x;
+// A prescribed face on the boundary passes its value (the Dirichlet extension; `ud` NaN where free).
+__device__ __forceinline__ double wall_u(const DevGrid<double>& g, const double2* __restrict__ x, const double2* ud, int i, int j) {
+    return (g.peripheral_fc(i, j) && !prescribed_u(g, ud, i, j)) ? 0.0 : x[g.u_idx(i, j)].x;
 }
-__device__ __forceinline__ double wall_v(const DevGrid<double>& g, const double2* __restrict__ x, int i, int j) {
-    return g.peripheral_cf(i, j) ? 0.0 : x[g.v_idx(i, j)].y;
+__device__ __forceinline__ double wall_v(const DevGrid<double>& g, const double2* __restrict__ x, const double2* ud, int i, int j) {
+    return (g.peripheral_cf(i, j) && !prescribed_v(g, ud, i, j)) ? 0.0 : x[g.v_idx(i, j)].y;
 }
-__device__ __forceinline__ double strain_xy(const DevGrid<double>& g, const double2* __restrict__ x, int i, int j, double wf) {
-    double dudy = (wall_u(g, x, i, j) - wall_u(g, x, i, j - 1)) * g.rdyf[j];
-    double dvdx = (wall_v(g, x, i, j) - wall_v(g, x, i - 1, j)) * g.rdxf[i];
+__device__ __forceinline__ double strain_xy(const DevGrid<double>& g, const double2* __restrict__ x, const double2* ud, int i, int j,
+                                            double wf) {
+    double dudy = (wall_u(g, x, ud, i, j) - wall_u(g, x, ud, i, j - 1)) * g.rdyf[j];
+    double dvdx = (wall_v(g, x, ud, i, j) - wall_v(g, x, ud, i - 1, j)) * g.rdxf[i];
     double e = (dudy + dvdx) / 2;
     return g.peripheral_ff(i, j) ? wf * e : e;
 }
 // effective_strain_rate², strain_rates.jl:116-121
-__device__ __forceinline__ double effective_strain_rate2(const DevGrid<double>& g, const double2* __restrict__ x, int i, int j, double wf) {
-    double exx = (wall_u(g, x, i + 1, j) - wall_u(g, x, i, j)) * g.rdxc[i];
-    double eyy = (wall_v(g, x, i, j + 1) - wall_v(g, x, i, j)) * g.rdyc[j];
-    double e00 = strain_xy(g, x, i, j, wf), e10 = strain_xy(g, x, i + 1, j, wf);
-    double e01 = strain_xy(g, x, i, j + 1, wf), e11 = strain_xy(g, x, i + 1, j + 1, wf);
+__device__ __forceinline__ double effective_strain_rate2(const DevGrid<double>& g, const double2* __restrict__ x, const double2* ud,
+                                                         int i, int j, double wf) {
+    double exx = (wall_u(g, x, ud, i + 1, j) - wall_u(g, x, ud, i, j)) * g.rdxc[i];
+    double eyy = (wall_v(g, x, ud, i, j + 1) - wall_v(g, x, ud, i, j)) * g.rdyc[j];
+    double e00 = strain_xy(g, x, ud, i, j, wf), e10 = strain_xy(g, x, ud, i + 1, j, wf);
+    double e01 = strain_xy(g, x, ud, i, j + 1, wf), e11 = strain_xy(g, x, ud, i + 1, j + 1, wf);
     double exy2 = ((e00 * e00 + e10 * e10) / 2 + (e01 * e01 + e11 * e11) / 2) / 2;
     return exx * exx + eyy * eyy + exx * eyy + exy2;
 }
@@ -48,7 +51,7 @@ __global__ void k_viscosity(PhysView ph, const double2* __restrict__ x, double* 
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i >= g.Nx || j >= g.Ny) return;
     int c = g.idx(i, j);
-    double ee = effective_strain_rate2(g, x, i, j, ph.wall_factor) + ph.eps0 * ph.eps0;
+    double ee = effective_strain_rate2(g, x, ph.ud, i, j, ph.wall_factor) + ph.eps0 * ph.eps0;
     double eta_bar = 0.0, F = 0.0;
     double eta_uniform = ph.rate_sigma ? 0.0 : glen(ph.A[c], ee, ph.n);
     for (int k = 0; k < ph.sig.N; ++k) {
@@ -74,7 +77,7 @@ __global__ void k_viscosity_diva(PhysView ph, const double2* __restrict__ x, con
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i >= g.Nx || j >= g.Ny) return;
     int c = g.idx(i, j);
-    double e2 = effective_strain_rate2(g, x, i, j, ph.wall_factor);
+    double e2 = effective_strain_rate2(g, x, ph.ud, i, j, ph.wall_factor);
     int u0 = g.u_idx(i, j), u1 = g.u_idx(i + 1, j), v0 = g.v_idx(i, j), v1 = g.v_idx(i, j + 1);
     double tx = (bb[u0].x * ub[u0].x + bb[u1].x * ub[u1].x) / 2;
     double ty = (bb[v0].y * ub[v0].y + bb[v1].y * ub[v1].y) / 2;
@@ -355,6 +358,7 @@ __global__ void k_driving_stress(GeometryView v) {
         if (v.gl_stress) tg = g.dyc[j] * gl_stress(v, cw, ce, straddles);
         double t = -g.Az_fc(i, j) * v.rho_i * v.gacc * ((v.H[cw] + v.H[ce]) / 2) * ((v.s[ce] - v.s[cw]) * g.rdxf[i]);
         tau.x = wall ? 0.0 : (front ? tf : (straddles ? tg : t));
+        if (prescribed_u(g, v.ud, i, j)) tau.x = v.ud[k].x;   // the identity row's right-hand side
     }
     if (i < g.Nx && (j < g.Ny || !g.py)) {   // _compute_y_driving_stress!, :118-125
         int cs = g.c_idx(i, j - 1), cn = g.c_idx(i, j);
@@ -370,6 +374,7 @@ __global__ void k_driving_stress(GeometryView v) {
         if (v.gl_stress) tg = g.dxc[i] * gl_stress(v, cs, cn, straddles);
         double t = -g.Az_cf(i, j) * v.rho_i * v.gacc * ((v.H[cs] + v.H[cn]) / 2) * ((v.s[cn] - v.s[cs]) * g.rdyf[j]);
         tau.y = wall ? 0.0 : (front ? tf : (straddles ? tg : t));
+        if (prescribed_v(g, v.ud, i, j)) tau.y = v.ud[k].y;
     }
     v.tau[k] = tau;
 }
@@ -527,7 +532,7 @@ __global__ void k_adjoint_viscosity(AdjointView v) {
     for (int a = 0; a < nx; ++a)
         for (int b = 0; b < ny; ++b) eb += (wx[a] * wy[b]) * v.cbar[g.idx(fx[a], fy[b])].y / 4;
     const PhysView& ph = v.ph;
-    double S = effective_strain_rate2(g, v.xs, i, j, ph.wall_factor) + ph.eps0 * ph.eps0;
+    double S = effective_strain_rate2(g, v.xs, ph.ud, i, j, ph.wall_factor) + ph.eps0 * ph.eps0;
     v.gbar[k] = eb * v.o.coef[k].x * ((1 - ph.n) / (2 * ph.n)) / S;
     if (v.grad_log_A) {
         // η = ½ A^(-1/n) S^((1-n)/2n): ∂η/∂log A = -η / n; with a 2-D A every layer shares it, so the cell's
@@ -571,15 +576,16 @@ __device__ __forceinline__ bool first_time(int* seen, int& n, int k) {
 __device__ double strain_sensitivity(const DevGrid<double>& g, const double2* __restrict__ x, double wf, int ci, int cj, int k, int comp) {
     auto uref = [&](int a, int b) { return !g.peripheral_fc(a, b) && g.u_idx(a, b) == k; };
     auto vref = [&](int a, int b) { return !g.peripheral_cf(a, b) && g.v_idx(a, b) == k; };
-    double exx = (wall_u(g, x, ci + 1, cj) - wall_u(g, x, ci, cj)) * g.rdxc[ci];
-    double eyy = (wall_v(g, x, ci, cj + 1) - wall_v(g, x, ci, cj)) * g.rdyc[cj];
+    // no prescribed faces here: the adjoint is refused for problems that have them
+    double exx = (wall_u(g, x, nullptr, ci + 1, cj) - wall_u(g, x, nullptr, ci, cj)) * g.rdxc[ci];
+    double eyy = (wall_v(g, x, nullptr, ci, cj + 1) - wall_v(g, x, nullptr, ci, cj)) * g.rdyc[cj];
     double d = 0.0;
     if (comp == 0) d += (2 * exx + eyy) * g.rdxc[ci] * ((double)uref(ci + 1, cj) - (double)uref(ci, cj));
     else d += (2 * eyy + exx) * g.rdyc[cj] * ((double)vref(ci, cj + 1) - (double)vref(ci, cj));
     for (int a = 0; a < 2; ++a)
         for (int b = 0; b < 2; ++b) {
             int fi = ci + a, fj = cj + b;
-            double e = strain_xy(g, x, fi, fj, wf);
+            double e = strain_xy(g, x, nullptr, fi, fj, wf);
             double sf = g.peripheral_ff(fi, fj) ? wf : 1.0;
             double de = comp == 0 ? sf / 2 * g.rdyf[fj] * ((double)uref(fi, fj) - (double)uref(fi, fj - 1))
                                   : sf / 2 * g.rdxf[fi] * ((double)vref(fi, fj) - (double)vref(fi - 1, fj));

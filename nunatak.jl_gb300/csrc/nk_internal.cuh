@@ -41,6 +41,14 @@ constexpr uint8_t U_INACTIVE = 1;   // u point is a wall or ice free: identity r
 constexpr uint8_t V_INACTIVE = 2;
 constexpr uint8_t U_WALL = 4;       // wall (peripheral) only: the viscosity masks walls, not ice-free points
 constexpr uint8_t V_WALL = 8;
+// Prescribed velocity (the Dirichlet extension; the reference has none): the row is an identity row (the bit comes
+// with U_INACTIVE / V_INACTIVE) whose value, held fixed at the prescribed one, still enters the strain rates.
+constexpr uint8_t U_DIRICHLET = 16;
+constexpr uint8_t V_DIRICHLET = 32;
+// Read as zero in the strain rates: inactive and not prescribed.  Kept as its own bit so that the hot reads of
+// the operator test one bit.
+constexpr uint8_t U_ZERO = 64;
+constexpr uint8_t V_ZERO = 128;
 
 template <typename T> struct Vec2;
 template <> struct Vec2<double> { using type = double2; };
@@ -80,6 +88,18 @@ struct DevGrid {
     __device__ __forceinline__ T Az_cf(int i, int j) const { return dxc[i] * dyf[j]; }
     __device__ __forceinline__ T Az_cc(int i, int j) const { return dxc[i] * dyc[j]; }
 };
+
+// A velocity prescribed at the u face (i, j) / v face (i, j).  Prescribable faces are those of the solved rows,
+// (i, j) in 0..Nx-1 x 0..Ny-1 (wrapped when periodic): the west and south boundary faces of a Bounded direction
+// and every interior face, but not the east / north boundary faces, which no row of the operator solves.
+__device__ __forceinline__ bool prescribed_u(const DevGrid<double>& g, const double2* ud, int i, int j) {
+    if (!ud || (!g.px && (i < 0 || i >= g.Nx)) || (!g.py && (j < 0 || j >= g.Ny))) return false;
+    return !isnan(ud[g.idx(g.px ? g.wrap(i, g.Nx) : i, g.py ? g.wrap(j, g.Ny) : j)].x);
+}
+__device__ __forceinline__ bool prescribed_v(const DevGrid<double>& g, const double2* ud, int i, int j) {
+    if (!ud || (!g.px && (i < 0 || i >= g.Nx)) || (!g.py && (j < 0 || j >= g.Ny))) return false;
+    return !isnan(ud[g.idx(g.px ? g.wrap(i, g.Nx) : i, g.py ? g.wrap(j, g.Ny) : j)].y);
+}
 
 // Per-solve scalars of conjugate gradients and Picard, device resident.
 struct SolverScalars {

@@ -31,6 +31,7 @@ struct PhysView {
     const double* mu;
     const double2* phi;           // (phi_u, phi_v)
     int use_mask, use_N;
+    const double2* ud = nullptr;  // prescribed (u, v) per face, NaN where free
 };
 
 // ---- layout conversion ---------------------------------------------------------------------------------
@@ -45,7 +46,9 @@ void launch_fill(double* dst, int count, double value, cudaStream_t s);
 void launch_apply(const OpView<double>& o, const double2* p, double2* q, cudaStream_t s);
 // mask bits from eta_H and the topology, over 0..Nx x 0..Ny
 template <typename T>
-void launch_mask(const OpView<T>& o, uint8_t* mask, cudaStream_t s);
+void launch_mask(const OpView<T>& o, uint8_t* mask, cudaStream_t s, const double2* ud = nullptr);
+// x = val on the prescribed faces (ud finite)
+void launch_impose_prescribed(const DevGrid<double>& g, double2* x, const double2* ud, const double2* val, cudaStream_t s);
 // inverse diagonal (Jacobi) of the fine grid
 void launch_inverse_diagonal(const OpView<double>& o, double2* invd, cudaStream_t s);
 template <typename T>
@@ -139,6 +142,7 @@ struct GeometryView {
     double rho_i, rho_w, gacc;
     int grounding, gl_stress, use_mask;
     double mask_min, mask_trans;
+    const double2* ud = nullptr;  // prescribed (u, v) per face, NaN where free: the right-hand side there
 };
 void launch_geometry(const GeometryView& v, cudaStream_t s);
 void launch_rate_factor(const DevGrid<double>& g, const SigmaTable& sig, int plane, const double* H, const double* T, double* A,

@@ -461,7 +461,7 @@ __global__ void __launch_bounds__(1024, 1)
                 int k = g.idx(g.px ? g.wrap(i, Nx) : i, g.py ? g.wrap(j, Ny) : j);
                 uint8_t mk = L.o.mask[k];
                 pk[a] = k;
-                pf[a] = (uok && !(mk & U_INACTIVE) ? 1 : 0) | (vok && !(mk & V_INACTIVE) ? 2 : 0);
+                pf[a] = (uok && !(mk & U_ZERO) ? 1 : 0) | (vok && !(mk & V_ZERO) ? 2 : 0);
             }
         }
     }

@@ -14,24 +14,25 @@ template <typename T>
 struct OpView {
     DevGrid<T> g;
     const typename Vec4<T>::type* coef;   // (eta_H, eta_H_ff, beta_u, beta_v) per (i, j)
-    const uint8_t* mask;                  // U_INACTIVE | V_INACTIVE | U_WALL | V_WALL per (i, j)
+    const uint8_t* mask;                  // U/V_INACTIVE, _WALL, _DIRICHLET, _ZERO bits per (i, j)
     T wall_factor;                        // wall_shear_factor: 0 free slip, 2 no slip (ssa_operator.jl:100-101)
 };
 
-// interior_u / interior_v (ssa_operator.jl:94-95) with the operator's mask (walls and ice-free points).
+// interior_u / interior_v (ssa_operator.jl:94-95) with the operator's mask (walls and ice-free points); a prescribed
+// face passes its value (U_DIRICHLET / V_DIRICHLET).
 template <typename T, typename V2>
 __device__ __forceinline__ T masked_u(const OpView<T>& o, const V2* __restrict__ p, int i, int j) {
     const DevGrid<T>& g = o.g;
     if ((!g.px && (i < 0 || i > g.Nx)) || g.out_y(j)) return T(0);
     int k = g.idx(g.px ? g.wrap(i, g.Nx) : i, g.py ? g.wrap(j, g.Ny) : j);
-    return (__ldg(o.mask + k) & U_INACTIVE) ? T(0) : p[k].x;
+    return (__ldg(o.mask + k) & U_ZERO) ? T(0) : p[k].x;
 }
 template <typename T, typename V2>
 __device__ __forceinline__ T masked_v(const OpView<T>& o, const V2* __restrict__ p, int i, int j) {
     const DevGrid<T>& g = o.g;
     if (g.out_x(i) || (!g.py && (j < 0 || j > g.Ny))) return T(0);
     int k = g.idx(g.px ? g.wrap(i, g.Nx) : i, g.py ? g.wrap(j, g.Ny) : j);
-    return (__ldg(o.mask + k) & V_INACTIVE) ? T(0) : p[k].y;
+    return (__ldg(o.mask + k) & V_ZERO) ? T(0) : p[k].y;
 }
 
 // Δy Txx and Δx Tyy at centre (i, j): normal_stress_xx/yy times the face length (ssa_operator.jl:60-65).

@@ -195,6 +195,9 @@ struct nk_problem {
     double* adj_g = nullptr;
     double* adj_grad = nullptr;
     double* adj_grad_A = nullptr;                // Nσ planes (the first alone for a 2-D rate factor)
+    // Prescribed velocities (u_D, v_D) per face, NaN where free; allocated by the first set of either prescribed
+    // field.  Its faces become identity rows whose values enter their neighbours' strain rates.
+    double2* ud = nullptr;
 
     // ---- views ---------------------------------------------------------------------------------------------
     OpView<double> fine_op() const {
@@ -235,6 +238,7 @@ struct nk_problem {
         ph.phi = phi_uv;
         ph.use_mask = pd.use_ice_mask;
         ph.use_N = pd.use_effective_pressure;
+        ph.ud = ud;
         return ph;
     }
     template <typename TT>
@@ -466,7 +470,7 @@ static void build(nk_problem* P, bool dry = false) {
 // Mask (and the Jacobi inverse diagonal) after η̄H, η̄Hᶠᶠ or β changed.
 static void prepare_operator(nk_problem* P) {
     OpView<double> o = P->fine_op();
-    launch_mask<double>(o, P->fine.mask, P->stream);
+    launch_mask<double>(o, P->fine.mask, P->stream, P->ud);
     if (P->precond == NK_PRECONDITIONER_DIAGONAL) launch_inverse_diagonal(o, P->invd, P->stream);
     NK_CHECK_LAUNCH();
 }
@@ -852,8 +856,17 @@ static void host_picard(nk_problem* P) {
     }
 }
 
+// The warm start takes the prescribed values, so the identity rows start (and stay) solved: their residual is
+// zero and the conjugate-gradient directions vanish there.
+static void impose_prescribed(nk_problem* P, const double2* val) {
+    if (!P->ud) return;
+    launch_impose_prescribed(P->fine.g, P->x, P->ud, val, P->stream);
+    NK_CHECK_LAUNCH();
+}
+
 // solve!(x, solver, b, ...) with b already on the device in tmp_b
 static void linear_solve(nk_problem* P, nk_solve_stats* st) {
+    impose_prescribed(P, P->tmp_b);   // an identity row's solution is its right-hand side
     if (!use_graphs()) {
         set_control(P);
         host_cg(P, P->tmp_b);
@@ -871,6 +884,7 @@ static void linear_solve(nk_problem* P, nk_solve_stats* st) {
 
 // picard_solve!, picard.jl:63-90
 static void picard_solve(nk_problem* P, nk_solve_stats* st) {
+    impose_prescribed(P, P->ud);
     if (!use_graphs()) {
         set_control(P);
         host_picard(P);
@@ -910,6 +924,7 @@ struct FieldLoc {
     double* base = nullptr;   // pitched device array (first plane)
     int stride = 1, offset = 0, nx = 0, ny = 0, planes = 1;
     bool coef = false;        // a coefficient: the operator mask and diagonal follow it
+    bool prescribed = false;  // a prescribed velocity (allocated on first use)
 };
 
 static FieldLoc field_loc(nk_problem* P, int id) {
@@ -948,9 +963,24 @@ static FieldLoc field_loc(nk_problem* P, int id) {
         case NK_FIELD_U_SIGMA: fu(P->usig); f.planes = P->Ns; break;
         case NK_FIELD_V_SIGMA: fv(P->usig); f.planes = P->Ns; break;
         case NK_FIELD_TEMPERATURE: if (P->T) { cc(P->T); f.planes = P->Ns; } break;
+        case NK_FIELD_U_PRESCRIBED: fu(P->ud); f.prescribed = true; break;
+        case NK_FIELD_V_PRESCRIBED: fv(P->ud); f.prescribed = true; break;
         default: break;
     }
     return f;
+}
+
+// The prescribed-velocity pairs, all NaN (free) at first.  Graphs captured before hold no pointer to them and
+// are rebuilt.
+static void ensure_prescribed(nk_problem* P) {
+    if (P->ud) return;
+    NK_CUDA(cudaMalloc((void**)&P->ud, P->plane * sizeof(double2)));
+    launch_fill((double*)P->ud, (int)(2 * P->plane), std::nan(""), P->stream);
+    NK_CHECK_LAUNCH();
+    if (P->picard_exec) { cudaGraphExecDestroy(P->picard_exec); P->picard_exec = nullptr; }
+    if (P->linear_exec) { cudaGraphExecDestroy(P->linear_exec); P->linear_exec = nullptr; }
+    if (P->picard_graph) { cudaGraphDestroy(P->picard_graph); P->picard_graph = nullptr; }
+    if (P->linear_graph) { cudaGraphDestroy(P->linear_graph); P->linear_graph = nullptr; }
 }
 
 static void copy_in(nk_problem* P, const FieldLoc& f, const double* host) {
@@ -1111,6 +1141,7 @@ nk_status nk_problem_destroy(nk_problem* P) {
     if (P->ev0) cudaEventDestroy(P->ev0);
     if (P->ev1) cudaEventDestroy(P->ev1);
     if (P->adj_base) cudaFree(P->adj_base);
+    if (P->ud) cudaFree(P->ud);
     if (P->stream) cudaStreamDestroy(P->stream);
     delete P;
     return NK_OK;
@@ -1119,17 +1150,27 @@ nk_status nk_problem_destroy(nk_problem* P) {
 int64_t nk_problem_field_size(const nk_problem* P, int32_t id) {
     if (!P) return 0;
     FieldLoc f = field_loc(const_cast<nk_problem*>(P), id);
-    return f.base ? (int64_t)f.nx * f.ny * f.planes : 0;
+    return (f.base || f.prescribed) ? (int64_t)f.nx * f.ny * f.planes : 0;
 }
 
 nk_status nk_problem_set_field(nk_problem* P, int32_t id, const double* host, int64_t count) {
     if (!P || !host) return NK_BAD_ARGUMENT;
     return guarded(P->ctx, [&] {
         FieldLoc f = field_loc(P, id);
+        if (f.prescribed) {
+            if (count != (int64_t)f.nx * f.ny * f.planes) bad("field size mismatch");
+            ensure_prescribed(P);
+            f = field_loc(P, id);
+        }
         if (!f.base) bad("unknown field id or field not held by this problem");
         if (count != (int64_t)f.nx * f.ny * f.planes) bad("field size mismatch");
         copy_in(P, f, host);
-        if (f.coef) prepare_operator(P);
+        if (f.coef || f.prescribed) prepare_operator(P);
+        if (f.prescribed) {   // the right-hand side and the velocity of the identity rows
+            launch_impose_prescribed(P->fine.g, P->tau, P->ud, P->ud, P->stream);
+            launch_impose_prescribed(P->fine.g, P->x, P->ud, P->ud, P->stream);
+            NK_CHECK_LAUNCH();
+        }
         NK_CUDA(cudaStreamSynchronize(P->stream));
     });
 }
@@ -1139,6 +1180,10 @@ nk_status nk_problem_get_field(const nk_problem* Pc, int32_t id, double* host, i
     if (!P || !host) return NK_BAD_ARGUMENT;
     return guarded(P->ctx, [&] {
         FieldLoc f = field_loc(P, id);
+        if (f.prescribed) {
+            ensure_prescribed(P);
+            f = field_loc(P, id);
+        }
         if (!f.base) bad("unknown field id or field not held by this problem");
         if (count != (int64_t)f.nx * f.ny * f.planes) bad("field size mismatch");
         copy_out(P, f, host);
@@ -1154,6 +1199,7 @@ nk_status nk_compute_geometry(nk_problem* P) {
         v.rho_i = P->pd.ice_density; v.rho_w = P->pd.ocean_density; v.gacc = P->pd.gravitational_acceleration;
         v.grounding = P->pd.grounding; v.gl_stress = P->pd.grounding_line_driving_stress; v.use_mask = P->pd.use_ice_mask;
         v.mask_min = P->pd.mask_minimum_thickness; v.mask_trans = P->pd.mask_transition_thickness;
+        v.ud = P->ud;
         launch_geometry(v, P->stream);
         NK_CHECK_LAUNCH();
         NK_CUDA(cudaStreamSynchronize(P->stream));
@@ -1250,6 +1296,10 @@ nk_status nk_linear_solve(nk_problem* P, const double* bu, const double* bv, nk_
 
 nk_status nk_adjoint_solve(nk_problem* P, const double* bu, const double* bv, nk_solve_stats* stats) {
     if (!P || !bu || !bv) return NK_BAD_ARGUMENT;
+    if (P->ud) {   // identity rows with lifted neighbours are not symmetric
+        if (P->ctx) P->ctx->error = "nk_adjoint_solve: not available for a problem with prescribed velocities";
+        return NK_BAD_ARGUMENT;
+    }
     return linear_solve_impl(P, bu, bv, stats);   // the operator is self-adjoint (conjugate_gradient.jl:186-189)
 }
 
@@ -1261,6 +1311,7 @@ static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar
                            double* lv, double* grad, double* grad_A, nk_solve_stats* st) {
     if (P->pd.stress_balance == NK_DIVA)
         bad("nk_picard_adjoint covers the SSA; the DIVA step's lagged basal-drag state is not differentiated");
+    if (P->ud) bad("nk_picard_adjoint: not available for a problem with prescribed velocities");
     cudaStream_t s = P->stream;
     size_t pl = P->plane;
     if (!P->adj_base) {
@@ -1387,6 +1438,7 @@ nk_status nk_picard_solve_async(nk_problem* P) {
         if (!P->picard_exec) build_picard_graph(P);
         set_control(P);
         NK_CUDA(cudaEventRecord(P->ev0, P->stream));
+        impose_prescribed(P, P->ud);
         NK_CUDA(cudaGraphLaunch(P->picard_exec, P->stream));
         NK_CUDA(cudaMemcpyAsync(P->sc_host, P->sc, sizeof(SolverScalars), cudaMemcpyDeviceToHost, P->stream));
         NK_CUDA(cudaEventRecord(P->ev1, P->stream));
@@ -1818,6 +1870,7 @@ static void start(nk_server* S, ServerRequest& R, Resident& r) {
     gv.rho_i = P->pd.ice_density; gv.rho_w = P->pd.ocean_density; gv.gacc = P->pd.gravitational_acceleration;
     gv.grounding = P->pd.grounding; gv.gl_stress = P->pd.grounding_line_driving_stress; gv.use_mask = P->pd.use_ice_mask;
     gv.mask_min = P->pd.mask_minimum_thickness; gv.mask_trans = P->pd.mask_transition_thickness;
+    gv.ud = P->ud;
     launch_geometry(gv, s);
     set_control(P);
     if (use_graphs()) {

@@ -83,9 +83,10 @@ void launch_apply(const OpView<double>& o, const double2* p, double2* q, cudaStr
     count_launch();
 }
 
-// inactiveᶠᶜᶜ / inactiveᶜᶠᶜ with η̄H (ssa_operator.jl:91-92, smooth_ice_mask.jl:429-430) and the wall bits
+// inactiveᶠᶜᶜ / inactiveᶜᶠᶜ with η̄H (ssa_operator.jl:91-92, smooth_ice_mask.jl:429-430) and the wall bits; `ud` (the
+// fine level only) marks prescribed faces as identity rows that keep their value (U_DIRICHLET / V_DIRICHLET)
 template <typename T>
-__global__ void k_mask(OpView<T> o, uint8_t* mask) {
+__global__ void k_mask(OpView<T> o, uint8_t* mask, const double2* ud) {
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     const DevGrid<T>& g = o.g;
     if (i > g.Nx || j > g.Ny) return;
@@ -97,15 +98,40 @@ __global__ void k_mask(OpView<T> o, uint8_t* mask) {
     if (wv) m |= V_WALL;
     if (wu || fu) m |= U_INACTIVE;
     if (wv || fv) m |= V_INACTIVE;
+    if (ud && i < g.Nx && j < g.Ny) {   // the faces of the solved rows (prescribed_u / prescribed_v)
+        double2 d = ud[g.idx(i, j)];
+        if (!isnan(d.x)) m |= U_DIRICHLET | U_INACTIVE;
+        if (!isnan(d.y)) m |= V_DIRICHLET | V_INACTIVE;
+    }
+    if ((m & U_INACTIVE) && !(m & U_DIRICHLET)) m |= U_ZERO;
+    if ((m & V_INACTIVE) && !(m & V_DIRICHLET)) m |= V_ZERO;
     mask[g.idx(i, j)] = m;
 }
 template <typename T>
-void launch_mask(const OpView<T>& o, uint8_t* mask, cudaStream_t s) {
+void launch_mask(const OpView<T>& o, uint8_t* mask, cudaStream_t s, const double2* ud) {
     LaunchDims d = dims2d(o.g.Nx + 1, o.g.Ny + 1);
-    k_mask<T><<<d.grid, d.block, 0, s>>>(o, mask); count_launch();
+    k_mask<T><<<d.grid, d.block, 0, s>>>(o, mask, ud); count_launch();
 }
-template void launch_mask<double>(const OpView<double>&, uint8_t*, cudaStream_t);
-template void launch_mask<float>(const OpView<float>&, uint8_t*, cudaStream_t);
+template void launch_mask<double>(const OpView<double>&, uint8_t*, cudaStream_t, const double2*);
+template void launch_mask<float>(const OpView<float>&, uint8_t*, cudaStream_t, const double2*);
+
+// x = val on the prescribed faces (those where ud is finite): the identity rows' values before a solve
+__global__ void k_impose_prescribed(DevGrid<double> g, double2* x, const double2* __restrict__ ud, const double2* __restrict__ val) {
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;   // the faces of the solved rows (prescribed_u / prescribed_v)
+    int k = g.idx(i, j);
+    double2 d = ud[k];
+    bool cu = !isnan(d.x), cv = !isnan(d.y);
+    if (!(cu || cv)) return;
+    double2 v = x[k], w = val[k];
+    if (cu) v.x = w.x;
+    if (cv) v.y = w.y;
+    x[k] = v;
+}
+void launch_impose_prescribed(const DevGrid<double>& g, double2* x, const double2* ud, const double2* val, cudaStream_t s) {
+    LaunchDims d = dims2d(g.Nx, g.Ny);
+    k_impose_prescribed<<<d.grid, d.block, 0, s>>>(g, x, ud, val); count_launch();
+}
 
 __global__ void k_inverse_diagonal(OpView<double> o, double2* invd) {
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;

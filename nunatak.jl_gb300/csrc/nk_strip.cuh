@@ -53,8 +53,8 @@ struct StripRow {
     typename Vec2<T>::type raw;
     uint8_t m;
     bool uok, vok;
-    __device__ __forceinline__ T mu() const { return (uok && !(m & U_INACTIVE)) ? raw.x : T(0); }
-    __device__ __forceinline__ T mv() const { return (vok && !(m & V_INACTIVE)) ? raw.y : T(0); }
+    __device__ __forceinline__ T mu() const { return (uok && !(m & U_ZERO)) ? raw.x : T(0); }
+    __device__ __forceinline__ T mv() const { return (vok && !(m & V_ZERO)) ? raw.y : T(0); }
 };
 
 // The pair at (i, j) as masked_u / masked_v read it; zero outside the ranges those functions read.

@@ -31,6 +31,7 @@ FIELD_IDS = {
     "N": 9, "tau_u": 10, "tau_v": 11, "A": 12, "C": 13, "eta_H": 14, "eta_H_ff": 15,
     "beta_u": 16, "beta_v": 17, "eta_sigma": 18, "F2": 19, "beta_b_u": 20, "beta_b_v": 21,
     "u_b": 22, "v_b": 23, "u_sigma": 24, "v_sigma": 25, "T": 26,
+    "u_prescribed": 27, "v_prescribed": 28,
 }
 
 # (location x, location y, on the sigma grid) of each field: "c" Center, "f" Face.
@@ -44,6 +45,7 @@ FIELD_LOCATIONS = {
     "F2": ("c", "c", False), "beta_b_u": ("f", "c", False), "beta_b_v": ("c", "f", False),
     "u_b": ("f", "c", False), "v_b": ("c", "f", False), "u_sigma": ("f", "c", True),
     "v_sigma": ("c", "f", True), "T": ("c", "c", True),
+    "u_prescribed": ("f", "c", False), "v_prescribed": ("c", "f", False),
 }
 
 

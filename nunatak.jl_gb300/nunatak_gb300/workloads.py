@@ -85,10 +85,19 @@ def _centers(grid):
     return np.meshgrid(grid.centers(0), grid.centers(1))
 
 
-def channel_shelf(Nx=84, Ny=40, dx=1e3, velocity_solver=None):
+def west_inflow(grid, speed):
+    """u_prescribed with `speed` m/yr (stored in m/s) on the faces at the west edge (i = 0) and NaN (free) on every
+    other face."""
+    u = np.full((grid.Ny, grid.face_count(0)), np.nan)
+    u[:, 0] = speed / YEAR
+    return u
+
+
+def channel_shelf(Nx=84, Ny=40, dx=1e3, velocity_solver=None, inflow=None):
     """Floating shelf in a channel: H = 600 - 400 x / 80 km up to the calving front at x = 80 km (ice free
     beyond), bed -1000 m (all floating), Glen n = 3, A = 3.17e-24, no-slip side walls, no friction,
-    Jacobi-PCG to 1e-10 inside Picard to 1e-6.  The west wall is impenetrable (u = 0)."""
+    Jacobi-PCG to 1e-10 inside Picard to 1e-6.  The west wall is impenetrable (u = 0), or, with `inflow` (m/yr),
+    its faces hold that prescribed velocity."""
     grid = M.RectilinearGrid(size=(Nx, Ny), x=(0.0, Nx * dx), y=(0.0, Ny * dx), halo=(4, 4))
     X, _ = _centers(grid)
     H = np.where(X < 80e3, 600.0 - 400.0 * X / 80e3, 0.0)
@@ -98,7 +107,10 @@ def channel_shelf(Nx=84, Ny=40, dx=1e3, velocity_solver=None):
     cfg = dict(Nsigma=10, stress_balance=M.DepthIntegrated(side_walls=M.NoSlipWalls()),
                rheology=M.GlenFlowLaw(rate_factor=3.17e-24, strain_rate_regularization=1e-13), friction=None,
                grounding=M.SubgridGroundedFraction(), velocity_solver=solver)
-    return Case("channel_shelf", grid, cfg, {"H": H, "bed": np.full_like(H, -1000.0), "A": np.full_like(H, 3.17e-24)})
+    fields = {"H": H, "bed": np.full_like(H, -1000.0), "A": np.full_like(H, 3.17e-24)}
+    if inflow is not None:
+        fields["u_prescribed"] = west_inflow(grid, inflow)
+    return Case("channel_shelf" if inflow is None else "channel_shelf_inflow", grid, cfg, fields)
 
 
 def marine_sheet(Nx=256, Ny=128, seed=1, seed_friction=None, Lx=512e3, Ly=256e3, velocity_solver=None,

@@ -96,8 +96,14 @@ struct Axis {
     bool inactive_cell(int i) const { return !periodic && (i < 1 || i > N); }
 };
 
+struct Field;
+
 struct Grid {
     Axis x, y;
+    // Prescribed velocities (the extension for an inflow; the reference has no velocity boundary condition):
+    // u_D at Face-Center, v_D at Center-Face, NaN where free.  Null on the coarse multigrid levels.
+    const Field* pu = nullptr;
+    const Field* pv = nullptr;
     int Nx() const { return x.N; }
     int Ny() const { return y.N; }
     bool inactive_cell(int i, int j) const { return x.inactive_cell(i) || y.inactive_cell(j); }
@@ -190,10 +196,27 @@ static void for_xy(int Nx, int Ny, F&& f) {   // launch!(arch, grid, :xyz, ...) 
 // ------------------------------------------------------------------------------------------------
 static inline bool ice_free_fc(int i, int j, const Field* mu) { return mu && ((*mu)(i - 1, j) + (*mu)(i, j)) == 0.0; }   // smooth_ice_mask.jl:429
 static inline bool ice_free_cf(int i, int j, const Field* mu) { return mu && ((*mu)(i, j - 1) + (*mu)(i, j)) == 0.0; }   // smooth_ice_mask.jl:430
-static inline bool inactive_fc(const Grid& g, int i, int j, const Field* eta) { return g.peripheral_fc(i, j) || ice_free_fc(i, j, eta); }  // ssa_operator.jl:91
-static inline bool inactive_cf(const Grid& g, int i, int j, const Field* eta) { return g.peripheral_cf(i, j) || ice_free_cf(i, j, eta); }  // ssa_operator.jl:92
-static inline double interior_u(const Grid& g, int i, int j, const Field& u, const Field* eta) { return inactive_fc(g, i, j, eta) ? 0.0 : u(i, j); }  // :94
-static inline double interior_v(const Grid& g, int i, int j, const Field& v, const Field* eta) { return inactive_cf(g, i, j, eta) ? 0.0 : v(i, j); }  // :95
+// A prescribed face: one of the solved rows (i, j in 1..Nx x 1..Ny, wrapped when periodic: the west / south
+// boundary faces and the interior faces) whose prescribed value is finite.  Its row is an identity row
+// (inactive) and its value still enters the strain rates (interior_u / interior_v pass it).
+static inline bool prescribed(const Grid& g, const Field* d, int i, int j) {
+    if (!d || (!g.x.periodic && (i < 1 || i > g.Nx())) || (!g.y.periodic && (j < 1 || j > g.Ny()))) return false;
+    return !std::isnan((*d)(i, j));   // periodic halos hold the wrapped values
+}
+static inline bool prescribed_fc(const Grid& g, int i, int j) { return prescribed(g, g.pu, i, j); }
+static inline bool prescribed_cf(const Grid& g, int i, int j) { return prescribed(g, g.pv, i, j); }
+static inline bool inactive_fc(const Grid& g, int i, int j, const Field* eta) {   // ssa_operator.jl:91 (+ prescribed)
+    return g.peripheral_fc(i, j) || ice_free_fc(i, j, eta) || prescribed_fc(g, i, j);
+}
+static inline bool inactive_cf(const Grid& g, int i, int j, const Field* eta) {   // ssa_operator.jl:92 (+ prescribed)
+    return g.peripheral_cf(i, j) || ice_free_cf(i, j, eta) || prescribed_cf(g, i, j);
+}
+static inline double interior_u(const Grid& g, int i, int j, const Field& u, const Field* eta) {   // :94
+    return (inactive_fc(g, i, j, eta) && !prescribed_fc(g, i, j)) ? 0.0 : u(i, j);
+}
+static inline double interior_v(const Grid& g, int i, int j, const Field& v, const Field* eta) {   // :95
+    return (inactive_cf(g, i, j, eta) && !prescribed_cf(g, i, j)) ? 0.0 : v(i, j);
+}
 
 static inline double strain_rate_xx(const Grid& g, int i, int j, const Field& u, const Field* eta) {   // :97
     return (interior_u(g, i + 1, j, u, eta) - interior_u(g, i, j, u, eta)) / g.dx_c(i);
@@ -759,6 +782,7 @@ struct Problem {
     double mask_min = 1, mask_trans = 1;
 
     VelocityVector x, tau;
+    VelocityVector ud;            // prescribed velocities, NaN where free (grid.pu / grid.pv once set)
     Field H, bed, s, mu, phi, phu, phv, N, C, A2, etaH, etaHff, bu, bv, F2, bbu, bbv, ub, vb;
     SigmaField A3, eta_s, T, us, vs;
 
@@ -769,6 +793,17 @@ struct Problem {
 };
 
 static Coefficients coeffs(Problem& P) { return Coefficients{&P.etaH, &P.etaHff, &P.bu, &P.bv}; }
+
+// x = val on the prescribed faces (the identity rows' values), halos refilled.
+static void impose_prescribed(Problem& P, VelocityVector& x, const VelocityVector& val) {
+    const Grid& g = P.grid;
+    if (!g.pu) return;
+    for_xy(g.Nx(), g.Ny(), [&](int i, int j) {
+        if (prescribed_fc(g, i, j)) x.u(i, j) = val.u(i, j);
+        if (prescribed_cf(g, i, j)) x.v(i, j) = val.v(i, j);
+    });
+    fill_halo(x);
+}
 
 static void update_preconditioner(Problem& P) {   // conjugate_gradient.jl:177; multigrid_preconditioner.jl:128
     if (P.sdesc.preconditioner == NK_PRECONDITIONER_MULTIGRID) coarsen_coefficients(P.mg.levels, 0, P.etaH, P.bu, P.bv);
@@ -872,6 +907,7 @@ static void update_coefficients(Problem& P) { if (P.stress_balance == NK_DIVA) u
 static void picard_solve(Problem& P, nk_solve_stats* st) {
     const Grid& g = P.grid;
     int status = NK_OK;
+    impose_prescribed(P, P.x, P.ud);   // the identity rows start solved
     const nk_iteration_control& ctl = P.sdesc.picard;
     int it = 0;
     if (st) { std::memset(st, 0, sizeof(*st)); }
@@ -973,6 +1009,7 @@ static void compute_geometry(Problem& P) {
             }
             double t = -g.Az_fcc(i, j) * ri * gg * ((P.H(i - 1, j) + P.H(i, j)) / 2) * ((P.s(i, j) - P.s(i - 1, j)) / g.dx_f(i));
             P.tau.u(i, j) = wall ? 0.0 : (front ? tf : (straddles ? tg : t));
+            if (prescribed_fc(g, i, j)) P.tau.u(i, j) = P.ud.u(i, j);   // the identity row's right-hand side
         }
     for (int j = 1; j <= P.tau.v.ny(); ++j)
         for (int i = 1; i <= P.tau.v.nx(); ++i) {   // _compute_y_driving_stress!, :118-125
@@ -989,6 +1026,7 @@ static void compute_geometry(Problem& P) {
             }
             double t = -g.Az_cfc(i, j) * ri * gg * ((P.H(i, j - 1) + P.H(i, j)) / 2) * ((P.s(i, j) - P.s(i, j - 1)) / g.dy_f(j));
             P.tau.v(i, j) = wall ? 0.0 : (front ? tf : (straddles ? tg : t));
+            if (prescribed_cf(g, i, j)) P.tau.v(i, j) = P.ud.v(i, j);
         }
 }
 
@@ -1060,6 +1098,8 @@ static FieldRef field_ref(Problem& P, int id) {
         case NK_FIELD_U_SIGMA: r.s = &P.us; break;
         case NK_FIELD_V_SIGMA: r.s = &P.vs; break;
         case NK_FIELD_TEMPERATURE: r.s = &P.T; break;
+        case NK_FIELD_U_PRESCRIBED: r.f = &P.ud.u; break;
+        case NK_FIELD_V_PRESCRIBED: r.f = &P.ud.v; break;
         default: break;
     }
     return r;
@@ -1123,6 +1163,9 @@ nk_status nko_problem_create(const nk_grid_desc* gd, const nk_physics_desc* pd, 
 
     const Grid* g = &P->grid;
     P->x.init(g); P->tau.init(g);
+    P->ud.init(g);
+    std::fill(P->ud.u.d.begin(), P->ud.u.d.end(), std::nan(""));
+    std::fill(P->ud.v.d.begin(), P->ud.v.d.end(), std::nan(""));
     for (Field* f : {&P->H, &P->bed, &P->s, &P->mu, &P->phi, &P->N, &P->C, &P->A2, &P->etaH, &P->F2}) f->init(g, CENTER, CENTER);
     for (Field* f : {&P->phu, &P->bu, &P->bbu, &P->ub}) f->init(g, FACE, CENTER);
     for (Field* f : {&P->phv, &P->bv, &P->bbv, &P->vb}) f->init(g, CENTER, FACE);
@@ -1152,6 +1195,12 @@ nk_status nko_problem_set_field(nko_problem* h, int32_t id, const double* src, i
     else {
         int64_t layer = (int64_t)r.s->k[0].nx() * r.s->k[0].ny();
         for (size_t k = 0; k < r.s->k.size(); ++k) copy_in(r.s->k[k], src + k * layer);
+    }
+    if (id == NK_FIELD_U_PRESCRIBED || id == NK_FIELD_V_PRESCRIBED) {   // the right-hand side and velocity take u_D
+        P.grid.pu = &P.ud.u;
+        P.grid.pv = &P.ud.v;
+        impose_prescribed(P, P.tau, P.ud);
+        impose_prescribed(P, P.x, P.ud);
     }
     return NK_OK;
 }
@@ -1224,6 +1273,7 @@ nk_status nko_linear_solve(nko_problem* h, const double* bu, const double* bv, n
     load_vector(b, bu, bv);
     if (st) std::memset(st, 0, sizeof(*st));
     int status = NK_OK;
+    impose_prescribed(P, P.x, b);   // an identity row's solution is its right-hand side
     conjugate_gradient(P, P.x, b, st, &status);
     fill_halo(P.x);
     if (st) st->status = status;
