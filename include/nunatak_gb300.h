@@ -92,9 +92,14 @@ typedef int32_t nk_status;
 /* Iteration control, src/Solvers/iteration_controls.jl:99-133. */
 #define NK_CONVERGENCE      0
 #define NK_FIXED_ITERATIONS 1
+/* An extension for the Picard control only (the reference tests the velocity change, picard.jl:79-85):
+ * stop when the depth-integrated viscosity of consecutive coefficient updates changes by
+ * ||etaH_k - etaH_(k-1)|| <= max(reltol ||etaH_k||, abstol) over the Nx x Ny centres, or at maxiter.  The first
+ * iteration has no previous etaH (change = infinity).  picard_change / picard_norm report ||d etaH|| / ||etaH||. */
+#define NK_VISCOSITY_CONVERGENCE 2
 
 typedef struct nk_iteration_control {
-    int32_t kind;        /* NK_CONVERGENCE or NK_FIXED_ITERATIONS */
+    int32_t kind;        /* NK_CONVERGENCE, NK_FIXED_ITERATIONS (or NK_VISCOSITY_CONVERGENCE for Picard) */
     int32_t iterations;  /* FixedIterations(iterations) */
     int32_t maxiter;     /* Convergence: maxiter */
     int32_t reserved;

@@ -87,6 +87,9 @@ void launch_copy_range(const DevGrid<double>& g, double2* dst, const double2* sr
 void launch_picard_begin(SolverScalars* sc, unsigned long long cond, cudaStream_t s);
 void launch_picard_end(const DevGrid<double>& g, double2* xprev, const double2* x, SolverScalars* sc, double2* partials,
                        unsigned long long cond, cudaStream_t s);
+// the same under the viscosity-change rule (NK_VISCOSITY_CONVERGENCE): Δ = ‖η̄H - η̄H⁻‖, X = ‖η̄H‖, η̄H⁻ = η̄H
+void launch_picard_end_viscosity(const DevGrid<double>& g, const double4* coef, double* eta_prev, SolverScalars* sc, double2* partials,
+                                 unsigned long long cond, cudaStream_t s);
 
 // ---- coefficients ---------------------------------------------------------------------------------------
 // SSA membrane viscosity (glen_flow_law.jl:208-212) and column integrals (column_integrals.jl:90-101)

@@ -763,6 +763,15 @@ static cudaGraph_t add_while(cudaGraph_t g, const std::vector<cudaGraphNode_t>& 
 // update_stress_balance_coefficients! / update_diva_coefficients!
 static void update_coefficients(nk_problem* P);
 
+// Picard's change measure and stopping test: the reference's velocity change, or the viscosity change of
+// NK_VISCOSITY_CONVERGENCE, whose previous η̄H lives in tmp_a (free during a Picard solve).
+static void picard_end(nk_problem* P, cudaGraphConditionalHandle h) {
+    if (P->sd.picard.kind == NK_VISCOSITY_CONVERGENCE)
+        launch_picard_end_viscosity(P->fine.g, P->fine.coef, (double*)P->tmp_a, P->sc, P->partials, h, P->stream);
+    else
+        launch_picard_end(P->fine.g, P->xprev, P->x, P->sc, P->partials, h, P->stream);
+}
+
 static void build_picard_graph(nk_problem* P) {
     cudaGraph_t g;
     NK_CUDA(cudaGraphCreate(&g, 0));
@@ -781,7 +790,7 @@ static void build_picard_graph(nk_problem* P) {
     });
     cudaGraph_t cg_body = add_while(body, leaves(body), hc);
     capture_into(P, cg_body, {}, [&] { cg_step(P, v); });
-    capture_into(P, body, leaves(body), [&] { launch_picard_end(P->fine.g, P->xprev, P->x, P->sc, P->partials, hp, P->stream); });
+    capture_into(P, body, leaves(body), [&] { picard_end(P, hp); });
     P->picard_kernels[0] = kernel_nodes(g);
     P->picard_kernels[1] = kernel_nodes(body);
     P->picard_kernels[2] = kernel_nodes(cg_body);
@@ -850,7 +859,7 @@ static void host_picard(nk_problem* P) {
         launch_copy_range(P->fine.g, P->xprev, P->x, P->stream);
         update_coefficients(P);
         host_cg(P, P->tau);
-        launch_picard_end(P->fine.g, P->xprev, P->x, P->sc, P->partials, 0, P->stream);
+        picard_end(P, 0);
         NK_CHECK_LAUNCH();
         read_scalars(P);
     }
@@ -1105,6 +1114,8 @@ static nk_status problem_create(nk_context* ctx, const nk_grid_desc* grid, const
         if (physics->glen_exponent <= 0) bad("glen exponent must be positive");
         if (physics->use_ice_mask && !(physics->mask_transition_thickness > 0)) bad("transition_thickness must be positive");
         if (solver->preconditioner < NK_PRECONDITIONER_NONE || solver->preconditioner > NK_PRECONDITIONER_MULTIGRID) bad("unknown preconditioner");
+        if (solver->linear.kind != NK_CONVERGENCE && solver->linear.kind != NK_FIXED_ITERATIONS) bad("unknown linear iteration control");
+        if (solver->picard.kind < NK_CONVERGENCE || solver->picard.kind > NK_VISCOSITY_CONVERGENCE) bad("unknown Picard iteration control");
         if (solver->precision == NK_PRECISION_MIXED && solver->preconditioner != NK_PRECONDITIONER_MULTIGRID)
             bad("mixed precision needs the multigrid preconditioner");
         P->ctx = ctx;
@@ -1406,6 +1417,7 @@ nk_status nk_picard_adjoint(nk_problem* P, const double* ubar, const double* vba
     return guarded(P->ctx, [&] {
         nk_iteration_control ctl = control ? *control : P->sd.picard;
         if (ctl.kind == NK_FIXED_ITERATIONS ? ctl.iterations < 0 : ctl.maxiter < 0) bad("negative iteration count");
+        if (ctl.kind != NK_CONVERGENCE && ctl.kind != NK_FIXED_ITERATIONS) bad("the adjoint takes Convergence or FixedIterations");
         nk_solve_stats local{};
         nk_solve_stats* st = stats ? stats : &local;
         NK_CUDA(cudaEventRecord(P->ev0, P->stream));

@@ -520,6 +520,45 @@ void launch_picard_end(const DevGrid<double>& g, double2* xprev, const double2* 
     k_picard_end<<<d.grid, d.block, 0, s>>>(g, xprev, x, sc, partials, cond); count_launch();
 }
 
+// End of one Picard iteration under the viscosity-change rule (NK_VISCOSITY_CONVERGENCE, an extension):
+// Δ = ‖η̄H - η̄H⁻‖ between this iteration's coefficients and the previous iteration's (Δ = ∞ at the first),
+// X = ‖η̄H‖, then η̄H⁻ = η̄H and the same loop test as k_picard_end.
+__global__ void k_picard_end_viscosity(DevGrid<double> g, const double4* __restrict__ coef, double* eta_prev, SolverScalars* sc,
+                                       double2* partials, unsigned long long cond) {
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    double dd = 0.0, xx = 0.0;
+    if (i < g.Nx && j < g.Ny) {
+        int k = g.idx(i, j);
+        double e = coef[k].x, d = e - eta_prev[k];
+        eta_prev[k] = e;
+        dd = d * d;
+        xx = e * e;
+    }
+    double tdd, txx;
+    if (grid_sum2(dd, xx, partials, &sc->ticket, tdd, txx) && threadIdx.x == 0 && threadIdx.y == 0) {
+        double D = sc->p_it == 0 ? INFINITY : sqrt(tdd), X = sqrt(txx);
+        sc->picard_dd = tdd;
+        sc->picard_xx = txx;
+        sc->p_D = D;
+        sc->p_X = X;
+        int it = sc->p_it + 1;
+        sc->p_it = it;
+        sc->it_total += sc->it;
+        int more = D > fmax(sc->p_reltol * X, sc->p_abstol) && it < sc->p_maxiter;
+        if (isnan(D) || !isfinite(X) || sc->status == NK_NONFINITE) {
+            sc->status = NK_NONFINITE;
+            more = 0;
+        }
+        sc->p_done = !more;
+        if (cond) cudaGraphSetConditional(cond, more ? 1u : 0u);
+    }
+}
+void launch_picard_end_viscosity(const DevGrid<double>& g, const double4* coef, double* eta_prev, SolverScalars* sc, double2* partials,
+                                 unsigned long long cond, cudaStream_t s) {
+    LaunchDims d = dims2d(g.Nx, g.Ny);
+    k_picard_end_viscosity<<<d.grid, d.block, 0, s>>>(g, coef, eta_prev, sc, partials, cond); count_launch();
+}
+
 // ---- vector helpers under the done predicate -------------------------------------------------------------------
 __global__ void k_copy_vec(DevGrid<double> g, double2* dst, const double2* __restrict__ src, const int* done) {
     if (done && *(volatile const int*)done) return;

@@ -7,13 +7,14 @@ from .model import (YEAR, Convergence, DepthIntegrated, DIVAShear, FixedIteratio
                     IceSheetConstants, LineJacobi, NoSlipWalls, PointJacobi, RectilinearGrid,
                     RegularizedCoulombFriction, SmoothIceMask, StressBalanceDiagonalPreconditioner,
                     StressBalanceMultigridPreconditioner, StressBalanceSolver, SubgridGroundedFraction,
-                    WeertmanFriction, make_descriptors, field_shape)
+                    ViscosityConvergence, WeertmanFriction, make_descriptors, field_shape)
 from .problem import NunatakError, Problem
 
 __all__ = [
     "abi", "YEAR", "Convergence", "DepthIntegrated", "DIVAShear", "FixedIterations", "FreeSlipWalls", "GlenFlowLaw",
     "IceSheetConstants", "LineJacobi", "NoSlipWalls", "PointJacobi", "RectilinearGrid", "RegularizedCoulombFriction",
     "SmoothIceMask", "StressBalanceDiagonalPreconditioner", "StressBalanceMultigridPreconditioner",
-    "StressBalanceSolver", "SubgridGroundedFraction", "WeertmanFriction", "make_descriptors", "field_shape",
+    "StressBalanceSolver", "SubgridGroundedFraction", "ViscosityConvergence", "WeertmanFriction", "make_descriptors",
+    "field_shape",
     "NunatakError", "Problem",
 ]

@@ -24,7 +24,7 @@ NK_RATE_FACTOR_2D, NK_RATE_FACTOR_SIGMA = 0, 1
 NK_PRECONDITIONER_NONE, NK_PRECONDITIONER_DIAGONAL, NK_PRECONDITIONER_MULTIGRID = 0, 1, 2
 NK_SMOOTHER_POINT_JACOBI, NK_SMOOTHER_LINE_JACOBI = 0, 1
 NK_PRECISION_FP64, NK_PRECISION_MIXED = 0, 1
-NK_CONVERGENCE, NK_FIXED_ITERATIONS = 0, 1
+NK_CONVERGENCE, NK_FIXED_ITERATIONS, NK_VISCOSITY_CONVERGENCE = 0, 1, 2
 
 FIELD_IDS = {
     "u": 0, "v": 1, "H": 2, "bed": 3, "s": 4, "ice_mask": 5, "phi": 6, "phi_u": 7, "phi_v": 8,

@@ -95,6 +95,18 @@ class FixedIterations:
         return abi.IterationControl(abi.NK_FIXED_ITERATIONS, self.iterations, self.iterations, 0, 0.0, 0.0)
 
 
+@dataclass
+class ViscosityConvergence:
+    """Picard stopping rule on the relative change of the depth-integrated viscosity between consecutive
+    coefficient updates (an extension; the reference's Convergence tests the velocity change)."""
+    reltol: float = 1e-6
+    abstol: float = 0.0
+    maxiter: int = 100
+
+    def desc(self):
+        return abi.IterationControl(abi.NK_VISCOSITY_CONVERGENCE, 0, self.maxiter, 0, self.reltol, self.abstol)
+
+
 # ---- physics ----------------------------------------------------------------------------------------
 @dataclass
 class FreeSlipWalls:

@@ -788,6 +788,7 @@ struct Problem {
 
     // CG workspace (VelocityConjugateGradientSolver, conjugate_gradient.jl:193-243) and Picard x⁻
     VelocityVector r, z, p, q, w, xprev;
+    Field eta_prev;               // η̄H of the previous Picard iteration (NK_VISCOSITY_CONVERGENCE)
     Multigrid mg;
     bool mg_ready = false;
 };
@@ -920,14 +921,27 @@ static void picard_solve(Problem& P, nk_solve_stats* st) {
             copyto(g, P.xprev, P.x);
             update_coefficients(P);
             conjugate_gradient(P, P.x, P.tau, st, &status);
-            axpy(g, -1.0, P.x, P.xprev);
-            D = std::sqrt(vector_dot(g, P.xprev, P.xprev));
-            X = std::sqrt(vector_dot(g, P.x, P.x));
+            if (ctl.kind == NK_VISCOSITY_CONVERGENCE) {   // the extension: change of η̄H between coefficient updates
+                double dd = 0, ee = 0;
+                for (int j = 1; j <= g.Ny(); ++j)
+                    for (int i = 1; i <= g.Nx(); ++i) {
+                        double e = P.etaH(i, j), d = e - P.eta_prev(i, j);
+                        dd += d * d;
+                        ee += e * e;
+                        P.eta_prev(i, j) = e;
+                    }
+                D = it == 0 ? std::numeric_limits<double>::infinity() : std::sqrt(dd);
+                X = std::sqrt(ee);
+            } else {
+                axpy(g, -1.0, P.x, P.xprev);
+                D = std::sqrt(vector_dot(g, P.xprev, P.xprev));
+                X = std::sqrt(vector_dot(g, P.x, P.x));
+            }
             ++it;
         }
         if (D > std::max(ctl.reltol * X, ctl.abstol) && status == NK_OK) status = NK_NOT_CONVERGED;
         if (st) { st->picard_change = D; st->picard_norm = X; }
-        if (!std::isfinite(D) && it > 0) status = NK_NONFINITE;
+        if ((ctl.kind == NK_VISCOSITY_CONVERGENCE ? (std::isnan(D) || !std::isfinite(X)) : !std::isfinite(D)) && it > 0) status = NK_NONFINITE;
     }
     fill_halo(P.x);
     if (st) { st->picard_iterations = it; st->status = status; }
@@ -1173,6 +1187,7 @@ nk_status nko_problem_create(const nk_grid_desc* gd, const nk_physics_desc* pd, 
     P->A3.init(g, CENTER, CENTER, gd->Nsigma); P->eta_s.init(g, CENTER, CENTER, gd->Nsigma); P->T.init(g, CENTER, CENTER, gd->Nsigma);
     P->us.init(g, FACE, CENTER, gd->Nsigma); P->vs.init(g, CENTER, FACE, gd->Nsigma);
     P->r.init(g); P->z.init(g); P->p.init(g); P->q.init(g); P->w.init(g); P->xprev.init(g);
+    P->eta_prev.init(g, CENTER, CENTER);
     if (sd->preconditioner == NK_PRECONDITIONER_MULTIGRID) {
         coarse_levels(P->grid, sd->minimum_coarse_size, P->mg.levels);
         P->mg.residual.init(g); P->mg.scratch.init(g, CENTER, CENTER);
