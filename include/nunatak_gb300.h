@@ -272,7 +272,7 @@ nk_status nk_adjoint_solve(nk_problem* problem, const double* bu, const double* 
 nk_status nk_picard_solve(nk_problem* problem, nk_solve_stats* stats);
 
 /* Fixed-point adjoint of a converged picard_solve! (the Enzyme reverse rule of ext/NunatakEnzymeExt.jl:167-240,
- * Christianson 1994) for the SSA with Weertman or regularised-Coulomb friction.  x* = (U, V) is the problem's
+ * Christianson 1994) for the SSA and DIVA with Weertman or regularised-Coulomb friction.  x* = (U, V) is the problem's
  * converged velocity and x̄ = (ubar, vbar) = ∂J/∂x* in the interior layout of U, V.  The coefficients are
  * refreshed to c(x*), then λ ← A⁻¹ (x̄ - (∂[A(c(x)) x*]/∂x)ᵀ λ) is iterated from λ = 0, each step one
  * preconditioned CG solve of the problem's linear control warm-started from λ, until
@@ -280,7 +280,10 @@ nk_status nk_picard_solve(nk_problem* problem, nk_solve_stats* stats);
  * (lambda_u, lambda_v, same layout as U, V), ∂J/∂log C per cell (grad_log_C, Nx x Ny) and ∂J/∂log A in the
  * layout of RATE_FACTOR (grad_log_A: Nx x Ny, or Nσ planes of them for a σ-grid rate factor); any output may be
  * NULL.  stats: picard_iterations = adjoint iterations, picard_change = ‖λ⁺ - λ‖, picard_norm = ‖λ‖,
- * status NK_NOT_CONVERGED when maxiter ended it.  U, V are left at x*. */
+ * status NK_NOT_CONVERGED when maxiter ended it.  U, V are left at x*.  DIVA: the step also reads its own
+ * previous beta_b, F2 and eta_sigma (diva.jl:77-80), whose adjoint is swept along with lambda; the stopping test
+ * watches lambda only, as the reference's does, and the lagged-state adjoint settles more slowly, so ask for a
+ * tighter reltol than for the SSA.  Problems with prescribed velocities are refused (NK_BAD_ARGUMENT). */
 nk_status nk_picard_adjoint(nk_problem* problem, const double* ubar, const double* vbar, const nk_iteration_control* control,
                             double* lambda_u, double* lambda_v, double* grad_log_C, double* grad_log_A, nk_solve_stats* stats);
 

@@ -535,16 +535,17 @@ __global__ void k_adjoint_viscosity(AdjointView v) {
     double S = effective_strain_rate2(g, v.xs, ph.ud, i, j, ph.wall_factor) + ph.eps0 * ph.eps0;
     v.gbar[k] = eb * v.o.coef[k].x * ((1 - ph.n) / (2 * ph.n)) / S;
     if (v.grad_log_A) {
-        // η = ½ A^(-1/n) S^((1-n)/2n): ∂η/∂log A = -η / n; with a 2-D A every layer shares it, so the cell's
-        // gradient is -η̄H̄ η̄H / n, and with a σ-grid A layer k carries -η̄H̄ μ H Δζₖ ηₖ / n
+        // η = ½ A^(-1/n) S^((1-n)/2n): ∂η/∂log A = -η / n.  The adjoint of η̄H is -eb (eb is λ-signed and
+        // p̄ = -(∂c/∂p)ᵀ eb), so with a 2-D A, which every layer shares, the cell's gradient is eb η̄H / n, and with
+        // a σ-grid A layer k carries eb μ H Δζₖ ηₖ / n
         if (ph.rate_sigma) {
             double muH = (ph.use_mask ? ph.mu[k] : 1.0) * ph.H[k];
             for (int l = 0; l < ph.sig.N; ++l) {
                 long long o = (long long)l * ph.plane + k;
-                v.grad_log_A[o] = -eb * (muH * ph.sig.dz[l] * v.eta_sigma[o]) / ph.n;
+                v.grad_log_A[o] = eb * (muH * ph.sig.dz[l] * v.eta_sigma[o]) / ph.n;
             }
         } else {
-            v.grad_log_A[k] = -eb * v.o.coef[k].x / ph.n;
+            v.grad_log_A[k] = eb * v.o.coef[k].x / ph.n;
         }
     }
 }
@@ -594,6 +595,25 @@ __device__ double strain_sensitivity(const DevGrid<double>& g, const double2* __
     return d;
 }
 
+// Σ over the centres whose effective strain rate reads velocity point k (u face (i, j) for comp 0, v face for
+// comp 1) of gbar(centre) ∂S/∂x_k: centres ci in i-1..i (u) or i-1..i+1 (v), cj in j-1..j+1 (u) or j-1..j (v).
+__device__ double viscosity_gather(const AdjointView& v, int i, int j, int k, int comp) {
+    const DevGrid<double>& g = v.o.g;
+    double acc = 0.0;
+    int seen[6], ns = 0;
+    int ilo = i - 1, ihi = comp == 0 ? i : i + 1, jlo = j - 1, jhi = comp == 0 ? j + 1 : j;
+    for (int a = ilo; a <= ihi; ++a)
+        for (int b2 = jlo; b2 <= jhi; ++b2) {
+            int ci, cj;
+            if (!map_index(a, g.Nx, g.px, g.Nx, ci) || !map_index(b2, g.Ny, g.py, g.Ny, cj)) continue;
+            int c = g.idx(ci, cj);
+            if (!first_time(seen, ns, c)) continue;
+            double gb = v.gbar[c];
+            if (gb != 0.0) acc += gb * strain_sensitivity(g, v.xs, v.ph.wall_factor, ci, cj, k, comp);
+        }
+    return acc;
+}
+
 // r = x̄ + ȳ with ȳ = -(∂[A(c(x)) x*]/∂x)ᵀ λ, gathered per velocity point from the centres whose strain rates
 // read it (viscosity) and the faces whose speed reads it (drag).
 __global__ void k_adjoint_velocity(AdjointView v) {
@@ -607,19 +627,7 @@ __global__ void k_adjoint_velocity(AdjointView v) {
     double u, vf, U, phi, b, dbdU, dbdC;
     for (int comp = 0; comp < 2; ++comp) {
         if (comp == 0 ? !has_u : !has_v) continue;
-        double acc = 0.0;
-        // viscosity: centres ci in i-1..i (u) or i-1..i+1 (v), cj in j-1..j+1 (u) or j-1..j (v)
-        int seen[6], ns = 0;
-        int ilo = i - 1, ihi = comp == 0 ? i : i + 1, jlo = j - 1, jhi = comp == 0 ? j + 1 : j;
-        for (int a = ilo; a <= ihi; ++a)
-            for (int b2 = jlo; b2 <= jhi; ++b2) {
-                int ci, cj;
-                if (!map_index(a, g.Nx, g.px, g.Nx, ci) || !map_index(b2, g.Ny, g.py, g.Ny, cj)) continue;
-                int c = g.idx(ci, cj);
-                if (!first_time(seen, ns, c)) continue;
-                double gb = v.gbar[c];
-                if (gb != 0.0) acc += gb * strain_sensitivity(g, v.xs, ph.wall_factor, ci, cj, k, comp);
-            }
+        double acc = viscosity_gather(v, i, j, k, comp);
         // drag of the point itself
         if (comp == 0 && u_drag(ph, v.xs, i, j, u, vf, U, phi, b, dbdU, dbdC)) acc += v.bbar[k].x * phi * dbdU * u / U;
         if (comp == 1 && v_drag(ph, v.xs, i, j, u, vf, U, phi, b, dbdU, dbdC)) acc += v.bbar[k].y * phi * dbdU * u / U;
@@ -688,6 +696,239 @@ __global__ void k_adjoint_gradient(AdjointView v) {
 void launch_adjoint_gradient(const AdjointView& v, cudaStream_t s) {
     LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
     k_adjoint_gradient<<<d.grid, d.block, 0, s>>>(v); count_launch();
+}
+
+// ---- DIVA: the reverse of one update_diva_coefficients! step at the fixed point ---------------------------------
+// The forward step (diva.jl:221-235) reads x, the lagged βᵇ⁻, F₂⁻ and ησ⁻ and writes:
+//   uᵇ = x / (1 + βᵇ⁻ ℑF₂⁻)                               (compute_basal_velocities!)
+//   βᵇ = φ drag(|uᵇ|, C, N)                                (compute_basal_drag! on uᵇ)
+//   ησₖ = glen(Aₖ, ε̇ₑ²(x) + (τxᵇ² + τyᵇ²) aₖ² + ε̇₀²),      τxᵇ = ℑxᶜ(βᵇᵘ uᵇ), aₖ = (1 - ζₖ) / 2ησ⁻ₖ
+//   η̄H = μ H Σ ησₖ Δζₖ,  F₂ = H Σ w₂ₖ / ησₖ,  β = βᵇ / (1 + βᵇ ℑF₂)
+// At the fixed point the lagged state equals the new one, so one set of arrays serves both.  True adjoints
+// throughout: the operator's coefficient adjoints are minus the λ-signed cbar / bbar.
+
+// u-face mean of F₂ (x_shear_factor) and v-face mean (y_shear_factor)
+__device__ __forceinline__ double u_face_F2(const DevGrid<double>& g, const double* F2, int i, int j) {
+    return (F2[g.c_idx(i - 1, j)] + F2[g.c_idx(i, j)]) / 2;
+}
+__device__ __forceinline__ double v_face_F2(const DevGrid<double>& g, const double* F2, int i, int j) {
+    return (F2[g.c_idx(i, j - 1)] + F2[g.c_idx(i, j)]) / 2;
+}
+
+// Σ over the faces whose ℑF₂ reads centre (i, j) = k of val(face index, component) × (times read) / 2
+template <typename F>
+__device__ __forceinline__ double face_mean_gather(const DevGrid<double>& g, int i, int j, int k, F&& val) {
+    double acc = 0.0;
+    int seen[2], n = 0;
+    for (int a = i; a <= i + 1; ++a) {
+        int fi;
+        if (!map_index(a, g.Nx, g.px, g.Nx + 1, fi)) continue;
+        int kf = g.idx(fi, j);
+        if (!first_time(seen, n, kf)) continue;
+        int m = (g.c_idx(fi - 1, j) == k) + (g.c_idx(fi, j) == k);
+        if (m) acc += val(fi, j, kf, 0) * (m / 2.0);
+    }
+    n = 0;
+    for (int b = j; b <= j + 1; ++b) {
+        int fj;
+        if (!map_index(b, g.Ny, g.py, g.Ny + 1, fj)) continue;
+        int kf = g.idx(i, fj);
+        if (!first_time(seen, n, kf)) continue;
+        int m = (g.c_idx(i, fj - 1) == k) + (g.c_idx(i, fj) == k);
+        if (m) acc += val(i, fj, kf, 1) * (m / 2.0);
+    }
+    return acc;
+}
+
+// Centre pass: F̄₂ = σ(F₂) + the effective drags' ℑF₂; ησ̄ₖ = σ(ησₖ) + η̄̄ Δζₖ - F̄ w₂ₖ / ησₖ², through glen to
+// ε̇̄ₑₖ; writes gbar = Σₖ ε̇̄ₑₖ (the membrane strain rate), txbar (the basal shear stresses), σ(ησ⁻) in place and,
+// when set, ∂J/∂log A.
+__global__ void k_adjoint_diva_centre(AdjointView v) {
+    const PhysView& ph = v.ph;
+    const DevGrid<double>& g = v.o.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int k = g.idx(i, j);
+    int fx[2], wx[2], fy[2], wy[2];
+    int nx = corners_of_centre(i, g.Nx, g.px, fx, wx), ny = corners_of_centre(j, g.Ny, g.py, fy, wy);
+    double eb = v.cbar[k].x;
+    for (int a = 0; a < nx; ++a)
+        for (int b = 0; b < ny; ++b) eb += (wx[a] * wy[b]) * v.cbar[g.idx(fx[a], fy[b])].y / 4;
+    double H = ph.H[k];
+    double etabar_b = -eb * (ph.use_mask ? ph.mu[k] : 1.0) * H;     // ∂J/∂η̄
+    double F2b = v.sig_F2[k] + face_mean_gather(g, i, j, k, [&](int fi, int fj, int kf, int comp) {
+        double b = comp == 0 ? v.bbs[kf].x : v.bbs[kf].y;
+        double mf = comp == 0 ? u_face_F2(g, v.F2s, fi, fj) : v_face_F2(g, v.F2s, fi, fj);
+        double den = 1 + b * mf;
+        return (comp == 0 ? v.bbar[kf].x : v.bbar[kf].y) * b * b / (den * den);   // -β̄ ∂β/∂ℑF₂ with β̄ = -bbar
+    });
+    double Fb = F2b * H;
+    int u0 = g.u_idx(i, j), u1 = g.u_idx(i + 1, j), v0 = g.v_idx(i, j), v1 = g.v_idx(i, j + 1);
+    double tx = (v.bbs[u0].x * v.ubs[u0].x + v.bbs[u1].x * v.ubs[u1].x) / 2;
+    double ty = (v.bbs[v0].y * v.ubs[v0].y + v.bbs[v1].y * v.ubs[v1].y) / 2;
+    double t2 = tx * tx + ty * ty;
+    double e2 = effective_strain_rate2(g, v.xs, nullptr, i, j, ph.wall_factor);
+    double e2b = 0.0, txb = 0.0, tyb = 0.0, gA = 0.0;
+    for (int l = 0; l < ph.sig.N; ++l) {
+        long long o = (long long)l * ph.plane + k;
+        double eta = v.eta_sigma[o];
+        double em = eta == 0.0 ? INFINITY : eta;
+        double a = (1 - ph.sig.zc[l]) / (2 * em), a2 = a * a;
+        double ee = e2 + t2 * a2 + ph.eps0 * ph.eps0;
+        double etab = v.sig_eta[o] + etabar_b * ph.sig.dz[l] - Fb * ph.sig.w2[l] / (eta * eta);
+        double eeb = etab * eta * ((1 - ph.n) / (2 * ph.n)) / ee;
+        e2b += eeb;
+        txb += eeb * 2 * tx * a2;
+        tyb += eeb * 2 * ty * a2;
+        v.sig_eta[o] = eta == 0.0 ? 0.0 : eeb * (-2 * t2 * a2 / em);
+        if (v.grad_log_A) {
+            double d = etab * (-eta / ph.n);
+            if (ph.rate_sigma) v.grad_log_A[o] = d; else gA += d;
+        }
+    }
+    if (v.grad_log_A && !ph.rate_sigma) v.grad_log_A[k] = gA;
+    v.gbar[k] = e2b;
+    v.txbar[k] = make_double2(txb, tyb);
+}
+
+// Face pass: β̄ᵇ = σ(βᵇ) + β̄ / (1 + βᵇ ℑF₂)² + the basal shear stresses that read βᵇ uᵇ here; Ū = β̄ᵇ φ ∂drag/∂U.
+__global__ void k_adjoint_diva_face(AdjointView v) {
+    const PhysView& ph = v.ph;
+    const DevGrid<double>& g = v.o.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i > g.Nx || j > g.Ny) return;
+    int k = g.idx(i, j);
+    bool has_u = j < g.Ny && (i < g.Nx || !g.px), has_v = i < g.Nx && (j < g.Ny || !g.py);
+    double2 Ub = make_double2(0.0, 0.0), up = make_double2(0.0, 0.0), bt = make_double2(0.0, 0.0);
+    double w, avg, U, phi, bd, dbdU, dbdC;
+    if (has_u) {
+        double b = v.bbs[k].x, den = 1 + b * u_face_F2(g, v.F2s, i, j);
+        double bbar = v.sig_bb[k].x - v.bbar[k].x / (den * den), upf = 0.0;
+        int seen[2], n = 0;
+        for (int a = i - 1; a <= i; ++a) {   // τxᵇ of centre (ci, j) reads u_idx(ci, j) and u_idx(ci + 1, j)
+            int ci;
+            if (!map_index(a, g.Nx, g.px, g.Nx, ci)) continue;
+            int kc = g.idx(ci, j);
+            if (!first_time(seen, n, kc)) continue;
+            int m = (g.u_idx(ci, j) == k) + (g.u_idx(ci + 1, j) == k);
+            double tb = v.txbar[kc].x * (m / 2.0);
+            bbar += tb * v.ubs[k].x;
+            upf += tb * b;
+        }
+        bt.x = bbar;
+        up.x = upf;
+        if (u_drag(ph, v.ubs, i, j, w, avg, U, phi, bd, dbdU, dbdC)) Ub.x = bbar * phi * dbdU;
+    }
+    if (has_v) {
+        double b = v.bbs[k].y, den = 1 + b * v_face_F2(g, v.F2s, i, j);
+        double bbar = v.sig_bb[k].y - v.bbar[k].y / (den * den), upf = 0.0;
+        int seen[2], n = 0;
+        for (int c = j - 1; c <= j; ++c) {   // τyᵇ of centre (i, cj) reads v_idx(i, cj) and v_idx(i, cj + 1)
+            int cj;
+            if (!map_index(c, g.Ny, g.py, g.Ny, cj)) continue;
+            int kc = g.idx(i, cj);
+            if (!first_time(seen, n, kc)) continue;
+            int m = (g.v_idx(i, cj) == k) + (g.v_idx(i, cj + 1) == k);
+            double tb = v.txbar[kc].y * (m / 2.0);
+            bbar += tb * v.ubs[k].y;
+            upf += tb * b;
+        }
+        bt.y = bbar;
+        up.y = upf;
+        if (v_drag(ph, v.ubs, i, j, w, avg, U, phi, bd, dbdU, dbdC)) Ub.y = bbar * phi * dbdU;
+    }
+    v.Ubar[k] = Ub;
+    v.ubp[k] = up;
+    v.bbt[k] = bt;
+}
+
+// Velocity pass: ūᵇ = ubp + the drag speeds that read uᵇ here; then uᵇ = x / S⁻ with S⁻ = 1 + βᵇ⁻ ℑF₂⁻ gives
+// x̄ += ūᵇ / S⁻, σ(βᵇ⁻) = S̄⁻ ℑF₂⁻ and the ℑF₂⁻ adjoint S̄⁻ βᵇ⁻ (mbar); r = x̄ + the membrane strain rates + ūᵇ / S⁻.
+__global__ void k_adjoint_diva_velocity(AdjointView v) {
+    const PhysView& ph = v.ph;
+    const DevGrid<double>& g = v.o.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i > g.Nx || j > g.Ny) return;
+    int k = g.idx(i, j);
+    bool has_u = j < g.Ny && (i < g.Nx || !g.px), has_v = i < g.Nx && (j < g.Ny || !g.py);
+    double2 xb = v.xbar[k], r = xb, sb = make_double2(0.0, 0.0), mb = make_double2(0.0, 0.0);
+    double u, vf, U, phi, b, dbdU, dbdC;
+    for (int comp = 0; comp < 2; ++comp) {
+        if (comp == 0 ? !has_u : !has_v) continue;
+        double ubb = comp == 0 ? v.ubp[k].x : v.ubp[k].y;
+        if (comp == 0 && u_drag(ph, v.ubs, i, j, u, vf, U, phi, b, dbdU, dbdC)) ubb += v.Ubar[k].x * u / U;
+        if (comp == 1 && v_drag(ph, v.ubs, i, j, u, vf, U, phi, b, dbdU, dbdC)) ubb += v.Ubar[k].y * u / U;
+        int fseen[4], nf = 0;   // the other component's drag speeds whose ℑxy average reads uᵇ here
+        for (int a = (comp == 0 ? i - 1 : i); a <= (comp == 0 ? i : i + 1); ++a)
+            for (int b2 = (comp == 0 ? j : j - 1); b2 <= (comp == 0 ? j + 1 : j); ++b2) {
+                int fi, fj;
+                if (comp == 0) {
+                    if (!map_index(a, g.Nx, g.px, g.Nx, fi) || !map_index(b2, g.Ny, g.py, g.Ny + 1, fj)) continue;
+                } else {
+                    if (!map_index(a, g.Nx, g.px, g.Nx + 1, fi) || !map_index(b2, g.Ny, g.py, g.Ny, fj)) continue;
+                }
+                int kf = g.idx(fi, fj);
+                if (!first_time(fseen, nf, kf)) continue;
+                double w, avg, Uf, phif, bf, dUf, dCf;
+                int m;
+                if (comp == 0) {
+                    if (!v_drag(ph, v.ubs, fi, fj, w, avg, Uf, phif, bf, dUf, dCf)) continue;
+                    m = (g.u_idx(fi, fj - 1) == k) + (g.u_idx(fi + 1, fj - 1) == k) + (g.u_idx(fi, fj) == k) + (g.u_idx(fi + 1, fj) == k);
+                    ubb += v.Ubar[kf].y * avg / Uf * (m / 4.0);
+                } else {
+                    if (!u_drag(ph, v.ubs, fi, fj, w, avg, Uf, phif, bf, dUf, dCf)) continue;
+                    m = (g.v_idx(fi - 1, fj) == k) + (g.v_idx(fi, fj) == k) + (g.v_idx(fi - 1, fj + 1) == k) + (g.v_idx(fi, fj + 1) == k);
+                    ubb += v.Ubar[kf].x * avg / Uf * (m / 4.0);
+                }
+            }
+        double bl = comp == 0 ? v.bbs[k].x : v.bbs[k].y;
+        double mf = comp == 0 ? u_face_F2(g, v.F2s, i, j) : v_face_F2(g, v.F2s, i, j);
+        double S = 1 + bl * mf;
+        double xv = comp == 0 ? v.xs[k].x : v.xs[k].y;
+        double Sb = -ubb * xv / (S * S);
+        double acc = (comp == 0 ? xb.x : xb.y) + viscosity_gather(v, i, j, k, comp) + ubb / S;
+        if (comp == 0) { r.x = acc; sb.x = Sb * mf; mb.x = Sb * bl; }
+        else { r.y = acc; sb.y = Sb * mf; mb.y = Sb * bl; }
+    }
+    v.r[k] = r;
+    v.sig_bb[k] = sb;
+    v.mbar[k] = mb;
+}
+
+// F₂⁻ pass: σ(F₂⁻) at each centre from the lagged shear factors of the faces beside it.
+__global__ void k_adjoint_diva_F2(AdjointView v) {
+    const DevGrid<double>& g = v.o.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int k = g.idx(i, j);
+    v.sig_F2[k] = face_mean_gather(g, i, j, k, [&](int, int, int kf, int comp) { return comp == 0 ? v.mbar[kf].x : v.mbar[kf].y; });
+}
+
+void launch_adjoint_diva(const AdjointView& v, cudaStream_t s) {
+    LaunchDims c = dims2d(v.o.g.Nx, v.o.g.Ny), f = dims2d(v.o.g.Nx + 1, v.o.g.Ny + 1);
+    k_adjoint_diva_centre<<<c.grid, c.block, 0, s>>>(v); count_launch();
+    k_adjoint_diva_face<<<f.grid, f.block, 0, s>>>(v); count_launch();
+    k_adjoint_diva_velocity<<<f.grid, f.block, 0, s>>>(v); count_launch();
+    k_adjoint_diva_F2<<<c.grid, c.block, 0, s>>>(v); count_launch();
+}
+
+// ∂J/∂log C = C Σ β̄ᵇ φ ∂drag/∂C̄ / 2 over the faces whose C̄ averages this cell (true adjoints).
+__global__ void k_adjoint_diva_gradient(AdjointView v) {
+    const PhysView& ph = v.ph;
+    const DevGrid<double>& g = v.o.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int k = g.idx(i, j);
+    double acc = face_mean_gather(g, i, j, k, [&](int fi, int fj, int kf, int comp) {
+        double w, avg, U, phi, b, dbdU, dbdC;
+        bool on = comp == 0 ? u_drag(ph, v.ubs, fi, fj, w, avg, U, phi, b, dbdU, dbdC) : v_drag(ph, v.ubs, fi, fj, w, avg, U, phi, b, dbdU, dbdC);
+        return on ? (comp == 0 ? v.bbt[kf].x : v.bbt[kf].y) * phi * dbdC : 0.0;
+    });
+    v.grad_log_C[k] = ph.C[k] * acc;
+}
+void launch_adjoint_diva_gradient(const AdjointView& v, cudaStream_t s) {
+    LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
+    k_adjoint_diva_gradient<<<d.grid, d.block, 0, s>>>(v); count_launch();
 }
 
 // Picard-adjoint progress (ext/NunatakEnzymeExt.jl:216-220): Δ = ‖λ⁺ - λ‖, M = ‖λ⁺‖ over the solved cells, then

@@ -31,7 +31,7 @@ struct PhysView {
     const double* mu;
     const double2* phi;           // (phi_u, phi_v)
     int use_mask, use_N;
-    const double2* ud = nullptr;  // prescribed (u, v) per face, NaN where free
+    const double2* ud = nullptr;      // prescribed (u, v) per face, NaN where free
 };
 
 // ---- layout conversion ---------------------------------------------------------------------------------
@@ -125,11 +125,31 @@ struct AdjointView {
     const double* eta_sigma;      // ησ of c(x*) (Nσ planes)
     double* grad_log_A;           // −λᵀ ∂[A(c) x*]/∂ log A per cell (2-D rate factor) or per cell and layer (σ);
                                   // written by k_adjoint_viscosity when not null
+    // DIVA: the step also reads its own previous βᵇ, F₂ and ησ (the lagged state s), so the fixed point is one of
+    // (x, s) and the adjoint carries σ = the adjoint of s next to λ.  These kernels work in true adjoints
+    // (q̄ = −λ), where the SSA kernels above use λ-signed sensitivities.
+    const double2* ubs = nullptr;     // basal velocities uᵇ of the step at x*
+    const double2* bbs = nullptr;     // basal drag βᵇ at x* (also the lagged βᵇ of the fixed point)
+    const double* F2s = nullptr;      // F₂ at x* (also the lagged F₂)
+    double2* txbar = nullptr;         // per centre: ∂J/∂(ℑxᶜ βᵇᵘuᵇ), ∂J/∂(ℑyᶜ βᵇᵛvᵇ)
+    double2* sig_bb = nullptr;        // σ of βᵇ per face
+    double* sig_F2 = nullptr;         // σ of F₂ per centre
+    double* sig_eta = nullptr;        // σ of ησ (Nσ planes)
+    double2* Ubar = nullptr;          // per face: ∂J/∂U of the basal speed
+    double2* ubp = nullptr;           // per face: ∂J/∂uᵇ through the basal shear stress of the centres
+    double2* mbar = nullptr;          // per face: ∂J/∂(ℑF₂⁻) of the lagged shear factor
+    double2* bbt = nullptr;           // per face: ∂J/∂βᵇ (all paths)
 };
 void launch_adjoint_coefficients(const AdjointView& v, cudaStream_t s);
 void launch_adjoint_viscosity(const AdjointView& v, cudaStream_t s);
 void launch_adjoint_velocity(const AdjointView& v, cudaStream_t s);
 void launch_adjoint_gradient(const AdjointView& v, cudaStream_t s);
+// DIVA reverse sweep of one Picard step at the fixed point (after launch_adjoint_coefficients): the centre pass
+// (viscosity, F₂, ησ; grad_log_A when set), the face pass (effective drag, basal shear stress, drag speed), the
+// velocity pass (uᵇ = x / (1 + βᵇ⁻ ℑF₂⁻), strain rates; writes r and σ of βᵇ) and the F₂⁻ pass (σ of F₂)
+void launch_adjoint_diva(const AdjointView& v, cudaStream_t s);
+// DIVA: ∂J/∂log C from bbt
+void launch_adjoint_diva_gradient(const AdjointView& v, cudaStream_t s);
 // Δ = ‖λ⁺ − λ‖, M = ‖λ⁺‖ over the solved cells into sc->p_D / sc->p_X, then λ = λ⁺
 void launch_adjoint_change(const DevGrid<double>& g, const double2* lam_new, double2* lam, SolverScalars* sc, double2* partials,
                            cudaStream_t s);
@@ -145,7 +165,7 @@ struct GeometryView {
     double rho_i, rho_w, gacc;
     int grounding, gl_stress, use_mask;
     double mask_min, mask_trans;
-    const double2* ud = nullptr;  // prescribed (u, v) per face, NaN where free: the right-hand side there
+    const double2* ud = nullptr;      // prescribed (u, v) per face, NaN where free: the right-hand side there
 };
 void launch_geometry(const GeometryView& v, cudaStream_t s);
 void launch_rate_factor(const DevGrid<double>& g, const SigmaTable& sig, int plane, const double* H, const double* T, double* A,

@@ -195,6 +195,9 @@ struct nk_problem {
     double* adj_g = nullptr;
     double* adj_grad = nullptr;
     double* adj_grad_A = nullptr;                // Nσ planes (the first alone for a 2-D rate factor)
+    // DIVA adjoint scratch (first DIVA nk_picard_adjoint): 8 pair planes (cbar, bbar, txbar, σ βᵇ, Ū, ūᵇ part,
+    // ℑF₂⁻ adjoint, β̄ᵇ), σ F₂ and σ ησ (Nσ planes)
+    void* adj_diva = nullptr;
     // Prescribed velocities (u_D, v_D) per face, NaN where free; allocated by the first set of either prescribed
     // field.  Its faces become identity rows whose values enter their neighbours' strain rates.
     double2* ud = nullptr;
@@ -1152,6 +1155,7 @@ nk_status nk_problem_destroy(nk_problem* P) {
     if (P->ev0) cudaEventDestroy(P->ev0);
     if (P->ev1) cudaEventDestroy(P->ev1);
     if (P->adj_base) cudaFree(P->adj_base);
+    if (P->adj_diva) cudaFree(P->adj_diva);
     if (P->ud) cudaFree(P->ud);
     if (P->stream) cudaStreamDestroy(P->stream);
     delete P;
@@ -1318,10 +1322,12 @@ nk_status nk_adjoint_solve(nk_problem* P, const double* bu, const double* bv, nk
 // A(c(x))⁻¹ b; at its fixed point x* the adjoint λ solves λ = A⁻ᵀ (x̄ - Nᵀ λ), N = ∂[A(c(x)) x*]/∂x, iterated
 // from λ = 0 with the problem's preconditioned CG warm-started from the previous λ, until
 // ‖λ⁺ - λ‖ ≤ max(reltol ‖λ⁺‖, abstol).  Then b̄ = λ and p̄ = -(∂[A(c(p)) x*]/∂p)ᵀ λ.
+// DIVA's step also maps its lagged state s = (βᵇ, F₂, ησ) (the overwritten coefficients it reads, diva.jl:77-80);
+// the adjoint σ of s is swept along with λ (:196-214): each iteration runs the step's reverse with q̄ = -λ and
+// the state adjoint σ, which yields r and the next σ.
 static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar, const nk_iteration_control& ctl, double* lu,
                            double* lv, double* grad, double* grad_A, nk_solve_stats* st) {
-    if (P->pd.stress_balance == NK_DIVA)
-        bad("nk_picard_adjoint covers the SSA; the DIVA step's lagged basal-drag state is not differentiated");
+    const bool diva = P->pd.stress_balance == NK_DIVA;
     if (P->ud) bad("nk_picard_adjoint: not available for a problem with prescribed velocities");
     cudaStream_t s = P->stream;
     size_t pl = P->plane;
@@ -1332,6 +1338,7 @@ static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar
         P->adj_grad = P->adj_g + pl;
         P->adj_grad_A = P->adj_grad + pl;
     }
+    if (diva && !P->adj_diva) NK_CUDA(cudaMalloc(&P->adj_diva, pl * (8 * sizeof(double2) + (1 + (size_t)P->Ns) * sizeof(double))));
     NK_CUDA(cudaMemcpyAsync(P->xprev, P->x, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));   // x*
     update_coefficients(P);                                                                         // c(x*)
     vector_in(P, P->adj_xbar, ubar, vbar);
@@ -1344,8 +1351,27 @@ static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar
     v.xs = P->xprev;
     v.lam = P->tmp_a;
     v.xbar = P->adj_xbar;
-    v.cbar = P->ub;
-    v.bbar = P->bb;
+    if (diva) {   // uᵇ, βᵇ and F₂ are the step's state: the coefficient adjoints get their own planes
+        double2* d2 = (double2*)P->adj_diva;
+        v.cbar = d2;
+        v.bbar = d2 + pl;
+        v.txbar = d2 + 2 * pl;
+        v.sig_bb = d2 + 3 * pl;
+        v.Ubar = d2 + 4 * pl;
+        v.ubp = d2 + 5 * pl;
+        v.mbar = d2 + 6 * pl;
+        v.bbt = d2 + 7 * pl;
+        v.sig_F2 = (double*)(d2 + 8 * pl);
+        v.sig_eta = v.sig_F2 + pl;
+        v.ubs = P->ub;
+        v.bbs = P->bb;
+        v.F2s = P->F2;
+        NK_CUDA(cudaMemsetAsync(v.sig_bb, 0, pl * sizeof(double2), s));
+        NK_CUDA(cudaMemsetAsync(v.sig_F2, 0, pl * (1 + (size_t)P->Ns) * sizeof(double), s));
+    } else {
+        v.cbar = P->ub;
+        v.bbar = P->bb;
+    }
     v.gbar = P->adj_g;
     v.r = P->tmp_b;
     v.grad_log_C = P->adj_grad;
@@ -1358,8 +1384,12 @@ static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar
     bool cg_failed = false;
     while (it < limit && (fixed || D > std::max(ctl.reltol * M, ctl.abstol))) {
         launch_adjoint_coefficients(v, s);
-        launch_adjoint_viscosity(v, s);
-        launch_adjoint_velocity(v, s);                       // tmp_b = x̄ - Nᵀ λ
+        if (diva) {
+            launch_adjoint_diva(v, s);                       // tmp_b = x̄ + ȳ, σ of the lagged state
+        } else {
+            launch_adjoint_viscosity(v, s);
+            launch_adjoint_velocity(v, s);                   // tmp_b = x̄ - Nᵀ λ
+        }
         nk_solve_stats lst{};
         linear_solve(P, &lst);                               // x = A⁻¹ tmp_b, from x = λ
         cg_total += lst.linear_iterations_total;
@@ -1375,11 +1405,14 @@ static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar
         if (!std::isfinite(D) || cg_failed) break;
     }
     launch_adjoint_coefficients(v, s);
-    if (grad_A) {
-        v.grad_log_A = P->adj_grad_A;
-        launch_adjoint_viscosity(v, s);
+    if (grad_A) v.grad_log_A = P->adj_grad_A;
+    if (diva) {
+        launch_adjoint_diva(v, s);
+        launch_adjoint_diva_gradient(v, s);
+    } else {
+        if (grad_A) launch_adjoint_viscosity(v, s);
+        launch_adjoint_gradient(v, s);
     }
-    launch_adjoint_gradient(v, s);
     NK_CHECK_LAUNCH();
     if (lu && lv) vector_out(P, P->tmp_a, lu, lv);
     if (grad) {

@@ -2,13 +2,18 @@
 centred finite differences, following the checks of test/test_enzyme.jl:221-381.
 
 J = ½ Σ (u - u_obs)² + (v - v_obs)² over the velocity points of a marine sheet, with u_obs from a solve with
-another friction seed.  ∂J/∂log C and ∂J/∂log A from the adjoint must match (J(p e^ε) - J(p e^-ε)) / 2ε of converged
-solves (Picard 1e-12, CG 1e-13) at seeded grounded cells:
-- on the GPU forward solve for three configurations (bounded / periodic x, free-slip / no-slip walls, Weertman /
-  regularised Coulomb friction);
-- for one layer of a σ-grid rate factor;
-- on the oracle's forward solve at one cell.
-Tolerance: 1e-4 relative to the largest gradient entry."""
+another friction seed.  The gradients from the adjoint must match centred differences of converged solves
+(Picard 1e-12, CG 1e-13):
+- ∂J/∂log C at seeded grounded cells, (J(C e^ε) - J(C e^-ε)) / 2ε, on the GPU forward solve for three
+  configurations (bounded / periodic x, free-slip / no-slip walls, Weertman / regularised Coulomb friction);
+- ∂J/∂log A along seeded random directions d over the whole field, (J(A e^(εd)) - J(A e^(-εd))) / 2ε against
+  ⟨∂J/∂log A, d⟩ (one cell's A moves J too little to be resolved against the solver tolerances), for the same
+  three configurations and for a σ-grid rate factor;
+- on the oracle's forward solve at one cell;
+- for DIVA (Arrhenius σ-grid rate factor, regularised Coulomb friction), whose step also carries its lagged
+  βᵇ, F₂ and ησ: log C and log A along random directions on the GPU forward map, log C on the oracle's.
+Tolerance: 1e-4 relative to the largest gradient entry (per cell) or to Σ|gᵢdᵢ| (directions).  The step ε is 1e-3
+(1e-4 for log A, whose second derivative along d is large against the misfit of these cases)."""
 import math
 
 import numpy as np
@@ -89,12 +94,14 @@ def test_picard_adjoint_matches_finite_differences(gpu_cls, kind):
     assert np.array_equal(P.get("u"), xs[0])              # the forward state is left at x*
     scale, scale_a = np.max(np.abs(grad)), np.max(np.abs(grad_a))
     assert scale > 0 and scale_a > 0
-    for n, cell in enumerate(_cells(P, 4, 7)):
+    for cell in _cells(P, 4, 7):
         fd = _fd(P, case, cell, xs, uo, vo)
         assert abs(fd - grad[cell]) <= RTOL * scale, (kind, cell, fd, grad[cell], scale)
-        if n < 2:
-            fd = _fd(P, case, cell, xs, uo, vo, "A")
-            assert abs(fd - grad_a[cell]) <= RTOL * scale_a, (kind, "A", cell, fd, grad_a[cell], scale_a)
+    A0 = P.get("A")
+    d = np.random.default_rng(31).standard_normal(A0.shape)
+    fd = _directional_fd(P, "A", A0, d, xs, uo, vo, eps=1e-6)
+    ad = float(np.sum(grad_a * d))
+    assert abs(fd - ad) <= RTOL * np.sum(np.abs(grad_a * d)), (kind, "A", fd, ad)
 
 
 def test_picard_adjoint_rate_factor_on_the_sigma_grid(gpu_cls):
@@ -116,11 +123,14 @@ def test_picard_adjoint_rate_factor_on_the_sigma_grid(gpu_cls):
     xs = (P.get("u"), P.get("v"))
     _, _, _, grad_a, st = P.picard_adjoint(ub, vb, M.Convergence(reltol=1e-12, maxiter=500))
     assert st.status == 0 and grad_a.shape == (ns,) + A2.shape
-    cell = _cells(P, 1, 3)[0]
-    for layer in (1, ns - 2):
-        idx = (layer,) + cell
-        fd = _fd(P, case, idx, xs, uo, vo, "A")
-        assert abs(fd - grad_a[idx]) <= RTOL * np.max(np.abs(grad_a)), (layer, cell, fd, grad_a[idx])
+    rng = np.random.default_rng(37)
+    for layer in (None, 1, ns - 2):   # every layer at once, then single layers
+        d = rng.standard_normal(grad_a.shape)
+        if layer is not None:
+            d[np.arange(ns) != layer] = 0.0
+        fd = _directional_fd(P, "A", fields["A"], d, xs, uo, vo, eps=1e-4)
+        ad = float(np.sum(grad_a * d))
+        assert abs(fd - ad) <= RTOL * np.sum(np.abs(grad_a * d)), (layer, fd, ad)
 
 
 def test_picard_adjoint_matches_oracle_finite_difference(gpu_cls, oracle_cls):
@@ -134,3 +144,84 @@ def test_picard_adjoint_matches_oracle_finite_difference(gpu_cls, oracle_cls):
     cell = _cells(P, 1, 11)[0]
     fd = _fd(O, case, cell, xs, uo, vo)
     assert abs(fd - grad[cell]) <= RTOL * np.max(np.abs(grad)), (cell, fd, grad[cell])
+
+
+def _diva(friction, obs=False):
+    solver = M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-13, maxiter=20_000),
+                                   picard_iteration_control=M.Convergence(reltol=1e-13, maxiter=1000),
+                                   preconditioner=M.StressBalanceMultigridPreconditioner(minimum_coarse_size=4))
+    case = workloads.diva_sheet(48, 24, dx=32e3, velocity_solver=solver, Nsigma=6)
+    cfg = dict(case.config)
+    if friction == "weertman":
+        cfg["friction"] = M.WeertmanFriction(coefficient=None, exponent=1.0 / 3.0)
+    fields = dict(case.fields)
+    if obs:   # other friction and a thinner sheet, so that the misfit dominates J's second-order terms
+        fields["C"] = fields["C"] * np.exp(0.3 * np.random.default_rng(5).standard_normal(fields["C"].shape))
+        fields["H"] = 0.97 * fields["H"]
+    return workloads.Case(f"diva_{friction}", case.grid, cfg, fields, temperature=case.temperature)
+
+
+def _directional_fd(P, name, p0, d, xs, uo, vo, eps=EPS):
+    """(J(p e^(εd)) - J(p e^(-εd))) / 2ε: the derivative of J along the log-space direction d, from converged solves
+    warm-started at x*."""
+    J = []
+    for sgn in (1.0, -1.0):
+        P.set(name, p0 * np.exp(sgn * eps * d))
+        P.set("u", xs[0])
+        P.set("v", xs[1])
+        assert P.picard_solve().status == 0
+        J.append(_cost(P, uo, vo)[0])
+    P.set(name, p0)
+    return (J[0] - J[1]) / (2 * eps)
+
+
+def _diva_setup(cls, friction):
+    obs = _diva(friction, obs=True).problem(cls)
+    assert obs.picard_solve().status == 0
+    uo, vo = obs.get("u"), obs.get("v")
+    case = _diva(friction)
+    P = case.problem(cls)
+    assert P.picard_solve().status == 0
+    return case, P, uo, vo
+
+
+# The DIVA adjoint's stopping test watches λ (as the reference's does); the lagged-state adjoint σ settles more
+# slowly, so these checks iterate to 1e-14.
+DIVA_ADJOINT = M.Convergence(reltol=1e-14, maxiter=3000)
+
+
+@pytest.mark.parametrize("friction", ["weertman", "coulomb"])
+def test_picard_adjoint_diva_matches_finite_differences(gpu_cls, friction):
+    """DIVA: ⟨∂J/∂log C, d⟩ and ⟨∂J/∂log A, d⟩ against directional differences along seeded random directions.
+    The Coulomb cap (τᵇ ≤ α²N) leaves J nearly insensitive to C, so there the C difference takes ε = 1e-2 and is
+    resolved to 1e-3 only."""
+    case, P, uo, vo = _diva_setup(gpu_cls, friction)
+    _, ub, vb = _cost(P, uo, vo)
+    xs = (P.get("u"), P.get("v"))
+    C0, A0 = P.get("C"), P.get("A")
+    lu, lv, grad, grad_a, st = P.picard_adjoint(ub, vb, DIVA_ADJOINT)
+    assert st.status == 0 and st.picard_iterations > 1
+    assert grad_a.shape == A0.shape
+    rng = np.random.default_rng(17)
+    checks = (("C", C0, grad, 1e-2 if friction == "coulomb" else EPS, 1e-3 if friction == "coulomb" else RTOL),
+              ("A", A0, grad_a, 1e-4, RTOL))
+    for name, p0, g, eps, tol in checks:
+        d = rng.standard_normal(p0.shape)
+        fd = _directional_fd(P, name, p0, d, xs, uo, vo, eps=eps)
+        ad = float(np.sum(g * d))
+        assert abs(fd - ad) <= tol * np.sum(np.abs(g * d)), (name, fd, ad)
+
+
+def test_picard_adjoint_diva_matches_oracle_finite_difference(gpu_cls, oracle_cls):
+    """The GPU DIVA adjoint against a directional difference of the oracle's forward solves (Weertman drag)."""
+    case, P, uo, vo = _diva_setup(gpu_cls, "weertman")
+    _, ub, vb = _cost(P, uo, vo)
+    _, _, grad, _, st = P.picard_adjoint(ub, vb, DIVA_ADJOINT)
+    assert st.status == 0
+    O = case.problem(oracle_cls)
+    assert O.picard_solve().status == 0
+    xs = (O.get("u"), O.get("v"))
+    d = np.random.default_rng(23).standard_normal(grad.shape)
+    fd = _directional_fd(O, "C", O.get("C"), d, xs, uo, vo)
+    ad = float(np.sum(grad * d))
+    assert abs(fd - ad) <= RTOL * np.sum(np.abs(grad * d)), (fd, ad)
