@@ -75,6 +75,9 @@ def parse():
                     help="the adjoint workload instead: gradient of a velocity misfit with respect to log C on the "
                          "512x256 marine sheet by the fixed-point Picard adjoint, checked against centred differences")
     ap.add_argument("--fd-cells", type=int, default=32, help="cells of the finite-difference check (--adjoint)")
+    ap.add_argument("--diva", action="store_true",
+                    help="the DIVA workload instead: one solve of the 2048x1024 DIVA sheet (Nσ = 10, Arrhenius A, "
+                         "regularised Coulomb drag) in mixed precision and in FP64, from rest")
     ap.add_argument("--profile-grid", type=int, nargs=2, default=[256, 128], metavar=("NX", "NY"),
                     help="grid of the marine-sheet solve that --profile solve runs")
     return ap.parse_args()
@@ -465,6 +468,42 @@ def run_adjoint(args, nk, workloads, ctx):
         "cells": [[int(c[0]), int(c[1]), a, f] for c, a, f in zip(cells, ad, fd)]}), flush=True)
 
 
+def run_diva(nk, workloads, ctx):
+    """The DIVA workload: the 2048x1024 (1 km) DIVA sheet with Nσ = 10, the Arrhenius rate factor of the seeded
+    temperature field, regularised Coulomb drag (α² = 0.5, m = 1/3) and a front at x = 1900 km, solved from rest
+    with Picard 1e-6 x multigrid PCG 1e-8, once in mixed precision and once in FP64 (after a first solve that
+    captures the CUDA graph).  Reports device time per solve, iterations, the mixed-vs-FP64 velocity error and the
+    transition speed (α² N / C)^(1/m) that the reference's regularised Coulomb law implies at grounded cells."""
+    nx, ny = 2048, 1024
+    res, vel = {}, {}
+    for prec in ("mixed", "fp64"):
+        P = workloads.diva_sheet(nx, ny, precision=prec).problem(nk.Problem, context=ctx)
+        zu, zv = np.zeros(P.shape("u")), np.zeros(P.shape("v"))
+        P.picard_solve()                                  # graph capture and warm-up
+        P.set("u", zu)
+        P.set("v", zv)
+        st = P.picard_solve()
+        res[prec] = {"ms_per_solve": st.device_ms, "picard_iterations": st.picard_iterations,
+                     "cg_iterations": st.linear_iterations_total, "status": st.status}
+        vel[prec] = (P.get("u"), P.get("v"))
+        if prec == "fp64":
+            N, C, phi, H = P.get("N"), P.get("C"), P.get("phi"), P.get("H")
+            grounded = (phi > 0.5) & (H > 0) & (N > 0)
+            ut = (0.5 * N[grounded] / C[grounded]) ** 3 * workloads.YEAR
+            transition = {"p10": float(np.percentile(ut, 10)), "median": float(np.median(ut)), "p90": float(np.percentile(ut, 90))}
+        P.close()
+    (um, vm), (u6, v6) = vel["mixed"], vel["fp64"]
+    err = float(np.sqrt(np.sum((um - u6) ** 2) + np.sum((vm - v6) ** 2)) / np.sqrt(np.sum(u6 ** 2) + np.sum(v6 ** 2)))
+    print(json.dumps({
+        "metric": "DIVA velocity solve time on GB300, mixed vs FP64",
+        "config": {"workload": "diva_sheet 2048x1024 dx=1km, Nsigma=10 (faces (k/10)^2), Arrhenius A from T(zeta) = 270 - 17 zeta "
+                               "+ 3 K x seeded field, regularised Coulomb (alpha^2 = 0.5, m = 1/3), front at x = 1900 km; "
+                               "Picard 1e-6 x multigrid PCG 1e-8, from rest"},
+        "mixed": res["mixed"], "fp64": res["fp64"], "speedup_mixed_vs_fp64": res["fp64"]["ms_per_solve"] / res["mixed"]["ms_per_solve"],
+        "rel_error_mixed_vs_fp64": err, "max_speed_m_per_yr": float(np.max(np.abs(u6)) * workloads.YEAR),
+        "coulomb_transition_speed_m_per_yr": transition}), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local_rank = dist_env()
@@ -490,6 +529,10 @@ def main():
     if args.adjoint:
         if rank == 0:
             run_adjoint(args, nk, workloads, ctx)
+        return
+    if args.diva:
+        if rank == 0:
+            run_diva(nk, workloads, ctx)
         return
 
     def barrier():

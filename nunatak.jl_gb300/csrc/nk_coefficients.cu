@@ -496,8 +496,8 @@ __global__ void k_adjoint_coefficients(AdjointView v) {
     }
     bool has_u = j < g.Ny && (i < g.Nx || !g.px), has_v = i < g.Nx && (j < g.Ny || !g.py);
     uint8_t m = o.mask[k];
-    if (has_u && !(m & U_INACTIVE)) bb.x = v.lam[k].x * g.Az_fc(i, j) * v.xs[k].x;
-    if (has_v && !(m & V_INACTIVE)) bb.y = v.lam[k].y * g.Az_cf(i, j) * v.xs[k].y;
+    if (has_u && !(m & U_IDENTITY)) bb.x = v.lam[k].x * g.Az_fc(i, j) * v.xs[k].x;
+    if (has_v && !(m & V_IDENTITY)) bb.y = v.lam[k].y * g.Az_cf(i, j) * v.xs[k].y;
     v.cbar[k] = cb;
     v.bbar[k] = bb;
 }

@@ -37,18 +37,17 @@ constexpr int BY = 8;
 constexpr int BLOCK_THREADS = BX * BY;
 
 // Mask bits of the operator (one byte per (i, j)).
-constexpr uint8_t U_INACTIVE = 1;   // u point is a wall or ice free: identity row, zero in strain rates
+constexpr uint8_t U_INACTIVE = 1;   // u point is a wall or ice free (and not prescribed): identity row, zero in strain rates
 constexpr uint8_t V_INACTIVE = 2;
 constexpr uint8_t U_WALL = 4;       // wall (peripheral) only: the viscosity masks walls, not ice-free points
 constexpr uint8_t V_WALL = 8;
-// Prescribed velocity (the Dirichlet extension; the reference has none): the row is an identity row (the bit comes
-// with U_INACTIVE / V_INACTIVE) whose value, held fixed at the prescribed one, still enters the strain rates.
+// Prescribed velocity (the Dirichlet extension; the reference has none): an identity row whose value, held fixed
+// at the prescribed one, still enters the strain rates.  U_INACTIVE is cleared on such a face, so the reads of the
+// strain rates test U_INACTIVE alone and the rows test U_IDENTITY.
 constexpr uint8_t U_DIRICHLET = 16;
 constexpr uint8_t V_DIRICHLET = 32;
-// Read as zero in the strain rates: inactive and not prescribed.  Kept as its own bit so that the hot reads of
-// the operator test one bit.
-constexpr uint8_t U_ZERO = 64;
-constexpr uint8_t V_ZERO = 128;
+constexpr uint8_t U_IDENTITY = U_INACTIVE | U_DIRICHLET;
+constexpr uint8_t V_IDENTITY = V_INACTIVE | V_DIRICHLET;
 
 template <typename T> struct Vec2;
 template <> struct Vec2<double> { using type = double2; };

@@ -154,7 +154,7 @@ __device__ __forceinline__ void restrict_at(const LevelView<T>& C, const OpView<
     uint8_t m = C.o.mask[k];
     T su = T(0), sv = T(0);
     int a0, a1, b0, b1;
-    if (!(m & U_INACTIVE)) {
+    if (!(m & U_IDENTITY)) {
         offsets(true, C.cx, a0, a1);
         offsets(false, C.cy, b0, b1);
         for (int a = a0; a <= a1; ++a)
@@ -164,7 +164,7 @@ __device__ __forceinline__ void restrict_at(const LevelView<T>& C, const OpView<
                 su += w * masked_u(fo, rf, i, j);
             }
     }
-    if (!(m & V_INACTIVE)) {
+    if (!(m & V_IDENTITY)) {
         offsets(false, C.cx, a0, a1);
         offsets(true, C.cy, b0, b1);
         for (int a = a0; a <= a1; ++a)
@@ -195,13 +195,13 @@ __device__ __forceinline__ typename Vec2<T>::type prolonged(const OpView<T>& fo,
     int I1, I2, J1, J2;
     T wx1, wx2, wy1, wy2;
     T pu = T(0), pv = T(0);
-    if (!(m & U_INACTIVE)) {
+    if (!(m & U_IDENTITY)) {
         parents<T>(i, cg.Nx, fg.px, true, C.cx, I1, I2, wx1, wx2);
         parents<T>(j, cg.Ny, fg.py, false, C.cy, J1, J2, wy1, wy2);
         pu = wx1 * (wy1 * masked_u(C.o, xc, I1, J1) + wy2 * masked_u(C.o, xc, I1, J2)) +
              wx2 * (wy1 * masked_u(C.o, xc, I2, J1) + wy2 * masked_u(C.o, xc, I2, J2));
     }
-    if (!(m & V_INACTIVE)) {
+    if (!(m & V_IDENTITY)) {
         parents<T>(i, cg.Nx, fg.px, false, C.cx, I1, I2, wx1, wx2);
         parents<T>(j, cg.Ny, fg.py, true, C.cy, J1, J2, wy1, wy2);
         pv = wx1 * (wy1 * masked_v(C.o, xc, I1, J1) + wy2 * masked_v(C.o, xc, I1, J2)) +
@@ -258,7 +258,9 @@ __global__ void k_smooth_first(LevelView<T> L, const typename Vec2<T>::type* __r
     if (i < L.o.g.Nx && j < L.o.g.Ny) smooth_point_at(L, xin, xout, true, i, j);
 }
 
-// One ℓ1-Jacobi sweep x' = x + (b - A x) / rowsum with the column-marching operator apply.
+// One ℓ1-Jacobi sweep x' = x + (b - A x) / rowsum with the column-marching operator apply.  A prescribed row has
+// weight 1/rowsum = 0 (k_inverse_row_sum), so the sweep keeps its value whatever q is there, and the identity
+// test can share the mask bit of the strain-rate reads.
 template <typename T, int R>
 __global__ void __launch_bounds__(32 * STRIP_WARPS) k_smooth_point(LevelView<T> L, const typename Vec2<T>::type* __restrict__ xin,
                                                                   typename Vec2<T>::type* __restrict__ xout, const int* done) {
@@ -268,7 +270,7 @@ __global__ void __launch_bounds__(32 * STRIP_WARPS) k_smooth_point(LevelView<T> 
     strip_origin<R>(i, j0);
     if (j0 >= L.o.g.Ny) return;   // whole warp
     struct BW { V2 b, w; };
-    strip_apply<R>(L.o, xin, i, j0, [&](int k) { return BW{L.b[k], L.irs[k]}; }, [&](int k, V2 q, V2 x, const BW& e) {
+    strip_apply<R, U_INACTIVE, V_INACTIVE>(L.o, xin, i, j0, [&](int k) { return BW{L.b[k], L.irs[k]}; }, [&](int k, V2 q, V2 x, const BW& e) {
         V2 out;
         out.x = x.x + (e.b.x - q.x) * e.w.x;
         out.y = x.y + (e.b.y - q.y) * e.w.y;
@@ -314,7 +316,8 @@ __global__ void __launch_bounds__(32 * STRIP_WARPS) k_smooth_first2(LevelView<T>
         return x;
     };
     struct BW { V2 b, w; };
-    strip_apply_src<R>(L.o, src, i, j0, [&](int k) { return BW{L.b[k], L.irs[k]}; }, [&](int k, V2 q, V2 x, const BW& e) {
+    strip_apply_src<R, U_INACTIVE, V_INACTIVE>(L.o, src, i, j0, [&](int k) { return BW{L.b[k], L.irs[k]}; },
+                                               [&](int k, V2 q, V2 x, const BW& e) {
         V2 out;
         out.x = x.x + (e.b.x - q.x) * e.w.x;
         out.y = x.y + (e.b.y - q.y) * e.w.y;
@@ -461,7 +464,7 @@ __global__ void __launch_bounds__(1024, 1)
                 int k = g.idx(g.px ? g.wrap(i, Nx) : i, g.py ? g.wrap(j, Ny) : j);
                 uint8_t mk = L.o.mask[k];
                 pk[a] = k;
-                pf[a] = (uok && !(mk & U_ZERO) ? 1 : 0) | (vok && !(mk & V_ZERO) ? 2 : 0);
+                pf[a] = (uok && !(mk & U_INACTIVE) ? 1 : 0) | (vok && !(mk & V_INACTIVE) ? 2 : 0);
             }
         }
     }
@@ -554,8 +557,8 @@ __global__ void __launch_bounds__(1024, 1)
                 T divu = (s0.x - sw.x) + (c_dxf * t01 - c_dxf * t00);
                 T divv = (s0.y - ss.y) + (c_dyf * t10 - c_dyf * t00);
                 V2 q;
-                q.x = (c_mask & U_INACTIVE) ? xx.x : azbu * xx.x - divu;
-                q.y = (c_mask & V_INACTIVE) ? xx.y : azbv * xx.y - divv;
+                q.x = (c_mask & U_IDENTITY) ? xx.x : azbu * xx.x - divu;
+                q.y = (c_mask & V_IDENTITY) ? xx.y : azbv * xx.y - divv;
                 nv.x = xx.x + (bb.x - q.x) * ww.x;
                 nv.y = xx.y + (bb.y - q.y) * ww.y;
             }

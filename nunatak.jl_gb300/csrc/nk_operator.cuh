@@ -14,7 +14,7 @@ template <typename T>
 struct OpView {
     DevGrid<T> g;
     const typename Vec4<T>::type* coef;   // (eta_H, eta_H_ff, beta_u, beta_v) per (i, j)
-    const uint8_t* mask;                  // U/V_INACTIVE, _WALL, _DIRICHLET, _ZERO bits per (i, j)
+    const uint8_t* mask;                  // U/V_INACTIVE, _WALL, _DIRICHLET bits per (i, j)
     T wall_factor;                        // wall_shear_factor: 0 free slip, 2 no slip (ssa_operator.jl:100-101)
 };
 
@@ -25,14 +25,14 @@ __device__ __forceinline__ T masked_u(const OpView<T>& o, const V2* __restrict__
     const DevGrid<T>& g = o.g;
     if ((!g.px && (i < 0 || i > g.Nx)) || g.out_y(j)) return T(0);
     int k = g.idx(g.px ? g.wrap(i, g.Nx) : i, g.py ? g.wrap(j, g.Ny) : j);
-    return (__ldg(o.mask + k) & U_ZERO) ? T(0) : p[k].x;
+    return (__ldg(o.mask + k) & U_INACTIVE) ? T(0) : p[k].x;
 }
 template <typename T, typename V2>
 __device__ __forceinline__ T masked_v(const OpView<T>& o, const V2* __restrict__ p, int i, int j) {
     const DevGrid<T>& g = o.g;
     if (g.out_x(i) || (!g.py && (j < 0 || j > g.Ny))) return T(0);
     int k = g.idx(g.px ? g.wrap(i, g.Nx) : i, g.py ? g.wrap(j, g.Ny) : j);
-    return (__ldg(o.mask + k) & V_ZERO) ? T(0) : p[k].y;
+    return (__ldg(o.mask + k) & V_INACTIVE) ? T(0) : p[k].y;
 }
 
 // Δy Txx and Δx Tyy at centre (i, j): normal_stress_xx/yy times the face length (ssa_operator.jl:60-65).
@@ -75,8 +75,8 @@ __device__ __forceinline__ V2 apply_at(const OpView<T>& o, const V2* __restrict_
     V2 q;
     T divu = (sxx0 - sxxw) + (g.dxf[i] * t01 - g.dxf[i] * t00);
     T divv = (syy0 - syys) + (g.dyf[j] * t10 - g.dyf[j] * t00);
-    q.x = (m & U_INACTIVE) ? pc.x : g.Az_fc(i, j) * c.z * pc.x - divu;
-    q.y = (m & V_INACTIVE) ? pc.y : g.Az_cf(i, j) * c.w * pc.y - divv;
+    q.x = (m & U_IDENTITY) ? pc.x : g.Az_fc(i, j) * c.z * pc.x - divu;
+    q.y = (m & V_IDENTITY) ? pc.y : g.Az_cf(i, j) * c.w * pc.y - divv;
     return q;
 }
 
@@ -101,13 +101,13 @@ template <typename T>
 __device__ __forceinline__ T x_diagonal(const OpView<T>& o, int i, int j, uint8_t m) {
     T d = o.g.Az_fc(i, j) * o.coef[o.g.idx(i, j)].z + x_normal_diagonal(o, i, j) + x_normal_diagonal(o, i - 1, j) +
           x_shear_diagonal(o, i, j) + x_shear_diagonal(o, i, j + 1);
-    return ((m & U_INACTIVE) || d == T(0)) ? T(1) : d;
+    return ((m & U_IDENTITY) || d == T(0)) ? T(1) : d;
 }
 template <typename T>
 __device__ __forceinline__ T y_diagonal(const OpView<T>& o, int i, int j, uint8_t m) {
     T d = o.g.Az_cf(i, j) * o.coef[o.g.idx(i, j)].w + y_normal_diagonal(o, i, j) + y_normal_diagonal(o, i, j - 1) +
           y_shear_diagonal(o, i, j) + y_shear_diagonal(o, i + 1, j);
-    return ((m & V_INACTIVE) || d == T(0)) ? T(1) : d;
+    return ((m & V_IDENTITY) || d == T(0)) ? T(1) : d;
 }
 
 // x_absolute_row_sum / y_absolute_row_sum (multigrid_preconditioner.jl:195-211).
@@ -118,7 +118,7 @@ __device__ __forceinline__ T x_row_sum(const OpView<T>& o, int i, int j, uint8_t
           T(4) * (eta_c(o, i, j) + eta_c(o, i - 1, j)) +
           T(2) * (x_shear_diagonal(o, i, j) + x_shear_diagonal(o, i, j + 1)) +
           T(2) * (corner_factor(o, i, j) * eta_ff(o, i, j) + corner_factor(o, i, j + 1) * eta_ff(o, i, j + 1));
-    return ((m & U_INACTIVE) || s == T(0)) ? T(1) : s;
+    return ((m & U_IDENTITY) || s == T(0)) ? T(1) : s;
 }
 template <typename T>
 __device__ __forceinline__ T y_row_sum(const OpView<T>& o, int i, int j, uint8_t m) {
@@ -127,7 +127,7 @@ __device__ __forceinline__ T y_row_sum(const OpView<T>& o, int i, int j, uint8_t
           T(4) * (eta_c(o, i, j) + eta_c(o, i, j - 1)) +
           T(2) * (y_shear_diagonal(o, i, j) + y_shear_diagonal(o, i + 1, j)) +
           T(2) * (corner_factor(o, i, j) * eta_ff(o, i, j) + corner_factor(o, i + 1, j) * eta_ff(o, i + 1, j));
-    return ((m & V_INACTIVE) || s == T(0)) ? T(1) : s;
+    return ((m & V_IDENTITY) || s == T(0)) ? T(1) : s;
 }
 
 // Operator mask inactive test of a face (peripheral or ice free) outside the stored range.
@@ -135,13 +135,13 @@ template <typename T>
 __device__ __forceinline__ bool u_inactive(const OpView<T>& o, int i, int j) {
     const DevGrid<T>& g = o.g;
     if ((!g.px && (i < 0 || i > g.Nx)) || g.out_y(j)) return true;
-    return __ldg(o.mask + g.idx(g.px ? g.wrap(i, g.Nx) : i, g.py ? g.wrap(j, g.Ny) : j)) & U_INACTIVE;
+    return __ldg(o.mask + g.idx(g.px ? g.wrap(i, g.Nx) : i, g.py ? g.wrap(j, g.Ny) : j)) & U_IDENTITY;
 }
 template <typename T>
 __device__ __forceinline__ bool v_inactive(const OpView<T>& o, int i, int j) {
     const DevGrid<T>& g = o.g;
     if (g.out_x(i) || (!g.py && (j < 0 || j > g.Ny))) return true;
-    return __ldg(o.mask + g.idx(g.px ? g.wrap(i, g.Nx) : i, g.py ? g.wrap(j, g.Ny) : j)) & V_INACTIVE;
+    return __ldg(o.mask + g.idx(g.px ? g.wrap(i, g.Nx) : i, g.py ? g.wrap(j, g.Ny) : j)) & V_IDENTITY;
 }
 
 // y-line couplings of the line smoother (multigrid_preconditioner.jl:223-227).
@@ -223,8 +223,8 @@ __device__ __forceinline__ V2 tiled_apply(const OpView<T>& o, const V2* __restri
     auto c = o.coef[k];
     T divu = (sm.sxx[ty + 1][tx + 1] - sm.sxx[ty + 1][tx]) + (g.dxf[i] * sm.txy[ty + 1][tx] - g.dxf[i] * sm.txy[ty][tx]);
     T divv = (sm.syy[ty + 1][tx + 1] - sm.syy[ty][tx + 1]) + (g.dyf[j] * sm.txy[ty][tx + 1] - g.dyf[j] * sm.txy[ty][tx]);
-    q.x = (m & U_INACTIVE) ? pc.x : g.Az_fc(i, j) * c.z * pc.x - divu;
-    q.y = (m & V_INACTIVE) ? pc.y : g.Az_cf(i, j) * c.w * pc.y - divv;
+    q.x = (m & U_IDENTITY) ? pc.x : g.Az_fc(i, j) * c.z * pc.x - divu;
+    q.y = (m & V_IDENTITY) ? pc.y : g.Az_cf(i, j) * c.w * pc.y - divv;
     return q;
 }
 

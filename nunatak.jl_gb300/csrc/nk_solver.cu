@@ -100,11 +100,9 @@ __global__ void k_mask(OpView<T> o, uint8_t* mask, const double2* ud) {
     if (wv || fv) m |= V_INACTIVE;
     if (ud && i < g.Nx && j < g.Ny) {   // the faces of the solved rows (prescribed_u / prescribed_v)
         double2 d = ud[g.idx(i, j)];
-        if (!isnan(d.x)) m |= U_DIRICHLET | U_INACTIVE;
-        if (!isnan(d.y)) m |= V_DIRICHLET | V_INACTIVE;
+        if (!isnan(d.x)) m = (m & ~U_INACTIVE) | U_DIRICHLET;
+        if (!isnan(d.y)) m = (m & ~V_INACTIVE) | V_DIRICHLET;
     }
-    if ((m & U_INACTIVE) && !(m & U_DIRICHLET)) m |= U_ZERO;
-    if ((m & V_INACTIVE) && !(m & V_DIRICHLET)) m |= V_ZERO;
     mask[g.idx(i, j)] = m;
 }
 template <typename T>
@@ -149,9 +147,9 @@ __global__ void k_inverse_row_sum(OpView<T> o, typename Vec2<T>::type* irs) {
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i >= o.g.Nx || j >= o.g.Ny) return;
     uint8_t m = o.mask[o.g.idx(i, j)];
-    typename Vec2<T>::type r;
-    r.x = T(1) / x_row_sum(o, i, j, m);
-    r.y = T(1) / y_row_sum(o, i, j, m);
+    typename Vec2<T>::type r;   // zero on prescribed rows: the point smoothers keep their value there
+    r.x = (m & U_DIRICHLET) ? T(0) : T(1) / x_row_sum(o, i, j, m);
+    r.y = (m & V_DIRICHLET) ? T(0) : T(1) / y_row_sum(o, i, j, m);
     irs[o.g.idx(i, j)] = r;
 }
 template <typename T>

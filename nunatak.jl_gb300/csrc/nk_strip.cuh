@@ -53,8 +53,8 @@ struct StripRow {
     typename Vec2<T>::type raw;
     uint8_t m;
     bool uok, vok;
-    __device__ __forceinline__ T mu() const { return (uok && !(m & U_ZERO)) ? raw.x : T(0); }
-    __device__ __forceinline__ T mv() const { return (vok && !(m & V_ZERO)) ? raw.y : T(0); }
+    __device__ __forceinline__ T mu() const { return (uok && !(m & U_INACTIVE)) ? raw.x : T(0); }
+    __device__ __forceinline__ T mv() const { return (vok && !(m & V_INACTIVE)) ? raw.y : T(0); }
 };
 
 // The pair at (i, j) as masked_u / masked_v read it; zero outside the ranges those functions read.
@@ -85,7 +85,9 @@ struct NoExtra {};
 // `extra(k)` is called first (with the loads of the walk, so its global reads are in flight together with them)
 // and later `emit(k, q, raw, e)` with k = idx(i, j), q the operator result, raw the stored pair p(i, j) and e what
 // extra(k) returned.  Every lane of the warp must call this (shuffles); lanes with nothing to do pass through.
-template <int R, typename T, typename Src, typename Extra, typename Emit>
+// IU / IV: the mask bits of the identity rows (q = p).  A caller whose own rule already fixes the prescribed rows
+// may pass U_INACTIVE / V_INACTIVE, the bits of the strain-rate reads, which then serve both tests.
+template <int R, uint8_t IU = U_IDENTITY, uint8_t IV = V_IDENTITY, typename T, typename Src, typename Extra, typename Emit>
 __device__ __forceinline__ void strip_apply_src(const OpView<T>& o, Src&& src, int i, int j0, Extra&& extra, Emit&& emit) {
     using V2 = typename Vec2<T>::type;
     using V4 = typename Vec4<T>::type;
@@ -175,8 +177,8 @@ __device__ __forceinline__ void strip_apply_src(const OpView<T>& o, Src&& src, i
             T divu = (sxx - sxx_w) + (dxf_i * t_n - dxf_i * t_c);
             T divv = (syy - syy_s) + (dyf[r] * t_e - dyf[r] * t_c);
             V2 q;
-            q.x = (row[r + 1].m & U_INACTIVE) ? x.x : (dxf_i * dyc[r + 1]) * c.z * x.x - divu;
-            q.y = (row[r + 1].m & V_INACTIVE) ? x.y : (dxc_i * dyf[r]) * c.w * x.y - divv;
+            q.x = (row[r + 1].m & IU) ? x.x : (dxf_i * dyc[r + 1]) * c.z * x.x - divu;
+            q.y = (row[r + 1].m & IV) ? x.y : (dxc_i * dyf[r]) * c.w * x.y - divv;
             emit(g.idx(i, j), q, x, ex[r]);
         }
         syy_s = syy;
@@ -185,10 +187,10 @@ __device__ __forceinline__ void strip_apply_src(const OpView<T>& o, Src&& src, i
 }
 
 // strip_apply_src with the operand read from an array.
-template <int R, typename T, typename Extra, typename Emit>
+template <int R, uint8_t IU = U_IDENTITY, uint8_t IV = V_IDENTITY, typename T, typename Extra, typename Emit>
 __device__ __forceinline__ void strip_apply(const OpView<T>& o, const typename Vec2<T>::type* __restrict__ p, int i, int j0,
                                             Extra&& extra, Emit&& emit) {
-    strip_apply_src<R>(o, [p](int k, int, int) { return p[k]; }, i, j0, extra, emit);
+    strip_apply_src<R, IU, IV>(o, [p](int k, int, int) { return p[k]; }, i, j0, extra, emit);
 }
 
 // Column and first row of the calling thread in a strip launch of R rows per warp (strip_dims).
