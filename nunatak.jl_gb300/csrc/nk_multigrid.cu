@@ -371,13 +371,68 @@ void launch_line_relax(const LevelView<T>& L, typename Vec2<T>::type* x, int fir
     k_line_relax<T><<<nb, 128, 0, s>>>(L, x, first, done); count_launch();
 }
 
+// restrict_at for a coarse point away from every edge of a level halved in both directions: its 4 x 4 fine
+// footprint (2I-1..2I+2) x (2J-1..2J+2) needs no clamp, wrap or range test and its weights no folding, so the
+// pairs and mask bytes are loaded once for both components.  The sums run in restrict_at's order (x offset
+// outer, y offset inner) with the same weight products, so the result is bit for bit restrict_at's.
+template <typename T>
+__device__ __forceinline__ void restrict_interior(const LevelView<T>& C, const OpView<T>& fo, const typename Vec2<T>::type* __restrict__ rf,
+                                                  typename Vec2<T>::type* bc, typename Vec2<T>::type* first_out, int I, int J) {
+    using V2 = typename Vec2<T>::type;
+    const DevGrid<T>& cg = C.o.g;
+    const DevGrid<T>& fg = fo.g;
+    int k = cg.idx(I, J);
+    uint8_t m = C.o.mask[k];
+    const T wf[3] = {T(1) / T(2), T(1), T(1) / T(2)};                     // face offsets -1, 0, 1
+    const T wc[4] = {T(1) / T(4), T(3) / T(4), T(3) / T(4), T(1) / T(4)}; // centre offsets -1, 0, 1, 2
+    T pu[4][3], pv[3][4];   // masked u at [y][x] offsets (-1..2, -1..1), masked v at (-1..1, -1..2)
+    int k0 = fg.idx(2 * I - 1, 2 * J - 1);
+#pragma unroll
+    for (int b = 0; b < 4; ++b)
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            int kf = k0 + b * fg.pitch + a;
+            uint8_t mf = __ldg(fo.mask + kf);
+            V2 r = rf[kf];
+            if (a < 3) pu[b][a] = (mf & U_INACTIVE) ? T(0) : r.x;
+            if (b < 3) pv[b][a] = (mf & V_INACTIVE) ? T(0) : r.y;
+        }
+    T su = T(0), sv = T(0);
+    if (!(m & U_IDENTITY)) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) su += (wf[a] * wc[b]) * pu[b][a];
+    }
+    if (!(m & V_IDENTITY)) {
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) sv += (wc[a] * wf[b]) * pv[b][a];
+    }
+    V2 o;
+    o.x = su;
+    o.y = sv;
+    bc[k] = o;
+    if (first_out) {
+        V2 w = C.irs[k], x;
+        x.x = su * w.x;
+        x.y = sv * w.y;
+        first_out[k] = x;
+    }
+}
+
 template <typename T>
 __global__ void k_restrict(LevelView<T> C, OpView<T> fo, const typename Vec2<T>::type* __restrict__ rf,
                            typename Vec2<T>::type* bc, typename Vec2<T>::type* first_out, const int* done) {
     if (stopped(done)) return;
     int I = blockIdx.x * BX + threadIdx.x, J = blockIdx.y * BY + threadIdx.y;
-    if (I >= C.o.g.Nx || J >= C.o.g.Ny) return;
-    restrict_at(C, fo, rf, bc, first_out, I, J);
+    const DevGrid<T>& cg = C.o.g;
+    if (I >= cg.Nx || J >= cg.Ny) return;
+    if (C.cx == 2 && C.cy == 2 && I >= 1 && I <= cg.Nx - 2 && J >= 1 && J <= cg.Ny - 2)
+        restrict_interior(C, fo, rf, bc, first_out, I, J);
+    else
+        restrict_at(C, fo, rf, bc, first_out, I, J);
 }
 template <typename T>
 void launch_restrict(const LevelView<T>& coarse, const LevelView<T>& fine, const typename Vec2<T>::type* r_fine,
@@ -386,13 +441,46 @@ void launch_restrict(const LevelView<T>& coarse, const LevelView<T>& fine, const
     k_restrict<T><<<d.grid, d.block, 0, s>>>(coarse, fine.o, r_fine, b_coarse, first_out, done); count_launch();
 }
 
+// prolong_at for a fine point (i, j) in 2..Nx-3 x 2..Ny-3 of a level halved in both directions: its coarse
+// parents (i/2 and a neighbour, j/2 and a neighbour) need no clamp, wrap or range test.  Same expression and
+// operands as prolonged(), so the result is bit for bit prolong_at's.
+template <typename T>
+__device__ __forceinline__ void prolong_interior(const OpView<T>& fo, const LevelView<T>& C, typename Vec2<T>::type* xf,
+                                                 const typename Vec2<T>::type* __restrict__ xc, int i, int j) {
+    const DevGrid<T>& cg = C.o.g;
+    int k = fo.g.idx(i, j);
+    uint8_t m = fo.mask[k];
+    typename Vec2<T>::type x = xf[k];
+    int I = i >> 1, J = j >> 1;
+    bool ei = (i & 1) == 0, ej = (j & 1) == 0;   // the 1-based index is odd
+    auto cu = [&](int a, int b) { int kc = cg.idx(a, b); return (__ldg(C.o.mask + kc) & U_INACTIVE) ? T(0) : xc[kc].x; };
+    auto cv = [&](int a, int b) { int kc = cg.idx(a, b); return (__ldg(C.o.mask + kc) & V_INACTIVE) ? T(0) : xc[kc].y; };
+    T pu = T(0), pv = T(0);
+    if (!(m & U_IDENTITY)) {   // x: face parents (I, I or I + 1); y: centre parents (J, J -+ 1)
+        int I2 = ei ? I : I + 1, J2 = ej ? J - 1 : J + 1;
+        T wx1 = ei ? T(1) : T(1) / T(2), wx2 = ei ? T(0) : T(1) / T(2), wy1 = T(3) / T(4), wy2 = T(1) / T(4);
+        pu = wx1 * (wy1 * cu(I, J) + wy2 * cu(I, J2)) + wx2 * (wy1 * cu(I2, J) + wy2 * cu(I2, J2));
+    }
+    if (!(m & V_IDENTITY)) {   // x: centre parents (I, I -+ 1); y: face parents (J, J or J + 1)
+        int I2 = ei ? I - 1 : I + 1, J2 = ej ? J : J + 1;
+        T wx1 = T(3) / T(4), wx2 = T(1) / T(4), wy1 = ej ? T(1) : T(1) / T(2), wy2 = ej ? T(0) : T(1) / T(2);
+        pv = wx1 * (wy1 * cv(I, J) + wy2 * cv(I, J2)) + wx2 * (wy1 * cv(I2, J) + wy2 * cv(I2, J2));
+    }
+    x.x += pu;
+    x.y += pv;
+    xf[k] = x;
+}
+
 template <typename T>
 __global__ void k_prolongate(OpView<T> fo, LevelView<T> C, typename Vec2<T>::type* xf, const typename Vec2<T>::type* __restrict__ xc,
                              const int* done) {
     if (stopped(done)) return;
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i >= fo.g.Nx || j >= fo.g.Ny) return;
-    prolong_at(fo, C, xf, xc, i, j);
+    if (C.cx == 2 && C.cy == 2 && i >= 2 && i <= fo.g.Nx - 3 && j >= 2 && j <= fo.g.Ny - 3)
+        prolong_interior(fo, C, xf, xc, i, j);
+    else
+        prolong_at(fo, C, xf, xc, i, j);
 }
 template <typename T>
 void launch_prolongate(const LevelView<T>& fine, const LevelView<T>& coarse, typename Vec2<T>::type* x_fine,
