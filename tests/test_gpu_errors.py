@@ -42,9 +42,19 @@ def test_wait_without_a_pending_solve_is_refused():
         P.wait()
 
 
-def test_picard_adjoint_refuses_diva():
+def test_picard_adjoint_refuses_prescribed_velocities():
+    P = workloads.channel_shelf(inflow=100.0).problem(nk.Problem)
+    P.picard_solve()
+    u, v = P.get("u"), P.get("v")
+    with pytest.raises(ValueError, match="prescribed velocities"):
+        P.picard_adjoint(np.zeros_like(u), np.zeros_like(v))
+
+
+def test_picard_adjoint_of_zero_misfit_is_zero():
+    """DIVA: x̄ = 0 gives λ = 0 and zero gradients (the lagged-state sweep adds nothing from nothing)."""
     P = workloads.diva_sheet(32, 16, precision="fp64").problem(nk.Problem)
     P.picard_solve()
     u, v = P.get("u"), P.get("v")
-    with pytest.raises(ValueError, match="covers the SSA"):
-        P.picard_adjoint(np.zeros_like(u), np.zeros_like(v))
+    lu, lv, grad, grad_a, st = P.picard_adjoint(np.zeros_like(u), np.zeros_like(v))
+    assert st.status == 0
+    assert not lu.any() and not lv.any() and not grad.any() and not grad_a.any()
