@@ -46,3 +46,21 @@ def test_descriptor_struct_sizes_match_header():
     assert ctypes.sizeof(abi.IterationControl) == 32
     assert ctypes.sizeof(abi.GridDesc) == 32 + 8 * 2 + 8 * 4 + 8 + 8
     assert ctypes.sizeof(abi.SolverDesc) == 24 + 2 * 32
+
+
+def header_defines():
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    return {m.group(1): int(m.group(2)) for m in re.finditer(r"#define\s+(NK_[A-Z0-9_]+)\s+(-?\d+)\b", text)}
+
+
+def test_python_constants_match_the_header():
+    """Field ids (including the prescribed velocities) and iteration-control kinds of the ctypes mirror."""
+    from nunatak_gb300 import abi
+    d = header_defines()
+    fields = {k[len("NK_FIELD_"):].lower(): v for k, v in d.items() if k.startswith("NK_FIELD_") and k != "NK_FIELD_COUNT"}
+    assert d["NK_FIELD_COUNT"] == len(fields) == len(abi.FIELD_IDS)
+    assert sorted(abi.FIELD_IDS.values()) == sorted(fields.values())
+    assert abi.FIELD_IDS["u_prescribed"] == d["NK_FIELD_U_PRESCRIBED"] and abi.FIELD_IDS["v_prescribed"] == d["NK_FIELD_V_PRESCRIBED"]
+    for name in ("NK_CONVERGENCE", "NK_FIXED_ITERATIONS", "NK_VISCOSITY_CONVERGENCE"):
+        assert getattr(abi, name) == d[name]
+    assert set(abi.FIELD_LOCATIONS) == set(abi.FIELD_IDS)
