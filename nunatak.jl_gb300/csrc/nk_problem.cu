@@ -986,6 +986,8 @@ static FieldLoc field_loc(nk_problem* P, int id) {
 // are rebuilt.
 static void ensure_prescribed(nk_problem* P) {
     if (P->ud) return;
+    if (P->async_pending) bad("an asynchronous solve is pending (nk_problem_wait first)");
+    NK_CUDA(cudaStreamSynchronize(P->stream));   // no graph of this problem is still running when it is destroyed
     NK_CUDA(cudaMalloc((void**)&P->ud, P->plane * sizeof(double2)));
     launch_fill((double*)P->ud, (int)(2 * P->plane), std::nan(""), P->stream);
     NK_CHECK_LAUNCH();
