@@ -233,6 +233,16 @@ nk_status nk_problem_set_field(nk_problem* problem, int32_t field, const double*
 nk_status nk_problem_get_field(const nk_problem* problem, int32_t field, double* host, int64_t count);
 /* Number of values of a field in interior layout (0 for an unknown id). */
 int64_t   nk_problem_field_size(const nk_problem* problem, int32_t field);
+/* The same two copies with the field's Oceananigans parent array (parent(field), what set!/interior views wrap;
+ * the sigma grid's z halo, src/Grids/sigma_grid.jl:57): x fastest, then y, then the level, with hx, hy halo
+ * points on each side horizontally and hz levels below and above (hz = 0 for a 2-D field, whose parent has one
+ * level).  The parent's x extent is the interior count plus 2 hx (Nx + 1 + 2 hx for a Face location in a Bounded
+ * x), likewise in y; count is the parent's length.  set reads the interior points only; get writes them only and
+ * leaves the halo values as they were.  Host or device memory, as above. */
+nk_status nk_problem_set_field_parent(nk_problem* problem, int32_t field, const double* parent, int32_t hx, int32_t hy,
+                                      int32_t hz, int64_t count);
+nk_status nk_problem_get_field_parent(const nk_problem* problem, int32_t field, double* parent, int32_t hx, int32_t hy,
+                                      int32_t hz, int64_t count);
 
 /* update_geometry! + compute_driving_stress! (src/Models/ice_sheet_model_methods.jl:103-111, :126):
  * s, phi, phi_u, phi_v, N, mu from H and bed, then tau.  Replaces the reference's

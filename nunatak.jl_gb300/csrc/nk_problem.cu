@@ -1003,6 +1003,36 @@ static void copy_in(nk_problem* P, const FieldLoc& f, const double* host) {
     launch_pack(f.base, P->pitch, (int)P->plane, f.stride, f.offset, P->staging, f.nx, f.ny, f.planes, P->stream);
     NK_CHECK_LAUNCH();
 }
+// Oceananigans parent layout: the interior rows of each level are gathered into the dense staging array by
+// pitched 2-D copies (host or device source), then packed as above; out, the reverse, halos untouched.
+struct ParentLayout { size_t px, py; int hx, hy, hz; };
+static ParentLayout parent_layout(const FieldLoc& f, int hx, int hy, int hz, int64_t count) {
+    if (hx < 0 || hy < 0 || hz < 0) bad("negative halo");
+    if (f.planes == 1 && hz != 0) bad("a 2-D field's parent has one level (hz = 0)");
+    ParentLayout L{(size_t)f.nx + 2 * (size_t)hx, (size_t)f.ny + 2 * (size_t)hy, hx, hy, hz};
+    if (count != (int64_t)(L.px * L.py * ((size_t)f.planes + 2 * (size_t)hz))) bad("parent array size mismatch");
+    return L;
+}
+static size_t parent_offset(const ParentLayout& L, int level) {
+    return (((size_t)level + L.hz) * L.py + L.hy) * L.px + L.hx;
+}
+static void copy_in_parent(nk_problem* P, const FieldLoc& f, const double* parent, const ParentLayout& L) {
+    size_t n2 = (size_t)f.nx * f.ny;
+    for (int k = 0; k < f.planes; ++k)
+        NK_CUDA(cudaMemcpy2DAsync(P->staging + k * n2, f.nx * sizeof(double), parent + parent_offset(L, k), L.px * sizeof(double),
+                                  f.nx * sizeof(double), f.ny, cudaMemcpyDefault, P->stream));
+    launch_pack(f.base, P->pitch, (int)P->plane, f.stride, f.offset, P->staging, f.nx, f.ny, f.planes, P->stream);
+    NK_CHECK_LAUNCH();
+}
+static void copy_out_parent(nk_problem* P, const FieldLoc& f, double* parent, const ParentLayout& L) {
+    size_t n2 = (size_t)f.nx * f.ny;
+    launch_unpack(P->staging, f.base, P->pitch, (int)P->plane, f.stride, f.offset, f.nx, f.ny, f.planes, P->stream);
+    NK_CHECK_LAUNCH();
+    for (int k = 0; k < f.planes; ++k)
+        NK_CUDA(cudaMemcpy2DAsync(parent + parent_offset(L, k), L.px * sizeof(double), P->staging + k * n2, f.nx * sizeof(double),
+                                  f.nx * sizeof(double), f.ny, cudaMemcpyDefault, P->stream));
+    NK_CUDA(cudaStreamSynchronize(P->stream));
+}
 static void copy_out(nk_problem* P, const FieldLoc& f, double* host) {
     size_t n = (size_t)f.nx * f.ny * f.planes;
     launch_unpack(P->staging, f.base, P->pitch, (int)P->plane, f.stride, f.offset, f.nx, f.ny, f.planes, P->stream);
@@ -1204,6 +1234,45 @@ nk_status nk_problem_get_field(const nk_problem* Pc, int32_t id, double* host, i
         if (!f.base) bad("unknown field id or field not held by this problem");
         if (count != (int64_t)f.nx * f.ny * f.planes) bad("field size mismatch");
         copy_out(P, f, host);
+    });
+}
+
+// set! / interior copies on Oceananigans parent arrays: the same field handling as nk_problem_set_field /
+// nk_problem_get_field, with the interior gathered from (scattered into) the halo-padded parent
+nk_status nk_problem_set_field_parent(nk_problem* P, int32_t id, const double* parent, int32_t hx, int32_t hy, int32_t hz,
+                                      int64_t count) {
+    if (!P || !parent) return NK_BAD_ARGUMENT;
+    return guarded(P->ctx, [&] {
+        FieldLoc f = field_loc(P, id);
+        if (f.prescribed) {
+            parent_layout(f, hx, hy, hz, count);
+            ensure_prescribed(P);
+            f = field_loc(P, id);
+        }
+        if (!f.base) bad("unknown field id or field not held by this problem");
+        copy_in_parent(P, f, parent, parent_layout(f, hx, hy, hz, count));
+        if (f.coef || f.prescribed) prepare_operator(P);
+        if (f.prescribed) {
+            launch_impose_prescribed(P->fine.g, P->tau, P->ud, P->ud, P->stream);
+            launch_impose_prescribed(P->fine.g, P->x, P->ud, P->ud, P->stream);
+            NK_CHECK_LAUNCH();
+        }
+        NK_CUDA(cudaStreamSynchronize(P->stream));
+    });
+}
+
+nk_status nk_problem_get_field_parent(const nk_problem* Pc, int32_t id, double* parent, int32_t hx, int32_t hy, int32_t hz,
+                                      int64_t count) {
+    nk_problem* P = const_cast<nk_problem*>(Pc);
+    if (!P || !parent) return NK_BAD_ARGUMENT;
+    return guarded(P->ctx, [&] {
+        FieldLoc f = field_loc(P, id);
+        if (f.prescribed) {
+            ensure_prescribed(P);
+            f = field_loc(P, id);
+        }
+        if (!f.base) bad("unknown field id or field not held by this problem");
+        copy_out_parent(P, f, parent, parent_layout(f, hx, hy, hz, count));
     });
 }
 

@@ -28,6 +28,8 @@ def _declare(lib):
         "nk_problem_set_field": ([vp, i32, dp, i64], i32),
         "nk_problem_get_field": ([vp, i32, dp, i64], i32),
         "nk_problem_field_size": ([vp, i32], i64),
+        "nk_problem_set_field_parent": ([vp, i32, dp, i32, i32, i32, i64], i32),
+        "nk_problem_get_field_parent": ([vp, i32, dp, i32, i32, i32, i64], i32),
         "nk_compute_geometry": ([vp], i32),
         "nk_compute_rate_factor": ([vp] + [C.c_double] * 9, i32),
         "nk_update_coefficients": ([vp], i32),

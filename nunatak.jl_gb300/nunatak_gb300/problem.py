@@ -109,6 +109,34 @@ class Problem:
         st = self._fn("problem_set_field")(self._h, abi.FIELD_IDS[name], C.cast(C.c_void_p(int(address)), _dptr), C.c_int64(n))
         _check(st, f"set {name}", self._err())
 
+    def parent_shape(self, name, halo):
+        """Shape of the field's Oceananigans parent array for halo = (hx, hy) or (hx, hy, hz): the interior shape with
+        2 hx, 2 hy (and 2 hz levels on the sigma grid) added; C order, x fastest."""
+        hx, hy, hz = (tuple(halo) + (0,))[:3]
+        shp = self.shape(name)
+        if len(shp) == 2:
+            return (shp[0] + 2 * hy, shp[1] + 2 * hx)
+        return (shp[0] + 2 * hz, shp[1] + 2 * hy, shp[2] + 2 * hx)
+
+    def set_parent(self, name, parent, halo):
+        """set! from the field's parent array (interior points read, halos ignored)."""
+        hx, hy, hz = (tuple(halo) + (0,))[:3]
+        a = _as_f64(np.asarray(parent, dtype=np.float64))
+        if a.shape != self.parent_shape(name, halo):
+            raise ValueError(f"set_parent {name}: shape {a.shape}, expected {self.parent_shape(name, halo)}")
+        st = self._fn("problem_set_field_parent")(self._h, abi.FIELD_IDS[name], a.ctypes.data_as(_dptr), hx, hy, hz, C.c_int64(a.size))
+        _check(st, f"set_parent {name}", self._err())
+
+    def get_parent(self, name, parent, halo):
+        """Write the field into the interior of `parent` (a C-contiguous float64 array of parent_shape), halos kept."""
+        hx, hy, hz = (tuple(halo) + (0,))[:3]
+        if parent.dtype != np.float64 or not parent.flags.c_contiguous or parent.shape != self.parent_shape(name, halo):
+            raise ValueError(f"get_parent {name}: needs a C-contiguous float64 array of shape {self.parent_shape(name, halo)}")
+        st = self._fn("problem_get_field_parent")(self._h, abi.FIELD_IDS[name], parent.ctypes.data_as(_dptr), hx, hy, hz,
+                                                  C.c_int64(parent.size))
+        _check(st, f"get_parent {name}", self._err())
+        return parent
+
     def get(self, name):
         out = np.empty(self.shape(name), dtype=np.float64)
         st = self._fn("problem_get_field")(self._h, abi.FIELD_IDS[name], out.ctypes.data_as(_dptr), C.c_int64(out.size))
