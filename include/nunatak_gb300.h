@@ -372,9 +372,13 @@ nk_status nk_picard_change_noalloc(nk_context* ctx, const nk_grid_desc* grid, co
  * is that of a solve alone. */
 typedef struct nk_server_desc {
     int32_t max_in_flight;          /* requests on the device at once (>= 1) */
-    int32_t reserved;
+    int32_t flags;                  /* NK_SERVER_ADMISSION_THREAD or 0 */
     int64_t memory_cap_bytes;       /* device memory reserved for the resident problems */
 } nk_server_desc;
+/* The server runs its own host thread that retires finished requests and admits queued ones as soon as a slot
+ * frees, without the caller driving nk_server_progress / nk_server_wait; the calls below are then thread-safe
+ * and wait on it.  Without the flag the caller's calls drive the loop (one host thread). */
+#define NK_SERVER_ADMISSION_THREAD 1
 
 typedef struct nk_request {
     nk_grid_desc grid;              /* face / sigma vectors, if any, are read during nk_server_submit */

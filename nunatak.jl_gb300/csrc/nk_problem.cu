@@ -1743,8 +1743,10 @@ nk_status nk_time_kernel(nk_problem* P, int32_t kernel, int32_t repeats, int64_t
 // Serving: a request loop over resident problems, one stream per in-flight request.
 // =================================================================================================================
 #include <chrono>
+#include <condition_variable>
 #include <deque>
 #include <map>
+#include <mutex>
 #include <thread>
 #include <unordered_map>
 
@@ -1865,8 +1867,19 @@ struct nk_server {
     char* dev_base = nullptr;
     char* pin_base = nullptr;
     SubAllocator dev, pin;
+    // NK_SERVER_ADMISSION_THREAD: the loop runs on `worker`; every API call holds `mu`
+    bool threaded = false, stop = false;
+    std::thread worker;
+    mutable std::mutex mu;
+    std::condition_variable work_cv, done_cv;
+    nk_status worker_status = NK_OK;
+    std::string worker_error;
 
     double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+    // the lock of an API call: held in threaded mode, a no-op otherwise
+    std::unique_lock<std::mutex> lock() const {
+        return threaded ? std::unique_lock<std::mutex>(mu) : std::unique_lock<std::mutex>();
+    }
 };
 
 namespace nk {
@@ -2062,6 +2075,31 @@ static void progress(nk_server* S) {
     }
 }
 
+// The admission thread: retire and admit while requests are queued or on the device (polling their events every
+// 20 us, with the lock released), sleep on work_cv otherwise.  A CUDA failure is kept for the waiting calls and ends the loop.
+static void admission_loop(nk_server* S) {
+    cudaSetDevice(S->ctx->device);
+    std::unique_lock<std::mutex> lk(S->mu);
+    while (!S->stop) {
+        try {
+            progress(S);
+        } catch (const Failure& f) {
+            S->worker_status = f.status;
+            S->worker_error = f.message;
+            S->done_cv.notify_all();
+            break;
+        }
+        S->done_cv.notify_all();
+        if (S->in_flight > 0 || !S->queue.empty()) {   // requests to retire, or queued ones waiting for a slot
+            lk.unlock();
+            std::this_thread::sleep_for(std::chrono::microseconds(20));
+            lk.lock();
+        } else {
+            S->work_cv.wait(lk, [&] { return S->stop || !S->queue.empty(); });
+        }
+    }
+}
+
 }  // namespace nk
 
 extern "C" {
@@ -2085,12 +2123,25 @@ nk_status nk_server_create(nk_context* ctx, const nk_server_desc* desc, nk_serve
     }
     S->dev.init((size_t)desc->memory_cap_bytes);
     S->pin.init(pin_cap);
+    if (desc->flags & NK_SERVER_ADMISSION_THREAD) {
+        S->threaded = true;
+        S->worker = std::thread(admission_loop, S);
+    }
     *out = S;
     return NK_OK;
 }
 
 nk_status nk_server_destroy(nk_server* S) {
     if (!S) return NK_OK;
+    if (S->threaded) {
+        {
+            std::lock_guard<std::mutex> g(S->mu);
+            S->stop = true;
+        }
+        S->work_cv.notify_all();
+        S->worker.join();
+        S->threaded = false;
+    }
     if (const char* e = std::getenv("NK_SERVER_TRACE"))
         if (e[0] == '1')
             std::fprintf(stderr, "nk_server: %d problems created in %.3f s (graph capture %.3f s); host time starting requests %.3f s, "
@@ -2132,19 +2183,30 @@ nk_status nk_server_submit(nk_server* S, const nk_request* q, int64_t* ticket) {
         R->u_out = q->u_out;
         R->v_out = q->v_out;
         R->key = request_key(*R);
-        R->ticket = S->next_ticket++;
         R->t_submit = S->now();
+        auto lk = S->lock();
+        R->ticket = S->next_ticket++;
         *ticket = R->ticket;
         S->queue.push_back(R->ticket);
         S->requests[R->ticket] = std::move(R);
-        progress(S);
+        if (S->threaded) {
+            lk.unlock();
+            S->work_cv.notify_one();
+        } else {
+            progress(S);
+        }
     });
 }
 
 nk_status nk_server_progress(nk_server* S, int32_t* pending) {
     if (!S) return NK_BAD_ARGUMENT;
     return guarded(S->ctx, [&] {
-        progress(S);
+        auto lk = S->lock();
+        if (S->threaded) {
+            if (S->worker_status != NK_OK) throw Failure{S->worker_status, S->worker_error};
+        } else {
+            progress(S);
+        }
         if (pending) {
             int32_t n = 0;
             for (auto& kv : S->requests) n += kv.second->state != 2;
@@ -2155,9 +2217,15 @@ nk_status nk_server_progress(nk_server* S, int32_t* pending) {
 
 nk_status nk_server_wait(nk_server* S, int64_t ticket, nk_solve_stats* stats, double* t_submit, double* t_admit, double* t_done) {
     if (!S) return NK_BAD_ARGUMENT;
+    auto lk = S->lock();
     auto it = S->requests.find(ticket);
     if (it == S->requests.end()) return NK_BAD_ARGUMENT;
     nk_status st = guarded(S->ctx, [&] {
+        if (S->threaded) {
+            S->done_cv.wait(lk, [&] { return it->second->state == 2 || S->worker_status != NK_OK; });
+            if (it->second->state != 2) throw Failure{S->worker_status, S->worker_error};
+            return;
+        }
         while (it->second->state != 2) {
             progress(S);
             if (it->second->state != 2) std::this_thread::sleep_for(std::chrono::microseconds(20));
@@ -2175,11 +2243,20 @@ nk_status nk_server_wait(nk_server* S, int64_t ticket, nk_solve_stats* stats, do
 nk_status nk_server_wait_all(nk_server* S) {
     if (!S) return NK_BAD_ARGUMENT;
     return guarded(S->ctx, [&] {
+        auto lk = S->lock();
+        auto all_done = [&] {
+            for (auto& kv : S->requests)
+                if (kv.second->state != 2) return false;
+            return true;
+        };
+        if (S->threaded) {
+            S->done_cv.wait(lk, [&] { return all_done() || S->worker_status != NK_OK; });
+            if (!all_done()) throw Failure{S->worker_status, S->worker_error};
+            return;
+        }
         while (true) {
             progress(S);
-            bool all = true;
-            for (auto& kv : S->requests) all = all && kv.second->state == 2;
-            if (all) break;
+            if (all_done()) break;
             std::this_thread::sleep_for(std::chrono::microseconds(20));
         }
     });
@@ -2187,6 +2264,7 @@ nk_status nk_server_wait_all(nk_server* S) {
 
 nk_status nk_server_info(const nk_server* S, int32_t* resident, int64_t* device_bytes, int32_t* peak_in_flight) {
     if (!S) return NK_BAD_ARGUMENT;
+    auto lk = S->lock();
     if (resident) *resident = (int32_t)S->residents.size();
     if (device_bytes) *device_bytes = S->device_bytes;
     if (peak_in_flight) *peak_in_flight = S->peak;

@@ -18,11 +18,13 @@ def _ptr(a):
 
 
 class Server:
-    def __init__(self, max_in_flight=16, memory_cap_bytes=16 << 30, context=None):
+    def __init__(self, max_in_flight=16, memory_cap_bytes=16 << 30, context=None, admission_thread=False):
+        """`admission_thread`: the library's own host thread admits and retires requests (NK_SERVER_ADMISSION_THREAD);
+        otherwise submit / progress / wait drive the loop."""
         self.ctx = context or library.default_context()
         self.lib = library.load()
         self.h = C.c_void_p()
-        d = abi.ServerDesc(max_in_flight, 0, int(memory_cap_bytes))
+        d = abi.ServerDesc(max_in_flight, abi.NK_SERVER_ADMISSION_THREAD if admission_thread else 0, int(memory_cap_bytes))
         _check(self.lib.nk_server_create(self.ctx.handle, C.byref(d), C.byref(self.h)), "server_create", self.ctx.last_error())
         self._keep = {}
 

@@ -54,3 +54,37 @@ def test_memory_cap_admits_one_problem_at_a_time():
     for (u, v, st, _), (ur, vr, _) in zip(got, ref):
         assert np.array_equal(u, ur) and np.array_equal(v, vr)
     assert info["peak_in_flight"] == 1 and info["device_bytes"] <= one + 1
+
+
+def test_admission_thread_runs_requests_without_the_caller():
+    """NK_SERVER_ADMISSION_THREAD: requests are admitted and retired by the library's own thread while the caller
+    only sleeps and reads the pending count; the results are those of each request solved alone."""
+    import time
+    cases = requests()
+    ref = [alone(c) for c in cases]
+    S = Server(max_in_flight=3, admission_thread=True)
+    tickets = [S.submit(c) for c in cases]
+    t0 = time.time()
+    while S.progress() > 0:       # a query in this mode: the thread does the work
+        assert time.time() - t0 < 120, "requests did not finish"
+        time.sleep(0.01)
+    got = [S.wait(t) for t in tickets]
+    info = S.info()
+    S.close()
+    for (u, v, st, times), (ur, vr, sr) in zip(got, ref):
+        assert st.status == 0 and st.picard_iterations == sr.picard_iterations
+        assert np.array_equal(u, ur) and np.array_equal(v, vr)
+        assert times[0] <= times[1] <= times[2]
+    assert info["peak_in_flight"] > 1
+
+
+def test_admission_thread_wait_blocks_until_done():
+    cases = requests()[:2]
+    ref = [alone(c) for c in cases]
+    S = Server(max_in_flight=2, admission_thread=True)
+    tickets = [S.submit(c) for c in cases]
+    S.wait_all()
+    got = [S.wait(t) for t in tickets]
+    S.close()
+    for (u, v, st, _), (ur, vr, sr) in zip(got, ref):
+        assert np.array_equal(u, ur) and np.array_equal(v, vr)
