@@ -121,7 +121,7 @@ struct SolverScalars {
     int p_done, it_total, cg_unconverged;
     int r32_exp;                   // mixed precision: the FP32 residual in the V-cycle is r 2^-r32_exp, z = z32 2^r32_exp
     int r32_exp_next;              // exponent the next k_cg_update scales its residual with (from the latest ‖r‖)
-    int pad;
+    int zold_exp;                  // mixed precision: z_old = zold32 2^zold_exp (the exponent of the z32 it copies)
 };
 
 // Binary exponent that brings a residual of norm `norm` near 1 before it is rounded to FP32.  Scaling by a power of

@@ -64,6 +64,8 @@ struct CGView {
     unsigned long long cond;      // conditional-node handle of the conjugate-gradient while loop (0: none)
     float2* r32;                  // mixed precision: FP32 copy of r written for the V-cycle (or nullptr)
     const float2* z32;            // mixed precision: FP32 V-cycle result read back as z (or nullptr)
+    float2* zold32;               // mixed precision: z_old kept as the FP32 z32 it equals exactly (or nullptr);
+                                  // z itself is then never stored: each kernel that needs it rescales z32
 };
 // r = b - A x; if the preconditioner is not multigrid also z = M r, p = z, rho = r.z; r0, tol, done
 void launch_cg_init(const CGView& v, cudaStream_t s);

@@ -259,7 +259,7 @@ struct nk_problem {
         CGView v;
         v.o = fine_op();
         v.x = x; v.b = b; v.r = r; v.z = z; v.p = p; v.q = q;
-        v.zold = mixed && precond == NK_PRECONDITIONER_MULTIGRID ? zold : nullptr;
+        v.zold = nullptr;
         v.invd = invd;
         v.precond = precond;
         v.sc = sc;
@@ -268,6 +268,7 @@ struct nk_problem {
         bool fused = mixed && precond == NK_PRECONDITIONER_MULTIGRID;
         v.r32 = fused ? lv32[0].b : nullptr;
         v.z32 = fused ? lv32[0].x : nullptr;
+        v.zold32 = fused ? reinterpret_cast<float2*>(zold) : nullptr;   // flexible CG: z_old in FP32
         return v;
     }
 };

@@ -248,7 +248,7 @@ __global__ void k_cg_init_finish(CGView v) {
                 float2 f = v.z32[k];
                 int ze = v.sc->r32_exp;
                 z = make_double2(scale_pow2((double)f.x, ze), scale_pow2((double)f.y, ze));
-                v.z[k] = z;
+                if (v.zold32) v.zold32[k] = f;
             } else {
                 z = v.z[k];
             }
@@ -260,6 +260,7 @@ __global__ void k_cg_init_finish(CGView v) {
     double trz, dummy;
     if (grid_sum2(rz, 0.0, v.partials, &v.sc->ticket, trz, dummy) && threadIdx.x == 0 && threadIdx.y == 0) {
         v.sc->rho = trz;
+        v.sc->zold_exp = v.sc->r32_exp;   // the exponent of the z32 now in zold32
         if (v.cond) cudaGraphSetConditional(v.cond, v.sc->done ? 0u : 1u);
     }
 }
@@ -372,12 +373,16 @@ __global__ void k_cg_dots_after_precondition(CGView v) {
                 float2 f = v.z32[k];
                 int ze = v.sc->r32_exp;
                 z = make_double2(scale_pow2((double)f.x, ze), scale_pow2((double)f.y, ze));
-                v.z[k] = z;
             } else {
                 z = v.z[k];
             }
             rz += r.x * z.x + r.y * z.y;
-            if (v.zold) {
+            if (v.zold32) {
+                float2 fo = v.zold32[k];
+                int zo_e = v.sc->zold_exp;
+                double2 zo = make_double2(scale_pow2((double)fo.x, zo_e), scale_pow2((double)fo.y, zo_e));
+                rzo += r.x * zo.x + r.y * zo.y;
+            } else if (v.zold) {
                 double2 zo = v.zold[k];
                 rzo += r.x * zo.x + r.y * zo.y;
             }
@@ -403,12 +408,20 @@ __global__ void k_cg_xpby(CGView v) {
     if (read_done(v.sc)) return;
     int i = blockIdx.x * BX + threadIdx.x, j0 = blockIdx.y * BY * VEC_ROWS + threadIdx.y;
     double beta = v.sc->beta;
+    int ze = v.sc->r32_exp;
 #pragma unroll
     for (int row = 0; row < VEC_ROWS; ++row) {
         int j = j0 + row * BY;
         if (i < v.o.g.Nx && j < v.o.g.Ny) {
             int k = v.o.g.idx(i, j);
-            double2 z = v.z[k], p = v.p[k];
+            double2 z, p = v.p[k];
+            if (v.z32) {   // z = z32 2^e, as k_cg_dots_after_precondition formed it; z_old keeps z32 itself
+                float2 f = v.z32[k];
+                z = make_double2(scale_pow2((double)f.x, ze), scale_pow2((double)f.y, ze));
+                if (v.zold32) v.zold32[k] = f;
+            } else {
+                z = v.z[k];
+            }
             p.x = z.x + beta * p.x;
             p.y = z.y + beta * p.y;
             v.p[k] = p;
@@ -422,6 +435,7 @@ __global__ void k_cg_xpby(CGView v) {
         unsigned int t = atomicAdd(&v.sc->ticket2, 1u);
         if (t == n - 1) {
             v.sc->ticket2 = 0u;
+            v.sc->zold_exp = v.sc->r32_exp;   // the exponent of the z32 now in zold32
             int d = v.sc->done_next;
             v.sc->done = d;
             if (v.cond) cudaGraphSetConditional(v.cond, d ? 0u : 1u);
