@@ -185,6 +185,10 @@ struct LevelView {
     const typename Vec2<T>::type* irs;  // inverse ℓ1 row sums
     int cx, cy;                      // coarsening factor from the finer level (1 or 2)
 };
+// Mean device time in ms of `repeats` launches of one level's sweep (kind STRIP_SMOOTH, x -> x2) or residual
+// (STRIP_RESIDUAL, into q) with walks of `rows` rows; negative if a CUDA call failed (the strip autotuner)
+template <typename T>
+float time_strip_kernel(const LevelView<T>& L, int kind, int rows, int repeats, cudaStream_t s);
 // coarse coefficients from the finer level (multigrid_preconditioner.jl:331-344), then corners
 template <typename T, typename TF>
 void launch_coarsen(const LevelView<T>& coarse, const DevGrid<TF>& fine_g, const typename Vec4<TF>::type* fine_coef,

@@ -284,7 +284,7 @@ void launch_smooth_point(const LevelView<T>& L, const typename Vec2<T>::type* x_
         LaunchDims d = dims2d(L.o.g.Nx, L.o.g.Ny);
         k_smooth_first<T><<<d.grid, d.block, 0, s>>>(L, x_in, x_out, done); count_launch();
     } else {
-        int rows = strip_rows(L.o.g.Nx, L.o.g.Ny, (int)sizeof(T));
+        int rows = strip_rows(L.o.g.Nx, L.o.g.Ny, (int)sizeof(T), STRIP_SMOOTH);
         LaunchDims d = strip_dims(L.o.g.Nx, L.o.g.Ny, rows);
         with_strip_rows(rows, [&](auto r) { k_smooth_point<T, decltype(r)::value><<<d.grid, d.block, 0, s>>>(L, x_in, x_out, done); });
         count_launch();
@@ -326,7 +326,7 @@ __global__ void __launch_bounds__(32 * STRIP_WARPS) k_smooth_first2(LevelView<T>
 }
 template <typename T>
 void launch_smooth_first2(const LevelView<T>& L, typename Vec2<T>::type* x_out, const int* done, cudaStream_t s) {
-    int rows = strip_rows(L.o.g.Nx, L.o.g.Ny, (int)sizeof(T));
+    int rows = strip_rows(L.o.g.Nx, L.o.g.Ny, (int)sizeof(T), STRIP_SMOOTH);
     LaunchDims d = strip_dims(L.o.g.Nx, L.o.g.Ny, rows);
     with_strip_rows(rows, [&](auto r) { k_smooth_first2<T, decltype(r)::value><<<d.grid, d.block, 0, s>>>(L, x_out, done); });
     count_launch();
@@ -352,10 +352,34 @@ __global__ void __launch_bounds__(32 * STRIP_WARPS) k_level_apply(LevelView<T> L
 template <typename T>
 void launch_level_apply(const LevelView<T>& L, const typename Vec2<T>::type* x, typename Vec2<T>::type* q, int residual,
                         const int* done, cudaStream_t s) {
-    int rows = strip_rows(L.o.g.Nx, L.o.g.Ny, (int)sizeof(T));
+    int rows = strip_rows(L.o.g.Nx, L.o.g.Ny, (int)sizeof(T), STRIP_RESIDUAL);
     LaunchDims d = strip_dims(L.o.g.Nx, L.o.g.Ny, rows);
     with_strip_rows(rows, [&](auto r) { k_level_apply<T, decltype(r)::value><<<d.grid, d.block, 0, s>>>(L, x, q, residual, done); });
     count_launch();
+}
+
+template <typename T>
+float time_strip_kernel(const LevelView<T>& L, int kind, int rows, int repeats, cudaStream_t s) {
+    LaunchDims d = strip_dims(L.o.g.Nx, L.o.g.Ny, rows);
+    auto once = [&] {
+        with_strip_rows(rows, [&](auto r) {
+            if (kind == STRIP_SMOOTH) k_smooth_point<T, decltype(r)::value><<<d.grid, d.block, 0, s>>>(L, L.x, L.x2, nullptr);
+            else k_level_apply<T, decltype(r)::value><<<d.grid, d.block, 0, s>>>(L, L.x, L.q, 1, nullptr);
+        });
+        count_launch();
+    };
+    once();   // warm-up
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    float ms = -1.f;
+    if (cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess && cudaEventRecord(e0, s) == cudaSuccess) {
+        for (int k = 0; k < repeats; ++k) once();
+        if (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess || cudaGetLastError() != cudaSuccess)
+            ms = -1.f;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    return ms < 0.f ? ms : ms / repeats;
 }
 
 template <typename T>
@@ -783,7 +807,8 @@ void launch_coarse_vcycle(const CoarseLevels<T>& C, const int* done, cudaStream_
     template void launch_prolongate<T>(const LevelView<T>&, const LevelView<T>&, Vec2<T>::type*, const Vec2<T>::type*, const int*, \
                                        cudaStream_t);                                                                               \
     template void launch_zero_vec<T>(const DevGrid<T>&, Vec2<T>::type*, const int*, cudaStream_t);                                 \
-    template void launch_coarse_vcycle<T>(const CoarseLevels<T>&, const int*, cudaStream_t);
+    template void launch_coarse_vcycle<T>(const CoarseLevels<T>&, const int*, cudaStream_t);                     \
+    template float time_strip_kernel<T>(const LevelView<T>&, int, int, int, cudaStream_t);
 
 NK_INSTANTIATE(double)
 NK_INSTANTIATE(float)

@@ -14,8 +14,11 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "nk_kernels.cuh"
@@ -42,14 +45,34 @@ static void bad(const std::string& m) { throw Failure{NK_BAD_ARGUMENT, m}; }
 // (56 registers: the memory-bound sweeps want occupancy; the 2048x1024 sweep takes 36.9 us against 41.6 us at 4
 // rows, and the serving stream is unchanged) and, for FP64, 4 from 2^18 cells (the FP64 kernels are bound by
 // the FP64 pipe; the two extra rows of each walk are a smaller share at 4).
-int strip_rows(int nx, int ny, int elem_bytes) {
+// Walk lengths measured by the strip autotuner, per (kernel kind, Nx, Ny, element bytes), shared by every
+// problem of the process.
+static std::mutex& tuned_mutex() {
+    static std::mutex m;
+    return m;
+}
+static std::map<std::tuple<int, int, int, int>, int>& tuned_rows() {
+    static std::map<std::tuple<int, int, int, int>, int> t;
+    return t;
+}
+
+int strip_rows(int nx, int ny, int elem_bytes, int kind) {
     static const int forced = [] {
         const char* e = std::getenv("NK_STRIP_ROWS");
         int r = e ? std::atoi(e) : 0;
         return (r == 1 || r == 2 || r == 4 || r == 8) ? r : 0;
     }();
     if (forced) return elem_bytes == 8 ? std::min(forced, 4) : forced;
+    if (kind != STRIP_OPERATOR) {
+        std::lock_guard<std::mutex> g(tuned_mutex());
+        auto it = tuned_rows().find(std::make_tuple(kind, nx, ny, elem_bytes));
+        if (it != tuned_rows().end()) return it->second;
+    }
     long long cells = (long long)nx * ny;
+    // FP64 multigrid sweeps and residuals: what the autotuner measured for one solve at a time on GB300 (one row
+    // below 2^16 cells, two above; 1.48 -> 1.68 solves/s on the FP64 stream); FP32 and the FP64 operator kernels
+    // keep two rows (four from 2^18 cells for the operator), which the concurrent mixed stream prefers
+    if (elem_bytes == 8 && kind != STRIP_OPERATOR) return cells < (1 << 16) ? 1 : 2;
     if (elem_bytes == 8) return cells >= (1 << 18) ? 4 : 2;
     return 2;
 }
@@ -187,6 +210,7 @@ struct nk_problem {
     long long picard_kernels[3] = {0, 0, 0};   // kernel nodes: top level, Picard body, CG body
     long long linear_kernels[2] = {0, 0};      // kernel nodes: top level, CG body
     bool async_pending = false;                // nk_picard_solve_async issued, nk_problem_wait not yet called
+    bool strips_tuned = false;                 // the strip autotuner has seen this problem's levels
     double instantiate_s = 0;                  // host seconds of the last graph instantiation
     // Picard adjoint scratch, allocated by the first nk_picard_adjoint: ∂J/∂x (pairs), the strain-rate adjoint
     // per centre and the log C gradient per cell
@@ -767,6 +791,64 @@ static cudaGraph_t add_while(cudaGraph_t g, const std::vector<cudaGraphNode_t>& 
 // update_stress_balance_coefficients! / update_diva_coefficients!
 static void update_coefficients(nk_problem* P);
 
+// The strip autotuner: for every multigrid level whose shape the process has not timed yet, times the sweep and
+// the residual with walks of 1, 2 and 4 rows (a warm-up and 5 launches each, on this problem's own scratch
+// buffers, before any graph is captured) and records the fastest.  Those kernels write one value per cell with
+// no reduction; the walk length still changes how the compiler contracts their multiply-adds, so a tuned walk
+// moves results in the last bits, and a timing-dependent choice would make them depend on the run.  Tuning is
+// therefore opt-in (NK_AUTOTUNE=1; NK_AUTOTUNE_REPORT=1 prints the choices) and the fixed rule of strip_rows
+// carries what it found.
+static bool autotune_enabled() {
+    static const bool on = [] {
+        const char* e = std::getenv("NK_AUTOTUNE");
+        return e && e[0] == '1';
+    }();
+    return on;
+}
+static bool autotune_report() {
+    static const bool on = [] {
+        const char* e = std::getenv("NK_AUTOTUNE_REPORT");
+        return e && e[0] == '1';
+    }();
+    return on;
+}
+template <typename T>
+static void autotune_levels(nk_problem* P, std::vector<Level<T>>& lv) {
+    for (int l = 0; l <= P->nlevels; ++l) {
+        LevelView<T> v = P->level_view(lv[l]);
+        if (!v.x || !v.x2 || !v.q) continue;
+        for (int kind : {STRIP_SMOOTH, STRIP_RESIDUAL}) {
+            auto key = std::make_tuple(kind, v.o.g.Nx, v.o.g.Ny, (int)sizeof(T));
+            {
+                std::lock_guard<std::mutex> g(tuned_mutex());
+                if (tuned_rows().count(key)) continue;
+            }
+            int best = 0;
+            float best_ms = 0.f;
+            for (int rows : {1, 2, 4}) {
+                float ms = time_strip_kernel<T>(v, kind, rows, 5, P->stream);
+                if (ms < 0.f) throw Failure{NK_CUDA_ERROR, "strip autotuner: a timing launch failed"};
+                if (!best || ms < best_ms) { best = rows; best_ms = ms; }
+            }
+            std::lock_guard<std::mutex> g(tuned_mutex());
+            tuned_rows().emplace(key, best);
+            if (autotune_report())
+                std::fprintf(stderr, "nk autotune: %s %dx%d fp%d -> %d rows (%.2f us)\n", kind == STRIP_SMOOTH ? "sweep" : "residual",
+                             v.o.g.Nx, v.o.g.Ny, 8 * (int)sizeof(T), best, 1e3 * best_ms);
+        }
+    }
+}
+// FP64 hierarchies only.  Timed alone, the FP32 sweeps prefer shorter walks on the coarse levels, but with 32
+// solves sharing the GPU those choices lowered the mixed serving stream from 11.26 to 10.83 solves/s: there the
+// SM time of a launch counts, not its latency, so FP32 keeps the fixed two-row walk.  The FP64 solver runs one
+// solve at a time, and the tuned walks raised it from 1.48 to 1.68 solves/s on the same box.
+static void autotune_strips(nk_problem* P) {
+    if (P->strips_tuned) return;
+    P->strips_tuned = true;
+    if (!autotune_enabled() || P->precond != NK_PRECONDITIONER_MULTIGRID || P->mixed) return;
+    autotune_levels<double>(P, P->lv64);
+}
+
 // Picard's change measure and stopping test: the reference's velocity change, or the viscosity change of
 // NK_VISCOSITY_CONVERGENCE, whose previous η̄H lives in tmp_a (free during a Picard solve).
 static void picard_end(nk_problem* P, cudaGraphConditionalHandle h) {
@@ -777,6 +859,7 @@ static void picard_end(nk_problem* P, cudaGraphConditionalHandle h) {
 }
 
 static void build_picard_graph(nk_problem* P) {
+    autotune_strips(P);
     cudaGraph_t g;
     NK_CUDA(cudaGraphCreate(&g, 0));
     cudaGraphConditionalHandle hp;
@@ -805,6 +888,7 @@ static void build_picard_graph(nk_problem* P) {
 }
 
 static void build_linear_graph(nk_problem* P) {
+    autotune_strips(P);
     cudaGraph_t g;
     NK_CUDA(cudaGraphCreate(&g, 0));
     cudaGraphConditionalHandle hc;
@@ -840,6 +924,7 @@ static void fill_stats(nk_problem* P, nk_solve_stats* st, bool picard) { fill_st
 // The same solve issued from the host (NK_GRAPHS=0): CG steps in growing batches, the device `done` flag read
 // after each batch; Picard reads its stopping decision after every iteration.
 static void host_cg(nk_problem* P, const double2* b) {
+    autotune_strips(P);
     CGView v = P->cg_view(b);
     cg_start(P, v);
     const nk_iteration_control& ctl = P->sd.linear;

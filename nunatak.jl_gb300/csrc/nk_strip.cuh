@@ -32,7 +32,11 @@ inline LaunchDims strip_dims(int nx, int ny, int rows) {
 
 // Rows per warp for an nx x ny grid of `elem_bytes`-byte values (host side; nk_problem.cu).  Long walks
 // amortise the two priming rows on large grids; short ones keep enough warps in flight on small grids.
-int strip_rows(int nx, int ny, int elem_bytes);
+// `kind` names the kernel: the multigrid sweeps and residuals write one value per cell with no reduction, so
+// their walk length cannot change a bit of the result and is taken from the autotuner's table when it has an
+// entry (nk_problem.cu); the FP64 operator kernels carry block reductions and keep the fixed rule.
+enum StripKernel { STRIP_OPERATOR = 0, STRIP_SMOOTH = 1, STRIP_RESIDUAL = 2 };
+int strip_rows(int nx, int ny, int elem_bytes, int kind = STRIP_OPERATOR);
 constexpr int STRIP_MIN_ROWS = 1;
 
 // Calls f(std::integral_constant<int, R>) for the supported walk lengths R.
