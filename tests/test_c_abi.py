@@ -52,3 +52,53 @@ def test_c_client_solve_equals_python_solve(tmp_path, gpu_cls):
     u = np.frombuffer((tmp_path / "u.bin").read_bytes(), dtype=np.float64).reshape(P.shape("u"))
     v = np.frombuffer((tmp_path / "v.bin").read_bytes(), dtype=np.float64).reshape(P.shape("v"))
     assert np.array_equal(u, P.get("u")) and np.array_equal(v, P.get("v"))
+
+
+LAYOUT_PROGRAM = r"""
+#include <stddef.h>
+#include <stdio.h>
+#include "nunatak_gb300.h"
+#define F(T, m) printf("%s.%s %zu %zu\n", #T, #m, offsetof(T, m), sizeof(((T*)0)->m));
+#define S(T) printf("%s %zu\n", #T, sizeof(T));
+int main(void) {
+    S(nk_iteration_control) F(nk_iteration_control, kind) F(nk_iteration_control, reltol) F(nk_iteration_control, abstol)
+    S(nk_grid_desc) F(nk_grid_desc, Nsigma) F(nk_grid_desc, x_faces) F(nk_grid_desc, x0) F(nk_grid_desc, sigma_faces)
+    F(nk_grid_desc, bed_refinement)
+    S(nk_physics_desc) F(nk_physics_desc, glen_exponent) F(nk_physics_desc, use_ice_mask) F(nk_physics_desc, mask_transition_thickness)
+    S(nk_solver_desc) F(nk_solver_desc, linear) F(nk_solver_desc, picard)
+    S(nk_solve_stats) F(nk_solve_stats, residual_norm) F(nk_solve_stats, device_end_ms)
+    S(nk_server_desc) F(nk_server_desc, flags) F(nk_server_desc, memory_cap_bytes)
+    S(nk_request) F(nk_request, physics) F(nk_request, solver) F(nk_request, H) F(nk_request, v_out)
+    return 0;
+}
+"""
+
+
+def test_ctypes_mirrors_match_the_c_layout(tmp_path):
+    """Sizes and field offsets of every descriptor, as the C compiler lays them out, against the ctypes mirrors."""
+    import ctypes
+    from nunatak_gb300 import abi
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "layout.c"
+    src.write_text(LAYOUT_PROGRAM)
+    exe = str(tmp_path / "layout")
+    r = subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
+    mirrors = {"nk_iteration_control": abi.IterationControl, "nk_grid_desc": abi.GridDesc, "nk_physics_desc": abi.PhysicsDesc,
+               "nk_solver_desc": abi.SolverDesc, "nk_solve_stats": abi.SolveStats, "nk_server_desc": abi.ServerDesc,
+               "nk_request": abi.Request}
+    checked = 0
+    for line in filter(None, out):
+        parts = line.split()
+        if "." in parts[0]:
+            struct, field = parts[0].split(".")
+            off, size = int(parts[1]), int(parts[2])
+            m = getattr(mirrors[struct], field)
+            assert (m.offset, m.size) == (off, size), (struct, field, m.offset, m.size, off, size)
+        else:
+            assert ctypes.sizeof(mirrors[parts[0]]) == int(parts[1]), parts
+        checked += 1
+    assert checked == 28
