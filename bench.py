@@ -504,6 +504,21 @@ def run_diva(nk, workloads, ctx):
         "coulomb_transition_speed_m_per_yr": transition}), flush=True)
 
 
+# Algorithmic bytes per cell of the solve's repeated work (each array a kernel touches, once, at its precision):
+# the FP64 flexible CG iteration (operator 65 B, update 104 B, dots after the V-cycle 32 B, xpby 48 B), the FP32
+# V-cycle (about 62 four-byte words per fine cell, times 4/3 for the coarse levels) and the SSA coefficient update
+# of each Picard iteration (15 eight-byte words).
+CG_BYTES_PER_CELL = 65 + 104 + 32 + 48
+VCYCLE_BYTES_PER_CELL = int(round(62 * 4 / 3 * 4))
+COEF_BYTES_PER_CELL = 15 * 8
+
+
+def stream_algorithmic_bytes(cells, picard_iterations, cg_iterations):
+    """Σ over requests of cells × (Picard iterations × coefficient bytes + CG iterations × (CG + V-cycle bytes))."""
+    return float(sum(n * (p * COEF_BYTES_PER_CELL + c * (CG_BYTES_PER_CELL + VCYCLE_BYTES_PER_CELL))
+                     for n, p, c in zip(cells, picard_iterations, cg_iterations)))
+
+
 def main():
     args = parse()
     rank, world, local_rank = dist_env()
@@ -608,15 +623,6 @@ def main():
     d2h = sum(8 * (c.grid.Ny * c.grid.face_count(0) + c.grid.face_count(1) * c.grid.Nx) for c in cases) / args.steps
     e2e_err = max(abs(a.picard_iterations - b.picard_iterations) for a, b in zip(stats, e2e_stats))
 
-    # ---- roofline of the dominant kernel on a grid larger than L2 ---------------------------------------
-    peak, peak_kind = measured_peaks()
-    Pb = roofline_problem(nk, workloads, ctx)
-    Pb.time_kernel("smoother", repeats=3, flush_bytes=0)
-    sm_ms, sm_bytes = Pb.time_kernel("smoother", repeats=20, flush_bytes=512 << 20)
-    op_ms, op_bytes = Pb.time_kernel("operator_fp64", repeats=20, flush_bytes=512 << 20)
-    achieved = sm_bytes / (sm_ms * 1e-3) / 1e9
-    del Pb
-
     piters = [x.picard_iterations for x in stats]
     citers = [x.linear_iterations_total for x in stats]
     line = {
@@ -666,6 +672,15 @@ def main():
                           "achieved_gbs": op_bytes / (op_ms * 1e-3) / 1e9, "bound": "fp64 pipe",
                           "fp64_ginstr_per_s": fp64_rate, "fp64_peak_ginstr_per_s": fp64_peak, "frac": fp64_rate / fp64_peak,
                           "traffic": profile_traffic("operator_fp64_2048x1024.md")}}
+    # ---- the stream as a whole: algorithmic bytes of every request's iterations over the device span ------------
+    stream_bytes = stream_algorithmic_bytes([c.grid.Nx * c.grid.Ny for c in cases], piters, citers)
+    stream_gbs = stream_bytes / (span_ms * 1e-3) / 1e9 * world
+    line["roofline_stream"] = {
+        "achieved": stream_gbs, "peak": peak, "unit": "GB/s", "frac": stream_gbs / (peak * world), "peak_source": peak_kind,
+        "bytes": stream_bytes,
+        "model": "per request and cell: Picard iterations x %d B (SSA coefficient update, 15 words FP64) + CG iterations x "
+                 "(%d B FP64 flexible CG iteration + %d B FP32 V-cycle, 62 words x 4/3 levels)"
+                 % (COEF_BYTES_PER_CELL, CG_BYTES_PER_CELL, VCYCLE_BYTES_PER_CELL)}
     if not args.no_cpu_baseline:
         from nunatak_gb300 import workloads as W
         reqs = cpu_sample_requests(2)
