@@ -183,3 +183,42 @@ def test_sigma_grid_column_integrals(backend):
     e = eta[0, 0, 0]
     np.testing.assert_allclose(P.get("eta_H"), e * H, rtol=1e-14)
     np.testing.assert_allclose(P.get("F2"), H / (3 * e), rtol=1e-14)
+
+
+# ---- the model-level velocity update (test/test_model.jl) ------------------------------------------------------
+
+def test_model_diva_update(backend):
+    """test/test_model.jl:87-111.  Without basal drag DIVA reduces to the SSA: the n = 3 ice stream to 1e-3, uᵇ = ū
+    and every layer of uσ equal to ū.  With Weertman drag (C = 1e12, m = 1) on a sloped sheet DIVA flows more than
+    twice as fast as the SSA, |uᵇ| ≤ |ū|, and the layer velocities average to ū within 1e-2."""
+    from support import ice_sheet_model
+    L, Nx, H0, delta, rho, A = 100e3, 64, 500.0, 20.0, 917.0, 1e-24
+    g = grid((Nx, 4), x=(0.0, L), y=(0.0, L / Nx * 4))
+    solver = M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-12, maxiter=10_000),
+                                   picard_iteration_control=M.Convergence(reltol=1e-10, maxiter=300))
+    c = M.IceSheetConstants(ice_density=rho)
+    P, st = ice_sheet_model(backend, g, H=H0, bed=lambda x, y: delta * math.cos(math.pi * x / L),
+                            rheology=M.GlenFlowLaw(rate_factor=A), stress_balance=M.DepthIntegrated(shear=M.DIVAShear()),
+                            constants=c, velocity_solver=solver, Nsigma=4)
+    U = A * (rho * c.gravitational_acceleration * delta / 2) ** 3 * L / math.pi
+    xf = g.faces(0)
+    ue = np.broadcast_to(U * (np.sin(np.pi * xf / L) - np.sin(np.pi * xf / L) ** 3 / 3), (4, Nx + 1))
+    u = P.get("u")
+    assert np.max(np.abs(u - ue)) / (2 * U / 3) < 1e-3
+    assert np.array_equal(P.get("u_b"), u)
+    us = P.get("u_sigma")
+    for k in range(us.shape[0]):
+        np.testing.assert_allclose(us[k], u, rtol=1.5e-8, atol=0)
+
+    g2 = grid((32, 4), x=(0.0, 1e5), y=(0.0, 1.25e4))
+    fr = M.WeertmanFriction(coefficient=1e12, exponent=1.0)
+    rh = M.GlenFlowLaw(rate_factor=1e-24)
+    ssa, _ = ice_sheet_model(backend, g2, H=lambda x, y: 1000 + x / 1e2, rheology=rh, friction=fr)
+    diva, st = ice_sheet_model(backend, g2, H=lambda x, y: 1000 + x / 1e2, rheology=rh, friction=fr,
+                               stress_balance=M.DepthIntegrated(shear=M.DIVAShear()))
+    ubar, ub, us = diva.get("u"), diva.get("u_b"), diva.get("u_sigma")
+    dz = np.diff(sigma_nodes(us.shape[0])[0]).reshape(-1, 1, 1)
+    assert 0 < st.picard_iterations < 100
+    assert np.max(np.abs(ubar)) > 2 * np.max(np.abs(ssa.get("u")))
+    assert np.all(np.abs(ub) <= np.abs(ubar))
+    assert np.max(np.abs(np.sum(us * dz, axis=0) - ubar)) < 1e-2 * np.max(np.abs(ubar))
