@@ -222,3 +222,30 @@ def test_model_diva_update(backend):
     assert np.max(np.abs(ubar)) > 2 * np.max(np.abs(ssa.get("u")))
     assert np.all(np.abs(ub) <= np.abs(ubar))
     assert np.max(np.abs(np.sum(us * dz, axis=0) - ubar)) < 1e-2 * np.max(np.abs(ubar))
+
+
+def test_model_stress_balance_update(backend):
+    """test/test_model.jl:62-85 (the parts about the velocity update and the geometry it reads; the ice stream
+    itself is test_ice_stream_n3).  s = bed + H and φ = 1 without a grounding treatment; the SSA's uᵇ and every
+    layer of uσ equal ū; a floating sheet (bed -2000 m, H = 100 m, SubgridGroundedFraction) has
+    s = (1 - ρᵢ/ρw) H, φ = 0 and N = 0."""
+    from support import ice_sheet_model
+    L = 100e3
+    g = grid((32, 4), x=(0.0, L), y=(0.0, L / 8))
+    solver = M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-12, maxiter=10_000),
+                                   picard_iteration_control=M.Convergence(reltol=1e-10, maxiter=300))
+    P, st = ice_sheet_model(backend, g, H=500.0, bed=lambda x, y: 20 * math.cos(math.pi * x / L),
+                            rheology=M.GlenFlowLaw(rate_factor=1e-24), constants=M.IceSheetConstants(ice_density=917.0),
+                            velocity_solver=solver, Nsigma=4)
+    assert 0 < st.picard_iterations < 300
+    np.testing.assert_allclose(P.get("s"), P.get("bed") + P.get("H"), rtol=1e-15)
+    assert np.all(P.get("phi") == 1) and np.all(P.get("phi_u") == 1)
+    u = P.get("u")
+    assert np.array_equal(P.get("u_b"), u)
+    assert all(np.array_equal(layer, u) for layer in P.get("u_sigma"))
+
+    box = grid((4, 4), x=(0.0, 1e4), y=(0.0, 1e4))
+    F, _ = ice_sheet_model(backend, box, H=100.0, bed=-2000.0, grounding=M.SubgridGroundedFraction(), solve=False)
+    c = M.IceSheetConstants()
+    np.testing.assert_allclose(F.get("s"), (1 - c.ice_density / c.ocean_density) * 100, rtol=1e-14)
+    assert np.all(F.get("phi") == 0) and np.all(F.get("N") == 0)
