@@ -1,5 +1,6 @@
-"""More of the reference's own known answers, restated from test/test_rate_factor.jl and test/test_sigma_grid.jl
-(file:line given per test).  Each runs on both backends: the FP64 CPU oracle and the GPU library (marked gpu)."""
+"""More of the reference's own known answers, restated from test/test_rate_factor.jl, test/test_sigma_grid.jl and
+test/test_model.jl (file:line given per test).  Each runs on both backends: the FP64 CPU oracle and the GPU library
+(marked gpu)."""
 import math
 
 import numpy as np
@@ -12,7 +13,7 @@ def grid(size, x=(0.0, 1.0), y=(0.0, 1.0), topology=("Bounded", "Bounded"), halo
     return M.RectilinearGrid(size=size, x=x, y=y, topology=topology, halo=halo)
 
 
-# Paterson-Budd branches of the Arrhenius law with the reference's constants (test/test_rate_factor.jl:6-8).
+# Paterson-Budd branches of the Arrhenius law with the reference's constants (test/test_rate_factor.jl:7-8).
 def cold_branch(t):
     return 3.61e-13 * math.exp(-6.0e4 / (8.31441 * t))
 
@@ -40,7 +41,7 @@ def rate_factor_at(cls, temperatures, H=0.0, Nsigma=1, clausius_clapeyron=0.0, i
 
 
 def test_arrhenius_values(backend):
-    """test/test_rate_factor.jl:67-74: A(T', ω = 0) equals the cold branch below 263.15 K and the warm one above,
+    """test/test_rate_factor.jl:70-79: A(T', ω = 0) equals the cold branch below 263.15 K and the warm one above,
     to 1e-13 (zero pressure, so T' = T)."""
     cold, warm = (223.15, 243.15, 262.6), (263.7, 268.15, 273.15)
     A = rate_factor_at(backend, cold + warm)[0, 0]
@@ -51,7 +52,7 @@ def test_arrhenius_values(backend):
 
 
 def test_arrhenius_smooth_transition(backend):
-    """test/test_rate_factor.jl:80-88: across 262-264 K A rises monotonically, log A has no kink, and at the
+    """test/test_rate_factor.jl:81-89: across 262-264 K A rises monotonically, log A has no kink, and at the
     transition temperature A is the geometric mean of the two branches."""
     t = np.linspace(262.0, 264.0, 2001)
     A = rate_factor_at(backend, t)[0, 0]
@@ -64,7 +65,7 @@ def test_arrhenius_smooth_transition(backend):
 
 
 def test_rate_factor_with_pressure_melting(backend):
-    """test/test_rate_factor.jl:153-160: with the Clausius-Clapeyron slope β, T' = T + β ρ g H (1 - ζ), and A is
+    """test/test_rate_factor.jl:166-174: with the Clausius-Clapeyron slope β, T' = T + β ρ g H (1 - ζ), and A is
     the cold branch there (ρ = 910, H = 1000 m, T = 253.15 K), to 1e-12."""
     Nsigma, beta, rho, H = 10, 7.9e-8, 910.0, 1000.0
     A = rate_factor_at(backend, [253.15] * 4, H=H, Nsigma=Nsigma, clausius_clapeyron=beta, ice_density=rho)
@@ -92,7 +93,7 @@ def _viscosity_problem(cls, Nsigma, rate_factor, diva=False):
 
 
 def test_uniform_sigma_rate_factor_equals_the_2d_one(backend):
-    """test/test_rate_factor.jl:90-111: a σ-grid A of uniform value gives the same layer viscosities, bit for bit,
+    """test/test_rate_factor.jl:91-115: a σ-grid A of uniform value gives the same layer viscosities, bit for bit,
     as the 2-D A of that value, for the SSA and the DIVA viscosity."""
     Nsigma = 4
     for diva in (False, True):
@@ -107,7 +108,7 @@ def test_uniform_sigma_rate_factor_equals_the_2d_one(backend):
 
 
 def test_depth_varying_rate_factor_reaches_the_column_integrals(backend):
-    """test/test_rate_factor.jl:113-138: with A(ζ) = A₀ (1 + 7ζ) the layer viscosities scale as (1 + 7ζ)^(-1/3),
+    """test/test_rate_factor.jl:117-145: with A(ζ) = A₀ (1 + 7ζ) the layer viscosities scale as (1 + 7ζ)^(-1/3),
     η̄H = H η₀ Σ Δζ (1 + 7ζ)^(-1/3) and F₂ = H Σ wₖ (1 + 7ζ)^(1/3) / η₀ with wₖ the exact layer integrals of
     (1 - ζ)², all to 1e-13."""
     Nsigma, A0 = 8, 1e-24
@@ -131,7 +132,7 @@ def test_depth_varying_rate_factor_reaches_the_column_integrals(backend):
 
 
 def depth_varying_slab_error(cls, Nsigma, H0=1000.0, tau0=1e4, A0=1e-21, C=1e10):
-    """depth_varying_slab_error, test/test_rate_factor.jl:10-50: the DIVA slab with A(ζ) = A₀ (1 + 3 (1 - ζ)),
+    """depth_varying_slab_error, test/test_rate_factor.jl:11-50: the DIVA slab with A(ζ) = A₀ (1 + 3 (1 - ζ)),
     whose exact profile is u = uᵇ + U (17/20 - s⁴/4 - 3 s⁵/5), s = 1 - ζ, U = 2 A₀ τ₀³ H₀, uᵇ = τ₀ / C."""
     g = grid((4, 4), x=(0.0, 4e3), y=(0.0, 4e3), topology=("Periodic", "Periodic"))
     solver = M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-12, maxiter=100),
@@ -158,7 +159,7 @@ def depth_varying_slab_error(cls, Nsigma, H0=1000.0, tau0=1e4, A0=1e-21, C=1e10)
 
 
 def test_diva_shear_follows_a_depth_varying_rate_factor(backend):
-    """test/test_rate_factor.jl:140-147."""
+    """test/test_rate_factor.jl:147-155."""
     coarse, fine = depth_varying_slab_error(backend, 10), depth_varying_slab_error(backend, 40)
     assert 0 < fine["iterations"] < 300
     assert fine["profile"] < 1e-2
