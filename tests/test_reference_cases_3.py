@@ -250,3 +250,46 @@ def test_model_stress_balance_update(backend):
     c = M.IceSheetConstants()
     np.testing.assert_allclose(F.get("s"), (1 - c.ice_density / c.ocean_density) * 100, rtol=1e-14)
     assert np.all(F.get("phi") == 0) and np.all(F.get("N") == 0)
+
+
+def _rate_factor_model(cls, stress_balance, T=None, A=None):
+    """rate_factor_model + set!(model; H = 1000 + x / 100, T), test/test_rate_factor.jl:52-62 and :64: 16 x 4 cells
+    over 160 km x 40 km, Weertman drag (C = 1e10, m = 1), ρᵢ = 910, CG 1e-12 inside Picard 1e-11, and A either from
+    the temperature (Arrhenius, Clausius-Clapeyron slope 0 as in rate_factor_model) or prescribed."""
+    g = grid((16, 4), x=(0.0, 1.6e5), y=(0.0, 4e4))
+    solver = M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-12, maxiter=10_000),
+                                   picard_iteration_control=M.Convergence(reltol=1e-11, maxiter=500))
+    sigma = A is None
+    P = make(cls, g, stress_balance=stress_balance, friction=M.WeertmanFriction(coefficient=1e10, exponent=1.0),
+             rheology=M.GlenFlowLaw(rate_factor="sigma" if sigma else A, strain_rate_regularization=1e-16),
+             constants=M.IceSheetConstants(ice_density=910.0), velocity_solver=solver)
+    P.set("H", np.broadcast_to(1000 + g.centers(0) / 1e2, (4, 16)))
+    P.set("bed", 0.0)
+    P.set("C", 1e10)
+    if sigma:
+        _, zeta = sigma_nodes(P.shape("A")[0])
+        t = np.array([T(z) for z in zeta]) if callable(T) else np.full(zeta.shape, float(T))
+        P.set("T", np.broadcast_to(t.reshape(-1, 1, 1), P.shape("T")))
+        P.compute_rate_factor(clausius_clapeyron=0.0)
+    else:
+        P.set("A", A)
+    P.compute_geometry()
+    st = P.picard_solve()
+    assert st.status == 0
+    return P.get("u")
+
+
+def test_stress_balance_feels_the_temperature(backend):
+    """test/test_rate_factor.jl:186-206: the Arrhenius A of a uniform 253.15 K gives the velocities of the
+    prescribed cold-branch A to 1e-9, a warmer 268.15 K flows faster (SSA and DIVA), and in DIVA a warm base
+    (268.15 - 30ζ) flows faster than a warm surface (238.15 + 30ζ)."""
+    for sb in (M.DepthIntegrated(), M.DepthIntegrated(shear=M.DIVAShear())):
+        arrhenius = _rate_factor_model(backend, sb, T=253.15)
+        prescribed = _rate_factor_model(backend, sb, A=cold_branch(253.15))
+        assert np.linalg.norm(arrhenius - prescribed) <= 1e-9 * max(np.linalg.norm(arrhenius), np.linalg.norm(prescribed))
+        warm = _rate_factor_model(backend, sb, T=268.15)
+        assert np.max(np.abs(warm)) > np.max(np.abs(arrhenius))
+    diva = M.DepthIntegrated(shear=M.DIVAShear())
+    base = _rate_factor_model(backend, diva, T=lambda z: 268.15 - 30 * z)
+    surface = _rate_factor_model(backend, diva, T=lambda z: 238.15 + 30 * z)
+    assert np.max(np.abs(base)) > np.max(np.abs(surface))
