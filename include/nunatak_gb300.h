@@ -9,10 +9,10 @@
  *     -> picard_solve!(x, picard, linear_solver, update_coefficients!, b, coefficients...)
  *       src/Solvers/picard.jl:63-90
  *       -> update_stress_balance_coefficients!   src/StressBalances/stress_balance_coefficients.jl:10-20
- *          update_diva_coefficients!             src/StressBalances/diva.jl:221-235
- *       -> solve!(x, solver, b, args...)         src/Solvers/conjugate_gradient.jl:269-364
+ *          update_diva_coefficients!             src/StressBalances/diva.jl:61-75
+ *       -> solve!(x, solver, b, args...)         src/Solvers/conjugate_gradient.jl:128-223
  *          -> ssa_operator!                      src/StressBalances/ssa_operator.jl:47-89
- *          -> precondition!                      src/StressBalances/diagonal_preconditioner.jl:132-175
+ *          -> precondition!                      src/StressBalances/diagonal_preconditioner.jl:11-54
  *                                                src/StressBalances/multigrid_preconditioner.jl:122-360
  *
  * Plain C types only: no CUDA, C++ or torch types cross this boundary.  Every function returns an
@@ -40,7 +40,7 @@ extern "C" {
 #define NK_API_VERSION 1
 
 /* Status codes.  The reference signals these through return values, @warn and ArgumentError
- * (src/Solvers/conjugate_gradient.jl:326-341 stops silently at maxiter, src/Solvers/picard.jl:79-89 likewise,
+ * (src/Solvers/conjugate_gradient.jl:185-200 stops silently at maxiter, src/Solvers/picard.jl:79-89 likewise,
  *  src/StressBalances/ssa_operator.jl:56 throws ArgumentError). */
 typedef int32_t nk_status;
 #define NK_OK               0
@@ -57,11 +57,11 @@ typedef int32_t nk_status;
 #define NK_BOUNDED   0
 #define NK_PERIODIC  1
 
-/* Tangential wall condition, src/StressBalances/depth_integrated.jl:204-220. */
+/* Tangential wall condition, src/StressBalances/depth_integrated.jl:31-45. */
 #define NK_FREE_SLIP 0
 #define NK_NO_SLIP   1
 
-/* Stress balance, src/StressBalances/depth_integrated.jl:187-233 (SSA = shear nothing, DIVA = DIVAShear()). */
+/* Stress balance, src/StressBalances/depth_integrated.jl:1-58 (SSA = shear nothing, DIVA = DIVAShear()). */
 #define NK_SSA  0
 #define NK_DIVA 1
 
@@ -70,13 +70,13 @@ typedef int32_t nk_status;
 #define NK_WEERTMAN             1
 #define NK_REGULARIZED_COULOMB  2
 
-/* Rate factor layout of GlenFlowLaw, src/Rheologies/glen_flow_law.jl:161-169. */
+/* Rate factor layout of GlenFlowLaw, src/Rheologies/glen_flow_law.jl:60-68. */
 #define NK_RATE_FACTOR_2D     0   /* Center-Center field, uniform in depth */
 #define NK_RATE_FACTOR_SIGMA  1   /* field on the sigma grid */
 
 /* Preconditioner of the velocity conjugate-gradient solver. */
-#define NK_PRECONDITIONER_NONE       0   /* precondition!(z, ::Nothing, r)          conjugate_gradient.jl:174 */
-#define NK_PRECONDITIONER_DIAGONAL   1   /* StressBalanceDiagonalPreconditioner     diagonal_preconditioner.jl:130 */
+#define NK_PRECONDITIONER_NONE       0   /* precondition!(z, ::Nothing, r)          conjugate_gradient.jl:33 */
+#define NK_PRECONDITIONER_DIAGONAL   1   /* StressBalanceDiagonalPreconditioner     diagonal_preconditioner.jl:9 */
 #define NK_PRECONDITIONER_MULTIGRID  2   /* StressBalanceMultigridPreconditioner    multigrid_preconditioner.jl:18 */
 
 /* Multigrid smoother, src/StressBalances/multigrid_preconditioner.jl:69-78. */
@@ -89,7 +89,7 @@ typedef int32_t nk_status;
 #define NK_PRECISION_FP64  0
 #define NK_PRECISION_MIXED 1
 
-/* Iteration control, src/Solvers/iteration_controls.jl:99-133. */
+/* Iteration control, src/Solvers/iteration_controls.jl:1-43. */
 #define NK_CONVERGENCE      0
 #define NK_FIXED_ITERATIONS 1
 /* An extension for the Picard control only (the reference tests the velocity change, picard.jl:79-85):
@@ -107,7 +107,7 @@ typedef struct nk_iteration_control {
     double  abstol;      /* Convergence: abstol */
 } nk_iteration_control;
 
-/* Horizontal RectilinearGrid (Flat z) plus the sigma column of SigmaGrid, src/Grids/sigma_grid.jl:264-306. */
+/* Horizontal RectilinearGrid (Flat z) plus the sigma column of SigmaGrid, src/Grids/sigma_grid.jl:20-62. */
 typedef struct nk_grid_desc {
     int32_t Nx, Ny;
     int32_t topology_x, topology_y;   /* NK_BOUNDED / NK_PERIODIC */
@@ -137,11 +137,11 @@ typedef struct nk_physics_desc {
     int32_t grounding;                /* 0: nothing (all grounded), 1: SubgridGroundedFraction */
     int32_t grounding_line_driving_stress;   /* SubgridGroundedFraction(driving_stress = true) */
     int32_t use_effective_pressure;   /* 1: the friction law receives N (0 passes `nothing`) */
-    double  mask_minimum_thickness;   /* SmoothIceMask, src/Models/smooth_ice_mask.jl:398 */
+    double  mask_minimum_thickness;   /* SmoothIceMask, src/Models/smooth_ice_mask.jl:41 */
     double  mask_transition_thickness;
 } nk_physics_desc;
 
-/* StressBalanceSolver options, src/StressBalances/stress_balance_solver.jl:176-185. */
+/* StressBalanceSolver options, src/StressBalances/stress_balance_solver.jl:43-52. */
 typedef struct nk_solver_desc {
     int32_t precision;                /* NK_PRECISION_FP64 / NK_PRECISION_MIXED */
     int32_t preconditioner;           /* NK_PRECONDITIONER_* */
@@ -221,7 +221,7 @@ int32_t     nk_api_version(void);
 
 /* IceSheetModel(grid; stress_balance, rheology, friction, grounding, masking, velocity_solver)
  * restricted to what the velocity solve reads (src/Models/ice_sheet_model.jl:79-120,
- * src/StressBalances/stress_balance_solver.jl:176-185).  Allocates every device buffer once. */
+ * src/StressBalances/stress_balance_solver.jl:43-52).  Allocates every device buffer once. */
 nk_status nk_problem_create(nk_context* ctx, const nk_grid_desc* grid, const nk_physics_desc* physics,
                             const nk_solver_desc* solver, nk_problem** out);
 nk_status nk_problem_destroy(nk_problem* problem);
@@ -247,7 +247,7 @@ nk_status nk_problem_get_field_parent(const nk_problem* problem, int32_t field, 
 /* update_geometry! + compute_driving_stress! (src/Models/ice_sheet_model_methods.jl:103-111, :126):
  * s, phi, phi_u, phi_v, N, mu from H and bed, then tau.  Replaces the reference's
  * compute_surface_elevation!, compute_grounded_fractions!, compute_effective_pressure!, compute_ice_mask!
- * (src/Groundings/subgrid_grounded_fraction.jl:234-357, src/Models/smooth_ice_mask.jl:417-426) and
+ * (src/Groundings/subgrid_grounded_fraction.jl:109-232, src/Models/smooth_ice_mask.jl:60-69) and
  * compute_driving_stress! (src/StressBalances/driving_stress.jl:43-125). */
 nk_status nk_compute_geometry(nk_problem* problem);
 
@@ -310,7 +310,7 @@ nk_status nk_problem_query(nk_problem* problem, int32_t* done);
  * nk_picard_solve and copies u, v out.  u, v in interior layout. */
 nk_status nk_solve_velocities(nk_problem* problem, double* u, double* v, nk_solve_stats* stats);
 
-/* DIVA: compute_velocity_profile! (src/StressBalances/diva.jl:249-269); SSA: extend_depth_average!
+/* DIVA: compute_velocity_profile! (src/StressBalances/diva.jl:89-109); SSA: extend_depth_average!
  * (src/Models/ice_sheet_model_methods.jl:167-180).  Fills U_B, V_B, U_SIGMA, V_SIGMA. */
 nk_status nk_velocity_profile(nk_problem* problem);
 
@@ -420,7 +420,7 @@ nk_status nk_server_info(const nk_server* server, int32_t* resident, int64_t* de
 #define NK_KERNEL_CG_UPDATE       2   /* x += alpha p, r -= alpha q with the fused r.r (and r.z) reductions */
 
 /* Instrumentation (no counterpart in the reference, which times whole solves with @elapsed,
- * benchmarks/multigrid_scaling.jl:146-157): launches one hot kernel `repeats` times on the problem's
+ * benchmarks/multigrid_scaling.jl:36-47): launches one hot kernel `repeats` times on the problem's
  * current state and stream, each launch bracketed by CUDA events; when flush_bytes > 0 a device buffer of
  * that size is overwritten before every launch so the launch starts with a cold L2.  Returns the mean
  * launch duration and the algorithmic bytes of one launch (every array it reads or writes counted once).

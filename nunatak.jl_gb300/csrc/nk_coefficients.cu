@@ -24,7 +24,7 @@ __device__ __forceinline__ double strain_xy(const DevGrid<double>& g, const doub
     double e = (dudy + dvdx) / 2;
     return g.peripheral_ff(i, j) ? wf * e : e;
 }
-// effective_strain_rate², strain_rates.jl:116-121
+// effective_strain_rate², strain_rates.jl:27-32
 __device__ __forceinline__ double effective_strain_rate2(const DevGrid<double>& g, const double2* __restrict__ x, const double2* ud,
                                                          int i, int j, double wf) {
     double exx = (wall_u(g, x, ud, i + 1, j) - wall_u(g, x, ud, i, j)) * g.rdxc[i];
@@ -35,7 +35,7 @@ __device__ __forceinline__ double effective_strain_rate2(const DevGrid<double>& 
     return exx * exx + eyy * eyy + exx * eyy + exy2;
 }
 
-// η = ½ A^(-1/n) ε̇ₑ²^((1-n)/2n) (glen_flow_law.jl:211).  For n = 3 both powers are reciprocal cube roots.
+// η = ½ A^(-1/n) ε̇ₑ²^((1-n)/2n) (glen_flow_law.jl:110).  For n = 3 both powers are reciprocal cube roots.
 __device__ __forceinline__ double glen(double A, double ee, double n) {
     if (n == 3.0) return rcbrt(A) * rcbrt(ee) / 2;
     return pow(A, -1 / n) * pow(ee, (1 - n) / (2 * n)) / 2;
@@ -45,7 +45,7 @@ __device__ __forceinline__ double rate_factor(const PhysView& ph, int c, int k) 
     return ph.rate_sigma ? ph.A[(long long)k * ph.plane + c] : ph.A[c];
 }
 
-// compute_viscosity! (glen_flow_law.jl:198-212) fused with compute_column_integrals! (column_integrals.jl:83-101)
+// compute_viscosity! (glen_flow_law.jl:97-111) fused with compute_column_integrals! (column_integrals.jl:54-72)
 __global__ void k_viscosity(PhysView ph, const double2* __restrict__ x, double* eta_sigma, double4* coef, double* F2) {
     const DevGrid<double>& g = ph.g;
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
@@ -69,7 +69,7 @@ void launch_viscosity(const PhysView& ph, const double2* x, double* eta_sigma, d
     k_viscosity<<<d.grid, d.block, 0, s>>>(ph, x, eta_sigma, coef, F2); count_launch();
 }
 
-// _compute_shear_viscosity! (glen_flow_law.jl:235-244): the basal stress βᵇ uᵇ drives a vertical shear
+// _compute_shear_viscosity! (glen_flow_law.jl:134-143): the basal stress βᵇ uᵇ drives a vertical shear
 // ε̇xz = ℑxᶜ(βᵇᵘ uᵇ)(1 - ζ) / 2η⁻ with the previous viscosity η⁻ (left out where η⁻ is still zero)
 __global__ void k_viscosity_diva(PhysView ph, const double2* __restrict__ x, const double2* __restrict__ bb,
                                  const double2* __restrict__ ub, double* eta_sigma, double4* coef, double* F2) {
@@ -174,7 +174,7 @@ void launch_basal_drag(const PhysView& ph, const double2* x, double4* coef, doub
     k_basal_drag<<<d.grid, d.block, 0, s>>>(ph, x, coef, bb); count_launch();
 }
 
-// 1 + βᵇ ℑF₂ at the velocity points, diva.jl:161-163
+// 1 + βᵇ ℑF₂ at the velocity points, diva.jl:1-3
 __device__ __forceinline__ double x_shear_factor(const DevGrid<double>& g, double b, const double* F2, int i, int j) {
     return 1 + b * ((F2[g.c_idx(i - 1, j)] + F2[g.c_idx(i, j)]) / 2);
 }
@@ -216,14 +216,14 @@ void launch_effective_drag(const PhysView& ph, const double2* bb, const double* 
     k_effective_drag<<<d.grid, d.block, 0, s>>>(ph, bb, F2, coef); count_launch();
 }
 
-// shear_integral (column_integrals.jl:71): H ∫₀^ζₖ (1 - ζ′)/η dζ′
+// shear_integral (column_integrals.jl:42): H ∫₀^ζₖ (1 - ζ′)/η dζ′
 __device__ __forceinline__ double shear_integral(const PhysView& ph, const double* eta_sigma, int c, int k) {
     double I = 0.0;
     for (int kp = 0; kp <= k; ++kp) I += (1 / eta_sigma[(long long)kp * ph.plane + c]) * ph.sig.w1[k * ph.sig.N + kp];
     return I * ph.H[c];
 }
 
-// _compute_x/y_velocity_profile! (diva.jl:259-269) or _extend_depth_average! (SSA)
+// _compute_x/y_velocity_profile! (diva.jl:99-109) or _extend_depth_average! (SSA)
 __global__ void k_velocity_profile(PhysView ph, int diva, const double2* __restrict__ x, const double2* __restrict__ bb,
                                    const double* __restrict__ eta_sigma, const double2* __restrict__ ub, double2* usig) {
     const DevGrid<double>& g = ph.g;
@@ -266,13 +266,13 @@ void launch_velocity_profile(const PhysView& ph, int diva, const double2* x, con
 
 // ---- geometry ---------------------------------------------------------------------------------------------
 __device__ __forceinline__ double nonzero(double x) { return x == 0.0 ? 1.0 : x; }
-// segment_grounded_fraction, subgrid_grounded_fraction.jl:159-163
+// segment_grounded_fraction, subgrid_grounded_fraction.jl:34-38
 __device__ __forceinline__ double segment_fraction(double f1, double f2) {
     double fp = fmax(f1, 0.0) + fmax(f2, 0.0);
     double S = fabs(f1) + fabs(f2);
     return S == 0.0 ? 1.0 : fp / nonzero(S);
 }
-// triangle_grounded_fraction, :166-174
+// triangle_grounded_fraction, subgrid_grounded_fraction.jl:41-49
 __device__ __forceinline__ double triangle_fraction(double f1, double f2, double f3) {
     double a = fmin(fmin(f1, f2), f3);
     double c = fmax(fmax(f1, f2), f3);
@@ -699,7 +699,7 @@ void launch_adjoint_gradient(const AdjointView& v, cudaStream_t s) {
 }
 
 // ---- DIVA: the reverse of one update_diva_coefficients! step at the fixed point ---------------------------------
-// The forward step (diva.jl:221-235) reads x, the lagged βᵇ⁻, F₂⁻ and ησ⁻ and writes:
+// The forward step (diva.jl:61-75) reads x, the lagged βᵇ⁻, F₂⁻ and ησ⁻ and writes:
 //   uᵇ = x / (1 + βᵇ⁻ ℑF₂⁻)                               (compute_basal_velocities!)
 //   βᵇ = φ drag(|uᵇ|, C, N)                                (compute_basal_drag! on uᵇ)
 //   ησₖ = glen(Aₖ, ε̇ₑ²(x) + (τxᵇ² + τyᵇ²) aₖ² + ε̇₀²),      τxᵇ = ℑxᶜ(βᵇᵘ uᵇ), aₖ = (1 - ζₖ) / 2ησ⁻ₖ

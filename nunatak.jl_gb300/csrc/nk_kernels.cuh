@@ -5,7 +5,7 @@
 
 namespace nk {
 
-// Sigma column constants (src/StressBalances/column_integrals.jl:31-74, src/Grids/sigma_grid.jl:264-266).
+// Sigma column constants (src/StressBalances/column_integrals.jl:1-45, src/Grids/sigma_grid.jl:20-22).
 constexpr int MAX_SIGMA = 64;
 struct SigmaTable {
     int N;
@@ -94,9 +94,9 @@ void launch_picard_end_viscosity(const DevGrid<double>& g, const double4* coef, 
                                  unsigned long long cond, cudaStream_t s);
 
 // ---- coefficients ---------------------------------------------------------------------------------------
-// SSA membrane viscosity (glen_flow_law.jl:208-212) and column integrals (column_integrals.jl:90-101)
+// SSA membrane viscosity (glen_flow_law.jl:107-111) and column integrals (column_integrals.jl:61-72)
 void launch_viscosity(const PhysView& ph, const double2* x, double* eta_sigma, double4* coef, double* F2, cudaStream_t s);
-// DIVA viscosity with lagged vertical shear (glen_flow_law.jl:235-244) and column integrals
+// DIVA viscosity with lagged vertical shear (glen_flow_law.jl:134-143) and column integrals
 void launch_viscosity_diva(const PhysView& ph, const double2* x, const double2* bb, const double2* ub, double* eta_sigma,
                            double4* coef, double* F2, cudaStream_t s);
 // eta_H_ff = ℑxyᶠᶠ(eta_H) over 0..Nx x 0..Ny (stress_balance_coefficients.jl:26-29)
@@ -105,9 +105,9 @@ void launch_corners(const DevGrid<T>& g, typename Vec4<T>::type* coef, cudaStrea
 // basal drag at the faces from the velocity `x` (frictions.jl:142-160): writes beta into (coef.z, coef.w)
 // when `coef` is given, else into the pair array `bb` (DIVA friction-law drag)
 void launch_basal_drag(const PhysView& ph, const double2* x, double4* coef, double2* bb, cudaStream_t s);
-// DIVA basal velocity u_b = u / (1 + beta_b ℑF2) (diva.jl:179-187)
+// DIVA basal velocity u_b = u / (1 + beta_b ℑF2) (diva.jl:19-27)
 void launch_basal_velocity(const PhysView& ph, const double2* x, const double2* bb, const double* F2, double2* ub, cudaStream_t s);
-// DIVA effective drag beta = beta_b / (1 + beta_b ℑF2) (diva.jl:203-211)
+// DIVA effective drag beta = beta_b / (1 + beta_b ℑF2) (diva.jl:43-51)
 void launch_effective_drag(const PhysView& ph, const double2* bb, const double* F2, double4* coef, cudaStream_t s);
 
 // ---- fixed-point adjoint of the SSA Picard step (nk_coefficients.cu) ------------------------------------------
@@ -155,7 +155,7 @@ void launch_adjoint_diva_gradient(const AdjointView& v, cudaStream_t s);
 // Δ = ‖λ⁺ − λ‖, M = ‖λ⁺‖ over the solved cells into sc->p_D / sc->p_X, then λ = λ⁺
 void launch_adjoint_change(const DevGrid<double>& g, const double2* lam_new, double2* lam, SolverScalars* sc, double2* partials,
                            cudaStream_t s);
-// DIVA velocity profile (diva.jl:259-269) / SSA depth extension (ice_sheet_model_methods.jl:167-180)
+// DIVA velocity profile (diva.jl:99-109) / SSA depth extension (ice_sheet_model_methods.jl:167-180)
 void launch_velocity_profile(const PhysView& ph, int diva, const double2* x, const double2* bb, const double* F2,
                              const double* eta_sigma, double2* ub, double2* usig, cudaStream_t s);
 

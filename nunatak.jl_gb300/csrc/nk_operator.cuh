@@ -1,7 +1,7 @@
 // nk_operator.cuh — device functions of the matrix-free SSA / DIVA operator on the C grid.
 //
-// Restates src/StressBalances/ssa_operator.jl:47-121 (operator, strain rates, wall handling),
-// src/StressBalances/diagonal_preconditioner.jl:141-165 (operator diagonal) and
+// Restates src/StressBalances/ssa_operator.jl:47-89 and strain_rates.jl:1-32 (operator, strain rates, wall handling),
+// src/StressBalances/diagonal_preconditioner.jl:20-44 (operator diagonal) and
 // src/StressBalances/multigrid_preconditioner.jl:195-227 (ℓ1 row sums, line couplings), with the
 // metric divisions replaced by multiplications with precomputed reciprocals.
 #pragma once
@@ -15,10 +15,10 @@ struct OpView {
     DevGrid<T> g;
     const typename Vec4<T>::type* coef;   // (eta_H, eta_H_ff, beta_u, beta_v) per (i, j)
     const uint8_t* mask;                  // U/V_INACTIVE, _WALL, _DIRICHLET bits per (i, j)
-    T wall_factor;                        // wall_shear_factor: 0 free slip, 2 no slip (ssa_operator.jl:100-101)
+    T wall_factor;                        // wall_shear_factor: 0 free slip, 2 no slip (strain_rates.jl:11-12)
 };
 
-// interior_u / interior_v (ssa_operator.jl:94-95) with the operator's mask (walls and ice-free points); a prescribed
+// interior_u / interior_v (strain_rates.jl:5-6) with the operator's mask (walls and ice-free points); a prescribed
 // face passes its value (U_DIRICHLET / V_DIRICHLET).
 template <typename T, typename V2>
 __device__ __forceinline__ T masked_u(const OpView<T>& o, const V2* __restrict__ p, int i, int j) {
@@ -46,7 +46,7 @@ __device__ __forceinline__ void center_stress(const OpView<T>& o, const V2* __re
     syy = g.dxc[i] * (T(2) * eta * (T(2) * eyy + exx));
 }
 
-// shear_stress at corner (i, j) = 2 η̄Hᶠᶠ ε̇xy, ε̇xy scaled by the wall factor on wall corners (ssa_operator.jl:62, :103-106).
+// shear_stress at corner (i, j) = 2 η̄Hᶠᶠ ε̇xy, ε̇xy scaled by the wall factor on wall corners (ssa_operator.jl:62, strain_rates.jl:14-17).
 template <typename T, typename V2>
 __device__ __forceinline__ T corner_shear(const OpView<T>& o, const V2* __restrict__ p, int i, int j) {
     const DevGrid<T>& g = o.g;
@@ -96,7 +96,7 @@ __device__ __forceinline__ T x_shear_diagonal(const OpView<T>& o, int i, int j) 
 template <typename T>
 __device__ __forceinline__ T y_shear_diagonal(const OpView<T>& o, int i, int j) { return corner_factor(o, i, j) * o.g.dyf[j] * eta_ff(o, i, j) * o.g.rdxf[i]; }
 
-// x_diagonal / y_diagonal (diagonal_preconditioner.jl:153-165); unit where inactive or zero.
+// x_diagonal / y_diagonal (diagonal_preconditioner.jl:32-44); unit where inactive or zero.
 template <typename T>
 __device__ __forceinline__ T x_diagonal(const OpView<T>& o, int i, int j, uint8_t m) {
     T d = o.g.Az_fc(i, j) * o.coef[o.g.idx(i, j)].z + x_normal_diagonal(o, i, j) + x_normal_diagonal(o, i - 1, j) +

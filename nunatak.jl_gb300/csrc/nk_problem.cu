@@ -356,7 +356,7 @@ static void upload_metrics(Level<T>& L, cudaStream_t s) {
     L.g.rdyf = m + METRIC_PAD;
 }
 
-// Exact integral of (1 - ζ)^p, column_integrals.jl:31
+// Exact integral of (1 - ζ)^p, column_integrals.jl:1-2
 static double ipow(double x, int n) { double r = x; for (int m = 1; m < n; ++m) r *= x; return r; }
 static double power_integral(double zm, double zp, int p) { return (ipow(1 - zm, p + 1) - ipow(1 - zp, p + 1)) / (p + 1); }
 
@@ -715,7 +715,7 @@ static void cg_step(nk_problem* P, const CGView& v) {
     launch_cg_xpby(v, s);
 }
 
-// conjugate_gradient!, conjugate_gradient.jl:306-312 (everything before the iteration loop)
+// conjugate_gradient!, conjugate_gradient.jl:165-171 (everything before the iteration loop)
 static void cg_start(nk_problem* P, const CGView& v) {
     update_preconditioner(P);
     launch_cg_init(v, P->stream);
@@ -1422,7 +1422,7 @@ nk_status nk_precondition(nk_problem* P, const double* ru, const double* rv, dou
         if (P->precond == NK_PRECONDITIONER_NONE) {
             launch_copy_range(g, P->z, P->r, P->stream);                      // copyto!(z, r) over Nx x Ny
         } else if (P->precond == NK_PRECONDITIONER_DIAGONAL) {
-            // z = r / diag over size(z); the wall faces are unit rows (diagonal_preconditioner.jl:132-139)
+            // z = r / diag over size(z); the wall faces are unit rows (diagonal_preconditioner.jl:11-18)
             launch_inverse_diagonal(P->fine_op(), P->invd, P->stream);
             launch_precondition_diagonal(g, P->z, P->r, P->invd, P->stream);
         } else {
@@ -1472,7 +1472,7 @@ nk_status nk_adjoint_solve(nk_problem* P, const double* bu, const double* bv, nk
         if (P->ctx) P->ctx->error = "nk_adjoint_solve: not available for a problem with prescribed velocities";
         return NK_BAD_ARGUMENT;
     }
-    return linear_solve_impl(P, bu, bv, stats);   // the operator is self-adjoint (conjugate_gradient.jl:186-189)
+    return linear_solve_impl(P, bu, bv, stats);   // the operator is self-adjoint (conjugate_gradient.jl:45-48, 155-156)
 }
 
 // Fixed-point adjoint of a converged picard_solve! (ext/NunatakEnzymeExt.jl:167-240).  The Picard step maps x to
@@ -1480,7 +1480,7 @@ nk_status nk_adjoint_solve(nk_problem* P, const double* bu, const double* bv, nk
 // from λ = 0 with the problem's preconditioned CG warm-started from the previous λ, until
 // ‖λ⁺ - λ‖ ≤ max(reltol ‖λ⁺‖, abstol).  Then b̄ = λ and p̄ = -(∂[A(c(p)) x*]/∂p)ᵀ λ.
 // DIVA's step also maps its lagged state s = (βᵇ, F₂, ησ) (the overwritten coefficients it reads, diva.jl:77-80);
-// the adjoint σ of s is swept along with λ (:196-214): each iteration runs the step's reverse with q̄ = -λ and
+// the adjoint σ of s is swept along with λ (ext/NunatakEnzymeExt.jl:204-214): each iteration runs the step's reverse with q̄ = -λ and
 // the state adjoint σ, which yields r and the next σ.
 static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar, const nk_iteration_control& ctl, double* lu,
                            double* lv, double* grad, double* grad_A, nk_solve_stats* st) {

@@ -1,6 +1,6 @@
 // nk_solver.cu — operator apply, operator masks and diagonals, and the fused conjugate-gradient kernels.
 //
-// Conjugate gradients restate src/Solvers/conjugate_gradient.jl:299-364 with the vector operations of
+// Conjugate gradients restate src/Solvers/conjugate_gradient.jl:158-223 with the vector operations of
 // src/Solvers/velocity_vector.jl:48-141 fused into the kernels that produce their operands:
 //   step k:  apply   q = A p,  alpha = rho / p.q                       (one kernel + fused dot)
 //            update  x += alpha p, r -= alpha q [, z = r / diag], dots (one kernel + fused dots)
@@ -83,7 +83,7 @@ void launch_apply(const OpView<double>& o, const double2* p, double2* q, cudaStr
     count_launch();
 }
 
-// inactiveᶠᶜᶜ / inactiveᶜᶠᶜ with η̄H (ssa_operator.jl:91-92, smooth_ice_mask.jl:429-430) and the wall bits; `ud` (the
+// inactiveᶠᶜᶜ / inactiveᶜᶠᶜ with η̄H (strain_rates.jl:2-3, smooth_ice_mask.jl:72-73) and the wall bits; `ud` (the
 // fine level only) marks prescribed faces as identity rows that keep their value (U_DIRICHLET / V_DIRICHLET)
 template <typename T>
 __global__ void k_mask(OpView<T> o, uint8_t* mask, const double2* ud) {
@@ -169,7 +169,7 @@ __device__ __forceinline__ int stop_after(const SolverScalars* sc, double rnorm,
     return !(rnorm > sc->tol && it < sc->maxiter);
 }
 
-// conjugate_gradient!, conjugate_gradient.jl:306-312: r = b - A x, z = M r, p = z, rho = r.z
+// conjugate_gradient!, conjugate_gradient.jl:165-171: r = b - A x, z = M r, p = z, rho = r.z
 template <int R>
 __global__ void __launch_bounds__(32 * STRIP_WARPS) k_cg_init(CGView v) {
     int i, j0;
@@ -269,7 +269,7 @@ void launch_cg_init_finish(const CGView& v, cudaStream_t s) {
     k_cg_init_finish<<<d.grid, d.block, 0, s>>>(v); count_launch();
 }
 
-// conjugate_gradient_step!, conjugate_gradient.jl:350-353: q = A p, alpha = rho / p.q (0 if p.q = 0)
+// conjugate_gradient_step!, conjugate_gradient.jl:209-212: q = A p, alpha = rho / p.q (0 if p.q = 0)
 template <int R>
 __global__ void __launch_bounds__(32 * STRIP_WARPS) k_cg_apply(CGView v) {
     if (read_done(v.sc)) return;
@@ -297,7 +297,7 @@ void launch_cg_apply(const CGView& v, cudaStream_t s) {
     count_launch();
 }
 
-// conjugate_gradient_step!, :355-360 and the stopping test of :334-338
+// conjugate_gradient_step!, conjugate_gradient.jl:214-219 and the stopping test of :193-197
 __global__ void k_cg_update(CGView v) {
     if (read_done(v.sc)) return;
     int i = blockIdx.x * BX + threadIdx.x, j0 = blockIdx.y * BY * VEC_ROWS + threadIdx.y;
@@ -403,7 +403,7 @@ void launch_cg_dots_after_precondition(const CGView& v, cudaStream_t s) {
     k_cg_dots_after_precondition<<<d.grid, d.block, 0, s>>>(v); count_launch();
 }
 
-// xpby!(z, beta, p), conjugate_gradient.jl:361; the last block commits the stopping decision
+// xpby!(z, beta, p), conjugate_gradient.jl:220; the last block commits the stopping decision
 __global__ void k_cg_xpby(CGView v) {
     if (read_done(v.sc)) return;
     int i = blockIdx.x * BX + threadIdx.x, j0 = blockIdx.y * BY * VEC_ROWS + threadIdx.y;

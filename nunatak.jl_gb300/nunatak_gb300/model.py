@@ -2,20 +2,20 @@
 descriptors (include/nunatak_gb300.h).  Nothing here touches a device.
 
 Reference constructors mirrored (file:line in Nunatak.jl):
-  RectilinearGrid (Oceananigans; halo default 3), SigmaGrid                 src/Grids/sigma_grid.jl:287-306
-  Convergence / FixedIterations                                             src/Solvers/iteration_controls.jl:118-133
-  GlenFlowLaw(grid; rate_factor, exponent = 3, strain_rate_regularization = 1e-13)   src/Rheologies/glen_flow_law.jl:137-141
+  RectilinearGrid (Oceananigans; halo default 3), SigmaGrid                 src/Grids/sigma_grid.jl:43-62
+  Convergence / FixedIterations                                             src/Solvers/iteration_controls.jl:18-43
+  GlenFlowLaw(grid; rate_factor, exponent = 3, strain_rate_regularization = 1e-13)   src/Rheologies/glen_flow_law.jl:36-40
   WeertmanFriction(grid; coefficient, exponent = 1/3, velocity_regularization = 1e-8) src/Frictions/frictions.jl:34-37
   RegularizedCoulombFriction(grid; coefficient, coulomb_coefficient, ...)   src/Frictions/frictions.jl:65-71
-  DepthIntegrated(; shear = nothing, side_walls = FreeSlipWalls())          src/StressBalances/depth_integrated.jl:204
-  SubgridGroundedFraction(; driving_stress = false)                         src/Groundings/subgrid_grounded_fraction.jl:148
-  SmoothIceMask(grid; minimum_thickness = 1, transition_thickness = 1)      src/Models/smooth_ice_mask.jl:398-402
-  IceSheetConstants(grid; 918, 1028, 9.81)                                  src/Models/ice_sheet_constants.jl:468-471
+  DepthIntegrated(; shear = nothing, side_walls = FreeSlipWalls())          src/StressBalances/depth_integrated.jl:29
+  SubgridGroundedFraction(; driving_stress = false)                         src/Groundings/subgrid_grounded_fraction.jl:23
+  SmoothIceMask(grid; minimum_thickness = 1, transition_thickness = 1)      src/Models/smooth_ice_mask.jl:41-45
+  IceSheetConstants(grid; 918, 1028, 9.81)                                  src/Models/ice_sheet_constants.jl:33-36
   StressBalanceMultigridPreconditioner(grid; smoother = PointJacobi(), smoothing_sweeps = 2,
                                        coarsest_sweeps = 20, minimum_coarse_size = 2)   src/StressBalances/multigrid_preconditioner.jl:57
   StressBalanceSolver(grid; linear_iteration_control = Convergence(reltol = 1e-8, maxiter = 10_000),
                       picard_iteration_control = Convergence(reltol = 1e-6, maxiter = 100),
-                      preconditioner = StressBalanceDiagonalPreconditioner())     src/StressBalances/stress_balance_solver.jl:176-185
+                      preconditioner = StressBalanceDiagonalPreconditioner())     src/StressBalances/stress_balance_solver.jl:43-52
 """
 import ctypes as C
 from dataclasses import dataclass, field
@@ -25,7 +25,7 @@ import numpy as np
 
 from . import abi
 
-YEAR = 31556926.0   # seconds, benchmarks/multigrid_scaling.jl:118
+YEAR = 31556926.0   # seconds, benchmarks/multigrid_scaling.jl:8
 
 
 # ---- grid ---------------------------------------------------------------------------------------

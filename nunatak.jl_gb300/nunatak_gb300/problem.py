@@ -6,11 +6,11 @@ hierarchy, resident on the GPU.  Its methods are the reference's entry points fo
   set! / interior(field)            -> Problem.set / Problem.get
   update_geometry! + driving stress -> Problem.compute_geometry   (src/Models/ice_sheet_model_methods.jl:103-111, :126)
   update_stress_balance_coefficients! / update_diva_coefficients!
-                                    -> Problem.update_coefficients (stress_balance_coefficients.jl:10-20, diva.jl:221-235)
+                                    -> Problem.update_coefficients (stress_balance_coefficients.jl:10-20, diva.jl:61-75)
   ssa_operator!(q, p, ...)          -> Problem.apply_operator      (src/StressBalances/ssa_operator.jl:47-52)
   precondition!(z, P, r, ...)       -> Problem.precondition
-  solve!(x, solver, b, ...)         -> Problem.linear_solve        (src/Solvers/conjugate_gradient.jl:269-270)
-  adjoint_solve!(λ, solver, b, ...) -> Problem.adjoint_solve       (src/Solvers/conjugate_gradient.jl:296-297)
+  solve!(x, solver, b, ...)         -> Problem.linear_solve        (src/Solvers/conjugate_gradient.jl:128-129)
+  adjoint_solve!(λ, solver, b, ...) -> Problem.adjoint_solve       (src/Solvers/conjugate_gradient.jl:155-156)
   picard_solve!(x, picard, ...)     -> Problem.picard_solve        (src/Solvers/picard.jl:63-90)
   compute_velocity_profile! / extend_depth_average! -> Problem.velocity_profile
 

@@ -192,10 +192,10 @@ static void for_xy(int Nx, int Ny, F&& f) {   // launch!(arch, grid, :xyz, ...) 
 
 // ------------------------------------------------------------------------------------------------
 // Masks and strain rates, src/StressBalances/strain_rates.jl:1-32 and
-// src/StressBalances/ssa_operator.jl:90-121.  `eta` is η̄H (operator) or nullptr (`nothing`).
+// src/Models/smooth_ice_mask.jl:72-75.  `eta` is η̄H (operator) or nullptr (`nothing`).
 // ------------------------------------------------------------------------------------------------
-static inline bool ice_free_fc(int i, int j, const Field* mu) { return mu && ((*mu)(i - 1, j) + (*mu)(i, j)) == 0.0; }   // smooth_ice_mask.jl:429
-static inline bool ice_free_cf(int i, int j, const Field* mu) { return mu && ((*mu)(i, j - 1) + (*mu)(i, j)) == 0.0; }   // smooth_ice_mask.jl:430
+static inline bool ice_free_fc(int i, int j, const Field* mu) { return mu && ((*mu)(i - 1, j) + (*mu)(i, j)) == 0.0; }   // smooth_ice_mask.jl:72
+static inline bool ice_free_cf(int i, int j, const Field* mu) { return mu && ((*mu)(i, j - 1) + (*mu)(i, j)) == 0.0; }   // smooth_ice_mask.jl:73
 // A prescribed face: one of the solved rows (i, j in 1..Nx x 1..Ny, wrapped when periodic: the west / south
 // boundary faces and the interior faces) whose prescribed value is finite.  Its row is an identity row
 // (inactive) and its value still enters the strain rates (interior_u / interior_v pass it).
@@ -205,37 +205,37 @@ static inline bool prescribed(const Grid& g, const Field* d, int i, int j) {
 }
 static inline bool prescribed_fc(const Grid& g, int i, int j) { return prescribed(g, g.pu, i, j); }
 static inline bool prescribed_cf(const Grid& g, int i, int j) { return prescribed(g, g.pv, i, j); }
-static inline bool inactive_fc(const Grid& g, int i, int j, const Field* eta) {   // ssa_operator.jl:91 (+ prescribed)
+static inline bool inactive_fc(const Grid& g, int i, int j, const Field* eta) {   // strain_rates.jl:2 (+ prescribed)
     return g.peripheral_fc(i, j) || ice_free_fc(i, j, eta) || prescribed_fc(g, i, j);
 }
-static inline bool inactive_cf(const Grid& g, int i, int j, const Field* eta) {   // ssa_operator.jl:92 (+ prescribed)
+static inline bool inactive_cf(const Grid& g, int i, int j, const Field* eta) {   // strain_rates.jl:3 (+ prescribed)
     return g.peripheral_cf(i, j) || ice_free_cf(i, j, eta) || prescribed_cf(g, i, j);
 }
-static inline double interior_u(const Grid& g, int i, int j, const Field& u, const Field* eta) {   // :94
+static inline double interior_u(const Grid& g, int i, int j, const Field& u, const Field* eta) {   // strain_rates.jl:5
     return (inactive_fc(g, i, j, eta) && !prescribed_fc(g, i, j)) ? 0.0 : u(i, j);
 }
-static inline double interior_v(const Grid& g, int i, int j, const Field& v, const Field* eta) {   // :95
+static inline double interior_v(const Grid& g, int i, int j, const Field& v, const Field* eta) {   // strain_rates.jl:6
     return (inactive_cf(g, i, j, eta) && !prescribed_cf(g, i, j)) ? 0.0 : v(i, j);
 }
 
-static inline double strain_rate_xx(const Grid& g, int i, int j, const Field& u, const Field* eta) {   // :97
+static inline double strain_rate_xx(const Grid& g, int i, int j, const Field& u, const Field* eta) {   // strain_rates.jl:8
     return (interior_u(g, i + 1, j, u, eta) - interior_u(g, i, j, u, eta)) / g.dx_c(i);
 }
-static inline double strain_rate_yy(const Grid& g, int i, int j, const Field& v, const Field* eta) {   // :98
+static inline double strain_rate_yy(const Grid& g, int i, int j, const Field& v, const Field* eta) {   // strain_rates.jl:9
     return (interior_v(g, i, j + 1, v, eta) - interior_v(g, i, j, v, eta)) / g.dy_c(j);
 }
-static inline double wall_shear_factor(int walls) { return walls == NK_NO_SLIP ? 2.0 : 0.0; }         // :100-101
-static inline double strain_rate_xy(const Grid& g, int i, int j, const Field& u, const Field& v, int walls, const Field* eta) {  // :103-106
+static inline double wall_shear_factor(int walls) { return walls == NK_NO_SLIP ? 2.0 : 0.0; }         // strain_rates.jl:11-12
+static inline double strain_rate_xy(const Grid& g, int i, int j, const Field& u, const Field& v, int walls, const Field* eta) {  // strain_rates.jl:14-17
     double dudy = (interior_u(g, i, j, u, eta) - interior_u(g, i, j - 1, u, eta)) / g.dy_f(j);
     double dvdx = (interior_v(g, i, j, v, eta) - interior_v(g, i - 1, j, v, eta)) / g.dx_f(i);
     double e = (dudy + dvdx) / 2;
     return g.peripheral_ff(i, j) ? wall_shear_factor(walls) * e : e;
 }
-static inline double strain_rate_xy2(const Grid& g, int i, int j, const Field& u, const Field& v, int walls) {  // :108
+static inline double strain_rate_xy2(const Grid& g, int i, int j, const Field& u, const Field& v, int walls) {  // strain_rates.jl:19
     double e = strain_rate_xy(g, i, j, u, v, walls, nullptr);
     return e * e;
 }
-// effective_strain_rate², strain_rates.jl:116-121; ℑxyᶜᶜᵃ = ℑyᵃᶜᵃ(ℑxᶜᵃᵃ(·))
+// effective_strain_rate², strain_rates.jl:27-32; ℑxyᶜᶜᵃ = ℑyᵃᶜᵃ(ℑxᶜᵃᵃ(·))
 static inline double effective_strain_rate2(const Grid& g, int i, int j, const Field& u, const Field& v, int walls) {
     double exx = strain_rate_xx(g, i, j, u, nullptr);
     double eyy = strain_rate_yy(g, i, j, v, nullptr);
@@ -284,28 +284,28 @@ static void ssa_operator(const Grid& g, VelocityVector& q, const VelocityVector&
 }
 
 // ------------------------------------------------------------------------------------------------
-// Diagonal preconditioner, src/StressBalances/diagonal_preconditioner.jl:130-175.
+// Diagonal preconditioner, src/StressBalances/diagonal_preconditioner.jl:9-54.
 // ------------------------------------------------------------------------------------------------
-static inline double x_normal_diagonal(const Grid& g, int i, int j, const Field& eta) { return 4 * g.dy_c(j) * eta(i, j) / g.dx_c(i); }  // :141
-static inline double y_normal_diagonal(const Grid& g, int i, int j, const Field& eta) { return 4 * g.dx_c(i) * eta(i, j) / g.dy_c(j); }  // :142
-static inline double corner_shear_factor(const Grid& g, int i, int j, int walls) { return g.peripheral_ff(i, j) ? wall_shear_factor(walls) : 1.0; }  // :146
-static inline double x_shear_diagonal(const Grid& g, int i, int j, const Field& ff, int walls) {   // :148-149
+static inline double x_normal_diagonal(const Grid& g, int i, int j, const Field& eta) { return 4 * g.dy_c(j) * eta(i, j) / g.dx_c(i); }  // :20
+static inline double y_normal_diagonal(const Grid& g, int i, int j, const Field& eta) { return 4 * g.dx_c(i) * eta(i, j) / g.dy_c(j); }  // :21
+static inline double corner_shear_factor(const Grid& g, int i, int j, int walls) { return g.peripheral_ff(i, j) ? wall_shear_factor(walls) : 1.0; }  // :25
+static inline double x_shear_diagonal(const Grid& g, int i, int j, const Field& ff, int walls) {   // :27-28
     return corner_shear_factor(g, i, j, walls) * g.dx_f(i) * ff(i, j) / g.dy_f(j);
 }
-static inline double y_shear_diagonal(const Grid& g, int i, int j, const Field& ff, int walls) {   // :150-151
+static inline double y_shear_diagonal(const Grid& g, int i, int j, const Field& ff, int walls) {   // :29-30
     return corner_shear_factor(g, i, j, walls) * g.dy_f(j) * ff(i, j) / g.dx_f(i);
 }
-static inline double x_diagonal(const Grid& g, int i, int j, const Coefficients& c, int walls) {   // :153-158
+static inline double x_diagonal(const Grid& g, int i, int j, const Coefficients& c, int walls) {   // :32-37
     double d = g.Az_fcc(i, j) * (*c.bu)(i, j) + x_normal_diagonal(g, i, j, *c.etaH) + x_normal_diagonal(g, i - 1, j, *c.etaH) +
                x_shear_diagonal(g, i, j, *c.etaHff, walls) + x_shear_diagonal(g, i, j + 1, *c.etaHff, walls);
     return (inactive_fc(g, i, j, c.etaH) || d == 0.0) ? 1.0 : d;
 }
-static inline double y_diagonal(const Grid& g, int i, int j, const Coefficients& c, int walls) {   // :160-165
+static inline double y_diagonal(const Grid& g, int i, int j, const Coefficients& c, int walls) {   // :39-44
     double d = g.Az_cfc(i, j) * (*c.bv)(i, j) + y_normal_diagonal(g, i, j, *c.etaH) + y_normal_diagonal(g, i, j - 1, *c.etaH) +
                y_shear_diagonal(g, i, j, *c.etaHff, walls) + y_shear_diagonal(g, i + 1, j, *c.etaHff, walls);
     return (inactive_cf(g, i, j, c.etaH) || d == 0.0) ? 1.0 : d;
 }
-static void diagonal_precondition(const Grid& g, VelocityVector& z, const VelocityVector& r, const Coefficients& c, int walls) {  // :132-139
+static void diagonal_precondition(const Grid& g, VelocityVector& z, const VelocityVector& r, const Coefficients& c, int walls) {  // :11-18, 46-54
     int nux = z.u.nx(), nuy = z.u.ny(), nvx = z.v.nx(), nvy = z.v.ny();
 #pragma omp parallel for schedule(static)
     for (int j = 1; j <= nuy; ++j) for (int i = 1; i <= nux; ++i) z.u(i, j) = r.u(i, j) / x_diagonal(g, i, j, c, walls);
@@ -619,23 +619,23 @@ static void v_cycle(const Grid& g, VelocityVector& x, const VelocityVector& b, V
 // ------------------------------------------------------------------------------------------------
 // Rheology, friction, column integrals, DIVA.
 // ------------------------------------------------------------------------------------------------
-struct Sigma {   // SigmaGrid column: faces ζ_0..ζ_Nσ (src/Grids/sigma_grid.jl:264-266)
+struct Sigma {   // SigmaGrid column: faces ζ_0..ζ_Nσ (src/Grids/sigma_grid.jl:20-22)
     int N = 1;
     std::vector<double> faces;
     double zf(int k) const { return faces[k - 1]; }                       // znode(k, Face), k = 1..N+1
     double zc(int k) const { return (faces[k - 1] + faces[k]) / 2; }      // znode(k, Center)
 };
 
-// Exact integral of (1 - ζ)^p, src/StressBalances/column_integrals.jl:31
+// Exact integral of (1 - ζ)^p, src/StressBalances/column_integrals.jl:1-2
 static inline double ipow(double x, int n) { double r = x; for (int m = 1; m < n; ++m) r *= x; return r; }
 static inline double power_integral(double zm, double zp, int p) { return (ipow(1 - zm, p + 1) - ipow(1 - zp, p + 1)) / (p + 1); }
-static inline double layer_weight(const Sigma& s, int k, int p) { return power_integral(s.zf(k), s.zf(k + 1), p); }   // :34-35
-static inline double profile_weight(const Sigma& s, int kp, int k, int p) {   // :38-43
+static inline double layer_weight(const Sigma& s, int k, int p) { return power_integral(s.zf(k), s.zf(k + 1), p); }   // :4-6
+static inline double profile_weight(const Sigma& s, int kp, int k, int p) {   // :8-14
     double zm = s.zf(kp);
     double zp = (kp == k) ? s.zc(k) : s.zf(kp + 1);
     return power_integral(zm, zp, p);
 }
-static inline double layer_thickness(const Sigma& s, int k) { return s.zf(k + 1) - s.zf(k); }   // :73-74
+static inline double layer_thickness(const Sigma& s, int k) { return s.zf(k + 1) - s.zf(k); }   // :44-45
 
 struct Physics {
     int walls = NK_FREE_SLIP;
@@ -678,7 +678,7 @@ static void compute_basal_drag(const Grid& g, Field& bu, Field& bv, const Physic
         }
 }
 
-// Glen viscosity, src/Rheologies/glen_flow_law.jl:198-212 (membrane) and :223-244 (DIVA vertical shear).
+// Glen viscosity, src/Rheologies/glen_flow_law.jl:97-111 (membrane) and :122-143 (DIVA vertical shear).
 // A is 2-D (A2) or on the sigma grid (A3); bbu/bbv/ub/vb non-null selects the DIVA form.
 static void compute_viscosity(const Grid& g, const Sigma& sg, SigmaField& eta_s, const Physics& ph, const Field& u, const Field& v,
                               const Field* A2, const SigmaField* A3,
@@ -707,7 +707,7 @@ static void compute_viscosity(const Grid& g, const Sigma& sg, SigmaField& eta_s,
     });
 }
 
-// compute_column_integrals!, src/StressBalances/column_integrals.jl:83-101.  mu may be nullptr.
+// compute_column_integrals!, src/StressBalances/column_integrals.jl:54-72.  mu may be nullptr.
 static void compute_column_integrals(const Grid& g, const Sigma& sg, Field& etaH, Field& F2, const SigmaField& eta_s,
                                      const Field& H, const Field* mu) {
     for_xy(g.Nx(), g.Ny(), [&](int i, int j) {
@@ -722,7 +722,7 @@ static void compute_column_integrals(const Grid& g, const Sigma& sg, Field& etaH
     });
 }
 
-// DIVA, src/StressBalances/diva.jl:161-211
+// DIVA, src/StressBalances/diva.jl:1-51
 static void compute_basal_velocities(const Grid& g, Field& ub, Field& vb, const Field& u, const Field& v, const Field& bbu, const Field& bbv, const Field& F2) {
 #pragma omp parallel for schedule(static)
     for (int j = 1; j <= ub.ny(); ++j)
@@ -744,13 +744,13 @@ static void compute_effective_drag(Field& bu, Field& bv, const Field& bbu, const
 // ------------------------------------------------------------------------------------------------
 // Geometry and driving stress.
 // ------------------------------------------------------------------------------------------------
-static inline double nonzero(double x) { return x == 0.0 ? 1.0 : x; }   // subgrid_grounded_fraction.jl:176
-static inline double segment_grounded_fraction(double f1, double f2) {   // :159-163
+static inline double nonzero(double x) { return x == 0.0 ? 1.0 : x; }   // subgrid_grounded_fraction.jl:51
+static inline double segment_grounded_fraction(double f1, double f2) {   // :34-38
     double fp = std::max(f1, 0.0) + std::max(f2, 0.0);
     double S = std::abs(f1) + std::abs(f2);
     return S == 0.0 ? 1.0 : fp / nonzero(S);
 }
-static inline double triangle_grounded_fraction(double f1, double f2, double f3) {   // :166-174
+static inline double triangle_grounded_fraction(double f1, double f2, double f3) {   // :41-49
     double a = std::min(std::min(f1, f2), f3);
     double c = std::max(std::max(f1, f2), f3);
     double b = f1 + f2 + f3 - a - c;
@@ -786,7 +786,7 @@ struct Problem {
     Field H, bed, s, mu, phi, phu, phv, N, C, A2, etaH, etaHff, bu, bv, F2, bbu, bbv, ub, vb;
     SigmaField A3, eta_s, T, us, vs;
 
-    // CG workspace (VelocityConjugateGradientSolver, conjugate_gradient.jl:193-243) and Picard x⁻
+    // CG workspace (VelocityConjugateGradientSolver, conjugate_gradient.jl:52-102) and Picard x⁻
     VelocityVector r, z, p, q, w, xprev;
     Field eta_prev;               // η̄H of the previous Picard iteration (NK_VISCOSITY_CONVERGENCE)
     Multigrid mg;
@@ -806,20 +806,20 @@ static void impose_prescribed(Problem& P, VelocityVector& x, const VelocityVecto
     fill_halo(x);
 }
 
-static void update_preconditioner(Problem& P) {   // conjugate_gradient.jl:177; multigrid_preconditioner.jl:128
+static void update_preconditioner(Problem& P) {   // conjugate_gradient.jl:36; multigrid_preconditioner.jl:128
     if (P.sdesc.preconditioner == NK_PRECONDITIONER_MULTIGRID) coarsen_coefficients(P.mg.levels, 0, P.etaH, P.bu, P.bv);
 }
 
 static void precondition(Problem& P, VelocityVector& z, VelocityVector& r) {
     Coefficients c = coeffs(P);
     switch (P.sdesc.preconditioner) {
-        case NK_PRECONDITIONER_NONE: copyto(P.grid, z, r); break;                        // conjugate_gradient.jl:174
+        case NK_PRECONDITIONER_NONE: copyto(P.grid, z, r); break;                        // conjugate_gradient.jl:33
         case NK_PRECONDITIONER_DIAGONAL: diagonal_precondition(P.grid, z, r, c, P.ph.walls); break;
         default: v_cycle(P.grid, z, r, P.mg.residual, P.mg.scratch, c, P.mg, 0, P.ph.walls); break;  // multigrid :122-126
     }
 }
 
-// conjugate_gradient!, conjugate_gradient.jl:299-364.  Returns the iteration count.
+// conjugate_gradient!, conjugate_gradient.jl:158-223.  Returns the iteration count.
 static int conjugate_gradient(Problem& P, VelocityVector& x, const VelocityVector& b, nk_solve_stats* st, int* status) {
     const Grid& g = P.grid;
     Coefficients c = coeffs(P);
@@ -850,11 +850,11 @@ static int conjugate_gradient(Problem& P, VelocityVector& x, const VelocityVecto
     int it = 0;
     double r0 = std::sqrt(vector_dot(g, r, r));
     double rn = r0;
-    if (ctl.kind == NK_FIXED_ITERATIONS) {   // :319-324
+    if (ctl.kind == NK_FIXED_ITERATIONS) {   // :178-183
         for (int k = 0; k < ctl.iterations; ++k) rho = step(rho);
         it = ctl.iterations;
         rn = std::sqrt(vector_dot(g, r, r));
-    } else {                                  // :326-341
+    } else {                                  // :185-200
         double tol = std::max(ctl.reltol * r0, ctl.abstol);
         while (rn > tol && it < ctl.maxiter) {
             rho = step(rho);
@@ -884,7 +884,7 @@ static void update_ssa(Problem& P) {
     fill_halo(P.bu); fill_halo(P.bv);
 }
 
-// update_diva_coefficients!, diva.jl:221-235
+// update_diva_coefficients!, diva.jl:61-75
 static void update_diva(Problem& P) {
     const Grid& g = P.grid;
     fill_halo(P.x);
@@ -952,7 +952,7 @@ static void compute_geometry(Problem& P) {
     const Grid& g = P.grid;
     double rw_ri = P.ph.rho_w / P.ph.rho_i, ri_rw = P.ph.rho_i / P.ph.rho_w;
     int Nx = g.Nx(), Ny = g.Ny();
-    // compute_surface_elevation!, subgrid_grounded_fraction.jl:336-357
+    // compute_surface_elevation!, subgrid_grounded_fraction.jl:211-232
     for_xy(Nx, Ny, [&](int i, int j) {
         P.s(i, j) = P.grounding ? std::max(P.bed(i, j) + P.H(i, j), (1 - ri_rw) * P.H(i, j)) : P.bed(i, j) + P.H(i, j);
     });
@@ -985,7 +985,7 @@ static void compute_geometry(Problem& P) {
         double P0 = rig * P.H(i, j);
         P.N(i, j) = std::max(P0 + rwg * std::min(P.bed(i, j), 0.0), 0.0);
     });
-    // compute_ice_mask!, smooth_ice_mask.jl:407-426
+    // compute_ice_mask!, smooth_ice_mask.jl:50-69
     for_xy(Nx, Ny, [&](int i, int j) {
         double t = std::min(std::max((P.H(i, j) - P.mask_min) / P.mask_trans, 0.0), 1.0);
         P.mu(i, j) = t * t * (3 - 2 * t);
@@ -1044,7 +1044,7 @@ static void compute_geometry(Problem& P) {
         }
 }
 
-// compute_velocity_profile! (DIVA, diva.jl:249-269) / extend_depth_average! (SSA, ice_sheet_model_methods.jl:167-180)
+// compute_velocity_profile! (DIVA, diva.jl:89-109) / extend_depth_average! (SSA, ice_sheet_model_methods.jl:167-180)
 static void velocity_profile(Problem& P) {
     const Grid& g = P.grid;
     fill_halo(P.x);
@@ -1060,7 +1060,7 @@ static void velocity_profile(Problem& P) {
     for (auto& f : P.eta_s.k) fill_halo(f);
     compute_basal_velocities(g, P.ub, P.vb, P.x.u, P.x.v, P.bbu, P.bbv, P.F2);
     const Sigma& sg = P.sigma;
-    auto shear_integral = [&](int i, int j, int k) {   // column_integrals.jl:71
+    auto shear_integral = [&](int i, int j, int k) {   // column_integrals.jl:42
         double I = 0;
         for (int kp = 1; kp <= k; ++kp) I += (1 / P.eta_s.k[kp - 1](i, j)) * profile_weight(sg, kp, k, 1);
         return I * P.H(i, j);

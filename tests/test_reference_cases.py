@@ -54,7 +54,7 @@ def test_driving_stress_doctests(backend):
 
 
 def test_viscosity_doctest(backend):
-    """src/Rheologies/glen_flow_law.jl:179-196: A = 1, n = 1 gives η = 1/2."""
+    """src/Rheologies/glen_flow_law.jl:78-95: A = 1, n = 1 gives η = 1/2."""
     g = grid((4, 4), topology=("Periodic", "Periodic"))
     P = make(backend, g, Nsigma=3, rheology=M.GlenFlowLaw(rate_factor=1.0, exponent=1.0), masking=None)
     P.set("A", 1.0)
@@ -77,7 +77,7 @@ def test_basal_drag_doctest(backend):
 
 
 def test_grounded_fraction_doctest(backend):
-    """src/Groundings/subgrid_grounded_fraction.jl:207-232: φ = [1, 0.75, 0, 0]."""
+    """src/Groundings/subgrid_grounded_fraction.jl:82-107: φ = [1, 0.75, 0, 0]."""
     g = grid((4, 1), x=(0.0, 4.0), topology=("Bounded", "Periodic"))
     c = M.IceSheetConstants(1.0, 1.0, 9.81)
     P, _ = ice_sheet_model(backend, g, H=100.0, bed=lambda x, y: -100 * (x - 0.75), constants=c,
@@ -86,7 +86,7 @@ def test_grounded_fraction_doctest(backend):
 
 
 def test_effective_pressure_and_surface_doctests(backend):
-    """src/Groundings/subgrid_grounded_fraction.jl:274-291 (N = [10, 5]) and :317-334 (s = [80, 50])."""
+    """src/Groundings/subgrid_grounded_fraction.jl:149-166 (N = [10, 5]) and :192-209 (s = [80, 50])."""
     g = grid((2, 1), x=(0.0, 2.0), topology=("Bounded", "Periodic"))
     P, _ = ice_sheet_model(backend, g, H=10.0, bed=lambda x, y: 5.0 if x < 1 else -5.0,
                            constants=M.IceSheetConstants(1.0, 1.0, 1.0), grounding=M.SubgridGroundedFraction(), solve=False)
@@ -273,7 +273,7 @@ def uniform_strain_viscosity(cls, g, ue):
 
 
 def test_uniform_strain_viscosity(backend):
-    """test/test_glen_viscosity.jl:131-138."""
+    """test/test_glen_viscosity.jl:48-55."""
     a = 2.0
     eta = uniform_strain_viscosity(backend, grid((8, 4), topology=("Bounded", "Periodic")), lambda x, y: a * x)
     np.testing.assert_allclose(eta[:, :, 1:7], a ** (-2 / 3) / 2, rtol=1e-12)
@@ -282,7 +282,7 @@ def test_uniform_strain_viscosity(backend):
 
 
 def test_driving_stress_closed_form(backend):
-    """test/test_glen_viscosity.jl:140-155."""
+    """test/test_glen_viscosity.jl:57-72."""
     g = grid((6, 5), x=(0.0, 3.0))
     P, _ = ice_sheet_model(backend, g, H=lambda x, y: 1 + x, bed=lambda x, y: 2 * x + 3 * y - (1 + x), masking=None,
                            constants=M.IceSheetConstants(2.0, 2.0, 5.0), solve=False)
@@ -296,7 +296,7 @@ def test_driving_stress_closed_form(backend):
 
 
 def ice_stream_error(cls, Nx, L=100e3, H0=500.0, delta=20.0, rho=917.0, gacc=9.81, A=1e-24):
-    """ice_stream_error, test/test_glen_viscosity.jl:97-128 (n = 3 analytic ice stream)."""
+    """ice_stream_error, test/test_glen_viscosity.jl:14-45 (n = 3 analytic ice stream)."""
     g = grid((Nx, 4), x=(0.0, L), y=(0.0, L / Nx * 4))
     solver = M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-12, maxiter=10_000),
                                    picard_iteration_control=M.Convergence(reltol=1e-10, maxiter=300), preconditioner=None)
@@ -310,7 +310,7 @@ def ice_stream_error(cls, Nx, L=100e3, H0=500.0, delta=20.0, rho=917.0, gacc=9.8
 
 
 def test_ice_stream_n3(backend):
-    """test/test_glen_viscosity.jl:157-163."""
+    """test/test_glen_viscosity.jl:74-80."""
     r = [ice_stream_error(backend, N) for N in (32, 64)]
     assert all(it < 300 for _, it, _ in r)
     assert all(v < 1e-10 for _, _, v in r)
@@ -335,7 +335,7 @@ def uniform_drag(cls, friction, U, phi0=1.0, N0=None):
 
 
 def test_friction_laws(backend):
-    """test/test_friction.jl:223-232."""
+    """test/test_friction.jl:59-68."""
     m, C, U = 1 / 3, 3e4, 1e-5
     w = M.WeertmanFriction(coefficient=C, exponent=m, velocity_regularization=0.0)
     np.testing.assert_allclose(uniform_drag(backend, w, U), C * U ** (m - 1), rtol=1e-12)
@@ -347,7 +347,7 @@ def test_friction_laws(backend):
 
 
 def sliding_slab_speed(cls, friction, tau0, N0):
-    """sliding_slab_speed, test/test_friction.jl:182-204."""
+    """sliding_slab_speed, test/test_friction.jl:18-40."""
     g = grid((4, 4), x=(0.0, 1e3), y=(0.0, 1e3), topology=("Periodic", "Periodic"))
     solver = M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-13, maxiter=100),
                                    picard_iteration_control=M.Convergence(reltol=1e-12, maxiter=300), preconditioner=None)
@@ -364,7 +364,7 @@ def sliding_slab_speed(cls, friction, tau0, N0):
 
 
 def test_sliding_slab(backend):
-    """test/test_friction.jl:234-245."""
+    """test/test_friction.jl:70-81."""
     m, C, N0, tau0 = 1 / 3, 3e4, 1e6, 1e5
     u, it = sliding_slab_speed(backend, M.WeertmanFriction(coefficient=C, exponent=m, velocity_regularization=1e-12), tau0, N0)
     assert it < 300
@@ -379,7 +379,7 @@ def test_sliding_slab(backend):
 
 
 def test_diagonal_preconditioner_is_operator_diagonal(backend):
-    """test/test_friction.jl:247-258: z = r / diag with the diagonal probed by unit vectors."""
+    """test/test_friction.jl:83-95: z = r / diag with the diagonal probed by unit vectors."""
     Nx, Ny = 7, 6
     xs = list(np.linspace(0, 1, Nx + 1) ** 1.4)
     g = grid((Nx, Ny), x=xs)
@@ -400,7 +400,7 @@ def test_diagonal_preconditioner_is_operator_diagonal(backend):
 
 
 def test_jacobi_beats_plain_cg(backend):
-    """test/test_friction.jl:260-274."""
+    """test/test_friction.jl:97-110."""
     g = grid((48, 32), topology=("Bounded", "Periodic"))
     control = M.Convergence(reltol=1e-10, maxiter=10_000)
     res = {}

@@ -162,7 +162,7 @@ def test_diva_slab(backend):
 
 
 def test_grounded_fraction_and_effective_pressure(backend):
-    """test/test_grounding.jl:72-125."""
+    """test/test_grounding.jl:14-67."""
     g = grid((16, 2), x=(0.0, 16.0), y=(0.0, 2.0), topology=("Bounded", "Periodic"))
     c = M.IceSheetConstants()
     ri, rw, gg, H0 = c.ice_density, c.ocean_density, c.gravitational_acceleration, 1000.0
@@ -201,7 +201,7 @@ def test_grounded_fraction_and_effective_pressure(backend):
 
 
 def test_grounding_line_split_driving_stress(backend):
-    """test/test_grounding.jl:127-172."""
+    """test/test_grounding.jl:69-114."""
     ri, rw, gg, D = 918.0, 1028.0, 9.81, 1e3
     c = M.IceSheetConstants(ri, rw, gg)
     for Nx, Ny, xgl in ((16, 2, 7.3e3), (2, 16, 7.3e3)):
@@ -252,7 +252,7 @@ def test_calving_front_force(backend):
 
 
 def test_confined_shelf_spreading(backend):
-    """test/test_calving_front.jl:195-212."""
+    """test/test_calving_front.jl:23-40."""
     L, xf, H0, A, Nx = 64e3, 40e3, 500.0, 1e-24, 32
     g = grid((Nx, 4), x=(0.0, L), y=(0.0, 4 * L / Nx), halo=(4, 4))
     solver = M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-12, maxiter=10_000),
@@ -271,7 +271,7 @@ def test_confined_shelf_spreading(backend):
 
 
 def test_steady_shelf_second_order(backend):
-    """test/test_calving_front.jl:214-238."""
+    """test/test_calving_front.jl:42-66."""
     L, xf, H0, A, n = 256e3, 192e3, 1e3, 1e-25, 3
     q = H0 * 1e-5
     c = M.IceSheetConstants()
@@ -296,7 +296,7 @@ def test_steady_shelf_second_order(backend):
 
 
 def test_smooth_ice_mask_values(backend):
-    """test/test_ice_mask.jl:266-275 through compute_ice_mask!."""
+    """test/test_ice_mask.jl:27-36 through compute_ice_mask!."""
     g = grid((5, 1), x=(0.0, 5.0), topology=("Bounded", "Periodic"))
     Hs = [10.0, 30.0, 20.0, 10.0 + 1e-6, 30.0 - 1e-6]
     P, _ = ice_sheet_model(backend, g, H=lambda x, y: Hs[int(x)], masking=M.SmoothIceMask(10.0, 20.0), solve=False)
@@ -307,7 +307,7 @@ def test_smooth_ice_mask_values(backend):
 
 
 def test_ice_free_points_decoupled(backend):
-    """test/test_ice_mask.jl:277-300."""
+    """test/test_ice_mask.jl:38-61."""
     Nx, Ny = 8, 6
     g = grid((Nx, Ny), topology=("Bounded", "Periodic"))
     ice = lambda x, y: 1.0 if x < 0.5 else 0.0
@@ -339,7 +339,7 @@ def test_ice_free_points_decoupled(backend):
 
 @pytest.mark.parametrize("H_edge", [0.0, 0.5])
 def test_ice_cap_with_ice_free_margins(backend, H_edge):
-    """test/test_ice_mask.jl:302-318."""
+    """test/test_ice_mask.jl:63-79."""
     P, st = ice_cap(backend, H_edge=H_edge)
     mu = P.get("ice_mask")
     assert np.count_nonzero(mu == 0) > 0
