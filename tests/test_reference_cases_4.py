@@ -1,5 +1,5 @@
-"""The checks of the reference's conjugate-gradient testset (test/test_conjugate_gradient.jl:7-54), restated on
-the library's own linear operation.
+"""The checks of the reference's conjugate-gradient testset (test/test_conjugate_gradient.jl:7-54) and the three
+doctests of src/Solvers/conjugate_gradient.jl, restated on the library's own linear operation.
 
 The reference runs them on toy_operator! (test/toy_problems.jl:6-21: identity plus a weighted graph Laplacian on
 an 8 x 8 Periodic x Periodic grid).  The library's solver has exactly one linear operation, the SSA operator, so
@@ -83,6 +83,44 @@ def test_jacobi_preconditioned_solve_equals_plain(backend):
     pu, pv, st = _solve(toy_problem(backend, preconditioner=M.StressBalanceDiagonalPreconditioner()), bu, bv)
     assert st.status == 0 and 0 < st.linear_iterations_last < 500
     assert isapprox(pu, xu, rtol=RTOL_APPROX) and isapprox(pv, xv, rtol=RTOL_APPROX)
+
+
+# ---- doctests of src/Solvers/conjugate_gradient.jl on a 4 x 4 Periodic x Periodic grid --------------------
+# The doctests use a stored diagonal 2 and the operator double!(q, p) = 2p.  The SSA operator reproduces both
+# exactly on that grid: with η̄H = η̄Hᶠᶠ = 1/8 and Az β = 3/4 its diagonal is 3/4 + 2 (4 Δy η̄H / Δx) +
+# 2 (Δx η̄Hᶠᶠ / Δy) = 2, and with Az β = 2 it maps every constant vector to twice itself (the strain rates of a
+# constant field are zero), so one CG iteration from zero reaches x = b / 2 exactly.  Every number involved
+# is a power of two or a small sum of them, so the answers are exact, as in the doctests.
+
+def _doctest_problem(cls, eta, beta, preconditioner=None):
+    g = M.RectilinearGrid(size=(4, 4), x=(0.0, 1.0), y=(0.0, 1.0), topology=("Periodic", "Periodic"), halo=(3, 3))
+    solver = M.StressBalanceSolver(preconditioner=preconditioner)
+    P = make(cls, g, stress_balance=M.DepthIntegrated(side_walls=M.FreeSlipWalls()), masking=None, velocity_solver=solver)
+    for name in ("eta_H", "eta_H_ff"):
+        P.set(name, eta)
+    for name in ("beta_u", "beta_v"):
+        P.set(name, beta)
+    return P
+
+
+def test_jacobi_precondition_doctest(backend):
+    """src/Solvers/conjugate_gradient.jl:18-32: z = r / diagonal with r = 3 and diagonal 2 gives 1.5."""
+    P = _doctest_problem(backend, 0.125, 12.0, preconditioner=M.StressBalanceDiagonalPreconditioner())
+    zu, zv = P.precondition(np.full(P.shape("u"), 3.0), np.full(P.shape("v"), 3.0))
+    assert (zu.min(), zu.max()) == (1.5, 1.5) and (zv.min(), zv.max()) == (1.5, 1.5)
+
+
+def test_solve_and_adjoint_solve_doctests(backend):
+    """src/Solvers/conjugate_gradient.jl:107-126 (solve!) and :133-153 (adjoint_solve!): A = 2I, b = 1 gives
+    x = λ = 0.5 everywhere, starting from zero."""
+    P = _doctest_problem(backend, 0.125, 32.0)
+    one_u, one_v = np.ones(P.shape("u")), np.ones(P.shape("v"))
+    qu, qv = P.apply_operator(one_u, one_v)
+    assert np.all(qu == 2.0) and np.all(qv == 2.0)
+    for adjoint in (False, True):
+        xu, xv, st = _solve(P, one_u, one_v, adjoint=adjoint)
+        assert st.status == 0 and st.linear_iterations_last == 1
+        assert (xu.min(), xu.max()) == (0.5, 0.5) and (xv.min(), xv.max()) == (0.5, 0.5)
 
 
 def test_fixed_picard_around_fixed_cg_reports_the_linear_count(backend):
