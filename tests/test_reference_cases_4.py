@@ -104,14 +104,14 @@ def _doctest_problem(cls, eta, beta, preconditioner=None):
 
 
 def test_jacobi_precondition_doctest(backend):
-    """src/Solvers/conjugate_gradient.jl:18-32: z = r / diagonal with r = 3 and diagonal 2 gives 1.5."""
+    """src/Solvers/conjugate_gradient.jl:18-31: z = r / diagonal with r = 3 and diagonal 2 gives 1.5."""
     P = _doctest_problem(backend, 0.125, 12.0, preconditioner=M.StressBalanceDiagonalPreconditioner())
     zu, zv = P.precondition(np.full(P.shape("u"), 3.0), np.full(P.shape("v"), 3.0))
     assert (zu.min(), zu.max()) == (1.5, 1.5) and (zv.min(), zv.max()) == (1.5, 1.5)
 
 
 def test_solve_and_adjoint_solve_doctests(backend):
-    """src/Solvers/conjugate_gradient.jl:107-126 (solve!) and :133-153 (adjoint_solve!): A = 2I, b = 1 gives
+    """src/Solvers/conjugate_gradient.jl:109-126 (solve!) and :136-153 (adjoint_solve!): A = 2I, b = 1 gives
     x = λ = 0.5 everywhere, starting from zero."""
     P = _doctest_problem(backend, 0.125, 32.0)
     one_u, one_v = np.ones(P.shape("u")), np.ones(P.shape("v"))
