@@ -15,6 +15,7 @@ Reference constructors mirrored (file:line in Nunatak.jl):
                                        coarsest_sweeps = 20, minimum_coarse_size = 2)   src/StressBalances/multigrid_preconditioner.jl:57
   StressBalanceSolver(grid; linear_iteration_control = Convergence(reltol = 1e-8, maxiter = 10_000),
                       picard_iteration_control = Convergence(reltol = 1e-6, maxiter = 100),
+                      adjoint_iteration_control = picard_iteration_control,
                       preconditioner = StressBalanceDiagonalPreconditioner())     src/StressBalances/stress_balance_solver.jl:43-52
 """
 import ctypes as C
@@ -200,14 +201,24 @@ class StressBalanceSolver:
     picard_iteration_control: object = field(default_factory=lambda: Convergence(reltol=1e-6, maxiter=100))
     preconditioner: object = field(default_factory=StressBalanceDiagonalPreconditioner)   # None = no preconditioner
     precision: str = "fp64"             # "fp64" or "mixed" (FP32 multigrid under FP64 outer iterations)
+    adjoint_iteration_control: object = None   # stops the fixed-point adjoint; None = picard_iteration_control
+
+    @property
+    def adjoint_control(self):
+        """The control of the fixed-point adjoint of converged Picard iterations; like the reference's
+        `adjoint_iteration_control = picard_iteration_control` default it falls back to the Picard control."""
+        c = self.adjoint_iteration_control
+        return self.picard_iteration_control if c is None else c
 
 
 # ---- descriptors ------------------------------------------------------------------------------------
 class Descriptors:
-    """C descriptors plus the arrays their pointers refer to (kept alive with the object)."""
+    """C descriptors plus the arrays their pointers refer to (kept alive with the object).  `adjoint_control`
+    is the StressBalanceSolver's adjoint iteration control, the default of Problem.picard_adjoint."""
 
-    def __init__(self, grid, physics, solver, keep):
+    def __init__(self, grid, physics, solver, keep, adjoint_control=None):
         self.grid, self.physics, self.solver, self._keep = grid, physics, solver, keep
+        self.adjoint_control = adjoint_control
 
 
 def _as_ptr(a):
@@ -298,7 +309,7 @@ def make_descriptors(grid: RectilinearGrid, Nsigma=10, bed_refinement=2.0, sigma
         s.smoother, s.smoothing_sweeps, s.coarsest_sweeps, s.minimum_coarse_size = 0, 2, 20, 2
     s.linear = velocity_solver.linear_iteration_control.desc()
     s.picard = velocity_solver.picard_iteration_control.desc()
-    return Descriptors(g, p, s, keep)
+    return Descriptors(g, p, s, keep, velocity_solver.adjoint_control)
 
 
 def field_shape(grid: RectilinearGrid, name: str, Nsigma: int, rate_layout_sigma=False):

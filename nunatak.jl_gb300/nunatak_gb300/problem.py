@@ -214,7 +214,10 @@ class Problem:
     def picard_adjoint(self, ubar, vbar, control=None):
         """Fixed-point adjoint of the converged picard_solve! (the reverse rule of ext/NunatakEnzymeExt.jl:167-240)
         for x̄ = (ubar, vbar) = ∂J/∂(u, v): returns (λu, λv, ∂J/∂log C per cell, ∂J/∂log A in the layout of the rate
-        factor, stats), λ being ∂J/∂τ.  `control` is a Convergence / FixedIterations (default: the Picard control)."""
+        factor, stats), λ being ∂J/∂τ.  `control` is a Convergence / FixedIterations (default: the solver's
+        adjoint_iteration_control, which itself defaults to the Picard control)."""
+        if control is None:
+            control = getattr(self.desc, "adjoint_control", None)
         ub, vb = self._vec_in(ubar, vbar)
         lu, lv = np.empty(self.shape("u")), np.empty(self.shape("v"))
         grad = np.empty((self.grid.Ny, self.grid.Nx))

@@ -16,6 +16,7 @@ The reference's zero-allocation check (:51-53) has its counterpart in nk_picard_
 import math
 
 import numpy as np
+import pytest
 
 from nunatak_gb300 import model as M
 from nunatak_gb300 import workloads
@@ -132,3 +133,76 @@ def test_fixed_picard_around_fixed_cg_reports_the_linear_count(backend):
     assert (st.picard_iterations, st.linear_iterations_last, st.linear_iterations_total) == (3, 4, 12)
     st = P.picard_solve()   # a second call with the same workspaces counts the same way
     assert (st.picard_iterations, st.linear_iterations_last, st.linear_iterations_total) == (3, 4, 12)
+
+
+# ---- constructor doctests of the configuration objects (host side, no device) ---------------------------
+
+def test_configuration_doctests():
+    """The reference's constructor doctests, on the host-side mirrors of its configuration objects:
+    Convergence(; reltol = 1e-10, maxiter = 50) = (1e-10, 0, 50) (src/Solvers/iteration_controls.jl:21-26);
+    DepthIntegrated(side_walls = NoSlipWalls()) is SSA with no-slip walls (src/StressBalances/depth_integrated.jl:22-27);
+    WeertmanFriction(grid; coefficient = 3e4).exponent = 1/3 (src/Frictions/frictions.jl:23-32);
+    GlenFlowLaw(grid; rate_factor = 1e-24).exponent = 3 (src/Rheologies/glen_flow_law.jl:25-34);
+    IceSheetConstants(grid) has ρw/ρᵢ = 1.1198257080610021 (src/Models/ice_sheet_constants.jl:22-31);
+    the adjoint control defaults to the Picard control (src/Solvers/picard.jl:27-34,
+    src/StressBalances/stress_balance_solver.jl:46); the solver's linear control is the one given
+    (src/Solvers/conjugate_gradient.jl:80-91, src/StressBalances/stress_balance_solver.jl:29-41 for the Picard one)."""
+    c = M.Convergence(reltol=1e-10, maxiter=50)
+    assert (c.reltol, c.abstol, c.maxiter) == (1e-10, 0.0, 50)
+    d = M.DepthIntegrated(side_walls=M.NoSlipWalls())
+    assert d.shear is None and isinstance(d.side_walls, M.NoSlipWalls)
+    assert M.WeertmanFriction(coefficient=3e4).exponent == 0.3333333333333333
+    assert M.GlenFlowLaw(rate_factor=1e-24).exponent == 3.0
+    k = M.IceSheetConstants()
+    assert k.ocean_density / k.ice_density == 1.1198257080610021
+    s = M.StressBalanceSolver(picard_iteration_control=M.Convergence(reltol=1e-8))
+    assert s.adjoint_control == M.Convergence(reltol=1e-8, abstol=0.0, maxiter=1000)
+    assert M.StressBalanceSolver(picard_iteration_control=M.FixedIterations(5)).picard_iteration_control == M.FixedIterations(5)
+    assert M.StressBalanceSolver(linear_iteration_control=M.FixedIterations(2)).linear_iteration_control == M.FixedIterations(2)
+    desc = M.make_descriptors(toy_grid(), velocity_solver=M.StressBalanceSolver(adjoint_iteration_control=M.FixedIterations(7)))
+    assert desc.adjoint_control == M.FixedIterations(7)
+
+
+def test_velocity_vector_doctest(backend):
+    """src/Solvers/velocity_vector.jl:22-31: on a 4 x 3 Periodic x Bounded grid u holds 4 x 3 and v 4 x 4 values."""
+    g = M.RectilinearGrid(size=(4, 3), x=(0.0, 1.0), y=(0.0, 1.0), topology=("Periodic", "Bounded"), halo=(3, 3))
+    P = make(backend, g, masking=None)
+    assert P.shape("u") == (3, 4) and P.shape("v") == (4, 4)   # numpy (y, x) order
+    assert P.get("u").shape == (3, 4) and P.get("v").shape == (4, 4)
+
+
+def test_smooth_ice_mask_doctest(backend):
+    """src/Models/smooth_ice_mask.jl:23-39: minimum 1, transition 2 gives μ = 0, 0, 0.5, 1, 1 for
+    H = 0.5, 1, 2, 3, 10."""
+    g = M.RectilinearGrid(size=(5, 1), x=(0.0, 5.0), y=(0.0, 1.0), topology=("Bounded", "Periodic"), halo=(3, 3))
+    Hs = [0.5, 1.0, 2.0, 3.0, 10.0]
+    P = make(backend, g, masking=M.SmoothIceMask(minimum_thickness=1.0, transition_thickness=2.0))
+    P.set("H", np.array([Hs]))
+    P.set("bed", 0.0)
+    P.compute_geometry()
+    assert P.get("ice_mask")[0].tolist() == [0.0, 0.0, 0.5, 1.0, 1.0]
+
+
+@pytest.mark.gpu
+def test_picard_adjoint_defaults_to_the_solver_adjoint_control(gpu_cls):
+    """StressBalanceSolver(adjoint_iteration_control = ...) sets the control of Problem.picard_adjoint when none
+    is passed (the reference's PicardIteration keeps it beside the forward control); an explicit control wins.
+    The 40 x 20 marine sheet with Weertman drag of the adjoint finite-difference tests."""
+    def run(adjoint_control, explicit=None):
+        solver = M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-13, maxiter=20_000),
+                                       picard_iteration_control=M.Convergence(reltol=1e-12, maxiter=500),
+                                       preconditioner=M.StressBalanceDiagonalPreconditioner(),
+                                       adjoint_iteration_control=adjoint_control)
+        P = workloads.marine_sheet(40, 20, seed=2, seed_friction=1100, velocity_solver=solver).problem(gpu_cls)
+        assert P.picard_solve().status == 0
+        lu, _, _, _, st = P.picard_adjoint(1e-3 * P.get("u"), 1e-3 * P.get("v"), explicit)
+        P.close()
+        return lu, st
+    _, st = run(M.FixedIterations(4))
+    assert st.picard_iterations == 4
+    _, st = run(M.FixedIterations(4), explicit=M.FixedIterations(2))
+    assert st.picard_iterations == 2
+    l_default, st_default = run(None)
+    l_picard, st_picard = run(None, explicit=M.Convergence(reltol=1e-12, maxiter=500))
+    assert st_default.status == 0 and st_default.picard_iterations == st_picard.picard_iterations
+    assert np.array_equal(l_default, l_picard)
