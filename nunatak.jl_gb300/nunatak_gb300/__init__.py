@@ -7,7 +7,7 @@ from .model import (YEAR, Convergence, DepthIntegrated, DIVAShear, FixedIteratio
                     IceSheetConstants, LineJacobi, NoSlipWalls, PointJacobi, RectilinearGrid,
                     RegularizedCoulombFriction, SmoothIceMask, StressBalanceDiagonalPreconditioner,
                     StressBalanceMultigridPreconditioner, StressBalanceSolver, SubgridGroundedFraction,
-                    ViscosityConvergence, WeertmanFriction, make_descriptors, field_shape)
+                    ViscosityConvergence, WeertmanFriction, make_descriptors, field_shape, sigma_faces)
 from .problem import NunatakError, Problem
 
 __all__ = [
@@ -15,6 +15,6 @@ __all__ = [
     "IceSheetConstants", "LineJacobi", "NoSlipWalls", "PointJacobi", "RectilinearGrid", "RegularizedCoulombFriction",
     "SmoothIceMask", "StressBalanceDiagonalPreconditioner", "StressBalanceMultigridPreconditioner",
     "StressBalanceSolver", "SubgridGroundedFraction", "ViscosityConvergence", "WeertmanFriction", "make_descriptors",
-    "field_shape",
+    "field_shape", "sigma_faces",
     "NunatakError", "Problem",
 ]

@@ -77,6 +77,13 @@ class RectilinearGrid:
         return nx, ny
 
 
+def sigma_faces(Nsigma, bed_refinement=2):
+    """sigma_faces(Nσ; bed_refinement = 2) (src/Grids/sigma_grid.jl:20-22): the Nσ + 1 faces (k / Nσ)^bed_refinement
+    of the normalised height above the bed, the rule nk_problem_create applies when nk_grid_desc.sigma_faces is
+    NULL."""
+    return [(k / Nsigma) ** bed_refinement for k in range(Nsigma + 1)]
+
+
 # ---- iteration controls ---------------------------------------------------------------------------
 @dataclass
 class Convergence:

@@ -72,3 +72,42 @@ def isapprox(a, b, rtol=1.4901161193847656e-08, atol=0.0):
     a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
     d = np.linalg.norm((a - b).ravel())
     return d <= max(atol, rtol * max(np.linalg.norm(a.ravel()), np.linalg.norm(b.ravel())))
+
+
+# ---- the reference's doctests as golden values (tests/golden/reference_doctests.json) -------------------------
+
+_DOCTESTS = None
+
+
+def reference_doctests():
+    """Every doctest block of the reference's velocity-solve sources, as extracted from its text by
+    tests/golden/make_reference_doctests.py: [{"file", "lines": [first, last], "steps": [{"input", "output"}]}]."""
+    global _DOCTESTS
+    if _DOCTESTS is None:
+        import json
+        import os
+        path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_doctests.json")
+        with open(path, encoding="utf-8") as f:
+            _DOCTESTS = json.load(f)["doctests"]
+    return _DOCTESTS
+
+
+def reference_doctest(file, first_line):
+    """The printed outputs, in order, of the doctest whose opening fence is at file:first_line."""
+    for d in reference_doctests():
+        if d["file"] == file and d["lines"][0] == first_line:
+            return [s["output"] for s in d["steps"] if s["output"]]
+    raise KeyError(f"no doctest at {file}:{first_line}")
+
+
+def julia_value(text):
+    """A value as Julia prints it: a number, a tuple (nested tuples of numbers) or an `n-element Vector{T}:`
+    listing, as Python floats, tuples and lists."""
+    import ast
+    text = text.strip()
+    if "-element Vector" in text:
+        return [float(line) for line in text.split("\n")[1:]]
+    value = ast.literal_eval(text)
+    if isinstance(value, tuple):
+        return tuple(julia_value(repr(v)) if isinstance(v, tuple) else float(v) for v in value)
+    return float(value)

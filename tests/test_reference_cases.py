@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from nunatak_gb300 import model as M
-from support import evaluate, ice_sheet_model, isapprox, make, set_fn, vector_dot
+from support import evaluate, ice_sheet_model, isapprox, julia_value, make, reference_doctest, set_fn, vector_dot
 
 
 def grid(size, x=(0.0, 1.0), y=(0.0, 1.0), topology=("Bounded", "Bounded"), halo=(3, 3)):
@@ -30,27 +30,29 @@ def apply(P, pu, pv):
 
 
 # ---- doctests ---------------------------------------------------------------------------------------
+# The expected values are the doctests' printed outputs, read from tests/golden/reference_doctests.json.
 
 def test_ssa_operator_doctest(backend):
     """src/StressBalances/ssa_operator.jl:20-45: rigid translation feels only the drag, 2 × 3 × (1/4)² = 0.375."""
     g = grid((4, 4), topology=("Periodic", "Periodic"))
     P = coefficients_problem(backend, g, eta=1.0, beta=2.0)
     qu, qv = apply(P, 3.0, 0.0)
-    assert qu[0, 0] == 0.375
+    assert qu[0, 0] == julia_value(reference_doctest("src/StressBalances/ssa_operator.jl", 20)[0])   # 0.375
 
 
 def test_driving_stress_doctests(backend):
     """src/StressBalances/driving_stress.jl:13-41."""
     g = grid((4, 4))
+    expected = [julia_value(o) for o in reference_doctest("src/StressBalances/driving_stress.jl", 13)]
     c = M.IceSheetConstants(1.0, 1.0, 1.0)
     # s = x with H = 1 and no grounding treatment: s = b + H, so b = x - 1.
     P, _ = ice_sheet_model(backend, g, H=1.0, bed=lambda x, y: x - 1, masking=None, constants=c, solve=False)
-    assert P.get("tau_u")[0, 1] == -0.0625
+    assert P.get("tau_u")[0, 1] == expected[0]   # -0.0625
     # Grounding line inside the face: b = -2x, H = 2 - 2x, s = max(2 - 4x, 1 - x) with ρw = 2.
     c2 = M.IceSheetConstants(1.0, 2.0, 1.0)
     P, _ = ice_sheet_model(backend, g, H=lambda x, y: 2 - 2 * x, bed=lambda x, y: -2 * x, masking=None, constants=c2,
                            grounding=M.SubgridGroundedFraction(driving_stress=True), solve=False)
-    assert abs(P.get("tau_u")[0, 1] - 0.33463541666666663) < 1e-15
+    assert abs(P.get("tau_u")[0, 1] - expected[1]) < 1e-15   # 0.33463541666666663
 
 
 def test_viscosity_doctest(backend):
@@ -59,7 +61,7 @@ def test_viscosity_doctest(backend):
     P = make(backend, g, Nsigma=3, rheology=M.GlenFlowLaw(rate_factor=1.0, exponent=1.0), masking=None)
     P.set("A", 1.0)
     P.update_coefficients()
-    assert P.get("eta_sigma")[0, 0, 0] == 0.5
+    assert P.get("eta_sigma")[0, 0, 0] == julia_value(reference_doctest("src/Rheologies/glen_flow_law.jl", 78)[0])   # 0.5
 
 
 def test_basal_drag_doctest(backend):
@@ -73,7 +75,7 @@ def test_basal_drag_doctest(backend):
     P.set("phi_v", 1.0)
     P.set("u", 1.0)
     P.update_coefficients()
-    assert P.get("beta_u")[0, 1] == 2.0
+    assert P.get("beta_u")[0, 1] == julia_value(reference_doctest("src/Frictions/frictions.jl", 102)[0])   # 2.0
 
 
 def test_grounded_fraction_doctest(backend):
@@ -82,7 +84,7 @@ def test_grounded_fraction_doctest(backend):
     c = M.IceSheetConstants(1.0, 1.0, 9.81)
     P, _ = ice_sheet_model(backend, g, H=100.0, bed=lambda x, y: -100 * (x - 0.75), constants=c,
                            grounding=M.SubgridGroundedFraction(), solve=False)
-    np.testing.assert_array_equal(P.get("phi")[0], [1.0, 0.75, 0.0, 0.0])
+    np.testing.assert_array_equal(P.get("phi")[0], julia_value(reference_doctest("src/Groundings/subgrid_grounded_fraction.jl", 82)[0]))
 
 
 def test_effective_pressure_and_surface_doctests(backend):
@@ -90,17 +92,19 @@ def test_effective_pressure_and_surface_doctests(backend):
     g = grid((2, 1), x=(0.0, 2.0), topology=("Bounded", "Periodic"))
     P, _ = ice_sheet_model(backend, g, H=10.0, bed=lambda x, y: 5.0 if x < 1 else -5.0,
                            constants=M.IceSheetConstants(1.0, 1.0, 1.0), grounding=M.SubgridGroundedFraction(), solve=False)
-    np.testing.assert_array_equal(P.get("N")[0], [10.0, 5.0])
+    np.testing.assert_array_equal(P.get("N")[0], julia_value(reference_doctest("src/Groundings/subgrid_grounded_fraction.jl", 149)[0]))
     P, _ = ice_sheet_model(backend, g, H=100.0, bed=lambda x, y: -20.0 if x < 1 else -500.0,
                            constants=M.IceSheetConstants(1.0, 2.0, 9.81), grounding=M.SubgridGroundedFraction(), solve=False)
-    np.testing.assert_array_equal(P.get("s")[0], [80.0, 50.0])
+    np.testing.assert_array_equal(P.get("s")[0], julia_value(reference_doctest("src/Groundings/subgrid_grounded_fraction.jl", 192)[0]))
 
 
 def test_multigrid_levels(backend):
     """src/StressBalances/multigrid_preconditioner.jl:41-55 and test/test_multigrid_preconditioner.jl:30-37."""
     mg = M.StressBalanceSolver(preconditioner=M.StressBalanceMultigridPreconditioner())
-    cases = [((32, 16), ("Bounded", "Periodic"), (3, 3), [(16, 8), (8, 4), (4, 4)]),
-             ((64, 4), ("Bounded", "Bounded"), (4, 4), [(32, 4), (16, 4), (8, 4), (4, 4)]),
+    doc = [[(int(nx), int(ny)) for nx, ny, _ in julia_value(o)]
+           for o in reference_doctest("src/StressBalances/multigrid_preconditioner.jl", 41)]
+    cases = [((32, 16), ("Bounded", "Periodic"), (3, 3), doc[0]),     # (16, 8), (8, 4), (4, 4)
+             ((64, 4), ("Bounded", "Bounded"), (4, 4), doc[1]),       # (32, 4), (16, 4), (8, 4), (4, 4)
              ((15, 8), ("Bounded", "Periodic"), (3, 3), [(15, 4)]),
              ((15, 5), ("Bounded", "Periodic"), (3, 3), [])]
     for size, topo, halo, levels in cases:
@@ -109,14 +113,14 @@ def test_multigrid_levels(backend):
 
 
 def test_arrhenius_doctest(backend):
-    """src/Rheologies/arrhenius_rate_factor.jl:89-101: A(253.15 K, ω = 0) ≈ 1.5e-25 (3 significant digits)."""
+    """src/Rheologies/arrhenius_rate_factor.jl:89-100: A(253.15 K, ω = 0) ≈ 1.5e-25 (3 significant digits)."""
     g = grid((2, 2))
     P = make(backend, g, Nsigma=2, rheology=M.GlenFlowLaw(rate_factor="sigma"))
     P.set("H", 0.0)          # zero pressure, so T′ = T
     P.set("T", 253.15)
     P.compute_rate_factor()
     A = P.get("A")
-    assert float(f"{A[0, 0, 0]:.2e}") == 1.5e-25
+    assert float(f"{A[0, 0, 0]:.2e}") == julia_value(reference_doctest("src/Rheologies/arrhenius_rate_factor.jl", 89)[0])
 
 
 # ---- SSA operator (test/test_ssa_operator.jl) --------------------------------------------------------
