@@ -3,9 +3,10 @@ tests/golden/make_oracle_solves.py from the FP64 oracle; cases in tests/golden_c
 
 - The oracle reproduces every fixture bit for bit (it is deterministic: row sums in a fixed order, no
   floating-point contraction), so a change of the oracle cannot go unnoticed.
-- The GPU library reproduces every fixture within 1e-10 (relative L2 per field): each case runs Picard and CG
-  with fixed iteration counts, so the two differ by rounding only (the tolerance of the fixed-count parity
-  tests)."""
+- The GPU library reproduces every fixture: each case runs Picard and CG with fixed iteration counts, so the two
+  differ by rounding only.  Velocities within 1e-10 relative L2 over each velocity pair ((u, v) and
+  (u_sigma, v_sigma), the measure of the fixed-count parity tests) and u_b on its own; the coefficients of the
+  last Picard update (η̄H, β, ησ) within 1e-9 per field."""
 import os
 
 import numpy as np
@@ -14,7 +15,9 @@ import pytest
 import golden_cases
 
 FIXTURES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "oracle_solves.npz")
-RTOL_GPU = 1e-10
+RTOL_VELOCITY = 1e-10
+RTOL_COEFFICIENT = 1e-9
+PAIRS = {"u": ("u", "v"), "v": ("u", "v"), "u_sigma": ("u_sigma", "v_sigma"), "v_sigma": ("u_sigma", "v_sigma")}
 
 
 def _fixture(name):
@@ -43,5 +46,8 @@ def test_gpu_matches_golden_solves(gpu_cls, name):
     got, want = golden_cases.solve(name, gpu_cls), _fixture(name)
     for k, w in want.items():
         assert got[k].shape == w.shape, (name, k)
-        err = np.linalg.norm((got[k] - w).ravel()) / np.linalg.norm(w.ravel())
-        assert err <= RTOL_GPU, (name, k, err)
+        group = PAIRS.get(k, (k,))
+        scale = np.sqrt(sum(np.sum(want[m] ** 2) for m in group))
+        err = np.linalg.norm((got[k] - w).ravel()) / scale
+        tol = RTOL_VELOCITY if k in PAIRS or k == "u_b" else RTOL_COEFFICIENT
+        assert err <= tol, (name, k, err)
