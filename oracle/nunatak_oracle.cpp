@@ -1079,6 +1079,251 @@ static void velocity_profile(Problem& P) {
     }
 }
 
+// ------------------------------------------------------------------------------------------------
+// Fixed-point adjoint of a converged SSA picard_solve! (the reverse rule of ext/NunatakEnzymeExt.jl:159-240,
+// with picard_coefficient_step! :142-146 and picard_step_adjoint! :148-157).  One Picard step maps x to
+// A(c(x))⁻¹ b.  At its fixed point x* the adjoint λ solves λ = A⁻ᵀ (x̄ + ȳ(λ)), ȳ = -(∂[A(c(x)) x*]/∂x)ᵀ λ,
+// iterated from λ = 0 with the problem's CG warm-started from the previous λ until
+// ‖λ⁺ - λ‖ ≤ max(reltol ‖λ⁺‖, abstol).  Then b̄ = λ and p̄ = -(∂[A(c(p)) x*]/∂p)ᵀ λ for p = log C, log A.
+//
+// The transposes below are written as reverse-mode sweeps over the forward functions of this file, in their
+// representation: every forward read of an input accumulates the adjoint into that input, reads of halo cells
+// included, and fill_halo_adjoint then returns each halo cell's adjoint to the cell fill_halo copied it from.
+// G fields hold λ-signed sensitivities ∂(λᵀ q)/∂(·) with q = A(c) x* over the operator's active rows.
+// ------------------------------------------------------------------------------------------------
+
+// The transpose of fill_halo: the assignments run backwards, each adding the target's adjoint to its source and
+// clearing the target.  Halo cells that fill_halo leaves alone (Face locations in a Bounded direction) hold
+// constants, so their adjoints are dropped.
+static void fill_halo_adjoint(Field& f) {
+    const Grid& g = *f.g;
+    int Hx = g.x.H + 1, Hy = g.y.H + 1;
+    int Nx = g.x.N, Ny = g.y.N;
+    int nxi = f.nx(), nyi = f.ny();
+    for (int i = Nx + 1 + Hx - 1; i >= -Hx; --i) {
+        if (g.y.periodic) {
+            for (int m = Hy; m >= 1; --m) {
+                f(i, m) += f(i, Ny + m); f(i, Ny + m) = 0;
+                f(i, Ny + 1 - m) += f(i, 1 - m); f(i, 1 - m) = 0;
+            }
+        } else if (f.ly == CENTER) {
+            for (int m = Hy; m >= 1; --m) {
+                f(i, Ny) += f(i, Ny + m); f(i, Ny + m) = 0;
+                f(i, 1) += f(i, 1 - m); f(i, 1 - m) = 0;
+            }
+        }
+    }
+    for (int j = nyi; j >= 1; --j) {
+        if (g.x.periodic) {
+            for (int m = Hx; m >= 1; --m) {
+                f(m, j) += f(Nx + m, j); f(Nx + m, j) = 0;
+                f(Nx + 1 - m, j) += f(1 - m, j); f(1 - m, j) = 0;
+            }
+        } else if (f.lx == CENTER) {
+            for (int m = Hx; m >= 1; --m) {
+                f(Nx, j) += f(Nx + m, j); f(Nx + m, j) = 0;
+                f(1, j) += f(1 - m, j); f(1 - m, j) = 0;
+            }
+        }
+    }
+    // what is left outside the interior sits on cells that are never copied into: constants
+    for (int j = -(g.y.H + 2); j < f.sy - (g.y.H + 2); ++j)
+        for (int i = -(g.x.H + 2); i < f.sx - (g.x.H + 2); ++i)
+            if (i < 1 || i > nxi || j < 1 || j > nyi) f(i, j) = 0;
+}
+
+// basal_drag and its derivatives with respect to the speed U and the face coefficient C (frictions.jl:83-89):
+// Weertman β = C U^(m-1); regularised Coulomb β = C U^(m-1) τc / (C^(1/m) U + τc^(1/m))^m, τc = α² N.
+static void basal_drag_and_derivatives(double U, double C, double N, const Physics& ph, double& b, double& dU, double& dC) {
+    b = basal_drag(U, C, N, ph);
+    if (ph.friction == NK_WEERTMAN) {
+        dU = (ph.m - 1) * b / U;
+        dC = std::pow(U, ph.m - 1);
+        return;
+    }
+    if (b == 0.0) { dU = 0.0; dC = 0.0; return; }
+    double cm = std::pow(C, 1 / ph.m), den = cm * U + std::pow(ph.alpha2 * N, 1 / ph.m);
+    dU = b * ((ph.m - 1) / U - ph.m * cm / den);
+    dC = b * (1 / C - cm * U / (C * den));
+}
+
+struct AdjointSweep {   // the G fields of one reverse sweep
+    VelocityVector x;             // ∂(λᵀq)/∂x through the coefficients (x* frozen in the product)
+    Field eta, ff, bu, bv, C;     // ∂(λᵀq)/∂η̄H, ∂/∂η̄Hᶠᶠ, ∂/∂βᵘ, ∂/∂βᵛ, ∂/∂C
+    SigmaField logA;              // ∂(λᵀq)/∂log A per layer
+    void init(const Grid* g, int Ns) {
+        x.init(g);
+        eta.init(g, CENTER, CENTER); ff.init(g, FACE, FACE); bu.init(g, FACE, CENTER); bv.init(g, CENTER, FACE);
+        C.init(g, CENTER, CENTER);
+        logA.init(g, CENTER, CENTER, Ns);
+    }
+    void zero() {
+        x.u.zero(); x.v.zero(); eta.zero(); ff.zero(); bu.zero(); bv.zero(); C.zero();
+        for (auto& f : logA.k) f.zero();
+    }
+};
+
+// One reverse sweep of q = A(c(x)) x* for the seed λ (halos of λ filled): the operator (ssa_operator.jl:60-89),
+// fill_halo(η̄Hᶠᶠ), _interpolate_to_corners!, fill_halo(η̄H), compute_column_integrals!, compute_viscosity!
+// (membrane, wall-masked strain rates) and compute_basal_drag!, in reverse order.
+static void adjoint_sweep(Problem& P, const VelocityVector& lam, AdjointSweep& G) {
+    const Grid& g = P.grid;
+    const Physics& ph = P.ph;
+    const VelocityVector& xs = P.x;
+    const Field& eta = P.etaH;
+    G.zero();
+    // operator: q_u = Az βᵘ u - [Δy Txx(i) - Δy Txx(i-1) + Δx Txy(i, j+1) - Δx Txy(i, j)] on the active rows
+    for (int j = 1; j <= g.Ny(); ++j)
+        for (int i = 1; i <= g.Nx(); ++i) {
+            if (!inactive_fc(g, i, j, &eta)) {
+                double l = lam.u(i, j);
+                G.eta(i, j) += -g.dy_c(j) * l * 2 * (2 * strain_rate_xx(g, i, j, xs.u, &eta) + strain_rate_yy(g, i, j, xs.v, &eta));
+                G.eta(i - 1, j) += g.dy_c(j) * l * 2 * (2 * strain_rate_xx(g, i - 1, j, xs.u, &eta) + strain_rate_yy(g, i - 1, j, xs.v, &eta));
+                G.ff(i, j + 1) += -g.dx_f(i) * l * 2 * strain_rate_xy(g, i, j + 1, xs.u, xs.v, ph.walls, &eta);
+                G.ff(i, j) += g.dx_f(i) * l * 2 * strain_rate_xy(g, i, j, xs.u, xs.v, ph.walls, &eta);
+                G.bu(i, j) += l * g.Az_fcc(i, j) * xs.u(i, j);
+            }
+            if (!inactive_cf(g, i, j, &eta)) {
+                double l = lam.v(i, j);
+                G.eta(i, j) += -g.dx_c(i) * l * 2 * (2 * strain_rate_yy(g, i, j, xs.v, &eta) + strain_rate_xx(g, i, j, xs.u, &eta));
+                G.eta(i, j - 1) += g.dx_c(i) * l * 2 * (2 * strain_rate_yy(g, i, j - 1, xs.v, &eta) + strain_rate_xx(g, i, j - 1, xs.u, &eta));
+                G.ff(i + 1, j) += -g.dy_f(j) * l * 2 * strain_rate_xy(g, i + 1, j, xs.u, xs.v, ph.walls, &eta);
+                G.ff(i, j) += g.dy_f(j) * l * 2 * strain_rate_xy(g, i, j, xs.u, xs.v, ph.walls, &eta);
+                G.bv(i, j) += l * g.Az_cfc(i, j) * xs.v(i, j);
+            }
+        }
+    fill_halo_adjoint(G.ff);
+    for (int j = 1; j <= G.ff.ny(); ++j)          // ff = ((η(i-1,j-1) + η(i,j-1)) / 2 + (η(i-1,j) + η(i,j)) / 2) / 2
+        for (int i = 1; i <= G.ff.nx(); ++i) {
+            double w = G.ff(i, j) / 4;
+            G.eta(i - 1, j - 1) += w; G.eta(i, j - 1) += w; G.eta(i - 1, j) += w; G.eta(i, j) += w;
+        }
+    fill_halo_adjoint(G.eta);
+    // column integrals and viscosity: η̄H = μ H Σₖ ηₖ Δζₖ, ηₖ = ½ Aₖ^(-1/n) S^((1-n)/2n), S = ε̇ₑ² + ε̇₀²
+    double n = ph.n, p = (1 - n) / (2 * n);
+    for (int j = 1; j <= g.Ny(); ++j)
+        for (int i = 1; i <= g.Nx(); ++i) {
+            double ge = G.eta(i, j) * P.H(i, j) * (P.use_mask ? P.mu(i, j) : 1.0);
+            if (ge == 0.0) continue;
+            double exx = strain_rate_xx(g, i, j, xs.u, nullptr), eyy = strain_rate_yy(g, i, j, xs.v, nullptr);
+            double S = effective_strain_rate2(g, i, j, xs.u, xs.v, ph.walls) + ph.eps0 * ph.eps0;
+            double gS = 0;
+            for (int k = 1; k <= P.sigma.N; ++k) {
+                double ek = P.eta_s.k[k - 1](i, j);
+                double gk = ge * layer_thickness(P.sigma, k);
+                gS += gk * ek * p / S;
+                G.logA.k[k - 1](i, j) = gk * (-ek / n);
+            }
+            // S = exx² + eyy² + exx eyy + ((e²(i,j) + e²(i+1,j)) / 2 + (e²(i,j+1) + e²(i+1,j+1)) / 2) / 2 + ε̇₀²
+            double gxx = gS * (2 * exx + eyy), gyy = gS * (2 * eyy + exx);
+            if (!inactive_fc(g, i + 1, j, nullptr)) G.x.u(i + 1, j) += gxx / g.dx_c(i);
+            if (!inactive_fc(g, i, j, nullptr)) G.x.u(i, j) -= gxx / g.dx_c(i);
+            if (!inactive_cf(g, i, j + 1, nullptr)) G.x.v(i, j + 1) += gyy / g.dy_c(j);
+            if (!inactive_cf(g, i, j, nullptr)) G.x.v(i, j) -= gyy / g.dy_c(j);
+            for (int b = j; b <= j + 1; ++b)
+                for (int a = i; a <= i + 1; ++a) {
+                    double e = strain_rate_xy(g, a, b, xs.u, xs.v, ph.walls, nullptr);
+                    double ge_raw = gS / 4 * 2 * e * (g.peripheral_ff(a, b) ? wall_shear_factor(ph.walls) : 1.0);
+                    double gdudy = ge_raw / 2, gdvdx = ge_raw / 2;
+                    if (!inactive_fc(g, a, b, nullptr)) G.x.u(a, b) += gdudy / g.dy_f(b);
+                    if (!inactive_fc(g, a, b - 1, nullptr)) G.x.u(a, b - 1) -= gdudy / g.dy_f(b);
+                    if (!inactive_cf(g, a, b, nullptr)) G.x.v(a, b) += gdvdx / g.dx_f(a);
+                    if (!inactive_cf(g, a - 1, b, nullptr)) G.x.v(a - 1, b) -= gdvdx / g.dx_f(a);
+                }
+        }
+    // basal drag: βᵘ = φᵘ β(U, C̄, N̄), U = √(u² + ℑxy(v)² + u₀²), C̄ and N̄ face means; zero on peripheral faces
+    if (ph.friction != NK_FRICTION_NONE) {
+        double u02 = ph.u0 * ph.u0;
+        const Field* N = P.use_N ? &P.N : nullptr;
+        for (int j = 1; j <= P.bu.ny(); ++j)
+            for (int i = 1; i <= P.bu.nx(); ++i) {
+                if (g.peripheral_fc(i, j) || G.bu(i, j) == 0.0) continue;
+                double vf = ((xs.v(i - 1, j) + xs.v(i, j)) / 2 + (xs.v(i - 1, j + 1) + xs.v(i, j + 1)) / 2) / 2;
+                double U = std::sqrt(xs.u(i, j) * xs.u(i, j) + vf * vf + u02);
+                double Cf = (P.C(i - 1, j) + P.C(i, j)) / 2, Nf = N ? ((*N)(i - 1, j) + (*N)(i, j)) / 2 : 0.0;
+                double b, dU, dC;
+                basal_drag_and_derivatives(U, Cf, Nf, ph, b, dU, dC);
+                double gb = G.bu(i, j) * P.phu(i, j);
+                double gU = gb * dU;
+                G.x.u(i, j) += gU * xs.u(i, j) / U;
+                double gv = gU * vf / U / 4;
+                G.x.v(i - 1, j) += gv; G.x.v(i, j) += gv; G.x.v(i - 1, j + 1) += gv; G.x.v(i, j + 1) += gv;
+                G.C(i - 1, j) += gb * dC / 2; G.C(i, j) += gb * dC / 2;
+            }
+        for (int j = 1; j <= P.bv.ny(); ++j)
+            for (int i = 1; i <= P.bv.nx(); ++i) {
+                if (g.peripheral_cf(i, j) || G.bv(i, j) == 0.0) continue;
+                double uf = ((xs.u(i, j - 1) + xs.u(i + 1, j - 1)) / 2 + (xs.u(i, j) + xs.u(i + 1, j)) / 2) / 2;
+                double U = std::sqrt(xs.v(i, j) * xs.v(i, j) + uf * uf + u02);
+                double Cf = (P.C(i, j - 1) + P.C(i, j)) / 2, Nf = N ? ((*N)(i, j - 1) + (*N)(i, j)) / 2 : 0.0;
+                double b, dU, dC;
+                basal_drag_and_derivatives(U, Cf, Nf, ph, b, dU, dC);
+                double gb = G.bv(i, j) * P.phv(i, j);
+                double gU = gb * dU;
+                G.x.v(i, j) += gU * xs.v(i, j) / U;
+                double gu = gU * uf / U / 4;
+                G.x.u(i, j - 1) += gu; G.x.u(i + 1, j - 1) += gu; G.x.u(i, j) += gu; G.x.u(i + 1, j) += gu;
+                G.C(i, j - 1) += gb * dC / 2; G.C(i, j) += gb * dC / 2;
+            }
+    }
+    fill_halo_adjoint(G.x.u);
+    fill_halo_adjoint(G.x.v);
+    fill_halo_adjoint(G.C);
+}
+
+// nk_picard_adjoint for the SSA.  xbar (interior layout of u, v) = ∂J/∂x*; lam receives λ = ∂J/∂τ, gradC
+// ∂J/∂log C per cell, gradA ∂J/∂log A in the rate factor's layout (2-D: summed over the layers that share it).
+static int picard_adjoint(Problem& P, const VelocityVector& xbar, const nk_iteration_control& ctl, VelocityVector& lam,
+                          Field& gradC, SigmaField& gradA, nk_solve_stats* st) {
+    const Grid& g = P.grid;
+    fill_halo(P.x);
+    update_coefficients(P);                   // c(x*)
+    AdjointSweep G;
+    G.init(&g, P.sigma.N);
+    VelocityVector r, next;
+    r.init(&g); next.init(&g);
+    lam.init(&g);
+    bool fixed = ctl.kind == NK_FIXED_ITERATIONS;
+    int limit = fixed ? ctl.iterations : ctl.maxiter;
+    int it = 0, status = NK_OK;
+    double D = std::numeric_limits<double>::infinity(), M = 0.0;
+    std::memset(st, 0, sizeof(*st));
+    while (it < limit && (fixed || D > std::max(ctl.reltol * M, ctl.abstol))) {
+        fill_halo(lam);
+        adjoint_sweep(P, lam, G);
+        for (int j = 1; j <= r.u.ny(); ++j) for (int i = 1; i <= r.u.nx(); ++i) r.u(i, j) = xbar.u(i, j) - G.x.u(i, j);
+        for (int j = 1; j <= r.v.ny(); ++j) for (int i = 1; i <= r.v.nx(); ++i) r.v(i, j) = xbar.v(i, j) - G.x.v(i, j);
+        fill_halo(r);
+        for (int j = 1; j <= lam.u.ny(); ++j) for (int i = 1; i <= lam.u.nx(); ++i) next.u(i, j) = lam.u(i, j);
+        for (int j = 1; j <= lam.v.ny(); ++j) for (int i = 1; i <= lam.v.nx(); ++i) next.v(i, j) = lam.v(i, j);
+        int cg_status = NK_OK;
+        conjugate_gradient(P, next, r, st, &cg_status);   // next = A⁻ᵀ r from the previous λ (A is symmetric)
+        if (cg_status == NK_NONFINITE) status = NK_NONFINITE;
+        VelocityVector& d = r;                              // r is free again: Δ = ‖next - λ‖
+        linear_combination(g, d, 1.0, next, -1.0, lam);
+        D = std::sqrt(vector_dot(g, d, d));
+        M = std::sqrt(vector_dot(g, next, next));
+        for (int j = 1; j <= lam.u.ny(); ++j) for (int i = 1; i <= lam.u.nx(); ++i) lam.u(i, j) = next.u(i, j);
+        for (int j = 1; j <= lam.v.ny(); ++j) for (int i = 1; i <= lam.v.nx(); ++i) lam.v(i, j) = next.v(i, j);
+        ++it;
+        if (!std::isfinite(D) || status == NK_NONFINITE) break;
+    }
+    fill_halo(lam);
+    adjoint_sweep(P, lam, G);
+    gradC.init(&g, CENTER, CENTER);
+    for (int j = 1; j <= g.Ny(); ++j) for (int i = 1; i <= g.Nx(); ++i) gradC(i, j) = -P.C(i, j) * G.C(i, j);
+    int planes = P.rate_layout == NK_RATE_FACTOR_SIGMA ? P.sigma.N : 1;
+    gradA.init(&g, CENTER, CENTER, planes);
+    for (int j = 1; j <= g.Ny(); ++j)
+        for (int i = 1; i <= g.Nx(); ++i)
+            for (int k = 1; k <= P.sigma.N; ++k) gradA.k[planes == 1 ? 0 : k - 1](i, j) += -G.logA.k[k - 1](i, j);
+    st->picard_iterations = it;
+    st->picard_change = D;
+    st->picard_norm = M;
+    st->status = (!std::isfinite(D) || status == NK_NONFINITE) ? NK_NONFINITE : NK_OK;
+    return st->status;
+}
+
 // ---- field access in interior layout -------------------------------------------------------------
 struct FieldRef { Field* f = nullptr; SigmaField* s = nullptr; };
 
@@ -1302,6 +1547,31 @@ nk_status nko_picard_solve(nko_problem* h, nk_solve_stats* st) {
 }
 
 nk_status nko_velocity_profile(nko_problem* h) { velocity_profile(*reinterpret_cast<Problem*>(h)); return NK_OK; }
+
+// nk_picard_adjoint (SSA).  DIVA and problems with prescribed velocities are refused with NK_BAD_ARGUMENT.
+nk_status nko_picard_adjoint(nko_problem* h, const double* ubar, const double* vbar, const nk_iteration_control* control,
+                             double* lu, double* lv, double* grad_log_C, double* grad_log_A, nk_solve_stats* stats) {
+    if (!h || !ubar || !vbar) return NK_BAD_ARGUMENT;
+    Problem& P = *reinterpret_cast<Problem*>(h);
+    if (P.stress_balance != NK_SSA || P.grid.pu || P.grid.pv) return NK_BAD_ARGUMENT;
+    nk_iteration_control ctl = control ? *control : P.sdesc.picard;
+    if (ctl.kind != NK_CONVERGENCE && ctl.kind != NK_FIXED_ITERATIONS) return NK_BAD_ARGUMENT;
+    VelocityVector xbar, lam;
+    xbar.init(&P.grid);
+    load_vector(xbar, ubar, vbar);
+    Field gradC;
+    SigmaField gradA;
+    nk_solve_stats local{};
+    nk_solve_stats* st = stats ? stats : &local;
+    int status = picard_adjoint(P, xbar, ctl, lam, gradC, gradA, st);
+    if (lu && lv) store_vector(lam, lu, lv);
+    if (grad_log_C) copy_out(gradC, grad_log_C);
+    if (grad_log_A) {
+        size_t plane = (size_t)P.grid.Nx() * P.grid.Ny();
+        for (size_t k = 0; k < gradA.k.size(); ++k) copy_out(gradA.k[k], grad_log_A + k * plane);
+    }
+    return status == NK_NONFINITE ? NK_NONFINITE : NK_OK;
+}
 
 nk_status nko_multigrid_levels(nko_problem* h, int32_t* count, int32_t* nx, int32_t* ny, int32_t cap) {
     Problem& P = *reinterpret_cast<Problem*>(h);

@@ -1,0 +1,118 @@
+"""The oracle's fixed-point Picard adjoint (nko_picard_adjoint; the reverse rule of ext/NunatakEnzymeExt.jl:159-240
+for the SSA) against centred differences of the oracle's own forward solves, and the GPU library's adjoint against
+the oracle's.
+
+J = ½ Σ (u - u_obs)² + (v - v_obs)² on the 40 x 20 marine sheet with u_obs from a solve with another friction
+seed (the cases of tests/test_gpu_adjoint.py: bounded with free-slip walls and Weertman drag, periodic in x, and
+no-slip walls with regularised Coulomb drag), converged solves (Picard 1e-12, CG 1e-13):
+- ∂J/∂log C at seeded grounded cells against (J(C e^ε) - J(C e^-ε)) / 2ε, ε = 1e-3, within 1e-4 of the largest
+  gradient entry;
+- ∂J/∂log A along a seeded random direction d against the Richardson extrapolation of centred differences with
+  ε = 4e-5 and 2e-5, within 1e-4 of Σ|gᵢdᵢ| (the third derivative along d is large for the Coulomb case: a plain
+  centred difference with ε = 1e-4 is 0.8 % off, and its error falls as ε²);
+- GPU (marked gpu): λ, ∂J/∂log C and ∂J/∂log A of nk_picard_adjoint against the oracle's, within 1e-6 of each
+  one's largest entry.
+The oracle refuses the DIVA and problems with prescribed velocities."""
+import math
+
+import numpy as np
+import pytest
+
+from nunatak_gb300 import model as M, workloads
+
+CONTROL = M.Convergence(reltol=1e-12, maxiter=500)
+KINDS = ["bounded", "periodic_x", "no_slip_coulomb"]
+
+
+def _solver():
+    return M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-13, maxiter=20_000),
+                                 picard_iteration_control=M.Convergence(reltol=1e-12, maxiter=500),
+                                 preconditioner=M.StressBalanceDiagonalPreconditioner())
+
+
+def _case(kind, seed_friction):
+    base = workloads.marine_sheet(40, 20, seed=2, seed_friction=seed_friction, velocity_solver=_solver())
+    cfg, grid = dict(base.config), base.grid
+    if kind == "periodic_x":
+        grid = M.RectilinearGrid(size=(40, 20), x=(0.0, 512e3), y=(0.0, 256e3), halo=(4, 4), topology=("Periodic", "Bounded"))
+    if kind == "no_slip_coulomb":
+        cfg["stress_balance"] = M.DepthIntegrated(side_walls=M.NoSlipWalls())
+        cfg["friction"] = M.RegularizedCoulombFriction(coefficient=None, coulomb_coefficient=0.5, exponent=1.0 / 3.0)
+    return workloads.Case(f"marine_sheet_{kind}", grid, cfg, base.fields)
+
+
+def _setup(cls, kind):
+    obs = _case(kind, 1200).problem(cls)
+    obs.picard_solve()
+    uo, vo = obs.get("u"), obs.get("v")
+    P = _case(kind, 1100).problem(cls)
+    assert P.picard_solve().status == 0
+    return P, uo, vo
+
+
+def _cost(P, uo, vo):
+    return 0.5 * (np.sum((P.get("u") - uo) ** 2) + np.sum((P.get("v") - vo) ** 2))
+
+
+def _centred(P, name, factor_plus, factor_minus, xs, uo, vo, eps):
+    p0 = P.get(name)
+    J = []
+    for factor in (factor_plus, factor_minus):
+        P.set(name, p0 * factor)
+        P.set("u", xs[0])
+        P.set("v", xs[1])
+        P.picard_solve()
+        J.append(_cost(P, uo, vo))
+    P.set(name, p0)
+    return (J[0] - J[1]) / (2 * eps)
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_oracle_adjoint_matches_finite_differences(oracle_cls, kind):
+    P, uo, vo = _setup(oracle_cls, kind)
+    xs = (P.get("u"), P.get("v"))
+    lu, lv, grad, grad_a, st = P.picard_adjoint(xs[0] - uo, xs[1] - vo, CONTROL)
+    assert st.status == 0 and st.picard_iterations > 1 and st.picard_change <= 1e-12 * st.picard_norm
+    assert np.array_equal(P.get("u"), xs[0])          # the forward state is left at x*
+    scale = np.max(np.abs(grad))
+    assert scale > 0
+    phi, H = P.get("phi"), P.get("H")
+    cand = np.argwhere((phi > 0.5) & (H > 200.0))
+    for k in np.random.default_rng(7).choice(len(cand), size=3, replace=False):
+        cell = tuple(cand[k])
+        e = np.ones_like(grad)
+        e[cell] = math.exp(1e-3)
+        fd = _centred(P, "C", e, 1 / e, xs, uo, vo, 1e-3)
+        assert abs(fd - grad[cell]) <= 1e-4 * scale, (kind, cell, fd, grad[cell], scale)
+    d = np.random.default_rng(3).standard_normal(grad_a.shape)
+    eps = 4e-5
+    fd1 = _centred(P, "A", np.exp(eps * d), np.exp(-eps * d), xs, uo, vo, eps)
+    fd2 = _centred(P, "A", np.exp(eps / 2 * d), np.exp(-eps / 2 * d), xs, uo, vo, eps / 2)
+    fd = (4 * fd2 - fd1) / 3                                 # Richardson: the ε² term cancels
+    ad = float(np.sum(grad_a * d))
+    assert abs(fd - ad) <= 1e-4 * float(np.sum(np.abs(grad_a * d))), (kind, fd, ad)
+
+
+def test_oracle_adjoint_refuses_diva_and_prescribed_faces(oracle_cls):
+    diva = workloads.diva_sheet(24, 12, dx=32e3, Nsigma=4).problem(oracle_cls)
+    u, v = np.zeros(diva.shape("u")), np.zeros(diva.shape("v"))
+    with pytest.raises(ValueError):
+        diva.picard_adjoint(u, v, CONTROL)
+    inflow = workloads.channel_shelf(inflow=100.0).problem(oracle_cls)
+    with pytest.raises(ValueError):
+        inflow.picard_adjoint(np.zeros(inflow.shape("u")), np.zeros(inflow.shape("v")), CONTROL)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", KINDS)
+def test_gpu_adjoint_matches_oracle_adjoint(oracle_cls, gpu_cls, kind):
+    out = {}
+    for key, cls in (("o", oracle_cls), ("g", gpu_cls)):
+        P, uo, vo = _setup(cls, kind)
+        ub, vb = P.get("u") - uo, P.get("v") - vo
+        out[key] = P.picard_adjoint(ub, vb, CONTROL)
+        assert out[key][4].status == 0
+    for idx, name in ((0, "lambda_u"), (1, "lambda_v"), (2, "grad_log_C"), (3, "grad_log_A")):
+        g, o = out["g"][idx], out["o"][idx]
+        assert g.shape == o.shape, name
+        assert np.max(np.abs(g - o)) <= 1e-6 * np.max(np.abs(o)), (kind, name)
