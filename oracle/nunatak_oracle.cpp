@@ -1163,10 +1163,9 @@ struct AdjointSweep {   // the G fields of one reverse sweep
     }
 };
 
-// One reverse sweep of q = A(c(x)) x* for the seed λ (halos of λ filled): the operator (ssa_operator.jl:60-89),
-// fill_halo(η̄Hᶠᶠ), _interpolate_to_corners!, fill_halo(η̄H), compute_column_integrals!, compute_viscosity!
-// (membrane, wall-masked strain rates) and compute_basal_drag!, in reverse order.
-static void adjoint_sweep(Problem& P, const VelocityVector& lam, AdjointSweep& G) {
+// The operator part of a reverse sweep: ∂(λᵀq)/∂η̄H, ∂/∂η̄Hᶠᶠ (after fill_halo(η̄Hᶠᶠ) and _interpolate_to_corners!
+// are reversed, both land on G.eta, halos returned), ∂/∂βᵘ and ∂/∂βᵛ for q = A(c) x* (ssa_operator.jl:60-89).
+static void operator_sweep(Problem& P, const VelocityVector& lam, AdjointSweep& G) {
     const Grid& g = P.grid;
     const Physics& ph = P.ph;
     const VelocityVector& xs = P.x;
@@ -1199,13 +1198,84 @@ static void adjoint_sweep(Problem& P, const VelocityVector& lam, AdjointSweep& G
             G.eta(i - 1, j - 1) += w; G.eta(i, j - 1) += w; G.eta(i - 1, j) += w; G.eta(i, j) += w;
         }
     fill_halo_adjoint(G.eta);
+}
+
+// Reverse of the wall-masked membrane strain rate S(i, j) = ε̇xx² + ε̇yy² + ε̇xx ε̇yy + ℑxyᶜᶜ(ε̇xy²) of the viscosity
+// (strain_rates.jl:27-32 with η̄H absent) for the adjoint gS of S: accumulates into gx (halos included).
+static void strain_rate2_adjoint(const Grid& g, const VelocityVector& xs, int walls, int i, int j, double gS, VelocityVector& gx) {
+    double exx = strain_rate_xx(g, i, j, xs.u, nullptr), eyy = strain_rate_yy(g, i, j, xs.v, nullptr);
+    double gxx = gS * (2 * exx + eyy), gyy = gS * (2 * eyy + exx);
+    if (!inactive_fc(g, i + 1, j, nullptr)) gx.u(i + 1, j) += gxx / g.dx_c(i);
+    if (!inactive_fc(g, i, j, nullptr)) gx.u(i, j) -= gxx / g.dx_c(i);
+    if (!inactive_cf(g, i, j + 1, nullptr)) gx.v(i, j + 1) += gyy / g.dy_c(j);
+    if (!inactive_cf(g, i, j, nullptr)) gx.v(i, j) -= gyy / g.dy_c(j);
+    for (int b = j; b <= j + 1; ++b)          // ((e²(i,j) + e²(i+1,j)) / 2 + (e²(i,j+1) + e²(i+1,j+1)) / 2) / 2
+        for (int a = i; a <= i + 1; ++a) {
+            double e = strain_rate_xy(g, a, b, xs.u, xs.v, walls, nullptr);
+            double ge_raw = gS / 4 * 2 * e * (g.peripheral_ff(a, b) ? wall_shear_factor(walls) : 1.0);
+            double gdudy = ge_raw / 2, gdvdx = ge_raw / 2;
+            if (!inactive_fc(g, a, b, nullptr)) gx.u(a, b) += gdudy / g.dy_f(b);
+            if (!inactive_fc(g, a, b - 1, nullptr)) gx.u(a, b - 1) -= gdudy / g.dy_f(b);
+            if (!inactive_cf(g, a, b, nullptr)) gx.v(a, b) += gdvdx / g.dx_f(a);
+            if (!inactive_cf(g, a - 1, b, nullptr)) gx.v(a - 1, b) -= gdvdx / g.dx_f(a);
+        }
+}
+
+// Reverse of compute_basal_drag! (frictions.jl:127-160) read on the velocity pair (u, v) for the drag adjoints
+// gbu, gbv: βᵘ = φᵘ β(U, C̄, N̄), U = √(u² + ℑxy(v)² + u₀²), C̄ and N̄ face means, zero on peripheral faces.
+// Accumulates into gx and gC (halos included).
+static void basal_drag_adjoint(Problem& P, const VelocityVector& xs, const Field& gbu, const Field& gbv, VelocityVector& gx, Field& gC) {
+    const Grid& g = P.grid;
+    const Physics& ph = P.ph;
+    if (ph.friction == NK_FRICTION_NONE) return;
+    double u02 = ph.u0 * ph.u0;
+    const Field* N = P.use_N ? &P.N : nullptr;
+    for (int j = 1; j <= gbu.ny(); ++j)
+        for (int i = 1; i <= gbu.nx(); ++i) {
+            if (g.peripheral_fc(i, j) || gbu(i, j) == 0.0) continue;
+            double vf = ((xs.v(i - 1, j) + xs.v(i, j)) / 2 + (xs.v(i - 1, j + 1) + xs.v(i, j + 1)) / 2) / 2;
+            double U = std::sqrt(xs.u(i, j) * xs.u(i, j) + vf * vf + u02);
+            double Cf = (P.C(i - 1, j) + P.C(i, j)) / 2, Nf = N ? ((*N)(i - 1, j) + (*N)(i, j)) / 2 : 0.0;
+            double b, dU, dC;
+            basal_drag_and_derivatives(U, Cf, Nf, ph, b, dU, dC);
+            double gb = gbu(i, j) * P.phu(i, j);
+            double gU = gb * dU;
+            gx.u(i, j) += gU * xs.u(i, j) / U;
+            double gv = gU * vf / U / 4;
+            gx.v(i - 1, j) += gv; gx.v(i, j) += gv; gx.v(i - 1, j + 1) += gv; gx.v(i, j + 1) += gv;
+            gC(i - 1, j) += gb * dC / 2; gC(i, j) += gb * dC / 2;
+        }
+    for (int j = 1; j <= gbv.ny(); ++j)
+        for (int i = 1; i <= gbv.nx(); ++i) {
+            if (g.peripheral_cf(i, j) || gbv(i, j) == 0.0) continue;
+            double uf = ((xs.u(i, j - 1) + xs.u(i + 1, j - 1)) / 2 + (xs.u(i, j) + xs.u(i + 1, j)) / 2) / 2;
+            double U = std::sqrt(xs.v(i, j) * xs.v(i, j) + uf * uf + u02);
+            double Cf = (P.C(i, j - 1) + P.C(i, j)) / 2, Nf = N ? ((*N)(i, j - 1) + (*N)(i, j)) / 2 : 0.0;
+            double b, dU, dC;
+            basal_drag_and_derivatives(U, Cf, Nf, ph, b, dU, dC);
+            double gb = gbv(i, j) * P.phv(i, j);
+            double gU = gb * dU;
+            gx.v(i, j) += gU * xs.v(i, j) / U;
+            double gu = gU * uf / U / 4;
+            gx.u(i, j - 1) += gu; gx.u(i + 1, j - 1) += gu; gx.u(i, j) += gu; gx.u(i + 1, j) += gu;
+            gC(i, j - 1) += gb * dC / 2; gC(i, j) += gb * dC / 2;
+        }
+}
+
+// One reverse sweep of the SSA step q = A(c(x)) x* for the seed λ (halos of λ filled): the operator, then
+// compute_column_integrals! and compute_viscosity! (membrane, wall-masked strain rates) and
+// compute_basal_drag!, in reverse order.  λ-signed: G.x = ∂(λᵀq)/∂x.
+static void adjoint_sweep(Problem& P, const VelocityVector& lam, AdjointSweep& G) {
+    const Grid& g = P.grid;
+    const Physics& ph = P.ph;
+    const VelocityVector& xs = P.x;
+    operator_sweep(P, lam, G);
     // column integrals and viscosity: η̄H = μ H Σₖ ηₖ Δζₖ, ηₖ = ½ Aₖ^(-1/n) S^((1-n)/2n), S = ε̇ₑ² + ε̇₀²
     double n = ph.n, p = (1 - n) / (2 * n);
     for (int j = 1; j <= g.Ny(); ++j)
         for (int i = 1; i <= g.Nx(); ++i) {
             double ge = G.eta(i, j) * P.H(i, j) * (P.use_mask ? P.mu(i, j) : 1.0);
             if (ge == 0.0) continue;
-            double exx = strain_rate_xx(g, i, j, xs.u, nullptr), eyy = strain_rate_yy(g, i, j, xs.v, nullptr);
             double S = effective_strain_rate2(g, i, j, xs.u, xs.v, ph.walls) + ph.eps0 * ph.eps0;
             double gS = 0;
             for (int k = 1; k <= P.sigma.N; ++k) {
@@ -1214,72 +1284,151 @@ static void adjoint_sweep(Problem& P, const VelocityVector& lam, AdjointSweep& G
                 gS += gk * ek * p / S;
                 G.logA.k[k - 1](i, j) = gk * (-ek / n);
             }
-            // S = exx² + eyy² + exx eyy + ((e²(i,j) + e²(i+1,j)) / 2 + (e²(i,j+1) + e²(i+1,j+1)) / 2) / 2 + ε̇₀²
-            double gxx = gS * (2 * exx + eyy), gyy = gS * (2 * eyy + exx);
-            if (!inactive_fc(g, i + 1, j, nullptr)) G.x.u(i + 1, j) += gxx / g.dx_c(i);
-            if (!inactive_fc(g, i, j, nullptr)) G.x.u(i, j) -= gxx / g.dx_c(i);
-            if (!inactive_cf(g, i, j + 1, nullptr)) G.x.v(i, j + 1) += gyy / g.dy_c(j);
-            if (!inactive_cf(g, i, j, nullptr)) G.x.v(i, j) -= gyy / g.dy_c(j);
-            for (int b = j; b <= j + 1; ++b)
-                for (int a = i; a <= i + 1; ++a) {
-                    double e = strain_rate_xy(g, a, b, xs.u, xs.v, ph.walls, nullptr);
-                    double ge_raw = gS / 4 * 2 * e * (g.peripheral_ff(a, b) ? wall_shear_factor(ph.walls) : 1.0);
-                    double gdudy = ge_raw / 2, gdvdx = ge_raw / 2;
-                    if (!inactive_fc(g, a, b, nullptr)) G.x.u(a, b) += gdudy / g.dy_f(b);
-                    if (!inactive_fc(g, a, b - 1, nullptr)) G.x.u(a, b - 1) -= gdudy / g.dy_f(b);
-                    if (!inactive_cf(g, a, b, nullptr)) G.x.v(a, b) += gdvdx / g.dx_f(a);
-                    if (!inactive_cf(g, a - 1, b, nullptr)) G.x.v(a - 1, b) -= gdvdx / g.dx_f(a);
-                }
+            strain_rate2_adjoint(g, xs, ph.walls, i, j, gS, G.x);
         }
-    // basal drag: βᵘ = φᵘ β(U, C̄, N̄), U = √(u² + ℑxy(v)² + u₀²), C̄ and N̄ face means; zero on peripheral faces
-    if (ph.friction != NK_FRICTION_NONE) {
-        double u02 = ph.u0 * ph.u0;
-        const Field* N = P.use_N ? &P.N : nullptr;
-        for (int j = 1; j <= P.bu.ny(); ++j)
-            for (int i = 1; i <= P.bu.nx(); ++i) {
-                if (g.peripheral_fc(i, j) || G.bu(i, j) == 0.0) continue;
-                double vf = ((xs.v(i - 1, j) + xs.v(i, j)) / 2 + (xs.v(i - 1, j + 1) + xs.v(i, j + 1)) / 2) / 2;
-                double U = std::sqrt(xs.u(i, j) * xs.u(i, j) + vf * vf + u02);
-                double Cf = (P.C(i - 1, j) + P.C(i, j)) / 2, Nf = N ? ((*N)(i - 1, j) + (*N)(i, j)) / 2 : 0.0;
-                double b, dU, dC;
-                basal_drag_and_derivatives(U, Cf, Nf, ph, b, dU, dC);
-                double gb = G.bu(i, j) * P.phu(i, j);
-                double gU = gb * dU;
-                G.x.u(i, j) += gU * xs.u(i, j) / U;
-                double gv = gU * vf / U / 4;
-                G.x.v(i - 1, j) += gv; G.x.v(i, j) += gv; G.x.v(i - 1, j + 1) += gv; G.x.v(i, j + 1) += gv;
-                G.C(i - 1, j) += gb * dC / 2; G.C(i, j) += gb * dC / 2;
-            }
-        for (int j = 1; j <= P.bv.ny(); ++j)
-            for (int i = 1; i <= P.bv.nx(); ++i) {
-                if (g.peripheral_cf(i, j) || G.bv(i, j) == 0.0) continue;
-                double uf = ((xs.u(i, j - 1) + xs.u(i + 1, j - 1)) / 2 + (xs.u(i, j) + xs.u(i + 1, j)) / 2) / 2;
-                double U = std::sqrt(xs.v(i, j) * xs.v(i, j) + uf * uf + u02);
-                double Cf = (P.C(i, j - 1) + P.C(i, j)) / 2, Nf = N ? ((*N)(i, j - 1) + (*N)(i, j)) / 2 : 0.0;
-                double b, dU, dC;
-                basal_drag_and_derivatives(U, Cf, Nf, ph, b, dU, dC);
-                double gb = G.bv(i, j) * P.phv(i, j);
-                double gU = gb * dU;
-                G.x.v(i, j) += gU * xs.v(i, j) / U;
-                double gu = gU * uf / U / 4;
-                G.x.u(i, j - 1) += gu; G.x.u(i + 1, j - 1) += gu; G.x.u(i, j) += gu; G.x.u(i + 1, j) += gu;
-                G.C(i, j - 1) += gb * dC / 2; G.C(i, j) += gb * dC / 2;
-            }
-    }
+    basal_drag_adjoint(P, xs, G.bu, G.bv, G.x, G.C);
     fill_halo_adjoint(G.x.u);
     fill_halo_adjoint(G.x.v);
     fill_halo_adjoint(G.C);
 }
 
-// nk_picard_adjoint for the SSA.  xbar (interior layout of u, v) = ∂J/∂x*; lam receives λ = ∂J/∂τ, gradC
-// ∂J/∂log C per cell, gradA ∂J/∂log A in the rate factor's layout (2-D: summed over the layers that share it).
+// ---- DIVA: the reverse of one update_diva_coefficients! step (diva.jl:61-75) at the fixed point ----------------
+// The step reads x and the lagged state s⁻ = (βᵇ⁻, F₂⁻, ησ⁻) and writes uᵇ = x / (1 + βᵇ⁻ ℑF₂⁻), βᵇ = φ drag(uᵇ),
+// ησ (Glen with the lagged vertical shear), η̄H, F₂, the corners and β = βᵇ / (1 + βᵇ ℑF₂); its state outputs are
+// (βᵇ, F₂, ησ).  At the fixed point the lagged and new state coincide, so the problem's arrays after the last
+// update serve both.  The reference's rule sweeps the adjoint σ of the state along with λ
+// (ext/NunatakEnzymeExt.jl:204-214).  True adjoints here (q̄ = -λ): the operator's λ-signed sensitivities are
+// negated.
+struct DivaState {   // adjoints of (βᵇᵘ, βᵇᵛ, F₂, ησ), halos included
+    Field bbu, bbv, F2;
+    SigmaField eta;
+    void init(const Grid* g, int Ns) {
+        bbu.init(g, FACE, CENTER); bbv.init(g, CENTER, FACE); F2.init(g, CENTER, CENTER);
+        eta.init(g, CENTER, CENTER, Ns);
+    }
+    void zero() { bbu.zero(); bbv.zero(); F2.zero(); for (auto& f : eta.k) f.zero(); }
+};
+
+// One reverse sweep: seeds λ (halos filled) and the state outputs' adjoints sin; returns ȳ in G.x, C̄ in G.C,
+// ∂J/∂log A in G.logA (all true adjoints) and the adjoints of the lagged state inputs in sout.
+static void diva_sweep(Problem& P, const VelocityVector& lam, const DivaState& sin, DivaState& sout, AdjointSweep& G) {
+    const Grid& g = P.grid;
+    const Physics& ph = P.ph;
+    const VelocityVector& xs = P.x;
+    operator_sweep(P, lam, G);
+    sout.zero();
+    Field bbub = sin.bbu, bbvb = sin.bbv, F2b = sin.F2;
+    VelocityVector ubb;
+    ubb.init(&g);
+    // β = βᵇ / (1 + βᵇ ℑF₂) over size(β); β̄ = -G.bu
+    for (int j = 1; j <= P.bu.ny(); ++j)
+        for (int i = 1; i <= P.bu.nx(); ++i) {
+            double b = P.bbu(i, j), m = (P.F2(i - 1, j) + P.F2(i, j)) / 2, den = 1 + b * m;
+            double gb = -G.bu(i, j);
+            bbub(i, j) += gb / (den * den);
+            double dm = gb * (-b * b / (den * den));
+            F2b(i - 1, j) += dm / 2; F2b(i, j) += dm / 2;
+        }
+    for (int j = 1; j <= P.bv.ny(); ++j)
+        for (int i = 1; i <= P.bv.nx(); ++i) {
+            double b = P.bbv(i, j), m = (P.F2(i, j - 1) + P.F2(i, j)) / 2, den = 1 + b * m;
+            double gb = -G.bv(i, j);
+            bbvb(i, j) += gb / (den * den);
+            double dm = gb * (-b * b / (den * den));
+            F2b(i, j - 1) += dm / 2; F2b(i, j) += dm / 2;
+        }
+    fill_halo_adjoint(F2b);
+    // column integrals and the Glen law with the lagged shear: η̄H = μ H Σ ησₖ Δζₖ, F₂ = H Σ w₂ₖ / ησₖ,
+    // ησₖ = ½ Aₖ^(-1/n) eeₖ^((1-n)/2n), eeₖ = ε̇ₑ²(x) + (τx aₖ)² + (τy aₖ)² + ε̇₀², aₖ = (1 - ζₖ) / 2ησ⁻ₖ,
+    // τx = ℑxᶜ(βᵇᵘ uᵇ), τy = ℑyᶜ(βᵇᵛ vᵇ)
+    double n = ph.n, p = (1 - n) / (2 * n);
+    for (int j = 1; j <= g.Ny(); ++j)
+        for (int i = 1; i <= g.Nx(); ++i) {
+            double H = P.H(i, j);
+            double eb = -G.eta(i, j) * H * (P.use_mask ? P.mu(i, j) : 1.0);
+            double fb = F2b(i, j) * H;
+            double tx = (P.bbu(i, j) * P.ub(i, j) + P.bbu(i + 1, j) * P.ub(i + 1, j)) / 2;
+            double ty = (P.bbv(i, j) * P.vb(i, j) + P.bbv(i, j + 1) * P.vb(i, j + 1)) / 2;
+            double e2 = effective_strain_rate2(g, i, j, xs.u, xs.v, ph.walls);
+            double gS = 0, txb = 0, tyb = 0;
+            for (int k = 1; k <= P.sigma.N; ++k) {
+                double eta = P.eta_s.k[k - 1](i, j);
+                double em = eta == 0.0 ? std::numeric_limits<double>::infinity() : eta;
+                double zeta = P.sigma.zc(k);
+                double exz = tx * (1 - zeta) / (2 * em), eyz = ty * (1 - zeta) / (2 * em);
+                double ee = e2 + exz * exz + eyz * eyz + ph.eps0 * ph.eps0;
+                double etab = sin.eta.k[k - 1](i, j) + eb * layer_thickness(P.sigma, k) + fb * (-layer_weight(P.sigma, k, 2) / (eta * eta));
+                double eeb = etab * eta * p / ee;
+                gS += eeb;
+                double exzb = eeb * 2 * exz, eyzb = eeb * 2 * eyz;
+                txb += exzb * (1 - zeta) / (2 * em);
+                tyb += eyzb * (1 - zeta) / (2 * em);
+                sout.eta.k[k - 1](i, j) = eta == 0.0 ? 0.0 : -(exzb * exz + eyzb * eyz) / em;
+                G.logA.k[k - 1](i, j) = etab * (-eta / n);
+            }
+            strain_rate2_adjoint(g, xs, ph.walls, i, j, gS, G.x);
+            bbub(i, j) += txb * P.ub(i, j) / 2; ubb.u(i, j) += txb * P.bbu(i, j) / 2;
+            bbub(i + 1, j) += txb * P.ub(i + 1, j) / 2; ubb.u(i + 1, j) += txb * P.bbu(i + 1, j) / 2;
+            bbvb(i, j) += tyb * P.vb(i, j) / 2; ubb.v(i, j) += tyb * P.bbv(i, j) / 2;
+            bbvb(i, j + 1) += tyb * P.vb(i, j + 1) / 2; ubb.v(i, j + 1) += tyb * P.bbv(i, j + 1) / 2;
+        }
+    // βᵇ = φ drag(uᵇ): the drag reads the basal velocities
+    fill_halo_adjoint(bbub);
+    fill_halo_adjoint(bbvb);
+    VelocityVector ubs;
+    ubs.init(&g);
+    ubs.u = P.ub;
+    ubs.v = P.vb;
+    basal_drag_adjoint(P, ubs, bbub, bbvb, ubb, G.C);
+    fill_halo_adjoint(ubb.u);
+    fill_halo_adjoint(ubb.v);
+    // uᵇ = x / (1 + βᵇ⁻ ℑF₂⁻) over size(uᵇ)
+    for (int j = 1; j <= P.ub.ny(); ++j)
+        for (int i = 1; i <= P.ub.nx(); ++i) {
+            double m = (P.F2(i - 1, j) + P.F2(i, j)) / 2, den = 1 + P.bbu(i, j) * m;
+            double gub = ubb.u(i, j);
+            G.x.u(i, j) += gub / den;
+            double d = gub * (-P.ub(i, j) / den);
+            sout.bbu(i, j) += d * m;
+            sout.F2(i - 1, j) += d * P.bbu(i, j) / 2; sout.F2(i, j) += d * P.bbu(i, j) / 2;
+        }
+    for (int j = 1; j <= P.vb.ny(); ++j)
+        for (int i = 1; i <= P.vb.nx(); ++i) {
+            double m = (P.F2(i, j - 1) + P.F2(i, j)) / 2, den = 1 + P.bbv(i, j) * m;
+            double gvb = ubb.v(i, j);
+            G.x.v(i, j) += gvb / den;
+            double d = gvb * (-P.vb(i, j) / den);
+            sout.bbv(i, j) += d * m;
+            sout.F2(i, j - 1) += d * P.bbv(i, j) / 2; sout.F2(i, j) += d * P.bbv(i, j) / 2;
+        }
+    fill_halo_adjoint(G.x.u);
+    fill_halo_adjoint(G.x.v);
+    fill_halo_adjoint(G.C);
+}
+
+// nk_picard_adjoint.  xbar (interior layout of u, v) = ∂J/∂x*; lam receives λ = ∂J/∂τ, gradC ∂J/∂log C per
+// cell, gradA ∂J/∂log A in the rate factor's layout (2-D: summed over the layers that share it).  The SSA sweep is
+// λ-signed (ȳ = -G.x), the DIVA sweep true (ȳ = G.x) and carries the lagged-state adjoint σ.
 static int picard_adjoint(Problem& P, const VelocityVector& xbar, const nk_iteration_control& ctl, VelocityVector& lam,
                           Field& gradC, SigmaField& gradA, nk_solve_stats* st) {
     const Grid& g = P.grid;
+    const bool diva = P.stress_balance == NK_DIVA;
+    const double sign = diva ? 1.0 : -1.0;
     fill_halo(P.x);
     update_coefficients(P);                   // c(x*)
     AdjointSweep G;
     G.init(&g, P.sigma.N);
+    DivaState sig, sig_next;
+    if (diva) { sig.init(&g, P.sigma.N); sig_next.init(&g, P.sigma.N); }
+    auto sweep = [&] {
+        fill_halo(lam);
+        if (diva) {
+            diva_sweep(P, lam, sig, sig_next, G);
+            std::swap(sig, sig_next);
+        } else {
+            adjoint_sweep(P, lam, G);
+        }
+    };
     VelocityVector r, next;
     r.init(&g); next.init(&g);
     lam.init(&g);
@@ -1289,10 +1438,9 @@ static int picard_adjoint(Problem& P, const VelocityVector& xbar, const nk_itera
     double D = std::numeric_limits<double>::infinity(), M = 0.0;
     std::memset(st, 0, sizeof(*st));
     while (it < limit && (fixed || D > std::max(ctl.reltol * M, ctl.abstol))) {
-        fill_halo(lam);
-        adjoint_sweep(P, lam, G);
-        for (int j = 1; j <= r.u.ny(); ++j) for (int i = 1; i <= r.u.nx(); ++i) r.u(i, j) = xbar.u(i, j) - G.x.u(i, j);
-        for (int j = 1; j <= r.v.ny(); ++j) for (int i = 1; i <= r.v.nx(); ++i) r.v(i, j) = xbar.v(i, j) - G.x.v(i, j);
+        sweep();
+        for (int j = 1; j <= r.u.ny(); ++j) for (int i = 1; i <= r.u.nx(); ++i) r.u(i, j) = xbar.u(i, j) + sign * G.x.u(i, j);
+        for (int j = 1; j <= r.v.ny(); ++j) for (int i = 1; i <= r.v.nx(); ++i) r.v(i, j) = xbar.v(i, j) + sign * G.x.v(i, j);
         fill_halo(r);
         for (int j = 1; j <= lam.u.ny(); ++j) for (int i = 1; i <= lam.u.nx(); ++i) next.u(i, j) = lam.u(i, j);
         for (int j = 1; j <= lam.v.ny(); ++j) for (int i = 1; i <= lam.v.nx(); ++i) next.v(i, j) = lam.v(i, j);
@@ -1308,15 +1456,14 @@ static int picard_adjoint(Problem& P, const VelocityVector& xbar, const nk_itera
         ++it;
         if (!std::isfinite(D) || status == NK_NONFINITE) break;
     }
-    fill_halo(lam);
-    adjoint_sweep(P, lam, G);
+    sweep();
     gradC.init(&g, CENTER, CENTER);
-    for (int j = 1; j <= g.Ny(); ++j) for (int i = 1; i <= g.Nx(); ++i) gradC(i, j) = -P.C(i, j) * G.C(i, j);
+    for (int j = 1; j <= g.Ny(); ++j) for (int i = 1; i <= g.Nx(); ++i) gradC(i, j) = sign * P.C(i, j) * G.C(i, j);
     int planes = P.rate_layout == NK_RATE_FACTOR_SIGMA ? P.sigma.N : 1;
     gradA.init(&g, CENTER, CENTER, planes);
     for (int j = 1; j <= g.Ny(); ++j)
         for (int i = 1; i <= g.Nx(); ++i)
-            for (int k = 1; k <= P.sigma.N; ++k) gradA.k[planes == 1 ? 0 : k - 1](i, j) += -G.logA.k[k - 1](i, j);
+            for (int k = 1; k <= P.sigma.N; ++k) gradA.k[planes == 1 ? 0 : k - 1](i, j) += sign * G.logA.k[k - 1](i, j);
     st->picard_iterations = it;
     st->picard_change = D;
     st->picard_norm = M;
@@ -1548,12 +1695,12 @@ nk_status nko_picard_solve(nko_problem* h, nk_solve_stats* st) {
 
 nk_status nko_velocity_profile(nko_problem* h) { velocity_profile(*reinterpret_cast<Problem*>(h)); return NK_OK; }
 
-// nk_picard_adjoint (SSA).  DIVA and problems with prescribed velocities are refused with NK_BAD_ARGUMENT.
+// nk_picard_adjoint (SSA and DIVA).  Problems with prescribed velocities are refused with NK_BAD_ARGUMENT.
 nk_status nko_picard_adjoint(nko_problem* h, const double* ubar, const double* vbar, const nk_iteration_control* control,
                              double* lu, double* lv, double* grad_log_C, double* grad_log_A, nk_solve_stats* stats) {
     if (!h || !ubar || !vbar) return NK_BAD_ARGUMENT;
     Problem& P = *reinterpret_cast<Problem*>(h);
-    if (P.stress_balance != NK_SSA || P.grid.pu || P.grid.pv) return NK_BAD_ARGUMENT;
+    if (P.grid.pu || P.grid.pv) return NK_BAD_ARGUMENT;
     nk_iteration_control ctl = control ? *control : P.sdesc.picard;
     if (ctl.kind != NK_CONVERGENCE && ctl.kind != NK_FIXED_ITERATIONS) return NK_BAD_ARGUMENT;
     VelocityVector xbar, lam;

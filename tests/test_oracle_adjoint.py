@@ -10,9 +10,11 @@ no-slip walls with regularised Coulomb drag), converged solves (Picard 1e-12, CG
 - ∂J/∂log A along a seeded random direction d against the Richardson extrapolation of centred differences with
   ε = 4e-5 and 2e-5, within 1e-4 of Σ|gᵢdᵢ| (the third derivative along d is large for the Coulomb case: a plain
   centred difference with ε = 1e-4 is 0.8 % off, and its error falls as ε²);
+- the DIVA adjoint, which sweeps the adjoint of the step's lagged state (βᵇ, F₂, ησ) along with λ, on a 24 x 12
+  DIVA sheet with Weertman and regularised Coulomb drag, log C and σ-grid log A along directions;
 - GPU (marked gpu): λ, ∂J/∂log C and ∂J/∂log A of nk_picard_adjoint against the oracle's, within 1e-6 of each
-  one's largest entry.
-The oracle refuses the DIVA and problems with prescribed velocities."""
+  one's largest entry, for the three SSA cases and the two DIVA ones.
+The oracle refuses problems with prescribed velocities, as the library does."""
 import math
 
 import numpy as np
@@ -93,14 +95,60 @@ def test_oracle_adjoint_matches_finite_differences(oracle_cls, kind):
     assert abs(fd - ad) <= 1e-4 * float(np.sum(np.abs(grad_a * d))), (kind, fd, ad)
 
 
-def test_oracle_adjoint_refuses_diva_and_prescribed_faces(oracle_cls):
-    diva = workloads.diva_sheet(24, 12, dx=32e3, Nsigma=4).problem(oracle_cls)
-    u, v = np.zeros(diva.shape("u")), np.zeros(diva.shape("v"))
-    with pytest.raises(ValueError):
-        diva.picard_adjoint(u, v, CONTROL)
+def test_oracle_adjoint_refuses_prescribed_faces(oracle_cls):
     inflow = workloads.channel_shelf(inflow=100.0).problem(oracle_cls)
     with pytest.raises(ValueError):
         inflow.picard_adjoint(np.zeros(inflow.shape("u")), np.zeros(inflow.shape("v")), CONTROL)
+
+
+# ---- DIVA: the step also maps its lagged state (βᵇ, F₂, ησ), whose adjoint is swept along with λ --------------
+# The stopping test watches λ (as the reference's does); the state adjoint settles more slowly, so 1e-14.
+DIVA_CONTROL = M.Convergence(reltol=1e-14, maxiter=3000)
+
+
+def _diva(friction, obs=False):
+    """24 x 12 DIVA sheet (64 km cells, Nσ = 4, Arrhenius rate factor on the σ grid); the observations come from
+    other friction coefficients and a 3 % thinner sheet, so the misfit dominates J's second-order terms."""
+    solver = M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-13, maxiter=20_000),
+                                   picard_iteration_control=M.Convergence(reltol=1e-13, maxiter=1000),
+                                   preconditioner=M.StressBalanceMultigridPreconditioner(minimum_coarse_size=4))
+    case = workloads.diva_sheet(24, 12, dx=64e3, velocity_solver=solver, Nsigma=4)
+    cfg = dict(case.config)
+    if friction == "weertman":
+        cfg["friction"] = M.WeertmanFriction(coefficient=None, exponent=1.0 / 3.0)
+    fields = dict(case.fields)
+    if obs:
+        fields["C"] = fields["C"] * np.exp(0.3 * np.random.default_rng(5).standard_normal(fields["C"].shape))
+        fields["H"] = 0.97 * fields["H"]
+    return workloads.Case(f"diva_{friction}", case.grid, cfg, fields, temperature=case.temperature)
+
+
+def _diva_setup(cls, friction):
+    obs = _diva(friction, obs=True).problem(cls)
+    assert obs.picard_solve().status == 0
+    uo, vo = obs.get("u"), obs.get("v")
+    P = _diva(friction).problem(cls)
+    assert P.picard_solve().status == 0
+    return P, uo, vo
+
+
+@pytest.mark.parametrize("friction", ["weertman", "coulomb"])
+def test_oracle_diva_adjoint_matches_finite_differences(oracle_cls, friction):
+    """⟨∂J/∂log C, d⟩ and ⟨∂J/∂log A, d⟩ (σ-grid A) along seeded random directions against centred differences:
+    ε = 1e-3 and 1e-4 within 1e-4 of Σ|gᵢdᵢ| (measured 1.3e-6 and 4e-9 with Weertman drag).  The Coulomb cap
+    leaves J nearly insensitive to C, so its C difference takes ε = 1e-2 and is resolved to 1e-3 (measured 4e-4)."""
+    P, uo, vo = _diva_setup(oracle_cls, friction)
+    xs = (P.get("u"), P.get("v"))
+    lu, lv, grad, grad_a, st = P.picard_adjoint(xs[0] - uo, xs[1] - vo, DIVA_CONTROL)
+    assert st.status == 0 and st.picard_iterations > 1
+    assert grad_a.shape == P.get("A").shape
+    rng = np.random.default_rng(17)
+    coulomb = friction == "coulomb"
+    for name, g, eps, tol in (("C", grad, 1e-2 if coulomb else 1e-3, 1e-3 if coulomb else 1e-4), ("A", grad_a, 1e-4, 1e-4)):
+        d = rng.standard_normal(g.shape)
+        fd = _centred(P, name, np.exp(eps * d), np.exp(-eps * d), xs, uo, vo, eps)
+        ad = float(np.sum(g * d))
+        assert abs(fd - ad) <= tol * float(np.sum(np.abs(g * d))), (friction, name, fd, ad)
 
 
 @pytest.mark.gpu
@@ -116,3 +164,17 @@ def test_gpu_adjoint_matches_oracle_adjoint(oracle_cls, gpu_cls, kind):
         g, o = out["g"][idx], out["o"][idx]
         assert g.shape == o.shape, name
         assert np.max(np.abs(g - o)) <= 1e-6 * np.max(np.abs(o)), (kind, name)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("friction", ["weertman", "coulomb"])
+def test_gpu_diva_adjoint_matches_oracle_adjoint(oracle_cls, gpu_cls, friction):
+    out = {}
+    for key, cls in (("o", oracle_cls), ("g", gpu_cls)):
+        P, uo, vo = _diva_setup(cls, friction)
+        out[key] = P.picard_adjoint(P.get("u") - uo, P.get("v") - vo, DIVA_CONTROL)
+        assert out[key][4].status == 0
+    for idx, name in ((0, "lambda_u"), (1, "lambda_v"), (2, "grad_log_C"), (3, "grad_log_A")):
+        g, o = out["g"][idx], out["o"][idx]
+        assert g.shape == o.shape, name
+        assert np.max(np.abs(g - o)) <= 1e-6 * np.max(np.abs(o)), (friction, name)
