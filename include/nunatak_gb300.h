@@ -189,7 +189,9 @@ typedef struct nk_solver_desc {
  * refuse nk_adjoint_solve and nk_picard_adjoint (the lifted operator is not symmetric) with NK_BAD_ARGUMENT. */
 #define NK_FIELD_U_PRESCRIBED  27   /* u_D                                  Face-Center */
 #define NK_FIELD_V_PRESCRIBED  28   /* v_D                                  Center-Face */
-#define NK_FIELD_COUNT         29
+#define NK_FIELD_ENTHALPY      29   /* enthalpy E on the sigma grid (input of nk_compute_thermal_diagnostics) */
+#define NK_FIELD_WATER_FRACTION 30  /* water fraction omega on the sigma grid (written by nk_compute_thermal_diagnostics) */
+#define NK_FIELD_COUNT         31
 
 typedef struct nk_solve_stats {
     int32_t status;                   /* nk_status of the solve */
@@ -258,6 +260,30 @@ nk_status nk_compute_rate_factor(nk_problem* problem, double cold_prefactor, dou
                                  double cold_activation_energy, double warm_activation_energy,
                                  double transition_temperature, double transition_width, double gas_constant,
                                  double clausius_clapeyron, double melting_temperature);
+
+/* Constants of the rate factor from the enthalpy: ArrheniusParameters (src/Rheologies/arrhenius_rate_factor.jl:10-29,
+ * defaults :60-69: 3.61e-13, 1.73e3, 6.0e4, 13.9e4, 263.15, 1, 8.31441, 181.25, 0.01) and the EnthalpyThermodynamics
+ * constants the conversions read (src/Thermodynamics/enthalpy_thermodynamics.jl:92-104: 2009, 3.34e5, 7.9e-8,
+ * 273.15, 223.15). */
+typedef struct nk_thermal_params {
+    double cold_prefactor, warm_prefactor;                   /* Pa^-3 s^-1 */
+    double cold_activation_energy, warm_activation_energy;   /* J mol^-1 */
+    double transition_temperature, transition_width;         /* K */
+    double gas_constant;                                     /* J mol^-1 K^-1 */
+    double water_softening_coefficient;                      /* c in the softening 1 + c min(omega, omega_max) */
+    double maximum_water_fraction;                           /* omega_max */
+    double heat_capacity, latent_heat;                       /* c_i (J kg^-1 K^-1), L (J kg^-1) */
+    double clausius_clapeyron;                               /* beta (K Pa^-1): T_pm = T_0 - beta p */
+    double melting_temperature, reference_temperature;       /* T_0, T_r (K) */
+} nk_thermal_params;
+
+/* update_thermal_diagnostics! with an ArrheniusRateFactor (src/Thermodynamics/column_energy_solve.jl:85-110 and the
+ * conversions of src/Thermodynamics/enthalpy_conversions.jl:1-64): on every layer k of every column, with
+ * p = rho_i g H (1 - zeta_k), T_pm = T_0 - beta p and E_pm = c_i (T_pm - T_r):
+ *   T = min(T_pm, T_r + E / c_i),  omega = max(0, E - E_pm) / L,  A = arrhenius_rate_factor(T - T_pm + T_0, omega).
+ * Reads NK_FIELD_ENTHALPY and H; writes NK_FIELD_TEMPERATURE, NK_FIELD_WATER_FRACTION and the rate factor, which
+ * must have the sigma layout.  Until an enthalpy is set the enthalpy field holds zeros. */
+nk_status nk_compute_thermal_diagnostics(nk_problem* problem, const nk_thermal_params* params);
 
 /* update_stress_balance_coefficients!(x, ...) (SSA) or update_diva_coefficients!(x, ...) (DIVA) at the
  * current velocity fields U, V: eta_sigma, eta_H, F2, eta_H_ff, beta (and beta_b, u_b, v_b for DIVA). */

@@ -409,6 +409,42 @@ void launch_rate_factor(const DevGrid<double>& g, const SigmaTable& sig, int pla
     k_rate_factor<<<d.grid, d.block, 0, s>>>(g, sig, plane, H, T, A, rho_i, gacc, params); count_launch();
 }
 
+// update_thermal_diagnostics! with an ArrheniusRateFactor (column_energy_solve.jl:85-110): per layer, from the
+// enthalpy, the temperature and water fraction (temperature / water_fraction, enthalpy_conversions.jl:35, :42) and
+// the rate factor of the pressure-adjusted temperature with the water softening (arrhenius_rate_factor.jl:102-110).
+// prm: the 14 doubles of nk_thermal_params in order.
+__global__ void k_thermal_diagnostics(DevGrid<double> g, SigmaTable sig, int plane, const double* __restrict__ H,
+                                      const double* __restrict__ E, double* T, double* omega, double* A, double rho_i, double gacc,
+                                      const double* __restrict__ prm) {
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int c = g.idx(i, j);
+    double Ac = prm[0], Aw = prm[1], Qc = prm[2], Qw = prm[3], Tt = prm[4], Tw = prm[5], R = prm[6], cw = prm[7], wmax = prm[8];
+    double ci = prm[9], L = prm[10], bcc = prm[11], T0 = prm[12], Tr = prm[13];
+    for (int k = 0; k < sig.N; ++k) {
+        long long o = (long long)k * plane + c;
+        double p = rho_i * gacc * H[c] * (1 - sig.zc[k]);      // layer_pressure
+        double Tpm = T0 - bcc * p;                             // pressure_melting_temperature
+        double Epm = ci * (Tpm - Tr);                          // pressure_melting_enthalpy
+        double e = E[o];
+        double t = fmin(Tpm, Tr + e / ci);
+        double w = fmax(0.0, e - Epm) / L;
+        double Tp = t - Tpm + T0;
+        double log_cold = log(Ac) - Qc / (R * Tp);
+        double log_warm = log(Aw) - Qw / (R * Tp);
+        double x = fmin(fmax((Tp - Tt) / Tw + 1.0 / 2, 0.0), 1.0);
+        double s = x * x * (3 - 2 * x);
+        T[o] = t;
+        omega[o] = w;
+        A[o] = exp((1 - s) * log_cold + s * log_warm) * (1 + cw * fmin(w, wmax));
+    }
+}
+void launch_thermal_diagnostics(const DevGrid<double>& g, const SigmaTable& sig, int plane, const double* H, const double* E, double* T,
+                                double* omega, double* A, double rho_i, double gacc, const double* params, cudaStream_t s) {
+    LaunchDims d = dims2d(g.Nx, g.Ny);
+    k_thermal_diagnostics<<<d.grid, d.block, 0, s>>>(g, sig, plane, H, E, T, omega, A, rho_i, gacc, params); count_launch();
+}
+
 // ---- fixed-point adjoint of the SSA Picard step -------------------------------------------------------------
 // The reverse of picard_coefficient_step! (ext/NunatakEnzymeExt.jl:142-157): with q = A(c(x)) x*, the seed
 // q̄ = -λ, and x* the converged velocity, it returns ȳ = -(∂q/∂x)ᵀ λ.  Only active operator rows depend on

@@ -172,6 +172,8 @@ struct GeometryView {
 void launch_geometry(const GeometryView& v, cudaStream_t s);
 void launch_rate_factor(const DevGrid<double>& g, const SigmaTable& sig, int plane, const double* H, const double* T, double* A,
                         double rho_i, double gacc, const double* params, cudaStream_t s);
+void launch_thermal_diagnostics(const DevGrid<double>& g, const SigmaTable& sig, int plane, const double* H, const double* E, double* T,
+                                double* omega, double* A, double rho_i, double gacc, const double* params, cudaStream_t s);
 
 // ---- multigrid ------------------------------------------------------------------------------------------
 template <typename T>

@@ -198,7 +198,8 @@ struct nk_problem {
     SolverScalars* sc = nullptr;
     SolverScalars* sc_host = nullptr;          // pinned mirror
     double* sig_tables = nullptr;              // dz, w2, zc (Ns each) + w1 (Ns * Ns)
-    double* rate_params = nullptr;             // 9
+    double* rate_params = nullptr;             // 9 (nk_compute_rate_factor) or 14 (nk_thermal_params)
+    double* thermal = nullptr;                 // enthalpy then water fraction (Ns planes each), allocated on first use
     std::vector<double> sig_dz, sig_w2, sig_zc, sig_w1;
 
     // coarse levels
@@ -1023,6 +1024,7 @@ struct FieldLoc {
     int stride = 1, offset = 0, nx = 0, ny = 0, planes = 1;
     bool coef = false;        // a coefficient: the operator mask and diagonal follow it
     bool prescribed = false;  // a prescribed velocity (allocated on first use)
+    bool thermal = false;     // the enthalpy or the water fraction (allocated on first use, sigma layout only)
 };
 
 static FieldLoc field_loc(nk_problem* P, int id) {
@@ -1063,9 +1065,26 @@ static FieldLoc field_loc(nk_problem* P, int id) {
         case NK_FIELD_TEMPERATURE: if (P->T) { cc(P->T); f.planes = P->Ns; } break;
         case NK_FIELD_U_PRESCRIBED: fu(P->ud); f.prescribed = true; break;
         case NK_FIELD_V_PRESCRIBED: fv(P->ud); f.prescribed = true; break;
+        case NK_FIELD_ENTHALPY:
+        case NK_FIELD_WATER_FRACTION:
+            if (P->pd.rate_factor_layout == NK_RATE_FACTOR_SIGMA) {
+                cc(P->thermal ? P->thermal + (id == NK_FIELD_WATER_FRACTION ? (size_t)P->Ns * P->plane : 0) : nullptr);
+                f.planes = P->Ns;
+                f.thermal = true;
+            }
+            break;
         default: break;
     }
     return f;
+}
+
+// The enthalpy and water-fraction planes (zero at first).  No graph reads them, so none is rebuilt.
+static void ensure_thermal(nk_problem* P) {
+    if (P->thermal || P->pd.rate_factor_layout != NK_RATE_FACTOR_SIGMA) return;
+    if (P->async_pending) bad("an asynchronous solve is pending (nk_problem_wait first)");
+    size_t bytes = 2 * (size_t)P->Ns * P->plane * sizeof(double);
+    NK_CUDA(cudaMalloc((void**)&P->thermal, bytes));
+    NK_CUDA(cudaMemsetAsync(P->thermal, 0, bytes, P->stream));
 }
 
 // The prescribed-velocity pairs, all NaN (free) at first.  Graphs captured before hold no pointer to them and
@@ -1275,6 +1294,7 @@ nk_status nk_problem_destroy(nk_problem* P) {
     if (P->adj_base) cudaFree(P->adj_base);
     if (P->adj_diva) cudaFree(P->adj_diva);
     if (P->ud) cudaFree(P->ud);
+    if (P->thermal) cudaFree(P->thermal);
     if (P->stream) cudaStreamDestroy(P->stream);
     delete P;
     return NK_OK;
@@ -1283,7 +1303,7 @@ nk_status nk_problem_destroy(nk_problem* P) {
 int64_t nk_problem_field_size(const nk_problem* P, int32_t id) {
     if (!P) return 0;
     FieldLoc f = field_loc(const_cast<nk_problem*>(P), id);
-    return (f.base || f.prescribed) ? (int64_t)f.nx * f.ny * f.planes : 0;
+    return (f.base || f.prescribed || f.thermal) ? (int64_t)f.nx * f.ny * f.planes : 0;
 }
 
 nk_status nk_problem_set_field(nk_problem* P, int32_t id, const double* host, int64_t count) {
@@ -1293,6 +1313,10 @@ nk_status nk_problem_set_field(nk_problem* P, int32_t id, const double* host, in
         if (f.prescribed) {
             if (count != (int64_t)f.nx * f.ny * f.planes) bad("field size mismatch");
             ensure_prescribed(P);
+            f = field_loc(P, id);
+        }
+        if (f.thermal) {
+            ensure_thermal(P);
             f = field_loc(P, id);
         }
         if (!f.base) bad("unknown field id or field not held by this problem");
@@ -1317,6 +1341,10 @@ nk_status nk_problem_get_field(const nk_problem* Pc, int32_t id, double* host, i
             ensure_prescribed(P);
             f = field_loc(P, id);
         }
+        if (f.thermal) {
+            ensure_thermal(P);
+            f = field_loc(P, id);
+        }
         if (!f.base) bad("unknown field id or field not held by this problem");
         if (count != (int64_t)f.nx * f.ny * f.planes) bad("field size mismatch");
         copy_out(P, f, host);
@@ -1333,6 +1361,10 @@ nk_status nk_problem_set_field_parent(nk_problem* P, int32_t id, const double* p
         if (f.prescribed) {
             parent_layout(f, hx, hy, hz, count);
             ensure_prescribed(P);
+            f = field_loc(P, id);
+        }
+        if (f.thermal) {
+            ensure_thermal(P);
             f = field_loc(P, id);
         }
         if (!f.base) bad("unknown field id or field not held by this problem");
@@ -1355,6 +1387,10 @@ nk_status nk_problem_get_field_parent(const nk_problem* Pc, int32_t id, double* 
         FieldLoc f = field_loc(P, id);
         if (f.prescribed) {
             ensure_prescribed(P);
+            f = field_loc(P, id);
+        }
+        if (f.thermal) {
+            ensure_thermal(P);
             f = field_loc(P, id);
         }
         if (!f.base) bad("unknown field id or field not held by this problem");
@@ -1389,6 +1425,23 @@ nk_status nk_compute_rate_factor(nk_problem* P, double cold_prefactor, double wa
         NK_CUDA(cudaMemcpyAsync(P->rate_params, prm, sizeof(prm), cudaMemcpyHostToDevice, P->stream));
         launch_rate_factor(P->fine.g, P->sigma_table(), (int)P->plane, P->H, P->T, P->A3, P->pd.ice_density,
                            P->pd.gravitational_acceleration, P->rate_params, P->stream);
+        NK_CHECK_LAUNCH();
+        NK_CUDA(cudaStreamSynchronize(P->stream));
+    });
+}
+
+nk_status nk_compute_thermal_diagnostics(nk_problem* P, const nk_thermal_params* prm) {
+    if (!P || !prm) return NK_BAD_ARGUMENT;
+    return guarded(P->ctx, [&] {
+        static_assert(sizeof(nk_thermal_params) == 14 * sizeof(double), "nk_thermal_params is 14 doubles");
+        if (P->pd.rate_factor_layout != NK_RATE_FACTOR_SIGMA) bad("the rate factor from the enthalpy needs the sigma layout");
+        if (!(prm->heat_capacity > 0) || !(prm->latent_heat > 0) || !(prm->gas_constant > 0) || !(prm->transition_width > 0))
+            bad("heat capacity, latent heat, gas constant and transition width must be positive");
+        ensure_thermal(P);
+        NK_CUDA(cudaMemcpyAsync(P->rate_params, prm, sizeof(nk_thermal_params), cudaMemcpyHostToDevice, P->stream));
+        launch_thermal_diagnostics(P->fine.g, P->sigma_table(), (int)P->plane, P->H, P->thermal, P->T,
+                                   P->thermal + (size_t)P->Ns * P->plane, P->A3, P->pd.ice_density, P->pd.gravitational_acceleration,
+                                   P->rate_params, P->stream);
         NK_CHECK_LAUNCH();
         NK_CUDA(cudaStreamSynchronize(P->stream));
     });

@@ -31,7 +31,7 @@ FIELD_IDS = {
     "N": 9, "tau_u": 10, "tau_v": 11, "A": 12, "C": 13, "eta_H": 14, "eta_H_ff": 15,
     "beta_u": 16, "beta_v": 17, "eta_sigma": 18, "F2": 19, "beta_b_u": 20, "beta_b_v": 21,
     "u_b": 22, "v_b": 23, "u_sigma": 24, "v_sigma": 25, "T": 26,
-    "u_prescribed": 27, "v_prescribed": 28,
+    "u_prescribed": 27, "v_prescribed": 28, "E": 29, "omega": 30,
 }
 
 # (location x, location y, on the sigma grid) of each field: "c" Center, "f" Face.
@@ -46,6 +46,7 @@ FIELD_LOCATIONS = {
     "u_b": ("f", "c", False), "v_b": ("c", "f", False), "u_sigma": ("f", "c", True),
     "v_sigma": ("c", "f", True), "T": ("c", "c", True),
     "u_prescribed": ("f", "c", False), "v_prescribed": ("c", "f", False),
+    "E": ("c", "c", True), "omega": ("c", "c", True),
 }
 
 
@@ -60,6 +61,14 @@ class GridDesc(C.Structure):
                 ("x_faces", C.POINTER(C.c_double)), ("y_faces", C.POINTER(C.c_double)),
                 ("x0", C.c_double), ("Lx", C.c_double), ("y0", C.c_double), ("Ly", C.c_double),
                 ("sigma_faces", C.POINTER(C.c_double)), ("bed_refinement", C.c_double)]
+
+
+class ThermalParams(C.Structure):
+    """nk_thermal_params: ArrheniusParameters and the enthalpy constants the conversions read."""
+    _fields_ = [(name, C.c_double) for name in (
+        "cold_prefactor", "warm_prefactor", "cold_activation_energy", "warm_activation_energy", "transition_temperature",
+        "transition_width", "gas_constant", "water_softening_coefficient", "maximum_water_fraction", "heat_capacity",
+        "latent_heat", "clausius_clapeyron", "melting_temperature", "reference_temperature")]
 
 
 class PhysicsDesc(C.Structure):

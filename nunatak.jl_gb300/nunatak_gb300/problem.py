@@ -157,6 +157,21 @@ class Problem:
             transition_width, gas_constant, clausius_clapeyron, melting_temperature)])
         _check(st, "compute_rate_factor", self._err())
 
+    def compute_thermal_diagnostics(self, cold_prefactor=3.61e-13, warm_prefactor=1.73e3, cold_activation_energy=6.0e4,
+                                    warm_activation_energy=13.9e4, transition_temperature=263.15, transition_width=1.0,
+                                    gas_constant=8.31441, water_softening_coefficient=181.25, maximum_water_fraction=0.01,
+                                    heat_capacity=2009.0, latent_heat=3.34e5, clausius_clapeyron=7.9e-8,
+                                    melting_temperature=273.15, reference_temperature=223.15):
+        """update_thermal_diagnostics! with an ArrheniusRateFactor: T and the water fraction from the enthalpy field
+        "E", then the σ-grid rate factor with the water softening.  Defaults: ArrheniusRateFactor
+        (src/Rheologies/arrhenius_rate_factor.jl:60-69) and EnthalpyThermodynamics
+        (src/Thermodynamics/enthalpy_thermodynamics.jl:92-104)."""
+        prm = abi.ThermalParams(cold_prefactor, warm_prefactor, cold_activation_energy, warm_activation_energy,
+                                transition_temperature, transition_width, gas_constant, water_softening_coefficient,
+                                maximum_water_fraction, heat_capacity, latent_heat, clausius_clapeyron,
+                                melting_temperature, reference_temperature)
+        _check(self._fn("compute_thermal_diagnostics")(self._h, C.byref(prm)), "compute_thermal_diagnostics", self._err())
+
     def update_coefficients(self):
         _check(self._fn("update_coefficients")(self._h), "update_coefficients", self._err())
 

@@ -785,6 +785,7 @@ struct Problem {
     VelocityVector ud;            // prescribed velocities, NaN where free (grid.pu / grid.pv once set)
     Field H, bed, s, mu, phi, phu, phv, N, C, A2, etaH, etaHff, bu, bv, F2, bbu, bbv, ub, vb;
     SigmaField A3, eta_s, T, us, vs;
+    SigmaField E, omega;          // enthalpy and water fraction (nko_compute_thermal_diagnostics)
 
     // CG workspace (VelocityConjugateGradientSolver, conjugate_gradient.jl:52-102) and Picard x⁻
     VelocityVector r, z, p, q, w, xprev;
@@ -1506,6 +1507,8 @@ static FieldRef field_ref(Problem& P, int id) {
         case NK_FIELD_TEMPERATURE: r.s = &P.T; break;
         case NK_FIELD_U_PRESCRIBED: r.f = &P.ud.u; break;
         case NK_FIELD_V_PRESCRIBED: r.f = &P.ud.v; break;
+        case NK_FIELD_ENTHALPY: if (P.rate_layout == NK_RATE_FACTOR_SIGMA) r.s = &P.E; break;
+        case NK_FIELD_WATER_FRACTION: if (P.rate_layout == NK_RATE_FACTOR_SIGMA) r.s = &P.omega; break;
         default: break;
     }
     return r;
@@ -1577,6 +1580,7 @@ nk_status nko_problem_create(const nk_grid_desc* gd, const nk_physics_desc* pd, 
     for (Field* f : {&P->phv, &P->bv, &P->bbv, &P->vb}) f->init(g, CENTER, FACE);
     P->etaHff.init(g, FACE, FACE);
     P->A3.init(g, CENTER, CENTER, gd->Nsigma); P->eta_s.init(g, CENTER, CENTER, gd->Nsigma); P->T.init(g, CENTER, CENTER, gd->Nsigma);
+    P->E.init(g, CENTER, CENTER, gd->Nsigma); P->omega.init(g, CENTER, CENTER, gd->Nsigma);
     P->us.init(g, FACE, CENTER, gd->Nsigma); P->vs.init(g, CENTER, FACE, gd->Nsigma);
     P->r.init(g); P->z.init(g); P->p.init(g); P->q.init(g); P->w.init(g); P->xprev.init(g);
     P->eta_prev.init(g, CENTER, CENTER);
@@ -1645,6 +1649,40 @@ nk_status nko_compute_rate_factor(nko_problem* h, double Ac, double Aw, double Q
             P.A3.k[k - 1](i, j) = std::exp((1 - s) * log_cold + s * log_warm) * softening;
         });
         fill_halo(P.A3.k[k - 1]);
+    }
+    return NK_OK;
+}
+
+// update_thermal_diagnostics! with an ArrheniusRateFactor, src/Thermodynamics/column_energy_solve.jl:85-110:
+// _compute_thermal_diagnostics! (:112-117) with temperature / water_fraction (enthalpy_conversions.jl:35, :42),
+// then _compute_rate_factor! (:104-110) with arrhenius_rate_factor (arrhenius_rate_factor.jl:102-110).
+nk_status nko_compute_thermal_diagnostics(nko_problem* h, const nk_thermal_params* q) {
+    if (!h || !q) return NK_BAD_ARGUMENT;
+    Problem& P = *reinterpret_cast<Problem*>(h);
+    if (P.rate_layout != NK_RATE_FACTOR_SIGMA) return NK_BAD_ARGUMENT;
+    if (!(q->heat_capacity > 0) || !(q->latent_heat > 0) || !(q->gas_constant > 0) || !(q->transition_width > 0)) return NK_BAD_ARGUMENT;
+    const Grid& g = P.grid;
+    for (int k = 1; k <= P.sigma.N; ++k) {
+        double zeta = P.sigma.zc(k);
+        for_xy(g.Nx(), g.Ny(), [&](int i, int j) {
+            double p = P.ph.rho_i * P.ph.g * P.H(i, j) * (1 - zeta);                        // layer_pressure, :61-64
+            double Tpm = q->melting_temperature - q->clausius_clapeyron * p;                // :6
+            double Epm = q->heat_capacity * (Tpm - q->reference_temperature);              // :13
+            double E = P.E.k[k - 1](i, j);
+            double T = std::min(Tpm, q->reference_temperature + E / q->heat_capacity);     // :35
+            double w = std::max(0.0, E - Epm) / q->latent_heat;                            // :42
+            P.T.k[k - 1](i, j) = T;
+            P.omega.k[k - 1](i, j) = w;
+            double Tp = T - Tpm + q->melting_temperature;                                   // T′ = T - Tₚₘ + T₀
+            double R = q->gas_constant;
+            double log_cold = std::log(q->cold_prefactor) - q->cold_activation_energy / (R * Tp);
+            double log_warm = std::log(q->warm_prefactor) - q->warm_activation_energy / (R * Tp);
+            double x = std::min(std::max((Tp - q->transition_temperature) / q->transition_width + 1.0 / 2, 0.0), 1.0);
+            double s = x * x * (3 - 2 * x);
+            double softening = 1 + q->water_softening_coefficient * std::min(w, q->maximum_water_fraction);
+            P.A3.k[k - 1](i, j) = std::exp((1 - s) * log_cold + s * log_warm) * softening;
+        });
+        fill_halo(P.T.k[k - 1]); fill_halo(P.omega.k[k - 1]); fill_halo(P.A3.k[k - 1]);
     }
     return NK_OK;
 }

@@ -45,6 +45,7 @@ def load():
             "nko_linear_solve": [vp, dp, dp, C.POINTER(abi.SolveStats)],
             "nko_picard_solve": [vp, C.POINTER(abi.SolveStats)],
             "nko_velocity_profile": [vp],
+            "nko_compute_thermal_diagnostics": [vp, C.POINTER(abi.ThermalParams)],
             "nko_picard_adjoint": [vp, dp, dp, C.POINTER(abi.IterationControl), dp, dp, dp, dp, C.POINTER(abi.SolveStats)],
             "nko_multigrid_levels": [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), i32],
             "nko_multigrid_restrict": [vp, i32, dp, dp, dp, dp],

@@ -29,6 +29,7 @@ FILES = [
     "src/Models/smooth_ice_mask.jl",
     "src/Models/ice_sheet_constants.jl",
     "src/Grids/sigma_grid.jl",
+    "src/Thermodynamics/enthalpy_conversions.jl",
 ]
 
 

@@ -55,6 +55,7 @@ def test_null_handles_are_refused(lib):
         "nk_problem_get_field_parent": lambda: lib.nk_problem_get_field_parent(null, 0, d, 0, 0, 0, 0),
         "nk_compute_geometry": lambda: lib.nk_compute_geometry(null),
         "nk_compute_rate_factor": lambda: lib.nk_compute_rate_factor(null, *([0.0] * 9)),
+        "nk_compute_thermal_diagnostics": lambda: lib.nk_compute_thermal_diagnostics(null, null),
         "nk_update_coefficients": lambda: lib.nk_update_coefficients(null),
         "nk_apply_operator": lambda: lib.nk_apply_operator(null, d, d, d, d),
         "nk_precondition": lambda: lib.nk_precondition(null, d, d, d, d),

@@ -269,11 +269,13 @@ DOCTEST_RESTATEMENTS = {
     ("src/Models/ice_sheet_constants.jl", 22): "test_reference_cases_4::test_configuration_doctests",
     ("src/Grids/sigma_grid.jl", 8): "test_reference_cases_4::test_configuration_doctests",
     ("src/Grids/sigma_grid.jl", 32): "test_reference_cases_4::test_sigma_grid_doctest",
+    ("src/Thermodynamics/enthalpy_conversions.jl", 20): "test_thermal_diagnostics::test_enthalpy_doctest",
 }
 
 
 def test_every_reference_doctest_is_restated():
-    """The golden file holds the 27 doctests of the velocity solve's sources, and each has its restating test."""
+    """The golden file holds the 28 doctests of the velocity solve's sources and of the enthalpy conversions,
+    and each has its restating test."""
     import importlib
     found = {(d["file"], d["lines"][0]) for d in reference_doctests()}
     assert found == set(DOCTEST_RESTATEMENTS)
