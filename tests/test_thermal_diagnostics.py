@@ -6,7 +6,8 @@ the GPU library marked gpu), against the reference's own known answers:
 - "Enthalpy conversions round trip" (test/test_thermodynamics.jl:99-114): cold ice at three pressures gives back
   its temperature with ω = 0; temperate ice with ω = 0.01 at 10 MPa sits at T_pm = 273.15 - 7.9e-8 p with
   ω = 0.01;
-- the temperate half of "Model diagnoses A from the enthalpy" (test/test_rate_factor.jl:157-184): on the
+- "Model diagnoses A from the enthalpy" (test/test_rate_factor.jl:157-184): the surface enthalpy of a new model
+  (243.15 K, no ice) gives A = cold_branch(243.15); on the
   16 x 4 grid of rate_factor_model (ρᵢ = 910, H = 1000 m, Nσ = 10, Clausius-Clapeyron 7.9e-8), the enthalpy
   E_pm(p) + 0.005 L gives A = warm_branch(273.15) (1 + 181.25 × 0.005) on every layer (rtol 1e-9), and
   E_pm(p) + 0.05 L the capped softening (1 + 181.25 × 0.01).
@@ -79,6 +80,22 @@ def test_enthalpy_conversions_round_trip(backend):
     P.compute_thermal_diagnostics()
     assert abs(P.get("omega")[0, 0, 0] - 0.01) <= 1.4901161193847656e-08 * 0.01
     assert abs(P.get("T")[0, 0, 0] - pressure_melting_temperature(Pa)) <= 1.4901161193847656e-08 * 273.15
+
+
+def cold_branch(t):
+    return 3.61e-13 * math.exp(-6.0e4 / (8.31441 * t))
+
+
+def test_rate_factor_of_the_surface_enthalpy(backend):
+    """test/test_rate_factor.jl:162-165: a new model holds the surface enthalpy enthalpy(243.15, 0, 0) on every layer
+    and no ice yet (H = 0, so p = 0), which gives A = cold_branch(243.15)."""
+    g = M.RectilinearGrid(size=(16, 4), x=(0.0, 1.6e5), y=(0.0, 4e4), topology=("Bounded", "Bounded"), halo=(4, 4))
+    P = make(backend, g, Nsigma=10, rheology=M.GlenFlowLaw(rate_factor="sigma"), constants=M.IceSheetConstants(ice_density=910.0))
+    P.set("H", 0.0)
+    P.set("E", enthalpy(243.15, 0.0, 0.0))
+    P.compute_thermal_diagnostics()
+    np.testing.assert_allclose(P.get("A"), cold_branch(243.15), rtol=1.4901161193847656e-08)
+    assert np.all(P.get("omega") == 0.0)
 
 
 @pytest.mark.parametrize("excess,omega_eff", [(0.005, 0.005), (0.05, 0.01)])
