@@ -181,3 +181,35 @@ def diva_sheet(Nx=2048, Ny=1024, seed=3, dx=1e3, velocity_solver=None, precision
                friction=M.RegularizedCoulombFriction(coefficient=None, coulomb_coefficient=0.5, exponent=1.0 / 3.0),
                grounding=M.SubgridGroundedFraction(), velocity_solver=solver)
     return Case("diva_sheet", grid, cfg, {"H": H, "bed": bed, "C": C}, temperature=T)
+
+
+def mismip_stream(dx, velocity_solver=None):
+    """The MISMIP+-like marine ice stream of the reference's multigrid scaling benchmark
+    (benchmarks/multigrid_scaling.jl:10-34): a 640 km x 80 km channel with Bounded free-slip walls, the MISMIP+
+    polynomial bed with side walls (Asay-Davis et al. 2016, the benchmark's constants), the prescribed thickness
+    1500 sqrt(1 - x / 650 km) up to a calving front at 600 km, Glen A = 2.0392e-17 / yr with ε̇₀ = 1e-5 / yr,
+    regularised Coulomb drag (C = 1e4 yr^(1/3), α² = 0.5, m = 1/3, u₀ = 1e-5 / yr), the subgrid grounded
+    fraction, the smooth ice mask and Nσ = 10; grid spacing dx (m), halo 4.  The benchmark's velocity solver
+    (multigrid PCG to 1e-6, five Picard iterations) is the default."""
+    Lx, Ly = 640e3, 80e3
+    nx, ny = int(round(Lx / dx)), int(round(Ly / dx))
+    grid = M.RectilinearGrid(size=(nx, ny), x=(0.0, Lx), y=(0.0, Ly), halo=(4, 4))
+    X, Y = _centers(grid)
+    B0, B2, B4, B6, xbar = -150.0, -728.8, 343.91, -50.57, 300e3
+    fc, dc, wc, z_deep = 4e3, 500.0, 24e3, -720.0
+    along = B0 + B2 * (X / xbar) ** 2 + B4 * (X / xbar) ** 4 + B6 * (X / xbar) ** 6
+    across = dc / (1 + np.exp(-2 * (Y - Ly / 2 - wc) / fc)) + dc / (1 + np.exp(2 * (Y - Ly / 2 + wc) / fc))
+    bed = np.maximum(along + across, z_deep)
+    H = np.where(X < 600e3, 1500.0 * np.sqrt(np.maximum(0.0, 1 - X / 650e3)), 0.0)
+    solver = velocity_solver or M.StressBalanceSolver(
+        preconditioner=M.StressBalanceMultigridPreconditioner(),
+        linear_iteration_control=M.Convergence(reltol=1e-6, maxiter=50_000),
+        picard_iteration_control=M.FixedIterations(5))
+    A = 2.0392e-17 / YEAR
+    cfg = dict(Nsigma=10, stress_balance=M.DepthIntegrated(side_walls=M.FreeSlipWalls()),
+               rheology=M.GlenFlowLaw(rate_factor=A, strain_rate_regularization=1e-5 / YEAR),
+               friction=M.RegularizedCoulombFriction(coefficient=None, coulomb_coefficient=0.5, exponent=1.0 / 3.0,
+                                                     velocity_regularization=1e-5 / YEAR),
+               grounding=M.SubgridGroundedFraction(), velocity_solver=solver)
+    C = np.full_like(H, 1e4 * YEAR ** (1.0 / 3.0))
+    return Case("mismip_stream", grid, cfg, {"H": H, "bed": bed, "A": np.full_like(H, A), "C": C})
