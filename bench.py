@@ -78,6 +78,9 @@ def parse():
     ap.add_argument("--diva", action="store_true",
                     help="the DIVA workload instead: one solve of the 2048x1024 DIVA sheet (Nσ = 10, Arrhenius A, "
                          "regularised Coulomb drag) in mixed precision and in FP64, from rest")
+    ap.add_argument("--scaling", action="store_true",
+                    help="the reference's published multigrid scaling benchmark instead: iterations and device time of "
+                         "one SSA solve to 1e-8 at six grid spacings, beside the published numbers")
     ap.add_argument("--profile-grid", type=int, nargs=2, default=[256, 128], metavar=("NX", "NY"),
                     help="grid of the marine-sheet solve that --profile solve runs")
     return ap.parse_args()
@@ -504,6 +507,54 @@ def run_diva(nk, workloads, ctx):
         "coulomb_transition_speed_m_per_yr": transition}), flush=True)
 
 
+def run_scaling(nk, workloads, ctx, problem_cls=None, rows=None):
+    """The reference's published multigrid scaling benchmark (benchmarks/multigrid_scaling.jl; its table in
+    docs/src/model/numerics.md:42-49, kept in tests/golden/reference_scaling.json): the MISMIP+-like ice stream
+    at six spacings, five Picard iterations of multigrid PCG to 1e-6 from rest, then one SSA solve of the last
+    coefficients from zero to 1e-8 with the diagonal and with the multigrid preconditioner (FP64, and the
+    multigrid also in mixed precision).  Each timed solve follows an untimed one of the same system (graph
+    capture).  Reports device milliseconds and iterations per row beside the published H200 seconds."""
+    from nunatak_gb300 import model as M
+    cls = problem_cls or nk.Problem
+    with open(os.path.join(ROOT, "tests", "golden", "reference_scaling.json"), encoding="utf-8") as f:
+        table = json.load(f)["rows"]
+    out = []
+    for row in table if rows is None else [r for r in table if r["dx_m"] in rows]:
+        case = workloads.mismip_stream(row["dx_m"])
+        P = case.problem(cls, context=ctx) if ctx is not None else case.problem(cls)
+        P.picard_solve()
+        coefficients = {k: P.get(k) for k in ("eta_H", "eta_H_ff", "beta_u", "beta_v")}
+        tau = P.get("tau_u"), P.get("tau_v")
+        P.close()
+        entry = {"dx_m": row["dx_m"], "grid": [row["nx"], row["ny"]],
+                 "published": {"diagonal_iterations": row["diagonal_iterations"], "diagonal_cpu_gpu_s": row["diagonal_cpu_gpu_s"],
+                               "multigrid_iterations": row["multigrid_iterations"], "multigrid_cpu_gpu_s": row["multigrid_cpu_gpu_s"]}}
+        for name, pre, prec in (("diagonal", M.StressBalanceDiagonalPreconditioner(), "fp64"),
+                                ("multigrid", M.StressBalanceMultigridPreconditioner(), "fp64"),
+                                ("multigrid_mixed", M.StressBalanceMultigridPreconditioner(), "mixed")):
+            solver = M.StressBalanceSolver(preconditioner=pre, precision=prec, picard_iteration_control=M.FixedIterations(1),
+                                           linear_iteration_control=M.Convergence(reltol=1e-8, maxiter=100_000))
+            c2 = workloads.Case("mismip_stream", case.grid, dict(case.config, velocity_solver=solver), case.fields)
+            Q = c2.problem(cls, context=ctx) if ctx is not None else c2.problem(cls)
+            for k, value in coefficients.items():
+                Q.set(k, value)
+            for _ in range(2):                           # the first solve captures the graph
+                Q.set("u", 0.0)
+                Q.set("v", 0.0)
+                st = Q.linear_solve(*tau)
+            entry[name] = {"iterations": st.linear_iterations_last, "device_ms": st.device_ms, "status": st.status}
+            Q.close()
+        out.append(entry)
+    print(json.dumps({
+        "metric": "one SSA solve from zero to 1e-8 (reference multigrid scaling benchmark): CG iterations and device time",
+        "config": {"workload": "MISMIP+-like ice stream of benchmarks/multigrid_scaling.jl (640 x 80 km, bed and thickness "
+                               "formulas of the benchmark, calving front at 600 km), coefficients after 5 Picard iterations "
+                               "of multigrid PCG to 1e-6 from rest",
+                   "published": "docs/src/model/numerics.md:42-49: CPU = one thread of an AMD EPYC 9745, GPU = one H200"},
+        "rows": out}), flush=True)
+    return out
+
+
 # Algorithmic bytes per cell of the solve's repeated work (each array a kernel touches, once, at its precision):
 # the FP64 flexible CG iteration (operator 65 B, update 104 B, dots after the V-cycle 32 B, xpby 48 B), the FP32
 # V-cycle (about 62 four-byte words per fine cell, times 4/3 for the coarse levels) and the SSA coefficient update
@@ -548,6 +599,10 @@ def main():
     if args.diva:
         if rank == 0:
             run_diva(nk, workloads, ctx)
+        return
+    if args.scaling:
+        if rank == 0:
+            run_scaling(nk, workloads, ctx)
         return
 
     def barrier():
