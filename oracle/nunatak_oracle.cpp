@@ -261,25 +261,56 @@ static inline double normal_stress_yy(const Grid& g, int i, int j, const Field& 
 static inline double shear_stress(const Grid& g, int i, int j, const Field& u, const Field& v, const Field& etaff, int walls, const Field& eta) {  // :62
     return 2 * etaff(i, j) * strain_rate_xy(g, i, j, u, v, walls, &eta);
 }
-static inline double x_stress_balance(const Grid& g, int i, int j, const Field& u, const Field& v, const Field& eta,
-                                      const Field& etaff, const Field& bu, int walls) {   // :69-73
-    double div = (g.dy_c(j) * normal_stress_xx(g, i, j, u, v, eta) - g.dy_c(j) * normal_stress_xx(g, i - 1, j, u, v, eta)) +
-                 (g.dx_f(i) * shear_stress(g, i, j + 1, u, v, etaff, walls, eta) - g.dx_f(i) * shear_stress(g, i, j, u, v, etaff, walls, eta));
-    return g.Az_fcc(i, j) * bu(i, j) * u(i, j) - div;
-}
-static inline double y_stress_balance(const Grid& g, int i, int j, const Field& u, const Field& v, const Field& eta,
-                                      const Field& etaff, const Field& bv, int walls) {   // :75-79
-    double div = (g.dx_c(i) * normal_stress_yy(g, i, j, u, v, eta) - g.dx_c(i) * normal_stress_yy(g, i, j - 1, u, v, eta)) +
-                 (g.dy_f(j) * shear_stress(g, i + 1, j, u, v, etaff, walls, eta) - g.dy_f(j) * shear_stress(g, i, j, u, v, etaff, walls, eta));
-    return g.Az_cfc(i, j) * bv(i, j) * v(i, j) - div;
-}
-
-// The halos of p, η̄H and η̄Hᶠᶠ must be filled.
+// The halos of p, η̄H and η̄Hᶠᶠ must be filled.  ssa_operator.jl:47-89 evaluates every stress of a row from the
+// masked velocities (interior_u / interior_v with η̄H).  Here the masked velocities are taken once per point and
+// each stress once per centre or corner, by the same expressions on the same values, and the rows read them: the
+// results (and bits) are those of the per-row evaluation.  Txx at centres 0..Nx x 1..Ny, Tyy at 1..Nx x 0..Ny,
+// Txy at corners 1..Nx+1 x 1..Ny+1; the masked velocities at the points those read.
 static void ssa_operator(const Grid& g, VelocityVector& q, const VelocityVector& p, const Coefficients& c, int walls) {  // :47-52, :81-89
-    for_xy(g.Nx(), g.Ny(), [&](int i, int j) {
+    const int Nx = g.Nx(), Ny = g.Ny(), sx = Nx + 3;
+    const size_t n = (size_t)sx * (Ny + 3);
+    std::unique_ptr<double[]> mu(new double[n]), mv(new double[n]), txx(new double[n]), tyy(new double[n]), txy(new double[n]);
+    auto at = [sx](int i, int j) { return (size_t)(j + 1) * sx + (i + 1); };   // i, j from -1
+    const Field &eta = *c.etaH, &ff = *c.etaHff;
+#pragma omp parallel for schedule(static)
+    for (int j = -1; j <= Ny + 1; ++j)
+        for (int i = -1; i <= Nx + 1; ++i) {
+            mu[at(i, j)] = interior_u(g, i, j, p.u, &eta);
+            mv[at(i, j)] = interior_v(g, i, j, p.v, &eta);
+        }
+    const double wf = wall_shear_factor(walls);
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j <= Ny + 1; ++j)
+        for (int i = 0; i <= Nx + 1; ++i) {
+            if (i <= Nx && j <= Ny) {
+                double exx = (mu[at(i + 1, j)] - mu[at(i, j)]) / g.dx_c(i);   // strain_rate_xx
+                double eyy = (mv[at(i, j + 1)] - mv[at(i, j)]) / g.dy_c(j);   // strain_rate_yy
+                txx[at(i, j)] = 2 * eta(i, j) * (2 * exx + eyy);               // normal_stress_xx, :60
+                tyy[at(i, j)] = 2 * eta(i, j) * (2 * eyy + exx);               // normal_stress_yy, :61
+            }
+            if (i >= 1 && j >= 1) {                                            // shear_stress, :62; strain_rate_xy
+                double dudy = (mu[at(i, j)] - mu[at(i, j - 1)]) / g.dy_f(j);
+                double dvdx = (mv[at(i, j)] - mv[at(i - 1, j)]) / g.dx_f(i);
+                double e = (dudy + dvdx) / 2;
+                txy[at(i, j)] = 2 * ff(i, j) * (g.peripheral_ff(i, j) ? wf * e : e);
+            }
+        }
+    for_xy(Nx, Ny, [&](int i, int j) {
         bool wu = inactive_fc(g, i, j, c.etaH), wv = inactive_cf(g, i, j, c.etaH);
-        q.u(i, j) = wu ? p.u(i, j) : x_stress_balance(g, i, j, p.u, p.v, *c.etaH, *c.etaHff, *c.bu, walls);
-        q.v(i, j) = wv ? p.v(i, j) : y_stress_balance(g, i, j, p.u, p.v, *c.etaH, *c.etaHff, *c.bv, walls);
+        if (wu) {
+            q.u(i, j) = p.u(i, j);
+        } else {   // x_stress_balance, :69-73
+            double div = (g.dy_c(j) * txx[at(i, j)] - g.dy_c(j) * txx[at(i - 1, j)]) +
+                         (g.dx_f(i) * txy[at(i, j + 1)] - g.dx_f(i) * txy[at(i, j)]);
+            q.u(i, j) = g.Az_fcc(i, j) * (*c.bu)(i, j) * p.u(i, j) - div;
+        }
+        if (wv) {
+            q.v(i, j) = p.v(i, j);
+        } else {   // y_stress_balance, :75-79
+            double div = (g.dx_c(i) * tyy[at(i, j)] - g.dx_c(i) * tyy[at(i, j - 1)]) +
+                         (g.dy_f(j) * txy[at(i + 1, j)] - g.dy_f(j) * txy[at(i, j)]);
+            q.v(i, j) = g.Az_cfc(i, j) * (*c.bv)(i, j) * p.v(i, j) - div;
+        }
     });
 }
 
@@ -566,13 +597,24 @@ static void line_relax(const Grid& g, Field& x, const Field& b, Field& q, Field&
 // smooth!, :165-180 and _smooth! / _line_smooth!, :213-219, :255-259
 static void smooth(const Grid& g, VelocityVector& x, const VelocityVector& b, VelocityVector& q, Field& t, const Coefficients& c,
                    int walls, int smoother, int sweeps) {
+    // the ℓ1 row sums depend on the coefficients only: evaluated once for all sweeps, by the same functions
+    std::unique_ptr<double[]> rsu, rsv;
+    const int sx = g.Nx() + 1;
+    if (smoother == NK_SMOOTHER_POINT_JACOBI) {
+        rsu.reset(new double[(size_t)sx * (g.Ny() + 1)]);
+        rsv.reset(new double[(size_t)sx * (g.Ny() + 1)]);
+        for_xy(g.Nx(), g.Ny(), [&](int i, int j) {
+            rsu[(size_t)j * sx + i] = x_absolute_row_sum(g, i, j, c, walls);
+            rsv[(size_t)j * sx + i] = y_absolute_row_sum(g, i, j, c, walls);
+        });
+    }
     for (int s = 0; s < sweeps; ++s) {
         fill_halo(x);
         ssa_operator(g, q, x, c, walls);
         if (smoother == NK_SMOOTHER_POINT_JACOBI) {
             for_xy(g.Nx(), g.Ny(), [&](int i, int j) {
-                x.u(i, j) += (b.u(i, j) - q.u(i, j)) / x_absolute_row_sum(g, i, j, c, walls);
-                x.v(i, j) += (b.v(i, j) - q.v(i, j)) / y_absolute_row_sum(g, i, j, c, walls);
+                x.u(i, j) += (b.u(i, j) - q.u(i, j)) / rsu[(size_t)j * sx + i];
+                x.v(i, j) += (b.v(i, j) - q.v(i, j)) / rsv[(size_t)j * sx + i];
             });
         } else {
 #pragma omp parallel for schedule(static)
