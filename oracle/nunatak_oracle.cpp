@@ -269,7 +269,9 @@ static inline double shear_stress(const Grid& g, int i, int j, const Field& u, c
 static void ssa_operator(const Grid& g, VelocityVector& q, const VelocityVector& p, const Coefficients& c, int walls) {  // :47-52, :81-89
     const int Nx = g.Nx(), Ny = g.Ny(), sx = Nx + 3;
     const size_t n = (size_t)sx * (Ny + 3);
-    std::unique_ptr<double[]> mu(new double[n]), mv(new double[n]), txx(new double[n]), tyy(new double[n]), txy(new double[n]);
+    static thread_local std::vector<double> scratch;   // grown once, so repeated applies touch no new pages
+    if (scratch.size() < 5 * n) scratch.resize(5 * n);
+    double *mu = scratch.data(), *mv = mu + n, *txx = mv + n, *tyy = txx + n, *txy = tyy + n;
     auto at = [sx](int i, int j) { return (size_t)(j + 1) * sx + (i + 1); };   // i, j from -1
     const Field &eta = *c.etaH, &ff = *c.etaHff;
 #pragma omp parallel for schedule(static)
@@ -598,11 +600,14 @@ static void line_relax(const Grid& g, Field& x, const Field& b, Field& q, Field&
 static void smooth(const Grid& g, VelocityVector& x, const VelocityVector& b, VelocityVector& q, Field& t, const Coefficients& c,
                    int walls, int smoother, int sweeps) {
     // the ℓ1 row sums depend on the coefficients only: evaluated once for all sweeps, by the same functions
-    std::unique_ptr<double[]> rsu, rsv;
+    static thread_local std::vector<double> sums;
     const int sx = g.Nx() + 1;
+    const size_t n = (size_t)sx * (g.Ny() + 1);
+    double *rsu = nullptr, *rsv = nullptr;
     if (smoother == NK_SMOOTHER_POINT_JACOBI) {
-        rsu.reset(new double[(size_t)sx * (g.Ny() + 1)]);
-        rsv.reset(new double[(size_t)sx * (g.Ny() + 1)]);
+        if (sums.size() < 2 * n) sums.resize(2 * n);
+        rsu = sums.data();
+        rsv = rsu + n;
         for_xy(g.Nx(), g.Ny(), [&](int i, int j) {
             rsu[(size_t)j * sx + i] = x_absolute_row_sum(g, i, j, c, walls);
             rsv[(size_t)j * sx + i] = y_absolute_row_sum(g, i, j, c, walls);
