@@ -56,6 +56,11 @@ WORKLOAD = ("serving stream: 512 marine-sheet SSA solve requests, Poisson arriva
             "steps of {B} consecutive requests")
 N_REQUESTS = 512
 ARRIVAL_RATE = 200.0
+# How the CPU restatement's speed compares with the reference's own CPU code, on the reference's published scaling
+# benchmark (docs/src/model/numerics.md:47-48, one thread each, same iteration counts).
+ORACLE_CALIBRATION = ("one oracle thread takes about 5.5x the reference's published single-thread time on its multigrid "
+                      "scaling benchmark (1 km: 1.29 / 0.55 s diagonal / multigrid against 0.22 / 0.10 s; 0.5 km: 10.2 / 2.5 s "
+                      "against 1.9 / 0.43 s; a 2.7 GHz Xeon core against an AMD EPYC 9745 core)")
 
 
 def parse():
@@ -237,7 +242,8 @@ def run_reference(args, rank):
             "config": {"workload": WORKLOAD.format(B=1).replace(
                 "mixed precision (FP32 multigrid, FP64 outer CG / Picard)", "FP64 throughout"), "sample_grids": sizes},
             "latency_ms": {"p50": 1e3 * statistics.median(times), "p99": 1e3 * max(times)},
-            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": used, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": used, "kind": "port", "sample": sample,
+                             "calibration": ORACLE_CALIBRATION},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -747,6 +753,7 @@ def main():
                 if tr["index"] == r["index"] and k in kept:
                     errs[str(r["index"])] = rel_l2(kept[k][0], kept[k][1], uo, vo)
         line["cpu_baseline"] = {"value": len(reqs) / total, "unit": "solves/s", "cores": used, "kind": "port",
+                                "calibration": ORACLE_CALIBRATION,
                                 "sample": "FP64 solves of the stream's first 128x64 and first 256x128 requests "
                                           "(oracle restatement, multigrid PCG, OpenMP on all host cores)"}
         line["rel_error_mixed_vs_fp64_oracle"] = errs
