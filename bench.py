@@ -58,8 +58,8 @@ N_REQUESTS = 512
 ARRIVAL_RATE = 200.0
 # How the CPU restatement's speed compares with the reference's own CPU code, on the reference's published scaling
 # benchmark (docs/src/model/numerics.md:47-48, one thread each, same iteration counts).
-ORACLE_CALIBRATION = ("one oracle thread takes about 5.5x the reference's published single-thread time on its multigrid "
-                      "scaling benchmark (1 km: 1.29 / 0.55 s diagonal / multigrid against 0.22 / 0.10 s; 0.5 km: 10.2 / 2.5 s "
+ORACLE_CALIBRATION = ("one oracle thread takes 3.7-5.6x the reference's published single-thread time on its multigrid "
+                      "scaling benchmark (1 km: 0.85 / 0.55 s diagonal / multigrid against 0.22 / 0.10 s; 0.5 km: 7.0 / 2.4 s "
                       "against 1.9 / 0.43 s; a 2.7 GHz Xeon core against an AMD EPYC 9745 core)")
 
 

@@ -338,13 +338,6 @@ static inline double y_diagonal(const Grid& g, int i, int j, const Coefficients&
                y_shear_diagonal(g, i, j, *c.etaHff, walls) + y_shear_diagonal(g, i + 1, j, *c.etaHff, walls);
     return (inactive_cf(g, i, j, c.etaH) || d == 0.0) ? 1.0 : d;
 }
-static void diagonal_precondition(const Grid& g, VelocityVector& z, const VelocityVector& r, const Coefficients& c, int walls) {  // :11-18, 46-54
-    int nux = z.u.nx(), nuy = z.u.ny(), nvx = z.v.nx(), nvy = z.v.ny();
-#pragma omp parallel for schedule(static)
-    for (int j = 1; j <= nuy; ++j) for (int i = 1; i <= nux; ++i) z.u(i, j) = r.u(i, j) / x_diagonal(g, i, j, c, walls);
-#pragma omp parallel for schedule(static)
-    for (int j = 1; j <= nvy; ++j) for (int i = 1; i <= nvx; ++i) z.v(i, j) = r.v(i, j) / y_diagonal(g, i, j, c, walls);
-}
 
 // ------------------------------------------------------------------------------------------------
 // Vector operations, src/Solvers/velocity_vector.jl:48-141.  All act on the Nx x Ny range.
@@ -838,6 +831,7 @@ struct Problem {
     VelocityVector r, z, p, q, w, xprev;
     Field eta_prev;               // η̄H of the previous Picard iteration (NK_VISCOSITY_CONVERGENCE)
     Multigrid mg;
+    VelocityVector diag;          // the operator diagonal of the current coefficients (diagonal preconditioner)
     bool mg_ready = false;
 };
 
@@ -854,15 +848,35 @@ static void impose_prescribed(Problem& P, VelocityVector& x, const VelocityVecto
     fill_halo(x);
 }
 
-static void update_preconditioner(Problem& P) {   // conjugate_gradient.jl:36; multigrid_preconditioner.jl:128
+// conjugate_gradient.jl:36; multigrid_preconditioner.jl:128.  The diagonal preconditioner recomputes the operator
+// diagonal from the coefficients at every application (diagonal_preconditioner.jl:11-18); the coefficients are
+// fixed during a solve, so it is taken here once per solve, by the same functions, and divided by as before.
+static void update_preconditioner(Problem& P) {
     if (P.sdesc.preconditioner == NK_PRECONDITIONER_MULTIGRID) coarsen_coefficients(P.mg.levels, 0, P.etaH, P.bu, P.bv);
+    if (P.sdesc.preconditioner == NK_PRECONDITIONER_DIAGONAL) {
+        const Grid& g = P.grid;
+        Coefficients c{&P.etaH, &P.etaHff, &P.bu, &P.bv};
+        if (!P.diag.u.g) P.diag.init(&g);
+        int nux = P.diag.u.nx(), nuy = P.diag.u.ny(), nvx = P.diag.v.nx(), nvy = P.diag.v.ny();
+#pragma omp parallel for schedule(static)
+        for (int j = 1; j <= nuy; ++j) for (int i = 1; i <= nux; ++i) P.diag.u(i, j) = x_diagonal(g, i, j, c, P.ph.walls);
+#pragma omp parallel for schedule(static)
+        for (int j = 1; j <= nvy; ++j) for (int i = 1; i <= nvx; ++i) P.diag.v(i, j) = y_diagonal(g, i, j, c, P.ph.walls);
+    }
 }
 
 static void precondition(Problem& P, VelocityVector& z, VelocityVector& r) {
     Coefficients c = coeffs(P);
     switch (P.sdesc.preconditioner) {
         case NK_PRECONDITIONER_NONE: copyto(P.grid, z, r); break;                        // conjugate_gradient.jl:33
-        case NK_PRECONDITIONER_DIAGONAL: diagonal_precondition(P.grid, z, r, c, P.ph.walls); break;
+        case NK_PRECONDITIONER_DIAGONAL: {   // z = r / diag, diagonal_preconditioner.jl:11-18, 46-54
+            int nux = z.u.nx(), nuy = z.u.ny(), nvx = z.v.nx(), nvy = z.v.ny();
+#pragma omp parallel for schedule(static)
+            for (int j = 1; j <= nuy; ++j) for (int i = 1; i <= nux; ++i) z.u(i, j) = r.u(i, j) / P.diag.u(i, j);
+#pragma omp parallel for schedule(static)
+            for (int j = 1; j <= nvy; ++j) for (int i = 1; i <= nvx; ++i) z.v(i, j) = r.v(i, j) / P.diag.v(i, j);
+            break;
+        }
         default: v_cycle(P.grid, z, r, P.mg.residual, P.mg.scratch, c, P.mg, 0, P.ph.walls); break;  // multigrid :122-126
     }
 }
