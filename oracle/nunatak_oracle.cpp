@@ -826,6 +826,10 @@ struct Problem {
     Field H, bed, s, mu, phi, phu, phv, N, C, A2, etaH, etaHff, bu, bv, F2, bbu, bbv, ub, vb;
     SigmaField A3, eta_s, T, us, vs;
     SigmaField E, omega;          // enthalpy and water fraction (nko_compute_thermal_diagnostics)
+    // energy step (nko_step_enthalpy): basal water Hw, grounded melt mᵍ (gmelt), geothermal flux G, surface and ocean
+    // temperatures, basal melt rate m, thickness of the previous energy step Hⁿ, strain heating Φ
+    Field Hw, gmelt, G, Ts, To, melt, Hn;
+    SigmaField Phi;
 
     // CG workspace (VelocityConjugateGradientSolver, conjugate_gradient.jl:52-102) and Picard x⁻
     VelocityVector r, z, p, q, w, xprev;
@@ -1533,6 +1537,192 @@ static int picard_adjoint(Problem& P, const VelocityVector& xbar, const nk_itera
     return st->status;
 }
 
+// ------------------------------------------------------------------------------------------------
+// One energy step of EnthalpyThermodynamics (TEST INFRASTRUCTURE: no library counterpart yet).
+// step_thermodynamics! / advance_enthalpy!, src/Thermodynamics/column_energy_solve.jl:26-78: the strain heating of
+// the current velocities (strain_heating.jl:7-56), the layer volume fluxes (layer_transport.jl:34-44), the basal
+// state (column_energy_solve.jl:127-146), one implicit tridiagonal system per column (:148-221), solved by the
+// Thomas algorithm (Oceananigans' BatchedTridiagonalSolver in z: row k reads a[k-1] E[k-1] + b[k] E[k] +
+// c[k] E[k+1] = f[k]), the basal water and drainage (:223-259), then the thermal diagnostics (:112-117).
+// prm: the EnthalpyThermodynamics constants in the order of struct EnergyParams.
+// ------------------------------------------------------------------------------------------------
+struct EnergyParams {
+    double k, c, L, beta, T0, Tr;              // conductivity, heat capacity, latent heat, Clausius-Clapeyron, melting, reference
+    double temperate_ratio, blend, water_blend, min_thickness, drainage_fraction, max_drainage_rate;
+    int coupled;                               // grounded_melt_coupling
+};
+
+static inline double unit_ramp(double x, double w) { return std::min(std::max(x / w, 0.0), 1.0); }   // enthalpy_conversions.jl:69
+
+static void step_enthalpy(Problem& P, const EnergyParams& q, double dt) {
+    const Grid& g = P.grid;
+    const Sigma& sg = P.sigma;
+    const int Ns = sg.N, Nx = g.Nx(), Ny = g.Ny();
+    const double rho = P.ph.rho_i, ga = P.ph.g;
+    const bool diva = P.stress_balance == NK_DIVA;
+    const Field& bu = diva ? P.bbu : P.bu;   // basal_drag(::SSA) = (βᵘ, βᵛ), (::DIVA) = (βᵇᵘ, βᵇᵛ), column_energy_solve.jl:18-20
+    const Field& bv = diva ? P.bbv : P.bv;
+    auto Tpm = [&](double p) { return q.T0 - q.beta * p; };                                   // :6
+    auto Epm = [&](double p) { return q.c * (Tpm(p) - q.Tr); };                               // :13
+    auto enthalpy = [&](double T, double w, double p) { return q.c * (std::min(T, Tpm(p)) - q.Tr) + w * q.L; };   // :49-52
+    auto water_fraction = [&](double E, double p) { return std::max(0.0, E - Epm(p)) / q.L; };   // :42
+    auto thickness = [&](double H) { return std::max(H, q.min_thickness); };                 // column_thickness, :56
+    auto layer_pressure = [&](int i, int j, int k) { return rho * ga * P.H(i, j) * (1 - sg.zc(k)); };   // :61-64
+    auto diffusivity = [&](int i, int j, int k) {                                             // layer_diffusivity, :72-78
+        double w = unit_ramp(P.E.k[k - 1](i, j) - Epm(layer_pressure(i, j, k)) + q.blend, q.blend);
+        return q.k / q.c * (1 - w + w * q.temperate_ratio);
+    };
+    auto grounded_part = [&](int i, int j) { return P.grounding ? P.phi(i, j) : 1.0; };        // :118-119
+    for (int k = 0; k < Ns; ++k) fill_halo(P.E.k[k]);
+    for (Field* f : {&P.Hw, &P.gmelt, &P.G, &P.Ts, &P.To, &P.melt, &P.Hn}) fill_halo(*f);
+
+    // strain heating Φ = 4 η ε̇ₑ² (membrane, without ε̇₀), plus τᵇ² w₂ₖ / Δζₖ / η for DIVA (strain_heating.jl:43-56)
+    fill_halo(P.x);
+    for_xy(Nx, Ny, [&](int i, int j) {
+        double e2 = effective_strain_rate2(g, i, j, P.x.u, P.x.v, P.ph.walls);
+        double tb2 = 0;
+        if (diva) {
+            auto sq = [](double a) { return a * a; };
+            tb2 = (sq(P.bbu(i, j) * P.ub(i, j)) + sq(P.bbu(i + 1, j) * P.ub(i + 1, j))) / 2 +
+                  (sq(P.bbv(i, j) * P.vb(i, j)) + sq(P.bbv(i, j + 1) * P.vb(i, j + 1))) / 2;
+        }
+        for (int k = 1; k <= Ns; ++k) {
+            double eta = P.eta_s.k[k - 1](i, j);
+            double phi = 4 * eta * e2;
+            if (diva) phi += tb2 * layer_weight(sg, k, 2) / layer_thickness(sg, k) / (eta == 0.0 ? std::numeric_limits<double>::infinity() : eta);
+            P.Phi.k[k - 1](i, j) = phi;
+        }
+    });
+
+    // layer volume fluxes W (faces 1..Nσ+1 of each column), layer_transport.jl:8-44
+    auto layer_u = [&](int i, int j, int k) { return g.peripheral_fc(i, j) ? 0.0 : P.us.k[k - 1](i, j); };
+    auto layer_v = [&](int i, int j, int k) { return g.peripheral_cf(i, j) ? 0.0 : P.vs.k[k - 1](i, j); };
+    auto upwind = [](double u, double cm, double cp) { return u > 0 ? cm : cp; };
+    auto xvol = [&](int i, int j, int k) { double u = layer_u(i, j, k); return g.dy_c(j) * u * upwind(u, P.Hn(i - 1, j), P.Hn(i, j)); };
+    auto yvol = [&](int i, int j, int k) { double v = layer_v(i, j, k); return g.dx_c(i) * v * upwind(v, P.Hn(i, j - 1), P.Hn(i, j)); };
+    auto xenth = [&](int i, int j, int k) { return xvol(i, j, k) * upwind(P.us.k[k - 1](i, j), P.E.k[k - 1](i - 1, j), P.E.k[k - 1](i, j)); };
+    auto yenth = [&](int i, int j, int k) { return yvol(i, j, k) * upwind(P.vs.k[k - 1](i, j), P.E.k[k - 1](i, j - 1), P.E.k[k - 1](i, j)); };
+    for (int k = 1; k <= Ns; ++k) { fill_halo(P.us.k[k - 1]); fill_halo(P.vs.k[k - 1]); }
+
+    std::vector<double> W((size_t)(Ns + 1) * Nx * Ny), rb((size_t)Nx * Ny), sb(rb.size()), Db(rb.size()), qg(rb.size());
+    auto col = [&](int i, int j) { return (size_t)(j - 1) * Nx + (i - 1); };
+    for_xy(Nx, Ny, [&](int i, int j) {
+        double* w = &W[col(i, j) * (Ns + 1)];
+        double dHdt = (thickness(P.H(i, j)) - thickness(P.Hn(i, j))) / dt;
+        double m = P.grounding ? (1 - P.phi(i, j)) * P.melt(i, j) : P.melt(i, j);   // basal_melt, time_stepping.jl:51-52
+        w[0] = -m - (q.coupled ? P.gmelt(i, j) : 0.0);
+        for (int k = 1; k <= Ns; ++k) {
+            double div = (xvol(i + 1, j, k) - xvol(i, j, k) + yvol(i, j + 1, k) - yvol(i, j, k)) / g.Az_ccc(i, j);
+            w[k] = w[k - 1] - layer_thickness(sg, k) * (dHdt + div);
+        }
+        // basal state, column_energy_solve.jl:127-146
+        double Ht = thickness(P.H(i, j));
+        double D = diffusivity(i, j, 1) / (Ht * sg.zc(1));
+        double F = (bu(i, j) * P.ub(i, j) * P.ub(i, j) + bu(i + 1, j) * P.ub(i + 1, j) * P.ub(i + 1, j) +
+                    bv(i, j) * P.vb(i, j) * P.vb(i, j) + bv(i, j + 1) * P.vb(i, j + 1) * P.vb(i, j + 1)) / 2;
+        double Epm_b = Epm(rho * ga * P.H(i, j));
+        double Eb = P.E.k[0](i, j) + (P.G(i, j) + F) / D;
+        double r = std::max(unit_ramp(Eb - Epm_b, q.blend), unit_ramp(P.Hw(i, j), q.water_blend));
+        double E1pm = Epm(layer_pressure(i, j, 1));
+        Db[col(i, j)] = D;
+        rb[col(i, j)] = r;
+        sb[col(i, j)] = unit_ramp(P.E.k[0](i, j) - E1pm + q.blend, q.blend);
+        qg[col(i, j)] = grounded_part(i, j) * P.G(i, j) + F;
+    });
+
+    // the column systems (from the old E), then the Thomas solve into E
+    std::vector<double> a((size_t)Ns * Nx * Ny), b(a.size()), cc(a.size()), f(a.size());
+    for_xy(Nx, Ny, [&](int i, int j) {
+        size_t o = col(i, j) * Ns;
+        const double* w = &W[col(i, j) * (Ns + 1)];
+        double Ht = thickness(P.H(i, j)), Hnt = thickness(P.Hn(i, j));
+        bool mu = P.H(i, j) > q.min_thickness;                                   // column_has_ice, :58
+        double Es = enthalpy(P.Ts(i, j), 0.0, 0.0);                              // surface_enthalpy, :54
+        double phi = grounded_part(i, j), r = rb[col(i, j)];
+        double chi = phi * r * (1 - sb[col(i, j)]);
+        double pb = rho * ga * P.H(i, j);
+        double Epm_b = Epm(pb), Eo = enthalpy(P.To(i, j), 0.0, pb);
+        double Fb = rho * w[0];
+        double Lam = Db[col(i, j)] * (chi + 1 - phi) + std::max(-Fb, 0.0);
+        double S = (1 - r) * qg[col(i, j)] + Db[col(i, j)] * (chi * Epm_b + (1 - phi) * Eo) + std::max(Fb, 0.0) * Epm_b;
+        double Fs = rho * w[Ns];
+        double Ks = diffusivity(i, j, Ns) / (Ht * (1 - sg.zc(Ns)));             // surface_conductance, :160-165
+        double Ds = Ks + std::max(Fs, 0.0), Ss = (Ks + std::max(-Fs, 0.0)) * Es;
+        auto couplings = [&](int kf, double& lower, double& upper) {            // face_couplings, :169-177, interior face kf
+            double zf = sg.zf(kf), zm = sg.zc(kf - 1), zp = sg.zc(kf);
+            double theta = (zf - zm) / (zp - zm);
+            double Fk = rho * w[kf - 1];
+            double cond = 1 / (Ht * ((zf - zm) / diffusivity(i, j, kf - 1) + (zp - zf) / diffusivity(i, j, kf)));   // face_conductance
+            double Dk = std::max(cond, std::max(std::max(Fk, 0.0) * theta, std::max(-Fk, 0.0) * (1 - theta)));
+            lower = -Fk * (1 - theta) - Dk;
+            upper = Fk * theta - Dk;
+        };
+        for (int k = 1; k <= Ns; ++k) {
+            double dz = layer_thickness(sg, k);
+            double lower_m = 0, upper_m = 0, lower_p = 0, upper_p = 0;
+            if (k > 1) couplings(k, lower_m, upper_m);
+            if (k < Ns) couplings(k + 1, lower_p, upper_p);
+            double diag_m = k == 1 ? Lam : -upper_m;
+            double diag_p = k == Ns ? Ds : -lower_p;
+            double forcing = (k == 1 ? S : 0.0) + (k == Ns ? Ss : 0.0);
+            double transport = rho * dz * ((xenth(i + 1, j, k) - xenth(i, j, k) + yenth(i, j + 1, k) - yenth(i, j, k)) / g.Az_ccc(i, j));
+            a[o + k - 1] = mu ? lower_p : 0.0;
+            cc[o + k - 1] = mu ? upper_p : 0.0;
+            b[o + k - 1] = mu ? rho * Ht * dz / dt + diag_m + diag_p : 1.0;
+            f[o + k - 1] = mu ? rho * Hnt * dz * P.E.k[k - 1](i, j) / dt - transport + Ht * dz * P.Phi.k[k - 1](i, j) + forcing : Es;
+        }
+    });
+    for_xy(Nx, Ny, [&](int i, int j) {                                          // Thomas algorithm, top-down then back
+        size_t o = col(i, j) * Ns;
+        std::vector<double> t(Ns + 1, 0.0), e(Ns + 1, 0.0);
+        double beta_ = b[o];
+        e[1] = f[o] / beta_;
+        for (int k = 2; k <= Ns; ++k) {
+            t[k] = cc[o + k - 2] / beta_;
+            beta_ = b[o + k - 1] - a[o + k - 2] * t[k];
+            e[k] = (f[o + k - 1] - a[o + k - 2] * e[k - 1]) / beta_;
+        }
+        for (int k = Ns - 1; k >= 1; --k) e[k] -= t[k + 1] * e[k + 1];
+        for (int k = 1; k <= Ns; ++k) P.E.k[k - 1](i, j) = e[k];
+    });
+
+    // basal water and drainage, column_energy_solve.jl:223-259 (no till: drain_till leaves Hw)
+    for_xy(Nx, Ny, [&](int i, int j) {
+        double Ht = thickness(P.H(i, j));
+        bool mu = P.H(i, j) > q.min_thickness;
+        double Epm_b = Epm(rho * ga * P.H(i, j));
+        double qb = Db[col(i, j)] * (Epm_b - P.E.k[0](i, j));
+        double m = rb[col(i, j)] * (qg[col(i, j)] - grounded_part(i, j) * (1 - sb[col(i, j)]) * qb) / (rho * q.L);
+        double drained = 0;
+        for (int k = 1; k <= Ns; ++k) {
+            double w = water_fraction(P.E.k[k - 1](i, j), layer_pressure(i, j, k));
+            double x = w / q.drainage_fraction;                                   // drainage_rate, :212-216
+            double rate = q.max_drainage_rate * (std::min(std::max(x - 1, 0.0), 1.0) / 10 + 9 * std::min(std::max(x - 2, 0.0), 1.0) / 10);
+            double dw = std::min(dt * rate, std::max(w - q.drainage_fraction, 0.0));
+            dw = mu ? dw : 0.0;
+            P.E.k[k - 1](i, j) -= q.L * dw;
+            drained += Ht * layer_thickness(sg, k) * dw;
+        }
+        double Hstar = P.Hw(i, j) + dt * (mu ? m : 0.0) + drained;
+        double Hplus = std::max(0.0, Hstar);
+        double missing = Hplus - Hstar;
+        P.gmelt(i, j) = (Hplus - P.Hw(i, j)) / dt;
+        P.Hw(i, j) = Hplus;
+        P.E.k[0](i, j) -= q.L * missing / (Ht * layer_thickness(sg, 1));
+    });
+
+    // thermal diagnostics (T and the water fraction), and Hⁿ = H
+    for (int k = 1; k <= Ns; ++k)
+        for_xy(Nx, Ny, [&](int i, int j) {
+            double p = layer_pressure(i, j, k), E = P.E.k[k - 1](i, j);
+            P.T.k[k - 1](i, j) = std::min(Tpm(p), q.Tr + E / q.c);
+            P.omega.k[k - 1](i, j) = water_fraction(E, p);
+        });
+    for_xy(Nx, Ny, [&](int i, int j) { P.Hn(i, j) = P.H(i, j); });
+    for (int k = 0; k < Ns; ++k) { fill_halo(P.E.k[k]); fill_halo(P.T.k[k]); fill_halo(P.omega.k[k]); }
+    for (Field* f : {&P.Hw, &P.gmelt, &P.Hn}) fill_halo(*f);
+}
+
 // ---- field access in interior layout -------------------------------------------------------------
 struct FieldRef { Field* f = nullptr; SigmaField* s = nullptr; };
 
@@ -1642,6 +1832,8 @@ nk_status nko_problem_create(const nk_grid_desc* gd, const nk_physics_desc* pd, 
     P->etaHff.init(g, FACE, FACE);
     P->A3.init(g, CENTER, CENTER, gd->Nsigma); P->eta_s.init(g, CENTER, CENTER, gd->Nsigma); P->T.init(g, CENTER, CENTER, gd->Nsigma);
     P->E.init(g, CENTER, CENTER, gd->Nsigma); P->omega.init(g, CENTER, CENTER, gd->Nsigma);
+    for (Field* f : {&P->Hw, &P->gmelt, &P->G, &P->Ts, &P->To, &P->melt, &P->Hn}) f->init(g, CENTER, CENTER);
+    P->Phi.init(g, CENTER, CENTER, gd->Nsigma);
     P->us.init(g, FACE, CENTER, gd->Nsigma); P->vs.init(g, CENTER, FACE, gd->Nsigma);
     P->r.init(g); P->z.init(g); P->p.init(g); P->q.init(g); P->w.init(g); P->xprev.init(g);
     P->eta_prev.init(g, CENTER, CENTER);
@@ -1745,6 +1937,41 @@ nk_status nko_compute_thermal_diagnostics(nko_problem* h, const nk_thermal_param
         });
         fill_halo(P.T.k[k - 1]); fill_halo(P.omega.k[k - 1]); fill_halo(P.A3.k[k - 1]);
     }
+    return NK_OK;
+}
+
+// The energy step's own fields (no library counterpart yet): which = 0 Hw, 1 mᵍ, 2 G, 3 Tₛ, 4 Tₒ, 5 basal melt rate,
+// 6 Hⁿ (2-D), 7 Φ (σ grid); set = 1 copies data in, 0 out.
+nk_status nko_energy_field(nko_problem* h, int32_t which, double* data, int64_t count, int32_t set) {
+    if (!h || !data) return NK_BAD_ARGUMENT;
+    Problem& P = *reinterpret_cast<Problem*>(h);
+    Field* two[] = {&P.Hw, &P.gmelt, &P.G, &P.Ts, &P.To, &P.melt, &P.Hn};
+    if (which >= 0 && which < 7) {
+        Field& f = *two[which];
+        if (count != (int64_t)f.nx() * f.ny()) return NK_BAD_ARGUMENT;
+        if (set) copy_in(f, data); else copy_out(f, data);
+        return NK_OK;
+    }
+    if (which == 7) {
+        size_t plane = (size_t)P.grid.Nx() * P.grid.Ny();
+        if (count != (int64_t)(plane * P.Phi.k.size())) return NK_BAD_ARGUMENT;
+        for (size_t k = 0; k < P.Phi.k.size(); ++k) {
+            if (set) copy_in(P.Phi.k[k], data + k * plane); else copy_out(P.Phi.k[k], data + k * plane);
+        }
+        return NK_OK;
+    }
+    return NK_BAD_ARGUMENT;
+}
+
+// One energy step of length dt (step_thermodynamics!, src/Thermodynamics/column_energy_solve.jl:26-31).  prm: thermal
+// conductivity, heat capacity, latent heat, Clausius-Clapeyron slope, melting and reference temperatures, temperate
+// diffusivity ratio, enthalpy blend width, water layer blend thickness, minimum thickness, drainage water fraction,
+// maximum drainage rate, grounded melt coupling (0 / 1): EnthalpyThermodynamics' keywords
+// (src/Thermodynamics/enthalpy_thermodynamics.jl:92-110).
+nk_status nko_step_enthalpy(nko_problem* h, const double* prm, double dt) {
+    if (!h || !prm || !(dt > 0)) return NK_BAD_ARGUMENT;
+    EnergyParams q{prm[0], prm[1], prm[2], prm[3], prm[4], prm[5], prm[6], prm[7], prm[8], prm[9], prm[10], prm[11], prm[12] != 0.0};
+    step_enthalpy(*reinterpret_cast<Problem*>(h), q, dt);
     return NK_OK;
 }
 

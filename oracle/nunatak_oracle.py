@@ -46,6 +46,8 @@ def load():
             "nko_picard_solve": [vp, C.POINTER(abi.SolveStats)],
             "nko_velocity_profile": [vp],
             "nko_compute_thermal_diagnostics": [vp, C.POINTER(abi.ThermalParams)],
+            "nko_energy_field": [vp, C.c_int32, dp, i64, C.c_int32],
+            "nko_step_enthalpy": [vp, dp, C.c_double],
             "nko_picard_adjoint": [vp, dp, dp, C.POINTER(abi.IterationControl), dp, dp, dp, dp, C.POINTER(abi.SolveStats)],
             "nko_multigrid_levels": [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), i32],
             "nko_multigrid_restrict": [vp, i32, dp, dp, dp, dp],
@@ -80,6 +82,32 @@ class OracleProblem(Problem):
 
     def adjoint_solve(self, bu, bv):
         return self.linear_solve(bu, bv)
+
+    # ---- the energy step (test infrastructure for EnthalpyThermodynamics; no library counterpart yet) ----
+    ENERGY_FIELDS = {"Hw": 0, "grounded_melt": 1, "geothermal_flux": 2, "surface_temperature": 3,
+                     "ocean_temperature": 4, "basal_melt_rate": 5, "H_previous": 6, "strain_heating": 7}
+
+    def _energy_shape(self, name):
+        return (self.Nsigma, self.grid.Ny, self.grid.Nx) if name == "strain_heating" else (self.grid.Ny, self.grid.Nx)
+
+    def energy_set(self, name, value):
+        a = np.ascontiguousarray(np.broadcast_to(np.asarray(value, dtype=np.float64), self._energy_shape(name)))
+        _check(self._lib.nko_energy_field(self._h, self.ENERGY_FIELDS[name], a.ctypes.data_as(_dptr), a.size, 1), "energy_set")
+
+    def energy_get(self, name):
+        a = np.empty(self._energy_shape(name))
+        _check(self._lib.nko_energy_field(self._h, self.ENERGY_FIELDS[name], a.ctypes.data_as(_dptr), a.size, 0), "energy_get")
+        return a
+
+    def step_enthalpy(self, dt, thermal_conductivity=2.1, heat_capacity=2009.0, latent_heat=3.34e5, clausius_clapeyron=7.9e-8,
+                      melting_temperature=273.15, reference_temperature=223.15, temperate_diffusivity_ratio=1e-3,
+                      enthalpy_blend_width=1.0, water_layer_blend_thickness=1e-3, minimum_thickness=1.0,
+                      drainage_water_fraction=0.01, maximum_drainage_rate=1.58443823077064e-9, grounded_melt_coupling=True):
+        """One energy step of length dt (step_thermodynamics!); defaults: EnthalpyThermodynamics'."""
+        prm = np.array([thermal_conductivity, heat_capacity, latent_heat, clausius_clapeyron, melting_temperature,
+                        reference_temperature, temperate_diffusivity_ratio, enthalpy_blend_width, water_layer_blend_thickness,
+                        minimum_thickness, drainage_water_fraction, maximum_drainage_rate, float(grounded_melt_coupling)])
+        _check(self._lib.nko_step_enthalpy(self._h, prm.ctypes.data_as(_dptr), float(dt)), "step_enthalpy")
 
     def grid_metrics(self, which):
         n = (self.grid.Nx if which in (0,) else self.grid.Nx + 1 if which == 1 else self.grid.Ny if which == 2 else self.grid.Ny + 1)

@@ -1,0 +1,172 @@
+"""The oracle's energy step (nko_step_enthalpy: step_thermodynamics!, src/Thermodynamics/column_energy_solve.jl:26-78)
+against the column testsets of test/test_thermodynamics.jl.  Test infrastructure for the enthalpy row that comes
+after the velocity solve: the library has no energy step yet, so these run on the oracle only.
+
+column_model (test/test_thermodynamics.jl:3-14): one Periodic column, 1 km wide, ρᵢ = 910, no velocity solve and
+no thickness change, so each time step is one energy step of the same length:
+- steady conduction on uniform and refined layers is linear in height, T = Tₛ + G H (1 - ζ) / k, within 1e-8 K
+  after four 1e14 s steps, with no basal water (:116-128);
+- surface warming by 10 K converges at second order to the Fourier series of the step response (:130-156);
+- the column energy changes by Δt (G + β uᵇ² - surface flux) at every step, within 1e-11 (:158-173);
+- a warm base melts at the analytic rate (G - k (T_pm - Tₛ) / H) / (ρᵢ L) within 1e-3, and once the geothermal
+  flux stops, refreezes its stored water while the total energy stays balanced within 1e-10 (:175-208);
+- a floating base sits at the ocean temperature, T linear from Tₒ to Tₛ, with no grounded melt (:210-222);
+- an ice-free column holds the surface enthalpy (:224-231)."""
+import math
+
+import numpy as np
+import pytest
+
+from nunatak_gb300 import model as M
+from support import make
+
+K, CI, LATENT, BETA, T0, TR = 2.1, 2009.0, 3.34e5, 7.9e-8, 273.15, 223.15
+RHO, GRAV = 910.0, 9.81
+
+
+def enthalpy(T, omega, p):
+    """enthalpy(T, ω, p, parameters), src/Thermodynamics/enthalpy_conversions.jl:49-52."""
+    return CI * (np.minimum(T, T0 - BETA * p) - TR) + omega * LATENT
+
+
+class Column:
+    """column_model(; H₀, Nσ, bed_refinement, geothermal_flux, surface_temperature, grounding, bed) on the oracle."""
+
+    def __init__(self, cls, H0=1000.0, Nsigma=10, bed_refinement=1.0, G=0.042, Ts=243.15, grounding=None, bed=0.0):
+        g = M.RectilinearGrid(size=(1, 1), x=(0.0, 1e3), y=(0.0, 1e3), topology=("Periodic", "Periodic"), halo=(3, 3))
+        self.P = make(cls, g, Nsigma=Nsigma, bed_refinement=bed_refinement, rheology=M.GlenFlowLaw(rate_factor="sigma"),
+                      constants=M.IceSheetConstants(ice_density=RHO), grounding=grounding)
+        self.H0 = H0
+        self.P.set("H", H0)
+        self.P.set("bed", bed)
+        self.P.compute_geometry()
+        faces = np.array(M.sigma_faces(Nsigma, bed_refinement))
+        self.faces, self.zeta = faces, (faces[1:] + faces[:-1]) / 2
+        self.pressure = RHO * GRAV * H0 * (1 - self.zeta)
+        for name, value in (("geothermal_flux", G), ("surface_temperature", Ts), ("ocean_temperature", 271.15),
+                            ("basal_melt_rate", 0.0), ("H_previous", H0), ("Hw", 0.0)):
+            self.P.energy_set(name, value)
+        self.set_temperature(np.full(Nsigma, Ts))   # a new model holds the surface enthalpy
+        self.set_enthalpy(np.full(Nsigma, enthalpy(Ts, 0.0, 0.0)))
+
+    def set_temperature(self, T):
+        self.set_enthalpy(enthalpy(np.asarray(T, dtype=np.float64), 0.0, self.pressure))
+
+    def set_enthalpy(self, E):
+        self.P.set("E", np.asarray(E, dtype=np.float64).reshape(-1, 1, 1))
+
+    def step(self, dt):
+        self.P.step_enthalpy(dt, grounded_melt_coupling=False)
+
+    def column(self, name):
+        return self.P.get(name)[:, 0, 0]
+
+    def value(self, name):
+        return float(self.P.energy_get(name)[0, 0])
+
+    def energy(self):
+        """ρ ∫E dz per unit area."""
+        return RHO * self.H0 * float(np.sum(np.diff(self.faces) * self.column("E")))
+
+    def surface_heat_flux(self, Ts):
+        EN, Es = self.column("E")[-1], CI * (Ts - TR)
+        return K / CI * (EN - Es) / (self.H0 * (1 - self.zeta[-1]))
+
+
+@pytest.mark.parametrize("bed_refinement", [1.0, 2.0])
+def test_steady_conduction_is_linear_in_height(oracle_cls, bed_refinement):
+    H0, G, Ts = 1000.0, 0.042, 243.15
+    c = Column(oracle_cls, H0=H0, G=G, Ts=Ts, bed_refinement=bed_refinement)
+    for _ in range(4):
+        c.step(1e14)
+    exact = Ts + G * H0 * (1 - c.zeta) / K
+    assert np.max(np.abs(c.column("T") - exact)) < 1e-8
+    assert c.value("Hw") == 0.0
+
+
+def test_surface_warming_converges_at_second_order(oracle_cls):
+    H0, G, Ts, dT, t_end = 1000.0, 0.042, 243.15, 10.0, 6.3e10
+    errors = []
+    for Nsigma in (10, 20, 40):
+        c = Column(oracle_cls, H0=H0, Nsigma=Nsigma, G=G, Ts=Ts)
+        c.set_temperature(Ts + G * H0 * (1 - c.zeta) / K)
+        c.P.energy_set("surface_temperature", Ts + dT)
+        Nt = 4 * Nsigma ** 2
+        for _ in range(Nt):
+            c.step(t_end / Nt)
+        kappa = K / (RHO * CI)
+        z = c.zeta * H0
+        steady = Ts + dT + G * (H0 - z) / K
+        transient = np.zeros_like(z)
+        for n in range(201):
+            lam = (2 * n + 1) * math.pi / (2 * H0)
+            transient += -dT * 4 / math.pi * (-1) ** n / (2 * n + 1) * np.cos(lam * z) * math.exp(-kappa * lam ** 2 * t_end)
+        errors.append(float(np.max(np.abs(c.column("T") - (steady + transient)))))
+    assert errors[2] < 0.01
+    assert errors[0] / errors[1] > 3 and errors[1] / errors[2] > 3
+
+
+def test_energy_budget_closes_with_geothermal_and_frictional_heating(oracle_cls):
+    H0, G, Ts = 800.0, 0.05, 243.15
+    c = Column(oracle_cls, H0=H0, G=G, Nsigma=12, bed_refinement=2.0, Ts=Ts)
+    c.set_temperature(250 - 5 * c.zeta)
+    beta, ub = 1e8, 1e-6
+    c.P.set("beta_u", beta)
+    c.P.set("u_b", ub)
+    F = beta * ub ** 2
+    dt = 1e9
+    for _ in range(50):
+        before = c.energy()
+        c.step(dt)
+        budget = c.energy() - before - dt * (G + F - c.surface_heat_flux(Ts))
+        assert abs(budget) < 1e-11 * abs(before)
+
+
+def test_warm_base_melts_at_the_analytic_rate_then_refreezes(oracle_cls):
+    H0, G, Ts = 1000.0, 0.1, 263.15
+    c = Column(oracle_cls, H0=H0, G=G, Ts=Ts, Nsigma=20)
+    Tpm = T0 - BETA * RHO * GRAV * H0
+    for _ in range(20):
+        c.step(1e13)
+    exact = (G - K * (Tpm - Ts) / H0) / (RHO * LATENT)
+    assert exact > 0
+    assert abs(c.value("grounded_melt") - exact) <= 1e-3 * exact
+    assert c.value("Hw") > 0
+    # too little water for one step, so the column pays back the excess latent heat itself
+    c.P.energy_set("Hw", 1e-2)
+    c.P.energy_set("geothermal_flux", 0.0)
+    dt = 1e9
+
+    def total():
+        return c.energy() + RHO * LATENT * c.value("Hw")
+
+    froze_out = False
+    for _ in range(200):
+        before = total()
+        c.step(dt)
+        q = K / CI * (c.column("E")[-1] - CI * (Ts - TR)) / (H0 * (1 - c.zeta[-1]))
+        assert abs(total() - before + dt * q) < 1e-10 * abs(before)
+        froze_out |= c.value("Hw") == 0.0
+    assert froze_out
+    assert c.value("grounded_melt") == 0.0
+
+
+def test_floating_base_sits_at_the_ocean_temperature(oracle_cls):
+    H0, Ts = 500.0, 253.15
+    c = Column(oracle_cls, H0=H0, Ts=Ts, G=0.05, grounding=M.SubgridGroundedFraction(), bed=-3000.0)
+    assert c.P.get("phi")[0, 0] == 0.0
+    for _ in range(4):
+        c.step(1e14)
+    To = 271.15
+    exact = To + (Ts - To) * c.zeta
+    assert np.max(np.abs(c.column("T") - exact)) < 1e-8
+    assert c.value("grounded_melt") == 0.0
+
+
+def test_ice_free_columns_hold_the_surface_enthalpy(oracle_cls):
+    Ts = 253.15
+    c = Column(oracle_cls, H0=0.5, Ts=Ts)
+    c.set_temperature(np.full(10, 240.0))
+    c.step(1e9)
+    assert np.allclose(c.column("T"), Ts, rtol=1.4901161193847656e-08, atol=0)
+    assert c.value("Hw") == 0.0
