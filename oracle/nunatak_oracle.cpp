@@ -828,7 +828,7 @@ struct Problem {
     SigmaField E, omega;          // enthalpy and water fraction (nko_compute_thermal_diagnostics)
     // energy step (nko_step_enthalpy): basal water Hw, grounded melt mᵍ (gmelt), geothermal flux G, surface and ocean
     // temperatures, basal melt rate m, thickness of the previous energy step Hⁿ, strain heating Φ
-    Field Hw, gmelt, G, Ts, To, melt, Hn;
+    Field Hw, gmelt, G, Ts, To, melt, Hn, sb;   // sb: the temperate fraction sᵇ of the basal layer (output)
     SigmaField Phi;
 
     // CG workspace (VelocityConjugateGradientSolver, conjugate_gradient.jl:52-102) and Picard x⁻
@@ -1627,6 +1627,7 @@ static void step_enthalpy(Problem& P, const EnergyParams& q, double dt) {
         Db[col(i, j)] = D;
         rb[col(i, j)] = r;
         sb[col(i, j)] = unit_ramp(P.E.k[0](i, j) - E1pm + q.blend, q.blend);
+        P.sb(i, j) = sb[col(i, j)];
         qg[col(i, j)] = grounded_part(i, j) * P.G(i, j) + F;
     });
 
@@ -1832,7 +1833,7 @@ nk_status nko_problem_create(const nk_grid_desc* gd, const nk_physics_desc* pd, 
     P->etaHff.init(g, FACE, FACE);
     P->A3.init(g, CENTER, CENTER, gd->Nsigma); P->eta_s.init(g, CENTER, CENTER, gd->Nsigma); P->T.init(g, CENTER, CENTER, gd->Nsigma);
     P->E.init(g, CENTER, CENTER, gd->Nsigma); P->omega.init(g, CENTER, CENTER, gd->Nsigma);
-    for (Field* f : {&P->Hw, &P->gmelt, &P->G, &P->Ts, &P->To, &P->melt, &P->Hn}) f->init(g, CENTER, CENTER);
+    for (Field* f : {&P->Hw, &P->gmelt, &P->G, &P->Ts, &P->To, &P->melt, &P->Hn, &P->sb}) f->init(g, CENTER, CENTER);
     P->Phi.init(g, CENTER, CENTER, gd->Nsigma);
     P->us.init(g, FACE, CENTER, gd->Nsigma); P->vs.init(g, CENTER, FACE, gd->Nsigma);
     P->r.init(g); P->z.init(g); P->p.init(g); P->q.init(g); P->w.init(g); P->xprev.init(g);
@@ -1941,13 +1942,13 @@ nk_status nko_compute_thermal_diagnostics(nko_problem* h, const nk_thermal_param
 }
 
 // The energy step's own fields (no library counterpart yet): which = 0 Hw, 1 mᵍ, 2 G, 3 Tₛ, 4 Tₒ, 5 basal melt rate,
-// 6 Hⁿ (2-D), 7 Φ (σ grid); set = 1 copies data in, 0 out.
+// 6 Hⁿ (2-D), 7 Φ (σ grid), 8 sᵇ (2-D); set = 1 copies data in, 0 out.
 nk_status nko_energy_field(nko_problem* h, int32_t which, double* data, int64_t count, int32_t set) {
     if (!h || !data) return NK_BAD_ARGUMENT;
     Problem& P = *reinterpret_cast<Problem*>(h);
     Field* two[] = {&P.Hw, &P.gmelt, &P.G, &P.Ts, &P.To, &P.melt, &P.Hn};
-    if (which >= 0 && which < 7) {
-        Field& f = *two[which];
+    if ((which >= 0 && which < 7) || which == 8) {
+        Field& f = which == 8 ? P.sb : *two[which];
         if (count != (int64_t)f.nx() * f.ny()) return NK_BAD_ARGUMENT;
         if (set) copy_in(f, data); else copy_out(f, data);
         return NK_OK;

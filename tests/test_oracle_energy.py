@@ -11,7 +11,9 @@ no thickness change, so each time step is one energy step of the same length:
 - a warm base melts at the analytic rate (G - k (T_pm - Tₛ) / H) / (ρᵢ L) within 1e-3, and once the geothermal
   flux stops, refreezes its stored water while the total energy stays balanced within 1e-10 (:175-208);
 - a floating base sits at the ocean temperature, T linear from Tₒ to Tₛ, with no grounded melt (:210-222);
-- an ice-free column holds the surface enthalpy (:224-231)."""
+- an ice-free column holds the surface enthalpy (:224-231);
+- a temperate layer over a wet base insulates it, so all basal heat melts (:400-412);
+- temperate layers drain at the maximum rate and then down to the drainage water fraction (:414-434)."""
 import math
 
 import numpy as np
@@ -170,3 +172,33 @@ def test_ice_free_columns_hold_the_surface_enthalpy(oracle_cls):
     c.step(1e9)
     assert np.allclose(c.column("T"), Ts, rtol=1.4901161193847656e-08, atol=0)
     assert c.value("Hw") == 0.0
+
+
+def test_temperate_layer_above_the_base_insulates_it(oracle_cls):
+    """test/test_thermodynamics.jl:400-412: a temperate layer (ζ < 0.2, ω = 1/50) over a wet base insulates it, so
+    the basal layer is fully temperate and all the geothermal heat melts: mᵍ = G / (ρᵢ L) within 1e-12."""
+    H0, G = 1000.0, 0.08
+    c = Column(oracle_cls, H0=H0, G=G, Ts=263.15, Nsigma=20)
+    c.P.energy_set("Hw", 1.0)
+    c.set_enthalpy(np.where(c.zeta < 0.2, CI * (T0 - TR) + LATENT / 50, CI * (260 - TR)))
+    c.P.compute_thermal_diagnostics(clausius_clapeyron=BETA)
+    assert c.column("omega")[0] > 0
+    c.P.step_enthalpy(1e8, grounded_melt_coupling=False, maximum_drainage_rate=0.0)
+    assert c.value("basal_temperate_fraction") == 1.0
+    assert abs(c.value("grounded_melt") - G / (RHO * LATENT)) <= 1e-12 * G / (RHO * LATENT)
+
+
+def test_temperate_layers_drain_into_the_basal_water(oracle_cls):
+    """test/test_thermodynamics.jl:414-434: with ω above 3 ω_d everywhere the first 1 s step drains at the maximum
+    rate, Hw = H R_max Δt (1e-8); a hundred 1e9 s steps bring every layer down to ω_d and leave the water below."""
+    H0, wd, Rmax = 1000.0, 0.01, 1.58443823077064e-9
+    c = Column(oracle_cls, H0=H0, G=0.0, Ts=263.15, Nsigma=10)
+    c.set_enthalpy(np.full(10, CI * (T0 - TR) + 5 * wd * LATENT))
+    c.P.compute_thermal_diagnostics(clausius_clapeyron=BETA)
+    assert np.min(c.column("omega")) > 3 * wd
+    c.step(1.0)
+    assert abs(c.value("Hw") - H0 * Rmax) <= 1e-8 * H0 * Rmax
+    for _ in range(100):
+        c.step(1e9)
+    assert np.max(c.column("omega")) <= wd + 1e-12
+    assert c.value("Hw") > 0.1 * H0 * wd
