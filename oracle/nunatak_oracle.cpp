@@ -829,6 +829,7 @@ struct Problem {
     // energy step (nko_step_enthalpy): basal water Hw, grounded melt mᵍ (gmelt), geothermal flux G, surface and ocean
     // temperatures, basal melt rate m, thickness of the previous energy step Hⁿ, strain heating Φ
     Field Hw, gmelt, G, Ts, To, melt, Hn, sb;   // sb: the temperate fraction sᵇ of the basal layer (output)
+    Field smb, clipped;           // thickness step (nko_step_thickness): surface mass balance, clipped thickness
     SigmaField Phi;
 
     // CG workspace (VelocityConjugateGradientSolver, conjugate_gradient.jl:52-102) and Picard x⁻
@@ -1724,6 +1725,53 @@ static void step_enthalpy(Problem& P, const EnergyParams& q, double dt) {
     for (Field* f : {&P.Hw, &P.gmelt, &P.Hn}) fill_halo(*f);
 }
 
+// ------------------------------------------------------------------------------------------------
+// One ice time step of the thickness (TEST INFRASTRUCTURE: no library counterpart yet), time_stepping.jl:15-72:
+// three split Runge-Kutta stages H = max(0, H⁻ + Δτ G(H)) from the thickness H⁻ at the start of the step, with
+// Δτ = Δt/3, Δt/2, Δt (Oceananigans 0.117's SplitRungeKutta3, the Wicker-Skamarock scheme), the thickness added by
+// the clip in the last stage accumulated in `clipped`, and the geometry updated after every stage (update_state!).
+// G = a - (1 - φ) m - mᵍ - ∇⋅(ū H) with the first-order upwind flux (UpwindBiased(order = 1)): through a face,
+// Δ u H of the upwind cell; Bounded walls pass nothing.  The velocities are held (no velocity solve).
+// ------------------------------------------------------------------------------------------------
+static void compute_geometry(Problem& P);
+
+static void step_thickness(Problem& P, double dt, bool coupled) {
+    const Grid& g = P.grid;
+    const int Nx = g.Nx(), Ny = g.Ny();
+    fill_halo(P.x);
+    for (Field* f : {&P.smb, &P.melt, &P.gmelt, &P.clipped}) fill_halo(*f);
+    Field H0 = P.H, Gt(&g, CENTER, CENTER);
+    const double stages[3] = {1.0 / 3, 1.0 / 2, 1.0};
+    for (int st = 0; st < 3; ++st) {
+        fill_halo(P.H);
+        auto xflux = [&](int i, int j) {
+            if (g.peripheral_fc(i, j)) return 0.0;
+            double u = P.x.u(i, j);
+            return g.dy_c(j) * u * (u > 0 ? P.H(i - 1, j) : P.H(i, j));
+        };
+        auto yflux = [&](int i, int j) {
+            if (g.peripheral_cf(i, j)) return 0.0;
+            double v = P.x.v(i, j);
+            return g.dx_c(i) * v * (v > 0 ? P.H(i, j - 1) : P.H(i, j));
+        };
+        for_xy(Nx, Ny, [&](int i, int j) {   // _compute_thickness_tendency!, :59-63
+            double m = P.grounding ? (1 - P.phi(i, j)) * P.melt(i, j) : P.melt(i, j);
+            double S = P.smb(i, j) - m - (coupled ? P.gmelt(i, j) : 0.0);
+            double div = (xflux(i + 1, j) - xflux(i, j) + yflux(i, j + 1) - yflux(i, j)) / g.Az_ccc(i, j);
+            Gt(i, j) = S - div;
+        });
+        double dtau = stages[st] * dt;
+        bool final_stage = st == 2;
+        for_xy(Nx, Ny, [&](int i, int j) {   // _thickness_substep!, :65-72
+            double Hs = H0(i, j) + dtau * Gt(i, j);
+            P.H(i, j) = std::max(0.0, Hs);
+            if (final_stage) P.clipped(i, j) += std::max(0.0, -Hs);
+        });
+        fill_halo(P.H);
+        compute_geometry(P);
+    }
+}
+
 // ---- field access in interior layout -------------------------------------------------------------
 struct FieldRef { Field* f = nullptr; SigmaField* s = nullptr; };
 
@@ -1833,7 +1881,7 @@ nk_status nko_problem_create(const nk_grid_desc* gd, const nk_physics_desc* pd, 
     P->etaHff.init(g, FACE, FACE);
     P->A3.init(g, CENTER, CENTER, gd->Nsigma); P->eta_s.init(g, CENTER, CENTER, gd->Nsigma); P->T.init(g, CENTER, CENTER, gd->Nsigma);
     P->E.init(g, CENTER, CENTER, gd->Nsigma); P->omega.init(g, CENTER, CENTER, gd->Nsigma);
-    for (Field* f : {&P->Hw, &P->gmelt, &P->G, &P->Ts, &P->To, &P->melt, &P->Hn, &P->sb}) f->init(g, CENTER, CENTER);
+    for (Field* f : {&P->Hw, &P->gmelt, &P->G, &P->Ts, &P->To, &P->melt, &P->Hn, &P->sb, &P->smb, &P->clipped}) f->init(g, CENTER, CENTER);
     P->Phi.init(g, CENTER, CENTER, gd->Nsigma);
     P->us.init(g, FACE, CENTER, gd->Nsigma); P->vs.init(g, CENTER, FACE, gd->Nsigma);
     P->r.init(g); P->z.init(g); P->p.init(g); P->q.init(g); P->w.init(g); P->xprev.init(g);
@@ -1942,13 +1990,14 @@ nk_status nko_compute_thermal_diagnostics(nko_problem* h, const nk_thermal_param
 }
 
 // The energy step's own fields (no library counterpart yet): which = 0 Hw, 1 mᵍ, 2 G, 3 Tₛ, 4 Tₒ, 5 basal melt rate,
-// 6 Hⁿ (2-D), 7 Φ (σ grid), 8 sᵇ (2-D); set = 1 copies data in, 0 out.
+// 6 Hⁿ (2-D), 7 Φ (σ grid), 8 sᵇ, 9 surface mass balance, 10 clipped thickness (2-D); set = 1 copies data in,
+// 0 out.
 nk_status nko_energy_field(nko_problem* h, int32_t which, double* data, int64_t count, int32_t set) {
     if (!h || !data) return NK_BAD_ARGUMENT;
     Problem& P = *reinterpret_cast<Problem*>(h);
-    Field* two[] = {&P.Hw, &P.gmelt, &P.G, &P.Ts, &P.To, &P.melt, &P.Hn};
-    if ((which >= 0 && which < 7) || which == 8) {
-        Field& f = which == 8 ? P.sb : *two[which];
+    Field* two[] = {&P.Hw, &P.gmelt, &P.G, &P.Ts, &P.To, &P.melt, &P.Hn, nullptr, &P.sb, &P.smb, &P.clipped};
+    if (which >= 0 && which <= 10 && which != 7) {
+        Field& f = *two[which];
         if (count != (int64_t)f.nx() * f.ny()) return NK_BAD_ARGUMENT;
         if (set) copy_in(f, data); else copy_out(f, data);
         return NK_OK;
@@ -1969,6 +2018,14 @@ nk_status nko_energy_field(nko_problem* h, int32_t which, double* data, int64_t 
 // diffusivity ratio, enthalpy blend width, water layer blend thickness, minimum thickness, drainage water fraction,
 // maximum drainage rate, grounded melt coupling (0 / 1): EnthalpyThermodynamics' keywords
 // (src/Thermodynamics/enthalpy_thermodynamics.jl:92-110).
+// One ice time step of the thickness of length dt (time_step! with a held velocity); coupled: the grounded melt
+// mᵍ of the energy step thins the ice.
+nk_status nko_step_thickness(nko_problem* h, double dt, int32_t coupled) {
+    if (!h || !(dt > 0)) return NK_BAD_ARGUMENT;
+    step_thickness(*reinterpret_cast<Problem*>(h), dt, coupled != 0);
+    return NK_OK;
+}
+
 nk_status nko_step_enthalpy(nko_problem* h, const double* prm, double dt) {
     if (!h || !prm || !(dt > 0)) return NK_BAD_ARGUMENT;
     EnergyParams q{prm[0], prm[1], prm[2], prm[3], prm[4], prm[5], prm[6], prm[7], prm[8], prm[9], prm[10], prm[11], prm[12] != 0.0};

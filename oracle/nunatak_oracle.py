@@ -48,6 +48,7 @@ def load():
             "nko_compute_thermal_diagnostics": [vp, C.POINTER(abi.ThermalParams)],
             "nko_energy_field": [vp, C.c_int32, dp, i64, C.c_int32],
             "nko_step_enthalpy": [vp, dp, C.c_double],
+            "nko_step_thickness": [vp, C.c_double, C.c_int32],
             "nko_picard_adjoint": [vp, dp, dp, C.POINTER(abi.IterationControl), dp, dp, dp, dp, C.POINTER(abi.SolveStats)],
             "nko_multigrid_levels": [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), i32],
             "nko_multigrid_restrict": [vp, i32, dp, dp, dp, dp],
@@ -86,7 +87,7 @@ class OracleProblem(Problem):
     # ---- the energy step (test infrastructure for EnthalpyThermodynamics; no library counterpart yet) ----
     ENERGY_FIELDS = {"Hw": 0, "grounded_melt": 1, "geothermal_flux": 2, "surface_temperature": 3,
                      "ocean_temperature": 4, "basal_melt_rate": 5, "H_previous": 6, "strain_heating": 7,
-                     "basal_temperate_fraction": 8}
+                     "basal_temperate_fraction": 8, "surface_mass_balance": 9, "clipped_thickness": 10}
 
     def _energy_shape(self, name):
         return (self.Nsigma, self.grid.Ny, self.grid.Nx) if name == "strain_heating" else (self.grid.Ny, self.grid.Nx)
@@ -109,6 +110,10 @@ class OracleProblem(Problem):
                         reference_temperature, temperate_diffusivity_ratio, enthalpy_blend_width, water_layer_blend_thickness,
                         minimum_thickness, drainage_water_fraction, maximum_drainage_rate, float(grounded_melt_coupling)])
         _check(self._lib.nko_step_enthalpy(self._h, prm.ctypes.data_as(_dptr), float(dt)), "step_enthalpy")
+
+    def step_thickness(self, dt, grounded_melt_coupling=False):
+        """One ice time step of the thickness with the velocities held (time_step! without a velocity solve)."""
+        _check(self._lib.nko_step_thickness(self._h, float(dt), int(grounded_melt_coupling)), "step_thickness")
 
     def grid_metrics(self, which):
         n = (self.grid.Nx if which in (0,) else self.grid.Nx + 1 if which == 1 else self.grid.Ny if which == 2 else self.grid.Ny + 1)
