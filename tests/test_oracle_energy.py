@@ -18,7 +18,9 @@ with the thickness step of the oracle as well:
 - a thickening or thinning column follows the heat equation in fixed height at second order (:293-320;
   measured 0.056 / 0.014 / 0.0036 K thickening and 0.31 / 0.086 / 0.023 K thinning at 10 / 20 / 40 layers);
 - a uniform enthalpy stays uniform to 1e-9 under variable thickness, shearing layer velocities, accumulation
-  and melt (:322-331)."""
+  and melt (:322-331);
+- strong accumulation over a sharp front creates no new extrema (:360-370);
+- upwind transport at unit Courant number shifts each moving layer by one cell and leaves the others (:372-390)."""
 import math
 
 import numpy as np
@@ -271,3 +273,47 @@ def test_uniform_enthalpy_stays_uniform(oracle_cls):
         P.step_enthalpy(1e9, grounded_melt_coupling=True)
     assert np.max(np.abs(P.get("H") - H)) > 10
     assert np.max(np.abs(P.get("E") - E0)) < 1e-9 * E0
+
+
+def test_strong_accumulation_over_a_sharp_front_creates_no_new_extrema(oracle_cls):
+    """test/test_thermodynamics.jl:360-370: 2e-7 m/s of accumulation over a 230 / 260 K step keeps every layer
+    within [230, 260] K for 20 steps of 1e8 s."""
+    c = Column(oracle_cls, H0=1000.0, Nsigma=10, G=0.0, Ts=250.0)
+    c.P.energy_set("surface_mass_balance", 2e-7)
+    c.set_temperature(np.where(c.zeta < 0.5, 230.0, 260.0))
+    for _ in range(20):
+        c.P.step_thickness(1e8)
+        c.step(1e8)
+        T = c.column("T")
+        assert np.min(T) >= 230 - 1e-8 and np.max(T) <= 260 + 1e-8
+
+
+@pytest.mark.parametrize("direction", ["x", "y"])
+def test_upwind_transport_at_unit_courant_number_shifts_each_layer(oracle_cls, direction):
+    """test/test_thermodynamics.jl:372-390: on an 8-cell periodic row (Nσ = 4, conduction switched off with
+    k = 1e-12), layer velocities of one cell per step above ζ = 0.5 and none below move the upper two layers'
+    enthalpy by exactly one cell and leave the lower two, to 1e-10, with no vertical flux."""
+    Nx, dx, dt = 8, 1e3, 1e9
+    size = (Nx, 1) if direction == "x" else (1, Nx)
+    g = M.RectilinearGrid(size=size, x=(0.0, size[0] * dx), y=(0.0, size[1] * dx), topology=("Periodic", "Periodic"), halo=(3, 3))
+    P = make(oracle_cls, g, Nsigma=4, bed_refinement=1.0, rheology=M.GlenFlowLaw(rate_factor="sigma"))
+    P.set("H", 500.0)
+    P.set("bed", 0.0)
+    P.compute_geometry()
+    zeta = (np.arange(4) + 0.5) / 4
+    name = "u_sigma" if direction == "x" else "v_sigma"
+    P.set(name, np.stack([np.full(P.shape(name)[1:], dx / dt if z > 0.5 else 0.0) for z in zeta]))
+    pos = g.centers(0) if direction == "x" else g.centers(1)
+    T = 250 + 10 * np.sin(2 * math.pi * pos / (Nx * dx))
+    T2 = T.reshape(1, -1) if direction == "x" else T.reshape(-1, 1)
+    P.set("E", np.stack([enthalpy(T2, 0.0, 918.0 * GRAV * 500.0 * (1 - z)) for z in zeta]))
+    for name_, value in (("geothermal_flux", 0.0), ("surface_temperature", 243.15), ("ocean_temperature", 271.15),
+                         ("basal_melt_rate", 0.0), ("H_previous", 500.0), ("Hw", 0.0), ("surface_mass_balance", 0.0)):
+        P.energy_set(name_, value)
+    E0 = P.get("E")
+    P.step_thickness(dt)
+    P.step_enthalpy(dt, thermal_conductivity=1e-12)
+    E = P.get("E")
+    np.testing.assert_allclose(E[:2], E0[:2], rtol=1e-10)
+    axis = 2 if direction == "x" else 1
+    np.testing.assert_allclose(E[2:], np.roll(E0[2:], 1, axis=axis), rtol=1e-10)
