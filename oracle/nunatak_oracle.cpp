@@ -830,6 +830,7 @@ struct Problem {
     // temperatures, basal melt rate m, thickness of the previous energy step Hⁿ, strain heating Φ
     Field Hw, gmelt, G, Ts, To, melt, Hn, sb;   // sb: the temperate fraction sᵇ of the basal layer (output)
     Field smb, clipped;           // thickness step (nko_step_thickness): surface mass balance, clipped thickness
+    Field qg;                     // basal heat flux qᵍ = φ G + τᵇ⋅uᵇ of the last energy step (output)
     SigmaField Phi;
 
     // CG workspace (VelocityConjugateGradientSolver, conjugate_gradient.jl:52-102) and Picard x⁻
@@ -1576,6 +1577,8 @@ static void step_enthalpy(Problem& P, const EnergyParams& q, double dt) {
     auto grounded_part = [&](int i, int j) { return P.grounding ? P.phi(i, j) : 1.0; };        // :118-119
     for (int k = 0; k < Ns; ++k) fill_halo(P.E.k[k]);
     for (Field* f : {&P.Hw, &P.gmelt, &P.G, &P.Ts, &P.To, &P.melt, &P.Hn}) fill_halo(*f);
+    // fill_halo_regions!((basal_drag(...)..., uᵇ, vᵇ)) and ((uσ, vσ)), column_energy_solve.jl:28-29
+    for (Field* f : {&P.ub, &P.vb, diva ? &P.bbu : &P.bu, diva ? &P.bbv : &P.bv}) fill_halo(*f);
 
     // strain heating Φ = 4 η ε̇ₑ² (membrane, without ε̇₀), plus τᵇ² w₂ₖ / Δζₖ / η for DIVA (strain_heating.jl:43-56)
     fill_halo(P.x);
@@ -1630,6 +1633,7 @@ static void step_enthalpy(Problem& P, const EnergyParams& q, double dt) {
         sb[col(i, j)] = unit_ramp(P.E.k[0](i, j) - E1pm + q.blend, q.blend);
         P.sb(i, j) = sb[col(i, j)];
         qg[col(i, j)] = grounded_part(i, j) * P.G(i, j) + F;
+        P.qg(i, j) = qg[col(i, j)];
     });
 
     // the column systems (from the old E), then the Thomas solve into E
@@ -1807,8 +1811,10 @@ static FieldRef field_ref(Problem& P, int id) {
         case NK_FIELD_TEMPERATURE: r.s = &P.T; break;
         case NK_FIELD_U_PRESCRIBED: r.f = &P.ud.u; break;
         case NK_FIELD_V_PRESCRIBED: r.f = &P.ud.v; break;
-        case NK_FIELD_ENTHALPY: if (P.rate_layout == NK_RATE_FACTOR_SIGMA) r.s = &P.E; break;
-        case NK_FIELD_WATER_FRACTION: if (P.rate_layout == NK_RATE_FACTOR_SIGMA) r.s = &P.omega; break;
+        // held for every rate-factor layout here (the energy step needs them with a constant A as well); the
+        // library holds them with the σ-grid rate factor only, the one its thermal diagnostics write
+        case NK_FIELD_ENTHALPY: r.s = &P.E; break;
+        case NK_FIELD_WATER_FRACTION: r.s = &P.omega; break;
         default: break;
     }
     return r;
@@ -1881,7 +1887,7 @@ nk_status nko_problem_create(const nk_grid_desc* gd, const nk_physics_desc* pd, 
     P->etaHff.init(g, FACE, FACE);
     P->A3.init(g, CENTER, CENTER, gd->Nsigma); P->eta_s.init(g, CENTER, CENTER, gd->Nsigma); P->T.init(g, CENTER, CENTER, gd->Nsigma);
     P->E.init(g, CENTER, CENTER, gd->Nsigma); P->omega.init(g, CENTER, CENTER, gd->Nsigma);
-    for (Field* f : {&P->Hw, &P->gmelt, &P->G, &P->Ts, &P->To, &P->melt, &P->Hn, &P->sb, &P->smb, &P->clipped}) f->init(g, CENTER, CENTER);
+    for (Field* f : {&P->Hw, &P->gmelt, &P->G, &P->Ts, &P->To, &P->melt, &P->Hn, &P->sb, &P->smb, &P->clipped, &P->qg}) f->init(g, CENTER, CENTER);
     P->Phi.init(g, CENTER, CENTER, gd->Nsigma);
     P->us.init(g, FACE, CENTER, gd->Nsigma); P->vs.init(g, CENTER, FACE, gd->Nsigma);
     P->r.init(g); P->z.init(g); P->p.init(g); P->q.init(g); P->w.init(g); P->xprev.init(g);
@@ -1990,13 +1996,13 @@ nk_status nko_compute_thermal_diagnostics(nko_problem* h, const nk_thermal_param
 }
 
 // The energy step's own fields (no library counterpart yet): which = 0 Hw, 1 mᵍ, 2 G, 3 Tₛ, 4 Tₒ, 5 basal melt rate,
-// 6 Hⁿ (2-D), 7 Φ (σ grid), 8 sᵇ, 9 surface mass balance, 10 clipped thickness (2-D); set = 1 copies data in,
-// 0 out.
+// 6 Hⁿ (2-D), 7 Φ (σ grid), 8 sᵇ, 9 surface mass balance, 10 clipped thickness, 11 basal heat flux qᵍ (2-D);
+// set = 1 copies data in, 0 out.
 nk_status nko_energy_field(nko_problem* h, int32_t which, double* data, int64_t count, int32_t set) {
     if (!h || !data) return NK_BAD_ARGUMENT;
     Problem& P = *reinterpret_cast<Problem*>(h);
-    Field* two[] = {&P.Hw, &P.gmelt, &P.G, &P.Ts, &P.To, &P.melt, &P.Hn, nullptr, &P.sb, &P.smb, &P.clipped};
-    if (which >= 0 && which <= 10 && which != 7) {
+    Field* two[] = {&P.Hw, &P.gmelt, &P.G, &P.Ts, &P.To, &P.melt, &P.Hn, nullptr, &P.sb, &P.smb, &P.clipped, &P.qg};
+    if (which >= 0 && which <= 11 && which != 7) {
         Field& f = *two[which];
         if (count != (int64_t)f.nx() * f.ny()) return NK_BAD_ARGUMENT;
         if (set) copy_in(f, data); else copy_out(f, data);

@@ -87,7 +87,8 @@ class OracleProblem(Problem):
     # ---- the energy step (test infrastructure for EnthalpyThermodynamics; no library counterpart yet) ----
     ENERGY_FIELDS = {"Hw": 0, "grounded_melt": 1, "geothermal_flux": 2, "surface_temperature": 3,
                      "ocean_temperature": 4, "basal_melt_rate": 5, "H_previous": 6, "strain_heating": 7,
-                     "basal_temperate_fraction": 8, "surface_mass_balance": 9, "clipped_thickness": 10}
+                     "basal_temperate_fraction": 8, "surface_mass_balance": 9, "clipped_thickness": 10,
+                     "basal_heat_flux": 11}
 
     def _energy_shape(self, name):
         return (self.Nsigma, self.grid.Ny, self.grid.Nx) if name == "strain_heating" else (self.grid.Ny, self.grid.Nx)

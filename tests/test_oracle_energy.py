@@ -20,7 +20,9 @@ with the thickness step of the oracle as well:
 - a uniform enthalpy stays uniform to 1e-9 under variable thickness, shearing layer velocities, accumulation
   and melt (:322-331);
 - strong accumulation over a sharp front creates no new extrema (:360-370);
-- upwind transport at unit Courant number shifts each moving layer by one cell and leaves the others (:372-390)."""
+- upwind transport at unit Courant number shifts each moving layer by one cell and leaves the others (:372-390);
+with the velocity solve as well:
+- the basal plus strain heat equals the power of the driving stress to 1e-8, SSA and DIVA (:392-398)."""
 import math
 
 import numpy as np
@@ -317,3 +319,44 @@ def test_upwind_transport_at_unit_courant_number_shifts_each_layer(oracle_cls, d
     np.testing.assert_allclose(E[:2], E0[:2], rtol=1e-10)
     axis = 2 if direction == "x" else 1
     np.testing.assert_allclose(E[2:], np.roll(E0[2:], 1, axis=axis), rtol=1e-10)
+
+
+@pytest.mark.parametrize("shear", [None, M.DIVAShear()], ids=["SSA", "DIVA"])
+def test_friction_and_strain_heat_account_for_the_driving_work(oracle_cls, shear):
+    """test/test_thermodynamics.jl:392-398 with dissipation_mismatch (:65-95): on a 16 x 16 periodic sheet (Weertman
+    m = 1, A = 1e-24) after one time step of 1e6 s with converged velocities, the basal heat qᵍ plus the strain
+    heat H Σ Δζ Φ of the energy step equals the power Σ τ⋅u of the driving stress to 1e-8.  For the SSA the
+    membrane heat 4 η ε̇ₑ² balances the viscous work exactly (the corner viscosity is the mean of the four
+    centres); for the DIVA the shear heat τᵇ² F₂ adds the work of the vertical shear."""
+    Nx, L = 16, 3.2e5
+    g = M.RectilinearGrid(size=(Nx, Nx), x=(0.0, L), y=(0.0, L), topology=("Periodic", "Periodic"), halo=(4, 4))
+    solver = M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-12, maxiter=10_000),
+                                   picard_iteration_control=M.Convergence(reltol=1e-11, maxiter=500))
+    P = make(oracle_cls, g, Nsigma=10, rheology=M.GlenFlowLaw(rate_factor=1e-24, strain_rate_regularization=1e-16),
+             friction=M.WeertmanFriction(coefficient=1e10, exponent=1.0), velocity_solver=solver,
+             stress_balance=M.DepthIntegrated(shear=shear), constants=M.IceSheetConstants(ice_density=RHO))
+    P.set("H", evaluate(g, "H", lambda x, y: 1000 + 100 * math.sin(2 * math.pi * x / L) * math.cos(2 * math.pi * y / L)))
+    P.set("bed", 0.0)
+    P.set("A", 1e-24)
+    P.set("C", 1e10)
+    P.compute_geometry()
+    assert P.picard_solve().status == 0                 # set!(model; H): the velocity solve of update_state!
+    P.velocity_profile()
+    for name, value in (("geothermal_flux", 0.0), ("surface_temperature", 243.15), ("ocean_temperature", 271.15),
+                        ("basal_melt_rate", 0.0), ("H_previous", P.get("H")), ("Hw", 0.0), ("surface_mass_balance", 0.0)):
+        P.energy_set(name, value)
+    P.set("E", enthalpy(243.15, 0.0, 0.0))
+    dt = 1e6
+    P.step_thickness(dt)
+    assert P.picard_solve().status == 0                 # the final stage's velocity update
+    P.velocity_profile()
+    P.step_enthalpy(dt)
+    faces = np.array(M.sigma_faces(10))
+    dz = np.diff(faces)[:, None, None]
+    H = P.get("H")
+    strain = np.sum(dz * P.energy_get("strain_heating"), axis=0)
+    area = (L / Nx) ** 2
+    heat = area * float(np.sum(P.energy_get("basal_heat_flux") + H * strain))
+    power = float(np.sum(P.get("tau_u") * P.get("u")) + np.sum(P.get("tau_v") * P.get("v")))
+    assert power > 0
+    assert abs(heat - power) / power < 1e-8, (heat, power)
