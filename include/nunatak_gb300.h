@@ -191,7 +191,15 @@ typedef struct nk_solver_desc {
 #define NK_FIELD_V_PRESCRIBED  28   /* v_D                                  Center-Face */
 #define NK_FIELD_ENTHALPY      29   /* enthalpy E on the sigma grid (input of nk_compute_thermal_diagnostics) */
 #define NK_FIELD_WATER_FRACTION 30  /* water fraction omega on the sigma grid (written by nk_compute_thermal_diagnostics) */
-#define NK_FIELD_COUNT         31
+/* The thickness step's sources and its clip (nk_step_thickness), Center-Center, zero at first (allocated on first
+ * use): IceSheetModel.surface_mass_balance a and basal_melt_rate m (src/Models/ice_sheet_model.jl:39-41), the
+ * thermodynamics' grounded melt m^g (thermodynamics.state, read when grounded_melt_coupling is set) and
+ * geometry.clipped_thickness (src/Models/time_stepping.jl:60-72), all in m s^-1 except the clip in m. */
+#define NK_FIELD_SURFACE_MASS_BALANCE 31
+#define NK_FIELD_BASAL_MELT_RATE      32
+#define NK_FIELD_GROUNDED_MELT_RATE   33
+#define NK_FIELD_CLIPPED_THICKNESS    34
+#define NK_FIELD_COUNT         35
 
 typedef struct nk_solve_stats {
     int32_t status;                   /* nk_status of the solve */
@@ -284,6 +292,16 @@ typedef struct nk_thermal_params {
  * Reads NK_FIELD_ENTHALPY and H; writes NK_FIELD_TEMPERATURE, NK_FIELD_WATER_FRACTION and the rate factor, which
  * must have the sigma layout.  Until an enthalpy is set the enthalpy field holds zeros. */
 nk_status nk_compute_thermal_diagnostics(nk_problem* problem, const nk_thermal_params* params);
+
+/* One ice time step of the thickness with the velocities held (replaces the three rk_substep! calls of
+ * time_step!, src/Models/time_stepping.jl:15-72, with UpwindBiased(order = 1) advection and no PartialCellFront):
+ * Delta tau = dt/3, dt/2, dt; each stage sets H = max(0, H_start + Delta tau G(H)) with
+ * G = a - (1 - phi) m - m^g - div(u H) (phi only with a grounding-line treatment, m^g only when
+ * grounded_melt_coupling is non-zero), the upwind flux through each face and none through a Bounded wall; the
+ * last stage adds its clip max(0, -H*) to NK_FIELD_CLIPPED_THICKNESS; nk_compute_geometry runs after every
+ * stage (update_state! without the velocity solve), so the surface, masks, grounded fractions, effective
+ * pressure and driving stress follow the new thickness.  NK_BAD_ARGUMENT when dt is not finite and positive. */
+nk_status nk_step_thickness(nk_problem* problem, double dt, int32_t grounded_melt_coupling);
 
 /* update_stress_balance_coefficients!(x, ...) (SSA) or update_diva_coefficients!(x, ...) (DIVA) at the
  * current velocity fields U, V: eta_sigma, eta_H, F2, eta_H_ff, beta (and beta_b, u_b, v_b for DIVA). */

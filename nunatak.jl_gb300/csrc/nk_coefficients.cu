@@ -445,6 +445,41 @@ void launch_thermal_diagnostics(const DevGrid<double>& g, const SigmaTable& sig,
     k_thermal_diagnostics<<<d.grid, d.block, 0, s>>>(g, sig, plane, H, E, T, omega, A, rho_i, gacc, params); count_launch();
 }
 
+// ---- thickness transport -----------------------------------------------------------------------------------
+// One split Runge-Kutta stage of the mass balance, the tendency and the substep fused (_compute_thickness_tendency!
+// and _thickness_substep!, src/Models/time_stepping.jl:59-72): G = a - (1 - φ) m - mᵍ - ∇⋅(ū H) at cell (i, j) from
+// the stage-start thickness Hs, with the first-order upwind flux through each face (the face's normal velocity times
+// the upwind cell's thickness times the face length, UpwindBiased(order = 1); nothing through a Bounded wall), then
+// H = max(0, H⁻ + Δτ G) from the step-start thickness H⁻, and in the last stage the clip max(0, -H★) added to Hc.
+// Hs and H are distinct arrays: every cell reads its four neighbours' stage-start thickness.
+__global__ void k_thickness_stage(ThicknessView v, double dtau, int final_stage) {
+    const DevGrid<double>& g = v.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    const double* __restrict__ Hs = v.Hs;
+    auto xflux = [&](int f) {
+        if (g.peripheral_fc(f, j)) return 0.0;
+        double u = v.x[g.u_idx(f, j)].x;
+        return g.dyc[j] * u * (u > 0 ? Hs[g.c_idx(f - 1, j)] : Hs[g.c_idx(f, j)]);
+    };
+    auto yflux = [&](int f) {
+        if (g.peripheral_cf(i, f)) return 0.0;
+        double w = v.x[g.v_idx(i, f)].y;
+        return g.dxc[i] * w * (w > 0 ? Hs[g.c_idx(i, f - 1)] : Hs[g.c_idx(i, f)]);
+    };
+    int c = g.idx(i, j);
+    double m = v.grounding ? (1 - v.phi[c]) * v.melt[c] : v.melt[c];
+    double S = v.smb[c] - m - (v.coupled ? v.gmelt[c] : 0.0);
+    double div = (xflux(i + 1) - xflux(i) + yflux(j + 1) - yflux(j)) / g.Az_cc(i, j);
+    double Hstar = v.H0[c] + dtau * (S - div);
+    v.H[c] = 0.0 < Hstar ? Hstar : 0.0;
+    if (final_stage) v.clipped[c] += 0.0 < -Hstar ? -Hstar : 0.0;
+}
+void launch_thickness_stage(const ThicknessView& v, double dtau, int final_stage, cudaStream_t s) {
+    LaunchDims d = dims2d(v.g.Nx, v.g.Ny);
+    k_thickness_stage<<<d.grid, d.block, 0, s>>>(v, dtau, final_stage); count_launch();
+}
+
 // ---- fixed-point adjoint of the SSA Picard step -------------------------------------------------------------
 // The reverse of picard_coefficient_step! (ext/NunatakEnzymeExt.jl:142-157): with q = A(c(x)) x*, the seed
 // q̄ = -λ, and x* the converged velocity, it returns ȳ = -(∂q/∂x)ᵀ λ.  Only active operator rows depend on

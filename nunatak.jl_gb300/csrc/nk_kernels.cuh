@@ -175,6 +175,18 @@ void launch_rate_factor(const DevGrid<double>& g, const SigmaTable& sig, int pla
 void launch_thermal_diagnostics(const DevGrid<double>& g, const SigmaTable& sig, int plane, const double* H, const double* E, double* T,
                                 double* omega, double* A, double rho_i, double gacc, const double* params, cudaStream_t s);
 
+// ---- thickness transport --------------------------------------------------------------------------------
+struct ThicknessView {
+    DevGrid<double> g;
+    const double2* x;                 // depth-averaged (u, v) per face, held through the step
+    const double* Hs;                 // thickness at the start of the stage (read with its neighbours)
+    const double* H0;                 // thickness at the start of the step (H⁻)
+    const double* smb; const double* melt; const double* gmelt; const double* phi;
+    double* H; double* clipped;
+    int grounding, coupled;
+};
+void launch_thickness_stage(const ThicknessView& v, double dtau, int final_stage, cudaStream_t s);
+
 // ---- multigrid ------------------------------------------------------------------------------------------
 template <typename T>
 struct LevelView {

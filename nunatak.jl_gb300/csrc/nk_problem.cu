@@ -200,6 +200,7 @@ struct nk_problem {
     double* sig_tables = nullptr;              // dz, w2, zc (Ns each) + w1 (Ns * Ns)
     double* rate_params = nullptr;             // 9 (nk_compute_rate_factor) or 14 (nk_thermal_params)
     double* thermal = nullptr;                 // enthalpy then water fraction (Ns planes each), allocated on first use
+    double* transport = nullptr;               // a, m, mᵍ, clipped thickness, then H at the step's and the stage's start
     std::vector<double> sig_dz, sig_w2, sig_zc, sig_w1;
 
     // coarse levels
@@ -1025,6 +1026,7 @@ struct FieldLoc {
     bool coef = false;        // a coefficient: the operator mask and diagonal follow it
     bool prescribed = false;  // a prescribed velocity (allocated on first use)
     bool thermal = false;     // the enthalpy or the water fraction (allocated on first use, sigma layout only)
+    bool transport = false;   // a source or the clip of the thickness step (allocated on first use)
 };
 
 static FieldLoc field_loc(nk_problem* P, int id) {
@@ -1073,6 +1075,13 @@ static FieldLoc field_loc(nk_problem* P, int id) {
                 f.thermal = true;
             }
             break;
+        case NK_FIELD_SURFACE_MASS_BALANCE:
+        case NK_FIELD_BASAL_MELT_RATE:
+        case NK_FIELD_GROUNDED_MELT_RATE:
+        case NK_FIELD_CLIPPED_THICKNESS:
+            cc(P->transport ? P->transport + (size_t)(id - NK_FIELD_SURFACE_MASS_BALANCE) * P->plane : nullptr);
+            f.transport = true;
+            break;
         default: break;
     }
     return f;
@@ -1085,6 +1094,17 @@ static void ensure_thermal(nk_problem* P) {
     size_t bytes = 2 * (size_t)P->Ns * P->plane * sizeof(double);
     NK_CUDA(cudaMalloc((void**)&P->thermal, bytes));
     NK_CUDA(cudaMemsetAsync(P->thermal, 0, bytes, P->stream));
+}
+
+// The thickness step's planes (zero at first): the four fields of NK_FIELD_SURFACE_MASS_BALANCE ..
+// NK_FIELD_CLIPPED_THICKNESS, then the thickness at the start of the step and of the stage.  No graph reads them.
+static const int TRANSPORT_PLANES = 6;
+static void ensure_transport(nk_problem* P) {
+    if (P->transport) return;
+    if (P->async_pending) bad("an asynchronous solve is pending (nk_problem_wait first)");
+    size_t bytes = TRANSPORT_PLANES * P->plane * sizeof(double);
+    NK_CUDA(cudaMalloc((void**)&P->transport, bytes));
+    NK_CUDA(cudaMemsetAsync(P->transport, 0, bytes, P->stream));
 }
 
 // The prescribed-velocity pairs, all NaN (free) at first.  Graphs captured before hold no pointer to them and
@@ -1295,6 +1315,7 @@ nk_status nk_problem_destroy(nk_problem* P) {
     if (P->adj_diva) cudaFree(P->adj_diva);
     if (P->ud) cudaFree(P->ud);
     if (P->thermal) cudaFree(P->thermal);
+    if (P->transport) cudaFree(P->transport);
     if (P->stream) cudaStreamDestroy(P->stream);
     delete P;
     return NK_OK;
@@ -1303,7 +1324,7 @@ nk_status nk_problem_destroy(nk_problem* P) {
 int64_t nk_problem_field_size(const nk_problem* P, int32_t id) {
     if (!P) return 0;
     FieldLoc f = field_loc(const_cast<nk_problem*>(P), id);
-    return (f.base || f.prescribed || f.thermal) ? (int64_t)f.nx * f.ny * f.planes : 0;
+    return (f.base || f.prescribed || f.thermal || f.transport) ? (int64_t)f.nx * f.ny * f.planes : 0;
 }
 
 nk_status nk_problem_set_field(nk_problem* P, int32_t id, const double* host, int64_t count) {
@@ -1317,6 +1338,10 @@ nk_status nk_problem_set_field(nk_problem* P, int32_t id, const double* host, in
         }
         if (f.thermal) {
             ensure_thermal(P);
+            f = field_loc(P, id);
+        }
+        if (f.transport) {
+            ensure_transport(P);
             f = field_loc(P, id);
         }
         if (!f.base) bad("unknown field id or field not held by this problem");
@@ -1345,6 +1370,10 @@ nk_status nk_problem_get_field(const nk_problem* Pc, int32_t id, double* host, i
             ensure_thermal(P);
             f = field_loc(P, id);
         }
+        if (f.transport) {
+            ensure_transport(P);
+            f = field_loc(P, id);
+        }
         if (!f.base) bad("unknown field id or field not held by this problem");
         if (count != (int64_t)f.nx * f.ny * f.planes) bad("field size mismatch");
         copy_out(P, f, host);
@@ -1365,6 +1394,10 @@ nk_status nk_problem_set_field_parent(nk_problem* P, int32_t id, const double* p
         }
         if (f.thermal) {
             ensure_thermal(P);
+            f = field_loc(P, id);
+        }
+        if (f.transport) {
+            ensure_transport(P);
             f = field_loc(P, id);
         }
         if (!f.base) bad("unknown field id or field not held by this problem");
@@ -1393,23 +1426,59 @@ nk_status nk_problem_get_field_parent(const nk_problem* Pc, int32_t id, double* 
             ensure_thermal(P);
             f = field_loc(P, id);
         }
+        if (f.transport) {
+            ensure_transport(P);
+            f = field_loc(P, id);
+        }
         if (!f.base) bad("unknown field id or field not held by this problem");
         copy_out_parent(P, f, parent, parent_layout(f, hx, hy, hz, count));
     });
 }
 
+// The geometry and the driving stress from H and the bed (update_state! without the velocity solve), on the
+// problem's stream.
+static void launch_problem_geometry(nk_problem* P) {
+    GeometryView v;
+    v.g = P->fine.g;
+    v.H = P->H; v.bed = P->bed; v.s = P->s; v.N = P->N; v.mu = P->mu; v.phi = P->phi; v.phi_uv = P->phi_uv; v.tau = P->tau;
+    v.rho_i = P->pd.ice_density; v.rho_w = P->pd.ocean_density; v.gacc = P->pd.gravitational_acceleration;
+    v.grounding = P->pd.grounding; v.gl_stress = P->pd.grounding_line_driving_stress; v.use_mask = P->pd.use_ice_mask;
+    v.mask_min = P->pd.mask_minimum_thickness; v.mask_trans = P->pd.mask_transition_thickness;
+    v.ud = P->ud;
+    launch_geometry(v, P->stream);
+}
+
 nk_status nk_compute_geometry(nk_problem* P) {
     if (!P) return NK_BAD_ARGUMENT;
     return guarded(P->ctx, [&] {
-        GeometryView v;
-        v.g = P->fine.g;
-        v.H = P->H; v.bed = P->bed; v.s = P->s; v.N = P->N; v.mu = P->mu; v.phi = P->phi; v.phi_uv = P->phi_uv; v.tau = P->tau;
-        v.rho_i = P->pd.ice_density; v.rho_w = P->pd.ocean_density; v.gacc = P->pd.gravitational_acceleration;
-        v.grounding = P->pd.grounding; v.gl_stress = P->pd.grounding_line_driving_stress; v.use_mask = P->pd.use_ice_mask;
-        v.mask_min = P->pd.mask_minimum_thickness; v.mask_trans = P->pd.mask_transition_thickness;
-        v.ud = P->ud;
-        launch_geometry(v, P->stream);
+        launch_problem_geometry(P);
         NK_CHECK_LAUNCH();
+        NK_CUDA(cudaStreamSynchronize(P->stream));
+    });
+}
+
+nk_status nk_step_thickness(nk_problem* P, double dt, int32_t grounded_melt_coupling) {
+    if (!P) return NK_BAD_ARGUMENT;
+    return guarded(P->ctx, [&] {
+        if (!(dt > 0) || !std::isfinite(dt)) bad("the time step must be finite and positive");
+        if (P->async_pending) bad("an asynchronous solve is pending (nk_problem_wait first)");
+        ensure_transport(P);
+        double* H0 = P->transport + 4 * P->plane;
+        double* Hs = P->transport + 5 * P->plane;
+        ThicknessView v;
+        v.g = P->fine.g;
+        v.x = P->x; v.Hs = Hs; v.H0 = H0;
+        v.smb = P->transport; v.melt = P->transport + P->plane; v.gmelt = P->transport + 2 * P->plane; v.phi = P->phi;
+        v.H = P->H; v.clipped = P->transport + 3 * P->plane;
+        v.grounding = P->pd.grounding != 0; v.coupled = grounded_melt_coupling != 0;
+        NK_CUDA(cudaMemcpyAsync(H0, P->H, P->plane * sizeof(double), cudaMemcpyDeviceToDevice, P->stream));
+        const double stages[3] = {1.0 / 3, 1.0 / 2, 1.0};     // SplitRungeKutta3 (Wicker-Skamarock) fractions
+        for (int st = 0; st < 3; ++st) {
+            NK_CUDA(cudaMemcpyAsync(Hs, P->H, P->plane * sizeof(double), cudaMemcpyDeviceToDevice, P->stream));
+            launch_thickness_stage(v, stages[st] * dt, st == 2, P->stream);
+            launch_problem_geometry(P);
+            NK_CHECK_LAUNCH();
+        }
         NK_CUDA(cudaStreamSynchronize(P->stream));
     });
 }

@@ -32,6 +32,7 @@ FIELD_IDS = {
     "beta_u": 16, "beta_v": 17, "eta_sigma": 18, "F2": 19, "beta_b_u": 20, "beta_b_v": 21,
     "u_b": 22, "v_b": 23, "u_sigma": 24, "v_sigma": 25, "T": 26,
     "u_prescribed": 27, "v_prescribed": 28, "E": 29, "omega": 30,
+    "surface_mass_balance": 31, "basal_melt_rate": 32, "grounded_melt": 33, "clipped_thickness": 34,
 }
 
 # (location x, location y, on the sigma grid) of each field: "c" Center, "f" Face.
@@ -47,6 +48,8 @@ FIELD_LOCATIONS = {
     "v_sigma": ("c", "f", True), "T": ("c", "c", True),
     "u_prescribed": ("f", "c", False), "v_prescribed": ("c", "f", False),
     "E": ("c", "c", True), "omega": ("c", "c", True),
+    "surface_mass_balance": ("c", "c", False), "basal_melt_rate": ("c", "c", False),
+    "grounded_melt": ("c", "c", False), "clipped_thickness": ("c", "c", False),
 }
 
 

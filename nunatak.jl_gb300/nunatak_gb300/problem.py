@@ -172,6 +172,24 @@ class Problem:
                                 melting_temperature, reference_temperature)
         _check(self._fn("compute_thermal_diagnostics")(self._h, C.byref(prm)), "compute_thermal_diagnostics", self._err())
 
+    # the thickness step's sources and clip, under the names of the energy-step fields
+    TRANSPORT_FIELDS = ("surface_mass_balance", "basal_melt_rate", "grounded_melt", "clipped_thickness")
+
+    def energy_set(self, name, value):
+        if name not in self.TRANSPORT_FIELDS:
+            raise KeyError(f"the library holds no energy-step field {name!r}")
+        self.set(name, value)
+
+    def energy_get(self, name):
+        if name not in self.TRANSPORT_FIELDS:
+            raise KeyError(f"the library holds no energy-step field {name!r}")
+        return self.get(name)
+
+    def step_thickness(self, dt, grounded_melt_coupling=False):
+        """One ice time step of the thickness with the velocities held (the three rk_substep! stages of time_step!,
+        src/Models/time_stepping.jl:15-72, first-order upwind, the geometry after every stage)."""
+        _check(self._fn("step_thickness")(self._h, float(dt), int(grounded_melt_coupling)), "step_thickness", self._err())
+
     def update_coefficients(self):
         _check(self._fn("update_coefficients")(self._h), "update_coefficients", self._err())
 

@@ -1815,6 +1815,10 @@ static FieldRef field_ref(Problem& P, int id) {
         // library holds them with the σ-grid rate factor only, the one its thermal diagnostics write
         case NK_FIELD_ENTHALPY: r.s = &P.E; break;
         case NK_FIELD_WATER_FRACTION: r.s = &P.omega; break;
+        case NK_FIELD_SURFACE_MASS_BALANCE: r.f = &P.smb; break;
+        case NK_FIELD_BASAL_MELT_RATE: r.f = &P.melt; break;
+        case NK_FIELD_GROUNDED_MELT_RATE: r.f = &P.gmelt; break;
+        case NK_FIELD_CLIPPED_THICKNESS: r.f = &P.clipped; break;
         default: break;
     }
     return r;

@@ -1,0 +1,175 @@
+"""The thickness step on both backends (the oracle's nko_step_thickness on the CPU, the library's nk_step_thickness
+marked gpu): three split Runge-Kutta stages of the mass balance, src/Models/time_stepping.jl:15-72, with
+first-order upwind fluxes, against the first-order testsets of test/test_thickness.jl, and the library against
+the oracle on the same seeded inputs.
+
+transport_model (test/test_thickness.jl:4-12): eastward flow u = U sin(πx/L) between walls on a 64 x 4 grid, a
+Gaussian bump on a background thickness, velocities held:
+- the volume is conserved to 1e-13 (:31-37, the upwind scheme);
+- sources change it by 16 Δt (a - m) A to 1e-13 (:39-47);
+- uniform flow moves the centre of mass by U t to 1e-12 (:49-58);
+- the clip closes the volume budget, V = V₀ - melted + clipped, to 1e-13 (:75-89);
+- basal melt acts on the floating part only, ΔH = -Δt m (1 - φ) (:91-102).
+The library against the oracle (gpu): a 48 x 40 ice shelf over a sloping bed, Bounded in x and Periodic in y,
+with velocities in both directions, the subgrid grounded fraction, sources, grounded melt and the clip, four
+steps: H, the clipped thickness and the geometry agree to 1e-12 relative (the grounded fractions feed the
+floating melt of the next stage, and the two backends may round them apart by an ulp); at 2048 x 2048 the
+library conserves the volume of a periodic sheet without sources to 1e-12."""
+import math
+
+import numpy as np
+import pytest
+
+from nunatak_gb300 import model as M
+from support import evaluate, make
+
+
+class Transport:
+    def __init__(self, cls, Nx=64, L=64e3, U=1e-6, width=None, velocity=None, background=0.0, smb=0.0, melt=0.0):
+        width = L / 16 if width is None else width
+        self.g = M.RectilinearGrid(size=(Nx, 4), x=(0.0, L), y=(0.0, 4 * L / Nx), topology=("Bounded", "Periodic"), halo=(4, 4))
+        self.P = make(cls, self.g, Nsigma=2, masking=M.SmoothIceMask())
+        self.L, self.dx = L, L / Nx
+        velocity = velocity or (lambda x, y: U * math.sin(math.pi * x / L))
+        self.P.set("H", evaluate(self.g, "H", lambda x, y: background + 100 * math.exp(-((x - L / 4) / width) ** 2)))
+        self.P.set("bed", 0.0)
+        self.P.compute_geometry()
+        self.P.set("u", evaluate(self.g, "u", velocity))
+        self.P.set("v", 0.0)
+        self.P.energy_set("surface_mass_balance", evaluate(self.g, "H", smb) if callable(smb) else smb)
+        self.P.energy_set("basal_melt_rate", evaluate(self.g, "H", melt) if callable(melt) else melt)
+        self.P.energy_set("clipped_thickness", 0.0)
+        self.umax = float(np.max(np.abs(self.P.get("u"))))
+
+    def volume(self):
+        return float(np.sum(self.P.get("H"))) * self.dx * self.g.y[1] / 4
+
+    def timescale(self):
+        """cell_advection_timescale: the shortest time to cross a cell."""
+        return self.dx / self.umax
+
+    def run(self, dt, n):
+        for _ in range(n):
+            self.P.step_thickness(dt)
+
+
+def test_upwind_conserves_volume(backend):
+    t = Transport(backend, background=100.0)
+    V0 = t.volume()
+    t.run(0.5 * t.timescale(), 32)
+    assert abs(t.volume() - V0) / V0 < 1e-13
+
+
+def test_sources_change_the_volume_by_the_integrated_balance(backend):
+    a, m = 3e-9, 1e-9
+    t = Transport(backend, background=100.0, smb=a, melt=lambda x, y: 2 * m * x / 64e3)
+    V0 = t.volume()
+    dt = 0.5 * t.timescale()
+    t.run(dt, 16)
+    expected = V0 + 16 * dt * (a - m) * 64e3 * 4e3
+    assert abs(t.volume() - expected) <= 1e-13 * expected
+
+
+def test_uniform_flow_moves_the_centre_of_mass(backend):
+    U, L = 1e-6, 128e3
+    t = Transport(backend, U=U, L=L, Nx=128, width=2e3, velocity=lambda x, y: U if 0 < x < L else 0.0)
+    x = t.g.centers(0)
+
+    def centre():
+        H = t.P.get("H")
+        return float(np.sum(H * x[None, :]) / np.sum(H))
+
+    X0 = centre()
+    dt = 0.5 * t.timescale()
+    assert abs(dt - 0.5 * 1e3 / U) <= 1e-12 * dt
+    t.run(dt, 16)
+    assert abs(centre() - (X0 + U * 16 * dt)) <= 1e-12 * (X0 + U * 16 * dt)
+
+
+def test_clipped_thickness_closes_the_volume_budget(backend):
+    m = 1e-7
+    t = Transport(backend, width=4e3, melt=lambda x, y: m if x > 24e3 else 0.0)
+    V0 = t.volume()
+    dt, Nt = 0.5 * t.timescale(), 32
+    t.run(dt, Nt)
+    Az = t.dx * t.g.y[1] / 4
+    melted = Nt * dt * float(np.sum(t.P.energy_get("basal_melt_rate"))) * Az
+    clipped = float(np.sum(t.P.energy_get("clipped_thickness"))) * Az
+    assert clipped > 0
+    assert np.min(t.P.get("H")) == 0.0
+    assert abs(t.volume() - (V0 - melted + clipped)) < 1e-13 * (V0 + melted)
+
+
+def test_basal_melt_acts_on_the_floating_part_only(backend):
+    Nx, L, H0, m, dt = 8, 8e3, 500.0, 1e-6, 1e3
+    g = M.RectilinearGrid(size=(Nx, 1), x=(0.0, L), y=(0.0, L / Nx), topology=("Bounded", "Periodic"), halo=(4, 4))
+    P = make(backend, g, Nsigma=2, grounding=M.SubgridGroundedFraction())
+    P.set("H", H0)
+    P.set("bed", evaluate(g, "H", lambda x, y: -100.0 if x < L / 2 else -2000.0))
+    P.compute_geometry()
+    P.energy_set("basal_melt_rate", m)
+    phi = P.get("phi")[0]
+    P.step_thickness(dt)
+    dH = P.get("H")[0] - H0
+    assert phi[0] == 1.0 and phi[-1] == 0.0 and 0 < phi[Nx // 2 - 1] < 1
+    np.testing.assert_allclose(dH, -dt * m * (1 - phi), rtol=1e-6)
+
+
+def seeded_shelf(cls, Nx=48, Ny=40, steps=4, dt=2e8):
+    """Four thickness steps of a seeded ice shelf over a sloping bed (grounded at x = 0, afloat downstream),
+    Bounded in x and Periodic in y, with random velocities in both directions, the subgrid grounded fraction,
+    sources, a coupled grounded melt and thin cells that the melt clips."""
+    rng = np.random.default_rng(20261203)
+    g = M.RectilinearGrid(size=(Nx, Ny), x=(0.0, Nx * 1e3), y=(0.0, Ny * 1e3), topology=("Bounded", "Periodic"), halo=(4, 4))
+    P = make(cls, g, Nsigma=2, grounding=M.SubgridGroundedFraction(), masking=M.SmoothIceMask())
+    x = g.centers(0)
+    H = 500 - 6 * x[None, :] / 1e3 + rng.uniform(0, 40, (Ny, Nx))
+    H[rng.uniform(size=(Ny, Nx)) < 0.08] = 1.0
+    P.set("H", H)
+    P.set("bed", np.broadcast_to(-300 - 10 * x[None, :] / 1e3, (Ny, Nx)) + rng.uniform(-5, 5, (Ny, Nx)))
+    P.compute_geometry()
+    P.set("u", rng.normal(5e-7, 5e-7, P.shape("u")))
+    P.set("v", rng.normal(0.0, 5e-7, P.shape("v")))
+    P.energy_set("surface_mass_balance", rng.uniform(-1e-9, 3e-9, (Ny, Nx)))
+    P.energy_set("basal_melt_rate", rng.uniform(0, 2e-8, (Ny, Nx)))
+    P.energy_set("grounded_melt", rng.uniform(0, 1e-9, (Ny, Nx)))
+    P.energy_set("clipped_thickness", 0.0)
+    for _ in range(steps):
+        P.step_thickness(dt, grounded_melt_coupling=True)
+    out = {k: P.get(k) for k in ("H", "s", "phi", "phi_u", "phi_v", "ice_mask", "N", "tau_u", "tau_v")}
+    out["clipped_thickness"] = P.energy_get("clipped_thickness")
+    P.close()
+    return out
+
+
+def test_seeded_shelf_clips_and_grounds(oracle_cls):
+    """The case the library is held to exercises the clip and both grounded and floating cells."""
+    out = seeded_shelf(oracle_cls)
+    assert np.max(out["clipped_thickness"]) > 0 and np.min(out["H"]) == 0.0
+    assert np.any(out["phi"] == 1.0) and np.any(out["phi"] == 0.0)
+
+
+@pytest.mark.gpu
+def test_gpu_matches_the_oracle(oracle_cls, gpu_cls):
+    want, got = seeded_shelf(oracle_cls), seeded_shelf(gpu_cls)
+    for k in want:
+        scale = max(1.0, float(np.max(np.abs(want[k]))))
+        np.testing.assert_allclose(got[k], want[k], rtol=1e-12, atol=1e-12 * scale, err_msg=k)
+
+
+@pytest.mark.gpu
+def test_gpu_conserves_volume_at_2048(gpu_cls):
+    N, L = 2048, 2048e3
+    g = M.RectilinearGrid(size=(N, N), x=(0.0, L), y=(0.0, L), topology=("Periodic", "Periodic"), halo=(4, 4))
+    P = make(gpu_cls, g, Nsigma=2, masking=M.SmoothIceMask())
+    P.set("H", evaluate(g, "H", lambda x, y: 800 + 200 * math.sin(2 * math.pi * x / L) * math.cos(4 * math.pi * y / L)))
+    P.set("bed", 0.0)
+    P.compute_geometry()
+    P.set("u", evaluate(g, "u", lambda x, y: 1e-6 * math.cos(2 * math.pi * y / L)))
+    P.set("v", evaluate(g, "v", lambda x, y: 1e-6 * math.sin(2 * math.pi * x / L)))
+    V0 = float(np.sum(P.get("H")))
+    for _ in range(3):
+        P.step_thickness(2e8)
+    assert abs(float(np.sum(P.get("H"))) - V0) <= 1e-12 * V0
+    assert np.all(P.energy_get("clipped_thickness") == 0.0)
+    P.close()
