@@ -199,7 +199,21 @@ typedef struct nk_solver_desc {
 #define NK_FIELD_BASAL_MELT_RATE      32
 #define NK_FIELD_GROUNDED_MELT_RATE   33
 #define NK_FIELD_CLIPPED_THICKNESS    34
-#define NK_FIELD_COUNT         35
+/* The energy step's inputs, state and diagnostics (nk_step_enthalpy), zero at first (allocated on first use):
+ * EnthalpyThermodynamics' state (src/Thermodynamics/enthalpy_thermodynamics.jl): the basal water layer H_w (m),
+ * the geothermal flux G (W m^-2), the surface and ocean temperatures (K), the thickness of the last energy step
+ * H^n (m; nk_step_enthalpy sets it to H), and the diagnostics of the last step: the temperate fraction of the
+ * basal layer s_b, the basal heat flux q^g = phi G + friction heat (W m^-2) and the strain heating Phi on the
+ * sigma grid (W m^-3).  All Center-Center; the strain heating has Nsigma planes. */
+#define NK_FIELD_BASAL_WATER_THICKNESS    35
+#define NK_FIELD_GEOTHERMAL_FLUX          36
+#define NK_FIELD_SURFACE_TEMPERATURE      37
+#define NK_FIELD_OCEAN_TEMPERATURE        38
+#define NK_FIELD_THICKNESS_PREVIOUS       39
+#define NK_FIELD_BASAL_TEMPERATE_FRACTION 40
+#define NK_FIELD_BASAL_HEAT_FLUX          41
+#define NK_FIELD_STRAIN_HEATING           42
+#define NK_FIELD_COUNT         43
 
 typedef struct nk_solve_stats {
     int32_t status;                   /* nk_status of the solve */
@@ -302,6 +316,37 @@ nk_status nk_compute_thermal_diagnostics(nk_problem* problem, const nk_thermal_p
  * stage (update_state! without the velocity solve), so the surface, masks, grounded fractions, effective
  * pressure and driving stress follow the new thickness.  NK_BAD_ARGUMENT when dt is not finite and positive. */
 nk_status nk_step_thickness(nk_problem* problem, double dt, int32_t grounded_melt_coupling);
+
+/* The EnthalpyThermodynamics constants of the energy step (src/Thermodynamics/enthalpy_thermodynamics.jl:92-104,
+ * defaults 2.1, 2009, 3.34e5, 7.9e-8, 273.15, 223.15, 1e-3, 1, 1e-3, 1, 0.01, 0.05 / year, coupling on). */
+typedef struct nk_energy_params {
+    double thermal_conductivity;          /* W m^-1 K^-1 */
+    double heat_capacity, latent_heat;    /* J kg^-1 K^-1, J kg^-1 */
+    double clausius_clapeyron;            /* K Pa^-1 */
+    double melting_temperature, reference_temperature;   /* K */
+    double temperate_diffusivity_ratio;   /* temperate / cold diffusivity */
+    double enthalpy_blend_width;          /* J kg^-1 */
+    double water_layer_blend_thickness;   /* m */
+    double minimum_thickness;             /* m: thinner columns hold the surface enthalpy */
+    double drainage_water_fraction;       /* water fraction above which temperate ice drains */
+    double maximum_drainage_rate;         /* s^-1 */
+    int32_t grounded_melt_coupling;       /* the thickness step reads the grounded melt (non-zero) */
+    int32_t reserved;                     /* 0 */
+} nk_energy_params;
+
+#define NK_ENERGY_MAX_LAYERS 64
+
+/* One energy step of length dt (replaces step_thermodynamics!, src/Thermodynamics/column_energy_solve.jl:26-78):
+ * the strain heating of the current velocities and viscosity (strain_heating.jl:7-56), the layer volume and
+ * enthalpy fluxes with first-order upwinding (layer_transport.jl:8-44), the basal state (:127-146), one implicit
+ * tridiagonal system per column in the sigma direction (:148-221) solved in place, the basal water and the
+ * drainage of temperate ice (:223-259), then T and omega from the new enthalpy and H^n = H.  Reads
+ * NK_FIELD_ENTHALPY, H, H^n, the velocities, u_sigma / v_sigma, u_b / v_b, the basal drag and eta_sigma of the
+ * last solve (nk_velocity_profile first), phi, the basal and grounded melt rates and the state fields above;
+ * writes E, T, omega, H_w, the grounded melt rate, H^n and the diagnostics.  The rate factor is not updated
+ * (nk_compute_thermal_diagnostics does that).  NK_BAD_ARGUMENT without the sigma rate-factor layout, with more
+ * than NK_ENERGY_MAX_LAYERS layers, or when dt is not finite and positive. */
+nk_status nk_step_enthalpy(nk_problem* problem, const nk_energy_params* params, double dt);
 
 /* update_stress_balance_coefficients!(x, ...) (SSA) or update_diva_coefficients!(x, ...) (DIVA) at the
  * current velocity fields U, V: eta_sigma, eta_H, F2, eta_H_ff, beta (and beta_b, u_b, v_b for DIVA). */

@@ -480,6 +480,197 @@ void launch_thickness_stage(const ThicknessView& v, double dtau, int final_stage
     k_thickness_stage<<<d.grid, d.block, 0, s>>>(v, dtau, final_stage); count_launch();
 }
 
+// ---- the energy step ----------------------------------------------------------------------------------------
+__device__ __forceinline__ double dmin(double a, double b) { return b < a ? b : a; }
+__device__ __forceinline__ double dmax(double a, double b) { return a < b ? b : a; }
+// unit_ramp(x, w) = clamp(x / w, 0, 1), src/Thermodynamics/enthalpy_conversions.jl:69
+__device__ __forceinline__ double unit_ramp(double x, double w) { return dmin(dmax(x / w, 0.0), 1.0); }
+
+// step_thermodynamics! (src/Thermodynamics/column_energy_solve.jl:26-78) for one column (i, j), one thread:
+// 1. the strain heating Φₖ = 4 ηₖ ε̇ₑ² (+ τᵇ² w₂ₖ / Δζₖ / ηₖ for the DIVA), strain_heating.jl:43-56;
+// 2. the layer volume fluxes Wₖ from the basal melt up, layer_transport.jl:34-44 (upwind Hⁿ through each face);
+// 3. the basal state: conductance D, friction heat F, the ramps r (warm or wet base) and s_b (temperate basal
+//    layer), qᵍ = φ G + F, :127-146;
+// 4. the implicit system of the Nσ layers (:148-221: storage, the upwind-or-diffusive face couplings, the basal
+//    and surface boundary rows, the horizontal upwind enthalpy transport of the old E), built row by row inside the
+//    forward sweep of the Thomas algorithm (row k: a[k-1] E[k-1] + b[k] E[k] + c[k] E[k+1] = f[k]), then the
+//    backward sweep;
+// 5. the basal water balance and the drainage of temperate ice, :223-259;
+// 6. T = min(T_pm, T_r + E / c) and ω = max(0, E - E_pm) / L on every layer.
+// Columns thinner than the minimum thickness hold the surface enthalpy.  E_old is a copy of E: the neighbours'
+// old enthalpy is read while this column writes its new one.
+__global__ void __launch_bounds__(128) k_step_enthalpy(EnergyView v, double dt) {
+    const DevGrid<double>& g = v.g;
+    int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 4 + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    const EnergyConstants& q = v.q;
+    const SigmaTable& sg = v.sig;
+    const int Ns = sg.N;
+    const long long P = v.plane;
+    const int c = g.idx(i, j);
+    const double rho = v.rho_i, ga = v.gacc, H = v.H[c], Hn = v.Hn[c];
+    auto Tpm = [&](double p) { return q.T0 - q.beta * p; };
+    auto Epm = [&](double p) { return q.c * (Tpm(p) - q.Tr); };
+    auto enthalpy = [&](double T, double p) { return q.c * (dmin(T, Tpm(p)) - q.Tr) + 0.0 * q.L; };
+    auto water_fraction = [&](double E, double p) { return dmax(0.0, E - Epm(p)) / q.L; };
+    auto thickness = [&](double h) { return dmax(h, q.min_thickness); };
+    auto layer_pressure = [&](int k) { return rho * ga * H * (1 - sg.zc[k - 1]); };
+    auto Eold = [&](int k, int ii, int jj) { return v.E_old[(k - 1) * P + g.c_idx(ii, jj)]; };
+    auto diffusivity = [&](int k) {
+        double w = unit_ramp(Eold(k, i, j) - Epm(layer_pressure(k)) + q.blend, q.blend);
+        return q.k / q.c * (1 - w + w * q.temperate_ratio);
+    };
+    const double phi_g = v.grounding ? v.phi[c] : 1.0;
+
+    // 1. strain heating
+    double e2 = effective_strain_rate2(g, v.x, v.ud, i, j, v.wall_factor);
+    double tb2 = 0.0;
+    if (v.diva) {
+        int u0 = g.u_idx(i, j), u1 = g.u_idx(i + 1, j), v0 = g.v_idx(i, j), v1 = g.v_idx(i, j + 1);
+        double a0 = v.bb[u0].x * v.ub[u0].x, a1 = v.bb[u1].x * v.ub[u1].x;
+        double b0 = v.bb[v0].y * v.ub[v0].y, b1 = v.bb[v1].y * v.ub[v1].y;
+        tb2 = (a0 * a0 + a1 * a1) / 2 + (b0 * b0 + b1 * b1) / 2;
+    }
+    for (int k = 1; k <= Ns; ++k) {
+        double eta = v.eta_sigma[(k - 1) * P + c];
+        double ph = 4 * eta * e2;
+        if (v.diva) ph += tb2 * sg.w2[k - 1] / sg.dz[k - 1] / (eta == 0.0 ? INFINITY : eta);
+        v.Phi[(k - 1) * P + c] = ph;
+    }
+
+    // 2. layer volume fluxes
+    auto layer_u = [&](int f, int k) { return g.peripheral_fc(f, j) ? 0.0 : v.usig[(k - 1) * P + g.u_idx(f, j)].x; };
+    auto layer_v = [&](int f, int k) { return g.peripheral_cf(i, f) ? 0.0 : v.usig[(k - 1) * P + g.v_idx(i, f)].y; };
+    auto xvol = [&](int f, int k) {
+        double u = layer_u(f, k);
+        return g.dyc[j] * u * (u > 0 ? v.Hn[g.c_idx(f - 1, j)] : v.Hn[g.c_idx(f, j)]);
+    };
+    auto yvol = [&](int f, int k) {
+        double w = layer_v(f, k);
+        return g.dxc[i] * w * (w > 0 ? v.Hn[g.c_idx(i, f - 1)] : v.Hn[g.c_idx(i, f)]);
+    };
+    auto xenth = [&](int f, int k) {
+        double u = v.usig[(k - 1) * P + g.u_idx(f, j)].x;
+        return xvol(f, k) * (u > 0 ? Eold(k, f - 1, j) : Eold(k, f, j));
+    };
+    auto yenth = [&](int f, int k) {
+        double w = v.usig[(k - 1) * P + g.v_idx(i, f)].y;
+        return yvol(f, k) * (w > 0 ? Eold(k, i, f - 1) : Eold(k, i, f));
+    };
+    const double Az = g.Az_cc(i, j);
+    double W[ENERGY_MAX_LAYERS + 1];
+    {
+        double dHdt = (thickness(H) - thickness(Hn)) / dt;
+        double m = v.grounding ? (1 - v.phi[c]) * v.melt[c] : v.melt[c];
+        W[0] = -m - (q.coupled ? v.gmelt[c] : 0.0);
+        for (int k = 1; k <= Ns; ++k) {
+            double div = (xvol(i + 1, k) - xvol(i, k) + yvol(j + 1, k) - yvol(j, k)) / Az;
+            W[k] = W[k - 1] - sg.dz[k - 1] * (dHdt + div);
+        }
+    }
+
+    // 3. basal state
+    const double Ht = thickness(H), Hnt = thickness(Hn);
+    const double D = diffusivity(1) / (Ht * sg.zc[0]);
+    double F;
+    {
+        int u0 = g.u_idx(i, j), u1 = g.u_idx(i + 1, j), v0 = g.v_idx(i, j), v1 = g.v_idx(i, j + 1);
+        double bu0 = v.diva ? v.bb[u0].x : v.coef[u0].z, bu1 = v.diva ? v.bb[u1].x : v.coef[u1].z;
+        double bv0 = v.diva ? v.bb[v0].y : v.coef[v0].w, bv1 = v.diva ? v.bb[v1].y : v.coef[v1].w;
+        double ub0 = v.ub[u0].x, ub1 = v.ub[u1].x, vb0 = v.ub[v0].y, vb1 = v.ub[v1].y;
+        F = (bu0 * ub0 * ub0 + bu1 * ub1 * ub1 + bv0 * vb0 * vb0 + bv1 * vb1 * vb1) / 2;
+    }
+    const double pb = rho * ga * H;
+    const double Epm_b = Epm(pb);
+    const double Hw0 = v.Hw[c], G = v.G[c];
+    const double r = dmax(unit_ramp(Eold(1, i, j) + (G + F) / D - Epm_b, q.blend), unit_ramp(Hw0, q.water_blend));
+    const double sb = unit_ramp(Eold(1, i, j) - Epm(layer_pressure(1)) + q.blend, q.blend);
+    const double qg = phi_g * G + F;
+    v.sb[c] = sb;
+    v.qg[c] = qg;
+
+    // 4. the column system and the Thomas algorithm
+    const bool mu = H > q.min_thickness;
+    const double Es = enthalpy(v.Ts[c], 0.0);
+    const double chi = phi_g * r * (1 - sb);
+    const double Eo = enthalpy(v.To[c], pb);
+    const double Fb = rho * W[0];
+    const double Lam = D * (chi + 1 - phi_g) + dmax(-Fb, 0.0);
+    const double S = (1 - r) * qg + D * (chi * Epm_b + (1 - phi_g) * Eo) + dmax(Fb, 0.0) * Epm_b;
+    const double Fs = rho * W[Ns];
+    const double Ks = diffusivity(Ns) / (Ht * (1 - sg.zc[Ns - 1]));
+    const double Ds = Ks + dmax(Fs, 0.0), Ss = (Ks + dmax(-Fs, 0.0)) * Es;
+    auto couplings = [&](int kf, double& lower, double& upper) {   // interior face kf = 2..Nσ
+        double zf = sg.zf[kf - 1], zm = sg.zc[kf - 2], zp = sg.zc[kf - 1];
+        double theta = (zf - zm) / (zp - zm);
+        double Fk = rho * W[kf - 1];
+        double cond = 1 / (Ht * ((zf - zm) / diffusivity(kf - 1) + (zp - zf) / diffusivity(kf)));
+        double Dk = dmax(cond, dmax(dmax(Fk, 0.0) * theta, dmax(-Fk, 0.0) * (1 - theta)));
+        lower = -Fk * (1 - theta) - Dk;
+        upper = Fk * theta - Dk;
+    };
+    double t[ENERGY_MAX_LAYERS + 1], e[ENERGY_MAX_LAYERS + 1];
+    double lower_m = 0, upper_m = 0, prev_a = 0, prev_c = 0, piv = 1;
+    for (int k = 1; k <= Ns; ++k) {
+        double dz = sg.dz[k - 1];
+        double lower_p = 0, upper_p = 0;
+        if (k < Ns) couplings(k + 1, lower_p, upper_p);
+        double diag_m = k == 1 ? Lam : -upper_m;
+        double diag_p = k == Ns ? Ds : -lower_p;
+        double forcing = (k == 1 ? S : 0.0) + (k == Ns ? Ss : 0.0);
+        double transport = rho * dz * ((xenth(i + 1, k) - xenth(i, k) + yenth(j + 1, k) - yenth(j, k)) / Az);
+        double ak = mu ? lower_p : 0.0;
+        double ck = mu ? upper_p : 0.0;
+        double bk = mu ? rho * Ht * dz / dt + diag_m + diag_p : 1.0;
+        double fk = mu ? rho * Hnt * dz * Eold(k, i, j) / dt - transport + Ht * dz * v.Phi[(k - 1) * P + c] + forcing : Es;
+        if (k == 1) {
+            piv = bk;
+            e[1] = fk / piv;
+        } else {
+            t[k] = prev_c / piv;
+            piv = bk - prev_a * t[k];
+            e[k] = (fk - prev_a * e[k - 1]) / piv;
+        }
+        prev_a = ak; prev_c = ck;
+        lower_m = lower_p; upper_m = upper_p;
+    }
+    for (int k = Ns - 1; k >= 1; --k) e[k] -= t[k + 1] * e[k + 1];
+
+    // 5. basal water and drainage
+    {
+        double qb = D * (Epm_b - e[1]);
+        double m = r * (qg - phi_g * (1 - sb) * qb) / (rho * q.L);
+        double drained = 0;
+        for (int k = 1; k <= Ns; ++k) {
+            double w = water_fraction(e[k], layer_pressure(k));
+            double x = w / q.drainage_fraction;
+            double rate = q.max_drainage_rate * (dmin(dmax(x - 1, 0.0), 1.0) / 10 + 9 * dmin(dmax(x - 2, 0.0), 1.0) / 10);
+            double dw = dmin(dt * rate, dmax(w - q.drainage_fraction, 0.0));
+            dw = mu ? dw : 0.0;
+            e[k] -= q.L * dw;
+            drained += Ht * sg.dz[k - 1] * dw;
+        }
+        double Hstar = Hw0 + dt * (mu ? m : 0.0) + drained;
+        double Hplus = dmax(0.0, Hstar);
+        double missing = Hplus - Hstar;
+        v.gmelt[c] = (Hplus - Hw0) / dt;
+        v.Hw[c] = Hplus;
+        e[1] -= q.L * missing / (Ht * sg.dz[0]);
+    }
+
+    // 6. the new enthalpy and its diagnostics
+    for (int k = 1; k <= Ns; ++k) {
+        double p = layer_pressure(k), E = e[k];
+        v.E[(k - 1) * P + c] = E;
+        v.T[(k - 1) * P + c] = dmin(Tpm(p), q.Tr + E / q.c);
+        v.omega[(k - 1) * P + c] = water_fraction(E, p);
+    }
+}
+void launch_step_enthalpy(const EnergyView& v, double dt, cudaStream_t s) {
+    dim3 block(32, 4), grid((v.g.Nx + 31) / 32, (v.g.Ny + 3) / 4);
+    k_step_enthalpy<<<grid, block, 0, s>>>(v, dt); count_launch();
+}
+
 // ---- fixed-point adjoint of the SSA Picard step -------------------------------------------------------------
 // The reverse of picard_coefficient_step! (ext/NunatakEnzymeExt.jl:142-157): with q = A(c(x)) x*, the seed
 // q̄ = -λ, and x* the converged velocity, it returns ȳ = -(∂q/∂x)ᵀ λ.  Only active operator rows depend on

@@ -13,6 +13,7 @@ struct SigmaTable {
     const double* w2;     // layer_weight(k, 2)
     const double* zc;     // znode(k, Center)
     const double* w1;     // profile_weight(k', k, 1) at [k * N + k'] for k' <= k
+    const double* zf;     // znode(k, Face), the N + 1 faces
 };
 
 // Fine-grid inputs of the coefficient update (all FP64, pitched; pairs interleave the u and v faces).
@@ -186,6 +187,34 @@ struct ThicknessView {
     int grounding, coupled;
 };
 void launch_thickness_stage(const ThicknessView& v, double dtau, int final_stage, cudaStream_t s);
+
+// ---- the energy step -------------------------------------------------------------------------------------
+constexpr int ENERGY_MAX_LAYERS = 64;
+struct EnergyConstants {
+    double k, c, L, beta, T0, Tr;              // conductivity, heat capacity, latent heat, Clausius-Clapeyron, melting, reference
+    double temperate_ratio, blend, water_blend, min_thickness, drainage_fraction, max_drainage_rate;
+    int coupled;
+};
+struct EnergyView {
+    DevGrid<double> g;
+    SigmaTable sig;
+    long long plane;
+    EnergyConstants q;
+    double rho_i, gacc, wall_factor;
+    int diva, grounding;
+    const double2* x; const double2* ud;       // depth-averaged velocities, prescribed faces (or null)
+    const double2* usig;                       // layer velocities (σ planes)
+    const double2* ub;                         // basal velocities
+    const double4* coef;                       // SSA basal drag (βᵘ, βᵛ) in .z / .w
+    const double2* bb;                         // DIVA basal drag (βᵇᵘ, βᵇᵛ)
+    const double* eta_sigma;                   // layer viscosity (σ planes)
+    const double* H; const double* Hn; const double* phi;
+    const double* melt; const double* G; const double* Ts; const double* To;
+    const double* E_old;                       // the enthalpy at the start of the step (σ planes, read with neighbours)
+    double* E; double* T; double* omega;       // σ planes
+    double* Hw; double* gmelt; double* sb; double* qg; double* Phi;
+};
+void launch_step_enthalpy(const EnergyView& v, double dt, cudaStream_t s);
 
 // ---- multigrid ------------------------------------------------------------------------------------------
 template <typename T>

@@ -197,11 +197,12 @@ struct nk_problem {
     double2* partials = nullptr;
     SolverScalars* sc = nullptr;
     SolverScalars* sc_host = nullptr;          // pinned mirror
-    double* sig_tables = nullptr;              // dz, w2, zc (Ns each) + w1 (Ns * Ns)
+    double* sig_tables = nullptr;              // dz, w2, zc (Ns each) + w1 (Ns * Ns) + zf (Ns + 1)
     double* rate_params = nullptr;             // 9 (nk_compute_rate_factor) or 14 (nk_thermal_params)
     double* thermal = nullptr;                 // enthalpy then water fraction (Ns planes each), allocated on first use
     double* transport = nullptr;               // a, m, mᵍ, clipped thickness, then H at the step's and the stage's start
-    std::vector<double> sig_dz, sig_w2, sig_zc, sig_w1;
+    double* energy = nullptr;                  // H_w, G, T_s, T_o, Hⁿ, s_b, qᵍ, then Φ and the step-start E (Ns planes each)
+    std::vector<double> sig_dz, sig_w2, sig_zc, sig_w1, sig_zf;
 
     // coarse levels
     std::vector<Level<double>> lv64;           // FP64 hierarchy: [0] is the fine grid view
@@ -244,6 +245,7 @@ struct nk_problem {
         t.w2 = sig_tables + Ns;
         t.zc = sig_tables + 2 * Ns;
         t.w1 = sig_tables + 3 * Ns;
+        t.zf = sig_tables + 3 * Ns + (size_t)Ns * Ns;
         return t;
     }
     PhysView phys() const {
@@ -382,6 +384,7 @@ static void build(nk_problem* P, bool dry = false) {
     auto zf = [&](int k1) { return faces[k1 - 1]; };                      // znode(k, Face), 1-based
     auto zc = [&](int k1) { return (faces[k1 - 1] + faces[k1]) / 2; };   // znode(k, Center)
     P->sig_dz.resize(P->Ns); P->sig_w2.resize(P->Ns); P->sig_zc.resize(P->Ns); P->sig_w1.assign((size_t)P->Ns * P->Ns, 0.0);
+    P->sig_zf = faces;
     for (int k = 1; k <= P->Ns; ++k) {
         P->sig_dz[k - 1] = zf(k + 1) - zf(k);
         P->sig_w2[k - 1] = power_integral(zf(k), zf(k + 1), 2);
@@ -458,7 +461,7 @@ static void build(nk_problem* P, bool dry = false) {
     size_t nblocks = std::max((size_t)big.grid.x * big.grid.y, (size_t)strips.grid.x * strips.grid.y);
     slots.push_back({(void**)&P->partials, A.reserve(nblocks * sizeof(double2))});
     slots.push_back({(void**)&P->sc, A.reserve(sizeof(SolverScalars))});
-    slots.push_back({(void**)&P->sig_tables, A.reserve((3 * P->Ns + (size_t)P->Ns * P->Ns) * sizeof(double))});
+    slots.push_back({(void**)&P->sig_tables, A.reserve((4 * P->Ns + 1 + (size_t)P->Ns * P->Ns) * sizeof(double))});
     slots.push_back({(void**)&P->rate_params, A.reserve(16 * sizeof(double))});
     if (P->precond == NK_PRECONDITIONER_MULTIGRID) {
         if (P->mixed) {
@@ -480,6 +483,7 @@ static void build(nk_problem* P, bool dry = false) {
     tables.insert(tables.end(), P->sig_w2.begin(), P->sig_w2.end());
     tables.insert(tables.end(), P->sig_zc.begin(), P->sig_zc.end());
     tables.insert(tables.end(), P->sig_w1.begin(), P->sig_w1.end());
+    tables.insert(tables.end(), P->sig_zf.begin(), P->sig_zf.end());
     NK_CUDA(cudaMemcpyAsync(P->sig_tables, tables.data(), tables.size() * sizeof(double), cudaMemcpyHostToDevice, P->stream));
     NK_CUDA(cudaStreamSynchronize(P->stream));
     if (P->precond == NK_PRECONDITIONER_MULTIGRID) {
@@ -1027,7 +1031,10 @@ struct FieldLoc {
     bool prescribed = false;  // a prescribed velocity (allocated on first use)
     bool thermal = false;     // the enthalpy or the water fraction (allocated on first use, sigma layout only)
     bool transport = false;   // a source or the clip of the thickness step (allocated on first use)
+    bool energy = false;      // a state field or diagnostic of the energy step (allocated on first use)
 };
+
+static const int ENERGY_PLANES_2D = 7;   // the energy step's Center-Center planes before Φ
 
 static FieldLoc field_loc(nk_problem* P, int id) {
     FieldLoc f;
@@ -1082,6 +1089,21 @@ static FieldLoc field_loc(nk_problem* P, int id) {
             cc(P->transport ? P->transport + (size_t)(id - NK_FIELD_SURFACE_MASS_BALANCE) * P->plane : nullptr);
             f.transport = true;
             break;
+        case NK_FIELD_BASAL_WATER_THICKNESS:
+        case NK_FIELD_GEOTHERMAL_FLUX:
+        case NK_FIELD_SURFACE_TEMPERATURE:
+        case NK_FIELD_OCEAN_TEMPERATURE:
+        case NK_FIELD_THICKNESS_PREVIOUS:
+        case NK_FIELD_BASAL_TEMPERATE_FRACTION:
+        case NK_FIELD_BASAL_HEAT_FLUX:
+            cc(P->energy ? P->energy + (size_t)(id - NK_FIELD_BASAL_WATER_THICKNESS) * P->plane : nullptr);
+            f.energy = true;
+            break;
+        case NK_FIELD_STRAIN_HEATING:
+            cc(P->energy ? P->energy + (size_t)ENERGY_PLANES_2D * P->plane : nullptr);
+            f.planes = P->Ns;
+            f.energy = true;
+            break;
         default: break;
     }
     return f;
@@ -1094,6 +1116,16 @@ static void ensure_thermal(nk_problem* P) {
     size_t bytes = 2 * (size_t)P->Ns * P->plane * sizeof(double);
     NK_CUDA(cudaMalloc((void**)&P->thermal, bytes));
     NK_CUDA(cudaMemsetAsync(P->thermal, 0, bytes, P->stream));
+}
+
+// The energy step's planes (zero at first): the seven fields NK_FIELD_BASAL_WATER_THICKNESS ..
+// NK_FIELD_BASAL_HEAT_FLUX, the strain heating (Ns planes) and the enthalpy at the start of the step (Ns planes).
+static void ensure_energy(nk_problem* P) {
+    if (P->energy) return;
+    if (P->async_pending) bad("an asynchronous solve is pending (nk_problem_wait first)");
+    size_t bytes = (ENERGY_PLANES_2D + 2 * (size_t)P->Ns) * P->plane * sizeof(double);
+    NK_CUDA(cudaMalloc((void**)&P->energy, bytes));
+    NK_CUDA(cudaMemsetAsync(P->energy, 0, bytes, P->stream));
 }
 
 // The thickness step's planes (zero at first): the four fields of NK_FIELD_SURFACE_MASS_BALANCE ..
@@ -1316,6 +1348,7 @@ nk_status nk_problem_destroy(nk_problem* P) {
     if (P->ud) cudaFree(P->ud);
     if (P->thermal) cudaFree(P->thermal);
     if (P->transport) cudaFree(P->transport);
+    if (P->energy) cudaFree(P->energy);
     if (P->stream) cudaStreamDestroy(P->stream);
     delete P;
     return NK_OK;
@@ -1324,7 +1357,7 @@ nk_status nk_problem_destroy(nk_problem* P) {
 int64_t nk_problem_field_size(const nk_problem* P, int32_t id) {
     if (!P) return 0;
     FieldLoc f = field_loc(const_cast<nk_problem*>(P), id);
-    return (f.base || f.prescribed || f.thermal || f.transport) ? (int64_t)f.nx * f.ny * f.planes : 0;
+    return (f.base || f.prescribed || f.thermal || f.transport || f.energy) ? (int64_t)f.nx * f.ny * f.planes : 0;
 }
 
 nk_status nk_problem_set_field(nk_problem* P, int32_t id, const double* host, int64_t count) {
@@ -1342,6 +1375,10 @@ nk_status nk_problem_set_field(nk_problem* P, int32_t id, const double* host, in
         }
         if (f.transport) {
             ensure_transport(P);
+            f = field_loc(P, id);
+        }
+        if (f.energy) {
+            ensure_energy(P);
             f = field_loc(P, id);
         }
         if (!f.base) bad("unknown field id or field not held by this problem");
@@ -1374,6 +1411,10 @@ nk_status nk_problem_get_field(const nk_problem* Pc, int32_t id, double* host, i
             ensure_transport(P);
             f = field_loc(P, id);
         }
+        if (f.energy) {
+            ensure_energy(P);
+            f = field_loc(P, id);
+        }
         if (!f.base) bad("unknown field id or field not held by this problem");
         if (count != (int64_t)f.nx * f.ny * f.planes) bad("field size mismatch");
         copy_out(P, f, host);
@@ -1398,6 +1439,10 @@ nk_status nk_problem_set_field_parent(nk_problem* P, int32_t id, const double* p
         }
         if (f.transport) {
             ensure_transport(P);
+            f = field_loc(P, id);
+        }
+        if (f.energy) {
+            ensure_energy(P);
             f = field_loc(P, id);
         }
         if (!f.base) bad("unknown field id or field not held by this problem");
@@ -1430,6 +1475,10 @@ nk_status nk_problem_get_field_parent(const nk_problem* Pc, int32_t id, double* 
             ensure_transport(P);
             f = field_loc(P, id);
         }
+        if (f.energy) {
+            ensure_energy(P);
+            f = field_loc(P, id);
+        }
         if (!f.base) bad("unknown field id or field not held by this problem");
         copy_out_parent(P, f, parent, parent_layout(f, hx, hy, hz, count));
     });
@@ -1453,6 +1502,51 @@ nk_status nk_compute_geometry(nk_problem* P) {
     return guarded(P->ctx, [&] {
         launch_problem_geometry(P);
         NK_CHECK_LAUNCH();
+        NK_CUDA(cudaStreamSynchronize(P->stream));
+    });
+}
+
+nk_status nk_step_enthalpy(nk_problem* P, const nk_energy_params* prm, double dt) {
+    if (!P || !prm) return NK_BAD_ARGUMENT;
+    return guarded(P->ctx, [&] {
+        static_assert(sizeof(nk_energy_params) == 12 * sizeof(double) + 2 * sizeof(int32_t), "nk_energy_params layout");
+        if (!(dt > 0) || !std::isfinite(dt)) bad("the time step must be finite and positive");
+        if (P->pd.rate_factor_layout != NK_RATE_FACTOR_SIGMA) bad("the energy step needs the sigma rate-factor layout");
+        if (P->Ns > ENERGY_MAX_LAYERS) bad("the energy step takes at most NK_ENERGY_MAX_LAYERS layers");
+        if (!(prm->heat_capacity > 0) || !(prm->latent_heat > 0) || !(prm->thermal_conductivity > 0) ||
+            !(prm->enthalpy_blend_width > 0) || !(prm->water_layer_blend_thickness > 0) || !(prm->drainage_water_fraction > 0) ||
+            !(prm->minimum_thickness > 0))
+            bad("conductivity, heat capacity, latent heat, blend widths, minimum thickness and drainage fraction must be positive");
+        if (P->async_pending) bad("an asynchronous solve is pending (nk_problem_wait first)");
+        static_assert(ENERGY_MAX_LAYERS == NK_ENERGY_MAX_LAYERS, "one layer limit");
+        ensure_thermal(P);
+        ensure_transport(P);
+        ensure_energy(P);
+        const size_t pl = P->plane;
+        EnergyView v;
+        v.g = P->fine.g;
+        v.sig = P->sigma_table();
+        v.plane = (long long)pl;
+        v.q = {prm->thermal_conductivity, prm->heat_capacity, prm->latent_heat, prm->clausius_clapeyron, prm->melting_temperature,
+               prm->reference_temperature, prm->temperate_diffusivity_ratio, prm->enthalpy_blend_width,
+               prm->water_layer_blend_thickness, prm->minimum_thickness, prm->drainage_water_fraction, prm->maximum_drainage_rate,
+               prm->grounded_melt_coupling != 0};
+        v.rho_i = P->pd.ice_density; v.gacc = P->pd.gravitational_acceleration;
+        v.wall_factor = P->pd.side_walls == NK_NO_SLIP ? 2.0 : 0.0;
+        v.diva = P->pd.stress_balance == NK_DIVA; v.grounding = P->pd.grounding != 0;
+        v.x = P->x; v.ud = P->ud; v.usig = P->usig; v.ub = P->ub; v.coef = P->fine.coef; v.bb = P->bb; v.eta_sigma = P->eta_sigma;
+        v.H = P->H; v.phi = P->phi;
+        double* en = P->energy;
+        v.Hw = en; v.G = en + pl; v.Ts = en + 2 * pl; v.To = en + 3 * pl; v.Hn = en + 4 * pl; v.sb = en + 5 * pl; v.qg = en + 6 * pl;
+        v.Phi = en + ENERGY_PLANES_2D * pl;
+        double* E_old = en + (ENERGY_PLANES_2D + (size_t)P->Ns) * pl;
+        v.E_old = E_old;
+        v.melt = P->transport + pl; v.gmelt = P->transport + 2 * pl;
+        v.E = P->thermal; v.omega = P->thermal + (size_t)P->Ns * pl; v.T = P->T;
+        NK_CUDA(cudaMemcpyAsync(E_old, P->thermal, (size_t)P->Ns * pl * sizeof(double), cudaMemcpyDeviceToDevice, P->stream));
+        launch_step_enthalpy(v, dt, P->stream);
+        NK_CHECK_LAUNCH();
+        NK_CUDA(cudaMemcpyAsync(en + 4 * pl, P->H, pl * sizeof(double), cudaMemcpyDeviceToDevice, P->stream));   // Hⁿ = H
         NK_CUDA(cudaStreamSynchronize(P->stream));
     });
 }

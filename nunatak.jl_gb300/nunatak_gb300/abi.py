@@ -33,6 +33,8 @@ FIELD_IDS = {
     "u_b": 22, "v_b": 23, "u_sigma": 24, "v_sigma": 25, "T": 26,
     "u_prescribed": 27, "v_prescribed": 28, "E": 29, "omega": 30,
     "surface_mass_balance": 31, "basal_melt_rate": 32, "grounded_melt": 33, "clipped_thickness": 34,
+    "Hw": 35, "geothermal_flux": 36, "surface_temperature": 37, "ocean_temperature": 38, "H_previous": 39,
+    "basal_temperate_fraction": 40, "basal_heat_flux": 41, "strain_heating": 42,
 }
 
 # (location x, location y, on the sigma grid) of each field: "c" Center, "f" Face.
@@ -50,7 +52,20 @@ FIELD_LOCATIONS = {
     "E": ("c", "c", True), "omega": ("c", "c", True),
     "surface_mass_balance": ("c", "c", False), "basal_melt_rate": ("c", "c", False),
     "grounded_melt": ("c", "c", False), "clipped_thickness": ("c", "c", False),
+    "Hw": ("c", "c", False), "geothermal_flux": ("c", "c", False), "surface_temperature": ("c", "c", False),
+    "ocean_temperature": ("c", "c", False), "H_previous": ("c", "c", False),
+    "basal_temperate_fraction": ("c", "c", False), "basal_heat_flux": ("c", "c", False),
+    "strain_heating": ("c", "c", True),
 }
+
+
+class EnergyParams(C.Structure):
+    """nk_energy_params: the EnthalpyThermodynamics constants of nk_step_enthalpy."""
+    _fields_ = [(n, C.c_double) for n in (
+        "thermal_conductivity", "heat_capacity", "latent_heat", "clausius_clapeyron", "melting_temperature",
+        "reference_temperature", "temperate_diffusivity_ratio", "enthalpy_blend_width", "water_layer_blend_thickness",
+        "minimum_thickness", "drainage_water_fraction", "maximum_drainage_rate")] + \
+        [("grounded_melt_coupling", C.c_int32), ("reserved", C.c_int32)]
 
 
 class IterationControl(C.Structure):

@@ -172,8 +172,10 @@ class Problem:
                                 melting_temperature, reference_temperature)
         _check(self._fn("compute_thermal_diagnostics")(self._h, C.byref(prm)), "compute_thermal_diagnostics", self._err())
 
-    # the thickness step's sources and clip, under the names of the energy-step fields
-    TRANSPORT_FIELDS = ("surface_mass_balance", "basal_melt_rate", "grounded_melt", "clipped_thickness")
+    # the thickness and energy steps' sources, state and diagnostics
+    TRANSPORT_FIELDS = ("surface_mass_balance", "basal_melt_rate", "grounded_melt", "clipped_thickness", "Hw",
+                        "geothermal_flux", "surface_temperature", "ocean_temperature", "H_previous",
+                        "basal_temperate_fraction", "basal_heat_flux", "strain_heating")
 
     def energy_set(self, name, value):
         if name not in self.TRANSPORT_FIELDS:
@@ -184,6 +186,19 @@ class Problem:
         if name not in self.TRANSPORT_FIELDS:
             raise KeyError(f"the library holds no energy-step field {name!r}")
         return self.get(name)
+
+    def step_enthalpy(self, dt, thermal_conductivity=2.1, heat_capacity=2009.0, latent_heat=3.34e5, clausius_clapeyron=7.9e-8,
+                      melting_temperature=273.15, reference_temperature=223.15, temperate_diffusivity_ratio=1e-3,
+                      enthalpy_blend_width=1.0, water_layer_blend_thickness=1e-3, minimum_thickness=1.0,
+                      drainage_water_fraction=0.01, maximum_drainage_rate=1.58443823077064e-9, grounded_melt_coupling=True):
+        """One energy step of length dt (step_thermodynamics!, src/Thermodynamics/column_energy_solve.jl:26-78) from
+        the velocities and viscosity of the last solve (velocity_profile first); defaults: EnthalpyThermodynamics'
+        (src/Thermodynamics/enthalpy_thermodynamics.jl:92-104)."""
+        prm = abi.EnergyParams(thermal_conductivity, heat_capacity, latent_heat, clausius_clapeyron, melting_temperature,
+                               reference_temperature, temperate_diffusivity_ratio, enthalpy_blend_width,
+                               water_layer_blend_thickness, minimum_thickness, drainage_water_fraction, maximum_drainage_rate,
+                               int(grounded_melt_coupling), 0)
+        _check(self._fn("step_enthalpy")(self._h, C.byref(prm), float(dt)), "step_enthalpy", self._err())
 
     def step_thickness(self, dt, grounded_melt_coupling=False):
         """One ice time step of the thickness with the velocities held (the three rk_substep! stages of time_step!,

@@ -1819,6 +1819,14 @@ static FieldRef field_ref(Problem& P, int id) {
         case NK_FIELD_BASAL_MELT_RATE: r.f = &P.melt; break;
         case NK_FIELD_GROUNDED_MELT_RATE: r.f = &P.gmelt; break;
         case NK_FIELD_CLIPPED_THICKNESS: r.f = &P.clipped; break;
+        case NK_FIELD_BASAL_WATER_THICKNESS: r.f = &P.Hw; break;
+        case NK_FIELD_GEOTHERMAL_FLUX: r.f = &P.G; break;
+        case NK_FIELD_SURFACE_TEMPERATURE: r.f = &P.Ts; break;
+        case NK_FIELD_OCEAN_TEMPERATURE: r.f = &P.To; break;
+        case NK_FIELD_THICKNESS_PREVIOUS: r.f = &P.Hn; break;
+        case NK_FIELD_BASAL_TEMPERATE_FRACTION: r.f = &P.sb; break;
+        case NK_FIELD_BASAL_HEAT_FLUX: r.f = &P.qg; break;
+        case NK_FIELD_STRAIN_HEATING: r.s = &P.Phi; break;
         default: break;
     }
     return r;

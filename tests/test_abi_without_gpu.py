@@ -57,6 +57,7 @@ def test_null_handles_are_refused(lib):
         "nk_compute_rate_factor": lambda: lib.nk_compute_rate_factor(null, *([0.0] * 9)),
         "nk_compute_thermal_diagnostics": lambda: lib.nk_compute_thermal_diagnostics(null, null),
         "nk_step_thickness": lambda: lib.nk_step_thickness(null, 1.0, 0),
+        "nk_step_enthalpy": lambda: lib.nk_step_enthalpy(null, null, 1.0),
         "nk_update_coefficients": lambda: lib.nk_update_coefficients(null),
         "nk_apply_operator": lambda: lib.nk_apply_operator(null, d, d, d, d),
         "nk_precondition": lambda: lib.nk_precondition(null, d, d, d, d),

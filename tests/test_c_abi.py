@@ -70,6 +70,7 @@ int main(void) {
     S(nk_server_desc) F(nk_server_desc, flags) F(nk_server_desc, memory_cap_bytes)
     S(nk_request) F(nk_request, physics) F(nk_request, solver) F(nk_request, H) F(nk_request, v_out)
     S(nk_thermal_params) F(nk_thermal_params, water_softening_coefficient) F(nk_thermal_params, reference_temperature)
+    S(nk_energy_params) F(nk_energy_params, maximum_drainage_rate) F(nk_energy_params, grounded_melt_coupling) F(nk_energy_params, reserved)
     return 0;
 }
 """
@@ -90,7 +91,8 @@ def test_ctypes_mirrors_match_the_c_layout(tmp_path):
     out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
     mirrors = {"nk_iteration_control": abi.IterationControl, "nk_grid_desc": abi.GridDesc, "nk_physics_desc": abi.PhysicsDesc,
                "nk_solver_desc": abi.SolverDesc, "nk_solve_stats": abi.SolveStats, "nk_server_desc": abi.ServerDesc,
-               "nk_request": abi.Request, "nk_thermal_params": abi.ThermalParams}
+               "nk_request": abi.Request, "nk_thermal_params": abi.ThermalParams,
+               "nk_energy_params": abi.EnergyParams}
     checked = 0
     for line in filter(None, out):
         parts = line.split()
@@ -102,4 +104,4 @@ def test_ctypes_mirrors_match_the_c_layout(tmp_path):
         else:
             assert ctypes.sizeof(mirrors[parts[0]]) == int(parts[1]), parts
         checked += 1
-    assert checked == 31
+    assert checked == 35

@@ -1,6 +1,6 @@
 """The oracle's energy step (nko_step_enthalpy: step_thermodynamics!, src/Thermodynamics/column_energy_solve.jl:26-78)
-against the column testsets of test/test_thermodynamics.jl.  Test infrastructure for the enthalpy row that comes
-after the velocity solve: the library has no energy step yet, so these run on the oracle only.
+against the column testsets of test/test_thermodynamics.jl, and the library's energy step (nk_step_enthalpy,
+marked gpu) against the oracle's on the same seeded inputs.
 
 column_model (test/test_thermodynamics.jl:3-14): one Periodic column, 1 km wide, ρᵢ = 910, no velocity solve and
 no thickness change, so each time step is one energy step of the same length:
@@ -22,7 +22,11 @@ with the thickness step of the oracle as well:
 - strong accumulation over a sharp front creates no new extrema (:360-370);
 - upwind transport at unit Courant number shifts each moving layer by one cell and leaves the others (:372-390);
 with the velocity solve as well:
-- the basal plus strain heat equals the power of the driving stress to 1e-8, SSA and DIVA (:392-398)."""
+- the basal plus strain heat equals the power of the driving stress to 1e-8, SSA and DIVA (:392-398).
+The library against the oracle (gpu), SSA and DIVA: a 24 x 20 sheet over a sloping bed, Bounded in x and Periodic
+in y, 8 layers, the velocity state of the oracle's solve copied into the library, seeded enthalpy with cold,
+temperate and draining layers, wet and dry beds, thinning and thickening columns: two energy steps agree in E,
+T, ω, H_w, mᵍ, s_b, qᵍ and Φ to 1e-10 relative (FMA contraction on the GPU rounds apart by a few ulps)."""
 import math
 
 import numpy as np
@@ -360,3 +364,68 @@ def test_friction_and_strain_heat_account_for_the_driving_work(oracle_cls, shear
     power = float(np.sum(P.get("tau_u") * P.get("u")) + np.sum(P.get("tau_v") * P.get("v")))
     assert power > 0
     assert abs(heat - power) / power < 1e-8, (heat, power)
+
+
+def seeded_energy_case(cls, shear, state=None):
+    """Two energy steps of a seeded sheet on backend cls.  Without `state` the oracle solves the velocities and
+    returns their state with the result; with it, that state is set instead of solving."""
+    rng = np.random.default_rng(1203)
+    Nx, Ny, Ns = 24, 20, 8
+    g = M.RectilinearGrid(size=(Nx, Ny), x=(0.0, Nx * 2e3), y=(0.0, Ny * 2e3), topology=("Bounded", "Periodic"), halo=(4, 4))
+    P = make(cls, g, Nsigma=Ns, rheology=M.GlenFlowLaw(rate_factor="sigma"), grounding=M.SubgridGroundedFraction(),
+             friction=M.WeertmanFriction(coefficient=1e10, exponent=1.0), stress_balance=M.DepthIntegrated(shear=shear),
+             constants=M.IceSheetConstants(ice_density=RHO))
+    x = g.centers(0)
+    H = 900 - 8 * x[None, :] / 1e3 + rng.uniform(0, 50, (Ny, Nx))
+    H[rng.uniform(size=(Ny, Nx)) < 0.05] = 0.5
+    P.set("H", H)
+    P.set("bed", np.broadcast_to(-200 - 12 * x[None, :] / 1e3, (Ny, Nx)) + rng.uniform(-10, 10, (Ny, Nx)))
+    P.set("A", 1e-24)
+    P.set("C", 1e10)
+    P.compute_geometry()
+    names = ["u", "v", "eta_sigma", "u_sigma", "v_sigma", "u_b", "v_b"] + (["beta_b_u", "beta_b_v"] if shear else ["beta_u", "beta_v"])
+    if state is None:
+        assert P.picard_solve().status == 0
+        P.velocity_profile()
+        state = {k: P.get(k) for k in names}
+    else:
+        for k in names:
+            P.set(k, state[k])
+    zeta = np.array([(a + b) / 2 for a, b in zip(M.sigma_faces(Ns)[:-1], M.sigma_faces(Ns)[1:])])
+    p = RHO * GRAV * H[None] * (1 - zeta[:, None, None])
+    T = 255 + 25 * rng.uniform(size=(Ns, Ny, Nx))
+    w = np.where(rng.uniform(size=(Ns, Ny, Nx)) < 0.3, rng.uniform(0, 0.04, (Ns, Ny, Nx)), 0.0)
+    P.set("E", enthalpy(T, w, p))
+    for name, value in (("Hw", np.where(rng.uniform(size=(Ny, Nx)) < 0.5, rng.uniform(0, 0.01, (Ny, Nx)), 0.0)),
+                        ("geothermal_flux", rng.uniform(0.04, 0.08, (Ny, Nx))),
+                        ("surface_temperature", rng.uniform(240, 265, (Ny, Nx))),
+                        ("ocean_temperature", rng.uniform(270, 272, (Ny, Nx))),
+                        ("H_previous", H * (1 + rng.uniform(-0.01, 0.01, (Ny, Nx)))),
+                        ("basal_melt_rate", rng.uniform(0, 1e-8, (Ny, Nx))),
+                        ("grounded_melt", rng.uniform(0, 1e-10, (Ny, Nx)))):
+        P.energy_set(name, value)
+    for _ in range(2):
+        P.step_enthalpy(3e9)
+    out = {k: P.get(k) for k in ("E", "T", "omega")}
+    for k in ("Hw", "grounded_melt", "basal_temperate_fraction", "basal_heat_flux", "strain_heating", "H_previous"):
+        out[k] = P.energy_get(k)
+    P.close()
+    return out, state
+
+
+@pytest.mark.parametrize("shear", [None, M.DIVAShear()], ids=["SSA", "DIVA"])
+def test_seeded_energy_case_exercises_every_branch(oracle_cls, shear):
+    out, _ = seeded_energy_case(oracle_cls, shear)
+    assert np.any(out["omega"] > 0.01) and np.any(out["omega"] == 0.0)        # temperate and cold layers
+    assert np.any(out["Hw"] > 0) and np.any(out["Hw"] == 0.0)                  # wet and dry beds
+    assert np.any(out["basal_temperate_fraction"] > 0) and np.any(out["strain_heating"] > 0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shear", [None, M.DIVAShear()], ids=["SSA", "DIVA"])
+def test_gpu_energy_step_matches_the_oracle(oracle_cls, gpu_cls, shear):
+    want, state = seeded_energy_case(oracle_cls, shear)
+    got, _ = seeded_energy_case(gpu_cls, shear, state)
+    for k in want:
+        scale = max(1e-300, float(np.max(np.abs(want[k]))))
+        np.testing.assert_allclose(got[k], want[k], rtol=1e-10, atol=1e-10 * scale, err_msg=k)
