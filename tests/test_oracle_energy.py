@@ -26,7 +26,9 @@ with the velocity solve as well:
 The library against the oracle (gpu), SSA and DIVA: a 24 x 20 sheet over a sloping bed, Bounded in x and Periodic
 in y, 8 layers, the velocity state of the oracle's solve copied into the library, seeded enthalpy with cold,
 temperate and draining layers, wet and dry beds, thinning and thickening columns: two energy steps agree in E,
-T, ω, H_w, mᵍ, s_b, qᵍ and Φ to 1e-10 relative (FMA contraction on the GPU rounds apart by a few ulps)."""
+T, ω, H_w, mᵍ, s_b, qᵍ and Φ to 1e-10 relative (FMA contraction on the GPU rounds apart by a few ulps); at
+1024 x 1024 the columns of a uniform sheet at rest stay bitwise alike through three steps and match the
+oracle's single column (melt, drainage and a growing basal water layer)."""
 import math
 
 import numpy as np
@@ -429,3 +431,46 @@ def test_gpu_energy_step_matches_the_oracle(oracle_cls, gpu_cls, shear):
     for k in want:
         scale = max(1e-300, float(np.max(np.abs(want[k]))))
         np.testing.assert_allclose(got[k], want[k], rtol=1e-10, atol=1e-10 * scale, err_msg=k)
+
+
+def uniform_sheet(cls, N):
+    """An N x N periodic sheet at rest, every column alike: 1000 m of ice with a temperate base over a wet bed."""
+    g = M.RectilinearGrid(size=(N, N), x=(0.0, N * 1e3), y=(0.0, N * 1e3), topology=("Periodic", "Periodic"), halo=(4, 4))
+    Ns = 16
+    P = make(cls, g, Nsigma=Ns, rheology=M.GlenFlowLaw(rate_factor="sigma"), constants=M.IceSheetConstants(ice_density=RHO))
+    P.set("H", 1000.0)
+    P.set("bed", 0.0)
+    P.compute_geometry()
+    zeta = np.array([(a + b) / 2 for a, b in zip(M.sigma_faces(Ns)[:-1], M.sigma_faces(Ns)[1:])])
+    T = np.minimum(243.15 + 35 * (1 - zeta), 300.0)
+    w = np.where(zeta < 0.1, 0.02, 0.0)
+    E = enthalpy(T, w, RHO * GRAV * 1000.0 * (1 - zeta))
+    P.set("E", np.broadcast_to(E[:, None, None], (Ns, N, N)).copy())
+    for name, value in (("Hw", 0.005), ("geothermal_flux", 0.06), ("surface_temperature", 243.15),
+                        ("ocean_temperature", 271.15), ("H_previous", 1000.0)):
+        P.energy_set(name, value)
+    for _ in range(3):
+        P.step_enthalpy(1e9)
+    out = {k: P.get(k) for k in ("E", "T", "omega")}
+    out["Hw"] = P.energy_get("Hw")
+    out["grounded_melt"] = P.energy_get("grounded_melt")
+    P.close()
+    return out
+
+
+@pytest.mark.gpu
+def test_gpu_uniform_columns_stay_alike_at_1024(oracle_cls, gpu_cls):
+    """At rest every column of a uniform sheet takes the same three energy steps: at 1024 x 1024 the library's
+    columns agree bitwise with each other and with the oracle's single-column result to 1e-10."""
+    want = uniform_sheet(oracle_cls, 1)
+    got = uniform_sheet(gpu_cls, 1024)
+    for k, a in got.items():
+        first = a[..., :1, :1]
+        assert np.array_equal(a, np.broadcast_to(first, a.shape)), k
+        np.testing.assert_allclose(first, want[k], rtol=1e-10, atol=1e-10 * max(1e-300, float(np.max(np.abs(want[k])))), err_msg=k)
+
+
+def test_uniform_sheet_melts_and_drains(oracle_cls):
+    out = uniform_sheet(oracle_cls, 2)
+    assert np.all(out["Hw"] > 0.005) and np.all(out["grounded_melt"] > 0)
+    assert np.all(out["E"] == out["E"][:, :1, :1])
