@@ -19,17 +19,22 @@ walk the stream from its first request and wrap around after 512.  The warm-up s
             flushed.
   e2e       the same requests through the C ABI serving loop (nk_server_*) from host buffers, submitted at
             their Poisson arrival times.  Covers upload, geometry, solve and read-back of u and v; host wall
-            clock.  p50 and p99 latency run from arrival to result.
+            clock.  p50 and p99 latency run from arrival to result; a second pass over the first requests at 0.8x
+            the measured capacity gives the latency at a sustainable arrival rate.
   fp64      the plain FP64 solver one solve at a time, timed on one request of each size.  Its stream rate is
             the stream's size mix divided by those times.
   roofline  the fine-level FP32 l1-Jacobi sweep (the most frequent kernel) on a 2048x1024 grid with L2
             flushed before each launch, against the measured HBM copy bandwidth.  The FP64 CG operator is
             given with its FP64-pipe bound.
-  cpu_baseline  the FP64 CPU restatement of the reference solve (the oracle) on all host cores, timed on the
-            stream's smallest requests (a bounded sample).
+  published_scaling  the reference's published multigrid scaling benchmark (one SSA solve to 1e-8 at six grid
+            spacings, diagonal and multigrid PCG): iterations and GPU device time beside the published CPU and H200
+            times.
+  cpu_baseline  the FP64 CPU restatement of the reference solve (the oracle) on all host cores: one solve of the
+            first timed request of each grid size, weighted by the stream's size counts.  The same solves give
+            the mixed solver's relative L2 velocity error against the FP64 oracle for every grid size.
 
-`--impl reference` times that CPU restatement alone.  One step is one request from the stream's 128x64 and
-256x128 requests, in stream order.
+`--impl reference` times that CPU restatement alone, on the same stream and config: one FP64 solve per step, the
+grid sizes taken in turn, weighted by the stream's size counts.
 Multi-GPU: replicas only.  Each rank serves its own copy of the stream; there is no collective on the data
 path."""
 import argparse
@@ -70,7 +75,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="nunatak", choices=["nunatak", "reference"])
     ap.add_argument("--batch", type=int, default=32, help="requests per step, and solves in flight at once")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true",
+                    help="skip the oracle solves (CPU baseline and the mixed-vs-oracle errors of every grid size)")
+    ap.add_argument("--no-scaling", action="store_true", help="skip the reference's published scaling benchmark rows")
     ap.add_argument("--rate", type=float, default=ARRIVAL_RATE,
                     help="Poisson arrival rate of the e2e leg, requests/s (the workload's is 200)")
     ap.add_argument("--profile", choices=["solve", "smoother", "operator"], default=None,
@@ -195,14 +202,6 @@ def cpu_solve(case, threads):
     return dt, st, P.get("u"), P.get("v"), used
 
 
-def cpu_sample_requests(n):
-    """The first n requests of the stream with the two smallest grids, in stream order: the bounded CPU sample
-    (a 512x256 or 1024x512 FP64 solve takes minutes on the host cores)."""
-    from nunatak_gb300 import workloads
-    small = [r for r in workloads.serving_stream(n_requests=N_REQUESTS, rate=ARRIVAL_RATE) if r["size"][0] <= 256]
-    return [small[k % len(small)] for k in range(n)]
-
-
 def replica_throughput(requests, span_ms, world, device):
     """Whole-job solves/s of `world` replicas that each served `requests`: the slowest replica's span (max over
     ranks, one all-reduce of the timing only) divides the requests of all ranks.  Returns (value, span_ms)."""
@@ -214,8 +213,38 @@ def replica_throughput(requests, span_ms, world, device):
     return world * requests / (span_ms / 1e3), span_ms
 
 
+def stream_config(B, timed_reqs, world):
+    """The `config` of both arms' lines: the workload, its timed requests and their grid sizes."""
+    count = {}
+    for r in timed_reqs:
+        key = "%dx%d" % r["size"]
+        count[key] = count.get(key, 0) + 1
+    return {"workload": WORKLOAD.format(B=B), "requests": len(timed_reqs), "batch": B, "in_flight": B,
+            "grids": {k: count[k] for k in sorted(count, key=lambda k: int(k.split("x")[0]))},
+            "parallelism": f"replicas{world}",
+            "l2": "not flushed: inputs larger than L2 (up to 32 resident 1024x512 problems in flight)"}
+
+
+def stream_rate(count, seconds_per_solve):
+    """Solves/s of the stream's size mix: its requests over the sum of count x seconds per solve of each size."""
+    return sum(count.values()) / sum(count[k] * seconds_per_solve[k] for k in count)
+
+
+def size_rotation(timed_reqs, n):
+    """n requests of the timed stream with the grid sizes taken in turn (smallest first): the k-th step of the
+    reference arm solves the (k // 4)-th timed request of the (k % 4)-th size."""
+    by_size = {}
+    for r in timed_reqs:
+        by_size.setdefault(r["size"], []).append(r)
+    sizes = sorted(by_size)
+    return [by_size[sizes[k % len(sizes)]][(k // len(sizes)) % len(by_size[sizes[k % len(sizes)]])] for k in range(n)]
+
+
 def run_reference(args, rank):
-    """`--impl reference`: the reference's CPU path (restated as the FP64 oracle) on all host threads."""
+    """`--impl reference`: the reference's CPU path (restated as the FP64 oracle) on all host threads, on the same
+    stream, config and metric as the GPU arm.  Every step is one FP64 solve of a timed request, the grid sizes taken
+    in turn (128x64, 256x128, 512x256, 1024x512, 128x64, ...), so that every size is timed; the value is the stream's
+    size mix over those times (stream_rate).  Warm-up steps solve 128x64 requests."""
     if rank != 0:
         return
     sys.path.insert(0, ROOT)
@@ -223,25 +252,35 @@ def run_reference(args, rank):
     from nunatak_gb300 import workloads
     __graft_entry__.build()
     threads = os.cpu_count() or 1
-    reqs = cpu_sample_requests(args.warmup + args.steps)
+    warm_reqs, timed_reqs = stream_requests(N_REQUESTS, args.batch, args.steps, args.warmup, args.rate)
+    config = stream_config(args.batch, timed_reqs, dist_env()[1])
+    smallest = [r for r in timed_reqs if r["size"] == workloads.SERVING_SIZES[0]]
     used = threads
-    for r in reqs[:args.warmup]:
-        cpu_solve(workloads.serving_case(r, "fp64"), threads)
-    times = []
-    for r in reqs[args.warmup:]:
+    for k in range(args.warmup):
+        cpu_solve(workloads.serving_case(smallest[k % len(smallest)], "fp64"), threads)
+    times, per_size = [], {}
+    for r in size_rotation(timed_reqs, args.steps):
         dt, st, _, _, used = cpu_solve(workloads.serving_case(r, "fp64"), threads)
         times.append(dt)
-    total = sum(times)
-    value = args.steps / total
-    sizes = sorted({"%dx%d" % r["size"] for r in reqs[args.warmup:]})
-    sample = (f"{args.steps} FP64 solves (oracle restatement of the reference solve, multigrid PCG) of the stream's "
-              f"requests with grids {', '.join(sizes)}, in stream order; one request per step")
+        per_size.setdefault("%dx%d" % r["size"], []).append(dt)
+    mean_s = {k: statistics.mean(v) for k, v in per_size.items()}
+    count = {k: n for k, n in config["grids"].items() if k in mean_s}
+    value = stream_rate(count, mean_s)
+    one_thread = {}
+    if args.steps:
+        dt1, _, _, _, _ = cpu_solve(workloads.serving_case(smallest[0], "fp64"), 1)
+        one_thread = {"128x64_s_per_solve": dt1, "note": "one 128x64 request on one thread (untimed extra)"}
+    sample = (f"{args.steps} FP64 solves (oracle restatement of the reference solve, multigrid PCG) of the timed stream's "
+              f"requests, one per step, grid sizes in turn ({', '.join(sorted(per_size, key=lambda k: int(k.split('x')[0])))}); "
+              f"value = the stream's size mix over the mean time per size")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded marine ice sheets)",
-            "config": {"workload": WORKLOAD.format(B=1).replace(
-                "mixed precision (FP32 multigrid, FP64 outer CG / Picard)", "FP64 throughout"), "sample_grids": sizes},
-            "latency_ms": {"p50": 1e3 * statistics.median(times), "p99": 1e3 * max(times)},
+            "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / max(1, len(times)), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded marine ice sheets, no dataset)",
+            "config": config,
+            "seconds_per_solve": mean_s,
+            "latency_ms": {"p50": 1e3 * statistics.median(times), "p99": 1e3 * max(times),
+                           "note": "one solve at a time: latency is the solve time"},
+            "one_thread": one_thread,
             "cpu_baseline": {"value": value, "unit": "solves/s", "cores": used, "kind": "port", "sample": sample,
                              "calibration": ORACLE_CALIBRATION},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -513,7 +552,7 @@ def run_diva(nk, workloads, ctx):
         "coulomb_transition_speed_m_per_yr": transition}), flush=True)
 
 
-def run_scaling(nk, workloads, ctx, problem_cls=None, rows=None):
+def run_scaling(nk, workloads, ctx, problem_cls=None, rows=None, quiet=False):
     """The reference's published multigrid scaling benchmark (benchmarks/multigrid_scaling.jl; its table in
     docs/src/model/numerics.md:42-49, kept in tests/golden/reference_scaling.json): the MISMIP+-like ice stream
     at six spacings, five Picard iterations of multigrid PCG to 1e-6 from rest, then one SSA solve of the last
@@ -551,6 +590,8 @@ def run_scaling(nk, workloads, ctx, problem_cls=None, rows=None):
             entry[name] = {"iterations": st.linear_iterations_last, "device_ms": st.device_ms, "status": st.status}
             Q.close()
         out.append(entry)
+    if quiet:
+        return out
     print(json.dumps({
         "metric": "one SSA solve from zero to 1e-8 (reference multigrid scaling benchmark): CG iterations and device time",
         "config": {"workload": "MISMIP+-like ice stream of benchmarks/multigrid_scaling.jl (640 x 80 km, bed and thickness "
@@ -620,10 +661,11 @@ def main():
     warm_reqs, timed_reqs = stream_requests(N_REQUESTS, B, args.steps, args.warmup, args.rate)
     warm_cases = build_cases(warm_reqs, "mixed")
     cases = build_cases(timed_reqs, "mixed")
-    sizes = sorted({(c.grid.Nx, c.grid.Ny) for c in cases})
+    config = stream_config(B, timed_reqs, world)
+    count = config["grids"]
     first_of_size = {}
     for k, c in enumerate(cases):
-        first_of_size.setdefault((c.grid.Nx, c.grid.Ny), k)
+        first_of_size.setdefault("%dx%d" % (c.grid.Nx, c.grid.Ny), k)
 
     # ---- value: the timed requests with inputs staged in HBM, continuous batching of B in flight --------------
     pool = ResidentPool(nk, ctx)
@@ -655,20 +697,18 @@ def main():
 
     # ---- fp64: the plain FP64 solver one solve at a time, one request of each size ----------------------------
     fp64_ms, rel_err = {}, {}
-    for key, k in sorted(first_of_size.items()):
-        from nunatak_gb300 import workloads as W
-        P64 = W.serving_case(timed_reqs[k], "fp64").problem(nk.Problem, context=ctx)
+    for key, k in first_of_size.items():
+        P64 = workloads.serving_case(timed_reqs[k], "fp64").problem(nk.Problem, context=ctx)
         zu, zv = np.zeros(P64.shape("u")), np.zeros(P64.shape("v"))
         P64.picard_solve()                  # warm-up: graph capture
         P64.set("u", zu)
         P64.set("v", zv)
         st = P64.picard_solve()
-        fp64_ms["%dx%d" % key] = st.device_ms
+        fp64_ms[key] = st.device_ms
         um, vm = kept[k]
-        rel_err["%dx%d" % key] = rel_l2(um, vm, P64.get("u"), P64.get("v"))
+        rel_err[key] = rel_l2(um, vm, P64.get("u"), P64.get("v"))
         P64.close()
-    count = {"%dx%d" % key: sum(1 for c in cases if (c.grid.Nx, c.grid.Ny) == key) for key in sizes}
-    fp64_value = len(cases) / (sum(count[k] * fp64_ms[k] for k in count) / 1e3)
+    fp64_value = stream_rate(count, {k: fp64_ms[k] / 1e3 for k in count})
 
     # ---- e2e: the same requests through the serving loop of the C ABI, host buffers, Poisson arrivals ---------
     from nunatak_gb300.server import Server
@@ -678,6 +718,12 @@ def main():
     S.wait_all()
     arrivals = arrival_times(timed_reqs, args.rate)
     e2e_value, e2e_lat, e2e_stats = run_server(S, cases, arrivals)
+    # the same server at a sustainable arrival rate (0.8 x the capacity just measured) on the first requests, so that
+    # the latency describes the server and not the queue of an overloaded stream
+    sus_rate = 0.8 * e2e_value
+    n_sus = min(len(cases), max(B, int(round(10.0 * sus_rate))))
+    sus_arrivals = arrival_times(timed_reqs[:n_sus], sus_rate)
+    _, sus_lat, _ = run_server(S, cases[:n_sus], sus_arrivals)
     sinfo = S.info()
     S.close()
     h2d = sum(sum(np.asarray(v).nbytes for v in c.fields.values()) for c in cases) / args.steps
@@ -690,10 +736,8 @@ def main():
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": span_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (multigrid) + f64 (CG, Picard)", "data": "synthetic (seeded marine ice sheets, no dataset)",
-        "config": {"workload": WORKLOAD.format(B=B), "requests": len(cases), "batch": B, "in_flight": B,
-                   "grids": {k: count[k] for k in count}, "parallelism": f"replicas{world}",
-                   "l2": "not flushed: inputs larger than L2 (up to 32 resident 1024x512 problems in flight)",
-                   "wall_s": wall, "problems_created_in_timed_region": created_timed},
+        "config": config,
+        "timing": {"wall_s": wall, "problems_created_in_timed_region": created_timed},
         "latency_ms": {"p50": statistics.median(service), "p99": float(np.percentile(service, 99)),
                        "note": "device time of each solve (start to end event) while sharing the GPU with the others"},
         "picard_iterations": {"min": min(piters), "max": max(piters)},
@@ -707,7 +751,12 @@ def main():
         "roofline": None,
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "latency_ms": {"p50": statistics.median(e2e_lat), "p99": float(np.percentile(e2e_lat, 99)),
-                               "note": f"arrival (Poisson, {args.rate:g}/s) to result on the host"},
+                               "note": f"arrival (Poisson, {args.rate:g}/s) to result on the host; arrivals exceed capacity, "
+                                       "so this is mostly queueing"},
+                "latency_ms_sustainable": {"rate_per_s": sus_rate, "requests": n_sus,
+                                           "p50": statistics.median(sus_lat), "p99": float(np.percentile(sus_lat, 99)),
+                                           "note": "the first requests of the stream at Poisson arrivals of 0.8 x the "
+                                                   "measured e2e capacity, arrival to result on the host"},
                 "path": "nk_server_submit / nk_server_wait (host inputs, upload, geometry, solve, read-back)",
                 "picard_iteration_mismatch_vs_resident": e2e_err, "server": sinfo},
         "clocks": clocks.summary(),
@@ -742,21 +791,23 @@ def main():
         "model": "per request and cell: Picard iterations x %d B (SSA coefficient update, 15 words FP64) + CG iterations x "
                  "(%d B FP64 flexible CG iteration + %d B FP32 V-cycle, 62 words x 4/3 levels)"
                  % (COEF_BYTES_PER_CELL, CG_BYTES_PER_CELL, VCYCLE_BYTES_PER_CELL)}
+    # ---- the reference's published scaling benchmark: GPU device times beside the published H200 and CPU times ----
+    if not args.no_scaling:
+        line["published_scaling"] = run_scaling(nk, workloads, ctx, quiet=True)
+    # ---- the FP64 CPU restatement (the oracle): one solve of each size, the parity of the mixed solves against it and
+    # the CPU baseline of the stream's size mix -----------------------------------------------------------------------
     if not args.no_cpu_baseline:
-        from nunatak_gb300 import workloads as W
-        reqs = cpu_sample_requests(2)
-        total, used, errs = 0.0, 1, {}
-        for r in reqs:
-            dt, st, uo, vo, used = cpu_solve(W.serving_case(r, "fp64"), os.cpu_count() or 1)
-            total += dt
-            for k, tr in enumerate(timed_reqs):
-                if tr["index"] == r["index"] and k in kept:
-                    errs[str(r["index"])] = rel_l2(kept[k][0], kept[k][1], uo, vo)
-        line["cpu_baseline"] = {"value": len(reqs) / total, "unit": "solves/s", "cores": used, "kind": "port",
-                                "calibration": ORACLE_CALIBRATION,
-                                "sample": "FP64 solves of the stream's first 128x64 and first 256x128 requests "
-                                          "(oracle restatement, multigrid PCG, OpenMP on all host cores)"}
-        line["rel_error_mixed_vs_fp64_oracle"] = errs
+        cpu_s, errs, used = {}, {}, 1
+        for key, k in first_of_size.items():
+            dt, _, uo, vo, used = cpu_solve(workloads.serving_case(timed_reqs[k], "fp64"), os.cpu_count() or 1)
+            cpu_s[key] = dt
+            errs[key] = rel_l2(kept[k][0], kept[k][1], uo, vo)
+        line["cpu_baseline"] = {"value": stream_rate(count, cpu_s), "unit": "solves/s", "cores": used, "kind": "port",
+                                "calibration": ORACLE_CALIBRATION, "seconds_per_solve": cpu_s,
+                                "sample": "one FP64 solve (oracle restatement, multigrid PCG, OpenMP on all host cores) of the "
+                                          "first timed request of each grid size; value = the stream's size mix over those times"}
+        line["rel_error_mixed_vs_fp64_oracle"] = {key: errs[key] for key in errs}
+        line["rel_error_mixed_vs_fp64_oracle_requests"] = {key: int(timed_reqs[k]["index"]) for key, k in first_of_size.items()}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.barrier()

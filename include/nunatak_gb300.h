@@ -151,7 +151,16 @@ typedef struct nk_solver_desc {
     int32_t minimum_coarse_size;      /* default 2 */
     nk_iteration_control linear;      /* default Convergence(reltol = 1e-8, maxiter = 10_000) */
     nk_iteration_control picard;      /* default Convergence(reltol = 1e-6, maxiter = 100) */
+    int32_t flags;                    /* NK_SOLVER_* bits, 0 by default */
+    int32_t reserved;                 /* 0 */
 } nk_solver_desc;
+
+/* Issue the solve's kernels one by one from a host loop (conjugate-gradient steps in batches, the device stopping
+ * flag read after each batch; Picard reads its decision after every iteration) instead of replaying one CUDA graph
+ * with conditional WHILE nodes.  Same kernels, same arithmetic, same results; slower, and refused by
+ * nk_picard_solve_async.  Kernels inside conditional graph nodes are invisible to kernel profilers; this path shows
+ * every launch.  The NK_GRAPHS=0 environment variable sets it for every problem of the process. */
+#define NK_SOLVER_HOST_LOOP 1
 
 /* Field identifiers for nk_problem_set_field / nk_problem_get_field (the reference's names). */
 #define NK_FIELD_U              0   /* model.velocities.u                   Face-Center */
@@ -421,7 +430,7 @@ nk_status nk_multigrid_prolongate(nk_problem* problem, int32_t level, const doub
  * No counterpart in the reference.  For callers that cannot let the library allocate device memory while
  * they run: a model whose host framework pools the whole device (a CUDA.jl or PyTorch caching allocator),
  * where an extra cudaMalloc fails and a cudaFree stalls the device, or a coupled time loop that must not
- * synchronise.  Computes the Picard change measure of picard_solve! (src/Solvers/picard.jl:83-86)
+ * synchronise.  Computes the two Euclidean norms that a velocity-change stopping test compares,
  *   change_and_norm[0] = ||(u, v) - (u_prev, v_prev)||,   change_and_norm[1] = ||(u, v)||
  * over the cells of the grid (u at the west and v at the south face of each cell), with the same reduction
  * and summation order as the picard_change and picard_norm of nk_picard_solve.  u, v, u_prev, v_prev and

@@ -568,15 +568,15 @@ static int fused_level(const std::vector<Level<T>>& lv, int nlevels) {
     return nlevels + 1;
 }
 
-// CUDA graphs are the solve path.  NK_GRAPHS=0 issues the same kernel sequence from a host loop (steps in
-// batches, one read of the device stopping flag per batch): profilers cannot see inside graphs with
-// conditional nodes.
-static bool use_graphs() {
+// CUDA graphs are the solve path.  NK_SOLVER_HOST_LOOP in the solver flags (or NK_GRAPHS=0 for the whole
+// process) issues the same kernel sequence from a host loop (steps in batches, one read of the device stopping
+// flag per batch): profilers cannot see inside graphs with conditional nodes.
+static bool use_graphs(const nk_problem* P) {
     static bool on = [] {
         const char* e = std::getenv("NK_GRAPHS");
         return !(e && e[0] == '0');
     }();
-    return on;
+    return on && !(P->sd.flags & NK_SOLVER_HOST_LOOP);
 }
 
 // Buffer that receives the first of `sweeps` point sweeps started from zero, so that the last lands in L.x.
@@ -971,7 +971,7 @@ static void impose_prescribed(nk_problem* P, const double2* val) {
 // solve!(x, solver, b, ...) with b already on the device in tmp_b
 static void linear_solve(nk_problem* P, nk_solve_stats* st) {
     impose_prescribed(P, P->tmp_b);   // an identity row's solution is its right-hand side
-    if (!use_graphs()) {
+    if (!use_graphs(P)) {
         set_control(P);
         host_cg(P, P->tmp_b);
         read_scalars(P);
@@ -989,7 +989,7 @@ static void linear_solve(nk_problem* P, nk_solve_stats* st) {
 // picard_solve!, picard.jl:63-90
 static void picard_solve(nk_problem* P, nk_solve_stats* st) {
     impose_prescribed(P, P->ud);
-    if (!use_graphs()) {
+    if (!use_graphs(P)) {
         set_control(P);
         host_picard(P);
         read_scalars(P);
@@ -1310,6 +1310,7 @@ static nk_status problem_create(nk_context* ctx, const nk_grid_desc* grid, const
         if (solver->picard.kind < NK_CONVERGENCE || solver->picard.kind > NK_VISCOSITY_CONVERGENCE) bad("unknown Picard iteration control");
         if (solver->precision == NK_PRECISION_MIXED && solver->preconditioner != NK_PRECONDITIONER_MULTIGRID)
             bad("mixed precision needs the multigrid preconditioner");
+        if (solver->flags & ~NK_SOLVER_HOST_LOOP) bad("unknown solver flags");
         P->ctx = ctx;
         P->gd = *grid;             // build() reads the caller's face vectors during this call only
         P->pd = *physics;
@@ -1852,7 +1853,7 @@ nk_status nk_picard_solve(nk_problem* P, nk_solve_stats* stats) {
 nk_status nk_picard_solve_async(nk_problem* P) {
     if (!P) return NK_BAD_ARGUMENT;
     return guarded(P->ctx, [&] {
-        if (!use_graphs()) bad("asynchronous solves need CUDA graphs (NK_GRAPHS=0 is set)");
+        if (!use_graphs(P)) bad("asynchronous solves need CUDA graphs (NK_SOLVER_HOST_LOOP or NK_GRAPHS=0 is set)");
         if (!P->picard_exec) build_picard_graph(P);
         set_control(P);
         NK_CUDA(cudaEventRecord(P->ev0, P->stream));
@@ -2259,7 +2260,7 @@ static Resident* acquire(nk_server* S, ServerRequest& R) {
     r->pin_count = 4 * cells + 4 * faces;
     NK_CUDA(cudaEventCreateWithFlags(&r->done, cudaEventDisableTiming));
     double tg0 = S->now();
-    if (use_graphs()) build_picard_graph(P);
+    if (use_graphs(P)) build_picard_graph(P);
     S->t_graph += S->now() - tg0;
     if (const char* e = std::getenv("NK_SERVER_TRACE"))
         if (e[0] == '1')
@@ -2304,7 +2305,7 @@ static void start(nk_server* S, ServerRequest& R, Resident& r) {
     gv.ud = P->ud;
     launch_geometry(gv, s);
     set_control(P);
-    if (use_graphs()) {
+    if (use_graphs(P)) {
         NK_CUDA(cudaGraphLaunch(P->picard_exec, s));
     } else {
         host_picard(P);
@@ -2336,7 +2337,7 @@ static void finish(nk_server* S, Resident& r) {
     if (R.v_out) std::memcpy(R.v_out, uout + nu, nv * sizeof(double));
     fill_stats_from(*r.sc_out, &R.stats, true);
     const SolverScalars& h = *r.sc_out;
-    if (use_graphs())
+    if (use_graphs(P))
         count_launches(P->picard_kernels[0] + (long long)h.p_it * P->picard_kernels[1] + (long long)h.it_total * P->picard_kernels[2]);
     R.status = R.stats.status == NK_NONFINITE ? NK_NONFINITE : NK_OK;
     R.state = 2;

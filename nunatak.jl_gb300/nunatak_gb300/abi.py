@@ -103,7 +103,10 @@ class PhysicsDesc(C.Structure):
 class SolverDesc(C.Structure):
     _fields_ = [("precision", C.c_int32), ("preconditioner", C.c_int32), ("smoother", C.c_int32),
                 ("smoothing_sweeps", C.c_int32), ("coarsest_sweeps", C.c_int32), ("minimum_coarse_size", C.c_int32),
-                ("linear", IterationControl), ("picard", IterationControl)]
+                ("linear", IterationControl), ("picard", IterationControl), ("flags", C.c_int32), ("reserved", C.c_int32)]
+
+
+NK_SOLVER_HOST_LOOP = 1
 
 
 class SolveStats(C.Structure):

@@ -209,6 +209,7 @@ class StressBalanceSolver:
     preconditioner: object = field(default_factory=StressBalanceDiagonalPreconditioner)   # None = no preconditioner
     precision: str = "fp64"             # "fp64" or "mixed" (FP32 multigrid under FP64 outer iterations)
     adjoint_iteration_control: object = None   # stops the fixed-point adjoint; None = picard_iteration_control
+    host_loop: bool = False             # issue the kernels from a host loop instead of one CUDA graph (NK_SOLVER_HOST_LOOP)
 
     @property
     def adjoint_control(self):
@@ -316,6 +317,7 @@ def make_descriptors(grid: RectilinearGrid, Nsigma=10, bed_refinement=2.0, sigma
         s.smoother, s.smoothing_sweeps, s.coarsest_sweeps, s.minimum_coarse_size = 0, 2, 20, 2
     s.linear = velocity_solver.linear_iteration_control.desc()
     s.picard = velocity_solver.picard_iteration_control.desc()
+    s.flags = abi.NK_SOLVER_HOST_LOOP if velocity_solver.host_loop else 0
     return Descriptors(g, p, s, keep, velocity_solver.adjoint_control)
 
 

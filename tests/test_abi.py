@@ -45,7 +45,7 @@ def test_descriptor_struct_sizes_match_header():
     from nunatak_gb300 import abi
     assert ctypes.sizeof(abi.IterationControl) == 32
     assert ctypes.sizeof(abi.GridDesc) == 32 + 8 * 2 + 8 * 4 + 8 + 8
-    assert ctypes.sizeof(abi.SolverDesc) == 24 + 2 * 32
+    assert ctypes.sizeof(abi.SolverDesc) == 24 + 2 * 32 + 8
 
 
 def header_defines():
