@@ -3,7 +3,7 @@ centred finite differences, following the checks of test/test_enzyme.jl:221-381.
 
 J = ½ Σ (u - u_obs)² + (v - v_obs)² over the velocity points of a marine sheet, with u_obs from a solve with
 another friction seed.  The gradients from the adjoint must match centred differences of converged solves
-(Picard 1e-12, CG 1e-13):
+(Picard 1e-14, CG 1e-15):
 - ∂J/∂log C at seeded grounded cells, (J(C e^ε) - J(C e^-ε)) / 2ε, on the GPU forward solve for three
   configurations (bounded / periodic x, free-slip / no-slip walls, Weertman / regularised Coulomb friction);
 - ∂J/∂log A along seeded random directions d over the whole field, (J(A e^(εd)) - J(A e^(-εd))) / 2ε against
@@ -12,8 +12,10 @@ another friction seed.  The gradients from the adjoint must match centred differ
 - on the oracle's forward solve at one cell;
 - for DIVA (Arrhenius σ-grid rate factor, regularised Coulomb friction), whose step also carries its lagged
   βᵇ, F₂ and ησ: log C and log A along random directions on the GPU forward map, log C on the oracle's.
-Tolerance: 1e-4 relative to the largest gradient entry (per cell) or to Σ|gᵢdᵢ| (directions).  The step ε is 1e-3
-(1e-4 for log A, whose second derivative along d is large against the misfit of these cases)."""
+Tolerance: 1e-4 relative to the cell's own gradient (per cell, at cells whose gradient is at least 1e-3 of the
+largest entry) or to Σ|gᵢdᵢ| (directions).  The step ε is 1e-3 (1e-4 for log A, whose second derivative along d is
+large against the misfit of these cases).  A per-cell difference is taken as ½ Σ (x₊ - x₋)(x₊ + x₋ - 2 x_obs) from
+the two perturbed solves, not as the difference of two costs."""
 import math
 
 import numpy as np
@@ -29,8 +31,10 @@ RTOL = 1e-4
 
 
 def _solver():
-    return M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-13, maxiter=20_000),
-                                 picard_iteration_control=M.Convergence(reltol=1e-12, maxiter=500),
+    """Converged to Picard 1e-14 and CG 1e-15 (at most 5000 CG iterations per solve): a per-cell difference resolves
+    1e-4 of a cell's gradient only when the perturbed solves leave less noise than that."""
+    return M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-15, maxiter=5000),
+                                 picard_iteration_control=M.Convergence(reltol=1e-14, maxiter=2000),
                                  preconditioner=M.StressBalanceDiagonalPreconditioner())
 
 
@@ -51,10 +55,17 @@ def _cost(P, uo, vo):
     return 0.5 * (np.sum((u - uo) ** 2) + np.sum((v - vo) ** 2)), u - uo, v - vo
 
 
+def _cost_difference(plus, minus, uo, vo):
+    """J(+) - J(-) as ½ Σ (x₊ - x₋)(x₊ + x₋ - 2 x_obs), without forming either cost: subtracting two rounded sums
+    of the whole field would bury the small differences of weakly sensitive cells."""
+    (up, vp), (um, vm) = plus, minus
+    return 0.5 * (float(np.sum((up - um) * (up + um - 2 * uo))) + float(np.sum((vp - vm) * (vp + vm - 2 * vo))))
+
+
 def _fd(P, case, cell, xs, uo, vo, name="C"):
     """Centred difference of J in log `name` at `cell` (an index of that field) from converged solves warm-started
     at x*."""
-    J = []
+    vel = []
     for s in (1.0, -1.0):
         p = case.fields[name].copy()
         p[cell] *= math.exp(s * EPS)
@@ -62,16 +73,17 @@ def _fd(P, case, cell, xs, uo, vo, name="C"):
         P.set("u", xs[0])
         P.set("v", xs[1])
         P.picard_solve()
-        J.append(_cost(P, uo, vo)[0])
+        vel.append((P.get("u"), P.get("v")))
     P.set(name, case.fields[name])
-    return (J[0] - J[1]) / (2 * EPS)
+    return _cost_difference(vel[0], vel[1], uo, vo) / (2 * EPS)
 
 
-def _cells(P, n, seed):
-    phi, H = P.get("phi"), P.get("H")
-    cand = np.argwhere((phi > 0.5) & (H > 200.0))
+def _cells(grad, n, seed, floor=1e-3):
+    """n seeded cells among those whose gradient is at least `floor` of the largest entry: each is checked against
+    its own value, and a centred difference cannot resolve cells far below that."""
+    cand = np.argwhere(np.abs(grad) >= floor * np.max(np.abs(grad)))
     rng = np.random.default_rng(seed)
-    return [tuple(cand[k]) for k in rng.choice(len(cand), size=n, replace=False)]
+    return [tuple(cand[k]) for k in rng.choice(len(cand), size=min(n, len(cand)), replace=False)]
 
 
 def _adjoint(cls, kind):
@@ -94,9 +106,9 @@ def test_picard_adjoint_matches_finite_differences(gpu_cls, kind):
     assert np.array_equal(P.get("u"), xs[0])              # the forward state is left at x*
     scale, scale_a = np.max(np.abs(grad)), np.max(np.abs(grad_a))
     assert scale > 0 and scale_a > 0
-    for cell in _cells(P, 4, 7):
+    for cell in _cells(grad, 6, 7):
         fd = _fd(P, case, cell, xs, uo, vo)
-        assert abs(fd - grad[cell]) <= RTOL * scale, (kind, cell, fd, grad[cell], scale)
+        assert abs(fd - grad[cell]) <= RTOL * abs(grad[cell]), (kind, cell, fd, grad[cell], scale)
     A0 = P.get("A")
     d = np.random.default_rng(31).standard_normal(A0.shape)
     fd = _directional_fd(P, "A", A0, d, xs, uo, vo, eps=1e-6)
@@ -141,9 +153,9 @@ def test_picard_adjoint_matches_oracle_finite_difference(gpu_cls, oracle_cls):
     O = case.problem(oracle_cls)
     O.picard_solve()
     xs = (O.get("u"), O.get("v"))
-    cell = _cells(P, 1, 11)[0]
-    fd = _fd(O, case, cell, xs, uo, vo)
-    assert abs(fd - grad[cell]) <= RTOL * np.max(np.abs(grad)), (cell, fd, grad[cell])
+    for cell in _cells(grad, 2, 11):
+        fd = _fd(O, case, cell, xs, uo, vo)
+        assert abs(fd - grad[cell]) <= RTOL * abs(grad[cell]), (cell, fd, grad[cell])
 
 
 def _diva(friction, obs=False):

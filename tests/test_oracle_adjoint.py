@@ -4,9 +4,10 @@ the oracle's.
 
 J = ½ Σ (u - u_obs)² + (v - v_obs)² on the 40 x 20 marine sheet with u_obs from a solve with another friction
 seed (the cases of tests/test_gpu_adjoint.py: bounded with free-slip walls and Weertman drag, periodic in x, and
-no-slip walls with regularised Coulomb drag), converged solves (Picard 1e-12, CG 1e-13):
-- ∂J/∂log C at seeded grounded cells against (J(C e^ε) - J(C e^-ε)) / 2ε, ε = 1e-3, within 1e-4 of the largest
-  gradient entry;
+no-slip walls with regularised Coulomb drag), converged solves (Picard 1e-14, CG 1e-15):
+- ∂J/∂log C against (J(C e^ε) - J(C e^-ε)) / 2ε, ε = 1e-3, within 1e-4 of the cell's own gradient, at seeded cells
+  whose gradient is at least 1e-3 of the largest entry and at the largest-gradient cells of the rows beside the
+  south and north walls (J(+) - J(-) formed from the two solves' velocities, not as a difference of two costs);
 - ∂J/∂log A along a seeded random direction d against the Richardson extrapolation of centred differences with
   ε = 4e-5 and 2e-5, within 1e-4 of Σ|gᵢdᵢ| (the third derivative along d is large for the Coulomb case: a plain
   centred difference with ε = 1e-4 is 0.8 % off, and its error falls as ε²);
@@ -27,8 +28,11 @@ KINDS = ["bounded", "periodic_x", "no_slip_coulomb"]
 
 
 def _solver():
-    return M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-13, maxiter=20_000),
-                                 picard_iteration_control=M.Convergence(reltol=1e-12, maxiter=500),
+    """Converged to Picard 1e-14 and CG 1e-15: the per-cell differences below resolve 1e-6 of a cell's gradient only
+    when the perturbed solves leave no more than that (at 1e-12 / 1e-13 a cell at 1 % of the largest gradient
+    carried 2e-4 of solver noise, growing as 1/ε)."""
+    return M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-15, maxiter=20_000),
+                                 picard_iteration_control=M.Convergence(reltol=1e-14, maxiter=2000),
                                  preconditioner=M.StressBalanceDiagonalPreconditioner())
 
 
@@ -57,16 +61,33 @@ def _cost(P, uo, vo):
 
 
 def _centred(P, name, factor_plus, factor_minus, xs, uo, vo, eps):
+    """(J(p f₊) - J(p f₋)) / 2ε from converged solves warm-started at x*, with J(+) - J(-) formed as
+    ½ Σ (x₊ - x₋)(x₊ + x₋ - 2 x_obs): subtracting two rounded costs would bury weakly sensitive cells."""
     p0 = P.get(name)
-    J = []
+    vel = []
     for factor in (factor_plus, factor_minus):
         P.set(name, p0 * factor)
         P.set("u", xs[0])
         P.set("v", xs[1])
         P.picard_solve()
-        J.append(_cost(P, uo, vo))
+        vel.append((P.get("u"), P.get("v")))
     P.set(name, p0)
-    return (J[0] - J[1]) / (2 * eps)
+    (up, vp), (um, vm) = vel
+    dJ = 0.5 * (float(np.sum((up - um) * (up + um - 2 * uo))) + float(np.sum((vp - vm) * (vp + vm - 2 * vo))))
+    return dJ / (2 * eps)
+
+
+def _check_cells(grad, ny):
+    """Seeded cells whose gradient is at least 1e-3 of the largest, plus the largest-gradient cell of the first and
+    the last row (next to the south and north walls)."""
+    floor = 1e-3 * np.max(np.abs(grad))
+    cand = np.argwhere(np.abs(grad) >= floor)
+    cells = [tuple(cand[k]) for k in np.random.default_rng(7).choice(len(cand), size=min(3, len(cand)), replace=False)]
+    for j in (0, ny - 1):
+        i = int(np.argmax(np.abs(grad[j])))
+        if abs(grad[j, i]) >= floor:
+            cells.append((j, i))
+    return cells
 
 
 @pytest.mark.parametrize("kind", KINDS)
@@ -78,14 +99,11 @@ def test_oracle_adjoint_matches_finite_differences(oracle_cls, kind):
     assert np.array_equal(P.get("u"), xs[0])          # the forward state is left at x*
     scale = np.max(np.abs(grad))
     assert scale > 0
-    phi, H = P.get("phi"), P.get("H")
-    cand = np.argwhere((phi > 0.5) & (H > 200.0))
-    for k in np.random.default_rng(7).choice(len(cand), size=3, replace=False):
-        cell = tuple(cand[k])
+    for cell in _check_cells(grad, grad.shape[0]):
         e = np.ones_like(grad)
         e[cell] = math.exp(1e-3)
         fd = _centred(P, "C", e, 1 / e, xs, uo, vo, 1e-3)
-        assert abs(fd - grad[cell]) <= 1e-4 * scale, (kind, cell, fd, grad[cell], scale)
+        assert abs(fd - grad[cell]) <= 1e-4 * abs(grad[cell]), (kind, cell, fd, grad[cell], scale)
     d = np.random.default_rng(3).standard_normal(grad_a.shape)
     eps = 4e-5
     fd1 = _centred(P, "A", np.exp(eps * d), np.exp(-eps * d), xs, uo, vo, eps)
