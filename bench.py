@@ -90,6 +90,8 @@ def parse():
     ap.add_argument("--diva", action="store_true",
                     help="the DIVA workload instead: one solve of the 2048x1024 DIVA sheet (Nσ = 10, Arrhenius A, "
                          "regularised Coulomb drag) in mixed precision and in FP64, from rest")
+    ap.add_argument("--timestep", action="store_true",
+                    help="the time-step kernels (thickness stage, WENO limiter, energy step) at 2048x1024 against HBM")
     ap.add_argument("--scaling", action="store_true",
                     help="the reference's published multigrid scaling benchmark instead: iterations and device time of "
                          "one SSA solve to 1e-8 at six grid spacings, beside the published numbers")
@@ -622,6 +624,35 @@ def run_scaling(nk, workloads, ctx, problem_cls=None, rows=None, quiet=False):
     return out
 
 
+def timestep_kernels(nk, workloads, ctx, peak):
+    """The time-step kernels on the 2048x1024 DIVA sheet (Nσ = 10, the workload's geometry, temperature and drag) after
+    a short solve and its velocity profile, L2 flushed before each launch: one Runge-Kutta stage of the thickness step
+    with first-order upwinding and with the default bounded WENO-5, the bounded WENO's limiter, and the column energy
+    step from the enthalpy of the seeded temperature.  Algorithmic bytes per launch over CUDA-event time against the
+    measured HBM bandwidth."""
+    from nunatak_gb300 import model as M
+    solver = M.StressBalanceSolver(linear_iteration_control=M.FixedIterations(5), picard_iteration_control=M.FixedIterations(2),
+                                   preconditioner=M.StressBalanceMultigridPreconditioner(minimum_coarse_size=32), precision="mixed")
+    case = workloads.diva_sheet(2048, 1024, velocity_solver=solver)
+    P = case.problem(nk.Problem, context=ctx)
+    P.picard_solve()
+    P.velocity_profile()
+    P.set("E", 2009.0 * (case.temperature - 223.15))
+    out = {}
+    for name, kernel, adv in (("thickness_stage_upwind1", "thickness_stage", M.UpwindBiased(order=1)),
+                              ("thickness_stage_weno5_bounded", "thickness_stage", M.default_thickness_advection()),
+                              ("thickness_limiter", "thickness_limiter", M.default_thickness_advection()),
+                              ("step_enthalpy", "step_enthalpy", None)):
+        if adv is not None:
+            P.set_thickness_advection(adv)
+        P.time_kernel(kernel, repeats=2, flush_bytes=0)
+        ms, by = P.time_kernel(kernel, repeats=10, flush_bytes=512 << 20)
+        gbs = by / (ms * 1e-3) / 1e9
+        out[name] = {"ms_per_launch": ms, "bytes_per_launch": by, "achieved_gbs": gbs, "frac_of_hbm": gbs / peak}
+    P.close()
+    return {"grid": "2048x1024, Nsigma = 10 (DIVA sheet), L2 flushed before each launch", "kernels": out}
+
+
 # Algorithmic bytes per cell of the solve's repeated work (each array a kernel touches, once, at its precision):
 # the FP64 flexible CG iteration (operator 65 B, update 104 B, dots after the V-cycle 32 B, xpby 48 B), the FP32
 # V-cycle (about 62 four-byte words per fine cell, times 4/3 for the coarse levels) and the SSA coefficient update
@@ -670,6 +701,10 @@ def main():
     if args.scaling:
         if rank == 0:
             run_scaling(nk, workloads, ctx)
+        return
+    if args.timestep:
+        if rank == 0:
+            print(json.dumps({"metric": "time-step kernels vs HBM", **timestep_kernels(nk, workloads, ctx, measured_peaks()[0])}), flush=True)
         return
 
     def barrier():
@@ -811,6 +846,7 @@ def main():
         "model": "per request and cell: Picard iterations x %d B (SSA coefficient update, 15 words FP64) + CG iterations x "
                  "(%d B FP64 flexible CG iteration + %d B FP32 V-cycle, 62 words x 4/3 levels)"
                  % (COEF_BYTES_PER_CELL, CG_BYTES_PER_CELL, VCYCLE_BYTES_PER_CELL)}
+    line["roofline_timestep"] = timestep_kernels(nk, workloads, ctx, peak)
     # ---- the reference's published scaling benchmark: GPU device times beside the published H200 and CPU times ----
     if not args.no_scaling:
         line["published_scaling"] = run_scaling(nk, workloads, ctx, quiet=True)

@@ -317,14 +317,41 @@ typedef struct nk_thermal_params {
 nk_status nk_compute_thermal_diagnostics(nk_problem* problem, const nk_thermal_params* params);
 
 /* One ice time step of the thickness with the velocities held (replaces the three rk_substep! calls of
- * time_step!, src/Models/time_stepping.jl:15-72, with UpwindBiased(order = 1) advection and no PartialCellFront):
- * Delta tau = dt/3, dt/2, dt; each stage sets H = max(0, H_start + Delta tau G(H)) with
+ * time_step!, src/Models/time_stepping.jl:15-72, with the problem's advection scheme, nk_set_thickness_advection,
+ * and no PartialCellFront): Delta tau = dt/3, dt/2, dt; each stage sets H = max(0, H_start + Delta tau G(H)) with
  * G = a - (1 - phi) m - m^g - div(u H) (phi only with a grounding-line treatment, m^g only when
- * grounded_melt_coupling is non-zero), the upwind flux through each face and none through a Bounded wall; the
+ * grounded_melt_coupling is non-zero), u H through each face with the scheme's upwind-biased face thickness (the
+ * bounds-preserving limiter recomputed from the stage's thickness first) and nothing through a Bounded wall; the
  * last stage adds its clip max(0, -H*) to NK_FIELD_CLIPPED_THICKNESS; nk_compute_geometry runs after every
  * stage (update_state! without the velocity solve), so the surface, masks, grounded fractions, effective
  * pressure and driving stress follow the new thickness.  NK_BAD_ARGUMENT when dt is not finite and positive. */
 nk_status nk_step_thickness(nk_problem* problem, double dt, int32_t grounded_melt_coupling);
+
+/* The thickness advection scheme of nk_step_thickness, IceSheetModel's `advection` keyword
+ * (src/Models/ice_sheet_model.jl:79-123):
+ *   NK_ADVECTION_UPWIND, order 1 or 3   UpwindBiased(order = 1) / UpwindBiased(order = 3)
+ *   NK_ADVECTION_WENO, order 5          WENO(order = 5), and with bounded = 1 WENO(order = 5, bounds = (lower, upper)),
+ *                                       whose bounds-preserving limiter is recomputed before every tendency
+ *                                       (update_bounds_preserving_limiter!, src/Models/time_stepping.jl:35-42).
+ * A new problem starts with the reference's default for the SSA and the DIVA, WENO(order = 5, bounds = (0, 1e5))
+ * (default_thickness_advection, src/Models/ice_sheet_model.jl:123).  The face value through which u H passes is the
+ * upwind-biased reconstruction of H: order 1 the upwind cell; order 3 (-H₋₁ + 5 H₀ + 2 H₁) / 6; WENO-5 the
+ * Jiang-Shu smoothness indicators with the WENO-Z weights (Borges et al. 2008, exponent 1, ε = 1e-8) of the three third-order
+ * candidates; H₀ the upwind cell, H₋₁ the one behind it, H₁ the downwind one.  The limiter (Zhang and Shu 2010) scales
+ * each cell's face values towards its mean so that they and the cell's interior quadrature value stay in
+ * [lower, upper] (weights 5/18 at the faces, per direction).  NK_BAD_ARGUMENT for other schemes or orders, for
+ * lower >= upper, and (at nk_step_thickness) for a bounded WENO on a grid whose smaller horizontal halo is below 4,
+ * which the reference refuses (check_advection_halo, src/Models/ice_sheet_model.jl:131-135). */
+#define NK_ADVECTION_UPWIND 0
+#define NK_ADVECTION_WENO   1
+typedef struct nk_advection_desc {
+    int32_t scheme;                   /* NK_ADVECTION_UPWIND / NK_ADVECTION_WENO */
+    int32_t order;                    /* 1 or 3 (upwind), 5 (WENO) */
+    int32_t bounded;                  /* WENO only: 1 = bounds-preserving limiter to [lower, upper] */
+    int32_t reserved;                 /* 0 */
+    double lower, upper;              /* the bounds (m), lower < upper (either may be infinite) */
+} nk_advection_desc;
+nk_status nk_set_thickness_advection(nk_problem* problem, const nk_advection_desc* advection);
 
 /* The EnthalpyThermodynamics constants of the energy step (src/Thermodynamics/enthalpy_thermodynamics.jl:92-104,
  * defaults 2.1, 2009, 3.34e5, 7.9e-8, 273.15, 223.15, 1e-3, 1, 1e-3, 1, 0.01, 0.05 / year, coupling on). */
@@ -516,6 +543,11 @@ nk_status nk_server_info(const nk_server* server, int32_t* resident, int64_t* de
 #define NK_KERNEL_SMOOTHER        1   /* one fine-level ℓ1-Jacobi sweep x' = x + (b - A x) / rowsum, in the
                                          multigrid precision (FP32 when mixed, FP64 otherwise) */
 #define NK_KERNEL_CG_UPDATE       2   /* x += alpha p, r -= alpha q with the fused r.r (and r.z) reductions */
+#define NK_KERNEL_THICKNESS_STAGE 3   /* one Runge-Kutta stage of nk_step_thickness with the problem's advection scheme
+                                         (the bounded WENO's limiter launched once before the timed launches) */
+#define NK_KERNEL_THICKNESS_LIMITER 4 /* the bounded WENO's limiter from the current thickness */
+#define NK_KERNEL_STEP_ENTHALPY   5   /* the column energy step of nk_step_enthalpy with EnthalpyThermodynamics' defaults
+                                         (needs the sigma rate-factor layout) */
 
 /* Instrumentation (no counterpart in the reference, which times whole solves with @elapsed,
  * benchmarks/multigrid_scaling.jl:36-47): launches one hot kernel `repeats` times on the problem's

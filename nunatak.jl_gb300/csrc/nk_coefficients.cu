@@ -446,26 +446,104 @@ void launch_thermal_diagnostics(const DevGrid<double>& g, const SigmaTable& sig,
 }
 
 // ---- thickness transport -----------------------------------------------------------------------------------
+// The face thickness that u H carries through a face (UpwindBiased(order = 1 or 3) and WENO(order = 5) of the
+// reference's advection, restated from their published algorithms).  s[m + 2], m = -2..2, is the stage thickness m
+// cells from the upwind cell s[2] of the face, m > 0 towards and past the face.  A periodic stencil wraps as often as
+// the grid is short; a Bounded one takes the edge cell (the zero-gradient halo).
+__device__ __forceinline__ int wide_map(int i, int n, int periodic) {
+    if (periodic) { int r = i % n; return r < 0 ? r + n : r; }
+    return i < 0 ? 0 : (i > n - 1 ? n - 1 : i);
+}
+__device__ __forceinline__ void stencil_x(const DevGrid<double>& g, const double* __restrict__ H, int f, int j, bool east, double* s) {
+    int row = wide_map(j, g.Ny, g.py) * g.pitch;
+#pragma unroll
+    for (int m = -2; m <= 2; ++m) s[m + 2] = H[row + wide_map(east ? f - 1 + m : f - m, g.Nx, g.px)];
+}
+__device__ __forceinline__ void stencil_y(const DevGrid<double>& g, const double* __restrict__ H, int i, int f, bool north, double* s) {
+    int col = wide_map(i, g.Nx, g.px);
+#pragma unroll
+    for (int m = -2; m <= 2; ++m) s[m + 2] = H[wide_map(north ? f - 1 + m : f - m, g.Ny, g.py) * g.pitch + col];
+}
+// WENO-5: the three third-order candidates, their Jiang-Shu smoothness indicators and the WENO-Z weights
+// α_k = d_k (1 + τ / (β_k + ε)), τ = |β₀ - β₂|, ε = 1e-8, d = (1, 6, 3) / 10 (Jiang and Shu 1996; Borges et al. 2008,
+// exponent 1).
+__device__ __forceinline__ double weno5_face(const double* s) {
+    const double a = s[0], b = s[1], c = s[2], d = s[3], e = s[4];
+    double q0 = (2 * a - 7 * b + 11 * c) / 6;
+    double q1 = (-b + 5 * c + 2 * d) / 6;
+    double q2 = (2 * c + 5 * d - e) / 6;
+    double b0 = 13.0 / 12 * (a - 2 * b + c) * (a - 2 * b + c) + 0.25 * (a - 4 * b + 3 * c) * (a - 4 * b + 3 * c);
+    double b1 = 13.0 / 12 * (b - 2 * c + d) * (b - 2 * c + d) + 0.25 * (b - d) * (b - d);
+    double b2 = 13.0 / 12 * (c - 2 * d + e) * (c - 2 * d + e) + 0.25 * (3 * c - 4 * d + e) * (3 * c - 4 * d + e);
+    const double eps = 1e-8;
+    double tau = fabs(b0 - b2);
+    double r0 = tau / (b0 + eps), r1 = tau / (b1 + eps), r2 = tau / (b2 + eps);
+    double a0 = 0.1 * (1 + r0), a1 = 0.6 * (1 + r1), a2 = 0.3 * (1 + r2);
+    return (a0 * q0 + a1 * q1 + a2 * q2) / (a0 + a1 + a2);
+}
+__device__ __forceinline__ double face_value(const ThicknessView& v, const double* s) {
+    if (v.scheme == NK_ADVECTION_WENO) return weno5_face(s);
+    return v.order == 3 ? (-s[1] + 5 * s[2] + 2 * s[3]) / 6 : s[2];
+}
+
+// update_bounds_preserving_limiter! (src/Models/time_stepping.jl:35-42) restated as the Zhang-Shu (2010) limiter per
+// direction: from cell (i, j)'s own WENO face values W, E, S, N and the interior quadrature values
+// p̃ = (H̄ - ω (W + E)) / (1 - 2ω), ω = 5/18 (likewise in y), θ = min(1, |(upper - H̄) / (M - H̄ + ε)|,
+// |(lower - H̄) / (m - H̄ - ε)|) with M, m the largest and smallest of the six and ε = 2 eps.
+__global__ void k_thickness_limiter(ThicknessView v) {
+    const DevGrid<double>& g = v.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    const double* __restrict__ Hs = v.Hs;
+    double s[5], Hc = Hs[g.idx(i, j)];
+    stencil_x(g, Hs, i + 1, j, true, s);
+    double E = weno5_face(s);
+    stencil_x(g, Hs, i, j, false, s);
+    double W = weno5_face(s);
+    stencil_y(g, Hs, i, j + 1, true, s);
+    double N = weno5_face(s);
+    stencil_y(g, Hs, i, j, false, s);
+    double S = weno5_face(s);
+    const double w = 5.0 / 18, eps = 2 * 2.220446049250313e-16;
+    double px = (Hc - w * W - w * E) / (1 - 2 * w);
+    double py = (Hc - w * S - w * N) / (1 - 2 * w);
+    double M = fmax(fmax(fmax(px, py), fmax(W, E)), fmax(S, N));
+    double m = fmin(fmin(fmin(px, py), fmin(W, E)), fmin(S, N));
+    v.theta[g.idx(i, j)] = fmin(fmin(fabs((v.upper - Hc) / (M - Hc + eps)), fabs((v.lower - Hc) / (m - Hc - eps))), 1.0);
+}
+void launch_thickness_limiter(const ThicknessView& v, cudaStream_t s) {
+    LaunchDims d = dims2d(v.g.Nx, v.g.Ny);
+    k_thickness_limiter<<<d.grid, d.block, 0, s>>>(v); count_launch();
+}
+
 // One split Runge-Kutta stage of the mass balance, the tendency and the substep fused (_compute_thickness_tendency!
 // and _thickness_substep!, src/Models/time_stepping.jl:59-72): G = a - (1 - φ) m - mᵍ - ∇⋅(ū H) at cell (i, j) from
-// the stage-start thickness Hs, with the first-order upwind flux through each face (the face's normal velocity times
-// the upwind cell's thickness times the face length, UpwindBiased(order = 1); nothing through a Bounded wall), then
+// the stage-start thickness Hs, the flux through each face Δ (u H_face) with the scheme's upwind-biased face thickness
+// (limited by the upwind cell's θ for a bounded WENO: H̄ + θ (H_face - H̄)); nothing through a Bounded wall; then
 // H = max(0, H⁻ + Δτ G) from the step-start thickness H⁻, and in the last stage the clip max(0, -H★) added to Hc.
-// Hs and H are distinct arrays: every cell reads its four neighbours' stage-start thickness.
+// Hs and H are distinct arrays: every cell reads its neighbours' stage-start thickness.
 __global__ void k_thickness_stage(ThicknessView v, double dtau, int final_stage) {
     const DevGrid<double>& g = v.g;
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i >= g.Nx || j >= g.Ny) return;
     const double* __restrict__ Hs = v.Hs;
+    const bool bounded = v.scheme == NK_ADVECTION_WENO && v.bounded;
+    auto limited = [&](double h, int k) { return bounded ? Hs[k] + v.theta[k] * (h - Hs[k]) : h; };
     auto xflux = [&](int f) {
         if (g.peripheral_fc(f, j)) return 0.0;
-        double u = v.x[g.u_idx(f, j)].x;
-        return g.dyc[j] * u * (u > 0 ? Hs[g.c_idx(f - 1, j)] : Hs[g.c_idx(f, j)]);
+        double u = v.x[g.u_idx(f, j)].x, s[5];
+        bool east = u > 0;
+        stencil_x(g, Hs, f, j, east, s);
+        double h = limited(face_value(v, s), g.c_idx(east ? f - 1 : f, j));
+        return g.dyc[j] * (u * h);
     };
     auto yflux = [&](int f) {
         if (g.peripheral_cf(i, f)) return 0.0;
-        double w = v.x[g.v_idx(i, f)].y;
-        return g.dxc[i] * w * (w > 0 ? Hs[g.c_idx(i, f - 1)] : Hs[g.c_idx(i, f)]);
+        double w = v.x[g.v_idx(i, f)].y, s[5];
+        bool north = w > 0;
+        stencil_y(g, Hs, i, f, north, s);
+        double h = limited(face_value(v, s), g.c_idx(i, north ? f - 1 : f));
+        return g.dxc[i] * (w * h);
     };
     int c = g.idx(i, j);
     double m = v.grounding ? (1 - v.phi[c]) * v.melt[c] : v.melt[c];

@@ -185,7 +185,11 @@ struct ThicknessView {
     const double* smb; const double* melt; const double* gmelt; const double* phi;
     double* H; double* clipped;
     int grounding, coupled;
+    int scheme, order, bounded;       // nk_advection_desc
+    double lower, upper;
+    double* theta;                    // the bounds-preserving limiter per cell (bounded WENO only)
 };
+void launch_thickness_limiter(const ThicknessView& v, cudaStream_t s);
 void launch_thickness_stage(const ThicknessView& v, double dtau, int final_stage, cudaStream_t s);
 
 // ---- the energy step -------------------------------------------------------------------------------------

@@ -202,6 +202,9 @@ struct nk_problem {
     double* thermal = nullptr;                 // enthalpy then water fraction (Ns planes each), allocated on first use
     double* transport = nullptr;               // a, m, mᵍ, clipped thickness, then H at the step's and the stage's start
     double* energy = nullptr;                  // H_w, G, T_s, T_o, Hⁿ, s_b, qᵍ, then Φ and the step-start E (Ns planes each)
+    // the thickness advection of nk_step_thickness: the reference's default for the SSA and the DIVA,
+    // WENO(order = 5, bounds = (0, 1e5)) (default_thickness_advection, src/Models/ice_sheet_model.jl:123)
+    nk_advection_desc advection{NK_ADVECTION_WENO, 5, 1, 0, 0.0, 1e5};
     std::vector<double> sig_dz, sig_w2, sig_zc, sig_w1, sig_zf;
 
     // coarse levels
@@ -1129,8 +1132,9 @@ static void ensure_energy(nk_problem* P) {
 }
 
 // The thickness step's planes (zero at first): the four fields of NK_FIELD_SURFACE_MASS_BALANCE ..
-// NK_FIELD_CLIPPED_THICKNESS, then the thickness at the start of the step and of the stage.  No graph reads them.
-static const int TRANSPORT_PLANES = 6;
+// NK_FIELD_CLIPPED_THICKNESS, then the thickness at the start of the step and of the stage, and the bounds-preserving
+// limiter of each cell.  No graph reads them.
+static const int TRANSPORT_PLANES = 7;
 static void ensure_transport(nk_problem* P) {
     if (P->transport) return;
     if (P->async_pending) bad("an asynchronous solve is pending (nk_problem_wait first)");
@@ -1507,6 +1511,66 @@ nk_status nk_compute_geometry(nk_problem* P) {
     });
 }
 
+}  // extern "C"
+
+namespace nk {
+// The energy step's view of the problem (its planes allocated first).
+static EnergyView energy_view(nk_problem* P, const nk_energy_params* prm) {
+    ensure_thermal(P);
+    ensure_transport(P);
+    ensure_energy(P);
+    const size_t pl = P->plane;
+    EnergyView v;
+    v.g = P->fine.g;
+    v.sig = P->sigma_table();
+    v.plane = (long long)pl;
+    v.q = {prm->thermal_conductivity, prm->heat_capacity, prm->latent_heat, prm->clausius_clapeyron, prm->melting_temperature,
+           prm->reference_temperature, prm->temperate_diffusivity_ratio, prm->enthalpy_blend_width,
+           prm->water_layer_blend_thickness, prm->minimum_thickness, prm->drainage_water_fraction, prm->maximum_drainage_rate,
+           prm->grounded_melt_coupling != 0};
+    v.rho_i = P->pd.ice_density; v.gacc = P->pd.gravitational_acceleration;
+    v.wall_factor = P->pd.side_walls == NK_NO_SLIP ? 2.0 : 0.0;
+    v.diva = P->pd.stress_balance == NK_DIVA; v.grounding = P->pd.grounding != 0;
+    v.x = P->x; v.ud = P->ud; v.usig = P->usig; v.ub = P->ub; v.coef = P->fine.coef; v.bb = P->bb; v.eta_sigma = P->eta_sigma;
+    v.H = P->H; v.phi = P->phi;
+    double* en = P->energy;
+    v.Hw = en; v.G = en + pl; v.Ts = en + 2 * pl; v.To = en + 3 * pl; v.Hn = en + 4 * pl; v.sb = en + 5 * pl; v.qg = en + 6 * pl;
+    v.Phi = en + ENERGY_PLANES_2D * pl;
+    v.E_old = en + (ENERGY_PLANES_2D + (size_t)P->Ns) * pl;
+    v.melt = P->transport + pl; v.gmelt = P->transport + 2 * pl;
+    v.E = P->thermal; v.omega = P->thermal + (size_t)P->Ns * pl; v.T = P->T;
+    return v;
+}
+
+// The thickness step's view of the problem with its advection scheme (its planes allocated first).
+static ThicknessView thickness_view(nk_problem* P, bool coupled) {
+    ensure_transport(P);
+    const nk_advection_desc& adv = P->advection;
+    ThicknessView v;
+    v.g = P->fine.g;
+    v.x = P->x; v.Hs = P->transport + 5 * P->plane; v.H0 = P->transport + 4 * P->plane;
+    v.smb = P->transport; v.melt = P->transport + P->plane; v.gmelt = P->transport + 2 * P->plane; v.phi = P->phi;
+    v.H = P->H; v.clipped = P->transport + 3 * P->plane;
+    v.grounding = P->pd.grounding != 0; v.coupled = coupled;
+    v.scheme = adv.scheme; v.order = adv.order; v.bounded = adv.bounded;
+    v.lower = adv.lower; v.upper = adv.upper;
+    v.theta = P->transport + 6 * P->plane;
+    return v;
+}
+
+// EnthalpyThermodynamics' defaults (src/Thermodynamics/enthalpy_thermodynamics.jl:92-104).
+static nk_energy_params default_energy_params() {
+    nk_energy_params q{};
+    q.thermal_conductivity = 2.1; q.heat_capacity = 2009; q.latent_heat = 3.34e5; q.clausius_clapeyron = 7.9e-8;
+    q.melting_temperature = 273.15; q.reference_temperature = 223.15; q.temperate_diffusivity_ratio = 1e-3;
+    q.enthalpy_blend_width = 1; q.water_layer_blend_thickness = 1e-3; q.minimum_thickness = 1;
+    q.drainage_water_fraction = 0.01; q.maximum_drainage_rate = 0.05 / 31556926.0; q.grounded_melt_coupling = 1;
+    return q;
+}
+}  // namespace nk
+
+extern "C" {
+
 nk_status nk_step_enthalpy(nk_problem* P, const nk_energy_params* prm, double dt) {
     if (!P || !prm) return NK_BAD_ARGUMENT;
     return guarded(P->ctx, [&] {
@@ -1520,34 +1584,12 @@ nk_status nk_step_enthalpy(nk_problem* P, const nk_energy_params* prm, double dt
             bad("conductivity, heat capacity, latent heat, blend widths, minimum thickness and drainage fraction must be positive");
         if (P->async_pending) bad("an asynchronous solve is pending (nk_problem_wait first)");
         static_assert(ENERGY_MAX_LAYERS == NK_ENERGY_MAX_LAYERS, "one layer limit");
-        ensure_thermal(P);
-        ensure_transport(P);
-        ensure_energy(P);
+        EnergyView v = energy_view(P, prm);
         const size_t pl = P->plane;
-        EnergyView v;
-        v.g = P->fine.g;
-        v.sig = P->sigma_table();
-        v.plane = (long long)pl;
-        v.q = {prm->thermal_conductivity, prm->heat_capacity, prm->latent_heat, prm->clausius_clapeyron, prm->melting_temperature,
-               prm->reference_temperature, prm->temperate_diffusivity_ratio, prm->enthalpy_blend_width,
-               prm->water_layer_blend_thickness, prm->minimum_thickness, prm->drainage_water_fraction, prm->maximum_drainage_rate,
-               prm->grounded_melt_coupling != 0};
-        v.rho_i = P->pd.ice_density; v.gacc = P->pd.gravitational_acceleration;
-        v.wall_factor = P->pd.side_walls == NK_NO_SLIP ? 2.0 : 0.0;
-        v.diva = P->pd.stress_balance == NK_DIVA; v.grounding = P->pd.grounding != 0;
-        v.x = P->x; v.ud = P->ud; v.usig = P->usig; v.ub = P->ub; v.coef = P->fine.coef; v.bb = P->bb; v.eta_sigma = P->eta_sigma;
-        v.H = P->H; v.phi = P->phi;
-        double* en = P->energy;
-        v.Hw = en; v.G = en + pl; v.Ts = en + 2 * pl; v.To = en + 3 * pl; v.Hn = en + 4 * pl; v.sb = en + 5 * pl; v.qg = en + 6 * pl;
-        v.Phi = en + ENERGY_PLANES_2D * pl;
-        double* E_old = en + (ENERGY_PLANES_2D + (size_t)P->Ns) * pl;
-        v.E_old = E_old;
-        v.melt = P->transport + pl; v.gmelt = P->transport + 2 * pl;
-        v.E = P->thermal; v.omega = P->thermal + (size_t)P->Ns * pl; v.T = P->T;
-        NK_CUDA(cudaMemcpyAsync(E_old, P->thermal, (size_t)P->Ns * pl * sizeof(double), cudaMemcpyDeviceToDevice, P->stream));
+        NK_CUDA(cudaMemcpyAsync(const_cast<double*>(v.E_old), P->thermal, (size_t)P->Ns * pl * sizeof(double), cudaMemcpyDeviceToDevice, P->stream));
         launch_step_enthalpy(v, dt, P->stream);
         NK_CHECK_LAUNCH();
-        NK_CUDA(cudaMemcpyAsync(en + 4 * pl, P->H, pl * sizeof(double), cudaMemcpyDeviceToDevice, P->stream));   // Hⁿ = H
+        NK_CUDA(cudaMemcpyAsync(P->energy + 4 * pl, P->H, pl * sizeof(double), cudaMemcpyDeviceToDevice, P->stream));   // Hⁿ = H
         NK_CUDA(cudaStreamSynchronize(P->stream));
     });
 }
@@ -1557,24 +1599,36 @@ nk_status nk_step_thickness(nk_problem* P, double dt, int32_t grounded_melt_coup
     return guarded(P->ctx, [&] {
         if (!(dt > 0) || !std::isfinite(dt)) bad("the time step must be finite and positive");
         if (P->async_pending) bad("an asynchronous solve is pending (nk_problem_wait first)");
-        ensure_transport(P);
-        double* H0 = P->transport + 4 * P->plane;
-        double* Hs = P->transport + 5 * P->plane;
-        ThicknessView v;
-        v.g = P->fine.g;
-        v.x = P->x; v.Hs = Hs; v.H0 = H0;
-        v.smb = P->transport; v.melt = P->transport + P->plane; v.gmelt = P->transport + 2 * P->plane; v.phi = P->phi;
-        v.H = P->H; v.clipped = P->transport + 3 * P->plane;
-        v.grounding = P->pd.grounding != 0; v.coupled = grounded_melt_coupling != 0;
-        NK_CUDA(cudaMemcpyAsync(H0, P->H, P->plane * sizeof(double), cudaMemcpyDeviceToDevice, P->stream));
+        const nk_advection_desc& adv = P->advection;
+        const bool bounded = adv.scheme == NK_ADVECTION_WENO && adv.bounded;
+        int halo = std::min(P->gd.halo_x, P->gd.halo_y);
+        if (bounded && halo < 4)   // check_advection_halo, src/Models/ice_sheet_model.jl:131-135
+            bad("bounded WENO(order = 5) needs a horizontal halo of at least 4, got (" + std::to_string(P->gd.halo_x) + ", " +
+                std::to_string(P->gd.halo_y) + ")");
+        if ((adv.scheme == NK_ADVECTION_WENO || adv.order == 3) && halo < 3)
+            bad("the advection scheme's stencil needs a horizontal halo of at least 3");
+        ThicknessView v = thickness_view(P, grounded_melt_coupling != 0);
+        NK_CUDA(cudaMemcpyAsync((double*)v.H0, P->H, P->plane * sizeof(double), cudaMemcpyDeviceToDevice, P->stream));
         const double stages[3] = {1.0 / 3, 1.0 / 2, 1.0};     // SplitRungeKutta3 (Wicker-Skamarock) fractions
         for (int st = 0; st < 3; ++st) {
-            NK_CUDA(cudaMemcpyAsync(Hs, P->H, P->plane * sizeof(double), cudaMemcpyDeviceToDevice, P->stream));
+            NK_CUDA(cudaMemcpyAsync((double*)v.Hs, P->H, P->plane * sizeof(double), cudaMemcpyDeviceToDevice, P->stream));
+            if (bounded) launch_thickness_limiter(v, P->stream);
             launch_thickness_stage(v, stages[st] * dt, st == 2, P->stream);
             launch_problem_geometry(P);
             NK_CHECK_LAUNCH();
         }
         NK_CUDA(cudaStreamSynchronize(P->stream));
+    });
+}
+
+nk_status nk_set_thickness_advection(nk_problem* P, const nk_advection_desc* adv) {
+    if (!P || !adv) return NK_BAD_ARGUMENT;
+    return guarded(P->ctx, [&] {
+        bool upwind = adv->scheme == NK_ADVECTION_UPWIND && (adv->order == 1 || adv->order == 3) && !adv->bounded;
+        bool weno = adv->scheme == NK_ADVECTION_WENO && adv->order == 5 && (!adv->bounded || adv->lower < adv->upper);
+        if (!upwind && !weno)
+            bad("thickness advection: UpwindBiased(order = 1 or 3) or WENO(order = 5) with bounds lower < upper");
+        P->advection = *adv;
     });
 }
 
@@ -1996,6 +2050,8 @@ nk_status nk_time_kernel(nk_problem* P, int32_t kernel, int32_t repeats, int64_t
         if (flush_bytes > 0) NK_CUDA(cudaMalloc((void**)&flush, (size_t)flush_bytes));
         double total = 0.0;
         double bytes = 0.0;
+        ThicknessView tv{};
+        EnergyView ev{};
         auto launch = [&]() {
             if (kernel == NK_KERNEL_OPERATOR_FP64) {
                 launch_apply(P->fine_op(), P->p, P->q, s);
@@ -2011,13 +2067,38 @@ nk_status nk_time_kernel(nk_problem* P, int32_t kernel, int32_t repeats, int64_t
             } else if (kernel == NK_KERNEL_CG_UPDATE) {
                 CGView v = P->cg_view(P->tau);
                 launch_cg_update(v, s);
+            } else if (kernel == NK_KERNEL_THICKNESS_STAGE) {
+                launch_thickness_stage(tv, 1.0, 0, s);
+            } else if (kernel == NK_KERNEL_THICKNESS_LIMITER) {
+                launch_thickness_limiter(tv, s);
+            } else if (kernel == NK_KERNEL_STEP_ENTHALPY) {
+                launch_step_enthalpy(ev, 1.0, s);
             } else {
                 bad("unknown kernel id");
             }
         };
+        const bool bounded = P->advection.scheme == NK_ADVECTION_WENO && P->advection.bounded;
         if (kernel == NK_KERNEL_OPERATOR_FP64) bytes = cells * (16 + 32 + 1 + 16);
         else if (kernel == NK_KERNEL_SMOOTHER) bytes = cells * (P->mixed ? (8 + 8 + 8 + 16 + 1 + 8) : (16 + 16 + 16 + 32 + 1 + 16));
-        else bytes = cells * (64 + 32 + (P->precond == NK_PRECONDITIONER_DIAGONAL ? 16 + 16 : 0));
+        else if (kernel == NK_KERNEL_CG_UPDATE) bytes = cells * (64 + 32 + (P->precond == NK_PRECONDITIONER_DIAGONAL ? 16 + 16 : 0));
+        // Hs, H⁻, a, m, (u, v), H written; φ with a grounding treatment; θ for a bounded WENO
+        else if (kernel == NK_KERNEL_THICKNESS_STAGE) bytes = cells * (8 + 8 + 8 + 8 + 16 + 8 + (P->pd.grounding ? 8 : 0) + (bounded ? 8 : 0));
+        else if (kernel == NK_KERNEL_THICKNESS_LIMITER) bytes = cells * (8 + 8);
+        // per column: H, Hⁿ, φ, m, mᵍ, G, Tₛ, Tₒ, H_w, (u, v), (uᵇ, vᵇ) and the drag; per layer E_old, η, (uσ, vσ) read and E,
+        // T, ω, Φ written
+        else if (kernel == NK_KERNEL_STEP_ENTHALPY) bytes = cells * 8 * (11 + 8.0 * P->Ns);
+        if (kernel == NK_KERNEL_THICKNESS_STAGE || kernel == NK_KERNEL_THICKNESS_LIMITER) {
+            tv = thickness_view(P, false);
+            NK_CUDA(cudaMemcpyAsync((double*)tv.Hs, P->H, P->plane * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            NK_CUDA(cudaMemcpyAsync((double*)tv.H0, P->H, P->plane * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            if (kernel == NK_KERNEL_THICKNESS_STAGE && !bounded) tv.bounded = 0;
+            if (kernel == NK_KERNEL_THICKNESS_STAGE && bounded) launch_thickness_limiter(tv, s);
+        } else if (kernel == NK_KERNEL_STEP_ENTHALPY) {
+            if (P->pd.rate_factor_layout != NK_RATE_FACTOR_SIGMA || P->Ns > ENERGY_MAX_LAYERS) bad("the energy step needs the sigma rate factor");
+            nk_energy_params q = default_energy_params();
+            ev = energy_view(P, &q);
+            NK_CUDA(cudaMemcpyAsync(const_cast<double*>(ev.E_old), P->thermal, (size_t)P->Ns * P->plane * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        }
         if (kernel == NK_KERNEL_CG_UPDATE) {
             // run the update with done = 0 so it is not skipped
             P->sc_host->done = 0;

@@ -7,7 +7,8 @@ from .model import (YEAR, Convergence, DepthIntegrated, DIVAShear, FixedIteratio
                     IceSheetConstants, LineJacobi, NoSlipWalls, PointJacobi, RectilinearGrid,
                     RegularizedCoulombFriction, SmoothIceMask, StressBalanceDiagonalPreconditioner,
                     StressBalanceMultigridPreconditioner, StressBalanceSolver, SubgridGroundedFraction,
-                    ViscosityConvergence, WeertmanFriction, make_descriptors, field_shape, sigma_faces)
+                    UpwindBiased, ViscosityConvergence, WENO, WeertmanFriction, default_thickness_advection,
+                    make_descriptors, field_shape, sigma_faces)
 from .problem import NunatakError, Problem
 
 __all__ = [
@@ -15,6 +16,6 @@ __all__ = [
     "IceSheetConstants", "LineJacobi", "NoSlipWalls", "PointJacobi", "RectilinearGrid", "RegularizedCoulombFriction",
     "SmoothIceMask", "StressBalanceDiagonalPreconditioner", "StressBalanceMultigridPreconditioner",
     "StressBalanceSolver", "SubgridGroundedFraction", "ViscosityConvergence", "WeertmanFriction", "make_descriptors",
-    "field_shape", "sigma_faces",
+    "field_shape", "sigma_faces", "UpwindBiased", "WENO", "default_thickness_advection",
     "NunatakError", "Problem",
 ]

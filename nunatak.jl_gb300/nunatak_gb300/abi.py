@@ -68,6 +68,15 @@ class EnergyParams(C.Structure):
         [("grounded_melt_coupling", C.c_int32), ("reserved", C.c_int32)]
 
 
+NK_ADVECTION_UPWIND, NK_ADVECTION_WENO = 0, 1
+
+
+class AdvectionDesc(C.Structure):
+    """nk_advection_desc: the thickness advection scheme of nk_step_thickness."""
+    _fields_ = [("scheme", C.c_int32), ("order", C.c_int32), ("bounded", C.c_int32), ("reserved", C.c_int32),
+                ("lower", C.c_double), ("upper", C.c_double)]
+
+
 class IterationControl(C.Structure):
     _fields_ = [("kind", C.c_int32), ("iterations", C.c_int32), ("maxiter", C.c_int32),
                 ("reserved", C.c_int32), ("reltol", C.c_double), ("abstol", C.c_double)]

@@ -177,6 +177,33 @@ class IceSheetConstants:
     gravitational_acceleration: float = 9.81
 
 
+# ---- thickness advection ----------------------------------------------------------------------------------
+@dataclass
+class UpwindBiased:
+    """UpwindBiased(order = 1 or 3), Oceananigans' upwind-biased advection of the thickness."""
+    order: int = 1
+
+    def desc(self):
+        return abi.AdvectionDesc(abi.NK_ADVECTION_UPWIND, int(self.order), 0, 0, 0.0, 0.0)
+
+
+@dataclass
+class WENO:
+    """WENO(order = 5), and with `bounds = (lower, upper)` its bounds-preserving form.  The reference's default thickness
+    advection for the SSA and the DIVA is WENO(order = 5, bounds = (0, 1e5)) (src/Models/ice_sheet_model.jl:123)."""
+    order: int = 5
+    bounds: Optional[Tuple[float, float]] = None
+
+    def desc(self):
+        lo, hi = self.bounds if self.bounds is not None else (0.0, 0.0)
+        return abi.AdvectionDesc(abi.NK_ADVECTION_WENO, int(self.order), 1 if self.bounds is not None else 0, 0, float(lo), float(hi))
+
+
+def default_thickness_advection():
+    """default_thickness_advection(grid, stress_balance) of the SSA and the DIVA (src/Models/ice_sheet_model.jl:123)."""
+    return WENO(order=5, bounds=(0.0, 1e5))
+
+
 # ---- solver -------------------------------------------------------------------------------------------
 @dataclass
 class PointJacobi:

@@ -200,9 +200,15 @@ class Problem:
                                int(grounded_melt_coupling), 0)
         _check(self._fn("step_enthalpy")(self._h, C.byref(prm), float(dt)), "step_enthalpy", self._err())
 
+    def set_thickness_advection(self, advection):
+        """The thickness advection scheme of step_thickness (IceSheetModel's `advection`): an UpwindBiased(order = 1 or 3)
+        or a WENO(order = 5, bounds = None or (lower, upper)); a new problem has WENO(order = 5, bounds = (0, 1e5))."""
+        d = advection.desc()
+        _check(self._fn("set_thickness_advection")(self._h, C.byref(d)), "set_thickness_advection", self._err())
+
     def step_thickness(self, dt, grounded_melt_coupling=False):
         """One ice time step of the thickness with the velocities held (the three rk_substep! stages of time_step!,
-        src/Models/time_stepping.jl:15-72, first-order upwind, the geometry after every stage)."""
+        src/Models/time_stepping.jl:15-72, with the problem's advection scheme, the geometry after every stage)."""
         _check(self._fn("step_thickness")(self._h, float(dt), int(grounded_melt_coupling)), "step_thickness", self._err())
 
     def update_coefficients(self):
@@ -329,7 +335,8 @@ class Problem:
         return fu, fv
 
     # -- measurement ---------------------------------------------------------------------------------------
-    KERNELS = {"operator_fp64": 0, "smoother": 1, "cg_update": 2}
+    KERNELS = {"operator_fp64": 0, "smoother": 1, "cg_update": 2, "thickness_stage": 3, "thickness_limiter": 4,
+               "step_enthalpy": 5}
 
     def time_kernel(self, kernel, repeats=20, flush_bytes=0):
         """Mean CUDA-event duration (ms) of one launch of a hot kernel and its algorithmic bytes

@@ -830,6 +830,10 @@ struct Problem {
     // temperatures, basal melt rate m, thickness of the previous energy step Hⁿ, strain heating Φ
     Field Hw, gmelt, G, Ts, To, melt, Hn, sb;   // sb: the temperate fraction sᵇ of the basal layer (output)
     Field smb, clipped;           // thickness step (nko_step_thickness): surface mass balance, clipped thickness
+    // thickness advection (nko_set_thickness_advection); the reference's default for the SSA and the DIVA is
+    // WENO(order = 5, bounds = (0, 1e5)) (default_thickness_advection, src/Models/ice_sheet_model.jl:123)
+    nk_advection_desc advection{NK_ADVECTION_WENO, 5, 1, 0, 0.0, 1e5};
+    Field theta;                  // the bounds-preserving limiter of each cell (and of the first halo layer)
     Field qg;                     // basal heat flux qᵍ = φ G + τᵇ⋅uᵇ of the last energy step (output)
     SigmaField Phi;
 
@@ -1730,33 +1734,114 @@ static void step_enthalpy(Problem& P, const EnergyParams& q, double dt) {
 }
 
 // ------------------------------------------------------------------------------------------------
-// One ice time step of the thickness (TEST INFRASTRUCTURE: no library counterpart yet), time_stepping.jl:15-72:
-// three split Runge-Kutta stages H = max(0, H⁻ + Δτ G(H)) from the thickness H⁻ at the start of the step, with
-// Δτ = Δt/3, Δt/2, Δt (Oceananigans 0.117's SplitRungeKutta3, the Wicker-Skamarock scheme), the thickness added by
-// the clip in the last stage accumulated in `clipped`, and the geometry updated after every stage (update_state!).
-// G = a - (1 - φ) m - mᵍ - ∇⋅(ū H) with the first-order upwind flux (UpwindBiased(order = 1)): through a face,
-// Δ u H of the upwind cell; Bounded walls pass nothing.  The velocities are held (no velocity solve).
+// Thickness advection (the face thickness that u H carries through a face).  The reference takes it from
+// Oceananigans 0.117's UpwindBiased and WENO schemes (src/Models/time_stepping.jl:59-63 through div_Uc), which are
+// not vendored; this restates their published algorithms.  s(m), m = -2..2, is the thickness m cells away from the
+// upwind cell s(0) of the face, m > 0 towards the face and beyond (downwind).  Stored as s[m + 2].
+// ------------------------------------------------------------------------------------------------
+// UpwindBiased(order = 3): the third-order upwind-biased interpolation.
+static double upwind3_face(const double* s) { return (-s[1] + 5 * s[2] + 2 * s[3]) / 6; }
+
+// WENO(order = 5): the three third-order candidates on the stencils (-2..0), (-1..1), (0..2), their Jiang-Shu
+// smoothness indicators β and the WENO-Z weights α_k = d_k (1 + τ / (β_k + ε)), τ = |β₀ - β₂|, ε = 1e-8, with
+// the optimal weights d = (1, 6, 3) / 10 (Jiang and Shu 1996; Borges, Carmona, Costa and Don 2008).
+static double weno5_face(const double* s) {
+    const double a = s[0], b = s[1], c = s[2], d = s[3], e = s[4];
+    double q0 = (2 * a - 7 * b + 11 * c) / 6;
+    double q1 = (-b + 5 * c + 2 * d) / 6;
+    double q2 = (2 * c + 5 * d - e) / 6;
+    double b0 = 13.0 / 12 * (a - 2 * b + c) * (a - 2 * b + c) + 0.25 * (a - 4 * b + 3 * c) * (a - 4 * b + 3 * c);
+    double b1 = 13.0 / 12 * (b - 2 * c + d) * (b - 2 * c + d) + 0.25 * (b - d) * (b - d);
+    double b2 = 13.0 / 12 * (c - 2 * d + e) * (c - 2 * d + e) + 0.25 * (3 * c - 4 * d + e) * (3 * c - 4 * d + e);
+    const double eps = 1e-8;
+    double tau = std::fabs(b0 - b2);
+    double r0 = tau / (b0 + eps), r1 = tau / (b1 + eps), r2 = tau / (b2 + eps);
+    double a0 = 0.1 * (1 + r0), a1 = 0.6 * (1 + r1), a2 = 0.3 * (1 + r2);
+    return (a0 * q0 + a1 * q1 + a2 * q2) / (a0 + a1 + a2);
+}
+
+// The unlimited face value of the scheme from the stencil s.
+static double face_value(const nk_advection_desc& adv, const double* s) {
+    if (adv.scheme == NK_ADVECTION_WENO) return weno5_face(s);
+    return adv.order == 3 ? upwind3_face(s) : s[2];
+}
+
+// Stencils of the upwind cell ic of face f along x (ic = f - 1 when the flow is eastward: s(m) = H(f - 1 + m);
+// ic = f when westward: s(m) = H(f - m)) and likewise along y, from the halo-filled stage thickness.
+static void x_stencil(const Field& H, int f, int j, bool east, double* s) {
+    for (int m = -2; m <= 2; ++m) s[m + 2] = east ? H(f - 1 + m, j) : H(f - m, j);
+}
+static void y_stencil(const Field& H, int i, int f, bool north, double* s) {
+    for (int m = -2; m <= 2; ++m) s[m + 2] = north ? H(i, f - 1 + m) : H(i, f - m);
+}
+
+// The bounds-preserving limiter θ of cell (i, j) (Zhang and Shu 2010, applied per direction): with the cell's own
+// face values W, E (x) and S, N (y), each direction's interior quadrature value p̃ = (H̄ - ω(W + E)) / (1 - 2ω),
+// ω = 5/18, and M, m the largest and smallest of the six, θ = min(1, |(upper - H̄) / (M - H̄ + ε)|,
+// |(lower - H̄) / (m - H̄ - ε)|), ε = 2 eps; the limited face value is H̄ + θ (face - H̄).
+static double bounds_limiter(const nk_advection_desc& adv, const Field& H, int i, int j) {
+    double s[5], Hc = H(i, j);
+    x_stencil(H, i + 1, j, true, s);
+    double E = weno5_face(s);
+    x_stencil(H, i, j, false, s);
+    double W = weno5_face(s);
+    y_stencil(H, i, j + 1, true, s);
+    double N = weno5_face(s);
+    y_stencil(H, i, j, false, s);
+    double S = weno5_face(s);
+    const double w = 5.0 / 18, eps = 2 * std::numeric_limits<double>::epsilon();
+    double px = (Hc - w * W - w * E) / (1 - 2 * w);
+    double py = (Hc - w * S - w * N) / (1 - 2 * w);
+    double M = std::max(std::max(std::max(px, py), std::max(W, E)), std::max(S, N));
+    double m = std::min(std::min(std::min(px, py), std::min(W, E)), std::min(S, N));
+    return std::min(std::min(std::fabs((adv.upper - Hc) / (M - Hc + eps)), std::fabs((adv.lower - Hc) / (m - Hc - eps))), 1.0);
+}
+
+// ------------------------------------------------------------------------------------------------
+// One ice time step of the thickness, time_stepping.jl:15-72: three split Runge-Kutta stages
+// H = max(0, H⁻ + Δτ G(H)) from the thickness H⁻ at the start of the step, with Δτ = Δt/3, Δt/2, Δt (Oceananigans
+// 0.117's SplitRungeKutta3, the Wicker-Skamarock scheme), the thickness added by the clip in the last stage
+// accumulated in `clipped`, and the geometry updated after every stage (update_state!).
+// G = a - (1 - φ) m - mᵍ - ∇⋅(ū H), the flux through a face Δ (u H_face) with H_face the scheme's upwind-biased face
+// thickness (the limited one for a bounded WENO, whose limiter is recomputed from the stage's thickness first,
+// update_bounds_preserving_limiter!, :35-42, also in the first halo layer); Bounded walls pass nothing.  The
+// velocities are held (no velocity solve).
 // ------------------------------------------------------------------------------------------------
 static void compute_geometry(Problem& P);
 
 static void step_thickness(Problem& P, double dt, bool coupled) {
     const Grid& g = P.grid;
     const int Nx = g.Nx(), Ny = g.Ny();
+    const nk_advection_desc adv = P.advection;
+    const bool bounded = adv.scheme == NK_ADVECTION_WENO && adv.bounded;
     fill_halo(P.x);
     for (Field* f : {&P.smb, &P.melt, &P.gmelt, &P.clipped}) fill_halo(*f);
     Field H0 = P.H, Gt(&g, CENTER, CENTER);
+    if (bounded && !P.theta.g) P.theta.init(&g, CENTER, CENTER);
     const double stages[3] = {1.0 / 3, 1.0 / 2, 1.0};
     for (int st = 0; st < 3; ++st) {
         fill_halo(P.H);
+        if (bounded) {
+#pragma omp parallel for schedule(static)
+            for (int j = 0; j <= Ny + 1; ++j)
+                for (int i = 0; i <= Nx + 1; ++i) P.theta(i, j) = bounds_limiter(adv, P.H, i, j);
+        }
+        auto limited = [&](double v, int ic, int jc) { return bounded ? P.H(ic, jc) + P.theta(ic, jc) * (v - P.H(ic, jc)) : v; };
         auto xflux = [&](int i, int j) {
             if (g.peripheral_fc(i, j)) return 0.0;
-            double u = P.x.u(i, j);
-            return g.dy_c(j) * u * (u > 0 ? P.H(i - 1, j) : P.H(i, j));
+            double u = P.x.u(i, j), s[5];
+            bool east = u > 0;
+            x_stencil(P.H, i, j, east, s);
+            double h = limited(face_value(adv, s), east ? i - 1 : i, j);
+            return g.dy_c(j) * (u * h);
         };
         auto yflux = [&](int i, int j) {
             if (g.peripheral_cf(i, j)) return 0.0;
-            double v = P.x.v(i, j);
-            return g.dx_c(i) * v * (v > 0 ? P.H(i, j - 1) : P.H(i, j));
+            double v = P.x.v(i, j), s[5];
+            bool north = v > 0;
+            y_stencil(P.H, i, j, north, s);
+            double h = limited(face_value(adv, s), i, north ? j - 1 : j);
+            return g.dx_c(i) * (v * h);
         };
         for_xy(Nx, Ny, [&](int i, int j) {   // _compute_thickness_tendency!, :59-63
             double m = P.grounding ? (1 - P.phi(i, j)) * P.melt(i, j) : P.melt(i, j);
@@ -2040,7 +2125,24 @@ nk_status nko_energy_field(nko_problem* h, int32_t which, double* data, int64_t 
 // mᵍ of the energy step thins the ice.
 nk_status nko_step_thickness(nko_problem* h, double dt, int32_t coupled) {
     if (!h || !(dt > 0)) return NK_BAD_ARGUMENT;
-    step_thickness(*reinterpret_cast<Problem*>(h), dt, coupled != 0);
+    Problem& P = *reinterpret_cast<Problem*>(h);
+    int halo = std::min(P.grid.x.H, P.grid.y.H);
+    if (P.advection.scheme == NK_ADVECTION_WENO && P.advection.bounded && halo < 4)
+        return NK_BAD_ARGUMENT;   // check_advection_halo, src/Models/ice_sheet_model.jl:131-135
+    if ((P.advection.scheme == NK_ADVECTION_WENO || P.advection.order == 3) && halo < 3)
+        return NK_BAD_ARGUMENT;   // the five-point stencils reach three cells beyond a face
+    step_thickness(P, dt, coupled != 0);
+    return NK_OK;
+}
+
+// The thickness advection scheme (IceSheetModel's advection keyword): UpwindBiased(order = 1 or 3) or WENO(order = 5),
+// bounded to [lower, upper] or not.
+nk_status nko_set_thickness_advection(nko_problem* h, const nk_advection_desc* adv) {
+    if (!h || !adv) return NK_BAD_ARGUMENT;
+    bool ok = (adv->scheme == NK_ADVECTION_UPWIND && (adv->order == 1 || adv->order == 3) && !adv->bounded) ||
+              (adv->scheme == NK_ADVECTION_WENO && adv->order == 5 && (!adv->bounded || adv->lower < adv->upper));
+    if (!ok) return NK_BAD_ARGUMENT;
+    reinterpret_cast<Problem*>(h)->advection = *adv;
     return NK_OK;
 }
 

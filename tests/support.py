@@ -27,8 +27,13 @@ def evaluate(grid, name, f, Nsigma=None):
     return np.full((y.size, x.size), float(f))
 
 
-def make(cls, grid, **kw):
-    return cls(grid, M.make_descriptors(grid, **kw))
+def make(cls, grid, advection=None, **kw):
+    """A problem of class `cls`; `advection` (an UpwindBiased or a WENO) sets its thickness advection scheme, which is
+    otherwise the reference's default WENO(order = 5, bounds = (0, 1e5))."""
+    P = cls(grid, M.make_descriptors(grid, **kw))
+    if advection is not None:
+        P.set_thickness_advection(advection)
+    return P
 
 
 def set_fn(P, name, f):

@@ -51,7 +51,7 @@ class Column:
 
     def __init__(self, cls, H0=1000.0, Nsigma=10, bed_refinement=1.0, G=0.042, Ts=243.15, grounding=None, bed=0.0):
         g = M.RectilinearGrid(size=(1, 1), x=(0.0, 1e3), y=(0.0, 1e3), topology=("Periodic", "Periodic"), halo=(3, 3))
-        self.P = make(cls, g, Nsigma=Nsigma, bed_refinement=bed_refinement, rheology=M.GlenFlowLaw(rate_factor="sigma"),
+        self.P = make(cls, g, advection=M.UpwindBiased(order=1), Nsigma=Nsigma, bed_refinement=bed_refinement, rheology=M.GlenFlowLaw(rate_factor="sigma"),
                       constants=M.IceSheetConstants(ice_density=RHO), grounding=grounding)
         self.H0 = H0
         self.P.set("H", H0)
@@ -256,7 +256,7 @@ def test_uniform_enthalpy_stays_uniform(oracle_cls):
     thickness changes by more than 10 m."""
     L = 8e4
     g = M.RectilinearGrid(size=(8, 8), x=(0.0, L), y=(0.0, L), topology=("Periodic", "Periodic"), halo=(4, 4))
-    P = make(oracle_cls, g, Nsigma=10, bed_refinement=2.0, rheology=M.GlenFlowLaw(rate_factor="sigma"),
+    P = make(oracle_cls, g, advection=M.UpwindBiased(order=1), Nsigma=10, bed_refinement=2.0, rheology=M.GlenFlowLaw(rate_factor="sigma"),
              constants=M.IceSheetConstants(ice_density=RHO))
     ubar = lambda x, y: 1e-6 * (1 + math.sin(2 * math.pi * y / L) / 2)
     vbar = lambda x, y: 5e-7 * math.cos(2 * math.pi * x / L)
@@ -304,7 +304,7 @@ def test_upwind_transport_at_unit_courant_number_shifts_each_layer(oracle_cls, d
     Nx, dx, dt = 8, 1e3, 1e9
     size = (Nx, 1) if direction == "x" else (1, Nx)
     g = M.RectilinearGrid(size=size, x=(0.0, size[0] * dx), y=(0.0, size[1] * dx), topology=("Periodic", "Periodic"), halo=(3, 3))
-    P = make(oracle_cls, g, Nsigma=4, bed_refinement=1.0, rheology=M.GlenFlowLaw(rate_factor="sigma"))
+    P = make(oracle_cls, g, advection=M.UpwindBiased(order=1), Nsigma=4, bed_refinement=1.0, rheology=M.GlenFlowLaw(rate_factor="sigma"))
     P.set("H", 500.0)
     P.set("bed", 0.0)
     P.compute_geometry()
@@ -338,7 +338,7 @@ def test_friction_and_strain_heat_account_for_the_driving_work(oracle_cls, shear
     g = M.RectilinearGrid(size=(Nx, Nx), x=(0.0, L), y=(0.0, L), topology=("Periodic", "Periodic"), halo=(4, 4))
     solver = M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-12, maxiter=10_000),
                                    picard_iteration_control=M.Convergence(reltol=1e-11, maxiter=500))
-    P = make(oracle_cls, g, Nsigma=10, rheology=M.GlenFlowLaw(rate_factor=1e-24, strain_rate_regularization=1e-16),
+    P = make(oracle_cls, g, advection=M.UpwindBiased(order=1), Nsigma=10, rheology=M.GlenFlowLaw(rate_factor=1e-24, strain_rate_regularization=1e-16),
              friction=M.WeertmanFriction(coefficient=1e10, exponent=1.0), velocity_solver=solver,
              stress_balance=M.DepthIntegrated(shear=shear), constants=M.IceSheetConstants(ice_density=RHO))
     P.set("H", evaluate(g, "H", lambda x, y: 1000 + 100 * math.sin(2 * math.pi * x / L) * math.cos(2 * math.pi * y / L)))
@@ -374,7 +374,7 @@ def seeded_energy_case(cls, shear, state=None):
     rng = np.random.default_rng(1203)
     Nx, Ny, Ns = 24, 20, 8
     g = M.RectilinearGrid(size=(Nx, Ny), x=(0.0, Nx * 2e3), y=(0.0, Ny * 2e3), topology=("Bounded", "Periodic"), halo=(4, 4))
-    P = make(cls, g, Nsigma=Ns, rheology=M.GlenFlowLaw(rate_factor="sigma"), grounding=M.SubgridGroundedFraction(),
+    P = make(cls, g, advection=M.UpwindBiased(order=1), Nsigma=Ns, rheology=M.GlenFlowLaw(rate_factor="sigma"), grounding=M.SubgridGroundedFraction(),
              friction=M.WeertmanFriction(coefficient=1e10, exponent=1.0), stress_balance=M.DepthIntegrated(shear=shear),
              constants=M.IceSheetConstants(ice_density=RHO))
     x = g.centers(0)
@@ -437,7 +437,7 @@ def uniform_sheet(cls, N):
     """An N x N periodic sheet at rest, every column alike: 1000 m of ice with a temperate base over a wet bed."""
     g = M.RectilinearGrid(size=(N, N), x=(0.0, N * 1e3), y=(0.0, N * 1e3), topology=("Periodic", "Periodic"), halo=(4, 4))
     Ns = 16
-    P = make(cls, g, Nsigma=Ns, rheology=M.GlenFlowLaw(rate_factor="sigma"), constants=M.IceSheetConstants(ice_density=RHO))
+    P = make(cls, g, advection=M.UpwindBiased(order=1), Nsigma=Ns, rheology=M.GlenFlowLaw(rate_factor="sigma"), constants=M.IceSheetConstants(ice_density=RHO))
     P.set("H", 1000.0)
     P.set("bed", 0.0)
     P.compute_geometry()

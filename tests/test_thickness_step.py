@@ -25,10 +25,12 @@ from support import evaluate, make
 
 
 class Transport:
-    def __init__(self, cls, Nx=64, L=64e3, U=1e-6, width=None, velocity=None, background=0.0, smb=0.0, melt=0.0):
+    def __init__(self, cls, Nx=64, L=64e3, U=1e-6, width=None, velocity=None, background=0.0, smb=0.0, melt=0.0,
+                 advection=None, halo=4):
         width = L / 16 if width is None else width
-        self.g = M.RectilinearGrid(size=(Nx, 4), x=(0.0, L), y=(0.0, 4 * L / Nx), topology=("Bounded", "Periodic"), halo=(4, 4))
-        self.P = make(cls, self.g, Nsigma=2, masking=M.SmoothIceMask())
+        self.g = M.RectilinearGrid(size=(Nx, 4), x=(0.0, L), y=(0.0, 4 * L / Nx), topology=("Bounded", "Periodic"),
+                                   halo=(halo, halo))
+        self.P = make(cls, self.g, advection=advection or M.UpwindBiased(order=1), Nsigma=2, masking=M.SmoothIceMask())
         self.L, self.dx = L, L / Nx
         velocity = velocity or (lambda x, y: U * math.sin(math.pi * x / L))
         self.P.set("H", evaluate(self.g, "H", lambda x, y: background + 100 * math.exp(-((x - L / 4) / width) ** 2)))
@@ -103,7 +105,7 @@ def test_clipped_thickness_closes_the_volume_budget(backend):
 def test_basal_melt_acts_on_the_floating_part_only(backend):
     Nx, L, H0, m, dt = 8, 8e3, 500.0, 1e-6, 1e3
     g = M.RectilinearGrid(size=(Nx, 1), x=(0.0, L), y=(0.0, L / Nx), topology=("Bounded", "Periodic"), halo=(4, 4))
-    P = make(backend, g, Nsigma=2, grounding=M.SubgridGroundedFraction())
+    P = make(backend, g, advection=M.UpwindBiased(order=1), Nsigma=2, grounding=M.SubgridGroundedFraction())
     P.set("H", H0)
     P.set("bed", evaluate(g, "H", lambda x, y: -100.0 if x < L / 2 else -2000.0))
     P.compute_geometry()
@@ -115,13 +117,14 @@ def test_basal_melt_acts_on_the_floating_part_only(backend):
     np.testing.assert_allclose(dH, -dt * m * (1 - phi), rtol=1e-6)
 
 
-def seeded_shelf(cls, Nx=48, Ny=40, steps=4, dt=2e8):
+def seeded_shelf(cls, Nx=48, Ny=40, steps=4, dt=2e8, advection=None):
     """Four thickness steps of a seeded ice shelf over a sloping bed (grounded at x = 0, afloat downstream),
     Bounded in x and Periodic in y, with random velocities in both directions, the subgrid grounded fraction,
     sources, a coupled grounded melt and thin cells that the melt clips."""
     rng = np.random.default_rng(20261203)
     g = M.RectilinearGrid(size=(Nx, Ny), x=(0.0, Nx * 1e3), y=(0.0, Ny * 1e3), topology=("Bounded", "Periodic"), halo=(4, 4))
-    P = make(cls, g, Nsigma=2, grounding=M.SubgridGroundedFraction(), masking=M.SmoothIceMask())
+    P = make(cls, g, advection=advection or M.UpwindBiased(order=1), Nsigma=2, grounding=M.SubgridGroundedFraction(),
+             masking=M.SmoothIceMask())
     x = g.centers(0)
     H = 500 - 6 * x[None, :] / 1e3 + rng.uniform(0, 40, (Ny, Nx))
     H[rng.uniform(size=(Ny, Nx)) < 0.08] = 1.0
@@ -149,19 +152,89 @@ def test_seeded_shelf_clips_and_grounds(oracle_cls):
     assert np.any(out["phi"] == 1.0) and np.any(out["phi"] == 0.0)
 
 
+SCHEMES = {"upwind1": M.UpwindBiased(order=1), "upwind3": M.UpwindBiased(order=3), "weno5": M.WENO(order=5),
+           "weno5_bounded": M.WENO(order=5, bounds=(0.0, 1e5))}
+
+
 @pytest.mark.gpu
-def test_gpu_matches_the_oracle(oracle_cls, gpu_cls):
-    want, got = seeded_shelf(oracle_cls), seeded_shelf(gpu_cls)
+@pytest.mark.parametrize("scheme", list(SCHEMES))
+def test_gpu_matches_the_oracle(oracle_cls, gpu_cls, scheme):
+    want, got = seeded_shelf(oracle_cls, advection=SCHEMES[scheme]), seeded_shelf(gpu_cls, advection=SCHEMES[scheme])
     for k in want:
         scale = max(1.0, float(np.max(np.abs(want[k]))))
-        np.testing.assert_allclose(got[k], want[k], rtol=1e-12, atol=1e-12 * scale, err_msg=k)
+        np.testing.assert_allclose(got[k], want[k], rtol=1e-12, atol=1e-12 * scale, err_msg=f"{scheme} {k}")
+
+
+# ---- the reference's higher-order schemes (test/test_thickness.jl:29-73) ------------------------------------------
+@pytest.mark.parametrize("scheme", ["upwind1", "upwind3", "weno5", "weno5_bounded_inf"])
+def test_volume_is_conserved_by_every_scheme(backend, scheme):
+    """test/test_thickness.jl:31-37 for UpwindBiased(order = 1), UpwindBiased(order = 3), WENO(order = 5) and
+    WENO(order = 5, bounds = (0, Inf)): 32 steps at half the cell-crossing time conserve the volume to 1e-13."""
+    adv = SCHEMES.get(scheme) or M.WENO(order=5, bounds=(0.0, math.inf))
+    t = Transport(backend, background=100.0, advection=adv)
+    V0 = t.volume()
+    t.run(0.5 * t.timescale(), 32)
+    assert abs(t.volume() - V0) / V0 < 1e-13
+
+
+def test_bounded_weno_keeps_a_compact_bump_nonnegative_without_clipping(backend):
+    """test/test_thickness.jl:60-73: a 2 km bump on no background, 64 steps at a quarter of the cell-crossing time.
+    The bounded WENO stays non-negative and loses no volume to the clip (drift < 1e-12); the unbounded one
+    undershoots, and the clip changes its volume by more than 1e-9."""
+    drift = []
+    for adv in (M.WENO(order=5, bounds=(0.0, math.inf)), M.WENO(order=5)):
+        t = Transport(backend, width=2e3, advection=adv)
+        V0 = t.volume()
+        t.run(0.25 * t.timescale(), 64)
+        assert np.min(t.P.get("H")) >= 0
+        drift.append(abs(t.volume() - V0) / V0)
+    assert drift[0] < 1e-12
+    assert drift[1] > 1e-9
+
+
+def test_bounded_weno_needs_a_halo_of_four(backend):
+    """test/test_thickness.jl:70-71 (check_advection_halo, src/Models/ice_sheet_model.jl:131-135): the default bounded
+    WENO(order = 5) refuses a grid whose halo is 3 (Oceananigans' default); UpwindBiased(order = 1) steps it."""
+    t = Transport(backend, halo=3, advection=M.WENO(order=5, bounds=(0.0, 1e5)))
+    with pytest.raises(ValueError):
+        t.P.step_thickness(1.0)
+    t.P.set_thickness_advection(M.UpwindBiased(order=1))
+    t.P.step_thickness(1.0)
+
+
+def test_default_advection_is_the_bounded_weno(backend):
+    """A new problem transports the thickness with the reference's default for the SSA and the DIVA,
+    WENO(order = 5, bounds = (0, 1e5)) (src/Models/ice_sheet_model.jl:123): the same result as setting it."""
+    out = []
+    for adv in (None, M.default_thickness_advection()):
+        t = Transport(backend, width=2e3)
+        if adv is None:
+            t.P.close()
+            t.P = make(backend, t.g, Nsigma=2, masking=M.SmoothIceMask())
+            t.P.set("H", evaluate(t.g, "H", lambda x, y: 100 * math.exp(-((x - 16e3) / 2e3) ** 2)))
+            t.P.set("bed", 0.0)
+            t.P.compute_geometry()
+            t.P.set("u", evaluate(t.g, "u", lambda x, y: 1e-6 * math.sin(math.pi * x / 64e3)))
+            t.P.set("v", 0.0)
+        else:
+            t.P.set_thickness_advection(adv)
+        t.run(0.25 * t.timescale(), 8)
+        out.append(t.P.get("H"))
+    assert np.array_equal(out[0], out[1])
+
+
+def test_advection_schemes_are_refused_outside_the_reference(backend):
+    P = Transport(backend).P
+    for bad in (M.UpwindBiased(order=2), M.UpwindBiased(order=5), M.WENO(order=3), M.WENO(order=5, bounds=(1.0, 0.0))):
+        with pytest.raises(ValueError):
+            P.set_thickness_advection(bad)
 
 
 @pytest.mark.gpu
 def test_gpu_conserves_volume_at_2048(gpu_cls):
     N, L = 2048, 2048e3
     g = M.RectilinearGrid(size=(N, N), x=(0.0, L), y=(0.0, L), topology=("Periodic", "Periodic"), halo=(4, 4))
-    P = make(gpu_cls, g, Nsigma=2, masking=M.SmoothIceMask())
+    P = make(gpu_cls, g, advection=M.UpwindBiased(order=1), Nsigma=2, masking=M.SmoothIceMask())
     P.set("H", evaluate(g, "H", lambda x, y: 800 + 200 * math.sin(2 * math.pi * x / L) * math.cos(4 * math.pi * y / L)))
     P.set("bed", 0.0)
     P.compute_geometry()
