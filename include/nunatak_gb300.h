@@ -222,7 +222,13 @@ typedef struct nk_solver_desc {
 #define NK_FIELD_BASAL_TEMPERATE_FRACTION 40
 #define NK_FIELD_BASAL_HEAT_FLUX          41
 #define NK_FIELD_STRAIN_HEATING           42
-#define NK_FIELD_COUNT         43
+/* The partial-cell front (nk_set_front; PartialCellFront, src/Models/partial_cell_front.jl:1-66), Center-Center, zero
+ * at first: the ice thickness H^r of the partial front cells (geometry.front_thickness), the thickness removed by
+ * calving (calved_thickness) and the region MaximumExtentCalving keeps ice in (extent, positive inside). */
+#define NK_FIELD_FRONT_THICKNESS  43
+#define NK_FIELD_CALVED_THICKNESS 44
+#define NK_FIELD_CALVING_EXTENT   45
+#define NK_FIELD_COUNT         46
 
 typedef struct nk_solve_stats {
     int32_t status;                   /* nk_status of the solve */
@@ -352,6 +358,42 @@ typedef struct nk_advection_desc {
     double lower, upper;              /* the bounds (m), lower < upper (either may be infinite) */
 } nk_advection_desc;
 nk_status nk_set_thickness_advection(nk_problem* problem, const nk_advection_desc* advection);
+
+/* Calving law of a partial-cell front, src/Models/calving.jl:1-150. */
+#define NK_CALVING_NONE                 0
+#define NK_CALVING_THICKNESS_THRESHOLD  1   /* ThicknessThresholdCalving(thickness) */
+#define NK_CALVING_EIGEN                2   /* EigenCalving(coefficient) */
+#define NK_CALVING_VON_MISES            3   /* VonMisesCalving(stress_threshold, floating_stress_threshold) */
+#define NK_CALVING_FRONT_VELOCITY       4   /* FrontVelocityCalving(front_velocity) */
+#define NK_CALVING_MAXIMUM_EXTENT       5   /* MaximumExtentCalving(extent): NK_FIELD_CALVING_EXTENT */
+
+/* PartialCellFront(grid; passes, calving) as the masking of a model (src/Models/partial_cell_front.jl:1-66).  With
+ * `enabled`, the ice mask is the prognostic 0/1 flag of full cells: nk_compute_geometry no longer computes it from
+ * H, only full cells enter the stress balance, and nk_step_thickness moves thickness only between full cells (the
+ * scheme's flux), upwind from a full cell into a front cell and not out of a front cell, applies the sources to full
+ * cells only, and after its last stage advances the front (advance_front!, :167-195): empties full cells that
+ * drained, updates the front thickness H^r, fills front cells that reached it and spills their excess volume into
+ * empty neighbours up to `passes` times, calves marine front cells under the calving law (:276-327), and applies
+ * the sources of the step to the partial cells and to the cells that filled or calved.  A time-dependent front
+ * velocity w(t) is set before each step with a new nk_front_desc. */
+typedef struct nk_front_desc {
+    int32_t enabled;                  /* 1: PartialCellFront masking; 0: the SmoothIceMask / no masking of the physics */
+    int32_t passes;                   /* overflow passes per time step (the reference's default 4) */
+    int32_t calving;                  /* NK_CALVING_* */
+    int32_t reserved;                 /* 0 */
+    double thickness;                 /* ThicknessThresholdCalving: calving below this thickness (m) */
+    double coefficient;               /* EigenCalving: K (m s) */
+    double stress_threshold;          /* VonMisesCalving: sigma_max of grounded ice (Pa) */
+    double floating_stress_threshold; /* VonMisesCalving: sigma_max of floating ice (Pa) */
+    double front_velocity;            /* FrontVelocityCalving: w (m s^-1), positive for advance */
+} nk_front_desc;
+nk_status nk_set_front(nk_problem* problem, const nk_front_desc* front);
+/* initialize_front! (src/Models/partial_cell_front.jl:80-92), which set! calls when it sets the thickness: every cell
+ * holding ice is full (mask 1, else 0) and no cell is partial (H^r = 0).  NK_BAD_ARGUMENT without a front. */
+nk_status nk_initialize_front(nk_problem* problem);
+/* advance_front!(front, model, dt) alone (the end of nk_step_thickness's last stage), then the geometry.
+ * NK_BAD_ARGUMENT without a front or when dt is not finite and positive. */
+nk_status nk_advance_front(nk_problem* problem, double dt);
 
 /* The EnthalpyThermodynamics constants of the energy step (src/Thermodynamics/enthalpy_thermodynamics.jl:92-104,
  * defaults 2.1, 2009, 3.34e5, 7.9e-8, 273.15, 223.15, 1e-3, 1, 1e-3, 1, 0.01, 0.05 / year, coupling on). */

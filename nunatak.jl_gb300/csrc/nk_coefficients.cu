@@ -297,7 +297,7 @@ __global__ void k_geometry(GeometryView v) {
         double rig = v.rho_i * v.gacc, rwg = v.rho_w * v.gacc;
         v.N[k] = fmax(rig * H + rwg * fmin(b, 0.0), 0.0);
         double t = fmin(fmax((H - v.mask_min) / v.mask_trans, 0.0), 1.0);
-        v.mu[k] = t * t * (3 - 2 * t);
+        if (!v.front) v.mu[k] = t * t * (3 - 2 * t);   // a partial-cell front's flag is prognostic
         if (v.grounding) {
             double fc = f(i, j);
             double fe = (fc + f(i + 1, j)) / 2, fw = (fc + f(i - 1, j)) / 2, fn = (fc + f(i, j + 1)) / 2, fs = (fc + f(i, j - 1)) / 2;
@@ -529,25 +529,35 @@ __global__ void k_thickness_stage(ThicknessView v, double dtau, int final_stage)
     const double* __restrict__ Hs = v.Hs;
     const bool bounded = v.scheme == NK_ADVECTION_WENO && v.bounded;
     auto limited = [&](double h, int k) { return bounded ? Hs[k] + v.theta[k] * (h - Hs[k]) : h; };
+    // with a partial-cell front (front_flux_x / front_flux_y, partial_cell_front.jl:114-132): the scheme's flux between
+    // full cells, the upwind flux out of a full cell into a front cell, nothing out of a front cell
+    auto full = [&](int k) { return !v.mu || v.mu[k] > 0; };
     auto xflux = [&](int f) {
         if (g.peripheral_fc(f, j)) return 0.0;
         double u = v.x[g.u_idx(f, j)].x, s[5];
+        int kw = g.c_idx(f - 1, j), ke = g.c_idx(f, j);
+        bool west = full(kw), eastc = full(ke);
+        if (!(west && eastc)) return (west || eastc) ? g.dyc[j] * (west ? fmax(u, 0.0) * Hs[kw] : fmin(u, 0.0) * Hs[ke]) : 0.0;
         bool east = u > 0;
         stencil_x(g, Hs, f, j, east, s);
-        double h = limited(face_value(v, s), g.c_idx(east ? f - 1 : f, j));
+        double h = limited(face_value(v, s), east ? kw : ke);
         return g.dyc[j] * (u * h);
     };
     auto yflux = [&](int f) {
         if (g.peripheral_cf(i, f)) return 0.0;
         double w = v.x[g.v_idx(i, f)].y, s[5];
+        int ks = g.c_idx(i, f - 1), kn = g.c_idx(i, f);
+        bool south = full(ks), northc = full(kn);
+        if (!(south && northc)) return (south || northc) ? g.dxc[i] * (south ? fmax(w, 0.0) * Hs[ks] : fmin(w, 0.0) * Hs[kn]) : 0.0;
         bool north = w > 0;
         stencil_y(g, Hs, i, f, north, s);
-        double h = limited(face_value(v, s), g.c_idx(i, north ? f - 1 : f));
+        double h = limited(face_value(v, s), north ? ks : kn);
         return g.dxc[i] * (w * h);
     };
     int c = g.idx(i, j);
     double m = v.grounding ? (1 - v.phi[c]) * v.melt[c] : v.melt[c];
     double S = v.smb[c] - m - (v.coupled ? v.gmelt[c] : 0.0);
+    if (!full(c)) S = 0.0;   // sources on full cells only (ice_source_mask)
     double div = (xflux(i + 1) - xflux(i) + yflux(j + 1) - yflux(j)) / g.Az_cc(i, j);
     double Hstar = v.H0[c] + dtau * (S - div);
     v.H[c] = 0.0 < Hstar ? Hstar : 0.0;

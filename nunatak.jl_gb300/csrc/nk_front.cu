@@ -1,0 +1,357 @@
+// nk_front.cu — the partial-cell calving front (PartialCellFront, src/Models/partial_cell_front.jl) and its calving
+// laws (src/Models/calving.jl) as one thread per cell.
+//
+// μ is the prognostic 0/1 flag of full cells and Hʳ the ice thickness of a partial front cell, which covers the
+// fraction H / Hʳ of its area.  A neighbour outside a Bounded direction is inactive (never full, empty or a donor);
+// a periodic neighbour wraps.  Every kernel writes only its own cell.  Where a kernel reads neighbours that another
+// thread of the same launch may rewrite (the overflow passes), it reads a snapshot taken before the launch.
+#include "nk_kernels.cuh"
+
+namespace nk {
+
+namespace {
+
+// the four neighbours in the reference's order: west, east, south, north
+__device__ __forceinline__ int DI(int d) { return d == 0 ? -1 : (d == 1 ? 1 : 0); }
+__device__ __forceinline__ int DJ(int d) { return d == 2 ? -1 : (d == 3 ? 1 : 0); }
+
+__device__ __forceinline__ bool inactive(const DevGrid<double>& g, int i, int j) { return g.out_x(i) || g.out_y(j); }
+__device__ __forceinline__ bool full_at(const double* mu, int k) { return mu[k] > 0; }
+// full_neighbor (:102): full and active
+__device__ __forceinline__ bool full_neighbor(const DevGrid<double>& g, const double* mu, int i, int j) {
+    return !inactive(g, i, j) && full_at(mu, g.c_idx(i, j));
+}
+// empty_cell (:103): not full, no ice, active
+__device__ __forceinline__ bool empty_at(const DevGrid<double>& g, const double* mu, const double* H, int i, int j) {
+    if (inactive(g, i, j)) return false;
+    int k = g.c_idx(i, j);
+    return !full_at(mu, k) && H[k] <= 0;
+}
+
+// interior_u / interior_v with the front's flag as the ice mask (strain_rates.jl:5-6, smooth_ice_mask.jl:72-73)
+__device__ __forceinline__ double mu_u(const FrontView& v, int i, int j) {
+    const DevGrid<double>& g = v.g;
+    if (g.peripheral_fc(i, j) || (v.mu[g.c_idx(i - 1, j)] + v.mu[g.c_idx(i, j)]) == 0.0) return 0.0;
+    return v.x[g.u_idx(i, j)].x;
+}
+__device__ __forceinline__ double mu_v(const FrontView& v, int i, int j) {
+    const DevGrid<double>& g = v.g;
+    if (g.peripheral_cf(i, j) || (v.mu[g.c_idx(i, j - 1)] + v.mu[g.c_idx(i, j)]) == 0.0) return 0.0;
+    return v.x[g.v_idx(i, j)].y;
+}
+// strain_rate_xy with the flag as the mask (strain_rates.jl:14-17)
+__device__ __forceinline__ double mu_strain_xy(const FrontView& v, int i, int j) {
+    const DevGrid<double>& g = v.g;
+    double dudy = (mu_u(v, i, j) - mu_u(v, i, j - 1)) / g.dyf[j];
+    double dvdx = (mu_v(v, i, j) - mu_v(v, i - 1, j)) / g.dxf[i];
+    double e = (dudy + dvdx) / 2;
+    return g.peripheral_ff(i, j) ? v.wall_factor * e : e;
+}
+// the wall-masked strain rates of the viscosity (no ice mask): effective_strain_rate² (strain_rates.jl:27-32)
+__device__ __forceinline__ double wall_u(const FrontView& v, int i, int j) {
+    return v.g.peripheral_fc(i, j) ? 0.0 : v.x[v.g.u_idx(i, j)].x;
+}
+__device__ __forceinline__ double wall_v(const FrontView& v, int i, int j) {
+    return v.g.peripheral_cf(i, j) ? 0.0 : v.x[v.g.v_idx(i, j)].y;
+}
+__device__ __forceinline__ double wall_strain_xy2(const FrontView& v, int i, int j) {
+    const DevGrid<double>& g = v.g;
+    double dudy = (wall_u(v, i, j) - wall_u(v, i, j - 1)) / g.dyf[j];
+    double dvdx = (wall_v(v, i, j) - wall_v(v, i - 1, j)) / g.dxf[i];
+    double e = (dudy + dvdx) / 2;
+    e = g.peripheral_ff(i, j) ? v.wall_factor * e : e;
+    return e * e;
+}
+__device__ double effective_strain_rate2(const FrontView& v, int i, int j) {
+    const DevGrid<double>& g = v.g;
+    double exx = (wall_u(v, i + 1, j) - wall_u(v, i, j)) / g.dxc[i];
+    double eyy = (wall_v(v, i, j + 1) - wall_v(v, i, j)) / g.dyc[j];
+    double a = (wall_strain_xy2(v, i, j) + wall_strain_xy2(v, i + 1, j)) / 2;
+    double b = (wall_strain_xy2(v, i, j + 1) + wall_strain_xy2(v, i + 1, j + 1)) / 2;
+    return exx * exx + eyy * eyy + exx * eyy + (a + b) / 2;
+}
+
+// principal_strain_rates (calving.jl:144-152) with the velocities masked by the flag
+__device__ void principal_strain_rates(const FrontView& v, int i, int j, double& e1, double& e2) {
+    const DevGrid<double>& g = v.g;
+    double exx = (mu_u(v, i + 1, j) - mu_u(v, i, j)) / g.dxc[i];
+    double eyy = (mu_v(v, i, j + 1) - mu_v(v, i, j)) / g.dyc[j];
+    double exy = ((mu_strain_xy(v, i, j) + mu_strain_xy(v, i + 1, j)) / 2 + (mu_strain_xy(v, i, j + 1) + mu_strain_xy(v, i + 1, j + 1)) / 2) / 2;
+    double eb = (exx + eyy) / 2;
+    double r = sqrt(((exx - eyy) / 2) * ((exx - eyy) / 2) + exy * exy + v.eps0 * v.eps0);
+    e1 = eb + r;
+    e2 = eb - r;
+}
+
+// front_flow_speed (calving.jl:176-181): the larger face speed along each axis
+__device__ double front_flow_speed(const FrontView& v, int i, int j) {
+    double ut = fmax(fabs(mu_u(v, i, j)), fabs(mu_u(v, i + 1, j)));
+    double vt = fmax(fabs(mu_v(v, i, j)), fabs(mu_v(v, i, j + 1)));
+    double e = v.eps0 * v.g.dxc[i];
+    return sqrt(ut * ut + vt * vt + e * e);
+}
+
+// calving_rate of a full cell (calving.jl:154-190)
+__device__ double calving_rate(const FrontView& v, int i, int j) {
+    int k = v.g.c_idx(i, j);
+    if (v.law == NK_CALVING_EIGEN) {
+        double e1, e2;
+        principal_strain_rates(v, i, j, e1, e2);
+        return v.coefficient * fmax(e1, 0.0) * fmax(e2, 0.0);
+    }
+    if (v.law == NK_CALVING_VON_MISES) {
+        double e1, e2;
+        principal_strain_rates(v, i, j, e1, e2);
+        double n = v.n, e0 = v.eps0;
+        double et2 = (fmax(e1, 0.0) * fmax(e1, 0.0) + fmax(e2, 0.0) * fmax(e2, 0.0)) / 2;
+        double ee2 = effective_strain_rate2(v, i, j) + e0 * e0;
+        double Hi = v.H[k];
+        double eta = v.coef[k].x / (Hi > 0 ? Hi : 1.0);
+        double smax = v.phi[k] * v.stress_threshold + (1 - v.phi[k]) * v.floating_stress_threshold;
+        double B = 2 * eta * pow(ee2, (n - 1) / (2 * n));
+        double sig = sqrt(3.0) * B * et2 * pow(et2 + e0 * e0, (1 - 2 * n) / (2 * n));
+        return front_flow_speed(v, i, j) * sig / smax;
+    }
+    if (v.law == NK_CALVING_FRONT_VELOCITY) {
+        double c = fmax(front_flow_speed(v, i, j) - v.front_velocity, 0.0);
+        return (1 - v.phi[k]) * c;
+    }
+    return 0.0;
+}
+
+// front_ice_thickness (:331): its own thickness when full or not yet given an Hʳ
+__device__ __forceinline__ double front_ice_thickness(const FrontView& v, int k) {
+    return (full_at(v.mu, k) || v.Hr[k] <= 0) ? v.H[k] : v.Hr[k];
+}
+
+// remove_front_fraction! (:353-368) on the calling thread's own cell; returns the part of g beyond its ice
+__device__ double remove_front_fraction(const FrontView& v, int k, double gfrac) {
+    double Hi = v.H[k], Hf = front_ice_thickness(v, k);
+    bool calves = (gfrac > 0) && (Hi > 0);
+    double Hn = fmax(Hi - gfrac * Hf, 0.0);
+    double a = Hf > 0 ? Hi / (Hf > 0 ? Hf : 1.0) : 0.0;
+    if (calves) {
+        v.calved[k] += Hi - Hn;
+        v.H[k] = Hn;
+        v.Hr[k] = Hn > 0 ? Hf : 0.0;
+        v.mu[k] = 0.0;
+    }
+    return calves ? fmax(gfrac - a, 0.0) : 0.0;
+}
+
+}  // namespace
+
+// initialize_front! (:80-92)
+__global__ void k_initialize_front(FrontView v) {
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= v.g.Nx || j >= v.g.Ny) return;
+    int k = v.g.idx(i, j);
+    v.mu[k] = v.H[k] > 0 ? 1.0 : 0.0;
+    v.Hr[k] = 0.0;
+}
+
+// _empty_drained_cells! (:197-200)
+__global__ void k_front_drained(FrontView v) {
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= v.g.Nx || j >= v.g.Ny) return;
+    int k = v.g.idx(i, j);
+    if (v.H[k] <= 0) v.mu[k] = 0.0;
+}
+
+// _compute_reference_thickness! (:206-230): the mean thickness of the full neighbours flowing in; otherwise the kept
+// Hʳ, the mean of all full neighbours, or H.  Reads only its own Hʳ.
+__global__ void k_front_reference(FrontView v) {
+    const DevGrid<double>& g = v.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int k = g.idx(i, j);
+    bool inflow[4] = {v.x[g.u_idx(i, j)].x > 0, v.x[g.u_idx(i + 1, j)].x < 0, v.x[g.v_idx(i, j)].y > 0, v.x[g.v_idx(i, j + 1)].y < 0};
+    double Sin = 0, Sf = 0;
+    int nin = 0, nf = 0;
+#pragma unroll
+    for (int d = 0; d < 4; ++d) {
+        int a = i + DI(d), b = j + DJ(d);
+        if (!full_neighbor(g, v.mu, a, b)) continue;
+        double Hn = v.H[g.c_idx(a, b)];
+        Sf += Hn;
+        ++nf;
+        if (inflow[d]) { Sin += Hn; ++nin; }
+    }
+    // the reference sums the four neighbours in the order west, east, south, north with zeros for the others
+    double Hi = v.H[k];
+    double Hs = nf > 0 ? Sf / (double)(nf > 1 ? nf : 1) : Hi;
+    double Hp = Hi > 0 ? (v.Hr[k] > 0 ? v.Hr[k] : Hs) : 0.0;
+    double Hbar = nin > 0 ? Sin / (double)(nin > 1 ? nin : 1) : Hp;
+    v.Hr[k] = full_at(v.mu, k) ? 0.0 : Hbar;
+}
+
+// _fill_front_cells! (:235-251) from the snapshots H_in, mu_in
+__global__ void k_front_fill(FrontView v) {
+    const DevGrid<double>& g = v.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int k = g.idx(i, j);
+    int n = 0;
+#pragma unroll
+    for (int d = 0; d < 4; ++d) n += empty_at(g, v.mu_in, v.H_in, i + DI(d), j + DJ(d)) ? 1 : 0;
+    double Hi = v.H_in[k], Hri = v.Hr[k];
+    bool fills = !full_at(v.mu_in, k) && (Hri > 0) && (Hi >= Hri);
+    bool spills = fills && n > 0;
+    v.O[k] = spills ? (Hi - Hri) * g.Az_cc(i, j) / (double)(n > 1 ? n : 1) : 0.0;
+    v.H[k] = spills ? Hri : Hi;
+    if (fills) v.mu[k] = 1.0;
+}
+
+// _receive_overflow! (:257-268): every donor counted each of its empty neighbours; H_in is the thickness after the fill
+__global__ void k_front_receive(FrontView v) {
+    const DevGrid<double>& g = v.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int k = g.idx(i, j);
+    bool receives = empty_at(g, v.mu, v.H_in, i, j);
+    double V = 0, S = 0;
+    int n = 0;
+#pragma unroll
+    for (int d = 0; d < 4; ++d) {
+        int a = i + DI(d), b = j + DJ(d);
+        if (inactive(g, a, b)) continue;
+        int c = g.c_idx(a, b);
+        V += v.O[c];
+        if (v.O[c] > 0) { S += v.H_in[c]; ++n; }
+    }
+    if (receives) v.H[k] = V / g.Az_cc(i, j);
+    if (receives && n > 0) v.Hr[k] = S / (double)(n > 1 ? n : 1);
+}
+
+// _compute_retreat_fraction! (:311-322) with front_length (:334-343) and retreat_fraction (calving.jl:212-227), from
+// the state before any cell retreats
+__global__ void k_calve_fraction(FrontView v, double dt) {
+    const DevGrid<double>& g = v.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int k = g.idx(i, j);
+    double dx = g.dxc[i], dy = g.dyc[j];
+    auto ocean = [&](int a, int b, double len) { return (empty_at(g, v.mu, v.H, a, b) && v.bed[g.c_idx(a, b)] < 0) ? len : 0.0; };
+    double lw = ocean(i - 1, j, dy), le = ocean(i + 1, j, dy), ls = ocean(i, j - 1, dx), ln = ocean(i, j + 1, dx);
+    double r = 0.0;
+    if (v.H[k] > 0 && (lw + le + ls + ln > 0)) {
+        double Hf = front_ice_thickness(v, k);
+        if (v.law == NK_CALVING_THICKNESS_THRESHOLD) {
+            r = Hf < v.thickness ? 1.0 : 0.0;
+        } else if (v.law == NK_CALVING_MAXIMUM_EXTENT) {
+            r = v.extent[k] > 0 ? 0.0 : 1.0;
+        } else {
+            double ub = fabs((mu_u(v, i, j) + mu_u(v, i + 1, j)) / 2);
+            double vb = fabs((mu_v(v, i, j) + mu_v(v, i, j + 1)) / 2);
+            double speed = sqrt(ub * ub + vb * vb);
+            double l2 = (le - lw) * (le - lw) + (ln - ls) * (ln - ls);
+            double lv = l2 > 0 ? sqrt(l2 > 0 ? l2 : 1.0) : lw + le + ls + ln;
+            double lu = (ub * (lw + le) + vb * (ls + ln)) / (speed > 0 ? speed : 1.0);
+            double l = speed > 0 ? lu : lv;
+            // front_calving_rate (calving.jl:197-206): a partial cell takes the mean rate of its full neighbours
+            double c;
+            if (full_at(v.mu, k)) {
+                c = calving_rate(v, i, j);
+            } else {
+                double S = 0;
+                int n = 0;
+#pragma unroll
+                for (int d = 0; d < 4; ++d)
+                    if (full_neighbor(g, v.mu, i + DI(d), j + DJ(d))) { S += calving_rate(v, i + DI(d), j + DJ(d)); ++n; }
+                c = S / (double)(n > 1 ? n : 1);
+            }
+            r = fmin(1.0, c * dt * l / g.Az_cc(i, j));
+        }
+    }
+    v.f[k] = r;
+}
+
+// _retreat_front_cells! (:371-375): f becomes the area of retreat left once the cell is empty (rate laws only)
+__global__ void k_calve_retreat(FrontView v) {
+    const DevGrid<double>& g = v.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int k = g.idx(i, j);
+    double r = remove_front_fraction(v, k, v.f[k]);
+    bool removal = v.law == NK_CALVING_THICKNESS_THRESHOLD || v.law == NK_CALVING_MAXIMUM_EXTENT;
+    v.f[k] = (removal ? 0.0 : r) * g.Az_cc(i, j);
+}
+
+// _share_residual_retreat! (:379-385): among the neighbours that hold ice
+__global__ void k_calve_share(FrontView v) {
+    const DevGrid<double>& g = v.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int k = g.idx(i, j);
+    int n = 0;
+#pragma unroll
+    for (int d = 0; d < 4; ++d) {
+        int a = i + DI(d), b = j + DJ(d);
+        n += (!inactive(g, a, b) && v.H[g.c_idx(a, b)] > 0) ? 1 : 0;
+    }
+    v.share[k] = n > 0 ? v.f[k] / (double)(n > 1 ? n : 1) : 0.0;
+}
+
+// _receive_residual_retreat! (:390-397): what the receiving cell cannot take is not passed on
+__global__ void k_calve_receive(FrontView v) {
+    const DevGrid<double>& g = v.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int k = g.idx(i, j);
+    double A = 0;
+#pragma unroll
+    for (int d = 0; d < 4; ++d) {
+        int a = i + DI(d), b = j + DJ(d);
+        A += inactive(g, a, b) ? 0.0 : v.share[g.c_idx(a, b)];
+    }
+    remove_front_fraction(v, k, A / g.Az_cc(i, j));
+}
+
+// _force_front_cells! (:271-286): the sources of the step on partial cells and on cells that filled or calved
+__global__ void k_front_force(FrontView v, double dt) {
+    const DevGrid<double>& g = v.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int k = g.idx(i, j);
+    double Hi = v.H[k], Hri = v.Hr[k];
+    double m = v.grounding ? (1 - v.phi[k]) * v.melt[k] : v.melt[k];
+    double S = v.smb[k] - m - (v.coupled ? v.gmelt[k] : 0.0);
+    bool full = full_at(v.mu, k);
+    bool forced = (Hi > 0) && (Hri > 0);
+    double Hf = full ? Hi : Hri;
+    bool melted = forced && (Hf + S * dt <= 0);
+    double Hn = full ? Hi + S * dt : Hi / (Hri > 0 ? Hri : 1.0) * (Hri + S * dt);
+    if (melted) v.clipped[k] += -Hn;
+    v.H[k] = melted ? 0.0 : (forced ? Hn : Hi);
+    v.Hr[k] = (melted || full) ? 0.0 : (forced ? Hri + S * dt : Hri);
+    if (melted) v.mu[k] = 0.0;
+}
+
+void launch_initialize_front(const FrontView& v, cudaStream_t s) {
+    LaunchDims d = dims2d(v.g.Nx, v.g.Ny);
+    k_initialize_front<<<d.grid, d.block, 0, s>>>(v); count_launch();
+}
+
+// advance_front!(front, model, Δt), partial_cell_front.jl:167-195
+void launch_advance_front(const FrontView& v, int passes, double dt, size_t plane, cudaStream_t s) {
+    LaunchDims d = dims2d(v.g.Nx, v.g.Ny);
+    const size_t bytes = plane * sizeof(double);
+    k_front_drained<<<d.grid, d.block, 0, s>>>(v); count_launch();
+    k_front_reference<<<d.grid, d.block, 0, s>>>(v); count_launch();
+    for (int p = 0; p < passes; ++p) {
+        cudaMemcpyAsync(v.H_in, v.H, bytes, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(v.mu_in, v.mu, bytes, cudaMemcpyDeviceToDevice, s);
+        k_front_fill<<<d.grid, d.block, 0, s>>>(v); count_launch();
+        cudaMemcpyAsync(v.H_in, v.H, bytes, cudaMemcpyDeviceToDevice, s);
+        k_front_receive<<<d.grid, d.block, 0, s>>>(v); count_launch();
+    }
+    if (v.law != NK_CALVING_NONE) {
+        k_calve_fraction<<<d.grid, d.block, 0, s>>>(v, dt); count_launch();
+        k_calve_retreat<<<d.grid, d.block, 0, s>>>(v); count_launch();
+        k_calve_share<<<d.grid, d.block, 0, s>>>(v); count_launch();
+        k_calve_receive<<<d.grid, d.block, 0, s>>>(v); count_launch();
+    }
+    k_front_force<<<d.grid, d.block, 0, s>>>(v, dt); count_launch();
+}
+
+}  // namespace nk

@@ -169,6 +169,7 @@ struct GeometryView {
     int grounding, gl_stress, use_mask;
     double mask_min, mask_trans;
     const double2* ud = nullptr;      // prescribed (u, v) per face, NaN where free: the right-hand side there
+    int front = 0;                    // a partial-cell front: the ice mask is its prognostic flag, not recomputed
 };
 void launch_geometry(const GeometryView& v, cudaStream_t s);
 void launch_rate_factor(const DevGrid<double>& g, const SigmaTable& sig, int plane, const double* H, const double* T, double* A,
@@ -188,7 +189,24 @@ struct ThicknessView {
     int scheme, order, bounded;       // nk_advection_desc
     double lower, upper;
     double* theta;                    // the bounds-preserving limiter per cell (bounded WENO only)
+    const double* mu = nullptr;       // a partial-cell front's flag of full cells (null without a front)
 };
+
+// ---- the partial-cell front and calving (nk_front.cu) ------------------------------------------------------------
+struct FrontView {
+    DevGrid<double> g;
+    double* H; double* mu; double* Hr; double* O; double* calved; double* clipped;
+    double* H_in; double* mu_in;      // snapshots read by the overflow passes
+    double* f; double* share;         // calving: retreat fraction, then the residual area shared among neighbours
+    const double2* x; const double* bed; const double* phi; const double4* coef; const double* extent;
+    const double* smb; const double* melt; const double* gmelt;
+    int grounding, coupled, law;
+    double thickness, coefficient, stress_threshold, floating_stress_threshold, front_velocity;
+    double n, eps0, wall_factor;
+};
+void launch_initialize_front(const FrontView& v, cudaStream_t s);
+// advance_front!: the whole sequence of its kernels (with the snapshot copies of the passes) on stream s
+void launch_advance_front(const FrontView& v, int passes, double dt, size_t plane, cudaStream_t s);
 void launch_thickness_limiter(const ThicknessView& v, cudaStream_t s);
 void launch_thickness_stage(const ThicknessView& v, double dtau, int final_stage, cudaStream_t s);
 

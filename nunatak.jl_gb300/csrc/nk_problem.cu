@@ -205,6 +205,9 @@ struct nk_problem {
     // the thickness advection of nk_step_thickness: the reference's default for the SSA and the DIVA,
     // WENO(order = 5, bounds = (0, 1e5)) (default_thickness_advection, src/Models/ice_sheet_model.jl:123)
     nk_advection_desc advection{NK_ADVECTION_WENO, 5, 1, 0, 0.0, 1e5};
+    // a partial-cell front (nk_set_front): its settings and planes (ensure_front)
+    nk_front_desc front{0, 4, NK_CALVING_NONE, 0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    double* front_buf = nullptr;
     std::vector<double> sig_dz, sig_w2, sig_zc, sig_w1, sig_zf;
 
     // coarse levels
@@ -1035,6 +1038,7 @@ struct FieldLoc {
     bool thermal = false;     // the enthalpy or the water fraction (allocated on first use, sigma layout only)
     bool transport = false;   // a source or the clip of the thickness step (allocated on first use)
     bool energy = false;      // a state field or diagnostic of the energy step (allocated on first use)
+    bool front = false;       // a field of the partial-cell front (allocated on first use)
 };
 
 static const int ENERGY_PLANES_2D = 7;   // the energy step's Center-Center planes before Φ
@@ -1107,6 +1111,12 @@ static FieldLoc field_loc(nk_problem* P, int id) {
             f.planes = P->Ns;
             f.energy = true;
             break;
+        case NK_FIELD_FRONT_THICKNESS:
+        case NK_FIELD_CALVED_THICKNESS:
+        case NK_FIELD_CALVING_EXTENT:
+            cc(P->front_buf ? P->front_buf + (size_t)(id - NK_FIELD_FRONT_THICKNESS) * P->plane : nullptr);
+            f.front = true;
+            break;
         default: break;
     }
     return f;
@@ -1141,6 +1151,18 @@ static void ensure_transport(nk_problem* P) {
     size_t bytes = TRANSPORT_PLANES * P->plane * sizeof(double);
     NK_CUDA(cudaMalloc((void**)&P->transport, bytes));
     NK_CUDA(cudaMemsetAsync(P->transport, 0, bytes, P->stream));
+}
+
+// The partial-cell front's planes (zero at first): Hʳ, the calved thickness and the calving extent (the fields
+// NK_FIELD_FRONT_THICKNESS .. NK_FIELD_CALVING_EXTENT), then the overflow, two snapshots of H and μ and the two
+// calving scratch planes.  No graph reads them.
+static const int FRONT_PLANES = 8;
+static void ensure_front(nk_problem* P) {
+    if (P->front_buf) return;
+    if (P->async_pending) bad("an asynchronous solve is pending (nk_problem_wait first)");
+    size_t bytes = FRONT_PLANES * P->plane * sizeof(double);
+    NK_CUDA(cudaMalloc((void**)&P->front_buf, bytes));
+    NK_CUDA(cudaMemsetAsync(P->front_buf, 0, bytes, P->stream));
 }
 
 // The prescribed-velocity pairs, all NaN (free) at first.  Graphs captured before hold no pointer to them and
@@ -1354,6 +1376,7 @@ nk_status nk_problem_destroy(nk_problem* P) {
     if (P->thermal) cudaFree(P->thermal);
     if (P->transport) cudaFree(P->transport);
     if (P->energy) cudaFree(P->energy);
+    if (P->front_buf) cudaFree(P->front_buf);
     if (P->stream) cudaStreamDestroy(P->stream);
     delete P;
     return NK_OK;
@@ -1384,6 +1407,10 @@ nk_status nk_problem_set_field(nk_problem* P, int32_t id, const double* host, in
         }
         if (f.energy) {
             ensure_energy(P);
+            f = field_loc(P, id);
+        }
+        if (f.front) {
+            ensure_front(P);
             f = field_loc(P, id);
         }
         if (!f.base) bad("unknown field id or field not held by this problem");
@@ -1420,6 +1447,10 @@ nk_status nk_problem_get_field(const nk_problem* Pc, int32_t id, double* host, i
             ensure_energy(P);
             f = field_loc(P, id);
         }
+        if (f.front) {
+            ensure_front(P);
+            f = field_loc(P, id);
+        }
         if (!f.base) bad("unknown field id or field not held by this problem");
         if (count != (int64_t)f.nx * f.ny * f.planes) bad("field size mismatch");
         copy_out(P, f, host);
@@ -1448,6 +1479,10 @@ nk_status nk_problem_set_field_parent(nk_problem* P, int32_t id, const double* p
         }
         if (f.energy) {
             ensure_energy(P);
+            f = field_loc(P, id);
+        }
+        if (f.front) {
+            ensure_front(P);
             f = field_loc(P, id);
         }
         if (!f.base) bad("unknown field id or field not held by this problem");
@@ -1484,6 +1519,10 @@ nk_status nk_problem_get_field_parent(const nk_problem* Pc, int32_t id, double* 
             ensure_energy(P);
             f = field_loc(P, id);
         }
+        if (f.front) {
+            ensure_front(P);
+            f = field_loc(P, id);
+        }
         if (!f.base) bad("unknown field id or field not held by this problem");
         copy_out_parent(P, f, parent, parent_layout(f, hx, hy, hz, count));
     });
@@ -1499,6 +1538,7 @@ static void launch_problem_geometry(nk_problem* P) {
     v.grounding = P->pd.grounding; v.gl_stress = P->pd.grounding_line_driving_stress; v.use_mask = P->pd.use_ice_mask;
     v.mask_min = P->pd.mask_minimum_thickness; v.mask_trans = P->pd.mask_transition_thickness;
     v.ud = P->ud;
+    v.front = P->front.enabled;
     launch_geometry(v, P->stream);
 }
 
@@ -1555,6 +1595,28 @@ static ThicknessView thickness_view(nk_problem* P, bool coupled) {
     v.scheme = adv.scheme; v.order = adv.order; v.bounded = adv.bounded;
     v.lower = adv.lower; v.upper = adv.upper;
     v.theta = P->transport + 6 * P->plane;
+    v.mu = P->front.enabled ? P->mu : nullptr;
+    return v;
+}
+
+// The partial-cell front's view of the problem (its planes and the thickness step's allocated first).
+static FrontView front_view(nk_problem* P, bool coupled) {
+    ensure_transport(P);
+    ensure_front(P);
+    const size_t pl = P->plane;
+    FrontView v;
+    v.g = P->fine.g;
+    v.H = P->H; v.mu = P->mu;
+    v.Hr = P->front_buf; v.calved = P->front_buf + pl; v.extent = P->front_buf + 2 * pl; v.O = P->front_buf + 3 * pl;
+    v.H_in = P->front_buf + 4 * pl; v.mu_in = P->front_buf + 5 * pl; v.f = P->front_buf + 6 * pl; v.share = P->front_buf + 7 * pl;
+    v.clipped = P->transport + 3 * pl;
+    v.x = P->x; v.bed = P->bed; v.phi = P->phi; v.coef = P->fine.coef;
+    v.smb = P->transport; v.melt = P->transport + pl; v.gmelt = P->transport + 2 * pl;
+    v.grounding = P->pd.grounding != 0; v.coupled = coupled; v.law = P->front.calving;
+    v.thickness = P->front.thickness; v.coefficient = P->front.coefficient; v.stress_threshold = P->front.stress_threshold;
+    v.floating_stress_threshold = P->front.floating_stress_threshold; v.front_velocity = P->front.front_velocity;
+    v.n = P->pd.glen_exponent; v.eps0 = P->pd.strain_rate_regularization;
+    v.wall_factor = P->pd.side_walls == NK_NO_SLIP ? 2.0 : 0.0;
     return v;
 }
 
@@ -1614,9 +1676,48 @@ nk_status nk_step_thickness(nk_problem* P, double dt, int32_t grounded_melt_coup
             NK_CUDA(cudaMemcpyAsync((double*)v.Hs, P->H, P->plane * sizeof(double), cudaMemcpyDeviceToDevice, P->stream));
             if (bounded) launch_thickness_limiter(v, P->stream);
             launch_thickness_stage(v, stages[st] * dt, st == 2, P->stream);
+            if (st == 2 && P->front.enabled)   // rk_substep!: advance_front! after the final stage (time_stepping.jl:23)
+                launch_advance_front(front_view(P, grounded_melt_coupling != 0), P->front.passes, stages[st] * dt, P->plane, P->stream);
             launch_problem_geometry(P);
             NK_CHECK_LAUNCH();
         }
+        NK_CUDA(cudaStreamSynchronize(P->stream));
+    });
+}
+
+nk_status nk_set_front(nk_problem* P, const nk_front_desc* f) {
+    if (!P || !f) return NK_BAD_ARGUMENT;
+    return guarded(P->ctx, [&] {
+        if (f->enabled) {
+            if (!P->pd.use_ice_mask) bad("a PartialCellFront masks the stress balance with its flag: create the problem with use_ice_mask = 1");
+            if (f->passes < 0) bad("passes must be non-negative");
+            if (f->calving < NK_CALVING_NONE || f->calving > NK_CALVING_MAXIMUM_EXTENT) bad("unknown calving law");
+            ensure_front(P);
+        }
+        P->front = *f;
+    });
+}
+
+nk_status nk_initialize_front(nk_problem* P) {
+    if (!P) return NK_BAD_ARGUMENT;
+    return guarded(P->ctx, [&] {
+        if (!P->front.enabled) bad("the problem has no partial-cell front (nk_set_front)");
+        if (P->async_pending) bad("an asynchronous solve is pending (nk_problem_wait first)");
+        launch_initialize_front(front_view(P, false), P->stream);
+        NK_CHECK_LAUNCH();
+        NK_CUDA(cudaStreamSynchronize(P->stream));
+    });
+}
+
+nk_status nk_advance_front(nk_problem* P, double dt) {
+    if (!P) return NK_BAD_ARGUMENT;
+    return guarded(P->ctx, [&] {
+        if (!P->front.enabled) bad("the problem has no partial-cell front (nk_set_front)");
+        if (!(dt > 0) || !std::isfinite(dt)) bad("the time step must be finite and positive");
+        if (P->async_pending) bad("an asynchronous solve is pending (nk_problem_wait first)");
+        launch_advance_front(front_view(P, false), P->front.passes, dt, P->plane, P->stream);
+        launch_problem_geometry(P);
+        NK_CHECK_LAUNCH();
         NK_CUDA(cudaStreamSynchronize(P->stream));
     });
 }

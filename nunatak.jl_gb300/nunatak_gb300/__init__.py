@@ -8,6 +8,8 @@ from .model import (YEAR, Convergence, DepthIntegrated, DIVAShear, FixedIteratio
                     RegularizedCoulombFriction, SmoothIceMask, StressBalanceDiagonalPreconditioner,
                     StressBalanceMultigridPreconditioner, StressBalanceSolver, SubgridGroundedFraction,
                     UpwindBiased, ViscosityConvergence, WENO, WeertmanFriction, default_thickness_advection,
+                    PartialCellFront, ThicknessThresholdCalving, EigenCalving, VonMisesCalving, FrontVelocityCalving,
+                    MaximumExtentCalving,
                     make_descriptors, field_shape, sigma_faces)
 from .problem import NunatakError, Problem
 
@@ -16,6 +18,7 @@ __all__ = [
     "IceSheetConstants", "LineJacobi", "NoSlipWalls", "PointJacobi", "RectilinearGrid", "RegularizedCoulombFriction",
     "SmoothIceMask", "StressBalanceDiagonalPreconditioner", "StressBalanceMultigridPreconditioner",
     "StressBalanceSolver", "SubgridGroundedFraction", "ViscosityConvergence", "WeertmanFriction", "make_descriptors",
-    "field_shape", "sigma_faces", "UpwindBiased", "WENO", "default_thickness_advection",
+    "field_shape", "sigma_faces", "UpwindBiased", "WENO", "default_thickness_advection", "PartialCellFront",
+    "ThicknessThresholdCalving", "EigenCalving", "VonMisesCalving", "FrontVelocityCalving", "MaximumExtentCalving",
     "NunatakError", "Problem",
 ]

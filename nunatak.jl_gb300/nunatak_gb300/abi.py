@@ -35,6 +35,7 @@ FIELD_IDS = {
     "surface_mass_balance": 31, "basal_melt_rate": 32, "grounded_melt": 33, "clipped_thickness": 34,
     "Hw": 35, "geothermal_flux": 36, "surface_temperature": 37, "ocean_temperature": 38, "H_previous": 39,
     "basal_temperate_fraction": 40, "basal_heat_flux": 41, "strain_heating": 42,
+    "front_thickness": 43, "calved_thickness": 44, "calving_extent": 45,
 }
 
 # (location x, location y, on the sigma grid) of each field: "c" Center, "f" Face.
@@ -56,6 +57,7 @@ FIELD_LOCATIONS = {
     "ocean_temperature": ("c", "c", False), "H_previous": ("c", "c", False),
     "basal_temperate_fraction": ("c", "c", False), "basal_heat_flux": ("c", "c", False),
     "strain_heating": ("c", "c", True),
+    "front_thickness": ("c", "c", False), "calved_thickness": ("c", "c", False), "calving_extent": ("c", "c", False),
 }
 
 
@@ -69,6 +71,15 @@ class EnergyParams(C.Structure):
 
 
 NK_ADVECTION_UPWIND, NK_ADVECTION_WENO = 0, 1
+(NK_CALVING_NONE, NK_CALVING_THICKNESS_THRESHOLD, NK_CALVING_EIGEN, NK_CALVING_VON_MISES, NK_CALVING_FRONT_VELOCITY,
+ NK_CALVING_MAXIMUM_EXTENT) = range(6)
+
+
+class FrontDesc(C.Structure):
+    """nk_front_desc: a PartialCellFront and its calving law."""
+    _fields_ = [("enabled", C.c_int32), ("passes", C.c_int32), ("calving", C.c_int32), ("reserved", C.c_int32),
+                ("thickness", C.c_double), ("coefficient", C.c_double), ("stress_threshold", C.c_double),
+                ("floating_stress_threshold", C.c_double), ("front_velocity", C.c_double)]
 
 
 class AdvectionDesc(C.Structure):

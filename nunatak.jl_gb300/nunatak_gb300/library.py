@@ -35,6 +35,9 @@ def _declare(lib):
         "nk_compute_thermal_diagnostics": ([vp, C.POINTER(abi.ThermalParams)], i32),
         "nk_step_thickness": ([vp, C.c_double, i32], i32),
         "nk_set_thickness_advection": ([vp, C.POINTER(abi.AdvectionDesc)], i32),
+        "nk_set_front": ([vp, C.POINTER(abi.FrontDesc)], i32),
+        "nk_initialize_front": ([vp], i32),
+        "nk_advance_front": ([vp, C.c_double], i32),
         "nk_step_enthalpy": ([vp, C.POINTER(abi.EnergyParams), C.c_double], i32),
         "nk_update_coefficients": ([vp], i32),
         "nk_apply_operator": ([vp, dp, dp, dp, dp], i32),

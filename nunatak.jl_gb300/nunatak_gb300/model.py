@@ -170,6 +170,63 @@ class SmoothIceMask:
     transition_thickness: float = 1.0
 
 
+# ---- partial-cell front and calving (src/Models/partial_cell_front.jl, src/Models/calving.jl) ----------------------
+@dataclass
+class ThicknessThresholdCalving:
+    thickness: float
+    code: int = abi.NK_CALVING_THICKNESS_THRESHOLD
+
+
+@dataclass
+class EigenCalving:
+    coefficient: float
+    code: int = abi.NK_CALVING_EIGEN
+
+
+@dataclass
+class VonMisesCalving:
+    stress_threshold: float
+    floating_stress_threshold: Optional[float] = None
+    code: int = abi.NK_CALVING_VON_MISES
+
+
+@dataclass
+class FrontVelocityCalving:
+    """front_velocity w (m/s) as a number; a time-dependent w(t) is set before each step (Problem.set_front)."""
+    front_velocity: float = 0.0
+    code: int = abi.NK_CALVING_FRONT_VELOCITY
+
+
+@dataclass
+class MaximumExtentCalving:
+    """The region the ice may cover, positive inside: an (Ny, Nx) array or a number, set as the "calving_extent" field."""
+    extent: object = None
+    code: int = abi.NK_CALVING_MAXIMUM_EXTENT
+
+
+@dataclass
+class PartialCellFront:
+    """PartialCellFront(grid; passes = 4, calving = nothing) (src/Models/partial_cell_front.jl:49-54)."""
+    passes: int = 4
+    calving: object = None
+
+    def desc(self):
+        c = self.calving
+        d = abi.FrontDesc()
+        d.enabled, d.passes = 1, int(self.passes)
+        d.calving = abi.NK_CALVING_NONE if c is None else c.code
+        if isinstance(c, ThicknessThresholdCalving):
+            d.thickness = float(c.thickness)
+        elif isinstance(c, EigenCalving):
+            d.coefficient = float(c.coefficient)
+        elif isinstance(c, VonMisesCalving):
+            d.stress_threshold = float(c.stress_threshold)
+            d.floating_stress_threshold = float(c.stress_threshold if c.floating_stress_threshold is None else c.floating_stress_threshold)
+        elif isinstance(c, FrontVelocityCalving):
+            d.front_velocity = float(c.front_velocity)
+        return d
+
+
 @dataclass
 class IceSheetConstants:
     ice_density: float = 918.0
@@ -251,9 +308,10 @@ class Descriptors:
     """C descriptors plus the arrays their pointers refer to (kept alive with the object).  `adjoint_control`
     is the StressBalanceSolver's adjoint iteration control, the default of Problem.picard_adjoint."""
 
-    def __init__(self, grid, physics, solver, keep, adjoint_control=None):
+    def __init__(self, grid, physics, solver, keep, adjoint_control=None, front=None):
         self.grid, self.physics, self.solver, self._keep = grid, physics, solver, keep
         self.adjoint_control = adjoint_control
+        self.front = front                  # a PartialCellFront, applied when the problem is created
 
 
 def _as_ptr(a):
@@ -266,7 +324,7 @@ def make_descriptors(grid: RectilinearGrid, Nsigma=10, bed_refinement=2.0, sigma
                      velocity_solver: StressBalanceSolver = None, use_effective_pressure=True):
     """Translate the configuration objects into (nk_grid_desc, nk_physics_desc, nk_solver_desc).
 
-    masking: "default" -> SmoothIceMask(), None -> no mask (the reference's `nothing`)."""
+    masking: "default" -> SmoothIceMask(), None -> no mask (the reference's `nothing`), or a PartialCellFront."""
     stress_balance = stress_balance or DepthIntegrated()
     rheology = rheology or GlenFlowLaw(rate_factor=1e-24)
     constants = constants or IceSheetConstants()
@@ -321,6 +379,9 @@ def make_descriptors(grid: RectilinearGrid, Nsigma=10, bed_refinement=2.0, sigma
     p.ice_density = constants.ice_density
     p.ocean_density = constants.ocean_density
     p.gravitational_acceleration = constants.gravitational_acceleration
+    front = masking if isinstance(masking, PartialCellFront) else None
+    if front is not None:
+        masking = SmoothIceMask()           # its thickness parameters are unused: the front's flag is the mask
     p.use_ice_mask = 1 if masking is not None else 0
     p.grounding = 1 if isinstance(grounding, SubgridGroundedFraction) else 0
     p.grounding_line_driving_stress = 1 if (isinstance(grounding, SubgridGroundedFraction) and grounding.driving_stress) else 0
@@ -345,7 +406,7 @@ def make_descriptors(grid: RectilinearGrid, Nsigma=10, bed_refinement=2.0, sigma
     s.linear = velocity_solver.linear_iteration_control.desc()
     s.picard = velocity_solver.picard_iteration_control.desc()
     s.flags = abi.NK_SOLVER_HOST_LOOP if velocity_solver.host_loop else 0
-    return Descriptors(g, p, s, keep, velocity_solver.adjoint_control)
+    return Descriptors(g, p, s, keep, velocity_solver.adjoint_control, front)
 
 
 def field_shape(grid: RectilinearGrid, name: str, Nsigma: int, rate_layout_sigma=False):

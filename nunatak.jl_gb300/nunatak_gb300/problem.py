@@ -62,6 +62,8 @@ class Problem:
         self._ctx = context if context is not None else (library.default_context() if self.prefix == "nk_" else None)
         self._h = C.c_void_p()
         self._create()
+        if getattr(desc, "front", None) is not None:
+            self.set_front(desc.front)
 
     # -- library plumbing ------------------------------------------------------------------------
     def _load(self):
@@ -199,6 +201,22 @@ class Problem:
                                water_layer_blend_thickness, minimum_thickness, drainage_water_fraction, maximum_drainage_rate,
                                int(grounded_melt_coupling), 0)
         _check(self._fn("step_enthalpy")(self._h, C.byref(prm), float(dt)), "step_enthalpy", self._err())
+
+    def set_front(self, front):
+        """The masking becomes a PartialCellFront (src/Models/partial_cell_front.jl): its 0/1 flag of full cells is the
+        ice mask, the thickness step advances the front and calves it under `front.calving`."""
+        d = front.desc()
+        _check(self._fn("set_front")(self._h, C.byref(d)), "set_front", self._err())
+        if getattr(front.calving, "extent", None) is not None:
+            self.set("calving_extent", front.calving.extent)
+
+    def initialize_front(self):
+        """initialize_front!: every cell holding ice is full, none partial (what set!(model; H) does)."""
+        _check(self._fn("initialize_front")(self._h), "initialize_front", self._err())
+
+    def advance_front(self, dt):
+        """advance_front!(front, model, dt) alone, then the geometry."""
+        _check(self._fn("advance_front")(self._h, float(dt)), "advance_front", self._err())
 
     def set_thickness_advection(self, advection):
         """The thickness advection scheme of step_thickness (IceSheetModel's `advection`): an UpwindBiased(order = 1 or 3)

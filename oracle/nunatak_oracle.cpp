@@ -834,6 +834,10 @@ struct Problem {
     // WENO(order = 5, bounds = (0, 1e5)) (default_thickness_advection, src/Models/ice_sheet_model.jl:123)
     nk_advection_desc advection{NK_ADVECTION_WENO, 5, 1, 0, 0.0, 1e5};
     Field theta;                  // the bounds-preserving limiter of each cell (and of the first halo layer)
+    // PartialCellFront (nko_set_front): the front thickness Hʳ, the calved thickness, MaximumExtentCalving's extent and
+    // the overflow / retreat scratch; the ice mask μ is then the prognostic 0/1 flag of full cells
+    nk_front_desc front{0, 4, NK_CALVING_NONE, 0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    Field Hr, calved, extent, O;
     Field qg;                     // basal heat flux qᵍ = φ G + τᵇ⋅uᵇ of the last energy step (output)
     SigmaField Phi;
 
@@ -1057,11 +1061,12 @@ static void compute_geometry(Problem& P) {
         double P0 = rig * P.H(i, j);
         P.N(i, j) = std::max(P0 + rwg * std::min(P.bed(i, j), 0.0), 0.0);
     });
-    // compute_ice_mask!, smooth_ice_mask.jl:50-69
-    for_xy(Nx, Ny, [&](int i, int j) {
-        double t = std::min(std::max((P.H(i, j) - P.mask_min) / P.mask_trans, 0.0), 1.0);
-        P.mu(i, j) = t * t * (3 - 2 * t);
-    });
+    // compute_ice_mask!, smooth_ice_mask.jl:50-69; a PartialCellFront's flag is prognostic (partial_cell_front.jl:95)
+    if (!P.front.enabled)
+        for_xy(Nx, Ny, [&](int i, int j) {
+            double t = std::min(std::max((P.H(i, j) - P.mask_min) / P.mask_trans, 0.0), 1.0);
+            P.mu(i, j) = t * t * (3 - 2 * t);
+        });
     fill_halo(P.s); fill_halo(P.N); fill_halo(P.mu); fill_halo(P.phi); fill_halo(P.phu); fill_halo(P.phv);
 
     // compute_driving_stress!, driving_stress.jl:43-125
@@ -1798,6 +1803,251 @@ static double bounds_limiter(const nk_advection_desc& adv, const Field& H, int i
 }
 
 // ------------------------------------------------------------------------------------------------
+// Partial-cell front (PartialCellFront, src/Models/partial_cell_front.jl) and calving (src/Models/calving.jl).
+// μ (P.mu) is the prognostic 0/1 flag of full cells, Hʳ (P.Hr) the ice thickness of a partial front cell, which covers
+// the fraction H / Hʳ of its area.  Halo cells of a Bounded direction are inactive; periodic halos wrap.
+// ------------------------------------------------------------------------------------------------
+static inline bool full_cell(const Problem& P, int i, int j) { return P.mu(i, j) > 0; }                          // :101
+static inline bool full_neighbor(const Problem& P, int i, int j) { return full_cell(P, i, j) && !P.grid.inactive_cell(i, j); }   // :102
+static inline bool empty_cell(const Problem& P, const Field& H, int i, int j) {                                   // :103
+    return !full_cell(P, i, j) && H(i, j) <= 0 && !P.grid.inactive_cell(i, j);
+}
+
+// initialize_front!, :80-92: every cell holding ice is full, none is partial.
+static void initialize_front(Problem& P) {
+    for_xy(P.grid.Nx(), P.grid.Ny(), [&](int i, int j) {
+        P.mu(i, j) = P.H(i, j) > 0 ? 1.0 : 0.0;
+        P.Hr(i, j) = 0.0;
+    });
+    fill_halo(P.mu);
+    fill_halo(P.Hr);
+}
+
+// front_ice_thickness, :331: its own thickness when full or not yet given an Hʳ.
+static inline double front_ice_thickness(const Problem& P, int i, int j) {
+    return (full_cell(P, i, j) || P.Hr(i, j) <= 0) ? P.H(i, j) : P.Hr(i, j);
+}
+
+// remove_front_fraction!, :353-368: remove the fraction g of the cell's area; returns the part of g beyond its ice.
+static double remove_front_fraction(Problem& P, int i, int j, double g) {
+    double Hi = P.H(i, j), Hf = front_ice_thickness(P, i, j);
+    bool calves = (g > 0) && (Hi > 0);
+    double Hn = std::max(Hi - g * Hf, 0.0);
+    double a = Hf > 0 ? Hi / (Hf > 0 ? Hf : 1.0) : 0.0;
+    if (calves) {
+        P.calved(i, j) += Hi - Hn;
+        P.H(i, j) = Hn;
+        P.Hr(i, j) = Hn > 0 ? Hf : 0.0;
+        P.mu(i, j) = 0.0;
+    }
+    return calves ? std::max(g - a, 0.0) : 0.0;
+}
+
+// principal_strain_rates, calving.jl:144-152, with the velocities masked by μ (interior_u / interior_v with μ)
+static void principal_strain_rates(const Problem& P, int i, int j, double& e1, double& e2) {
+    const Grid& g = P.grid;
+    const Field* mu = &P.mu;
+    double exx = strain_rate_xx(g, i, j, P.x.u, mu), eyy = strain_rate_yy(g, i, j, P.x.v, mu);
+    // ℑxyᶜᶜᵃ = ℑyᵃᶜᵃ(ℑxᶜᵃᵃ(·)) of the corner shear
+    double exy = ((strain_rate_xy(g, i, j, P.x.u, P.x.v, P.ph.walls, mu) + strain_rate_xy(g, i + 1, j, P.x.u, P.x.v, P.ph.walls, mu)) / 2 +
+                  (strain_rate_xy(g, i, j + 1, P.x.u, P.x.v, P.ph.walls, mu) + strain_rate_xy(g, i + 1, j + 1, P.x.u, P.x.v, P.ph.walls, mu)) / 2) / 2;
+    double eb = (exx + eyy) / 2;
+    double r = std::sqrt(((exx - eyy) / 2) * ((exx - eyy) / 2) + exy * exy + P.ph.eps0 * P.ph.eps0);
+    e1 = eb + r;
+    e2 = eb - r;
+}
+
+// front_flow_speed, calving.jl:176-181: the larger face speed along each axis.
+static double front_flow_speed(const Problem& P, int i, int j) {
+    const Grid& g = P.grid;
+    double ut = std::max(std::fabs(interior_u(g, i, j, P.x.u, &P.mu)), std::fabs(interior_u(g, i + 1, j, P.x.u, &P.mu)));
+    double vt = std::max(std::fabs(interior_v(g, i, j, P.x.v, &P.mu)), std::fabs(interior_v(g, i, j + 1, P.x.v, &P.mu)));
+    double e = P.ph.eps0 * g.dx_c(i);
+    return std::sqrt(ut * ut + vt * vt + e * e);
+}
+
+// calving_rate of a full cell, calving.jl:154-190
+static double calving_rate(const Problem& P, int i, int j) {
+    const nk_front_desc& law = P.front;
+    if (law.calving == NK_CALVING_EIGEN) {
+        double e1, e2;
+        principal_strain_rates(P, i, j, e1, e2);
+        return law.coefficient * std::max(e1, 0.0) * std::max(e2, 0.0);
+    }
+    if (law.calving == NK_CALVING_VON_MISES) {
+        double e1, e2;
+        principal_strain_rates(P, i, j, e1, e2);
+        double n = P.ph.n, e0 = P.ph.eps0;
+        double et2 = (std::max(e1, 0.0) * std::max(e1, 0.0) + std::max(e2, 0.0) * std::max(e2, 0.0)) / 2;
+        double ee2 = effective_strain_rate2(P.grid, i, j, P.x.u, P.x.v, P.ph.walls) + e0 * e0;
+        double Hi = P.H(i, j);
+        double eta = P.etaH(i, j) / (Hi > 0 ? Hi : 1.0);
+        double smax = P.phi(i, j) * law.stress_threshold + (1 - P.phi(i, j)) * law.floating_stress_threshold;
+        double B = 2 * eta * std::pow(ee2, (n - 1) / (2 * n));
+        double sig = std::sqrt(3.0) * B * et2 * std::pow(et2 + e0 * e0, (1 - 2 * n) / (2 * n));
+        return front_flow_speed(P, i, j) * sig / smax;
+    }
+    if (law.calving == NK_CALVING_FRONT_VELOCITY) {
+        double c = std::max(front_flow_speed(P, i, j) - law.front_velocity, 0.0);
+        return (1 - P.phi(i, j)) * c;
+    }
+    return 0.0;
+}
+
+// front_calving_rate, calving.jl:197-206: a partial cell takes the mean rate of its full neighbours.
+static double front_calving_rate(const Problem& P, int i, int j) {
+    if (full_cell(P, i, j)) return calving_rate(P, i, j);
+    double S = 0;
+    int n = 0;
+    const int di[4] = {-1, 1, 0, 0}, dj[4] = {0, 0, -1, 1};
+    for (int k = 0; k < 4; ++k)
+        if (full_neighbor(P, i + di[k], j + dj[k])) { S += calving_rate(P, i + di[k], j + dj[k]); ++n; }
+    return S / std::max(n, 1);
+}
+
+// calve_front!, partial_cell_front.jl:276-296, with _compute_retreat_fraction!, _retreat_front_cells!,
+// _share_residual_retreat! and _receive_residual_retreat! (:311-389) and retreat_fraction (calving.jl:212-227).
+static void calve_front(Problem& P, double dt) {
+    const Grid& g = P.grid;
+    const int Nx = g.Nx(), Ny = g.Ny();
+    const int law = P.front.calving;
+    fill_halo(P.bed);
+    Field f(&g, CENTER, CENTER);
+    // the retreat fraction of each front cell, from the state before any cell retreats
+    for_xy(Nx, Ny, [&](int i, int j) {
+        double dx = g.dx_c(i), dy = g.dy_c(j);
+        auto ocean = [&](int a, int b, double len) { return (empty_cell(P, P.H, a, b) && P.bed(a, b) < 0) ? len : 0.0; };
+        double lw = ocean(i - 1, j, dy), le = ocean(i + 1, j, dy), ls = ocean(i, j - 1, dx), ln = ocean(i, j + 1, dx);
+        // front_length, :334-343
+        double ub = std::fabs((interior_u(g, i, j, P.x.u, &P.mu) + interior_u(g, i + 1, j, P.x.u, &P.mu)) / 2);
+        double vb = std::fabs((interior_v(g, i, j, P.x.v, &P.mu) + interior_v(g, i, j + 1, P.x.v, &P.mu)) / 2);
+        double speed = std::sqrt(ub * ub + vb * vb);
+        double l2 = (le - lw) * (le - lw) + (ln - ls) * (ln - ls);
+        double lv = l2 > 0 ? std::sqrt(l2 > 0 ? l2 : 1.0) : lw + le + ls + ln;
+        double lu = (ub * (lw + le) + vb * (ls + ln)) / (speed > 0 ? speed : 1.0);
+        double l = speed > 0 ? lu : lv;
+        double Hf = front_ice_thickness(P, i, j);
+        bool front = P.H(i, j) > 0 && (lw + le + ls + ln > 0);
+        double r = 0;
+        if (front) {
+            if (law == NK_CALVING_THICKNESS_THRESHOLD) r = Hf < P.front.thickness ? 1.0 : 0.0;
+            else if (law == NK_CALVING_MAXIMUM_EXTENT) r = P.extent(i, j) > 0 ? 0.0 : 1.0;
+            else r = std::min(1.0, front_calving_rate(P, i, j) * dt * l / g.Az_ccc(i, j));
+        }
+        f(i, j) = r;
+    });
+    // retreat (each cell changes only itself), then the area a cell could not take (rate laws only)
+    const bool removal = law == NK_CALVING_THICKNESS_THRESHOLD || law == NK_CALVING_MAXIMUM_EXTENT;
+    for (int j = 1; j <= Ny; ++j)
+        for (int i = 1; i <= Nx; ++i) {
+            double r = remove_front_fraction(P, i, j, f(i, j));
+            f(i, j) = (removal ? 0.0 : r) * g.Az_ccc(i, j);
+        }
+    fill_halo(f);
+    fill_halo(P.H);
+    // _share_residual_retreat!: among the neighbours that hold ice
+    Field share(&g, CENTER, CENTER);
+    for_xy(Nx, Ny, [&](int i, int j) {
+        auto ice = [&](int a, int b) { return (!g.inactive_cell(a, b) && P.H(a, b) > 0) ? 1 : 0; };
+        int n = ice(i - 1, j) + ice(i + 1, j) + ice(i, j - 1) + ice(i, j + 1);
+        share(i, j) = n > 0 ? f(i, j) / std::max(n, 1) : 0.0;
+    });
+    fill_halo(share);
+    // _receive_residual_retreat!: what the receiving cell cannot take is not passed on
+    Field A(&g, CENTER, CENTER);
+    for_xy(Nx, Ny, [&](int i, int j) {
+        auto area = [&](int a, int b) { return g.inactive_cell(a, b) ? 0.0 : share(a, b); };
+        A(i, j) = area(i - 1, j) + area(i + 1, j) + area(i, j - 1) + area(i, j + 1);
+    });
+    for (int j = 1; j <= Ny; ++j)
+        for (int i = 1; i <= Nx; ++i) remove_front_fraction(P, i, j, A(i, j) / g.Az_ccc(i, j));
+    fill_halo(P.mu);
+    fill_halo(P.Hr);
+    fill_halo(P.H);
+}
+
+// advance_front!(front, model, Δt), partial_cell_front.jl:167-195.
+static void advance_front(Problem& P, double dt, bool coupled) {
+    const Grid& g = P.grid;
+    const int Nx = g.Nx(), Ny = g.Ny();
+    fill_halo(P.H);
+    for_xy(Nx, Ny, [&](int i, int j) { if (P.H(i, j) <= 0) P.mu(i, j) = 0.0; });          // _empty_drained_cells!, :197-200
+    fill_halo(P.mu);
+    fill_halo(P.x);
+    // _compute_reference_thickness!, :206-230
+    {
+        Field Hr0 = P.Hr;
+        for_xy(Nx, Ny, [&](int i, int j) {
+            bool west = P.x.u(i, j) > 0, east = P.x.u(i + 1, j) < 0, south = P.x.v(i, j) > 0, north = P.x.v(i, j + 1) < 0;
+            auto donor = [&](int a, int b, bool inflow) { return (inflow && full_neighbor(P, a, b)) ? P.H(a, b) : 0.0; };
+            auto count = [&](int a, int b, bool inflow) { return (inflow && full_neighbor(P, a, b)) ? 1 : 0; };
+            double Sin = donor(i - 1, j, west) + donor(i + 1, j, east) + donor(i, j - 1, south) + donor(i, j + 1, north);
+            int nin = count(i - 1, j, west) + count(i + 1, j, east) + count(i, j - 1, south) + count(i, j + 1, north);
+            double Sf = donor(i - 1, j, true) + donor(i + 1, j, true) + donor(i, j - 1, true) + donor(i, j + 1, true);
+            int nf = count(i - 1, j, true) + count(i + 1, j, true) + count(i, j - 1, true) + count(i, j + 1, true);
+            double Hi = P.H(i, j);
+            double Hs = nf > 0 ? Sf / std::max(nf, 1) : Hi;
+            double Hp = Hi > 0 ? (Hr0(i, j) > 0 ? Hr0(i, j) : Hs) : 0.0;
+            double Hbar = nin > 0 ? Sin / std::max(nin, 1) : Hp;
+            P.Hr(i, j) = full_cell(P, i, j) ? 0.0 : Hbar;
+        });
+        fill_halo(P.Hr);
+    }
+    // overflow passes: _fill_front_cells! then _receive_overflow!, :235-268
+    for (int pass = 0; pass < P.front.passes; ++pass) {
+        Field H0 = P.H, mu0 = P.mu;
+        for_xy(Nx, Ny, [&](int i, int j) {
+            auto empty0 = [&](int a, int b) {
+                return (!(mu0(a, b) > 0) && H0(a, b) <= 0 && !g.inactive_cell(a, b)) ? 1 : 0;
+            };
+            int n = empty0(i - 1, j) + empty0(i + 1, j) + empty0(i, j - 1) + empty0(i, j + 1);
+            double Hi = H0(i, j), Hri = P.Hr(i, j);
+            bool fills = !(mu0(i, j) > 0) && (Hri > 0) && (Hi >= Hri);
+            bool spills = fills && n > 0;
+            P.O(i, j) = spills ? (Hi - Hri) * g.Az_ccc(i, j) / std::max(n, 1) : 0.0;
+            P.H(i, j) = spills ? Hri : Hi;
+            if (fills) P.mu(i, j) = 1.0;
+        });
+        fill_halo(P.mu);
+        fill_halo(P.O);
+        fill_halo(P.H);
+        Field H1 = P.H;
+        for_xy(Nx, Ny, [&](int i, int j) {
+            bool receives = empty_cell(P, H1, i, j);
+            auto vol = [&](int a, int b) { return g.inactive_cell(a, b) ? 0.0 : P.O(a, b); };
+            auto donor = [&](int a, int b) { return !g.inactive_cell(a, b) && P.O(a, b) > 0; };
+            double V = vol(i - 1, j) + vol(i + 1, j) + vol(i, j - 1) + vol(i, j + 1);
+            double S = (donor(i - 1, j) ? H1(i - 1, j) : 0.0) + (donor(i + 1, j) ? H1(i + 1, j) : 0.0) +
+                       (donor(i, j - 1) ? H1(i, j - 1) : 0.0) + (donor(i, j + 1) ? H1(i, j + 1) : 0.0);
+            int n = donor(i - 1, j) + donor(i + 1, j) + donor(i, j - 1) + donor(i, j + 1);
+            if (receives) P.H(i, j) = V / g.Az_ccc(i, j);
+            if (receives && n > 0) P.Hr(i, j) = S / std::max(n, 1);
+        });
+        fill_halo(P.H);
+        fill_halo(P.Hr);
+    }
+    if (P.front.calving != NK_CALVING_NONE) calve_front(P, dt);
+    // _force_front_cells!, :271-286
+    for_xy(Nx, Ny, [&](int i, int j) {
+        double Hi = P.H(i, j), Hri = P.Hr(i, j);
+        double m = P.grounding ? (1 - P.phi(i, j)) * P.melt(i, j) : P.melt(i, j);
+        double S = P.smb(i, j) - m - (coupled ? P.gmelt(i, j) : 0.0);
+        bool full = full_cell(P, i, j);
+        bool forced = (Hi > 0) && (Hri > 0);
+        double Hf = full ? Hi : Hri;
+        bool melted = forced && (Hf + S * dt <= 0);
+        double Hn = full ? Hi + S * dt : Hi / (Hri > 0 ? Hri : 1.0) * (Hri + S * dt);
+        if (melted) P.clipped(i, j) += -Hn;
+        P.H(i, j) = melted ? 0.0 : (forced ? Hn : Hi);
+        P.Hr(i, j) = (melted || full) ? 0.0 : (forced ? Hri + S * dt : Hri);
+        if (melted) P.mu(i, j) = 0.0;
+    });
+    fill_halo(P.mu);
+    fill_halo(P.Hr);
+    fill_halo(P.H);
+}
+
+// ------------------------------------------------------------------------------------------------
 // One ice time step of the thickness, time_stepping.jl:15-72: three split Runge-Kutta stages
 // H = max(0, H⁻ + Δτ G(H)) from the thickness H⁻ at the start of the step, with Δτ = Δt/3, Δt/2, Δt (Oceananigans
 // 0.117's SplitRungeKutta3, the Wicker-Skamarock scheme), the thickness added by the clip in the last stage
@@ -1827,9 +2077,15 @@ static void step_thickness(Problem& P, double dt, bool coupled) {
                 for (int i = 0; i <= Nx + 1; ++i) P.theta(i, j) = bounds_limiter(adv, P.H, i, j);
         }
         auto limited = [&](double v, int ic, int jc) { return bounded ? P.H(ic, jc) + P.theta(ic, jc) * (v - P.H(ic, jc)) : v; };
+        // with a PartialCellFront (front_flux_x / front_flux_y, partial_cell_front.jl:114-132): the scheme's flux
+        // between full cells, the upwind flux out of a full cell into a front cell, nothing out of a front cell
+        const bool front = P.front.enabled != 0;
         auto xflux = [&](int i, int j) {
             if (g.peripheral_fc(i, j)) return 0.0;
             double u = P.x.u(i, j), s[5];
+            bool west = !front || full_cell(P, i - 1, j), eastc = !front || full_cell(P, i, j);
+            if (!(west && eastc))
+                return (west || eastc) ? g.dy_c(j) * (west ? std::max(u, 0.0) * P.H(i - 1, j) : std::min(u, 0.0) * P.H(i, j)) : 0.0;
             bool east = u > 0;
             x_stencil(P.H, i, j, east, s);
             double h = limited(face_value(adv, s), east ? i - 1 : i, j);
@@ -1838,14 +2094,18 @@ static void step_thickness(Problem& P, double dt, bool coupled) {
         auto yflux = [&](int i, int j) {
             if (g.peripheral_cf(i, j)) return 0.0;
             double v = P.x.v(i, j), s[5];
+            bool south = !front || full_cell(P, i, j - 1), northc = !front || full_cell(P, i, j);
+            if (!(south && northc))
+                return (south || northc) ? g.dx_c(i) * (south ? std::max(v, 0.0) * P.H(i, j - 1) : std::min(v, 0.0) * P.H(i, j)) : 0.0;
             bool north = v > 0;
             y_stencil(P.H, i, j, north, s);
             double h = limited(face_value(adv, s), i, north ? j - 1 : j);
             return g.dx_c(i) * (v * h);
         };
-        for_xy(Nx, Ny, [&](int i, int j) {   // _compute_thickness_tendency!, :59-63
+        for_xy(Nx, Ny, [&](int i, int j) {   // _compute_thickness_tendency!, :59-63 (sources on full cells only)
             double m = P.grounding ? (1 - P.phi(i, j)) * P.melt(i, j) : P.melt(i, j);
             double S = P.smb(i, j) - m - (coupled ? P.gmelt(i, j) : 0.0);
+            if (front && !full_cell(P, i, j)) S = 0.0;
             double div = (xflux(i + 1, j) - xflux(i, j) + yflux(i, j + 1) - yflux(i, j)) / g.Az_ccc(i, j);
             Gt(i, j) = S - div;
         });
@@ -1857,6 +2117,7 @@ static void step_thickness(Problem& P, double dt, bool coupled) {
             if (final_stage) P.clipped(i, j) += std::max(0.0, -Hs);
         });
         fill_halo(P.H);
+        if (final_stage && P.front.enabled) advance_front(P, dtau, coupled);   // rk_substep!, :23
         compute_geometry(P);
     }
 }
@@ -1912,6 +2173,9 @@ static FieldRef field_ref(Problem& P, int id) {
         case NK_FIELD_BASAL_TEMPERATE_FRACTION: r.f = &P.sb; break;
         case NK_FIELD_BASAL_HEAT_FLUX: r.f = &P.qg; break;
         case NK_FIELD_STRAIN_HEATING: r.s = &P.Phi; break;
+        case NK_FIELD_FRONT_THICKNESS: r.f = &P.Hr; break;
+        case NK_FIELD_CALVED_THICKNESS: r.f = &P.calved; break;
+        case NK_FIELD_CALVING_EXTENT: r.f = &P.extent; break;
         default: break;
     }
     return r;
@@ -1985,6 +2249,7 @@ nk_status nko_problem_create(const nk_grid_desc* gd, const nk_physics_desc* pd, 
     P->A3.init(g, CENTER, CENTER, gd->Nsigma); P->eta_s.init(g, CENTER, CENTER, gd->Nsigma); P->T.init(g, CENTER, CENTER, gd->Nsigma);
     P->E.init(g, CENTER, CENTER, gd->Nsigma); P->omega.init(g, CENTER, CENTER, gd->Nsigma);
     for (Field* f : {&P->Hw, &P->gmelt, &P->G, &P->Ts, &P->To, &P->melt, &P->Hn, &P->sb, &P->smb, &P->clipped, &P->qg}) f->init(g, CENTER, CENTER);
+    for (Field* f : {&P->Hr, &P->calved, &P->extent, &P->O}) f->init(g, CENTER, CENTER);
     P->Phi.init(g, CENTER, CENTER, gd->Nsigma);
     P->us.init(g, FACE, CENTER, gd->Nsigma); P->vs.init(g, CENTER, FACE, gd->Nsigma);
     P->r.init(g); P->z.init(g); P->p.init(g); P->q.init(g); P->w.init(g); P->xprev.init(g);
@@ -2132,6 +2397,35 @@ nk_status nko_step_thickness(nko_problem* h, double dt, int32_t coupled) {
     if ((P.advection.scheme == NK_ADVECTION_WENO || P.advection.order == 3) && halo < 3)
         return NK_BAD_ARGUMENT;   // the five-point stencils reach three cells beyond a face
     step_thickness(P, dt, coupled != 0);
+    return NK_OK;
+}
+
+// PartialCellFront(grid; passes, calving) as the masking (partial_cell_front.jl:1-66, calving.jl); needs the ice mask.
+nk_status nko_set_front(nko_problem* h, const nk_front_desc* f) {
+    if (!h || !f) return NK_BAD_ARGUMENT;
+    Problem& P = *reinterpret_cast<Problem*>(h);
+    if (f->enabled && (!P.use_mask || f->passes < 0 || f->calving < NK_CALVING_NONE || f->calving > NK_CALVING_MAXIMUM_EXTENT))
+        return NK_BAD_ARGUMENT;
+    P.front = *f;
+    return NK_OK;
+}
+
+nk_status nko_initialize_front(nko_problem* h) {
+    if (!h) return NK_BAD_ARGUMENT;
+    Problem& P = *reinterpret_cast<Problem*>(h);
+    if (!P.front.enabled) return NK_BAD_ARGUMENT;
+    initialize_front(P);
+    return NK_OK;
+}
+
+nk_status nko_advance_front(nko_problem* h, double dt) {
+    if (!h || !(dt > 0)) return NK_BAD_ARGUMENT;
+    Problem& P = *reinterpret_cast<Problem*>(h);
+    if (!P.front.enabled) return NK_BAD_ARGUMENT;
+    fill_halo(P.x);
+    for (Field* f : {&P.smb, &P.melt, &P.gmelt, &P.clipped, &P.Hr, &P.extent}) fill_halo(*f);
+    advance_front(P, dt, false);
+    compute_geometry(P);
     return NK_OK;
 }
 

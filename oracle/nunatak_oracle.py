@@ -50,6 +50,9 @@ def load():
             "nko_step_enthalpy": [vp, dp, C.c_double],
             "nko_step_thickness": [vp, C.c_double, C.c_int32],
             "nko_set_thickness_advection": [vp, C.POINTER(abi.AdvectionDesc)],
+            "nko_set_front": [vp, C.POINTER(abi.FrontDesc)],
+            "nko_initialize_front": [vp],
+            "nko_advance_front": [vp, C.c_double],
             "nko_picard_adjoint": [vp, dp, dp, C.POINTER(abi.IterationControl), dp, dp, dp, dp, C.POINTER(abi.SolveStats)],
             "nko_multigrid_levels": [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), i32],
             "nko_multigrid_restrict": [vp, i32, dp, dp, dp, dp],
