@@ -421,9 +421,13 @@ typedef struct nk_energy_params {
  * drainage of temperate ice (:223-259), then T and omega from the new enthalpy and H^n = H.  Reads
  * NK_FIELD_ENTHALPY, H, H^n, the velocities, u_sigma / v_sigma, u_b / v_b, the basal drag and eta_sigma of the
  * last solve (nk_velocity_profile first), phi, the basal and grounded melt rates and the state fields above;
- * writes E, T, omega, H_w, the grounded melt rate, H^n and the diagnostics.  The rate factor is not updated
- * (nk_compute_thermal_diagnostics does that).  NK_BAD_ARGUMENT without the sigma rate-factor layout, with more
- * than NK_ENERGY_MAX_LAYERS layers, or when dt is not finite and positive. */
+ * writes E, T, omega, H_w, the grounded melt rate, H^n and the diagnostics.  The rate factor is not updated: the
+ * reference's advance_enthalpy! ends with update_thermal_diagnostics! (:85-97), so call
+ * nk_compute_thermal_diagnostics after this step before the next velocity solve.  The basal water is not drained by
+ * a till (TillEffectivePressure's drain_till, src/Thermodynamics/till_effective_pressure.jl, is not built: H_w is
+ * the water balance's H+ uncapped, and nk_compute_geometry's effective pressure is the ocean-connected one).
+ * NK_BAD_ARGUMENT without the sigma rate-factor layout, with more than NK_ENERGY_MAX_LAYERS layers, or when dt is not
+ * finite and positive. */
 nk_status nk_step_enthalpy(nk_problem* problem, const nk_energy_params* params, double dt);
 
 /* update_stress_balance_coefficients!(x, ...) (SSA) or update_diva_coefficients!(x, ...) (DIVA) at the

@@ -92,7 +92,7 @@ struct NoExtra {};
 // IU / IV: the mask bits of the identity rows (q = p).  A caller whose own rule already fixes the prescribed rows
 // may pass U_INACTIVE / V_INACTIVE, the bits of the strain-rate reads, which then serve both tests.
 template <int R, uint8_t IU = U_IDENTITY, uint8_t IV = V_IDENTITY, typename T, typename Src, typename Extra, typename Emit>
-__device__ __forceinline__ void strip_apply_src(const OpView<T>& o, Src&& src, int i, int j0, Extra&& extra, Emit&& emit) {
+__device__ __forceinline__ void strip_apply_general(const OpView<T>& o, Src&& src, int i, int j0, Extra&& extra, Emit&& emit) {
     using V2 = typename Vec2<T>::type;
     using V4 = typename Vec4<T>::type;
     using E = decltype(extra(0));
@@ -188,6 +188,105 @@ __device__ __forceinline__ void strip_apply_src(const OpView<T>& o, Src&& src, i
         syy_s = syy;
         t_c = t_n;
     }
+}
+
+// The same walk for a warp whose 32 columns and R + 2 rows lie strictly inside the grid (columns 1 .. Nx - 2, rows
+// 1 .. Ny - 2): every index is its own stored index (no wrap, no clamp), every velocity takes part in the strain rates
+// (only the mask byte decides), no corner is a wall corner, and the corner record of row j is the centre record of
+// row j, so it is not loaded twice.  The arithmetic is the general walk's, expression for expression, so both give
+// the same bits.
+template <int R, uint8_t IU = U_IDENTITY, uint8_t IV = V_IDENTITY, typename T, typename Src, typename Extra, typename Emit>
+__device__ __forceinline__ void strip_apply_interior(const OpView<T>& o, Src&& src, int i, int j0, Extra&& extra, Emit&& emit) {
+    using V2 = typename Vec2<T>::type;
+    using V4 = typename Vec4<T>::type;
+    using E = decltype(extra(0));
+    const DevGrid<T>& g = o.g;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x;
+    const bool own_col = lane >= 1 && lane <= STRIP_COLS;
+    const T rdxc_i = g.rdxc[i], dxc_i = g.dxc[i], rdxf_i = g.rdxf[i], dxf_i = g.dxf[i];
+
+    V2 raw[R + 2];            // rows j0 - 1 .. j0 + R
+    uint8_t msk[R + 2];
+    V4 rec[R + 1];            // centre (i, j), rows j0 - 1 .. j0 + R - 1
+    T cffR;                   // η̄Hᶠᶠ of corner (i, j0 + R); the others are rec[r + 1].y
+    T rdyc[R + 1], dyc[R + 1], rdyf[R + 1], dyf[R];
+    E ex[R];
+#pragma unroll
+    for (int r = 0; r < R + 2; ++r) {
+        int k = g.idx(i, j0 - 1 + r);
+        msk[r] = __ldg(o.mask + k);
+        raw[r] = src(k, i, j0 - 1 + r);
+    }
+#pragma unroll
+    for (int r = 0; r < R + 1; ++r) {
+        int jc = j0 - 1 + r;
+        rec[r] = o.coef[g.idx(i, jc)];
+        rdyc[r] = g.rdyc[jc];
+        dyc[r] = g.dyc[jc];
+        rdyf[r] = g.rdyf[jc + 1];
+    }
+    cffR = o.coef[g.idx(i, j0 + R)].y;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        dyf[r] = g.dyf[j0 + r];
+        if (own_col) ex[r] = extra(g.idx(i, j0 + r));
+    }
+    auto mu = [&](int a) { return (msk[a] & U_INACTIVE) ? T(0) : raw[a].x; };
+    auto mv = [&](int a) { return (msk[a] & V_INACTIVE) ? T(0) : raw[a].y; };
+    auto cff = [&](int c) { return c < R ? rec[c + 1].y : cffR; };
+
+    auto centre = [&](int a, int c, T& sxx, T& syy) {
+        T u0 = mu(a), v0 = mv(a), vn = mv(a + 1);
+        T ue = __shfl_down_sync(full, u0, 1);
+        T exx = (ue - u0) * rdxc_i;
+        T eyy = (vn - v0) * rdyc[c];
+        T eta = rec[c].x;
+        sxx = dyc[c] * (T(2) * eta * (T(2) * exx + eyy));
+        syy = dxc_i * (T(2) * eta * (T(2) * eyy + exx));
+    };
+    auto corner = [&](int a, int c) -> T {
+        T u0 = mu(a), us = mu(a - 1), v0 = mv(a);
+        T vw = __shfl_up_sync(full, v0, 1);
+        T dudy = (u0 - us) * rdyf[c];
+        T dvdx = (v0 - vw) * rdxf_i;
+        T e = dudy + dvdx;
+        return cff(c) * e;
+    };
+
+    T sxx_s, syy_s;
+    centre(0, 0, sxx_s, syy_s);
+    T t_c = corner(1, 0);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        T sxx, syy;
+        centre(r + 1, r + 1, sxx, syy);
+        T t_n = corner(r + 2, r + 1);
+        T sxx_w = __shfl_up_sync(full, sxx, 1);
+        T t_e = __shfl_down_sync(full, t_c, 1);
+        if (own_col) {
+            const V4& c = rec[r + 1];
+            const V2& x = raw[r + 1];
+            T divu = (sxx - sxx_w) + (dxf_i * t_n - dxf_i * t_c);
+            T divv = (syy - syy_s) + (dyf[r] * t_e - dyf[r] * t_c);
+            V2 q;
+            q.x = (msk[r + 1] & IU) ? x.x : (dxf_i * dyc[r + 1]) * c.z * x.x - divu;
+            q.y = (msk[r + 1] & IV) ? x.y : (dxc_i * dyf[r]) * c.w * x.y - divv;
+            emit(g.idx(i, j0 + r), q, x, ex[r]);
+        }
+        syy_s = syy;
+        t_c = t_n;
+    }
+}
+
+// The walk of the calling warp: the interior form when all its columns and rows are strictly inside the grid
+// (warp-uniform test), the general one otherwise.
+template <int R, uint8_t IU = U_IDENTITY, uint8_t IV = V_IDENTITY, typename T, typename Src, typename Extra, typename Emit>
+__device__ __forceinline__ void strip_apply_src(const OpView<T>& o, Src&& src, int i, int j0, Extra&& extra, Emit&& emit) {
+    const int i_first = i - (int)threadIdx.x;
+    const bool interior = i_first >= 1 && i_first + 31 <= o.g.Nx - 2 && j0 - 1 >= 1 && j0 + R <= o.g.Ny - 2;
+    if (interior) strip_apply_interior<R, IU, IV>(o, src, i, j0, extra, emit);
+    else strip_apply_general<R, IU, IV>(o, src, i, j0, extra, emit);
 }
 
 // strip_apply_src with the operand read from an array.

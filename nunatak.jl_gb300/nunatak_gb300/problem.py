@@ -192,15 +192,23 @@ class Problem:
     def step_enthalpy(self, dt, thermal_conductivity=2.1, heat_capacity=2009.0, latent_heat=3.34e5, clausius_clapeyron=7.9e-8,
                       melting_temperature=273.15, reference_temperature=223.15, temperate_diffusivity_ratio=1e-3,
                       enthalpy_blend_width=1.0, water_layer_blend_thickness=1e-3, minimum_thickness=1.0,
-                      drainage_water_fraction=0.01, maximum_drainage_rate=1.58443823077064e-9, grounded_melt_coupling=True):
+                      drainage_water_fraction=0.01, maximum_drainage_rate=1.58443823077064e-9, grounded_melt_coupling=True,
+                      rate_factor=None):
         """One energy step of length dt (step_thermodynamics!, src/Thermodynamics/column_energy_solve.jl:26-78) from
         the velocities and viscosity of the last solve (velocity_profile first); defaults: EnthalpyThermodynamics'
-        (src/Thermodynamics/enthalpy_thermodynamics.jl:92-104)."""
+        (src/Thermodynamics/enthalpy_thermodynamics.jl:92-104).  The step leaves the rate factor as it was; with
+        `rate_factor` (a dict of compute_thermal_diagnostics' keywords, {} for the ArrheniusRateFactor defaults) the
+        rate factor follows the new enthalpy, as advance_enthalpy! ends with update_thermal_diagnostics! (:85-97)."""
         prm = abi.EnergyParams(thermal_conductivity, heat_capacity, latent_heat, clausius_clapeyron, melting_temperature,
                                reference_temperature, temperate_diffusivity_ratio, enthalpy_blend_width,
                                water_layer_blend_thickness, minimum_thickness, drainage_water_fraction, maximum_drainage_rate,
                                int(grounded_melt_coupling), 0)
         _check(self._fn("step_enthalpy")(self._h, C.byref(prm), float(dt)), "step_enthalpy", self._err())
+        if rate_factor is not None:
+            self.compute_thermal_diagnostics(**dict(dict(heat_capacity=heat_capacity, latent_heat=latent_heat,
+                                                         clausius_clapeyron=clausius_clapeyron,
+                                                         melting_temperature=melting_temperature,
+                                                         reference_temperature=reference_temperature), **rate_factor))
 
     def set_front(self, front):
         """The masking becomes a PartialCellFront (src/Models/partial_cell_front.jl): its 0/1 flag of full cells is the
