@@ -47,6 +47,7 @@ __device__ __forceinline__ double rate_factor(const PhysView& ph, int c, int k) 
 
 // compute_viscosity! (glen_flow_law.jl:97-111) fused with compute_column_integrals! (column_integrals.jl:54-72)
 __global__ void k_viscosity(PhysView ph, const double2* __restrict__ x, double* eta_sigma, double4* coef, double* F2) {
+    NK_BATCH_ENTER(ph.g, ph, x, eta_sigma, coef, F2)
     const DevGrid<double>& g = ph.g;
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i >= g.Nx || j >= g.Ny) return;
@@ -73,6 +74,7 @@ void launch_viscosity(const PhysView& ph, const double2* x, double* eta_sigma, d
 // ε̇xz = ℑxᶜ(βᵇᵘ uᵇ)(1 - ζ) / 2η⁻ with the previous viscosity η⁻ (left out where η⁻ is still zero)
 __global__ void k_viscosity_diva(PhysView ph, const double2* __restrict__ x, const double2* __restrict__ bb,
                                  const double2* __restrict__ ub, double* eta_sigma, double4* coef, double* F2) {
+    NK_BATCH_ENTER(ph.g, ph, x, bb, ub, eta_sigma, coef, F2)
     const DevGrid<double>& g = ph.g;
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i >= g.Nx || j >= g.Ny) return;
@@ -108,6 +110,7 @@ void launch_viscosity_diva(const PhysView& ph, const double2* x, const double2* 
 // _interpolate_to_corners! (stress_balance_coefficients.jl:26-29): ℑxyᶠᶠᵃ = ℑyᵃᶠᵃ(ℑxᶠᵃᵃ(η̄H))
 template <typename T>
 __global__ void k_corners(DevGrid<T> g, typename Vec4<T>::type* coef) {
+    NK_BATCH_ENTER(g, g, coef)
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i > g.Nx || j > g.Ny) return;
     T lo = (coef[g.c_idx(i - 1, j - 1)].x + coef[g.c_idx(i, j - 1)].x) / T(2);
@@ -132,6 +135,7 @@ __device__ __forceinline__ double basal_drag(const PhysView& ph, double U, doubl
 
 // _compute_x_basal_drag! / _compute_y_basal_drag!, frictions.jl:142-160, over size(βᵘ), size(βᵛ)
 __global__ void k_basal_drag(PhysView ph, const double2* __restrict__ x, double4* coef, double2* bb) {
+    NK_BATCH_ENTER(ph.g, ph, x, coef, bb)
     const DevGrid<double>& g = ph.g;
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i > g.Nx || j > g.Ny) return;
@@ -184,6 +188,7 @@ __device__ __forceinline__ double y_shear_factor(const DevGrid<double>& g, doubl
 
 __global__ void k_basal_velocity(PhysView ph, const double2* __restrict__ x, const double2* __restrict__ bb, const double* __restrict__ F2,
                                  double2* ub) {
+    NK_BATCH_ENTER(ph.g, ph, x, bb, F2, ub)
     const DevGrid<double>& g = ph.g;
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i > g.Nx || j > g.Ny) return;
@@ -201,6 +206,7 @@ void launch_basal_velocity(const PhysView& ph, const double2* x, const double2* 
 }
 
 __global__ void k_effective_drag(PhysView ph, const double2* __restrict__ bb, const double* __restrict__ F2, double4* coef) {
+    NK_BATCH_ENTER(ph.g, ph, bb, F2, coef)
     const DevGrid<double>& g = ph.g;
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i > g.Nx || j > g.Ny) return;

@@ -64,6 +64,11 @@ struct DevGrid {
     int px, py;                         // periodic flags
     const T* dxc; const T* dxf; const T* dyc; const T* dyf;      // spacings
     const T* rdxc; const T* rdxf; const T* rdyc; const T* rdyf;  // their reciprocals
+    // A batched launch (gridDim.z slots of identical problems whose device arenas lie slot_stride bytes apart):
+    // slot z of a block shifts every pointer by z * slot_stride and stops when its Picard flag p_done (slot 0's,
+    // shifted the same way) is set.  Zero and null outside a batch.
+    long long slot_stride = 0;
+    const int* p_done = nullptr;
 
     __device__ __forceinline__ int idx(int i, int j) const { return j * pitch + i; }
     __device__ __forceinline__ static int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
@@ -218,7 +223,58 @@ __device__ __forceinline__ bool grid_sum2(double a, double b, double2* partials,
     return true;   // totals valid in thread 0
 }
 
+// ---- batched launches ------------------------------------------------------------------------------------
+// `p` moved by d bytes (null stays null): the same buffer in another slot of a batch.  Q is a pointer type,
+// restrict-qualified or not (anything else fails the casts).
+template <typename Q>
+__device__ __forceinline__ void shift_ptr(Q& p, long long d) {
+    if (p) p = reinterpret_cast<Q>(reinterpret_cast<unsigned long long>(p) + (unsigned long long)d);
+}
+template <typename T>
+__device__ __forceinline__ void rebase(DevGrid<T>& g, long long d) {
+    shift_ptr(g.dxc, d); shift_ptr(g.dxf, d); shift_ptr(g.dyc, d); shift_ptr(g.dyf, d);
+    shift_ptr(g.rdxc, d); shift_ptr(g.rdxf, d); shift_ptr(g.rdyc, d); shift_ptr(g.rdyf, d);
+    shift_ptr(g.p_done, d);
+}
+template <typename Q>
+__device__ __forceinline__ void rebase(Q& p, long long d) { shift_ptr(p, d); }   // a pointer (restrict-qualified or not)
+// The byte shift of this block's slot; false when the slot has stopped (its Picard flag is set).
+template <typename T>
+__device__ __forceinline__ bool batch_slot(const DevGrid<T>& g, long long& d) {
+    d = 0;
+    if (!g.slot_stride) return true;
+    d = (long long)blockIdx.z * g.slot_stride;
+    const int* pd = g.p_done;
+    shift_ptr(pd, d);
+    return !*(volatile const int*)pd;
+}
+inline __device__ void rebase_all(long long) {}
+template <typename A, typename... Rest>
+__device__ __forceinline__ void rebase_all(long long d, A& a, Rest&... rest) {
+    rebase(a, d);
+    rebase_all(d, rest...);
+}
+// First statement of every kernel of the solve: under a batched launch, stop for a finished slot and move the
+// listed views and pointers (G's grid first) to this block's slot.
+#define NK_BATCH_ENTER(G, ...)                                              \
+    {                                                                       \
+        long long nk_slot_shift_;                                           \
+        if (!::nk::batch_slot((G), nk_slot_shift_)) return;                  \
+        if (nk_slot_shift_) ::nk::rebase_all(nk_slot_shift_, __VA_ARGS__);   \
+    }
+
 // ---- host side helpers ------------------------------------------------------------------------------------
+// Slots of the batched launch being captured on this host thread (1 outside); the grid helpers below give every
+// launch that many z blocks.
+int batch_slots();
+void set_batch_slots(int n);
+// Sets the slot count for the lifetime of the scope (graph capture of a batch).
+struct BatchScope {
+    explicit BatchScope(int n) { set_batch_slots(n); }
+    ~BatchScope() { set_batch_slots(1); }
+    BatchScope(const BatchScope&) = delete;
+    BatchScope& operator=(const BatchScope&) = delete;
+};
 // Kernels launched by the library in this process (instrumentation; every launch site calls count_launch()).
 void count_launch();
 void count_launches(long long n);
@@ -235,13 +291,13 @@ constexpr int VEC_ROWS = 4;
 inline LaunchDims vec_dims(int nx, int ny) {
     LaunchDims d;
     d.block = dim3(BX, BY);
-    d.grid = dim3((nx + BX - 1) / BX, (ny + BY * VEC_ROWS - 1) / (BY * VEC_ROWS));
+    d.grid = dim3((nx + BX - 1) / BX, (ny + BY * VEC_ROWS - 1) / (BY * VEC_ROWS), batch_slots());
     return d;
 }
 inline LaunchDims dims2d(int nx, int ny) {
     LaunchDims d;
     d.block = dim3(BX, BY);
-    d.grid = dim3((nx + BX - 1) / BX, (ny + BY - 1) / BY);
+    d.grid = dim3((nx + BX - 1) / BX, (ny + BY - 1) / BY, batch_slots());
     return d;
 }
 

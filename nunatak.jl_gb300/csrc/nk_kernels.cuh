@@ -15,6 +15,9 @@ struct SigmaTable {
     const double* w1;     // profile_weight(k', k, 1) at [k * N + k'] for k' <= k
     const double* zf;     // znode(k, Face), the N + 1 faces
 };
+__device__ __forceinline__ void rebase(SigmaTable& t, long long d) {
+    shift_ptr(t.dz, d); shift_ptr(t.w2, d); shift_ptr(t.zc, d); shift_ptr(t.w1, d); shift_ptr(t.zf, d);
+}
 
 // Fine-grid inputs of the coefficient update (all FP64, pitched; pairs interleave the u and v faces).
 struct PhysView {
@@ -34,6 +37,12 @@ struct PhysView {
     int use_mask, use_N;
     const double2* ud = nullptr;      // prescribed (u, v) per face, NaN where free
 };
+__device__ __forceinline__ void rebase(PhysView& v, long long d) {
+    rebase(v.g, d);
+    rebase(v.sig, d);
+    shift_ptr(v.A, d); shift_ptr(v.H, d); shift_ptr(v.C, d); shift_ptr(v.N, d); shift_ptr(v.mu, d); shift_ptr(v.phi, d);
+    shift_ptr(v.ud, d);
+}
 
 // ---- layout conversion ---------------------------------------------------------------------------------
 // dst[(j * pitch + i) * stride + offset] = src[j * nx + i] for i < nx, j < ny, `planes` planes.
@@ -68,6 +77,12 @@ struct CGView {
     float2* zold32;               // mixed precision: z_old kept as the FP32 z32 it equals exactly (or nullptr);
                                   // z itself is then never stored: each kernel that needs it rescales z32
 };
+__device__ __forceinline__ void rebase(CGView& v, long long d) {
+    rebase(v.o, d);
+    shift_ptr(v.x, d); shift_ptr(v.b, d); shift_ptr(v.r, d); shift_ptr(v.z, d); shift_ptr(v.p, d); shift_ptr(v.q, d);
+    shift_ptr(v.zold, d); shift_ptr(v.invd, d); shift_ptr(v.sc, d); shift_ptr(v.partials, d);
+    shift_ptr(v.r32, d); shift_ptr(v.z32, d); shift_ptr(v.zold32, d);
+}
 // r = b - A x; if the preconditioner is not multigrid also z = M r, p = z, rho = r.z; r0, tol, done
 void launch_cg_init(const CGView& v, cudaStream_t s);
 // multigrid: after z = V(r): p = z, rho = r.z, done
@@ -87,7 +102,9 @@ void launch_precondition_diagonal(const DevGrid<double>& g, double2* z, const do
 void launch_copy_range(const DevGrid<double>& g, double2* dst, const double2* src, cudaStream_t s);
 // Picard loop control on the device: begin (iteration 0) and end of one iteration (Δ, X, stopping test),
 // each setting the conditional-node handle `cond` of the Picard while loop
-void launch_picard_begin(SolverScalars* sc, unsigned long long cond, cudaStream_t s);
+void launch_picard_begin(SolverScalars* sc, unsigned long long cond, long long stride, cudaStream_t s);
+// sets `cond` to whether any of `slots` slots (scalars `stride` bytes apart) goes on: Picard (cg = 0) or CG (cg = 1)
+void launch_batch_condition(const SolverScalars* sc, long long stride, int slots, int cg, unsigned long long cond, cudaStream_t s);
 void launch_picard_end(const DevGrid<double>& g, double2* xprev, const double2* x, SolverScalars* sc, double2* partials,
                        unsigned long long cond, cudaStream_t s);
 // the same under the viscosity-change rule (NK_VISCOSITY_CONVERGENCE): Δ = ‖η̄H - η̄H⁻‖, X = ‖η̄H‖, η̄H⁻ = η̄H
@@ -250,6 +267,11 @@ struct LevelView {
     const typename Vec2<T>::type* irs;  // inverse ℓ1 row sums
     int cx, cy;                      // coarsening factor from the finer level (1 or 2)
 };
+template <typename T>
+__device__ __forceinline__ void rebase(LevelView<T>& L, long long d) {
+    rebase(L.o, d);
+    shift_ptr(L.x, d); shift_ptr(L.x2, d); shift_ptr(L.b, d); shift_ptr(L.q, d); shift_ptr(L.t, d); shift_ptr(L.irs, d);
+}
 // Mean device time in ms of `repeats` launches of one level's sweep (kind STRIP_SMOOTH, x -> x2) or residual
 // (STRIP_RESIDUAL, into q) with walks of `rows` rows; negative if a CUDA call failed (the strip autotuner)
 template <typename T>
@@ -290,6 +312,10 @@ void launch_prolongate(const LevelView<T>& fine, const LevelView<T>& coarse, typ
                        const typename Vec2<T>::type* x_coarse, const int* done, cudaStream_t s);
 template <typename T>
 void launch_zero_vec(const DevGrid<T>& g, typename Vec2<T>::type* x, const int* done, cudaStream_t s);
+// dst = src over the first n entries of a level's pitched plane (batch-aware device copy)
+template <typename T>
+void launch_copy_plane(const DevGrid<T>& g, typename Vec2<T>::type* dst, const typename Vec2<T>::type* src, int n, const int* done,
+                       cudaStream_t s);
 // Every level from one level down to the coarsest, handled by a single thread block.
 constexpr int MAX_COARSE_LEVELS = 12;
 template <typename T>

@@ -65,6 +65,7 @@ __device__ __forceinline__ void parents(int i, int Nc, bool periodic, bool face,
 template <typename T, typename TF>
 __global__ void k_coarsen(OpView<T> co, int cxf, int cyf, DevGrid<TF> fg, const typename Vec4<TF>::type* __restrict__ fcoef,
                           typename Vec4<T>::type* ccoef) {
+    NK_BATCH_ENTER(co.g, co, fg, fcoef, ccoef)
     const DevGrid<T>& cg = co.g;
     int I = blockIdx.x * BX + threadIdx.x, J = blockIdx.y * BY + threadIdx.y;
     if (I >= cg.Nx || J >= cg.Ny) return;
@@ -253,6 +254,7 @@ __device__ __forceinline__ void line_relax_column(const LevelView<T>& L, typenam
 template <typename T>
 __global__ void k_smooth_first(LevelView<T> L, const typename Vec2<T>::type* __restrict__ xin, typename Vec2<T>::type* __restrict__ xout,
                                const int* done) {
+    NK_BATCH_ENTER(L.o.g, L, xin, xout, done)
     if (stopped(done)) return;
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i < L.o.g.Nx && j < L.o.g.Ny) smooth_point_at(L, xin, xout, true, i, j);
@@ -264,6 +266,7 @@ __global__ void k_smooth_first(LevelView<T> L, const typename Vec2<T>::type* __r
 template <typename T, int R>
 __global__ void __launch_bounds__(32 * STRIP_WARPS) k_smooth_point(LevelView<T> L, const typename Vec2<T>::type* __restrict__ xin,
                                                                   typename Vec2<T>::type* __restrict__ xout, const int* done) {
+    NK_BATCH_ENTER(L.o.g, L, xin, xout, done)
     if (stopped(done)) return;
     using V2 = typename Vec2<T>::type;
     int i, j0;
@@ -296,6 +299,7 @@ void launch_smooth_point(const LevelView<T>& L, const typename Vec2<T>::type* x_
 template <typename T, int R>
 __global__ void __launch_bounds__(32 * STRIP_WARPS) k_smooth_first2(LevelView<T> L, typename Vec2<T>::type* __restrict__ xout,
                                                                    const int* done) {
+    NK_BATCH_ENTER(L.o.g, L, xout, done)
     if (stopped(done)) return;
     using V2 = typename Vec2<T>::type;
     int i, j0;
@@ -335,6 +339,7 @@ void launch_smooth_first2(const LevelView<T>& L, typename Vec2<T>::type* x_out, 
 template <typename T, int R>
 __global__ void __launch_bounds__(32 * STRIP_WARPS) k_level_apply(LevelView<T> L, const typename Vec2<T>::type* __restrict__ x,
                                                                  typename Vec2<T>::type* __restrict__ q, int residual, const int* done) {
+    NK_BATCH_ENTER(L.o.g, L, x, q, done)
     if (stopped(done)) return;
     using V2 = typename Vec2<T>::type;
     int i, j0;
@@ -384,6 +389,7 @@ float time_strip_kernel(const LevelView<T>& L, int kind, int rows, int repeats, 
 
 template <typename T>
 __global__ void k_line_relax(LevelView<T> L, typename Vec2<T>::type* x, int first, const int* done) {
+    NK_BATCH_ENTER(L.o.g, L, x, done)
     if (stopped(done)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= L.o.g.Nx) return;
@@ -391,7 +397,7 @@ __global__ void k_line_relax(LevelView<T> L, typename Vec2<T>::type* x, int firs
 }
 template <typename T>
 void launch_line_relax(const LevelView<T>& L, typename Vec2<T>::type* x, int first, const int* done, cudaStream_t s) {
-    int nb = (L.o.g.Nx + 127) / 128;
+    dim3 nb((L.o.g.Nx + 127) / 128, 1, batch_slots());
     k_line_relax<T><<<nb, 128, 0, s>>>(L, x, first, done); count_launch();
 }
 
@@ -449,6 +455,7 @@ __device__ __forceinline__ void restrict_interior(const LevelView<T>& C, const O
 template <typename T>
 __global__ void k_restrict(LevelView<T> C, OpView<T> fo, const typename Vec2<T>::type* __restrict__ rf,
                            typename Vec2<T>::type* bc, typename Vec2<T>::type* first_out, const int* done) {
+    NK_BATCH_ENTER(C.o.g, C, fo, rf, bc, first_out, done)
     if (stopped(done)) return;
     int I = blockIdx.x * BX + threadIdx.x, J = blockIdx.y * BY + threadIdx.y;
     const DevGrid<T>& cg = C.o.g;
@@ -498,6 +505,7 @@ __device__ __forceinline__ void prolong_interior(const OpView<T>& fo, const Leve
 template <typename T>
 __global__ void k_prolongate(OpView<T> fo, LevelView<T> C, typename Vec2<T>::type* xf, const typename Vec2<T>::type* __restrict__ xc,
                              const int* done) {
+    NK_BATCH_ENTER(fo.g, fo, C, xf, xc, done)
     if (stopped(done)) return;
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i >= fo.g.Nx || j >= fo.g.Ny) return;
@@ -515,6 +523,7 @@ void launch_prolongate(const LevelView<T>& fine, const LevelView<T>& coarse, typ
 
 template <typename T>
 __global__ void k_zero_vec(DevGrid<T> g, typename Vec2<T>::type* x, const int* done) {
+    NK_BATCH_ENTER(g, g, x, done)
     if (stopped(done)) return;
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i > g.Nx || j > g.Ny) return;
@@ -527,6 +536,22 @@ template <typename T>
 void launch_zero_vec(const DevGrid<T>& g, typename Vec2<T>::type* x, const int* done, cudaStream_t s) {
     LaunchDims d = dims2d(g.Nx + 1, g.Ny + 1);
     k_zero_vec<T><<<d.grid, d.block, 0, s>>>(g, x, done); count_launch();
+}
+
+// dst = src over a level's whole pitched plane (halo and padding included), the batched form of a device copy:
+// a plain copy in a batched graph would move slot 0 alone.
+template <typename T>
+__global__ void k_copy_plane(DevGrid<T> g, typename Vec2<T>::type* dst, const typename Vec2<T>::type* __restrict__ src, int n,
+                             const int* done) {
+    NK_BATCH_ENTER(g, g, dst, src, done)
+    if (stopped(done)) return;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) dst[t] = src[t];
+}
+template <typename T>
+void launch_copy_plane(const DevGrid<T>& g, typename Vec2<T>::type* dst, const typename Vec2<T>::type* src, int n, const int* done,
+                       cudaStream_t s) {
+    dim3 grid((n + 255) / 256, 1, batch_slots());
+    k_copy_plane<T><<<grid, 256, 0, s>>>(g, dst, src, n, done); count_launch();
 }
 
 // ---- the coarsest level in shared memory ----------------------------------------------------------------------
@@ -544,6 +569,7 @@ template <typename T>
 __global__ void __launch_bounds__(1024, 1)
     k_coarsest_smem_1(LevelView<T> L, int plane, const typename Vec2<T>::type* __restrict__ xin, int sweeps, int from_zero,
                       typename Vec2<T>::type* xout, const int* done) {
+    NK_BATCH_ENTER(L.o.g, L, xin, xout, done)
     if (stopped(done)) return;
     using V2 = typename Vec2<T>::type;
     const DevGrid<T>& g = L.o.g;
@@ -710,7 +736,7 @@ void launch_coarsest_smem(const LevelView<T>& L, int plane, const typename Vec2<
         int nx = L.o.g.Nx, ny = L.o.g.Ny;
         size_t bytes = (size_t)plane * sizeof(typename Vec2<T>::type) + (size_t)nx * ny * sizeof(typename Vec2<T>::type) +
                        (size_t)(nx + 2) * (ny + 2) * sizeof(typename Vec2<T>::type) + (size_t)(nx + 1) * (ny + 1) * sizeof(T);
-        k_coarsest_smem_1<T><<<1, 1024, bytes, s>>>(L, plane, x_in, sweeps, from_zero, x_out, done);
+        k_coarsest_smem_1<T><<<dim3(1, 1, batch_slots()), 1024, bytes, s>>>(L, plane, x_in, sweeps, from_zero, x_out, done);
         count_launch();
     }
 }
@@ -807,6 +833,7 @@ void launch_coarse_vcycle(const CoarseLevels<T>& C, const int* done, cudaStream_
     template void launch_prolongate<T>(const LevelView<T>&, const LevelView<T>&, Vec2<T>::type*, const Vec2<T>::type*, const int*, \
                                        cudaStream_t);                                                                               \
     template void launch_zero_vec<T>(const DevGrid<T>&, Vec2<T>::type*, const int*, cudaStream_t);                                 \
+    template void launch_copy_plane<T>(const DevGrid<T>&, Vec2<T>::type*, const Vec2<T>::type*, int, const int*, cudaStream_t);    \
     template void launch_coarse_vcycle<T>(const CoarseLevels<T>&, const int*, cudaStream_t);                     \
     template float time_strip_kernel<T>(const LevelView<T>&, int, int, int, cudaStream_t);
 

@@ -17,6 +17,12 @@ struct OpView {
     const uint8_t* mask;                  // U/V_INACTIVE, _WALL, _DIRICHLET bits per (i, j)
     T wall_factor;                        // wall_shear_factor: 0 free slip, 2 no slip (strain_rates.jl:11-12)
 };
+template <typename T>
+__device__ __forceinline__ void rebase(OpView<T>& o, long long d) {
+    rebase(o.g, d);
+    shift_ptr(o.coef, d);
+    shift_ptr(o.mask, d);
+}
 
 // interior_u / interior_v (strain_rates.jl:5-6) with the operator's mask (walls and ice-free points); a prescribed
 // face passes its value (U_DIRICHLET / V_DIRICHLET).

@@ -876,7 +876,7 @@ static void build_picard_graph(nk_problem* P) {
     NK_CUDA(cudaGraphCreate(&g, 0));
     cudaGraphConditionalHandle hp;
     NK_CUDA(cudaGraphConditionalHandleCreate(&hp, g, 0, 0));
-    capture_into(P, g, {}, [&] { launch_picard_begin(P->sc, hp, P->stream); });
+    capture_into(P, g, {}, [&] { launch_picard_begin(P->sc, hp, 0, P->stream); });
     cudaGraph_t body = add_while(g, leaves(g), hp);
     cudaGraphConditionalHandle hc;
     NK_CUDA(cudaGraphConditionalHandleCreate(&hc, body, 0, 0));
@@ -954,7 +954,7 @@ static void host_cg(nk_problem* P, const double2* b) {
 }
 
 static void host_picard(nk_problem* P) {
-    launch_picard_begin(P->sc, 0, P->stream);
+    launch_picard_begin(P->sc, 0, 0, P->stream);
     read_scalars(P);
     while (!P->sc_host->p_done) {
         launch_copy_range(P->fine.g, P->xprev, P->x, P->stream);

@@ -22,6 +22,9 @@ static thread_local bool g_capturing = false;   // launches recorded into a grap
 void count_launch() { if (!g_capturing) g_launches.fetch_add(1, std::memory_order_relaxed); }
 void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 void set_capturing(bool on) { g_capturing = on; }
+static thread_local int g_batch_slots = 1;
+int batch_slots() { return g_batch_slots; }
+void set_batch_slots(int n) { g_batch_slots = n < 1 ? 1 : n; }
 long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 // ---- layout conversion --------------------------------------------------------------------------------
@@ -87,6 +90,7 @@ void launch_apply(const OpView<double>& o, const double2* p, double2* q, cudaStr
 // fine level only) marks prescribed faces as identity rows that keep their value (U_DIRICHLET / V_DIRICHLET)
 template <typename T>
 __global__ void k_mask(OpView<T> o, uint8_t* mask, const double2* ud) {
+    NK_BATCH_ENTER(o.g, o, mask, ud)
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     const DevGrid<T>& g = o.g;
     if (i > g.Nx || j > g.Ny) return;
@@ -132,6 +136,7 @@ void launch_impose_prescribed(const DevGrid<double>& g, double2* x, const double
 }
 
 __global__ void k_inverse_diagonal(OpView<double> o, double2* invd) {
+    NK_BATCH_ENTER(o.g, o, invd)
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i >= o.g.Nx || j >= o.g.Ny) return;
     uint8_t m = o.mask[o.g.idx(i, j)];
@@ -144,6 +149,7 @@ void launch_inverse_diagonal(const OpView<double>& o, double2* invd, cudaStream_
 
 template <typename T>
 __global__ void k_inverse_row_sum(OpView<T> o, typename Vec2<T>::type* irs) {
+    NK_BATCH_ENTER(o.g, o, irs)
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i >= o.g.Nx || j >= o.g.Ny) return;
     uint8_t m = o.mask[o.g.idx(i, j)];
@@ -172,6 +178,7 @@ __device__ __forceinline__ int stop_after(const SolverScalars* sc, double rnorm,
 // conjugate_gradient!, conjugate_gradient.jl:165-171: r = b - A x, z = M r, p = z, rho = r.z
 template <int R>
 __global__ void __launch_bounds__(32 * STRIP_WARPS) k_cg_init(CGView v) {
+    NK_BATCH_ENTER(v.o.g, v)
     int i, j0;
     strip_origin<R>(i, j0);
     double rz = 0.0, rr = 0.0;
@@ -221,6 +228,7 @@ void launch_cg_init(const CGView& v, cudaStream_t s) {
 
 // mixed precision start: the FP32 copy of r0 for the first V-cycle, scaled by 2^-e with e the exponent of ‖r0‖
 __global__ void k_cg_scale_r32(CGView v) {
+    NK_BATCH_ENTER(v.o.g, v)
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     int e = v.sc->r32_exp;   // set with ‖r0‖ by the last block of k_cg_init
     if (i < v.o.g.Nx && j < v.o.g.Ny) {
@@ -236,6 +244,7 @@ void launch_cg_scale_r32(const CGView& v, cudaStream_t s) {
 
 // multigrid start: p = z, rho = r.z (and z_old = z for flexible conjugate gradients)
 __global__ void k_cg_init_finish(CGView v) {
+    NK_BATCH_ENTER(v.o.g, v)
     int i = blockIdx.x * BX + threadIdx.x, j0 = blockIdx.y * BY * VEC_ROWS + threadIdx.y;
     double rz = 0.0;
 #pragma unroll
@@ -272,6 +281,7 @@ void launch_cg_init_finish(const CGView& v, cudaStream_t s) {
 // conjugate_gradient_step!, conjugate_gradient.jl:209-212: q = A p, alpha = rho / p.q (0 if p.q = 0)
 template <int R>
 __global__ void __launch_bounds__(32 * STRIP_WARPS) k_cg_apply(CGView v) {
+    NK_BATCH_ENTER(v.o.g, v)
     if (read_done(v.sc)) return;
     int i, j0;
     strip_origin<R>(i, j0);
@@ -299,6 +309,7 @@ void launch_cg_apply(const CGView& v, cudaStream_t s) {
 
 // conjugate_gradient_step!, conjugate_gradient.jl:214-219 and the stopping test of :193-197
 __global__ void k_cg_update(CGView v) {
+    NK_BATCH_ENTER(v.o.g, v)
     if (read_done(v.sc)) return;
     int i = blockIdx.x * BX + threadIdx.x, j0 = blockIdx.y * BY * VEC_ROWS + threadIdx.y;
     double alpha = v.sc->alpha;
@@ -360,6 +371,7 @@ void launch_cg_update(const CGView& v, cudaStream_t s) {
 // after z = V-cycle(r): rho_new = r.z; beta = rho_new / rho, or the flexible (Polak-Ribière) form
 // beta = (r.z - r.z_old) / rho when the preconditioner varies between steps
 __global__ void k_cg_dots_after_precondition(CGView v) {
+    NK_BATCH_ENTER(v.o.g, v)
     if (read_done(v.sc)) return;
     int i = blockIdx.x * BX + threadIdx.x, j0 = blockIdx.y * BY * VEC_ROWS + threadIdx.y;
     double rz = 0.0, rzo = 0.0;
@@ -405,6 +417,7 @@ void launch_cg_dots_after_precondition(const CGView& v, cudaStream_t s) {
 
 // xpby!(z, beta, p), conjugate_gradient.jl:220; the last block commits the stopping decision
 __global__ void k_cg_xpby(CGView v) {
+    NK_BATCH_ENTER(v.o.g, v)
     if (read_done(v.sc)) return;
     int i = blockIdx.x * BX + threadIdx.x, j0 = blockIdx.y * BY * VEC_ROWS + threadIdx.y;
     double beta = v.sc->beta;
@@ -449,6 +462,7 @@ void launch_cg_xpby(const CGView& v, cudaStream_t s) {
 
 // precondition!(z, ::StressBalanceDiagonalPreconditioner, r, ...) over size(z.u), size(z.v)
 __global__ void k_precondition_diagonal(DevGrid<double> g, double2* z, const double2* __restrict__ r, const double2* __restrict__ invd) {
+    NK_BATCH_ENTER(g, g, z, r, invd)
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i > g.Nx || j > g.Ny) return;
     int k = g.idx(i, j);
@@ -468,6 +482,7 @@ void launch_precondition_diagonal(const DevGrid<double>& g, double2* z, const do
 
 // ---- Picard -------------------------------------------------------------------------------------------------
 __global__ void k_copy_range(DevGrid<double> g, double2* dst, const double2* __restrict__ src) {
+    NK_BATCH_ENTER(g, g, dst, src)
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i >= g.Nx || j >= g.Ny) return;
     dst[g.idx(i, j)] = src[g.idx(i, j)];
@@ -477,8 +492,13 @@ void launch_copy_range(const DevGrid<double>& g, double2* dst, const double2* sr
     k_copy_range<<<d.grid, d.block, 0, s>>>(g, dst, src); count_launch();
 }
 
-// picard_solve! loop head (picard.jl:71-79): Δ = ∞, X = 0, iteration = 0
-__global__ void k_picard_begin(SolverScalars* sc, unsigned long long cond) {
+// picard_solve! loop head (picard.jl:71-79): Δ = ∞, X = 0, iteration = 0.  Batched (stride ≠ 0): block z starts
+// slot z, whose scalars lie z * stride bytes after `sc`, unless the slot holds no request (p_done set).
+__global__ void k_picard_begin(SolverScalars* sc, unsigned long long cond, long long stride) {
+    if (stride) {
+        shift_ptr(sc, (long long)blockIdx.z * stride);
+        if (*(volatile const int*)&sc->p_done) return;
+    }
     sc->p_it = 0;
     sc->p_D = INFINITY;
     sc->p_X = 0.0;
@@ -489,13 +509,32 @@ __global__ void k_picard_begin(SolverScalars* sc, unsigned long long cond) {
     sc->p_done = !run;
     if (cond) cudaGraphSetConditional(cond, run ? 1u : 0u);
 }
-void launch_picard_begin(SolverScalars* sc, unsigned long long cond, cudaStream_t s) {
-    k_picard_begin<<<1, 1, 0, s>>>(sc, cond); count_launch();
+void launch_picard_begin(SolverScalars* sc, unsigned long long cond, long long stride, cudaStream_t s) {
+    k_picard_begin<<<dim3(1, 1, batch_slots()), 1, 0, s>>>(sc, cond, stride); count_launch();
+}
+
+// The loop conditions of a batched graph, one warp over the slots' scalars: Picard goes on while a slot is still
+// iterating (cg = 0), conjugate gradients while a slot still iterating has not stopped (cg = 1).
+__global__ void k_batch_condition(const SolverScalars* sc, long long stride, int slots, int cg, unsigned long long cond) {
+    int more = 0;
+    for (int z = threadIdx.x; z < slots; z += 32) {
+        const SolverScalars* t = sc;
+        shift_ptr(t, (long long)z * stride);
+        int going = !*(volatile const int*)&t->p_done;
+        if (cg) going = going && !*(volatile const int*)&t->done;
+        more |= going;
+    }
+    more = __any_sync(0xffffffffu, more);
+    if (threadIdx.x == 0) cudaGraphSetConditional(cond, more ? 1u : 0u);
+}
+void launch_batch_condition(const SolverScalars* sc, long long stride, int slots, int cg, unsigned long long cond, cudaStream_t s) {
+    k_batch_condition<<<1, 32, 0, s>>>(sc, stride, slots, cg, cond); count_launch();
 }
 
 // end of one Picard iteration (picard.jl:83-86): x⁻ = x⁻ - x, Δ = ‖x⁻‖, X = ‖x‖, then the loop test of :79
 __global__ void k_picard_end(DevGrid<double> g, double2* xprev, const double2* __restrict__ x, SolverScalars* sc, double2* partials,
                              unsigned long long cond) {
+    NK_BATCH_ENTER(g, g, xprev, x, sc, partials)
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     double dd = 0.0, xx = 0.0;
     if (i < g.Nx && j < g.Ny) {
@@ -537,6 +576,7 @@ void launch_picard_end(const DevGrid<double>& g, double2* xprev, const double2* 
 // X = ‖η̄H‖, then η̄H⁻ = η̄H and the same loop test as k_picard_end.
 __global__ void k_picard_end_viscosity(DevGrid<double> g, const double4* __restrict__ coef, double* eta_prev, SolverScalars* sc,
                                        double2* partials, unsigned long long cond) {
+    NK_BATCH_ENTER(g, g, coef, eta_prev, sc, partials)
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     double dd = 0.0, xx = 0.0;
     if (i < g.Nx && j < g.Ny) {
@@ -573,6 +613,7 @@ void launch_picard_end_viscosity(const DevGrid<double>& g, const double4* coef, 
 
 // ---- vector helpers under the done predicate -------------------------------------------------------------------
 __global__ void k_copy_vec(DevGrid<double> g, double2* dst, const double2* __restrict__ src, const int* done) {
+    NK_BATCH_ENTER(g, g, dst, src, done)
     if (done && *(volatile const int*)done) return;
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i >= g.Nx || j >= g.Ny) return;
@@ -584,6 +625,7 @@ void launch_copy_vec(const DevGrid<double>& g, double2* dst, const double2* src,
 }
 
 __global__ void k_to_float(DevGrid<double> g, const double2* __restrict__ src, float2* dst, const int* done) {
+    NK_BATCH_ENTER(g, g, src, dst, done)
     if (done && *(volatile const int*)done) return;
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i >= g.Nx || j >= g.Ny) return;
@@ -595,6 +637,7 @@ void launch_to_float(const DevGrid<double>& g, const double2* src, float2* dst, 
     k_to_float<<<d.grid, d.block, 0, s>>>(g, src, dst, done); count_launch();
 }
 __global__ void k_to_double(DevGrid<double> g, const float2* __restrict__ src, double2* dst, const int* done) {
+    NK_BATCH_ENTER(g, g, src, dst, done)
     if (done && *(volatile const int*)done) return;
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i >= g.Nx || j >= g.Ny) return;
@@ -606,6 +649,7 @@ void launch_to_double(const DevGrid<double>& g, const float2* src, double2* dst,
     k_to_double<<<d.grid, d.block, 0, s>>>(g, src, dst, done); count_launch();
 }
 __global__ void k_coef_to_float(DevGrid<double> g, const double4* __restrict__ src, float4* dst) {
+    NK_BATCH_ENTER(g, g, src, dst)
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i > g.Nx || j > g.Ny) return;
     double4 a = src[g.idx(i, j)];

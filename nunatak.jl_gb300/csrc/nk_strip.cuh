@@ -26,7 +26,7 @@ constexpr int STRIP_WARPS = 4;   // warps per block, stacked in y
 inline LaunchDims strip_dims(int nx, int ny, int rows) {
     LaunchDims d;
     d.block = dim3(32, STRIP_WARPS);
-    d.grid = dim3((nx + STRIP_COLS - 1) / STRIP_COLS, (ny + rows * STRIP_WARPS - 1) / (rows * STRIP_WARPS));
+    d.grid = dim3((nx + STRIP_COLS - 1) / STRIP_COLS, (ny + rows * STRIP_WARPS - 1) / (rows * STRIP_WARPS), batch_slots());
     return d;
 }
 
