@@ -75,6 +75,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="nunatak", choices=["nunatak", "reference"])
     ap.add_argument("--batch", type=int, default=32, help="requests per step, and solves in flight at once")
+    ap.add_argument("--batch-slots", type=int, default=8,
+                    help="requests of one grid size solved together by one batched graph (nk_batch) in the value and e2e "
+                         "legs; 0 or 1: one solve per request")
     ap.add_argument("--no-cpu-baseline", action="store_true",
                     help="skip the oracle solves (CPU baseline and the mixed-vs-oracle errors of every grid size)")
     ap.add_argument("--no-scaling", action="store_true", help="skip the reference's published scaling benchmark rows")
@@ -362,6 +365,29 @@ class ResidentPool:
         self.free = {}
 
 
+class BatchPool:
+    """Resident batches (nk_batch) of `slots` mixed-precision problems keyed by grid size."""
+
+    def __init__(self, nk, ctx, slots):
+        self.nk, self.ctx, self.slots, self.free, self.created = nk, ctx, slots, {}, 0
+
+    def take(self, case):
+        lst = self.free.setdefault((case.grid.Nx, case.grid.Ny), [])
+        if lst:
+            return lst.pop()
+        self.created += 1
+        return self.nk.Batch(case.grid, case.descriptors(), self.slots, context=self.ctx)
+
+    def give(self, B):
+        self.free[(B.grid.Nx, B.grid.Ny)].append(B)
+
+    def close(self):
+        for lst in self.free.values():
+            for B in lst:
+                B.close()
+        self.free = {}
+
+
 def stage(cases):
     """Every request's input fields copied to HBM (float64 CUDA tensors), plus zero velocities per grid size."""
     import torch
@@ -406,6 +432,51 @@ def run_resident(pool, cases, staged, zeros, in_flight, keep=()):
                 kept[k] = (P.get("u"), P.get("v"))
             del running[id(P)]
             pool.give(P)
+        if not finished:
+            time.sleep(0.0002)
+    return stats, kept
+
+
+def run_batched(pool, cases, staged, zeros, in_flight, keep=()):
+    """run_resident with batches: the oldest queued request and the next queued ones of its grid size (up to the
+    batch's slots and the requests allowed in flight) share one batched solve; a finished batch takes the next group
+    at once.  Returns the per-request stats and the (u, v) of the requests in `keep`."""
+    queue = list(range(len(cases)))
+    running, stats, kept, n_running = {}, [None] * len(cases), {}, 0
+    size = lambda k: (cases[k].grid.Nx, cases[k].grid.Ny)
+
+    def start(ks):
+        B = pool.take(cases[ks[0]])
+        for slot, k in enumerate(ks):
+            P = B.problem(slot)
+            for name, t in staged[k].items():
+                P.set_device(name, t.data_ptr())
+            P.compute_geometry()
+            zu, zv = zeros[size(k)]
+            P.set_device("u", zu.data_ptr())
+            P.set_device("v", zv.data_ptr())
+        B.picard_solve_async(list(range(len(ks))))
+        running[id(B)] = (B, ks)
+
+    while queue or running:
+        while queue and n_running < in_flight:
+            room = min(pool.slots, in_flight - n_running)
+            key = size(queue[0])
+            ks = [k for k in queue if size(k) == key][:room]
+            for k in ks:
+                queue.remove(k)
+            start(ks)
+            n_running += len(ks)
+        finished = [(B, ks) for B, ks in running.values() if B.query()]
+        for B, ks in finished:
+            st = B.wait()
+            for slot, k in enumerate(ks):
+                stats[k] = st[slot]
+                if k in keep:
+                    kept[k] = (B.problem(slot).get("u"), B.problem(slot).get("v"))
+            del running[id(B)]
+            n_running -= len(ks)
+            pool.give(B)
         if not finished:
             time.sleep(0.0002)
     return stats, kept
@@ -744,6 +815,34 @@ def main():
     pool.close()
     del staged, zeros
     torch.cuda.empty_cache()
+    unbatched = None
+    if args.batch_slots > 1:
+        # ---- the same timed requests in batches: requests of one grid size share one batched graph (nk_batch) -----
+        unbatched = {"value": value, "unit": "solves/s", "ms_per_step": span_ms / args.steps, "wall_s": wall,
+                     "gpu_launches": int(launches), "latency_ms": {"p50": statistics.median(service),
+                                                                    "p99": float(np.percentile(service, 99))},
+                     "mode": f"one solve per request, {B} in flight on {B} streams"}
+        bpool = BatchPool(nk, ctx, args.batch_slots)
+        w_staged, w_zeros = stage(warm_cases)
+        run_batched(bpool, warm_cases, w_staged, w_zeros, B)
+        del w_staged, w_zeros
+        staged, zeros = stage(cases)
+        barrier()
+        created0 = bpool.created
+        launches0 = library.launch_count()
+        with ClockSampler(local_rank) as clocks:
+            t0 = time.perf_counter()
+            stats, kept = run_batched(bpool, cases, staged, zeros, B, keep=set(first_of_size.values()))
+            barrier()
+            wall = time.perf_counter() - t0
+        launches = library.launch_count() - launches0
+        span_ms = max(x.device_end_ms for x in stats) - min(x.device_start_ms for x in stats)
+        value, span_ms = replica_throughput(len(cases), span_ms, world, "cuda")
+        service = [x.device_end_ms - x.device_start_ms for x in stats]
+        created_timed = bpool.created - created0
+        bpool.close()
+        del staged, zeros
+        torch.cuda.empty_cache()
 
     if rank != 0:
         if world > 1:
@@ -767,7 +866,7 @@ def main():
 
     # ---- e2e: the same requests through the serving loop of the C ABI, host buffers, Poisson arrivals ---------
     from nunatak_gb300.server import Server
-    S = Server(max_in_flight=B, memory_cap_bytes=64 << 30, context=ctx)
+    S = Server(max_in_flight=B, memory_cap_bytes=64 << 30, context=ctx, batch_slots=max(args.batch_slots, 0))
     for c in warm_cases:
         S.submit(c)
     S.wait_all()
@@ -793,6 +892,11 @@ def main():
         "dtype": "f32 (multigrid) + f64 (CG, Picard)", "data": "synthetic (seeded marine ice sheets, no dataset)",
         "config": config,
         "timing": {"wall_s": wall, "problems_created_in_timed_region": created_timed},
+        "batching": {"slots": args.batch_slots if args.batch_slots > 1 else 1,
+                     "mode": (f"requests of one grid size solved together, up to {args.batch_slots} per batched graph "
+                              f"(nk_batch; one launch per kernel for every slot), {B} requests in flight"
+                              if args.batch_slots > 1 else "one solve per request")},
+        "unbatched": unbatched,
         "latency_ms": {"p50": statistics.median(service), "p99": float(np.percentile(service, 99)),
                        "note": "device time of each solve (start to end event) while sharing the GPU with the others"},
         "picard_iterations": {"min": min(piters), "max": max(piters)},

@@ -477,6 +477,37 @@ nk_status nk_problem_wait(nk_problem* problem, nk_solve_stats* stats);
  * once), 0 while it runs. */
 nk_status nk_problem_query(nk_problem* problem, int32_t* done);
 
+/* ---- batched solves --------------------------------------------------------------------------------------
+ *
+ * No counterpart in the reference, which solves one grid per picard_solve!.  A batch holds `slots` problems of one
+ * configuration (the same grid, physics and solver descriptors), their device state in one allocation at a fixed
+ * stride, and solves the slots chosen per call with one CUDA graph: every kernel launch of that graph covers all
+ * slots (one z block row per slot), and the Picard and conjugate-gradient loops run until the last chosen slot
+ * has stopped, a slot that has stopped leaving every later launch at once.  Each slot's arithmetic, and so its
+ * result, is that of the same problem solved alone by nk_picard_solve.  For many small solves the GPU is limited
+ * by how fast the host and the graph engine can issue launches, not by the work in them; a batch of S slots
+ * issues the launches of its slowest slot once instead of S times.
+ *
+ * nk_batch_problem gives slot k's problem: set its fields, compute its geometry and read its results with the
+ * nk_problem calls, as for any problem.  All slots share the batch's stream, so those calls and the batched
+ * solve are ordered.  The slots' problems are owned by the batch (do not destroy them) and also solve alone.
+ * Refused (NK_BAD_ARGUMENT): NK_SOLVER_HOST_LOOP, process-wide NK_GRAPHS=0, fused coarse multigrid levels
+ * (NK_COARSE_CELLS > 0 with the mixed solver), and a batched solve of a slot with prescribed velocities. */
+typedef struct nk_batch nk_batch;
+#define NK_MAX_BATCH_SLOTS 1024
+nk_status   nk_batch_create(nk_context* ctx, const nk_grid_desc* grid, const nk_physics_desc* physics,
+                            const nk_solver_desc* solver, int32_t slots, nk_batch** out);
+nk_status   nk_batch_destroy(nk_batch* batch);
+int32_t     nk_batch_slots(const nk_batch* batch);
+nk_problem* nk_batch_problem(nk_batch* batch, int32_t slot);   /* NULL when slot is out of range */
+/* picard_solve! of the slots whose active[k] != 0 (every slot when active is NULL), enqueued on the batch's
+ * stream without waiting.  nk_batch_wait blocks until it has finished and writes `slots` statistics (zeros for the
+ * slots not solved); it returns NK_NONFINITE when a solved slot has, and NK_OK otherwise (read each slot's
+ * status).  nk_batch_query: *done = 1 once finished, without blocking. */
+nk_status   nk_batch_picard_solve_async(nk_batch* batch, const uint8_t* active);
+nk_status   nk_batch_query(nk_batch* batch, int32_t* done);
+nk_status   nk_batch_wait(nk_batch* batch, nk_solve_stats* stats);
+
 /* The whole update_velocities! body for host callers: copies u, v (warm start) in, runs
  * nk_picard_solve and copies u, v out.  u, v in interior layout. */
 nk_status nk_solve_velocities(nk_problem* problem, double* u, double* v, nk_solve_stats* stats);
@@ -545,6 +576,10 @@ typedef struct nk_server_desc {
     int32_t max_in_flight;          /* requests on the device at once (>= 1) */
     int32_t flags;                  /* NK_SERVER_ADMISSION_THREAD or 0 */
     int64_t memory_cap_bytes;       /* device memory reserved for the resident problems */
+    int32_t batch_slots;            /* > 1: requests of one shape are solved together, up to batch_slots per solve, by a
+                                     * resident nk_batch (one launch per kernel for all of them); 0 or 1: one request per
+                                     * solve.  max_in_flight still counts requests. */
+    int32_t reserved;               /* 0 */
 } nk_server_desc;
 /* The server runs its own host thread that retires finished requests and admits queued ones as soon as a slot
  * frees, without the caller driving nk_server_progress / nk_server_wait; the calls below are then thread-safe

@@ -103,8 +103,10 @@ void launch_copy_range(const DevGrid<double>& g, double2* dst, const double2* sr
 // Picard loop control on the device: begin (iteration 0) and end of one iteration (Δ, X, stopping test),
 // each setting the conditional-node handle `cond` of the Picard while loop
 void launch_picard_begin(SolverScalars* sc, unsigned long long cond, long long stride, cudaStream_t s);
-// sets `cond` to whether any of `slots` slots (scalars `stride` bytes apart) goes on: Picard (cg = 0) or CG (cg = 1)
-void launch_batch_condition(const SolverScalars* sc, long long stride, int slots, int cg, unsigned long long cond, cudaStream_t s);
+// sets `cond` to whether any of `slots` slots (scalars `stride` bytes apart) goes on: Picard (cg = 0) or CG (cg = 1);
+// adds one to *counter (if given) when it does
+void launch_batch_condition(const SolverScalars* sc, long long stride, int slots, int cg, unsigned long long cond, int* counter,
+                            cudaStream_t s);
 void launch_picard_end(const DevGrid<double>& g, double2* xprev, const double2* x, SolverScalars* sc, double2* partials,
                        unsigned long long cond, cudaStream_t s);
 // the same under the viscosity-change rule (NK_VISCOSITY_CONVERGENCE): Δ = ‖η̄H - η̄H⁻‖, X = ‖η̄H‖, η̄H⁻ = η̄H

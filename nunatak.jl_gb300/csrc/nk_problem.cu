@@ -186,6 +186,7 @@ struct nk_problem {
     Arena arena;
     bool external_arena = false;              // arena.base sub-allocated by a server (not cudaMalloc'd here)
     bool external_pinned = false;             // sc_host sub-allocated from a server's pinned pool
+    bool external_stream = false;             // `stream` belongs to a batch (nk_batch) shared by its slots
     // fine level (FP64)
     Level<double> fine;                         // metrics, coef, mask, irs (multigrid FP64), x2, q, t
     double *H = nullptr, *bed = nullptr, *s = nullptr, *N = nullptr, *mu = nullptr, *phi = nullptr, *C = nullptr, *F2 = nullptr, *A2 = nullptr;
@@ -619,7 +620,8 @@ static void smooth(nk_problem* P, Level<T>& L, int sweeps, bool first, const int
         in = out;
         k0 = 2;
     } else if (!first && sweeps % 2 == 1) {   // an odd number of ping-pong sweeps starting from L.x would write L.x in place
-        cudaMemcpyAsync(L.x2, L.x, L.plane() * sizeof(V2), cudaMemcpyDeviceToDevice, s);
+        if (batch_slots() > 1) launch_copy_plane<T>(L.g, L.x2, L.x, (int)L.plane(), done, s);
+        else cudaMemcpyAsync(L.x2, L.x, L.plane() * sizeof(V2), cudaMemcpyDeviceToDevice, s);
         in = L.x2;
     }
     for (int k = k0; k < sweeps; ++k) {
@@ -697,7 +699,7 @@ static void precondition_mg(nk_problem* P, const int* done, bool fused = false) 
 //   picard_begin ─► WHILE(picard) { x⁻ = x ─► coefficient update ─► coarse coefficients ─► CG start
 //                                    ─► WHILE(cg) { apply ─► update ─► [V-cycle ─► dots] ─► xpby }
 //                                    ─► picard_end (Δ, X, stopping test) }
-static void set_control(nk_problem* P) {
+static SolverScalars control_scalars(const nk_problem* P) {
     SolverScalars h{};
     const nk_iteration_control& c = P->sd.linear;
     h.reltol = c.reltol;
@@ -712,7 +714,10 @@ static void set_control(nk_problem* P) {
     h.p_fixed = pc.kind == NK_FIXED_ITERATIONS;
     h.p_iterations = pc.iterations;
     h.p_maxiter = pc.maxiter;
-    *P->sc_host = h;
+    return h;
+}
+static void set_control(nk_problem* P) {
+    *P->sc_host = control_scalars(P);
     NK_CUDA(cudaMemcpyAsync(P->sc, P->sc_host, sizeof(SolverScalars), cudaMemcpyHostToDevice, P->stream));
 }
 
@@ -1377,7 +1382,7 @@ nk_status nk_problem_destroy(nk_problem* P) {
     if (P->transport) cudaFree(P->transport);
     if (P->energy) cudaFree(P->energy);
     if (P->front_buf) cudaFree(P->front_buf);
-    if (P->stream) cudaStreamDestroy(P->stream);
+    if (P->stream && !P->external_stream) cudaStreamDestroy(P->stream);
     delete P;
     return NK_OK;
 }
@@ -2225,6 +2230,305 @@ nk_status nk_time_kernel(nk_problem* P, int32_t kernel, int32_t repeats, int64_t
 }  // extern "C"
 
 // =================================================================================================================
+// Batched solves: problems of one configuration in one allocation at a fixed stride, solved by one graph whose
+// launches cover every slot (gridDim.z = slots, the kernels' NK_BATCH_ENTER moving each block to its slot).
+// =================================================================================================================
+struct nk_batch {
+    nk_context* ctx = nullptr;
+    int slots = 0;
+    size_t stride = 0;                   // bytes between two slots' arenas (a multiple of 256)
+    char* base = nullptr;                // slots * stride bytes of arenas, then the loop counters
+    char* pinned = nullptr;              // the slots' own scalars, the control records, the results, the counters
+    bool external = false;               // base and pinned belong to a server
+    int* counters = nullptr;             // device: Picard and CG loop bodies run by the last solve
+    SolverScalars* control = nullptr;    // pinned, one per slot: the solver settings, p_done = 1 for idle slots
+    SolverScalars* results = nullptr;    // pinned, one per slot: the scalars after the solve
+    int* counters_host = nullptr;        // pinned copy of `counters`
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<nk_problem*> P;
+    std::vector<uint8_t> active;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long kernels[3] = {0, 0, 0};    // kernel nodes: top level, Picard body, CG body
+    bool pending = false;
+};
+
+namespace nk {
+
+static_assert(sizeof(SolverScalars) <= 256, "a slot's pinned scalars take one 256-byte record");
+static size_t batch_pinned_bytes(int slots) { return (size_t)slots * (256 + 2 * sizeof(SolverScalars)) + 256; }
+static size_t batch_device_bytes(size_t stride, int slots) { return stride * (size_t)slots + 256; }
+
+// Device footprint of one problem of this configuration, rounded up to 256 bytes: the slot stride.
+static size_t batch_stride(const nk_grid_desc* g, const nk_physics_desc* p, const nk_solver_desc* s) {
+    nk_problem probe;
+    probe.gd = *g;
+    probe.pd = *p;
+    probe.sd = *s;
+    build(&probe, true);
+    return (probe.arena.size + 255) / 256 * 256;
+}
+
+// The slot stride and the address of slot 0's Picard flag in every grid of P's hierarchy (0 and null: unbatched).
+static void set_batch_grids(nk_problem* P, long long stride) {
+    const int* pd = stride ? &P->sc->p_done : nullptr;
+    P->fine.g.slot_stride = stride;
+    P->fine.g.p_done = pd;
+    for (auto& L : P->lv64) { L.g.slot_stride = stride; L.g.p_done = pd; }
+    for (auto& L : P->lv32) { L.g.slot_stride = stride; L.g.p_done = pd; }
+}
+
+// The graph of build_picard_graph over every slot, captured from slot 0's problem: the kernels' stopping decisions
+// stay per slot (p_done, done), and the loop conditions come from k_batch_condition over all slots:
+//   picard_begin ─► any(Picard) ─► WHILE { x⁻ = x ─► coefficients ─► CG start ─► any(CG)
+//                                          ─► WHILE { CG step ─► any(CG) } ─► picard_end ─► any(Picard) }
+static void build_batch_graph(nk_batch* B) {
+    nk_problem* P = B->P[0];
+    autotune_strips(P);
+    long long stride = (long long)B->stride;
+    int S = B->slots;
+    int* cp = B->counters;
+    int* cc = B->counters + 1;
+    set_batch_grids(P, stride);
+    try {
+        BatchScope scope(S);
+        cudaGraph_t g;
+        NK_CUDA(cudaGraphCreate(&g, 0));
+        B->graph = g;
+        cudaGraphConditionalHandle hp;
+        NK_CUDA(cudaGraphConditionalHandleCreate(&hp, g, 0, 0));
+        capture_into(P, g, {}, [&] {
+            launch_picard_begin(P->sc, 0, stride, P->stream);
+            launch_batch_condition(P->sc, stride, S, 0, hp, cp, P->stream);
+        });
+        cudaGraph_t body = add_while(g, leaves(g), hp);
+        cudaGraphConditionalHandle hc;
+        NK_CUDA(cudaGraphConditionalHandleCreate(&hc, body, 0, 0));
+        CGView v = P->cg_view(P->tau);   // its grids carry the stride (set above)
+        v.cond = 0;
+        capture_into(P, body, {}, [&] {
+            launch_copy_range(P->fine.g, P->xprev, P->x, P->stream);
+            update_coefficients(P);
+            cg_start(P, v);
+            launch_batch_condition(P->sc, stride, S, 1, hc, cc, P->stream);
+        });
+        cudaGraph_t cg_body = add_while(body, leaves(body), hc);
+        capture_into(P, cg_body, {}, [&] {
+            cg_step(P, v);
+            launch_batch_condition(P->sc, stride, S, 1, hc, cc, P->stream);
+        });
+        capture_into(P, body, leaves(body), [&] {
+            picard_end(P, 0);
+            launch_batch_condition(P->sc, stride, S, 0, hp, cp, P->stream);
+        });
+        B->kernels[0] = kernel_nodes(g);
+        B->kernels[1] = kernel_nodes(body);
+        B->kernels[2] = kernel_nodes(cg_body);
+        NK_CUDA(cudaGraphInstantiate(&B->exec, g, 0));
+    } catch (...) {
+        set_batch_grids(P, 0);
+        throw;
+    }
+    set_batch_grids(P, 0);
+}
+
+// Offsets of the buffers the solve graph reaches, relative to the arena: equal in every slot by construction
+// (build is deterministic), checked once because the batched kernels rely on it.
+static std::vector<long long> arena_offsets(const nk_problem* P) {
+    const char* b = P->arena.base;
+    auto off = [&](const void* q) { return q ? (long long)((const char*)q - b) : -1ll; };
+    std::vector<long long> o = {(long long)P->arena.size, off(P->sc), off(P->x), off(P->tau), off(P->partials), off(P->fine.coef),
+                                off(P->fine.metrics), off(P->fine.mask), off(P->H), off(P->A2), off(P->A3), off(P->sig_tables)};
+    for (const auto& L : P->lv64) { o.push_back(off(L.x)); o.push_back(off(L.metrics)); o.push_back(off(L.coef)); }
+    for (const auto& L : P->lv32) { o.push_back(off(L.x)); o.push_back(off(L.metrics)); o.push_back(off(L.coef)); }
+    return o;
+}
+
+static void batch_free(nk_batch* B) {
+    if (!B) return;
+    if (B->ctx) cudaSetDevice(B->ctx->device);
+    if (B->stream) cudaStreamSynchronize(B->stream);
+    for (nk_problem* P : B->P) nk_problem_destroy(P);
+    if (B->exec) cudaGraphExecDestroy(B->exec);
+    if (B->graph) cudaGraphDestroy(B->graph);
+    if (B->ev0) cudaEventDestroy(B->ev0);
+    if (B->ev1) cudaEventDestroy(B->ev1);
+    if (B->stream) cudaStreamDestroy(B->stream);
+    if (!B->external) {
+        if (B->base) cudaFree(B->base);
+        if (B->pinned) cudaFreeHost(B->pinned);
+    }
+    delete B;
+}
+
+// `device_base` (batch_device_bytes) and `pinned_base` (batch_pinned_bytes) from a server, or null to allocate.
+static nk_status batch_create(nk_context* ctx, const nk_grid_desc* grid, const nk_physics_desc* physics, const nk_solver_desc* solver,
+                              int slots, char* device_base, char* pinned_base, nk_batch** out) {
+    if (!ctx || !grid || !physics || !solver || !out) return NK_BAD_ARGUMENT;
+    auto* B = new nk_batch();
+    B->ctx = ctx;
+    B->slots = slots;
+    nk_status st = guarded(ctx, [&] {
+        if (slots < 1 || slots > NK_MAX_BATCH_SLOTS) bad("batch slots out of range (1 .. NK_MAX_BATCH_SLOTS)");
+        if (solver->flags & NK_SOLVER_HOST_LOOP) bad("batched solves run as CUDA graphs: NK_SOLVER_HOST_LOOP is set");
+        if (solver->precision == NK_PRECISION_MIXED && solver->preconditioner == NK_PRECONDITIONER_MULTIGRID && coarse_cells_limit() > 0)
+            bad("fused coarse multigrid levels (NK_COARSE_CELLS > 0) are not batched");
+        if (grid->Nx < 1 || grid->Ny < 1 || grid->Nsigma < 1 || grid->Nsigma > MAX_SIGMA) bad("grid size or Nsigma out of range");
+        B->stride = batch_stride(grid, physics, solver);
+        if (device_base) {
+            B->base = device_base;
+            B->pinned = pinned_base;
+            B->external = true;
+        } else {
+            NK_CUDA(cudaMalloc((void**)&B->base, batch_device_bytes(B->stride, slots)));
+            NK_CUDA(cudaHostAlloc((void**)&B->pinned, batch_pinned_bytes(slots), cudaHostAllocDefault));
+        }
+        B->counters = reinterpret_cast<int*>(B->base + B->stride * (size_t)slots);
+        B->control = reinterpret_cast<SolverScalars*>(B->pinned + (size_t)slots * 256);
+        B->results = B->control + slots;
+        B->counters_host = reinterpret_cast<int*>(B->results + slots);
+        B->active.assign(slots, 0);
+        NK_CUDA(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
+        NK_CUDA(cudaEventCreate(&B->ev0));
+        NK_CUDA(cudaEventCreate(&B->ev1));
+        for (int k = 0; k < slots; ++k) {
+            nk_problem* P = nullptr;
+            nk_status ps = problem_create(ctx, grid, physics, solver, &P, B->base + B->stride * (size_t)k,
+                                          reinterpret_cast<SolverScalars*>(B->pinned + (size_t)k * 256));
+            if (ps != NK_OK) throw Failure{ps, ctx->error};
+            NK_CUDA(cudaStreamDestroy(P->stream));
+            P->stream = B->stream;
+            P->external_stream = true;
+            B->P.push_back(P);
+        }
+        if (!use_graphs(B->P[0])) bad("batched solves run as CUDA graphs: NK_GRAPHS=0 is set");
+        std::vector<long long> o0 = arena_offsets(B->P[0]);
+        for (int k = 1; k < slots; ++k)
+            if (arena_offsets(B->P[k]) != o0) bad("batch slots with different arena layouts");
+        if ((size_t)o0[0] > B->stride) bad("batch slot larger than its stride");
+        build_batch_graph(B);
+        NK_CUDA(cudaStreamSynchronize(B->stream));
+    });
+    if (st != NK_OK) {
+        batch_free(B);
+        return st;
+    }
+    *out = B;
+    return NK_OK;
+}
+
+// Scalars of every slot between pinned records (one SolverScalars each) and the slots' arenas.
+static void batch_scalars(nk_batch* B, SolverScalars* host, bool to_device) {
+    SolverScalars* dev = B->P[0]->sc;
+    size_t w = sizeof(SolverScalars);
+    if (B->stride <= (size_t)1 << 30) {   // one strided copy
+        if (to_device) NK_CUDA(cudaMemcpy2DAsync(dev, B->stride, host, w, w, B->slots, cudaMemcpyHostToDevice, B->stream));
+        else NK_CUDA(cudaMemcpy2DAsync(host, w, dev, B->stride, w, B->slots, cudaMemcpyDeviceToHost, B->stream));
+        return;
+    }
+    for (int k = 0; k < B->slots; ++k) {   // slots too far apart for a pitched copy
+        SolverScalars* d = B->P[k]->sc;
+        if (to_device) NK_CUDA(cudaMemcpyAsync(d, host + k, w, cudaMemcpyHostToDevice, B->stream));
+        else NK_CUDA(cudaMemcpyAsync(host + k, d, w, cudaMemcpyDeviceToHost, B->stream));
+    }
+}
+
+static void batch_solve_async(nk_batch* B, const uint8_t* active) {
+    if (B->pending) bad("a batched solve is pending (nk_batch_wait first)");
+    SolverScalars h = control_scalars(B->P[0]);
+    for (int k = 0; k < B->slots; ++k) {
+        uint8_t a = active ? (active[k] != 0) : 1;
+        if (a && B->P[k]->ud) bad("batch slot " + std::to_string(k) + " has prescribed velocities, which batched solves do not take");
+        B->active[k] = a;
+        B->control[k] = h;
+        B->control[k].p_done = !a;
+    }
+    batch_scalars(B, B->control, true);
+    NK_CUDA(cudaMemsetAsync(B->counters, 0, 2 * sizeof(int), B->stream));
+    NK_CUDA(cudaEventRecord(B->ev0, B->stream));
+    NK_CUDA(cudaGraphLaunch(B->exec, B->stream));
+    NK_CUDA(cudaEventRecord(B->ev1, B->stream));
+    batch_scalars(B, B->results, false);
+    NK_CUDA(cudaMemcpyAsync(B->counters_host, B->counters, 2 * sizeof(int), cudaMemcpyDeviceToHost, B->stream));
+    B->pending = true;
+}
+
+// Statistics of every slot after the pending solve has finished (the caller has waited on the stream).
+static bool batch_finish(nk_batch* B, nk_solve_stats* stats) {
+    B->pending = false;
+    float ms = 0, a = 0, b = 0;
+    NK_CUDA(cudaEventElapsedTime(&ms, B->ev0, B->ev1));
+    NK_CUDA(cudaEventElapsedTime(&a, B->ctx->ref, B->ev0));
+    NK_CUDA(cudaEventElapsedTime(&b, B->ctx->ref, B->ev1));
+    bool nonfinite = false;
+    for (int k = 0; k < B->slots; ++k) {
+        nk_solve_stats st{};
+        if (B->active[k]) {
+            fill_stats_from(B->results[k], &st, true);
+            st.device_ms = ms;
+            st.device_start_ms = a;
+            st.device_end_ms = b;
+            nonfinite = nonfinite || st.status == NK_NONFINITE;
+        }
+        if (stats) stats[k] = st;
+    }
+    count_launches(B->kernels[0] + (long long)B->counters_host[0] * B->kernels[1] + (long long)B->counters_host[1] * B->kernels[2]);
+    return !nonfinite;
+}
+
+}  // namespace nk
+
+extern "C" {
+
+nk_status nk_batch_create(nk_context* ctx, const nk_grid_desc* grid, const nk_physics_desc* physics, const nk_solver_desc* solver,
+                          int32_t slots, nk_batch** out) {
+    return batch_create(ctx, grid, physics, solver, slots, nullptr, nullptr, out);
+}
+
+nk_status nk_batch_destroy(nk_batch* B) {
+    batch_free(B);
+    return NK_OK;
+}
+
+int32_t nk_batch_slots(const nk_batch* B) { return B ? B->slots : 0; }
+
+nk_problem* nk_batch_problem(nk_batch* B, int32_t slot) {
+    if (!B || slot < 0 || slot >= B->slots) return nullptr;
+    return B->P[slot];
+}
+
+nk_status nk_batch_picard_solve_async(nk_batch* B, const uint8_t* active) {
+    if (!B) return NK_BAD_ARGUMENT;
+    return guarded(B->ctx, [&] { batch_solve_async(B, active); });
+}
+
+nk_status nk_batch_query(nk_batch* B, int32_t* done) {
+    if (!B || !done) return NK_BAD_ARGUMENT;
+    return guarded(B->ctx, [&] {
+        if (!B->pending) bad("no batched solve pending");
+        cudaError_t e = cudaEventQuery(B->ev1);
+        if (e == cudaErrorNotReady) {
+            *done = 0;
+            return;
+        }
+        NK_CUDA(e);
+        *done = 1;
+    });
+}
+
+nk_status nk_batch_wait(nk_batch* B, nk_solve_stats* stats) {
+    if (!B) return NK_BAD_ARGUMENT;
+    return guarded(B->ctx, [&] {
+        if (!B->pending) bad("no batched solve pending");
+        NK_CUDA(cudaStreamSynchronize(B->stream));
+        if (!batch_finish(B, stats)) throw Failure{NK_NONFINITE, "non-finite velocity change in a batch slot"};
+    });
+}
+
+}  // extern "C"
+
+// =================================================================================================================
 // Serving: a request loop over resident problems, one stream per in-flight request.
 // =================================================================================================================
 #include <chrono>
@@ -2294,14 +2598,17 @@ struct ServerRequest {
 
 struct Resident {
     nk_problem* P = nullptr;
+    nk_batch* B = nullptr;            // a batch resident (nk_server_desc.batch_slots > 1): P is its slot 0
+    std::vector<int64_t> tickets;     // batch resident: the request in each slot (0: none)
     std::string key;
     bool busy = false;
     int64_t ticket = 0;
     size_t bytes = 0;                // device bytes sub-allocated at dev_off
     size_t dev_off = 0, pin_off = 0, pin_bytes = 0;
     double last_used = 0;
-    double* pin = nullptr;          // pinned staging: H, bed, C, A, u0, v0 in; u, v out
+    double* pin = nullptr;          // pinned staging: H, bed, C, A, u0, v0 in; u, v out (one block per slot)
     size_t pin_count = 0;
+    size_t pin_slot = 0;            // doubles between two slots' staging blocks
     SolverScalars* sc_out = nullptr; // pinned copy of the solver scalars at completion
     cudaEvent_t done = nullptr;
 };
@@ -2369,6 +2676,8 @@ struct nk_server {
 
 namespace nk {
 
+static int batch_slots_of(const nk_server* S) { return std::max(1, (int)S->desc.batch_slots); }
+
 static size_t problem_bytes(ServerRequest& R) {
     nk_problem probe;
     probe.gd = grid_with_vectors(R);
@@ -2382,15 +2691,24 @@ static void destroy_resident(nk_server* S, size_t idx) {
     Resident* r = S->residents[idx].get();
     S->device_bytes -= (int64_t)r->bytes;
     if (r->done) cudaEventDestroy(r->done);
-    nk_problem_destroy(r->P);
+    if (r->B) batch_free(r->B);
+    else nk_problem_destroy(r->P);
     S->dev.release(r->dev_off, r->bytes);
     S->pin.release(r->pin_off, r->pin_bytes);
     S->residents.erase(S->residents.begin() + idx);
 }
 
-static size_t pinned_bytes(const ServerRequest& R) {
+static size_t staging_doubles(const ServerRequest& R) {
     size_t cells = (size_t)R.grid.Nx * R.grid.Ny, faces = (size_t)(R.grid.Nx + 1) * (R.grid.Ny + 1);
-    return (4 * cells + 4 * faces) * sizeof(double) + 2 * 256 + 2 * sizeof(SolverScalars);
+    return 4 * cells + 4 * faces;
+}
+static size_t pinned_bytes(const ServerRequest& R) {
+    return staging_doubles(R) * sizeof(double) + 2 * 256 + 2 * sizeof(SolverScalars);
+}
+// A batch resident's pinned block: the batch's own records, then one 256-byte-aligned staging block per slot.
+static size_t batch_slot_doubles(const ServerRequest& R) { return (staging_doubles(R) * sizeof(double) + 255) / 256 * 256 / sizeof(double); }
+static size_t batch_resident_pinned(const ServerRequest& R, int slots) {
+    return (batch_pinned_bytes(slots) + 255) / 256 * 256 + (size_t)slots * batch_slot_doubles(R) * sizeof(double);
 }
 
 // A resident problem for R: an idle one of the same shape, else a new one carved out of the server's
@@ -2399,7 +2717,14 @@ static size_t pinned_bytes(const ServerRequest& R) {
 static Resident* acquire(nk_server* S, ServerRequest& R) {
     for (auto& r : S->residents)
         if (!r->busy && r->key == R.key) return r.get();
-    size_t need = problem_bytes(R), pneed = pinned_bytes(R);
+    int slots = batch_slots_of(S);
+    size_t stride = 0;
+    if (slots > 1) {
+        nk_grid_desc g = grid_with_vectors(R);
+        stride = batch_stride(&g, &R.physics, &R.solver);
+    }
+    size_t need = slots > 1 ? batch_device_bytes(stride, slots) : problem_bytes(R);
+    size_t pneed = slots > 1 ? batch_resident_pinned(R, slots) : pinned_bytes(R);
     size_t off = 0, poff = 0;
     auto fits = [&] {
         if (!S->dev.alloc(need, off)) return false;
@@ -2426,6 +2751,27 @@ static Resident* acquire(nk_server* S, ServerRequest& R) {
     r->pin_off = poff;
     r->pin_bytes = pneed;
     char* pin = S->pin_base + poff;
+    if (slots > 1) {
+        nk_grid_desc g = grid_with_vectors(R);
+        nk_status st = batch_create(S->ctx, &g, &R.physics, &R.solver, slots, S->dev_base + off, pin, &r->B);
+        if (st != NK_OK) {
+            S->dev.release(off, need);
+            S->pin.release(poff, pneed);
+            throw Failure{st, S->ctx->error};
+        }
+        r->P = r->B->P[0];
+        r->key = R.key;
+        r->tickets.assign(slots, 0);
+        r->pin_slot = batch_slot_doubles(R);
+        r->pin = reinterpret_cast<double*>(pin + (batch_pinned_bytes(slots) + 255) / 256 * 256);
+        r->pin_count = staging_doubles(R);
+        NK_CUDA(cudaEventCreateWithFlags(&r->done, cudaEventDisableTiming));
+        S->device_bytes += (int64_t)r->bytes;
+        S->residents.push_back(std::move(r));
+        S->created += 1;
+        S->t_create += S->now() - tc0;
+        return S->residents.back().get();
+    }
     r->sc_out = reinterpret_cast<SolverScalars*>(pin);
     SolverScalars* sc_host = reinterpret_cast<SolverScalars*>(pin + 256);
     r->pin = reinterpret_cast<double*>(pin + 512);
@@ -2455,14 +2801,12 @@ static Resident* acquire(nk_server* S, ServerRequest& R) {
     return S->residents.back().get();
 }
 
-// Stage the request's inputs and enqueue its whole solve on the resident problem's stream.
-static void start(nk_server* S, ServerRequest& R, Resident& r) {
-    nk_problem* P = r.P;
+// Enqueue on P's stream: the request's inputs from the pinned block `pin` into P, the warm start, the geometry.
+static void stage_request(const ServerRequest& R, nk_problem* P, double* pin) {
     cudaStream_t s = P->stream;
     size_t cells = (size_t)P->Nx * P->Ny;
-    FieldLoc fu = field_loc(P, NK_FIELD_U), fv = field_loc(P, NK_FIELD_V);
-    size_t nu = (size_t)fu.nx * fu.ny, nv = (size_t)fv.nx * fv.ny;
-    double* pin = r.pin;
+    FieldLoc fu = field_loc(P, NK_FIELD_U);
+    size_t nu = (size_t)fu.nx * fu.ny;
     auto stage = [&](int id, const std::vector<double>& src, double* at) {
         FieldLoc f = field_loc(P, id);
         std::memcpy(at, src.data(), src.size() * sizeof(double));
@@ -2486,29 +2830,101 @@ static void start(nk_server* S, ServerRequest& R, Resident& r) {
     gv.mask_min = P->pd.mask_minimum_thickness; gv.mask_trans = P->pd.mask_transition_thickness;
     gv.ud = P->ud;
     launch_geometry(gv, s);
-    set_control(P);
-    if (use_graphs(P)) {
-        NK_CUDA(cudaGraphLaunch(P->picard_exec, s));
-    } else {
-        host_picard(P);
-    }
-    double* uout = uin + nu + nv;
+}
+
+// Enqueue on P's stream: u and v of P's solution into the output part of the pinned block `pin`.
+static void read_back(nk_problem* P, double* pin) {
+    cudaStream_t s = P->stream;
+    size_t cells = (size_t)P->Nx * P->Ny;
+    FieldLoc fu = field_loc(P, NK_FIELD_U), fv = field_loc(P, NK_FIELD_V);
+    size_t nu = (size_t)fu.nx * fu.ny, nv = (size_t)fv.nx * fv.ny;
+    double* uout = pin + 4 * cells + nu + nv;
     launch_unpack(P->staging, (const double*)P->x, P->pitch, (int)P->plane, 2, 0, fu.nx, fu.ny, 1, s);
     NK_CUDA(cudaMemcpyAsync(uout, P->staging, nu * sizeof(double), cudaMemcpyDeviceToHost, s));
     launch_unpack(P->staging, (const double*)P->x, P->pitch, (int)P->plane, 2, 1, fv.nx, fv.ny, 1, s);
     NK_CUDA(cudaMemcpyAsync(uout + nu, P->staging, nv * sizeof(double), cudaMemcpyDeviceToHost, s));
-    NK_CUDA(cudaMemcpyAsync(r.sc_out, P->sc, sizeof(SolverScalars), cudaMemcpyDeviceToHost, s));
-    NK_CUDA(cudaEventRecord(r.done, s));
-    NK_CHECK_LAUNCH();
-    r.busy = true;
-    r.ticket = R.ticket;
+}
+
+static void admitted(nk_server* S, ServerRequest& R) {
     R.state = 1;
     R.t_admit = S->now();
     S->in_flight += 1;
     S->peak = std::max(S->peak, S->in_flight);
 }
 
+// Stage the request's inputs and enqueue its whole solve on the resident problem's stream.
+static void start(nk_server* S, ServerRequest& R, Resident& r) {
+    nk_problem* P = r.P;
+    cudaStream_t s = P->stream;
+    stage_request(R, P, r.pin);
+    set_control(P);
+    if (use_graphs(P)) {
+        NK_CUDA(cudaGraphLaunch(P->picard_exec, s));
+    } else {
+        host_picard(P);
+    }
+    read_back(P, r.pin);
+    NK_CUDA(cudaMemcpyAsync(r.sc_out, P->sc, sizeof(SolverScalars), cudaMemcpyDeviceToHost, s));
+    NK_CUDA(cudaEventRecord(r.done, s));
+    NK_CHECK_LAUNCH();
+    r.busy = true;
+    r.ticket = R.ticket;
+    admitted(S, R);
+}
+
+// The requests `reqs` (of one shape, at most the batch's slots) into slots 0, 1, ... of a batch resident and one
+// batched solve of those slots.
+static void start_batch(nk_server* S, const std::vector<ServerRequest*>& reqs, Resident& r) {
+    nk_batch* B = r.B;
+    std::vector<uint8_t> active(B->slots, 0);
+    for (size_t k = 0; k < reqs.size(); ++k) {
+        stage_request(*reqs[k], B->P[k], r.pin + k * r.pin_slot);
+        active[k] = 1;
+    }
+    batch_solve_async(B, active.data());
+    for (size_t k = 0; k < reqs.size(); ++k) read_back(B->P[k], r.pin + k * r.pin_slot);
+    NK_CUDA(cudaEventRecord(r.done, B->stream));
+    NK_CHECK_LAUNCH();
+    r.busy = true;
+    std::fill(r.tickets.begin(), r.tickets.end(), 0);
+    for (size_t k = 0; k < reqs.size(); ++k) {
+        r.tickets[k] = reqs[k]->ticket;
+        admitted(S, *reqs[k]);
+    }
+}
+
+// A batch resident's requests after its solve: each slot's results and statistics.
+static void finish_batch(nk_server* S, Resident& r) {
+    nk_batch* B = r.B;
+    std::vector<nk_solve_stats> stats(B->slots);
+    batch_finish(B, stats.data());
+    double t = S->now();
+    for (int k = 0; k < B->slots; ++k) {
+        if (!r.tickets[k]) continue;
+        ServerRequest& R = *S->requests.at(r.tickets[k]);
+        nk_problem* P = B->P[k];
+        FieldLoc fu = field_loc(P, NK_FIELD_U), fv = field_loc(P, NK_FIELD_V);
+        size_t nu = (size_t)fu.nx * fu.ny, nv = (size_t)fv.nx * fv.ny;
+        size_t cells = (size_t)P->Nx * P->Ny;
+        const double* uout = r.pin + k * r.pin_slot + 4 * cells + nu + nv;
+        if (R.u_out) std::memcpy(R.u_out, uout, nu * sizeof(double));
+        if (R.v_out) std::memcpy(R.v_out, uout + nu, nv * sizeof(double));
+        R.stats = stats[k];
+        R.status = R.stats.status == NK_NONFINITE ? NK_NONFINITE : NK_OK;
+        R.state = 2;
+        R.t_done = t;
+        S->in_flight -= 1;
+        r.tickets[k] = 0;
+    }
+    r.busy = false;
+    r.last_used = t;
+}
+
 static void finish(nk_server* S, Resident& r) {
+    if (r.B) {
+        finish_batch(S, r);
+        return;
+    }
     ServerRequest& R = *S->requests.at(r.ticket);
     nk_problem* P = r.P;
     FieldLoc fu = field_loc(P, NK_FIELD_U), fv = field_loc(P, NK_FIELD_V);
@@ -2553,9 +2969,25 @@ static void progress(nk_server* S) {
             continue;
         }
         if (!r) break;   // wait for memory
-        S->queue.pop_front();
         double ts0 = S->now();
-        start(S, R, *r);
+        if (r->B) {
+            // this request and the next queued ones of its shape, up to the slots and the requests allowed in flight
+            size_t room = (size_t)std::min(r->B->slots, S->desc.max_in_flight - S->in_flight);
+            std::vector<ServerRequest*> batch;
+            for (auto it = S->queue.begin(); it != S->queue.end() && batch.size() < room;) {
+                ServerRequest& Q = *S->requests.at(*it);
+                if (Q.key == R.key) {
+                    batch.push_back(&Q);
+                    it = S->queue.erase(it);
+                } else {
+                    ++it;
+                }
+            }
+            start_batch(S, batch, *r);
+        } else {
+            S->queue.pop_front();
+            start(S, R, *r);
+        }
         S->t_start += S->now() - ts0;
     }
 }
@@ -2591,6 +3023,7 @@ extern "C" {
 
 nk_status nk_server_create(nk_context* ctx, const nk_server_desc* desc, nk_server** out) {
     if (!ctx || !desc || !out || desc->max_in_flight < 1 || desc->memory_cap_bytes <= 0) return NK_BAD_ARGUMENT;
+    if (desc->batch_slots < 0 || desc->batch_slots > NK_MAX_BATCH_SLOTS) return NK_BAD_ARGUMENT;
     auto* S = new nk_server();
     S->ctx = ctx;
     S->desc = *desc;

@@ -514,8 +514,9 @@ void launch_picard_begin(SolverScalars* sc, unsigned long long cond, long long s
 }
 
 // The loop conditions of a batched graph, one warp over the slots' scalars: Picard goes on while a slot is still
-// iterating (cg = 0), conjugate gradients while a slot still iterating has not stopped (cg = 1).
-__global__ void k_batch_condition(const SolverScalars* sc, long long stride, int slots, int cg, unsigned long long cond) {
+// iterating (cg = 0), conjugate gradients while a slot still iterating has not stopped (cg = 1).  `counter` counts
+// the loop bodies that will run (the launch count of the solve).
+__global__ void k_batch_condition(const SolverScalars* sc, long long stride, int slots, int cg, unsigned long long cond, int* counter) {
     int more = 0;
     for (int z = threadIdx.x; z < slots; z += 32) {
         const SolverScalars* t = sc;
@@ -525,10 +526,14 @@ __global__ void k_batch_condition(const SolverScalars* sc, long long stride, int
         more |= going;
     }
     more = __any_sync(0xffffffffu, more);
-    if (threadIdx.x == 0) cudaGraphSetConditional(cond, more ? 1u : 0u);
+    if (threadIdx.x == 0) {
+        cudaGraphSetConditional(cond, more ? 1u : 0u);
+        if (more && counter) *counter += 1;
+    }
 }
-void launch_batch_condition(const SolverScalars* sc, long long stride, int slots, int cg, unsigned long long cond, cudaStream_t s) {
-    k_batch_condition<<<1, 32, 0, s>>>(sc, stride, slots, cg, cond); count_launch();
+void launch_batch_condition(const SolverScalars* sc, long long stride, int slots, int cg, unsigned long long cond, int* counter,
+                            cudaStream_t s) {
+    k_batch_condition<<<1, 32, 0, s>>>(sc, stride, slots, cg, cond, counter); count_launch();
 }
 
 // end of one Picard iteration (picard.jl:83-86): x⁻ = x⁻ - x, Δ = ‖x⁻‖, X = ‖x‖, then the loop test of :79

@@ -12,6 +12,7 @@ from .model import (YEAR, Convergence, DepthIntegrated, DIVAShear, FixedIteratio
                     MaximumExtentCalving,
                     make_descriptors, field_shape, sigma_faces)
 from .problem import NunatakError, Problem
+from .batch import Batch
 
 __all__ = [
     "abi", "YEAR", "Convergence", "DepthIntegrated", "DIVAShear", "FixedIterations", "FreeSlipWalls", "GlenFlowLaw",
@@ -20,5 +21,5 @@ __all__ = [
     "StressBalanceSolver", "SubgridGroundedFraction", "ViscosityConvergence", "WeertmanFriction", "make_descriptors",
     "field_shape", "sigma_faces", "UpwindBiased", "WENO", "default_thickness_advection", "PartialCellFront",
     "ThicknessThresholdCalving", "EigenCalving", "VonMisesCalving", "FrontVelocityCalving", "MaximumExtentCalving",
-    "NunatakError", "Problem",
+    "NunatakError", "Problem", "Batch",
 ]

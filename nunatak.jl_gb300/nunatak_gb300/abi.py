@@ -141,7 +141,8 @@ class SolveStats(C.Structure):
 
 
 class ServerDesc(C.Structure):
-    _fields_ = [("max_in_flight", C.c_int32), ("flags", C.c_int32), ("memory_cap_bytes", C.c_int64)]
+    _fields_ = [("max_in_flight", C.c_int32), ("flags", C.c_int32), ("memory_cap_bytes", C.c_int64), ("batch_slots", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 NK_SERVER_ADMISSION_THREAD = 1

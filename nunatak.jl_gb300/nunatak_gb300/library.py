@@ -63,6 +63,13 @@ def _declare(lib):
         "nk_server_clock": ([vp], C.c_double),
         "nk_server_info": ([vp, ip, C.POINTER(i64), ip], i32),
         "nk_multigrid_prolongate": ([vp, i32, dp, dp, dp, dp], i32),
+        "nk_batch_create": ([vp, C.POINTER(abi.GridDesc), C.POINTER(abi.PhysicsDesc), C.POINTER(abi.SolverDesc), i32, C.POINTER(vp)], i32),
+        "nk_batch_destroy": ([vp], i32),
+        "nk_batch_slots": ([vp], i32),
+        "nk_batch_problem": ([vp, i32], vp),
+        "nk_batch_picard_solve_async": ([vp, C.POINTER(C.c_uint8)], i32),
+        "nk_batch_query": ([vp, ip], i32),
+        "nk_batch_wait": ([vp, C.POINTER(abi.SolveStats)], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

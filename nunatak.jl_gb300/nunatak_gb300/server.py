@@ -18,13 +18,15 @@ def _ptr(a):
 
 
 class Server:
-    def __init__(self, max_in_flight=16, memory_cap_bytes=16 << 30, context=None, admission_thread=False):
+    def __init__(self, max_in_flight=16, memory_cap_bytes=16 << 30, context=None, admission_thread=False, batch_slots=0):
         """`admission_thread`: the library's own host thread admits and retires requests (NK_SERVER_ADMISSION_THREAD);
-        otherwise submit / progress / wait drive the loop."""
+        otherwise submit / progress / wait drive the loop.  `batch_slots` > 1: queued requests of one shape are
+        solved together, up to batch_slots per solve, by one batched graph (nk_batch)."""
         self.ctx = context or library.default_context()
         self.lib = library.load()
         self.h = C.c_void_p()
-        d = abi.ServerDesc(max_in_flight, abi.NK_SERVER_ADMISSION_THREAD if admission_thread else 0, int(memory_cap_bytes))
+        d = abi.ServerDesc(max_in_flight, abi.NK_SERVER_ADMISSION_THREAD if admission_thread else 0, int(memory_cap_bytes),
+                           int(batch_slots), 0)
         _check(self.lib.nk_server_create(self.ctx.handle, C.byref(d), C.byref(self.h)), "server_create", self.ctx.last_error())
         self._keep = {}
 

@@ -88,3 +88,28 @@ def test_admission_thread_wait_blocks_until_done():
     S.close()
     for (u, v, st, _), (ur, vr, sr) in zip(got, ref):
         assert np.array_equal(u, ur) and np.array_equal(v, vr)
+
+
+@pytest.mark.parametrize("threaded", [False, True])
+def test_batched_server_equals_solves_alone(threaded):
+    """batch_slots > 1: queued requests of one shape share one batched solve (nk_batch); every result is still the
+    request solved alone, and a later wave reuses the resident batches."""
+    cases = requests() + requests()[:4]
+    ref = [alone(c) for c in cases]
+    S = Server(max_in_flight=6, batch_slots=3, admission_thread=threaded)
+    tickets = [S.submit(c) for c in cases]
+    got = [S.wait(t) for t in tickets]
+    again = [S.wait(S.submit(c)) for c in cases[:3]]
+    info = S.info()
+    S.close()
+    for (u, v, st, times), (ur, vr, sr) in zip(got + again, ref + ref[:3]):
+        assert st.status == 0 and st.picard_iterations == sr.picard_iterations
+        assert st.linear_iterations_total == sr.linear_iterations_total
+        assert np.array_equal(u, ur) and np.array_equal(v, vr)
+        assert times[0] <= times[1] <= times[2]
+    assert info["resident"] >= 3   # a batch per shape (three shapes), more where a shape's batch was busy
+
+
+def test_batch_slots_out_of_range_is_refused():
+    with pytest.raises(ValueError):
+        Server(max_in_flight=2, batch_slots=-1)
