@@ -17,6 +17,8 @@ walk the stream from its first request and wrap around after 512.  The warm-up s
             next request at once (continuous batching).  Time runs from the first solve's start event to the
             last one's end event.  Requests of up to 1024x512 keep the working set far above L2, so L2 is not
             flushed.
+  batched   with --batch-slots S > 1 (default 8), the same timed requests in batches of up to S requests of one
+            grid size (nk_batch: one launch per kernel for the whole batch), beside the headline.
   e2e       the same requests through the C ABI serving loop (nk_server_*) from host buffers, submitted at
             their Poisson arrival times.  Covers upload, geometry, solve and read-back of u and v; host wall
             clock.  p50 and p99 latency run from arrival to result; a second pass over the first requests at 0.8x
@@ -76,8 +78,8 @@ def parse():
     ap.add_argument("--impl", default="nunatak", choices=["nunatak", "reference"])
     ap.add_argument("--batch", type=int, default=32, help="requests per step, and solves in flight at once")
     ap.add_argument("--batch-slots", type=int, default=8,
-                    help="requests of one grid size solved together by one batched graph (nk_batch) in the value and e2e "
-                         "legs; 0 or 1: one solve per request")
+                    help="slots of the batched leg reported beside the headline (nk_batch: requests of one grid size solved "
+                         "together); 0 or 1: no batched leg")
     ap.add_argument("--no-cpu-baseline", action="store_true",
                     help="skip the oracle solves (CPU baseline and the mixed-vs-oracle errors of every grid size)")
     ap.add_argument("--no-scaling", action="store_true", help="skip the reference's published scaling benchmark rows")
@@ -794,55 +796,50 @@ def main():
         first_of_size.setdefault("%dx%d" % (c.grid.Nx, c.grid.Ny), k)
 
     # ---- value: the timed requests with inputs staged in HBM, continuous batching of B in flight --------------
-    pool = ResidentPool(nk, ctx)
-    w_staged, w_zeros = stage(warm_cases)
-    run_resident(pool, warm_cases, w_staged, w_zeros, B)
-    del w_staged, w_zeros
-    staged, zeros = stage(cases)
-    barrier()
-    created0 = pool.created
-    launches0 = library.launch_count()
-    with ClockSampler(local_rank) as clocks:
-        t0 = time.perf_counter()
-        stats, kept = run_resident(pool, cases, staged, zeros, B, keep=set(first_of_size.values()))
-        barrier()
-        wall = time.perf_counter() - t0
-    launches = library.launch_count() - launches0
-    span_ms = max(x.device_end_ms for x in stats) - min(x.device_start_ms for x in stats)
-    value, span_ms = replica_throughput(len(cases), span_ms, world, "cuda")
-    service = [x.device_end_ms - x.device_start_ms for x in stats]
-    created_timed = pool.created - created0
-    pool.close()
-    del staged, zeros
-    torch.cuda.empty_cache()
-    unbatched = None
-    if args.batch_slots > 1:
-        # ---- the same timed requests in batches: requests of one grid size share one batched graph (nk_batch) -----
-        unbatched = {"value": value, "unit": "solves/s", "ms_per_step": span_ms / args.steps, "wall_s": wall,
-                     "gpu_launches": int(launches), "latency_ms": {"p50": statistics.median(service),
-                                                                    "p99": float(np.percentile(service, 99))},
-                     "mode": f"one solve per request, {B} in flight on {B} streams"}
-        bpool = BatchPool(nk, ctx, args.batch_slots)
-        w_staged, w_zeros = stage(warm_cases)
-        run_batched(bpool, warm_cases, w_staged, w_zeros, B)
+    def stream_leg(pool, runner, warm, timed):
+        """One pass over the timed requests (after one over the warm-up requests) with inputs staged in HBM."""
+        w_staged, w_zeros = stage(warm)
+        runner(pool, warm, w_staged, w_zeros, B)
         del w_staged, w_zeros
-        staged, zeros = stage(cases)
+        staged, zeros = stage(timed)
         barrier()
-        created0 = bpool.created
+        created0 = pool.created
         launches0 = library.launch_count()
         with ClockSampler(local_rank) as clocks:
             t0 = time.perf_counter()
-            stats, kept = run_batched(bpool, cases, staged, zeros, B, keep=set(first_of_size.values()))
+            stats, kept = runner(pool, timed, staged, zeros, B, keep=set(first_of_size.values()))
             barrier()
             wall = time.perf_counter() - t0
         launches = library.launch_count() - launches0
         span_ms = max(x.device_end_ms for x in stats) - min(x.device_start_ms for x in stats)
-        value, span_ms = replica_throughput(len(cases), span_ms, world, "cuda")
-        service = [x.device_end_ms - x.device_start_ms for x in stats]
-        created_timed = bpool.created - created0
-        bpool.close()
+        value, span_ms = replica_throughput(len(timed), span_ms, world, "cuda")
+        leg = {"value": value, "span_ms": span_ms, "stats": stats, "kept": kept, "clocks": clocks, "wall": wall,
+               "launches": launches, "service": [x.device_end_ms - x.device_start_ms for x in stats],
+               "created": pool.created - created0}
+        pool.close()
         del staged, zeros
         torch.cuda.empty_cache()
+        return leg
+
+    def leg_summary(leg, mode):
+        return {"value": leg["value"], "unit": "solves/s", "ms_per_step": leg["span_ms"] / args.steps, "wall_s": leg["wall"],
+                "gpu_launches": int(leg["launches"]),
+                "latency_ms": {"p50": statistics.median(leg["service"]), "p99": float(np.percentile(leg["service"], 99))},
+                "cg_iterations_per_solve": {"min": min(x.linear_iterations_total for x in leg["stats"]),
+                                            "max": max(x.linear_iterations_total for x in leg["stats"])},
+                "mode": mode}
+
+    head = stream_leg(ResidentPool(nk, ctx), run_resident, warm_cases, cases)
+    batched = None
+    if args.batch_slots > 1:
+        # the same requests in batches: requests of one grid size share one batched graph (nk_batch)
+        b_leg = stream_leg(BatchPool(nk, ctx, args.batch_slots), run_batched, warm_cases, cases)
+        batched = leg_summary(b_leg, f"requests of one grid size solved together, up to {args.batch_slots} per batched graph "
+                                     f"(nk_batch; one launch per kernel for every slot), {B} requests in flight")
+        batched["rel_error_vs_headline"] = {key: rel_l2(*b_leg["kept"][k], *head["kept"][k]) for key, k in first_of_size.items()}
+        del b_leg
+    value, span_ms, stats, kept, clocks = head["value"], head["span_ms"], head["stats"], head["kept"], head["clocks"]
+    wall, launches, service, created_timed = head["wall"], head["launches"], head["service"], head["created"]
 
     if rank != 0:
         if world > 1:
@@ -866,7 +863,7 @@ def main():
 
     # ---- e2e: the same requests through the serving loop of the C ABI, host buffers, Poisson arrivals ---------
     from nunatak_gb300.server import Server
-    S = Server(max_in_flight=B, memory_cap_bytes=64 << 30, context=ctx, batch_slots=max(args.batch_slots, 0))
+    S = Server(max_in_flight=B, memory_cap_bytes=64 << 30, context=ctx)
     for c in warm_cases:
         S.submit(c)
     S.wait_all()
@@ -892,11 +889,7 @@ def main():
         "dtype": "f32 (multigrid) + f64 (CG, Picard)", "data": "synthetic (seeded marine ice sheets, no dataset)",
         "config": config,
         "timing": {"wall_s": wall, "problems_created_in_timed_region": created_timed},
-        "batching": {"slots": args.batch_slots if args.batch_slots > 1 else 1,
-                     "mode": (f"requests of one grid size solved together, up to {args.batch_slots} per batched graph "
-                              f"(nk_batch; one launch per kernel for every slot), {B} requests in flight"
-                              if args.batch_slots > 1 else "one solve per request")},
-        "unbatched": unbatched,
+        "batched": batched,
         "latency_ms": {"p50": statistics.median(service), "p99": float(np.percentile(service, 99)),
                        "note": "device time of each solve (start to end event) while sharing the GPU with the others"},
         "picard_iterations": {"min": min(piters), "max": max(piters)},

@@ -1339,6 +1339,7 @@ static nk_status problem_create(nk_context* ctx, const nk_grid_desc* grid, const
         if (solver->preconditioner < NK_PRECONDITIONER_NONE || solver->preconditioner > NK_PRECONDITIONER_MULTIGRID) bad("unknown preconditioner");
         if (solver->linear.kind != NK_CONVERGENCE && solver->linear.kind != NK_FIXED_ITERATIONS) bad("unknown linear iteration control");
         if (solver->picard.kind < NK_CONVERGENCE || solver->picard.kind > NK_VISCOSITY_CONVERGENCE) bad("unknown Picard iteration control");
+        if (solver->precision != NK_PRECISION_FP64 && solver->precision != NK_PRECISION_MIXED) bad("unknown precision");
         if (solver->precision == NK_PRECISION_MIXED && solver->preconditioner != NK_PRECONDITIONER_MULTIGRID)
             bad("mixed precision needs the multigrid preconditioner");
         if (solver->flags & ~NK_SOLVER_HOST_LOOP) bad("unknown solver flags");

@@ -391,6 +391,8 @@ def make_descriptors(grid: RectilinearGrid, Nsigma=10, bed_refinement=2.0, sigma
     p.mask_transition_thickness = m.transition_thickness
 
     s = abi.SolverDesc()
+    if velocity_solver.precision not in ("fp64", "mixed"):
+        raise ValueError(f"precision {velocity_solver.precision!r}: 'fp64' or 'mixed'")
     s.precision = abi.NK_PRECISION_MIXED if velocity_solver.precision == "mixed" else abi.NK_PRECISION_FP64
     P = velocity_solver.preconditioner
     if P is None:
