@@ -1054,6 +1054,187 @@ void launch_adjoint_gradient(const AdjointView& v, cudaStream_t s) {
     k_adjoint_gradient<<<d.grid, d.block, 0, s>>>(v); count_launch();
 }
 
+// ---- ∂J/∂H of the SSA fixed point with the geometry and the driving stress recomputed from H ----------------
+// J(x*(H)) where update_geometry! (ice_sheet_model_methods.jl:103-111: s, φᵘ, φᵛ, N, μ) and compute_driving_stress!
+// (driving_stress.jl:43-125) take H before the Picard solve, and update_stress_balance_coefficients! reads H in
+// η̄H = μ H Σ ησ Δζ (column_integrals.jl:61-71) and φᵘ, φᵛ, N in the drag (frictions.jl:142-160).  With the adjoint
+// state of the fixed point (λ = ∂J/∂τ, and the λ-signed sensitivities eb of η̄H and bb of β whose true adjoints are
+// -eb and -bb) each cell gathers, from its centre and its four faces:
+//   ∂J/∂H = -eb η̄ μ + Σ_faces λ ∂τ/∂H + (∂J/∂s) ds/dH + (∂J/∂μ) dμ/dH + Σ_faces (-bb) β̂ ∂φ/∂f + (∂J/∂N) dN/dH
+// with β = φ β̂, f = H + ρw b / ρᵢ.  The discrete switches (walls, fronts and ice-free faces from μ > 0, the branch of
+// s, the clamp of D) are held where they are.
+
+// ∂ front_force / ∂H and ∂s of the front cell c (driving_stress.jl:56-60)
+__device__ __forceinline__ void front_force_partials(const GeometryView& v, int c, double& dH, double& ds) {
+    double Hi = v.H[c], y = Hi - v.s[c];
+    double D, dDdH, dDds;
+    if (y <= 0.0) { D = 0.0; dDdH = 0.0; dDds = 0.0; }
+    else if (y >= Hi) { D = Hi; dDdH = 1.0; dDds = 0.0; }
+    else { D = y; dDdH = 1.0; dDds = -1.0; }
+    dH = v.gacc * (v.rho_i * Hi - v.rho_w * D * dDdH);
+    ds = -v.gacc * v.rho_w * D * dDds;
+}
+
+// Partials of one face's driving stress (u face: c1 west, c2 east, `w` = Δy at the face, `a` = Az ρᵢ g rdxf; v face
+// likewise in y) with respect to H and s of its two centres; false when the face carries no dependence on them.
+__device__ __forceinline__ bool tau_partials(const GeometryView& v, bool wall, int c1, int c2, double w, double a, double* dH, double* ds) {
+    dH[0] = dH[1] = ds[0] = ds[1] = 0.0;
+    if (wall) return false;
+    if (v.use_mask) {
+        bool m1 = v.mu[c1] > 0, m2 = v.mu[c2] > 0;
+        bool ice1 = m1 && !m2, ice2 = !m1 && m2;
+        if (ice1 || ice2) {   // the front: τ = Δ (ff(c1) if ice1) - Δ (ff(c2) if ice2)
+            double fh, fs;
+            if (ice1) { front_force_partials(v, c1, fh, fs); dH[0] = w * fh; ds[0] = w * fs; }
+            else { front_force_partials(v, c2, fh, fs); dH[1] = -w * fh; ds[1] = -w * fs; }
+            return true;
+        }
+    }
+    double H1 = v.H[c1], H2 = v.H[c2], s1 = v.s[c1], s2 = v.s[c2];
+    if (v.gl_stress) {   // grounding_line_stress, driving_stress.jl:84-92
+        double ri = v.rho_i, rw = v.rho_w;
+        double f1 = H1 + rw / ri * v.bed[c1], f2 = H2 + rw / ri * v.bed[c2];
+        bool straddles = ((f1 > 0) != (f2 > 0)) && (H1 > 0) && (H2 > 0);
+        if (straddles) {
+            double df = f1 - f2;
+            double theta = f1 / df;
+            double Hg = H1 + theta * (H2 - H1);
+            double cg = 1 - ri / rw;
+            double sg = cg * Hg;
+            double K = -ri * v.gacc / 2 * w;
+            double dHg = K * ((s2 - s1) + cg * (H1 - H2));   // ∂τ/∂Hg
+            double dth1 = -f2 / (df * df), dth2 = f1 / (df * df);
+            double dHg1 = 1 - theta + (H2 - H1) * dth1, dHg2 = theta + (H2 - H1) * dth2;
+            dH[0] = K * (sg - s1) + dHg * dHg1;
+            dH[1] = K * (s2 - sg) + dHg * dHg2;
+            ds[0] = -K * (H1 + Hg);
+            ds[1] = K * (Hg + H2);
+            return true;
+        }
+    }
+    // τ = -Az ρᵢ g ½ (H1 + H2) (s2 - s1) / Δ
+    dH[0] = dH[1] = -a * 0.5 * (s2 - s1);
+    ds[1] = -a * 0.5 * (H1 + H2);
+    ds[0] = -ds[1];
+    return true;
+}
+
+// ∂φ/∂f₁, ∂φ/∂f₂ of segment_fraction (subgrid_grounded_fraction.jl:34-38)
+__device__ __forceinline__ void segment_fraction_partials(double f1, double f2, double& d1, double& d2) {
+    double S = fabs(f1) + fabs(f2);
+    d1 = d2 = 0.0;
+    if (S == 0.0) return;
+    double fp = fmax(f1, 0.0) + fmax(f2, 0.0);
+    auto sg = [](double f) { return f > 0 ? 1.0 : (f < 0 ? -1.0 : 0.0); };
+    d1 = ((f1 > 0 ? 1.0 : 0.0) * S - fp * sg(f1)) / (S * S);
+    d2 = ((f2 > 0 ? 1.0 : 0.0) * S - fp * sg(f2)) / (S * S);
+}
+
+// β̂ = basal_drag(U, C, N) and ∂β̂/∂N (regularised Coulomb; zero for Weertman)
+__device__ __forceinline__ double basal_drag_dN(const PhysView& ph, double U, double C, double N, double& dN) {
+    double w = C * pow(U, ph.m - 1);
+    dN = 0.0;
+    if (ph.friction == NK_WEERTMAN) return w;
+    double tc = ph.alpha2 * N;
+    double Q = pow(C, 1 / ph.m) * U + pow(tc, 1 / ph.m);
+    double Qm = pow(Q, ph.m);
+    if (tc > 0) dN = ph.alpha2 * (w / Qm) * (1 - pow(tc, 1 / ph.m) / Q);
+    return w * tc / Qm;
+}
+
+// One face's drag partials for its two centres: (-bb) β̂ ∂φ/∂f into gf, (-bb) φ ∂β̂/∂N ½ into gN.
+__device__ __forceinline__ void drag_partials(const AdjointView& v, const GeometryView& gv, bool has, bool wall, int k, double U,
+                                              int c1, int c2, double phi, double bbar, double* gf, double* gN) {
+    gf[0] = gf[1] = gN[0] = gN[1] = 0.0;
+    if (!has || wall || v.ph.friction == NK_FRICTION_NONE) return;
+    const PhysView& ph = v.ph;
+    double Cf = (ph.C[c1] + ph.C[c2]) / 2;
+    double Nf = ph.use_N ? (ph.N[c1] + ph.N[c2]) / 2 : 0.0;
+    double dbN;
+    double bh = basal_drag_dN(ph, U, Cf, Nf, dbN);
+    double tb = -bbar;   // the true adjoint of β
+    if (gv.grounding) {
+        double rw_ri = gv.rho_w / gv.rho_i;
+        double d1, d2;
+        segment_fraction_partials(gv.H[c1] + rw_ri * gv.bed[c1], gv.H[c2] + rw_ri * gv.bed[c2], d1, d2);
+        gf[0] = tb * bh * d1;
+        gf[1] = tb * bh * d2;
+    }
+    if (ph.use_N) gN[0] = gN[1] = tb * phi * dbN * 0.5;
+}
+
+__global__ void k_adjoint_thickness(AdjointView v, GeometryView gv, double* grad_H) {
+    const DevGrid<double>& g = v.o.g;
+    const PhysView& ph = v.ph;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int c = g.idx(i, j);
+    // the centre: η̄H = μ H η̄ with eb gathered as in k_adjoint_viscosity
+    int fx[2], wx[2], fy[2], wy[2];
+    int nx = corners_of_centre(i, g.Nx, g.px, fx, wx), ny = corners_of_centre(j, g.Ny, g.py, fy, wy);
+    double eb = v.cbar[c].x;
+    for (int a = 0; a < nx; ++a)
+        for (int b = 0; b < ny; ++b) eb += (wx[a] * wy[b]) * v.cbar[g.idx(fx[a], fy[b])].y / 4;
+    double etab = 0.0;
+    for (int l = 0; l < ph.sig.N; ++l) etab += v.eta_sigma[(long long)l * ph.plane + c] * ph.sig.dz[l];
+    double H = gv.H[c];
+    double mu = ph.use_mask ? ph.mu[c] : 1.0;
+    double gH = -eb * etab * mu, gmu = ph.use_mask ? -eb * etab * H : 0.0, gs = 0.0, gf = 0.0, gN = 0.0;
+    double u02 = ph.u0 * ph.u0;
+    // the four faces; `side` is this centre's place in the face's pair
+    for (int f = 0; f < 4; ++f) {
+        bool xf = f < 2;
+        int fi = xf ? i + (f == 1) : i, fj = xf ? j : j + (f == 3);
+        int side = (f == 1 || f == 3) ? 0 : 1;
+        bool has = xf ? (fj < g.Ny && (fi < g.Nx || !g.px)) : (fi < g.Nx && (fj < g.Ny || !g.py));
+        if (!has) continue;
+        int k = xf ? g.u_idx(fi, fj) : g.v_idx(fi, fj);
+        int c1 = xf ? g.c_idx(fi - 1, fj) : g.c_idx(fi, fj - 1), c2 = g.c_idx(fi, fj);
+        bool peri = xf ? g.peripheral_fc(fi, fj) : g.peripheral_cf(fi, fj);
+        // driving stress
+        bool wall = peri || (gv.use_mask && (gv.mu[c1] + gv.mu[c2]) == 0.0);
+        double w = xf ? g.dyc[fj] : g.dxc[fi];
+        double a = xf ? g.Az_fc(fi, fj) * gv.rho_i * gv.gacc * g.rdxf[fi] : g.Az_cf(fi, fj) * gv.rho_i * gv.gacc * g.rdyf[fj];
+        double dH[2], ds[2];
+        if (tau_partials(gv, wall, c1, c2, w, a, dH, ds)) {
+            double lam = xf ? v.lam[k].x : v.lam[k].y;
+            gH += lam * dH[side];
+            gs += lam * ds[side];
+        }
+        // drag
+        double U;
+        if (xf) {
+            const double2* x = v.xs;
+            double vf = ((x[g.v_idx(fi - 1, fj)].y + x[g.v_idx(fi, fj)].y) / 2 + (x[g.v_idx(fi - 1, fj + 1)].y + x[g.v_idx(fi, fj + 1)].y) / 2) / 2;
+            double u = x[k].x;
+            U = sqrt(u * u + vf * vf + u02);
+        } else {
+            const double2* x = v.xs;
+            double uf = ((x[g.u_idx(fi, fj - 1)].x + x[g.u_idx(fi + 1, fj - 1)].x) / 2 + (x[g.u_idx(fi, fj)].x + x[g.u_idx(fi + 1, fj)].x) / 2) / 2;
+            double vv = x[k].y;
+            U = sqrt(vv * vv + uf * uf + u02);
+        }
+        double gfp[2], gNp[2];
+        double phi = xf ? ph.phi[k].x : ph.phi[k].y;
+        double bbar = xf ? v.bbar[k].x : v.bbar[k].y;
+        drag_partials(v, gv, true, peri, k, U, c1, c2, phi, bbar, gfp, gNp);
+        gf += gfp[side];
+        gN += gNp[side];
+    }
+    // chain through s, μ, f and N of this centre (update_geometry!)
+    double b = gv.bed[c];
+    double dsdH = gv.grounding ? ((b + H >= (1 - gv.rho_i / gv.rho_w) * H) ? 1.0 : 1 - gv.rho_i / gv.rho_w) : 1.0;
+    double t = (H - gv.mask_min) / gv.mask_trans;
+    double dmudH = (!gv.front && t > 0 && t < 1) ? 6 * t * (1 - t) / gv.mask_trans : 0.0;
+    double rig = gv.rho_i * gv.gacc;
+    double dNdH = (rig * H + gv.rho_w * gv.gacc * fmin(b, 0.0) > 0) ? rig : 0.0;
+    grad_H[c] = gH + gs * dsdH + gmu * dmudH + gf + gN * dNdH;
+}
+void launch_adjoint_thickness(const AdjointView& v, const GeometryView& gv, double* grad_H, cudaStream_t s) {
+    LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
+    k_adjoint_thickness<<<d.grid, d.block, 0, s>>>(v, gv, grad_H); count_launch();
+}
+
 // ---- DIVA: the reverse of one update_diva_coefficients! step at the fixed point ---------------------------------
 // The forward step (diva.jl:61-75) reads x, the lagged βᵇ⁻, F₂⁻ and ησ⁻ and writes:
 //   uᵇ = x / (1 + βᵇ⁻ ℑF₂⁻)                               (compute_basal_velocities!)

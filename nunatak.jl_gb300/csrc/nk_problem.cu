@@ -1536,7 +1536,7 @@ nk_status nk_problem_get_field_parent(const nk_problem* Pc, int32_t id, double* 
 
 // The geometry and the driving stress from H and the bed (update_state! without the velocity solve), on the
 // problem's stream.
-static void launch_problem_geometry(nk_problem* P) {
+static GeometryView problem_geometry_view(nk_problem* P) {
     GeometryView v;
     v.g = P->fine.g;
     v.H = P->H; v.bed = P->bed; v.s = P->s; v.N = P->N; v.mu = P->mu; v.phi = P->phi; v.phi_uv = P->phi_uv; v.tau = P->tau;
@@ -1545,8 +1545,9 @@ static void launch_problem_geometry(nk_problem* P) {
     v.mask_min = P->pd.mask_minimum_thickness; v.mask_trans = P->pd.mask_transition_thickness;
     v.ud = P->ud;
     v.front = P->front.enabled;
-    launch_geometry(v, P->stream);
+    return v;
 }
+static void launch_problem_geometry(nk_problem* P) { launch_geometry(problem_geometry_view(P), P->stream); }
 
 nk_status nk_compute_geometry(nk_problem* P) {
     if (!P) return NK_BAD_ARGUMENT;
@@ -1861,9 +1862,10 @@ nk_status nk_adjoint_solve(nk_problem* P, const double* bu, const double* bv, nk
 // the adjoint σ of s is swept along with λ (ext/NunatakEnzymeExt.jl:204-214): each iteration runs the step's reverse with q̄ = -λ and
 // the state adjoint σ, which yields r and the next σ.
 static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar, const nk_iteration_control& ctl, double* lu,
-                           double* lv, double* grad, double* grad_A, nk_solve_stats* st) {
+                           double* lv, double* grad, double* grad_A, double* grad_H, nk_solve_stats* st) {
     const bool diva = P->pd.stress_balance == NK_DIVA;
     if (P->ud) bad("nk_picard_adjoint: not available for a problem with prescribed velocities");
+    if (grad_H && diva) bad("nk_picard_adjoint_gradients: the thickness gradient is built for the SSA only");
     cudaStream_t s = P->stream;
     size_t pl = P->plane;
     if (!P->adj_base) {
@@ -1947,6 +1949,7 @@ static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar
     } else {
         if (grad_A) launch_adjoint_viscosity(v, s);
         launch_adjoint_gradient(v, s);
+        if (grad_H) launch_adjoint_thickness(v, problem_geometry_view(P), P->adj_g, s);   // gbar is free after the last pass
     }
     NK_CHECK_LAUNCH();
     if (lu && lv) vector_out(P, P->tmp_a, lu, lv);
@@ -1956,6 +1959,13 @@ static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar
         f.nx = P->Nx;
         f.ny = P->Ny;
         copy_out(P, f, grad);
+    }
+    if (grad_H) {
+        FieldLoc f;
+        f.base = P->adj_g;
+        f.nx = P->Nx;
+        f.ny = P->Ny;
+        copy_out(P, f, grad_H);
     }
     if (grad_A) {
         FieldLoc f;
@@ -1979,8 +1989,9 @@ static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar
     else if (!fixed && !(D <= std::max(ctl.reltol * M, ctl.abstol))) st->status = NK_NOT_CONVERGED;
 }
 
-nk_status nk_picard_adjoint(nk_problem* P, const double* ubar, const double* vbar, const nk_iteration_control* control,
-                            double* lambda_u, double* lambda_v, double* grad_log_C, double* grad_log_A, nk_solve_stats* stats) {
+nk_status nk_picard_adjoint_gradients(nk_problem* P, const double* ubar, const double* vbar, const nk_iteration_control* control,
+                                      double* lambda_u, double* lambda_v, double* grad_log_C, double* grad_log_A, double* grad_H,
+                                      nk_solve_stats* stats) {
     if (!P || !ubar || !vbar) return NK_BAD_ARGUMENT;
     return guarded(P->ctx, [&] {
         nk_iteration_control ctl = control ? *control : P->sd.picard;
@@ -1989,12 +2000,17 @@ nk_status nk_picard_adjoint(nk_problem* P, const double* ubar, const double* vba
         nk_solve_stats local{};
         nk_solve_stats* st = stats ? stats : &local;
         NK_CUDA(cudaEventRecord(P->ev0, P->stream));
-        picard_adjoint(P, ubar, vbar, ctl, lambda_u, lambda_v, grad_log_C, grad_log_A, st);
+        picard_adjoint(P, ubar, vbar, ctl, lambda_u, lambda_v, grad_log_C, grad_log_A, grad_H, st);
         NK_CUDA(cudaEventRecord(P->ev1, P->stream));
         NK_CUDA(cudaEventSynchronize(P->ev1));
         event_times(P, st);
         if (st->status == NK_NONFINITE) throw Failure{NK_NONFINITE, "non-finite Picard adjoint"};
     });
+}
+
+nk_status nk_picard_adjoint(nk_problem* P, const double* ubar, const double* vbar, const nk_iteration_control* control,
+                            double* lambda_u, double* lambda_v, double* grad_log_C, double* grad_log_A, nk_solve_stats* stats) {
+    return nk_picard_adjoint_gradients(P, ubar, vbar, control, lambda_u, lambda_v, grad_log_C, grad_log_A, nullptr, stats);
 }
 
 nk_status nk_picard_solve(nk_problem* P, nk_solve_stats* stats) {

@@ -49,6 +49,7 @@ def _declare(lib):
         "nk_problem_wait": ([vp, C.POINTER(abi.SolveStats)], i32),
         "nk_problem_query": ([vp, ip], i32),
         "nk_picard_adjoint": ([vp, dp, dp, C.POINTER(abi.IterationControl), dp, dp, dp, dp, C.POINTER(abi.SolveStats)], i32),
+        "nk_picard_adjoint_gradients": ([vp, dp, dp, C.POINTER(abi.IterationControl), dp, dp, dp, dp, dp, C.POINTER(abi.SolveStats)], i32),
         "nk_solve_velocities": ([vp, dp, dp, C.POINTER(abi.SolveStats)], i32),
         "nk_velocity_profile": ([vp], i32),
         "nk_multigrid_levels": ([vp, ip, ip, ip, i32], i32),

@@ -291,11 +291,13 @@ class Problem:
         """Enqueue picard_solve! on this problem's stream and return at once (see wait())."""
         _check(self._fn("picard_solve_async")(self._h), "picard_solve_async", self._err())
 
-    def picard_adjoint(self, ubar, vbar, control=None):
+    def picard_adjoint(self, ubar, vbar, control=None, thickness=False):
         """Fixed-point adjoint of the converged picard_solve! (the reverse rule of ext/NunatakEnzymeExt.jl:167-240)
         for x̄ = (ubar, vbar) = ∂J/∂(u, v): returns (λu, λv, ∂J/∂log C per cell, ∂J/∂log A in the layout of the rate
         factor, stats), λ being ∂J/∂τ.  `control` is a Convergence / FixedIterations (default: the solver's
-        adjoint_iteration_control, which itself defaults to the Picard control)."""
+        adjoint_iteration_control, which itself defaults to the Picard control).  thickness=True (SSA): also ∂J/∂H per
+        cell, the total derivative with the geometry and the driving stress recomputed from H
+        (nk_picard_adjoint_gradients), returned before the stats."""
         if control is None:
             control = getattr(self.desc, "adjoint_control", None)
         ub, vb = self._vec_in(ubar, vbar)
@@ -304,6 +306,14 @@ class Problem:
         grad_a = np.empty(self.shape("A"))
         stats = abi.SolveStats()
         ctl = C.byref(control.desc()) if control is not None else None
+        if thickness:
+            grad_h = np.empty((self.grid.Ny, self.grid.Nx))
+            st = self._fn("picard_adjoint_gradients")(self._h, ub.ctypes.data_as(_dptr), vb.ctypes.data_as(_dptr), ctl,
+                                                      lu.ctypes.data_as(_dptr), lv.ctypes.data_as(_dptr),
+                                                      grad.ctypes.data_as(_dptr), grad_a.ctypes.data_as(_dptr),
+                                                      grad_h.ctypes.data_as(_dptr), C.byref(stats))
+            _check(st, "picard_adjoint_gradients", self._err())
+            return lu, lv, grad, grad_a, grad_h, stats
         st = self._fn("picard_adjoint")(self._h, ub.ctypes.data_as(_dptr), vb.ctypes.data_as(_dptr), ctl,
                                         lu.ctypes.data_as(_dptr), lv.ctypes.data_as(_dptr), grad.ctypes.data_as(_dptr),
                                         grad_a.ctypes.data_as(_dptr), C.byref(stats))

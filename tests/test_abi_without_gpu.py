@@ -66,6 +66,7 @@ def test_null_handles_are_refused(lib):
         "nk_picard_solve": lambda: lib.nk_picard_solve(null, null),
         "nk_picard_solve_async": lambda: lib.nk_picard_solve_async(null),
         "nk_picard_adjoint": lambda: lib.nk_picard_adjoint(null, d, d, null, d, d, d, d, null),
+        "nk_picard_adjoint_gradients": lambda: lib.nk_picard_adjoint_gradients(null, d, d, null, d, d, d, d, d, null),
         "nk_problem_query": lambda: lib.nk_problem_query(null, C.byref(i32)),
         "nk_problem_wait": lambda: lib.nk_problem_wait(null, null),
         "nk_solve_velocities": lambda: lib.nk_solve_velocities(null, d, d, null),
@@ -81,6 +82,10 @@ def test_null_handles_are_refused(lib):
         "nk_server_wait_all": lambda: lib.nk_server_wait_all(null),
         "nk_server_info": lambda: lib.nk_server_info(null, None, None, None),
         "nk_picard_change_noalloc": lambda: lib.nk_picard_change_noalloc(null, null, null, null, null, null, null, null),
+        "nk_batch_create": lambda: lib.nk_batch_create(null, null, null, null, 2, null),
+        "nk_batch_picard_solve_async": lambda: lib.nk_batch_picard_solve_async(null, None),
+        "nk_batch_query": lambda: lib.nk_batch_query(null, C.byref(i32)),
+        "nk_batch_wait": lambda: lib.nk_batch_wait(null, null),
     }
     got = {name: f() for name, f in calls.items()}
     assert got == {name: bad for name in calls}
@@ -89,3 +94,6 @@ def test_null_handles_are_refused(lib):
     assert lib.nk_context_destroy(null) == abi.NK_OK
     assert lib.nk_problem_field_size(null, 0) == 0
     assert lib.nk_server_clock(null) == 0.0
+    assert lib.nk_batch_destroy(null) == abi.NK_OK
+    assert lib.nk_batch_slots(null) == 0
+    assert lib.nk_batch_problem(null, 0) is None

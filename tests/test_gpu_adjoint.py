@@ -237,3 +237,89 @@ def test_picard_adjoint_diva_matches_oracle_finite_difference(gpu_cls, oracle_cl
     fd = _directional_fd(O, "C", O.get("C"), d, xs, uo, vo)
     ad = float(np.sum(grad * d))
     assert abs(fd - ad) <= RTOL * np.sum(np.abs(grad * d)), (fd, ad)
+
+
+# ---- ∂J/∂H (nk_picard_adjoint_gradients) -----------------------------------------------------------------------------
+def _fd_thickness(P, case, cell, xs, uo, vo, delta):
+    """Centred difference of J in H at `cell`, the geometry and the driving stress recomputed from the perturbed H
+    (nk_compute_geometry), from converged solves warm-started at x*."""
+    vel = []
+    for sgn in (1.0, -1.0):
+        H = case.fields["H"].copy()
+        H[cell] += sgn * delta
+        P.set("H", H)
+        P.compute_geometry()
+        P.set("u", xs[0])
+        P.set("v", xs[1])
+        assert P.picard_solve().status == 0
+        vel.append((P.get("u"), P.get("v")))
+    P.set("H", case.fields["H"])
+    P.compute_geometry()
+    return _cost_difference(vel[0], vel[1], uo, vo) / (2 * delta)
+
+
+def _smooth_cells(case, grad, n, seed, delta_rel=1e-3):
+    """Seeded cells whose gradient is at least 1e-3 of the largest entry, with ice (H > 20 m, so the ice mask is 1 on
+    both sides of the difference) and the flotation function f = H + ρw b / ρᵢ of the cell and of its four neighbours
+    more than 100 steps from zero (the grounded fractions, s and N switch branch at f = 0)."""
+    H, b = case.fields["H"], case.fields["bed"]
+    f = H + 1028.0 / 918.0 * b
+    ny, nx = H.shape
+    ok = np.zeros_like(H, dtype=bool)
+    for j in range(ny):
+        for i in range(nx):
+            d = delta_rel * max(H[j, i], 10.0)
+            nb = [f[j, i]] + [f[jj, ii] for jj, ii in ((j, i - 1), (j, i + 1), (j - 1, i), (j + 1, i)) if 0 <= jj < ny and 0 <= ii < nx]
+            ok[j, i] = H[j, i] > 20.0 and min(abs(x) for x in nb) > 100 * d
+    cand = np.argwhere(ok & (np.abs(grad) >= 1e-3 * np.max(np.abs(grad))))
+    rng = np.random.default_rng(seed)
+    return [tuple(cand[k]) for k in rng.choice(len(cand), size=min(n, len(cand)), replace=False)]
+
+
+@pytest.mark.parametrize("kind", ["bounded", "periodic_x", "no_slip_coulomb"])
+def test_thickness_gradient_matches_finite_differences(gpu_cls, kind):
+    """∂J/∂H per cell against centred differences in H with the geometry (s, φᵘ, φᵛ, N, μ) and the driving stress
+    recomputed: through η̄H = μ H ∫η dζ, the drag's grounded fractions and effective pressure, the surface slope and
+    the calving-front force of the driving stress."""
+    case, P, uo, vo, ub, vb = _adjoint(gpu_cls, kind)
+    xs = (P.get("u"), P.get("v"))
+    ctl = M.Convergence(reltol=1e-12, maxiter=500)
+    lu, lv, grad, grad_a, grad_h, st = P.picard_adjoint(ub, vb, ctl, thickness=True)
+    assert st.status == 0
+    # the same call computes the other gradients unchanged
+    lu2, lv2, grad2, grad_a2, st2 = P.picard_adjoint(ub, vb, ctl)
+    assert np.array_equal(grad, grad2) and np.array_equal(lu, lu2)
+    assert np.max(np.abs(grad_h)) > 0
+    cells = _smooth_cells(case, grad_h, 8, 13)
+    assert len(cells) >= 4
+    for cell in cells:
+        delta = 1e-3 * max(case.fields["H"][cell], 10.0)
+        fd = _fd_thickness(P, case, cell, xs, uo, vo, delta)
+        assert abs(fd - grad_h[cell]) <= RTOL * abs(grad_h[cell]), (kind, cell, fd, grad_h[cell])
+
+
+def test_thickness_gradient_front_cells():
+    """The last ice cells of each row (the calving-front force path) against centred differences."""
+    case, P, uo, vo, ub, vb = _adjoint(nk.Problem, "bounded")
+    xs = (P.get("u"), P.get("v"))
+    *_, grad_h, st = P.picard_adjoint(ub, vb, M.Convergence(reltol=1e-12, maxiter=500), thickness=True)
+    H = case.fields["H"]
+    checked = 0
+    for j in range(2, H.shape[0] - 2, 3):
+        i = int(np.max(np.nonzero(H[j] > 0)[0]))
+        cell = (j, i)
+        if abs(grad_h[cell]) < 1e-3 * np.max(np.abs(grad_h)) or cell not in _smooth_cells(case, grad_h, 10**6, 0):
+            continue
+        checked += 1
+        delta = 1e-3 * H[cell]
+        fd = _fd_thickness(P, case, cell, xs, uo, vo, delta)
+        assert abs(fd - grad_h[cell]) <= RTOL * abs(grad_h[cell]), (cell, fd, grad_h[cell])
+    assert checked >= 2
+
+
+def test_thickness_gradient_refused_for_the_diva():
+    P = _diva("weertman").problem(nk.Problem)
+    assert P.picard_solve().status == 0
+    u, v = P.get("u"), P.get("v")
+    with pytest.raises(ValueError):
+        P.picard_adjoint(u, v, thickness=True)
