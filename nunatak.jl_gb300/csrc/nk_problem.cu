@@ -356,6 +356,10 @@ static void upload_metrics(Level<T>& L, cudaStream_t s) {
     add(xc); add(xf); add(yc); add(yf); add(inv(xc)); add(inv(xf)); add(inv(yc)); add(inv(yf));
     NK_CUDA(cudaMemcpyAsync(L.metrics, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice, s));
     NK_CUDA(cudaStreamSynchronize(s));   // host vector goes out of scope
+    bool uniform = true;
+    for (const auto* v : {&xc, &xf, &yc, &yf})
+        for (T e : *v) uniform = uniform && e == xc[0];
+    L.g.h = uniform ? xc[0] : T(0);
     T* m = L.metrics;
     L.g.dxc = m + METRIC_PAD; m += nx;
     L.g.dxf = m + METRIC_PAD; m += nx;

@@ -279,13 +279,90 @@ __device__ __forceinline__ void strip_apply_interior(const OpView<T>& o, Src&& s
     }
 }
 
+// The interior walk on a regular square grid (every spacing h, DevGrid::h != 0): with Δx = Δy = h the metric factors
+// of the stencil cancel, Δy Txx = 2η̄H (2 Δu + Δv), Δx Tyy = 2η̄H (2 Δv + Δu), Δx η̄Hᶠᶠ (∂u/∂y + ∂v/∂x) =
+// η̄Hᶠᶠ (Δᵧu + Δₓv) and Az β = h² β, with Δ the differences of neighbouring velocities.  The same operator in the same
+// sums, with the products by h and 1/h left out: results differ from the general walk in the last bits only.  No
+// metric is loaded.
+template <int R, uint8_t IU = U_IDENTITY, uint8_t IV = V_IDENTITY, typename T, typename Src, typename Extra, typename Emit>
+__device__ __forceinline__ void strip_apply_uniform(const OpView<T>& o, Src&& src, int i, int j0, Extra&& extra, Emit&& emit) {
+    using V2 = typename Vec2<T>::type;
+    using V4 = typename Vec4<T>::type;
+    using E = decltype(extra(0));
+    const DevGrid<T>& g = o.g;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x;
+    const bool own_col = lane >= 1 && lane <= STRIP_COLS;
+    const T h2 = g.h * g.h;
+
+    V2 raw[R + 2];            // rows j0 - 1 .. j0 + R
+    uint8_t msk[R + 2];
+    V4 rec[R + 1];            // centre (i, j), rows j0 - 1 .. j0 + R - 1
+    T cffR;                   // η̄Hᶠᶠ of corner (i, j0 + R); the others are rec[r + 1].y
+    E ex[R];
+#pragma unroll
+    for (int r = 0; r < R + 2; ++r) {
+        int k = g.idx(i, j0 - 1 + r);
+        msk[r] = __ldg(o.mask + k);
+        raw[r] = src(k, i, j0 - 1 + r);
+    }
+#pragma unroll
+    for (int r = 0; r < R + 1; ++r) rec[r] = o.coef[g.idx(i, j0 - 1 + r)];
+    cffR = o.coef[g.idx(i, j0 + R)].y;
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+        if (own_col) ex[r] = extra(g.idx(i, j0 + r));
+    auto mu = [&](int a) { return (msk[a] & U_INACTIVE) ? T(0) : raw[a].x; };
+    auto mv = [&](int a) { return (msk[a] & V_INACTIVE) ? T(0) : raw[a].y; };
+    auto cff = [&](int c) { return c < R ? rec[c + 1].y : cffR; };
+
+    auto centre = [&](int a, int c, T& sxx, T& syy) {
+        T u0 = mu(a), v0 = mv(a), vn = mv(a + 1);
+        T ue = __shfl_down_sync(full, u0, 1);
+        T du = ue - u0, dv = vn - v0;
+        T e2 = T(2) * rec[c].x;
+        sxx = e2 * (T(2) * du + dv);
+        syy = e2 * (T(2) * dv + du);
+    };
+    auto corner = [&](int a, int c) -> T {   // Δx × the corner shear (= Δy × it)
+        T u0 = mu(a), us = mu(a - 1), v0 = mv(a);
+        T vw = __shfl_up_sync(full, v0, 1);
+        return cff(c) * ((u0 - us) + (v0 - vw));
+    };
+
+    T sxx_s, syy_s;
+    centre(0, 0, sxx_s, syy_s);
+    T t_c = corner(1, 0);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        T sxx, syy;
+        centre(r + 1, r + 1, sxx, syy);
+        T t_n = corner(r + 2, r + 1);
+        T sxx_w = __shfl_up_sync(full, sxx, 1);
+        T t_e = __shfl_down_sync(full, t_c, 1);
+        if (own_col) {
+            const V4& c = rec[r + 1];
+            const V2& x = raw[r + 1];
+            T divu = (sxx - sxx_w) + (t_n - t_c);
+            T divv = (syy - syy_s) + (t_e - t_c);
+            V2 q;
+            q.x = (msk[r + 1] & IU) ? x.x : h2 * c.z * x.x - divu;
+            q.y = (msk[r + 1] & IV) ? x.y : h2 * c.w * x.y - divv;
+            emit(g.idx(i, j0 + r), q, x, ex[r]);
+        }
+        syy_s = syy;
+        t_c = t_n;
+    }
+}
+
 // The walk of the calling warp: the interior form when all its columns and rows are strictly inside the grid
-// (warp-uniform test), the general one otherwise.
+// (warp-uniform test; its regular-square-grid form when the level is one), the general one otherwise.
 template <int R, uint8_t IU = U_IDENTITY, uint8_t IV = V_IDENTITY, typename T, typename Src, typename Extra, typename Emit>
 __device__ __forceinline__ void strip_apply_src(const OpView<T>& o, Src&& src, int i, int j0, Extra&& extra, Emit&& emit) {
     const int i_first = i - (int)threadIdx.x;
     const bool interior = i_first >= 1 && i_first + 31 <= o.g.Nx - 2 && j0 - 1 >= 1 && j0 + R <= o.g.Ny - 2;
-    if (interior) strip_apply_interior<R, IU, IV>(o, src, i, j0, extra, emit);
+    if (interior && o.g.h != decltype(o.g.h)(0)) strip_apply_uniform<R, IU, IV>(o, src, i, j0, extra, emit);
+    else if (interior) strip_apply_interior<R, IU, IV>(o, src, i, j0, extra, emit);
     else strip_apply_general<R, IU, IV>(o, src, i, j0, extra, emit);
 }
 

@@ -258,6 +258,16 @@ def _fd_thickness(P, case, cell, xs, uo, vo, delta):
     return _cost_difference(vel[0], vel[1], uo, vo) / (2 * delta)
 
 
+def _fd_thickness_extrapolated(P, case, cell, xs, uo, vo):
+    """Richardson extrapolation (16 D(δ/4) - D(δ)) / 15 of centred differences with δ = 1e-3 H: near the calving front
+    the response to H curves strongly (the front force grows as H²), and the O(δ²) error of one centred difference
+    there reaches 1e-2 while the two-step combination is accurate to O(δ⁴)."""
+    delta = 1e-3 * max(case.fields["H"][cell], 10.0)
+    d1 = _fd_thickness(P, case, cell, xs, uo, vo, delta)
+    d4 = _fd_thickness(P, case, cell, xs, uo, vo, delta / 4)
+    return (16 * d4 - d1) / 15
+
+
 def _smooth_cells(case, grad, n, seed, delta_rel=1e-3):
     """Seeded cells whose gradient is at least 1e-3 of the largest entry, with ice (H > 20 m, so the ice mask is 1 on
     both sides of the difference) and the flotation function f = H + ρw b / ρᵢ of the cell and of its four neighbours
@@ -278,9 +288,9 @@ def _smooth_cells(case, grad, n, seed, delta_rel=1e-3):
 
 @pytest.mark.parametrize("kind", ["bounded", "periodic_x", "no_slip_coulomb"])
 def test_thickness_gradient_matches_finite_differences(gpu_cls, kind):
-    """∂J/∂H per cell against centred differences in H with the geometry (s, φᵘ, φᵛ, N, μ) and the driving stress
-    recomputed: through η̄H = μ H ∫η dζ, the drag's grounded fractions and effective pressure, the surface slope and
-    the calving-front force of the driving stress."""
+    """∂J/∂H per cell against extrapolated centred differences in H with the geometry (s, φᵘ, φᵛ, N, μ) and the
+    driving stress recomputed: through η̄H = μ H ∫η dζ, the drag's grounded fractions and effective pressure, the
+    surface slope and the calving-front force of the driving stress."""
     case, P, uo, vo, ub, vb = _adjoint(gpu_cls, kind)
     xs = (P.get("u"), P.get("v"))
     ctl = M.Convergence(reltol=1e-12, maxiter=500)
@@ -293,13 +303,12 @@ def test_thickness_gradient_matches_finite_differences(gpu_cls, kind):
     cells = _smooth_cells(case, grad_h, 8, 13)
     assert len(cells) >= 4
     for cell in cells:
-        delta = 1e-3 * max(case.fields["H"][cell], 10.0)
-        fd = _fd_thickness(P, case, cell, xs, uo, vo, delta)
+        fd = _fd_thickness_extrapolated(P, case, cell, xs, uo, vo)
         assert abs(fd - grad_h[cell]) <= RTOL * abs(grad_h[cell]), (kind, cell, fd, grad_h[cell])
 
 
 def test_thickness_gradient_front_cells():
-    """The last ice cells of each row (the calving-front force path) against centred differences."""
+    """The last ice cells of the rows (the calving-front force path) against extrapolated centred differences."""
     case, P, uo, vo, ub, vb = _adjoint(nk.Problem, "bounded")
     xs = (P.get("u"), P.get("v"))
     *_, grad_h, st = P.picard_adjoint(ub, vb, M.Convergence(reltol=1e-12, maxiter=500), thickness=True)
@@ -311,8 +320,7 @@ def test_thickness_gradient_front_cells():
         if abs(grad_h[cell]) < 1e-3 * np.max(np.abs(grad_h)) or cell not in _smooth_cells(case, grad_h, 10**6, 0):
             continue
         checked += 1
-        delta = 1e-3 * H[cell]
-        fd = _fd_thickness(P, case, cell, xs, uo, vo, delta)
+        fd = _fd_thickness_extrapolated(P, case, cell, xs, uo, vo)
         assert abs(fd - grad_h[cell]) <= RTOL * abs(grad_h[cell]), (cell, fd, grad_h[cell])
     assert checked >= 2
 
