@@ -467,7 +467,7 @@ nk_status nk_picard_solve(nk_problem* problem, nk_solve_stats* stats);
  * tighter reltol than for the SSA.  Problems with prescribed velocities are refused (NK_BAD_ARGUMENT). */
 nk_status nk_picard_adjoint(nk_problem* problem, const double* ubar, const double* vbar, const nk_iteration_control* control,
                             double* lambda_u, double* lambda_v, double* grad_log_C, double* grad_log_A, nk_solve_stats* stats);
-/* nk_picard_adjoint plus, in grad_H (Nx x Ny, or NULL), the thickness gradient ∂J/∂H of the SSA: the total derivative
+/* nk_picard_adjoint plus, in grad_H (Nx x Ny, or NULL), the thickness gradient ∂J/∂H: the total derivative
  * of J(x*(H)) when H enters the way update_velocities! uses it (src/Models/ice_sheet_model_methods.jl:103-131):
  * through the geometry of update_geometry! (s, the face grounded fractions, N and the ice mask of nk_compute_geometry),
  * the driving stress of compute_driving_stress! (interior slope, calving-front force, grounding-line split), and
@@ -476,8 +476,8 @@ nk_status nk_picard_adjoint(nk_problem* problem, const double* ubar, const doubl
  * (ext/NunatakEnzymeExt.jl:226-231) and Enzyme adds the geometry and driving-stress parts through update_state!;
  * here they come in one gradient.  The discrete switches (walls, fronts and ice-free faces, the grounded or floating
  * branch of s, the clamps of the mask and of N) are held where they are: the gradient is that of the smooth piece
- * containing H.  A partial-cell front's mask is its prognostic flag and carries no H derivative.  DIVA problems
- * with grad_H are refused (NK_BAD_ARGUMENT). */
+ * containing H.  A partial-cell front's mask is its prognostic flag and carries no H derivative.  For the DIVA H
+ * also enters F2 = H ∫(1-ζ)²/η dζ, whose adjoint the DIVA sweep carries, and the drag is the basal βᵇ on |uᵇ|. */
 nk_status nk_picard_adjoint_gradients(nk_problem* problem, const double* ubar, const double* vbar, const nk_iteration_control* control,
                                       double* lambda_u, double* lambda_v, double* grad_log_C, double* grad_log_A, double* grad_H,
                                       nk_solve_stats* stats);

@@ -1142,9 +1142,10 @@ __device__ __forceinline__ double basal_drag_dN(const PhysView& ph, double U, do
     return w * tc / Qm;
 }
 
-// One face's drag partials for its two centres: (-bb) β̂ ∂φ/∂f into gf, (-bb) φ ∂β̂/∂N ½ into gN.
+// One face's drag partials for its two centres: tb β̂ ∂φ/∂f into gf, tb φ ∂β̂/∂N ½ into gN, with tb the true adjoint of
+// the face's drag (β = φ β̂; the DIVA's βᵇ).
 __device__ __forceinline__ void drag_partials(const AdjointView& v, const GeometryView& gv, bool has, bool wall, int k, double U,
-                                              int c1, int c2, double phi, double bbar, double* gf, double* gN) {
+                                              int c1, int c2, double phi, double tb, double* gf, double* gN) {
     gf[0] = gf[1] = gN[0] = gN[1] = 0.0;
     if (!has || wall || v.ph.friction == NK_FRICTION_NONE) return;
     const PhysView& ph = v.ph;
@@ -1152,7 +1153,6 @@ __device__ __forceinline__ void drag_partials(const AdjointView& v, const Geomet
     double Nf = ph.use_N ? (ph.N[c1] + ph.N[c2]) / 2 : 0.0;
     double dbN;
     double bh = basal_drag_dN(ph, U, Cf, Nf, dbN);
-    double tb = -bbar;   // the true adjoint of β
     if (gv.grounding) {
         double rw_ri = gv.rho_w / gv.rho_i;
         double d1, d2;
@@ -1163,23 +1163,29 @@ __device__ __forceinline__ void drag_partials(const AdjointView& v, const Geomet
     if (ph.use_N) gN[0] = gN[1] = tb * phi * dbN * 0.5;
 }
 
-__global__ void k_adjoint_thickness(AdjointView v, GeometryView gv, double* grad_H) {
+__global__ void k_adjoint_thickness(AdjointView v, GeometryView gv, int diva, double* grad_H) {
     const DevGrid<double>& g = v.o.g;
     const PhysView& ph = v.ph;
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i >= g.Nx || j >= g.Ny) return;
     int c = g.idx(i, j);
-    // the centre: η̄H = μ H η̄ with eb gathered as in k_adjoint_viscosity
-    int fx[2], wx[2], fy[2], wy[2];
-    int nx = corners_of_centre(i, g.Nx, g.px, fx, wx), ny = corners_of_centre(j, g.Ny, g.py, fy, wy);
-    double eb = v.cbar[c].x;
-    for (int a = 0; a < nx; ++a)
-        for (int b = 0; b < ny; ++b) eb += (wx[a] * wy[b]) * v.cbar[g.idx(fx[a], fy[b])].y / 4;
-    double etab = 0.0;
-    for (int l = 0; l < ph.sig.N; ++l) etab += v.eta_sigma[(long long)l * ph.plane + c] * ph.sig.dz[l];
     double H = gv.H[c];
-    double mu = ph.use_mask ? ph.mu[c] : 1.0;
-    double gH = -eb * etab * mu, gmu = ph.use_mask ? -eb * etab * H : 0.0, gs = 0.0, gf = 0.0, gN = 0.0;
+    double gH, gmu, gs = 0.0, gf = 0.0, gN = 0.0;
+    if (diva) {   // the centre pass of the DIVA sweep left (∂J/∂H through η̄H and F₂, ∂J/∂μ)
+        gH = v.hmu[c].x;
+        gmu = v.hmu[c].y;
+    } else {      // η̄H = μ H η̄ with eb gathered as in k_adjoint_viscosity
+        int fx[2], wx[2], fy[2], wy[2];
+        int nx = corners_of_centre(i, g.Nx, g.px, fx, wx), ny = corners_of_centre(j, g.Ny, g.py, fy, wy);
+        double eb = v.cbar[c].x;
+        for (int a = 0; a < nx; ++a)
+            for (int b = 0; b < ny; ++b) eb += (wx[a] * wy[b]) * v.cbar[g.idx(fx[a], fy[b])].y / 4;
+        double etab = 0.0;
+        for (int l = 0; l < ph.sig.N; ++l) etab += v.eta_sigma[(long long)l * ph.plane + c] * ph.sig.dz[l];
+        double mu = ph.use_mask ? ph.mu[c] : 1.0;
+        gH = -eb * etab * mu;
+        gmu = ph.use_mask ? -eb * etab * H : 0.0;
+    }
     double u02 = ph.u0 * ph.u0;
     // the four faces; `side` is this centre's place in the face's pair
     for (int f = 0; f < 4; ++f) {
@@ -1201,23 +1207,22 @@ __global__ void k_adjoint_thickness(AdjointView v, GeometryView gv, double* grad
             gH += lam * dH[side];
             gs += lam * ds[side];
         }
-        // drag
+        // drag: β = φ β̂(|x|) for the SSA, βᵇ = φ β̂(|uᵇ|) for the DIVA
         double U;
+        const double2* x = diva ? v.ubs : v.xs;
         if (xf) {
-            const double2* x = v.xs;
             double vf = ((x[g.v_idx(fi - 1, fj)].y + x[g.v_idx(fi, fj)].y) / 2 + (x[g.v_idx(fi - 1, fj + 1)].y + x[g.v_idx(fi, fj + 1)].y) / 2) / 2;
             double u = x[k].x;
             U = sqrt(u * u + vf * vf + u02);
         } else {
-            const double2* x = v.xs;
             double uf = ((x[g.u_idx(fi, fj - 1)].x + x[g.u_idx(fi + 1, fj - 1)].x) / 2 + (x[g.u_idx(fi, fj)].x + x[g.u_idx(fi + 1, fj)].x) / 2) / 2;
             double vv = x[k].y;
             U = sqrt(vv * vv + uf * uf + u02);
         }
         double gfp[2], gNp[2];
         double phi = xf ? ph.phi[k].x : ph.phi[k].y;
-        double bbar = xf ? v.bbar[k].x : v.bbar[k].y;
-        drag_partials(v, gv, true, peri, k, U, c1, c2, phi, bbar, gfp, gNp);
+        double tb = diva ? (xf ? v.bbt[k].x : v.bbt[k].y) : -(xf ? v.bbar[k].x : v.bbar[k].y);   // true adjoints
+        drag_partials(v, gv, true, peri, k, U, c1, c2, phi, tb, gfp, gNp);
         gf += gfp[side];
         gN += gNp[side];
     }
@@ -1230,9 +1235,9 @@ __global__ void k_adjoint_thickness(AdjointView v, GeometryView gv, double* grad
     double dNdH = (rig * H + gv.rho_w * gv.gacc * fmin(b, 0.0) > 0) ? rig : 0.0;
     grad_H[c] = gH + gs * dsdH + gmu * dmudH + gf + gN * dNdH;
 }
-void launch_adjoint_thickness(const AdjointView& v, const GeometryView& gv, double* grad_H, cudaStream_t s) {
+void launch_adjoint_thickness(const AdjointView& v, const GeometryView& gv, int diva, double* grad_H, cudaStream_t s) {
     LaunchDims d = dims2d(v.o.g.Nx, v.o.g.Ny);
-    k_adjoint_thickness<<<d.grid, d.block, 0, s>>>(v, gv, grad_H); count_launch();
+    k_adjoint_thickness<<<d.grid, d.block, 0, s>>>(v, gv, diva, grad_H); count_launch();
 }
 
 // ---- DIVA: the reverse of one update_diva_coefficients! step at the fixed point ---------------------------------
@@ -1305,10 +1310,12 @@ __global__ void k_adjoint_diva_centre(AdjointView v) {
     double ty = (v.bbs[v0].y * v.ubs[v0].y + v.bbs[v1].y * v.ubs[v1].y) / 2;
     double t2 = tx * tx + ty * ty;
     double e2 = effective_strain_rate2(g, v.xs, nullptr, i, j, ph.wall_factor);
-    double e2b = 0.0, txb = 0.0, tyb = 0.0, gA = 0.0;
+    double e2b = 0.0, txb = 0.0, tyb = 0.0, gA = 0.0, etab_sum = 0.0, F_sum = 0.0;
     for (int l = 0; l < ph.sig.N; ++l) {
         long long o = (long long)l * ph.plane + k;
         double eta = v.eta_sigma[o];
+        etab_sum += eta * ph.sig.dz[l];
+        F_sum += (1 / eta) * ph.sig.w2[l];
         double em = eta == 0.0 ? INFINITY : eta;
         double a = (1 - ph.sig.zc[l]) / (2 * em), a2 = a * a;
         double ee = e2 + t2 * a2 + ph.eps0 * ph.eps0;
@@ -1324,6 +1331,10 @@ __global__ void k_adjoint_diva_centre(AdjointView v) {
         }
     }
     if (v.grad_log_A && !ph.rate_sigma) v.grad_log_A[k] = gA;
+    if (v.hmu) {   // η̄H = μ H η̄ and F₂ = H F
+        double mu = ph.use_mask ? ph.mu[k] : 1.0;
+        v.hmu[k] = make_double2(-eb * mu * etab_sum + F2b * F_sum, ph.use_mask ? -eb * H * etab_sum : 0.0);
+    }
     v.gbar[k] = e2b;
     v.txbar[k] = make_double2(txb, tyb);
 }

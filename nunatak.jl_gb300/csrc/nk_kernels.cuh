@@ -161,15 +161,18 @@ struct AdjointView {
     double2* ubp = nullptr;           // per face: ∂J/∂uᵇ through the basal shear stress of the centres
     double2* mbar = nullptr;          // per face: ∂J/∂(ℑF₂⁻) of the lagged shear factor
     double2* bbt = nullptr;           // per face: ∂J/∂βᵇ (all paths)
+    double2* hmu = nullptr;           // when set, the centre pass writes per centre (∂J/∂H through η̄H and F₂ at
+                                      // fixed μ, ∂J/∂μ through η̄H): the thickness gradient's coefficient part
 };
 void launch_adjoint_coefficients(const AdjointView& v, cudaStream_t s);
 void launch_adjoint_viscosity(const AdjointView& v, cudaStream_t s);
 void launch_adjoint_velocity(const AdjointView& v, cudaStream_t s);
 void launch_adjoint_gradient(const AdjointView& v, cudaStream_t s);
 struct GeometryView;
-// SSA: ∂J/∂H per centre with update_geometry! and compute_driving_stress! recomputed from H (after the final
-// launch_adjoint_coefficients; eta_sigma of c(x*), λ and the drag sensitivities as the adjoint left them)
-void launch_adjoint_thickness(const AdjointView& v, const GeometryView& gv, double* grad_H, cudaStream_t s);
+// ∂J/∂H per centre with update_geometry! and compute_driving_stress! recomputed from H, after the final pass of the
+// adjoint (SSA: launch_adjoint_coefficients, eta_sigma of c(x*), λ and the drag sensitivities; DIVA: the sweep with
+// v.hmu set, and bbt)
+void launch_adjoint_thickness(const AdjointView& v, const GeometryView& gv, int diva, double* grad_H, cudaStream_t s);
 // DIVA reverse sweep of one Picard step at the fixed point (after launch_adjoint_coefficients): the centre pass
 // (viscosity, F₂, ησ; grad_log_A when set), the face pass (effective drag, basal shear stress, drag speed), the
 // velocity pass (uᵇ = x / (1 + βᵇ⁻ ℑF₂⁻), strain rates; writes r and σ of βᵇ) and the F₂⁻ pass (σ of F₂)

@@ -232,6 +232,7 @@ struct nk_problem {
     // DIVA adjoint scratch (first DIVA nk_picard_adjoint): 8 pair planes (cbar, bbar, txbar, σ βᵇ, Ū, ūᵇ part,
     // ℑF₂⁻ adjoint, β̄ᵇ), σ F₂ and σ ησ (Nσ planes)
     void* adj_diva = nullptr;
+    double2* adj_hmu = nullptr;                  // DIVA thickness gradient: (∂J/∂H via η̄H and F₂, ∂J/∂μ) per centre
     // Prescribed velocities (u_D, v_D) per face, NaN where free; allocated by the first set of either prescribed
     // field.  Its faces become identity rows whose values enter their neighbours' strain rates.
     double2* ud = nullptr;
@@ -356,9 +357,9 @@ static void upload_metrics(Level<T>& L, cudaStream_t s) {
     add(xc); add(xf); add(yc); add(yf); add(inv(xc)); add(inv(xf)); add(inv(yc)); add(inv(yf));
     NK_CUDA(cudaMemcpyAsync(L.metrics, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice, s));
     NK_CUDA(cudaStreamSynchronize(s));   // host vector goes out of scope
-    bool uniform = true;
+    bool uniform = true;   // over the filled entries (metric_host leaves the last one of each array at zero)
     for (const auto* v : {&xc, &xf, &yc, &yf})
-        for (T e : *v) uniform = uniform && e == xc[0];
+        for (size_t q = 0; q + 1 < v->size(); ++q) uniform = uniform && (*v)[q] == xc[0];
     L.g.h = uniform ? xc[0] : T(0);
     T* m = L.metrics;
     L.g.dxc = m + METRIC_PAD; m += nx;
@@ -1382,6 +1383,7 @@ nk_status nk_problem_destroy(nk_problem* P) {
     if (P->ev1) cudaEventDestroy(P->ev1);
     if (P->adj_base) cudaFree(P->adj_base);
     if (P->adj_diva) cudaFree(P->adj_diva);
+    if (P->adj_hmu) cudaFree(P->adj_hmu);
     if (P->ud) cudaFree(P->ud);
     if (P->thermal) cudaFree(P->thermal);
     if (P->transport) cudaFree(P->transport);
@@ -1869,7 +1871,6 @@ static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar
                            double* lv, double* grad, double* grad_A, double* grad_H, nk_solve_stats* st) {
     const bool diva = P->pd.stress_balance == NK_DIVA;
     if (P->ud) bad("nk_picard_adjoint: not available for a problem with prescribed velocities");
-    if (grad_H && diva) bad("nk_picard_adjoint_gradients: the thickness gradient is built for the SSA only");
     cudaStream_t s = P->stream;
     size_t pl = P->plane;
     if (!P->adj_base) {
@@ -1880,6 +1881,7 @@ static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar
         P->adj_grad_A = P->adj_grad + pl;
     }
     if (diva && !P->adj_diva) NK_CUDA(cudaMalloc(&P->adj_diva, pl * (8 * sizeof(double2) + (1 + (size_t)P->Ns) * sizeof(double))));
+    if (diva && grad_H && !P->adj_hmu) NK_CUDA(cudaMalloc((void**)&P->adj_hmu, pl * sizeof(double2)));
     NK_CUDA(cudaMemcpyAsync(P->xprev, P->x, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));   // x*
     update_coefficients(P);                                                                         // c(x*)
     vector_in(P, P->adj_xbar, ubar, vbar);
@@ -1948,12 +1950,14 @@ static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar
     launch_adjoint_coefficients(v, s);
     if (grad_A) v.grad_log_A = P->adj_grad_A;
     if (diva) {
+        if (grad_H) v.hmu = P->adj_hmu;
         launch_adjoint_diva(v, s);
         launch_adjoint_diva_gradient(v, s);
+        if (grad_H) launch_adjoint_thickness(v, problem_geometry_view(P), 1, P->adj_g, s);   // gbar is free after the last pass
     } else {
         if (grad_A) launch_adjoint_viscosity(v, s);
         launch_adjoint_gradient(v, s);
-        if (grad_H) launch_adjoint_thickness(v, problem_geometry_view(P), P->adj_g, s);   // gbar is free after the last pass
+        if (grad_H) launch_adjoint_thickness(v, problem_geometry_view(P), 0, P->adj_g, s);
     }
     NK_CHECK_LAUNCH();
     if (lu && lv) vector_out(P, P->tmp_a, lu, lv);

@@ -295,7 +295,7 @@ class Problem:
         """Fixed-point adjoint of the converged picard_solve! (the reverse rule of ext/NunatakEnzymeExt.jl:167-240)
         for x̄ = (ubar, vbar) = ∂J/∂(u, v): returns (λu, λv, ∂J/∂log C per cell, ∂J/∂log A in the layout of the rate
         factor, stats), λ being ∂J/∂τ.  `control` is a Convergence / FixedIterations (default: the solver's
-        adjoint_iteration_control, which itself defaults to the Picard control).  thickness=True (SSA): also ∂J/∂H per
+        adjoint_iteration_control, which itself defaults to the Picard control).  thickness=True: also ∂J/∂H per
         cell, the total derivative with the geometry and the driving stress recomputed from H
         (nk_picard_adjoint_gradients), returned before the stats."""
         if control is None:

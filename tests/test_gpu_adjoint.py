@@ -325,9 +325,37 @@ def test_thickness_gradient_front_cells():
     assert checked >= 2
 
 
-def test_thickness_gradient_refused_for_the_diva():
-    P = _diva("weertman").problem(nk.Problem)
-    assert P.picard_solve().status == 0
-    u, v = P.get("u"), P.get("v")
-    with pytest.raises(ValueError):
-        P.picard_adjoint(u, v, thickness=True)
+@pytest.mark.parametrize("friction", ["weertman", "coulomb"])
+def test_thickness_gradient_diva_matches_directional_differences(gpu_cls, friction):
+    """DIVA ∂J/∂H (H also in F₂ = H ∫(1-ζ)²/η dζ and in the basal drag's grounded fractions on |uᵇ|) against
+    Richardson-extrapolated directional differences along a seeded direction d H over the cells away from the
+    flotation switch (one cell moves J too little against the solver tolerances); the rate factor is held."""
+    case, P, uo, vo = _diva_setup(gpu_cls, friction)
+    _, ub, vb = _cost(P, uo, vo)
+    xs = (P.get("u"), P.get("v"))
+    *_, gh, st = P.picard_adjoint(ub, vb, DIVA_ADJOINT, thickness=True)
+    assert st.status == 0 and np.max(np.abs(gh)) > 0
+    H0 = case.fields["H"]
+    keep = np.zeros(H0.shape, bool)
+    for cell in _smooth_cells(case, gh, 10**6, 0):
+        keep[cell] = True
+    assert keep.sum() > 20
+    d = np.random.default_rng(23).standard_normal(H0.shape) * keep * H0
+
+    def fd(eps):
+        vel = []
+        for sgn in (1.0, -1.0):
+            P.set("H", H0 + sgn * eps * d)
+            P.compute_geometry()
+            P.set("u", xs[0])
+            P.set("v", xs[1])
+            assert P.picard_solve().status == 0
+            vel.append((P.get("u"), P.get("v")))
+        P.set("H", H0)
+        P.compute_geometry()
+        return _cost_difference(vel[0], vel[1], uo, vo) / (2 * eps)
+
+    eps = 1e-4
+    rich = (16 * fd(eps / 4) - fd(eps)) / 15
+    ad = float(np.sum(gh * d))
+    assert abs(rich - ad) <= RTOL * np.sum(np.abs(gh * d)), (friction, rich, ad)
