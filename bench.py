@@ -295,8 +295,9 @@ def run_reference(args, rank):
 
 
 # FP64 instructions (DADD + DMUL + DFMA) per cell of the operator apply, from the ncu counts of
-# smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on on the 2048x1024 k_apply (10.5 + 16.8 + 8.3).
-FP64_OPERATOR_INSTR_PER_CELL = 35.6
+# smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on on the 2048x1024 k_apply, regular-grid walk
+# (14.0 + 6.4 + 4.5; profiles/operator_fp64_2048x1024.md).
+FP64_OPERATOR_INSTR_PER_CELL = 24.9
 FP64_INSTR_PER_SM_CLOCK = 2      # GB300 FP64 pipe: 2 thread instructions per SM per clock
 SMS = 152
 
