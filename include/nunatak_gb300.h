@@ -332,6 +332,12 @@ nk_status nk_compute_thermal_diagnostics(nk_problem* problem, const nk_thermal_p
  * stage (update_state! without the velocity solve), so the surface, masks, grounded fractions, effective
  * pressure and driving stress follow the new thickness.  NK_BAD_ARGUMENT when dt is not finite and positive. */
 nk_status nk_step_thickness(nk_problem* problem, double dt, int32_t grounded_melt_coupling);
+/* One stage (1, 2 or 3) of nk_step_thickness: stage 1 records the step's starting thickness, which stages 2 and 3
+ * start from; the three in order, with nothing between them, equal nk_step_thickness bit for bit.  The reference's
+ * default velocity schedule, IterationInterval(1) (src/StressBalances/stress_balance_solver.jl:43-52), solves the
+ * velocity in update_state! after every stage; a host that follows it calls stage 1, nk_picard_solve, stage 2,
+ * nk_picard_solve, stage 3, nk_picard_solve, so each stage advects with the previous stage's velocities. */
+nk_status nk_step_thickness_stage(nk_problem* problem, double dt, int32_t stage, int32_t grounded_melt_coupling);
 
 /* The thickness advection scheme of nk_step_thickness, IceSheetModel's `advection` keyword
  * (src/Models/ice_sheet_model.jl:79-123):

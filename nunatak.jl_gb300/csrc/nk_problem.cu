@@ -1669,31 +1669,57 @@ nk_status nk_step_enthalpy(nk_problem* P, const nk_energy_params* prm, double dt
     });
 }
 
+}  // extern "C"
+
+namespace nk {
+static void check_thickness_step(nk_problem* P, double dt) {
+    if (!(dt > 0) || !std::isfinite(dt)) bad("the time step must be finite and positive");
+    if (P->async_pending) bad("an asynchronous solve is pending (nk_problem_wait first)");
+    const nk_advection_desc& adv = P->advection;
+    const bool bounded = adv.scheme == NK_ADVECTION_WENO && adv.bounded;
+    int halo = std::min(P->gd.halo_x, P->gd.halo_y);
+    if (bounded && halo < 4)   // check_advection_halo, src/Models/ice_sheet_model.jl:131-135
+        bad("bounded WENO(order = 5) needs a horizontal halo of at least 4, got (" + std::to_string(P->gd.halo_x) + ", " +
+            std::to_string(P->gd.halo_y) + ")");
+    if ((adv.scheme == NK_ADVECTION_WENO || adv.order == 3) && halo < 3)
+        bad("the advection scheme's stencil needs a horizontal halo of at least 3");
+}
+
+// Stage st (0, 1, 2) of one thickness step: the first caches the step's starting H; each recomputes the limiter from
+// the stage's thickness, sets H = max(0, H_start + Δτ G(H)), the last adds its clip and advances a front; then the
+// geometry (rk_substep! and update_state! without the velocity solve, time_stepping.jl:15-25).
+static void thickness_stage(nk_problem* P, double dt, int st, int coupling) {
+    const bool bounded = P->advection.scheme == NK_ADVECTION_WENO && P->advection.bounded;
+    ThicknessView v = thickness_view(P, coupling != 0);
+    if (st == 0) NK_CUDA(cudaMemcpyAsync((double*)v.H0, P->H, P->plane * sizeof(double), cudaMemcpyDeviceToDevice, P->stream));
+    const double stages[3] = {1.0 / 3, 1.0 / 2, 1.0};     // SplitRungeKutta3 (Wicker-Skamarock) fractions
+    NK_CUDA(cudaMemcpyAsync((double*)v.Hs, P->H, P->plane * sizeof(double), cudaMemcpyDeviceToDevice, P->stream));
+    if (bounded) launch_thickness_limiter(v, P->stream);
+    launch_thickness_stage(v, stages[st] * dt, st == 2, P->stream);
+    if (st == 2 && P->front.enabled)   // rk_substep!: advance_front! after the final stage (time_stepping.jl:23)
+        launch_advance_front(front_view(P, coupling != 0), P->front.passes, stages[st] * dt, P->plane, P->stream);
+    launch_problem_geometry(P);
+    NK_CHECK_LAUNCH();
+}
+}  // namespace nk
+
+extern "C" {
+
 nk_status nk_step_thickness(nk_problem* P, double dt, int32_t grounded_melt_coupling) {
     if (!P) return NK_BAD_ARGUMENT;
     return guarded(P->ctx, [&] {
-        if (!(dt > 0) || !std::isfinite(dt)) bad("the time step must be finite and positive");
-        if (P->async_pending) bad("an asynchronous solve is pending (nk_problem_wait first)");
-        const nk_advection_desc& adv = P->advection;
-        const bool bounded = adv.scheme == NK_ADVECTION_WENO && adv.bounded;
-        int halo = std::min(P->gd.halo_x, P->gd.halo_y);
-        if (bounded && halo < 4)   // check_advection_halo, src/Models/ice_sheet_model.jl:131-135
-            bad("bounded WENO(order = 5) needs a horizontal halo of at least 4, got (" + std::to_string(P->gd.halo_x) + ", " +
-                std::to_string(P->gd.halo_y) + ")");
-        if ((adv.scheme == NK_ADVECTION_WENO || adv.order == 3) && halo < 3)
-            bad("the advection scheme's stencil needs a horizontal halo of at least 3");
-        ThicknessView v = thickness_view(P, grounded_melt_coupling != 0);
-        NK_CUDA(cudaMemcpyAsync((double*)v.H0, P->H, P->plane * sizeof(double), cudaMemcpyDeviceToDevice, P->stream));
-        const double stages[3] = {1.0 / 3, 1.0 / 2, 1.0};     // SplitRungeKutta3 (Wicker-Skamarock) fractions
-        for (int st = 0; st < 3; ++st) {
-            NK_CUDA(cudaMemcpyAsync((double*)v.Hs, P->H, P->plane * sizeof(double), cudaMemcpyDeviceToDevice, P->stream));
-            if (bounded) launch_thickness_limiter(v, P->stream);
-            launch_thickness_stage(v, stages[st] * dt, st == 2, P->stream);
-            if (st == 2 && P->front.enabled)   // rk_substep!: advance_front! after the final stage (time_stepping.jl:23)
-                launch_advance_front(front_view(P, grounded_melt_coupling != 0), P->front.passes, stages[st] * dt, P->plane, P->stream);
-            launch_problem_geometry(P);
-            NK_CHECK_LAUNCH();
-        }
+        check_thickness_step(P, dt);
+        for (int st = 0; st < 3; ++st) thickness_stage(P, dt, st, grounded_melt_coupling);
+        NK_CUDA(cudaStreamSynchronize(P->stream));
+    });
+}
+
+nk_status nk_step_thickness_stage(nk_problem* P, double dt, int32_t stage, int32_t grounded_melt_coupling) {
+    if (!P) return NK_BAD_ARGUMENT;
+    return guarded(P->ctx, [&] {
+        check_thickness_step(P, dt);
+        if (stage < 1 || stage > 3) bad("stage must be 1, 2 or 3");
+        thickness_stage(P, dt, stage - 1, grounded_melt_coupling);
         NK_CUDA(cudaStreamSynchronize(P->stream));
     });
 }

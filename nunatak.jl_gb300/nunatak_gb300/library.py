@@ -34,6 +34,7 @@ def _declare(lib):
         "nk_compute_rate_factor": ([vp] + [C.c_double] * 9, i32),
         "nk_compute_thermal_diagnostics": ([vp, C.POINTER(abi.ThermalParams)], i32),
         "nk_step_thickness": ([vp, C.c_double, i32], i32),
+        "nk_step_thickness_stage": ([vp, C.c_double, i32, i32], i32),
         "nk_set_thickness_advection": ([vp, C.POINTER(abi.AdvectionDesc)], i32),
         "nk_set_front": ([vp, C.POINTER(abi.FrontDesc)], i32),
         "nk_initialize_front": ([vp], i32),

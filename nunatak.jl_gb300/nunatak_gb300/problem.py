@@ -237,6 +237,12 @@ class Problem:
         src/Models/time_stepping.jl:15-72, with the problem's advection scheme, the geometry after every stage)."""
         _check(self._fn("step_thickness")(self._h, float(dt), int(grounded_melt_coupling)), "step_thickness", self._err())
 
+    def step_thickness_stage(self, dt, stage, grounded_melt_coupling=False):
+        """One stage (1, 2 or 3) of step_thickness (nk_step_thickness_stage): a host that solves the velocity after
+        every stage, as the reference's default IterationInterval(1) schedule does, calls stage, picard_solve, ..."""
+        _check(self._fn("step_thickness_stage")(self._h, float(dt), int(stage), int(grounded_melt_coupling)),
+               "step_thickness_stage", self._err())
+
     def update_coefficients(self):
         _check(self._fn("update_coefficients")(self._h), "update_coefficients", self._err())
 

@@ -830,6 +830,7 @@ struct Problem {
     // temperatures, basal melt rate m, thickness of the previous energy step Hⁿ, strain heating Φ
     Field Hw, gmelt, G, Ts, To, melt, Hn, sb;   // sb: the temperate fraction sᵇ of the basal layer (output)
     Field smb, clipped;           // thickness step (nko_step_thickness): surface mass balance, clipped thickness
+    Field H_step0;                // the thickness at the start of the current step (its stages start from it)
     // thickness advection (nko_set_thickness_advection); the reference's default for the SSA and the DIVA is
     // WENO(order = 5, bounds = (0, 1e5)) (default_thickness_advection, src/Models/ice_sheet_model.jl:123)
     nk_advection_desc advection{NK_ADVECTION_WENO, 5, 1, 0, 0.0, 1e5};
@@ -2059,17 +2060,21 @@ static void advance_front(Problem& P, double dt, bool coupled) {
 // ------------------------------------------------------------------------------------------------
 static void compute_geometry(Problem& P);
 
-static void step_thickness(Problem& P, double dt, bool coupled) {
+// Stage st (0, 1, 2) of one thickness step (rk_substep! then update_state! without the velocity solve); stage 0
+// records the step's starting thickness, which every stage starts from.
+static void step_thickness_stage(Problem& P, double dt, int st, bool coupled) {
     const Grid& g = P.grid;
     const int Nx = g.Nx(), Ny = g.Ny();
     const nk_advection_desc adv = P.advection;
     const bool bounded = adv.scheme == NK_ADVECTION_WENO && adv.bounded;
     fill_halo(P.x);
     for (Field* f : {&P.smb, &P.melt, &P.gmelt, &P.clipped}) fill_halo(*f);
-    Field H0 = P.H, Gt(&g, CENTER, CENTER);
+    if (st == 0) P.H_step0 = P.H;
+    Field& H0 = P.H_step0;
+    Field Gt(&g, CENTER, CENTER);
     if (bounded && !P.theta.g) P.theta.init(&g, CENTER, CENTER);
     const double stages[3] = {1.0 / 3, 1.0 / 2, 1.0};
-    for (int st = 0; st < 3; ++st) {
+    {
         fill_halo(P.H);
         if (bounded) {
 #pragma omp parallel for schedule(static)
@@ -2120,6 +2125,10 @@ static void step_thickness(Problem& P, double dt, bool coupled) {
         if (final_stage && P.front.enabled) advance_front(P, dtau, coupled);   // rk_substep!, :23
         compute_geometry(P);
     }
+}
+
+static void step_thickness(Problem& P, double dt, bool coupled) {
+    for (int st = 0; st < 3; ++st) step_thickness_stage(P, dt, st, coupled);
 }
 
 // ---- field access in interior layout -------------------------------------------------------------
@@ -2397,6 +2406,17 @@ nk_status nko_step_thickness(nko_problem* h, double dt, int32_t coupled) {
     if ((P.advection.scheme == NK_ADVECTION_WENO || P.advection.order == 3) && halo < 3)
         return NK_BAD_ARGUMENT;   // the five-point stencils reach three cells beyond a face
     step_thickness(P, dt, coupled != 0);
+    return NK_OK;
+}
+
+// One stage (1, 2, 3) of nko_step_thickness; the three in order equal it.
+nk_status nko_step_thickness_stage(nko_problem* h, double dt, int32_t stage, int32_t coupled) {
+    if (!h || !(dt > 0) || stage < 1 || stage > 3) return NK_BAD_ARGUMENT;
+    Problem& P = *reinterpret_cast<Problem*>(h);
+    int halo = std::min(P.grid.x.H, P.grid.y.H);
+    if (P.advection.scheme == NK_ADVECTION_WENO && P.advection.bounded && halo < 4) return NK_BAD_ARGUMENT;
+    if ((P.advection.scheme == NK_ADVECTION_WENO || P.advection.order == 3) && halo < 3) return NK_BAD_ARGUMENT;
+    step_thickness_stage(P, dt, stage - 1, coupled != 0);
     return NK_OK;
 }
 

@@ -49,6 +49,7 @@ def load():
             "nko_energy_field": [vp, C.c_int32, dp, i64, C.c_int32],
             "nko_step_enthalpy": [vp, dp, C.c_double],
             "nko_step_thickness": [vp, C.c_double, C.c_int32],
+            "nko_step_thickness_stage": [vp, C.c_double, C.c_int32, C.c_int32],
             "nko_set_thickness_advection": [vp, C.POINTER(abi.AdvectionDesc)],
             "nko_set_front": [vp, C.POINTER(abi.FrontDesc)],
             "nko_initialize_front": [vp],
@@ -119,6 +120,10 @@ class OracleProblem(Problem):
     def step_thickness(self, dt, grounded_melt_coupling=False):
         """One ice time step of the thickness with the velocities held (time_step! without a velocity solve)."""
         _check(self._lib.nko_step_thickness(self._h, float(dt), int(grounded_melt_coupling)), "step_thickness")
+
+    def step_thickness_stage(self, dt, stage, grounded_melt_coupling=False):
+        """One stage (1, 2, 3) of step_thickness."""
+        _check(self._lib.nko_step_thickness_stage(self._h, float(dt), int(stage), int(grounded_melt_coupling)), "step_thickness_stage")
 
     def grid_metrics(self, which):
         n = (self.grid.Nx if which in (0,) else self.grid.Nx + 1 if which == 1 else self.grid.Ny if which == 2 else self.grid.Ny + 1)

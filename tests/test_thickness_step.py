@@ -20,7 +20,7 @@ import math
 import numpy as np
 import pytest
 
-from nunatak_gb300 import model as M
+from nunatak_gb300 import model as M, workloads
 from support import evaluate, make
 
 
@@ -117,7 +117,7 @@ def test_basal_melt_acts_on_the_floating_part_only(backend):
     np.testing.assert_allclose(dH, -dt * m * (1 - phi), rtol=1e-6)
 
 
-def seeded_shelf(cls, Nx=48, Ny=40, steps=4, dt=2e8, advection=None):
+def seeded_shelf(cls, Nx=48, Ny=40, steps=4, dt=2e8, advection=None, by_stage=False):
     """Four thickness steps of a seeded ice shelf over a sloping bed (grounded at x = 0, afloat downstream),
     Bounded in x and Periodic in y, with random velocities in both directions, the subgrid grounded fraction,
     sources, a coupled grounded melt and thin cells that the melt clips."""
@@ -138,7 +138,11 @@ def seeded_shelf(cls, Nx=48, Ny=40, steps=4, dt=2e8, advection=None):
     P.energy_set("grounded_melt", rng.uniform(0, 1e-9, (Ny, Nx)))
     P.energy_set("clipped_thickness", 0.0)
     for _ in range(steps):
-        P.step_thickness(dt, grounded_melt_coupling=True)
+        if by_stage:
+            for stage in (1, 2, 3):
+                P.step_thickness_stage(dt, stage, grounded_melt_coupling=True)
+        else:
+            P.step_thickness(dt, grounded_melt_coupling=True)
     out = {k: P.get(k) for k in ("H", "s", "phi", "phi_u", "phi_v", "ice_mask", "N", "tau_u", "tau_v")}
     out["clipped_thickness"] = P.energy_get("clipped_thickness")
     P.close()
@@ -163,6 +167,46 @@ def test_gpu_matches_the_oracle(oracle_cls, gpu_cls, scheme):
     for k in want:
         scale = max(1.0, float(np.max(np.abs(want[k]))))
         np.testing.assert_allclose(got[k], want[k], rtol=1e-12, atol=1e-12 * scale, err_msg=f"{scheme} {k}")
+
+
+@pytest.mark.parametrize("scheme", ["upwind1", "weno5_bounded"])
+def test_the_three_stages_equal_the_step(backend, scheme):
+    """nk_step_thickness_stage 1, 2, 3 in order is nk_step_thickness, bit for bit."""
+    want = seeded_shelf(backend, steps=2, advection=SCHEMES[scheme])
+    got = seeded_shelf(backend, steps=2, advection=SCHEMES[scheme], by_stage=True)
+    for k in want:
+        assert np.array_equal(got[k], want[k]), (scheme, k)
+
+
+def test_stage_refuses_a_stage_outside_one_to_three(backend):
+    P = Transport(backend).P
+    for stage in (0, 4):
+        with pytest.raises(ValueError):
+            P.step_thickness_stage(1e6, stage)
+
+
+@pytest.mark.gpu
+def test_reference_schedule_velocity_after_every_stage(oracle_cls, gpu_cls):
+    """The reference's default IterationInterval(1) schedule: a velocity solve after every stage (update_state!), so
+    each stage advects with the previous stage's velocities; GPU against the oracle over two steps of a marine sheet."""
+    out = {}
+    for key, cls in (("o", oracle_cls), ("g", gpu_cls)):
+        solver = M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-12, maxiter=5000),
+                                       picard_iteration_control=M.Convergence(reltol=1e-11, maxiter=500),
+                                       preconditioner=M.StressBalanceMultigridPreconditioner(minimum_coarse_size=8))
+        P = workloads.marine_sheet(32, 16, seed=3, velocity_solver=solver).problem(cls)
+        P.set_thickness_advection(M.UpwindBiased(order=1))
+        P.energy_set("surface_mass_balance", 1e-9)
+        P.energy_set("basal_melt_rate", 2e-9)
+        P.energy_set("clipped_thickness", 0.0)
+        assert P.picard_solve().status == 0
+        for _ in range(2):
+            for stage in (1, 2, 3):
+                P.step_thickness_stage(3e8, stage)
+                assert P.picard_solve().status == 0
+        out[key] = (P.get("H"), P.get("u"), P.get("v"))
+    for a, b, name in zip(out["g"], out["o"], ("H", "u", "v")):
+        np.testing.assert_allclose(a, b, rtol=1e-8, atol=1e-8 * float(np.max(np.abs(b))), err_msg=name)
 
 
 # ---- the reference's higher-order schemes (test/test_thickness.jl:29-73) ------------------------------------------
