@@ -715,6 +715,7 @@ def timestep_kernels(nk, workloads, ctx, peak):
     out = {}
     for name, kernel, adv in (("thickness_stage_upwind1", "thickness_stage", M.UpwindBiased(order=1)),
                               ("thickness_stage_weno5_bounded", "thickness_stage", M.default_thickness_advection()),
+                              ("thickness_faces_weno5", "thickness_faces", M.default_thickness_advection()),
                               ("thickness_limiter", "thickness_limiter", M.default_thickness_advection()),
                               ("step_enthalpy", "step_enthalpy", None)):
         if adv is not None:

@@ -645,10 +645,12 @@ nk_status nk_server_info(const nk_server* server, int32_t* resident, int64_t* de
                                          multigrid precision (FP32 when mixed, FP64 otherwise) */
 #define NK_KERNEL_CG_UPDATE       2   /* x += alpha p, r -= alpha q with the fused r.r (and r.z) reductions */
 #define NK_KERNEL_THICKNESS_STAGE 3   /* one Runge-Kutta stage of nk_step_thickness with the problem's advection scheme
-                                         (the bounded WENO's limiter launched once before the timed launches) */
+                                         (the WENO face reconstructions and the bounded WENO's limiter launched once
+                                         before the timed launches) */
 #define NK_KERNEL_THICKNESS_LIMITER 4 /* the bounded WENO's limiter from the current thickness */
 #define NK_KERNEL_STEP_ENTHALPY   5   /* the column energy step of nk_step_enthalpy with EnthalpyThermodynamics' defaults
                                          (needs the sigma rate-factor layout) */
+#define NK_KERNEL_THICKNESS_FACES 6   /* the WENO schemes' two reconstructions of every face, once per stage */
 
 /* Instrumentation (no counterpart in the reference, which times whole solves with @elapsed,
  * benchmarks/multigrid_scaling.jl:36-47): launches one hot kernel `repeats` times on the problem's

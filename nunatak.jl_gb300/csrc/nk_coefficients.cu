@@ -496,20 +496,46 @@ __device__ __forceinline__ double face_value(const ThicknessView& v, const doubl
 // direction: from cell (i, j)'s own WENO face values W, E, S, N and the interior quadrature values
 // p̃ = (H̄ - ω (W + E)) / (1 - 2ω), ω = 5/18 (likewise in y), θ = min(1, |(upper - H̄) / (M - H̄ + ε)|,
 // |(lower - H̄) / (m - H̄ - ε)|) with M, m the largest and smallest of the six and ε = 2 eps.
+// The two WENO reconstructions of every face, once: x faces (i, j) for i in 0..Nx, j < Ny and y faces for i < Nx,
+// j in 0..Ny (on a periodic axis the last face repeats the first, from the same wrapped stencils).
+__global__ void k_thickness_faces(ThicknessView v) {
+    const DevGrid<double>& g = v.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i > g.Nx || j > g.Ny) return;
+    const double* __restrict__ Hs = v.Hs;
+    double s[5];
+    int k = g.idx(i, j);
+    if (j < g.Ny) {
+        double2 r;
+        stencil_x(g, Hs, i, j, true, s);
+        r.x = weno5_face(s);
+        stencil_x(g, Hs, i, j, false, s);
+        r.y = weno5_face(s);
+        v.fx[k] = r;
+    }
+    if (i < g.Nx) {
+        double2 r;
+        stencil_y(g, Hs, i, j, true, s);
+        r.x = weno5_face(s);
+        stencil_y(g, Hs, i, j, false, s);
+        r.y = weno5_face(s);
+        v.fy[k] = r;
+    }
+}
+void launch_thickness_faces(const ThicknessView& v, cudaStream_t s) {
+    LaunchDims d = dims2d(v.g.Nx + 1, v.g.Ny + 1);
+    k_thickness_faces<<<d.grid, d.block, 0, s>>>(v); count_launch();
+}
+
 __global__ void k_thickness_limiter(ThicknessView v) {
     const DevGrid<double>& g = v.g;
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i >= g.Nx || j >= g.Ny) return;
     const double* __restrict__ Hs = v.Hs;
-    double s[5], Hc = Hs[g.idx(i, j)];
-    stencil_x(g, Hs, i + 1, j, true, s);
-    double E = weno5_face(s);
-    stencil_x(g, Hs, i, j, false, s);
-    double W = weno5_face(s);
-    stencil_y(g, Hs, i, j + 1, true, s);
-    double N = weno5_face(s);
-    stencil_y(g, Hs, i, j, false, s);
-    double S = weno5_face(s);
+    double Hc = Hs[g.idx(i, j)];
+    // the cell's own reconstructions at its four faces (k_thickness_faces)
+    double E = v.fx[g.idx(i + 1, j)].x, W = v.fx[g.idx(i, j)].y;
+    double N = v.fy[g.idx(i, j + 1)].x, S = v.fy[g.idx(i, j)].y;
     const double w = 5.0 / 18, eps = 2 * 2.220446049250313e-16;
     double px = (Hc - w * W - w * E) / (1 - 2 * w);
     double py = (Hc - w * S - w * N) / (1 - 2 * w);
@@ -545,8 +571,15 @@ __global__ void k_thickness_stage(ThicknessView v, double dtau, int final_stage)
         bool west = full(kw), eastc = full(ke);
         if (!(west && eastc)) return (west || eastc) ? g.dyc[j] * (west ? fmax(u, 0.0) * Hs[kw] : fmin(u, 0.0) * Hs[ke]) : 0.0;
         bool east = u > 0;
-        stencil_x(g, Hs, f, j, east, s);
-        double h = limited(face_value(v, s), east ? kw : ke);
+        double h0;
+        if (v.fx) {
+            double2 r = v.fx[g.idx(f, j)];
+            h0 = east ? r.x : r.y;
+        } else {
+            stencil_x(g, Hs, f, j, east, s);
+            h0 = face_value(v, s);
+        }
+        double h = limited(h0, east ? kw : ke);
         return g.dyc[j] * (u * h);
     };
     auto yflux = [&](int f) {
@@ -556,8 +589,15 @@ __global__ void k_thickness_stage(ThicknessView v, double dtau, int final_stage)
         bool south = full(ks), northc = full(kn);
         if (!(south && northc)) return (south || northc) ? g.dxc[i] * (south ? fmax(w, 0.0) * Hs[ks] : fmin(w, 0.0) * Hs[kn]) : 0.0;
         bool north = w > 0;
-        stencil_y(g, Hs, i, f, north, s);
-        double h = limited(face_value(v, s), north ? ks : kn);
+        double h0;
+        if (v.fy) {
+            double2 r = v.fy[g.idx(i, f)];
+            h0 = north ? r.x : r.y;
+        } else {
+            stencil_y(g, Hs, i, f, north, s);
+            h0 = face_value(v, s);
+        }
+        double h = limited(h0, north ? ks : kn);
         return g.dxc[i] * (w * h);
     };
     int c = g.idx(i, j);

@@ -216,6 +216,11 @@ struct ThicknessView {
     double lower, upper;
     double* theta;                    // the bounds-preserving limiter per cell (bounded WENO only)
     const double* mu = nullptr;       // a partial-cell front's flag of full cells (null without a front)
+    // WENO: each face's two reconstructions of the stage thickness, computed once by k_thickness_faces for the
+    // limiter and the stage (x face (i, j): from cell i-1 (flow east), from cell i (flow west); y face likewise
+    // from the south and from the north cell); null for the upwind schemes, which read the stencil directly
+    double2* fx = nullptr;
+    double2* fy = nullptr;
 };
 
 // ---- the partial-cell front and calving (nk_front.cu) ------------------------------------------------------------
@@ -233,6 +238,7 @@ struct FrontView {
 void launch_initialize_front(const FrontView& v, cudaStream_t s);
 // advance_front!: the whole sequence of its kernels (with the snapshot copies of the passes) on stream s
 void launch_advance_front(const FrontView& v, int passes, double dt, size_t plane, cudaStream_t s);
+void launch_thickness_faces(const ThicknessView& v, cudaStream_t s);
 void launch_thickness_limiter(const ThicknessView& v, cudaStream_t s);
 void launch_thickness_stage(const ThicknessView& v, double dtau, int final_stage, cudaStream_t s);
 

@@ -1154,7 +1154,7 @@ static void ensure_energy(nk_problem* P) {
 // The thickness step's planes (zero at first): the four fields of NK_FIELD_SURFACE_MASS_BALANCE ..
 // NK_FIELD_CLIPPED_THICKNESS, then the thickness at the start of the step and of the stage, and the bounds-preserving
 // limiter of each cell.  No graph reads them.
-static const int TRANSPORT_PLANES = 7;
+static const int TRANSPORT_PLANES = 11;   // 7 fields, then the WENO face reconstructions (two double2 planes)
 static void ensure_transport(nk_problem* P) {
     if (P->transport) return;
     if (P->async_pending) bad("an asynchronous solve is pending (nk_problem_wait first)");
@@ -1609,6 +1609,10 @@ static ThicknessView thickness_view(nk_problem* P, bool coupled) {
     v.lower = adv.lower; v.upper = adv.upper;
     v.theta = P->transport + 6 * P->plane;
     v.mu = P->front.enabled ? P->mu : nullptr;
+    if (adv.scheme == NK_ADVECTION_WENO) {
+        v.fx = reinterpret_cast<double2*>(P->transport + 7 * P->plane);
+        v.fy = reinterpret_cast<double2*>(P->transport + 9 * P->plane);
+    }
     return v;
 }
 
@@ -1694,6 +1698,7 @@ static void thickness_stage(nk_problem* P, double dt, int st, int coupling) {
     if (st == 0) NK_CUDA(cudaMemcpyAsync((double*)v.H0, P->H, P->plane * sizeof(double), cudaMemcpyDeviceToDevice, P->stream));
     const double stages[3] = {1.0 / 3, 1.0 / 2, 1.0};     // SplitRungeKutta3 (Wicker-Skamarock) fractions
     NK_CUDA(cudaMemcpyAsync((double*)v.Hs, P->H, P->plane * sizeof(double), cudaMemcpyDeviceToDevice, P->stream));
+    if (v.fx) launch_thickness_faces(v, P->stream);
     if (bounded) launch_thickness_limiter(v, P->stream);
     launch_thickness_stage(v, stages[st] * dt, st == 2, P->stream);
     if (st == 2 && P->front.enabled)   // rk_substep!: advance_front! after the final stage (time_stepping.jl:23)
@@ -2228,6 +2233,8 @@ nk_status nk_time_kernel(nk_problem* P, int32_t kernel, int32_t repeats, int64_t
                 launch_thickness_stage(tv, 1.0, 0, s);
             } else if (kernel == NK_KERNEL_THICKNESS_LIMITER) {
                 launch_thickness_limiter(tv, s);
+            } else if (kernel == NK_KERNEL_THICKNESS_FACES) {
+                launch_thickness_faces(tv, s);
             } else if (kernel == NK_KERNEL_STEP_ENTHALPY) {
                 launch_step_enthalpy(ev, 1.0, s);
             } else {
@@ -2235,19 +2242,25 @@ nk_status nk_time_kernel(nk_problem* P, int32_t kernel, int32_t repeats, int64_t
             }
         };
         const bool bounded = P->advection.scheme == NK_ADVECTION_WENO && P->advection.bounded;
+        const bool weno = P->advection.scheme == NK_ADVECTION_WENO;
         if (kernel == NK_KERNEL_OPERATOR_FP64) bytes = cells * (16 + 32 + 1 + 16);
         else if (kernel == NK_KERNEL_SMOOTHER) bytes = cells * (P->mixed ? (8 + 8 + 8 + 16 + 1 + 8) : (16 + 16 + 16 + 32 + 1 + 16));
         else if (kernel == NK_KERNEL_CG_UPDATE) bytes = cells * (64 + 32 + (P->precond == NK_PRECONDITIONER_DIAGONAL ? 16 + 16 : 0));
         // Hs, H⁻, a, m, (u, v), H written; φ with a grounding treatment; θ for a bounded WENO
-        else if (kernel == NK_KERNEL_THICKNESS_STAGE) bytes = cells * (8 + 8 + 8 + 8 + 16 + 8 + (P->pd.grounding ? 8 : 0) + (bounded ? 8 : 0));
-        else if (kernel == NK_KERNEL_THICKNESS_LIMITER) bytes = cells * (8 + 8);
+        // (a WENO stage reads the face reconstructions, one pair per x and per y face of the cell, instead of the stencils)
+        else if (kernel == NK_KERNEL_THICKNESS_STAGE)
+            bytes = cells * (8 + 8 + 8 + 8 + 16 + 8 + (P->pd.grounding ? 8 : 0) + (bounded ? 8 : 0) + (weno ? 32 : 0));
+        else if (kernel == NK_KERNEL_THICKNESS_LIMITER) bytes = cells * (8 + 8 + 32);
+        else if (kernel == NK_KERNEL_THICKNESS_FACES) bytes = cells * (8 + 32);
         // per column: H, Hⁿ, φ, m, mᵍ, G, Tₛ, Tₒ, H_w, (u, v), (uᵇ, vᵇ) and the drag; per layer E_old, η, (uσ, vσ) read and E,
         // T, ω, Φ written
         else if (kernel == NK_KERNEL_STEP_ENTHALPY) bytes = cells * 8 * (11 + 8.0 * P->Ns);
-        if (kernel == NK_KERNEL_THICKNESS_STAGE || kernel == NK_KERNEL_THICKNESS_LIMITER) {
+        if (kernel == NK_KERNEL_THICKNESS_STAGE || kernel == NK_KERNEL_THICKNESS_LIMITER || kernel == NK_KERNEL_THICKNESS_FACES) {
             tv = thickness_view(P, false);
+            if (kernel == NK_KERNEL_THICKNESS_FACES && !tv.fx) bad("the face reconstructions belong to the WENO schemes");
             NK_CUDA(cudaMemcpyAsync((double*)tv.Hs, P->H, P->plane * sizeof(double), cudaMemcpyDeviceToDevice, s));
             NK_CUDA(cudaMemcpyAsync((double*)tv.H0, P->H, P->plane * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            if (tv.fx) launch_thickness_faces(tv, s);
             if (kernel == NK_KERNEL_THICKNESS_STAGE && !bounded) tv.bounded = 0;
             if (kernel == NK_KERNEL_THICKNESS_STAGE && bounded) launch_thickness_limiter(tv, s);
         } else if (kernel == NK_KERNEL_STEP_ENTHALPY) {

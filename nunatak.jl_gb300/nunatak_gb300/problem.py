@@ -378,7 +378,7 @@ class Problem:
 
     # -- measurement ---------------------------------------------------------------------------------------
     KERNELS = {"operator_fp64": 0, "smoother": 1, "cg_update": 2, "thickness_stage": 3, "thickness_limiter": 4,
-               "step_enthalpy": 5}
+               "step_enthalpy": 5, "thickness_faces": 6}
 
     def time_kernel(self, kernel, repeats=20, flush_bytes=0):
         """Mean CUDA-event duration (ms) of one launch of a hot kernel and its algorithmic bytes
