@@ -85,9 +85,10 @@ def parse():
     ap.add_argument("--no-scaling", action="store_true", help="skip the reference's published scaling benchmark rows")
     ap.add_argument("--rate", type=float, default=ARRIVAL_RATE,
                     help="Poisson arrival rate of the e2e leg, requests/s (the workload's is 200)")
-    ap.add_argument("--profile", choices=["solve", "smoother", "operator"], default=None,
+    ap.add_argument("--profile", choices=["solve", "smoother", "operator", "enthalpy"], default=None,
                     help="profiling runs for ncu: 'solve' = warm-up solves then one timed solve of the workload; "
-                         "'smoother' / 'operator' = the roofline kernel on the 2048x1024 grid, 3 launches")
+                         "'smoother' / 'operator' = the roofline kernel on the 2048x1024 grid, 3 launches; "
+                         "'enthalpy' = the column energy step on the 1024x512 DIVA sheet (Nσ = 10), 3 launches")
     ap.add_argument("--adjoint", action="store_true",
                     help="the adjoint workload instead: gradient of a velocity misfit with respect to log C on the "
                          "512x256 marine sheet by the fixed-point Picard adjoint, checked against centred differences")
@@ -337,6 +338,18 @@ def profile(args, nk, workloads, ctx):
             st = P.picard_solve()
         print(json.dumps({"profile": "solve", "picard_iterations": st.picard_iterations, "cg_iterations": st.linear_iterations_total,
                           "device_ms": st.device_ms}))
+    elif args.profile == "enthalpy":
+        from nunatak_gb300 import model as M
+        solver = M.StressBalanceSolver(linear_iteration_control=M.FixedIterations(5), picard_iteration_control=M.FixedIterations(2),
+                                       preconditioner=M.StressBalanceMultigridPreconditioner(minimum_coarse_size=32), precision="mixed")
+        case = workloads.diva_sheet(1024, 512, dx=2e3, velocity_solver=solver)
+        P = case.problem(nk.Problem, context=ctx)
+        P.picard_solve()
+        P.velocity_profile()
+        P.set("E", 2009.0 * (case.temperature - 223.15))
+        ms, by = P.time_kernel("step_enthalpy", repeats=3, flush_bytes=512 << 20)
+        P.close()
+        print(json.dumps({"profile": "enthalpy", "ms_per_launch": ms, "bytes_per_launch": by}))
     else:
         Pb = roofline_problem(nk, workloads, ctx)
         kernel = "smoother" if args.profile == "smoother" else "operator_fp64"
