@@ -646,16 +646,21 @@ __global__ void __launch_bounds__(128) k_step_enthalpy(EnergyView v, double dt) 
     const long long P = v.plane;
     const int c = g.idx(i, j);
     const double rho = v.rho_i, ga = v.gacc, H = v.H[c], Hn = v.Hn[c];
+    // The kernel is bound by the FP64 pipe, where a division costs about ten multiply-adds: divisors that stay fixed
+    // through the column are inverted once and each layer's diffusivity is evaluated once (the results differ from
+    // the quotients of the formulas in the last bits only).
+    const double r_L = 1 / q.L, r_c = 1 / q.c, r_blend = 1 / q.blend, r_dt = 1 / dt, k_c = q.k / q.c;
+    auto ramp = [](double x, double rw) { return dmin(dmax(x * rw, 0.0), 1.0); };   // unit_ramp with 1/w
     auto Tpm = [&](double p) { return q.T0 - q.beta * p; };
     auto Epm = [&](double p) { return q.c * (Tpm(p) - q.Tr); };
     auto enthalpy = [&](double T, double p) { return q.c * (dmin(T, Tpm(p)) - q.Tr) + 0.0 * q.L; };
-    auto water_fraction = [&](double E, double p) { return dmax(0.0, E - Epm(p)) / q.L; };
+    auto water_fraction = [&](double E, double p) { return dmax(0.0, E - Epm(p)) * r_L; };
     auto thickness = [&](double h) { return dmax(h, q.min_thickness); };
     auto layer_pressure = [&](int k) { return rho * ga * H * (1 - sg.zc[k - 1]); };
     auto Eold = [&](int k, int ii, int jj) { return v.E_old[(k - 1) * P + g.c_idx(ii, jj)]; };
     auto diffusivity = [&](int k) {
-        double w = unit_ramp(Eold(k, i, j) - Epm(layer_pressure(k)) + q.blend, q.blend);
-        return q.k / q.c * (1 - w + w * q.temperate_ratio);
+        double w = ramp(Eold(k, i, j) - Epm(layer_pressure(k)) + q.blend, r_blend);
+        return k_c * (1 - w + w * q.temperate_ratio);
     };
     const double phi_g = v.grounding ? v.phi[c] : 1.0;
 
@@ -671,7 +676,7 @@ __global__ void __launch_bounds__(128) k_step_enthalpy(EnergyView v, double dt) 
     for (int k = 1; k <= Ns; ++k) {
         double eta = v.eta_sigma[(k - 1) * P + c];
         double ph = 4 * eta * e2;
-        if (v.diva) ph += tb2 * sg.w2[k - 1] / sg.dz[k - 1] / (eta == 0.0 ? INFINITY : eta);
+        if (v.diva) ph += tb2 * sg.w2[k - 1] / (sg.dz[k - 1] * (eta == 0.0 ? INFINITY : eta));
         v.Phi[(k - 1) * P + c] = ph;
     }
 
@@ -694,21 +699,22 @@ __global__ void __launch_bounds__(128) k_step_enthalpy(EnergyView v, double dt) 
         double w = v.usig[(k - 1) * P + g.v_idx(i, f)].y;
         return yvol(f, k) * (w > 0 ? Eold(k, i, f - 1) : Eold(k, i, f));
     };
-    const double Az = g.Az_cc(i, j);
+    const double Az = g.Az_cc(i, j), r_Az = 1 / Az;
     double W[ENERGY_MAX_LAYERS + 1];
     {
-        double dHdt = (thickness(H) - thickness(Hn)) / dt;
+        double dHdt = (thickness(H) - thickness(Hn)) * r_dt;
         double m = v.grounding ? (1 - v.phi[c]) * v.melt[c] : v.melt[c];
         W[0] = -m - (q.coupled ? v.gmelt[c] : 0.0);
         for (int k = 1; k <= Ns; ++k) {
-            double div = (xvol(i + 1, k) - xvol(i, k) + yvol(j + 1, k) - yvol(j, k)) / Az;
+            double div = (xvol(i + 1, k) - xvol(i, k) + yvol(j + 1, k) - yvol(j, k)) * r_Az;
             W[k] = W[k - 1] - sg.dz[k - 1] * (dHdt + div);
         }
     }
 
     // 3. basal state
     const double Ht = thickness(H), Hnt = thickness(Hn);
-    const double D = diffusivity(1) / (Ht * sg.zc[0]);
+    const double kap1 = diffusivity(1);
+    const double D = kap1 / (Ht * sg.zc[0]);
     double F;
     {
         int u0 = g.u_idx(i, j), u1 = g.u_idx(i + 1, j), v0 = g.v_idx(i, j), v1 = g.v_idx(i, j + 1);
@@ -720,8 +726,8 @@ __global__ void __launch_bounds__(128) k_step_enthalpy(EnergyView v, double dt) 
     const double pb = rho * ga * H;
     const double Epm_b = Epm(pb);
     const double Hw0 = v.Hw[c], G = v.G[c];
-    const double r = dmax(unit_ramp(Eold(1, i, j) + (G + F) / D - Epm_b, q.blend), unit_ramp(Hw0, q.water_blend));
-    const double sb = unit_ramp(Eold(1, i, j) - Epm(layer_pressure(1)) + q.blend, q.blend);
+    const double r = dmax(ramp(Eold(1, i, j) + (G + F) / D - Epm_b, r_blend), unit_ramp(Hw0, q.water_blend));
+    const double sb = ramp(Eold(1, i, j) - Epm(layer_pressure(1)) + q.blend, r_blend);
     const double qg = phi_g * G + F;
     v.sb[c] = sb;
     v.qg[c] = qg;
@@ -735,38 +741,45 @@ __global__ void __launch_bounds__(128) k_step_enthalpy(EnergyView v, double dt) 
     const double Lam = D * (chi + 1 - phi_g) + dmax(-Fb, 0.0);
     const double S = (1 - r) * qg + D * (chi * Epm_b + (1 - phi_g) * Eo) + dmax(Fb, 0.0) * Epm_b;
     const double Fs = rho * W[Ns];
-    const double Ks = diffusivity(Ns) / (Ht * (1 - sg.zc[Ns - 1]));
+    const double kapN = Ns == 1 ? kap1 : diffusivity(Ns);
+    const double Ks = kapN / (Ht * (1 - sg.zc[Ns - 1]));
     const double Ds = Ks + dmax(Fs, 0.0), Ss = (Ks + dmax(-Fs, 0.0)) * Es;
-    auto couplings = [&](int kf, double& lower, double& upper) {   // interior face kf = 2..Nσ
+    // interior face kf = 2..Nσ between layers of diffusivities km (below) and kp (above)
+    auto couplings = [&](int kf, double km, double kp, double& lower, double& upper) {
         double zf = sg.zf[kf - 1], zm = sg.zc[kf - 2], zp = sg.zc[kf - 1];
         double theta = (zf - zm) / (zp - zm);
         double Fk = rho * W[kf - 1];
-        double cond = 1 / (Ht * ((zf - zm) / diffusivity(kf - 1) + (zp - zf) / diffusivity(kf)));
+        double cond = km * kp / (Ht * ((zf - zm) * kp + (zp - zf) * km));   // 1 / (Ht ((zf - zm) / km + (zp - zf) / kp))
         double Dk = dmax(cond, dmax(dmax(Fk, 0.0) * theta, dmax(-Fk, 0.0) * (1 - theta)));
         lower = -Fk * (1 - theta) - Dk;
         upper = Fk * theta - Dk;
     };
     double t[ENERGY_MAX_LAYERS + 1], e[ENERGY_MAX_LAYERS + 1];
-    double lower_m = 0, upper_m = 0, prev_a = 0, prev_c = 0, piv = 1;
+    double lower_m = 0, upper_m = 0, prev_a = 0, prev_c = 0, rpiv = 1;
+    double kap_k = kap1;
     for (int k = 1; k <= Ns; ++k) {
         double dz = sg.dz[k - 1];
         double lower_p = 0, upper_p = 0;
-        if (k < Ns) couplings(k + 1, lower_p, upper_p);
+        if (k < Ns) {
+            double kap_n = k + 1 == Ns ? kapN : diffusivity(k + 1);
+            couplings(k + 1, kap_k, kap_n, lower_p, upper_p);
+            kap_k = kap_n;
+        }
         double diag_m = k == 1 ? Lam : -upper_m;
         double diag_p = k == Ns ? Ds : -lower_p;
         double forcing = (k == 1 ? S : 0.0) + (k == Ns ? Ss : 0.0);
-        double transport = rho * dz * ((xenth(i + 1, k) - xenth(i, k) + yenth(j + 1, k) - yenth(j, k)) / Az);
+        double transport = rho * dz * ((xenth(i + 1, k) - xenth(i, k) + yenth(j + 1, k) - yenth(j, k)) * r_Az);
         double ak = mu ? lower_p : 0.0;
         double ck = mu ? upper_p : 0.0;
-        double bk = mu ? rho * Ht * dz / dt + diag_m + diag_p : 1.0;
-        double fk = mu ? rho * Hnt * dz * Eold(k, i, j) / dt - transport + Ht * dz * v.Phi[(k - 1) * P + c] + forcing : Es;
+        double bk = mu ? rho * Ht * dz * r_dt + diag_m + diag_p : 1.0;
+        double fk = mu ? rho * Hnt * dz * Eold(k, i, j) * r_dt - transport + Ht * dz * v.Phi[(k - 1) * P + c] + forcing : Es;
         if (k == 1) {
-            piv = bk;
-            e[1] = fk / piv;
+            rpiv = 1 / bk;
+            e[1] = fk * rpiv;
         } else {
-            t[k] = prev_c / piv;
-            piv = bk - prev_a * t[k];
-            e[k] = (fk - prev_a * e[k - 1]) / piv;
+            t[k] = prev_c * rpiv;
+            rpiv = 1 / (bk - prev_a * t[k]);
+            e[k] = (fk - prev_a * e[k - 1]) * rpiv;
         }
         prev_a = ak; prev_c = ck;
         lower_m = lower_p; upper_m = upper_p;
@@ -778,10 +791,11 @@ __global__ void __launch_bounds__(128) k_step_enthalpy(EnergyView v, double dt) 
         double qb = D * (Epm_b - e[1]);
         double m = r * (qg - phi_g * (1 - sb) * qb) / (rho * q.L);
         double drained = 0;
+        const double r_drain = 1 / q.drainage_fraction;
         for (int k = 1; k <= Ns; ++k) {
             double w = water_fraction(e[k], layer_pressure(k));
-            double x = w / q.drainage_fraction;
-            double rate = q.max_drainage_rate * (dmin(dmax(x - 1, 0.0), 1.0) / 10 + 9 * dmin(dmax(x - 2, 0.0), 1.0) / 10);
+            double x = w * r_drain;
+            double rate = q.max_drainage_rate * (dmin(dmax(x - 1, 0.0), 1.0) + 9 * dmin(dmax(x - 2, 0.0), 1.0)) * 0.1;
             double dw = dmin(dt * rate, dmax(w - q.drainage_fraction, 0.0));
             dw = mu ? dw : 0.0;
             e[k] -= q.L * dw;
@@ -790,7 +804,7 @@ __global__ void __launch_bounds__(128) k_step_enthalpy(EnergyView v, double dt) 
         double Hstar = Hw0 + dt * (mu ? m : 0.0) + drained;
         double Hplus = dmax(0.0, Hstar);
         double missing = Hplus - Hstar;
-        v.gmelt[c] = (Hplus - Hw0) / dt;
+        v.gmelt[c] = (Hplus - Hw0) * r_dt;
         v.Hw[c] = Hplus;
         e[1] -= q.L * missing / (Ht * sg.dz[0]);
     }
@@ -799,7 +813,7 @@ __global__ void __launch_bounds__(128) k_step_enthalpy(EnergyView v, double dt) 
     for (int k = 1; k <= Ns; ++k) {
         double p = layer_pressure(k), E = e[k];
         v.E[(k - 1) * P + c] = E;
-        v.T[(k - 1) * P + c] = dmin(Tpm(p), q.Tr + E / q.c);
+        v.T[(k - 1) * P + c] = dmin(Tpm(p), q.Tr + E * r_c);
         v.omega[(k - 1) * P + c] = water_fraction(E, p);
     }
 }
