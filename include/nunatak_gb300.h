@@ -488,6 +488,73 @@ nk_status nk_picard_adjoint_gradients(nk_problem* problem, const double* ubar, c
                                       double* lambda_u, double* lambda_v, double* grad_log_C, double* grad_log_A, double* grad_H,
                                       nk_solve_stats* stats);
 
+/* ---- the gradient through time steps (checkpointed_gradient!, ext/NunatakEnzymeExt.jl:245-263) ------------------
+ * The cost J = Σₙ Jₙ of the states after steps n = 1..steps of time_step!: each step the three split Runge-Kutta
+ * stages of nk_step_thickness_stage with the problem's advection, each followed, with velocity_solves, by a Picard
+ * solve (the reference's IterationInterval(1) velocity schedule), else with the velocities held.  The host gives Jₙ
+ * and its gradient in a callback; the library returns J and its gradient with respect to the thickness and the
+ * velocities at the start, the surface mass balance, the basal melt rate, and, with velocity solves, log C and log A.
+ *
+ * The forward run stores the state (H, U, V, and for the DIVA its lagged beta_b and F2) every checkpoint_interval
+ * steps; the reverse pass restores each checkpoint, re-runs its segment storing every stage's state, and runs the
+ * segment backwards: the cost's gradient at each step end, the fixed-point Picard adjoint of each velocity solve
+ * (nk_picard_adjoint_gradients: λ of the velocities to ∂J/∂H, log C, log A) and the reverse of each stage (the clip,
+ * the sources, the fluxes, the bounds-preserving limiter, the WENO or upwind reconstructions and the centre grounded
+ * fraction of the floating melt; nk_time_adjoint.cu).  Only one segment's stages are held at a time.  The problem is
+ * left at the final state, as checkpointed_gradient! leaves the model.
+ *
+ * The initial velocities are an input, as the model's stored velocities are for the reference (their gradient is
+ * the shadow of the velocity fields); the geometry is recomputed from the initial H.  Discrete switches (the clip, the
+ * upwind direction, the limiter's branch, walls and masks) are held where the forward run put them.  Not covered:
+ * a partial-cell front (refused), the energy step and its grounded-melt coupling (the stages run uncoupled), and
+ * prescribed velocities with velocity solves (refused, as for nk_picard_adjoint). */
+typedef struct nk_cost_state {
+    int32_t step;              /* the state after this many steps, 1..steps */
+    int32_t steps;
+    const double* H;           /* Nx x Ny, interior layout (host) */
+    const double* u;           /* the interior layouts of U, V (host) */
+    const double* v;
+    const double* ice_mask;    /* Nx x Ny */
+} nk_cost_state;
+/* Jₙ into *J and ∂Jₙ/∂(H, U, V) into the arrays (zeroed before the call; the layouts of the state's arrays).
+ * Return 0; anything else stops the gradient with NK_BAD_ARGUMENT. */
+typedef int32_t (*nk_cost_fn)(void* user, const nk_cost_state* state, double* J, double* dJ_dH, double* dJ_du, double* dJ_dv);
+
+typedef struct nk_time_gradient_desc {
+    double dt;
+    int32_t steps;
+    int32_t checkpoint_interval;            /* steps per segment; 0: ceil(sqrt(steps)) */
+    int32_t velocity_solves;                /* 1: a Picard solve after every stage; 0: the velocities held */
+    int32_t reserved;
+    const double* melt_weights;             /* steps factors wₙ: step n melts wₙ m; NULL: all 1 */
+    const nk_iteration_control* adjoint_control;   /* the Picard adjoints' control; NULL: the problem's Picard control */
+} nk_time_gradient_desc;
+
+/* Outputs, each Nx x Ny in interior layout unless noted; any may be NULL. */
+typedef struct nk_time_gradient {
+    double* grad_H;            /* ∂J/∂H at the start (the initial velocities held) */
+    double* grad_u;            /* ∂J/∂(U, V) of the initial velocities (the interior layouts of U, V) */
+    double* grad_v;
+    double* grad_smb;          /* ∂J/∂a */
+    double* grad_melt;         /* ∂J/∂m of the base melt rate the weights scale */
+    double* grad_log_C;        /* ∂J/∂log C (velocity solves) */
+    double* grad_log_A;        /* ∂J/∂log A in the layout of RATE_FACTOR (velocity solves) */
+} nk_time_gradient;
+
+typedef struct nk_time_gradient_stats {
+    double J;                  /* Σₙ Jₙ */
+    int32_t segments;          /* checkpoints stored */
+    int32_t picard_solves;     /* forward and re-run */
+    int32_t picard_adjoints;
+    int32_t adjoint_iterations;     /* Picard adjoint iterations, all solves */
+    int32_t worst_solve_status;     /* the worst nk_status of the Picard solves and adjoints (NK_NOT_CONVERGED kept) */
+    int32_t reserved;
+    double elapsed_ms;         /* wall time of the call */
+} nk_time_gradient_stats;
+
+nk_status nk_checkpointed_gradient(nk_problem* problem, const nk_time_gradient_desc* desc, nk_cost_fn cost, void* user,
+                                   const nk_time_gradient* out, nk_time_gradient_stats* stats);
+
 /* picard_solve! enqueued on the problem's stream without waiting (one CUDA-graph launch); independent problems
  * solved this way run concurrently on the device.  nk_problem_wait blocks until it has finished and returns its
  * statistics (the status of the solve is the return value, as for nk_picard_solve). */

@@ -11,7 +11,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libnunatak_gb300.so")
-UNITS = ["nk_solver.cu", "nk_coefficients.cu", "nk_multigrid.cu", "nk_problem.cu", "nk_noalloc.cu", "nk_front.cu"]
+UNITS = ["nk_solver.cu", "nk_coefficients.cu", "nk_multigrid.cu", "nk_problem.cu", "nk_noalloc.cu", "nk_front.cu",
+         "nk_time_adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", "-Xptxas", "-v"] + ARCH
 

@@ -6,6 +6,7 @@
 #include <cmath>
 
 #include "nk_kernels.cuh"
+#include "nk_transport.cuh"
 
 namespace nk {
 
@@ -452,49 +453,6 @@ void launch_thermal_diagnostics(const DevGrid<double>& g, const SigmaTable& sig,
 }
 
 // ---- thickness transport -----------------------------------------------------------------------------------
-// The face thickness that u H carries through a face (UpwindBiased(order = 1 or 3) and WENO(order = 5) of the
-// reference's advection, restated from their published algorithms).  s[m + 2], m = -2..2, is the stage thickness m
-// cells from the upwind cell s[2] of the face, m > 0 towards and past the face.  A periodic stencil wraps as often as
-// the grid is short; a Bounded one takes the edge cell (the zero-gradient halo).
-__device__ __forceinline__ int wide_map(int i, int n, int periodic) {
-    if (periodic) { int r = i % n; return r < 0 ? r + n : r; }
-    return i < 0 ? 0 : (i > n - 1 ? n - 1 : i);
-}
-__device__ __forceinline__ void stencil_x(const DevGrid<double>& g, const double* __restrict__ H, int f, int j, bool east, double* s) {
-    int row = wide_map(j, g.Ny, g.py) * g.pitch;
-#pragma unroll
-    for (int m = -2; m <= 2; ++m) s[m + 2] = H[row + wide_map(east ? f - 1 + m : f - m, g.Nx, g.px)];
-}
-__device__ __forceinline__ void stencil_y(const DevGrid<double>& g, const double* __restrict__ H, int i, int f, bool north, double* s) {
-    int col = wide_map(i, g.Nx, g.px);
-#pragma unroll
-    for (int m = -2; m <= 2; ++m) s[m + 2] = H[wide_map(north ? f - 1 + m : f - m, g.Ny, g.py) * g.pitch + col];
-}
-// WENO-5: the three third-order candidates, their Jiang-Shu smoothness indicators and the WENO-Z weights
-// α_k = d_k (1 + τ / (β_k + ε)), τ = |β₀ - β₂|, ε = 1e-8, d = (1, 6, 3) / 10 (Jiang and Shu 1996; Borges et al. 2008,
-// exponent 1).
-__device__ __forceinline__ double weno5_face(const double* s) {
-    const double a = s[0], b = s[1], c = s[2], d = s[3], e = s[4];
-    const double sixth = 1.0 / 6;
-    double q0 = (2 * a - 7 * b + 11 * c) * sixth;
-    double q1 = (-b + 5 * c + 2 * d) * sixth;
-    double q2 = (2 * c + 5 * d - e) * sixth;
-    double b0 = 13.0 / 12 * (a - 2 * b + c) * (a - 2 * b + c) + 0.25 * (a - 4 * b + 3 * c) * (a - 4 * b + 3 * c);
-    double b1 = 13.0 / 12 * (b - 2 * c + d) * (b - 2 * c + d) + 0.25 * (b - d) * (b - d);
-    double b2 = 13.0 / 12 * (c - 2 * d + e) * (c - 2 * d + e) + 0.25 * (3 * c - 4 * d + e) * (3 * c - 4 * d + e);
-    const double eps = 1e-8;
-    double tau = fabs(b0 - b2);
-    // αₖ = dₖ (1 + τ / (βₖ + ε)) over the common denominator Π(βₖ + ε): one FP64 division per face instead of four
-    // (the weights' ratio is unchanged; the rounding differs from the separate quotients in the last bits)
-    double e0 = b0 + eps, e1 = b1 + eps, e2 = b2 + eps;
-    double a0 = 0.1 * (e0 + tau) * (e1 * e2), a1 = 0.6 * (e1 + tau) * (e0 * e2), a2 = 0.3 * (e2 + tau) * (e0 * e1);
-    return (a0 * q0 + a1 * q1 + a2 * q2) / (a0 + a1 + a2);
-}
-__device__ __forceinline__ double face_value(const ThicknessView& v, const double* s) {
-    if (v.scheme == NK_ADVECTION_WENO) return weno5_face(s);
-    return v.order == 3 ? (-s[1] + 5 * s[2] + 2 * s[3]) / 6 : s[2];
-}
-
 // update_bounds_preserving_limiter! (src/Models/time_stepping.jl:35-42) restated as the Zhang-Shu (2010) limiter per
 // direction: from cell (i, j)'s own WENO face values W, E, S, N and the interior quadrature values
 // p̃ = (H̄ - ω (W + E)) / (1 - 2ω), ω = 5/18 (likewise in y), θ = min(1, |(upper - H̄) / (M - H̄ + ε)|,

@@ -242,6 +242,36 @@ void launch_thickness_faces(const ThicknessView& v, cudaStream_t s);
 void launch_thickness_limiter(const ThicknessView& v, cudaStream_t s);
 void launch_thickness_stage(const ThicknessView& v, double dtau, int final_stage, cudaStream_t s);
 
+// ---- the reverse of a thickness stage (nk_time_adjoint.cu) ------------------------------------------------------
+// The forward view t at the stage (Hs, H0, the velocities, the effective melt, φ of Hs, and the faces and θ
+// recomputed from Hs), the stage's output thickness and its adjoint λ: adds the adjoints of H0, the velocities, the
+// surface mass balance and the base melt rate, and writes the adjoint of Hs (through the fluxes, the limiter, the
+// reconstructions and the centre grounded fraction of the melt).
+struct StageAdjointView {
+    ThicknessView t;
+    const double* Hout;               // the stage's output thickness (its clip: H★ > 0 where Hout > 0)
+    const double* bed;                // the flotation of φ: f = H + (ρw / ρi) b
+    double rw_ri;
+    double dtau, melt_weight;         // Δτ of the stage; the factor of the base melt rate in the step
+    const double* lam_out;            // λ of the output thickness
+    double* lam_H0;                   // += λ of the step-start thickness
+    double* lam_Hs;                   // = λ of the stage-start thickness
+    double2* lam_x;                   // += λ of (u, v) per face
+    double* lam_smb; double* lam_melt;   // += λ of the surface mass balance and of the base melt rate
+    // scratch planes
+    double* dv;                       // -Δτ λ★ / Az per cell (λ★ the adjoint of H★)
+    double* lam_phi;                  // λ of the centre grounded fraction per cell
+    double2* lamF;                    // λ of the flux through x face (i, j) (.x) and y face (i, j) (.y)
+    double2* lw_x; double2* lw_y;     // λ of a cell's own reconstructions (W, E) and (S, N) through its limiter θ
+};
+void launch_stage_adjoint(const StageAdjointView& a, cudaStream_t s);
+// y += x over the interior cells of `planes` planes (each `plane` doubles apart)
+void launch_add_planes(const DevGrid<double>& g, double* y, const double* x, int planes, size_t plane, cudaStream_t s);
+// y += x over the pair faces 0..Nx x 0..Ny
+void launch_add_pairs(const DevGrid<double>& g, double2* y, const double2* x, cudaStream_t s);
+// y = a x over the interior cells
+void launch_scale_plane(const DevGrid<double>& g, double* y, const double* x, double a, cudaStream_t s);
+
 // ---- the energy step -------------------------------------------------------------------------------------
 constexpr int ENERGY_MAX_LAYERS = 64;
 struct EnergyConstants {

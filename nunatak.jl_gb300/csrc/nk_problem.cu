@@ -1898,11 +1898,9 @@ nk_status nk_adjoint_solve(nk_problem* P, const double* bu, const double* bv, nk
 // DIVA's step also maps its lagged state s = (βᵇ, F₂, ησ) (the overwritten coefficients it reads, diva.jl:77-80);
 // the adjoint σ of s is swept along with λ (ext/NunatakEnzymeExt.jl:204-214): each iteration runs the step's reverse with q̄ = -λ and
 // the state adjoint σ, which yields r and the next σ.
-static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar, const nk_iteration_control& ctl, double* lu,
-                           double* lv, double* grad, double* grad_A, double* grad_H, nk_solve_stats* st) {
+static void ensure_adjoint(nk_problem* P, bool want_H) {
     const bool diva = P->pd.stress_balance == NK_DIVA;
     if (P->ud) bad("nk_picard_adjoint: not available for a problem with prescribed velocities");
-    cudaStream_t s = P->stream;
     size_t pl = P->plane;
     if (!P->adj_base) {
         NK_CUDA(cudaMalloc(&P->adj_base, pl * (sizeof(double2) + (2 + (size_t)P->Ns) * sizeof(double))));
@@ -1912,10 +1910,17 @@ static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar
         P->adj_grad_A = P->adj_grad + pl;
     }
     if (diva && !P->adj_diva) NK_CUDA(cudaMalloc(&P->adj_diva, pl * (8 * sizeof(double2) + (1 + (size_t)P->Ns) * sizeof(double))));
-    if (diva && grad_H && !P->adj_hmu) NK_CUDA(cudaMalloc((void**)&P->adj_hmu, pl * sizeof(double2)));
+    if (diva && want_H && !P->adj_hmu) NK_CUDA(cudaMalloc((void**)&P->adj_hmu, pl * sizeof(double2)));
+}
+
+// The adjoint with x̄ already in P->adj_xbar (ensure_adjoint first): leaves λ in tmp_a, ∂J/∂log C in adj_grad,
+// ∂J/∂log A in adj_grad_A (want_A) and ∂J/∂H in adj_g (want_H), and U, V = x* again.
+static void picard_adjoint_device(nk_problem* P, const nk_iteration_control& ctl, bool want_A, bool want_H, nk_solve_stats* st) {
+    const bool diva = P->pd.stress_balance == NK_DIVA;
+    cudaStream_t s = P->stream;
+    size_t pl = P->plane;
     NK_CUDA(cudaMemcpyAsync(P->xprev, P->x, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));   // x*
     update_coefficients(P);                                                                         // c(x*)
-    vector_in(P, P->adj_xbar, ubar, vbar);
     NK_CUDA(cudaMemsetAsync(P->adj_g, 0, pl * sizeof(double), s));
     NK_CUDA(cudaMemsetAsync(P->tmp_a, 0, pl * sizeof(double2), s));                                 // λ
     NK_CUDA(cudaMemsetAsync(P->x, 0, pl * sizeof(double2), s));                                     // CG iterate
@@ -1979,18 +1984,36 @@ static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar
         if (!std::isfinite(D) || cg_failed) break;
     }
     launch_adjoint_coefficients(v, s);
-    if (grad_A) v.grad_log_A = P->adj_grad_A;
+    if (want_A) v.grad_log_A = P->adj_grad_A;
     if (diva) {
-        if (grad_H) v.hmu = P->adj_hmu;
+        if (want_H) v.hmu = P->adj_hmu;
         launch_adjoint_diva(v, s);
         launch_adjoint_diva_gradient(v, s);
-        if (grad_H) launch_adjoint_thickness(v, problem_geometry_view(P), 1, P->adj_g, s);   // gbar is free after the last pass
+        if (want_H) launch_adjoint_thickness(v, problem_geometry_view(P), 1, P->adj_g, s);   // gbar is free after the last pass
     } else {
-        if (grad_A) launch_adjoint_viscosity(v, s);
+        if (want_A) launch_adjoint_viscosity(v, s);
         launch_adjoint_gradient(v, s);
-        if (grad_H) launch_adjoint_thickness(v, problem_geometry_view(P), 0, P->adj_g, s);
+        if (want_H) launch_adjoint_thickness(v, problem_geometry_view(P), 0, P->adj_g, s);
     }
     NK_CHECK_LAUNCH();
+    NK_CUDA(cudaMemcpyAsync(P->x, P->xprev, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));   // U, V = x*
+    std::memset(st, 0, sizeof(*st));
+    st->picard_iterations = it;
+    st->linear_iterations_total = cg_total;
+    st->linear_iterations_last = cg_last;
+    st->residual_norm = rnorm;
+    st->picard_change = D;
+    st->picard_norm = M;
+    st->status = NK_OK;
+    if (!std::isfinite(D) || cg_failed) st->status = NK_NONFINITE;
+    else if (!fixed && !(D <= std::max(ctl.reltol * M, ctl.abstol))) st->status = NK_NOT_CONVERGED;
+}
+
+static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar, const nk_iteration_control& ctl, double* lu,
+                           double* lv, double* grad, double* grad_A, double* grad_H, nk_solve_stats* st) {
+    ensure_adjoint(P, grad_H != nullptr);
+    vector_in(P, P->adj_xbar, ubar, vbar);
+    picard_adjoint_device(P, ctl, grad_A != nullptr, grad_H != nullptr, st);
     if (lu && lv) vector_out(P, P->tmp_a, lu, lv);
     if (grad) {
         FieldLoc f;
@@ -2014,18 +2037,7 @@ static void picard_adjoint(nk_problem* P, const double* ubar, const double* vbar
         f.planes = P->pd.rate_factor_layout == NK_RATE_FACTOR_SIGMA ? P->Ns : 1;
         copy_out(P, f, grad_A);
     }
-    NK_CUDA(cudaMemcpyAsync(P->x, P->xprev, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));   // U, V = x*
-    NK_CUDA(cudaStreamSynchronize(s));
-    std::memset(st, 0, sizeof(*st));
-    st->picard_iterations = it;
-    st->linear_iterations_total = cg_total;
-    st->linear_iterations_last = cg_last;
-    st->residual_norm = rnorm;
-    st->picard_change = D;
-    st->picard_norm = M;
-    st->status = NK_OK;
-    if (!std::isfinite(D) || cg_failed) st->status = NK_NONFINITE;
-    else if (!fixed && !(D <= std::max(ctl.reltol * M, ctl.abstol))) st->status = NK_NOT_CONVERGED;
+    NK_CUDA(cudaStreamSynchronize(P->stream));
 }
 
 nk_status nk_picard_adjoint_gradients(nk_problem* P, const double* ubar, const double* vbar, const nk_iteration_control* control,
@@ -2050,6 +2062,298 @@ nk_status nk_picard_adjoint_gradients(nk_problem* P, const double* ubar, const d
 nk_status nk_picard_adjoint(nk_problem* P, const double* ubar, const double* vbar, const nk_iteration_control* control,
                             double* lambda_u, double* lambda_v, double* grad_log_C, double* grad_log_A, nk_solve_stats* stats) {
     return nk_picard_adjoint_gradients(P, ubar, vbar, control, lambda_u, lambda_v, grad_log_C, grad_log_A, nullptr, stats);
+}
+
+}  // extern "C"
+
+namespace nk {
+// ---- the gradient through time steps (checkpointed_gradient!, ext/NunatakEnzymeExt.jl:245-263) ---------------------
+// A stored state: H, (U, V), and for the DIVA the lagged beta_b and F2 its next Picard step reads (diva.jl:77-80), so
+// that a restored state re-runs bit for bit and the adjoint of a solve linearises where the solve ended.
+static int time_state_planes(bool diva) { return diva ? 6 : 3; }
+static void save_time_state(nk_problem* P, double* rec, bool diva) {
+    const size_t pl = P->plane;
+    cudaStream_t s = P->stream;
+    NK_CUDA(cudaMemcpyAsync(rec, P->H, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    NK_CUDA(cudaMemcpyAsync(rec + pl, P->x, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    if (diva) {
+        NK_CUDA(cudaMemcpyAsync(rec + 3 * pl, P->bb, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        NK_CUDA(cudaMemcpyAsync(rec + 5 * pl, P->F2, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    }
+}
+static void load_time_state(nk_problem* P, const double* rec, bool diva) {
+    const size_t pl = P->plane;
+    cudaStream_t s = P->stream;
+    NK_CUDA(cudaMemcpyAsync(P->H, rec, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    NK_CUDA(cudaMemcpyAsync(P->x, rec + pl, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    if (diva) {
+        NK_CUDA(cudaMemcpyAsync(P->bb, rec + 3 * pl, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        NK_CUDA(cudaMemcpyAsync(P->F2, rec + 5 * pl, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    }
+    launch_problem_geometry(P);
+    NK_CHECK_LAUNCH();
+}
+
+struct TimeGradient {
+    nk_problem* P;
+    nk_time_gradient_desc d;
+    nk_iteration_control ctl;
+    nk_cost_fn cost;
+    void* user;
+    nk_time_gradient_stats* st;
+    bool solves, diva;
+    int N, K, S, rp, a_planes;
+    size_t pl;
+    double* mem = nullptr;
+    // scratch planes
+    double *lamH, *lamHs, *lamH0, *dv, *lamphi, *g_smb, *g_melt, *base_melt, *clipped_end, *g_logC, *g_logA;
+    double2 *lamF, *lwx, *lwy, *lamx_stage, *lamx_carry, *lamu_held;
+    std::vector<double> hH, hu, hv, hmask, gH, gu, gv;
+
+    ~TimeGradient() {
+        if (mem) cudaFree(mem);
+    }
+    double* ckpt(int s) const { return mem + (size_t)s * rp * pl; }
+    double* tape(int t) const { return mem + (size_t)(S + t) * rp * pl; }
+    double* final_rec() const { return mem + (size_t)(S + 3 * K + 1) * rp * pl; }
+    double weight(int n) const { return d.melt_weights ? d.melt_weights[n] : 1.0; }
+    double* melt() const { return P->transport + P->plane; }
+
+    void worst(int status) {
+        if (status > st->worst_solve_status) st->worst_solve_status = status;
+    }
+    void allocate() {
+        const int scratch = 22 + a_planes;
+        size_t planes = (size_t)(S + 3 * K + 2) * rp + scratch;
+        NK_CUDA(cudaMalloc(&mem, planes * pl * sizeof(double)));
+        double* b = mem + (size_t)(S + 3 * K + 2) * rp * pl;
+        auto one = [&](int k) { return b + (size_t)k * pl; };
+        auto two = [&](int k) { return reinterpret_cast<double2*>(b + (size_t)k * pl); };
+        lamH = one(0); lamHs = one(1); lamH0 = one(2); dv = one(3); lamphi = one(4); g_smb = one(5); g_melt = one(6);
+        base_melt = one(7); clipped_end = one(8); g_logC = one(9);
+        lamF = two(10); lwx = two(12); lwy = two(14); lamx_stage = two(16); lamx_carry = two(18); lamu_held = two(20);
+        g_logA = one(22);
+    }
+    void solve() {
+        nk_solve_stats ss{};
+        picard_solve(P, &ss);
+        ++st->picard_solves;
+        worst(ss.status);
+        if (ss.status == NK_NONFINITE) throw Failure{NK_NONFINITE, "non-finite Picard solve in the time steps"};
+    }
+    // step n (0-based) from the problem's state; record: the state before each stage into tape(3k + stage)
+    void step(int n, bool record, int k) {
+        launch_scale_plane(P->fine.g, melt(), base_melt, weight(n), P->stream);
+        for (int stg = 0; stg < 3; ++stg) {
+            if (record) save_time_state(P, tape(3 * k + stg), diva);
+            thickness_stage(P, d.dt, stg, 0);
+            if (solves) solve();
+        }
+    }
+    // the Picard adjoint of the solve that ended in the loaded state, for x̄ = xbar: λ_H += ∂J/∂H, log C, log A
+    void solve_adjoint(const double2* xbar, double* lam_H) {
+        NK_CUDA(cudaMemcpyAsync(P->adj_xbar, xbar, pl * sizeof(double2), cudaMemcpyDeviceToDevice, P->stream));
+        nk_solve_stats ss{};
+        picard_adjoint_device(P, ctl, true, true, &ss);
+        ++st->picard_adjoints;
+        st->adjoint_iterations += ss.picard_iterations;
+        worst(ss.status);
+        if (ss.status == NK_NONFINITE) throw Failure{NK_NONFINITE, "non-finite Picard adjoint in the time steps"};
+        const DevGrid<double>& g = P->fine.g;
+        launch_add_planes(g, lam_H, P->adj_g, 1, pl, P->stream);
+        launch_add_planes(g, g_logC, P->adj_grad, 1, pl, P->stream);
+        launch_add_planes(g, g_logA, P->adj_grad_A, a_planes, pl, P->stream);
+        NK_CHECK_LAUNCH();
+    }
+    // the host's cost after `step` steps on the loaded state: J, and its gradient into lamH and the velocity adjoint
+    void cost_at(int step) {
+        FieldLoc fH = field_loc(P, NK_FIELD_H), fu = field_loc(P, NK_FIELD_U), fv = field_loc(P, NK_FIELD_V);
+        FieldLoc fm = field_loc(P, NK_FIELD_ICE_MASK);
+        copy_out(P, fH, hH.data());
+        copy_out(P, fu, hu.data());
+        copy_out(P, fv, hv.data());
+        copy_out(P, fm, hmask.data());
+        std::fill(gH.begin(), gH.end(), 0.0);
+        std::fill(gu.begin(), gu.end(), 0.0);
+        std::fill(gv.begin(), gv.end(), 0.0);
+        nk_cost_state cs{step, N, hH.data(), hu.data(), hv.data(), hmask.data()};
+        double J = 0.0;
+        if (cost(user, &cs, &J, gH.data(), gu.data(), gv.data()) != 0) bad("the cost callback failed at step " + std::to_string(step));
+        st->J += J;
+        FieldLoc t = fH;
+        t.base = lamHs;   // free until the stage reverse writes it
+        copy_in(P, t, gH.data());
+        launch_add_planes(P->fine.g, lamH, lamHs, 1, pl, P->stream);
+        vector_in(P, lamx_stage, gu.data(), gv.data());
+        launch_add_pairs(P->fine.g, solves ? lamx_carry : lamu_held, lamx_stage, P->stream);
+        NK_CHECK_LAUNCH();
+    }
+    // the reverse of stage stg of step n (local k) from the loaded state tape(3k + stg): λ of its output in lamH,
+    // λ of its input into lamHs (and the step start into lamH0), the velocity adjoint into lamx_stage
+    void stage_reverse(int n, int k, int stg) {
+        static const double fractions[3] = {1.0 / 3, 1.0 / 2, 1.0};
+        cudaStream_t s = P->stream;
+        launch_scale_plane(P->fine.g, melt(), base_melt, weight(n), s);
+        ThicknessView tv = thickness_view(P, false);
+        NK_CUDA(cudaMemcpyAsync((double*)tv.Hs, P->H, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        NK_CUDA(cudaMemcpyAsync((double*)tv.H0, tape(3 * k), pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        if (tv.fx) launch_thickness_faces(tv, s);
+        if (P->advection.scheme == NK_ADVECTION_WENO && P->advection.bounded) launch_thickness_limiter(tv, s);
+        NK_CUDA(cudaMemsetAsync(lamx_stage, 0, pl * sizeof(double2), s));
+        StageAdjointView a;
+        a.t = tv;
+        a.Hout = tape(3 * k + stg + 1);
+        a.bed = P->bed;
+        a.rw_ri = P->pd.ocean_density / P->pd.ice_density;
+        a.dtau = fractions[stg] * d.dt;
+        a.melt_weight = weight(n);
+        a.lam_out = lamH;
+        a.lam_H0 = lamH0;
+        a.lam_Hs = lamHs;
+        a.lam_x = lamx_stage;
+        a.lam_smb = g_smb;
+        a.lam_melt = g_melt;
+        a.dv = dv;
+        a.lam_phi = lamphi;
+        a.lamF = lamF;
+        a.lw_x = lwx;
+        a.lw_y = lwy;
+        launch_stage_adjoint(a, s);
+        NK_CHECK_LAUNCH();
+    }
+
+    void run(nk_time_gradient_stats* stats) {
+        st = stats;
+        cudaStream_t s = P->stream;
+        const DevGrid<double>& g = P->fine.g;
+        ensure_transport(P);
+        if (solves) ensure_adjoint(P, true);
+        allocate();
+        // ---- forward: the checkpoints ----
+        launch_problem_geometry(P);
+        NK_CUDA(cudaMemcpyAsync(base_melt, melt(), pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        for (int sg = 0; sg < S; ++sg) {
+            save_time_state(P, ckpt(sg), diva);
+            for (int k = 0; k < std::min(K, N - sg * K); ++k) step(sg * K + k, false, k);
+        }
+        save_time_state(P, final_rec(), diva);
+        NK_CUDA(cudaMemcpyAsync(clipped_end, P->transport + 3 * pl, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        // ---- reverse, one segment at a time ----
+        for (double* z : {lamH, g_smb, g_melt, g_logC}) NK_CUDA(cudaMemsetAsync(z, 0, pl * sizeof(double), s));
+        NK_CUDA(cudaMemsetAsync(g_logA, 0, (size_t)a_planes * pl * sizeof(double), s));
+        for (double2* z : {lamx_carry, lamu_held, lamF, lwx, lwy}) NK_CUDA(cudaMemsetAsync(z, 0, pl * sizeof(double2), s));
+        double* lam = lamH;      // λ of the current thickness (the buffers swap roles as the sweep moves back)
+        double* lam_in = lamHs;
+        for (int sg = S - 1; sg >= 0; --sg) {
+            const int n0 = sg * K, len = std::min(K, N - n0);
+            load_time_state(P, ckpt(sg), diva);
+            for (int k = 0; k < len; ++k) step(n0 + k, true, k);
+            save_time_state(P, tape(3 * len), diva);
+            for (int k = len - 1; k >= 0; --k) {
+                const int n = n0 + k;
+                load_time_state(P, tape(3 * k + 3), diva);
+                lamH = lam;
+                lamHs = lam_in;
+                cost_at(n + 1);
+                if (solves) {
+                    solve_adjoint(lamx_carry, lam);
+                    NK_CUDA(cudaMemsetAsync(lamx_carry, 0, pl * sizeof(double2), s));
+                }
+                NK_CUDA(cudaMemsetAsync(lamH0, 0, pl * sizeof(double), s));
+                for (int stg = 2; stg >= 0; --stg) {
+                    load_time_state(P, tape(3 * k + stg), diva);
+                    lamH = lam;
+                    lamHs = lam_in;
+                    stage_reverse(n, k, stg);
+                    if (stg > 0) {
+                        if (solves) solve_adjoint(lamx_stage, lam_in);   // the solve that made x_t from H_t
+                        else launch_add_pairs(g, lamu_held, lamx_stage, s);
+                    } else {
+                        launch_add_planes(g, lam_in, lamH0, 1, pl, s);  // stage 1 reads H⁻ as its stage thickness
+                        if (solves) NK_CUDA(cudaMemcpyAsync(lamx_carry, lamx_stage, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+                        else launch_add_pairs(g, lamu_held, lamx_stage, s);
+                    }
+                    NK_CHECK_LAUNCH();
+                    std::swap(lam, lam_in);
+                }
+            }
+        }
+        lamH = lam;
+        lamHs = lam_in;
+        // ---- back to the final state ----
+        load_time_state(P, final_rec(), diva);
+        NK_CUDA(cudaMemcpyAsync(P->transport + 3 * pl, clipped_end, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        NK_CUDA(cudaMemcpyAsync(melt(), base_melt, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        NK_CUDA(cudaStreamSynchronize(s));
+    }
+    void copy_results(const nk_time_gradient* out) {
+        FieldLoc f = field_loc(P, NK_FIELD_H);
+        auto plane_out = [&](double* host, double* dev, int planes) {
+            if (!host) return;
+            FieldLoc t = f;
+            t.base = dev;
+            t.planes = planes;
+            copy_out(P, t, host);
+        };
+        plane_out(out->grad_H, lamH, 1);
+        plane_out(out->grad_smb, g_smb, 1);
+        plane_out(out->grad_melt, g_melt, 1);
+        plane_out(out->grad_log_C, g_logC, 1);
+        plane_out(out->grad_log_A, g_logA, a_planes);
+        if (out->grad_u && out->grad_v) vector_out(P, solves ? lamx_carry : lamu_held, out->grad_u, out->grad_v);
+    }
+};
+}  // namespace nk
+
+extern "C" {
+
+nk_status nk_checkpointed_gradient(nk_problem* P, const nk_time_gradient_desc* desc, nk_cost_fn cost, void* user,
+                                   const nk_time_gradient* out, nk_time_gradient_stats* stats) {
+    if (!P || !desc || !cost) return NK_BAD_ARGUMENT;
+    return guarded(P->ctx, [&] {
+        auto t0 = std::chrono::steady_clock::now();
+        check_thickness_step(P, desc->dt);
+        if (desc->steps < 1) bad("steps must be at least 1");
+        if (desc->checkpoint_interval < 0) bad("checkpoint_interval must be non-negative");
+        if (desc->velocity_solves != 0 && desc->velocity_solves != 1) bad("velocity_solves is 0 or 1");
+        if (P->front.enabled) bad("the gradient through time steps does not cover a partial-cell front");
+        if (desc->velocity_solves && P->ud) bad("the gradient through velocity solves is not available with prescribed velocities");
+        if (desc->melt_weights)
+            for (int n = 0; n < desc->steps; ++n)
+                if (!std::isfinite(desc->melt_weights[n])) bad("melt weights must be finite");
+        TimeGradient tg;
+        tg.P = P;
+        tg.d = *desc;
+        tg.ctl = desc->adjoint_control ? *desc->adjoint_control : P->sd.picard;
+        if (tg.ctl.kind != NK_CONVERGENCE && tg.ctl.kind != NK_FIXED_ITERATIONS) bad("the adjoint takes Convergence or FixedIterations");
+        if (tg.ctl.kind == NK_FIXED_ITERATIONS ? tg.ctl.iterations < 0 : tg.ctl.maxiter < 0) bad("negative iteration count");
+        tg.cost = cost;
+        tg.user = user;
+        tg.solves = desc->velocity_solves != 0;
+        tg.diva = P->pd.stress_balance == NK_DIVA;
+        tg.N = desc->steps;
+        tg.K = desc->checkpoint_interval > 0 ? std::min(desc->checkpoint_interval, tg.N)
+                                             : (int)std::ceil(std::sqrt((double)tg.N) - 1e-12);
+        tg.S = (tg.N + tg.K - 1) / tg.K;
+        tg.rp = time_state_planes(tg.diva);
+        tg.a_planes = P->pd.rate_factor_layout == NK_RATE_FACTOR_SIGMA ? P->Ns : 1;
+        tg.pl = P->plane;
+        auto count = [&](int id) { FieldLoc f = field_loc(P, id); return (size_t)f.nx * f.ny * f.planes; };
+        tg.hH.resize(count(NK_FIELD_H));
+        tg.gH.resize(tg.hH.size());
+        tg.hmask.resize(count(NK_FIELD_ICE_MASK));
+        tg.hu.resize(count(NK_FIELD_U));
+        tg.gu.resize(tg.hu.size());
+        tg.hv.resize(count(NK_FIELD_V));
+        tg.gv.resize(tg.hv.size());
+        nk_time_gradient_stats local{};
+        nk_time_gradient_stats* st = stats ? stats : &local;
+        std::memset(st, 0, sizeof(*st));
+        st->segments = tg.S;
+        tg.run(st);
+        if (out) tg.copy_results(out);
+        st->elapsed_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    });
 }
 
 nk_status nk_picard_solve(nk_problem* P, nk_solve_stats* stats) {

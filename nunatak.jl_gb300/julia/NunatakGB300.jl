@@ -22,7 +22,7 @@ using Nunatak: VelocityVector, PicardIteration, Convergence, FixedIterations
 using Nunatak: GlenFlowLaw, ArrheniusRateFactor, WeertmanFriction, RegularizedCoulombFriction
 using Nunatak: FreeSlipWalls, NoSlipWalls, SubgridGroundedFraction, SmoothIceMask, DIVAShear
 using Nunatak: StressBalanceMultigridPreconditioner, StressBalanceDiagonalPreconditioner, PointJacobi, LineJacobi
-using Nunatak.Oceananigans: interior, Field
+using Nunatak.Oceananigans: Oceananigans, interior, Field
 using Nunatak.Oceananigans.Grids: topology, Bounded, Periodic, halo_size, xnodes, ynodes, Face
 using Nunatak.Oceananigans.BoundaryConditions: fill_halo_regions!
 using Enzyme
@@ -30,7 +30,7 @@ using Enzyme.EnzymeRules
 
 import Nunatak: picard_solve!, solve!, adjoint_solve!, precondition!, update_preconditioner!
 
-export GB300StressBalanceSolver, GB300MultigridPreconditioner
+export GB300StressBalanceSolver, GB300MultigridPreconditioner, checkpointed_gradient!
 
 const libnk = get(ENV, "NUNATAK_GB300_LIB", joinpath(@__DIR__, "..", "_build", "libnunatak_gb300.so"))
 
@@ -49,7 +49,7 @@ const NK_CONVERGENCE, NK_FIXED_ITERATIONS = Int32(0), Int32(1)
 
 const FIELD = (u = 0, v = 1, H = 2, bed = 3, s = 4, ice_mask = 5, φ = 6, φᵘ = 7, φᵛ = 8, N = 9, τᵘ = 10, τᵛ = 11,
                A = 12, C = 13, η̄H = 14, η̄Hᶠᶠ = 15, βᵘ = 16, βᵛ = 17, ησ = 18, F₂ = 19, βᵇᵘ = 20, βᵇᵛ = 21,
-               uᵇ = 22, vᵇ = 23, uσ = 24, vσ = 25, T = 26)
+               uᵇ = 22, vᵇ = 23, uσ = 24, vσ = 25, T = 26, a = 31, m = 32)
 
 struct IterationControl
     kind::Int32; iterations::Int32; maxiter::Int32; reserved::Int32; reltol::Float64; abstol::Float64
@@ -445,6 +445,150 @@ function EnzymeRules.reverse(config, func::Const{typeof(solve!)}, ::Type{RT}, ta
     parent(x̄.u) .= 0
     parent(x̄.v) .= 0
     return (nothing, nothing, nothing, map(a -> nothing, args)...)
+end
+
+#####
+##### The gradient through time steps (checkpointed_gradient!, ext/NunatakEnzymeExt.jl:245-263)
+#####
+
+struct AdvectionDesc
+    scheme::Int32; order::Int32; bounded::Int32; reserved::Int32; lower::Float64; upper::Float64
+end
+
+struct CostState
+    step::Int32; steps::Int32; H::Ptr{Float64}; u::Ptr{Float64}; v::Ptr{Float64}; ice_mask::Ptr{Float64}
+end
+
+struct TimeGradientDesc
+    dt::Float64; steps::Int32; checkpoint_interval::Int32; velocity_solves::Int32; reserved::Int32
+    melt_weights::Ptr{Float64}; adjoint_control::Ptr{IterationControl}
+end
+
+struct TimeGradient
+    grad_H::Ptr{Float64}; grad_u::Ptr{Float64}; grad_v::Ptr{Float64}; grad_smb::Ptr{Float64}; grad_melt::Ptr{Float64}
+    grad_log_C::Ptr{Float64}; grad_log_A::Ptr{Float64}
+end
+
+mutable struct TimeGradientStats
+    J::Float64; segments::Int32; picard_solves::Int32; picard_adjoints::Int32; adjoint_iterations::Int32
+    worst_solve_status::Int32; reserved::Int32; elapsed_ms::Float64
+    TimeGradientStats() = new(0.0, 0, 0, 0, 0, 0, 0, 0.0)
+end
+
+# The model's thickness advection (IceSheetModel's `advection`) as the library's descriptor: UpwindBiased{N} and
+# WENO{N} carry their order as 2N - 1; a bounds-preserving WENO its bounds.
+scheme_order(::Oceananigans.Advection.UpwindBiased{N}) where N = Int32(2N - 1)
+scheme_order(::Oceananigans.Advection.WENO{N}) where N = Int32(2N - 1)
+advection_desc(a::Oceananigans.Advection.UpwindBiased) = AdvectionDesc(0, scheme_order(a), 0, 0, 0.0, 0.0)
+function advection_desc(a::Oceananigans.Advection.WENO)
+    b = a.bounds
+    return b === nothing ? AdvectionDesc(1, scheme_order(a), 0, 0, 0.0, 0.0) : AdvectionDesc(1, scheme_order(a), 1, 0, b[1], b[2])
+end
+
+# The host's cost of the final model, differentiated by Enzyme on the host: the model's H, u, v and ice mask are set
+# to the state the library hands over, and ∂J/∂(H, u, v) are the shadows of a zeroed model.  The library calls this
+# after every step; the reference's cost is a function of the final model only.
+mutable struct CostCallback{F, M}
+    cost::F
+    model::M
+    err::Any
+end
+
+function set_interior!(f, p::Ptr{Float64})
+    a = interior(f, :, :, 1)
+    a .= unsafe_wrap(Array, p, size(a))
+    fill_halo_regions!(f)
+    return f
+end
+get_interior!(p::Ptr{Float64}, f) = (unsafe_wrap(Array, p, size(interior(f, :, :, 1))) .= interior(f, :, :, 1); nothing)
+
+function cost_callback(user::Ptr{Cvoid}, state::Ptr{CostState}, J::Ptr{Float64}, dH::Ptr{Float64}, du::Ptr{Float64},
+                       dv::Ptr{Float64})::Int32
+    cb = unsafe_pointer_to_objref(user)::CostCallback
+    s = unsafe_load(state)
+    unsafe_store!(J, 0.0)
+    s.step == s.steps || return Int32(0)
+    try
+        model = cb.model
+        set_interior!(model.geometry.H, s.H)
+        set_interior!(model.velocities.u, s.u)
+        set_interior!(model.velocities.v, s.v)
+        set_interior!(model.geometry.ice_mask, s.ice_mask)
+        dmodel = Enzyme.make_zero(model)
+        _, Jv = autodiff(set_runtime_activity(ReverseWithPrimal), cb.cost, Active, Duplicated(model, dmodel))
+        unsafe_store!(J, Jv)
+        get_interior!(dH, dmodel.geometry.H)
+        get_interior!(du, dmodel.velocities.u)
+        get_interior!(dv, dmodel.velocities.v)
+        return Int32(0)
+    catch e
+        cb.err = e
+        return Int32(1)
+    end
+end
+
+"""
+    checkpointed_gradient!(dmodel, cost, model, Δt, Nt; checkpoint_interval = ceil(Int, sqrt(Nt)),
+                           solver = model.velocity_solver.linear_solver, melt_weights = nothing)
+
+`checkpointed_gradient!` for a model whose stress-balance solver is a `GB300StressBalanceSolver`: `Nt` time steps of
+`Δt` (three split Runge-Kutta thickness stages with the model's advection, a Picard solve after each) and the
+gradient of `cost(model)` after them, on the GPU, by nk_checkpointed_gradient.  The gradient with respect to the
+initial thickness and velocities, the surface mass balance, the basal melt rate, the friction coefficient and the
+rate factor accumulates into `dmodel`; `model` is left at the final state; returns the cost.  The cost itself is
+differentiated by Enzyme on the host.  Not covered by the library: a `PartialCellFront` and the energy step.
+"""
+function checkpointed_gradient!(dmodel, cost, model, Δt, Nt; checkpoint_interval = ceil(Int, sqrt(Nt)),
+                                solver::GB300StressBalanceSolver = model.velocity_solver.linear_solver, melt_weights = nothing)
+    s = solver
+    set_field!(s, FIELD.H, model.geometry.H)
+    set_field!(s, FIELD.bed, model.bed)
+    set_field!(s, FIELD.u, model.velocities.u); set_field!(s, FIELD.v, model.velocities.v)
+    A = rate_factor_field(model.rheology)
+    set_field!(s, FIELD.A, A)
+    C = friction_field(model.friction)
+    C === nothing || set_field!(s, FIELD.C, C)
+    set_field!(s, FIELD.a, model.surface_mass_balance)
+    set_field!(s, FIELD.m, model.basal_melt_rate)
+    adv = Ref(advection_desc(model.advection))
+    check(ccall((:nk_set_thickness_advection, libnk), Int32, (Ptr{Cvoid}, Ref{AdvectionDesc}), s.problem, adv), s.ctx,
+          "nk_set_thickness_advection")
+    check(ccall((:nk_compute_geometry, libnk), Int32, (Ptr{Cvoid},), s.problem), s.ctx, "nk_compute_geometry")
+
+    Nx, Ny = size(model.grid)[1:2]
+    gH, gsmb, gmelt, glogC = (zeros(Nx, Ny) for _ in 1:4)
+    gu, gv = zeros(size(interior(model.velocities.u, :, :, 1))), zeros(size(interior(model.velocities.v, :, :, 1)))
+    glogA = zeros(size(interior(A)))
+    w = melt_weights === nothing ? nothing : collect(Float64, melt_weights)
+    ctl = Ref(IterationControl(model.velocity_solver.adjoint_iteration_control))
+    cb = CostCallback(cost, model, nothing)
+    fn = @cfunction(cost_callback, Int32, (Ptr{Cvoid}, Ptr{CostState}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}))
+    stats = TimeGradientStats()
+    st = GC.@preserve cb gH gu gv gsmb gmelt glogC glogA w ctl begin
+        d = Ref(TimeGradientDesc(Δt, Nt, checkpoint_interval, 1, 0, w === nothing ? C_NULL : pointer(w),
+                                 Base.unsafe_convert(Ptr{IterationControl}, ctl)))
+        out = Ref(TimeGradient(pointer(gH), pointer(gu), pointer(gv), pointer(gsmb), pointer(gmelt), pointer(glogC),
+                               pointer(glogA)))
+        ccall((:nk_checkpointed_gradient, libnk), Int32,
+              (Ptr{Cvoid}, Ref{TimeGradientDesc}, Ptr{Cvoid}, Ptr{Cvoid}, Ref{TimeGradient}, Ref{TimeGradientStats}),
+              s.problem, d, fn, pointer_from_objref(cb), out, stats)
+    end
+    cb.err === nothing || throw(cb.err)
+    check(st, s.ctx, "nk_checkpointed_gradient")
+
+    interior(dmodel.geometry.H, :, :, 1) .+= gH
+    interior(dmodel.velocities.u, :, :, 1) .+= gu
+    interior(dmodel.velocities.v, :, :, 1) .+= gv
+    interior(dmodel.surface_mass_balance, :, :, 1) .+= gsmb
+    interior(dmodel.basal_melt_rate, :, :, 1) .+= gmelt
+    C === nothing || (interior(friction_field(dmodel.friction)) .+= glogC ./ interior(C))
+    interior(rate_factor_field(dmodel.rheology)) .+= glogA ./ interior(A)
+
+    # the final state, as checkpointed_gradient! leaves the model
+    get_field!(model.geometry.H, s, FIELD.H)
+    get_field!(model.velocities.u, s, FIELD.u); get_field!(model.velocities.v, s, FIELD.v)
+    Nunatak.update_geometry_state!(model)
+    return stats.J
 end
 
 end # module

@@ -154,3 +154,34 @@ class Request(C.Structure):
                 ("friction_coefficient", C.POINTER(C.c_double)), ("rate_factor", C.POINTER(C.c_double)),
                 ("u_init", C.POINTER(C.c_double)), ("v_init", C.POINTER(C.c_double)),
                 ("u_out", C.POINTER(C.c_double)), ("v_out", C.POINTER(C.c_double))]
+
+
+# ---- the gradient through time steps (nk_checkpointed_gradient) ----
+class CostState(C.Structure):
+    """nk_cost_state: the host copies of the state after `step` steps that the cost callback reads."""
+    _fields_ = [("step", C.c_int32), ("steps", C.c_int32), ("H", C.POINTER(C.c_double)), ("u", C.POINTER(C.c_double)),
+                ("v", C.POINTER(C.c_double)), ("ice_mask", C.POINTER(C.c_double))]
+
+
+COST_FN = C.CFUNCTYPE(C.c_int32, C.c_void_p, C.POINTER(CostState), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                      C.POINTER(C.c_double), C.POINTER(C.c_double))
+
+
+class TimeGradientDesc(C.Structure):
+    _fields_ = [("dt", C.c_double), ("steps", C.c_int32), ("checkpoint_interval", C.c_int32),
+                ("velocity_solves", C.c_int32), ("reserved", C.c_int32), ("melt_weights", C.POINTER(C.c_double)),
+                ("adjoint_control", C.POINTER(IterationControl))]
+
+
+class TimeGradient(C.Structure):
+    _fields_ = [(n, C.POINTER(C.c_double)) for n in ("grad_H", "grad_u", "grad_v", "grad_smb", "grad_melt", "grad_log_C",
+                                                      "grad_log_A")]
+
+
+class TimeGradientStats(C.Structure):
+    _fields_ = [("J", C.c_double), ("segments", C.c_int32), ("picard_solves", C.c_int32), ("picard_adjoints", C.c_int32),
+                ("adjoint_iterations", C.c_int32), ("worst_solve_status", C.c_int32), ("reserved", C.c_int32),
+                ("elapsed_ms", C.c_double)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}

@@ -72,6 +72,8 @@ def _declare(lib):
         "nk_batch_picard_solve_async": ([vp, C.POINTER(C.c_uint8)], i32),
         "nk_batch_query": ([vp, ip], i32),
         "nk_batch_wait": ([vp, C.POINTER(abi.SolveStats)], i32),
+        "nk_checkpointed_gradient": ([vp, C.POINTER(abi.TimeGradientDesc), abi.COST_FN, vp, C.POINTER(abi.TimeGradient),
+                                      C.POINTER(abi.TimeGradientStats)], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

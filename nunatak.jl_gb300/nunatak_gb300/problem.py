@@ -326,6 +326,68 @@ class Problem:
         _check(st, "picard_adjoint", self._err())
         return lu, lv, grad, grad_a, stats
 
+    def checkpointed_gradient(self, cost, dt, steps, checkpoint_interval=None, velocity_solves=True, melt_weights=None,
+                              adjoint_control=None):
+        """checkpointed_gradient!(dmodel, cost, model, Δt, Nt; checkpoint_interval) (ext/NunatakEnzymeExt.jl:245-263)
+        on the device (nk_checkpointed_gradient): `steps` time steps of dt from the problem's state, each the three
+        thickness stages with a Picard solve after every stage (velocity_solves) or with the velocities held.
+        cost(step, H, u, v, ice_mask) is called on the state after each step (1..steps) and returns None (no cost
+        there) or (J, ∂J/∂H, ∂J/∂u, ∂J/∂v), None for a zero part; the reference's cost of the final model is the one
+        returned at step == steps.  melt_weights: a factor of the basal melt rate per step.  Returns a dict: J, the
+        gradients "H", "u", "v" (of the initial thickness and velocities), "smb", "melt", "log_C", "log_A" (with
+        velocity solves), and "stats".  The problem is left at the final state."""
+        errors = []
+        shp = {n: self.shape(n) for n in ("H", "u", "v", "ice_mask")}
+
+        def callback(user, state_p, J_p, dH_p, du_p, dv_p):
+            try:
+                s = state_p.contents
+                arrays = [np.ctypeslib.as_array(getattr(s, n), shape=shp[n]).copy() for n in ("H", "u", "v", "ice_mask")]
+                r = cost(int(s.step), *arrays)
+                J_p[0] = 0.0
+                if r is None:
+                    return 0
+                J, dH, du, dv = r
+                J_p[0] = float(J)
+                for ptr, arr, n in ((dH_p, dH, "H"), (du_p, du, "u"), (dv_p, dv, "v")):
+                    if arr is not None:
+                        np.ctypeslib.as_array(ptr, shape=shp[n])[...] = arr
+                return 0
+            except Exception as e:   # the library stops the gradient; the exception is raised below
+                errors.append(e)
+                return 1
+
+        cb = abi.COST_FN(callback)
+        keep = []
+        desc = abi.TimeGradientDesc()
+        desc.dt = float(dt)
+        desc.steps = int(steps)
+        desc.checkpoint_interval = int(checkpoint_interval or 0)
+        desc.velocity_solves = int(bool(velocity_solves))
+        if melt_weights is not None:
+            w = _as_f64(np.asarray(melt_weights, dtype=np.float64).ravel())
+            if w.size != steps:
+                raise ValueError("melt_weights needs one factor per step")
+            keep.append(w)
+            desc.melt_weights = w.ctypes.data_as(_dptr)
+        if adjoint_control is None:
+            adjoint_control = getattr(self.desc, "adjoint_control", None)
+        if adjoint_control is not None:
+            ctl = adjoint_control.desc()
+            keep.append(ctl)
+            desc.adjoint_control = C.pointer(ctl)
+        grads = {"H": np.zeros(shp["H"]), "u": np.zeros(shp["u"]), "v": np.zeros(shp["v"]), "smb": np.zeros(shp["H"]),
+                 "melt": np.zeros(shp["H"]), "log_C": np.zeros(shp["H"]), "log_A": np.zeros(self.shape("A"))}
+        out = abi.TimeGradient(*(grads[n].ctypes.data_as(_dptr) for n in ("H", "u", "v", "smb", "melt", "log_C", "log_A")))
+        stats = abi.TimeGradientStats()
+        st = self._fn("checkpointed_gradient")(self._h, C.byref(desc), cb, None, C.byref(out), C.byref(stats))
+        if errors:
+            raise errors[0]
+        _check(st, "checkpointed_gradient", self._err())
+        grads["J"] = stats.J
+        grads["stats"] = stats.as_dict()
+        return grads
+
     def query(self):
         """True once the asynchronous solve has finished (wait() then returns at once)."""
         d = C.c_int32()

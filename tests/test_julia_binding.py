@@ -10,7 +10,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "nunatak_gb300.h")
 JULIA = os.path.join(ROOT, "nunatak.jl_gb300", "julia", "NunatakGB300.jl")
 
-C_TYPES = {"int32_t": "Int32", "double": "Float64", "const double*": "Ptr{Float64}", "double*": "Ptr{Float64}"}
+C_TYPES = {"int32_t": "Int32", "double": "Float64", "const double*": "Ptr{Float64}", "double*": "Ptr{Float64}",
+           "const nk_iteration_control*": "Ptr{IterationControl}"}
 
 
 def c_structs():
@@ -22,7 +23,8 @@ def c_structs():
             decl = " ".join(decl.split())
             if not decl:
                 continue
-            mt = re.match(r"(const double\*|double\*|int32_t|double|int64_t|nk_iteration_control|nk_grid_desc|"
+            mt = re.match(r"(const double\*|double\*|int32_t|double|int64_t|const nk_iteration_control\*|"
+                          r"nk_iteration_control|nk_grid_desc|"
                           r"nk_physics_desc|nk_solver_desc|const double \*)\s*(.*)", decl)
             assert mt, decl
             typ = mt.group(1).replace(" *", "*")
@@ -53,7 +55,9 @@ def julia_structs():
 
 
 PAIRS = {"IterationControl": "nk_iteration_control", "GridDesc": "nk_grid_desc", "PhysicsDesc": "nk_physics_desc",
-         "SolverDesc": "nk_solver_desc", "SolveStats": "nk_solve_stats"}
+         "SolverDesc": "nk_solver_desc", "SolveStats": "nk_solve_stats", "AdvectionDesc": "nk_advection_desc",
+         "CostState": "nk_cost_state", "TimeGradientDesc": "nk_time_gradient_desc", "TimeGradient": "nk_time_gradient",
+         "TimeGradientStats": "nk_time_gradient_stats"}
 
 
 def test_descriptor_mirrors_match_the_header():
@@ -70,7 +74,8 @@ def test_every_ccall_is_declared():
     assert called and called <= declared, called - declared
     # the drop-in covers the entry points of the boundary's Julia-side methods
     for name in ("nk_problem_create", "nk_picard_solve", "nk_linear_solve", "nk_adjoint_solve", "nk_precondition",
-                 "nk_picard_adjoint", "nk_problem_set_field_parent", "nk_problem_get_field_parent"):
+                 "nk_picard_adjoint", "nk_problem_set_field_parent", "nk_problem_get_field_parent",
+                 "nk_checkpointed_gradient"):
         assert name in called, name
 
 
@@ -84,7 +89,7 @@ def test_field_ids_match_the_header():
              "φᵘ": "PHI_U", "φᵛ": "PHI_V", "N": "EFFECTIVE_PRESSURE", "τᵘ": "TAU_U", "τᵛ": "TAU_V", "A": "RATE_FACTOR",
              "C": "FRICTION_COEFFICIENT", "η̄H": "ETA_H", "η̄Hᶠᶠ": "ETA_H_FF", "βᵘ": "BETA_U", "βᵛ": "BETA_V",
              "ησ": "ETA_SIGMA", "F₂": "F2", "βᵇᵘ": "BETA_B_U", "βᵇᵛ": "BETA_B_V", "uᵇ": "U_B", "vᵇ": "V_B",
-             "uσ": "U_SIGMA", "vσ": "V_SIGMA", "T": "TEMPERATURE"}
+             "uσ": "U_SIGMA", "vσ": "V_SIGMA", "T": "TEMPERATURE", "a": "SURFACE_MASS_BALANCE", "m": "BASAL_MELT_RATE"}
     assert set(got) == set(names)
     for k, v in got.items():
         assert ids[names[k]] == v, (k, v, ids[names[k]])
