@@ -1207,8 +1207,8 @@ __global__ void k_adjoint_thickness(AdjointView v, GeometryView gv, int diva, do
         bool xf = f < 2;
         int fi = xf ? i + (f == 1) : i, fj = xf ? j : j + (f == 3);
         int side = (f == 1 || f == 3) ? 0 : 1;
-        bool has = xf ? (fj < g.Ny && (fi < g.Nx || !g.px)) : (fi < g.Nx && (fj < g.Ny || !g.py));
-        if (!has) continue;
+        // every centre has its four faces: on a Periodic axis the east (north) face of the last column (row) is the
+        // first face, reached through the wrapped index; on a Bounded one the outer faces are walls
         int k = xf ? g.u_idx(fi, fj) : g.v_idx(fi, fj);
         int c1 = xf ? g.c_idx(fi - 1, fj) : g.c_idx(fi, fj - 1), c2 = g.c_idx(fi, fj);
         bool peri = xf ? g.peripheral_fc(fi, fj) : g.peripheral_cf(fi, fj);

@@ -2068,9 +2068,10 @@ nk_status nk_picard_adjoint(nk_problem* P, const double* ubar, const double* vba
 
 namespace nk {
 // ---- the gradient through time steps (checkpointed_gradient!, ext/NunatakEnzymeExt.jl:245-263) ---------------------
-// A stored state: H, (U, V), and for the DIVA the lagged beta_b and F2 its next Picard step reads (diva.jl:77-80), so
-// that a restored state re-runs bit for bit and the adjoint of a solve linearises where the solve ended.
-static int time_state_planes(bool diva) { return diva ? 6 : 3; }
+// A stored state: H, (U, V), and for the DIVA the lagged beta_b, F2 and eta_sigma its next Picard step reads
+// (diva.jl:77-80; the vertical shear of _compute_shear_viscosity! divides by the previous viscosity), so that a
+// restored state re-runs bit for bit and the adjoint of a solve linearises where the solve ended.
+static int time_state_planes(const nk_problem* P, bool diva) { return diva ? 6 + P->Ns : 3; }
 static void save_time_state(nk_problem* P, double* rec, bool diva) {
     const size_t pl = P->plane;
     cudaStream_t s = P->stream;
@@ -2079,6 +2080,7 @@ static void save_time_state(nk_problem* P, double* rec, bool diva) {
     if (diva) {
         NK_CUDA(cudaMemcpyAsync(rec + 3 * pl, P->bb, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));
         NK_CUDA(cudaMemcpyAsync(rec + 5 * pl, P->F2, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        NK_CUDA(cudaMemcpyAsync(rec + 6 * pl, P->eta_sigma, (size_t)P->Ns * pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
     }
 }
 static void load_time_state(nk_problem* P, const double* rec, bool diva) {
@@ -2089,6 +2091,7 @@ static void load_time_state(nk_problem* P, const double* rec, bool diva) {
     if (diva) {
         NK_CUDA(cudaMemcpyAsync(P->bb, rec + 3 * pl, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));
         NK_CUDA(cudaMemcpyAsync(P->F2, rec + 5 * pl, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        NK_CUDA(cudaMemcpyAsync(P->eta_sigma, rec + 6 * pl, (size_t)P->Ns * pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
     }
     launch_problem_geometry(P);
     NK_CHECK_LAUNCH();
@@ -2335,7 +2338,7 @@ nk_status nk_checkpointed_gradient(nk_problem* P, const nk_time_gradient_desc* d
         tg.K = desc->checkpoint_interval > 0 ? std::min(desc->checkpoint_interval, tg.N)
                                              : (int)std::ceil(std::sqrt((double)tg.N) - 1e-12);
         tg.S = (tg.N + tg.K - 1) / tg.K;
-        tg.rp = time_state_planes(tg.diva);
+        tg.rp = time_state_planes(P, tg.diva);
         tg.a_planes = P->pd.rate_factor_layout == NK_RATE_FACTOR_SIGMA ? P->Ns : 1;
         tg.pl = P->plane;
         auto count = [&](int id) { FieldLoc f = field_loc(P, id); return (size_t)f.nx * f.ny * f.planes; };

@@ -363,3 +363,51 @@ def test_thickness_gradient_diva_matches_directional_differences(gpu_cls, fricti
     rich = (16 * fd(eps / 4) - fd(eps)) / 15
     ad = float(np.sum(gh * d))
     assert abs(rich - ad) <= RTOL * np.sum(np.abs(gh * d)), (friction, rich, ad)
+
+
+@pytest.mark.parametrize("diva", [False, True], ids=["ssa", "diva"])
+def test_thickness_gradient_on_the_periodic_seam(gpu_cls, diva):
+    """∂J/∂H of the cells whose north (east) face is the periodic axis's first face, read through the wrapped index:
+    the top row of a ridge periodic in y and Bounded in x (test/test_enzyme.jl:79-88), against extrapolated centred
+    differences of a seeded linear cost Σ w·x (Picard 1e-14), per cell to 1e-6 of the cell's own gradient, beside
+    interior cells (1e-8 of the largest entry at the weakly sensitive ones)."""
+    from support import ice_sheet_model
+    L = 64e3
+    grid = M.RectilinearGrid(size=(16, 4), x=(0.0, L), y=(0.0, 16e3), topology=("Bounded", "Periodic"), halo=(4, 4))
+    solver = M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-15, maxiter=10_000),
+                                   picard_iteration_control=M.Convergence(reltol=1e-14, maxiter=1000))
+
+    def build():
+        P, st = ice_sheet_model(gpu_cls, grid,
+                                H=lambda x, y: 500 + 300 * math.exp(-((x - L / 2) / 12e3) ** 2) * (1 + math.sin(2 * math.pi * y / 16e3) / 5),
+                                bed=0.0, rheology=M.GlenFlowLaw(rate_factor=1e-24),
+                                friction=M.WeertmanFriction(coefficient=lambda x, y: 3e6 * (1 + x / L)),
+                                stress_balance=M.DepthIntegrated(shear=M.DIVAShear()) if diva else None,
+                                velocity_solver=solver, Nsigma=6 if diva else 4)
+        return P
+
+    P = build()
+    u0, v0, H0 = P.get("u"), P.get("v"), P.get("H")
+    rng = np.random.default_rng(5)
+    wu, wv = rng.standard_normal(u0.shape), rng.standard_normal(v0.shape)
+    *_, gh, st = P.picard_adjoint(wu, wv, M.Convergence(reltol=1e-14, maxiter=3000), thickness=True)
+    assert st.status == 0
+
+    def difference(cell, d):
+        out = []
+        for sgn in (1.0, -1.0):
+            Q = build()
+            H = H0.copy()
+            H[cell] += sgn * d
+            Q.set("H", H)
+            Q.compute_geometry()
+            Q.set("u", u0)
+            Q.set("v", v0)
+            Q.picard_solve()
+            out.append((Q.get("u"), Q.get("v")))
+        return (np.sum(wu * (out[0][0] - out[1][0])) + np.sum(wv * (out[0][1] - out[1][1]))) / (2 * d)
+
+    for cell in ((3, 15), (3, 7), (3, 0), (1, 5), (0, 8)):
+        d = 1e-3 * H0[cell]
+        fd = (16 * difference(cell, d / 4) - difference(cell, d)) / 15
+        assert abs(fd - gh[cell]) <= 1e-6 * abs(fd) + 1e-8 * np.max(np.abs(gh)), (cell, fd, gh[cell])

@@ -85,9 +85,12 @@ def transport_case(advection=None):
 def ridge_case(cls_for_dt, diva=False, steps=6, melt=0.0):
     L = 64e3
     grid = M.RectilinearGrid(size=(16, 4), x=(0.0, L), y=(0.0, 16e3), topology=("Bounded", "Periodic"), halo=(4, 4))
-    solver = M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-14, maxiter=10_000),
-                                   picard_iteration_control=M.Convergence(reltol=1e-12, maxiter=300),
-                                   adjoint_iteration_control=M.Convergence(reltol=1e-14 if diva else 1e-12, maxiter=2000))
+    # Picard to 1e-14, CG to 1e-15: a perturbed solve stops once its change falls below reltol ‖u‖, so with the
+    # reference's 1e-12 a difference in one cell's H (a velocity response of ~1e-6 ‖u‖) keeps a bias of ~1e-5 of
+    # its own size from the Picard iterations not run; the adjoint is the converged fixed point's
+    solver = M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-15, maxiter=10_000),
+                                   picard_iteration_control=M.Convergence(reltol=1e-14, maxiter=1000),
+                                   adjoint_iteration_control=M.Convergence(reltol=1e-14, maxiter=2000))
     sb = M.DepthIntegrated(shear=M.DIVAShear()) if diva else None
 
     def build(cls):
@@ -111,7 +114,9 @@ def grounding_line_case(advection):
 
     def build(cls):
         P = make(cls, grid, advection=advection, Nsigma=2, grounding=M.SubgridGroundedFraction())
-        set_fn(P, "H", lambda x, y: 700 - 400 * x / L + 30 * math.sin(2 * math.pi * y / 12e3))
+        # curved along the flow: on linear data WENO-Z's τ = |β₀ - β₂| sits at its kink, where a difference and the
+        # derivative of one branch part
+        set_fn(P, "H", lambda x, y: 700 - 400 * x / L + 40 * math.cos(2 * math.pi * x / L) + 30 * math.sin(2 * math.pi * y / 12e3))
         set_fn(P, "bed", lambda x, y: -300 - 700 * x / L)
         P.compute_geometry()
         P.set("u", 2e-6)
@@ -149,6 +154,11 @@ def fd_final_thickness(case, cls, field, index, h):
     Hp = case.forward(cls, mutate(+1)).get("H")
     Hm = case.forward(cls, mutate(-1)).get("H")
     return _difference(Hp, Hm) / (2 * h)
+
+
+def fd_extrapolated(case, cls, field, index, h):
+    """Richardson's (16 D(h/4) - D(h)) / 15 of fd_final_thickness: accurate to O(h⁴) where the response curves."""
+    return (16 * fd_final_thickness(case, cls, field, index, h / 4) - fd_final_thickness(case, cls, field, index, h)) / 15
 
 
 def gradient(case, cls, cost=None, **kw):
@@ -210,10 +220,10 @@ def test_picard_time_steps_gradient_matches_differences(gpu_cls, diva):
     assert g["stats"]["worst_solve_status"] == 0
     H0 = case.build(gpu_cls).get("H")
     for idx in ((1, 5), (2, 9)):
-        _close(g["H"][idx], fd_final_thickness(case, gpu_cls, "H", idx, 1e-4 * H0[idx]), rtol)
+        _close(g["H"][idx], fd_extrapolated(case, gpu_cls, "H", idx, 1e-3 * H0[idx]), rtol)
     C = case.build(gpu_cls).get("C")
-    _close(g["log_C"][1, 6] / C[1, 6], fd_final_thickness(case, gpu_cls, "C", (1, 6), 1e-4 * C[1, 6]), rtol)
-    _close(g["smb"][2, 8], fd_final_thickness(case, gpu_cls, "surface_mass_balance", (2, 8), 1e-4 * 1e-8), rtol)
+    _close(g["log_C"][1, 6] / C[1, 6], fd_extrapolated(case, gpu_cls, "C", (1, 6), 1e-3 * C[1, 6]), rtol)
+    _close(g["smb"][2, 8], fd_extrapolated(case, gpu_cls, "surface_mass_balance", (2, 8), 1e-2 * 1e-8), rtol)
 
 
 def test_picard_time_steps_against_the_oracle_forward(gpu_cls, oracle_cls):
@@ -223,8 +233,9 @@ def test_picard_time_steps_against_the_oracle_forward(gpu_cls, oracle_cls):
     _close(g["H"][1, 5], fd_final_thickness(case, oracle_cls, "H", (1, 5), 1e-4 * H0[1, 5]), 1e-5)
 
 
-def test_checkpoint_intervals_agree_and_the_problem_ends_at_the_final_state(gpu_cls):
-    case = ridge_case(gpu_cls)
+@pytest.mark.parametrize("diva", [False, True], ids=["ssa", "diva"])
+def test_checkpoint_intervals_agree_and_the_problem_ends_at_the_final_state(gpu_cls, diva):
+    case = ridge_case(gpu_cls, diva=diva)
     runs = []
     for k in (1, 2, case.steps):
         P, g = gradient(case, gpu_cls, checkpoint_interval=k)
@@ -304,7 +315,7 @@ def test_costs_at_two_steps_with_melt_weights(gpu_cls):
         return f
 
     for idx in ((1, 6), (3, 12)):
-        h = 1e-4 * 1e-9 * (1 + (idx[1] + 0.5) / 16)
+        h = 1e-2 * 1e-9 * (1 + (idx[1] + 0.5) / 16)
         _close(g["melt"][idx], fd(melt_at(idx, h), melt_at(idx, -h), h), 1e-5)
 
     H0 = case.build(gpu_cls).get("H")
