@@ -354,4 +354,131 @@ void launch_advance_front(const FrontView& v, int passes, double dt, size_t plan
     k_front_force<<<d.grid, d.block, 0, s>>>(v, dt); count_launch();
 }
 
+// ---- the reverse of advance_front! without passes or calving (the gradient through time steps) -------------------
+namespace {
+// full after _empty_drained_cells!: flagged, holding ice and active
+__device__ __forceinline__ bool drained_full(const DevGrid<double>& g, const double* mu, const double* H, int a, int b) {
+    if (inactive(g, a, b)) return false;
+    int c = g.c_idx(a, b);
+    return mu[c] > 0 && H[c] > 0;
+}
+// The reference pass of cell (i, j) after the drain (k_front_reference): its sums over the full neighbours and over
+// those flowing in, and the branch its Hʳ took.
+struct Reference {
+    double Hi, Hr_old, Hbar, Sin, Sf;
+    int nin, nf;
+    bool full, inflow[4];
+};
+__device__ Reference reference_of(const FrontView& v, int i, int j) {
+    const DevGrid<double>& g = v.g;
+    Reference r;
+    int k = g.idx(i, j);
+    r.inflow[0] = v.x[g.u_idx(i, j)].x > 0;
+    r.inflow[1] = v.x[g.u_idx(i + 1, j)].x < 0;
+    r.inflow[2] = v.x[g.v_idx(i, j)].y > 0;
+    r.inflow[3] = v.x[g.v_idx(i, j + 1)].y < 0;
+    r.Sin = r.Sf = 0.0;
+    r.nin = r.nf = 0;
+    for (int d = 0; d < 4; ++d) {
+        int a = i + DI(d), b = j + DJ(d);
+        if (!drained_full(g, v.mu, v.H, a, b)) continue;
+        double Hn = v.H[g.c_idx(a, b)];
+        r.Sf += Hn;
+        ++r.nf;
+        if (r.inflow[d]) { r.Sin += Hn; ++r.nin; }
+    }
+    r.Hi = v.H[k];
+    r.Hr_old = v.Hr[k];
+    r.full = v.mu[k] > 0 && r.Hi > 0;
+    double Hs = r.nf > 0 ? r.Sf / (double)(r.nf > 1 ? r.nf : 1) : r.Hi;
+    double Hp = r.Hi > 0 ? (r.Hr_old > 0 ? r.Hr_old : Hs) : 0.0;
+    r.Hbar = r.nin > 0 ? r.Sin / (double)(r.nin > 1 ? r.nin : 1) : Hp;
+    return r;
+}
+}  // namespace
+
+// Per cell: the reverse of _force_front_cells! (:271-286) and the cell's own terms of the reference pass.
+__global__ void k_front_adjoint_cells(FrontAdjointView a) {
+    const FrontView& v = a.f;
+    const DevGrid<double>& g = v.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int k = g.idx(i, j);
+    Reference r = reference_of(v, i, j);
+    double Hrp = r.full ? 0.0 : r.Hbar;
+    double m = v.grounding ? (1 - v.phi[k]) * v.melt[k] : v.melt[k];
+    double S = v.smb[k] - m;
+    double dt = a.dt;
+    bool forced = (r.Hi > 0) && (Hrp > 0);
+    double Hf = r.full ? r.Hi : Hrp;
+    bool melted = forced && (Hf + S * dt <= 0);
+    double lH = a.lam_H[k], lR = a.lam_Hr[k];
+    double lHi = 0.0, lHrp = 0.0, lS = 0.0;
+    if (melted) {
+        // H and Hʳ become zero: nothing flows back
+    } else if (forced) {   // a partial cell (a full one has Hʳ = 0): H (Hʳ + S Δt) / Hʳ, Hʳ + S Δt
+        lHi = lH * (Hrp + S * dt) / Hrp;
+        lHrp = lH * r.Hi * (-S * dt) / (Hrp * Hrp) + lR;
+        lS = (lH * r.Hi / Hrp + lR) * dt;
+    } else {
+        lHi = lH;
+        lHrp = r.full ? 0.0 : lR;
+    }
+    a.lam_smb[k] += lS;
+    a.lam_melt[k] -= lS * (v.grounding ? 1 - v.phi[k] : 1.0) * a.melt_weight;
+    a.lam_phi[k] = v.grounding ? lS * v.melt[k] : 0.0;
+    // Hʳ = H̄ on a cell not full: the donors' and full neighbours' shares are gathered by k_front_adjoint_gather
+    double lbar = r.full ? 0.0 : lHrp, lHr_old = 0.0;
+    if (r.nin == 0 && r.Hi > 0) {
+        if (r.Hr_old > 0) lHr_old = lbar;
+        else if (r.nf == 0) lHi += lbar;   // Hˢ = H of the cell itself
+    }
+    a.lam_Hrp[k] = lbar;
+    a.lam_Hd[k] = lHi;
+    a.lam_Hr[k] = lHr_old;
+}
+
+// Per cell c: its own part plus the shares of the reference thickness of the neighbours it is a full neighbour of
+// (the donors' mean when any flows in, else the full neighbours' mean when the cell had no Hʳ).
+__global__ void k_front_adjoint_gather(FrontAdjointView a) {
+    const FrontView& v = a.f;
+    const DevGrid<double>& g = v.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int c = g.idx(i, j);
+    double acc = a.lam_Hd[c];
+    if (drained_full(g, v.mu, v.H, i, j)) {
+        int seen[4], ns = 0;
+        for (int e = 0; e < 4; ++e) {
+            int ki = i + DI(e), kj = j + DJ(e);
+            if (inactive(g, ki, kj)) continue;
+            int kc = g.c_idx(ki, kj);
+            bool dup = false;
+            for (int q = 0; q < ns; ++q) dup |= seen[q] == kc;
+            if (dup) continue;
+            seen[ns++] = kc;
+            double lbar = a.lam_Hrp[kc];
+            if (lbar == 0.0) continue;
+            int ci = g.cx(ki), cj = g.cy(kj);
+            Reference r = reference_of(v, ci, cj);
+            for (int d = 0; d < 4; ++d) {
+                int na = ci + DI(d), nb = cj + DJ(d);
+                if (inactive(g, na, nb) || g.c_idx(na, nb) != c) continue;
+                if (r.nin > 0) {
+                    if (r.inflow[d]) acc += lbar / (double)r.nin;
+                } else if (r.Hi > 0 && !(r.Hr_old > 0) && r.nf > 0) {
+                    acc += lbar / (double)r.nf;
+                }
+            }
+        }
+    }
+    a.lam_H3[c] = acc;
+}
+
+void launch_front_adjoint(const FrontAdjointView& a, cudaStream_t s) {
+    LaunchDims d = dims2d(a.f.g.Nx, a.f.g.Ny);
+    k_front_adjoint_cells<<<d.grid, d.block, 0, s>>>(a); count_launch();
+    k_front_adjoint_gather<<<d.grid, d.block, 0, s>>>(a); count_launch();
+}
+
 }  // namespace nk

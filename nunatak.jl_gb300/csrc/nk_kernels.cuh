@@ -263,8 +263,25 @@ struct StageAdjointView {
     double* lam_phi;                  // λ of the centre grounded fraction per cell
     double2* lamF;                    // λ of the flux through x face (i, j) (.x) and y face (i, j) (.y)
     double2* lw_x; double2* lw_y;     // λ of a cell's own reconstructions (W, E) and (S, N) through its limiter θ
+    const double* lam_phi_in = nullptr;   // λ of φ from elsewhere (the front's forced melt), added before the gather
 };
 void launch_stage_adjoint(const StageAdjointView& a, cudaStream_t s);
+// The reverse of advance_front! without overflow passes or calving (nk_front.cu): the drained flags, the reference
+// thickness Hʳ of the front cells and the sources forced onto them.  f is the front's view at the end of the final
+// stage with f.H the stage's output before the front, f.mu and f.Hr the flag and Hʳ before it, the stage's
+// velocities, the effective melt and φ of the stage's input.
+struct FrontAdjointView {
+    FrontView f;
+    double dt, melt_weight;
+    const double* lam_H;              // λ of H after the front
+    double* lam_Hr;                   // in: λ of Hʳ after the front; out: λ of Hʳ before it
+    double* lam_H3;                   // = λ of the stage output before the front
+    double* lam_smb; double* lam_melt;   // +=
+    double* lam_phi;                  // = λ of φ of the forced cells' melt
+    double* lam_Hrp;                  // scratch: λ of Hʳ after the reference pass
+    double* lam_Hd;                   // scratch: the cell's own part of λ H3
+};
+void launch_front_adjoint(const FrontAdjointView& a, cudaStream_t s);
 // y += x over the interior cells of `planes` planes (each `plane` doubles apart)
 void launch_add_planes(const DevGrid<double>& g, double* y, const double* x, int planes, size_t plane, cudaStream_t s);
 // y += x over the pair faces 0..Nx x 0..Ny

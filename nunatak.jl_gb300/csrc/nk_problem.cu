@@ -2071,12 +2071,18 @@ namespace nk {
 // A stored state: H, (U, V), and for the DIVA the lagged beta_b, F2 and eta_sigma its next Picard step reads
 // (diva.jl:77-80; the vertical shear of _compute_shear_viscosity! divides by the previous viscosity), so that a
 // restored state re-runs bit for bit and the adjoint of a solve linearises where the solve ended.
-static int time_state_planes(const nk_problem* P, bool diva) { return diva ? 6 + P->Ns : 3; }
+// With a partial-cell front the flag μ and the front thickness Hʳ follow them (the step's last stage moves the front).
+static int time_state_planes(const nk_problem* P, bool diva) { return (diva ? 6 + P->Ns : 3) + (P->front.enabled ? 2 : 0); }
 static void save_time_state(nk_problem* P, double* rec, bool diva) {
     const size_t pl = P->plane;
     cudaStream_t s = P->stream;
     NK_CUDA(cudaMemcpyAsync(rec, P->H, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
     NK_CUDA(cudaMemcpyAsync(rec + pl, P->x, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    if (P->front.enabled) {
+        double* f = rec + (size_t)(time_state_planes(P, diva) - 2) * pl;
+        NK_CUDA(cudaMemcpyAsync(f, P->mu, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        NK_CUDA(cudaMemcpyAsync(f + pl, P->front_buf, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    }
     if (diva) {
         NK_CUDA(cudaMemcpyAsync(rec + 3 * pl, P->bb, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));
         NK_CUDA(cudaMemcpyAsync(rec + 5 * pl, P->F2, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
@@ -2088,6 +2094,11 @@ static void load_time_state(nk_problem* P, const double* rec, bool diva) {
     cudaStream_t s = P->stream;
     NK_CUDA(cudaMemcpyAsync(P->H, rec, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
     NK_CUDA(cudaMemcpyAsync(P->x, rec + pl, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    if (P->front.enabled) {
+        const double* f = rec + (size_t)(time_state_planes(P, diva) - 2) * pl;
+        NK_CUDA(cudaMemcpyAsync(P->mu, f, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        NK_CUDA(cudaMemcpyAsync(P->front_buf, f + pl, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    }
     if (diva) {
         NK_CUDA(cudaMemcpyAsync(P->bb, rec + 3 * pl, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));
         NK_CUDA(cudaMemcpyAsync(P->F2, rec + 5 * pl, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
@@ -2104,12 +2115,13 @@ struct TimeGradient {
     nk_cost_fn cost;
     void* user;
     nk_time_gradient_stats* st;
-    bool solves, diva;
+    bool solves, diva, front;
     int N, K, S, rp, a_planes;
     size_t pl;
     double* mem = nullptr;
     // scratch planes
     double *lamH, *lamHs, *lamH0, *dv, *lamphi, *g_smb, *g_melt, *base_melt, *clipped_end, *g_logC, *g_logA;
+    double *h3pre, *lamHr, *lamHrp, *lamHd, *lamphi_front;   // the front's reverse
     double2 *lamF, *lwx, *lwy, *lamx_stage, *lamx_carry, *lamu_held;
     std::vector<double> hH, hu, hv, hmask, gH, gu, gv;
 
@@ -2126,7 +2138,7 @@ struct TimeGradient {
         if (status > st->worst_solve_status) st->worst_solve_status = status;
     }
     void allocate() {
-        const int scratch = 22 + a_planes;
+        const int scratch = 27 + a_planes;
         size_t planes = (size_t)(S + 3 * K + 2) * rp + scratch;
         NK_CUDA(cudaMalloc(&mem, planes * pl * sizeof(double)));
         double* b = mem + (size_t)(S + 3 * K + 2) * rp * pl;
@@ -2135,7 +2147,8 @@ struct TimeGradient {
         lamH = one(0); lamHs = one(1); lamH0 = one(2); dv = one(3); lamphi = one(4); g_smb = one(5); g_melt = one(6);
         base_melt = one(7); clipped_end = one(8); g_logC = one(9);
         lamF = two(10); lwx = two(12); lwy = two(14); lamx_stage = two(16); lamx_carry = two(18); lamu_held = two(20);
-        g_logA = one(22);
+        h3pre = one(22); lamHr = one(23); lamHrp = one(24); lamHd = one(25); lamphi_front = one(26);
+        g_logA = one(27);
     }
     void solve() {
         nk_solve_stats ss{};
@@ -2193,7 +2206,7 @@ struct TimeGradient {
     }
     // the reverse of stage stg of step n (local k) from the loaded state tape(3k + stg): λ of its output in lamH,
     // λ of its input into lamHs (and the step start into lamH0), the velocity adjoint into lamx_stage
-    void stage_reverse(int n, int k, int stg) {
+    void stage_reverse(int n, int k, int stg, bool after_front) {
         static const double fractions[3] = {1.0 / 3, 1.0 / 2, 1.0};
         cudaStream_t s = P->stream;
         launch_scale_plane(P->fine.g, melt(), base_melt, weight(n), s);
@@ -2205,7 +2218,8 @@ struct TimeGradient {
         NK_CUDA(cudaMemsetAsync(lamx_stage, 0, pl * sizeof(double2), s));
         StageAdjointView a;
         a.t = tv;
-        a.Hout = tape(3 * k + stg + 1);
+        a.Hout = after_front ? h3pre : tape(3 * k + stg + 1);
+        a.lam_phi_in = after_front ? lamphi_front : nullptr;
         a.bed = P->bed;
         a.rw_ri = P->pd.ocean_density / P->pd.ice_density;
         a.dtau = fractions[stg] * d.dt;
@@ -2222,6 +2236,38 @@ struct TimeGradient {
         a.lw_x = lwx;
         a.lw_y = lwy;
         launch_stage_adjoint(a, s);
+        NK_CHECK_LAUNCH();
+    }
+
+    // The reverse of the front's advance after the last stage of step n (local k): the stage's output before the front is
+    // recomputed from the stored stage input; λ of H after the front (lamH) becomes λ of that output (lam_out), λ of Hʳ
+    // passes back through the step (lamHr), and the forced cells' melt leaves λ of φ for the stage's reverse.
+    void front_reverse(int n, int k, double* lam_out) {
+        static const double last = 1.0;
+        cudaStream_t s = P->stream;
+        load_time_state(P, tape(3 * k + 2), diva);
+        launch_scale_plane(P->fine.g, melt(), base_melt, weight(n), s);
+        ThicknessView tv = thickness_view(P, false);
+        NK_CUDA(cudaMemcpyAsync((double*)tv.Hs, P->H, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        NK_CUDA(cudaMemcpyAsync((double*)tv.H0, tape(3 * k), pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        if (tv.fx) launch_thickness_faces(tv, s);
+        if (P->advection.scheme == NK_ADVECTION_WENO && P->advection.bounded) launch_thickness_limiter(tv, s);
+        launch_thickness_stage(tv, last * d.dt, 1, s);   // P->H = the output before the front (the clip is restored at the end)
+        NK_CUDA(cudaMemcpyAsync(h3pre, P->H, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        FrontAdjointView fa;
+        fa.f = front_view(P, false);
+        fa.f.H = h3pre;
+        fa.dt = last * d.dt;
+        fa.melt_weight = weight(n);
+        fa.lam_H = lamH;
+        fa.lam_Hr = lamHr;
+        fa.lam_H3 = lam_out;
+        fa.lam_smb = g_smb;
+        fa.lam_melt = g_melt;
+        fa.lam_phi = lamphi_front;
+        fa.lam_Hrp = lamHrp;
+        fa.lam_Hd = lamHd;
+        launch_front_adjoint(fa, s);
         NK_CHECK_LAUNCH();
     }
 
@@ -2242,7 +2288,7 @@ struct TimeGradient {
         save_time_state(P, final_rec(), diva);
         NK_CUDA(cudaMemcpyAsync(clipped_end, P->transport + 3 * pl, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
         // ---- reverse, one segment at a time ----
-        for (double* z : {lamH, g_smb, g_melt, g_logC}) NK_CUDA(cudaMemsetAsync(z, 0, pl * sizeof(double), s));
+        for (double* z : {lamH, g_smb, g_melt, g_logC, lamHr}) NK_CUDA(cudaMemsetAsync(z, 0, pl * sizeof(double), s));
         NK_CUDA(cudaMemsetAsync(g_logA, 0, (size_t)a_planes * pl * sizeof(double), s));
         for (double2* z : {lamx_carry, lamu_held, lamF, lwx, lwy}) NK_CUDA(cudaMemsetAsync(z, 0, pl * sizeof(double2), s));
         double* lam = lamH;      // λ of the current thickness (the buffers swap roles as the sweep moves back)
@@ -2263,11 +2309,16 @@ struct TimeGradient {
                     NK_CUDA(cudaMemsetAsync(lamx_carry, 0, pl * sizeof(double2), s));
                 }
                 NK_CUDA(cudaMemsetAsync(lamH0, 0, pl * sizeof(double), s));
+                if (front) {
+                    lamH = lam;
+                    front_reverse(n, k, lam_in);
+                    std::swap(lam, lam_in);
+                }
                 for (int stg = 2; stg >= 0; --stg) {
                     load_time_state(P, tape(3 * k + stg), diva);
                     lamH = lam;
                     lamHs = lam_in;
-                    stage_reverse(n, k, stg);
+                    stage_reverse(n, k, stg, front && stg == 2);
                     if (stg > 0) {
                         if (solves) solve_adjoint(lamx_stage, lam_in);   // the solve that made x_t from H_t
                         else launch_add_pairs(g, lamu_held, lamx_stage, s);
@@ -2319,7 +2370,9 @@ nk_status nk_checkpointed_gradient(nk_problem* P, const nk_time_gradient_desc* d
         if (desc->steps < 1) bad("steps must be at least 1");
         if (desc->checkpoint_interval < 0) bad("checkpoint_interval must be non-negative");
         if (desc->velocity_solves != 0 && desc->velocity_solves != 1) bad("velocity_solves is 0 or 1");
-        if (P->front.enabled) bad("the gradient through time steps does not cover a partial-cell front");
+        if (P->front.enabled && (P->front.passes != 0 || P->front.calving != NK_CALVING_NONE))
+            bad("the gradient through time steps covers a partial-cell front without overflow passes or calving "
+                "(PartialCellFront(passes = 0))");
         if (desc->velocity_solves && P->ud) bad("the gradient through velocity solves is not available with prescribed velocities");
         if (desc->melt_weights)
             for (int n = 0; n < desc->steps; ++n)
@@ -2334,6 +2387,7 @@ nk_status nk_checkpointed_gradient(nk_problem* P, const nk_time_gradient_desc* d
         tg.user = user;
         tg.solves = desc->velocity_solves != 0;
         tg.diva = P->pd.stress_balance == NK_DIVA;
+        tg.front = P->front.enabled != 0;
         tg.N = desc->steps;
         tg.K = desc->checkpoint_interval > 0 ? std::min(desc->checkpoint_interval, tg.N)
                                              : (int)std::ceil(std::sqrt((double)tg.N) - 1e-12);

@@ -38,7 +38,7 @@ __global__ void k_stage_adjoint_cells(StageAdjointView a) {
         a.lam_melt[c] -= lS * (v.grounding ? 1 - v.phi[c] : 1.0) * a.melt_weight;
         if (v.grounding) lp = lS * v.melt[c];   // ∂S/∂φ = w m
     }
-    a.lam_phi[c] = lp;
+    a.lam_phi[c] = lp + (a.lam_phi_in ? a.lam_phi_in[c] : 0.0);
 }
 
 // The limited face thickness of a flux between two full cells (as k_thickness_stage evaluates it).

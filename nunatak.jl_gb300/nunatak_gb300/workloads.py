@@ -213,3 +213,34 @@ def mismip_stream(dx, velocity_solver=None):
                grounding=M.SubgridGroundedFraction(), velocity_solver=solver)
     C = np.full_like(H, 1e4 * YEAR ** (1.0 / 3.0))
     return Case("mismip_stream", grid, cfg, {"H": H, "bed": bed, "A": np.full_like(H, A), "C": C})
+
+
+def halfpipe_streamice(spec, Nsigma=10, velocity_solver=None):
+    """MITgcm STREAMICE's verification experiment halfpipe_streamice as Nunatak.jl sets it up
+    (benchmarks/halfpipe_streamice.jl:1-37, benchmarks/halfpipe_streamice_adjoint.jl:17-32): a mostly floating shelf
+    in a half-pipe channel of `Nx` x `Ny` cells of `dx_km`, fed through its west column by a mass source inflow / Δx,
+    with DIVA stress balance, no-slip side walls, the subgrid grounded fraction, a partial-cell front without overflow
+    passes, Glen A = (B²)^(-n) / yr and Weertman drag C² yr |u|⁰ u (ε̇₀ and u₀ 1e-12 / yr), and STREAMICE's analytic
+    initial shelf: 300 m beyond 50 km, thickening quadratically upstream, ice free beyond 70 km.  `spec` holds the
+    experiment's values (the densities, B, C, n, the grid, the inflow and the bed profile across the channel).  The
+    year is Oceananigans' 365 days.  Returns (Case, surface mass balance in m/s, seconds per year)."""
+    year = 365 * 86400.0
+    dx = spec["dx_km"] * 1e3
+    Nx, Ny = int(spec["Nx"]), int(spec["Ny"])
+    grid = M.RectilinearGrid(size=(Nx, Ny), x=(0.0, Nx * dx), y=(0.0, Ny * dx), halo=(4, 4))
+    B, C, n = spec["B"], spec["C"], spec["n"]
+    solver = velocity_solver or M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-10, maxiter=10_000),
+                                                      picard_iteration_control=M.Convergence(reltol=1e-8, maxiter=500))
+    cfg = dict(Nsigma=Nsigma, stress_balance=M.DepthIntegrated(shear=M.DIVAShear(), side_walls=M.NoSlipWalls()),
+               rheology=M.GlenFlowLaw(rate_factor=(B ** 2) ** (-n) / year, exponent=n, strain_rate_regularization=1e-12 / year),
+               friction=M.WeertmanFriction(coefficient=None, exponent=1.0, velocity_regularization=1e-12 / year),
+               grounding=M.SubgridGroundedFraction(), masking=M.PartialCellFront(passes=0),
+               constants=M.IceSheetConstants(ice_density=spec["ice_density"], ocean_density=spec["ocean_density"],
+                                             gravitational_acceleration=spec["gravitational_acceleration"]),
+               velocity_solver=solver)
+    X, _ = _centers(grid)
+    H = np.where(X < 70e3, 300.0 + 1000.0 * np.minimum(1.0, (np.maximum(50e3 - X, 0.0) / 62e3) ** 2), 0.0)
+    bed = np.repeat(np.asarray(spec["bed_profile"], dtype=np.float64)[:, None], Nx, axis=1)
+    fields = {"H": H, "bed": bed, "C": np.full_like(H, C ** 2 * year), "A": np.full_like(H, (B ** 2) ** (-n) / year)}
+    smb = np.where(X < dx, spec["inflow_m2_per_year"] / year / dx, 0.0)
+    return Case("halfpipe_streamice", grid, cfg, fields), smb, year
