@@ -101,6 +101,10 @@ def parse():
     ap.add_argument("--scaling", action="store_true",
                     help="the reference's published multigrid scaling benchmark instead: iterations and device time of "
                          "one SSA solve to 1e-8 at six grid spacings, beside the published numbers")
+    ap.add_argument("--halfpipe-adjoint", action="store_true",
+                    help="the STREAMICE halfpipe adjoint instead (benchmarks/halfpipe_streamice_adjoint.jl): the gradient "
+                         "through three DIVA time steps with a partial-cell front, beside centred differences and STREAMICE's "
+                         "published cost and gradient")
     ap.add_argument("--profile-grid", type=int, nargs=2, default=[256, 128], metavar=("NX", "NY"),
                     help="grid of the marine-sheet solve that --profile solve runs")
     return ap.parse_args()
@@ -661,6 +665,45 @@ def run_diva(nk, workloads, ctx):
         "coulomb_transition_speed_m_per_yr": transition}), flush=True)
 
 
+def run_halfpipe_adjoint(nk, workloads, ctx):
+    """The STREAMICE halfpipe adjoint (benchmarks/halfpipe_streamice_adjoint.jl:66-99) with the benchmark's tolerances
+    (Picard 1e-8, CG 1e-10, the adjoint at the Picard control): J and ∂J/∂xx at the four centreline cells from
+    nk_checkpointed_gradient, centred differences of the library's forward steps with the benchmark's ε = 0.1 m/yr, and
+    STREAMICE's published values (tests/golden/halfpipe_streamice.json).  Times: one gradient call and one forward run
+    (the three steps alone), wall clock on the host."""
+    with open(os.path.join(ROOT, "tests", "golden", "halfpipe_streamice.json"), encoding="utf-8") as f:
+        spec = json.load(f)
+    weights = spec["control_weights"]
+    cells = [(j - 1, i - 1) for i, j in spec["check_cells_julia"]]
+    P, year, st = workloads.halfpipe_problem(nk.Problem, spec, context=ctx)
+    t0 = time.perf_counter()
+    g = P.checkpointed_gradient(workloads.halfpipe_cost(year), 0.2 * year, 3, melt_weights=weights)
+    t_grad = time.perf_counter() - t0
+
+    def cost(control=None):
+        Q, _, _ = workloads.halfpipe_problem(nk.Problem, spec, context=ctx)
+        return workloads.halfpipe_forward_cost(Q, year, weights, control)
+
+    t0 = time.perf_counter()
+    J = cost()
+    t_fwd = time.perf_counter() - t0
+    rows = []
+    for k, cell in enumerate(cells):
+        xx = np.zeros((spec["Ny"], spec["Nx"]))
+        xx[cell] = 0.1
+        fd = (cost(xx) - cost(-xx)) / 0.2
+        ad = float(g["melt"][cell] / year)
+        sad, sfd = spec["streamice_adjoint_gradient"][k], spec["streamice_finite_difference"][k]
+        rows.append({"cell_julia": list(spec["check_cells_julia"][k]), "adjoint": ad, "finite_difference": fd,
+                     "rel_adjoint_vs_fd": (ad - fd) / abs(fd), "streamice_adjoint": sad, "streamice_finite_difference": sfd,
+                     "ratio_to_streamice_adjoint": ad / sad})
+    print(json.dumps({"metric": "STREAMICE halfpipe adjoint: dJ/dxx through 3 DIVA time steps with a partial-cell front",
+                      "J": g["J"], "J_forward": J, "streamice_cost": spec["streamice_cost"],
+                      "ratio_to_streamice_cost": g["J"] / spec["streamice_cost"], "rows": rows,
+                      "gradient_wall_s": t_grad, "forward_wall_s": t_fwd, "gradient_over_forward": t_grad / t_fwd,
+                      "stats": g["stats"]}), flush=True)
+
+
 def run_scaling(nk, workloads, ctx, problem_cls=None, rows=None, quiet=False):
     """The reference's published multigrid scaling benchmark (benchmarks/multigrid_scaling.jl; its table in
     docs/src/model/numerics.md:42-49, kept in tests/golden/reference_scaling.json): the MISMIP+-like ice stream
@@ -789,6 +832,10 @@ def main():
     if args.scaling:
         if rank == 0:
             run_scaling(nk, workloads, ctx)
+        return
+    if args.halfpipe_adjoint:
+        if rank == 0:
+            run_halfpipe_adjoint(nk, workloads, ctx)
         return
     if args.timestep:
         if rank == 0:

@@ -244,3 +244,74 @@ def halfpipe_streamice(spec, Nsigma=10, velocity_solver=None):
     fields = {"H": H, "bed": bed, "C": np.full_like(H, C ** 2 * year), "A": np.full_like(H, (B ** 2) ** (-n) / year)}
     smb = np.where(X < dx, spec["inflow_m2_per_year"] / year / dx, 0.0)
     return Case("halfpipe_streamice", grid, cfg, fields), smb, year
+
+
+def halfpipe_problem(cls, spec, velocity_solver=None, context=None):
+    """set!(model, H = initial_thickness) of the halfpipe (src/Models/ice_sheet_model_methods.jl:11-20): the fields, the
+    front flagged from H, the geometry, the inflow as the west column's surface mass balance, no melt, and a Picard
+    solve.  Returns (problem, seconds per year, solve stats)."""
+    case, smb, year = halfpipe_streamice(spec, velocity_solver=velocity_solver)
+    P = cls(case.grid, case.descriptors()) if context is None else cls(case.grid, case.descriptors(), context=context)
+    for k, v in case.fields.items():
+        P.set(k, v)
+    P.initialize_front()
+    P.compute_geometry()
+    P.energy_set("surface_mass_balance", smb)
+    P.energy_set("basal_melt_rate", 0.0)
+    P.energy_set("clipped_thickness", 0.0)
+    return P, year, P.picard_solve()
+
+
+def halfpipe_velocity_cost(u, v, mask, year):
+    """velocity_cost of the halfpipe adjoint (benchmarks/halfpipe_streamice_adjoint.jl:35-45): Σ over the full cells
+    (mask 1) of uᶜ² + vᶜ², uᶜ = (u[i, j-1] + u[i, j]) / 2 (0 in the first row) and vᶜ = (v[i-1, j] + v[i, j]) / 2 (0 in
+    the first column) in m/yr, with its gradient in the interior layouts of u and v."""
+    Ny, Nx = mask.shape
+    full = mask == 1
+    uc = np.zeros((Ny, Nx))
+    vc = np.zeros((Ny, Nx))
+    uc[1:, :] = (u[:Ny - 1, :Nx] + u[1:Ny, :Nx]) / 2 * year
+    vc[:, 1:] = (v[:Ny, :Nx - 1] + v[:Ny, 1:Nx]) / 2 * year
+    J = float(np.sum(np.where(full, uc * uc + vc * vc, 0.0)))
+    gu, gv = np.zeros_like(u), np.zeros_like(v)
+    wu = np.where(full, uc, 0.0) * year   # ∂(uᶜ²)/∂u of each of its two faces
+    wv = np.where(full, vc, 0.0) * year
+    gu[:Ny - 1, :Nx] += wu[1:, :]
+    gu[1:Ny, :Nx] += wu[1:, :]
+    gv[:Ny, :Nx - 1] += wv[:, 1:]
+    gv[:Ny, 1:Nx] += wv[:, 1:]
+    return J, gu, gv
+
+
+def halfpipe_cost(year):
+    """The halfpipe adjoint's cost as the callback of Problem.checkpointed_gradient (:47-64): the velocity cost of the
+    state after step 2 (STREAMICE solves the velocity at the start of each step) and Σ H² over the full cells after
+    step 3."""
+    def cost(step, H, u, v, mask):
+        if step == 2:
+            J, gu, gv = halfpipe_velocity_cost(u, v, mask, year)
+            return J, None, gu, gv
+        if step == 3:
+            full = mask == 1
+            return float(np.sum(np.where(full, H * H, 0.0))), np.where(full, 2 * H, 0.0), None, None
+        return None
+    return cost
+
+
+def halfpipe_forward_cost(P, year, weights, control=None):
+    """The same cost from the forward steps alone (adjoint_cost, :47-64), the control xx (m/yr) scaled per step."""
+    Ny, Nx = P.get("H").shape
+    base = np.zeros((Ny, Nx)) if control is None else control / year
+    J = 0.0
+    dt = 0.2 * year
+    for n, w in enumerate(weights):
+        P.energy_set("basal_melt_rate", w * base)
+        if n == 2:
+            J += halfpipe_velocity_cost(P.get("u"), P.get("v"), P.get("ice_mask"), year)[0]
+        for stage in (1, 2, 3):
+            P.step_thickness_stage(dt, stage)
+            st = P.picard_solve()
+            if st.status == 2:
+                raise RuntimeError("non-finite Picard solve")
+    H, mask = P.get("H"), P.get("ice_mask")
+    return J + float(np.sum(np.where(mask == 1, H * H, 0.0)))
