@@ -354,7 +354,11 @@ void launch_advance_front(const FrontView& v, int passes, double dt, size_t plan
     k_front_force<<<d.grid, d.block, 0, s>>>(v, dt); count_launch();
 }
 
-// ---- the reverse of advance_front! without passes or calving (the gradient through time steps) -------------------
+// ---- the reverse of advance_front! without calving (the gradient through time steps) ----------------------------
+// The forward is recorded first (launch_front_record): the drain and the reference pass, then per overflow pass the
+// state before its fill, after its fill and its overflow volumes, and the state before the forced sources.  The
+// reverse runs the forced sources, the passes last first (receive, then fill) and the reference pass, each kernel
+// writing only its own cell's adjoints and gathering its neighbours' shares.
 namespace {
 // full after _empty_drained_cells!: flagged, holding ice and active
 __device__ __forceinline__ bool drained_full(const DevGrid<double>& g, const double* mu, const double* H, int a, int b) {
@@ -395,58 +399,177 @@ __device__ Reference reference_of(const FrontView& v, int i, int j) {
     r.Hbar = r.nin > 0 ? r.Sin / (double)(r.nin > 1 ? r.nin : 1) : Hp;
     return r;
 }
+// the recorded levels: before fill p (p = passes: before the forced sources) H, μ, Hʳ; per pass after its fill H, O
+__device__ __forceinline__ const double* level(const FrontAdjointView& a, int p, int field) {
+    return a.snaps + ((size_t)3 * p + field) * a.plane;
+}
+__device__ __forceinline__ const double* filled(const FrontAdjointView& a, int p, int field) {
+    return a.snaps + ((size_t)3 * (a.passes + 1) + 2 * p + field) * a.plane;
+}
+// overflow donors among the active neighbours of (i, j) in pass p
+__device__ __forceinline__ int donors_of(const FrontAdjointView& a, const double* O, int i, int j) {
+    const DevGrid<double>& g = a.f.g;
+    int n = 0;
+    for (int d = 0; d < 4; ++d) {
+        int x = i + DI(d), y = j + DJ(d);
+        if (!inactive(g, x, y) && O[g.c_idx(x, y)] > 0) ++n;
+    }
+    return n;
+}
 }  // namespace
 
-// Per cell: the reverse of _force_front_cells! (:271-286) and the cell's own terms of the reference pass.
-__global__ void k_front_adjoint_cells(FrontAdjointView a) {
+void launch_front_record(const FrontView& v, int passes, size_t plane, double* snaps, cudaStream_t s) {
+    LaunchDims d = dims2d(v.g.Nx, v.g.Ny);
+    const size_t bytes = plane * sizeof(double);
+    auto keep = [&](double* to, const double* from) { cudaMemcpyAsync(to, from, bytes, cudaMemcpyDeviceToDevice, s); };
+    auto lev = [&](int p, int field) { return snaps + ((size_t)3 * p + field) * plane; };
+    auto fil = [&](int p, int field) { return snaps + ((size_t)3 * (passes + 1) + 2 * p + field) * plane; };
+    k_front_drained<<<d.grid, d.block, 0, s>>>(v); count_launch();
+    k_front_reference<<<d.grid, d.block, 0, s>>>(v); count_launch();
+    keep(lev(0, 0), v.H);
+    keep(lev(0, 1), v.mu);
+    keep(lev(0, 2), v.Hr);
+    for (int p = 0; p < passes; ++p) {
+        keep(v.H_in, v.H);
+        keep(v.mu_in, v.mu);
+        k_front_fill<<<d.grid, d.block, 0, s>>>(v); count_launch();
+        keep(fil(p, 0), v.H);
+        keep(fil(p, 1), v.O);
+        keep(v.H_in, v.H);
+        k_front_receive<<<d.grid, d.block, 0, s>>>(v); count_launch();
+        keep(lev(p + 1, 0), v.H);
+        keep(lev(p + 1, 1), v.mu);
+        keep(lev(p + 1, 2), v.Hr);
+    }
+}
+
+// The reverse of _force_front_cells! (:271-286) on the state before it: λ of H and Hʳ before, and of the sources.
+__global__ void k_front_rev_force(FrontAdjointView a) {
+    const FrontView& v = a.f;
+    const DevGrid<double>& g = v.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int k = g.idx(i, j);
+    const double Hi = level(a, a.passes, 0)[k], Hr = level(a, a.passes, 2)[k];
+    const bool full = level(a, a.passes, 1)[k] > 0;
+    double m = v.grounding ? (1 - v.phi[k]) * v.melt[k] : v.melt[k];
+    double S = v.smb[k] - m;
+    double dt = a.dt;
+    bool forced = (Hi > 0) && (Hr > 0);
+    double Hf = full ? Hi : Hr;
+    bool melted = forced && (Hf + S * dt <= 0);
+    double lH = a.lam_H[k], lR = a.lam_Hr[k];
+    double lHi = 0.0, lHr = 0.0, lS = 0.0;
+    if (melted) {
+        // H and Hʳ become zero: nothing flows back
+    } else if (forced && !full) {   // a partial cell: H (Hʳ + S Δt) / Hʳ, Hʳ + S Δt
+        lHi = lH * (Hr + S * dt) / Hr;
+        lHr = lH * Hi * (-S * dt) / (Hr * Hr) + lR;
+        lS = (lH * Hi / Hr + lR) * dt;
+    } else if (forced) {            // a full cell that filled this step: H + S Δt, Hʳ zero
+        lHi = lH;
+        lS = lH * dt;
+    } else {
+        lHi = lH;
+        lHr = full ? 0.0 : lR;
+    }
+    a.lam_smb[k] += lS;
+    a.lam_melt[k] -= lS * (v.grounding ? 1 - v.phi[k] : 1.0) * a.melt_weight;
+    a.lam_phi[k] = v.grounding ? lS * v.melt[k] : 0.0;
+    a.lam_a[k] = lHi;
+    a.lam_Hr[k] = lHr;
+}
+
+// The reverse of _receive_overflow! (:257-268) of pass p: λ of the thickness after the fill (own and as a donor's
+// mean), of the overflow volumes (as every receiving neighbour's sum) and of Hʳ before the receive.
+__global__ void k_front_rev_receive(FrontAdjointView a, int p) {
+    const DevGrid<double>& g = a.f.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int c = g.idx(i, j);
+    const double* Hf = filled(a, p, 0);
+    const double* O = filled(a, p, 1);
+    const double* mu1 = level(a, p + 1, 1);
+    auto receives = [&](int x, int y) { return empty_at(g, mu1, Hf, x, y); };
+    bool rc = receives(i, j);
+    int nc = donors_of(a, O, i, j);
+    double lHf = rc ? 0.0 : a.lam_a[c];
+    double lHr = (rc && nc > 0) ? 0.0 : a.lam_Hr[c];
+    double lO = 0.0;
+    int seen[4], ns = 0;
+    for (int e = 0; e < 4; ++e) {
+        int x = i + DI(e), y = j + DJ(e);
+        if (inactive(g, x, y)) continue;
+        int k = g.c_idx(x, y);
+        bool dup = false;
+        for (int q = 0; q < ns; ++q) dup |= seen[q] == k;
+        if (dup) continue;
+        seen[ns++] = k;
+        int kx = g.cx(x), ky = g.cy(y);
+        if (!receives(kx, ky)) continue;
+        // how often k reads c among its four neighbours (a short periodic axis can repeat one)
+        int reads = 0;
+        for (int d = 0; d < 4; ++d) {
+            int na = kx + DI(d), nb = ky + DJ(d);
+            if (!inactive(g, na, nb) && g.c_idx(na, nb) == c) ++reads;
+        }
+        lO += reads * a.lam_a[k] / g.Az_cc(kx, ky);
+        int nk = donors_of(a, O, kx, ky);
+        if (nk > 0 && O[c] > 0) lHf += reads * a.lam_Hr[k] / (double)nk;
+    }
+    a.lam_b[c] = lHf;
+    a.lam_c[c] = lO;
+    a.lam_d[c] = lHr;
+}
+
+// The reverse of _fill_front_cells! (:235-251) of pass p on its own cell: λ of the thickness and Hʳ before it.
+__global__ void k_front_rev_fill(FrontAdjointView a, int p) {
+    const DevGrid<double>& g = a.f.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int k = g.idx(i, j);
+    const double* H = level(a, p, 0);
+    const double* mu = level(a, p, 1);
+    const double* Hr = level(a, p, 2);
+    int n = 0;
+    for (int d = 0; d < 4; ++d) n += empty_at(g, mu, H, i + DI(d), j + DJ(d)) ? 1 : 0;
+    bool fills = !(mu[k] > 0) && (Hr[k] > 0) && (H[k] >= Hr[k]);
+    bool spills = fills && n > 0;
+    double lHf = a.lam_b[k], lO = a.lam_c[k];
+    double w = g.Az_cc(i, j) / (double)(n > 1 ? n : 1);
+    a.lam_a[k] = spills ? lO * w : lHf;
+    a.lam_Hr[k] = a.lam_d[k] + (spills ? lHf - lO * w : 0.0);
+}
+
+// Per cell: the cell's own terms of the reference pass (k_front_reference), from λ of H and Hʳ after it.
+__global__ void k_front_rev_reference(FrontAdjointView a) {
     const FrontView& v = a.f;
     const DevGrid<double>& g = v.g;
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i >= g.Nx || j >= g.Ny) return;
     int k = g.idx(i, j);
     Reference r = reference_of(v, i, j);
-    double Hrp = r.full ? 0.0 : r.Hbar;
-    double m = v.grounding ? (1 - v.phi[k]) * v.melt[k] : v.melt[k];
-    double S = v.smb[k] - m;
-    double dt = a.dt;
-    bool forced = (r.Hi > 0) && (Hrp > 0);
-    double Hf = r.full ? r.Hi : Hrp;
-    bool melted = forced && (Hf + S * dt <= 0);
-    double lH = a.lam_H[k], lR = a.lam_Hr[k];
-    double lHi = 0.0, lHrp = 0.0, lS = 0.0;
-    if (melted) {
-        // H and Hʳ become zero: nothing flows back
-    } else if (forced) {   // a partial cell (a full one has Hʳ = 0): H (Hʳ + S Δt) / Hʳ, Hʳ + S Δt
-        lHi = lH * (Hrp + S * dt) / Hrp;
-        lHrp = lH * r.Hi * (-S * dt) / (Hrp * Hrp) + lR;
-        lS = (lH * r.Hi / Hrp + lR) * dt;
-    } else {
-        lHi = lH;
-        lHrp = r.full ? 0.0 : lR;
-    }
-    a.lam_smb[k] += lS;
-    a.lam_melt[k] -= lS * (v.grounding ? 1 - v.phi[k] : 1.0) * a.melt_weight;
-    a.lam_phi[k] = v.grounding ? lS * v.melt[k] : 0.0;
-    // Hʳ = H̄ on a cell not full: the donors' and full neighbours' shares are gathered by k_front_adjoint_gather
-    double lbar = r.full ? 0.0 : lHrp, lHr_old = 0.0;
+    double lHi = a.lam_a[k];
+    // Hʳ = H̄ on a cell not full: the donors' and full neighbours' shares are gathered by k_front_rev_gather
+    double lbar = r.full ? 0.0 : a.lam_Hr[k], lHr_old = 0.0;
     if (r.nin == 0 && r.Hi > 0) {
         if (r.Hr_old > 0) lHr_old = lbar;
         else if (r.nf == 0) lHi += lbar;   // Hˢ = H of the cell itself
     }
-    a.lam_Hrp[k] = lbar;
-    a.lam_Hd[k] = lHi;
+    a.lam_b[k] = lbar;
+    a.lam_c[k] = lHi;
     a.lam_Hr[k] = lHr_old;
 }
 
 // Per cell c: its own part plus the shares of the reference thickness of the neighbours it is a full neighbour of
 // (the donors' mean when any flows in, else the full neighbours' mean when the cell had no Hʳ).
-__global__ void k_front_adjoint_gather(FrontAdjointView a) {
+__global__ void k_front_rev_gather(FrontAdjointView a) {
     const FrontView& v = a.f;
     const DevGrid<double>& g = v.g;
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i >= g.Nx || j >= g.Ny) return;
     int c = g.idx(i, j);
-    double acc = a.lam_Hd[c];
+    double acc = a.lam_c[c];
     if (drained_full(g, v.mu, v.H, i, j)) {
         int seen[4], ns = 0;
         for (int e = 0; e < 4; ++e) {
@@ -457,7 +580,7 @@ __global__ void k_front_adjoint_gather(FrontAdjointView a) {
             for (int q = 0; q < ns; ++q) dup |= seen[q] == kc;
             if (dup) continue;
             seen[ns++] = kc;
-            double lbar = a.lam_Hrp[kc];
+            double lbar = a.lam_b[kc];
             if (lbar == 0.0) continue;
             int ci = g.cx(ki), cj = g.cy(kj);
             Reference r = reference_of(v, ci, cj);
@@ -477,8 +600,13 @@ __global__ void k_front_adjoint_gather(FrontAdjointView a) {
 
 void launch_front_adjoint(const FrontAdjointView& a, cudaStream_t s) {
     LaunchDims d = dims2d(a.f.g.Nx, a.f.g.Ny);
-    k_front_adjoint_cells<<<d.grid, d.block, 0, s>>>(a); count_launch();
-    k_front_adjoint_gather<<<d.grid, d.block, 0, s>>>(a); count_launch();
+    k_front_rev_force<<<d.grid, d.block, 0, s>>>(a); count_launch();
+    for (int p = a.passes - 1; p >= 0; --p) {
+        k_front_rev_receive<<<d.grid, d.block, 0, s>>>(a, p); count_launch();
+        k_front_rev_fill<<<d.grid, d.block, 0, s>>>(a, p); count_launch();
+    }
+    k_front_rev_reference<<<d.grid, d.block, 0, s>>>(a); count_launch();
+    k_front_rev_gather<<<d.grid, d.block, 0, s>>>(a); count_launch();
 }
 
 }  // namespace nk

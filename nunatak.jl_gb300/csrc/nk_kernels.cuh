@@ -266,21 +266,27 @@ struct StageAdjointView {
     const double* lam_phi_in = nullptr;   // λ of φ from elsewhere (the front's forced melt), added before the gather
 };
 void launch_stage_adjoint(const StageAdjointView& a, cudaStream_t s);
-// The reverse of advance_front! without overflow passes or calving (nk_front.cu): the drained flags, the reference
-// thickness Hʳ of the front cells and the sources forced onto them.  f is the front's view at the end of the final
-// stage with f.H the stage's output before the front, f.mu and f.Hr the flag and Hʳ before it, the stage's
-// velocities, the effective melt and φ of the stage's input.
+// The reverse of advance_front! without calving (nk_front.cu).  f is the front's view at the end of the final stage
+// with f.H the stage's output before the front, f.mu and f.Hr the flag and Hʳ before it, the stage's velocities,
+// the effective melt and φ of the stage's input; snaps the advance as launch_front_record recorded it.
 struct FrontAdjointView {
     FrontView f;
+    int passes;
+    const double* snaps;
+    size_t plane;
     double dt, melt_weight;
     const double* lam_H;              // λ of H after the front
     double* lam_Hr;                   // in: λ of Hʳ after the front; out: λ of Hʳ before it
     double* lam_H3;                   // = λ of the stage output before the front
     double* lam_smb; double* lam_melt;   // +=
     double* lam_phi;                  // = λ of φ of the forced cells' melt
-    double* lam_Hrp;                  // scratch: λ of Hʳ after the reference pass
-    double* lam_Hd;                   // scratch: the cell's own part of λ H3
+    double* lam_a; double* lam_b; double* lam_c; double* lam_d;   // scratch planes
 };
+// The drain, the reference pass and the overflow passes of advance_front! on v's planes (v.H, v.mu, v.Hr set by the
+// caller to the state before it), recording into snaps per level p = 0..passes the thickness, flag and Hʳ before
+// fill p (the last level: before the forced sources), then per pass the thickness after its fill and its overflow
+// volumes: 3 (passes + 1) + 2 passes planes.
+void launch_front_record(const FrontView& v, int passes, size_t plane, double* snaps, cudaStream_t s);
 void launch_front_adjoint(const FrontAdjointView& a, cudaStream_t s);
 // y += x over the interior cells of `planes` planes (each `plane` doubles apart)
 void launch_add_planes(const DevGrid<double>& g, double* y, const double* x, int planes, size_t plane, cudaStream_t s);

@@ -2121,13 +2121,18 @@ struct TimeGradient {
     double* mem = nullptr;
     // scratch planes
     double *lamH, *lamHs, *lamH0, *dv, *lamphi, *g_smb, *g_melt, *base_melt, *clipped_end, *g_logC, *g_logA;
-    double *h3pre, *lamHr, *lamHrp, *lamHd, *lamphi_front;   // the front's reverse
+    double *h3pre, *lamHr, *lamphi_front;                    // the front's reverse
+    double* fmem = nullptr;                                     // its record and scratch (front_planes())
     double2 *lamF, *lwx, *lwy, *lamx_stage, *lamx_carry, *lamu_held;
     std::vector<double> hH, hu, hv, hmask, gH, gu, gv;
 
     ~TimeGradient() {
         if (mem) cudaFree(mem);
+        if (fmem) cudaFree(fmem);
     }
+    // the front's reverse: 7 work and adjoint planes, then the record of launch_front_record
+    int front_planes() const { return 7 + 3 * (P->front.passes + 1) + 2 * P->front.passes; }
+    double* fplane(int k) const { return fmem + (size_t)k * pl; }
     double* ckpt(int s) const { return mem + (size_t)s * rp * pl; }
     double* tape(int t) const { return mem + (size_t)(S + t) * rp * pl; }
     double* final_rec() const { return mem + (size_t)(S + 3 * K + 1) * rp * pl; }
@@ -2147,7 +2152,8 @@ struct TimeGradient {
         lamH = one(0); lamHs = one(1); lamH0 = one(2); dv = one(3); lamphi = one(4); g_smb = one(5); g_melt = one(6);
         base_melt = one(7); clipped_end = one(8); g_logC = one(9);
         lamF = two(10); lwx = two(12); lwy = two(14); lamx_stage = two(16); lamx_carry = two(18); lamu_held = two(20);
-        h3pre = one(22); lamHr = one(23); lamHrp = one(24); lamHd = one(25); lamphi_front = one(26);
+        h3pre = one(22); lamHr = one(23); lamphi_front = one(24);
+        if (front) NK_CUDA(cudaMalloc(&fmem, (size_t)front_planes() * pl * sizeof(double)));
         g_logA = one(27);
     }
     void solve() {
@@ -2254,9 +2260,21 @@ struct TimeGradient {
         if (P->advection.scheme == NK_ADVECTION_WENO && P->advection.bounded) launch_thickness_limiter(tv, s);
         launch_thickness_stage(tv, last * d.dt, 1, s);   // P->H = the output before the front (the clip is restored at the end)
         NK_CUDA(cudaMemcpyAsync(h3pre, P->H, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        // the advance again on copies, recorded pass by pass
+        FrontView rec = front_view(P, false);
+        rec.H = fplane(4);
+        rec.mu = fplane(5);
+        rec.Hr = fplane(6);
+        NK_CUDA(cudaMemcpyAsync(rec.H, h3pre, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        NK_CUDA(cudaMemcpyAsync(rec.mu, P->mu, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        NK_CUDA(cudaMemcpyAsync(rec.Hr, P->front_buf, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        launch_front_record(rec, P->front.passes, pl, fplane(7), s);
         FrontAdjointView fa;
         fa.f = front_view(P, false);
         fa.f.H = h3pre;
+        fa.passes = P->front.passes;
+        fa.snaps = fplane(7);
+        fa.plane = pl;
         fa.dt = last * d.dt;
         fa.melt_weight = weight(n);
         fa.lam_H = lamH;
@@ -2265,8 +2283,10 @@ struct TimeGradient {
         fa.lam_smb = g_smb;
         fa.lam_melt = g_melt;
         fa.lam_phi = lamphi_front;
-        fa.lam_Hrp = lamHrp;
-        fa.lam_Hd = lamHd;
+        fa.lam_a = fplane(0);
+        fa.lam_b = fplane(1);
+        fa.lam_c = fplane(2);
+        fa.lam_d = fplane(3);
         launch_front_adjoint(fa, s);
         NK_CHECK_LAUNCH();
     }
@@ -2370,9 +2390,8 @@ nk_status nk_checkpointed_gradient(nk_problem* P, const nk_time_gradient_desc* d
         if (desc->steps < 1) bad("steps must be at least 1");
         if (desc->checkpoint_interval < 0) bad("checkpoint_interval must be non-negative");
         if (desc->velocity_solves != 0 && desc->velocity_solves != 1) bad("velocity_solves is 0 or 1");
-        if (P->front.enabled && (P->front.passes != 0 || P->front.calving != NK_CALVING_NONE))
-            bad("the gradient through time steps covers a partial-cell front without overflow passes or calving "
-                "(PartialCellFront(passes = 0))");
+        if (P->front.enabled && P->front.calving != NK_CALVING_NONE)
+            bad("the gradient through time steps covers a partial-cell front without a calving law");
         if (desc->velocity_solves && P->ud) bad("the gradient through velocity solves is not available with prescribed velocities");
         if (desc->melt_weights)
             for (int n = 0; n < desc->steps; ++n)

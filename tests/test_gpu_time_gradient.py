@@ -344,13 +344,13 @@ def test_refusals(gpu_cls):
         P.checkpointed_gradient(broken, case.dt, 2, velocity_solves=False)
 
 
-# ---- the partial-cell front (test/test_enzyme.jl:490-514, without overflow passes) -----------------------------------
-def channel_front_case():
+# ---- the partial-cell front (test/test_enzyme.jl:490-514) -------------------------------------------------------------
+def channel_front_case(passes=4):
     dx, U, Hi = 1e3, 1.0, 100.0
     grid = M.RectilinearGrid(size=(16, 4), x=(0.0, 16 * dx), y=(0.0, 4 * dx), topology=("Bounded", "Periodic"), halo=(4, 4))
 
     def build(cls):
-        P = make(cls, grid, advection=M.UpwindBiased(order=1), Nsigma=2, masking=M.PartialCellFront(passes=0))
+        P = make(cls, grid, advection=M.UpwindBiased(order=1), Nsigma=2, masking=M.PartialCellFront(passes=passes))
         set_fn(P, "H", lambda x, y: Hi if x < 4 * dx else 0.0)
         P.set("bed", 0.0)
         P.initialize_front()
@@ -365,21 +365,24 @@ def channel_front_case():
     return Case(build, dx / U / 4, 6, solves=False)
 
 
-def test_surface_mass_balance_through_the_partial_cell_front(gpu_cls):
+@pytest.mark.parametrize("passes", [4, 0])
+def test_surface_mass_balance_through_the_partial_cell_front(gpu_cls, passes):
     """∂J/∂a of J = Σ H² after six steps of a front advancing through partially filled cells, at a full cell and at a
-    cell the front reaches (its sources forced onto the partial cell), to 1e-6 (the reference's h = 1e-9)."""
-    case = channel_front_case()
+    cell the front reaches (its sources forced onto the partial cell), to 1e-6 (the reference's h = 1e-9); with the
+    reference's default four overflow passes (filled cells spill their excess into empty neighbours) and without."""
+    case = channel_front_case(passes)
     _, g = gradient(case, gpu_cls)
     assert not np.any(np.isnan(g["smb"]))
     for idx in ((1, 2), (2, 4)):
         _close(g["smb"][idx], fd_final_thickness(case, gpu_cls, "surface_mass_balance", idx, 1e-9), 1e-6)
     H0 = case.build(gpu_cls).get("H")
-    _close(g["H"][1, 2], fd_final_thickness(case, gpu_cls, "H", (1, 2), 1e-6 * H0[1, 2]), 1e-6)
+    for idx in ((1, 2), (2, 3)):   # (2, 3): the last full cell, the inflowing donor of the first front cell
+        _close(g["H"][idx], fd_final_thickness(case, gpu_cls, "H", idx, 1e-6 * H0[idx]), 1e-6)
 
 
-def test_front_passes_are_refused(gpu_cls):
+def test_front_calving_is_refused(gpu_cls):
     case = channel_front_case()
     P = case.build(gpu_cls)
-    P.set_front(M.PartialCellFront(passes=2))
+    P.set_front(M.PartialCellFront(passes=2, calving=M.ThicknessThresholdCalving(thickness=50.0)))
     with pytest.raises(Exception):
         P.checkpointed_gradient(thickness_cost(2), case.dt, 2, velocity_solves=False)
