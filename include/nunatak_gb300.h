@@ -495,9 +495,9 @@ nk_status nk_picard_adjoint_gradients(nk_problem* problem, const double* ubar, c
  * and its gradient in a callback; the library returns J and its gradient with respect to the thickness and the
  * velocities at the start, the surface mass balance, the basal melt rate, and, with velocity solves, log C and log A.
  *
- * The forward run stores the state (H, U, V, and for the DIVA its lagged beta_b and F2) every checkpoint_interval
- * steps; the reverse pass restores each checkpoint, re-runs its segment storing every stage's state, and runs the
- * segment backwards: the cost's gradient at each step end, the fixed-point Picard adjoint of each velocity solve
+ * The forward run stores the state (H, U, V, a front's flag and H_r, and for the DIVA its lagged beta_b, F2 and
+ * eta_sigma) every checkpoint_interval steps; the reverse pass restores each checkpoint, re-runs its segment storing
+ * every stage's state, and runs the segment backwards: the cost's gradient at each step end, the fixed-point Picard adjoint of each velocity solve
  * (nk_picard_adjoint_gradients: λ of the velocities to ∂J/∂H, log C, log A) and the reverse of each stage (the clip,
  * the sources, the fluxes, the bounds-preserving limiter, the WENO or upwind reconstructions and the centre grounded
  * fraction of the floating melt; nk_time_adjoint.cu).  Only one segment's stages are held at a time.  The problem is
@@ -505,9 +505,10 @@ nk_status nk_picard_adjoint_gradients(nk_problem* problem, const double* ubar, c
  *
  * The initial velocities are an input, as the model's stored velocities are for the reference (their gradient is
  * the shadow of the velocity fields); the geometry is recomputed from the initial H.  Discrete switches (the clip, the
- * upwind direction, the limiter's branch, walls and masks) are held where the forward run put them.  Not covered:
- * a partial-cell front (refused), the energy step and its grounded-melt coupling (the stages run uncoupled), and
- * prescribed velocities with velocity solves (refused, as for nk_picard_adjoint). */
+ * upwind direction, the limiter's branch, walls, masks and the front's flags) are held where the forward run put them;
+ * a partial-cell front's advance (its overflow passes included) is reversed with the stages.  Not covered: a calving
+ * law (refused), the energy step and its grounded-melt coupling (the stages run uncoupled), and prescribed velocities
+ * with velocity solves (refused, as for nk_picard_adjoint). */
 typedef struct nk_cost_state {
     int32_t step;              /* the state after this many steps, 1..steps */
     int32_t steps;
