@@ -86,6 +86,7 @@ def test_null_handles_are_refused(lib):
         "nk_batch_picard_solve_async": lambda: lib.nk_batch_picard_solve_async(null, None),
         "nk_batch_query": lambda: lib.nk_batch_query(null, C.byref(i32)),
         "nk_batch_wait": lambda: lib.nk_batch_wait(null, null),
+        "nk_checkpointed_gradient": lambda: lib.nk_checkpointed_gradient(null, null, abi.COST_FN(), null, null, null),
     }
     got = {name: f() for name, f in calls.items()}
     assert got == {name: bad for name in calls}

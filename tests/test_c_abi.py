@@ -71,6 +71,10 @@ int main(void) {
     S(nk_request) F(nk_request, physics) F(nk_request, solver) F(nk_request, H) F(nk_request, v_out)
     S(nk_thermal_params) F(nk_thermal_params, water_softening_coefficient) F(nk_thermal_params, reference_temperature)
     S(nk_energy_params) F(nk_energy_params, maximum_drainage_rate) F(nk_energy_params, grounded_melt_coupling) F(nk_energy_params, reserved)
+    S(nk_cost_state) F(nk_cost_state, H) F(nk_cost_state, ice_mask)
+    S(nk_time_gradient_desc) F(nk_time_gradient_desc, steps) F(nk_time_gradient_desc, melt_weights) F(nk_time_gradient_desc, adjoint_control)
+    S(nk_time_gradient) F(nk_time_gradient, grad_log_A)
+    S(nk_time_gradient_stats) F(nk_time_gradient_stats, worst_solve_status) F(nk_time_gradient_stats, elapsed_ms)
     return 0;
 }
 """
@@ -92,7 +96,8 @@ def test_ctypes_mirrors_match_the_c_layout(tmp_path):
     mirrors = {"nk_iteration_control": abi.IterationControl, "nk_grid_desc": abi.GridDesc, "nk_physics_desc": abi.PhysicsDesc,
                "nk_solver_desc": abi.SolverDesc, "nk_solve_stats": abi.SolveStats, "nk_server_desc": abi.ServerDesc,
                "nk_request": abi.Request, "nk_thermal_params": abi.ThermalParams,
-               "nk_energy_params": abi.EnergyParams}
+               "nk_energy_params": abi.EnergyParams, "nk_cost_state": abi.CostState, "nk_time_gradient_desc": abi.TimeGradientDesc,
+               "nk_time_gradient": abi.TimeGradient, "nk_time_gradient_stats": abi.TimeGradientStats}
     checked = 0
     for line in filter(None, out):
         parts = line.split()
@@ -104,4 +109,4 @@ def test_ctypes_mirrors_match_the_c_layout(tmp_path):
         else:
             assert ctypes.sizeof(mirrors[parts[0]]) == int(parts[1]), parts
         checked += 1
-    assert checked == 35
+    assert checked == 47
