@@ -506,9 +506,9 @@ nk_status nk_picard_adjoint_gradients(nk_problem* problem, const double* ubar, c
  * The initial velocities are an input, as the model's stored velocities are for the reference (their gradient is
  * the shadow of the velocity fields); the geometry is recomputed from the initial H.  Discrete switches (the clip, the
  * upwind direction, the limiter's branch, walls, masks and the front's flags) are held where the forward run put them;
- * a partial-cell front's advance (its overflow passes included) is reversed with the stages.  Not covered: a calving
- * law (refused), the energy step and its grounded-melt coupling (the stages run uncoupled), and prescribed velocities
- * with velocity solves (refused, as for nk_picard_adjoint). */
+ * a partial-cell front's advance (its overflow passes and its calving included) is reversed with the stages.  Not
+ * covered: von Mises calving (refused), the energy step and its grounded-melt coupling (the stages run uncoupled),
+ * and prescribed velocities with velocity solves (refused, as for nk_picard_adjoint). */
 typedef struct nk_cost_state {
     int32_t step;              /* the state after this many steps, 1..steps */
     int32_t steps;

@@ -406,6 +406,14 @@ __device__ __forceinline__ const double* level(const FrontAdjointView& a, int p,
 __device__ __forceinline__ const double* filled(const FrontAdjointView& a, int p, int field) {
     return a.snaps + ((size_t)3 * (a.passes + 1) + 2 * p + field) * a.plane;
 }
+// the calving block: 0 fraction, 1-3 H, μ, Hʳ after the retreat, 4 its residual, 5 the shares, 6-8 after the receive
+__device__ __forceinline__ const double* calved(const FrontAdjointView& a, int field) {
+    return a.snaps + ((size_t)3 * (a.passes + 1) + 2 * a.passes + field) * a.plane;
+}
+// the state the forced sources read: after the calving, else after the last pass
+__device__ __forceinline__ const double* forced_level(const FrontAdjointView& a, int field) {
+    return a.f.law != NK_CALVING_NONE ? calved(a, 6 + field) : level(a, a.passes, field);
+}
 // overflow donors among the active neighbours of (i, j) in pass p
 __device__ __forceinline__ int donors_of(const FrontAdjointView& a, const double* O, int i, int j) {
     const DevGrid<double>& g = a.f.g;
@@ -418,7 +426,9 @@ __device__ __forceinline__ int donors_of(const FrontAdjointView& a, const double
 }
 }  // namespace
 
-void launch_front_record(const FrontView& v, int passes, size_t plane, double* snaps, cudaStream_t s) {
+int front_record_planes(int passes, int law) { return 3 * (passes + 1) + 2 * passes + (law != NK_CALVING_NONE ? 9 : 0); }
+
+void launch_front_record(const FrontView& v, int passes, size_t plane, double* snaps, double dt, cudaStream_t s) {
     LaunchDims d = dims2d(v.g.Nx, v.g.Ny);
     const size_t bytes = plane * sizeof(double);
     auto keep = [&](double* to, const double* from) { cudaMemcpyAsync(to, from, bytes, cudaMemcpyDeviceToDevice, s); };
@@ -441,6 +451,23 @@ void launch_front_record(const FrontView& v, int passes, size_t plane, double* s
         keep(lev(p + 1, 1), v.mu);
         keep(lev(p + 1, 2), v.Hr);
     }
+    if (v.law != NK_CALVING_NONE) {
+        double* c = snaps + ((size_t)3 * (passes + 1) + 2 * passes) * plane;
+        auto cal = [&](int field) { return c + (size_t)field * plane; };
+        k_calve_fraction<<<d.grid, d.block, 0, s>>>(v, dt); count_launch();
+        keep(cal(0), v.f);
+        k_calve_retreat<<<d.grid, d.block, 0, s>>>(v); count_launch();
+        keep(cal(1), v.H);
+        keep(cal(2), v.mu);
+        keep(cal(3), v.Hr);
+        keep(cal(4), v.f);
+        k_calve_share<<<d.grid, d.block, 0, s>>>(v); count_launch();
+        keep(cal(5), v.share);
+        k_calve_receive<<<d.grid, d.block, 0, s>>>(v); count_launch();
+        keep(cal(6), v.H);
+        keep(cal(7), v.mu);
+        keep(cal(8), v.Hr);
+    }
 }
 
 // The reverse of _force_front_cells! (:271-286) on the state before it: λ of H and Hʳ before, and of the sources.
@@ -450,8 +477,8 @@ __global__ void k_front_rev_force(FrontAdjointView a) {
     int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
     if (i >= g.Nx || j >= g.Ny) return;
     int k = g.idx(i, j);
-    const double Hi = level(a, a.passes, 0)[k], Hr = level(a, a.passes, 2)[k];
-    const bool full = level(a, a.passes, 1)[k] > 0;
+    const double Hi = forced_level(a, 0)[k], Hr = forced_level(a, 2)[k];
+    const bool full = forced_level(a, 1)[k] > 0;
     double m = v.grounding ? (1 - v.phi[k]) * v.melt[k] : v.melt[k];
     double S = v.smb[k] - m;
     double dt = a.dt;
@@ -598,9 +625,326 @@ __global__ void k_front_rev_gather(FrontAdjointView a) {
     a.lam_H3[c] = acc;
 }
 
+// ---- the reverse of the calving (calve_front!, :300-397) for the rate laws and the removal laws -------------------
+namespace {
+// a value and its derivative along one seeded face velocity
+struct Dual {
+    double v, d;
+};
+__device__ __forceinline__ Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
+__device__ __forceinline__ Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
+__device__ __forceinline__ Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+__device__ __forceinline__ Dual operator*(double s, Dual a) { return {s * a.v, s * a.d}; }
+__device__ __forceinline__ Dual operator/(Dual a, double s) { return {a.v / s, a.d / s}; }
+__device__ __forceinline__ Dual operator/(Dual a, Dual b) { return {a.v / b.v, (a.d * b.v - a.v * b.d) / (b.v * b.v)}; }
+__device__ __forceinline__ Dual dsqrt(Dual a) { double r = sqrt(a.v); return {r, r > 0 ? a.d / (2 * r) : 0.0}; }
+__device__ __forceinline__ Dual dabs(Dual a) { return a.v >= 0 ? a : Dual{-a.v, -a.d}; }
+__device__ __forceinline__ Dual dmax(Dual a, Dual b) { return fmax(a.v, b.v) == a.v ? a : b; }
+__device__ __forceinline__ Dual dpos(Dual a) { return a.v > 0 ? a : Dual{0.0, 0.0}; }   // fmax(a, 0)
+
+// The flag-masked face velocities of mu_u / mu_v with the seed's derivative: seed_u / seed_v is the stored index of
+// the seeded u / v face (-1: none).
+struct Seed {
+    int u, v;
+};
+__device__ __forceinline__ Dual dmu_u(const FrontView& v, int i, int j, Seed sd) {
+    const DevGrid<double>& g = v.g;
+    if (g.peripheral_fc(i, j) || (v.mu[g.c_idx(i - 1, j)] + v.mu[g.c_idx(i, j)]) == 0.0) return {0.0, 0.0};
+    int k = g.u_idx(i, j);
+    return {v.x[k].x, k == sd.u ? 1.0 : 0.0};
+}
+__device__ __forceinline__ Dual dmu_v(const FrontView& v, int i, int j, Seed sd) {
+    const DevGrid<double>& g = v.g;
+    if (g.peripheral_cf(i, j) || (v.mu[g.c_idx(i, j - 1)] + v.mu[g.c_idx(i, j)]) == 0.0) return {0.0, 0.0};
+    int k = g.v_idx(i, j);
+    return {v.x[k].y, k == sd.v ? 1.0 : 0.0};
+}
+__device__ __forceinline__ Dual dstrain_xy(const FrontView& v, int i, int j, Seed sd) {
+    const DevGrid<double>& g = v.g;
+    Dual dudy = (dmu_u(v, i, j, sd) - dmu_u(v, i, j - 1, sd)) / g.dyf[j];
+    Dual dvdx = (dmu_v(v, i, j, sd) - dmu_v(v, i - 1, j, sd)) / g.dxf[i];
+    Dual e = (dudy + dvdx) / 2.0;
+    return g.peripheral_ff(i, j) ? v.wall_factor * e : e;
+}
+// calving_rate of a full cell (calving.jl:154-190) for the eigencalving and front-velocity laws, with the seed's
+// derivative (principal_strain_rates and front_flow_speed as k_calve_fraction evaluates them)
+__device__ Dual dcalving_rate(const FrontView& v, int i, int j, Seed sd) {
+    const DevGrid<double>& g = v.g;
+    if (v.law == NK_CALVING_EIGEN) {
+        Dual exx = (dmu_u(v, i + 1, j, sd) - dmu_u(v, i, j, sd)) / g.dxc[i];
+        Dual eyy = (dmu_v(v, i, j + 1, sd) - dmu_v(v, i, j, sd)) / g.dyc[j];
+        Dual exy = ((dstrain_xy(v, i, j, sd) + dstrain_xy(v, i + 1, j, sd)) / 2.0 +
+                    (dstrain_xy(v, i, j + 1, sd) + dstrain_xy(v, i + 1, j + 1, sd)) / 2.0) / 2.0;
+        Dual eb = (exx + eyy) / 2.0;
+        Dual h = (exx - eyy) / 2.0;
+        Dual r = dsqrt(h * h + exy * exy + Dual{v.eps0 * v.eps0, 0.0});
+        return v.coefficient * (dpos(eb + r) * dpos(eb - r));
+    }
+    if (v.law == NK_CALVING_FRONT_VELOCITY) {
+        Dual ut = dmax(dabs(dmu_u(v, i, j, sd)), dabs(dmu_u(v, i + 1, j, sd)));
+        Dual vt = dmax(dabs(dmu_v(v, i, j, sd)), dabs(dmu_v(v, i, j + 1, sd)));
+        double e = v.eps0 * g.dxc[i];
+        Dual fs = dsqrt(ut * ut + vt * vt + Dual{e * e, 0.0});
+        return (1 - v.phi[g.c_idx(i, j)]) * dpos(fs - Dual{v.front_velocity, 0.0});
+    }
+    return {0.0, 0.0};
+}
+// The ocean-facing lengths of cell (i, j) and its front length l (k_calve_fraction), with the seed's derivative
+struct FrontLength {
+    double lw, le, ls, ln;
+    bool facing;
+};
+__device__ FrontLength front_lengths(const FrontView& v, int i, int j) {
+    const DevGrid<double>& g = v.g;
+    double dx = g.dxc[i], dy = g.dyc[j];
+    auto ocean = [&](int a, int b, double len) { return (empty_at(g, v.mu, v.H, a, b) && v.bed[g.c_idx(a, b)] < 0) ? len : 0.0; };
+    FrontLength f;
+    f.lw = ocean(i - 1, j, dy);
+    f.le = ocean(i + 1, j, dy);
+    f.ls = ocean(i, j - 1, dx);
+    f.ln = ocean(i, j + 1, dx);
+    f.facing = f.lw + f.le + f.ls + f.ln > 0;
+    return f;
+}
+__device__ Dual dfront_length(const FrontView& v, int i, int j, const FrontLength& f, Seed sd) {
+    Dual ub = dabs((dmu_u(v, i, j, sd) + dmu_u(v, i + 1, j, sd)) / 2.0);
+    Dual vb = dabs((dmu_v(v, i, j, sd) + dmu_v(v, i, j + 1, sd)) / 2.0);
+    Dual speed = dsqrt(ub * ub + vb * vb);
+    if (!(speed.v > 0)) {
+        double l2 = (f.le - f.lw) * (f.le - f.lw) + (f.ln - f.ls) * (f.ln - f.ls);
+        return {l2 > 0 ? sqrt(l2) : f.lw + f.le + f.ls + f.ln, 0.0};
+    }
+    return (Dual{f.lw + f.le, 0.0} * ub + Dual{f.ls + f.ln, 0.0} * vb) / speed;
+}
+__device__ __forceinline__ bool rate_law(int law) { return law == NK_CALVING_EIGEN || law == NK_CALVING_FRONT_VELOCITY; }
+__device__ __forceinline__ bool removal_law(int law) {
+    return law == NK_CALVING_THICKNESS_THRESHOLD || law == NK_CALVING_MAXIMUM_EXTENT;
+}
+// remove_front_fraction! (:353-368) of a cell with thickness H, flag mu and Hʳ Hr by the fraction g: the reverse from
+// λ of H and Hʳ after it and of its residual (times w) to λ of H, Hʳ and g.
+__device__ __forceinline__ void remove_fraction_reverse(double H, double mu, double Hr, double gfrac, double lH, double lR,
+                                                        double lres, double w, double& oH, double& oR, double& og) {
+    bool own = (mu > 0) || !(Hr > 0);      // front_ice_thickness: its own thickness, else Hʳ
+    double Hf = own ? H : Hr;
+    bool calves = (gfrac > 0) && (H > 0);
+    oH = oR = og = 0.0;
+    if (!calves) {
+        oH = lH;
+        oR = lR;
+        return;
+    }
+    double lHf = 0.0;
+    double Hn = H - gfrac * Hf;
+    if (Hn > 0) {           // H = H - g Hf, Hʳ = Hf
+        oH += lH;
+        lHf += -gfrac * lH + lR;
+        og += -Hf * lH;
+    }
+    double a = Hf > 0 ? H / Hf : 0.0;
+    if (lres != 0.0 && Hf > 0 && gfrac - a > 0) {   // residual max(g - H / Hf, 0) w
+        og += lres * w;
+        double la = -lres * w;
+        oH += la / Hf;
+        lHf += -la * H / (Hf * Hf);
+    }
+    if (own) oH += lHf; else oR += lHf;
+}
+}  // namespace
+
+// The reverse of _receive_residual_retreat! (:390-397): the received fraction A / Az removed from the cell after the
+// retreat; its λ goes to each neighbour's share.
+__global__ void k_calve_rev_receive(FrontAdjointView a) {
+    const DevGrid<double>& g = a.f.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int k = g.idx(i, j);
+    const double* share = calved(a, 5);
+    double A = 0;
+    for (int d = 0; d < 4; ++d) {
+        int x = i + DI(d), y = j + DJ(d);
+        A += inactive(g, x, y) ? 0.0 : share[g.c_idx(x, y)];
+    }
+    double Az = g.Az_cc(i, j);
+    double oH, oR, og;
+    remove_fraction_reverse(calved(a, 1)[k], calved(a, 2)[k], calved(a, 3)[k], A / Az, a.lam_a[k], a.lam_Hr[k], 0.0, 0.0, oH, oR, og);
+    a.lam_b[k] = oH;
+    a.lam_d[k] = oR;
+    a.lam_c[k] = og / Az;   // λ of the received A
+}
+
+// The reverse of _share_residual_retreat! (:379-385) and _retreat_front_cells! (:371-375) of cell c: λ of its residual
+// from the neighbours that received its shares, then back through its retreat by its own fraction.
+__global__ void k_calve_rev_retreat(FrontAdjointView a) {
+    const DevGrid<double>& g = a.f.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int c = g.idx(i, j);
+    const double* H1 = calved(a, 1);
+    int n = 0;
+    double lshare = 0.0;
+    int seen[4], ns = 0;
+    for (int e = 0; e < 4; ++e) {
+        int x = i + DI(e), y = j + DJ(e);
+        if (inactive(g, x, y)) continue;
+        int k = g.c_idx(x, y);
+        n += H1[k] > 0 ? 1 : 0;
+        bool dup = false;
+        for (int q = 0; q < ns; ++q) dup |= seen[q] == k;
+        if (dup) continue;
+        seen[ns++] = k;
+        int kx = g.cx(x), ky = g.cy(y), reads = 0;
+        for (int d = 0; d < 4; ++d) {
+            int na = kx + DI(d), nb = ky + DJ(d);
+            if (!inactive(g, na, nb) && g.c_idx(na, nb) == c) ++reads;
+        }
+        lshare += reads * a.lam_c[k];
+    }
+    double lres = n > 0 ? lshare / (double)n : 0.0;   // share = residual / n over the neighbours holding ice
+    double w = removal_law(a.f.law) ? 0.0 : g.Az_cc(i, j);
+    double oH, oR, og;
+    remove_fraction_reverse(level(a, a.passes, 0)[c], level(a, a.passes, 1)[c], level(a, a.passes, 2)[c], calved(a, 0)[c],
+                            a.lam_b[c], a.lam_d[c], lres, w, oH, oR, og);
+    a.lam_a[c] = oH;
+    a.lam_Hr[c] = oR;
+    a.lam_e[c] = og;   // λ of the retreat fraction
+}
+
+// The reverse of _compute_retreat_fraction! (:311-322) for the rate laws: r = min(1, c Δt l / Az) gives λ of the cell's
+// rate as used (its own, or a partial cell's mean of its full neighbours') and of its front length.
+__global__ void k_calve_rev_fraction(FrontAdjointView a) {
+    FrontView v = a.f;
+    const DevGrid<double>& g = v.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int k = g.idx(i, j);
+    v.H = const_cast<double*>(level(a, a.passes, 0));
+    v.mu = const_cast<double*>(level(a, a.passes, 1));
+    v.Hr = const_cast<double*>(level(a, a.passes, 2));
+    double lc = 0.0, ll = 0.0;
+    FrontLength f = front_lengths(v, i, j);
+    double lr = a.lam_e[k];
+    if (rate_law(v.law) && v.H[k] > 0 && f.facing && lr != 0.0) {
+        Seed none{-1, -1};
+        double c;
+        if (v.mu[k] > 0) {
+            c = dcalving_rate(v, i, j, none).v;
+        } else {
+            double S = 0;
+            int n = 0;
+            for (int d = 0; d < 4; ++d)
+                if (full_neighbor(g, v.mu, i + DI(d), j + DJ(d))) { S += dcalving_rate(v, i + DI(d), j + DJ(d), none).v; ++n; }
+            c = S / (double)(n > 1 ? n : 1);
+        }
+        double l = dfront_length(v, i, j, f, none).v;
+        if (c * a.dt * l / g.Az_cc(i, j) < 1.0) {
+            double lcl = lr * a.dt / g.Az_cc(i, j);
+            lc = lcl * l;
+            ll = lcl * c;
+        }
+    }
+    a.lam_f[k] = lc;
+    a.lam_h[k] = ll;
+}
+
+// λ of each cell's computed rate: its own use when full, and its share in the partial neighbours' means.
+__global__ void k_calve_rev_rate(FrontAdjointView a) {
+    const DevGrid<double>& g = a.f.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i >= g.Nx || j >= g.Ny) return;
+    int k = g.idx(i, j);
+    const double* mu = level(a, a.passes, 1);
+    double acc = 0.0;
+    if (mu[k] > 0) {
+        acc = a.lam_f[k];
+        int seen[4], ns = 0;
+        for (int e = 0; e < 4; ++e) {
+            int x = i + DI(e), y = j + DJ(e);
+            if (inactive(g, x, y)) continue;
+            int p = g.c_idx(x, y);
+            bool dup = false;
+            for (int q = 0; q < ns; ++q) dup |= seen[q] == p;
+            if (dup || mu[p] > 0 || a.lam_f[p] == 0.0) continue;
+            seen[ns++] = p;
+            int px = g.cx(x), py = g.cy(y), n = 0, reads = 0;
+            for (int d = 0; d < 4; ++d) {
+                int na = px + DI(d), nb = py + DJ(d);
+                if (full_neighbor(g, mu, na, nb)) {
+                    ++n;
+                    if (g.c_idx(na, nb) == k) ++reads;
+                }
+            }
+            if (n > 0) acc += reads * a.lam_f[p] / (double)n;
+        }
+    }
+    a.lam_g[k] = acc;
+}
+
+// λ of the face velocities: per face, every cell whose rate or front length reads it (cells within one column and
+// row of the face), each differentiated along that face.  The front-velocity law's (1 - φ) sends λ to φ too.
+__global__ void k_calve_rev_velocity(FrontAdjointView a) {
+    FrontView v = a.f;
+    const DevGrid<double>& g = v.g;
+    int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+    if (i > g.Nx || j > g.Ny) return;
+    int k = g.idx(i, j);
+    v.H = const_cast<double*>(level(a, a.passes, 0));
+    v.mu = const_cast<double*>(level(a, a.passes, 1));
+    v.Hr = const_cast<double*>(level(a, a.passes, 2));
+    double2 out = a.lam_x[k];
+    for (int comp = 0; comp < 2; ++comp) {
+        bool has = comp == 0 ? (j < g.Ny && (i < g.Nx || !g.px)) : (i < g.Nx && (j < g.Ny || !g.py));
+        if (!has) continue;
+        Seed sd{comp == 0 ? k : -1, comp == 1 ? k : -1};
+        int ilo = comp == 0 ? i - 1 : i - 1, ihi = comp == 0 ? i : i + 1;
+        int jlo = comp == 0 ? j - 1 : j - 1, jhi = comp == 0 ? j + 1 : j;
+        double acc = 0.0;
+        int seen[9], ns = 0;
+        for (int y = jlo; y <= jhi; ++y)
+            for (int x = ilo; x <= ihi; ++x) {
+                if (inactive(g, x, y)) continue;
+                int c = g.c_idx(x, y);
+                bool dup = false;
+                for (int q = 0; q < ns; ++q) dup |= seen[q] == c;
+                if (dup) continue;
+                seen[ns++] = c;
+                int cx = g.cx(x), cy = g.cy(y);
+                if (a.lam_g[c] != 0.0) acc += a.lam_g[c] * dcalving_rate(v, cx, cy, sd).d;
+                if (a.lam_h[c] != 0.0) {
+                    FrontLength f = front_lengths(v, cx, cy);
+                    acc += a.lam_h[c] * dfront_length(v, cx, cy, f, sd).d;
+                }
+            }
+        if (comp == 0) out.x += acc; else out.y += acc;
+    }
+    a.lam_x[k] = out;
+    // φ of the front-velocity law, per cell (each cell once)
+    if (v.law == NK_CALVING_FRONT_VELOCITY && i < g.Nx && j < g.Ny && a.lam_g[k] != 0.0) {
+        Seed none{-1, -1};
+        double c1 = 1 - v.phi[k];
+        double c = dcalving_rate(v, i, j, none).v;
+        if (c1 > 0) a.lam_phi[k] += -a.lam_g[k] * c / c1;
+        else {
+            // (1 - φ) = 0: the rate's φ derivative is −max(fs − v_f, 0), recomputed
+            Dual ut = dmax(dabs(dmu_u(v, i, j, none)), dabs(dmu_u(v, i + 1, j, none)));
+            Dual vt = dmax(dabs(dmu_v(v, i, j, none)), dabs(dmu_v(v, i, j + 1, none)));
+            double e = v.eps0 * g.dxc[i];
+            double fs = sqrt(ut.v * ut.v + vt.v * vt.v + e * e);
+            a.lam_phi[k] += -a.lam_g[k] * fmax(fs - v.front_velocity, 0.0);
+        }
+    }
+}
+
 void launch_front_adjoint(const FrontAdjointView& a, cudaStream_t s) {
     LaunchDims d = dims2d(a.f.g.Nx, a.f.g.Ny);
     k_front_rev_force<<<d.grid, d.block, 0, s>>>(a); count_launch();
+    if (a.f.law != NK_CALVING_NONE) {
+        LaunchDims df = dims2d(a.f.g.Nx + 1, a.f.g.Ny + 1);
+        k_calve_rev_receive<<<d.grid, d.block, 0, s>>>(a); count_launch();
+        k_calve_rev_retreat<<<d.grid, d.block, 0, s>>>(a); count_launch();
+        k_calve_rev_fraction<<<d.grid, d.block, 0, s>>>(a); count_launch();
+        k_calve_rev_rate<<<d.grid, d.block, 0, s>>>(a); count_launch();
+        k_calve_rev_velocity<<<df.grid, df.block, 0, s>>>(a); count_launch();
+    }
     for (int p = a.passes - 1; p >= 0; --p) {
         k_front_rev_receive<<<d.grid, d.block, 0, s>>>(a, p); count_launch();
         k_front_rev_fill<<<d.grid, d.block, 0, s>>>(a, p); count_launch();

@@ -281,12 +281,18 @@ struct FrontAdjointView {
     double* lam_smb; double* lam_melt;   // +=
     double* lam_phi;                  // = λ of φ of the forced cells' melt
     double* lam_a; double* lam_b; double* lam_c; double* lam_d;   // scratch planes
+    // calving (f.law a rate law or a removal law; von Mises is not covered): λ of the retreat fraction, of each
+    // cell's calving rate as used and as computed, of its ocean-facing length, and the λ of the velocities it adds
+    double* lam_e; double* lam_f; double* lam_g; double* lam_h;
+    double2* lam_x;
 };
-// The drain, the reference pass and the overflow passes of advance_front! on v's planes (v.H, v.mu, v.Hr set by the
-// caller to the state before it), recording into snaps per level p = 0..passes the thickness, flag and Hʳ before
-// fill p (the last level: before the forced sources), then per pass the thickness after its fill and its overflow
-// volumes: 3 (passes + 1) + 2 passes planes.
-void launch_front_record(const FrontView& v, int passes, size_t plane, double* snaps, cudaStream_t s);
+// The drain, the reference pass, the overflow passes and the calving of advance_front! on v's planes (v.H, v.mu, v.Hr
+// set by the caller to the state before it), recording into snaps (front_record_planes of them): per level
+// p = 0..passes the thickness, flag and Hʳ before fill p, then per pass the thickness after its fill and its overflow
+// volumes, then with a calving law the retreat fraction, the thickness, flag and Hʳ after the retreat, its residual,
+// the shares, and the thickness, flag and Hʳ after the receive (before the forced sources).
+int front_record_planes(int passes, int law);
+void launch_front_record(const FrontView& v, int passes, size_t plane, double* snaps, double dt, cudaStream_t s);
 void launch_front_adjoint(const FrontAdjointView& a, cudaStream_t s);
 // y += x over the interior cells of `planes` planes (each `plane` doubles apart)
 void launch_add_planes(const DevGrid<double>& g, double* y, const double* x, int planes, size_t plane, cudaStream_t s);

@@ -2130,8 +2130,9 @@ struct TimeGradient {
         if (mem) cudaFree(mem);
         if (fmem) cudaFree(fmem);
     }
-    // the front's reverse: 7 work and adjoint planes, then the record of launch_front_record
-    int front_planes() const { return 7 + 3 * (P->front.passes + 1) + 2 * P->front.passes; }
+    // the front's reverse: 13 work and adjoint planes (the last two one pair plane), then launch_front_record's record
+    int front_planes() const { return 13 + front_record_planes(P->front.passes, P->front.calving); }
+    double2* front_lamx() const { return reinterpret_cast<double2*>(fplane(11)); }
     double* fplane(int k) const { return fmem + (size_t)k * pl; }
     double* ckpt(int s) const { return mem + (size_t)s * rp * pl; }
     double* tape(int t) const { return mem + (size_t)(S + t) * rp * pl; }
@@ -2268,12 +2269,12 @@ struct TimeGradient {
         NK_CUDA(cudaMemcpyAsync(rec.H, h3pre, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
         NK_CUDA(cudaMemcpyAsync(rec.mu, P->mu, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
         NK_CUDA(cudaMemcpyAsync(rec.Hr, P->front_buf, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
-        launch_front_record(rec, P->front.passes, pl, fplane(7), s);
+        launch_front_record(rec, P->front.passes, pl, fplane(13), last * d.dt, s);
         FrontAdjointView fa;
         fa.f = front_view(P, false);
         fa.f.H = h3pre;
         fa.passes = P->front.passes;
-        fa.snaps = fplane(7);
+        fa.snaps = fplane(13);
         fa.plane = pl;
         fa.dt = last * d.dt;
         fa.melt_weight = weight(n);
@@ -2287,6 +2288,12 @@ struct TimeGradient {
         fa.lam_b = fplane(1);
         fa.lam_c = fplane(2);
         fa.lam_d = fplane(3);
+        fa.lam_e = fplane(7);
+        fa.lam_f = fplane(8);
+        fa.lam_g = fplane(9);
+        fa.lam_h = fplane(10);
+        fa.lam_x = front_lamx();
+        NK_CUDA(cudaMemsetAsync(fa.lam_x, 0, pl * sizeof(double2), s));
         launch_front_adjoint(fa, s);
         NK_CHECK_LAUNCH();
     }
@@ -2339,6 +2346,8 @@ struct TimeGradient {
                     lamH = lam;
                     lamHs = lam_in;
                     stage_reverse(n, k, stg, front && stg == 2);
+                    if (front && stg == 2 && P->front.calving != NK_CALVING_NONE)   // the calving rates read the stage's velocities
+                        launch_add_pairs(g, lamx_stage, front_lamx(), s);
                     if (stg > 0) {
                         if (solves) solve_adjoint(lamx_stage, lam_in);   // the solve that made x_t from H_t
                         else launch_add_pairs(g, lamu_held, lamx_stage, s);
@@ -2390,8 +2399,8 @@ nk_status nk_checkpointed_gradient(nk_problem* P, const nk_time_gradient_desc* d
         if (desc->steps < 1) bad("steps must be at least 1");
         if (desc->checkpoint_interval < 0) bad("checkpoint_interval must be non-negative");
         if (desc->velocity_solves != 0 && desc->velocity_solves != 1) bad("velocity_solves is 0 or 1");
-        if (P->front.enabled && P->front.calving != NK_CALVING_NONE)
-            bad("the gradient through time steps covers a partial-cell front without a calving law");
+        if (P->front.enabled && P->front.calving == NK_CALVING_VON_MISES)
+            bad("the gradient through time steps does not cover von Mises calving (its rate reads the viscosity)");
         if (desc->velocity_solves && P->ud) bad("the gradient through velocity solves is not available with prescribed velocities");
         if (desc->melt_weights)
             for (int n = 0; n < desc->steps; ++n)

@@ -380,9 +380,64 @@ def test_surface_mass_balance_through_the_partial_cell_front(gpu_cls, passes):
         _close(g["H"][idx], fd_final_thickness(case, gpu_cls, "H", idx, 1e-6 * H0[idx]), 1e-6)
 
 
-def test_front_calving_is_refused(gpu_cls):
+def test_von_mises_calving_is_refused(gpu_cls):
     case = channel_front_case()
     P = case.build(gpu_cls)
-    P.set_front(M.PartialCellFront(passes=2, calving=M.ThicknessThresholdCalving(thickness=50.0)))
+    P.set_front(M.PartialCellFront(passes=2, calving=M.VonMisesCalving(stress_threshold=1e5)))
     with pytest.raises(Exception):
         P.checkpointed_gradient(thickness_cost(2), case.dt, 2, velocity_solves=False)
+
+
+# ---- calving (test/test_enzyme.jl:516-536) -----------------------------------------------------------------------------
+def calving_case(law, steps=1, grounding=None):
+    """The reference's eigencalving case: a 12 x 6 shelf on a bed 500 m deep, 100 m of ice west of 4 km, spreading at
+    u = a x, v = b y (a = b = 1e-9 /s), the front's four overflow passes; one step of 1e7 s with the velocities held
+    (the stages move ice too, where the reference's cost advances the front alone).  The front-velocity law calves
+    floating ice only ((1 - φ) c), so its case takes the subgrid grounded fraction."""
+    dx, Hi, a, b = 1e3, 100.0, 1e-9, 1e-9
+    grid = M.RectilinearGrid(size=(12, 6), x=(0.0, 12 * dx), y=(0.0, 6 * dx), halo=(4, 4))
+
+    def build(cls):
+        P = make(cls, grid, advection=M.UpwindBiased(order=1), Nsigma=2, masking=M.PartialCellFront(calving=law),
+                 grounding=grounding)
+        set_fn(P, "H", lambda x, y: Hi if x < 4 * dx else 0.0)
+        P.set("bed", -500.0)
+        P.initialize_front()
+        P.compute_geometry()
+        set_fn(P, "u", lambda x, y: a * x)
+        set_fn(P, "v", lambda x, y: b * y)
+        P.energy_set("surface_mass_balance", 0.0)
+        P.energy_set("basal_melt_rate", 0.0)
+        P.energy_set("clipped_thickness", 0.0)
+        return P
+
+    return Case(build, 1e7, steps, solves=False)
+
+
+@pytest.mark.parametrize("law", [M.EigenCalving(coefficient=1e13), M.FrontVelocityCalving(front_velocity=1e-6)],
+                         ids=["eigen", "front_velocity"])
+def test_velocity_gradient_through_calving(gpu_cls, law):
+    """∂J/∂u of J = Σ H² at the faces the reference checks (its cells (4, 2) and (4, 3)), through the retreat the rate
+    law sets from the strain rates or the front speed, to 1e-5 (the reference's tolerance and h = 1e-12)."""
+    case = calving_case(law, grounding=M.SubgridGroundedFraction() if isinstance(law, M.FrontVelocityCalving) else None)
+    P0 = case.build(gpu_cls)
+    _, g = gradient(case, gpu_cls)
+    assert not np.any(np.isnan(g["u"]))
+    for idx in ((1, 3), (2, 3)):
+        fd = fd_final_thickness(case, gpu_cls, "u", idx, 1e-12)
+        _close(g["u"][idx], fd, 1e-5)
+    P1 = case.forward(gpu_cls)
+    assert np.sum(P1.get("calved_thickness")) > 0   # the law calved
+    H0 = P0.get("H")
+    _close(g["H"][2, 3], fd_final_thickness(case, gpu_cls, "H", (2, 3), 1e-6 * H0[2, 3]), 1e-5)
+
+
+def test_thickness_gradient_through_threshold_calving(gpu_cls):
+    """A removal law (thickness threshold): the calved cells hold no ice afterwards; ∂J/∂H₀ and ∂J/∂a elsewhere through
+    the front's advance, two steps, to 1e-6."""
+    case = calving_case(M.ThicknessThresholdCalving(thickness=150.0), steps=2)
+    P0 = case.build(gpu_cls)
+    _, g = gradient(case, gpu_cls)
+    H0 = P0.get("H")
+    for idx in ((2, 1), (3, 2)):
+        _close(g["H"][idx], fd_final_thickness(case, gpu_cls, "H", idx, 1e-6 * H0[idx]), 1e-6)
