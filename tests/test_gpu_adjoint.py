@@ -411,3 +411,51 @@ def test_thickness_gradient_on_the_periodic_seam(gpu_cls, diva):
         d = 1e-3 * H0[cell]
         fd = (16 * difference(cell, d / 4) - difference(cell, d)) / 15
         assert abs(fd - gh[cell]) <= 1e-6 * abs(fd) + 1e-8 * np.max(np.abs(gh)), (cell, fd, gh[cell])
+
+
+@pytest.mark.parametrize("driving_stress", [False, True], ids=["centred", "split"])
+def test_thickness_gradient_across_the_grounding_line(gpu_cls, driving_stress):
+    """∂J/∂H of J = Σ u² + v² across a grounding line (test/test_enzyme.jl:584-608): a 16 x 4 marine sheet on a bed
+    sloping down from 200 m, H = 1000 - 0.01 x - 100 ((y - 8 km) / 8 km)² up to a front at 56 km, Weertman drag,
+    the subgrid grounded fraction with and without the grounding-line split of the driving stress, at the reference's
+    four cells (two with 0 < φ < 1), to 1e-4 against extrapolated centred differences.  The reference differentiates
+    four fixed Picard iterations; here the solves are converged (Picard 1e-14) and the adjoint is the fixed point's."""
+    from support import ice_sheet_model
+    grid = M.RectilinearGrid(size=(16, 4), x=(0.0, 64e3), y=(0.0, 16e3), halo=(4, 4))
+    solver = M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-15, maxiter=10_000),
+                                   picard_iteration_control=M.Convergence(reltol=1e-14, maxiter=1000))
+
+    def build():
+        P, st = ice_sheet_model(gpu_cls, grid, H=lambda x, y: 1000 - 1e-2 * x - 100 * ((y - 8e3) / 8e3) ** 2 if x < 56e3 else 0.0,
+                                bed=lambda x, y: -200 - 1e-2 * x, rheology=M.GlenFlowLaw(rate_factor=1e-24),
+                                friction=M.WeertmanFriction(coefficient=3e6),
+                                grounding=M.SubgridGroundedFraction(driving_stress=driving_stress), velocity_solver=solver)
+        assert st.status == 0
+        return P
+
+    P = build()
+    phi = P.get("phi")
+    assert 0 < phi[1, 8] < 1 and 0 < phi[1, 9] < 1
+    u0, v0, H0 = P.get("u"), P.get("v"), P.get("H")
+    *_, gh, st = P.picard_adjoint(2 * u0, 2 * v0, M.Convergence(reltol=1e-14, maxiter=3000), thickness=True)
+    assert st.status == 0
+
+    def difference(cell, d):
+        out = []
+        for sgn in (1.0, -1.0):
+            Q = build()
+            H = H0.copy()
+            H[cell] += sgn * d
+            Q.set("H", H)
+            Q.compute_geometry()
+            Q.set("u", u0)
+            Q.set("v", v0)
+            Q.picard_solve()
+            out.append((Q.get("u"), Q.get("v")))
+        (up, vp), (um, vm) = out
+        return (np.sum((up - um) * (up + um)) + np.sum((vp - vm) * (vp + vm))) / (2 * d)
+
+    for cell in ((1, 7), (2, 8), (1, 9), (1, 11)):
+        d = 1e-3 * H0[cell]
+        fd = (16 * difference(cell, d / 4) - difference(cell, d)) / 15
+        assert abs(fd - gh[cell]) <= 1e-4 * abs(fd), (driving_stress, cell, fd, gh[cell])
