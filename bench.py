@@ -31,6 +31,10 @@ walk the stream from its first request and wrap around after 512.  The warm-up s
   published_scaling  the reference's published multigrid scaling benchmark (one SSA solve to 1e-8 at six grid
             spacings, diagonal and multigrid PCG): iterations and GPU device time beside the published CPU and H200
             times.
+  halfpipe_adjoint  the STREAMICE halfpipe adjoint (the reference's gradient benchmark): ∂J/∂xx through three DIVA
+            time steps with a partial-cell front by nk_checkpointed_gradient, beside centred differences of the
+            library's forward steps and STREAMICE's published cost and gradient; wall times of the gradient and of
+            one forward run.
   cpu_baseline  the FP64 CPU restatement of the reference solve (the oracle) on all host cores: one solve of the
             first timed request of each grid size, weighted by the stream's size counts.  The same solves give
             the mixed solver's relative L2 velocity error against the FP64 oracle for every grid size.
@@ -83,6 +87,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true",
                     help="skip the oracle solves (CPU baseline and the mixed-vs-oracle errors of every grid size)")
     ap.add_argument("--no-scaling", action="store_true", help="skip the reference's published scaling benchmark rows")
+    ap.add_argument("--no-halfpipe", action="store_true", help="skip the STREAMICE halfpipe adjoint of the default line")
     ap.add_argument("--rate", type=float, default=ARRIVAL_RATE,
                     help="Poisson arrival rate of the e2e leg, requests/s (the workload's is 200)")
     ap.add_argument("--profile", choices=["solve", "smoother", "operator", "enthalpy"], default=None,
@@ -665,7 +670,7 @@ def run_diva(nk, workloads, ctx):
         "coulomb_transition_speed_m_per_yr": transition}), flush=True)
 
 
-def run_halfpipe_adjoint(nk, workloads, ctx):
+def halfpipe_adjoint(nk, workloads, ctx):
     """The STREAMICE halfpipe adjoint (benchmarks/halfpipe_streamice_adjoint.jl:66-99) with the benchmark's tolerances
     (Picard 1e-8, CG 1e-10, the adjoint at the Picard control): J and ∂J/∂xx at the four centreline cells from
     nk_checkpointed_gradient, centred differences of the library's forward steps with the benchmark's ε = 0.1 m/yr, and
@@ -697,11 +702,15 @@ def run_halfpipe_adjoint(nk, workloads, ctx):
         rows.append({"cell_julia": list(spec["check_cells_julia"][k]), "adjoint": ad, "finite_difference": fd,
                      "rel_adjoint_vs_fd": (ad - fd) / abs(fd), "streamice_adjoint": sad, "streamice_finite_difference": sfd,
                      "ratio_to_streamice_adjoint": ad / sad})
-    print(json.dumps({"metric": "STREAMICE halfpipe adjoint: dJ/dxx through 3 DIVA time steps with a partial-cell front",
-                      "J": g["J"], "J_forward": J, "streamice_cost": spec["streamice_cost"],
-                      "ratio_to_streamice_cost": g["J"] / spec["streamice_cost"], "rows": rows,
-                      "gradient_wall_s": t_grad, "forward_wall_s": t_fwd, "gradient_over_forward": t_grad / t_fwd,
-                      "stats": g["stats"]}), flush=True)
+    return {"metric": "STREAMICE halfpipe adjoint: dJ/dxx through 3 DIVA time steps with a partial-cell front",
+            "J": g["J"], "J_forward": J, "streamice_cost": spec["streamice_cost"],
+            "ratio_to_streamice_cost": g["J"] / spec["streamice_cost"], "rows": rows,
+            "gradient_wall_s": t_grad, "forward_wall_s": t_fwd, "gradient_over_forward": t_grad / t_fwd,
+            "stats": g["stats"]}
+
+
+def run_halfpipe_adjoint(nk, workloads, ctx):
+    print(json.dumps(halfpipe_adjoint(nk, workloads, ctx)), flush=True)
 
 
 def run_scaling(nk, workloads, ctx, problem_cls=None, rows=None, quiet=False):
@@ -1009,6 +1018,9 @@ def main():
     # ---- the reference's published scaling benchmark: GPU device times beside the published H200 and CPU times ----
     if not args.no_scaling:
         line["published_scaling"] = run_scaling(nk, workloads, ctx, quiet=True)
+    # ---- the reference's gradient benchmark through the time steps ----
+    if not args.no_halfpipe:
+        line["halfpipe_adjoint"] = halfpipe_adjoint(nk, workloads, ctx)
     # ---- the FP64 CPU restatement (the oracle): one solve of each size, the parity of the mixed solves against it and
     # the CPU baseline of the stream's size mix -----------------------------------------------------------------------
     if not args.no_cpu_baseline:
