@@ -2131,6 +2131,313 @@ static void step_thickness(Problem& P, double dt, bool coupled) {
     for (int st = 0; st < 3; ++st) step_thickness_stage(P, dt, st, coupled);
 }
 
+// ------------------------------------------------------------------------------------------------
+// The gradient through time steps with the velocities held (checkpointed_gradient!, ext/NunatakEnzymeExt.jl:245-263,
+// for a model without a velocity solve): the oracle's own restatement, held to finite differences of its forward steps.
+// Every stage is stored (no checkpoints); the reverse of a stage takes the chain through the clip, the sources, the
+// divergence and the fluxes by hand, and the local derivatives of the face values, the limiter θ and the centre
+// grounded fraction by forward differentiation (a value and one derivative) of the same formulas the forward step
+// evaluates, input by input.
+// ------------------------------------------------------------------------------------------------
+struct Dn {
+    double v, d;
+};
+static inline Dn operator+(Dn a, Dn b) { return {a.v + b.v, a.d + b.d}; }
+static inline Dn operator-(Dn a, Dn b) { return {a.v - b.v, a.d - b.d}; }
+static inline Dn operator*(Dn a, Dn b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+static inline Dn operator*(double s, Dn a) { return {s * a.v, s * a.d}; }
+static inline Dn operator/(Dn a, Dn b) { return {a.v / b.v, (a.d * b.v - a.v * b.d) / (b.v * b.v)}; }
+static inline Dn operator/(Dn a, double s) { return {a.v / s, a.d / s}; }
+static inline Dn dn_abs(Dn a) { return a.v >= 0 ? a : Dn{-a.v, -a.d}; }
+static inline Dn dn_max(Dn a, Dn b) { return std::max(a.v, b.v) == a.v ? a : b; }
+static inline Dn dn_min(Dn a, Dn b) { return std::min(a.v, b.v) == a.v ? a : b; }
+
+// weno5_face, upwind3_face and face_value above, on values with a derivative
+static Dn weno5_face_dn(const Dn* s) {
+    const Dn a = s[0], b = s[1], c = s[2], d = s[3], e = s[4];
+    Dn q0 = (2 * a - 7 * b + 11 * c) / 6.0;
+    Dn q1 = ((-1.0) * b + 5 * c + 2 * d) / 6.0;
+    Dn q2 = (2 * c + 5 * d - e) / 6.0;
+    Dn t0 = a - 2 * b + c, u0 = a - 4 * b + 3 * c;
+    Dn t1 = b - 2 * c + d, u1 = b - d;
+    Dn t2 = c - 2 * d + e, u2 = 3 * c - 4 * d + e;
+    Dn b0 = (13.0 / 12) * (t0 * t0) + 0.25 * (u0 * u0);
+    Dn b1 = (13.0 / 12) * (t1 * t1) + 0.25 * (u1 * u1);
+    Dn b2 = (13.0 / 12) * (t2 * t2) + 0.25 * (u2 * u2);
+    const Dn eps{1e-8, 0.0};
+    Dn tau = dn_abs(b0 - b2);
+    Dn r0 = tau / (b0 + eps), r1 = tau / (b1 + eps), r2 = tau / (b2 + eps);
+    Dn a0 = 0.1 * (Dn{1, 0} + r0), a1 = 0.6 * (Dn{1, 0} + r1), a2 = 0.3 * (Dn{1, 0} + r2);
+    return (a0 * q0 + a1 * q1 + a2 * q2) / (a0 + a1 + a2);
+}
+static Dn face_value_dn(const nk_advection_desc& adv, const Dn* s) {
+    if (adv.scheme == NK_ADVECTION_WENO) return weno5_face_dn(s);
+    return adv.order == 3 ? ((-1.0) * s[1] + 5 * s[2] + 2 * s[3]) / 6.0 : s[2];
+}
+// bounds_limiter with the derivative along the stage thickness at halo position (si, sj)
+static Dn bounds_limiter_dn(const nk_advection_desc& adv, const Field& H, int i, int j, int si, int sj) {
+    auto h = [&](int a, int b) { return Dn{H(a, b), (a == si && b == sj) ? 1.0 : 0.0}; };
+    Dn s[5];
+    for (int m = -2; m <= 2; ++m) s[m + 2] = h(i + m, j);           // x_stencil(H, i + 1, j, east): H(i + m)
+    Dn E = weno5_face_dn(s);
+    for (int m = -2; m <= 2; ++m) s[m + 2] = h(i - m, j);           // x_stencil(H, i, j, west): H(i - m)
+    Dn W = weno5_face_dn(s);
+    for (int m = -2; m <= 2; ++m) s[m + 2] = h(i, j + m);
+    Dn N = weno5_face_dn(s);
+    for (int m = -2; m <= 2; ++m) s[m + 2] = h(i, j - m);
+    Dn S = weno5_face_dn(s);
+    Dn Hc = h(i, j);
+    const double w = 5.0 / 18, eps = 2 * std::numeric_limits<double>::epsilon();
+    Dn px = (Hc - w * W - w * E) / (1 - 2 * w);
+    Dn py = (Hc - w * S - w * N) / (1 - 2 * w);
+    Dn M = dn_max(dn_max(dn_max(px, py), dn_max(W, E)), dn_max(S, N));
+    Dn m = dn_min(dn_min(dn_min(px, py), dn_min(W, E)), dn_min(S, N));
+    Dn t1 = dn_abs((Dn{adv.upper, 0} - Hc) / (M - Hc + Dn{eps, 0}));
+    Dn t2 = dn_abs((Dn{adv.lower, 0} - Hc) / (m - Hc - Dn{eps, 0}));
+    return dn_min(dn_min(t1, t2), Dn{1.0, 0.0});
+}
+static Dn triangle_fraction_dn(Dn f1, Dn f2, Dn f3) {   // triangle_grounded_fraction
+    Dn a = dn_min(dn_min(f1, f2), f3), c = dn_max(dn_max(f1, f2), f3);
+    Dn b = f1 + f2 + f3 - a - c;
+    auto nz = [](Dn x) { return x.v == 0.0 ? Dn{1.0, 0.0} : x; };
+    Dn one_grounded = (c * c) / nz((c - a) * (c - b));
+    Dn one_floating = Dn{1.0, 0.0} - (a * a) / nz((b - a) * (c - a));
+    Dn phi = b.v > 0 ? one_floating : one_grounded;
+    return a.v >= 0 ? Dn{1.0, 0.0} : (c.v <= 0 ? Dn{0.0, 0.0} : phi);
+}
+// the centre grounded fraction of compute_geometry at (i, j) with the derivative along H at halo position (si, sj)
+static Dn centre_fraction_dn(const Problem& P, int i, int j, int si, int sj) {
+    double rw_ri = P.ph.rho_w / P.ph.rho_i;
+    auto f = [&](int a, int b) { return Dn{P.H(a, b) + rw_ri * P.bed(a, b), (a == si && b == sj) ? 1.0 : 0.0}; };
+    Dn fc = f(i, j);
+    Dn fe = (fc + f(i + 1, j)) / 2.0, fw = (fc + f(i - 1, j)) / 2.0, fn = (fc + f(i, j + 1)) / 2.0, fs = (fc + f(i, j - 1)) / 2.0;
+    Dn fne = (fc + f(i + 1, j) + f(i, j + 1) + f(i + 1, j + 1)) / 4.0;
+    Dn fnw = (fc + f(i - 1, j) + f(i, j + 1) + f(i - 1, j + 1)) / 4.0;
+    Dn fse = (fc + f(i + 1, j) + f(i, j - 1) + f(i + 1, j - 1)) / 4.0;
+    Dn fsw = (fc + f(i - 1, j) + f(i, j - 1) + f(i - 1, j - 1)) / 4.0;
+    Dn phi = triangle_fraction_dn(fc, fe, fne) + triangle_fraction_dn(fc, fn, fne) + triangle_fraction_dn(fc, fn, fnw) +
+             triangle_fraction_dn(fc, fw, fnw) + triangle_fraction_dn(fc, fw, fsw) + triangle_fraction_dn(fc, fs, fsw) +
+             triangle_fraction_dn(fc, fs, fse) + triangle_fraction_dn(fc, fe, fse);
+    return phi / 8.0;
+}
+
+// The interior cell a halo position of a Center-Center field copies (fill_halo: wrap, or the edge cell).
+static void fold(const Grid& g, int& i, int& j) {
+    i = g.x.periodic ? mod1(i, g.Nx()) : std::min(std::max(i, 1), g.Nx());
+    j = g.y.periodic ? mod1(j, g.Ny()) : std::min(std::max(j, 1), g.Ny());
+}
+
+// The reverse of step_thickness_stage (no front) at the stored stage: P.H holds the stage thickness (halos filled) and
+// P.phi its centre grounded fraction, P.melt the step's melt (w m); H0 the step start, Hout the stage output.  From λ
+// of the output (lam_out) it adds λ of H0, u, v, a and the base melt m and writes λ of the stage thickness (lam_Hs).
+static void stage_reverse(Problem& P, const Field& H0, const Field& Hout, double dtau, double w, const Field& lam_out,
+                          Field& lam_Hs, Field& lam_H0, VelocityVector& lam_x, Field& lam_smb, Field& lam_melt) {
+    const Grid& g = P.grid;
+    const int Nx = g.Nx(), Ny = g.Ny();
+    const nk_advection_desc adv = P.advection;
+    const bool bounded = adv.scheme == NK_ADVECTION_WENO && adv.bounded;
+    const Field& Hs = P.H;
+    Field dv(&g, CENTER, CENTER), lam_phi(&g, CENTER, CENTER), lam_theta(&g, CENTER, CENTER);
+    (void)H0;
+    lam_Hs.zero();
+    for (int j = 1; j <= Ny; ++j)
+        for (int i = 1; i <= Nx; ++i) {
+            double ls = Hout(i, j) > 0 ? lam_out(i, j) : 0.0;   // the clip max(0, H★)
+            lam_H0(i, j) += ls;
+            dv(i, j) = -dtau * ls / g.Az_ccc(i, j);
+            double lS = dtau * ls;
+            lam_smb(i, j) += lS;
+            lam_melt(i, j) -= lS * (P.grounding ? 1 - P.phi(i, j) : 1.0) * w;
+            lam_phi(i, j) = P.grounding ? lS * P.melt(i, j) : 0.0;
+        }
+    auto theta = [&](int ic, int jc) { return bounded ? P.theta(ic, jc) : 1.0; };
+    // a face's flux u Δ H_face: λ to the velocity, to the upwind cell (1 - θ), to its θ, and through the face value's
+    // derivative to the five stencil cells
+    auto face = [&](double lF, double u, double delta, bool pos, int ic, int jc, int ax, int ay, int f0x, int f0y, bool xdir,
+                    double& lam_u) {
+        Dn s[5];
+        double sv[5];
+        int px[5], py[5];
+        for (int m = -2; m <= 2; ++m) {
+            int a = xdir ? (pos ? f0x - 1 + m : f0x - m) : f0x;
+            int b = xdir ? f0y : (pos ? f0y - 1 + m : f0y - m);
+            px[m + 2] = a;
+            py[m + 2] = b;
+            sv[m + 2] = Hs(a, b);
+        }
+        for (int m = 0; m < 5; ++m) s[m] = Dn{sv[m], 0.0};
+        double h0 = face_value_dn(adv, s).v;
+        double th = theta(ic, jc);
+        double h = bounded ? Hs(ic, jc) + th * (h0 - Hs(ic, jc)) : h0;
+        lam_u += delta * h * lF;
+        double lh = delta * u * lF;
+        if (bounded) {
+            int fi = ic, fj = jc;
+            fold(g, fi, fj);
+            lam_Hs(fi, fj) += (1 - th) * lh;
+            lam_theta(fi, fj) += (h0 - Hs(ic, jc)) * lh;
+        }
+        double lh0 = th * lh;
+        for (int q = 0; q < 5; ++q) {
+            for (int m = 0; m < 5; ++m) s[m] = Dn{sv[m], m == q ? 1.0 : 0.0};
+            double d = face_value_dn(adv, s).d;
+            int a = px[q], b = py[q];
+            fold(g, a, b);
+            lam_Hs(a, b) += d * lh0;
+        }
+        (void)ax;
+        (void)ay;
+    };
+    // x faces f = 1 .. Nx + 1 (Nx on a periodic axis, whose face Nx + 1 is face 1)
+    int fxmax = g.x.periodic ? Nx : Nx + 1, fymax = g.y.periodic ? Ny : Ny + 1;
+    for (int j = 1; j <= Ny; ++j)
+        for (int f = 1; f <= fxmax; ++f) {
+            if (g.peripheral_fc(f, j)) continue;
+            int wi = f - 1, wj = j, ei = f, ej = j;
+            fold(g, wi, wj);
+            fold(g, ei, ej);
+            double lF = dv(wi, wj) - dv(ei, ej);
+            double u = P.x.u(f, j);
+            bool east = u > 0;
+            face(lF, u, g.dy_c(j), east, east ? f - 1 : f, j, 0, 0, f, j, true, lam_x.u(f, j));
+        }
+    for (int f = 1; f <= fymax; ++f)
+        for (int i = 1; i <= Nx; ++i) {
+            if (g.peripheral_cf(i, f)) continue;
+            int si = i, sj = f - 1, ni = i, nj = f;
+            fold(g, si, sj);
+            fold(g, ni, nj);
+            double lF = dv(si, sj) - dv(ni, nj);
+            double v = P.x.v(i, f);
+            bool north = v > 0;
+            face(lF, v, g.dx_c(i), north, i, north ? f - 1 : f, 0, 0, i, f, false, lam_x.v(i, f));
+        }
+    // θ of each cell, back to the thickness of its own stencils and itself
+    if (bounded)
+        for (int j = 1; j <= Ny; ++j)
+            for (int i = 1; i <= Nx; ++i) {
+                double lt = lam_theta(i, j);
+                if (lt == 0.0) continue;
+                for (int q = 0; q < 9; ++q) {
+                    int si = q < 5 ? i + q - 2 : i, sj = q < 5 ? j : j + (q < 7 ? q - 7 : q - 6);
+                    double d = bounds_limiter_dn(adv, Hs, i, j, si, sj).d;
+                    int a = si, b = sj;
+                    fold(g, a, b);
+                    lam_Hs(a, b) += lt * d;
+                }
+            }
+    // the centre grounded fraction of the floating melt, back to the nine flotations it reads
+    if (P.grounding)
+        for (int j = 1; j <= Ny; ++j)
+            for (int i = 1; i <= Nx; ++i) {
+                double lp = lam_phi(i, j);
+                if (lp == 0.0) continue;
+                for (int b = -1; b <= 1; ++b)
+                    for (int a = -1; a <= 1; ++a) {
+                        double d = centre_fraction_dn(P, i, j, i + a, j + b).d;
+                        int x = i + a, y = j + b;
+                        fold(g, x, y);
+                        lam_Hs(x, y) += lp * d;
+                    }
+            }
+}
+
+static void copy_in(Field& f, const double* src);
+static void copy_out(const Field& f, double* dst);
+
+// nk_checkpointed_gradient of the library with the velocities held and no front; every stage stored.
+static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_cost_fn cost, void* user, const nk_time_gradient* out,
+                               nk_time_gradient_stats* st) {
+    const Grid& g = P.grid;
+    const int Nx = g.Nx(), Ny = g.Ny(), N = d.steps;
+    const bool bounded = P.advection.scheme == NK_ADVECTION_WENO && P.advection.bounded;
+    const double fractions[3] = {1.0 / 3, 1.0 / 2, 1.0};
+    auto weight = [&](int n) { return d.melt_weights ? d.melt_weights[n] : 1.0; };
+    Field base = P.melt, clipped0 = P.clipped;
+    std::vector<Field> tape;   // H before each stage, then the final H
+    fill_halo(P.H);
+    compute_geometry(P);
+    for (int n = 0; n < N; ++n) {
+        for_xy(Nx, Ny, [&](int i, int j) { P.melt(i, j) = weight(n) * base(i, j); });
+        for (int stg = 0; stg < 3; ++stg) {
+            tape.push_back(P.H);
+            step_thickness_stage(P, d.dt, stg, false);
+        }
+    }
+    tape.push_back(P.H);
+    Field Hfinal = P.H, clipped_end = P.clipped;
+    Field lamH(&g, CENTER, CENTER), lamHs(&g, CENTER, CENTER), lamH0(&g, CENTER, CENTER);
+    Field gsmb(&g, CENTER, CENTER), gmelt(&g, CENTER, CENTER);
+    VelocityVector lamx;
+    lamx.init(&g);
+    int nu = P.x.u.nx() * P.x.u.ny(), nv = P.x.v.nx() * P.x.v.ny();
+    std::vector<double> hH(Nx * Ny), hu(nu), hv(nv), hm(Nx * Ny), gH(Nx * Ny), gu(nu), gv(nv);
+    std::memset(st, 0, sizeof(*st));
+    st->segments = 1;
+    for (int n = N - 1; n >= 0; --n) {
+        P.H = tape[3 * n + 3];
+        fill_halo(P.H);
+        compute_geometry(P);
+        copy_out(P.H, hH.data());
+        copy_out(P.x.u, hu.data());
+        copy_out(P.x.v, hv.data());
+        copy_out(P.mu, hm.data());
+        std::fill(gH.begin(), gH.end(), 0.0);
+        std::fill(gu.begin(), gu.end(), 0.0);
+        std::fill(gv.begin(), gv.end(), 0.0);
+        nk_cost_state cs{n + 1, N, hH.data(), hu.data(), hv.data(), hm.data()};
+        double J = 0.0;
+        if (cost(user, &cs, &J, gH.data(), gu.data(), gv.data()) != 0) return NK_BAD_ARGUMENT;
+        st->J += J;
+        {
+            Field t(&g, CENTER, CENTER);
+            copy_in(t, gH.data());
+            for_xy(Nx, Ny, [&](int i, int j) { lamH(i, j) += t(i, j); });
+            Field tu(&g, FACE, CENTER), tv(&g, CENTER, FACE);
+            copy_in(tu, gu.data());
+            copy_in(tv, gv.data());
+            for (int j = 1; j <= tu.ny(); ++j) for (int i = 1; i <= tu.nx(); ++i) lamx.u(i, j) += tu(i, j);
+            for (int j = 1; j <= tv.ny(); ++j) for (int i = 1; i <= tv.nx(); ++i) lamx.v(i, j) += tv(i, j);
+        }
+        lamH0.zero();
+        for (int stg = 2; stg >= 0; --stg) {
+            int t = 3 * n + stg;
+            P.H = tape[t];
+            fill_halo(P.H);
+            compute_geometry(P);
+            for_xy(Nx, Ny, [&](int i, int j) { P.melt(i, j) = weight(n) * base(i, j); });
+            fill_halo(P.melt);
+            fill_halo(P.x);
+            if (bounded) {
+                if (!P.theta.g) P.theta.init(&g, CENTER, CENTER);
+                for (int j = 0; j <= Ny + 1; ++j)
+                    for (int i = 0; i <= Nx + 1; ++i) P.theta(i, j) = bounds_limiter(P.advection, P.H, i, j);
+            }
+            stage_reverse(P, tape[3 * n], tape[t + 1], fractions[stg] * d.dt, weight(n), lamH, lamHs, lamH0, lamx, gsmb, gmelt);
+            if (stg > 0) lamH = lamHs;
+            else for_xy(Nx, Ny, [&](int i, int j) { lamH(i, j) = lamHs(i, j) + lamH0(i, j); });
+        }
+    }
+    if (out) {
+        if (out->grad_H) copy_out(lamH, out->grad_H);
+        if (out->grad_u && out->grad_v) { copy_out(lamx.u, out->grad_u); copy_out(lamx.v, out->grad_v); }
+        if (out->grad_smb) copy_out(gsmb, out->grad_smb);
+        if (out->grad_melt) copy_out(gmelt, out->grad_melt);
+        if (out->grad_log_C) std::fill(out->grad_log_C, out->grad_log_C + Nx * Ny, 0.0);
+        if (out->grad_log_A) {
+            int planes = P.rate_layout == NK_RATE_FACTOR_SIGMA ? P.sigma.N : 1;
+            std::fill(out->grad_log_A, out->grad_log_A + (size_t)planes * Nx * Ny, 0.0);
+        }
+    }
+    P.H = Hfinal;
+    P.clipped = clipped_end;
+    P.melt = base;
+    fill_halo(P.H);
+    compute_geometry(P);
+    (void)clipped0;
+    return NK_OK;
+}
+
 // ---- field access in interior layout -------------------------------------------------------------
 struct FieldRef { Field* f = nullptr; SigmaField* s = nullptr; };
 
@@ -2418,6 +2725,16 @@ nk_status nko_step_thickness_stage(nko_problem* h, double dt, int32_t stage, int
     if ((P.advection.scheme == NK_ADVECTION_WENO || P.advection.order == 3) && halo < 3) return NK_BAD_ARGUMENT;
     step_thickness_stage(P, dt, stage - 1, coupled != 0);
     return NK_OK;
+}
+
+// nk_checkpointed_gradient for a model whose velocities are held (no velocity solve) and without a front.
+nk_status nko_checkpointed_gradient(nko_problem* h, const nk_time_gradient_desc* d, nk_cost_fn cost, void* user,
+                                    const nk_time_gradient* out, nk_time_gradient_stats* stats) {
+    if (!h || !d || !cost || !(d->dt > 0) || d->steps < 1 || d->velocity_solves != 0) return NK_BAD_ARGUMENT;
+    Problem& P = *reinterpret_cast<Problem*>(h);
+    if (P.front.enabled) return NK_BAD_ARGUMENT;
+    nk_time_gradient_stats local{};
+    return time_gradient(P, *d, cost, user, out, stats ? stats : &local);
 }
 
 // PartialCellFront(grid; passes, calving) as the masking (partial_cell_front.jl:1-66, calving.jl); needs the ice mask.

@@ -60,6 +60,8 @@ def load():
             "nko_multigrid_prolongate": [vp, i32, dp, dp, dp, dp],
             "nko_grid_metrics": [vp, i32, dp],
             "nko_set_threads": [C.c_int],
+            "nko_checkpointed_gradient": [vp, C.POINTER(abi.TimeGradientDesc), abi.COST_FN, vp, C.POINTER(abi.TimeGradient),
+                                          C.POINTER(abi.TimeGradientStats)],
         }
         for name, args in sig.items():
             f = getattr(lib, name)

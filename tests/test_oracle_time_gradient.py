@@ -1,0 +1,42 @@
+"""The oracle's restatement of the gradient through time steps with the velocities held (nko_checkpointed_gradient)
+against centred differences of its own forward steps, on the CPU: the transport case of test/test_enzyme.jl:447-488
+(16 x 4, sources a and m, eight steps; the default bounded WENO-5 and first-order upwinding) at the reference's cells
+to 1e-6, and the floating melt across a grounding line (the centre grounded fraction) at the partially grounded cells
+to 1e-5.  The library's gradient is held to this one over the whole field in test_gpu_time_gradient."""
+import numpy as np
+import pytest
+
+from nunatak_gb300 import model as M
+from test_gpu_time_gradient import _close, fd_final_thickness, gradient, grounding_line_case, transport_case
+
+
+@pytest.mark.parametrize("advection", [None, M.UpwindBiased(order=1)], ids=["bounded_weno5", "upwind1"])
+def test_oracle_transport_gradient_matches_differences(oracle_cls, advection):
+    case = transport_case(advection)
+    _, g = gradient(case, oracle_cls)
+    for field, key, idx, val in (("surface_mass_balance", "smb", (1, 4), 1e-8), ("basal_melt_rate", "melt", (2, 8), 1e-9 * 8.5 / 16)):
+        _close(g[key][idx], fd_final_thickness(case, oracle_cls, field, idx, 1e-6 * val), 1e-6)
+    P = case.build(oracle_cls)
+    u0, H0 = P.get("u"), P.get("H")
+    for idx in ((0, 5), (3, 10)):
+        _close(g["u"][idx], fd_final_thickness(case, oracle_cls, "u", idx, 1e-6 * abs(u0[idx])), 1e-6)
+    for idx in ((1, 3), (2, 8)):
+        _close(g["H"][idx], fd_final_thickness(case, oracle_cls, "H", idx, 1e-6 * H0[idx]), 1e-6)
+
+
+def test_oracle_floating_melt_gradient(oracle_cls):
+    case = grounding_line_case(None)
+    P0 = case.build(oracle_cls)
+    phi, H0 = P0.get("phi"), P0.get("H")
+    _, g = gradient(case, oracle_cls)
+    partial = [tuple(ix) for ix in np.argwhere((phi > 0.05) & (phi < 0.95))]
+    assert len(partial) >= 3
+    for idx in partial[:3]:
+        _close(g["H"][idx], fd_final_thickness(case, oracle_cls, "H", idx, 1e-6 * H0[idx]), 1e-5)
+
+
+def test_oracle_refuses_velocity_solves(oracle_cls):
+    case = transport_case()
+    P = case.build(oracle_cls)
+    with pytest.raises(Exception):
+        P.checkpointed_gradient(lambda *a: None, case.dt, 2, velocity_solves=True)
