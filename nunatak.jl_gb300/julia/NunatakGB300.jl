@@ -560,7 +560,7 @@ function checkpointed_gradient!(dmodel, cost, model, Δt, Nt; checkpoint_interva
     gu, gv = zeros(size(interior(model.velocities.u, :, :, 1))), zeros(size(interior(model.velocities.v, :, :, 1)))
     glogA = zeros(size(interior(A)))
     w = melt_weights === nothing ? nothing : collect(Float64, melt_weights)
-    ctl = Ref(IterationControl(model.velocity_solver.adjoint_iteration_control))
+    ctl = Ref(IterationControl(model.velocity_solver.picard.adjoint_iteration_control))
     cb = CostCallback(cost, model, nothing)
     fn = @cfunction(cost_callback, Int32, (Ptr{Cvoid}, Ptr{CostState}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}))
     stats = TimeGradientStats()
