@@ -518,7 +518,8 @@ typedef struct nk_cost_state {
     const double* ice_mask;    /* Nx x Ny */
 } nk_cost_state;
 /* Jₙ into *J and ∂Jₙ/∂(H, U, V) into the arrays (zeroed before the call; the layouts of the state's arrays).
- * Return 0; anything else stops the gradient with NK_BAD_ARGUMENT. */
+ * Return 0; anything else stops the gradient with NK_BAD_ARGUMENT.  The library calls it once per step during the
+ * reverse pass, the last step first, from the calling thread. */
 typedef int32_t (*nk_cost_fn)(void* user, const nk_cost_state* state, double* J, double* dJ_dH, double* dJ_du, double* dJ_dv);
 
 typedef struct nk_time_gradient_desc {
@@ -553,6 +554,9 @@ typedef struct nk_time_gradient_stats {
     double elapsed_ms;         /* wall time of the call */
 } nk_time_gradient_stats;
 
+/* Device memory: the checkpoints and one segment's stage states, (⌈steps / K⌉ + 3K + 2) states of 3 planes (DIVA:
+ * 6 + Nσ; a front: 2 more) plus about 25 planes of adjoints, allocated for the call and freed before it returns.
+ * After an error the problem's fields are those of whichever step the sweep had reached. */
 nk_status nk_checkpointed_gradient(nk_problem* problem, const nk_time_gradient_desc* desc, nk_cost_fn cost, void* user,
                                    const nk_time_gradient* out, nk_time_gradient_stats* stats);
 
