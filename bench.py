@@ -110,6 +110,10 @@ def parse():
                     help="the STREAMICE halfpipe adjoint instead (benchmarks/halfpipe_streamice_adjoint.jl): the gradient "
                          "through three DIVA time steps with a partial-cell front, beside centred differences and STREAMICE's "
                          "published cost and gradient")
+    ap.add_argument("--time-gradient", action="store_true",
+                    help="the gradient through time steps at scale instead: four steps of the 1024x512 marine sheet "
+                         "(mixed precision, a Picard solve after every stage) forward alone and through "
+                         "nk_checkpointed_gradient")
     ap.add_argument("--profile-grid", type=int, nargs=2, default=[256, 128], metavar=("NX", "NY"),
                     help="grid of the marine-sheet solve that --profile solve runs")
     return ap.parse_args()
@@ -713,6 +717,57 @@ def run_halfpipe_adjoint(nk, workloads, ctx):
     print(json.dumps(halfpipe_adjoint(nk, workloads, ctx)), flush=True)
 
 
+def run_time_gradient(nk, workloads, ctx, nx=1024, ny=512, steps=4):
+    """The gradient through time steps at scale: the 1024x512 marine sheet in mixed precision (Picard 1e-6 x multigrid
+    PCG 1e-8), a surface mass balance of 0.3 m/yr and a basal melt of 1 m/yr under floating ice, four steps of half the
+    advective time scale of the first solve's velocities (the sheet's margin is fast), with a Picard solve after every
+    stage, J = Σ H² after the last.  Times (host wall clock, the device synchronised):
+    the forward steps alone from the same state, and one nk_checkpointed_gradient call (its forward, the segments'
+    re-runs and the reverse sweep with a Picard adjoint per solve); the gradient's magnitude per field."""
+    case = workloads.marine_sheet(nx, ny, precision="mixed")
+    year = workloads.YEAR
+    weights = None
+
+    def fresh():
+        P = case.problem(nk.Problem, context=ctx)
+        P.energy_set("surface_mass_balance", 0.3 / year)
+        P.energy_set("basal_melt_rate", 1.0 / year)
+        P.energy_set("clipped_thickness", 0.0)
+        st = P.picard_solve()
+        return P, st
+
+    P, st0 = fresh()
+    dx, dy = 512e3 / nx, 256e3 / ny
+    u, v = np.abs(P.get("u")), np.abs(P.get("v"))
+    dt = 0.5 / float(np.max(u[:, :nx] / dx + v[:ny, :] / dy))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for stage in (1, 2, 3):
+            P.step_thickness_stage(dt, stage)
+            P.picard_solve()
+    H = P.get("H")
+    t_fwd = time.perf_counter() - t0
+    J_fwd = float(np.sum(H * H))
+    P.close()
+    P, _ = fresh()
+
+    def cost(step, H, u, v, mask):
+        return (float(np.sum(H * H)), 2 * H, None, None) if step == steps else None
+
+    t0 = time.perf_counter()
+    g = P.checkpointed_gradient(cost, dt, steps, melt_weights=weights)
+    t_grad = time.perf_counter() - t0
+    print(json.dumps({
+        "metric": "gradient through time steps at scale (nk_checkpointed_gradient)",
+        "config": {"workload": "marine_sheet %dx%d (500 m), mixed precision, Picard 1e-6 x multigrid PCG 1e-8, a 0.3 m/yr, "
+                               "m 1 m/yr (floating), %d steps of %.4g yr (half the advective time scale), a Picard solve after "
+                               "every stage, J = sum H^2" % (nx, ny, steps, dt / year)},
+        "forward_wall_s": t_fwd, "gradient_wall_s": t_grad, "gradient_over_forward": t_grad / t_fwd,
+        "J": g["J"], "J_forward": J_fwd, "rel_J_difference": abs(g["J"] - J_fwd) / J_fwd,
+        "max_abs": {k: float(np.max(np.abs(g[k]))) for k in ("H", "u", "v", "smb", "melt", "log_C", "log_A")},
+        "stats": g["stats"]}), flush=True)
+
+
 def run_scaling(nk, workloads, ctx, problem_cls=None, rows=None, quiet=False):
     """The reference's published multigrid scaling benchmark (benchmarks/multigrid_scaling.jl; its table in
     docs/src/model/numerics.md:42-49, kept in tests/golden/reference_scaling.json): the MISMIP+-like ice stream
@@ -845,6 +900,10 @@ def main():
     if args.halfpipe_adjoint:
         if rank == 0:
             run_halfpipe_adjoint(nk, workloads, ctx)
+        return
+    if args.time_gradient:
+        if rank == 0:
+            run_time_gradient(nk, workloads, ctx)
         return
     if args.timestep:
         if rank == 0:
