@@ -2228,9 +2228,9 @@ static void fold(const Grid& g, int& i, int& j) {
 }
 
 // The reverse of step_thickness_stage (no front) at the stored stage: P.H holds the stage thickness (halos filled) and
-// P.phi its centre grounded fraction, P.melt the step's melt (w m); H0 the step start, Hout the stage output.  From λ
+// P.phi its centre grounded fraction, P.melt the step's melt (w m); Hout is the stage output.  From λ
 // of the output (lam_out) it adds λ of H0, u, v, a and the base melt m and writes λ of the stage thickness (lam_Hs).
-static void stage_reverse(Problem& P, const Field& H0, const Field& Hout, double dtau, double w, const Field& lam_out,
+static void stage_reverse(Problem& P, const Field& Hout, double dtau, double w, const Field& lam_out,
                           Field& lam_Hs, Field& lam_H0, VelocityVector& lam_x, Field& lam_smb, Field& lam_melt) {
     const Grid& g = P.grid;
     const int Nx = g.Nx(), Ny = g.Ny();
@@ -2238,7 +2238,6 @@ static void stage_reverse(Problem& P, const Field& H0, const Field& Hout, double
     const bool bounded = adv.scheme == NK_ADVECTION_WENO && adv.bounded;
     const Field& Hs = P.H;
     Field dv(&g, CENTER, CENTER), lam_phi(&g, CENTER, CENTER), lam_theta(&g, CENTER, CENTER);
-    (void)H0;
     lam_Hs.zero();
     for (int j = 1; j <= Ny; ++j)
         for (int i = 1; i <= Nx; ++i) {
@@ -2253,8 +2252,7 @@ static void stage_reverse(Problem& P, const Field& H0, const Field& Hout, double
     auto theta = [&](int ic, int jc) { return bounded ? P.theta(ic, jc) : 1.0; };
     // a face's flux u Δ H_face: λ to the velocity, to the upwind cell (1 - θ), to its θ, and through the face value's
     // derivative to the five stencil cells
-    auto face = [&](double lF, double u, double delta, bool pos, int ic, int jc, int ax, int ay, int f0x, int f0y, bool xdir,
-                    double& lam_u) {
+    auto face = [&](double lF, double u, double delta, bool pos, int ic, int jc, int f0x, int f0y, bool xdir, double& lam_u) {
         Dn s[5];
         double sv[5];
         int px[5], py[5];
@@ -2285,8 +2283,6 @@ static void stage_reverse(Problem& P, const Field& H0, const Field& Hout, double
             fold(g, a, b);
             lam_Hs(a, b) += d * lh0;
         }
-        (void)ax;
-        (void)ay;
     };
     // x faces f = 1 .. Nx + 1 (Nx on a periodic axis, whose face Nx + 1 is face 1)
     int fxmax = g.x.periodic ? Nx : Nx + 1, fymax = g.y.periodic ? Ny : Ny + 1;
@@ -2299,7 +2295,7 @@ static void stage_reverse(Problem& P, const Field& H0, const Field& Hout, double
             double lF = dv(wi, wj) - dv(ei, ej);
             double u = P.x.u(f, j);
             bool east = u > 0;
-            face(lF, u, g.dy_c(j), east, east ? f - 1 : f, j, 0, 0, f, j, true, lam_x.u(f, j));
+            face(lF, u, g.dy_c(j), east, east ? f - 1 : f, j, f, j, true, lam_x.u(f, j));
         }
     for (int f = 1; f <= fymax; ++f)
         for (int i = 1; i <= Nx; ++i) {
@@ -2310,7 +2306,7 @@ static void stage_reverse(Problem& P, const Field& H0, const Field& Hout, double
             double lF = dv(si, sj) - dv(ni, nj);
             double v = P.x.v(i, f);
             bool north = v > 0;
-            face(lF, v, g.dx_c(i), north, i, north ? f - 1 : f, 0, 0, i, f, false, lam_x.v(i, f));
+            face(lF, v, g.dx_c(i), north, i, north ? f - 1 : f, i, f, false, lam_x.v(i, f));
         }
     // θ of each cell, back to the thickness of its own stencils and itself
     if (bounded)
@@ -2353,7 +2349,7 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
     const bool bounded = P.advection.scheme == NK_ADVECTION_WENO && P.advection.bounded;
     const double fractions[3] = {1.0 / 3, 1.0 / 2, 1.0};
     auto weight = [&](int n) { return d.melt_weights ? d.melt_weights[n] : 1.0; };
-    Field base = P.melt, clipped0 = P.clipped;
+    Field base = P.melt;
     std::vector<Field> tape;   // H before each stage, then the final H
     fill_halo(P.H);
     compute_geometry(P);
@@ -2413,7 +2409,7 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
                 for (int j = 0; j <= Ny + 1; ++j)
                     for (int i = 0; i <= Nx + 1; ++i) P.theta(i, j) = bounds_limiter(P.advection, P.H, i, j);
             }
-            stage_reverse(P, tape[3 * n], tape[t + 1], fractions[stg] * d.dt, weight(n), lamH, lamHs, lamH0, lamx, gsmb, gmelt);
+            stage_reverse(P, tape[t + 1], fractions[stg] * d.dt, weight(n), lamH, lamHs, lamH0, lamx, gsmb, gmelt);
             if (stg > 0) lamH = lamHs;
             else for_xy(Nx, Ny, [&](int i, int j) { lamH(i, j) = lamHs(i, j) + lamH0(i, j); });
         }
@@ -2434,7 +2430,6 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
     P.melt = base;
     fill_halo(P.H);
     compute_geometry(P);
-    (void)clipped0;
     return NK_OK;
 }
 
