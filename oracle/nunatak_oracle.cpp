@@ -2060,9 +2060,9 @@ static void advance_front(Problem& P, double dt, bool coupled) {
 // ------------------------------------------------------------------------------------------------
 static void compute_geometry(Problem& P);
 
-// Stage st (0, 1, 2) of one thickness step (rk_substep! then update_state! without the velocity solve); stage 0
-// records the step's starting thickness, which every stage starts from.
-static void step_thickness_stage(Problem& P, double dt, int st, bool coupled) {
+// The tendency and the substep of stage st (0, 1, 2) of one thickness step (rk_substep! before the front's advance);
+// stage 0 records the step's starting thickness, which every stage starts from.
+static void thickness_substep(Problem& P, double dt, int st, bool coupled) {
     const Grid& g = P.grid;
     const int Nx = g.Nx(), Ny = g.Ny();
     const nk_advection_desc adv = P.advection;
@@ -2122,9 +2122,16 @@ static void step_thickness_stage(Problem& P, double dt, int st, bool coupled) {
             if (final_stage) P.clipped(i, j) += std::max(0.0, -Hs);
         });
         fill_halo(P.H);
-        if (final_stage && P.front.enabled) advance_front(P, dtau, coupled);   // rk_substep!, :23
-        compute_geometry(P);
     }
+}
+
+// Stage st (0, 1, 2) of one thickness step: rk_substep! (the substep, then the front's advance after the last stage,
+// :23) and update_state! without the velocity solve (the geometry).
+static void step_thickness_stage(Problem& P, double dt, int st, bool coupled) {
+    thickness_substep(P, dt, st, coupled);
+    const double stages[3] = {1.0 / 3, 1.0 / 2, 1.0};
+    if (st == 2 && P.front.enabled) advance_front(P, stages[st] * dt, coupled);
+    compute_geometry(P);
 }
 
 static void step_thickness(Problem& P, double dt, bool coupled) {
@@ -2231,12 +2238,15 @@ static void fold(const Grid& g, int& i, int& j) {
 // P.phi its centre grounded fraction, P.melt the step's melt (w m); Hout is the stage output.  From λ
 // of the output (lam_out) it adds λ of H0, u, v, a and the base melt m and writes λ of the stage thickness (lam_Hs).
 static void stage_reverse(Problem& P, const Field& Hout, double dtau, double w, const Field& lam_out,
-                          Field& lam_Hs, Field& lam_H0, VelocityVector& lam_x, Field& lam_smb, Field& lam_melt) {
+                          Field& lam_Hs, Field& lam_H0, VelocityVector& lam_x, Field& lam_smb, Field& lam_melt,
+                          const Field* lam_phi_in = nullptr) {
     const Grid& g = P.grid;
     const int Nx = g.Nx(), Ny = g.Ny();
     const nk_advection_desc adv = P.advection;
     const bool bounded = adv.scheme == NK_ADVECTION_WENO && adv.bounded;
     const Field& Hs = P.H;
+    const bool front = P.front.enabled != 0;
+    auto full = [&](int i, int j) { return !front || full_cell(P, i, j); };   // μ with its halo filled
     Field dv(&g, CENTER, CENTER), lam_phi(&g, CENTER, CENTER), lam_theta(&g, CENTER, CENTER);
     lam_Hs.zero();
     for (int j = 1; j <= Ny; ++j)
@@ -2244,10 +2254,10 @@ static void stage_reverse(Problem& P, const Field& Hout, double dtau, double w, 
             double ls = Hout(i, j) > 0 ? lam_out(i, j) : 0.0;   // the clip max(0, H★)
             lam_H0(i, j) += ls;
             dv(i, j) = -dtau * ls / g.Az_ccc(i, j);
-            double lS = dtau * ls;
+            double lS = full(i, j) ? dtau * ls : 0.0;           // sources on full cells only
             lam_smb(i, j) += lS;
             lam_melt(i, j) -= lS * (P.grounding ? 1 - P.phi(i, j) : 1.0) * w;
-            lam_phi(i, j) = P.grounding ? lS * P.melt(i, j) : 0.0;
+            lam_phi(i, j) = (P.grounding ? lS * P.melt(i, j) : 0.0) + (lam_phi_in ? (*lam_phi_in)(i, j) : 0.0);
         }
     auto theta = [&](int ic, int jc) { return bounded ? P.theta(ic, jc) : 1.0; };
     // a face's flux u Δ H_face: λ to the velocity, to the upwind cell (1 - θ), to its θ, and through the face value's
@@ -2294,6 +2304,12 @@ static void stage_reverse(Problem& P, const Field& Hout, double dtau, double w, 
             fold(g, ei, ej);
             double lF = dv(wi, wj) - dv(ei, ej);
             double u = P.x.u(f, j);
+            bool w = full(f - 1, j), e = full(f, j);
+            if (!(w && e)) {   // front_flux_x: the upwind flux out of the full side, nothing between two front cells
+                if (w) { lam_x.u(f, j) += g.dy_c(j) * (u > 0 ? Hs(f - 1, j) : 0.0) * lF; lam_Hs(wi, wj) += g.dy_c(j) * std::max(u, 0.0) * lF; }
+                else if (e) { lam_x.u(f, j) += g.dy_c(j) * (u < 0 ? Hs(f, j) : 0.0) * lF; lam_Hs(ei, ej) += g.dy_c(j) * std::min(u, 0.0) * lF; }
+                continue;
+            }
             bool east = u > 0;
             face(lF, u, g.dy_c(j), east, east ? f - 1 : f, j, f, j, true, lam_x.u(f, j));
         }
@@ -2305,6 +2321,12 @@ static void stage_reverse(Problem& P, const Field& Hout, double dtau, double w, 
             fold(g, ni, nj);
             double lF = dv(si, sj) - dv(ni, nj);
             double v = P.x.v(i, f);
+            bool so = full(i, f - 1), no = full(i, f);
+            if (!(so && no)) {
+                if (so) { lam_x.v(i, f) += g.dx_c(i) * (v > 0 ? Hs(i, f - 1) : 0.0) * lF; lam_Hs(si, sj) += g.dx_c(i) * std::max(v, 0.0) * lF; }
+                else if (no) { lam_x.v(i, f) += g.dx_c(i) * (v < 0 ? Hs(i, f) : 0.0) * lF; lam_Hs(ni, nj) += g.dx_c(i) * std::min(v, 0.0) * lF; }
+                continue;
+            }
             bool north = v > 0;
             face(lF, v, g.dx_c(i), north, i, north ? f - 1 : f, i, f, false, lam_x.v(i, f));
         }
@@ -2342,37 +2364,114 @@ static void copy_in(Field& f, const double* src);
 static void copy_out(const Field& f, double* dst);
 
 // nk_checkpointed_gradient of the library with the velocities held and no front; every stage stored.
+// The front's advance (advance_front without the grounded-melt coupling) as a function of its continuous inputs,
+// with the flag μ and the calved thickness of the step's start held: its H and Hʳ.
+struct FrontInputs {
+    Field H, Hr, smb, melt, phi;
+    VelocityVector x;
+};
+static void front_outputs(Problem& P, const FrontInputs& in, const Field& mu0, double dt, Field& Hout, Field& Hrout) {
+    Field clipped = P.clipped, calved = P.calved;
+    P.H = in.H; P.Hr = in.Hr; P.mu = mu0; P.smb = in.smb; P.melt = in.melt; P.phi = in.phi; P.x = in.x;
+    for (Field* f : {&P.H, &P.Hr, &P.mu, &P.smb, &P.melt, &P.phi}) fill_halo(*f);
+    fill_halo(P.x);
+    advance_front(P, dt, false);
+    Hout = P.H;
+    Hrout = P.Hr;
+    P.clipped = clipped;
+    P.calved = calved;
+}
+// Its reverse by the numerical Jacobian: every input entry moved by ±h, λ of the entry = Σ λ · (output(+) - output(-)) / 2h,
+// with h sized to move the thickness by about 1e-7 of itself or 1e-6 m (the sources over the step), so that the
+// differences keep their digits: 1e-7 of H and Hʳ (at least 1e-7 m), 1e-6 m / Δt of a and m, 1e-3 of φ and 1e-3 of a
+// velocity (the calving rates and front lengths are smooth in it, and the inflow flags hold).
+static void front_reverse_jacobian(Problem& P, const FrontInputs& in, const Field& mu0, double dt, const Field& lamH,
+                                   const Field& lamHr, FrontInputs& lam) {
+    const Grid& g = P.grid;
+    const int Nx = g.Nx(), Ny = g.Ny();
+    Field Hp(&g, CENTER, CENTER), Rp(&g, CENTER, CENTER), Hm(&g, CENTER, CENTER), Rm(&g, CENTER, CENTER);
+    auto entry = [&](Field FrontInputs::*field, bool velocity, bool u, int i, int j, double rel, double floor) {
+        FrontInputs a = in;
+        Field& f = velocity ? (u ? a.x.u : a.x.v) : a.*field;
+        double v0 = f(i, j), h = std::max(rel * std::fabs(v0), floor);
+        f(i, j) = v0 + h;
+        front_outputs(P, a, mu0, dt, Hp, Rp);
+        f(i, j) = v0 - h;
+        front_outputs(P, a, mu0, dt, Hm, Rm);
+        double acc = 0.0;
+        for (int y = 1; y <= Ny; ++y)
+            for (int x = 1; x <= Nx; ++x) acc += lamH(x, y) * (Hp(x, y) - Hm(x, y)) + lamHr(x, y) * (Rp(x, y) - Rm(x, y));
+        return acc / (2 * h);
+    };
+    struct Spec { Field FrontInputs::*f; double rel, floor; };
+    const Spec cells[5] = {{&FrontInputs::H, 1e-7, 1e-7}, {&FrontInputs::Hr, 1e-7, 1e-7}, {&FrontInputs::smb, 0.0, 1e-6 / dt},
+                           {&FrontInputs::melt, 0.0, 1e-6 / dt}, {&FrontInputs::phi, 0.0, 1e-3}};
+    for (const Spec& c : cells) {
+        (lam.*(c.f)).zero();
+        for (int j = 1; j <= Ny; ++j)
+            for (int i = 1; i <= Nx; ++i) (lam.*(c.f))(i, j) = entry(c.f, false, false, i, j, c.rel, c.floor);
+    }
+    lam.x.u.zero();
+    lam.x.v.zero();
+    for (int j = 1; j <= lam.x.u.ny(); ++j)
+        for (int i = 1; i <= lam.x.u.nx(); ++i) lam.x.u(i, j) = entry(nullptr, true, true, i, j, 1e-3, 1e-15);
+    for (int j = 1; j <= lam.x.v.ny(); ++j)
+        for (int i = 1; i <= lam.x.v.nx(); ++i) lam.x.v(i, j) = entry(nullptr, true, false, i, j, 1e-3, 1e-15);
+}
+
+// nk_checkpointed_gradient of the library with the velocities held; every stage stored.  A partial-cell front's
+// advance is reversed through its numerical Jacobian (the oracle's check of the library's hand-written reverse).
 static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_cost_fn cost, void* user, const nk_time_gradient* out,
                                nk_time_gradient_stats* st) {
     const Grid& g = P.grid;
     const int Nx = g.Nx(), Ny = g.Ny(), N = d.steps;
     const bool bounded = P.advection.scheme == NK_ADVECTION_WENO && P.advection.bounded;
+    const bool front = P.front.enabled != 0;
     const double fractions[3] = {1.0 / 3, 1.0 / 2, 1.0};
     auto weight = [&](int n) { return d.melt_weights ? d.melt_weights[n] : 1.0; };
     Field base = P.melt;
-    std::vector<Field> tape;   // H before each stage, then the final H
+    std::vector<Field> tape;                         // H before each stage, then the final H
+    std::vector<Field> mu_start, Hr_start, H3pre;   // a front: μ and Hʳ at each step's start, the last stage's output
     fill_halo(P.H);
     compute_geometry(P);
     for (int n = 0; n < N; ++n) {
         for_xy(Nx, Ny, [&](int i, int j) { P.melt(i, j) = weight(n) * base(i, j); });
+        if (front) {
+            mu_start.push_back(P.mu);
+            Hr_start.push_back(P.Hr);
+        }
         for (int stg = 0; stg < 3; ++stg) {
             tape.push_back(P.H);
-            step_thickness_stage(P, d.dt, stg, false);
+            if (front && stg == 2) {
+                thickness_substep(P, d.dt, stg, false);
+                H3pre.push_back(P.H);
+                advance_front(P, d.dt, false);
+                compute_geometry(P);
+            } else {
+                step_thickness_stage(P, d.dt, stg, false);
+            }
         }
     }
     tape.push_back(P.H);
-    Field Hfinal = P.H, clipped_end = P.clipped;
-    Field lamH(&g, CENTER, CENTER), lamHs(&g, CENTER, CENTER), lamH0(&g, CENTER, CENTER);
+    Field Hfinal = P.H, clipped_end = P.clipped, mu_end = P.mu, Hr_end = P.Hr, calved_end = P.calved;
+    Field lamH(&g, CENTER, CENTER), lamHs(&g, CENTER, CENTER), lamH0(&g, CENTER, CENTER), lamHr(&g, CENTER, CENTER);
     Field gsmb(&g, CENTER, CENTER), gmelt(&g, CENTER, CENTER);
     VelocityVector lamx;
     lamx.init(&g);
+    FrontInputs lamf;
+    if (front) {
+        for (Field* f : {&lamf.H, &lamf.Hr, &lamf.smb, &lamf.melt, &lamf.phi}) f->init(&g, CENTER, CENTER);
+        lamf.x.init(&g);
+    }
     int nu = P.x.u.nx() * P.x.u.ny(), nv = P.x.v.nx() * P.x.v.ny();
     std::vector<double> hH(Nx * Ny), hu(nu), hv(nv), hm(Nx * Ny), gH(Nx * Ny), gu(nu), gv(nv);
     std::memset(st, 0, sizeof(*st));
     st->segments = 1;
     for (int n = N - 1; n >= 0; --n) {
         P.H = tape[3 * n + 3];
+        if (front) P.mu = n + 1 < N ? mu_start[n + 1] : mu_end;
         fill_halo(P.H);
+        fill_halo(P.mu);
         compute_geometry(P);
         copy_out(P.H, hH.data());
         copy_out(P.x.u, hu.data());
@@ -2395,11 +2494,39 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
             for (int j = 1; j <= tu.ny(); ++j) for (int i = 1; i <= tu.nx(); ++i) lamx.u(i, j) += tu(i, j);
             for (int j = 1; j <= tv.ny(); ++j) for (int i = 1; i <= tv.nx(); ++i) lamx.v(i, j) += tv(i, j);
         }
+        if (front) {   // the front's advance after the last stage: its inputs at the step's state
+            P.H = tape[3 * n + 2];
+            P.mu = mu_start[n];
+            fill_halo(P.H);
+            fill_halo(P.mu);
+            compute_geometry(P);   // φ of the last stage's input
+            FrontInputs in;
+            in.H = H3pre[n];
+            in.Hr = Hr_start[n];
+            in.smb = P.smb;
+            in.melt = P.melt;
+            for_xy(Nx, Ny, [&](int i, int j) { in.melt(i, j) = weight(n) * base(i, j); });
+            in.phi = P.phi;
+            in.x = P.x;
+            Field phi2 = P.phi;
+            front_reverse_jacobian(P, in, mu_start[n], d.dt, lamH, lamHr, lamf);
+            lamH = lamf.H;
+            lamHr = lamf.Hr;
+            for_xy(Nx, Ny, [&](int i, int j) {
+                gsmb(i, j) += lamf.smb(i, j);
+                gmelt(i, j) += weight(n) * lamf.melt(i, j);
+            });
+            for (int j = 1; j <= lamx.u.ny(); ++j) for (int i = 1; i <= lamx.u.nx(); ++i) lamx.u(i, j) += lamf.x.u(i, j);
+            for (int j = 1; j <= lamx.v.ny(); ++j) for (int i = 1; i <= lamx.v.nx(); ++i) lamx.v(i, j) += lamf.x.v(i, j);
+            P.phi = phi2;
+        }
         lamH0.zero();
         for (int stg = 2; stg >= 0; --stg) {
             int t = 3 * n + stg;
             P.H = tape[t];
+            if (front) P.mu = mu_start[n];
             fill_halo(P.H);
+            fill_halo(P.mu);
             compute_geometry(P);
             for_xy(Nx, Ny, [&](int i, int j) { P.melt(i, j) = weight(n) * base(i, j); });
             fill_halo(P.melt);
@@ -2409,7 +2536,9 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
                 for (int j = 0; j <= Ny + 1; ++j)
                     for (int i = 0; i <= Nx + 1; ++i) P.theta(i, j) = bounds_limiter(P.advection, P.H, i, j);
             }
-            stage_reverse(P, tape[t + 1], fractions[stg] * d.dt, weight(n), lamH, lamHs, lamH0, lamx, gsmb, gmelt);
+            bool after_front = front && stg == 2;
+            stage_reverse(P, after_front ? H3pre[n] : tape[t + 1], fractions[stg] * d.dt, weight(n), lamH, lamHs, lamH0, lamx,
+                          gsmb, gmelt, after_front ? &lamf.phi : nullptr);
             if (stg > 0) lamH = lamHs;
             else for_xy(Nx, Ny, [&](int i, int j) { lamH(i, j) = lamHs(i, j) + lamH0(i, j); });
         }
@@ -2428,6 +2557,13 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
     P.H = Hfinal;
     P.clipped = clipped_end;
     P.melt = base;
+    if (front) {
+        P.mu = mu_end;
+        P.Hr = Hr_end;
+        P.calved = calved_end;
+        fill_halo(P.mu);
+        fill_halo(P.Hr);
+    }
     fill_halo(P.H);
     compute_geometry(P);
     return NK_OK;
@@ -2722,12 +2858,11 @@ nk_status nko_step_thickness_stage(nko_problem* h, double dt, int32_t stage, int
     return NK_OK;
 }
 
-// nk_checkpointed_gradient for a model whose velocities are held (no velocity solve) and without a front.
+// nk_checkpointed_gradient for a model whose velocities are held (no velocity solve).
 nk_status nko_checkpointed_gradient(nko_problem* h, const nk_time_gradient_desc* d, nk_cost_fn cost, void* user,
                                     const nk_time_gradient* out, nk_time_gradient_stats* stats) {
     if (!h || !d || !cost || !(d->dt > 0) || d->steps < 1 || d->velocity_solves != 0) return NK_BAD_ARGUMENT;
     Problem& P = *reinterpret_cast<Problem*>(h);
-    if (P.front.enabled) return NK_BAD_ARGUMENT;
     nk_time_gradient_stats local{};
     return time_gradient(P, *d, cost, user, out, stats ? stats : &local);
 }

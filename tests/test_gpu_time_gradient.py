@@ -445,16 +445,23 @@ def test_thickness_gradient_through_threshold_calving(gpu_cls):
 
 
 # ---- the library against the oracle's own restatement, every cell ------------------------------------------------------
-@pytest.mark.parametrize("which", ["transport_weno5", "transport_upwind1", "grounding_line_weno5"])
+@pytest.mark.parametrize("which", ["transport_weno5", "transport_upwind1", "grounding_line_weno5", "front_passes4", "front_passes0",
+                                   "eigencalving", "front_velocity_calving"])
 def test_gradient_equals_the_oracle_restatement(gpu_cls, oracle_cls, which):
     """With the velocities held, the oracle restates the gradient through the time steps (nko_checkpointed_gradient: the
-    chain by hand, the local derivatives by forward differentiation of its own forward formulas); the library's ∂J/∂H₀,
-    ∂J/∂(u, v), ∂J/∂a and ∂J/∂m agree with it at every cell and face to 1e-9 of each field's largest entry."""
-    case = {"transport_weno5": lambda: transport_case(None), "transport_upwind1": lambda: transport_case(M.UpwindBiased(order=1)),
-            "grounding_line_weno5": lambda: grounding_line_case(None)}[which]()
+    chain by hand, the local derivatives by forward differentiation of its own forward formulas, and a partial-cell
+    front's advance through its numerical Jacobian); the library's ∂J/∂H₀, ∂J/∂(u, v), ∂J/∂a and ∂J/∂m agree with it at
+    every cell and face to 1e-9 of each field's largest entry, and to 1e-6 with a front (the Jacobian's differences)."""
+    cases = {"transport_weno5": lambda: transport_case(None), "transport_upwind1": lambda: transport_case(M.UpwindBiased(order=1)),
+             "grounding_line_weno5": lambda: grounding_line_case(None), "front_passes4": lambda: channel_front_case(4),
+             "front_passes0": lambda: channel_front_case(0), "eigencalving": lambda: calving_case(M.EigenCalving(coefficient=1e13)),
+             "front_velocity_calving": lambda: calving_case(M.FrontVelocityCalving(front_velocity=1e-6),
+                                                            grounding=M.SubgridGroundedFraction())}
+    case = cases[which]()
+    rtol = 1e-9 if which.startswith(("transport", "grounding")) else 1e-6
     _, ga = gradient(case, gpu_cls)
     _, go = gradient(case, oracle_cls)
     assert abs(ga["J"] - go["J"]) <= 1e-12 * abs(go["J"])
     for key in ("H", "u", "v", "smb", "melt"):
         scale = max(np.max(np.abs(go[key])), 1e-300)
-        assert np.max(np.abs(ga[key] - go[key])) <= 1e-9 * scale, (which, key, np.max(np.abs(ga[key] - go[key])) / scale)
+        assert np.max(np.abs(ga[key] - go[key])) <= rtol * scale, (which, key, np.max(np.abs(ga[key] - go[key])) / scale)

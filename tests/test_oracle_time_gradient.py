@@ -1,13 +1,15 @@
 """The oracle's restatement of the gradient through time steps with the velocities held (nko_checkpointed_gradient)
 against centred differences of its own forward steps, on the CPU: the transport case of test/test_enzyme.jl:447-488
 (16 x 4, sources a and m, eight steps; the default bounded WENO-5 and first-order upwinding) at the reference's cells
-to 1e-6, and the floating melt across a grounding line (the centre grounded fraction) at the partially grounded cells
-to 1e-5.  The library's gradient is held to this one over the whole field in test_gpu_time_gradient."""
+to 1e-6, the floating melt across a grounding line (the centre grounded fraction) at the partially grounded cells
+to 1e-5, and a partial-cell front (its advance reversed through a numerical Jacobian) with and without overflow passes
+and under eigencalving, at the reference's cells (test/test_enzyme.jl:490-536) to 1e-5.  The library's gradient is held to this one over the whole field in test_gpu_time_gradient."""
 import numpy as np
 import pytest
 
 from nunatak_gb300 import model as M
-from test_gpu_time_gradient import _close, fd_final_thickness, gradient, grounding_line_case, transport_case
+from test_gpu_time_gradient import (_close, calving_case, channel_front_case, fd_final_thickness, gradient, grounding_line_case,
+                                    transport_case)
 
 
 @pytest.mark.parametrize("advection", [None, M.UpwindBiased(order=1)], ids=["bounded_weno5", "upwind1"])
@@ -40,3 +42,20 @@ def test_oracle_refuses_velocity_solves(oracle_cls):
     P = case.build(oracle_cls)
     with pytest.raises(Exception):
         P.checkpointed_gradient(lambda *a: None, case.dt, 2, velocity_solves=True)
+
+
+@pytest.mark.parametrize("passes", [4, 0])
+def test_oracle_front_gradient(oracle_cls, passes):
+    case = channel_front_case(passes)
+    _, g = gradient(case, oracle_cls)
+    for idx in ((1, 2), (2, 4)):
+        _close(g["smb"][idx], fd_final_thickness(case, oracle_cls, "surface_mass_balance", idx, 1e-9), 1e-5)
+    H0 = case.build(oracle_cls).get("H")
+    _close(g["H"][2, 3], fd_final_thickness(case, oracle_cls, "H", (2, 3), 1e-6 * H0[2, 3]), 1e-5)
+
+
+def test_oracle_eigencalving_gradient(oracle_cls):
+    case = calving_case(M.EigenCalving(coefficient=1e13))
+    _, g = gradient(case, oracle_cls)
+    for idx in ((1, 3), (2, 3)):
+        _close(g["u"][idx], fd_final_thickness(case, oracle_cls, "u", idx, 1e-12), 1e-5)
