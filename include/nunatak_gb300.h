@@ -506,9 +506,11 @@ nk_status nk_picard_adjoint_gradients(nk_problem* problem, const double* ubar, c
  * The initial velocities are an input, as the model's stored velocities are for the reference (their gradient is
  * the shadow of the velocity fields); the geometry is recomputed from the initial H.  Discrete switches (the clip, the
  * upwind direction, the limiter's branch, walls, masks and the front's flags) are held where the forward run put them;
- * a partial-cell front's advance (its overflow passes and its calving included) is reversed with the stages.  Not
- * covered: von Mises calving (refused), the energy step and its grounded-melt coupling (the stages run uncoupled),
- * and prescribed velocities with velocity solves (refused, as for nk_picard_adjoint). */
+ * a partial-cell front's advance (its overflow passes and its calving included) is reversed with the stages.  Von Mises
+ * rates read the viscosity η̄H of the solve before the front: its adjoint joins that solve's Picard adjoint, as the
+ * shadow of an overwritten coefficient; with the velocities held η̄H is held too.  Not covered: the energy step and
+ * its grounded-melt coupling (the stages run uncoupled), and prescribed velocities with velocity solves (refused, as
+ * for nk_picard_adjoint). */
 typedef struct nk_cost_state {
     int32_t step;              /* the state after this many steps, 1..steps */
     int32_t steps;
@@ -555,7 +557,8 @@ typedef struct nk_time_gradient_stats {
 } nk_time_gradient_stats;
 
 /* Device memory: the checkpoints and one segment's stage states, (⌈steps / K⌉ + 3K + 2) states of 3 planes (DIVA:
- * 6 + Nσ; a front: 2 more) plus about 25 planes of adjoints, allocated for the call and freed before it returns.
+ * 6 + Nσ; a front: 2 more, 3 with von Mises calving) plus about 25 planes of adjoints, allocated for the call and freed
+ * before it returns.
  * After an error the problem's fields are those of whichever step the sweep had reached. */
 nk_status nk_checkpointed_gradient(nk_problem* problem, const nk_time_gradient_desc* desc, nk_cost_fn cost, void* user,
                                    const nk_time_gradient* out, nk_time_gradient_stats* stats);

@@ -902,6 +902,7 @@ __global__ void k_adjoint_viscosity(AdjointView v) {
     double eb = v.cbar[k].x;
     for (int a = 0; a < nx; ++a)
         for (int b = 0; b < ny; ++b) eb += (wx[a] * wy[b]) * v.cbar[g.idx(fx[a], fy[b])].y / 4;
+    if (v.eta_bar_in) eb -= v.eta_bar_in[k];   // eb is λ-signed: minus the true adjoint
     const PhysView& ph = v.ph;
     double S = effective_strain_rate2(g, v.xs, ph.ud, i, j, ph.wall_factor) + ph.eps0 * ph.eps0;
     v.gbar[k] = eb * v.o.coef[k].x * ((1 - ph.n) / (2 * ph.n)) / S;
@@ -1195,6 +1196,7 @@ __global__ void k_adjoint_thickness(AdjointView v, GeometryView gv, int diva, do
         double eb = v.cbar[c].x;
         for (int a = 0; a < nx; ++a)
             for (int b = 0; b < ny; ++b) eb += (wx[a] * wy[b]) * v.cbar[g.idx(fx[a], fy[b])].y / 4;
+        if (v.eta_bar_in) eb -= v.eta_bar_in[c];
         double etab = 0.0;
         for (int l = 0; l < ph.sig.N; ++l) etab += v.eta_sigma[(long long)l * ph.plane + c] * ph.sig.dz[l];
         double mu = ph.use_mask ? ph.mu[c] : 1.0;
@@ -1311,6 +1313,7 @@ __global__ void k_adjoint_diva_centre(AdjointView v) {
     double eb = v.cbar[k].x;
     for (int a = 0; a < nx; ++a)
         for (int b = 0; b < ny; ++b) eb += (wx[a] * wy[b]) * v.cbar[g.idx(fx[a], fy[b])].y / 4;
+    if (v.eta_bar_in) eb -= v.eta_bar_in[k];   // λ-signed like cbar
     double H = ph.H[k];
     double etabar_b = -eb * (ph.use_mask ? ph.mu[k] : 1.0) * H;     // ∂J/∂η̄
     double F2b = v.sig_F2[k] + face_mean_gather(g, i, j, k, [&](int fi, int fj, int kf, int comp) {

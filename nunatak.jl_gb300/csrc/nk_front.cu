@@ -641,6 +641,10 @@ __device__ __forceinline__ Dual dsqrt(Dual a) { double r = sqrt(a.v); return {r,
 __device__ __forceinline__ Dual dabs(Dual a) { return a.v >= 0 ? a : Dual{-a.v, -a.d}; }
 __device__ __forceinline__ Dual dmax(Dual a, Dual b) { return fmax(a.v, b.v) == a.v ? a : b; }
 __device__ __forceinline__ Dual dpos(Dual a) { return a.v > 0 ? a : Dual{0.0, 0.0}; }   // fmax(a, 0)
+__device__ __forceinline__ Dual dpow(Dual a, double p) {
+    double r = pow(a.v, p);
+    return {r, a.d != 0.0 ? p * pow(a.v, p - 1) * a.d : 0.0};
+}
 
 // The flag-masked face velocities of mu_u / mu_v with the seed's derivative: seed_u / seed_v is the stored index of
 // the seeded u / v face (-1: none).
@@ -666,19 +670,82 @@ __device__ __forceinline__ Dual dstrain_xy(const FrontView& v, int i, int j, See
     Dual e = (dudy + dvdx) / 2.0;
     return g.peripheral_ff(i, j) ? v.wall_factor * e : e;
 }
-// calving_rate of a full cell (calving.jl:154-190) for the eigencalving and front-velocity laws, with the seed's
-// derivative (principal_strain_rates and front_flow_speed as k_calve_fraction evaluates them)
+// the wall-masked velocities and strain rates of effective_strain_rate2, with the seed's derivative
+__device__ __forceinline__ Dual dwall_u(const FrontView& v, int i, int j, Seed sd) {
+    const DevGrid<double>& g = v.g;
+    if (g.peripheral_fc(i, j)) return {0.0, 0.0};
+    int k = g.u_idx(i, j);
+    return {v.x[k].x, k == sd.u ? 1.0 : 0.0};
+}
+__device__ __forceinline__ Dual dwall_v(const FrontView& v, int i, int j, Seed sd) {
+    const DevGrid<double>& g = v.g;
+    if (g.peripheral_cf(i, j)) return {0.0, 0.0};
+    int k = g.v_idx(i, j);
+    return {v.x[k].y, k == sd.v ? 1.0 : 0.0};
+}
+__device__ __forceinline__ Dual dwall_strain_xy2(const FrontView& v, int i, int j, Seed sd) {
+    const DevGrid<double>& g = v.g;
+    Dual dudy = (dwall_u(v, i, j, sd) - dwall_u(v, i, j - 1, sd)) / g.dyf[j];
+    Dual dvdx = (dwall_v(v, i, j, sd) - dwall_v(v, i - 1, j, sd)) / g.dxf[i];
+    Dual e = (dudy + dvdx) / 2.0;
+    e = g.peripheral_ff(i, j) ? v.wall_factor * e : e;
+    return e * e;
+}
+__device__ Dual deffective_strain_rate2(const FrontView& v, int i, int j, Seed sd) {
+    const DevGrid<double>& g = v.g;
+    Dual exx = (dwall_u(v, i + 1, j, sd) - dwall_u(v, i, j, sd)) / g.dxc[i];
+    Dual eyy = (dwall_v(v, i, j + 1, sd) - dwall_v(v, i, j, sd)) / g.dyc[j];
+    Dual a = (dwall_strain_xy2(v, i, j, sd) + dwall_strain_xy2(v, i + 1, j, sd)) / 2.0;
+    Dual b = (dwall_strain_xy2(v, i, j + 1, sd) + dwall_strain_xy2(v, i + 1, j + 1, sd)) / 2.0;
+    return exx * exx + eyy * eyy + exx * eyy + (a + b) / 2.0;
+}
+// principal_strain_rates (calving.jl:144-152) with the seed's derivative
+__device__ __forceinline__ void dprincipal_strain_rates(const FrontView& v, int i, int j, Seed sd, Dual& e1, Dual& e2) {
+    const DevGrid<double>& g = v.g;
+    Dual exx = (dmu_u(v, i + 1, j, sd) - dmu_u(v, i, j, sd)) / g.dxc[i];
+    Dual eyy = (dmu_v(v, i, j + 1, sd) - dmu_v(v, i, j, sd)) / g.dyc[j];
+    Dual exy = ((dstrain_xy(v, i, j, sd) + dstrain_xy(v, i + 1, j, sd)) / 2.0 +
+                (dstrain_xy(v, i, j + 1, sd) + dstrain_xy(v, i + 1, j + 1, sd)) / 2.0) / 2.0;
+    Dual eb = (exx + eyy) / 2.0;
+    Dual h = (exx - eyy) / 2.0;
+    Dual r = dsqrt(h * h + exy * exy + Dual{v.eps0 * v.eps0, 0.0});
+    e1 = eb + r;
+    e2 = eb - r;
+}
+// The von Mises rate of a full cell (calving.jl:160-174) at viscosity eta, with the seed's derivative, in the order
+// calving_rate evaluates it; the rate is linear in eta, so eta = 1 gives its derivative with respect to eta.
+__device__ Dual dvon_mises_rate(const FrontView& v, int i, int j, Seed sd, double eta) {
+    const DevGrid<double>& g = v.g;
+    int k = g.c_idx(i, j);
+    Dual e1, e2;
+    dprincipal_strain_rates(v, i, j, sd, e1, e2);
+    double n = v.n, e0 = v.eps0;
+    Dual p1 = dpos(e1), p2 = dpos(e2);
+    Dual et2 = (p1 * p1 + p2 * p2) / 2.0;
+    Dual ee2 = deffective_strain_rate2(v, i, j, sd) + Dual{e0 * e0, 0.0};
+    double smax = v.phi[k] * v.stress_threshold + (1 - v.phi[k]) * v.floating_stress_threshold;
+    Dual B = (2 * eta) * dpow(ee2, (n - 1) / (2 * n));
+    Dual sig = sqrt(3.0) * B * et2 * dpow(et2 + Dual{e0 * e0, 0.0}, (1 - 2 * n) / (2 * n));
+    Dual ut = dmax(dabs(dmu_u(v, i, j, sd)), dabs(dmu_u(v, i + 1, j, sd)));
+    Dual vt = dmax(dabs(dmu_v(v, i, j, sd)), dabs(dmu_v(v, i, j + 1, sd)));
+    double e = e0 * g.dxc[i];
+    Dual fs = dsqrt(ut * ut + vt * vt + Dual{e * e, 0.0});
+    return fs * sig / smax;
+}
+// η = η̄H / H of cell k as the von Mises rate reads it
+__device__ __forceinline__ double von_mises_eta(const FrontView& v, int k) {
+    double Hi = v.H[k];
+    return v.coef[k].x / (Hi > 0 ? Hi : 1.0);
+}
+// calving_rate of a full cell (calving.jl:154-190) for the rate laws, with the seed's derivative (principal_strain_rates
+// and front_flow_speed as k_calve_fraction evaluates them)
 __device__ Dual dcalving_rate(const FrontView& v, int i, int j, Seed sd) {
     const DevGrid<double>& g = v.g;
+    if (v.law == NK_CALVING_VON_MISES) return dvon_mises_rate(v, i, j, sd, von_mises_eta(v, g.c_idx(i, j)));
     if (v.law == NK_CALVING_EIGEN) {
-        Dual exx = (dmu_u(v, i + 1, j, sd) - dmu_u(v, i, j, sd)) / g.dxc[i];
-        Dual eyy = (dmu_v(v, i, j + 1, sd) - dmu_v(v, i, j, sd)) / g.dyc[j];
-        Dual exy = ((dstrain_xy(v, i, j, sd) + dstrain_xy(v, i + 1, j, sd)) / 2.0 +
-                    (dstrain_xy(v, i, j + 1, sd) + dstrain_xy(v, i + 1, j + 1, sd)) / 2.0) / 2.0;
-        Dual eb = (exx + eyy) / 2.0;
-        Dual h = (exx - eyy) / 2.0;
-        Dual r = dsqrt(h * h + exy * exy + Dual{v.eps0 * v.eps0, 0.0});
-        return v.coefficient * (dpos(eb + r) * dpos(eb - r));
+        Dual e1, e2;
+        dprincipal_strain_rates(v, i, j, sd, e1, e2);
+        return v.coefficient * (dpos(e1) * dpos(e2));
     }
     if (v.law == NK_CALVING_FRONT_VELOCITY) {
         Dual ut = dmax(dabs(dmu_u(v, i, j, sd)), dabs(dmu_u(v, i + 1, j, sd)));
@@ -716,7 +783,9 @@ __device__ Dual dfront_length(const FrontView& v, int i, int j, const FrontLengt
     }
     return (Dual{f.lw + f.le, 0.0} * ub + Dual{f.ls + f.ln, 0.0} * vb) / speed;
 }
-__device__ __forceinline__ bool rate_law(int law) { return law == NK_CALVING_EIGEN || law == NK_CALVING_FRONT_VELOCITY; }
+__device__ __forceinline__ bool rate_law(int law) {
+    return law == NK_CALVING_EIGEN || law == NK_CALVING_FRONT_VELOCITY || law == NK_CALVING_VON_MISES;
+}
 __device__ __forceinline__ bool removal_law(int law) {
     return law == NK_CALVING_THICKNESS_THRESHOLD || law == NK_CALVING_MAXIMUM_EXTENT;
 }
@@ -880,7 +949,8 @@ __global__ void k_calve_rev_rate(FrontAdjointView a) {
 }
 
 // λ of the face velocities: per face, every cell whose rate or front length reads it (cells within one column and
-// row of the face), each differentiated along that face.  The front-velocity law's (1 - φ) sends λ to φ too.
+// row of the face), each differentiated along that face.  The front-velocity law's (1 - φ) sends λ to φ too; the von
+// Mises rate sends λ to the cell's own H and η̄H (through η = η̄H / H) and to φ (through σᵐᵃˣ).
 __global__ void k_calve_rev_velocity(FrontAdjointView a) {
     FrontView v = a.f;
     const DevGrid<double>& g = v.g;
@@ -931,6 +1001,21 @@ __global__ void k_calve_rev_velocity(FrontAdjointView a) {
             double fs = sqrt(ut.v * ut.v + vt.v * vt.v + e * e);
             a.lam_phi[k] += -a.lam_g[k] * fmax(fs - v.front_velocity, 0.0);
         }
+    }
+    if (v.law == NK_CALVING_VON_MISES && i < g.Nx && j < g.Ny) {
+        double lg = a.lam_g[k], le = 0.0;
+        if (lg != 0.0) {
+            Seed none{-1, -1};
+            double Hi = v.H[k], etaH = v.coef[k].x;
+            double unit = dvon_mises_rate(v, i, j, none, 1.0).v;   // ∂c/∂η
+            double Hd = Hi > 0 ? Hi : 1.0;
+            le = lg * unit / Hd;
+            if (Hi > 0) a.lam_a[k] += -lg * unit * etaH / (Hi * Hi);
+            double smax = v.phi[k] * v.stress_threshold + (1 - v.phi[k]) * v.floating_stress_threshold;
+            double c = dvon_mises_rate(v, i, j, none, etaH / Hd).v;
+            a.lam_phi[k] += -lg * c * (v.stress_threshold - v.floating_stress_threshold) / smax;
+        }
+        if (a.lam_eta) a.lam_eta[k] = le;
     }
 }
 

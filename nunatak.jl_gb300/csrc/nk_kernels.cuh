@@ -163,6 +163,9 @@ struct AdjointView {
     double2* bbt = nullptr;           // per face: ∂J/∂βᵇ (all paths)
     double2* hmu = nullptr;           // when set, the centre pass writes per centre (∂J/∂H through η̄H and F₂ at
                                       // fixed μ, ∂J/∂μ through η̄H): the thickness gradient's coefficient part
+    // when set, ∂J/∂η̄H per centre from outside the solve (a true adjoint): the shadow of the overwritten coefficient
+    // η̄H, which the fixed point's reverse carries with the operator's own η̄H adjoint in every pass
+    const double* eta_bar_in = nullptr;
 };
 void launch_adjoint_coefficients(const AdjointView& v, cudaStream_t s);
 void launch_adjoint_viscosity(const AdjointView& v, cudaStream_t s);
@@ -281,10 +284,12 @@ struct FrontAdjointView {
     double* lam_smb; double* lam_melt;   // +=
     double* lam_phi;                  // = λ of φ of the forced cells' melt
     double* lam_a; double* lam_b; double* lam_c; double* lam_d;   // scratch planes
-    // calving (f.law a rate law or a removal law; von Mises is not covered): λ of the retreat fraction, of each
-    // cell's calving rate as used and as computed, of its ocean-facing length, and the λ of the velocities it adds
+    // calving (f.law a rate law or a removal law): λ of the retreat fraction, of each cell's calving rate as used and
+    // as computed, of its ocean-facing length, and the λ of the velocities it adds
     double* lam_e; double* lam_f; double* lam_g; double* lam_h;
     double2* lam_x;
+    // von Mises: when set, = λ of the depth-averaged viscosity η̄H (f.coef[].x) per cell that the rates read (η = η̄H / H)
+    double* lam_eta = nullptr;
 };
 // The drain, the reference pass, the overflow passes and the calving of advance_front! on v's planes (v.H, v.mu, v.Hr
 // set by the caller to the state before it), recording into snaps (front_record_planes of them): per level

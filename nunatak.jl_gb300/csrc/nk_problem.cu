@@ -1915,7 +1915,9 @@ static void ensure_adjoint(nk_problem* P, bool want_H) {
 
 // The adjoint with x̄ already in P->adj_xbar (ensure_adjoint first): leaves λ in tmp_a, ∂J/∂log C in adj_grad,
 // ∂J/∂log A in adj_grad_A (want_A) and ∂J/∂H in adj_g (want_H), and U, V = x* again.
-static void picard_adjoint_device(nk_problem* P, const nk_iteration_control& ctl, bool want_A, bool want_H, nk_solve_stats* st) {
+// eta_bar_in: ∂J/∂η̄H per centre from outside the solve (NULL: none), carried through every pass
+static void picard_adjoint_device(nk_problem* P, const nk_iteration_control& ctl, bool want_A, bool want_H, nk_solve_stats* st,
+                                  const double* eta_bar_in = nullptr) {
     const bool diva = P->pd.stress_balance == NK_DIVA;
     cudaStream_t s = P->stream;
     size_t pl = P->plane;
@@ -1956,6 +1958,7 @@ static void picard_adjoint_device(nk_problem* P, const nk_iteration_control& ctl
     v.grad_log_C = P->adj_grad;
     v.eta_sigma = P->eta_sigma;
     v.grad_log_A = nullptr;   // only in the final pass
+    v.eta_bar_in = eta_bar_in;
     bool fixed = ctl.kind == NK_FIXED_ITERATIONS;
     int limit = fixed ? ctl.iterations : ctl.maxiter;
     int it = 0, cg_total = 0, cg_last = 0;
@@ -2071,17 +2074,25 @@ namespace nk {
 // A stored state: H, (U, V), and for the DIVA the lagged beta_b, F2 and eta_sigma its next Picard step reads
 // (diva.jl:77-80; the vertical shear of _compute_shear_viscosity! divides by the previous viscosity), so that a
 // restored state re-runs bit for bit and the adjoint of a solve linearises where the solve ended.
-// With a partial-cell front the flag μ and the front thickness Hʳ follow them (the step's last stage moves the front).
-static int time_state_planes(const nk_problem* P, bool diva) { return (diva ? 6 + P->Ns : 3) + (P->front.enabled ? 2 : 0); }
+// With a partial-cell front the flag μ and the front thickness Hʳ follow them (the step's last stage moves the front),
+// and under von Mises calving the depth-averaged viscosity η̄H its rates read (the last Picard step's coefficient).
+static bool von_mises_front(const nk_problem* P) { return P->front.enabled && P->front.calving == NK_CALVING_VON_MISES; }
+static int time_state_base(const nk_problem* P, bool diva) { return diva ? 6 + P->Ns : 3; }
+static int time_state_planes(const nk_problem* P, bool diva) {
+    return time_state_base(P, diva) + (P->front.enabled ? 2 : 0) + (von_mises_front(P) ? 1 : 0);
+}
 static void save_time_state(nk_problem* P, double* rec, bool diva) {
     const size_t pl = P->plane;
     cudaStream_t s = P->stream;
     NK_CUDA(cudaMemcpyAsync(rec, P->H, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
     NK_CUDA(cudaMemcpyAsync(rec + pl, P->x, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));
     if (P->front.enabled) {
-        double* f = rec + (size_t)(time_state_planes(P, diva) - 2) * pl;
+        double* f = rec + (size_t)time_state_base(P, diva) * pl;
         NK_CUDA(cudaMemcpyAsync(f, P->mu, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
         NK_CUDA(cudaMemcpyAsync(f + pl, P->front_buf, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        if (von_mises_front(P))   // η̄H = coef[].x, one double of every double4
+            NK_CUDA(cudaMemcpy2DAsync(f + 2 * pl, sizeof(double), P->fine.coef, sizeof(double4), sizeof(double), pl,
+                                      cudaMemcpyDeviceToDevice, s));
     }
     if (diva) {
         NK_CUDA(cudaMemcpyAsync(rec + 3 * pl, P->bb, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));
@@ -2095,9 +2106,12 @@ static void load_time_state(nk_problem* P, const double* rec, bool diva) {
     NK_CUDA(cudaMemcpyAsync(P->H, rec, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
     NK_CUDA(cudaMemcpyAsync(P->x, rec + pl, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));
     if (P->front.enabled) {
-        const double* f = rec + (size_t)(time_state_planes(P, diva) - 2) * pl;
+        const double* f = rec + (size_t)time_state_base(P, diva) * pl;
         NK_CUDA(cudaMemcpyAsync(P->mu, f, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
         NK_CUDA(cudaMemcpyAsync(P->front_buf, f + pl, pl * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        if (von_mises_front(P))
+            NK_CUDA(cudaMemcpy2DAsync(P->fine.coef, sizeof(double4), f + 2 * pl, sizeof(double), sizeof(double), pl,
+                                      cudaMemcpyDeviceToDevice, s));
     }
     if (diva) {
         NK_CUDA(cudaMemcpyAsync(P->bb, rec + 3 * pl, pl * sizeof(double2), cudaMemcpyDeviceToDevice, s));
@@ -2121,7 +2135,7 @@ struct TimeGradient {
     double* mem = nullptr;
     // scratch planes
     double *lamH, *lamHs, *lamH0, *dv, *lamphi, *g_smb, *g_melt, *base_melt, *clipped_end, *g_logC, *g_logA;
-    double *h3pre, *lamHr, *lamphi_front;                    // the front's reverse
+    double *h3pre, *lamHr, *lamphi_front, *lam_eta;          // the front's reverse (lam_eta: λ of η̄H, von Mises)
     double* fmem = nullptr;                                     // its record and scratch (front_planes())
     double2 *lamF, *lwx, *lwy, *lamx_stage, *lamx_carry, *lamu_held;
     std::vector<double> hH, hu, hv, hmask, gH, gu, gv;
@@ -2153,7 +2167,7 @@ struct TimeGradient {
         lamH = one(0); lamHs = one(1); lamH0 = one(2); dv = one(3); lamphi = one(4); g_smb = one(5); g_melt = one(6);
         base_melt = one(7); clipped_end = one(8); g_logC = one(9);
         lamF = two(10); lwx = two(12); lwy = two(14); lamx_stage = two(16); lamx_carry = two(18); lamu_held = two(20);
-        h3pre = one(22); lamHr = one(23); lamphi_front = one(24);
+        h3pre = one(22); lamHr = one(23); lamphi_front = one(24); lam_eta = one(25);
         if (front) NK_CUDA(cudaMalloc(&fmem, (size_t)front_planes() * pl * sizeof(double)));
         g_logA = one(27);
     }
@@ -2173,11 +2187,12 @@ struct TimeGradient {
             if (solves) solve();
         }
     }
-    // the Picard adjoint of the solve that ended in the loaded state, for x̄ = xbar: λ_H += ∂J/∂H, log C, log A
-    void solve_adjoint(const double2* xbar, double* lam_H) {
+    // the Picard adjoint of the solve that ended in the loaded state, for x̄ = xbar and, when set, the adjoint of the
+    // viscosity η̄H it left (eta_bar): λ_H += ∂J/∂H, log C, log A
+    void solve_adjoint(const double2* xbar, double* lam_H, const double* eta_bar = nullptr) {
         NK_CUDA(cudaMemcpyAsync(P->adj_xbar, xbar, pl * sizeof(double2), cudaMemcpyDeviceToDevice, P->stream));
         nk_solve_stats ss{};
-        picard_adjoint_device(P, ctl, true, true, &ss);
+        picard_adjoint_device(P, ctl, true, true, &ss, eta_bar);
         ++st->picard_adjoints;
         st->adjoint_iterations += ss.picard_iterations;
         worst(ss.status);
@@ -2248,7 +2263,9 @@ struct TimeGradient {
 
     // The reverse of the front's advance after the last stage of step n (local k): the stage's output before the front is
     // recomputed from the stored stage input; λ of H after the front (lamH) becomes λ of that output (lam_out), λ of Hʳ
-    // passes back through the step (lamHr), and the forced cells' melt leaves λ of φ for the stage's reverse.
+    // passes back through the step (lamHr), and the forced cells' melt leaves λ of φ for the stage's reverse.  Von Mises
+    // rates read the viscosity η̄H the stage's solve left (restored with the state): its λ (lam_eta) joins that solve's
+    // adjoint; with the velocities held η̄H is held too.
     void front_reverse(int n, int k, double* lam_out) {
         static const double last = 1.0;
         cudaStream_t s = P->stream;
@@ -2293,6 +2310,7 @@ struct TimeGradient {
         fa.lam_g = fplane(9);
         fa.lam_h = fplane(10);
         fa.lam_x = front_lamx();
+        fa.lam_eta = von_mises_front(P) && solves ? lam_eta : nullptr;
         NK_CUDA(cudaMemsetAsync(fa.lam_x, 0, pl * sizeof(double2), s));
         launch_front_adjoint(fa, s);
         NK_CHECK_LAUNCH();
@@ -2349,7 +2367,8 @@ struct TimeGradient {
                     if (front && stg == 2 && P->front.calving != NK_CALVING_NONE)   // the calving rates read the stage's velocities
                         launch_add_pairs(g, lamx_stage, front_lamx(), s);
                     if (stg > 0) {
-                        if (solves) solve_adjoint(lamx_stage, lam_in);   // the solve that made x_t from H_t
+                        // the solve that made x_t from H_t (and, before the front, η̄H)
+                        if (solves) solve_adjoint(lamx_stage, lam_in, front && stg == 2 && von_mises_front(P) ? lam_eta : nullptr);
                         else launch_add_pairs(g, lamu_held, lamx_stage, s);
                     } else {
                         launch_add_planes(g, lam_in, lamH0, 1, pl, s);  // stage 1 reads H⁻ as its stage thickness
@@ -2399,8 +2418,6 @@ nk_status nk_checkpointed_gradient(nk_problem* P, const nk_time_gradient_desc* d
         if (desc->steps < 1) bad("steps must be at least 1");
         if (desc->checkpoint_interval < 0) bad("checkpoint_interval must be non-negative");
         if (desc->velocity_solves != 0 && desc->velocity_solves != 1) bad("velocity_solves is 0 or 1");
-        if (P->front.enabled && P->front.calving == NK_CALVING_VON_MISES)
-            bad("the gradient through time steps does not cover von Mises calving (its rate reads the viscosity)");
         if (desc->velocity_solves && P->ud) bad("the gradient through velocity solves is not available with prescribed velocities");
         if (desc->melt_weights)
             for (int n = 0; n < desc->steps; ++n)

@@ -536,7 +536,7 @@ end
 gradient of `cost(model)` after them, on the GPU, by nk_checkpointed_gradient.  The gradient with respect to the
 initial thickness and velocities, the surface mass balance, the basal melt rate, the friction coefficient and the
 rate factor accumulates into `dmodel`; `model` is left at the final state; returns the cost.  The cost itself is
-differentiated by Enzyme on the host.  Not covered by the library: von Mises calving and the energy step.
+differentiated by Enzyme on the host.  Not covered by the library: the energy step.
 """
 function checkpointed_gradient!(dmodel, cost, model, Δt, Nt; checkpoint_interval = ceil(Int, sqrt(Nt)),
                                 solver::GB300StressBalanceSolver = model.velocity_solver.linear_solver, melt_weights = nothing)

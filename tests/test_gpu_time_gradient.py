@@ -17,7 +17,11 @@ step_thickness_stage followed by picard_solve for each stage), J = Σ H² after 
   0 < φ < 1 runs through the centre grounded fraction of the melt source, and ∂J/∂m at floating cells;
 - a cost at two steps with per-step melt factors (the structure of the STREAMICE halfpipe adjoint,
   benchmarks/halfpipe_streamice_adjoint.jl:50-64: velocities after step 2, thickness after step 3, melt weights
-  0.5, 1, 0.5): ∂J/∂m and ∂J/∂H₀ on the ridge to 1e-5.
+  0.5, 1, 0.5): ∂J/∂m and ∂J/∂H₀ on the ridge to 1e-5;
+- a partial-cell front with its overflow passes and its calving laws (test/test_enzyme.jl:490-536), von Mises calving
+  with the velocities held and, on a confined floating shelf, through Picard solves (its rates read the viscosity of
+  the solve before the front);
+- with the velocities held, the library's gradient equals the oracle's restatement over every cell and face.
 A difference is formed as Σ (x₊ - x₋)(x₊ + x₋) / 2δ from the two perturbed runs, never as the difference of two
 rounded costs."""
 import math
@@ -381,20 +385,13 @@ def test_surface_mass_balance_through_the_partial_cell_front(gpu_cls, passes):
         _close(g["H"][idx], fd_final_thickness(case, gpu_cls, "H", idx, 1e-6 * H0[idx]), 1e-6)
 
 
-def test_von_mises_calving_is_refused(gpu_cls):
-    case = channel_front_case()
-    P = case.build(gpu_cls)
-    P.set_front(M.PartialCellFront(passes=2, calving=M.VonMisesCalving(stress_threshold=1e5)))
-    with pytest.raises(Exception):
-        P.checkpointed_gradient(thickness_cost(2), case.dt, 2, velocity_solves=False)
-
-
 # ---- calving (test/test_enzyme.jl:516-536) -----------------------------------------------------------------------------
 def calving_case(law, steps=1, grounding=None):
     """The reference's eigencalving case: a 12 x 6 shelf on a bed 500 m deep, 100 m of ice west of 4 km, spreading at
     u = a x, v = b y (a = b = 1e-9 /s), the front's four overflow passes; one step of 1e7 s with the velocities held
     (the stages move ice too, where the reference's cost advances the front alone).  The front-velocity law calves
-    floating ice only ((1 - φ) c), so its case takes the subgrid grounded fraction."""
+    floating ice only ((1 - φ) c), so its case takes the subgrid grounded fraction.  η̄H = 10¹⁴ H (held with the
+    velocities) is read by the von Mises law alone."""
     dx, Hi, a, b = 1e3, 100.0, 1e-9, 1e-9
     grid = M.RectilinearGrid(size=(12, 6), x=(0.0, 12 * dx), y=(0.0, 6 * dx), halo=(4, 4))
 
@@ -407,6 +404,7 @@ def calving_case(law, steps=1, grounding=None):
         P.compute_geometry()
         set_fn(P, "u", lambda x, y: a * x)
         set_fn(P, "v", lambda x, y: b * y)
+        P.set("eta_H", 1e14 * np.maximum(P.get("H"), 1.0))
         P.energy_set("surface_mass_balance", 0.0)
         P.energy_set("basal_melt_rate", 0.0)
         P.energy_set("clipped_thickness", 0.0)
@@ -415,12 +413,17 @@ def calving_case(law, steps=1, grounding=None):
     return Case(build, 1e7, steps, solves=False)
 
 
-@pytest.mark.parametrize("law", [M.EigenCalving(coefficient=1e13), M.FrontVelocityCalving(front_velocity=1e-6)],
-                         ids=["eigen", "front_velocity"])
+VON_MISES = M.VonMisesCalving(stress_threshold=1e6, floating_stress_threshold=2e5)
+
+
+@pytest.mark.parametrize("law", [M.EigenCalving(coefficient=1e13), M.FrontVelocityCalving(front_velocity=1e-6), VON_MISES],
+                         ids=["eigen", "front_velocity", "von_mises"])
 def test_velocity_gradient_through_calving(gpu_cls, law):
     """∂J/∂u of J = Σ H² at the faces the reference checks (its cells (4, 2) and (4, 3)), through the retreat the rate
-    law sets from the strain rates or the front speed, to 1e-5 (the reference's tolerance and h = 1e-12)."""
-    case = calving_case(law, grounding=M.SubgridGroundedFraction() if isinstance(law, M.FrontVelocityCalving) else None)
+    law sets from the strain rates or the front speed, to 1e-5 (the reference's tolerance and h = 1e-12); ∂J/∂H₀ also
+    runs through η = η̄H / H of the von Mises rate."""
+    grounded = isinstance(law, (M.FrontVelocityCalving, M.VonMisesCalving))
+    case = calving_case(law, grounding=M.SubgridGroundedFraction() if grounded else None)
     P0 = case.build(gpu_cls)
     _, g = gradient(case, gpu_cls)
     assert not np.any(np.isnan(g["u"]))
@@ -444,9 +447,62 @@ def test_thickness_gradient_through_threshold_calving(gpu_cls):
         _close(g["H"][idx], fd_final_thickness(case, gpu_cls, "H", idx, 1e-6 * H0[idx]), 1e-6)
 
 
+def shelf_case(diva=False):
+    """A floating shelf in a channel with free-slip walls (Bounded x Bounded, 16 x 4 cells of 2 km, 400 m thinning
+    east and thicker mid-channel, ice west of 20 km over a bed 2 km deep), PartialCellFront under von Mises calving,
+    a converged Picard solve after every stage, two steps of 2e8 s: the rates read the viscosity η̄H of the solve
+    before the front."""
+    L, Ly, xf = 32e3, 8e3, 20e3
+    grid = M.RectilinearGrid(size=(16, 4), x=(0.0, L), y=(0.0, Ly), topology=("Bounded", "Bounded"), halo=(4, 4))
+    solver = M.StressBalanceSolver(linear_iteration_control=M.Convergence(reltol=1e-15, maxiter=10_000),
+                                   picard_iteration_control=M.Convergence(reltol=1e-14, maxiter=1000),
+                                   adjoint_iteration_control=M.Convergence(reltol=1e-14, maxiter=2000))
+    sb = M.DepthIntegrated(shear=M.DIVAShear()) if diva else None
+    law = M.VonMisesCalving(stress_threshold=3e6, floating_stress_threshold=1e6)
+
+    def build(cls):
+        P = make(cls, grid, advection=M.UpwindBiased(order=1), Nsigma=6 if diva else 4, masking=M.PartialCellFront(calving=law),
+                 rheology=M.GlenFlowLaw(rate_factor=1e-24), friction=M.WeertmanFriction(coefficient=1e6),
+                 grounding=M.SubgridGroundedFraction(), stress_balance=sb, velocity_solver=solver)
+        set_fn(P, "H", lambda x, y: 400 - 4e-3 * x + 20 * math.sin(math.pi * y / Ly) if x < xf else 0.0)
+        P.set("bed", -2000.0)
+        P.set("A", 1e-24)
+        P.set("C", 1e6)
+        P.compute_geometry()
+        P.initialize_front()
+        P.compute_geometry()
+        set_fn(P, "u", lambda x, y: 1e-9 * x)
+        P.set("v", 0.0)
+        P.energy_set("surface_mass_balance", 0.0)
+        P.energy_set("basal_melt_rate", 0.0)
+        P.energy_set("clipped_thickness", 0.0)
+        P.picard_solve()
+        return P
+
+    return Case(build, 2e7, 2, solves=True)
+
+
+@pytest.mark.parametrize("diva", [False, True], ids=["ssa", "diva"])
+def test_gradient_through_von_mises_calving_with_solves(gpu_cls, diva):
+    """Von Mises calving with the velocities solved: ∂J/∂H₀ at a shelf cell and at the front column, and ∂J/∂log A at a
+    cell near the front (A enters the velocities and the viscosity η̄H the rates read, whose adjoint joins the Picard
+    adjoint of the solve before the front) against Richardson-extrapolated differences, to 1e-5 (SSA) and 1e-4 (DIVA)."""
+    case = shelf_case(diva)
+    P0 = case.build(gpu_cls)
+    H0, A0 = P0.get("H"), P0.get("A")
+    _, g = gradient(case, gpu_cls)
+    P1 = case.forward(gpu_cls)
+    assert np.sum(P1.get("calved_thickness")) > 0   # the law calved
+    rtol = 1e-4 if diva else 1e-5
+    for idx in ((1, 4), (2, 9)):
+        _close(g["H"][idx], fd_extrapolated(case, gpu_cls, "H", idx, 1e-5 * H0[idx]), rtol)
+    idx = (1, 8)
+    _close(g["log_A"][idx], A0[idx] * fd_extrapolated(case, gpu_cls, "A", idx, 1e-4 * A0[idx]), rtol)
+
+
 # ---- the library against the oracle's own restatement, every cell ------------------------------------------------------
 @pytest.mark.parametrize("which", ["transport_weno5", "transport_upwind1", "grounding_line_weno5", "front_passes4", "front_passes0",
-                                   "eigencalving", "front_velocity_calving"])
+                                   "eigencalving", "front_velocity_calving", "von_mises_calving"])
 def test_gradient_equals_the_oracle_restatement(gpu_cls, oracle_cls, which):
     """With the velocities held, the oracle restates the gradient through the time steps (nko_checkpointed_gradient: the
     chain by hand, the local derivatives by forward differentiation of its own forward formulas, and a partial-cell
@@ -456,7 +512,8 @@ def test_gradient_equals_the_oracle_restatement(gpu_cls, oracle_cls, which):
              "grounding_line_weno5": lambda: grounding_line_case(None), "front_passes4": lambda: channel_front_case(4),
              "front_passes0": lambda: channel_front_case(0), "eigencalving": lambda: calving_case(M.EigenCalving(coefficient=1e13)),
              "front_velocity_calving": lambda: calving_case(M.FrontVelocityCalving(front_velocity=1e-6),
-                                                            grounding=M.SubgridGroundedFraction())}
+                                                            grounding=M.SubgridGroundedFraction()),
+             "von_mises_calving": lambda: calving_case(VON_MISES, grounding=M.SubgridGroundedFraction())}
     case = cases[which]()
     rtol = 1e-9 if which.startswith(("transport", "grounding")) else 1e-6
     _, ga = gradient(case, gpu_cls)

@@ -3,7 +3,8 @@ against centred differences of its own forward steps, on the CPU: the transport 
 (16 x 4, sources a and m, eight steps; the default bounded WENO-5 and first-order upwinding) at the reference's cells
 to 1e-6, the floating melt across a grounding line (the centre grounded fraction) at the partially grounded cells
 to 1e-5, and a partial-cell front (its advance reversed through a numerical Jacobian) with and without overflow passes
-and under eigencalving, at the reference's cells (test/test_enzyme.jl:490-536) to 1e-5.  The library's gradient is held to this one over the whole field in test_gpu_time_gradient."""
+and under eigencalving and von Mises calving, at the reference's cells (test/test_enzyme.jl:490-536) to 1e-5.  The
+library's gradient is held to this one over the whole field in test_gpu_time_gradient."""
 import numpy as np
 import pytest
 
@@ -59,3 +60,15 @@ def test_oracle_eigencalving_gradient(oracle_cls):
     _, g = gradient(case, oracle_cls)
     for idx in ((1, 3), (2, 3)):
         _close(g["u"][idx], fd_final_thickness(case, oracle_cls, "u", idx, 1e-12), 1e-5)
+
+
+def test_oracle_von_mises_gradient(oracle_cls):
+    """Von Mises calving with the velocities and the viscosity η̄H held: ∂J/∂u through the strain rates and the front
+    speed, ∂J/∂H₀ through η = η̄H / H as well."""
+    case = calving_case(M.VonMisesCalving(stress_threshold=1e6, floating_stress_threshold=2e5), grounding=M.SubgridGroundedFraction())
+    _, g = gradient(case, oracle_cls)
+    for idx in ((1, 3), (2, 3)):
+        _close(g["u"][idx], fd_final_thickness(case, oracle_cls, "u", idx, 1e-12), 1e-5)
+    H0 = case.build(oracle_cls).get("H")
+    _close(g["H"][2, 3], fd_final_thickness(case, oracle_cls, "H", (2, 3), 1e-6 * H0[2, 3]), 1e-5)
+    assert np.sum(case.forward(oracle_cls).get("calved_thickness")) > 0
