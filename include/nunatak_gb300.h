@@ -429,12 +429,32 @@ typedef struct nk_energy_params {
  * last solve (nk_velocity_profile first), phi, the basal and grounded melt rates and the state fields above;
  * writes E, T, omega, H_w, the grounded melt rate, H^n and the diagnostics.  The rate factor is not updated: the
  * reference's advance_enthalpy! ends with update_thermal_diagnostics! (:85-97), so call
- * nk_compute_thermal_diagnostics after this step before the next velocity solve.  The basal water is not drained by
- * a till (TillEffectivePressure's drain_till, src/Thermodynamics/till_effective_pressure.jl, is not built: H_w is
- * the water balance's H+ uncapped, and nk_compute_geometry's effective pressure is the ocean-connected one).
- * NK_BAD_ARGUMENT without the sigma rate-factor layout, with more than NK_ENERGY_MAX_LAYERS layers, or when dt is not
- * finite and positive. */
+ * nk_compute_thermal_diagnostics after this step before the next velocity solve.  With a till (nk_set_till) the
+ * basal water drains and is capped after the grounded melt rate is taken (drain_till); otherwise H_w is the water
+ * balance's H+.  NK_BAD_ARGUMENT without the sigma rate-factor layout, with more than NK_ENERGY_MAX_LAYERS layers, or
+ * when dt is not finite and positive. */
 nk_status nk_step_enthalpy(nk_problem* problem, const nk_energy_params* params, double dt);
+
+/* TillEffectivePressure (src/Thermodynamics/till_effective_pressure.jl), EnthalpyThermodynamics' `effective_pressure`
+ * (Bueler and van Pelt 2015): with s = clamp(H_w / W_max, 0, 1) and the overburden P0 = rho_i g H,
+ *   N = min(N0 (delta P0 / N0)^s 10^((e0 / Cc) (1 - s)), N_ocean),   N_ocean = max(P0 + rho_w g min(b, 0), 0),
+ * with N0 / delta standing in for P0 where P0 = 0; the energy step then drains the basal water,
+ * H_w = clamp(H+ - dt drainage_rate, 0, W_max).  Defaults (TillEffectivePressure(grid)): 1000 Pa, 0.02, 0.69, 0.12,
+ * 2 m, 1 mm per year. */
+typedef struct nk_till_desc {
+    int32_t enabled;                        /* 0: the ocean-connected N and no drainage (the default) */
+    int32_t reserved;                       /* 0 */
+    double reference_effective_pressure;    /* N0, Pa */
+    double overburden_fraction;             /* delta */
+    double reference_void_ratio;            /* e0 */
+    double compressibility;                 /* Cc */
+    double maximum_water_thickness;         /* W_max, m */
+    double drainage_rate;                   /* m s^-1 */
+} nk_till_desc;
+/* Set (or, enabled = 0, clear) the problem's till: nk_compute_geometry's N reads NK_FIELD_BASAL_WATER_THICKNESS
+ * through it and nk_step_enthalpy drains the basal water.  NK_BAD_ARGUMENT for parameters that are not positive and
+ * finite (the drainage rate may be 0). */
+nk_status nk_set_till(nk_problem* problem, const nk_till_desc* till);
 
 /* update_stress_balance_coefficients!(x, ...) (SSA) or update_diva_coefficients!(x, ...) (DIVA) at the
  * current velocity fields U, V: eta_sigma, eta_H, F2, eta_H_ff, beta (and beta_b, u_b, v_b for DIVA). */

@@ -290,6 +290,14 @@ __device__ __forceinline__ double triangle_fraction(double f1, double f2, double
     return a >= 0 ? 1.0 : (c <= 0 ? 0.0 : phi);
 }
 
+// effective_pressure of a TillEffectivePressure (till_effective_pressure.jl:63-70) at overburden P0 and basal water
+// Hw: the saturation s and the till's own N (before the cap by the ocean-connected one)
+__device__ __forceinline__ double till_pressure(const GeometryView& v, double P0, double Hw, double& sat) {
+    sat = fmin(fmax(Hw / v.till_Wmax, 0.0), 1.0);
+    double Pt = P0 > 0 ? P0 : v.till_N0 / v.till_delta;   // a positive stand-in where P0 = 0 (N is the cap's 0 there)
+    return v.till_N0 * pow(v.till_delta * Pt / v.till_N0, sat) * pow(10.0, v.till_e0_Cc * (1 - sat));
+}
+
 // update_geometry! (ice_sheet_model_methods.jl:103-111): s, φ, φᵘ, φᵛ, N, μ
 __global__ void k_geometry(GeometryView v) {
     const DevGrid<double>& g = v.g;
@@ -302,7 +310,9 @@ __global__ void k_geometry(GeometryView v) {
         double H = v.H[k], b = v.bed[k];
         v.s[k] = v.grounding ? fmax(b + H, (1 - ri_rw) * H) : b + H;
         double rig = v.rho_i * v.gacc, rwg = v.rho_w * v.gacc;
-        v.N[k] = fmax(rig * H + rwg * fmin(b, 0.0), 0.0);
+        double No = fmax(rig * H + rwg * fmin(b, 0.0), 0.0);
+        double sat;
+        v.N[k] = v.Hw ? fmin(till_pressure(v, rig * H, v.Hw[k], sat), No) : No;
         double t = fmin(fmax((H - v.mask_min) / v.mask_trans, 0.0), 1.0);
         if (!v.front) v.mu[k] = t * t * (3 - 2 * t);   // a partial-cell front's flag is prognostic
         if (v.grounding) {
@@ -763,7 +773,7 @@ __global__ void __launch_bounds__(128) k_step_enthalpy(EnergyView v, double dt) 
         double Hplus = dmax(0.0, Hstar);
         double missing = Hplus - Hstar;
         v.gmelt[c] = (Hplus - Hw0) * r_dt;
-        v.Hw[c] = Hplus;
+        v.Hw[c] = v.till ? dmin(dmax(Hplus - dt * v.till_drain, 0.0), v.till_Wmax) : Hplus;   // drain_till
         e[1] -= q.L * missing / (Ht * sg.dz[0]);
     }
 
@@ -1250,6 +1260,11 @@ __global__ void k_adjoint_thickness(AdjointView v, GeometryView gv, int diva, do
     double dmudH = (!gv.front && t > 0 && t < 1) ? 6 * t * (1 - t) / gv.mask_trans : 0.0;
     double rig = gv.rho_i * gv.gacc;
     double dNdH = (rig * H + gv.rho_w * gv.gacc * fmin(b, 0.0) > 0) ? rig : 0.0;
+    if (gv.Hw) {   // the till's N = N0 (δ P0 / N0)^s 10^(...) where it is below the ocean-connected cap: ∂N/∂H = N s / H
+        double sat, No = fmax(rig * H + gv.rho_w * gv.gacc * fmin(b, 0.0), 0.0);
+        double Nt = till_pressure(gv, rig * H, gv.Hw[c], sat);
+        if (Nt < No) dNdH = H > 0 ? Nt * sat / H : 0.0;
+    }
     grad_H[c] = gH + gs * dsdH + gmu * dmudH + gf + gN * dNdH;
 }
 void launch_adjoint_thickness(const AdjointView& v, const GeometryView& gv, int diva, double* grad_H, cudaStream_t s) {

@@ -199,6 +199,9 @@ struct GeometryView {
     double mask_min, mask_trans;
     const double2* ud = nullptr;      // prescribed (u, v) per face, NaN where free: the right-hand side there
     int front = 0;                    // a partial-cell front: the ice mask is its prognostic flag, not recomputed
+    // TillEffectivePressure: when Hw is set, N follows the basal water through the till (N0, δ, e0 / Cc, W_max)
+    const double* Hw = nullptr;
+    double till_N0 = 0, till_delta = 0, till_e0_Cc = 0, till_Wmax = 1;
 };
 void launch_geometry(const GeometryView& v, cudaStream_t s);
 void launch_rate_factor(const DevGrid<double>& g, const SigmaTable& sig, int plane, const double* H, const double* T, double* A,
@@ -331,6 +334,7 @@ struct EnergyView {
     const double* E_old;                       // the enthalpy at the start of the step (σ planes, read with neighbours)
     double* E; double* T; double* omega;       // σ planes
     double* Hw; double* gmelt; double* sb; double* qg; double* Phi;
+    int till = 0; double till_drain = 0, till_Wmax = 0;   // drain_till of TillEffectivePressure when till is set
 };
 void launch_step_enthalpy(const EnergyView& v, double dt, cudaStream_t s);
 

@@ -209,6 +209,8 @@ struct nk_problem {
     // a partial-cell front (nk_set_front): its settings and planes (ensure_front)
     nk_front_desc front{0, 4, NK_CALVING_NONE, 0, 0.0, 0.0, 0.0, 0.0, 0.0};
     double* front_buf = nullptr;
+    // a till (nk_set_till): N from the basal water, and its drainage in the energy step
+    nk_till_desc till{0, 0, 1000.0, 0.02, 0.69, 0.12, 2.0, 0.0};
     std::vector<double> sig_dz, sig_w2, sig_zc, sig_w1, sig_zf;
 
     // coarse levels
@@ -1551,6 +1553,13 @@ static GeometryView problem_geometry_view(nk_problem* P) {
     v.mask_min = P->pd.mask_minimum_thickness; v.mask_trans = P->pd.mask_transition_thickness;
     v.ud = P->ud;
     v.front = P->front.enabled;
+    if (P->till.enabled) {   // nk_set_till allocated the energy planes, H_w first
+        v.Hw = P->energy;
+        v.till_N0 = P->till.reference_effective_pressure;
+        v.till_delta = P->till.overburden_fraction;
+        v.till_e0_Cc = P->till.reference_void_ratio / P->till.compressibility;
+        v.till_Wmax = P->till.maximum_water_thickness;
+    }
     return v;
 }
 static void launch_problem_geometry(nk_problem* P) { launch_geometry(problem_geometry_view(P), P->stream); }
@@ -1592,6 +1601,9 @@ static EnergyView energy_view(nk_problem* P, const nk_energy_params* prm) {
     v.E_old = en + (ENERGY_PLANES_2D + (size_t)P->Ns) * pl;
     v.melt = P->transport + pl; v.gmelt = P->transport + 2 * pl;
     v.E = P->thermal; v.omega = P->thermal + (size_t)P->Ns * pl; v.T = P->T;
+    v.till = P->till.enabled;
+    v.till_drain = P->till.drainage_rate;
+    v.till_Wmax = P->till.maximum_water_thickness;
     return v;
 }
 
@@ -1739,6 +1751,22 @@ nk_status nk_set_front(nk_problem* P, const nk_front_desc* f) {
             ensure_front(P);
         }
         P->front = *f;
+    });
+}
+
+nk_status nk_set_till(nk_problem* P, const nk_till_desc* t) {
+    if (!P || !t) return NK_BAD_ARGUMENT;
+    return guarded(P->ctx, [&] {
+        if (t->enabled != 0 && t->enabled != 1) bad("enabled is 0 or 1");
+        if (t->enabled) {
+            auto positive = [](double x) { return x > 0 && std::isfinite(x); };
+            if (!positive(t->reference_effective_pressure) || !positive(t->overburden_fraction) ||
+                !positive(t->compressibility) || !positive(t->maximum_water_thickness) || !std::isfinite(t->reference_void_ratio))
+                bad("the till's parameters must be positive and finite");
+            if (!(t->drainage_rate >= 0) || !std::isfinite(t->drainage_rate)) bad("the till's drainage rate must be finite and non-negative");
+            ensure_energy(P);
+        }
+        P->till = *t;
     });
 }
 

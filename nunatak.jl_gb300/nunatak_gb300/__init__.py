@@ -9,7 +9,7 @@ from .model import (YEAR, Convergence, DepthIntegrated, DIVAShear, FixedIteratio
                     StressBalanceMultigridPreconditioner, StressBalanceSolver, SubgridGroundedFraction,
                     UpwindBiased, ViscosityConvergence, WENO, WeertmanFriction, default_thickness_advection,
                     PartialCellFront, ThicknessThresholdCalving, EigenCalving, VonMisesCalving, FrontVelocityCalving,
-                    MaximumExtentCalving,
+                    MaximumExtentCalving, TillEffectivePressure,
                     make_descriptors, field_shape, sigma_faces)
 from .problem import NunatakError, Problem
 from .batch import Batch
@@ -21,5 +21,5 @@ __all__ = [
     "StressBalanceSolver", "SubgridGroundedFraction", "ViscosityConvergence", "WeertmanFriction", "make_descriptors",
     "field_shape", "sigma_faces", "UpwindBiased", "WENO", "default_thickness_advection", "PartialCellFront",
     "ThicknessThresholdCalving", "EigenCalving", "VonMisesCalving", "FrontVelocityCalving", "MaximumExtentCalving",
-    "NunatakError", "Problem", "Batch",
+    "TillEffectivePressure", "NunatakError", "Problem", "Batch",
 ]

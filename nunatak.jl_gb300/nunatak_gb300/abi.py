@@ -82,6 +82,13 @@ class FrontDesc(C.Structure):
                 ("floating_stress_threshold", C.c_double), ("front_velocity", C.c_double)]
 
 
+class TillDesc(C.Structure):
+    """nk_till_desc: a TillEffectivePressure (the effective pressure from the basal water, and its drainage)."""
+    _fields_ = [("enabled", C.c_int32), ("reserved", C.c_int32), ("reference_effective_pressure", C.c_double),
+                ("overburden_fraction", C.c_double), ("reference_void_ratio", C.c_double), ("compressibility", C.c_double),
+                ("maximum_water_thickness", C.c_double), ("drainage_rate", C.c_double)]
+
+
 class AdvectionDesc(C.Structure):
     """nk_advection_desc: the thickness advection scheme of nk_step_thickness."""
     _fields_ = [("scheme", C.c_int32), ("order", C.c_int32), ("bounded", C.c_int32), ("reserved", C.c_int32),

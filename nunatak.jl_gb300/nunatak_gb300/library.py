@@ -37,6 +37,7 @@ def _declare(lib):
         "nk_step_thickness_stage": ([vp, C.c_double, i32, i32], i32),
         "nk_set_thickness_advection": ([vp, C.POINTER(abi.AdvectionDesc)], i32),
         "nk_set_front": ([vp, C.POINTER(abi.FrontDesc)], i32),
+        "nk_set_till": ([vp, C.POINTER(abi.TillDesc)], i32),
         "nk_initialize_front": ([vp], i32),
         "nk_advance_front": ([vp, C.c_double], i32),
         "nk_step_enthalpy": ([vp, C.POINTER(abi.EnergyParams), C.c_double], i32),

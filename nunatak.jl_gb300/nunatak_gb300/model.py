@@ -205,6 +205,24 @@ class MaximumExtentCalving:
 
 
 @dataclass
+class TillEffectivePressure:
+    """TillEffectivePressure(grid; ...) (src/Thermodynamics/till_effective_pressure.jl:44-57): the effective pressure of
+    a saturated till from the basal water (Bueler and van Pelt 2015), capped by the ocean-connected one, and the till's
+    drainage of 1 mm per year up to its maximum water thickness."""
+    reference_effective_pressure: float = 1000.0
+    overburden_fraction: float = 0.02
+    reference_void_ratio: float = 0.69
+    compressibility: float = 0.12
+    maximum_water_thickness: float = 2.0
+    drainage_rate: float = 1e-3 / (365.25 * 86400)
+
+    def desc(self):
+        return abi.TillDesc(1, 0, float(self.reference_effective_pressure), float(self.overburden_fraction),
+                            float(self.reference_void_ratio), float(self.compressibility),
+                            float(self.maximum_water_thickness), float(self.drainage_rate))
+
+
+@dataclass
 class PartialCellFront:
     """PartialCellFront(grid; passes = 4, calving = nothing) (src/Models/partial_cell_front.jl:49-54)."""
     passes: int = 4

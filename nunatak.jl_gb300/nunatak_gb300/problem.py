@@ -218,6 +218,12 @@ class Problem:
         if getattr(front.calving, "extent", None) is not None:
             self.set("calving_extent", front.calving.extent)
 
+    def set_till(self, till):
+        """EnthalpyThermodynamics' effective_pressure: a TillEffectivePressure makes the geometry's N follow the basal
+        water (the "Hw" energy field) and the energy step drain it; None restores the ocean-connected N."""
+        d = abi.TillDesc() if till is None else till.desc()
+        _check(self._fn("set_till")(self._h, C.byref(d)), "set_till", self._err())
+
     def initialize_front(self):
         """initialize_front!: every cell holding ice is full, none partial (what set!(model; H) does)."""
         _check(self._fn("initialize_front")(self._h), "initialize_front", self._err())

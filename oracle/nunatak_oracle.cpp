@@ -839,6 +839,8 @@ struct Problem {
     // the overflow / retreat scratch; the ice mask μ is then the prognostic 0/1 flag of full cells
     nk_front_desc front{0, 4, NK_CALVING_NONE, 0, 0.0, 0.0, 0.0, 0.0, 0.0};
     Field Hr, calved, extent, O;
+    // TillEffectivePressure (nko_set_till): N from the basal water Hw, and drain_till in the energy step
+    nk_till_desc till{0, 0, 1000.0, 0.02, 0.69, 0.12, 2.0, 0.0};
     Field qg;                     // basal heat flux qᵍ = φ G + τᵇ⋅uᵇ of the last energy step (output)
     SigmaField Phi;
 
@@ -1056,11 +1058,22 @@ static void compute_geometry(Problem& P) {
         for (int j = 1; j <= P.phu.ny(); ++j) for (int i = 1; i <= P.phu.nx(); ++i) P.phu(i, j) = 1;
         for (int j = 1; j <= P.phv.ny(); ++j) for (int i = 1; i <= P.phv.nx(); ++i) P.phv(i, j) = 1;
     }
-    // compute_effective_pressure!, :293-308 (ocean-connected law)
+    // compute_effective_pressure!, subgrid_grounded_fraction.jl:168-183: the ocean-connected law, or with a till
+    // effective_pressure of TillEffectivePressure (till_effective_pressure.jl:63-70) capped by it
     double rig = P.ph.rho_i * P.ph.g, rwg = P.ph.rho_w * P.ph.g;
+    const nk_till_desc& till = P.till;
     for_xy(Nx, Ny, [&](int i, int j) {
         double P0 = rig * P.H(i, j);
-        P.N(i, j) = std::max(P0 + rwg * std::min(P.bed(i, j), 0.0), 0.0);
+        double No = std::max(P0 + rwg * std::min(P.bed(i, j), 0.0), 0.0);
+        if (till.enabled) {
+            double N0 = till.reference_effective_pressure, delta = till.overburden_fraction;
+            double s = std::min(std::max(P.Hw(i, j) / till.maximum_water_thickness, 0.0), 1.0);
+            double Pt = P0 > 0 ? P0 : N0 / delta;
+            double Nt = N0 * std::pow(delta * Pt / N0, s) * std::pow(10.0, till.reference_void_ratio / till.compressibility * (1 - s));
+            P.N(i, j) = std::min(Nt, No);
+        } else {
+            P.N(i, j) = No;
+        }
     });
     // compute_ice_mask!, smooth_ice_mask.jl:50-69; a PartialCellFront's flag is prognostic (partial_cell_front.jl:95)
     if (!P.front.enabled)
@@ -1723,7 +1736,8 @@ static void step_enthalpy(Problem& P, const EnergyParams& q, double dt) {
         double Hplus = std::max(0.0, Hstar);
         double missing = Hplus - Hstar;
         P.gmelt(i, j) = (Hplus - P.Hw(i, j)) / dt;
-        P.Hw(i, j) = Hplus;
+        // drain_till, till_effective_pressure.jl:76-77: the till drains and holds at most its maximum water
+        P.Hw(i, j) = P.till.enabled ? std::min(std::max(Hplus - dt * P.till.drainage_rate, 0.0), P.till.maximum_water_thickness) : Hplus;
         P.E.k[0](i, j) -= q.L * missing / (Ht * layer_thickness(sg, 1));
     });
 
@@ -2880,6 +2894,16 @@ nk_status nko_set_front(nko_problem* h, const nk_front_desc* f) {
     if (f->enabled && (!P.use_mask || f->passes < 0 || f->calving < NK_CALVING_NONE || f->calving > NK_CALVING_MAXIMUM_EXTENT))
         return NK_BAD_ARGUMENT;
     P.front = *f;
+    return NK_OK;
+}
+
+// TillEffectivePressure as EnthalpyThermodynamics' effective_pressure (till_effective_pressure.jl:1-77).
+nk_status nko_set_till(nko_problem* h, const nk_till_desc* t) {
+    if (!h || !t || (t->enabled != 0 && t->enabled != 1)) return NK_BAD_ARGUMENT;
+    if (t->enabled && !(t->reference_effective_pressure > 0 && t->overburden_fraction > 0 && t->compressibility > 0 &&
+                        t->maximum_water_thickness > 0 && t->drainage_rate >= 0))
+        return NK_BAD_ARGUMENT;
+    reinterpret_cast<Problem*>(h)->till = *t;
     return NK_OK;
 }
 

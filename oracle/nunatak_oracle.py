@@ -52,6 +52,7 @@ def load():
             "nko_step_thickness_stage": [vp, C.c_double, C.c_int32, C.c_int32],
             "nko_set_thickness_advection": [vp, C.POINTER(abi.AdvectionDesc)],
             "nko_set_front": [vp, C.POINTER(abi.FrontDesc)],
+            "nko_set_till": [vp, C.POINTER(abi.TillDesc)],
             "nko_initialize_front": [vp],
             "nko_advance_front": [vp, C.c_double],
             "nko_picard_adjoint": [vp, dp, dp, C.POINTER(abi.IterationControl), dp, dp, dp, dp, C.POINTER(abi.SolveStats)],
