@@ -87,6 +87,8 @@ def test_null_handles_are_refused(lib):
         "nk_batch_query": lambda: lib.nk_batch_query(null, C.byref(i32)),
         "nk_batch_wait": lambda: lib.nk_batch_wait(null, null),
         "nk_checkpointed_gradient": lambda: lib.nk_checkpointed_gradient(null, null, abi.COST_FN(), null, null, null),
+        "nk_set_till": lambda: lib.nk_set_till(null, C.byref(abi.TillDesc())),
+        "nk_set_front": lambda: lib.nk_set_front(null, C.byref(abi.FrontDesc())),
     }
     got = {name: f() for name, f in calls.items()}
     assert got == {name: bad for name in calls}

@@ -75,6 +75,8 @@ int main(void) {
     S(nk_time_gradient_desc) F(nk_time_gradient_desc, steps) F(nk_time_gradient_desc, melt_weights) F(nk_time_gradient_desc, adjoint_control)
     S(nk_time_gradient) F(nk_time_gradient, grad_log_A)
     S(nk_time_gradient_stats) F(nk_time_gradient_stats, worst_solve_status) F(nk_time_gradient_stats, elapsed_ms)
+    S(nk_till_desc) F(nk_till_desc, reference_effective_pressure) F(nk_till_desc, drainage_rate)
+    S(nk_front_desc) F(nk_front_desc, calving) F(nk_front_desc, front_velocity)
     return 0;
 }
 """
@@ -97,7 +99,8 @@ def test_ctypes_mirrors_match_the_c_layout(tmp_path):
                "nk_solver_desc": abi.SolverDesc, "nk_solve_stats": abi.SolveStats, "nk_server_desc": abi.ServerDesc,
                "nk_request": abi.Request, "nk_thermal_params": abi.ThermalParams,
                "nk_energy_params": abi.EnergyParams, "nk_cost_state": abi.CostState, "nk_time_gradient_desc": abi.TimeGradientDesc,
-               "nk_time_gradient": abi.TimeGradient, "nk_time_gradient_stats": abi.TimeGradientStats}
+               "nk_time_gradient": abi.TimeGradient, "nk_time_gradient_stats": abi.TimeGradientStats,
+               "nk_till_desc": abi.TillDesc, "nk_front_desc": abi.FrontDesc}
     checked = 0
     for line in filter(None, out):
         parts = line.split()
@@ -109,4 +112,4 @@ def test_ctypes_mirrors_match_the_c_layout(tmp_path):
         else:
             assert ctypes.sizeof(mirrors[parts[0]]) == int(parts[1]), parts
         checked += 1
-    assert checked == 47
+    assert checked == 53
