@@ -2439,8 +2439,59 @@ static void front_reverse_jacobian(Problem& P, const FrontInputs& in, const Fiel
         for (int i = 1; i <= lam.x.v.nx(); ++i) lam.x.v(i, j) = entry(nullptr, true, false, i, j, 1e-3, 1e-15);
 }
 
-// nk_checkpointed_gradient of the library with the velocities held; every stage stored.  A partial-cell front's
-// advance is reversed through its numerical Jacobian (the oracle's check of the library's hand-written reverse).
+// The thickness part of the SSA Picard adjoint, ∂J/∂H = λᵀ ∂r/∂H with r(H) = τ(H) − A(c(x*, H)) x* at the converged
+// x* held (the fixed point A(c(x)) x = τ moves with H as −(∂F/∂x)⁻¹ ∂F/∂H, and λ solves (∂F/∂x)ᵀ λ = x̄): per cell
+// the centred difference of r with the geometry, the driving stress and the coefficients recomputed from H
+// (update_state! without the solve), h = 1e-6 max(H, 1).  A numerical restatement of the library's hand-written
+// chain through η̄H, the drag's grounded fractions and effective pressure, the slope and the front force.
+static void picard_thickness_gradient(Problem& P, const VelocityVector& lam, const VelocityVector& xs, Field& gH) {
+    const Grid& g = P.grid;
+    const int Nx = g.Nx(), Ny = g.Ny();
+    Field H0 = P.H;
+    VelocityVector rp, rm;
+    rp.init(&g);
+    rm.init(&g);
+    auto residual = [&](VelocityVector& r) {
+        fill_halo(P.H);
+        compute_geometry(P);
+        P.x = xs;
+        fill_halo(P.x);
+        update_coefficients(P);
+        VelocityVector q;
+        q.init(&g);
+        ssa_operator(g, q, xs, coeffs(P), P.ph.walls);
+        for (int j = 1; j <= r.u.ny(); ++j) for (int i = 1; i <= r.u.nx(); ++i) r.u(i, j) = P.tau.u(i, j) - q.u(i, j);
+        for (int j = 1; j <= r.v.ny(); ++j) for (int i = 1; i <= r.v.nx(); ++i) r.v(i, j) = P.tau.v(i, j) - q.v(i, j);
+    };
+    gH.init(&g, CENTER, CENTER);
+    for (int j = 1; j <= Ny; ++j)
+        for (int i = 1; i <= Nx; ++i) {
+            double h = 1e-6 * std::max(H0(i, j), 1.0);
+            P.H = H0;
+            P.H(i, j) += h;
+            residual(rp);
+            P.H = H0;
+            P.H(i, j) -= h;
+            residual(rm);
+            double acc = 0.0;
+            for (int b = 1; b <= lam.u.ny(); ++b) for (int a = 1; a <= lam.u.nx(); ++a) acc += lam.u(a, b) * (rp.u(a, b) - rm.u(a, b));
+            for (int b = 1; b <= lam.v.ny(); ++b) for (int a = 1; a <= lam.v.nx(); ++a) acc += lam.v(a, b) * (rp.v(a, b) - rm.v(a, b));
+            gH(i, j) = acc / (2 * h);
+        }
+    P.H = H0;
+    fill_halo(P.H);
+    compute_geometry(P);
+    P.x = xs;
+    fill_halo(P.x);
+    update_coefficients(P);
+}
+
+// nk_checkpointed_gradient of the library; every stage stored.  A partial-cell front's advance is reversed through its
+// numerical Jacobian (the oracle's check of the library's hand-written reverse).  With velocity_solves (the SSA
+// without a front) each stage is followed by a Picard solve, and the reverse runs the oracle's Picard adjoint of each
+// solve with picard_thickness_gradient, in the library's order: the step-end solve after the cost, then per stage
+// (3, 2, 1) the stage's reverse and the adjoint of the solve that made its velocities; the first stage's velocities are
+// the previous step's last solve's.
 static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_cost_fn cost, void* user, const nk_time_gradient* out,
                                nk_time_gradient_stats* st) {
     const Grid& g = P.grid;
@@ -2450,10 +2501,20 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
     const double fractions[3] = {1.0 / 3, 1.0 / 2, 1.0};
     auto weight = [&](int n) { return d.melt_weights ? d.melt_weights[n] : 1.0; };
     Field base = P.melt;
+    const bool solves = d.velocity_solves != 0;
+    const nk_iteration_control ctl = d.adjoint_control ? *d.adjoint_control : P.sdesc.picard;
     std::vector<Field> tape;                         // H before each stage, then the final H
+    std::vector<VelocityVector> xt;                  // with solves: the velocities before each stage, then the final ones
     std::vector<Field> mu_start, Hr_start, H3pre;   // a front: μ and Hʳ at each step's start, the last stage's output
     fill_halo(P.H);
     compute_geometry(P);
+    std::memset(st, 0, sizeof(*st));
+    auto solve = [&] {
+        nk_solve_stats ss{};
+        picard_solve(P, &ss);
+        ++st->picard_solves;
+        if (ss.status > st->worst_solve_status) st->worst_solve_status = ss.status;
+    };
     for (int n = 0; n < N; ++n) {
         for_xy(Nx, Ny, [&](int i, int j) { P.melt(i, j) = weight(n) * base(i, j); });
         if (front) {
@@ -2462,6 +2523,7 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
         }
         for (int stg = 0; stg < 3; ++stg) {
             tape.push_back(P.H);
+            if (solves) xt.push_back(P.x);
             if (front && stg == 2) {
                 thickness_substep(P, d.dt, stg, false);
                 H3pre.push_back(P.H);
@@ -2470,9 +2532,12 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
             } else {
                 step_thickness_stage(P, d.dt, stg, false);
             }
+            if (solves) solve();
         }
     }
     tape.push_back(P.H);
+    if (solves) xt.push_back(P.x);
+    VelocityVector x_end = P.x;
     Field Hfinal = P.H, clipped_end = P.clipped, mu_end = P.mu, Hr_end = P.Hr, calved_end = P.calved;
     Field lamH(&g, CENTER, CENTER), lamHs(&g, CENTER, CENTER), lamH0(&g, CENTER, CENTER), lamHr(&g, CENTER, CENTER);
     Field gsmb(&g, CENTER, CENTER), gmelt(&g, CENTER, CENTER);
@@ -2485,10 +2550,39 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
     }
     int nu = P.x.u.nx() * P.x.u.ny(), nv = P.x.v.nx() * P.x.v.ny();
     std::vector<double> hH(Nx * Ny), hu(nu), hv(nv), hm(Nx * Ny), gH(Nx * Ny), gu(nu), gv(nv);
-    std::memset(st, 0, sizeof(*st));
     st->segments = 1;
+    // with solves: λ of the velocities a solve made (the step end's, carried from the next step's first stage), and
+    // the gradients in log C and log A that the solves' adjoints add up
+    VelocityVector lamx_stage;
+    lamx_stage.init(&g);
+    Field glogC(&g, CENTER, CENTER);
+    SigmaField glogA;
+    glogA.init(&g, CENTER, CENTER, P.rate_layout == NK_RATE_FACTOR_SIGMA ? P.sigma.N : 1);
+    auto solve_adjoint = [&](int t, const VelocityVector& xbar, Field& lam_to) {
+        P.H = tape[t];
+        fill_halo(P.H);
+        compute_geometry(P);
+        P.x = xt[t];
+        fill_halo(P.x);
+        VelocityVector lam;
+        Field gC;
+        SigmaField gA;
+        nk_solve_stats ss{};
+        picard_adjoint(P, xbar, ctl, lam, gC, gA, &ss);
+        ++st->picard_adjoints;
+        st->adjoint_iterations += ss.picard_iterations;
+        if (ss.status > st->worst_solve_status) st->worst_solve_status = ss.status;
+        Field gHs;
+        picard_thickness_gradient(P, lam, xt[t], gHs);
+        for_xy(Nx, Ny, [&](int i, int j) {
+            lam_to(i, j) += gHs(i, j);
+            glogC(i, j) += gC(i, j);
+            for (size_t k = 0; k < glogA.k.size(); ++k) glogA.k[k](i, j) += gA.k[k](i, j);
+        });
+    };
     for (int n = N - 1; n >= 0; --n) {
         P.H = tape[3 * n + 3];
+        if (solves) P.x = xt[3 * n + 3];
         if (front) P.mu = n + 1 < N ? mu_start[n + 1] : mu_end;
         fill_halo(P.H);
         fill_halo(P.mu);
@@ -2513,6 +2607,10 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
             copy_in(tv, gv.data());
             for (int j = 1; j <= tu.ny(); ++j) for (int i = 1; i <= tu.nx(); ++i) lamx.u(i, j) += tu(i, j);
             for (int j = 1; j <= tv.ny(); ++j) for (int i = 1; i <= tv.nx(); ++i) lamx.v(i, j) += tv(i, j);
+        }
+        if (solves) {   // the solve that ended the step, for λ of its velocities; lamx then carries the next λ
+            solve_adjoint(3 * n + 3, lamx, lamH);
+            lamx.init(&g);
         }
         if (front) {   // the front's advance after the last stage: its inputs at the step's state
             P.H = tape[3 * n + 2];
@@ -2544,6 +2642,7 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
         for (int stg = 2; stg >= 0; --stg) {
             int t = 3 * n + stg;
             P.H = tape[t];
+            if (solves) P.x = xt[t];
             if (front) P.mu = mu_start[n];
             fill_halo(P.H);
             fill_halo(P.mu);
@@ -2557,8 +2656,17 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
                     for (int i = 0; i <= Nx + 1; ++i) P.theta(i, j) = bounds_limiter(P.advection, P.H, i, j);
             }
             bool after_front = front && stg == 2;
-            stage_reverse(P, after_front ? H3pre[n] : tape[t + 1], fractions[stg] * d.dt, weight(n), lamH, lamHs, lamH0, lamx,
-                          gsmb, gmelt, after_front ? &lamf.phi : nullptr);
+            if (solves) lamx_stage.init(&g);
+            stage_reverse(P, after_front ? H3pre[n] : tape[t + 1], fractions[stg] * d.dt, weight(n), lamH, lamHs, lamH0,
+                          solves ? lamx_stage : lamx, gsmb, gmelt, after_front ? &lamf.phi : nullptr);
+            if (solves) {
+                if (stg > 0) {
+                    solve_adjoint(t, lamx_stage, lamHs);   // the solve that made the stage's velocities from its H
+                } else {                                   // made by the previous step's last solve (or the input)
+                    for (int j = 1; j <= lamx.u.ny(); ++j) for (int i = 1; i <= lamx.u.nx(); ++i) lamx.u(i, j) += lamx_stage.u(i, j);
+                    for (int j = 1; j <= lamx.v.ny(); ++j) for (int i = 1; i <= lamx.v.nx(); ++i) lamx.v(i, j) += lamx_stage.v(i, j);
+                }
+            }
             if (stg > 0) lamH = lamHs;
             else for_xy(Nx, Ny, [&](int i, int j) { lamH(i, j) = lamHs(i, j) + lamH0(i, j); });
         }
@@ -2568,12 +2676,13 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
         if (out->grad_u && out->grad_v) { copy_out(lamx.u, out->grad_u); copy_out(lamx.v, out->grad_v); }
         if (out->grad_smb) copy_out(gsmb, out->grad_smb);
         if (out->grad_melt) copy_out(gmelt, out->grad_melt);
-        if (out->grad_log_C) std::fill(out->grad_log_C, out->grad_log_C + Nx * Ny, 0.0);
+        if (out->grad_log_C) copy_out(glogC, out->grad_log_C);
         if (out->grad_log_A) {
             int planes = P.rate_layout == NK_RATE_FACTOR_SIGMA ? P.sigma.N : 1;
-            std::fill(out->grad_log_A, out->grad_log_A + (size_t)planes * Nx * Ny, 0.0);
+            for (int k = 0; k < planes; ++k) copy_out(glogA.k[k], out->grad_log_A + (size_t)k * Nx * Ny);
         }
     }
+    if (solves) P.x = x_end;
     P.H = Hfinal;
     P.clipped = clipped_end;
     P.melt = base;
@@ -2881,8 +2990,14 @@ nk_status nko_step_thickness_stage(nko_problem* h, double dt, int32_t stage, int
 // nk_checkpointed_gradient for a model whose velocities are held (no velocity solve).
 nk_status nko_checkpointed_gradient(nko_problem* h, const nk_time_gradient_desc* d, nk_cost_fn cost, void* user,
                                     const nk_time_gradient* out, nk_time_gradient_stats* stats) {
-    if (!h || !d || !cost || !(d->dt > 0) || d->steps < 1 || d->velocity_solves != 0) return NK_BAD_ARGUMENT;
+    if (!h || !d || !cost || !(d->dt > 0) || d->steps < 1 || (d->velocity_solves != 0 && d->velocity_solves != 1))
+        return NK_BAD_ARGUMENT;
     Problem& P = *reinterpret_cast<Problem*>(h);
+    // velocity solves: the SSA without a front or prescribed faces (the DIVA's lagged state and the von Mises
+    // viscosity are not restated)
+    if (d->velocity_solves && (P.stress_balance == NK_DIVA || P.front.enabled || P.grid.pu || P.grid.pv)) return NK_BAD_ARGUMENT;
+    const nk_iteration_control ctl = d->adjoint_control ? *d->adjoint_control : P.sdesc.picard;
+    if (d->velocity_solves && ctl.kind != NK_CONVERGENCE && ctl.kind != NK_FIXED_ITERATIONS) return NK_BAD_ARGUMENT;
     nk_time_gradient_stats local{};
     return time_gradient(P, *d, cost, user, out, stats ? stats : &local);
 }

@@ -1,16 +1,17 @@
-"""The oracle's restatement of the gradient through time steps with the velocities held (nko_checkpointed_gradient)
-against centred differences of its own forward steps, on the CPU: the transport case of test/test_enzyme.jl:447-488
+"""The oracle's restatement of the gradient through time steps (nko_checkpointed_gradient) against centred differences
+of its own forward steps, on the CPU.  With the velocities held: the transport case of test/test_enzyme.jl:447-488
 (16 x 4, sources a and m, eight steps; the default bounded WENO-5 and first-order upwinding) at the reference's cells
 to 1e-6, the floating melt across a grounding line (the centre grounded fraction) at the partially grounded cells
 to 1e-5, and a partial-cell front (its advance reversed through a numerical Jacobian) with and without overflow passes
-and under eigencalving and von Mises calving, at the reference's cells (test/test_enzyme.jl:490-536) to 1e-5.  The
+and under eigencalving and von Mises calving, at the reference's cells (test/test_enzyme.jl:490-536) to 1e-5.  With a
+Picard solve after every stage (the SSA): the reference's ridge (:421-445) to 1e-5; the DIVA is refused.  The
 library's gradient is held to this one over the whole field in test_gpu_time_gradient."""
 import numpy as np
 import pytest
 
 from nunatak_gb300 import model as M
-from test_gpu_time_gradient import (_close, calving_case, channel_front_case, fd_final_thickness, gradient, grounding_line_case,
-                                    transport_case)
+from test_gpu_time_gradient import (_close, calving_case, channel_front_case, fd_extrapolated, fd_final_thickness, gradient,
+                                    grounding_line_case, ridge_case, transport_case)
 
 
 @pytest.mark.parametrize("advection", [None, M.UpwindBiased(order=1)], ids=["bounded_weno5", "upwind1"])
@@ -36,13 +37,6 @@ def test_oracle_floating_melt_gradient(oracle_cls):
     assert len(partial) >= 3
     for idx in partial[:3]:
         _close(g["H"][idx], fd_final_thickness(case, oracle_cls, "H", idx, 1e-6 * H0[idx]), 1e-5)
-
-
-def test_oracle_refuses_velocity_solves(oracle_cls):
-    case = transport_case()
-    P = case.build(oracle_cls)
-    with pytest.raises(Exception):
-        P.checkpointed_gradient(lambda *a: None, case.dt, 2, velocity_solves=True)
 
 
 @pytest.mark.parametrize("passes", [4, 0])
@@ -72,3 +66,26 @@ def test_oracle_von_mises_gradient(oracle_cls):
     H0 = case.build(oracle_cls).get("H")
     _close(g["H"][2, 3], fd_final_thickness(case, oracle_cls, "H", (2, 3), 1e-6 * H0[2, 3]), 1e-5)
     assert np.sum(case.forward(oracle_cls).get("calved_thickness")) > 0
+
+
+def test_oracle_picard_time_steps_gradient(oracle_cls):
+    """The reference's ridge (SSA, Weertman) with a Picard solve after every stage, two steps: the oracle's gradient
+    (its Picard adjoint of every solve, the thickness part by differences of the residual τ − A(c(x*, H)) x*) against
+    Richardson-extrapolated differences of its own forward steps, ∂J/∂H₀ at two cells, ∂J/∂log C and ∂J/∂a at one,
+    to 1e-5 (test/test_enzyme.jl:421-445)."""
+    case = ridge_case(oracle_cls, steps=2)
+    _, g = gradient(case, oracle_cls)
+    assert g["stats"]["picard_adjoints"] == 3 * case.steps and g["stats"]["worst_solve_status"] == 0
+    H0 = case.build(oracle_cls).get("H")
+    for idx in ((1, 5), (2, 9)):
+        _close(g["H"][idx], fd_extrapolated(case, oracle_cls, "H", idx, 1e-3 * H0[idx]), 1e-5)
+    C = case.build(oracle_cls).get("C")
+    _close(g["log_C"][1, 6] / C[1, 6], fd_extrapolated(case, oracle_cls, "C", (1, 6), 1e-3 * C[1, 6]), 1e-5)
+    _close(g["smb"][2, 8], fd_extrapolated(case, oracle_cls, "surface_mass_balance", (2, 8), 1e-2 * 1e-8), 1e-5)
+
+
+def test_oracle_refuses_solves_it_does_not_restate(oracle_cls):
+    case = ridge_case(oracle_cls, diva=True, steps=1)
+    P = case.build(oracle_cls)
+    with pytest.raises(Exception):
+        P.checkpointed_gradient(lambda *a: None, case.dt, 1, velocity_solves=True)
