@@ -490,7 +490,10 @@ nk_status nk_picard_solve(nk_problem* problem, nk_solve_stats* stats);
  * status NK_NOT_CONVERGED when maxiter ended it.  U, V are left at x*.  DIVA: the step also reads its own
  * previous beta_b, F2 and eta_sigma (diva.jl:77-80), whose adjoint is swept along with lambda; the stopping test
  * watches lambda only, as the reference's does, and the lagged-state adjoint settles more slowly, so ask for a
- * tighter reltol than for the SSA.  Problems with prescribed velocities are refused (NK_BAD_ARGUMENT). */
+ * tighter reltol than for the SSA.  Problems with prescribed velocities are refused (NK_BAD_ARGUMENT).  The adjoint is
+ * that of the fixed point whatever stopped the forward solve: a solve that FixedIterations stopped before converging
+ * is differentiated as if converged, where the reference's Enzyme, whose rule covers Convergence alone
+ * (ext/NunatakEnzymeExt.jl:121), unrolls its iterations. */
 nk_status nk_picard_adjoint(nk_problem* problem, const double* ubar, const double* vbar, const nk_iteration_control* control,
                             double* lambda_u, double* lambda_v, double* grad_log_C, double* grad_log_A, nk_solve_stats* stats);
 /* nk_picard_adjoint plus, in grad_H (Nx x Ny, or NULL), the thickness gradient ∂J/∂H: the total derivative
