@@ -19,6 +19,7 @@ stops at maxiter returns its iteration count with stats.status == NOT_CONVERGED 
 silently), a non-finite result raises FloatingPointError.
 """
 import ctypes as C
+import warnings
 
 import numpy as np
 
@@ -30,6 +31,13 @@ _dptr = C.POINTER(C.c_double)
 
 class NunatakError(RuntimeError):
     pass
+
+
+def _warn_unconverged(stats):
+    """The reverse rule's warning when maxiter ended the Picard adjoint (ext/NunatakEnzymeExt.jl:222)."""
+    if stats.status == abi.NK_NOT_CONVERGED:
+        warnings.warn(f"Picard adjoint did not converge in {stats.picard_iterations} iterations: "
+                      f"‖Δλ‖ = {stats.picard_change}, ‖λ‖ = {stats.picard_norm}", RuntimeWarning, stacklevel=3)
 
 
 def _check(status, what, message=""):
@@ -325,11 +333,13 @@ class Problem:
                                                       grad.ctypes.data_as(_dptr), grad_a.ctypes.data_as(_dptr),
                                                       grad_h.ctypes.data_as(_dptr), C.byref(stats))
             _check(st, "picard_adjoint_gradients", self._err())
+            _warn_unconverged(stats)
             return lu, lv, grad, grad_a, grad_h, stats
         st = self._fn("picard_adjoint")(self._h, ub.ctypes.data_as(_dptr), vb.ctypes.data_as(_dptr), ctl,
                                         lu.ctypes.data_as(_dptr), lv.ctypes.data_as(_dptr), grad.ctypes.data_as(_dptr),
                                         grad_a.ctypes.data_as(_dptr), C.byref(stats))
         _check(st, "picard_adjoint", self._err())
+        _warn_unconverged(stats)
         return lu, lv, grad, grad_a, stats
 
     def checkpointed_gradient(self, cost, dt, steps, checkpoint_interval=None, velocity_solves=True, melt_weights=None,

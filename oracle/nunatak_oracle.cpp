@@ -1558,7 +1558,9 @@ static int picard_adjoint(Problem& P, const VelocityVector& xbar, const nk_itera
     st->picard_iterations = it;
     st->picard_change = D;
     st->picard_norm = M;
-    st->status = (!std::isfinite(D) || status == NK_NONFINITE) ? NK_NONFINITE : NK_OK;
+    // the reverse rule's warning (ext/NunatakEnzymeExt.jl:222): the stopping test unmet when maxiter ended it
+    st->status = (!std::isfinite(D) || status == NK_NONFINITE) ? NK_NONFINITE
+               : (!fixed && !(D <= std::max(ctl.reltol * M, ctl.abstol))) ? NK_NOT_CONVERGED : NK_OK;
     return st->status;
 }
 

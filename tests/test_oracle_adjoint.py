@@ -15,13 +15,15 @@ no-slip walls with regularised Coulomb drag), converged solves (Picard 1e-14, CG
   DIVA sheet with Weertman and regularised Coulomb drag, log C and σ-grid log A along directions;
 - GPU (marked gpu): λ, ∂J/∂log C and ∂J/∂log A of nk_picard_adjoint against the oracle's, within 1e-6 of each
   one's largest entry, for the three SSA cases and the two DIVA ones.
-The oracle refuses problems with prescribed velocities, as the library does."""
+The oracle refuses problems with prescribed velocities, as the library does.  An adjoint stopped by its maxiter warns
+on both backends (test/test_enzyme.jl:383-389)."""
 import math
+import warnings
 
 import numpy as np
 import pytest
 
-from nunatak_gb300 import model as M, workloads
+from nunatak_gb300 import abi, model as M, workloads
 
 CONTROL = M.Convergence(reltol=1e-12, maxiter=500)
 KINDS = ["bounded", "periodic_x", "no_slip_coulomb"]
@@ -117,6 +119,20 @@ def test_oracle_adjoint_refuses_prescribed_faces(oracle_cls):
     inflow = workloads.channel_shelf(inflow=100.0).problem(oracle_cls)
     with pytest.raises(ValueError):
         inflow.picard_adjoint(np.zeros(inflow.shape("u")), np.zeros(inflow.shape("v")), CONTROL)
+
+
+def test_unconverged_adjoint_warns(backend):
+    """test/test_enzyme.jl:383-389: an adjoint whose control stops it at one iteration warns, and its stats say so;
+    a converged one does not."""
+    P, uo, vo = _setup(backend, "bounded")
+    ub, vb = P.get("u") - uo, P.get("v") - vo
+    with pytest.warns(RuntimeWarning, match="Picard adjoint did not converge"):
+        *_, st = P.picard_adjoint(ub, vb, M.Convergence(reltol=1e-12, maxiter=1))
+    assert st.status == abi.NK_NOT_CONVERGED and st.picard_iterations == 1
+    with warnings.catch_warnings():
+        warnings.simplefilter("error")
+        *_, st = P.picard_adjoint(ub, vb, CONTROL)
+    assert st.status == abi.NK_OK
 
 
 # ---- DIVA: the step also maps its lagged state (βᵇ, F₂, ησ), whose adjoint is swept along with λ --------------
