@@ -1356,11 +1356,15 @@ static void basal_drag_adjoint(Problem& P, const VelocityVector& xs, const Field
 // One reverse sweep of the SSA step q = A(c(x)) x* for the seed λ (halos of λ filled): the operator, then
 // compute_column_integrals! and compute_viscosity! (membrane, wall-masked strain rates) and
 // compute_basal_drag!, in reverse order.  λ-signed: G.x = ∂(λᵀq)/∂x.
-static void adjoint_sweep(Problem& P, const VelocityVector& lam, AdjointSweep& G) {
+// eta_bar: ∂J/∂η̄H per centre from outside the solve (a true adjoint; NULL: none), the shadow of the overwritten
+// coefficient that the reverse rule adds in every pass (ext/NunatakEnzymeExt.jl:204-214).
+static void adjoint_sweep(Problem& P, const VelocityVector& lam, AdjointSweep& G, const Field* eta_bar = nullptr) {
     const Grid& g = P.grid;
     const Physics& ph = P.ph;
     const VelocityVector& xs = P.x;
     operator_sweep(P, lam, G);
+    if (eta_bar)   // G.eta is λ-signed: minus the true adjoint
+        for (int j = 1; j <= g.Ny(); ++j) for (int i = 1; i <= g.Nx(); ++i) G.eta(i, j) -= (*eta_bar)(i, j);
     // column integrals and viscosity: η̄H = μ H Σₖ ηₖ Δζₖ, ηₖ = ½ Aₖ^(-1/n) S^((1-n)/2n), S = ε̇ₑ² + ε̇₀²
     double n = ph.n, p = (1 - n) / (2 * n);
     for (int j = 1; j <= g.Ny(); ++j)
@@ -1501,7 +1505,7 @@ static void diva_sweep(Problem& P, const VelocityVector& lam, const DivaState& s
 // cell, gradA ∂J/∂log A in the rate factor's layout (2-D: summed over the layers that share it).  The SSA sweep is
 // λ-signed (ȳ = -G.x), the DIVA sweep true (ȳ = G.x) and carries the lagged-state adjoint σ.
 static int picard_adjoint(Problem& P, const VelocityVector& xbar, const nk_iteration_control& ctl, VelocityVector& lam,
-                          Field& gradC, SigmaField& gradA, nk_solve_stats* st) {
+                          Field& gradC, SigmaField& gradA, nk_solve_stats* st, const Field* eta_bar = nullptr) {
     const Grid& g = P.grid;
     const bool diva = P.stress_balance == NK_DIVA;
     const double sign = diva ? 1.0 : -1.0;
@@ -1517,7 +1521,7 @@ static int picard_adjoint(Problem& P, const VelocityVector& xbar, const nk_itera
             diva_sweep(P, lam, sig, sig_next, G);
             std::swap(sig, sig_next);
         } else {
-            adjoint_sweep(P, lam, G);
+            adjoint_sweep(P, lam, G, eta_bar);
         }
     };
     VelocityVector r, next;
@@ -2385,10 +2389,12 @@ static void copy_out(const Field& f, double* dst);
 struct FrontInputs {
     Field H, Hr, smb, melt, phi;
     VelocityVector x;
+    Field etaH;                   // the viscosity the von Mises rates read (that law only)
 };
 static void front_outputs(Problem& P, const FrontInputs& in, const Field& mu0, double dt, Field& Hout, Field& Hrout) {
     Field clipped = P.clipped, calved = P.calved;
     P.H = in.H; P.Hr = in.Hr; P.mu = mu0; P.smb = in.smb; P.melt = in.melt; P.phi = in.phi; P.x = in.x;
+    if (P.front.calving == NK_CALVING_VON_MISES) P.etaH = in.etaH;
     for (Field* f : {&P.H, &P.Hr, &P.mu, &P.smb, &P.melt, &P.phi}) fill_halo(*f);
     fill_halo(P.x);
     advance_front(P, dt, false);
@@ -2439,6 +2445,11 @@ static void front_reverse_jacobian(Problem& P, const FrontInputs& in, const Fiel
         for (int i = 1; i <= lam.x.u.nx(); ++i) lam.x.u(i, j) = entry(nullptr, true, true, i, j, 1e-3, 1e-15);
     for (int j = 1; j <= lam.x.v.ny(); ++j)
         for (int i = 1; i <= lam.x.v.nx(); ++i) lam.x.v(i, j) = entry(nullptr, true, false, i, j, 1e-3, 1e-15);
+    if (P.front.calving == NK_CALVING_VON_MISES) {   // the rates are linear in η̄H: 1e-6 of it (at least 1)
+        lam.etaH.init(&g, CENTER, CENTER);
+        for (int j = 1; j <= Ny; ++j)
+            for (int i = 1; i <= Nx; ++i) lam.etaH(i, j) = entry(&FrontInputs::etaH, false, false, i, j, 1e-6, 1.0);
+    }
 }
 
 // The thickness part of the SSA Picard adjoint, ∂J/∂H = λᵀ ∂r/∂H with r(H) = τ(H) − A(c(x*, H)) x* at the converged
@@ -2446,14 +2457,17 @@ static void front_reverse_jacobian(Problem& P, const FrontInputs& in, const Fiel
 // the centred difference of r with the geometry, the driving stress and the coefficients recomputed from H
 // (update_state! without the solve), h = 1e-6 max(H, 1).  A numerical restatement of the library's hand-written
 // chain through η̄H, the drag's grounded fractions and effective pressure, the slope and the front force.
-static void picard_thickness_gradient(Problem& P, const VelocityVector& lam, const VelocityVector& xs, Field& gH) {
+// With eta_bar (the η̄H shadow of picard_adjoint) the shadow's own H part s̄ᵀ ∂η̄H/∂H joins it, by the same differences.
+static void picard_thickness_gradient(Problem& P, const VelocityVector& lam, const VelocityVector& xs, Field& gH,
+                                      const Field* eta_bar = nullptr) {
     const Grid& g = P.grid;
     const int Nx = g.Nx(), Ny = g.Ny();
     Field H0 = P.H;
     VelocityVector rp, rm;
     rp.init(&g);
     rm.init(&g);
-    auto residual = [&](VelocityVector& r) {
+    Field ep, em;
+    auto residual = [&](VelocityVector& r, Field& e) {
         fill_halo(P.H);
         compute_geometry(P);
         P.x = xs;
@@ -2464,6 +2478,7 @@ static void picard_thickness_gradient(Problem& P, const VelocityVector& lam, con
         ssa_operator(g, q, xs, coeffs(P), P.ph.walls);
         for (int j = 1; j <= r.u.ny(); ++j) for (int i = 1; i <= r.u.nx(); ++i) r.u(i, j) = P.tau.u(i, j) - q.u(i, j);
         for (int j = 1; j <= r.v.ny(); ++j) for (int i = 1; i <= r.v.nx(); ++i) r.v(i, j) = P.tau.v(i, j) - q.v(i, j);
+        e = P.etaH;
     };
     gH.init(&g, CENTER, CENTER);
     for (int j = 1; j <= Ny; ++j)
@@ -2471,11 +2486,13 @@ static void picard_thickness_gradient(Problem& P, const VelocityVector& lam, con
             double h = 1e-6 * std::max(H0(i, j), 1.0);
             P.H = H0;
             P.H(i, j) += h;
-            residual(rp);
+            residual(rp, ep);
             P.H = H0;
             P.H(i, j) -= h;
-            residual(rm);
+            residual(rm, em);
             double acc = 0.0;
+            if (eta_bar)
+                for (int b = 1; b <= Ny; ++b) for (int a = 1; a <= Nx; ++a) acc += (*eta_bar)(a, b) * (ep(a, b) - em(a, b));
             for (int b = 1; b <= lam.u.ny(); ++b) for (int a = 1; a <= lam.u.nx(); ++a) acc += lam.u(a, b) * (rp.u(a, b) - rm.u(a, b));
             for (int b = 1; b <= lam.v.ny(); ++b) for (int a = 1; a <= lam.v.nx(); ++a) acc += lam.v(a, b) * (rp.v(a, b) - rm.v(a, b));
             gH(i, j) = acc / (2 * h);
@@ -2489,11 +2506,12 @@ static void picard_thickness_gradient(Problem& P, const VelocityVector& lam, con
 }
 
 // nk_checkpointed_gradient of the library; every stage stored.  A partial-cell front's advance is reversed through its
-// numerical Jacobian (the oracle's check of the library's hand-written reverse).  With velocity_solves (the SSA
-// without a front) each stage is followed by a Picard solve, and the reverse runs the oracle's Picard adjoint of each
-// solve with picard_thickness_gradient, in the library's order: the step-end solve after the cost, then per stage
-// (3, 2, 1) the stage's reverse and the adjoint of the solve that made its velocities; the first stage's velocities are
-// the previous step's last solve's.
+// numerical Jacobian (the oracle's check of the library's hand-written reverse).  With velocity_solves (the SSA) each
+// stage is followed by a Picard solve, and the reverse runs the oracle's Picard adjoint of each solve with
+// picard_thickness_gradient, in the library's order: the step-end solve after the cost, then per stage (3, 2, 1) the
+// stage's reverse and the adjoint of the solve that made its velocities; the first stage's velocities are the previous
+// step's last solve's.  The front read the last stage's velocities and, under von Mises calving, the viscosity η̄H that
+// stage's solve left: their λ join that solve's adjoint, η̄H's as the shadow of an overwritten coefficient.
 static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_cost_fn cost, void* user, const nk_time_gradient* out,
                                nk_time_gradient_stats* st) {
     const Grid& g = P.grid;
@@ -2508,6 +2526,7 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
     std::vector<Field> tape;                         // H before each stage, then the final H
     std::vector<VelocityVector> xt;                  // with solves: the velocities before each stage, then the final ones
     std::vector<Field> mu_start, Hr_start, H3pre;   // a front: μ and Hʳ at each step's start, the last stage's output
+    std::vector<Field> etaH_front;                   // and the viscosity its von Mises rates read
     fill_halo(P.H);
     compute_geometry(P);
     std::memset(st, 0, sizeof(*st));
@@ -2529,6 +2548,7 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
             if (front && stg == 2) {
                 thickness_substep(P, d.dt, stg, false);
                 H3pre.push_back(P.H);
+                etaH_front.push_back(P.etaH);
                 advance_front(P, d.dt, false);
                 compute_geometry(P);
             } else {
@@ -2560,7 +2580,7 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
     Field glogC(&g, CENTER, CENTER);
     SigmaField glogA;
     glogA.init(&g, CENTER, CENTER, P.rate_layout == NK_RATE_FACTOR_SIGMA ? P.sigma.N : 1);
-    auto solve_adjoint = [&](int t, const VelocityVector& xbar, Field& lam_to) {
+    auto solve_adjoint = [&](int t, const VelocityVector& xbar, Field& lam_to, const Field* eta_bar = nullptr) {
         P.H = tape[t];
         fill_halo(P.H);
         compute_geometry(P);
@@ -2570,12 +2590,12 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
         Field gC;
         SigmaField gA;
         nk_solve_stats ss{};
-        picard_adjoint(P, xbar, ctl, lam, gC, gA, &ss);
+        picard_adjoint(P, xbar, ctl, lam, gC, gA, &ss, eta_bar);
         ++st->picard_adjoints;
         st->adjoint_iterations += ss.picard_iterations;
         if (ss.status > st->worst_solve_status) st->worst_solve_status = ss.status;
         Field gHs;
-        picard_thickness_gradient(P, lam, xt[t], gHs);
+        picard_thickness_gradient(P, lam, xt[t], gHs, eta_bar);
         for_xy(Nx, Ny, [&](int i, int j) {
             lam_to(i, j) += gHs(i, j);
             glogC(i, j) += gC(i, j);
@@ -2617,6 +2637,7 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
         if (front) {   // the front's advance after the last stage: its inputs at the step's state
             P.H = tape[3 * n + 2];
             P.mu = mu_start[n];
+            if (solves) P.x = xt[3 * n + 2];   // the velocities of the last stage
             fill_halo(P.H);
             fill_halo(P.mu);
             compute_geometry(P);   // φ of the last stage's input
@@ -2628,6 +2649,7 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
             for_xy(Nx, Ny, [&](int i, int j) { in.melt(i, j) = weight(n) * base(i, j); });
             in.phi = P.phi;
             in.x = P.x;
+            if (P.front.calving == NK_CALVING_VON_MISES) in.etaH = etaH_front[n];
             Field phi2 = P.phi;
             front_reverse_jacobian(P, in, mu_start[n], d.dt, lamH, lamHr, lamf);
             lamH = lamf.H;
@@ -2636,8 +2658,10 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
                 gsmb(i, j) += lamf.smb(i, j);
                 gmelt(i, j) += weight(n) * lamf.melt(i, j);
             });
-            for (int j = 1; j <= lamx.u.ny(); ++j) for (int i = 1; i <= lamx.u.nx(); ++i) lamx.u(i, j) += lamf.x.u(i, j);
-            for (int j = 1; j <= lamx.v.ny(); ++j) for (int i = 1; i <= lamx.v.nx(); ++i) lamx.v(i, j) += lamf.x.v(i, j);
+            if (!solves) {   // with solves they join the last stage's velocity adjoint below
+                for (int j = 1; j <= lamx.u.ny(); ++j) for (int i = 1; i <= lamx.u.nx(); ++i) lamx.u(i, j) += lamf.x.u(i, j);
+                for (int j = 1; j <= lamx.v.ny(); ++j) for (int i = 1; i <= lamx.v.nx(); ++i) lamx.v(i, j) += lamf.x.v(i, j);
+            }
             P.phi = phi2;
         }
         lamH0.zero();
@@ -2662,8 +2686,14 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
             stage_reverse(P, after_front ? H3pre[n] : tape[t + 1], fractions[stg] * d.dt, weight(n), lamH, lamHs, lamH0,
                           solves ? lamx_stage : lamx, gsmb, gmelt, after_front ? &lamf.phi : nullptr);
             if (solves) {
+                const Field* eta_bar = nullptr;
+                if (after_front) {   // the front read the last stage's velocities and, under von Mises, the viscosity
+                    for (int j = 1; j <= lamx_stage.u.ny(); ++j) for (int i = 1; i <= lamx_stage.u.nx(); ++i) lamx_stage.u(i, j) += lamf.x.u(i, j);
+                    for (int j = 1; j <= lamx_stage.v.ny(); ++j) for (int i = 1; i <= lamx_stage.v.nx(); ++i) lamx_stage.v(i, j) += lamf.x.v(i, j);
+                    if (P.front.calving == NK_CALVING_VON_MISES) eta_bar = &lamf.etaH;
+                }
                 if (stg > 0) {
-                    solve_adjoint(t, lamx_stage, lamHs);   // the solve that made the stage's velocities from its H
+                    solve_adjoint(t, lamx_stage, lamHs, eta_bar);   // the solve that made the stage's velocities from its H
                 } else {                                   // made by the previous step's last solve (or the input)
                     for (int j = 1; j <= lamx.u.ny(); ++j) for (int i = 1; i <= lamx.u.nx(); ++i) lamx.u(i, j) += lamx_stage.u(i, j);
                     for (int j = 1; j <= lamx.v.ny(); ++j) for (int i = 1; i <= lamx.v.nx(); ++i) lamx.v(i, j) += lamx_stage.v(i, j);
@@ -2995,9 +3025,8 @@ nk_status nko_checkpointed_gradient(nko_problem* h, const nk_time_gradient_desc*
     if (!h || !d || !cost || !(d->dt > 0) || d->steps < 1 || (d->velocity_solves != 0 && d->velocity_solves != 1))
         return NK_BAD_ARGUMENT;
     Problem& P = *reinterpret_cast<Problem*>(h);
-    // velocity solves: the SSA without a front or prescribed faces (the DIVA's lagged state and the von Mises
-    // viscosity are not restated)
-    if (d->velocity_solves && (P.stress_balance == NK_DIVA || P.front.enabled || P.grid.pu || P.grid.pv)) return NK_BAD_ARGUMENT;
+    // velocity solves: the SSA without prescribed faces (the DIVA's lagged state is not restated)
+    if (d->velocity_solves && (P.stress_balance == NK_DIVA || P.grid.pu || P.grid.pv)) return NK_BAD_ARGUMENT;
     const nk_iteration_control ctl = d->adjoint_control ? *d->adjoint_control : P.sdesc.picard;
     if (d->velocity_solves && ctl.kind != NK_CONVERGENCE && ctl.kind != NK_FIXED_ITERATIONS) return NK_BAD_ARGUMENT;
     nk_time_gradient_stats local{};

@@ -4,14 +4,15 @@ of its own forward steps, on the CPU.  With the velocities held: the transport c
 to 1e-6, the floating melt across a grounding line (the centre grounded fraction) at the partially grounded cells
 to 1e-5, and a partial-cell front (its advance reversed through a numerical Jacobian) with and without overflow passes
 and under eigencalving and von Mises calving, at the reference's cells (test/test_enzyme.jl:490-536) to 1e-5.  With a
-Picard solve after every stage (the SSA): the reference's ridge (:421-445) to 1e-5; the DIVA is refused.  The
+Picard solve after every stage (the SSA): the reference's ridge (:421-445) and von Mises calving on a confined shelf
+to 1e-5; the DIVA is refused.  The
 library's gradient is held to this one over the whole field in test_gpu_time_gradient."""
 import numpy as np
 import pytest
 
 from nunatak_gb300 import model as M
 from test_gpu_time_gradient import (_close, calving_case, channel_front_case, fd_extrapolated, fd_final_thickness, gradient,
-                                    grounding_line_case, ridge_case, transport_case)
+                                    grounding_line_case, ridge_case, shelf_case, transport_case)
 
 
 @pytest.mark.parametrize("advection", [None, M.UpwindBiased(order=1)], ids=["bounded_weno5", "upwind1"])
@@ -82,6 +83,21 @@ def test_oracle_picard_time_steps_gradient(oracle_cls):
     C = case.build(oracle_cls).get("C")
     _close(g["log_C"][1, 6] / C[1, 6], fd_extrapolated(case, oracle_cls, "C", (1, 6), 1e-3 * C[1, 6]), 1e-5)
     _close(g["smb"][2, 8], fd_extrapolated(case, oracle_cls, "surface_mass_balance", (2, 8), 1e-2 * 1e-8), 1e-5)
+
+
+def test_oracle_von_mises_gradient_with_solves(oracle_cls):
+    """Von Mises calving on the confined shelf with a Picard solve after every stage: the front's η̄H column of the
+    numerical Jacobian enters the oracle's Picard adjoint of the solve before the front as the coefficient's shadow;
+    ∂J/∂H₀ at a shelf cell and at the front column and ∂J/∂log A near the front against Richardson differences, 1e-5."""
+    case = shelf_case(False)
+    P0 = case.build(oracle_cls)
+    H0, A0 = P0.get("H"), P0.get("A")
+    _, g = gradient(case, oracle_cls)
+    assert g["stats"]["worst_solve_status"] == 0
+    for idx in ((1, 4), (2, 9)):
+        _close(g["H"][idx], fd_extrapolated(case, oracle_cls, "H", idx, 1e-5 * H0[idx]), 1e-5)
+    idx = (1, 8)
+    _close(g["log_A"][idx], A0[idx] * fd_extrapolated(case, oracle_cls, "A", idx, 1e-4 * A0[idx]), 1e-5)
 
 
 def test_oracle_refuses_solves_it_does_not_restate(oracle_cls):
