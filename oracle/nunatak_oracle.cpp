@@ -1504,8 +1504,10 @@ static void diva_sweep(Problem& P, const VelocityVector& lam, const DivaState& s
 // nk_picard_adjoint.  xbar (interior layout of u, v) = ∂J/∂x*; lam receives λ = ∂J/∂τ, gradC ∂J/∂log C per
 // cell, gradA ∂J/∂log A in the rate factor's layout (2-D: summed over the layers that share it).  The SSA sweep is
 // λ-signed (ȳ = -G.x), the DIVA sweep true (ȳ = G.x) and carries the lagged-state adjoint σ.
+// sig_final (DIVA): the adjoint σ of the lagged state's outputs seeded into the final pass (the reverse rule's s̄ + sweep).
 static int picard_adjoint(Problem& P, const VelocityVector& xbar, const nk_iteration_control& ctl, VelocityVector& lam,
-                          Field& gradC, SigmaField& gradA, nk_solve_stats* st, const Field* eta_bar = nullptr) {
+                          Field& gradC, SigmaField& gradA, nk_solve_stats* st, const Field* eta_bar = nullptr,
+                          DivaState* sig_final = nullptr) {
     const Grid& g = P.grid;
     const bool diva = P.stress_balance == NK_DIVA;
     const double sign = diva ? 1.0 : -1.0;
@@ -1551,6 +1553,7 @@ static int picard_adjoint(Problem& P, const VelocityVector& xbar, const nk_itera
         ++it;
         if (!std::isfinite(D) || status == NK_NONFINITE) break;
     }
+    if (diva && sig_final) *sig_final = sig;
     sweep();
     gradC.init(&g, CENTER, CENTER);
     for (int j = 1; j <= g.Ny(); ++j) for (int i = 1; i <= g.Nx(); ++i) gradC(i, j) = sign * P.C(i, j) * G.C(i, j);
@@ -2458,11 +2461,21 @@ static void front_reverse_jacobian(Problem& P, const FrontInputs& in, const Fiel
 // (update_state! without the solve), h = 1e-6 max(H, 1).  A numerical restatement of the library's hand-written
 // chain through η̄H, the drag's grounded fractions and effective pressure, the slope and the front force.
 // With eta_bar (the η̄H shadow of picard_adjoint) the shadow's own H part s̄ᵀ ∂η̄H/∂H joins it, by the same differences.
+// The DIVA's fixed point is one of (x, s) with the lagged state s = (βᵇ, F₂, ησ): with sig (picard_adjoint's
+// sig_final) the state's part σᵀ ∂S/∂H of the state update S(x*, s*, H) joins it, s* restored before each evaluation.
 static void picard_thickness_gradient(Problem& P, const VelocityVector& lam, const VelocityVector& xs, Field& gH,
-                                      const Field* eta_bar = nullptr) {
+                                      const Field* eta_bar = nullptr, const DivaState* sig = nullptr) {
     const Grid& g = P.grid;
     const int Nx = g.Nx(), Ny = g.Ny();
+    const bool diva = P.stress_balance == NK_DIVA;
     Field H0 = P.H;
+    Field s_bbu = P.bbu, s_bbv = P.bbv, s_F2 = P.F2;
+    SigmaField s_eta = P.eta_s;
+    auto restore_state = [&] {
+        if (!diva) return;
+        P.bbu = s_bbu; P.bbv = s_bbv; P.F2 = s_F2; P.eta_s = s_eta;
+    };
+    double sd = 0.0;   // σᵀ S of the last evaluation
     VelocityVector rp, rm;
     rp.init(&g);
     rm.init(&g);
@@ -2472,7 +2485,18 @@ static void picard_thickness_gradient(Problem& P, const VelocityVector& lam, con
         compute_geometry(P);
         P.x = xs;
         fill_halo(P.x);
+        restore_state();
         update_coefficients(P);
+        sd = 0.0;
+        if (diva && sig) {
+            for (int j = 1; j <= P.bbu.ny(); ++j) for (int i = 1; i <= P.bbu.nx(); ++i) sd += sig->bbu(i, j) * P.bbu(i, j);
+            for (int j = 1; j <= P.bbv.ny(); ++j) for (int i = 1; i <= P.bbv.nx(); ++i) sd += sig->bbv(i, j) * P.bbv(i, j);
+            for (int j = 1; j <= Ny; ++j)
+                for (int i = 1; i <= Nx; ++i) {
+                    sd += sig->F2(i, j) * P.F2(i, j);
+                    for (size_t k = 0; k < P.eta_s.k.size(); ++k) sd += sig->eta.k[k](i, j) * P.eta_s.k[k](i, j);
+                }
+        }
         VelocityVector q;
         q.init(&g);
         ssa_operator(g, q, xs, coeffs(P), P.ph.walls);
@@ -2487,10 +2511,11 @@ static void picard_thickness_gradient(Problem& P, const VelocityVector& lam, con
             P.H = H0;
             P.H(i, j) += h;
             residual(rp, ep);
+            double sdp = sd;
             P.H = H0;
             P.H(i, j) -= h;
             residual(rm, em);
-            double acc = 0.0;
+            double acc = sdp - sd;
             if (eta_bar)
                 for (int b = 1; b <= Ny; ++b) for (int a = 1; a <= Nx; ++a) acc += (*eta_bar)(a, b) * (ep(a, b) - em(a, b));
             for (int b = 1; b <= lam.u.ny(); ++b) for (int a = 1; a <= lam.u.nx(); ++a) acc += lam.u(a, b) * (rp.u(a, b) - rm.u(a, b));
@@ -2502,7 +2527,9 @@ static void picard_thickness_gradient(Problem& P, const VelocityVector& lam, con
     compute_geometry(P);
     P.x = xs;
     fill_halo(P.x);
+    restore_state();
     update_coefficients(P);
+    restore_state();
 }
 
 // nk_checkpointed_gradient of the library; every stage stored.  A partial-cell front's advance is reversed through its
@@ -2525,6 +2552,13 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
     const nk_iteration_control ctl = d.adjoint_control ? *d.adjoint_control : P.sdesc.picard;
     std::vector<Field> tape;                         // H before each stage, then the final H
     std::vector<VelocityVector> xt;                  // with solves: the velocities before each stage, then the final ones
+    struct Lagged { Field bbu, bbv, F2; SigmaField eta; };
+    std::vector<Lagged> st_t;                        // and the DIVA's lagged state the solve left with them
+    const bool diva = P.stress_balance == NK_DIVA;
+    auto keep_state = [&] {
+        if (solves) xt.push_back(P.x);
+        if (solves && diva) st_t.push_back(Lagged{P.bbu, P.bbv, P.F2, P.eta_s});
+    };
     std::vector<Field> mu_start, Hr_start, H3pre;   // a front: μ and Hʳ at each step's start, the last stage's output
     std::vector<Field> etaH_front;                   // and the viscosity its von Mises rates read
     fill_halo(P.H);
@@ -2544,7 +2578,7 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
         }
         for (int stg = 0; stg < 3; ++stg) {
             tape.push_back(P.H);
-            if (solves) xt.push_back(P.x);
+            keep_state();
             if (front && stg == 2) {
                 thickness_substep(P, d.dt, stg, false);
                 H3pre.push_back(P.H);
@@ -2558,7 +2592,7 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
         }
     }
     tape.push_back(P.H);
-    if (solves) xt.push_back(P.x);
+    keep_state();
     VelocityVector x_end = P.x;
     Field Hfinal = P.H, clipped_end = P.clipped, mu_end = P.mu, Hr_end = P.Hr, calved_end = P.calved;
     Field lamH(&g, CENTER, CENTER), lamHs(&g, CENTER, CENTER), lamH0(&g, CENTER, CENTER), lamHr(&g, CENTER, CENTER);
@@ -2586,16 +2620,18 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
         compute_geometry(P);
         P.x = xt[t];
         fill_halo(P.x);
+        if (diva) { P.bbu = st_t[t].bbu; P.bbv = st_t[t].bbv; P.F2 = st_t[t].F2; P.eta_s = st_t[t].eta; }
         VelocityVector lam;
         Field gC;
         SigmaField gA;
+        DivaState sig;
         nk_solve_stats ss{};
-        picard_adjoint(P, xbar, ctl, lam, gC, gA, &ss, eta_bar);
+        picard_adjoint(P, xbar, ctl, lam, gC, gA, &ss, eta_bar, diva ? &sig : nullptr);
         ++st->picard_adjoints;
         st->adjoint_iterations += ss.picard_iterations;
         if (ss.status > st->worst_solve_status) st->worst_solve_status = ss.status;
         Field gHs;
-        picard_thickness_gradient(P, lam, xt[t], gHs, eta_bar);
+        picard_thickness_gradient(P, lam, xt[t], gHs, eta_bar, diva ? &sig : nullptr);
         for_xy(Nx, Ny, [&](int i, int j) {
             lam_to(i, j) += gHs(i, j);
             glogC(i, j) += gC(i, j);
@@ -2715,6 +2751,7 @@ static nk_status time_gradient(Problem& P, const nk_time_gradient_desc& d, nk_co
         }
     }
     if (solves) P.x = x_end;
+    if (solves && diva) { P.bbu = st_t.back().bbu; P.bbv = st_t.back().bbv; P.F2 = st_t.back().F2; P.eta_s = st_t.back().eta; }
     P.H = Hfinal;
     P.clipped = clipped_end;
     P.melt = base;
@@ -3025,8 +3062,10 @@ nk_status nko_checkpointed_gradient(nko_problem* h, const nk_time_gradient_desc*
     if (!h || !d || !cost || !(d->dt > 0) || d->steps < 1 || (d->velocity_solves != 0 && d->velocity_solves != 1))
         return NK_BAD_ARGUMENT;
     Problem& P = *reinterpret_cast<Problem*>(h);
-    // velocity solves: the SSA without prescribed faces (the DIVA's lagged state is not restated)
-    if (d->velocity_solves && (P.stress_balance == NK_DIVA || P.grid.pu || P.grid.pv)) return NK_BAD_ARGUMENT;
+    // velocity solves: without prescribed faces; the DIVA without von Mises calving (its sweep takes no η̄H shadow)
+    if (d->velocity_solves && (P.grid.pu || P.grid.pv)) return NK_BAD_ARGUMENT;
+    if (d->velocity_solves && P.stress_balance == NK_DIVA && P.front.enabled && P.front.calving == NK_CALVING_VON_MISES)
+        return NK_BAD_ARGUMENT;
     const nk_iteration_control ctl = d->adjoint_control ? *d->adjoint_control : P.sdesc.picard;
     if (d->velocity_solves && ctl.kind != NK_CONVERGENCE && ctl.kind != NK_FIXED_ITERATIONS) return NK_BAD_ARGUMENT;
     nk_time_gradient_stats local{};

@@ -4,8 +4,8 @@ of its own forward steps, on the CPU.  With the velocities held: the transport c
 to 1e-6, the floating melt across a grounding line (the centre grounded fraction) at the partially grounded cells
 to 1e-5, and a partial-cell front (its advance reversed through a numerical Jacobian) with and without overflow passes
 and under eigencalving and von Mises calving, at the reference's cells (test/test_enzyme.jl:490-536) to 1e-5.  With a
-Picard solve after every stage (the SSA): the reference's ridge (:421-445) and von Mises calving on a confined shelf
-to 1e-5; the DIVA is refused.  The
+Picard solve after every stage: the reference's ridge (:421-445) and von Mises calving on a confined shelf to 1e-5,
+the DIVA ridge to 1e-4 (the DIVA with von Mises calving is refused).  The
 library's gradient is held to this one over the whole field in test_gpu_time_gradient."""
 import numpy as np
 import pytest
@@ -100,8 +100,24 @@ def test_oracle_von_mises_gradient_with_solves(oracle_cls):
     _close(g["log_A"][idx], A0[idx] * fd_extrapolated(case, oracle_cls, "A", idx, 1e-4 * A0[idx]), 1e-5)
 
 
+def test_oracle_diva_picard_time_steps_gradient(oracle_cls):
+    """The ridge under the DIVA (Nσ = 6) with a Picard solve after every stage, two steps: the thickness part of each
+    solve's adjoint adds the lagged state's σᵀ ∂S/∂H (βᵇ, F₂, ησ of the state update at the fixed point) to λᵀ ∂r/∂H.
+    The lagged state's adjoint settles more slowly than λ, whose change stops a Convergence control, so 3000 fixed
+    adjoint iterations: ∂J/∂H₀ at two cells then meets Richardson differences to 1e-6 (the state's term is 3e-5 to 4e-5
+    of it there), ∂J/∂log C at one to 1e-5."""
+    case = ridge_case(oracle_cls, diva=True, steps=2)
+    _, g = gradient(case, oracle_cls, adjoint_control=M.FixedIterations(3000))
+    assert g["stats"]["picard_adjoints"] == 3 * case.steps
+    H0 = case.build(oracle_cls).get("H")
+    for idx in ((1, 5), (2, 9)):
+        _close(g["H"][idx], fd_extrapolated(case, oracle_cls, "H", idx, 1e-3 * H0[idx]), 1e-6)
+    C = case.build(oracle_cls).get("C")
+    _close(g["log_C"][1, 6] / C[1, 6], fd_extrapolated(case, oracle_cls, "C", (1, 6), 1e-3 * C[1, 6]), 1e-5)
+
+
 def test_oracle_refuses_solves_it_does_not_restate(oracle_cls):
-    case = ridge_case(oracle_cls, diva=True, steps=1)
+    case = shelf_case(True)   # the DIVA under von Mises calving: its sweep takes no viscosity shadow
     P = case.build(oracle_cls)
     with pytest.raises(Exception):
         P.checkpointed_gradient(lambda *a: None, case.dt, 1, velocity_solves=True)
